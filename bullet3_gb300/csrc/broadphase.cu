@@ -1,0 +1,284 @@
+// World AABBs and the uniform-grid broadphase.
+//
+// Reference path:
+//   initializeGpuAabbsFull (src/Bullet3OpenCL/RigidBody/kernels/updateAabbsKernel.cl:38)
+//     -> b3ComputeWorldAabb / b3TransformAabb2 (Bullet3Collision/BroadPhaseCollision/shared/b3Aabb.h:24-43), margin 0
+//   b3GpuGridBroadphase::calculateOverlappingPairs (src/Bullet3OpenCL/BroadphaseCollision/b3GpuGridBroadphase.cpp:117-259):
+//     kCalcHashAABB (gridBroadphase.cl:25) cell of the AABB centre, floor(c * invCell) & (dim-1)
+//     radix sort of (hash, body), kFindCellStart (:60), kFindOverlappingPairs (:169) 27-cell scan with
+//     the inclusive overlap test testAABBOverlap (:89-94), one pair per (lower, higher) body index,
+//     large (static, mass 0) proxies against every small proxy (computePairsKernelTwoArrays, sap.cl:66).
+//
+// GB300 design: one fused AABB+hash kernel; stable 8-bit LSD radix sort; run starts written
+// into a dense hash table that is never cleared (entries are validated against the sorted keys);
+// the pair kernel works in sorted (spatially coherent) order, buffers pairs per thread and
+// reserves output with one warp-aggregated atomic; pairs are then radix-sorted on a packed
+// (a, b) key so the pair list is canonical and deterministic (a < b, ascending).
+#include "common.cuh"
+#include "world_internal.h"
+
+namespace b3g {
+
+static constexpr int BP_THREADS = 256;
+
+__device__ __forceinline__ void transform_aabb(const b3gAabb& local, v3 pos, quat q, float margin, v3& mn, v3& mx) {
+    v3 lmin = mk3(local.minv[0], local.minv[1], local.minv[2]);
+    v3 lmax = mk3(local.maxv[0], local.maxv[1], local.maxv[2]);
+    v3 he = 0.5f * (lmax - lmin);
+    he = he + mk3(margin, margin, margin);
+    v3 lc = 0.5f * (lmax + lmin);
+    m33 m = qmat(q);
+    m33 a;
+    a.r0 = mk3(fabsf(m.r0.x), fabsf(m.r0.y), fabsf(m.r0.z));
+    a.r1 = mk3(fabsf(m.r1.x), fabsf(m.r1.y), fabsf(m.r1.z));
+    a.r2 = mk3(fabsf(m.r2.x), fabsf(m.r2.y), fabsf(m.r2.z));
+    v3 c = mmul(m, lc) + pos;
+    v3 e = mk3(dot3(he, a.r0), dot3(he, a.r1), dot3(he, a.r2));
+    mn = c - e;
+    mx = c + e;
+}
+
+__device__ __forceinline__ int cell_coord(float c, float inv_cell, int mask) {
+    return ((int)floorf(c * inv_cell)) & mask;
+}
+
+__device__ __forceinline__ uint32_t cell_hash(int x, int y, int z, int bits, int mask) {
+    return ((uint32_t)(z & mask) << (2 * bits)) | ((uint32_t)(y & mask) << bits) | (uint32_t)(x & mask);
+}
+
+__global__ void __launch_bounds__(BP_THREADS) k_aabb_hash(const b3gBody* __restrict__ bodies,
+                                                          const b3gCollidable* __restrict__ cols,
+                                                          const b3gAabb* __restrict__ local_aabbs,
+                                                          const int* __restrict__ dyn_slot, int n,
+                                                          b3gAabb* __restrict__ aabbs, uint32_t* __restrict__ keys,
+                                                          uint32_t* __restrict__ vals, float inv_cell, int bits) {
+    const int mask = (1 << bits) - 1;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const b3gBody& b = bodies[i];
+        float4 p = ldg4(&b.pos);
+        float4 qq = ldg4(&b.quat);
+        int col = b.collidableIdx;
+        float inv_mass = b.invMass;
+        b3gAabb la = local_aabbs[col];
+        v3 mn, mx;
+        transform_aabb(la, mk3(p.x, p.y, p.z), quat{qq.x, qq.y, qq.z, qq.w}, 0.f, mn, mx);
+        b3gAabb w;
+        w.minv[0] = mn.x; w.minv[1] = mn.y; w.minv[2] = mn.z; w.minw = i;
+        w.maxv[0] = mx.x; w.maxv[1] = mx.y; w.maxv[2] = mx.z; w.maxw = inv_mass == 0.f ? 0 : 1;
+        aabbs[i] = w;
+        int slot = dyn_slot[i];
+        if (slot >= 0) {
+            float cx = (mn.x + mx.x) * 0.5f, cy = (mn.y + mx.y) * 0.5f, cz = (mn.z + mx.z) * 0.5f;
+            int gx = cell_coord(cx, inv_cell, mask), gy = cell_coord(cy, inv_cell, mask),
+                gz = cell_coord(cz, inv_cell, mask);
+            keys[slot] = cell_hash(gx, gy, gz, bits, mask);
+            vals[slot] = (uint32_t)i;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(BP_THREADS) k_cell_start(const uint32_t* __restrict__ keys, int n,
+                                                           uint32_t* __restrict__ cell_start) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        uint32_t h = keys[p];
+        if (p == 0 || keys[p - 1] != h) cell_start[h] = (uint32_t)p;
+    }
+}
+
+// inclusive overlap test (testAABBOverlap, gridBroadphase.cl:89-94)
+__device__ __forceinline__ bool overlap(const float4& amin, const float4& amax, const float4& bmin, const float4& bmax) {
+    return (amin.x <= bmax.x) && (bmin.x <= amax.x) && (amin.y <= bmax.y) && (bmin.y <= amax.y) &&
+           (amin.z <= bmax.z) && (bmin.z <= amax.z);
+}
+
+static constexpr int PAIR_BUF = 16;
+
+struct PairEmitter {
+    uint64_t buf[PAIR_BUF];
+    int cnt;
+    __device__ void flush_self(uint64_t* out, int* counter, int cap, unsigned int* status) {
+        if (cnt == 0) return;
+        int base = atomicAdd(counter, cnt);
+        for (int k = 0; k < cnt; k++) {
+            if (base + k < cap)
+                out[base + k] = buf[k];
+            else
+                atomicOr(status, B3G_FLAG_PAIR_OVERFLOW);
+        }
+        cnt = 0;
+    }
+    __device__ void push(uint64_t key, uint64_t* out, int* counter, int cap, unsigned int* status) {
+        if (cnt == PAIR_BUF) flush_self(out, counter, cap, status);
+        buf[cnt++] = key;
+    }
+};
+
+__global__ void __launch_bounds__(BP_THREADS) k_find_pairs(const b3gAabb* __restrict__ aabbs,
+                                                           const uint32_t* __restrict__ keys,
+                                                           const uint32_t* __restrict__ vals,
+                                                           const uint32_t* __restrict__ cell_start, int n_dyn,
+                                                           const int* __restrict__ large_list, int n_large,
+                                                           float inv_cell, int bits, int body_bits,
+                                                           uint64_t* __restrict__ out, int* __restrict__ counter,
+                                                           int cap, unsigned int* __restrict__ status) {
+    const int mask = (1 << bits) - 1;
+    const int lane = threadIdx.x & 31;
+    const float4* A = reinterpret_cast<const float4*>(aabbs);
+    // every lane of a warp runs the same number of outer iterations so the final
+    // warp-aggregated flush is convergent
+    const int stride = gridDim.x * blockDim.x;
+    const int start = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iters = (n_dyn + stride - 1) / stride;
+    PairEmitter em;
+    em.cnt = 0;
+    for (int it = 0; it < iters; it++) {
+        int p = start + it * stride;
+        if (p < n_dyn) {
+            uint32_t i = vals[p];
+            float4 amin = __ldg(&A[2 * i]), amax = __ldg(&A[2 * i + 1]);
+            float cx = (amin.x + amax.x) * 0.5f, cy = (amin.y + amax.y) * 0.5f, cz = (amin.z + amax.z) * 0.5f;
+            int gx = (int)floorf(cx * inv_cell), gy = (int)floorf(cy * inv_cell), gz = (int)floorf(cz * inv_cell);
+            for (int dz = -1; dz <= 1; dz++)
+                for (int dy = -1; dy <= 1; dy++)
+                    for (int dx = -1; dx <= 1; dx++) {
+                        uint32_t h = cell_hash(gx + dx, gy + dy, gz + dz, bits, mask);
+                        uint32_t s = __ldg(&cell_start[h]);
+                        if (s >= (uint32_t)n_dyn) continue;
+                        if (__ldg(&keys[s]) != h) continue;
+                        if (s > 0 && __ldg(&keys[s - 1]) == h) continue;
+                        for (uint32_t q = s; q < (uint32_t)n_dyn; q++) {
+                            if (__ldg(&keys[q]) != h) break;
+                            uint32_t j = __ldg(&vals[q]);
+                            if (j <= i) continue;
+                            float4 bmin = __ldg(&A[2 * j]), bmax = __ldg(&A[2 * j + 1]);
+                            if (overlap(amin, amax, bmin, bmax))
+                                em.push(((uint64_t)i << body_bits) | j, out, counter, cap, status);
+                        }
+                    }
+            for (int l = 0; l < n_large; l++) {
+                uint32_t j = (uint32_t)__ldg(&large_list[l]);
+                float4 bmin = __ldg(&A[2 * j]), bmax = __ldg(&A[2 * j + 1]);
+                if (overlap(amin, amax, bmin, bmax)) {
+                    uint32_t a = i < j ? i : j, b = i < j ? j : i;
+                    em.push(((uint64_t)a << body_bits) | b, out, counter, cap, status);
+                }
+            }
+        }
+    }
+    // warp-aggregated reservation of the remaining buffered pairs
+    int c = em.cnt;
+    int incl = c;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    int total = __shfl_sync(0xffffffffu, incl, 31);
+    int base = 0;
+    if (lane == 31 && total > 0) base = atomicAdd(counter, total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    int my = base + incl - c;
+    for (int k = 0; k < c; k++) {
+        if (my + k < cap)
+            out[my + k] = em.buf[k];
+        else
+            atomicOr(status, B3G_FLAG_PAIR_OVERFLOW);
+    }
+}
+
+__global__ void k_clamp_count(int* counter, int cap, int* clamped) {
+    int n = *counter;
+    *clamped = n < cap ? n : cap;
+}
+
+__device__ __forceinline__ int pair_type(int ta, int tb) {
+    if (ta == B3G_SHAPE_CONVEX_HULL && tb == B3G_SHAPE_CONVEX_HULL) return PT_HULL_HULL;
+    if ((ta == B3G_SHAPE_PLANE && tb == B3G_SHAPE_CONVEX_HULL) || (tb == B3G_SHAPE_PLANE && ta == B3G_SHAPE_CONVEX_HULL))
+        return PT_PLANE_HULL;
+    if ((ta == B3G_SHAPE_SPHERE && tb == B3G_SHAPE_CONVEX_HULL) || (tb == B3G_SHAPE_SPHERE && ta == B3G_SHAPE_CONVEX_HULL))
+        return PT_SPHERE_HULL;
+    if (ta == B3G_SHAPE_SPHERE && tb == B3G_SHAPE_SPHERE) return PT_SPHERE_SPHERE;
+    if ((ta == B3G_SHAPE_PLANE && tb == B3G_SHAPE_SPHERE) || (tb == B3G_SHAPE_PLANE && ta == B3G_SHAPE_SPHERE))
+        return PT_PLANE_SPHERE;
+    return -1;
+}
+
+// Unpack sorted keys into b3Int4 pairs, reset the per-pair contact flag, and bucket pairs
+// by shape-type combination for the narrowphase kernels.
+__global__ void __launch_bounds__(BP_THREADS) k_unpack_pairs(const uint64_t* __restrict__ keys,
+                                                             const int* __restrict__ d_np, int body_bits,
+                                                             const b3gBody* __restrict__ bodies,
+                                                             const b3gCollidable* __restrict__ cols,
+                                                             b3gPair* __restrict__ pairs, int* __restrict__ flags,
+                                                             int* __restrict__ type_lists, int max_pairs,
+                                                             int* __restrict__ type_count) {
+    const int np = *d_np;
+    const uint64_t bmask = (1ull << body_bits) - 1ull;
+    const int lane = threadIdx.x & 31;
+    const int stride = gridDim.x * blockDim.x;
+    const int iters = (np + stride - 1) / stride;
+    for (int it = 0; it < iters; it++) {
+        int p = blockIdx.x * blockDim.x + threadIdx.x + it * stride;
+        int t = -1;
+        if (p < np) {
+            uint64_t k = keys[p];
+            int a = (int)(k >> body_bits), b = (int)(k & bmask);
+            b3gPair pr;
+            pr.x = a; pr.y = b; pr.z = -1; pr.w = -1;
+            pairs[p] = pr;
+            flags[p] = 0;
+            int ta = cols[bodies[a].collidableIdx].shapeType;
+            int tb = cols[bodies[b].collidableIdx].shapeType;
+            t = pair_type(ta, tb);
+        }
+        unsigned peers = __match_any_sync(0xffffffffu, t);
+        int leader = __ffs(peers) - 1;
+        int rank = __popc(peers & ((1u << lane) - 1u));
+        int base = 0;
+        if (t >= 0 && lane == leader) base = atomicAdd(&type_count[t], __popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        if (t >= 0) type_lists[t * max_pairs + base + rank] = p;
+    }
+}
+
+int launch_aabbs(DeviceState& d, cudaStream_t s) {
+    int grid = d.num_sms * 4;
+    k_aabb_hash<<<grid, BP_THREADS, 0, s>>>(d.bodies, d.collidables, d.local_aabbs, d.dyn_slot, d.num_bodies, d.aabbs,
+                                            d.cell_keys[0], d.cell_vals[0], d.inv_cell, d.grid_bits);
+    return 1;
+}
+
+int launch_pairs(DeviceState& d, cudaStream_t s) {
+    int launches = 0;
+    long long ll = 0;
+    // 1. sort (cell hash, body) -- keys written by launch_aabbs
+    int which = radix_sort_u32(d.prim, d.cell_keys[0], d.cell_keys[1], d.cell_vals[0], d.cell_vals[1],
+                               d.d_num_dynamic, 3 * d.grid_bits, d.sort_scratch, s, &ll);
+    uint32_t* keys = d.cell_keys[which];
+    uint32_t* vals = d.cell_vals[which];
+    int grid = d.num_sms * 4;
+    // 2. run starts
+    k_cell_start<<<grid, BP_THREADS, 0, s>>>(keys, d.num_dynamic, d.cell_start);
+    launches++;
+    // 3. pairs
+    cudaMemsetAsync(d.counters, 0, sizeof(DevCounters), s);
+    k_find_pairs<<<d.num_sms * 8, BP_THREADS, 0, s>>>(d.aabbs, keys, vals, d.cell_start, d.num_dynamic, d.large_list,
+                                                      d.num_large, d.inv_cell, d.grid_bits, d.body_bits,
+                                                      d.pair_keys[0], &d.counters->num_pairs, d.max_pairs,
+                                                      &d.counters->status);
+    launches++;
+    // clamp the count to capacity for the consumers (the raw count stays in num_pairs)
+    int* d_np = &d.counters->pad[0];
+    k_clamp_count<<<1, 1, 0, s>>>(&d.counters->num_pairs, d.max_pairs, d_np);
+    launches++;
+    // 4. canonical order: sort packed (a, b) keys
+    int w2 = radix_sort_u64(d.prim, d.pair_keys[0], d.pair_keys[1], nullptr, nullptr, d_np, 2 * d.body_bits,
+                            d.sort_scratch, s, &ll);
+    // 5. unpack + classify
+    k_unpack_pairs<<<d.num_sms * 4, BP_THREADS, 0, s>>>(d.pair_keys[w2], d_np, d.body_bits, d.bodies, d.collidables,
+                                                        d.pairs, d.contact_flag, d.type_lists, d.max_pairs,
+                                                        d.counters->type_count);
+    launches++;
+    return launches + (int)ll;
+}
+
+}  // namespace b3g

@@ -1,0 +1,145 @@
+// Shared device helpers for the GPU rigid-body step.
+//
+// Arithmetic convention: every physics translation unit is compiled with --fmad=false
+// and IEEE division/square root, and every formula below fixes its evaluation order.
+// The CPU oracle restates the same formulas in the same order (compiled with
+// -ffp-contract=off), so the AABB, broadphase, SAT, clipping, reduction and solver
+// stages reproduce the oracle bit-for-bit; only the integrator's sinf/cosf differ.
+#ifndef B3G_COMMON_CUH
+#define B3G_COMMON_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "b3g_types.h"
+#include "b3g_capi.h"
+
+#define B3G_DEV __device__ __forceinline__
+#define B3G_HD __host__ __device__ __forceinline__
+
+struct v3 {
+    float x, y, z;
+};
+
+B3G_HD v3 mk3(float x, float y, float z) { return v3{x, y, z}; }
+B3G_HD v3 f4v3(const b3gFloat4& a) { return v3{a.x, a.y, a.z}; }
+B3G_HD v3 operator+(v3 a, v3 b) { return v3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+B3G_HD v3 operator-(v3 a, v3 b) { return v3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+B3G_HD v3 operator-(v3 a) { return v3{-a.x, -a.y, -a.z}; }
+B3G_HD v3 operator*(v3 a, float s) { return v3{a.x * s, a.y * s, a.z * s}; }
+B3G_HD v3 operator*(float s, v3 a) { return v3{s * a.x, s * a.y, s * a.z}; }
+B3G_HD float dot3(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+B3G_HD v3 cross3(v3 a, v3 b) {
+    return v3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+// v / |v| (division, not reciprocal multiply: b3Vector3::normalized, b3Vector3.h:897-905)
+B3G_HD v3 normalize3(v3 a) {
+    float l = sqrtf(dot3(a, a));
+    return v3{a.x / l, a.y / l, a.z / l};
+}
+
+struct quat {
+    float x, y, z, w;
+};
+B3G_HD quat f4q(const b3gFloat4& a) { return quat{a.x, a.y, a.z, a.w}; }
+
+// Hamilton product a*b
+B3G_HD quat qmul(quat a, quat b) {
+    quat r;
+    r.x = a.w * b.x + a.x * b.w + a.y * b.z - a.z * b.y;
+    r.y = a.w * b.y + a.y * b.w + a.z * b.x - a.x * b.z;
+    r.z = a.w * b.z + a.z * b.w + a.x * b.y - a.y * b.x;
+    r.w = a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z;
+    return r;
+}
+B3G_HD quat qconj(quat a) { return quat{-a.x, -a.y, -a.z, a.w}; }
+
+// 3x3 rotation matrix rows from a quaternion (b3Matrix3x3::setRotation order).
+struct m33 {
+    v3 r0, r1, r2;
+};
+B3G_HD m33 qmat(quat q) {
+    float d = q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w;
+    float s = 2.0f / d;
+    float xs = q.x * s, ys = q.y * s, zs = q.z * s;
+    float wx = q.w * xs, wy = q.w * ys, wz = q.w * zs;
+    float xx = q.x * xs, xy = q.x * ys, xz = q.x * zs;
+    float yy = q.y * ys, yz = q.y * zs, zz = q.z * zs;
+    m33 m;
+    m.r0 = v3{1.0f - (yy + zz), xy - wz, xz + wy};
+    m.r1 = v3{xy + wz, 1.0f - (xx + zz), yz - wx};
+    m.r2 = v3{xz - wy, yz + wx, 1.0f - (xx + yy)};
+    return m;
+}
+B3G_HD v3 mmul(const m33& m, v3 v) { return v3{dot3(m.r0, v), dot3(m.r1, v), dot3(m.r2, v)}; }
+// transpose(m) * v
+B3G_HD v3 mtmul(const m33& m, v3 v) {
+    return v3{m.r0.x * v.x + m.r1.x * v.y + m.r2.x * v.z, m.r0.y * v.x + m.r1.y * v.y + m.r2.y * v.z,
+              m.r0.z * v.x + m.r1.z * v.y + m.r2.z * v.z};
+}
+// rotate v by q: matrix form, used everywhere a world/local transform is needed
+B3G_HD v3 qrot(quat q, v3 v) { return mmul(qmat(q), v); }
+B3G_HD v3 qrot_inv(quat q, v3 v) { return mtmul(qmat(q), v); }
+B3G_HD v3 xform(v3 p, v3 pos, quat q) { return qrot(q, p) + pos; }
+
+// inverse inertia matrix (3 float4 rows in memory)
+B3G_HD v3 imul(const b3gMat3& m, v3 v) {
+    return v3{m.row[0].x * v.x + m.row[0].y * v.y + m.row[0].z * v.z,
+              m.row[1].x * v.x + m.row[1].y * v.y + m.row[1].z * v.z,
+              m.row[2].x * v.x + m.row[2].y * v.y + m.row[2].z * v.z};
+}
+
+B3G_DEV float4 ldg4(const b3gFloat4* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+
+// ----------------------------------------------------------------------------------------
+// Bounded grid barrier for persistent cooperative kernels.
+//
+// Every wait is capped: after B3G_BARRIER_SPIN_LIMIT polls a block raises the abort flag
+// and the barrier returns false in every block (they all poll the abort flag), so a
+// kernel can unwind and the host sees B3G_FLAG_BARRIER_TIMEOUT instead of a hang.
+struct GridBarrier {
+    unsigned int* count;      // arrivals in the current generation
+    unsigned int* gen;        // generation counter
+    unsigned int* abort_flag; // non-zero once any block gave up
+    unsigned int* status;     // device status word
+};
+
+#ifndef B3G_BARRIER_SPIN_LIMIT
+#define B3G_BARRIER_SPIN_LIMIT (1u << 22)
+#endif
+
+B3G_DEV bool grid_barrier(const GridBarrier& b, unsigned int nblocks, unsigned int spin_limit) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        volatile unsigned int* vgen = b.gen;
+        volatile unsigned int* vabort = b.abort_flag;
+        unsigned int g = *vgen;
+        __threadfence();
+        unsigned int arrived = atomicAdd(b.count, 1u);
+        if (arrived == nblocks - 1) {
+            atomicExch(b.count, 0u);
+            __threadfence();
+            atomicAdd(b.gen, 1u);
+        } else {
+            unsigned int spins = 0;
+            while (*vgen == g) {
+                if (*vabort) { ok = 0; break; }
+                if (++spins >= spin_limit) {
+                    atomicExch(b.abort_flag, 1u);
+                    atomicOr(b.status, B3G_FLAG_BARRIER_TIMEOUT);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        if (*vabort) ok = 0;
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+#endif

@@ -1,0 +1,623 @@
+// Narrowphase: contact manifolds (b3Contact4Data, up to 4 points) for every overlapping pair.
+//
+// Reference functions restated (paths relative to the reference's src/):
+//   hull-hull     b3ContactConvexConvexSAT          Bullet3Collision/NarrowPhaseCollision/shared/b3ContactConvexConvexSAT.h:403
+//                 b3FindSeparatingAxis              .../shared/b3FindSeparatingAxis.h:55-195 (face axes of A, of B, exact edge x edge)
+//                 b3ClipHullAgainstHull/b3ClipFace  .../shared/b3ContactConvexConvexSAT.h:20-259 (minDist -1, maxDist 0)
+//                 b3ReduceContacts                  .../shared/b3ReduceContacts.h:4-87
+//   plane-hull    computeContactPlaneConvex         Bullet3OpenCL/NarrowphaseCollision/b3ConvexHullContact.cpp:1272-1395
+//   sphere-hull   computeContactSphereConvex        Bullet3OpenCL/NarrowphaseCollision/b3ConvexHullContact.cpp:2323-2470
+//   sphere-sphere primitiveContactsKernel           Bullet3OpenCL/NarrowphaseCollision/kernels/primitiveContacts.cl:926-972
+//   plane-sphere  computeContactPlaneSphere         same file :729-790
+// A/B roles per shape pair follow the reference's dispatch (b3ConvexHullContact.cpp:2655-2735):
+// the sphere / plane is always body A, the hull body B; hull-hull and sphere-sphere use the
+// pair order (lower body index = A).
+//
+// GB300 design: pairs are bucketed by shape combination; the primitive cases run one thread
+// per pair; hull-hull runs one warp per pair -- lanes split the face and edge-edge axes,
+// vertex reads are warp-broadcast, the axis choice is a (depth, axis index) warp arg-min
+// (first minimum wins, as in the sequential loop), clipping polygons live in shared memory.
+// Each manifold is written to the slot of its pair; a scan over per-pair flags gives the
+// manifold order (= pair order), so the contact list is deterministic.
+#include <cfloat>
+
+#include "common.cuh"
+#include "world_internal.h"
+
+namespace b3g {
+
+static constexpr int NP_THREADS = 256;
+static constexpr int CLIP_CAP = 64;
+
+struct NPArgs {
+    const b3gBody* bodies;
+    const b3gCollidable* cols;
+    const b3gHull* hulls;
+    const b3gFace* faces;
+    const int* indices;
+    const b3gFloat4* verts;
+    const b3gFloat4* edges;
+    const b3gPair* pairs;
+    const int* type_list;
+    const int* type_count;
+    b3gContact4* slots;
+    int* flags;
+    unsigned int* status;
+    unsigned short friction_cmp;
+};
+
+__device__ __forceinline__ v3 ld3(const b3gFloat4* p) {
+    float4 a = __ldg(reinterpret_cast<const float4*>(p));
+    return mk3(a.x, a.y, a.z);
+}
+__device__ __forceinline__ float4 ldf4(const b3gFloat4* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+
+__device__ __forceinline__ int sgn_index(const b3gBody* bodies, int i) { return bodies[i].invMass == 0.f ? -i : i; }
+
+__device__ __forceinline__ void write_header(b3gContact4& c, const NPArgs& a, int bodyA, int bodyB, v3 n, int np) {
+    c.worldNormalOnB = b3gFloat4{n.x, n.y, n.z, (float)np};
+    c.restitutionCmp = 0;
+    c.frictionCmp = a.friction_cmp;
+    c.batchIdx = 0;
+    c.bodyA = sgn_index(a.bodies, bodyA);
+    c.bodyB = sgn_index(a.bodies, bodyB);
+    c.childIndexA = -1;
+    c.childIndexB = -1;
+    c.unused1 = 0;
+    c.unused2 = 0;
+}
+
+// b3ReduceContacts / extractManifoldSequentialGlobal: deepest point + extremes along +-u, +-v.
+// p: xyz + w = depth. idx receives 4 indices (pre-set to 0,1,2,3 by the caller's convention).
+__device__ int reduce_contacts(const float4* p, int n, v3 nearNormal, int idx[4]) {
+    idx[0] = 0; idx[1] = 1; idx[2] = 2; idx[3] = 3;
+    if (n == 0) return 0;
+    if (n <= 4) return n;
+    if (n > 64) n = 64;
+    float cx = 0.f, cy = 0.f, cz = 0.f;
+    for (int i = 0; i < n; i++) {
+        cx = cx + p[i].x;
+        cy = cy + p[i].y;
+        cz = cz + p[i].z;
+    }
+    float inv = 1.0f / (float)n;
+    cx = cx * inv; cy = cy * inv; cz = cz * inv;
+    v3 center = mk3(cx, cy, cz);
+    v3 aVector = mk3(p[0].x, p[0].y, p[0].z) - center;
+    v3 u = cross3(nearNormal, aVector);
+    v3 v = cross3(nearNormal, u);
+    u = normalize3(u);
+    v = normalize3(v);
+    float minW = FLT_MAX;
+    int minIndex = -1;
+    float m0 = FLT_MIN, m1 = FLT_MIN, m2 = FLT_MIN, m3 = FLT_MIN;
+    v3 nu = -u, nv = -v;
+    for (int ie = 0; ie < n; ie++) {
+        if (p[ie].w < minW) {
+            minW = p[ie].w;
+            minIndex = ie;
+        }
+        v3 r = mk3(p[ie].x, p[ie].y, p[ie].z) - center;
+        float f;
+        f = dot3(u, r);
+        if (f < m0) { m0 = f; idx[0] = ie; }
+        f = dot3(nu, r);
+        if (f < m1) { m1 = f; idx[1] = ie; }
+        f = dot3(v, r);
+        if (f < m2) { m2 = f; idx[2] = ie; }
+        f = dot3(nv, r);
+        if (f < m3) { m3 = f; idx[3] = ie; }
+    }
+    if (idx[0] != minIndex && idx[1] != minIndex && idx[2] != minIndex && idx[3] != minIndex) idx[0] = minIndex;
+    return 4;
+}
+
+// ------------------------------------------------------------------ plane (A) vs hull (B)
+__device__ void plane_hull(const NPArgs& a, int pairIdx, int bodyA, int bodyB) {
+    const b3gBody& BA = a.bodies[bodyA];
+    const b3gBody& BB = a.bodies[bodyB];
+    const b3gCollidable colA = a.cols[BA.collidableIdx];
+    const b3gCollidable colB = a.cols[BB.collidableIdx];
+    const b3gHull hull = a.hulls[colB.shapeIndex];
+    v3 posB = f4v3(BB.pos), posA = f4v3(BA.pos);
+    quat ornB = f4q(BB.quat), ornA = f4q(BA.quat);
+    float4 pe = ldf4(&a.faces[colA.shapeIndex].plane);
+    v3 planeNormal = mk3(pe.x, pe.y, pe.z);
+    float planeConstant = pe.w;
+    m33 RA = qmat(ornA), RB = qmat(ornB);
+    v3 planeNormalWorld = mmul(RA, planeNormal);
+    // planeInConvex basis = RB^T * RA ; planeNormalInConvex = RB^T (RA (-n))
+    v3 planeNormalInConvex = mtmul(RB, mmul(RA, -planeNormal));
+    float4 pts[64];
+    int numPoints = 0;
+    float maxDot = -1e30f;
+    for (int i = 0; i < hull.numVertices; i++) {
+        v3 vtx = ld3(&a.verts[hull.vertexOffset + i]);
+        float curDot = dot3(vtx, planeNormalInConvex);
+        if (curDot > maxDot) {
+            maxDot = curDot;
+            if (numPoints == 64) numPoints--;
+        }
+        if (numPoints < 64) {
+            v3 vtxWorld = mmul(RB, vtx) + posB;
+            v3 vtxInPlane = mtmul(RA, vtxWorld - posA);
+            float dist = dot3(planeNormal, vtxInPlane) - planeConstant;
+            if (dist < 0.f) {
+                pts[numPoints] = make_float4(vtxWorld.x, vtxWorld.y, vtxWorld.z, dist);
+                numPoints++;
+            }
+        }
+    }
+    int idx[4];
+    int nred = reduce_contacts(pts, numPoints, planeNormalInConvex, idx);
+    if (nred > 0) {
+        b3gContact4& c = a.slots[pairIdx];
+        write_header(c, a, bodyA, bodyB, -planeNormalWorld, nred);
+        for (int i = 0; i < nred; i++) {
+            float4 q = pts[idx[i]];
+            c.worldPosB[i] = b3gFloat4{q.x, q.y, q.z, q.w};
+        }
+        a.flags[pairIdx] = 1;
+    }
+}
+
+// ------------------------------------------------------------------ plane (A) vs sphere (B)
+__device__ void plane_sphere(const NPArgs& a, int pairIdx, int bodyA, int bodyB) {
+    const b3gBody& BA = a.bodies[bodyA];
+    const b3gBody& BB = a.bodies[bodyB];
+    float4 pe = ldf4(&a.faces[a.cols[BA.collidableIdx].shapeIndex].plane);
+    float radius = a.cols[BB.collidableIdx].radius;
+    v3 posA = f4v3(BA.pos), posB = f4v3(BB.pos);
+    quat ornA = f4q(BA.quat), ornB = f4q(BB.quat);
+    v3 n = mk3(pe.x, pe.y, pe.z);
+    float planeConstant = pe.w;
+    m33 RA = qmat(ornA), RB = qmat(ornB);
+    // sphere point nearest the plane, expressed in the plane frame:
+    // vtx1 = (RB^T RA)(-n) * r ; vtxInPlane = RA^T (RB vtx1 + posB - posA)
+    v3 vtx1 = mtmul(RB, mmul(RA, -n)) * radius;
+    v3 vtxInPlane = mtmul(RA, (mmul(RB, vtx1) + posB) - posA);
+    float distance = dot3(n, vtxInPlane) - planeConstant;
+    if (distance < 0.f) {
+        v3 projected = vtxInPlane - distance * n;
+        v3 world = mmul(RA, projected) + posA;
+        v3 normalOnSurfaceB = mmul(RA, n);
+        v3 pOnB = world + normalOnSurfaceB * distance;
+        b3gContact4& c = a.slots[pairIdx];
+        write_header(c, a, bodyA, bodyB, -normalOnSurfaceB, 1);
+        c.worldPosB[0] = b3gFloat4{pOnB.x, pOnB.y, pOnB.z, distance};
+        a.flags[pairIdx] = 1;
+    }
+}
+
+// ------------------------------------------------------------------ sphere (A) vs hull (B)
+__device__ bool point_in_polygon(v3 p, const b3gFace& face, const b3gFloat4* base, const int* indices, v3& out) {
+    v3 plane = mk3(face.plane.x, face.plane.y, face.plane.z);
+    if (face.numIndices < 2) return false;
+    v3 b = ld3(&base[indices[face.indexOffset + face.numIndices - 1]]);
+    for (int i = 0; i < face.numIndices; i++) {
+        v3 a = b;
+        b = ld3(&base[indices[face.indexOffset + i]]);
+        v3 ab = b - a;
+        v3 ap = p - a;
+        v3 v = cross3(ab, plane);
+        if (dot3(ap, v) > 0.f) {
+            float ab_m2 = dot3(ab, ab);
+            float rt = ab_m2 != 0.f ? dot3(ab, ap) / ab_m2 : 0.f;
+            if (rt <= 0.f)
+                out = a;
+            else if (rt >= 1.f)
+                out = b;
+            else {
+                float s = 1.f - rt;
+                out = mk3(s * a.x + rt * b.x, s * a.y + rt * b.y, s * a.z + rt * b.z);
+            }
+            return false;
+        }
+    }
+    return true;
+}
+
+__device__ void sphere_hull(const NPArgs& a, int pairIdx, int bodyA, int bodyB) {
+    const b3gBody& BA = a.bodies[bodyA];
+    const b3gBody& BB = a.bodies[bodyB];
+    float radius = a.cols[BA.collidableIdx].radius;
+    v3 spherePos1 = f4v3(BA.pos);
+    v3 pos = f4v3(BB.pos);
+    m33 R = qmat(f4q(BB.quat));
+    v3 spherePos = mtmul(R, spherePos1 - pos);
+    const b3gHull hull = a.hulls[a.cols[BB.collidableIdx].shapeIndex];
+    v3 closest = mk3(0, 0, 0);
+    float minDist = -1000000.f;
+    bool bCollide = true;
+    v3 localHitNormal = mk3(0, 0, 0);
+    const b3gFloat4* base = &a.verts[hull.vertexOffset];
+    for (int f = 0; f < hull.numFaces; f++) {
+        const b3gFace face = a.faces[hull.faceOffset + f];
+        v3 n = mk3(face.plane.x, face.plane.y, face.plane.z);
+        float dist = dot3(n, spherePos) + face.plane.w;
+        v3 pntReturn = spherePos - dist * n;
+        if (dist > radius) {
+            bCollide = false;
+            break;
+        }
+        if (dist > 0.f) {
+            v3 out;
+            bool inPoly = point_in_polygon(spherePos, face, base, a.indices, out);
+            if (inPoly) {
+                if (dist > minDist) {
+                    minDist = dist;
+                    closest = pntReturn;
+                    localHitNormal = n;
+                }
+            } else {
+                v3 tmp = spherePos - out;
+                float l2 = dot3(tmp, tmp);
+                if (l2 < radius * radius) {
+                    dist = sqrtf(l2);
+                    if (dist > minDist) {
+                        minDist = dist;
+                        closest = out;
+                        localHitNormal = mk3(tmp.x / dist, tmp.y / dist, tmp.z / dist);
+                    }
+                } else {
+                    bCollide = false;
+                    break;
+                }
+            }
+        } else {
+            if (dist > minDist) {
+                minDist = dist;
+                closest = pntReturn;
+                localHitNormal = n;
+            }
+        }
+    }
+    if (bCollide && minDist > -10000.f) {
+        v3 normalOnSurfaceB = mmul(R, localHitNormal);
+        v3 pOnB = mmul(R, closest) + pos;
+        float actualDepth = minDist - radius;
+        if (actualDepth < 0.f) {
+            b3gContact4& c = a.slots[pairIdx];
+            write_header(c, a, bodyA, bodyB, normalOnSurfaceB, 1);
+            c.worldPosB[0] = b3gFloat4{pOnB.x, pOnB.y, pOnB.z, actualDepth};
+            a.flags[pairIdx] = 1;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ sphere vs sphere
+__device__ void sphere_sphere(const NPArgs& a, int pairIdx, int bodyA, int bodyB) {
+    const b3gBody& BA = a.bodies[bodyA];
+    const b3gBody& BB = a.bodies[bodyB];
+    float rA = a.cols[BA.collidableIdx].radius, rB = a.cols[BB.collidableIdx].radius;
+    v3 posA = f4v3(BA.pos), posB = f4v3(BB.pos);
+    v3 diff = posA - posB;
+    float len = sqrtf(dot3(diff, diff));
+    if (len <= (rA + rB)) {
+        float dist = len - (rA + rB);
+        v3 n = mk3(1.f, 0.f, 0.f);
+        if (len > 0.00001f) n = mk3(diff.x / len, diff.y / len, diff.z / len);
+        v3 cp = posB + n * rB;
+        b3gContact4& c = a.slots[pairIdx];
+        write_header(c, a, bodyA, bodyB, n, 1);
+        c.worldPosB[0] = b3gFloat4{cp.x, cp.y, cp.z, dist};
+        a.flags[pairIdx] = 1;
+    }
+}
+
+__device__ __forceinline__ int shape_type(const NPArgs& a, int body) { return a.cols[a.bodies[body].collidableIdx].shapeType; }
+
+__global__ void __launch_bounds__(NP_THREADS) k_primitive_pairs(NPArgs a, int type, int max_pairs) {
+    const int n = a.type_count[type];
+    const int* list = a.type_list + (size_t)type * max_pairs;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        int p = list[t];
+        b3gPair pr = a.pairs[p];
+        int A = pr.x, B = pr.y;
+        int ta = shape_type(a, A);
+        if (type == PT_PLANE_HULL) {
+            if (ta == B3G_SHAPE_PLANE) plane_hull(a, p, A, B);
+            else plane_hull(a, p, B, A);
+        } else if (type == PT_PLANE_SPHERE) {
+            if (ta == B3G_SHAPE_PLANE) plane_sphere(a, p, A, B);
+            else plane_sphere(a, p, B, A);
+        } else if (type == PT_SPHERE_HULL) {
+            if (ta == B3G_SHAPE_SPHERE) sphere_hull(a, p, A, B);
+            else sphere_hull(a, p, B, A);
+        } else if (type == PT_SPHERE_SPHERE) {
+            sphere_sphere(a, p, A, B);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ hull vs hull, one warp per pair
+struct AxisBest {
+    float d;
+    int idx;
+};
+__device__ __forceinline__ AxisBest warp_argmin(AxisBest x) {
+    for (int o = 16; o; o >>= 1) {
+        float od = __shfl_xor_sync(0xffffffffu, x.d, o);
+        int oi = __shfl_xor_sync(0xffffffffu, x.idx, o);
+        if (od < x.d || (od == x.d && oi < x.idx)) {
+            x.d = od;
+            x.idx = oi;
+        }
+    }
+    return x;
+}
+__device__ __forceinline__ AxisBest warp_argmax(AxisBest x) {
+    for (int o = 16; o; o >>= 1) {
+        float od = __shfl_xor_sync(0xffffffffu, x.d, o);
+        int oi = __shfl_xor_sync(0xffffffffu, x.idx, o);
+        if (od > x.d || (od == x.d && oi < x.idx)) {
+            x.d = od;
+            x.idx = oi;
+        }
+    }
+    return x;
+}
+
+// b3ProjectAxis: project the hull's local vertices on the axis rotated into its frame.
+__device__ __forceinline__ void project(const b3gFloat4* verts, int nv, v3 pos, const m33& R, v3 dir, float& mn,
+                                        float& mx) {
+    v3 localDir = mtmul(R, dir);
+    float offset = dot3(pos, dir);
+    mn = FLT_MAX;
+    mx = -FLT_MAX;
+    for (int i = 0; i < nv; i++) {
+        float dp = dot3(ld3(&verts[i]), localDir);
+        if (dp < mn) mn = dp;
+        if (dp > mx) mx = dp;
+    }
+    if (mn > mx) {
+        float t = mn; mn = mx; mx = t;
+    }
+    mn = mn + offset;
+    mx = mx + offset;
+}
+
+// Axis k of the SAT sequence: faces of A, faces of B, then edges (e0 of A major, e1 of B minor).
+// Returns false when the edge cross product is almost zero (axis skipped).
+__device__ __forceinline__ bool sat_axis(int k, const b3gHull& hA, const b3gHull& hB, const b3gFace* faces,
+                                         const b3gFloat4* edges, const m33& RA, const m33& RB, v3 deltaC2, v3& axis) {
+    if (k < hA.numFaces) {
+        v3 n = ld3(&faces[hA.faceOffset + k].plane);
+        axis = mmul(RA, n);
+    } else if (k < hA.numFaces + hB.numFaces) {
+        v3 n = ld3(&faces[hB.faceOffset + (k - hA.numFaces)].plane);
+        axis = mmul(RB, n);
+    } else {
+        int e = k - hA.numFaces - hB.numFaces;
+        int e0 = e / hB.numUniqueEdges, e1 = e - e0 * hB.numUniqueEdges;
+        v3 w0 = mmul(RA, ld3(&edges[hA.uniqueEdgesOffset + e0]));
+        v3 w1 = mmul(RB, ld3(&edges[hB.uniqueEdgesOffset + e1]));
+        v3 c = cross3(w0, w1);
+        // b3IsAlmostZero compares |c| against the double 1e-6
+        if (!((double)fabsf(c.x) > 1e-6 || (double)fabsf(c.y) > 1e-6 || (double)fabsf(c.z) > 1e-6)) return false;
+        axis = normalize3(c);
+    }
+    if (dot3(deltaC2, axis) < 0.f) axis = -axis;
+    return true;
+}
+
+// Sutherland-Hodgman clip of a polygon against one plane (b3ClipFace)
+__device__ int clip_face(const float4* in, int nin, v3 n, float eq, float4* out, unsigned int* status) {
+    if (nin < 2) return 0;
+    int nout = 0;
+    float4 first = in[nin - 1];
+    float ds = dot3(n, mk3(first.x, first.y, first.z)) + eq;
+    for (int ve = 0; ve < nin; ve++) {
+        float4 end = in[ve];
+        float de = dot3(n, mk3(end.x, end.y, end.z)) + eq;
+        if (ds < 0.f) {
+            if (de < 0.f) {
+                if (nout < CLIP_CAP) out[nout++] = end; else atomicOr(status, B3G_FLAG_CLIP_OVERFLOW);
+            } else {
+                float t = ds * 1.f / (ds - de);
+                float4 l = make_float4(first.x + (end.x - first.x) * t, first.y + (end.y - first.y) * t,
+                                       first.z + (end.z - first.z) * t, 0.f);
+                if (nout < CLIP_CAP) out[nout++] = l; else atomicOr(status, B3G_FLAG_CLIP_OVERFLOW);
+            }
+        } else {
+            if (de < 0.f) {
+                float t = ds * 1.f / (ds - de);
+                float4 l = make_float4(first.x + (end.x - first.x) * t, first.y + (end.y - first.y) * t,
+                                       first.z + (end.z - first.z) * t, 0.f);
+                if (nout < CLIP_CAP) out[nout++] = l; else atomicOr(status, B3G_FLAG_CLIP_OVERFLOW);
+                if (nout < CLIP_CAP) out[nout++] = end; else atomicOr(status, B3G_FLAG_CLIP_OVERFLOW);
+            }
+        }
+        first = end;
+        ds = de;
+    }
+    return nout;
+}
+
+static constexpr int HH_WARPS = 4;
+
+__global__ void __launch_bounds__(HH_WARPS * 32) k_hull_hull(NPArgs a, int max_pairs) {
+    __shared__ float4 s_poly[HH_WARPS][2][CLIP_CAP];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int n = a.type_count[PT_HULL_HULL];
+    const int* list = a.type_list + (size_t)PT_HULL_HULL * max_pairs;
+    const int nwarps = gridDim.x * HH_WARPS;
+    for (int t = blockIdx.x * HH_WARPS + wib; t < n; t += nwarps) {
+        const int p = list[t];
+        const b3gPair pr = a.pairs[p];
+        const int iA = pr.x, iB = pr.y;
+        const b3gBody& BA = a.bodies[iA];
+        const b3gBody& BB = a.bodies[iB];
+        const b3gHull hA = a.hulls[a.cols[BA.collidableIdx].shapeIndex];
+        const b3gHull hB = a.hulls[a.cols[BB.collidableIdx].shapeIndex];
+        const v3 posA = f4v3(BA.pos), posB = f4v3(BB.pos);
+        const m33 RA = qmat(f4q(BA.quat)), RB = qmat(f4q(BB.quat));
+        const v3 c0 = mmul(RA, f4v3(hA.localCenter)) + posA;
+        const v3 c1 = mmul(RB, f4v3(hB.localCenter)) + posB;
+        const v3 deltaC2 = c0 - c1;
+        const int naxes = hA.numFaces + hB.numFaces + hA.numUniqueEdges * hB.numUniqueEdges;
+        AxisBest best{FLT_MAX, 0x7fffffff};
+        bool separated = false;
+        const b3gFloat4* vA = &a.verts[hA.vertexOffset];
+        const b3gFloat4* vB = &a.verts[hB.vertexOffset];
+        for (int k = lane; k < naxes; k += 32) {
+            v3 axis;
+            if (!sat_axis(k, hA, hB, a.faces, a.edges, RA, RB, deltaC2, axis)) continue;
+            float min0, max0, min1, max1;
+            project(vA, hA.numVertices, posA, RA, axis, min0, max0);
+            project(vB, hB.numVertices, posB, RB, axis, min1, max1);
+            if (max0 < min1 || max1 < min0) {
+                separated = true;
+                continue;
+            }
+            float d0 = max0 - min1, d1 = max1 - min0;
+            float depth = d0 < d1 ? d0 : d1;
+            if (depth < best.d || (depth == best.d && k < best.idx)) {
+                best.d = depth;
+                best.idx = k;
+            }
+        }
+        if (__any_sync(0xffffffffu, separated)) continue;
+        best = warp_argmin(best);
+        if (best.idx == 0x7fffffff) continue;  // no usable axis (degenerate)
+        v3 sep;
+        sat_axis(best.idx, hA, hB, a.faces, a.edges, RA, RB, deltaC2, sep);
+        if (dot3(-deltaC2, sep) > 0.0f) sep = -sep;
+
+        // incident face of B: max dot(world normal, sep), first max wins
+        AxisBest fb{-FLT_MAX, 0x7fffffff};
+        for (int f = lane; f < hB.numFaces; f += 32) {
+            float d = dot3(mmul(RB, ld3(&a.faces[hB.faceOffset + f].plane)), sep);
+            if (d > fb.d || (d == fb.d && f < fb.idx)) { fb.d = d; fb.idx = f; }
+        }
+        fb = warp_argmax(fb);
+        // reference face of A: min dot(world normal, sep), first min wins
+        AxisBest fa{FLT_MAX, 0x7fffffff};
+        for (int f = lane; f < hA.numFaces; f += 32) {
+            float d = dot3(mmul(RA, ld3(&a.faces[hA.faceOffset + f].plane)), sep);
+            if (d < fa.d || (d == fa.d && f < fa.idx)) { fa.d = d; fa.idx = f; }
+        }
+        fa = warp_argmin(fa);
+        if (fb.idx == 0x7fffffff || fa.idx == 0x7fffffff) continue;
+
+        if (lane == 0) {
+            float4* pin = s_poly[wib][0];
+            float4* pout = s_poly[wib][1];
+            const b3gFace polyB = a.faces[hB.faceOffset + fb.idx];
+            int nin = 0;
+            for (int e = 0; e < polyB.numIndices && e < CLIP_CAP; e++) {
+                v3 w = mmul(RB, ld3(&vB[a.indices[polyB.indexOffset + e]])) + posB;
+                pin[nin++] = make_float4(w.x, w.y, w.z, 0.f);
+            }
+            const b3gFace polyA = a.faces[hA.faceOffset + fa.idx];
+            const v3 planeNormalA = mk3(polyA.plane.x, polyA.plane.y, polyA.plane.z);
+            const v3 worldPlaneAnormal1 = mmul(RA, planeNormalA);
+            const int nva = polyA.numIndices;
+            for (int e0 = 0; e0 < nva; e0++) {
+                v3 va = ld3(&vA[a.indices[polyA.indexOffset + e0]]);
+                v3 vb = ld3(&vA[a.indices[polyA.indexOffset + ((e0 + 1) % nva)]]);
+                v3 worldEdge0 = mmul(RA, va - vb);
+                v3 planeNormalWS1 = -cross3(worldEdge0, worldPlaneAnormal1);
+                v3 worldA1 = mmul(RA, va) + posA;
+                float planeEqWS1 = -dot3(worldA1, planeNormalWS1);
+                int nout = clip_face(pin, nin, planeNormalWS1, planeEqWS1, pout, a.status);
+                float4* tmp = pout; pout = pin; pin = tmp;
+                nin = nout;
+            }
+            // keep points behind the reference face; depth clamped at minDist=-1, kept if <= maxDist=0
+            const float planeEqWS = polyA.plane.w - dot3(worldPlaneAnormal1, posA);
+            int ncont = 0;
+            for (int i = 0; i < nin; i++) {
+                float depth = dot3(worldPlaneAnormal1, mk3(pin[i].x, pin[i].y, pin[i].z)) + planeEqWS;
+                if (depth <= -1.0f) depth = -1.0f;
+                if (depth <= 0.0f) pout[ncont++] = make_float4(pin[i].x, pin[i].y, pin[i].z, depth);
+            }
+            if (ncont > 0) {
+                int idx[4];
+                int np = reduce_contacts(pout, ncont, sep, idx);
+                b3gContact4& c = a.slots[p];
+                write_header(c, a, iA, iB, sep, np);
+                for (int q = 0; q < np; q++) {
+                    float4 v = pout[idx[q]];
+                    c.worldPosB[q] = b3gFloat4{v.x, v.y, v.z, v.w};
+                }
+                a.flags[p] = 1;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// manifold list in pair order + pair.z = manifold index + point count
+__global__ void k_manifold_list(const int* __restrict__ flags, const int* __restrict__ cidx,
+                                const int* __restrict__ d_np, const b3gContact4* __restrict__ slots,
+                                b3gPair* __restrict__ pairs, int* __restrict__ manifold_pair,
+                                int* __restrict__ num_points) {
+    const int np = *d_np;
+    int local = 0;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+        if (flags[p]) {
+            int m = cidx[p];
+            manifold_pair[m] = p;
+            pairs[p].z = m;
+            local += (int)slots[p].worldNormalOnB.w;
+        }
+    }
+    for (int o = 16; o; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(num_points, local);
+}
+
+__global__ void k_compact_contacts(const int* __restrict__ d_nc, const int* __restrict__ manifold_pair,
+                                   const b3gContact4* __restrict__ slots, b3gContact4* __restrict__ out) {
+    const int nc = *d_nc;
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nc; m += gridDim.x * blockDim.x)
+        out[m] = slots[manifold_pair[m]];
+}
+
+static NPArgs make_args(DeviceState& d, unsigned short friction_cmp) {
+    NPArgs a;
+    a.bodies = d.bodies;
+    a.cols = d.collidables;
+    a.hulls = d.hulls;
+    a.faces = d.faces;
+    a.indices = d.indices;
+    a.verts = d.vertices;
+    a.edges = d.edges;
+    a.pairs = d.pairs;
+    a.type_list = d.type_lists;
+    a.type_count = d.counters->type_count;
+    a.slots = d.contact_slots;
+    a.flags = d.contact_flag;
+    a.status = &d.counters->status;
+    a.friction_cmp = friction_cmp;
+    return a;
+}
+
+unsigned short friction_to_cmp(float f) {
+    if (f < 0.f) f = 0.f;
+    if (f > 1.f) f = 1.f;
+    return (unsigned short)(f * 65535.0f);
+}
+
+int launch_contacts(DeviceState& d, float friction, cudaStream_t s) {
+    NPArgs a = make_args(d, friction_to_cmp(friction));
+    int grid = d.num_sms * 4;
+    for (int t = PT_PLANE_HULL; t < PT_COUNT; t++) k_primitive_pairs<<<grid, NP_THREADS, 0, s>>>(a, t, d.max_pairs);
+    k_hull_hull<<<d.num_sms * 16, HH_WARPS * 32, 0, s>>>(a, d.max_pairs);
+    long long ll = 0;
+    int* d_np = &d.counters->pad[0];
+    exclusive_scan_i32(d.prim, d.contact_flag, d.contact_index, d_np, &d.counters->num_contacts, d.scan_scratch, s,
+                       &ll);
+    k_manifold_list<<<grid, NP_THREADS, 0, s>>>(d.contact_flag, d.contact_index, d_np, d.contact_slots, d.pairs,
+                                                d.manifold_pair, &d.counters->num_points);
+    return 4 + 1 + 1 + (int)ll;
+}
+
+int launch_compact_contacts(DeviceState& d, cudaStream_t s) {
+    k_compact_contacts<<<d.num_sms * 4, NP_THREADS, 0, s>>>(&d.counters->num_contacts, d.manifold_pair,
+                                                            d.contact_slots, d.contacts_compact);
+    return 1;
+}
+
+}  // namespace b3g

@@ -1,0 +1,642 @@
+// Contact solver: b3PgsJacobiSolver semantics on the GPU.
+//
+// Reference (paths relative to the reference's src/Bullet3Dynamics/ConstraintSolver/):
+//   solveGroup                       b3PgsJacobiSolver.cpp:170-189
+//   per-body split counts (Jacobi)   :1020-1042
+//   convertContact                   :847-983   (2 friction directions, velocity dependent, no caching)
+//   setupContactConstraint           :654-804   (erp 0.2, no split impulse, restitution 0, cold start)
+//   setupFrictionConstraint          :457-536
+//   solveSingleIteration             :1281-1486 (all contact rows, [Jacobi: average], all friction rows)
+//   resolveSingleConstraintRowLowerLimit / Generic :236-317 (scalar path; USE_SIMD is not defined in Bullet3)
+//   averageVelocities                :1552-1587
+//   solveGroupCacheFriendlyFinish    :1589-1691 (PGS: v += dv; Jacobi: v += (S/count) once per split copy)
+//
+// GB300 design: rows are built one thread per manifold; the iterations run in ONE
+// cooperative persistent kernel with a bounded grid barrier:
+//   PGS    : parallel greedy colouring of manifolds (per round, a manifold takes the colour when it
+//            holds the highest hashed priority on both of its dynamic bodies -- exact per-body claims,
+//            no aliasing), counting sort by colour, then per iteration: contact rows colour by colour,
+//            friction rows colour by colour, one barrier per colour.
+//   Jacobi : per iteration: contact rows of every manifold on its own split copies, a per-body
+//            ordered reduction (same summation order as the reference's solver-body pool), friction
+//            rows, reduction.  Split copies live in a per-manifold array, per-body lists come from a
+//            stable radix sort, so the arithmetic matches the sequential reference order.
+#include <cfloat>
+
+#include "common.cuh"
+#include "world_internal.h"
+
+namespace b3g {
+
+static constexpr int SV_THREADS = 256;
+static constexpr float LARGE_UPPER = 1e10f;
+
+struct SolverArgs {
+    const b3gBody* bodies;
+    const b3gInertia* inertias;
+    const b3gContact4* slots;
+    const int* manifold_pair;
+    const int* d_nc;          // number of manifolds
+    SolverRow* rows;          // 12 per manifold
+    int4* hdr;                // bodyA, bodyB, active point mask, num points
+    float2* inv_mass;         // invMass A, B
+    float4* dv;               // per body: [2b] lin, [2b+1] ang (PGS, and Jacobi averaged delta)
+    float4* dv_sum;           // Jacobi: per body sum of split deltas from the last averaging
+    float4* split;            // Jacobi: per manifold 4 float4: A lin, A ang, B lin, B ang
+    const int* body_count;    // Jacobi split counts (manifolds per dynamic body)
+    const int* list_off;      // Jacobi per-body list offsets (exclusive scan of counts)
+    const uint32_t* list;     // Jacobi: entries 2*m+side grouped by body, in manifold order
+    int* color;               // per manifold
+    int* color_order;
+    int* color_offsets;       // B3G_MAX_COLORS + 2
+    int* color_fill;          // B3G_MAX_COLORS + 1
+    int* remaining;           // per round
+    unsigned long long* claim;
+    b3gBody* bodies_out;      // velocities written at finish
+    DevCounters* counters;
+    double* residual_acc;     // 2 per iteration
+    int num_bodies;
+    int mode;
+    int iterations;
+    float residual_tol;
+    float dt;
+    float erp;
+    float threshold;
+    GridBarrier bar;
+    unsigned int spin_limit;
+};
+
+// b3PlaneSpace1 (Bullet3Common/b3Vector3.h:1184-1212)
+__device__ __forceinline__ void plane_space(v3 n, v3& p, v3& q) {
+    if (fabsf(n.z) > 0.7071067811865475244008443621048490f) {
+        float a = n.y * n.y + n.z * n.z;
+        float k = 1.0f / sqrtf(a);
+        p = mk3(0.f, -n.z * k, n.y * k);
+        q = mk3(a * k, -n.x * p.z, n.x * p.y);
+    } else {
+        float a = n.x * n.x + n.y * n.y;
+        float k = 1.0f / sqrtf(a);
+        p = mk3(-n.y * k, n.x * k, 0.f);
+        q = mk3(-n.z * p.y, n.z * p.x, a * k);
+    }
+}
+
+__device__ __forceinline__ float4 f4(v3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
+__device__ __forceinline__ v3 xyz(float4 a) { return mk3(a.x, a.y, a.z); }
+
+// Jacobi split counts: number of manifolds touching each dynamic body.
+__global__ void k_count_manifolds(const b3gContact4* __restrict__ slots, const int* __restrict__ manifold_pair,
+                                  const int* __restrict__ d_nc, const b3gBody* __restrict__ bodies,
+                                  int* __restrict__ body_count, uint32_t* __restrict__ keys,
+                                  uint32_t* __restrict__ vals, uint32_t sentinel, int* __restrict__ d_n2) {
+    const int nc = *d_nc;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *d_n2 = 2 * nc;
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nc; m += gridDim.x * blockDim.x) {
+        const b3gContact4& c = slots[manifold_pair[m]];
+        int a = abs(c.bodyA), b = abs(c.bodyB);
+        bool da = bodies[a].invMass != 0.f, db = bodies[b].invMass != 0.f;
+        if (da) atomicAdd(&body_count[a], 1);
+        if (db) atomicAdd(&body_count[b], 1);
+        keys[2 * m] = da ? (uint32_t)a : sentinel;
+        vals[2 * m] = 2u * m;
+        keys[2 * m + 1] = db ? (uint32_t)b : sentinel;
+        vals[2 * m + 1] = 2u * m + 1u;
+    }
+}
+
+// Row setup: setupContactConstraint + convertContact friction rows.
+__global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
+    const int nc = *a.d_nc;
+    const bool pgs = a.mode == B3G_SOLVER_PGS;
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nc; m += gridDim.x * blockDim.x) {
+        const b3gContact4 c = a.slots[a.manifold_pair[m]];
+        const int iA = abs(c.bodyA), iB = abs(c.bodyB);
+        const b3gBody& A = a.bodies[iA];
+        const b3gBody& B = a.bodies[iB];
+        const float imA = A.invMass, imB = B.invMass;
+        int np = (int)c.worldNormalOnB.w;
+        if (np > 4) np = 4;
+        int mask = 0;
+        a.color[m] = -1;
+        a.inv_mass[m] = make_float2(imA, imB);
+        SolverRow* R = a.rows + (size_t)m * 12;
+        if (imA == 0.f && imB == 0.f) np = 0;  // static-static: no rows (b3PgsJacobiSolver.cpp:864-866)
+        const b3gMat3 IA = a.inertias[iA].invInertiaWorld;
+        const b3gMat3 IB = a.inertias[iB].invInertiaWorld;
+        const v3 posA = f4v3(A.pos), posB = f4v3(B.pos);
+        const v3 linA = f4v3(A.linVel), angA = f4v3(A.angVel);
+        const v3 linB = f4v3(B.linVel), angB = f4v3(B.angVel);
+        float countA = 1.f, countB = 1.f;
+        if (!pgs) {
+            if (imA != 0.f) countA = (float)a.body_count[iA];
+            if (imB != 0.f) countB = (float)a.body_count[iB];
+        }
+        // getContactPoint: normalised normal
+        v3 n0 = mk3(c.worldNormalOnB.x, c.worldNormalOnB.y, c.worldNormalOnB.z);
+        v3 n = normalize3(n0);
+        for (int j = 0; j < np; j++) {
+            const float dist = c.worldPosB[j].w;
+            if (!(dist <= a.threshold)) continue;
+            mask |= 1 << j;
+            const v3 pos2 = mk3(c.worldPosB[j].x, c.worldPosB[j].y, c.worldPosB[j].z);
+            const v3 pos1 = pos2 + n * dist;
+            const v3 rel1 = pos1 - posA;
+            const v3 rel2 = pos2 - posB;
+            // contact row
+            {
+                v3 torqueAxis0 = cross3(rel1, n);
+                v3 angCompA = imul(IA, torqueAxis0);
+                v3 torqueAxis1 = cross3(rel2, n);
+                v3 angCompB = imul(IB, -torqueAxis1);
+                float denom0 = imA + dot3(n, cross3(angCompA, rel1));
+                float denom1 = imB + dot3(n, cross3(-angCompB, rel2));
+                float jac = 1.0f / (denom0 + denom1);
+                float scaled = pgs ? jac : 1.0f / (denom0 * countA + denom1 * countB);
+                v3 r1xn = torqueAxis0, r2xn = -torqueAxis1;
+                float penetration = dist + 0.0f;
+                float vel1Dotn = dot3(n, linA) + dot3(r1xn, angA);
+                float vel2Dotn = -dot3(n, linB) + dot3(r2xn, angB);
+                float rel_vel = vel1Dotn + vel2Dotn;
+                float positionalError = 0.f;
+                float velocityError = 0.0f - rel_vel;
+                if (penetration > 0.f)
+                    velocityError -= penetration / a.dt;
+                else
+                    positionalError = -penetration * a.erp / a.dt;
+                float rhs = positionalError * scaled + velocityError * scaled;
+                SolverRow r;
+                r.normal_jac = f4(n, jac);
+                r.r1xn_rhs = f4(r1xn, rhs);
+                r.r2xn_imp = f4(r2xn, 0.f);
+                r.angA_fric = f4(angCompA, (float)c.frictionCmp / (float)0xffff);
+                r.angB_pad = f4(angCompB, 0.f);
+                R[j] = r;
+            }
+            // friction rows
+            {
+                v3 vel1 = linA + cross3(angA, rel1);
+                v3 vel2 = linB + cross3(angB, rel2);
+                v3 vel = vel1 - vel2;
+                float rel_vel = dot3(n, vel);
+                v3 dir1 = vel - n * rel_vel;
+                float lat = dot3(dir1, dir1);
+                v3 dir2;
+                if (lat > FLT_EPSILON) {
+                    float inv = 1.f / sqrtf(lat);
+                    dir1 = dir1 * inv;
+                    dir2 = cross3(dir1, n);
+                    float l2 = sqrtf(dot3(dir2, dir2));
+                    dir2 = dir2 * (1.f / l2);
+                } else {
+                    plane_space(n, dir1, dir2);
+                }
+                const float fric = (float)c.frictionCmp / (float)0xffff;
+                v3 dirs[2] = {dir2, dir1};
+                for (int k = 0; k < 2; k++) {
+                    v3 d = dirs[k];
+                    v3 r1xn = cross3(rel1, d);
+                    v3 angCompA = imul(IA, r1xn);
+                    v3 r2xn = cross3(rel2, -d);
+                    v3 angCompB = imul(IB, r2xn);
+                    float denom0 = imA + dot3(d, cross3(angCompA, rel1));
+                    float denom1 = imB + dot3(d, cross3(-angCompB, rel2));
+                    float jac = 1.0f / (denom0 + denom1);
+                    float scaled = pgs ? jac : 1.0f / (denom0 * countA + denom1 * countB);
+                    float v1 = dot3(d, linA) + dot3(r1xn, angA);
+                    float v2 = -dot3(d, linB) + dot3(r2xn, angB);
+                    float rv = v1 + v2;
+                    float velocityError = 0.0f - rv;
+                    SolverRow r;
+                    r.normal_jac = f4(d, jac);
+                    r.r1xn_rhs = f4(r1xn, velocityError * scaled);
+                    r.r2xn_imp = f4(r2xn, 0.f);
+                    r.angA_fric = f4(angCompA, fric);
+                    r.angB_pad = f4(angCompB, 0.f);
+                    R[4 + 2 * j + k] = r;
+                }
+            }
+        }
+        a.hdr[m] = make_int4(iA, iB, mask, np);
+    }
+}
+
+// One row against two body deltas; returns the impulse change.
+template <bool FRICTION>
+__device__ __forceinline__ void solve_row(SolverRow& r, float lower, float upper, v3& dlA, v3& daA, v3& dlB, v3& daB,
+                                          float imA, float imB, float& delta_out) {
+    v3 n = xyz(r.normal_jac);
+    float jac = r.normal_jac.w;
+    float rhs = r.r1xn_rhs.w;
+    float applied = r.r2xn_imp.w;
+    float deltaImpulse = rhs - applied * 0.0f;
+    float dv1 = dot3(n, dlA) + dot3(xyz(r.r1xn_rhs), daA);
+    float dv2 = -dot3(n, dlB) + dot3(xyz(r.r2xn_imp), daB);
+    deltaImpulse -= dv1 * jac;
+    deltaImpulse -= dv2 * jac;
+    float sum = applied + deltaImpulse;
+    if (sum < lower) {
+        deltaImpulse = lower - applied;
+        applied = lower;
+    } else if (FRICTION && sum > upper) {
+        deltaImpulse = upper - applied;
+        applied = upper;
+    } else {
+        applied = sum;
+    }
+    r.r2xn_imp.w = applied;
+    dlA = dlA + (n * imA) * deltaImpulse;
+    daA = daA + xyz(r.angA_fric) * deltaImpulse;
+    dlB = dlB + ((-n) * imB) * deltaImpulse;
+    daB = daB + xyz(r.angB_pad) * deltaImpulse;
+    delta_out = deltaImpulse;
+}
+
+// Solve the contact rows (pass 0) or friction rows (pass 1) of manifold m on the given deltas.
+__device__ __forceinline__ void solve_manifold(const SolverArgs& a, int m, int pass, v3& dlA, v3& daA, v3& dlB,
+                                               v3& daB, float imA, float imB, int mask, float& res_d, float& res_l) {
+    SolverRow* R = a.rows + (size_t)m * 12;
+    if (pass == 0) {
+        for (int j = 0; j < 4; j++) {
+            if (!(mask & (1 << j))) continue;
+            SolverRow r = R[j];
+            float old = r.r2xn_imp.w, d;
+            solve_row<false>(r, 0.f, LARGE_UPPER, dlA, daA, dlB, daB, imA, imB, d);
+            R[j].r2xn_imp.w = r.r2xn_imp.w;
+            float nd = r.r2xn_imp.w - old;
+            res_d += nd * nd;
+            res_l += r.r2xn_imp.w * r.r2xn_imp.w;
+        }
+    } else {
+        for (int j = 0; j < 4; j++) {
+            if (!(mask & (1 << j))) continue;
+            float totalImpulse = R[j].r2xn_imp.w;
+            for (int k = 0; k < 2; k++) {
+                SolverRow& rr = R[4 + 2 * j + k];
+                if (totalImpulse > 0.f) {
+                    SolverRow r = rr;
+                    float fr = r.angA_fric.w;
+                    float lower = -(fr * totalImpulse);
+                    float upper = fr * totalImpulse;
+                    float old = r.r2xn_imp.w, d;
+                    solve_row<true>(r, lower, upper, dlA, daA, dlB, daB, imA, imB, d);
+                    rr.r2xn_imp.w = r.r2xn_imp.w;
+                    float nd = r.r2xn_imp.w - old;
+                    res_d += nd * nd;
+                }
+                float l = rr.r2xn_imp.w;
+                res_l += l * l;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void block_accumulate(double* dst, float x, float y) {
+    __shared__ float sx[SV_THREADS / 32], sy[SV_THREADS / 32];
+    for (int o = 16; o; o >>= 1) {
+        x += __shfl_xor_sync(0xffffffffu, x, o);
+        y += __shfl_xor_sync(0xffffffffu, y, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sx[threadIdx.x >> 5] = x;
+        sy[threadIdx.x >> 5] = y;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float tx = 0, ty = 0;
+        for (int w = 0; w < SV_THREADS / 32; w++) {
+            tx += sx[w];
+            ty += sy[w];
+        }
+        if (tx != 0.f) atomicAdd(&dst[0], (double)tx);
+        if (ty != 0.f) atomicAdd(&dst[1], (double)ty);
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ unsigned int hash32(unsigned int x) {
+    x ^= x >> 16;
+    x *= 0x7feb352dU;
+    x ^= x >> 15;
+    x *= 0x846ca68bU;
+    x ^= x >> 16;
+    return x;
+}
+
+// ------------------------------------------------------------------ persistent PGS kernel
+__global__ void __launch_bounds__(SV_THREADS) k_solve_pgs(SolverArgs a) {
+    const int nc = *a.d_nc;
+    const unsigned nb = gridDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int stride = gridDim.x * blockDim.x;
+    // ---- colouring
+    int ncolors = 0;
+    for (int r = 0; r < B3G_MAX_COLORS; r++) {
+        const unsigned long long rk = (unsigned long long)r << 56;
+        for (int m = tid; m < nc; m += stride) {
+            if (a.color[m] >= 0) continue;
+            int4 h = a.hdr[m];
+            float2 im = a.inv_mass[m];
+            unsigned long long key = rk | ((unsigned long long)(hash32((unsigned)m) & 0xFFFFFFu) << 32) | (unsigned)m;
+            if (im.x != 0.f) atomicMax(&a.claim[h.x], key);
+            if (im.y != 0.f) atomicMax(&a.claim[h.y], key);
+        }
+        if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
+        int left = 0;
+        for (int m = tid; m < nc; m += stride) {
+            if (a.color[m] >= 0) continue;
+            int4 h = a.hdr[m];
+            float2 im = a.inv_mass[m];
+            unsigned long long key = rk | ((unsigned long long)(hash32((unsigned)m) & 0xFFFFFFu) << 32) | (unsigned)m;
+            bool okA = im.x == 0.f || a.claim[h.x] == key;
+            bool okB = im.y == 0.f || a.claim[h.y] == key;
+            if (okA && okB) {
+                a.color[m] = r;
+                atomicAdd(&a.color_fill[r], 1);
+            } else {
+                left++;
+            }
+        }
+        for (int o = 16; o; o >>= 1) left += __shfl_xor_sync(0xffffffffu, left, o);
+        if ((threadIdx.x & 31) == 0 && left) atomicAdd(&a.remaining[r], left);
+        if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
+        ncolors = r + 1;
+        if (*((volatile int*)&a.remaining[r]) == 0) break;
+    }
+    const bool overflow = *((volatile int*)&a.remaining[ncolors - 1 < 0 ? 0 : ncolors - 1]) != 0 && nc > 0;
+    // ---- counting sort by colour (order inside a colour is irrelevant: its manifolds are independent)
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        int s = 0;
+        for (int c = 0; c < ncolors; c++) {
+            a.color_offsets[c] = s;
+            s += a.color_fill[c];
+            a.color_fill[c] = 0;
+        }
+        a.color_offsets[ncolors] = s;
+        a.counters->num_colors = ncolors;
+        if (overflow) atomicOr(&a.counters->status, B3G_FLAG_BATCH_OVERFLOW);
+    }
+    if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
+    for (int m = tid; m < nc; m += stride) {
+        int c = a.color[m];
+        if (c >= 0) a.color_order[a.color_offsets[c] + atomicAdd(&a.color_fill[c], 1)] = m;
+    }
+    if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
+    // ---- iterations
+    int it = 0;
+    for (; it < a.iterations; it++) {
+        float res_d = 0.f, res_l = 0.f;
+        for (int pass = 0; pass < 2; pass++) {
+            for (int c = 0; c < ncolors; c++) {
+                const int lo = a.color_offsets[c], hi = a.color_offsets[c + 1];
+                for (int k = lo + tid; k < hi; k += stride) {
+                    const int m = a.color_order[k];
+                    const int4 h = a.hdr[m];
+                    if (!h.z) continue;
+                    const float2 im = a.inv_mass[m];
+                    v3 dlA = xyz(a.dv[2 * h.x]), daA = xyz(a.dv[2 * h.x + 1]);
+                    v3 dlB = xyz(a.dv[2 * h.y]), daB = xyz(a.dv[2 * h.y + 1]);
+                    solve_manifold(a, m, pass, dlA, daA, dlB, daB, im.x, im.y, h.z, res_d, res_l);
+                    if (im.x != 0.f) {
+                        a.dv[2 * h.x] = f4(dlA, 0.f);
+                        a.dv[2 * h.x + 1] = f4(daA, 0.f);
+                    }
+                    if (im.y != 0.f) {
+                        a.dv[2 * h.y] = f4(dlB, 0.f);
+                        a.dv[2 * h.y + 1] = f4(daB, 0.f);
+                    }
+                }
+                if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
+            }
+            // colour-overflow leftovers: one thread, in manifold order (always correct, slow)
+            if (overflow && tid == 0) {
+                for (int m = 0; m < nc; m++) {
+                    if (a.color[m] >= 0) continue;
+                    const int4 h = a.hdr[m];
+                    if (!h.z) continue;
+                    const float2 im = a.inv_mass[m];
+                    v3 dlA = xyz(a.dv[2 * h.x]), daA = xyz(a.dv[2 * h.x + 1]);
+                    v3 dlB = xyz(a.dv[2 * h.y]), daB = xyz(a.dv[2 * h.y + 1]);
+                    solve_manifold(a, m, pass, dlA, daA, dlB, daB, im.x, im.y, h.z, res_d, res_l);
+                    if (im.x != 0.f) { a.dv[2 * h.x] = f4(dlA, 0.f); a.dv[2 * h.x + 1] = f4(daA, 0.f); }
+                    if (im.y != 0.f) { a.dv[2 * h.y] = f4(dlB, 0.f); a.dv[2 * h.y + 1] = f4(daB, 0.f); }
+                }
+            }
+            if (overflow && !grid_barrier(a.bar, nb, a.spin_limit)) return;
+        }
+        block_accumulate(a.residual_acc + 2 * it, res_d, res_l);
+        if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
+        double dd = *((volatile double*)&a.residual_acc[2 * it]);
+        double ll = *((volatile double*)&a.residual_acc[2 * it + 1]);
+        double r = sqrt(dd) / fmax(sqrt(ll), 1e-12);
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            a.counters->residual = (float)r;
+            a.counters->iterations = it + 1;
+        }
+        if (a.residual_tol > 0.f && r <= (double)a.residual_tol) {
+            it++;
+            break;
+        }
+    }
+    // ---- finish: v += dv for dynamic bodies
+    for (int b = tid; b < a.num_bodies; b += stride) {
+        if (a.bodies[b].invMass == 0.f) continue;
+        v3 dl = xyz(a.dv[2 * b]), da = xyz(a.dv[2 * b + 1]);
+        b3gBody& B = a.bodies_out[b];
+        B.linVel.x = B.linVel.x + dl.x;
+        B.linVel.y = B.linVel.y + dl.y;
+        B.linVel.z = B.linVel.z + dl.z;
+        B.angVel.x = B.angVel.x + da.x;
+        B.angVel.y = B.angVel.y + da.y;
+        B.angVel.z = B.angVel.z + da.z;
+    }
+}
+
+// ------------------------------------------------------------------ persistent Jacobi kernel
+__device__ __forceinline__ void jacobi_average(const SolverArgs& a, int tid, int stride) {
+    for (int b = tid; b < a.num_bodies; b += stride) {
+        const int cnt = a.body_count[b];
+        if (cnt <= 0) continue;
+        const int off = a.list_off[b];
+        v3 sl = mk3(0.f, 0.f, 0.f), sa = mk3(0.f, 0.f, 0.f);
+        for (int k = 0; k < cnt; k++) {
+            uint32_t e = a.list[off + k];
+            uint32_t m = e >> 1, side = e & 1u;
+            sl = sl + xyz(a.split[4 * m + 2 * side]);
+            sa = sa + xyz(a.split[4 * m + 2 * side + 1]);
+        }
+        float factor = 1.f / (float)cnt;
+        a.dv_sum[2 * b] = f4(sl, 0.f);
+        a.dv_sum[2 * b + 1] = f4(sa, 0.f);
+        a.dv[2 * b] = f4(sl * factor, 0.f);
+        a.dv[2 * b + 1] = f4(sa * factor, 0.f);
+    }
+}
+
+__global__ void __launch_bounds__(SV_THREADS) k_solve_jacobi(SolverArgs a) {
+    const int nc = *a.d_nc;
+    const unsigned nb = gridDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int stride = gridDim.x * blockDim.x;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.counters->num_colors = 0;
+    int it = 0;
+    for (; it < a.iterations; it++) {
+        float res_d = 0.f, res_l = 0.f;
+        for (int pass = 0; pass < 2; pass++) {
+            for (int m = tid; m < nc; m += stride) {
+                const int4 h = a.hdr[m];
+                const float2 im = a.inv_mass[m];
+                v3 dlA = mk3(0, 0, 0), daA = mk3(0, 0, 0), dlB = mk3(0, 0, 0), daB = mk3(0, 0, 0);
+                if (im.x != 0.f) { dlA = xyz(a.dv[2 * h.x]); daA = xyz(a.dv[2 * h.x + 1]); }
+                if (im.y != 0.f) { dlB = xyz(a.dv[2 * h.y]); daB = xyz(a.dv[2 * h.y + 1]); }
+                if (h.z) solve_manifold(a, m, pass, dlA, daA, dlB, daB, im.x, im.y, h.z, res_d, res_l);
+                a.split[4 * m + 0] = f4(dlA, 0.f);
+                a.split[4 * m + 1] = f4(daA, 0.f);
+                a.split[4 * m + 2] = f4(dlB, 0.f);
+                a.split[4 * m + 3] = f4(daB, 0.f);
+            }
+            if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
+            jacobi_average(a, tid, stride);
+            if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
+        }
+        block_accumulate(a.residual_acc + 2 * it, res_d, res_l);
+        if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
+        double dd = *((volatile double*)&a.residual_acc[2 * it]);
+        double ll = *((volatile double*)&a.residual_acc[2 * it + 1]);
+        double r = sqrt(dd) / fmax(sqrt(ll), 1e-12);
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            a.counters->residual = (float)r;
+            a.counters->iterations = it + 1;
+        }
+        if (a.residual_tol > 0.f && r <= (double)a.residual_tol) {
+            it++;
+            break;
+        }
+    }
+    // finish: body velocity += (S * 1/count), applied once per split copy
+    for (int b = tid; b < a.num_bodies; b += stride) {
+        const int cnt = a.body_count[b];
+        if (cnt <= 0) continue;
+        float factor = 1.f / (float)cnt;
+        v3 dl = xyz(a.dv_sum[2 * b]) * factor, da = xyz(a.dv_sum[2 * b + 1]) * factor;
+        b3gBody& B = a.bodies_out[b];
+        v3 lv = f4v3(B.linVel), av = f4v3(B.angVel);
+        for (int k = 0; k < cnt; k++) {
+            lv = lv + dl;
+            av = av + da;
+        }
+        B.linVel.x = lv.x; B.linVel.y = lv.y; B.linVel.z = lv.z;
+        B.angVel.x = av.x; B.angVel.y = av.y; B.angVel.z = av.z;
+    }
+}
+
+__global__ void k_reset_solver(int* color_fill, int* remaining, unsigned int* barrier, double* residual_acc,
+                               int nres, DevCounters* counters) {
+    for (int i = threadIdx.x; i < B3G_MAX_COLORS + 1; i += blockDim.x) {
+        color_fill[i] = 0;
+        remaining[i] = 0;
+    }
+    for (int i = threadIdx.x; i < nres; i += blockDim.x) residual_acc[i] = 0.0;
+    if (threadIdx.x < 4) barrier[threadIdx.x] = 0;
+    if (threadIdx.x == 0) {
+        counters->iterations = 0;
+        counters->residual = 0.f;
+        counters->num_colors = 0;
+    }
+}
+
+static int solver_grid(DeviceState& d, const void* fn) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, SV_THREADS, 0);
+    if (per_sm < 1) per_sm = 1;
+    if (per_sm > 4) per_sm = 4;
+    return per_sm * d.num_sms;
+}
+
+int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s) {
+    int launches = 0;
+    long long ll = 0;
+    const int grid = d.num_sms * 4;
+    const int iters = cfg.solver_iterations > 0 ? cfg.solver_iterations : 1;
+    int* d_nc = &d.counters->num_contacts;
+    int* d_n2 = &d.counters->pad[1];
+    // per-step resets
+    cudaMemsetAsync(d.dv, 0, sizeof(float4) * 2 * (size_t)d.num_bodies, s);
+    cudaMemsetAsync(d.color_claim, 0, sizeof(unsigned long long) * (size_t)d.num_bodies, s);
+    cudaMemsetAsync(d.body_manifold_count, 0, sizeof(int) * (size_t)d.num_bodies, s);
+    int* color_fill = d.color_offsets + (B3G_MAX_COLORS + 2);
+    int* remaining = color_fill + (B3G_MAX_COLORS + 1);
+    k_reset_solver<<<1, 256, 0, s>>>(color_fill, remaining, d.barrier, d.residual_acc, 2 * iters, d.counters);
+    launches++;
+
+    SolverArgs a;
+    a.bodies = d.bodies;
+    a.inertias = d.inertias;
+    a.slots = d.contact_slots;
+    a.manifold_pair = d.manifold_pair;
+    a.d_nc = d_nc;
+    a.rows = d.rows;
+    a.hdr = d.manifold_hdr;
+    a.inv_mass = d.manifold_inv_mass;
+    a.dv = d.dv;
+    a.dv_sum = d.dv_sum;
+    a.split = d.split_dv;
+    a.body_count = d.body_manifold_count;
+    a.list_off = d.body_list_offsets;
+    a.list = nullptr;
+    a.color = d.manifold_color;
+    a.color_order = d.color_order;
+    a.color_offsets = d.color_offsets;
+    a.color_fill = color_fill;
+    a.remaining = remaining;
+    a.claim = d.color_claim;
+    a.bodies_out = d.bodies;
+    a.counters = d.counters;
+    a.residual_acc = d.residual_acc;
+    a.num_bodies = d.num_bodies;
+    a.mode = cfg.solver_mode;
+    a.iterations = iters;
+    a.residual_tol = cfg.residual_tol;
+    a.dt = dt;
+    a.erp = cfg.erp;
+    a.threshold = cfg.contact_threshold;
+    a.bar.count = d.barrier;
+    a.bar.gen = d.barrier + 1;
+    a.bar.abort_flag = d.barrier + 2;
+    a.bar.status = &d.counters->status;
+    a.spin_limit = B3G_BARRIER_SPIN_LIMIT;
+
+    if (cfg.solver_mode == B3G_SOLVER_JACOBI) {
+        const uint32_t sentinel = (1u << d.body_bits) - 1u;
+        k_count_manifolds<<<grid, SV_THREADS, 0, s>>>(d.contact_slots, d.manifold_pair, d_nc, d.bodies,
+                                                      d.body_manifold_count, d.jac_keys[0], d.jac_vals[0], sentinel,
+                                                      d_n2);
+        launches++;
+        int w = radix_sort_u32(d.prim, d.jac_keys[0], d.jac_keys[1], d.jac_vals[0], d.jac_vals[1], d_n2, d.body_bits,
+                               d.sort_scratch, s, &ll);
+        a.list = d.jac_vals[w];
+        exclusive_scan_i32(d.prim, d.body_manifold_count, d.body_list_offsets, d.d_num_bodies, nullptr,
+                           d.scan_scratch, s, &ll);
+    }
+    k_setup_rows<<<grid, SV_THREADS, 0, s>>>(a);
+    launches++;
+
+    const void* fn = cfg.solver_mode == B3G_SOLVER_JACOBI ? (const void*)k_solve_jacobi : (const void*)k_solve_pgs;
+    int sgrid = solver_grid(d, fn);
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3(sgrid);
+    lc.blockDim = dim3(SV_THREADS);
+    lc.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    if (cfg.solver_mode == B3G_SOLVER_JACOBI)
+        cudaLaunchKernelEx(&lc, k_solve_jacobi, a);
+    else
+        cudaLaunchKernelEx(&lc, k_solve_pgs, a);
+    launches++;
+    return launches + (int)ll;
+}
+
+}  // namespace b3g

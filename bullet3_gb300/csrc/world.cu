@@ -1,0 +1,910 @@
+// Host orchestration and the C ABI (include/b3g_capi.h).
+//
+// Mirrors the reference's host classes on the hot path:
+//   b3GpuNarrowPhase  shape/body registry + device tables (src/Bullet3OpenCL/RigidBody/b3GpuNarrowPhase.cpp)
+//   b3GpuGridBroadphase                        (src/Bullet3OpenCL/BroadphaseCollision/b3GpuGridBroadphase.cpp)
+//   b3GpuRigidBodyPipeline stepSimulation      (src/Bullet3OpenCL/RigidBody/b3GpuRigidBodyPipeline.cpp:221-463)
+// The step enqueues every stage on one stream with no host synchronisation; device-side
+// counts drive all kernels (fixed launch shapes), so the whole step can be captured once
+// as a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "b3g_capi.h"
+#include "common.cuh"
+#include "hull.h"
+#include "world_internal.h"
+
+using namespace b3g;
+
+static thread_local std::string g_last_error;
+
+static b3gStatus fail(b3gStatus st, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return st;
+}
+
+#define CUDA_TRY(expr)                                                                              \
+    do {                                                                                            \
+        cudaError_t _e = (expr);                                                                    \
+        if (_e != cudaSuccess)                                                                      \
+            return fail(B3G_ERR_CUDA, "%s failed: %s (%s:%d)", #expr, cudaGetErrorString(_e), __FILE__, \
+                        __LINE__);                                                                  \
+    } while (0)
+
+struct StageEvents {
+    cudaEvent_t ev[8];
+    bool created = false;
+};
+
+struct b3gWorld {
+    b3gConfig cfg;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    // host registries
+    std::vector<b3gCollidable> collidables;
+    std::vector<b3gAabb> local_aabbs;
+    std::vector<b3gHull> hulls;
+    std::vector<b3gFace> faces;
+    std::vector<int> indices;
+    std::vector<b3gFloat4> vertices;
+    std::vector<b3gFloat4> edges;
+    std::vector<b3gBody> bodies;
+    std::vector<b3gInertia> inertias;
+    std::vector<int> user_index;
+    bool uploaded = false;
+    DeviceState d;
+    std::vector<void*> allocations;
+    // graph
+    cudaGraphExec_t graph_exec = nullptr;
+    float graph_dt = -1.f;
+    int graph_mode = -1, graph_iters = -1;
+    float graph_tol = -1.f;
+    // profiling
+    bool profiling = false;
+    StageEvents events;
+    float stage_ms[7] = {0, 0, 0, 0, 0, 0, 0};
+    long long launches = 0;
+    long long graph_kernels = 0;
+    b3gStepStats last_stats{};
+};
+
+static void free_device(b3gWorld* w) {
+    if (w->graph_exec) {
+        cudaGraphExecDestroy(w->graph_exec);
+        w->graph_exec = nullptr;
+    }
+    for (void* p : w->allocations) cudaFree(p);
+    w->allocations.clear();
+    w->d = DeviceState();
+    w->uploaded = false;
+}
+
+template <typename T>
+static b3gStatus dalloc(b3gWorld* w, T** p, size_t count) {
+    if (count == 0) count = 1;
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, count * sizeof(T));
+    if (e != cudaSuccess)
+        return fail(B3G_ERR_CUDA, "cudaMalloc(%zu bytes) failed: %s", count * sizeof(T), cudaGetErrorString(e));
+    w->allocations.push_back(q);
+    *p = reinterpret_cast<T*>(q);
+    return B3G_OK;
+}
+
+#define TRY(expr)                         \
+    do {                                  \
+        b3gStatus _s = (expr);            \
+        if (_s != B3G_OK) return _s;      \
+    } while (0)
+
+// ---------------------------------------------------------------------------------- config
+extern "C" b3gStatus b3g_config_default(b3gConfig* c) {
+    if (!c) return fail(B3G_ERR_INVALID_ARG, "null config");
+    std::memset(c, 0, sizeof(*c));
+    c->max_bodies = 128 * 1024;  // b3Config::m_maxConvexBodies
+    c->max_shapes = 8 * 1024;
+    c->max_pairs = 0;
+    c->max_contacts = 0;
+    c->grid_cell_size = 0.f;
+    c->grid_dim = 128;
+    c->gravity[0] = 0.f;
+    c->gravity[1] = -9.8f;
+    c->gravity[2] = 0.f;
+    c->angular_damping = 0.99f;
+    c->solver_mode = B3G_SOLVER_PGS;
+    c->solver_iterations = 10;
+    c->erp = 0.2f;
+    c->contact_threshold = 0.02f;
+    c->contact_friction = 0.7f;
+    c->residual_tol = 0.f;
+    c->update_world_inertia = 0;
+    c->use_cuda_graph = 1;
+    c->warm_start = 0;
+    return B3G_OK;
+}
+
+extern "C" const char* b3g_last_error(void) { return g_last_error.c_str(); }
+extern "C" const char* b3g_version(void) { return "b3g-gb300 0.1 (sm_103a)"; }
+
+extern "C" b3gStatus b3g_create(const b3gConfig* cfg, int cuda_device, b3g_handle* out) {
+    if (!out) return fail(B3G_ERR_INVALID_ARG, "null output handle");
+    b3gWorld* w = new b3gWorld();
+    if (cfg)
+        w->cfg = *cfg;
+    else
+        b3g_config_default(&w->cfg);
+    if (w->cfg.grid_dim < 4 || (w->cfg.grid_dim & (w->cfg.grid_dim - 1))) {
+        delete w;
+        return fail(B3G_ERR_INVALID_ARG, "grid_dim must be a power of two >= 4");
+    }
+    if (w->cfg.grid_dim > 1024) {
+        delete w;
+        return fail(B3G_ERR_INVALID_ARG, "grid_dim must be <= 1024 (hash fits in 30 bits)");
+    }
+    w->device = cuda_device;
+    *out = w;
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_destroy(b3g_handle h) {
+    if (!h) return fail(B3G_ERR_INVALID_ARG, "null handle");
+    if (h->uploaded) {
+        cudaSetDevice(h->device);
+        cudaStreamSynchronize(h->stream);
+    }
+    free_device(h);
+    if (h->events.created)
+        for (auto& e : h->events.ev) cudaEventDestroy(e);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return B3G_OK;
+}
+
+// ---------------------------------------------------------------------------------- shapes
+static b3gStatus add_collidable(b3gWorld* w, const b3gCollidable& c, const b3gAabb& aabb, int* out) {
+    if ((int)w->collidables.size() >= w->cfg.max_shapes)
+        return fail(B3G_ERR_CAPACITY, "allocateCollidable out-of-range %d", w->cfg.max_shapes);
+    w->collidables.push_back(c);
+    w->local_aabbs.push_back(aabb);
+    if (out) *out = (int)w->collidables.size() - 1;
+    return B3G_OK;
+}
+
+static b3gAabb make_aabb(float x0, float y0, float z0, float x1, float y1, float z1) {
+    b3gAabb a;
+    a.minv[0] = x0; a.minv[1] = y0; a.minv[2] = z0; a.minw = 0;
+    a.maxv[0] = x1; a.maxv[1] = y1; a.maxv[2] = z1; a.maxw = 0;
+    return a;
+}
+
+extern "C" b3gStatus b3g_register_sphere(b3g_handle h, float radius, int* out) {
+    if (!h || !out) return fail(B3G_ERR_INVALID_ARG, "null argument");
+    if (!(radius > 0.f)) return fail(B3G_ERR_INVALID_ARG, "sphere radius must be positive");
+    b3gCollidable c{0, radius, B3G_SHAPE_SPHERE, 0};
+    return add_collidable(h, c, make_aabb(-radius, -radius, -radius, radius, radius, radius), out);
+}
+
+extern "C" b3gStatus b3g_register_plane(b3g_handle h, const float n[3], float constant, int* out) {
+    if (!h || !n || !out) return fail(B3G_ERR_INVALID_ARG, "null argument");
+    b3gFace f{};
+    f.plane = b3gFloat4{n[0], n[1], n[2], constant};
+    f.indexOffset = 0;
+    f.numIndices = 0;
+    int faceIndex = (int)h->faces.size();
+    h->faces.push_back(f);
+    b3gCollidable c{0, constant, B3G_SHAPE_PLANE, faceIndex};
+    return add_collidable(h, c, make_aabb(-1e30f, -1e30f, -1e30f, 1e30f, 1e30f, 1e30f), out);
+}
+
+static b3gStatus add_hull(b3gWorld* w, const std::vector<float>& vxyz, const std::vector<float>& planes,
+                          const std::vector<int>& counts, const std::vector<int>& idx, const std::vector<float>& exyz,
+                          int* out) {
+    const int nv = (int)vxyz.size() / 3;
+    if (nv < 1) return fail(B3G_ERR_INVALID_ARG, "hull has no vertices");
+    b3gHull hull{};
+    // local centre = vertex mean (b3GpuNarrowPhase.cpp:324-329)
+    float cx = 0, cy = 0, cz = 0;
+    for (int i = 0; i < nv; i++) {
+        cx = cx + vxyz[3 * i];
+        cy = cy + vxyz[3 * i + 1];
+        cz = cz + vxyz[3 * i + 2];
+    }
+    float inv = 1.f / (float)nv;
+    hull.localCenter = b3gFloat4{cx * inv, cy * inv, cz * inv, 0.f};
+    hull.numUniqueEdges = (int)exyz.size() / 3;
+    hull.uniqueEdgesOffset = (int)w->edges.size();
+    for (int i = 0; i < hull.numUniqueEdges; i++)
+        w->edges.push_back(b3gFloat4{exyz[3 * i], exyz[3 * i + 1], exyz[3 * i + 2], 0.f});
+    hull.faceOffset = (int)w->faces.size();
+    hull.numFaces = (int)counts.size();
+    int off = 0;
+    for (int f = 0; f < hull.numFaces; f++) {
+        b3gFace face{};
+        face.plane = b3gFloat4{planes[4 * f], planes[4 * f + 1], planes[4 * f + 2], planes[4 * f + 3]};
+        face.indexOffset = (int)w->indices.size();
+        face.numIndices = counts[f];
+        for (int k = 0; k < counts[f]; k++) {
+            int vi = idx[off + k];
+            if (vi < 0 || vi >= nv) return fail(B3G_ERR_INVALID_INDEX, "face index %d out of range", vi);
+            w->indices.push_back(vi);
+        }
+        off += counts[f];
+        w->faces.push_back(face);
+    }
+    hull.numVertices = nv;
+    hull.vertexOffset = (int)w->vertices.size();
+    float mn[3] = {1e30f, 1e30f, 1e30f}, mx[3] = {-1e30f, -1e30f, -1e30f};
+    for (int i = 0; i < nv; i++) {
+        w->vertices.push_back(b3gFloat4{vxyz[3 * i], vxyz[3 * i + 1], vxyz[3 * i + 2], 0.f});
+        for (int k = 0; k < 3; k++) {
+            mn[k] = std::min(mn[k], vxyz[3 * i + k]);
+            mx[k] = std::max(mx[k], vxyz[3 * i + k]);
+        }
+    }
+    int hullIndex = (int)w->hulls.size();
+    w->hulls.push_back(hull);
+    b3gCollidable c{0, 0.f, B3G_SHAPE_CONVEX_HULL, hullIndex};
+    return add_collidable(w, c, make_aabb(mn[0], mn[1], mn[2], mx[0], mx[1], mx[2]), out);
+}
+
+extern "C" b3gStatus b3g_register_hull(b3g_handle h, const float* verts, int stride_bytes, int num_verts,
+                                       const float scaling[3], int* out) {
+    if (!h || !verts || !out) return fail(B3G_ERR_INVALID_ARG, "null argument");
+    if (stride_bytes < 12) return fail(B3G_ERR_INVALID_ARG, "stride must be >= 12 bytes");
+    HullTables t;
+    if (build_hull(verts, stride_bytes, num_verts, scaling, t) != 0)
+        return fail(B3G_ERR_DEGENERATE, "degenerate convex hull input (%d points)", num_verts);
+    return add_hull(h, t.vertices, t.planes, t.face_counts, t.indices, t.edges, out);
+}
+
+extern "C" b3gStatus b3g_register_hull_tables(b3g_handle h, const float* verts_xyz, int num_verts,
+                                              const float* face_planes, const int* face_index_counts, int num_faces,
+                                              const int* face_indices, const float* unique_edges_xyz, int num_edges,
+                                              int* out) {
+    if (!h || !verts_xyz || !face_planes || !face_index_counts || !out || num_verts < 1 || num_faces < 1)
+        return fail(B3G_ERR_INVALID_ARG, "invalid hull tables");
+    std::vector<float> v(verts_xyz, verts_xyz + 3 * num_verts);
+    std::vector<float> p(face_planes, face_planes + 4 * num_faces);
+    std::vector<int> c(face_index_counts, face_index_counts + num_faces);
+    int total = 0;
+    for (int x : c) total += x;
+    std::vector<int> idx(face_indices, face_indices + total);
+    std::vector<float> e;
+    if (num_edges > 0) e.assign(unique_edges_xyz, unique_edges_xyz + 3 * num_edges);
+    return add_hull(h, v, p, c, idx, e, out);
+}
+
+// ---------------------------------------------------------------------------------- bodies
+static m33 host_qmat(const float q[4]) { return qmat(quat{q[0], q[1], q[2], q[3]}); }
+
+extern "C" b3gStatus b3g_register_body(b3g_handle h, float mass, const float pos[3], const float orn[4],
+                                       int collidable, int user_index, int* out) {
+    if (!h || !pos || !orn || !out) return fail(B3G_ERR_INVALID_ARG, "null argument");
+    if (collidable < 0 || collidable >= (int)h->collidables.size())
+        return fail(B3G_ERR_INVALID_INDEX, "registerPhysicsInstance using invalid collidableIndex");
+    if ((int)h->bodies.size() >= h->cfg.max_bodies)
+        return fail(B3G_ERR_CAPACITY, "registerRigidBody: exceeding the number of rigid bodies, %d > %d",
+                    (int)h->bodies.size(), h->cfg.max_bodies);
+    if (h->uploaded) return fail(B3G_ERR_INVALID_ARG, "register bodies before b3g_write_all_to_gpu");
+    // world AABB with margin 0.01 (b3TransformAabb, b3GpuRigidBodyPipeline.cpp:613-618)
+    const b3gAabb& la = h->local_aabbs[collidable];
+    const float margin = 0.01f;
+    m33 R = host_qmat(orn);
+    float he[3], c[3];
+    for (int k = 0; k < 3; k++) {
+        he[k] = 0.5f * (la.maxv[k] - la.minv[k]) + margin;
+        c[k] = 0.5f * (la.maxv[k] + la.minv[k]);
+    }
+    v3 cw = mmul(R, mk3(c[0], c[1], c[2])) + mk3(pos[0], pos[1], pos[2]);
+    v3 hv = mk3(he[0], he[1], he[2]);
+    v3 ext = mk3(dot3(hv, mk3(fabsf(R.r0.x), fabsf(R.r0.y), fabsf(R.r0.z))),
+                 dot3(hv, mk3(fabsf(R.r1.x), fabsf(R.r1.y), fabsf(R.r1.z))),
+                 dot3(hv, mk3(fabsf(R.r2.x), fabsf(R.r2.y), fabsf(R.r2.z))));
+    v3 amin = cw - ext, amax = cw + ext;
+
+    b3gBody b{};
+    b.pos = b3gFloat4{pos[0], pos[1], pos[2], 0.f};
+    b.quat = b3gFloat4{orn[0], orn[1], orn[2], orn[3]};
+    b.linVel = b3gFloat4{0, 0, 0, 0};
+    b.angVel = b3gFloat4{0, 0, 0, 0};
+    b.collidableIdx = collidable;
+    b.invMass = mass != 0.f ? 1.f / mass : 0.f;
+    b.restitution = 0.f;
+    b.friction = 1.f;  // b3GpuNarrowPhase.cpp:835-839
+    b3gInertia I{};
+    if (mass != 0.f) {
+        // AABB-box inertia with the full extent as "half extent" (b3GpuNarrowPhase.cpp:876-901)
+        float halfExtents[3] = {amax.x - amin.x, amax.y - amin.y, amax.z - amin.z};
+        float lx = 2.f * halfExtents[0], ly = 2.f * halfExtents[1], lz = 2.f * halfExtents[2];
+        float li[3] = {(mass / 12.0f) * (ly * ly + lz * lz), (mass / 12.0f) * (lx * lx + lz * lz),
+                       (mass / 12.0f) * (lx * lx + ly * ly)};
+        float inv[3] = {1.f / li[0], 1.f / li[1], 1.f / li[2]};
+        I.initInvInertia.row[0] = b3gFloat4{inv[0], 0, 0, 0};
+        I.initInvInertia.row[1] = b3gFloat4{0, inv[1], 0, 0};
+        I.initInvInertia.row[2] = b3gFloat4{0, 0, inv[2], 0};
+        v3 rows[3] = {mk3(R.r0.x * inv[0], R.r0.y * inv[1], R.r0.z * inv[2]),
+                      mk3(R.r1.x * inv[0], R.r1.y * inv[1], R.r1.z * inv[2]),
+                      mk3(R.r2.x * inv[0], R.r2.y * inv[1], R.r2.z * inv[2])};
+        for (int r = 0; r < 3; r++) {
+            I.invInertiaWorld.row[r].x = dot3(rows[r], R.r0);
+            I.invInertiaWorld.row[r].y = dot3(rows[r], R.r1);
+            I.invInertiaWorld.row[r].z = dot3(rows[r], R.r2);
+            I.invInertiaWorld.row[r].w = 0.f;
+        }
+    }
+    h->bodies.push_back(b);
+    h->inertias.push_back(I);
+    h->user_index.push_back(user_index);
+    *out = (int)h->bodies.size() - 1;
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_set_gravity(b3g_handle h, const float g[3]) {
+    if (!h || !g) return fail(B3G_ERR_INVALID_ARG, "null argument");
+    h->cfg.gravity[0] = g[0];
+    h->cfg.gravity[1] = g[1];
+    h->cfg.gravity[2] = g[2];
+    h->graph_dt = -1.f;  // force re-capture
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_set_solver(b3g_handle h, int mode, int iterations, float residual_tol) {
+    if (!h) return fail(B3G_ERR_INVALID_ARG, "null handle");
+    if (mode != B3G_SOLVER_PGS && mode != B3G_SOLVER_JACOBI) return fail(B3G_ERR_INVALID_ARG, "bad solver mode");
+    if (iterations < 1 || iterations > 4096) return fail(B3G_ERR_INVALID_ARG, "iterations out of range");
+    h->cfg.solver_mode = mode;
+    h->cfg.solver_iterations = iterations;
+    h->cfg.residual_tol = residual_tol;
+    return B3G_OK;
+}
+
+// ---------------------------------------------------------------------------------- upload
+static int bits_for(int n) {
+    int b = 1;
+    while ((1 << b) < n) b++;
+    return b;
+}
+
+extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
+    if (!h) return fail(B3G_ERR_INVALID_ARG, "null handle");
+    CUDA_TRY(cudaSetDevice(h->device));
+    if (!h->stream) CUDA_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    cudaStreamSynchronize(h->stream);
+    free_device(h);
+    DeviceState& d = h->d;
+    const int N = (int)h->bodies.size();
+    if (N < 1) return fail(B3G_ERR_INVALID_ARG, "no bodies registered");
+    int sms = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+    d.num_sms = sms;
+    d.num_bodies = N;
+    d.num_collidables = (int)h->collidables.size();
+    // dynamic (small) and static (large) proxies, as registerPhysicsInstance does (:650-657)
+    std::vector<int> dyn_slot(N, -1), large;
+    int nd = 0;
+    float max_extent = 0.f;
+    for (int i = 0; i < N; i++) {
+        if (h->bodies[i].invMass != 0.f) {
+            dyn_slot[i] = nd++;
+            const b3gAabb& la = h->local_aabbs[h->bodies[i].collidableIdx];
+            float hx = 0.5f * (la.maxv[0] - la.minv[0]), hy = 0.5f * (la.maxv[1] - la.minv[1]),
+                  hz = 0.5f * (la.maxv[2] - la.minv[2]);
+            // largest world-AABB extent the body can reach under any rotation: 2 |half extents|
+            float e = 2.f * std::sqrt(hx * hx + hy * hy + hz * hz);
+            max_extent = std::max(max_extent, e);
+        } else {
+            large.push_back(i);
+        }
+    }
+    d.num_dynamic = nd;
+    d.num_large = (int)large.size();
+    float cell = h->cfg.grid_cell_size > 0.f ? h->cfg.grid_cell_size : max_extent;
+    // exactness of the 27-cell search needs cell >= every dynamic AABB extent
+    if (cell < max_extent) cell = max_extent;
+    if (!(cell > 0.f)) cell = 1.f;
+    d.inv_cell = 1.f / cell;
+    d.grid_dim = h->cfg.grid_dim;
+    d.grid_bits = bits_for(d.grid_dim);
+    d.body_bits = bits_for(N + 1);
+    if (2 * d.body_bits > 64) return fail(B3G_ERR_CAPACITY, "too many bodies");
+    d.max_pairs = h->cfg.max_pairs > 0 ? h->cfg.max_pairs : std::max(1024, 12 * N);
+    d.max_contacts = h->cfg.max_contacts > 0 ? std::min(h->cfg.max_contacts, d.max_pairs) : d.max_pairs;
+    d.prim.sort_blocks = sms * 4;
+    d.prim.scan_blocks = sms * 2;
+
+    const size_t nh = std::max<size_t>(1, h->hulls.size()), nf = std::max<size_t>(1, h->faces.size()),
+                 ni = std::max<size_t>(1, h->indices.size()), nvx = std::max<size_t>(1, h->vertices.size()),
+                 ne = std::max<size_t>(1, h->edges.size());
+    TRY(dalloc(h, &d.bodies, N));
+    TRY(dalloc(h, &d.inertias, N));
+    TRY(dalloc(h, &d.collidables, d.num_collidables));
+    TRY(dalloc(h, &d.local_aabbs, d.num_collidables));
+    TRY(dalloc(h, &d.hulls, nh));
+    TRY(dalloc(h, &d.faces, nf));
+    TRY(dalloc(h, &d.indices, ni));
+    TRY(dalloc(h, &d.vertices, nvx));
+    TRY(dalloc(h, &d.edges, ne));
+    TRY(dalloc(h, &d.dyn_slot, N));
+    TRY(dalloc(h, &d.large_list, std::max(1, d.num_large)));
+    TRY(dalloc(h, &d.aabbs, N));
+    for (int k = 0; k < 2; k++) {
+        TRY(dalloc(h, &d.cell_keys[k], std::max(1, nd)));
+        TRY(dalloc(h, &d.cell_vals[k], std::max(1, nd)));
+        TRY(dalloc(h, &d.pair_keys[k], d.max_pairs));
+        TRY(dalloc(h, &d.jac_keys[k], 2 * (size_t)d.max_contacts));
+        TRY(dalloc(h, &d.jac_vals[k], 2 * (size_t)d.max_contacts));
+    }
+    const size_t ncells = (size_t)1 << (3 * d.grid_bits);
+    TRY(dalloc(h, &d.cell_start, ncells));
+    TRY(dalloc(h, &d.pairs, d.max_pairs));
+    TRY(dalloc(h, &d.type_lists, (size_t)PT_COUNT * d.max_pairs));
+    TRY(dalloc(h, &d.contact_slots, d.max_pairs));
+    TRY(dalloc(h, &d.contact_flag, d.max_pairs));
+    TRY(dalloc(h, &d.contact_index, d.max_pairs));
+    TRY(dalloc(h, &d.manifold_pair, d.max_pairs));
+    TRY(dalloc(h, &d.contacts_compact, d.max_contacts));
+    TRY(dalloc(h, &d.rows, (size_t)12 * d.max_contacts));
+    TRY(dalloc(h, &d.manifold_color, d.max_contacts));
+    TRY(dalloc(h, &d.color_order, d.max_contacts));
+    TRY(dalloc(h, &d.color_offsets, 3 * (B3G_MAX_COLORS + 2)));
+    TRY(dalloc(h, &d.color_claim, N));
+    TRY(dalloc(h, &d.dv, 2 * (size_t)N));
+    TRY(dalloc(h, &d.dv_sum, 2 * (size_t)N));
+    TRY(dalloc(h, &d.manifold_hdr, d.max_contacts));
+    TRY(dalloc(h, &d.manifold_inv_mass, d.max_contacts));
+    TRY(dalloc(h, &d.body_manifold_count, N + 1));
+    TRY(dalloc(h, &d.body_list_offsets, N + 1));
+    TRY(dalloc(h, &d.split_dv, 4 * (size_t)d.max_contacts));
+    TRY(dalloc(h, &d.residual_acc, 2 * 4096));
+    TRY(dalloc(h, &d.counters, 1));
+    TRY(dalloc(h, &d.barrier, 64));
+    {
+        unsigned char* p = nullptr;
+        TRY(dalloc(h, &p, radix_scratch_bytes(d.prim)));
+        d.sort_scratch = p;
+        TRY(dalloc(h, &p, scan_scratch_bytes(d.prim)));
+        d.scan_scratch = p;
+    }
+    TRY(dalloc(h, &d.d_num_dynamic, 4));
+    d.d_num_bodies = d.d_num_dynamic + 1;
+
+    cudaStream_t s = h->stream;
+    CUDA_TRY(cudaMemcpyAsync(d.bodies, h->bodies.data(), sizeof(b3gBody) * N, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(d.inertias, h->inertias.data(), sizeof(b3gInertia) * N, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(d.collidables, h->collidables.data(), sizeof(b3gCollidable) * d.num_collidables,
+                             cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(d.local_aabbs, h->local_aabbs.data(), sizeof(b3gAabb) * d.num_collidables,
+                             cudaMemcpyHostToDevice, s));
+    if (!h->hulls.empty())
+        CUDA_TRY(cudaMemcpyAsync(d.hulls, h->hulls.data(), sizeof(b3gHull) * h->hulls.size(), cudaMemcpyHostToDevice, s));
+    if (!h->faces.empty())
+        CUDA_TRY(cudaMemcpyAsync(d.faces, h->faces.data(), sizeof(b3gFace) * h->faces.size(), cudaMemcpyHostToDevice, s));
+    if (!h->indices.empty())
+        CUDA_TRY(cudaMemcpyAsync(d.indices, h->indices.data(), sizeof(int) * h->indices.size(), cudaMemcpyHostToDevice, s));
+    if (!h->vertices.empty())
+        CUDA_TRY(cudaMemcpyAsync(d.vertices, h->vertices.data(), sizeof(b3gFloat4) * h->vertices.size(),
+                                 cudaMemcpyHostToDevice, s));
+    if (!h->edges.empty())
+        CUDA_TRY(cudaMemcpyAsync(d.edges, h->edges.data(), sizeof(b3gFloat4) * h->edges.size(), cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(d.dyn_slot, dyn_slot.data(), sizeof(int) * N, cudaMemcpyHostToDevice, s));
+    if (!large.empty())
+        CUDA_TRY(cudaMemcpyAsync(d.large_list, large.data(), sizeof(int) * large.size(), cudaMemcpyHostToDevice, s));
+    int sizes[4] = {nd, N, 0, 0};
+    CUDA_TRY(cudaMemcpyAsync(d.d_num_dynamic, sizes, sizeof(sizes), cudaMemcpyHostToDevice, s));
+    // an all-ones cell table is never a valid run start (validated against sorted keys)
+    CUDA_TRY(cudaMemsetAsync(d.cell_start, 0xff, sizeof(uint32_t) * ncells, s));
+    CUDA_TRY(cudaMemsetAsync(d.counters, 0, sizeof(DevCounters), s));
+    CUDA_TRY(cudaMemsetAsync(d.barrier, 0, 64 * sizeof(unsigned int), s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    h->uploaded = true;
+    return B3G_OK;
+}
+
+// ---------------------------------------------------------------------------------- the step
+#define REQUIRE_UPLOADED(h)                                                                        \
+    do {                                                                                           \
+        if (!(h)) return fail(B3G_ERR_INVALID_ARG, "null handle");                                 \
+        if (!(h)->uploaded) return fail(B3G_ERR_NOT_UPLOADED, "call b3g_write_all_to_gpu first"); \
+    } while (0)
+
+static void record(b3gWorld* h, int k) {
+    if (h->profiling) cudaEventRecord(h->events.ev[k], h->stream);
+}
+
+static void enqueue_step(b3gWorld* h, float dt, bool with_events) {
+    cudaStream_t s = h->stream;
+    DeviceState& d = h->d;
+    long long n = 0;
+    if (with_events) record(h, 0);
+    n += launch_aabbs(d, s);
+    if (with_events) record(h, 1);
+    n += launch_pairs(d, s);
+    if (with_events) record(h, 2);
+    n += launch_contacts(d, h->cfg.contact_friction, s);
+    if (with_events) record(h, 3);
+    // batching is fused into the solver kernel; stage 3->4 is empty
+    if (with_events) record(h, 4);
+    n += launch_solver(d, h->cfg, dt, s);
+    if (with_events) record(h, 5);
+    if (with_events) record(h, 6);
+    n += launch_integrate(d, h->cfg, dt, s);
+    if (with_events) record(h, 7);
+    h->launches += n;
+}
+
+extern "C" b3gStatus b3g_step(b3g_handle h, float dt) {
+    REQUIRE_UPLOADED(h);
+    if (!(dt > 0.f)) return fail(B3G_ERR_INVALID_ARG, "dt must be positive");
+    CUDA_TRY(cudaSetDevice(h->device));
+    if (h->profiling || !h->cfg.use_cuda_graph) {
+        enqueue_step(h, dt, h->profiling);
+        CUDA_TRY(cudaGetLastError());
+        return B3G_OK;
+    }
+    if (!h->graph_exec || h->graph_dt != dt || h->graph_mode != h->cfg.solver_mode ||
+        h->graph_iters != h->cfg.solver_iterations || h->graph_tol != h->cfg.residual_tol) {
+        if (h->graph_exec) {
+            cudaGraphExecDestroy(h->graph_exec);
+            h->graph_exec = nullptr;
+        }
+        cudaGraph_t g;
+        long long before = h->launches;
+        CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_step(h, dt, false);
+        CUDA_TRY(cudaStreamEndCapture(h->stream, &g));
+        CUDA_TRY(cudaGraphInstantiate(&h->graph_exec, g, 0));
+        cudaGraphDestroy(g);
+        h->graph_dt = dt;
+        h->graph_mode = h->cfg.solver_mode;
+        h->graph_iters = h->cfg.solver_iterations;
+        h->graph_tol = h->cfg.residual_tol;
+        h->graph_kernels = h->launches - before;
+        h->launches = before;
+    }
+    CUDA_TRY(cudaGraphLaunch(h->graph_exec, h->stream));
+    h->launches += h->graph_kernels;
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_setup_aabbs(b3g_handle h) {
+    REQUIRE_UPLOADED(h);
+    h->launches += launch_aabbs(h->d, h->stream);
+    CUDA_TRY(cudaGetLastError());
+    return B3G_OK;
+}
+extern "C" b3gStatus b3g_calculate_overlapping_pairs(b3g_handle h) {
+    REQUIRE_UPLOADED(h);
+    h->launches += launch_pairs(h->d, h->stream);
+    CUDA_TRY(cudaGetLastError());
+    return B3G_OK;
+}
+extern "C" b3gStatus b3g_compute_contacts(b3g_handle h) {
+    REQUIRE_UPLOADED(h);
+    h->launches += launch_contacts(h->d, h->cfg.contact_friction, h->stream);
+    CUDA_TRY(cudaGetLastError());
+    return B3G_OK;
+}
+extern "C" b3gStatus b3g_solve_contacts(b3g_handle h, float dt) {
+    REQUIRE_UPLOADED(h);
+    h->launches += launch_solver(h->d, h->cfg, dt, h->stream);
+    CUDA_TRY(cudaGetLastError());
+    return B3G_OK;
+}
+extern "C" b3gStatus b3g_integrate(b3g_handle h, float dt) {
+    REQUIRE_UPLOADED(h);
+    h->launches += launch_integrate(h->d, h->cfg, dt, h->stream);
+    CUDA_TRY(cudaGetLastError());
+    return B3G_OK;
+}
+extern "C" b3gStatus b3g_synchronize(b3g_handle h) {
+    REQUIRE_UPLOADED(h);
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return B3G_OK;
+}
+
+static b3gStatus read_counters(b3g_handle h, DevCounters& c) {
+    CUDA_TRY(cudaMemcpyAsync(&c, h->d.counters, sizeof(DevCounters), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_get_stats(b3g_handle h, b3gStepStats* out) {
+    REQUIRE_UPLOADED(h);
+    if (!out) return fail(B3G_ERR_INVALID_ARG, "null output");
+    DevCounters c;
+    TRY(read_counters(h, c));
+    out->num_pairs = std::min(c.num_pairs, h->d.max_pairs);
+    out->num_contacts = c.num_contacts;
+    out->num_points = c.num_points;
+    out->num_colors = c.num_colors;
+    out->iterations = c.iterations;
+    out->residual = c.residual;
+    out->status = c.status;
+    out->num_large = h->d.num_large;
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_status(b3g_handle h, unsigned int* flags, int clear) {
+    REQUIRE_UPLOADED(h);
+    if (!flags) return fail(B3G_ERR_INVALID_ARG, "null output");
+    DevCounters c;
+    TRY(read_counters(h, c));
+    *flags = c.status;
+    if (clear) CUDA_TRY(cudaMemsetAsync(&h->d.counters->status, 0, sizeof(unsigned int), h->stream));
+    return B3G_OK;
+}
+
+// ---------------------------------------------------------------------------------- getters
+extern "C" b3gStatus b3g_get_num_bodies(b3g_handle h, int* n) {
+    if (!h || !n) return fail(B3G_ERR_INVALID_ARG, "null argument");
+    *n = (int)h->bodies.size();
+    return B3G_OK;
+}
+extern "C" b3gStatus b3g_get_body_buffer(b3g_handle h, void** p) {
+    REQUIRE_UPLOADED(h);
+    if (!p) return fail(B3G_ERR_INVALID_ARG, "null output");
+    *p = h->d.bodies;
+    return B3G_OK;
+}
+extern "C" b3gStatus b3g_get_inertia_buffer(b3g_handle h, void** p) {
+    REQUIRE_UPLOADED(h);
+    if (!p) return fail(B3G_ERR_INVALID_ARG, "null output");
+    *p = h->d.inertias;
+    return B3G_OK;
+}
+extern "C" b3gStatus b3g_get_aabb_buffer(b3g_handle h, void** p) {
+    REQUIRE_UPLOADED(h);
+    if (!p) return fail(B3G_ERR_INVALID_ARG, "null output");
+    *p = h->d.aabbs;
+    return B3G_OK;
+}
+extern "C" b3gStatus b3g_get_pair_buffer(b3g_handle h, void** p, int* n) {
+    REQUIRE_UPLOADED(h);
+    if (!p || !n) return fail(B3G_ERR_INVALID_ARG, "null output");
+    DevCounters c;
+    TRY(read_counters(h, c));
+    *p = h->d.pairs;
+    *n = std::min(c.num_pairs, h->d.max_pairs);
+    return B3G_OK;
+}
+extern "C" b3gStatus b3g_get_contact_buffer(b3g_handle h, void** p, int* n) {
+    REQUIRE_UPLOADED(h);
+    if (!p || !n) return fail(B3G_ERR_INVALID_ARG, "null output");
+    h->launches += launch_compact_contacts(h->d, h->stream);
+    DevCounters c;
+    TRY(read_counters(h, c));
+    *p = h->d.contacts_compact;
+    *n = c.num_contacts;
+    return B3G_OK;
+}
+extern "C" b3gStatus b3g_get_stream(b3g_handle h, void** s) {
+    REQUIRE_UPLOADED(h);
+    if (!s) return fail(B3G_ERR_INVALID_ARG, "null output");
+    *s = h->stream;
+    return B3G_OK;
+}
+
+// ---------------------------------------------------------------------------------- host copies
+static b3gStatus copy_out(b3g_handle h, void* dst, const void* src, size_t bytes) {
+    CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return B3G_OK;
+}
+static b3gStatus copy_in(b3g_handle h, void* dst, const void* src, size_t bytes) {
+    CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_read_bodies(b3g_handle h, void* host, int n) {
+    REQUIRE_UPLOADED(h);
+    if (!host || n < 0 || n > h->d.num_bodies) return fail(B3G_ERR_INVALID_ARG, "bad body buffer");
+    return copy_out(h, host, h->d.bodies, sizeof(b3gBody) * n);
+}
+extern "C" b3gStatus b3g_write_bodies(b3g_handle h, const void* host, int n) {
+    REQUIRE_UPLOADED(h);
+    if (!host || n < 0 || n > h->d.num_bodies) return fail(B3G_ERR_INVALID_ARG, "bad body buffer");
+    return copy_in(h, h->d.bodies, host, sizeof(b3gBody) * n);
+}
+extern "C" b3gStatus b3g_read_inertias(b3g_handle h, void* host, int n) {
+    REQUIRE_UPLOADED(h);
+    if (!host || n < 0 || n > h->d.num_bodies) return fail(B3G_ERR_INVALID_ARG, "bad inertia buffer");
+    return copy_out(h, host, h->d.inertias, sizeof(b3gInertia) * n);
+}
+extern "C" b3gStatus b3g_read_aabbs(b3g_handle h, void* host, int n) {
+    REQUIRE_UPLOADED(h);
+    if (!host || n < 0 || n > h->d.num_bodies) return fail(B3G_ERR_INVALID_ARG, "bad aabb buffer");
+    return copy_out(h, host, h->d.aabbs, sizeof(b3gAabb) * n);
+}
+extern "C" b3gStatus b3g_write_aabbs(b3g_handle h, const void* host, int n) {
+    REQUIRE_UPLOADED(h);
+    if (!host || n != h->d.num_bodies) return fail(B3G_ERR_INVALID_ARG, "bad aabb buffer");
+    return copy_in(h, h->d.aabbs, host, sizeof(b3gAabb) * n);
+}
+extern "C" b3gStatus b3g_read_pairs(b3g_handle h, void* host, int capacity, int* num) {
+    REQUIRE_UPLOADED(h);
+    if (!num) return fail(B3G_ERR_INVALID_ARG, "null count");
+    DevCounters c;
+    TRY(read_counters(h, c));
+    int n = std::min(c.num_pairs, h->d.max_pairs);
+    *num = n;
+    if (host && capacity > 0) TRY(copy_out(h, host, h->d.pairs, sizeof(b3gPair) * std::min(n, capacity)));
+    return B3G_OK;
+}
+extern "C" b3gStatus b3g_read_contacts(b3g_handle h, void* host, int capacity, int* num) {
+    REQUIRE_UPLOADED(h);
+    if (!num) return fail(B3G_ERR_INVALID_ARG, "null count");
+    h->launches += launch_compact_contacts(h->d, h->stream);
+    DevCounters c;
+    TRY(read_counters(h, c));
+    *num = c.num_contacts;
+    if (host && capacity > 0)
+        TRY(copy_out(h, host, h->d.contacts_compact, sizeof(b3gContact4) * std::min(c.num_contacts, capacity)));
+    return B3G_OK;
+}
+
+__global__ void k_expand_contacts(const b3gContact4* __restrict__ in, int n, b3gContact4* __restrict__ slots,
+                                  int* __restrict__ manifold_pair, int* __restrict__ flags, DevCounters* counters) {
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
+        slots[m] = in[m];
+        manifold_pair[m] = m;
+        flags[m] = 1;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) counters->num_contacts = n;
+}
+
+extern "C" b3gStatus b3g_write_contacts(b3g_handle h, const void* host, int n) {
+    REQUIRE_UPLOADED(h);
+    if (!host || n < 0 || n > h->d.max_contacts) return fail(B3G_ERR_INVALID_ARG, "bad contact buffer");
+    if (n > 0) TRY(copy_in(h, h->d.contacts_compact, host, sizeof(b3gContact4) * n));
+    k_expand_contacts<<<h->d.num_sms * 2, 256, 0, h->stream>>>(h->d.contacts_compact, n, h->d.contact_slots,
+                                                              h->d.manifold_pair, h->d.contact_flag, h->d.counters);
+    h->launches++;
+    CUDA_TRY(cudaGetLastError());
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_read_batches(b3g_handle h, int* host, int capacity, int* num) {
+    REQUIRE_UPLOADED(h);
+    if (!num) return fail(B3G_ERR_INVALID_ARG, "null count");
+    DevCounters c;
+    TRY(read_counters(h, c));
+    *num = c.num_contacts;
+    if (host && capacity > 0)
+        TRY(copy_out(h, host, h->d.manifold_color, sizeof(int) * std::min(c.num_contacts, capacity)));
+    return B3G_OK;
+}
+
+__global__ void k_gather_impulses(const SolverRow* __restrict__ rows, int n, float* __restrict__ out) {
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
+        for (int j = 0; j < 4; j++) {
+            out[(size_t)m * 12 + 3 * j + 0] = rows[(size_t)m * 12 + j].r2xn_imp.w;
+            out[(size_t)m * 12 + 3 * j + 1] = rows[(size_t)m * 12 + 4 + 2 * j + 1].r2xn_imp.w;  // lateral dir 1
+            out[(size_t)m * 12 + 3 * j + 2] = rows[(size_t)m * 12 + 4 + 2 * j + 0].r2xn_imp.w;  // lateral dir 2
+        }
+    }
+}
+
+extern "C" b3gStatus b3g_read_impulses(b3g_handle h, float* host, int capacity, int* num) {
+    REQUIRE_UPLOADED(h);
+    if (!num) return fail(B3G_ERR_INVALID_ARG, "null count");
+    DevCounters c;
+    TRY(read_counters(h, c));
+    *num = c.num_contacts;
+    int n = std::min(c.num_contacts, capacity);
+    if (host && n > 0) {
+        float* tmp = nullptr;
+        CUDA_TRY(cudaMalloc(&tmp, sizeof(float) * 12 * (size_t)n));
+        k_gather_impulses<<<h->d.num_sms * 2, 256, 0, h->stream>>>(h->d.rows, n, tmp);
+        b3gStatus st = copy_out(h, host, tmp, sizeof(float) * 12 * (size_t)n);
+        cudaFree(tmp);
+        return st;
+    }
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_get_num_collidables(b3g_handle h, int* n) {
+    if (!h || !n) return fail(B3G_ERR_INVALID_ARG, "null argument");
+    *n = (int)h->collidables.size();
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_read_registered_bodies(b3g_handle h, void* bodies, void* inertias, int n) {
+    if (!h) return fail(B3G_ERR_INVALID_ARG, "null handle");
+    if (n < 0 || n > (int)h->bodies.size()) return fail(B3G_ERR_INVALID_ARG, "bad body count");
+    if (bodies && n) std::memcpy(bodies, h->bodies.data(), sizeof(b3gBody) * n);
+    if (inertias && n) std::memcpy(inertias, h->inertias.data(), sizeof(b3gInertia) * n);
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_read_shape_tables(b3g_handle h, void* collidables, void* hulls, void* faces, int* indices,
+                                           void* vertices, void* edges, void* local_aabbs, int* counts6) {
+    if (!h || !counts6) return fail(B3G_ERR_INVALID_ARG, "null argument");
+    int caps[6];
+    std::memcpy(caps, counts6, sizeof(caps));
+    counts6[0] = (int)h->collidables.size();
+    counts6[1] = (int)h->hulls.size();
+    counts6[2] = (int)h->faces.size();
+    counts6[3] = (int)h->indices.size();
+    counts6[4] = (int)h->vertices.size();
+    counts6[5] = (int)h->edges.size();
+    auto cp = [&](void* dst, const void* src, size_t esz, int n, int cap) {
+        if (dst && n > 0 && cap >= n) std::memcpy(dst, src, esz * n);
+    };
+    cp(collidables, h->collidables.data(), sizeof(b3gCollidable), counts6[0], caps[0]);
+    cp(local_aabbs, h->local_aabbs.data(), sizeof(b3gAabb), counts6[0], caps[0]);
+    cp(hulls, h->hulls.data(), sizeof(b3gHull), counts6[1], caps[1]);
+    cp(faces, h->faces.data(), sizeof(b3gFace), counts6[2], caps[2]);
+    cp(indices, h->indices.data(), sizeof(int), counts6[3], caps[3]);
+    cp(vertices, h->vertices.data(), sizeof(b3gFloat4), counts6[4], caps[4]);
+    cp(edges, h->edges.data(), sizeof(b3gFloat4), counts6[5], caps[5]);
+    return B3G_OK;
+}
+
+// ---------------------------------------------------------------------------------- profiling
+extern "C" b3gStatus b3g_set_profiling(b3g_handle h, int on) {
+    if (!h) return fail(B3G_ERR_INVALID_ARG, "null handle");
+    if (on && !h->events.created) {
+        CUDA_TRY(cudaSetDevice(h->device));
+        for (auto& e : h->events.ev) CUDA_TRY(cudaEventCreate(&e));
+        h->events.created = true;
+    }
+    h->profiling = on != 0;
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_get_stage_times(b3g_handle h, float* ms7) {
+    REQUIRE_UPLOADED(h);
+    if (!ms7) return fail(B3G_ERR_INVALID_ARG, "null output");
+    if (!h->events.created) return fail(B3G_ERR_INVALID_ARG, "profiling was never enabled");
+    CUDA_TRY(cudaEventSynchronize(h->events.ev[7]));
+    for (int k = 0; k < 7; k++) {
+        float ms = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&ms, h->events.ev[k], h->events.ev[k + 1]));
+        ms7[k] = ms;
+    }
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_get_launch_count(b3g_handle h, long long* n) {
+    if (!h || !n) return fail(B3G_ERR_INVALID_ARG, "null argument");
+    *n = h->launches;
+    return B3G_OK;
+}
+
+// ---------------------------------------------------------------------------------- hull (host only)
+extern "C" b3gStatus b3g_hull_compute(const float* verts, int stride_bytes, int num_verts, const float scaling[3],
+                                      float* verts_out, float* planes_out, int* face_counts_out, int* indices_out,
+                                      float* edges_out, float* center_out, int* counts6) {
+    if (!verts || !counts6) return fail(B3G_ERR_INVALID_ARG, "null argument");
+    HullTables t;
+    if (build_hull(verts, stride_bytes, num_verts, scaling, t) != 0)
+        return fail(B3G_ERR_DEGENERATE, "degenerate convex hull input (%d points)", num_verts);
+    int nv = (int)t.vertices.size() / 3, nf = (int)t.face_counts.size(), ni = (int)t.indices.size(),
+        ne = (int)t.edges.size() / 3;
+    bool fits = counts6[0] >= nv && counts6[1] >= nf && counts6[2] >= ni && counts6[3] >= ne;
+    counts6[0] = nv;
+    counts6[1] = nf;
+    counts6[2] = ni;
+    counts6[3] = ne;
+    if (!fits) return fail(B3G_ERR_CAPACITY, "hull output buffers too small");
+    if (verts_out) std::memcpy(verts_out, t.vertices.data(), sizeof(float) * 3 * nv);
+    if (planes_out) std::memcpy(planes_out, t.planes.data(), sizeof(float) * 4 * nf);
+    if (face_counts_out) std::memcpy(face_counts_out, t.face_counts.data(), sizeof(int) * nf);
+    if (indices_out) std::memcpy(indices_out, t.indices.data(), sizeof(int) * ni);
+    if (edges_out && ne) std::memcpy(edges_out, t.edges.data(), sizeof(float) * 3 * ne);
+    if (center_out) std::memcpy(center_out, t.center, sizeof(float) * 3);
+    return B3G_OK;
+}

@@ -1,0 +1,113 @@
+// Internal state shared by the host orchestration (world.cu) and the stage launchers.
+#ifndef B3G_WORLD_INTERNAL_H
+#define B3G_WORLD_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "b3g_capi.h"
+#include "b3g_types.h"
+#include "primitives.h"
+
+namespace b3g {
+
+enum PairType { PT_HULL_HULL = 0, PT_PLANE_HULL = 1, PT_SPHERE_HULL = 2, PT_SPHERE_SPHERE = 3, PT_PLANE_SPHERE = 4,
+                PT_COUNT = 5 };
+
+// Per-step device counters (one 256-byte block, copied to the host once per step).
+struct DevCounters {
+    int num_pairs;        // pairs emitted (may exceed capacity -> overflow flag)
+    int num_contacts;     // manifolds
+    int num_points;
+    int num_colors;
+    int iterations;
+    float residual;
+    unsigned int status;
+    int type_count[PT_COUNT];
+    int pad[64 - 12];
+};
+
+// Solver row: b3SolverConstraint reduced to what a contact/friction row uses
+// (Bullet3Dynamics/ConstraintSolver/b3SolverConstraint.h).
+struct SolverRow {
+    float4 normal_jac;   // contact normal (or friction direction) xyz, w = jacDiagABInv
+    float4 r1xn_rhs;     // relpos1CrossNormal xyz, w = rhs
+    float4 r2xn_imp;     // relpos2CrossNormal xyz, w = applied impulse
+    float4 angA_fric;    // angularComponentA xyz, w = friction coefficient
+    float4 angB_pad;     // angularComponentB xyz, w = 0
+};
+
+struct DeviceState {
+    // sizes fixed at upload
+    int num_bodies = 0, num_dynamic = 0, num_large = 0, num_collidables = 0;
+    int max_pairs = 0, max_contacts = 0;
+    int num_sms = 0;
+    // registries
+    b3gBody* bodies = nullptr;
+    b3gInertia* inertias = nullptr;
+    b3gCollidable* collidables = nullptr;
+    b3gAabb* local_aabbs = nullptr;
+    b3gHull* hulls = nullptr;
+    b3gFace* faces = nullptr;
+    int* indices = nullptr;
+    b3gFloat4* vertices = nullptr;
+    b3gFloat4* edges = nullptr;
+    int* dyn_slot = nullptr;      // body -> dynamic slot or -1
+    int* large_list = nullptr;    // static bodies (large proxies)
+    // broadphase
+    b3gAabb* aabbs = nullptr;
+    uint32_t* cell_keys[2] = {nullptr, nullptr};
+    uint32_t* cell_vals[2] = {nullptr, nullptr};
+    uint32_t* cell_start = nullptr;   // dense per hash cell, validated on use (no per-step clear)
+    int grid_dim = 128, grid_bits = 7;
+    float inv_cell = 1.f;
+    int body_bits = 1;                // bits needed for a body index
+    uint64_t* pair_keys[2] = {nullptr, nullptr};
+    b3gPair* pairs = nullptr;
+    int* type_lists = nullptr;        // PT_COUNT * max_pairs
+    // narrowphase
+    b3gContact4* contact_slots = nullptr;  // one per pair slot
+    int* contact_flag = nullptr;           // per pair: 1 if a manifold was produced
+    int* contact_index = nullptr;          // per pair: exclusive scan of contact_flag
+    int* manifold_pair = nullptr;          // manifold -> pair index
+    b3gContact4* contacts_compact = nullptr;  // filled on demand for the drop-in getter
+    // solver
+    SolverRow* rows = nullptr;             // 12 rows per manifold: 4 contact, 8 friction
+    int* manifold_color = nullptr;
+    int* color_order = nullptr;            // manifolds sorted by colour
+    int* color_offsets = nullptr;          // B3G_MAX_COLORS + 1
+    unsigned long long* color_claim = nullptr;  // per body
+    float4* dv = nullptr;                  // per body: lin xyz | ang xyz (2 float4)
+    float4* dv_sum = nullptr;              // Jacobi: per body sum of split deltas (2 float4)
+    int4* manifold_hdr = nullptr;          // bodyA, bodyB, active point mask, points
+    float2* manifold_inv_mass = nullptr;
+    int* body_manifold_count = nullptr;    // Jacobi split counts
+    int* body_list_offsets = nullptr;
+    int* body_list = nullptr;              // Jacobi: manifold*2+side grouped by body
+    uint32_t* jac_keys[2] = {nullptr, nullptr};
+    uint32_t* jac_vals[2] = {nullptr, nullptr};
+    float4* split_dv = nullptr;            // Jacobi: 2 sides * 2 float4 per manifold
+    double* residual_acc = nullptr;        // per iteration: sum d^2, sum l^2
+    // control
+    DevCounters* counters = nullptr;
+    unsigned int* barrier = nullptr;       // count, gen, abort
+    void* sort_scratch = nullptr;
+    void* scan_scratch = nullptr;
+    int* d_num_dynamic = nullptr;          // device copy of num_dynamic (sort length)
+    int* d_num_bodies = nullptr;           // device copy of num_bodies
+    PrimConfig prim;
+};
+
+#define B3G_MAX_COLORS 256
+
+// stage launchers (each returns the number of kernels it launched)
+int launch_aabbs(DeviceState& d, cudaStream_t s);
+int launch_pairs(DeviceState& d, cudaStream_t s);
+int launch_contacts(DeviceState& d, float friction, cudaStream_t s);
+int launch_compact_contacts(DeviceState& d, cudaStream_t s);
+int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s);
+int launch_integrate(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s);
+
+}  // namespace b3g
+
+#endif

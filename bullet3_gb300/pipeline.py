@@ -1,0 +1,416 @@
+"""Host-side mirror of the reference's GPU rigid-body API.
+
+Same class names, method names, argument meaning and error behaviour as the reference's
+b3GpuNarrowPhase (src/Bullet3OpenCL/RigidBody/b3GpuNarrowPhase.h:9-99), b3GpuBroadphaseInterface /
+b3GpuGridBroadphase (src/Bullet3OpenCL/BroadphaseCollision/b3GpuBroadphaseInterface.h:12-40) and
+b3GpuRigidBodyPipeline (src/Bullet3OpenCL/RigidBody/b3GpuRigidBodyPipeline.h:25-67), implemented
+on the C ABI of libb3gpu.so.  Indices that the reference reports as -1 + b3Error are reported the
+same way here (the error text goes to `b3Error` below); CUDA failures raise.
+
+One native "world" backs the three objects, as the reference's three objects share one OpenCL
+context and queue: the narrowphase owns it, the broadphase and pipeline attach to it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+
+import numpy as np
+
+from . import capi
+from .capi import AABB, BODY, CONTACT, PAIR, INERTIA, call, fptr, iptr, ptr
+
+
+def b3Error(msg: str):
+    """The reference's b3Error sink (Bullet3Common/b3Logging.h:50-68): message to stderr."""
+    sys.stderr.write("b3Error: " + msg.rstrip() + "\n")
+
+
+class b3Config:
+    """b3Config (src/Bullet3Collision/.../b3Config.h:4-37) plus the constants the reference hard-codes."""
+
+    def __init__(self, **kw):
+        self.m_maxConvexBodies = 128 * 1024
+        self.m_maxConvexShapes = 8 * 1024
+        self.m_maxBroadphasePairs = 0
+        self.m_maxContactCapacity = 0
+        self.grid_cell_size = 0.0
+        self.grid_dim = 128
+        self.solver_mode = capi.SOLVER_PGS
+        self.solver_iterations = 10
+        self.residual_tol = 0.0
+        self.use_cuda_graph = True
+        self.contact_friction = 0.7
+        self.update_world_inertia = False
+        self.gravity = (0.0, -9.8, 0.0)
+        for k, v in kw.items():
+            if not hasattr(self, k):
+                raise AttributeError(k)
+            setattr(self, k, v)
+
+    def to_c(self) -> capi.b3gConfig:
+        return capi.default_config(max_bodies=self.m_maxConvexBodies, max_shapes=self.m_maxConvexShapes,
+                                   max_pairs=self.m_maxBroadphasePairs, max_contacts=self.m_maxContactCapacity,
+                                   grid_cell_size=self.grid_cell_size, grid_dim=self.grid_dim,
+                                   solver_mode=self.solver_mode, solver_iterations=self.solver_iterations,
+                                   residual_tol=self.residual_tol, use_cuda_graph=int(self.use_cuda_graph),
+                                   contact_friction=self.contact_friction,
+                                   update_world_inertia=int(self.update_world_inertia), gravity=self.gravity)
+
+
+class _World:
+    def __init__(self, config: b3Config, device: int = 0):
+        capi.load()
+        self.handle = C.c_void_p()
+        self.config = config
+        call("b3g_create", C.byref(config.to_c()), C.c_int(device), C.byref(self.handle))
+        self.uploaded = False
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value and capi._LIB is not None:
+            capi._LIB.b3g_destroy(h)
+            self.handle = None
+
+    def num_bodies(self) -> int:
+        n = C.c_int()
+        call("b3g_get_num_bodies", self.handle, C.byref(n))
+        return n.value
+
+
+class b3GpuNarrowPhase:
+    """b3GpuNarrowPhase: shape and body registry plus contact generation."""
+
+    def __init__(self, config: b3Config | None = None, device: int = 0):
+        self.m_config = config or b3Config()
+        self._w = _World(self.m_config, device)
+        self.m_static0Index = -1
+
+    @property
+    def world(self):
+        return self._w
+
+    # -- shapes -------------------------------------------------------------------------
+    def _reg(self, fn, *args) -> int:
+        out = C.c_int(-1)
+        st = getattr(capi.load(), fn)(self._w.handle, *args, C.byref(out))
+        if st in (2, 3, 8):  # invalid index / capacity / degenerate -> -1 + b3Error, as the reference
+            b3Error(capi._LIB.b3g_last_error().decode())
+            return -1
+        capi.check(st, fn)
+        return out.value
+
+    def registerSphereShape(self, radius: float) -> int:
+        return self._reg("b3g_register_sphere", C.c_float(radius))
+
+    def registerPlaneShape(self, planeNormal, planeConstant: float) -> int:
+        n = (C.c_float * 3)(*[float(x) for x in planeNormal[:3]])
+        return self._reg("b3g_register_plane", n, C.c_float(planeConstant))
+
+    def registerConvexHullShape(self, vertices, strideInBytes: int | None = None, numVertices: int | None = None,
+                                scaling=(1.0, 1.0, 1.0)) -> int:
+        v = np.ascontiguousarray(vertices, dtype=np.float32)
+        if strideInBytes is None:
+            v = v.reshape(-1, 3)
+            strideInBytes = 12
+            numVertices = len(v)
+        sc = (C.c_float * 3)(*[float(x) for x in scaling])
+        return self._reg("b3g_register_hull", fptr(v), C.c_int(strideInBytes), C.c_int(numVertices), sc)
+
+    def registerConvexHullShapeTables(self, vertices, planes, face_counts, indices, unique_edges) -> int:
+        """registerConvexHullShape(b3ConvexUtility*): precomputed hull tables."""
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+        p = np.ascontiguousarray(planes, np.float32).reshape(-1, 4)
+        fc = np.ascontiguousarray(face_counts, np.int32)
+        ix = np.ascontiguousarray(indices, np.int32)
+        e = np.ascontiguousarray(unique_edges, np.float32).reshape(-1, 3)
+        return self._reg("b3g_register_hull_tables", fptr(v), C.c_int(len(v)), fptr(p), iptr(fc), C.c_int(len(fc)),
+                         iptr(ix), fptr(e), C.c_int(len(e)))
+
+    def registerCompoundShape(self, childShapes) -> int:
+        b3Error("registerCompoundShape: compound shapes are not supported by this GPU step")
+        return -1
+
+    def registerConcaveMesh(self, vertices, indices, scaling) -> int:
+        b3Error("registerConcaveMesh: concave meshes are not supported by this GPU step")
+        return -1
+
+    # -- bodies -------------------------------------------------------------------------
+    def getNumRigidBodies(self) -> int:
+        return self._w.num_bodies()
+
+    def getNumCollidablesGpu(self) -> int:
+        n = C.c_int()
+        call("b3g_get_num_collidables", self._w.handle, C.byref(n))
+        return n.value
+
+    def writeAllBodiesToGpu(self):
+        call("b3g_write_all_to_gpu", self._w.handle)
+        self._w.uploaded = True
+
+    def readbackAllBodiesToCpu(self) -> np.ndarray:
+        n = self.getNumRigidBodies()
+        out = np.zeros(n, BODY)
+        call("b3g_read_bodies", self._w.handle, ptr(out), C.c_int(n))
+        return out
+
+    def writeBodiesToGpu(self, bodies: np.ndarray):
+        b = np.ascontiguousarray(bodies, BODY)
+        call("b3g_write_bodies", self._w.handle, ptr(b), C.c_int(len(b)))
+
+    def readInertiasToCpu(self) -> np.ndarray:
+        n = self.getNumRigidBodies()
+        out = np.zeros(n, INERTIA)
+        call("b3g_read_inertias", self._w.handle, ptr(out), C.c_int(n))
+        return out
+
+    def getObjectTransformFromCpu(self, bodyIndex: int):
+        b = self.readbackAllBodiesToCpu()[bodyIndex]
+        return b["pos"][:3].copy(), b["quat"].copy()
+
+    def computeContacts(self):
+        """computeContacts (b3GpuNarrowPhase.cpp:751-809) on the current overlapping pairs."""
+        call("b3g_compute_contacts", self._w.handle)
+
+    def getNumContactsGpu(self) -> int:
+        n = C.c_int()
+        call("b3g_read_contacts", self._w.handle, None, C.c_int(0), C.byref(n))
+        return n.value
+
+    def getContactsCPU(self) -> np.ndarray:
+        n = C.c_int()
+        call("b3g_read_contacts", self._w.handle, None, C.c_int(0), C.byref(n))
+        out = np.zeros(n.value, CONTACT)
+        if n.value:
+            call("b3g_read_contacts", self._w.handle, ptr(out), C.c_int(n.value), C.byref(n))
+        return out
+
+    def getContactsGpu(self) -> int:
+        p = C.c_void_p()
+        n = C.c_int()
+        call("b3g_get_contact_buffer", self._w.handle, C.byref(p), C.byref(n))
+        return p.value or 0
+
+    def setContactsFromCpu(self, contacts: np.ndarray):
+        c = np.ascontiguousarray(contacts, CONTACT)
+        call("b3g_write_contacts", self._w.handle, ptr(c), C.c_int(len(c)))
+
+    def getBodiesGpu(self) -> int:
+        p = C.c_void_p()
+        call("b3g_get_body_buffer", self._w.handle, C.byref(p))
+        return p.value or 0
+
+    def getBodyInertiasGpu(self) -> int:
+        p = C.c_void_p()
+        call("b3g_get_inertia_buffer", self._w.handle, C.byref(p))
+        return p.value or 0
+
+    def getStatic0Index(self) -> int:
+        return self.m_static0Index
+
+
+class b3GpuBroadphaseInterface:
+    """b3GpuBroadphaseInterface (pure interface)."""
+
+    def createProxy(self, aabbMin, aabbMax, userPtr, collisionFilterGroup, collisionFilterMask):
+        raise NotImplementedError
+
+    def createLargeProxy(self, aabbMin, aabbMax, userPtr, collisionFilterGroup, collisionFilterMask):
+        raise NotImplementedError
+
+    def calculateOverlappingPairs(self, maxPairs: int):
+        raise NotImplementedError
+
+    def calculateOverlappingPairsHost(self, maxPairs: int):
+        raise NotImplementedError
+
+
+class b3GpuGridBroadphase(b3GpuBroadphaseInterface):
+    """Uniform-grid broadphase (b3GpuGridBroadphase.cpp); large (static) proxies via the large-AABB path."""
+
+    CreateFunc = None
+
+    def __init__(self, narrowphase: b3GpuNarrowPhase | None = None):
+        self._np = narrowphase
+        self.m_smallAabbsMappingCPU = []
+        self.m_largeAabbsMappingCPU = []
+
+    def _attach(self, narrowphase: b3GpuNarrowPhase):
+        self._np = narrowphase
+
+    @property
+    def _h(self):
+        if self._np is None:
+            raise RuntimeError("broadphase not attached to a narrowphase/pipeline")
+        return self._np.world.handle
+
+    def createProxy(self, aabbMin, aabbMax, userPtr, collisionFilterGroup=1, collisionFilterMask=1):
+        self.m_smallAabbsMappingCPU.append(userPtr)
+
+    def createLargeProxy(self, aabbMin, aabbMax, userPtr, collisionFilterGroup=1, collisionFilterMask=1):
+        self.m_largeAabbsMappingCPU.append(userPtr)
+
+    def calculateOverlappingPairs(self, maxPairs: int = 0):
+        call("b3g_calculate_overlapping_pairs", self._h)
+
+    def calculateOverlappingPairsHost(self, maxPairs: int = 0):
+        raise NotImplementedError("there is no CPU broadphase in this library (the GPU path has no fallback)")
+
+    def writeAabbsToGpu(self):
+        pass  # AABBs are derived on the device from the body buffer every step
+
+    def getNumOverlap(self) -> int:
+        n = C.c_int()
+        call("b3g_read_pairs", self._h, None, C.c_int(0), C.byref(n))
+        return n.value
+
+    def getOverlappingPairsCPU(self) -> np.ndarray:
+        n = self.getNumOverlap()
+        out = np.zeros(n, PAIR)
+        if n:
+            m = C.c_int()
+            call("b3g_read_pairs", self._h, ptr(out), C.c_int(n), C.byref(m))
+        return out
+
+    def getOverlappingPairBuffer(self) -> int:
+        p = C.c_void_p()
+        n = C.c_int()
+        call("b3g_get_pair_buffer", self._h, C.byref(p), C.byref(n))
+        return p.value or 0
+
+    def getAabbBufferWS(self) -> int:
+        p = C.c_void_p()
+        call("b3g_get_aabb_buffer", self._h, C.byref(p))
+        return p.value or 0
+
+    def getAllAabbsCPU(self) -> np.ndarray:
+        n = self._np.getNumRigidBodies()
+        out = np.zeros(n, AABB)
+        call("b3g_read_aabbs", self._h, ptr(out), C.c_int(n))
+        return out
+
+    def setAllAabbsCPU(self, aabbs: np.ndarray):
+        a = np.ascontiguousarray(aabbs, AABB)
+        call("b3g_write_aabbs", self._h, ptr(a), C.c_int(len(a)))
+
+
+class b3GpuRigidBodyPipeline:
+    """b3GpuRigidBodyPipeline: registration and the per-frame step."""
+
+    def __init__(self, narrowphase: b3GpuNarrowPhase, broadphase: b3GpuBroadphaseInterface | None = None,
+                 broadphaseDbvt=None, config: b3Config | None = None):
+        self.m_narrowphase = narrowphase
+        self.m_broadphase = broadphase or b3GpuGridBroadphase()
+        if isinstance(self.m_broadphase, b3GpuGridBroadphase):
+            self.m_broadphase._attach(narrowphase)
+        self.m_config = config or narrowphase.m_config
+
+    @property
+    def _h(self):
+        return self.m_narrowphase.world.handle
+
+    def registerPhysicsInstance(self, mass: float, position, orientation, collidableIndex: int, userIndex: int = -1,
+                                writeInstanceToGpu: bool = False) -> int:
+        pos = (C.c_float * 3)(*[float(x) for x in position[:3]])
+        orn = (C.c_float * 4)(*[float(x) for x in orientation[:4]])
+        out = C.c_int(-1)
+        st = capi.load().b3g_register_body(self._h, C.c_float(mass), pos, orn, C.c_int(collidableIndex),
+                                           C.c_int(userIndex), C.byref(out))
+        if st in (2, 3):
+            b3Error(capi._LIB.b3g_last_error().decode())
+            return -1
+        capi.check(st, "b3g_register_body")
+        idx = out.value
+        if mass:
+            self.m_broadphase.createProxy(None, None, idx)
+        else:
+            self.m_broadphase.createLargeProxy(None, None, idx)
+            if self.m_narrowphase.m_static0Index < 0 and idx == 0:
+                self.m_narrowphase.m_static0Index = 0
+        return idx
+
+    def writeAllInstancesToGpu(self):
+        self.m_narrowphase.writeAllBodiesToGpu()
+
+    def setGravity(self, grav):
+        g = (C.c_float * 3)(*[float(x) for x in grav[:3]])
+        call("b3g_set_gravity", self._h, g)
+
+    def setSolver(self, mode: int, iterations: int, residual_tol: float = 0.0):
+        call("b3g_set_solver", self._h, C.c_int(mode), C.c_int(iterations), C.c_float(residual_tol))
+
+    def stepSimulation(self, deltaTime: float):
+        call("b3g_step", self._h, C.c_float(deltaTime))
+
+    def setupGpuAabbsFull(self):
+        call("b3g_setup_aabbs", self._h)
+
+    def solveContacts(self, deltaTime: float):
+        call("b3g_solve_contacts", self._h, C.c_float(deltaTime))
+
+    def integrate(self, timeStep: float):
+        call("b3g_integrate", self._h, C.c_float(timeStep))
+
+    def synchronize(self):
+        call("b3g_synchronize", self._h)
+
+    def getNumBodies(self) -> int:
+        return self.m_narrowphase.getNumRigidBodies()
+
+    def getBodyBuffer(self) -> int:
+        return self.m_narrowphase.getBodiesGpu()
+
+    def stats(self) -> capi.b3gStepStats:
+        s = capi.b3gStepStats()
+        call("b3g_get_stats", self._h, C.byref(s))
+        return s
+
+    def status(self, clear: bool = False) -> int:
+        f = C.c_uint()
+        call("b3g_status", self._h, C.byref(f), C.c_int(1 if clear else 0))
+        return f.value
+
+    def readBatches(self) -> np.ndarray:
+        n = C.c_int()
+        call("b3g_read_batches", self._h, None, C.c_int(0), C.byref(n))
+        out = np.zeros(n.value, np.int32)
+        if n.value:
+            call("b3g_read_batches", self._h, iptr(out), C.c_int(n.value), C.byref(n))
+        return out
+
+    def readImpulses(self) -> np.ndarray:
+        n = C.c_int()
+        call("b3g_read_impulses", self._h, None, C.c_int(0), C.byref(n))
+        out = np.zeros((n.value, 12), np.float32)
+        if n.value:
+            call("b3g_read_impulses", self._h, fptr(out), C.c_int(n.value), C.byref(n))
+        return out
+
+    def setProfiling(self, on: bool):
+        call("b3g_set_profiling", self._h, C.c_int(1 if on else 0))
+
+    def stageTimes(self) -> np.ndarray:
+        out = np.zeros(7, np.float32)
+        call("b3g_get_stage_times", self._h, fptr(out))
+        return out
+
+    def launchCount(self) -> int:
+        n = C.c_longlong()
+        call("b3g_get_launch_count", self._h, C.byref(n))
+        return n.value
+
+    # joints are outside this GPU step: the reference API exists, the call reports -1
+    def createPoint2PointConstraint(self, *a, **k) -> int:
+        b3Error("createPoint2PointConstraint: joints are not supported by this GPU step")
+        return -1
+
+    def createFixedConstraint(self, *a, **k) -> int:
+        b3Error("createFixedConstraint: joints are not supported by this GPU step")
+        return -1
+
+    def removeConstraintByUid(self, uid: int):
+        b3Error("removeConstraintByUid: joints are not supported by this GPU step")
+
+    def castRays(self, rays):
+        b3Error("castRays: ray casting is not part of this GPU step; no hits reported")
+        return [None] * len(rays)

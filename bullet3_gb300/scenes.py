@@ -1,0 +1,190 @@
+"""Seeded synthetic scenes with the shapes, sizes and value distributions of the benchmark
+configurations (numpy.random.Generator(PCG64(seed))).
+
+  box_pile       unit boxes (8-vertex hulls, half extent 0.5, mass 1) on a lattice above a static
+                 plane y=0; 10x10x10 spacing 1.1 jitter 0.01 (1,000 boxes) or 64x64x64 jitter 0.05
+                 (262,144 boxes)
+  mixed_scene    uniform positions in a cube, uniform random orientations; 50% boxes with half
+                 extents U[0.2,0.6], 25% spheres r U[0.2,0.5], 25% hulls of 12-32 N(0, 0.4^2) points;
+                 linear velocities N(0,1)
+  batched_piles  many independent box/sphere piles, each on its own plane, body counts log-uniform
+
+A Scene is plain numpy data; `load_scene` registers it through the reference-style API.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import capi
+
+
+@dataclass
+class Scene:
+    shapes: list = field(default_factory=list)        # dicts: type hull/sphere/plane + parameters
+    body_shape: np.ndarray = None                     # (N,) shape index per body
+    mass: np.ndarray = None                           # (N,)
+    pos: np.ndarray = None                            # (N,3)
+    orn: np.ndarray = None                            # (N,4) x,y,z,w
+    linvel: np.ndarray = None                         # (N,3) or None
+    angvel: np.ndarray = None
+    cell: float = 0.0                                 # grid cell size (0 = automatic)
+    name: str = ""
+
+    @property
+    def num_bodies(self) -> int:
+        return len(self.mass)
+
+
+def box_vertices(hx, hy, hz) -> np.ndarray:
+    s = np.array([[x, y, z] for x in (-1, 1) for y in (-1, 1) for z in (-1, 1)], np.float32)
+    return s * np.array([hx, hy, hz], np.float32)
+
+
+def random_quaternions(rng, n) -> np.ndarray:
+    q = rng.standard_normal((n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    return q.astype(np.float32)
+
+
+def box_pile(nx=10, ny=10, nz=10, spacing=1.1, base_y=0.6, jitter=0.01, half=0.5, mass=1.0, seed=0,
+             plane=True) -> Scene:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sc = Scene(name=f"box_pile_{nx}x{ny}x{nz}")
+    if plane:
+        sc.shapes.append({"type": "plane", "normal": (0.0, 1.0, 0.0), "constant": 0.0})
+    sc.shapes.append({"type": "hull", "verts": box_vertices(half, half, half)})
+    box = len(sc.shapes) - 1
+    ii, jj, kk = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    p = np.stack([ii.ravel() * spacing, base_y + jj.ravel() * spacing, kk.ravel() * spacing], axis=1)
+    p = p - np.array([(nx - 1) * spacing * 0.5, 0.0, (nz - 1) * spacing * 0.5])
+    p = p + rng.uniform(-jitter, jitter, p.shape)
+    n = len(p)
+    shapes = [box] * n
+    masses = [mass] * n
+    pos = list(p)
+    if plane:
+        shapes = [0] + shapes
+        masses = [0.0] + masses
+        pos = [np.zeros(3)] + pos
+    sc.body_shape = np.array(shapes, np.int32)
+    sc.mass = np.array(masses, np.float32)
+    sc.pos = np.array(pos, np.float32)
+    sc.orn = np.tile(np.array([0, 0, 0, 1], np.float32), (len(sc.mass), 1))
+    return sc
+
+
+def mixed_scene(n=131072, extent=64.0, seed=0, velocity_sigma=1.0, plane=False, cell_factor=2.0) -> Scene:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sc = Scene(name=f"mixed_{n}")
+    kinds = rng.permutation(np.repeat([0, 1, 2], [n // 2, n // 4, n - n // 2 - n // 4]))
+    shapes, masses = [], []
+    max_ext = 0.0
+    if plane:
+        sc.shapes.append({"type": "plane", "normal": (0.0, 1.0, 0.0), "constant": 0.0})
+    for k in kinds:
+        if k == 0:
+            h = rng.uniform(0.2, 0.6, 3).astype(np.float32)
+            sc.shapes.append({"type": "hull", "verts": box_vertices(*h)})
+            max_ext = max(max_ext, 2 * float(h.max()))
+        elif k == 1:
+            r = float(rng.uniform(0.2, 0.5))
+            sc.shapes.append({"type": "sphere", "radius": r})
+            max_ext = max(max_ext, 2 * r)
+        else:
+            m = int(rng.integers(12, 33))
+            pts = (rng.standard_normal((m, 3)) * 0.4).astype(np.float32)
+            sc.shapes.append({"type": "hull", "verts": pts})
+            max_ext = max(max_ext, float((pts.max(0) - pts.min(0)).max()))
+        shapes.append(len(sc.shapes) - 1)
+        masses.append(1.0)
+    pos = rng.uniform(0.0, extent, (n, 3)).astype(np.float32)
+    orn = random_quaternions(rng, n)
+    vel = (rng.standard_normal((n, 3)) * velocity_sigma).astype(np.float32)
+    if plane:
+        shapes = [0] + shapes
+        masses = [0.0] + masses
+        pos = np.vstack([np.zeros((1, 3), np.float32), pos])
+        orn = np.vstack([np.array([[0, 0, 0, 1]], np.float32), orn])
+        vel = np.vstack([np.zeros((1, 3), np.float32), vel])
+    sc.body_shape = np.array(shapes, np.int32)
+    sc.mass = np.array(masses, np.float32)
+    sc.pos = pos
+    sc.orn = orn
+    sc.linvel = vel
+    sc.cell = cell_factor * max_ext
+    return sc
+
+
+def load_scene(scene: Scene, config=None, device: int = 0, upload: bool = True):
+    """Register a Scene through the reference-style API; returns (narrowphase, broadphase, pipeline)."""
+    from .pipeline import b3Config, b3GpuGridBroadphase, b3GpuNarrowPhase, b3GpuRigidBodyPipeline
+    if config is None:
+        config = b3Config()
+    config.m_maxConvexBodies = max(config.m_maxConvexBodies, scene.num_bodies)
+    config.m_maxConvexShapes = max(config.m_maxConvexShapes, len(scene.shapes))
+    if scene.cell and not config.grid_cell_size:
+        config.grid_cell_size = scene.cell
+    np_ = b3GpuNarrowPhase(config, device)
+    bp = b3GpuGridBroadphase()
+    pl = b3GpuRigidBodyPipeline(np_, bp, None, config)
+    col = []
+    for s in scene.shapes:
+        if s["type"] == "hull":
+            c = np_.registerConvexHullShape(s["verts"])
+        elif s["type"] == "sphere":
+            c = np_.registerSphereShape(s["radius"])
+        elif s["type"] == "plane":
+            c = np_.registerPlaneShape(s["normal"], s["constant"])
+        elif s["type"] == "hull_tables":
+            c = np_.registerConvexHullShapeTables(s["verts"], s["planes"], s["face_counts"], s["indices"],
+                                                  s["edges"])
+        else:
+            raise ValueError(s["type"])
+        if c < 0:
+            raise RuntimeError(f"shape registration failed: {s['type']}")
+        col.append(c)
+    for i in range(scene.num_bodies):
+        b = pl.registerPhysicsInstance(float(scene.mass[i]), scene.pos[i], scene.orn[i], col[scene.body_shape[i]], i)
+        if b < 0:
+            raise RuntimeError("body registration failed")
+    if upload:
+        pl.writeAllInstancesToGpu()
+        if scene.linvel is not None or scene.angvel is not None:
+            bodies = np_.readbackAllBodiesToCpu()
+            if scene.linvel is not None:
+                bodies["linVel"][:, :3] = scene.linvel
+            if scene.angvel is not None:
+                bodies["angVel"][:, :3] = scene.angvel
+            np_.writeBodiesToGpu(bodies)
+    return np_, bp, pl
+
+
+def registered_tables(narrowphase):
+    """Host copies of the registered shape tables and bodies (no GPU needed)."""
+    import ctypes as C
+    h = narrowphase.world.handle
+    counts = np.zeros(6, np.int32)
+    capi.call("b3g_read_shape_tables", h, None, None, None, None, None, None, None, capi.iptr(counts))
+    ncol, nh, nf, ni, nv, ne = (int(x) for x in counts)
+    t = {
+        "collidables": np.zeros(max(ncol, 1), capi.COLLIDABLE),
+        "local_aabbs": np.zeros(max(ncol, 1), capi.AABB),
+        "hulls": np.zeros(max(nh, 1), capi.HULL),
+        "faces": np.zeros(max(nf, 1), capi.FACE),
+        "indices": np.zeros(max(ni, 1), np.int32),
+        "verts": np.zeros((max(nv, 1), 4), np.float32),
+        "edges": np.zeros((max(ne, 1), 4), np.float32),
+    }
+    caps = np.array([max(ncol, 1), max(nh, 1), max(nf, 1), max(ni, 1), max(nv, 1), max(ne, 1)], np.int32)
+    capi.call("b3g_read_shape_tables", h, capi.ptr(t["collidables"]), capi.ptr(t["hulls"]), capi.ptr(t["faces"]),
+              capi.iptr(t["indices"]), capi.ptr(t["verts"]), capi.ptr(t["edges"]), capi.ptr(t["local_aabbs"]),
+              capi.iptr(caps))
+    nb = narrowphase.getNumRigidBodies()
+    bodies = np.zeros(nb, capi.BODY)
+    inertias = np.zeros(nb, capi.INERTIA)
+    capi.call("b3g_read_registered_bodies", h, capi.ptr(bodies), capi.ptr(inertias), C.c_int(nb))
+    t["bodies"] = bodies
+    t["inertias"] = inertias
+    return t

@@ -1,0 +1,207 @@
+/*
+ * b3g_capi.h -- C ABI of the GB300-native GPU rigid-body step.
+ *
+ * This is the thin boundary that the drop-in C++ classes (b3GpuRigidBodyPipeline,
+ * b3GpuNarrowPhase, b3GpuGridBroadphase; see include/b3g_compat.h) and foreign
+ * bindings (ctypes, cgo, JNI) call.  Plain pointers and sizes only; every entry
+ * point returns a b3gStatus (0 = ok) and never aborts.  Each function names the
+ * reference interface it replaces (paths relative to the reference project root,
+ * src/Bullet3OpenCL/...).
+ *
+ * Threading: one world per host thread, one CUDA stream per world, exactly like
+ * the reference's single in-order cl_command_queue (b3GpuRigidBodyPipeline.h:33).
+ * Device pointers returned by getters are borrowed and stay valid until the next
+ * b3g_write_all_to_gpu / b3g_destroy.
+ */
+#ifndef B3G_CAPI_H
+#define B3G_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct b3gWorld* b3g_handle;
+
+typedef enum b3gStatus {
+    B3G_OK = 0,
+    B3G_ERR_INVALID_ARG = 1,      /* null handle / pointer, bad size */
+    B3G_ERR_INVALID_INDEX = 2,    /* reference returns -1 + b3Error (b3GpuRigidBodyPipeline.cpp:620-624) */
+    B3G_ERR_CAPACITY = 3,         /* a b3Config capacity was exceeded (b3GpuNarrowPhase.cpp:821-825) */
+    B3G_ERR_CUDA = 4,             /* a CUDA runtime call failed; see b3g_last_error() */
+    B3G_ERR_NOT_UPLOADED = 5,     /* step/stage called before b3g_write_all_to_gpu */
+    B3G_ERR_UNSUPPORTED = 6,      /* compound / concave shapes, joints */
+    B3G_ERR_BARRIER_TIMEOUT = 7,  /* a persistent kernel's bounded grid barrier gave up */
+    B3G_ERR_DEGENERATE = 8        /* convex hull input is degenerate (fewer than 4 affinely independent points) */
+} b3gStatus;
+
+/* Device-side status word bits (b3g_status). Set by kernels, read once per step. */
+#define B3G_FLAG_PAIR_OVERFLOW     0x1u   /* reference: b3GpuGridBroadphase.cpp:164-168,233-237 */
+#define B3G_FLAG_CONTACT_OVERFLOW  0x2u   /* reference: b3ConvexHullContact.cpp:2851-2855,4358-4362 */
+#define B3G_FLAG_BATCH_OVERFLOW    0x4u   /* reference: b3GpuPgsContactSolver.cpp:1499-1504 */
+#define B3G_FLAG_BARRIER_TIMEOUT   0x8u
+#define B3G_FLAG_NAN               0x10u
+#define B3G_FLAG_CLIP_OVERFLOW     0x20u
+
+#define B3G_SOLVER_PGS 0      /* b3PgsJacobiSolver(true)  -- graph-coloured Gauss-Seidel on the GPU */
+#define B3G_SOLVER_JACOBI 1   /* b3PgsJacobiSolver(false) -- mass-splitting Jacobi */
+
+/* One configuration struct replaces b3Config (b3Config.h:4-37) plus the constants the
+ * reference hard-codes (dt 1/60 b3GpuPgsContactSolver.cpp:672, damping 0.99
+ * b3GpuRigidBodyPipeline.cpp:468, gravity :92, friction 0.7 b3ConvexHullContact.cpp:1384). */
+typedef struct b3gConfig {
+    int max_bodies;            /* m_maxConvexBodies */
+    int max_shapes;            /* m_maxConvexShapes (collidables) */
+    int max_pairs;             /* m_maxBroadphasePairs; 0 = 8 * max_bodies */
+    int max_contacts;          /* m_maxContactCapacity; 0 = 4 * max_bodies */
+    float grid_cell_size;      /* 0 = automatic: the largest world-AABB extent any dynamic body can reach */
+    int grid_dim;              /* cells per axis, power of two (reference: 128, b3GpuGridBroadphase.cpp:38-49) */
+    float gravity[3];
+    float angular_damping;     /* 0.99 */
+    int solver_mode;           /* B3G_SOLVER_PGS or B3G_SOLVER_JACOBI */
+    int solver_iterations;     /* b3ContactSolverInfo::m_numIterations */
+    float erp;                 /* Baumgarte factor, b3ContactSolverInfo::m_erp = 0.2 */
+    float contact_threshold;   /* contact processing threshold 0.02 (b3PgsJacobiSolver.h:44) */
+    float contact_friction;    /* friction stored in every contact: 0.7 as in the reference */
+    float residual_tol;        /* >0: stop PGS/Jacobi when the impulse residual drops below it */
+    int update_world_inertia;  /* 0 = reference behaviour (world inverse inertia frozen at registration) */
+    int use_cuda_graph;        /* capture the whole step as one CUDA graph */
+    int warm_start;            /* 0 = cold start (reference); 1 = learned warm start if a model is loaded */
+    int reserved[8];
+} b3gConfig;
+
+/* Per-step counters, copied once per step from the device. */
+typedef struct b3gStepStats {
+    int num_pairs;
+    int num_contacts;       /* manifolds */
+    int num_points;         /* contact points (rows) */
+    int num_colors;         /* PGS batches */
+    int iterations;         /* solver sweeps actually run */
+    float residual;         /* last relative impulse residual (0 if not tracked) */
+    unsigned int status;    /* B3G_FLAG_* bits */
+    int num_large;          /* bodies handled by the large-AABB path */
+} b3gStepStats;
+
+/* ------------------------------------------------------------------ lifetime */
+/* Fills the defaults listed above. */
+b3gStatus b3g_config_default(b3gConfig* cfg);
+/* Replaces the b3GpuNarrowPhase + b3GpuGridBroadphase + b3GpuRigidBodyPipeline constructors
+ * (b3GpuNarrowPhase.cpp:18, b3GpuGridBroadphase.cpp:24, b3GpuRigidBodyPipeline.cpp:65).
+ * Host registries only; no device memory is touched until b3g_write_all_to_gpu. */
+b3gStatus b3g_create(const b3gConfig* cfg, int cuda_device, b3g_handle* out);
+b3gStatus b3g_destroy(b3g_handle h);
+/* Text of the last error on this thread. */
+const char* b3g_last_error(void);
+/* Library version string. */
+const char* b3g_version(void);
+
+/* ------------------------------------------------------------------ shapes (b3GpuNarrowPhase) */
+/* b3GpuNarrowPhase::registerSphereShape (b3GpuNarrowPhase.cpp:159) */
+b3gStatus b3g_register_sphere(b3g_handle h, float radius, int* out_collidable);
+/* b3GpuNarrowPhase::registerPlaneShape (b3GpuNarrowPhase.cpp:202) */
+b3gStatus b3g_register_plane(b3g_handle h, const float normal[3], float constant, int* out_collidable);
+/* b3GpuNarrowPhase::registerConvexHullShape(const float*, int stride, int n, const float* scaling)
+ * (b3GpuNarrowPhase.cpp:298-314): builds the hull, merges coplanar faces, finds unique edges. */
+b3gStatus b3g_register_hull(b3g_handle h, const float* verts, int stride_bytes, int num_verts,
+                            const float scaling[3], int* out_collidable);
+/* b3GpuNarrowPhase::registerConvexHullShape(b3ConvexUtility*) (b3GpuNarrowPhase.cpp:316-368):
+ * registers precomputed hull tables (vertices xyz, faces as plane + index lists, unique edges).
+ * face_planes: 4 floats per face; face_index_counts: indices per face; face_indices: flat.
+ * The local centre is the vertex mean, as in the reference (:324-329). */
+b3gStatus b3g_register_hull_tables(b3g_handle h, const float* verts_xyz, int num_verts,
+                                   const float* face_planes, const int* face_index_counts, int num_faces,
+                                   const int* face_indices, const float* unique_edges_xyz, int num_edges,
+                                   int* out_collidable);
+
+/* ------------------------------------------------------------------ bodies (b3GpuRigidBodyPipeline) */
+/* b3GpuRigidBodyPipeline::registerPhysicsInstance (b3GpuRigidBodyPipeline.cpp:603-669) together with
+ * b3GpuNarrowPhase::registerRigidBody (b3GpuNarrowPhase.cpp:816-908): world AABB with margin 0.01,
+ * AABB-box inertia, mass 0 => static large proxy. */
+b3gStatus b3g_register_body(b3g_handle h, float mass, const float pos[3], const float orn[4],
+                            int collidable, int user_index, int* out_body);
+/* writeAllInstancesToGpu (b3GpuRigidBodyPipeline.cpp:597) + writeAllBodiesToGpu
+ * (b3GpuNarrowPhase.cpp:915-944) + writeAabbsToGpu (b3GpuGridBroadphase.cpp:297-302):
+ * allocates every device buffer at its capacity and uploads the registries. */
+b3gStatus b3g_write_all_to_gpu(b3g_handle h);
+/* b3GpuRigidBodyPipeline::setGravity (b3GpuRigidBodyPipeline.cpp:587-590) */
+b3gStatus b3g_set_gravity(b3g_handle h, const float g[3]);
+/* Changes the solver mode / iteration count / residual target between steps. */
+b3gStatus b3g_set_solver(b3g_handle h, int mode, int iterations, float residual_tol);
+
+/* ------------------------------------------------------------------ the step */
+/* b3GpuRigidBodyPipeline::stepSimulation (b3GpuRigidBodyPipeline.cpp:221-463): AABBs, pairs,
+ * contacts, batching, solve, integrate -- enqueued on the world's stream (one CUDA graph
+ * launch when use_cuda_graph is set); returns without synchronising. */
+b3gStatus b3g_step(b3g_handle h, float dt);
+/* Individual stages, same order as stepSimulation. */
+b3gStatus b3g_setup_aabbs(b3g_handle h);                     /* setupGpuAabbsFull :500-575 */
+b3gStatus b3g_calculate_overlapping_pairs(b3g_handle h);     /* b3GpuGridBroadphase::calculateOverlappingPairs :117-259 */
+b3gStatus b3g_compute_contacts(b3g_handle h);                /* b3GpuNarrowPhase::computeContacts :751-809 */
+b3gStatus b3g_solve_contacts(b3g_handle h, float dt);        /* b3GpuPgsContactSolver::solveContacts :568-1103 */
+b3gStatus b3g_integrate(b3g_handle h, float dt);             /* b3GpuRigidBodyPipeline::integrate :465-498 */
+/* Waits for the world's stream. */
+b3gStatus b3g_synchronize(b3g_handle h);
+/* Reads the per-step counters (synchronises). */
+b3gStatus b3g_get_stats(b3g_handle h, b3gStepStats* out);
+/* Device status word (B3G_FLAG_*), synchronises; clear=1 resets it. */
+b3gStatus b3g_status(b3g_handle h, unsigned int* flags, int clear);
+
+/* ------------------------------------------------------------------ getters (borrowed device pointers) */
+b3gStatus b3g_get_num_bodies(b3g_handle h, int* n);                       /* getNumBodies */
+b3gStatus b3g_get_body_buffer(b3g_handle h, void** dptr);                 /* getBodyBuffer :65 -> b3RigidBodyData* */
+b3gStatus b3g_get_inertia_buffer(b3g_handle h, void** dptr);              /* b3GpuNarrowPhase::getBodyInertiasGpu */
+b3gStatus b3g_get_aabb_buffer(b3g_handle h, void** dptr);                 /* b3GpuBroadphaseInterface::getAabbBufferWS */
+b3gStatus b3g_get_pair_buffer(b3g_handle h, void** dptr, int* num_pairs); /* getOverlappingPairBuffer + getNumOverlap (syncs) */
+b3gStatus b3g_get_contact_buffer(b3g_handle h, void** dptr, int* num);    /* b3GpuNarrowPhase::getContactsGpu + getNumContactsGpu (syncs) */
+b3gStatus b3g_get_stream(b3g_handle h, void** cuda_stream);
+
+/* ------------------------------------------------------------------ host copies */
+b3gStatus b3g_read_bodies(b3g_handle h, void* host_bodies, int n);        /* readbackAllBodiesToCpu */
+b3gStatus b3g_write_bodies(b3g_handle h, const void* host_bodies, int n); /* setObjectTransform/VelocityCpu + write */
+b3gStatus b3g_read_inertias(b3g_handle h, void* host_inertias, int n);
+b3gStatus b3g_read_aabbs(b3g_handle h, void* host_aabbs, int n);
+b3gStatus b3g_write_aabbs(b3g_handle h, const void* host_aabbs, int n);   /* feeds the broadphase identical AABBs */
+b3gStatus b3g_read_pairs(b3g_handle h, void* host_pairs, int capacity, int* num_pairs);
+b3gStatus b3g_read_contacts(b3g_handle h, void* host_contacts, int capacity, int* num_contacts);
+/* Writes contacts for the solver stage (used to solve identical manifolds in parity tests). */
+b3gStatus b3g_write_contacts(b3g_handle h, const void* host_contacts, int num_contacts);
+/* Reads the colour (batch) of every manifold after the solver stage (PGS). */
+b3gStatus b3g_read_batches(b3g_handle h, int* host_batch, int capacity, int* num);
+/* Reads per-point solver impulses (normal, lateral1, lateral2) after the solve: 3 floats per
+ * point, 4 point slots per manifold. */
+b3gStatus b3g_read_impulses(b3g_handle h, float* host, int capacity_manifolds, int* num);
+
+/* Host-side reads of the shape tables (for checks). */
+b3gStatus b3g_get_num_collidables(b3g_handle h, int* n);
+/* Host registry copies of the registered bodies and inertias (as registered, before upload;
+ * b3GpuNarrowPhase::m_bodyBufferCPU / m_inertiaBufferCPU).  No GPU needed. */
+b3gStatus b3g_read_registered_bodies(b3g_handle h, void* bodies, void* inertias, int n);
+b3gStatus b3g_read_shape_tables(b3g_handle h, void* collidables, void* hulls, void* faces, int* indices,
+                                void* vertices, void* edges, void* local_aabbs, int* counts6);
+
+/* ------------------------------------------------------------------ stage profiling */
+/* Records CUDA events around each stage on the world's stream when on=1. */
+b3gStatus b3g_set_profiling(b3g_handle h, int on);
+/* Milliseconds per stage of the last profiled step: aabb, pairs, contacts, batching,
+ * setup, solve, integrate (7 floats). */
+b3gStatus b3g_get_stage_times(b3g_handle h, float* ms7);
+/* Number of kernels this library launched since creation (counted on the host at launch). */
+b3gStatus b3g_get_launch_count(b3g_handle h, long long* n);
+
+/* ------------------------------------------------------------------ convex hull (host only, no GPU) */
+/* b3ConvexUtility::initializePolyhedralFeatures (Bullet3Collision/NarrowPhaseCollision/b3ConvexUtility.cpp:26-246)
+ * as called from registerConvexHullShape.  Output capacities are given in counts6 on entry
+ * (vertices, faces, indices, edges, -, -) and replaced by the sizes written on return.
+ * verts_out: xyz per vertex; planes_out: 4 floats per face; face_counts_out: indices per face;
+ * indices_out: flat; edges_out: xyz per unique edge; center_out: vertex mean. */
+b3gStatus b3g_hull_compute(const float* verts, int stride_bytes, int num_verts, const float scaling[3],
+                           float* verts_out, float* planes_out, int* face_counts_out, int* indices_out,
+                           float* edges_out, float* center_out, int* counts6);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

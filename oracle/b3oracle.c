@@ -1,0 +1,1066 @@
+/*
+ * b3oracle.c -- CPU oracle for the GPU rigid-body step.  TEST INFRASTRUCTURE ONLY
+ * (used by tests/, the smoke check and the bench's CPU-baseline leg; never by the product).
+ *
+ * Restates, in plain C, the reference CPU code the GPU path must agree with.  Paths are
+ * relative to the reference project's src/ directory.  Compile with -ffp-contract=off.
+ */
+#include "b3oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define SHAPE_CONVEX_HULL 3
+#define SHAPE_PLANE 4
+#define SHAPE_SPHERE 7
+
+static int g_threads = 1;
+int oracle_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+void oracle_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
+
+/* ------------------------------------------------------------------ vector math (fixed order) */
+typedef struct { float x, y, z; } v3;
+typedef struct { float x, y, z, w; } qt;
+typedef struct { v3 r0, r1, r2; } m3;
+
+static inline v3 mk(float x, float y, float z) { v3 r = {x, y, z}; return r; }
+static inline v3 f4v(of4 a) { return mk(a.x, a.y, a.z); }
+static inline qt f4q(of4 a) { qt q = {a.x, a.y, a.z, a.w}; return q; }
+static inline v3 add(v3 a, v3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline v3 sub(v3 a, v3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline v3 neg(v3 a) { return mk(-a.x, -a.y, -a.z); }
+static inline v3 scl(v3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+static inline v3 lscl(float s, v3 a) { return mk(s * a.x, s * a.y, s * a.z); }
+static inline float dot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline v3 cross(v3 a, v3 b) { return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+static inline v3 nrm(v3 a) { float l = sqrtf(dot(a, a)); return mk(a.x / l, a.y / l, a.z / l); }
+
+static inline m3 qmat(qt q) {
+    float d = q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w;
+    float s = 2.0f / d;
+    float xs = q.x * s, ys = q.y * s, zs = q.z * s;
+    float wx = q.w * xs, wy = q.w * ys, wz = q.w * zs;
+    float xx = q.x * xs, xy = q.x * ys, xz = q.x * zs;
+    float yy = q.y * ys, yz = q.y * zs, zz = q.z * zs;
+    m3 m;
+    m.r0 = mk(1.0f - (yy + zz), xy - wz, xz + wy);
+    m.r1 = mk(xy + wz, 1.0f - (xx + zz), yz - wx);
+    m.r2 = mk(xz - wy, yz + wx, 1.0f - (xx + yy));
+    return m;
+}
+static inline v3 mmul(const m3* m, v3 v) { return mk(dot(m->r0, v), dot(m->r1, v), dot(m->r2, v)); }
+static inline v3 mtmul(const m3* m, v3 v) {
+    return mk(m->r0.x * v.x + m->r1.x * v.y + m->r2.x * v.z, m->r0.y * v.x + m->r1.y * v.y + m->r2.y * v.z,
+              m->r0.z * v.x + m->r1.z * v.y + m->r2.z * v.z);
+}
+static inline v3 imul(const omat3* m, v3 v) {
+    return mk(m->row[0].x * v.x + m->row[0].y * v.y + m->row[0].z * v.z,
+              m->row[1].x * v.x + m->row[1].y * v.y + m->row[1].z * v.z,
+              m->row[2].x * v.x + m->row[2].y * v.y + m->row[2].z * v.z);
+}
+static inline qt qmul(qt a, qt b) {
+    qt r;
+    r.x = a.w * b.x + a.x * b.w + a.y * b.z - a.z * b.y;
+    r.y = a.w * b.y + a.y * b.w + a.z * b.x - a.x * b.z;
+    r.z = a.w * b.z + a.z * b.w + a.x * b.y - a.y * b.x;
+    r.w = a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z;
+    return r;
+}
+
+/* ------------------------------------------------------------------ AABBs */
+/* b3TransformAabb2 (Bullet3Collision/BroadPhaseCollision/shared/b3Aabb.h:24-43) */
+static void transform_aabb(const oaabb* local, v3 pos, qt q, float margin, v3* mn, v3* mx) {
+    v3 lmin = mk(local->minv[0], local->minv[1], local->minv[2]);
+    v3 lmax = mk(local->maxv[0], local->maxv[1], local->maxv[2]);
+    v3 he = lscl(0.5f, sub(lmax, lmin));
+    he = add(he, mk(margin, margin, margin));
+    v3 lc = lscl(0.5f, add(lmax, lmin));
+    m3 m = qmat(q);
+    m3 a;
+    a.r0 = mk(fabsf(m.r0.x), fabsf(m.r0.y), fabsf(m.r0.z));
+    a.r1 = mk(fabsf(m.r1.x), fabsf(m.r1.y), fabsf(m.r1.z));
+    a.r2 = mk(fabsf(m.r2.x), fabsf(m.r2.y), fabsf(m.r2.z));
+    v3 c = add(mmul(&m, lc), pos);
+    v3 e = mk(dot(he, a.r0), dot(he, a.r1), dot(he, a.r2));
+    *mn = sub(c, e);
+    *mx = add(c, e);
+}
+
+void oracle_aabbs(const obody* bodies, int n, const oshapes* sh, oaabb* out) {
+    int i;
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (i = 0; i < n; i++) {
+        const obody* b = &bodies[i];
+        v3 mn, mx;
+        qt q = f4q(b->quat);
+        transform_aabb(&sh->local_aabbs[b->collidableIdx], f4v(b->pos), q, 0.f, &mn, &mx);
+        out[i].minv[0] = mn.x; out[i].minv[1] = mn.y; out[i].minv[2] = mn.z; out[i].minw = i;
+        out[i].maxv[0] = mx.x; out[i].maxv[1] = mx.y; out[i].maxv[2] = mx.z;
+        out[i].maxw = b->invMass == 0.f ? 0 : 1;
+    }
+}
+
+/* ------------------------------------------------------------------ pairs */
+static inline int overlap(const oaabb* a, const oaabb* b) {
+    return (a->minv[0] <= b->maxv[0]) && (b->minv[0] <= a->maxv[0]) && (a->minv[1] <= b->maxv[1]) &&
+           (b->minv[1] <= a->maxv[1]) && (a->minv[2] <= b->maxv[2]) && (b->minv[2] <= a->maxv[2]);
+}
+
+static int cmp_u64(const void* a, const void* b) {
+    uint64_t x = *(const uint64_t*)a, y = *(const uint64_t*)b;
+    return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+int oracle_pairs_bruteforce(const oaabb* aabbs, int n, opair* out, int cap) {
+    int count = 0, i, j;
+    for (i = 0; i < n; i++)
+        for (j = i + 1; j < n; j++) {
+            if (aabbs[i].maxw == 0 && aabbs[j].maxw == 0) continue; /* static-static */
+            if (overlap(&aabbs[i], &aabbs[j])) {
+                if (count < cap) {
+                    out[count].x = i; out[count].y = j; out[count].z = -1; out[count].w = -1;
+                }
+                count++;
+            }
+        }
+    return count;
+}
+
+typedef struct { int64_t cx, cy, cz; int idx; } cellrec;
+static int cmp_cell(const void* a, const void* b) {
+    const cellrec* p = (const cellrec*)a;
+    const cellrec* q = (const cellrec*)b;
+    if (p->cx != q->cx) return p->cx < q->cx ? -1 : 1;
+    if (p->cy != q->cy) return p->cy < q->cy ? -1 : 1;
+    if (p->cz != q->cz) return p->cz < q->cz ? -1 : 1;
+    return p->idx < q->idx ? -1 : (p->idx > q->idx ? 1 : 0);
+}
+static int find_cell(const cellrec* r, int n, int64_t x, int64_t y, int64_t z) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        const cellrec* m = &r[mid];
+        int less = m->cx < x || (m->cx == x && (m->cy < y || (m->cy == y && m->cz < z)));
+        if (less) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+/* Exact pair set through an unbounded integer grid (no hash wrap): dynamic bodies in cells
+ * of size `cell` (>= every dynamic AABB extent), neighbours in 27 cells; statics test every
+ * dynamic body.  Output sorted by (a, b). */
+int oracle_pairs_grid(const oaabb* aabbs, int n, float cell, opair* out, int cap) {
+    float inv = 1.f / cell;
+    int nd = 0, ns = 0, i;
+    cellrec* rec = (cellrec*)malloc(sizeof(cellrec) * (size_t)(n > 0 ? n : 1));
+    int* statics = (int*)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    for (i = 0; i < n; i++) {
+        if (aabbs[i].maxw) {
+            float cx = (aabbs[i].minv[0] + aabbs[i].maxv[0]) * 0.5f;
+            float cy = (aabbs[i].minv[1] + aabbs[i].maxv[1]) * 0.5f;
+            float cz = (aabbs[i].minv[2] + aabbs[i].maxv[2]) * 0.5f;
+            rec[nd].cx = (int64_t)floorf(cx * inv);
+            rec[nd].cy = (int64_t)floorf(cy * inv);
+            rec[nd].cz = (int64_t)floorf(cz * inv);
+            rec[nd].idx = i;
+            nd++;
+        } else {
+            statics[ns++] = i;
+        }
+    }
+    qsort(rec, (size_t)nd, sizeof(cellrec), cmp_cell);
+    size_t kcap = 1024, kn = 0;
+    uint64_t* keys = (uint64_t*)malloc(sizeof(uint64_t) * kcap);
+    int t;
+    for (t = 0; t < nd; t++) {
+        int a = rec[t].idx;
+        int dx, dy, dz;
+        for (dx = -1; dx <= 1; dx++)
+            for (dy = -1; dy <= 1; dy++)
+                for (dz = -1; dz <= 1; dz++) {
+                    int64_t x = rec[t].cx + dx, y = rec[t].cy + dy, z = rec[t].cz + dz;
+                    int s = find_cell(rec, nd, x, y, z);
+                    for (; s < nd && rec[s].cx == x && rec[s].cy == y && rec[s].cz == z; s++) {
+                        int b = rec[s].idx;
+                        if (b <= a) continue;
+                        if (overlap(&aabbs[a], &aabbs[b])) {
+                            if (kn == kcap) { kcap *= 2; keys = (uint64_t*)realloc(keys, sizeof(uint64_t) * kcap); }
+                            keys[kn++] = ((uint64_t)(uint32_t)a << 32) | (uint32_t)b;
+                        }
+                    }
+                }
+        {
+            int l;
+            for (l = 0; l < ns; l++) {
+                int s2 = statics[l];
+                if (overlap(&aabbs[a], &aabbs[s2])) {
+                    int lo = a < s2 ? a : s2, hi = a < s2 ? s2 : a;
+                    if (kn == kcap) { kcap *= 2; keys = (uint64_t*)realloc(keys, sizeof(uint64_t) * kcap); }
+                    keys[kn++] = ((uint64_t)(uint32_t)lo << 32) | (uint32_t)hi;
+                }
+            }
+        }
+    }
+    qsort(keys, kn, sizeof(uint64_t), cmp_u64);
+    {
+        size_t k;
+        for (k = 0; k < kn && (int)k < cap; k++) {
+            out[k].x = (int)(keys[k] >> 32);
+            out[k].y = (int)(keys[k] & 0xffffffffu);
+            out[k].z = -1;
+            out[k].w = -1;
+        }
+    }
+    free(keys);
+    free(rec);
+    free(statics);
+    return (int)kn;
+}
+
+/* ------------------------------------------------------------------ contacts */
+static int sgn_index(const obody* bodies, int i) { return bodies[i].invMass == 0.f ? -i : i; }
+
+static void write_header(ocontact* c, const obody* bodies, int A, int B, v3 n, int np, unsigned short fr) {
+    c->worldNormalOnB.x = n.x; c->worldNormalOnB.y = n.y; c->worldNormalOnB.z = n.z; c->worldNormalOnB.w = (float)np;
+    c->restitutionCmp = 0;
+    c->frictionCmp = fr;
+    c->batchIdx = 0;
+    c->bodyA = sgn_index(bodies, A);
+    c->bodyB = sgn_index(bodies, B);
+    c->childIndexA = -1;
+    c->childIndexB = -1;
+    c->unused1 = 0;
+    c->unused2 = 0;
+}
+
+typedef struct { float x, y, z, w; } p4;
+
+/* b3ReduceContacts (Bullet3Collision/NarrowPhaseCollision/shared/b3ReduceContacts.h:4-87) and its
+ * twin extractManifoldSequentialGlobal (b3ConvexHullContact.cpp:418-500) */
+static int reduce_contacts(const p4* p, int n, v3 nearNormal, int idx[4]) {
+    float cx = 0.f, cy = 0.f, cz = 0.f, inv, minW = FLT_MAX, m0 = FLT_MIN, m1 = FLT_MIN, m2 = FLT_MIN, m3v = FLT_MIN;
+    int i, ie, minIndex = -1;
+    v3 center, aVector, u, v, nu, nv;
+    idx[0] = 0; idx[1] = 1; idx[2] = 2; idx[3] = 3;
+    if (n == 0) return 0;
+    if (n <= 4) return n;
+    if (n > 64) n = 64;
+    for (i = 0; i < n; i++) {
+        cx = cx + p[i].x;
+        cy = cy + p[i].y;
+        cz = cz + p[i].z;
+    }
+    inv = 1.0f / (float)n;
+    cx = cx * inv; cy = cy * inv; cz = cz * inv;
+    center = mk(cx, cy, cz);
+    aVector = sub(mk(p[0].x, p[0].y, p[0].z), center);
+    u = cross(nearNormal, aVector);
+    v = cross(nearNormal, u);
+    u = nrm(u);
+    v = nrm(v);
+    nu = neg(u);
+    nv = neg(v);
+    for (ie = 0; ie < n; ie++) {
+        v3 r;
+        float f;
+        if (p[ie].w < minW) { minW = p[ie].w; minIndex = ie; }
+        r = sub(mk(p[ie].x, p[ie].y, p[ie].z), center);
+        f = dot(u, r); if (f < m0) { m0 = f; idx[0] = ie; }
+        f = dot(nu, r); if (f < m1) { m1 = f; idx[1] = ie; }
+        f = dot(v, r); if (f < m2) { m2 = f; idx[2] = ie; }
+        f = dot(nv, r); if (f < m3v) { m3v = f; idx[3] = ie; }
+    }
+    if (idx[0] != minIndex && idx[1] != minIndex && idx[2] != minIndex && idx[3] != minIndex) idx[0] = minIndex;
+    return 4;
+}
+
+/* computeContactPlaneConvex (Bullet3OpenCL/NarrowphaseCollision/b3ConvexHullContact.cpp:1272-1395);
+ * A = plane body, B = hull body */
+static int plane_hull(const obody* bodies, const oshapes* sh, int A, int B, ocontact* c, unsigned short fr) {
+    const obody* BA = &bodies[A];
+    const obody* BB = &bodies[B];
+    const ohull* hull = &sh->hulls[sh->cols[BB->collidableIdx].shapeIndex];
+    v3 posB = f4v(BB->pos), posA = f4v(BA->pos);
+    of4 pe = sh->faces[sh->cols[BA->collidableIdx].shapeIndex].plane;
+    v3 planeNormal = mk(pe.x, pe.y, pe.z);
+    float planeConstant = pe.w, maxDot = -1e30f;
+    m3 RA = qmat(f4q(BA->quat)), RB = qmat(f4q(BB->quat));
+    v3 planeNormalWorld = mmul(&RA, planeNormal);
+    v3 planeNormalInConvex = mtmul(&RB, mmul(&RA, neg(planeNormal)));
+    p4 pts[64];
+    int numPoints = 0, i, idx[4], nred;
+    for (i = 0; i < hull->numVertices; i++) {
+        v3 vtx = f4v(sh->verts[hull->vertexOffset + i]);
+        float curDot = dot(vtx, planeNormalInConvex);
+        if (curDot > maxDot) {
+            maxDot = curDot;
+            if (numPoints == 64) numPoints--;
+        }
+        if (numPoints < 64) {
+            v3 vtxWorld = add(mmul(&RB, vtx), posB);
+            v3 vtxInPlane = mtmul(&RA, sub(vtxWorld, posA));
+            float dist = dot(planeNormal, vtxInPlane) - planeConstant;
+            if (dist < 0.f) {
+                pts[numPoints].x = vtxWorld.x; pts[numPoints].y = vtxWorld.y; pts[numPoints].z = vtxWorld.z;
+                pts[numPoints].w = dist;
+                numPoints++;
+            }
+        }
+    }
+    nred = reduce_contacts(pts, numPoints, planeNormalInConvex, idx);
+    if (nred > 0) {
+        write_header(c, bodies, A, B, neg(planeNormalWorld), nred, fr);
+        for (i = 0; i < nred; i++) {
+            p4 q = pts[idx[i]];
+            c->worldPosB[i].x = q.x; c->worldPosB[i].y = q.y; c->worldPosB[i].z = q.z; c->worldPosB[i].w = q.w;
+        }
+        return 1;
+    }
+    return 0;
+}
+
+/* computeContactPlaneSphere (Bullet3OpenCL/NarrowphaseCollision/kernels/primitiveContacts.cl:729-790);
+ * A = plane, B = sphere.  The .cl has no CPU twin; this is the restatement. */
+static int plane_sphere(const obody* bodies, const oshapes* sh, int A, int B, ocontact* c, unsigned short fr) {
+    const obody* BA = &bodies[A];
+    const obody* BB = &bodies[B];
+    of4 pe = sh->faces[sh->cols[BA->collidableIdx].shapeIndex].plane;
+    float radius = sh->cols[BB->collidableIdx].radius;
+    v3 posA = f4v(BA->pos), posB = f4v(BB->pos);
+    v3 n = mk(pe.x, pe.y, pe.z);
+    float planeConstant = pe.w, distance;
+    m3 RA = qmat(f4q(BA->quat)), RB = qmat(f4q(BB->quat));
+    v3 vtx1 = scl(mtmul(&RB, mmul(&RA, neg(n))), radius);
+    v3 vtxInPlane = mtmul(&RA, sub(add(mmul(&RB, vtx1), posB), posA));
+    distance = dot(n, vtxInPlane) - planeConstant;
+    if (distance < 0.f) {
+        v3 projected = sub(vtxInPlane, lscl(distance, n));
+        v3 world = add(mmul(&RA, projected), posA);
+        v3 nB = mmul(&RA, n);
+        v3 pOnB = add(world, scl(nB, distance));
+        write_header(c, bodies, A, B, neg(nB), 1, fr);
+        c->worldPosB[0].x = pOnB.x; c->worldPosB[0].y = pOnB.y; c->worldPosB[0].z = pOnB.z; c->worldPosB[0].w = distance;
+        return 1;
+    }
+    return 0;
+}
+
+/* IsPointInPolygon (b3ConvexHullContact.cpp:362-411) */
+static int point_in_polygon(v3 p, const oface* face, const of4* base, const int* indices, v3* out) {
+    v3 plane = mk(face->plane.x, face->plane.y, face->plane.z), a, b;
+    int i;
+    if (face->numIndices < 2) return 0;
+    b = f4v(base[indices[face->indexOffset + face->numIndices - 1]]);
+    for (i = 0; i < face->numIndices; i++) {
+        v3 ab, ap, v;
+        a = b;
+        b = f4v(base[indices[face->indexOffset + i]]);
+        ab = sub(b, a);
+        ap = sub(p, a);
+        v = cross(ab, plane);
+        if (dot(ap, v) > 0.f) {
+            float ab_m2 = dot(ab, ab);
+            float rt = ab_m2 != 0.f ? dot(ab, ap) / ab_m2 : 0.f;
+            if (rt <= 0.f) *out = a;
+            else if (rt >= 1.f) *out = b;
+            else {
+                float s = 1.f - rt;
+                *out = mk(s * a.x + rt * b.x, s * a.y + rt * b.y, s * a.z + rt * b.z);
+            }
+            return 0;
+        }
+    }
+    return 1;
+}
+
+/* computeContactSphereConvex (b3ConvexHullContact.cpp:2323-2470); A = sphere, B = hull */
+static int sphere_hull(const obody* bodies, const oshapes* sh, int A, int B, ocontact* c, unsigned short fr) {
+    const obody* BA = &bodies[A];
+    const obody* BB = &bodies[B];
+    float radius = sh->cols[BA->collidableIdx].radius, minDist = -1000000.f;
+    v3 pos = f4v(BB->pos);
+    m3 R = qmat(f4q(BB->quat));
+    v3 spherePos = mtmul(&R, sub(f4v(BA->pos), pos));
+    const ohull* hull = &sh->hulls[sh->cols[BB->collidableIdx].shapeIndex];
+    v3 closest = mk(0, 0, 0), localHitNormal = mk(0, 0, 0);
+    int bCollide = 1, f;
+    const of4* base = &sh->verts[hull->vertexOffset];
+    for (f = 0; f < hull->numFaces; f++) {
+        const oface* face = &sh->faces[hull->faceOffset + f];
+        v3 n = mk(face->plane.x, face->plane.y, face->plane.z);
+        float dist = dot(n, spherePos) + face->plane.w;
+        v3 pntReturn = sub(spherePos, lscl(dist, n));
+        if (dist > radius) { bCollide = 0; break; }
+        if (dist > 0.f) {
+            v3 out;
+            if (point_in_polygon(spherePos, face, base, sh->indices, &out)) {
+                if (dist > minDist) { minDist = dist; closest = pntReturn; localHitNormal = n; }
+            } else {
+                v3 tmp = sub(spherePos, out);
+                float l2 = dot(tmp, tmp);
+                if (l2 < radius * radius) {
+                    dist = sqrtf(l2);
+                    if (dist > minDist) {
+                        minDist = dist;
+                        closest = out;
+                        localHitNormal = mk(tmp.x / dist, tmp.y / dist, tmp.z / dist);
+                    }
+                } else { bCollide = 0; break; }
+            }
+        } else {
+            if (dist > minDist) { minDist = dist; closest = pntReturn; localHitNormal = n; }
+        }
+    }
+    if (bCollide && minDist > -10000.f) {
+        v3 nB = mmul(&R, localHitNormal);
+        v3 pOnB = add(mmul(&R, closest), pos);
+        float actualDepth = minDist - radius;
+        if (actualDepth < 0.f) {
+            write_header(c, bodies, A, B, nB, 1, fr);
+            c->worldPosB[0].x = pOnB.x; c->worldPosB[0].y = pOnB.y; c->worldPosB[0].z = pOnB.z;
+            c->worldPosB[0].w = actualDepth;
+            return 1;
+        }
+    }
+    return 0;
+}
+
+/* sphere-sphere branch of primitiveContactsKernel (primitiveContacts.cl:926-972) */
+static int sphere_sphere(const obody* bodies, const oshapes* sh, int A, int B, ocontact* c, unsigned short fr) {
+    float rA = sh->cols[bodies[A].collidableIdx].radius, rB = sh->cols[bodies[B].collidableIdx].radius;
+    v3 diff = sub(f4v(bodies[A].pos), f4v(bodies[B].pos));
+    float len = sqrtf(dot(diff, diff));
+    if (len <= (rA + rB)) {
+        float dist = len - (rA + rB);
+        v3 n = mk(1.f, 0.f, 0.f), cp;
+        if (len > 0.00001f) n = mk(diff.x / len, diff.y / len, diff.z / len);
+        cp = add(f4v(bodies[B].pos), scl(n, rB));
+        write_header(c, bodies, A, B, n, 1, fr);
+        c->worldPosB[0].x = cp.x; c->worldPosB[0].y = cp.y; c->worldPosB[0].z = cp.z; c->worldPosB[0].w = dist;
+        return 1;
+    }
+    return 0;
+}
+
+/* b3ProjectAxis (Bullet3Collision/NarrowPhaseCollision/shared/b3FindSeparatingAxis.h:4-33) */
+static void project(const of4* verts, int nv, v3 pos, const m3* R, v3 dir, float* mn, float* mx) {
+    v3 localDir = mtmul(R, dir);
+    float offset = dot(pos, dir);
+    int i;
+    *mn = FLT_MAX;
+    *mx = -FLT_MAX;
+    for (i = 0; i < nv; i++) {
+        float dp = dot(f4v(verts[i]), localDir);
+        if (dp < *mn) *mn = dp;
+        if (dp > *mx) *mx = dp;
+    }
+    if (*mn > *mx) { float t = *mn; *mn = *mx; *mx = t; }
+    *mn = *mn + offset;
+    *mx = *mx + offset;
+}
+
+/* b3TestSepAxis (b3FindSeparatingAxis.h:35-53) */
+static int test_sep_axis(const ohull* hA, const ohull* hB, v3 posA, const m3* RA, v3 posB, const m3* RB, v3 axis,
+                         const of4* verts, float* depth) {
+    float min0, max0, min1, max1, d0, d1;
+    project(&verts[hA->vertexOffset], hA->numVertices, posA, RA, axis, &min0, &max0);
+    project(&verts[hB->vertexOffset], hB->numVertices, posB, RB, axis, &min1, &max1);
+    if (max0 < min1 || max1 < min0) return 0;
+    d0 = max0 - min1;
+    d1 = max1 - min0;
+    *depth = d0 < d1 ? d0 : d1;
+    return 1;
+}
+
+/* b3FindSeparatingAxis (b3FindSeparatingAxis.h:55-195): face normals of A, of B, exact edge-edge */
+static int find_separating_axis(const ohull* hA, const ohull* hB, v3 posA, const m3* RA, v3 posB, const m3* RB,
+                                const oshapes* sh, v3* sep) {
+    v3 c0 = add(mmul(RA, f4v(hA->localCenter)), posA);
+    v3 c1 = add(mmul(RB, f4v(hB->localCenter)), posB);
+    v3 deltaC2 = sub(c0, c1);
+    float dmin = FLT_MAX, d;
+    int i, e0, e1;
+    for (i = 0; i < hA->numFaces; i++) {
+        v3 n = mmul(RA, f4v(sh->faces[hA->faceOffset + i].plane));
+        if (dot(deltaC2, n) < 0.f) n = neg(n);
+        if (!test_sep_axis(hA, hB, posA, RA, posB, RB, n, sh->verts, &d)) return 0;
+        if (d < dmin) { dmin = d; *sep = n; }
+    }
+    for (i = 0; i < hB->numFaces; i++) {
+        v3 n = mmul(RB, f4v(sh->faces[hB->faceOffset + i].plane));
+        if (dot(deltaC2, n) < 0.f) n = neg(n);
+        if (!test_sep_axis(hA, hB, posA, RA, posB, RB, n, sh->verts, &d)) return 0;
+        if (d < dmin) { dmin = d; *sep = n; }
+    }
+    for (e0 = 0; e0 < hA->numUniqueEdges; e0++) {
+        v3 w0 = mmul(RA, f4v(sh->edges[hA->uniqueEdgesOffset + e0]));
+        for (e1 = 0; e1 < hB->numUniqueEdges; e1++) {
+            v3 w1 = mmul(RB, f4v(sh->edges[hB->uniqueEdgesOffset + e1]));
+            v3 cr = cross(w0, w1);
+            /* b3IsAlmostZero compares against the double constant 1e-6 */
+            if ((double)fabsf(cr.x) > 1e-6 || (double)fabsf(cr.y) > 1e-6 || (double)fabsf(cr.z) > 1e-6) {
+                cr = nrm(cr);
+                if (dot(deltaC2, cr) < 0.f) cr = neg(cr);
+                if (!test_sep_axis(hA, hB, posA, RA, posB, RB, cr, sh->verts, &d)) return 0;
+                if (d < dmin) { dmin = d; *sep = cr; }
+            }
+        }
+    }
+    if (dmin == FLT_MAX) return 0;
+    if (dot(neg(deltaC2), *sep) > 0.0f) *sep = neg(*sep);
+    return 1;
+}
+
+#define CLIP_CAP 64
+/* b3ClipFace (b3ContactConvexConvexSAT.h:20-63) */
+static int clip_face(const p4* in, int nin, v3 n, float eq, p4* out) {
+    int nout = 0, ve;
+    p4 first;
+    float ds;
+    if (nin < 2) return 0;
+    first = in[nin - 1];
+    ds = dot(n, mk(first.x, first.y, first.z)) + eq;
+    for (ve = 0; ve < nin; ve++) {
+        p4 end = in[ve];
+        float de = dot(n, mk(end.x, end.y, end.z)) + eq;
+        if (ds < 0.f) {
+            if (de < 0.f) {
+                if (nout < CLIP_CAP) out[nout++] = end;
+            } else {
+                float t = ds * 1.f / (ds - de);
+                p4 l = {first.x + (end.x - first.x) * t, first.y + (end.y - first.y) * t,
+                        first.z + (end.z - first.z) * t, 0.f};
+                if (nout < CLIP_CAP) out[nout++] = l;
+            }
+        } else {
+            if (de < 0.f) {
+                float t = ds * 1.f / (ds - de);
+                p4 l = {first.x + (end.x - first.x) * t, first.y + (end.y - first.y) * t,
+                        first.z + (end.z - first.z) * t, 0.f};
+                if (nout < CLIP_CAP) out[nout++] = l;
+                if (nout < CLIP_CAP) out[nout++] = end;
+            }
+        }
+        first = end;
+        ds = de;
+    }
+    return nout;
+}
+
+/* b3ContactConvexConvexSAT (b3ContactConvexConvexSAT.h:403-486) -> b3ClipHullHullSingle (:262-401)
+ * -> b3ClipHullAgainstHull (:169-260) -> b3ClipFaceAgainstHull (:65-167), minDist -1, maxDist 0 */
+static int hull_hull(const obody* bodies, const oshapes* sh, int A, int B, ocontact* c, unsigned short fr) {
+    const obody* BA = &bodies[A];
+    const obody* BB = &bodies[B];
+    const ohull* hA = &sh->hulls[sh->cols[BA->collidableIdx].shapeIndex];
+    const ohull* hB = &sh->hulls[sh->cols[BB->collidableIdx].shapeIndex];
+    v3 posA = f4v(BA->pos), posB = f4v(BB->pos), sep, planeNormalA, worldPlaneAnormal1;
+    m3 RA = qmat(f4q(BA->quat)), RB = qmat(f4q(BB->quat));
+    p4 buf0[CLIP_CAP], buf1[CLIP_CAP];
+    p4 *pin = buf0, *pout = buf1;
+    int fb = -1, fa = -1, f, nin = 0, e, e0, nva, ncont = 0, i;
+    float dmax = -FLT_MAX, dmn = FLT_MAX, planeEqWS;
+    const of4* vA = &sh->verts[hA->vertexOffset];
+    const of4* vB = &sh->verts[hB->vertexOffset];
+    const oface *polyA, *polyB;
+    if (!find_separating_axis(hA, hB, posA, &RA, posB, &RB, sh, &sep)) return 0;
+    for (f = 0; f < hB->numFaces; f++) {
+        float d = dot(mmul(&RB, f4v(sh->faces[hB->faceOffset + f].plane)), sep);
+        if (d > dmax) { dmax = d; fb = f; }
+    }
+    for (f = 0; f < hA->numFaces; f++) {
+        float d = dot(mmul(&RA, f4v(sh->faces[hA->faceOffset + f].plane)), sep);
+        if (d < dmn) { dmn = d; fa = f; }
+    }
+    if (fb < 0 || fa < 0) return 0;
+    polyB = &sh->faces[hB->faceOffset + fb];
+    for (e = 0; e < polyB->numIndices && e < CLIP_CAP; e++) {
+        v3 w = add(mmul(&RB, f4v(vB[sh->indices[polyB->indexOffset + e]])), posB);
+        pin[nin].x = w.x; pin[nin].y = w.y; pin[nin].z = w.z; pin[nin].w = 0.f;
+        nin++;
+    }
+    polyA = &sh->faces[hA->faceOffset + fa];
+    planeNormalA = mk(polyA->plane.x, polyA->plane.y, polyA->plane.z);
+    worldPlaneAnormal1 = mmul(&RA, planeNormalA);
+    nva = polyA->numIndices;
+    for (e0 = 0; e0 < nva; e0++) {
+        v3 va = f4v(vA[sh->indices[polyA->indexOffset + e0]]);
+        v3 vb = f4v(vA[sh->indices[polyA->indexOffset + ((e0 + 1) % nva)]]);
+        v3 worldEdge0 = mmul(&RA, sub(va, vb));
+        v3 planeNormalWS1 = neg(cross(worldEdge0, worldPlaneAnormal1));
+        v3 worldA1 = add(mmul(&RA, va), posA);
+        float planeEqWS1 = -dot(worldA1, planeNormalWS1);
+        int nout = clip_face(pin, nin, planeNormalWS1, planeEqWS1, pout);
+        p4* tmp = pout; pout = pin; pin = tmp;
+        nin = nout;
+    }
+    planeEqWS = polyA->plane.w - dot(worldPlaneAnormal1, posA);
+    for (i = 0; i < nin; i++) {
+        float depth = dot(worldPlaneAnormal1, mk(pin[i].x, pin[i].y, pin[i].z)) + planeEqWS;
+        if (depth <= -1.0f) depth = -1.0f;
+        if (depth <= 0.0f) {
+            pout[ncont].x = pin[i].x; pout[ncont].y = pin[i].y; pout[ncont].z = pin[i].z; pout[ncont].w = depth;
+            ncont++;
+        }
+    }
+    if (ncont > 0) {
+        int idx[4], np = reduce_contacts(pout, ncont, sep, idx), q;
+        write_header(c, bodies, A, B, sep, np, fr);
+        for (q = 0; q < np; q++) {
+            p4 v = pout[idx[q]];
+            c->worldPosB[q].x = v.x; c->worldPosB[q].y = v.y; c->worldPosB[q].z = v.z; c->worldPosB[q].w = v.w;
+        }
+        return 1;
+    }
+    return 0;
+}
+
+static int pair_contact(const obody* bodies, const oshapes* sh, int A, int B, ocontact* c, unsigned short fr) {
+    int ta = sh->cols[bodies[A].collidableIdx].shapeType, tb = sh->cols[bodies[B].collidableIdx].shapeType;
+    memset(c, 0, sizeof(*c));
+    /* dispatch as in computeConvexConvexContactsGPUSAT (b3ConvexHullContact.cpp:2655-2735) */
+    if (ta == SHAPE_CONVEX_HULL && tb == SHAPE_CONVEX_HULL) return hull_hull(bodies, sh, A, B, c, fr);
+    if (ta == SHAPE_PLANE && tb == SHAPE_CONVEX_HULL) return plane_hull(bodies, sh, A, B, c, fr);
+    if (tb == SHAPE_PLANE && ta == SHAPE_CONVEX_HULL) return plane_hull(bodies, sh, B, A, c, fr);
+    if (ta == SHAPE_SPHERE && tb == SHAPE_CONVEX_HULL) return sphere_hull(bodies, sh, A, B, c, fr);
+    if (tb == SHAPE_SPHERE && ta == SHAPE_CONVEX_HULL) return sphere_hull(bodies, sh, B, A, c, fr);
+    if (ta == SHAPE_SPHERE && tb == SHAPE_SPHERE) return sphere_sphere(bodies, sh, A, B, c, fr);
+    if (ta == SHAPE_PLANE && tb == SHAPE_SPHERE) return plane_sphere(bodies, sh, A, B, c, fr);
+    if (tb == SHAPE_PLANE && ta == SHAPE_SPHERE) return plane_sphere(bodies, sh, B, A, c, fr);
+    return 0;
+}
+
+int oracle_contacts(const obody* bodies, const oshapes* sh, opair* pairs, int npairs, ocontact* out, int cap,
+                    unsigned short friction_cmp) {
+    ocontact* tmp = (ocontact*)malloc(sizeof(ocontact) * (size_t)(npairs > 0 ? npairs : 1));
+    char* has = (char*)malloc((size_t)(npairs > 0 ? npairs : 1));
+    int p, n = 0;
+#pragma omp parallel for num_threads(g_threads) schedule(dynamic, 256)
+    for (p = 0; p < npairs; p++) has[p] = (char)pair_contact(bodies, sh, pairs[p].x, pairs[p].y, &tmp[p], friction_cmp);
+    for (p = 0; p < npairs; p++) {
+        if (has[p]) {
+            if (n < cap) out[n] = tmp[p];
+            pairs[p].z = n;
+            n++;
+        } else {
+            pairs[p].z = -1;
+        }
+    }
+    free(tmp);
+    free(has);
+    return n;
+}
+
+/* ------------------------------------------------------------------ solver */
+typedef struct {
+    v3 n;
+    float jac, rhs, applied, fric;
+    v3 r1xn, r2xn, angA, angB;
+} orow;
+
+typedef struct {
+    int A, B, mask;
+    float imA, imB;
+    orow rows[12]; /* 4 contact rows, then per point (dir2, dir1) friction rows */
+} omanifold;
+
+/* b3PlaneSpace1 (Bullet3Common/b3Vector3.h:1184-1212) */
+static void plane_space(v3 n, v3* p, v3* q) {
+    if (fabsf(n.z) > 0.7071067811865475244008443621048490f) {
+        float a = n.y * n.y + n.z * n.z, k = 1.0f / sqrtf(a);
+        *p = mk(0.f, -n.z * k, n.y * k);
+        *q = mk(a * k, -n.x * p->z, n.x * p->y);
+    } else {
+        float a = n.x * n.x + n.y * n.y, k = 1.0f / sqrtf(a);
+        *p = mk(-n.y * k, n.x * k, 0.f);
+        *q = mk(-n.z * p->y, n.z * p->x, a * k);
+    }
+}
+
+/* convertContact + setupContactConstraint + setupFrictionConstraint
+ * (Bullet3Dynamics/ConstraintSolver/b3PgsJacobiSolver.cpp:457-536, :654-804, :847-983) */
+static void setup_manifold(const obody* bodies, const oinertia* inertias, const ocontact* c, const int* counts,
+                           int pgs, float dt, float erp, float threshold, omanifold* M) {
+    int iA = abs(c->bodyA), iB = abs(c->bodyB), np = (int)c->worldNormalOnB.w, j, k;
+    const obody* A = &bodies[iA];
+    const obody* B = &bodies[iB];
+    float imA = A->invMass, imB = B->invMass, countA = 1.f, countB = 1.f, fric;
+    const omat3* IA = &inertias[iA].invInertiaWorld;
+    const omat3* IB = &inertias[iB].invInertiaWorld;
+    v3 posA = f4v(A->pos), posB = f4v(B->pos), linA = f4v(A->linVel), angA = f4v(A->angVel), linB = f4v(B->linVel),
+       angB = f4v(B->angVel), n;
+    memset(M, 0, sizeof(*M));
+    M->A = iA; M->B = iB; M->imA = imA; M->imB = imB;
+    if (np > 4) np = 4;
+    if (imA == 0.f && imB == 0.f) np = 0;
+    if (!pgs) {
+        if (imA != 0.f) countA = (float)counts[iA];
+        if (imB != 0.f) countB = (float)counts[iB];
+    }
+    n = nrm(mk(c->worldNormalOnB.x, c->worldNormalOnB.y, c->worldNormalOnB.z));
+    fric = (float)c->frictionCmp / (float)0xffff;
+    for (j = 0; j < np; j++) {
+        float dist = c->worldPosB[j].w;
+        v3 pos2, pos1, rel1, rel2;
+        if (!(dist <= threshold)) continue;
+        M->mask |= 1 << j;
+        pos2 = mk(c->worldPosB[j].x, c->worldPosB[j].y, c->worldPosB[j].z);
+        pos1 = add(pos2, scl(n, dist));
+        rel1 = sub(pos1, posA);
+        rel2 = sub(pos2, posB);
+        {
+            v3 torqueAxis0 = cross(rel1, n), angCompA = imul(IA, torqueAxis0);
+            v3 torqueAxis1 = cross(rel2, n), angCompB = imul(IB, neg(torqueAxis1));
+            float denom0 = imA + dot(n, cross(angCompA, rel1));
+            float denom1 = imB + dot(n, cross(neg(angCompB), rel2));
+            float jac = 1.0f / (denom0 + denom1);
+            float scaled = pgs ? jac : 1.0f / (denom0 * countA + denom1 * countB);
+            v3 r1xn = torqueAxis0, r2xn = neg(torqueAxis1);
+            float penetration = dist + 0.0f;
+            float vel1Dotn = dot(n, linA) + dot(r1xn, angA);
+            float vel2Dotn = -dot(n, linB) + dot(r2xn, angB);
+            float rel_vel = vel1Dotn + vel2Dotn;
+            float positionalError = 0.f, velocityError = 0.0f - rel_vel;
+            orow* r = &M->rows[j];
+            if (penetration > 0.f)
+                velocityError -= penetration / dt;
+            else
+                positionalError = -penetration * erp / dt;
+            r->n = n; r->jac = jac;
+            r->rhs = positionalError * scaled + velocityError * scaled;
+            r->applied = 0.f; r->fric = fric;
+            r->r1xn = r1xn; r->r2xn = r2xn; r->angA = angCompA; r->angB = angCompB;
+        }
+        {
+            v3 vel1 = add(linA, cross(angA, rel1)), vel2 = add(linB, cross(angB, rel2)), vel = sub(vel1, vel2);
+            float rel_vel = dot(n, vel), lat;
+            v3 dir1 = sub(vel, scl(n, rel_vel)), dir2, dirs[2];
+            lat = dot(dir1, dir1);
+            if (lat > FLT_EPSILON) {
+                float inv = 1.f / sqrtf(lat), l2;
+                dir1 = scl(dir1, inv);
+                dir2 = cross(dir1, n);
+                l2 = sqrtf(dot(dir2, dir2));
+                dir2 = scl(dir2, 1.f / l2);
+            } else {
+                plane_space(n, &dir1, &dir2);
+            }
+            dirs[0] = dir2;
+            dirs[1] = dir1;
+            for (k = 0; k < 2; k++) {
+                v3 d = dirs[k];
+                v3 r1xn = cross(rel1, d), angCompA = imul(IA, r1xn);
+                v3 r2xn = cross(rel2, neg(d)), angCompB = imul(IB, r2xn);
+                float denom0 = imA + dot(d, cross(angCompA, rel1));
+                float denom1 = imB + dot(d, cross(neg(angCompB), rel2));
+                float jac = 1.0f / (denom0 + denom1);
+                float scaled = pgs ? jac : 1.0f / (denom0 * countA + denom1 * countB);
+                float v1 = dot(d, linA) + dot(r1xn, angA);
+                float v2 = -dot(d, linB) + dot(r2xn, angB);
+                float rv = v1 + v2;
+                float velocityError = 0.0f - rv;
+                orow* r = &M->rows[4 + 2 * j + k];
+                r->n = d; r->jac = jac; r->rhs = velocityError * scaled; r->applied = 0.f; r->fric = fric;
+                r->r1xn = r1xn; r->r2xn = r2xn; r->angA = angCompA; r->angB = angCompB;
+            }
+        }
+    }
+}
+
+/* resolveSingleConstraintRowLowerLimit / Generic (b3PgsJacobiSolver.cpp:236-317) */
+static float solve_row(orow* r, float lower, float upper, int friction, v3* dlA, v3* daA, v3* dlB, v3* daB,
+                       float imA, float imB) {
+    float applied = r->applied, old = applied;
+    float deltaImpulse = r->rhs - applied * 0.0f;
+    float dv1 = dot(r->n, *dlA) + dot(r->r1xn, *daA);
+    float dv2 = -dot(r->n, *dlB) + dot(r->r2xn, *daB);
+    float sum;
+    deltaImpulse -= dv1 * r->jac;
+    deltaImpulse -= dv2 * r->jac;
+    sum = applied + deltaImpulse;
+    if (sum < lower) {
+        deltaImpulse = lower - applied;
+        applied = lower;
+    } else if (friction && sum > upper) {
+        deltaImpulse = upper - applied;
+        applied = upper;
+    } else {
+        applied = sum;
+    }
+    r->applied = applied;
+    *dlA = add(*dlA, scl(scl(r->n, imA), deltaImpulse));
+    *daA = add(*daA, scl(r->angA, deltaImpulse));
+    *dlB = add(*dlB, scl(scl(neg(r->n), imB), deltaImpulse));
+    *daB = add(*daB, scl(r->angB, deltaImpulse));
+    return applied - old;
+}
+
+static void solve_manifold(omanifold* M, int pass, v3* dlA, v3* daA, v3* dlB, v3* daB, double* rd, double* rl) {
+    int j, k;
+    if (pass == 0) {
+        for (j = 0; j < 4; j++) {
+            float d;
+            if (!(M->mask & (1 << j))) continue;
+            d = solve_row(&M->rows[j], 0.f, 1e10f, 0, dlA, daA, dlB, daB, M->imA, M->imB);
+            *rd += (double)d * d;
+            *rl += (double)M->rows[j].applied * M->rows[j].applied;
+        }
+    } else {
+        for (j = 0; j < 4; j++) {
+            float total;
+            if (!(M->mask & (1 << j))) continue;
+            total = M->rows[j].applied;
+            for (k = 0; k < 2; k++) {
+                orow* r = &M->rows[4 + 2 * j + k];
+                if (total > 0.f) {
+                    float fr = r->fric;
+                    float d = solve_row(r, -(fr * total), fr * total, 1, dlA, daA, dlB, daB, M->imA, M->imB);
+                    *rd += (double)d * d;
+                }
+                *rl += (double)r->applied * r->applied;
+            }
+        }
+    }
+}
+
+static void gather_impulses(const omanifold* Ms, int nc, float* out) {
+    int m, j;
+    if (!out) return;
+    for (m = 0; m < nc; m++)
+        for (j = 0; j < 4; j++) {
+            out[(size_t)m * 12 + 3 * j + 0] = Ms[m].rows[j].applied;
+            out[(size_t)m * 12 + 3 * j + 1] = Ms[m].rows[4 + 2 * j + 1].applied;
+            out[(size_t)m * 12 + 3 * j + 2] = Ms[m].rows[4 + 2 * j + 0].applied;
+        }
+}
+
+static int solve_pgs_impl(obody* bodies, const oinertia* inertias, int nbodies, const ocontact* contacts, int nc,
+                          const int* order, int iterations, float dt, float erp, float threshold, float tol,
+                          float* impulses_out, float* residual_out) {
+    omanifold* Ms = (omanifold*)malloc(sizeof(omanifold) * (size_t)(nc > 0 ? nc : 1));
+    v3* dl = (v3*)calloc((size_t)(nbodies > 0 ? nbodies : 1), sizeof(v3));
+    v3* da = (v3*)calloc((size_t)(nbodies > 0 ? nbodies : 1), sizeof(v3));
+    int m, it, pass, k, b, done = 0;
+    double r = 0.0;
+    for (m = 0; m < nc; m++) setup_manifold(bodies, inertias, &contacts[m], NULL, 1, dt, erp, threshold, &Ms[m]);
+    for (it = 0; it < iterations; it++) {
+        double rd = 0.0, rl = 0.0;
+        for (pass = 0; pass < 2; pass++)
+            for (k = 0; k < nc; k++) {
+                omanifold* M = &Ms[order ? order[k] : k];
+                v3 dlA = dl[M->A], daA = da[M->A], dlB = dl[M->B], daB = da[M->B];
+                if (!M->mask) continue;
+                solve_manifold(M, pass, &dlA, &daA, &dlB, &daB, &rd, &rl);
+                if (M->imA != 0.f) { dl[M->A] = dlA; da[M->A] = daA; }
+                if (M->imB != 0.f) { dl[M->B] = dlB; da[M->B] = daB; }
+            }
+        done = it + 1;
+        r = sqrt(rd) / fmax(sqrt(rl), 1e-12);
+        if (tol > 0.f && r <= (double)tol) break;
+    }
+    /* solveGroupCacheFriendlyFinish, PGS branch: v += dv */
+    for (b = 0; b < nbodies; b++) {
+        if (bodies[b].invMass == 0.f) continue;
+        bodies[b].linVel.x = bodies[b].linVel.x + dl[b].x;
+        bodies[b].linVel.y = bodies[b].linVel.y + dl[b].y;
+        bodies[b].linVel.z = bodies[b].linVel.z + dl[b].z;
+        bodies[b].angVel.x = bodies[b].angVel.x + da[b].x;
+        bodies[b].angVel.y = bodies[b].angVel.y + da[b].y;
+        bodies[b].angVel.z = bodies[b].angVel.z + da[b].z;
+    }
+    gather_impulses(Ms, nc, impulses_out);
+    if (residual_out) *residual_out = (float)r;
+    free(Ms); free(dl); free(da);
+    return done;
+}
+
+/* Jacobi (usePgs=false): split solver bodies per manifold, averaging after the contact and
+ * the friction sweep (solveSingleIteration :1389-1391, solveGroupCacheFriendlyIterations :1541-1546),
+ * summation in solver-body pool order (= manifold order, A before B), finish adds S/count once per
+ * split copy (:1654-1668). */
+static int solve_jacobi_impl(obody* bodies, const oinertia* inertias, int nbodies, const ocontact* contacts, int nc,
+                             int iterations, float dt, float erp, float threshold, float tol, float* impulses_out,
+                             float* residual_out) {
+    omanifold* Ms = (omanifold*)malloc(sizeof(omanifold) * (size_t)(nc > 0 ? nc : 1));
+    int* counts = (int*)calloc((size_t)(nbodies > 0 ? nbodies : 1), sizeof(int));
+    v3* avgl = (v3*)calloc((size_t)(nbodies > 0 ? nbodies : 1), sizeof(v3));
+    v3* avga = (v3*)calloc((size_t)(nbodies > 0 ? nbodies : 1), sizeof(v3));
+    v3* suml = (v3*)calloc((size_t)(nbodies > 0 ? nbodies : 1), sizeof(v3));
+    v3* suma = (v3*)calloc((size_t)(nbodies > 0 ? nbodies : 1), sizeof(v3));
+    v3* split = (v3*)calloc((size_t)(nc > 0 ? nc : 1) * 4, sizeof(v3));
+    int m, it, pass, b, done = 0, k;
+    double r = 0.0;
+    for (m = 0; m < nc; m++) {
+        int a = abs(contacts[m].bodyA), bb = abs(contacts[m].bodyB);
+        if (bodies[a].invMass != 0.f) counts[a]++;
+        if (bodies[bb].invMass != 0.f) counts[bb]++;
+    }
+    for (m = 0; m < nc; m++) setup_manifold(bodies, inertias, &contacts[m], counts, 0, dt, erp, threshold, &Ms[m]);
+    for (it = 0; it < iterations; it++) {
+        double rd = 0.0, rl = 0.0;
+        for (pass = 0; pass < 2; pass++) {
+            for (m = 0; m < nc; m++) {
+                omanifold* M = &Ms[m];
+                v3 z = mk(0, 0, 0), dlA = z, daA = z, dlB = z, daB = z;
+                if (M->imA != 0.f) { dlA = avgl[M->A]; daA = avga[M->A]; }
+                if (M->imB != 0.f) { dlB = avgl[M->B]; daB = avga[M->B]; }
+                if (M->mask) solve_manifold(M, pass, &dlA, &daA, &dlB, &daB, &rd, &rl);
+                split[4 * m + 0] = dlA; split[4 * m + 1] = daA; split[4 * m + 2] = dlB; split[4 * m + 3] = daB;
+            }
+            /* averageVelocities */
+            for (b = 0; b < nbodies; b++) { suml[b] = mk(0, 0, 0); suma[b] = mk(0, 0, 0); }
+            for (m = 0; m < nc; m++) {
+                omanifold* M = &Ms[m];
+                if (M->imA != 0.f) { suml[M->A] = add(suml[M->A], split[4 * m + 0]); suma[M->A] = add(suma[M->A], split[4 * m + 1]); }
+                if (M->imB != 0.f) { suml[M->B] = add(suml[M->B], split[4 * m + 2]); suma[M->B] = add(suma[M->B], split[4 * m + 3]); }
+            }
+            for (b = 0; b < nbodies; b++) {
+                if (counts[b] <= 0) continue;
+                {
+                    float f = 1.f / (float)counts[b];
+                    avgl[b] = scl(suml[b], f);
+                    avga[b] = scl(suma[b], f);
+                }
+            }
+        }
+        done = it + 1;
+        r = sqrt(rd) / fmax(sqrt(rl), 1e-12);
+        if (tol > 0.f && r <= (double)tol) break;
+    }
+    for (b = 0; b < nbodies; b++) {
+        float f;
+        v3 dl, da, lv, av;
+        if (counts[b] <= 0) continue;
+        f = 1.f / (float)counts[b];
+        dl = scl(suml[b], f);
+        da = scl(suma[b], f);
+        lv = f4v(bodies[b].linVel);
+        av = f4v(bodies[b].angVel);
+        for (k = 0; k < counts[b]; k++) { lv = add(lv, dl); av = add(av, da); }
+        bodies[b].linVel.x = lv.x; bodies[b].linVel.y = lv.y; bodies[b].linVel.z = lv.z;
+        bodies[b].angVel.x = av.x; bodies[b].angVel.y = av.y; bodies[b].angVel.z = av.z;
+    }
+    gather_impulses(Ms, nc, impulses_out);
+    if (residual_out) *residual_out = (float)r;
+    free(Ms); free(counts); free(avgl); free(avga); free(suml); free(suma); free(split);
+    return done;
+}
+
+int oracle_solve(obody* bodies, const oinertia* inertias, int nbodies, const ocontact* contacts, int ncontacts,
+                 int mode, int iterations, float dt, float erp, float threshold, float residual_tol,
+                 float* impulses_out, float* residual_out) {
+    if (mode == 1)
+        return solve_jacobi_impl(bodies, inertias, nbodies, contacts, ncontacts, iterations, dt, erp, threshold,
+                                 residual_tol, impulses_out, residual_out);
+    return solve_pgs_impl(bodies, inertias, nbodies, contacts, ncontacts, NULL, iterations, dt, erp, threshold,
+                          residual_tol, impulses_out, residual_out);
+}
+
+int oracle_solve_ordered(obody* bodies, const oinertia* inertias, int nbodies, const ocontact* contacts,
+                         int ncontacts, const int* order, int iterations, float dt, float erp, float threshold,
+                         float* impulses_out) {
+    return solve_pgs_impl(bodies, inertias, nbodies, contacts, ncontacts, order, iterations, dt, erp, threshold, 0.f,
+                          impulses_out, NULL);
+}
+
+/* ------------------------------------------------------------------ integrate */
+void oracle_integrate(obody* bodies, int n, float dt, float damping, const float g[3]) {
+    int i;
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (i = 0; i < n; i++) {
+        obody* b = &bodies[i];
+        const float threshold = 0.25f * 3.14159254f;
+        float fAngle, len;
+        v3 w, axis;
+        qt dorn, q;
+        if (b->invMass == 0.f) continue;
+        b->angVel.x *= damping;
+        b->angVel.y *= damping;
+        b->angVel.z *= damping;
+        w = mk(b->angVel.x, b->angVel.y, b->angVel.z);
+        fAngle = sqrtf(dot(w, w));
+        if (fAngle * dt > threshold) fAngle = threshold / dt;
+        if (fAngle < 0.001f)
+            axis = scl(w, (0.5f * dt - (dt * dt * dt) * 0.020833333333f * fAngle * fAngle));
+        else
+            axis = scl(w, (sinf(0.5f * fAngle * dt) / fAngle));
+        dorn.x = axis.x; dorn.y = axis.y; dorn.z = axis.z; dorn.w = cosf(fAngle * dt * 0.5f);
+        q = qmul(dorn, f4q(b->quat));
+        len = sqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
+        if (len > 0.f) {
+            float inv = 1.f / len;
+            q.x *= inv; q.y *= inv; q.z *= inv; q.w *= inv;
+        } else {
+            q.x = q.y = q.z = 0.f; q.w = 1.f;
+        }
+        b->quat.x = q.x; b->quat.y = q.y; b->quat.z = q.z; b->quat.w = q.w;
+        b->pos.x = b->pos.x + b->linVel.x * dt;
+        b->pos.y = b->pos.y + b->linVel.y * dt;
+        b->pos.z = b->pos.z + b->linVel.z * dt;
+        b->linVel.x = b->linVel.x + g[0] * dt;
+        b->linVel.y = b->linVel.y + g[1] * dt;
+        b->linVel.z = b->linVel.z + g[2] * dt;
+    }
+}
+
+/* ------------------------------------------------------------------ batching legality */
+int oracle_check_batches(const ocontact* contacts, int n, const int* color, const obody* bodies, int nbodies) {
+    int maxc = 0, m, bad = 0;
+    for (m = 0; m < n; m++) if (color[m] > maxc) maxc = color[m];
+    {
+        int* last = (int*)malloc(sizeof(int) * (size_t)(nbodies > 0 ? nbodies : 1));
+        int c;
+        for (c = 0; c <= maxc; c++) {
+            int b;
+            for (b = 0; b < nbodies; b++) last[b] = -1;
+            for (m = 0; m < n; m++) {
+                int a, bb;
+                if (color[m] != c) continue;
+                a = abs(contacts[m].bodyA);
+                bb = abs(contacts[m].bodyB);
+                if (bodies[a].invMass != 0.f) { if (last[a] >= 0) bad++; last[a] = m; }
+                if (bodies[bb].invMass != 0.f) { if (last[bb] >= 0) bad++; last[bb] = m; }
+            }
+        }
+        free(last);
+    }
+    for (m = 0; m < n; m++) if (color[m] < 0) bad++;
+    return bad;
+}
+
+/* ------------------------------------------------------------------ composed step */
+int oracle_step(obody* bodies, const oinertia* inertias, int n, const oshapes* sh, const ostep_params* p,
+                int* npairs_out, int* npoints_out) {
+    oaabb* aabbs = (oaabb*)malloc(sizeof(oaabb) * (size_t)(n > 0 ? n : 1));
+    int cap = 16 * n + 1024, np, nc, m, pts = 0;
+    opair* pairs;
+    ocontact* contacts;
+    oracle_aabbs(bodies, n, sh, aabbs);
+    pairs = (opair*)malloc(sizeof(opair) * (size_t)cap);
+    np = p->use_grid ? oracle_pairs_grid(aabbs, n, p->cell, pairs, cap) : oracle_pairs_bruteforce(aabbs, n, pairs, cap);
+    if (np > cap) np = cap;
+    contacts = (ocontact*)malloc(sizeof(ocontact) * (size_t)(np > 0 ? np : 1));
+    nc = oracle_contacts(bodies, sh, pairs, np, contacts, np, p->friction_cmp);
+    for (m = 0; m < nc; m++) pts += (int)contacts[m].worldNormalOnB.w;
+    oracle_solve(bodies, inertias, n, contacts, nc, p->mode, p->iterations, p->dt, p->erp, p->threshold,
+                 p->residual_tol, NULL, NULL);
+    oracle_integrate(bodies, n, p->dt, p->damping, p->gravity);
+    if (npairs_out) *npairs_out = np;
+    if (npoints_out) *npoints_out = pts;
+    free(aabbs);
+    free(pairs);
+    free(contacts);
+    return nc;
+}

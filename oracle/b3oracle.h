@@ -1,0 +1,109 @@
+/*
+ * b3oracle.h -- CPU oracle for the GPU rigid-body step.  TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference's CPU algorithms for this path (each function
+ * cites the reference file:line it follows).  Only the test-suite, the smoke check and
+ * the bench's CPU-baseline leg load it; the product library never links or calls it.
+ *
+ * Parity pin: the restatement is checked against outputs of the reference's own code,
+ * compiled in place from its sources (oracle/build_ref.sh -> oracle/_ref), and the
+ * resulting golden vectors are committed under tests/golden/.
+ *
+ * Arithmetic: compiled with -ffp-contract=off; every formula uses the same evaluation
+ * order as the CUDA kernels, so all stages except the integrator's sinf/cosf agree bit-for-bit.
+ * Layouts are byte-identical to the reference structs (b3RigidBodyData 80 B, b3InertiaData 96 B,
+ * b3Collidable 16 B, b3ConvexPolyhedronData 96 B, b3GpuFace 32 B, b3Aabb 32 B, b3Contact4Data 112 B).
+ */
+#ifndef B3ORACLE_H
+#define B3ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct { float x, y, z, w; } of4;
+typedef struct { of4 pos, quat, linVel, angVel; int collidableIdx; float invMass, restitution, friction; } obody;
+typedef struct { of4 row[3]; } omat3;
+typedef struct { omat3 invInertiaWorld, initInvInertia; } oinertia;
+typedef struct { int numChildShapes; float radius; int shapeType; int shapeIndex; } ocollidable;
+typedef struct {
+    of4 localCenter, extents, mC, mE;
+    float radius;
+    int faceOffset, numFaces, numVertices, vertexOffset, uniqueEdgesOffset, numUniqueEdges, unused;
+} ohull;
+typedef struct { of4 plane; int indexOffset, numIndices, pad0, pad1; } oface;
+typedef struct { float minv[3]; int minw; float maxv[3]; int maxw; } oaabb;
+typedef struct {
+    of4 worldPosB[4];
+    of4 worldNormalOnB;
+    unsigned short restitutionCmp, frictionCmp;
+    int batchIdx, bodyA, bodyB, childIndexA, childIndexB, unused1, unused2;
+} ocontact;
+typedef struct { int x, y, z, w; } opair;
+
+typedef struct {
+    const ocollidable* cols;
+    const oaabb* local_aabbs;
+    const ohull* hulls;
+    const oface* faces;
+    const int* indices;
+    const of4* verts;
+    const of4* edges;
+    int num_collidables;
+} oshapes;
+
+/* 1 = OpenMP threads available in this build */
+int oracle_num_threads(void);
+void oracle_set_threads(int n);
+
+/* b3TransformAabb2 (Bullet3Collision/BroadPhaseCollision/shared/b3Aabb.h:24-43), margin 0,
+ * min.w = body index, max.w = invMass != 0 */
+void oracle_aabbs(const obody* bodies, int n, const oshapes* sh, oaabb* out);
+
+/* Exact overlapping pairs (a < b, sorted) of the given AABBs, static-static excluded.
+ * brute force restates b3GpuGridBroadphase::calculateOverlappingPairsHost
+ * (src/Bullet3OpenCL/BroadphaseCollision/b3GpuGridBroadphase.cpp:260-294) with the inclusive
+ * test of gridBroadphase.cl:89-94; returns the pair count (may exceed cap; only cap written). */
+int oracle_pairs_bruteforce(const oaabb* aabbs, int n, opair* out, int cap);
+/* Same set through a sort-based uniform grid (cell >= every dynamic AABB extent) for large n. */
+int oracle_pairs_grid(const oaabb* aabbs, int n, float cell, opair* out, int cap);
+
+/* Contact manifolds for each pair in order (one manifold or none per pair); returns count,
+ * writes pair.z = manifold index or -1.  See b3oracle.c for the per-shape reference functions. */
+int oracle_contacts(const obody* bodies, const oshapes* sh, opair* pairs, int npairs, ocontact* out, int cap,
+                    unsigned short friction_cmp);
+
+/* b3PgsJacobiSolver::solveGroup (Bullet3Dynamics/ConstraintSolver/b3PgsJacobiSolver.cpp:170)
+ * with USE_2_FRICTION_DIRECTIONS, no warm start, no split impulse, erp, contact threshold.
+ * mode 0 = PGS (usePgs=true, sequential row order), 1 = Jacobi (mass splitting).
+ * impulses_out (optional): 12 floats per manifold: per point (normal, lateral1, lateral2).
+ * Returns the number of iterations run. residual_out (optional): last relative residual. */
+int oracle_solve(obody* bodies, const oinertia* inertias, int nbodies, const ocontact* contacts, int ncontacts,
+                 int mode, int iterations, float dt, float erp, float threshold, float residual_tol,
+                 float* impulses_out, float* residual_out);
+/* Solve in a given manifold order (PGS only): order[k] = manifold index solved k-th. */
+int oracle_solve_ordered(obody* bodies, const oinertia* inertias, int nbodies, const ocontact* contacts,
+                         int ncontacts, const int* order, int iterations, float dt, float erp, float threshold,
+                         float* impulses_out);
+
+/* integrateSingleTransform (Bullet3Dynamics/shared/b3IntegrateTransforms.h:5-55) for every body */
+void oracle_integrate(obody* bodies, int n, float dt, float damping, const float gravity[3]);
+
+/* Batch legality: no dynamic body appears twice within one colour.  Returns the number of
+ * violations (0 = legal); statics (invMass 0) never conflict. */
+int oracle_check_batches(const ocontact* contacts, int n, const int* color, const obody* bodies, int nbodies);
+
+/* One full step (AABB, pairs, contacts, solve, integrate); returns the manifold count. */
+typedef struct {
+    float dt, damping, gravity[3], erp, threshold, cell, residual_tol;
+    int mode, iterations, use_grid;
+    unsigned short friction_cmp;
+} ostep_params;
+int oracle_step(obody* bodies, const oinertia* inertias, int n, const oshapes* sh, const ostep_params* p,
+                int* npairs_out, int* npoints_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

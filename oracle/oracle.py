@@ -1,0 +1,264 @@
+"""ctypes wrappers of the CPU oracle (oracle/liboracle.so) and of the compiled reference
+(oracle/_ref/libb3ref.so).  TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and
+the bench's CPU-baseline leg; never by the product package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+
+BODY = np.dtype([("pos", "<f4", 4), ("quat", "<f4", 4), ("linVel", "<f4", 4), ("angVel", "<f4", 4),
+                 ("collidableIdx", "<i4"), ("invMass", "<f4"), ("restitution", "<f4"), ("friction", "<f4")])
+INERTIA = np.dtype([("invInertiaWorld", "<f4", (3, 4)), ("initInvInertia", "<f4", (3, 4))])
+COLLIDABLE = np.dtype([("numChildShapes", "<i4"), ("radius", "<f4"), ("shapeType", "<i4"), ("shapeIndex", "<i4")])
+HULL = np.dtype([("localCenter", "<f4", 4), ("extents", "<f4", 4), ("mC", "<f4", 4), ("mE", "<f4", 4),
+                 ("radius", "<f4"), ("faceOffset", "<i4"), ("numFaces", "<i4"), ("numVertices", "<i4"),
+                 ("vertexOffset", "<i4"), ("uniqueEdgesOffset", "<i4"), ("numUniqueEdges", "<i4"), ("unused", "<i4")])
+FACE = np.dtype([("plane", "<f4", 4), ("indexOffset", "<i4"), ("numIndices", "<i4"), ("pad", "<i4", 2)])
+AABB = np.dtype([("min", "<f4", 3), ("minw", "<i4"), ("max", "<f4", 3), ("maxw", "<i4")])
+CONTACT = np.dtype([("worldPosB", "<f4", (4, 4)), ("normal", "<f4", 4), ("restitutionCmp", "<u2"),
+                    ("frictionCmp", "<u2"), ("batchIdx", "<i4"), ("bodyA", "<i4"), ("bodyB", "<i4"),
+                    ("childA", "<i4"), ("childB", "<i4"), ("unused", "<i4", 2)])
+PAIR = np.dtype([("x", "<i4"), ("y", "<i4"), ("z", "<i4"), ("w", "<i4")])
+
+
+class OShapes(C.Structure):
+    _fields_ = [("cols", C.c_void_p), ("local_aabbs", C.c_void_p), ("hulls", C.c_void_p), ("faces", C.c_void_p),
+                ("indices", C.c_void_p), ("verts", C.c_void_p), ("edges", C.c_void_p), ("num_collidables", C.c_int)]
+
+
+class OStepParams(C.Structure):
+    _fields_ = [("dt", C.c_float), ("damping", C.c_float), ("gravity", C.c_float * 3), ("erp", C.c_float),
+                ("threshold", C.c_float), ("cell", C.c_float), ("residual_tol", C.c_float), ("mode", C.c_int),
+                ("iterations", C.c_int), ("use_grid", C.c_int), ("friction_cmp", C.c_ushort)]
+
+
+def _p(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else None
+
+
+_ORACLE = None
+_REF = None
+
+
+def load_oracle():
+    global _ORACLE
+    if _ORACLE is None:
+        p = HERE / "liboracle.so"
+        if not p.exists():
+            import sys
+            sys.path.insert(0, str(HERE.parent))
+            from bullet3_gb300 import _build
+            _build.build_oracle()
+        _ORACLE = C.CDLL(str(p))
+        _ORACLE.oracle_solve.restype = C.c_int
+    return _ORACLE
+
+
+def load_reference():
+    """The reference's own CPU code (only where its sources were available to build it)."""
+    global _REF
+    if _REF is None:
+        p = HERE / "_ref" / "libb3ref.so"
+        if not p.exists():
+            return None
+        _REF = C.CDLL(str(p))
+    return _REF
+
+
+class Shapes:
+    """Shape tables as numpy arrays (same layout the GPU library uses)."""
+
+    def __init__(self, collidables, local_aabbs, hulls, faces, indices, verts, edges):
+        self.collidables = np.ascontiguousarray(collidables, COLLIDABLE)
+        self.local_aabbs = np.ascontiguousarray(local_aabbs, AABB)
+        self.hulls = np.ascontiguousarray(hulls, HULL)
+        self.faces = np.ascontiguousarray(faces, FACE)
+        self.indices = np.ascontiguousarray(indices, np.int32)
+        self.verts = np.ascontiguousarray(verts, np.float32).reshape(-1, 4)
+        self.edges = np.ascontiguousarray(edges, np.float32).reshape(-1, 4)
+
+    @classmethod
+    def from_tables(cls, t: dict):
+        return cls(t["collidables"], t["local_aabbs"], t["hulls"], t["faces"], t["indices"], t["verts"], t["edges"])
+
+    def c(self) -> OShapes:
+        s = OShapes()
+        s.cols = self.collidables.ctypes.data
+        s.local_aabbs = self.local_aabbs.ctypes.data
+        s.hulls = self.hulls.ctypes.data
+        s.faces = self.faces.ctypes.data
+        s.indices = self.indices.ctypes.data
+        s.verts = self.verts.ctypes.data
+        s.edges = self.edges.ctypes.data
+        s.num_collidables = len(self.collidables)
+        return s
+
+
+def set_threads(n: int):
+    load_oracle().oracle_set_threads(C.c_int(n))
+
+
+def max_threads() -> int:
+    return int(load_oracle().oracle_num_threads())
+
+
+def aabbs(bodies, shapes: Shapes):
+    b = np.ascontiguousarray(bodies, BODY)
+    out = np.zeros(len(b), AABB)
+    sc = shapes.c()
+    load_oracle().oracle_aabbs(_p(b), C.c_int(len(b)), C.byref(sc), _p(out))
+    return out
+
+
+def pairs_bruteforce(aabbs_, cap=None):
+    a = np.ascontiguousarray(aabbs_, AABB)
+    cap = cap or max(1024, 64 * len(a))
+    out = np.zeros(cap, PAIR)
+    n = load_oracle().oracle_pairs_bruteforce(_p(a), C.c_int(len(a)), _p(out), C.c_int(cap))
+    return out[:min(n, cap)].copy()
+
+
+def pairs_grid(aabbs_, cell, cap=None):
+    a = np.ascontiguousarray(aabbs_, AABB)
+    cap = cap or max(1024, 64 * len(a))
+    out = np.zeros(cap, PAIR)
+    n = load_oracle().oracle_pairs_grid(_p(a), C.c_int(len(a)), C.c_float(cell), _p(out), C.c_int(cap))
+    return out[:min(n, cap)].copy()
+
+
+def contacts(bodies, shapes: Shapes, pairs, friction_cmp=45874):
+    b = np.ascontiguousarray(bodies, BODY)
+    pr = np.array(pairs, PAIR, copy=True)
+    out = np.zeros(max(1, len(pr)), CONTACT)
+    sc = shapes.c()
+    n = load_oracle().oracle_contacts(_p(b), C.byref(sc), _p(pr), C.c_int(len(pr)), _p(out), C.c_int(len(out)),
+                                      C.c_ushort(friction_cmp))
+    return out[:n].copy(), pr
+
+
+def solve(bodies, inertias, contacts_, mode=0, iterations=10, dt=1 / 60, erp=0.2, threshold=0.02, residual_tol=0.0):
+    """Returns (new bodies, impulses (nc,12), iterations run, residual)."""
+    b = np.array(bodies, BODY, copy=True)
+    I = np.ascontiguousarray(inertias, INERTIA)
+    c = np.ascontiguousarray(contacts_, CONTACT)
+    imp = np.zeros((max(1, len(c)), 12), np.float32)
+    res = C.c_float(0)
+    it = load_oracle().oracle_solve(_p(b), _p(I), C.c_int(len(b)), _p(c), C.c_int(len(c)), C.c_int(mode),
+                                    C.c_int(iterations), C.c_float(dt), C.c_float(erp), C.c_float(threshold),
+                                    C.c_float(residual_tol), _p(imp), C.byref(res))
+    return b, imp[:len(c)], it, res.value
+
+
+def solve_ordered(bodies, inertias, contacts_, order, iterations=10, dt=1 / 60, erp=0.2, threshold=0.02):
+    b = np.array(bodies, BODY, copy=True)
+    I = np.ascontiguousarray(inertias, INERTIA)
+    c = np.ascontiguousarray(contacts_, CONTACT)
+    o = np.ascontiguousarray(order, np.int32)
+    imp = np.zeros((max(1, len(c)), 12), np.float32)
+    load_oracle().oracle_solve_ordered(_p(b), _p(I), C.c_int(len(b)), _p(c), C.c_int(len(c)), _p(o),
+                                       C.c_int(iterations), C.c_float(dt), C.c_float(erp), C.c_float(threshold),
+                                       _p(imp))
+    return b, imp[:len(c)]
+
+
+def integrate(bodies, dt=1 / 60, damping=0.99, gravity=(0.0, -9.8, 0.0)):
+    b = np.array(bodies, BODY, copy=True)
+    g = (C.c_float * 3)(*gravity)
+    load_oracle().oracle_integrate(_p(b), C.c_int(len(b)), C.c_float(dt), C.c_float(damping), g)
+    return b
+
+
+def check_batches(contacts_, colors, bodies) -> int:
+    c = np.ascontiguousarray(contacts_, CONTACT)
+    col = np.ascontiguousarray(colors, np.int32)
+    b = np.ascontiguousarray(bodies, BODY)
+    return int(load_oracle().oracle_check_batches(_p(c), C.c_int(len(c)), _p(col), _p(b), C.c_int(len(b))))
+
+
+def step(bodies, inertias, shapes: Shapes, dt=1 / 60, mode=0, iterations=10, cell=0.0, use_grid=True,
+         gravity=(0.0, -9.8, 0.0), damping=0.99, residual_tol=0.0):
+    """One composed CPU step in place on a copy; returns (bodies, manifolds, pairs, points)."""
+    b = np.array(bodies, BODY, copy=True)
+    I = np.ascontiguousarray(inertias, INERTIA)
+    p = OStepParams()
+    p.dt, p.damping, p.erp, p.threshold, p.cell, p.residual_tol = dt, damping, 0.2, 0.02, cell, residual_tol
+    for i in range(3):
+        p.gravity[i] = gravity[i]
+    p.mode, p.iterations, p.use_grid, p.friction_cmp = mode, iterations, int(use_grid), 45874
+    npairs = C.c_int()
+    npts = C.c_int()
+    sc = shapes.c()
+    nc = load_oracle().oracle_step(_p(b), _p(I), C.c_int(len(b)), C.byref(sc), C.byref(p), C.byref(npairs),
+                                   C.byref(npts))
+    return b, nc, npairs.value, npts.value
+
+
+# ------------------------------------------------------------------ reference (compiled in place)
+def ref_hull(points):
+    lib = load_reference()
+    pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    cap = max(64, 8 * len(pts))
+    v = np.zeros((cap, 3), np.float32)
+    pl = np.zeros((cap, 4), np.float32)
+    fc = np.zeros(cap, np.int32)
+    ix = np.zeros(8 * cap, np.int32)
+    e = np.zeros((cap, 3), np.float32)
+    counts = np.array([cap, cap, 8 * cap, cap], np.int32)
+    r = lib.ref_hull(_p(pts), C.c_int(len(pts)), _p(v), _p(pl), _p(fc), _p(ix), _p(e), _p(counts))
+    assert r == 0
+    nv, nf, ni, ne = (int(x) for x in counts)
+    return v[:nv].copy(), pl[:nf].copy(), fc[:nf].copy(), ix[:ni].copy(), e[:ne].copy()
+
+
+def ref_aabbs(bodies, shapes: Shapes):
+    lib = load_reference()
+    b = np.ascontiguousarray(bodies, BODY)
+    out = np.zeros(len(b), AABB)
+    lib.ref_aabbs(_p(b), C.c_int(len(b)), _p(shapes.collidables), _p(shapes.local_aabbs), _p(out))
+    return out
+
+
+def ref_pairs_dbvt(aabbs_):
+    lib = load_reference()
+    a = np.ascontiguousarray(aabbs_, AABB)
+    cap = max(1024, 64 * len(a))
+    out = np.zeros((cap, 2), np.int32)
+    n = lib.ref_pairs_dbvt(_p(a), C.c_int(len(a)), _p(out), C.c_int(cap))
+    return out[:n].copy()
+
+
+def ref_contacts(bodies, shapes: Shapes, pairs_xy):
+    lib = load_reference()
+    b = np.ascontiguousarray(bodies, BODY)
+    pr = np.ascontiguousarray(pairs_xy, np.int32).reshape(-1, 2)
+    out = np.zeros(max(1, len(pr)), CONTACT)
+    pidx = np.zeros(max(1, len(pr)), np.int32)
+    n = lib.ref_contacts(_p(b), C.c_int(len(b)), _p(shapes.collidables), C.c_int(len(shapes.collidables)),
+                         _p(shapes.hulls), C.c_int(len(shapes.hulls)), _p(shapes.faces), C.c_int(len(shapes.faces)),
+                         _p(shapes.indices), C.c_int(len(shapes.indices)), _p(shapes.verts),
+                         C.c_int(len(shapes.verts)), _p(shapes.edges), C.c_int(len(shapes.edges)), _p(pr),
+                         C.c_int(len(pr)), _p(out), _p(pidx), C.c_int(len(out)))
+    return out[:n].copy(), pidx[:n].copy()
+
+
+def ref_solve(bodies, inertias, contacts_, use_pgs=True, iterations=10, dt=1 / 60):
+    lib = load_reference()
+    b = np.array(bodies, BODY, copy=True)
+    I = np.array(inertias, INERTIA, copy=True)
+    c = np.ascontiguousarray(contacts_, CONTACT)
+    lib.ref_solve(_p(b), _p(I), C.c_int(len(b)), _p(c), C.c_int(len(c)), C.c_int(int(use_pgs)), C.c_int(iterations),
+                  C.c_float(dt))
+    return b
+
+
+def ref_integrate(bodies, dt=1 / 60, damping=0.99, gravity=(0.0, -9.8, 0.0)):
+    lib = load_reference()
+    b = np.array(bodies, BODY, copy=True)
+    g = (C.c_float * 3)(*gravity)
+    lib.ref_integrate(_p(b), C.c_int(len(b)), C.c_float(dt), C.c_float(damping), g)
+    return b

@@ -1,0 +1,211 @@
+// ref_shim.cpp -- C entry points into the REFERENCE's own CPU code, compiled in place from the
+// reference sources by oracle/build_ref.sh into oracle/_ref/libb3ref.so.  TEST INFRASTRUCTURE
+// ONLY: it generates the golden vectors under tests/golden/ and pins the plain-C oracle
+// (oracle/b3oracle.c) to the reference; nothing in the product loads it.
+//
+// Functions wrapped (paths relative to the reference project's src/):
+//   b3ConvexUtility::initializePolyhedralFeatures   Bullet3Collision/NarrowPhaseCollision/b3ConvexUtility.cpp:26
+//   b3TransformAabb2                                Bullet3Collision/BroadPhaseCollision/shared/b3Aabb.h:24
+//   b3DynamicBvhBroadphase + b3TestAabbAgainstAabb  Bullet3Collision/BroadPhaseCollision/b3DynamicBvhBroadphase.cpp
+//   b3ContactConvexConvexSAT                        Bullet3Collision/NarrowPhaseCollision/shared/b3ContactConvexConvexSAT.h:403
+//   computeContactPlaneConvex / SphereConvex        Bullet3OpenCL/NarrowphaseCollision/b3ConvexHullContact.cpp:1272, :2323
+//   b3PgsJacobiSolver::solveGroup                   Bullet3Dynamics/ConstraintSolver/b3PgsJacobiSolver.cpp:170
+//   integrateSingleTransform                        Bullet3Dynamics/shared/b3IntegrateTransforms.h:5
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "Bullet3Common/b3AlignedObjectArray.h"
+#include "Bullet3Common/b3Vector3.h"
+#include "Bullet3Common/b3Quaternion.h"
+#include "Bullet3Common/b3Matrix3x3.h"
+#include "Bullet3Common/b3Transform.h"
+#include "Bullet3Common/shared/b3Int4.h"
+#include "Bullet3Collision/BroadPhaseCollision/shared/b3Aabb.h"
+#include "Bullet3Collision/BroadPhaseCollision/b3DynamicBvhBroadphase.h"
+#include "Bullet3Collision/NarrowPhaseCollision/b3ConvexUtility.h"
+#include "Bullet3Collision/NarrowPhaseCollision/b3Contact4.h"
+#include "Bullet3Collision/NarrowPhaseCollision/shared/b3RigidBodyData.h"
+#include "Bullet3Collision/NarrowPhaseCollision/shared/b3Collidable.h"
+#include "Bullet3Collision/NarrowPhaseCollision/shared/b3ConvexPolyhedronData.h"
+#include "Bullet3Collision/NarrowPhaseCollision/shared/b3ContactConvexConvexSAT.h"
+#include "Bullet3Dynamics/ConstraintSolver/b3PgsJacobiSolver.h"
+#include "Bullet3Dynamics/ConstraintSolver/b3ContactSolverInfo.h"
+#include "Bullet3Dynamics/shared/b3IntegrateTransforms.h"
+
+void computeContactPlaneConvex(int pairIndex, int bodyIndexA, int bodyIndexB, int collidableIndexA,
+                               int collidableIndexB, const b3RigidBodyData* rigidBodies,
+                               const b3Collidable* collidables, const b3ConvexPolyhedronData* convexShapes,
+                               const b3Vector3* convexVertices, const int* convexIndices, const b3GpuFace* faces,
+                               b3Contact4* globalContactsOut, int& nGlobalContactsOut, int maxContactCapacity);
+void computeContactSphereConvex(int pairIndex, int bodyIndexA, int bodyIndexB, int collidableIndexA,
+                                int collidableIndexB, const b3RigidBodyData* rigidBodies,
+                                const b3Collidable* collidables, const b3ConvexPolyhedronData* convexShapes,
+                                const b3Vector3* convexVertices, const int* convexIndices, const b3GpuFace* faces,
+                                b3Contact4* globalContactsOut, int& nGlobalContactsOut, int maxContactCapacity);
+
+extern "C" {
+
+// Hull tables from b3ConvexUtility (+ vertex-mean local centre as registerConvexHullShape sets it).
+// counts4 in: capacities (verts, faces, indices, edges); out: sizes.  Returns 0 on success.
+int ref_hull(const float* xyz, int n, float* verts_out, float* planes_out, int* face_counts_out, int* indices_out,
+             float* edges_out, int* counts4) {
+    b3AlignedObjectArray<b3Vector3> pts;
+    for (int i = 0; i < n; i++) pts.push_back(b3MakeVector3(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]));
+    b3ConvexUtility util;
+    util.initializePolyhedralFeatures(&pts[0], pts.size(), true);
+    int nv = util.m_vertices.size(), nf = util.m_faces.size(), ne = util.m_uniqueEdges.size(), ni = 0;
+    for (int f = 0; f < nf; f++) ni += util.m_faces[f].m_indices.size();
+    bool fits = counts4[0] >= nv && counts4[1] >= nf && counts4[2] >= ni && counts4[3] >= ne;
+    counts4[0] = nv; counts4[1] = nf; counts4[2] = ni; counts4[3] = ne;
+    if (!fits) return 1;
+    for (int i = 0; i < nv; i++)
+        for (int k = 0; k < 3; k++) verts_out[3 * i + k] = util.m_vertices[i][k];
+    int off = 0;
+    for (int f = 0; f < nf; f++) {
+        for (int k = 0; k < 4; k++) planes_out[4 * f + k] = util.m_faces[f].m_plane[k];
+        face_counts_out[f] = util.m_faces[f].m_indices.size();
+        for (int k = 0; k < face_counts_out[f]; k++) indices_out[off++] = util.m_faces[f].m_indices[k];
+    }
+    for (int i = 0; i < ne; i++)
+        for (int k = 0; k < 3; k++) edges_out[3 * i + k] = util.m_uniqueEdges[i][k];
+    return 0;
+}
+
+// World AABBs with b3TransformAabb2, margin 0 (as initializeGpuAabbsFull does per step).
+void ref_aabbs(const b3RigidBodyData* bodies, int n, const b3Collidable* cols, const b3Aabb* local_aabbs,
+               b3Aabb* out) {
+    (void)cols;
+    for (int i = 0; i < n; i++) {
+        const b3Aabb& la = local_aabbs[bodies[i].m_collidableIdx];
+        b3Float4 mn, mx;
+        b3TransformAabb2(la.m_minVec, la.m_maxVec, 0.f, bodies[i].m_pos, bodies[i].m_quat, &mn, &mx);
+        out[i].m_minVec = mn;
+        out[i].m_minIndices[3] = i;
+        out[i].m_maxVec = mx;
+        out[i].m_signedMaxIndices[3] = bodies[i].m_invMass == 0.f ? 0 : 1;
+    }
+}
+
+// Pair set from the reference's dynamic-BVH broadphase, filtered by the tight inclusive test
+// (b3TestAabbAgainstAabb) and with static-static pairs removed; output (a<b) sorted.
+int ref_pairs_dbvt(const b3Aabb* aabbs, int n, int* out_xy, int cap) {
+    b3DynamicBvhBroadphase bp(n);
+    for (int i = 0; i < n; i++) {
+        b3Vector3 mn = b3MakeVector3(aabbs[i].m_min[0], aabbs[i].m_min[1], aabbs[i].m_min[2]);
+        b3Vector3 mx = b3MakeVector3(aabbs[i].m_max[0], aabbs[i].m_max[1], aabbs[i].m_max[2]);
+        bp.createProxy(mn, mx, i, 0, 1, 1);
+    }
+    bp.calculateOverlappingPairs();
+    b3OverlappingPairCache* cache = bp.getOverlappingPairCache();
+    std::vector<std::pair<int, int>> ps;
+    for (int k = 0; k < cache->getNumOverlappingPairs(); k++) {
+        const b3BroadphasePair& p = cache->getOverlappingPairArray()[k];
+        int a = std::min(p.x, p.y), b = std::max(p.x, p.y);
+        if (aabbs[a].m_signedMaxIndices[3] == 0 && aabbs[b].m_signedMaxIndices[3] == 0) continue;
+        if (!b3TestAabbAgainstAabb(aabbs[a].m_minVec, aabbs[a].m_maxVec, aabbs[b].m_minVec, aabbs[b].m_maxVec))
+            continue;
+        ps.push_back({a, b});
+    }
+    std::sort(ps.begin(), ps.end());
+    ps.erase(std::unique(ps.begin(), ps.end()), ps.end());
+    int np = (int)ps.size();
+    for (int k = 0; k < np && k < cap; k++) {
+        out_xy[2 * k] = ps[k].first;
+        out_xy[2 * k + 1] = ps[k].second;
+    }
+    return np;
+}
+
+// Contacts for each pair with the reference's CPU functions; writes one manifold per pair that
+// produced contact (in pair order) and out_pair_index[m] = pair index.  Sphere-sphere and
+// plane-sphere have no CPU code in the reference; such pairs are skipped here (return count only).
+int ref_contacts(const b3RigidBodyData* bodies, int nbodies, const b3Collidable* cols, int ncols,
+                 const b3ConvexPolyhedronData* hulls, int nhulls, const b3GpuFace* faces, int nfaces,
+                 const int* indices, int nindices, const b3Vector3* verts, int nverts, const b3Vector3* edges,
+                 int nedges, const int* pairs_xy, int npairs, b3Contact4Data* out, int* out_pair_index, int cap) {
+    b3AlignedObjectArray<b3RigidBodyData> B;
+    B.resize(nbodies);
+    for (int i = 0; i < nbodies; i++) B[i] = bodies[i];
+    b3AlignedObjectArray<b3Collidable> C;
+    C.resize(ncols);
+    for (int i = 0; i < ncols; i++) C[i] = cols[i];
+    b3AlignedObjectArray<b3ConvexPolyhedronData> H;
+    H.resize(nhulls);
+    for (int i = 0; i < nhulls; i++) H[i] = hulls[i];
+    b3AlignedObjectArray<b3GpuFace> F;
+    F.resize(nfaces);
+    for (int i = 0; i < nfaces; i++) F[i] = faces[i];
+    b3AlignedObjectArray<int> I;
+    I.resize(nindices);
+    for (int i = 0; i < nindices; i++) I[i] = indices[i];
+    b3AlignedObjectArray<b3Float4> V;
+    V.resize(nverts);
+    for (int i = 0; i < nverts; i++) V[i] = verts[i];
+    b3AlignedObjectArray<b3Float4> E;
+    E.resize(nedges > 0 ? nedges : 1);
+    for (int i = 0; i < nedges; i++) E[i] = edges[i];
+    int n = 0;
+    for (int p = 0; p < npairs; p++) {
+        int a = pairs_xy[2 * p], b = pairs_xy[2 * p + 1];
+        int ca = bodies[a].m_collidableIdx, cb = bodies[b].m_collidableIdx;
+        int ta = cols[ca].m_shapeType, tb = cols[cb].m_shapeType;
+        int before = n;
+        if (ta == SHAPE_CONVEX_HULL && tb == SHAPE_CONVEX_HULL) {
+            b3AlignedObjectArray<b3Contact4Data> tmp;
+            int nc = 0;
+            b3ContactConvexConvexSAT(p, a, b, ca, cb, B, C, H, V, E, I, F, tmp, nc, 1);
+            if (nc > 0 && n < cap) out[n++] = tmp[0];
+        } else {
+            b3Contact4 c4;
+            int nc = 0;
+            if (ta == SHAPE_PLANE && tb == SHAPE_CONVEX_HULL)
+                computeContactPlaneConvex(p, a, b, ca, cb, bodies, cols, hulls, verts, indices, faces, &c4, nc, 1);
+            else if (tb == SHAPE_PLANE && ta == SHAPE_CONVEX_HULL)
+                computeContactPlaneConvex(p, b, a, cb, ca, bodies, cols, hulls, verts, indices, faces, &c4, nc, 1);
+            else if (ta == SHAPE_SPHERE && tb == SHAPE_CONVEX_HULL)
+                computeContactSphereConvex(p, a, b, ca, cb, bodies, cols, hulls, verts, indices, faces, &c4, nc, 1);
+            else if (tb == SHAPE_SPHERE && ta == SHAPE_CONVEX_HULL)
+                computeContactSphereConvex(p, b, a, cb, ca, bodies, cols, hulls, verts, indices, faces, &c4, nc, 1);
+            if (nc > 0 && n < cap) out[n++] = c4;
+        }
+        if (n > before) out_pair_index[n - 1] = p;
+    }
+    return n;
+}
+
+// b3PgsJacobiSolver(usePgs).solveGroup with 2 friction directions, no warm start (avoids the
+// dangling m_originalContactPoint write, b3PgsJacobiSolver.cpp:868,1595-1613), no split impulse.
+void ref_solve(b3RigidBodyData* bodies, b3InertiaData* inertias, int nbodies, const b3Contact4Data* contacts, int nc,
+               int use_pgs, int iterations, float dt) {
+    b3AlignedObjectArray<b3Contact4> C;
+    C.resize(nc);
+    for (int i = 0; i < nc; i++) memcpy(&C[i], &contacts[i], sizeof(b3Contact4Data));
+    b3PgsJacobiSolver solver(use_pgs != 0);
+    b3ContactSolverInfo info;
+    info.m_solverMode = B3_SOLVER_USE_2_FRICTION_DIRECTIONS | B3_SOLVER_SIMD;
+    info.m_splitImpulse = false;
+    info.m_numIterations = iterations;
+    info.m_timeStep = dt;
+    solver.solveGroup(bodies, inertias, nbodies, nc ? &C[0] : 0, nc, 0, 0, info);
+}
+
+void ref_integrate(b3RigidBodyData* bodies, int n, float dt, float damping, const float* g) {
+    b3Float4 grav = b3MakeFloat4(g[0], g[1], g[2], 0.f);
+    for (int i = 0; i < n; i++) integrateSingleTransform(bodies, i, dt, damping, grav);
+}
+
+int ref_sizeof(int which) {
+    switch (which) {
+        case 0: return (int)sizeof(b3RigidBodyData);
+        case 1: return (int)sizeof(b3InertiaData);
+        case 2: return (int)sizeof(b3Collidable);
+        case 3: return (int)sizeof(b3ConvexPolyhedronData);
+        case 4: return (int)sizeof(b3GpuFace);
+        case 5: return (int)sizeof(b3Aabb);
+        case 6: return (int)sizeof(b3Contact4Data);
+    }
+    return -1;
+}
+
+}  // extern "C"
