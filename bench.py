@@ -1,0 +1,323 @@
+#!/usr/bin/env python
+"""Benchmark: body-steps/s of the GPU rigid-body step on a 262,144-box pile.
+
+Workload (both arms): 64x64 columns of 64 unit boxes (8-vertex hulls, half extent 0.5, mass 1)
+resting on a static plane -- the settled form of the 64^3 lattice pile (x/z spacing 1.1,
+jitter +-0.05, seed 0) -- PGS solver, 10 iterations, dt 1/60, gravity -9.8.  One step =
+stepSimulation: AABBs, grid broadphase, narrowphase, colouring, PGS solve, integration.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's CPU algorithm for the same step (the composed CPU step:
+b3TransformAabb2, exact pair set, b3ContactConvexConvexSAT / computeContactPlaneConvex,
+b3PgsJacobiSolver, integrateSingleTransform) through the plain-C oracle restatement (pinned
+bit-for-bit to the reference's own code by tests/test_oracle_golden.py), with every host thread
+the oracle can use.  Prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "body-steps/s at 256k bodies"
+WORKLOAD = ("box pile 64x64x64 = 262,144 unit boxes resting in 64x64 columns on a static plane "
+            "(settled form of the spacing-1.1 jitter-0.05 lattice, seed 0), PGS 10 iterations, dt 1/60")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--nx", type=int, default=64)
+    p.add_argument("--cpu-steps", type=int, default=3)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--solver", choices=["pgs", "jacobi"], default="pgs")
+    p.add_argument("--iterations", type=int, default=10)
+    return p.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+def dist_init(world):
+    if world > 1:
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group("gloo")
+        return dist
+    return None
+
+
+def dist_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def solver_traffic():
+    p = ROOT / "profiles" / "solver_traffic.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return d
+        except Exception:
+            return None
+    return None
+
+
+def make_scene(nx):
+    from bullet3_gb300 import scenes
+    return scenes.box_stack(nx, 64, nx, seed=0)
+
+
+# ------------------------------------------------------------------------------ CPU arm
+def cpu_run(scene, steps, iterations, mode):
+    """Times `steps` composed oracle steps on the scene; returns (seconds, threads, bodies)."""
+    from bullet3_gb300 import scenes
+    from bullet3_gb300.pipeline import b3Config
+    from oracle import oracle as O
+    np_, bp, pl = scenes.load_scene(scene, b3Config(), upload=False)
+    t = scenes.registered_tables(np_)
+    shapes = O.Shapes.from_tables(t)
+    threads = O.max_threads()
+    O.set_threads(threads)
+    b, I = t["bodies"], t["inertias"]
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        b, nc, npairs, npts = O.step(b, I, shapes, mode=mode, iterations=iterations, cell=1.7320508, use_grid=True)
+    return time.perf_counter() - t0, threads, scene.num_bodies
+
+
+def reference_arm(args):
+    rank, world, local = dist_info()
+    if rank != 0:
+        return 0
+    scene = make_scene(args.nx)
+    mode = 0 if args.solver == "pgs" else 1
+    # warm-up steps are run (untimed) from the same initial state; each timed step is one full
+    # composed CPU step of the whole 262,144-body scene
+    cpu_run(scene, args.warmup, args.iterations, mode) if args.warmup else None
+    secs, threads, n = cpu_run(scene, args.steps, args.iterations, mode)
+    value = n * args.steps / secs
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "bodies": n, "solver": args.solver, "iterations": args.iterations},
+            "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} composed CPU steps of the full {n}-body scene"},
+            "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------------------ GPU arm
+def gpu_arm(args):
+    import ctypes as C
+
+    import numpy as np
+
+    import __graft_entry__ as ge
+    rank, world, local = dist_info()
+    dist = dist_init(world)
+    if rank == 0 or not (ROOT / "bullet3_gb300" / "libb3gpu.so").exists():
+        ge.build()
+    dist_barrier(dist)
+    from bullet3_gb300 import capi, scenes
+    from bullet3_gb300.pipeline import b3Config
+    capi.load()
+    scene = make_scene(args.nx)
+    mode = capi.SOLVER_PGS if args.solver == "pgs" else capi.SOLVER_JACOBI
+    cfg = b3Config(solver_mode=mode, solver_iterations=args.iterations, use_cuda_graph=True)
+    np_, bp, pl = scenes.load_scene(scene, cfg, device=local)
+    h = np_.world.handle
+    N = scene.num_bodies
+    dt = 1.0 / 60.0
+    for _ in range(max(3, args.warmup)):
+        pl.stepSimulation(dt)
+    pl.synchronize()
+    # ---- timed region: device events on the library's stream
+    clocks = ClockSampler(local)
+    dist_barrier(dist)
+    pl.synchronize()
+    clocks.start()
+    l0 = pl.launchCount()
+    capi.call("b3g_record_event", h, C.c_int(0))
+    for _ in range(args.steps):
+        pl.stepSimulation(dt)
+    capi.call("b3g_record_event", h, C.c_int(1))
+    ms = C.c_float()
+    capi.call("b3g_event_elapsed", h, C.c_int(0), C.c_int(1), C.byref(ms))
+    pl.synchronize()
+    launches = pl.launchCount() - l0
+    clk = clocks.stop()
+    dist_barrier(dist)
+    t_rank = ms.value / 1000.0
+    t_max = dist_max(dist, t_rank)
+    value = world * N * args.steps / t_max
+    st = pl.stats()
+    status = st.status
+
+    # ---- per-stage times (profiled steps after the timed region, events around each stage)
+    pl.setProfiling(True)
+    acc = np.zeros(7)
+    P = 3
+    for _ in range(P):
+        pl.stepSimulation(dt)
+        acc += pl.stageTimes()
+    pl.setProfiling(False)
+    acc /= P
+    st = pl.stats()
+    C_ = st.num_contacts
+    I_ = max(1, st.iterations)
+    P_ = st.num_pairs
+    # algorithmic bytes (fp32/int32 widths, each field once): solve stage = constraint setup
+    # 416 B + colouring 16 B + applied impulses 24 B per manifold, 352 B per manifold-iteration
+    solve_bytes = C_ * (416 + 16 + 24) + 352 * C_ * I_
+    stage_bytes = {"aabb": 56 * N, "pairs": 112 * N + 8 * P_, "contacts": 64 * P_ + 88 * C_,
+                   "solve": solve_bytes, "integrate": 116 * N}
+    stage_ms = {"aabb": acc[0], "pairs": acc[1], "contacts": acc[2], "solve": acc[4], "integrate": acc[6]}
+    peak, peak_kind = measured_peaks()
+    solve_s = stage_ms["solve"] / 1000.0
+    achieved = solve_bytes / solve_s / 1e9 if solve_s > 0 else 0.0
+    traffic = solver_traffic()
+    roofline = {"bound": "hbm", "kernel": "solve stage (k_setup_rows + k_solve_pgs persistent kernel)",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_kind": peak_kind, "algorithmic_bytes": solve_bytes,
+                "traffic": traffic.get("bytes_per_step_scaled") if traffic else None}
+    stages = {k: {"ms": float(v), "algorithmic_GBps": stage_bytes[k] / (v / 1000.0) / 1e9 if v > 0 else None,
+                  "frac_of_hbm": (stage_bytes[k] / (v / 1000.0) / 1e9 / peak) if v > 0 else None}
+              for k, v in stage_ms.items()}
+
+    # ---- end to end through the C ABI with host buffers (pinned): upload state, step, download
+    e2e = None
+    try:
+        import torch
+        nbytes = N * capi.BODY.itemsize
+        pin_in = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        pin_out = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        host_in = pin_in.numpy().view(capi.BODY)
+        host_out = pin_out.numpy().view(capi.BODY)
+        capi.call("b3g_read_bodies", h, capi.ptr(host_in), C.c_int(N))
+        pl.synchronize()
+        dist_barrier(dist)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            capi.call("b3g_write_bodies", h, capi.ptr(host_in), C.c_int(N))
+            capi.call("b3g_step", h, C.c_float(dt))
+            capi.call("b3g_read_bodies", h, capi.ptr(host_out), C.c_int(N))
+            host_in, host_out = host_out, host_in  # this step's result is the next step's input
+        t_e2e = dist_max(dist, time.perf_counter() - t0)
+        e2e = {"value": world * N * args.steps / t_e2e, "unit": "body-steps/s", "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": nbytes}
+    except Exception as ex:  # pinned memory needs torch; report why instead of guessing
+        e2e = {"value": None, "unit": "body-steps/s", "error": str(ex)}
+
+    # ---- CPU baseline: the oracle's composed step on the same scene, bounded sample
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        secs, threads, n = cpu_run(scene, args.cpu_steps, args.iterations, 0 if args.solver == "pgs" else 1)
+        cpu = {"value": n * args.cpu_steps / secs, "unit": "body-steps/s", "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_steps} composed CPU oracle steps of the same {n}-body scene from its initial state"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world, "steps": args.steps,
+                "warmup": max(3, args.warmup), "ms_per_step": 1000 * t_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "bodies": N, "solver": args.solver, "iterations": args.iterations,
+                           "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                           "l2": "inputs larger than L2 (constraint rows and pair buffers exceed 129 MB)",
+                           "pairs": P_, "manifolds": C_, "contact_points": st.num_points, "colors": st.num_colors},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+                "clocks": clk, "stages": stages, "device_status": int(status)}
+        print(json.dumps(line), flush=True)
+    dist_barrier(dist)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

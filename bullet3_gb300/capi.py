@@ -48,7 +48,8 @@ class b3gConfig(C.Structure):
                 ("gravity", C.c_float * 3), ("angular_damping", C.c_float), ("solver_mode", C.c_int),
                 ("solver_iterations", C.c_int), ("erp", C.c_float), ("contact_threshold", C.c_float),
                 ("contact_friction", C.c_float), ("residual_tol", C.c_float), ("update_world_inertia", C.c_int),
-                ("use_cuda_graph", C.c_int), ("warm_start", C.c_int), ("reserved", C.c_int * 8)]
+                ("use_cuda_graph", C.c_int), ("warm_start", C.c_int), ("barrier_spin_limit", C.c_int),
+                ("reserved", C.c_int * 7)]
 
 
 class b3gStepStats(C.Structure):
@@ -77,7 +78,7 @@ EXPORTS = [
     "b3g_write_aabbs", "b3g_read_pairs", "b3g_read_contacts", "b3g_write_contacts", "b3g_read_batches",
     "b3g_read_impulses", "b3g_get_num_collidables", "b3g_read_registered_bodies", "b3g_read_shape_tables",
     "b3g_set_profiling",
-    "b3g_get_stage_times", "b3g_get_launch_count", "b3g_hull_compute",
+    "b3g_get_stage_times", "b3g_get_launch_count", "b3g_record_event", "b3g_event_elapsed", "b3g_hull_compute",
 ]
 
 

@@ -31,10 +31,11 @@ B3G_HD float dot3(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 B3G_HD v3 cross3(v3 a, v3 b) {
     return v3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
-// v / |v| (division, not reciprocal multiply: b3Vector3::normalized, b3Vector3.h:897-905)
+// v * (1/|v|): b3Vector3::normalized / normalize scale by the reciprocal length
+// (Bullet3Common/b3Vector3.h:260-300, :791-803)
 B3G_HD v3 normalize3(v3 a) {
-    float l = sqrtf(dot3(a, a));
-    return v3{a.x / l, a.y / l, a.z / l};
+    float inv = 1.0f / sqrtf(dot3(a, a));
+    return v3{a.x * inv, a.y * inv, a.z * inv};
 }
 
 struct quat {
@@ -80,6 +81,66 @@ B3G_HD v3 mtmul(const m33& m, v3 v) {
 B3G_HD v3 qrot(quat q, v3 v) { return mmul(qmat(q), v); }
 B3G_HD v3 qrot_inv(quat q, v3 v) { return mtmul(qmat(q), v); }
 B3G_HD v3 xform(v3 p, v3 pos, quat q) { return qrot(q, p) + pos; }
+
+// b3Quaternion * b3Vector3 (Bullet3Common/b3Quaternion.h:651-729, scalar branch)
+B3G_HD quat qmulv(quat q, v3 w) {
+    return quat{q.w * w.x + q.y * w.z - q.z * w.y, q.w * w.y + q.z * w.x - q.x * w.z,
+                q.w * w.z + q.x * w.y - q.y * w.x, -q.x * w.x - q.y * w.y - q.z * w.z};
+}
+// b3QuatRotate (b3Quaternion.h:868-879): (q * v) * q^-1, the form the SAT and clipping code uses
+B3G_HD v3 qrotq(quat q, v3 v) {
+    quat t = qmul(qmulv(q, v), qconj(q));
+    return v3{t.x, t.y, t.z};
+}
+// b3Matrix3x3::getRotation (b3Matrix3x3.h:392-491, scalar branch): matrix -> quaternion
+B3G_HD quat quat_from_mat(const m33& m) {
+    float e[3][3] = {{m.r0.x, m.r0.y, m.r0.z}, {m.r1.x, m.r1.y, m.r1.z}, {m.r2.x, m.r2.y, m.r2.z}};
+    float t[4];
+    float trace = e[0][0] + e[1][1] + e[2][2];
+    if (trace > 0.0f) {
+        float s = sqrtf(trace + 1.0f);
+        t[3] = s * 0.5f;
+        s = 0.5f / s;
+        t[0] = (e[2][1] - e[1][2]) * s;
+        t[1] = (e[0][2] - e[2][0]) * s;
+        t[2] = (e[1][0] - e[0][1]) * s;
+    } else {
+        int i = e[0][0] < e[1][1] ? (e[1][1] < e[2][2] ? 2 : 1) : (e[0][0] < e[2][2] ? 2 : 0);
+        int j = (i + 1) % 3, k = (i + 2) % 3;
+        float s = sqrtf(e[i][i] - e[j][j] - e[k][k] + 1.0f);
+        t[i] = s * 0.5f;
+        s = 0.5f / s;
+        t[3] = (e[k][j] - e[j][k]) * s;
+        t[j] = (e[j][i] + e[i][j]) * s;
+        t[k] = (e[k][i] + e[i][k]) * s;
+    }
+    return quat{t[0], t[1], t[2], t[3]};
+}
+// transpose, product and rigid-transform helpers with b3Matrix3x3 / b3Transform operation order
+B3G_HD m33 mtrans(const m33& m) {
+    m33 r;
+    r.r0 = v3{m.r0.x, m.r1.x, m.r2.x};
+    r.r1 = v3{m.r0.y, m.r1.y, m.r2.y};
+    r.r2 = v3{m.r0.z, m.r1.z, m.r2.z};
+    return r;
+}
+// m1 * m2: element (i,j) = m2.tdot_j(m1[i]) (b3Matrix3x3.h:1190-1272)
+B3G_HD v3 mrow_times(const v3& a, const m33& m2) {
+    return v3{m2.r0.x * a.x + m2.r1.x * a.y + m2.r2.x * a.z, m2.r0.y * a.x + m2.r1.y * a.y + m2.r2.y * a.z,
+              m2.r0.z * a.x + m2.r1.z * a.y + m2.r2.z * a.z};
+}
+B3G_HD m33 mmul33(const m33& m1, const m33& m2) {
+    m33 r;
+    r.r0 = mrow_times(m1.r0, m2);
+    r.r1 = mrow_times(m1.r1, m2);
+    r.r2 = mrow_times(m1.r2, m2);
+    return r;
+}
+// b3Transform::inverse applied to a point: basis^T p + basis^T (-origin) (b3Transform.h:182-186)
+B3G_HD v3 xform_inv(const m33& R, v3 origin, v3 p) {
+    m33 t = mtrans(R);
+    return mmul(t, p) + mmul(t, -origin);
+}
 
 // inverse inertia matrix (3 float4 rows in memory)
 B3G_HD v3 imul(const b3gMat3& m, v3 v) {

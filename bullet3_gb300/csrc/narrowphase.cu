@@ -125,9 +125,9 @@ __device__ void plane_hull(const NPArgs& a, int pairIdx, int bodyA, int bodyB) {
     v3 planeNormal = mk3(pe.x, pe.y, pe.z);
     float planeConstant = pe.w;
     m33 RA = qmat(ornA), RB = qmat(ornB);
-    v3 planeNormalWorld = mmul(RA, planeNormal);
-    // planeInConvex basis = RB^T * RA ; planeNormalInConvex = RB^T (RA (-n))
-    v3 planeNormalInConvex = mtmul(RB, mmul(RA, -planeNormal));
+    v3 planeNormalWorld = qrotq(ornA, planeNormal);
+    // planeInConvex = inverse(convexWorld) * planeTransform: basis RB^T * RA (b3Transform order)
+    v3 planeNormalInConvex = mmul(mmul33(mtrans(RB), RA), -planeNormal);
     float4 pts[64];
     int numPoints = 0;
     float maxDot = -1e30f;
@@ -140,7 +140,7 @@ __device__ void plane_hull(const NPArgs& a, int pairIdx, int bodyA, int bodyB) {
         }
         if (numPoints < 64) {
             v3 vtxWorld = mmul(RB, vtx) + posB;
-            v3 vtxInPlane = mtmul(RA, vtxWorld - posA);
+            v3 vtxInPlane = xform_inv(RA, posA, vtxWorld);
             float dist = dot3(planeNormal, vtxInPlane) - planeConstant;
             if (dist < 0.f) {
                 pts[numPoints] = make_float4(vtxWorld.x, vtxWorld.y, vtxWorld.z, dist);
@@ -224,7 +224,7 @@ __device__ void sphere_hull(const NPArgs& a, int pairIdx, int bodyA, int bodyB) 
     v3 spherePos1 = f4v3(BA.pos);
     v3 pos = f4v3(BB.pos);
     m33 R = qmat(f4q(BB.quat));
-    v3 spherePos = mtmul(R, spherePos1 - pos);
+    v3 spherePos = xform_inv(R, pos, spherePos1);
     const b3gHull hull = a.hulls[a.cols[BB.collidableIdx].shapeIndex];
     v3 closest = mk3(0, 0, 0);
     float minDist = -1000000.f;
@@ -257,7 +257,8 @@ __device__ void sphere_hull(const NPArgs& a, int pairIdx, int bodyA, int bodyB) 
                     if (dist > minDist) {
                         minDist = dist;
                         closest = out;
-                        localHitNormal = mk3(tmp.x / dist, tmp.y / dist, tmp.z / dist);
+                        float inv = 1.0f / dist;  // b3Vector3 operator/ scales by the reciprocal
+                        localHitNormal = mk3(tmp.x * inv, tmp.y * inv, tmp.z * inv);
                     }
                 } else {
                     bCollide = false;
@@ -359,9 +360,9 @@ __device__ __forceinline__ AxisBest warp_argmax(AxisBest x) {
 }
 
 // b3ProjectAxis: project the hull's local vertices on the axis rotated into its frame.
-__device__ __forceinline__ void project(const b3gFloat4* verts, int nv, v3 pos, const m33& R, v3 dir, float& mn,
+__device__ __forceinline__ void project(const b3gFloat4* verts, int nv, v3 pos, quat orn, v3 dir, float& mn,
                                         float& mx) {
-    v3 localDir = mtmul(R, dir);
+    v3 localDir = qrotq(qconj(orn), dir);
     float offset = dot3(pos, dir);
     mn = FLT_MAX;
     mx = -FLT_MAX;
@@ -380,18 +381,18 @@ __device__ __forceinline__ void project(const b3gFloat4* verts, int nv, v3 pos, 
 // Axis k of the SAT sequence: faces of A, faces of B, then edges (e0 of A major, e1 of B minor).
 // Returns false when the edge cross product is almost zero (axis skipped).
 __device__ __forceinline__ bool sat_axis(int k, const b3gHull& hA, const b3gHull& hB, const b3gFace* faces,
-                                         const b3gFloat4* edges, const m33& RA, const m33& RB, v3 deltaC2, v3& axis) {
+                                         const b3gFloat4* edges, quat qA, quat qB, v3 deltaC2, v3& axis) {
     if (k < hA.numFaces) {
         v3 n = ld3(&faces[hA.faceOffset + k].plane);
-        axis = mmul(RA, n);
+        axis = qrotq(qA, n);
     } else if (k < hA.numFaces + hB.numFaces) {
         v3 n = ld3(&faces[hB.faceOffset + (k - hA.numFaces)].plane);
-        axis = mmul(RB, n);
+        axis = qrotq(qB, n);
     } else {
         int e = k - hA.numFaces - hB.numFaces;
         int e0 = e / hB.numUniqueEdges, e1 = e - e0 * hB.numUniqueEdges;
-        v3 w0 = mmul(RA, ld3(&edges[hA.uniqueEdgesOffset + e0]));
-        v3 w1 = mmul(RB, ld3(&edges[hB.uniqueEdgesOffset + e1]));
+        v3 w0 = qrotq(qA, ld3(&edges[hA.uniqueEdgesOffset + e0]));
+        v3 w1 = qrotq(qB, ld3(&edges[hB.uniqueEdgesOffset + e1]));
         v3 c = cross3(w0, w1);
         // b3IsAlmostZero compares |c| against the double 1e-6
         if (!((double)fabsf(c.x) > 1e-6 || (double)fabsf(c.y) > 1e-6 || (double)fabsf(c.z) > 1e-6)) return false;
@@ -452,7 +453,8 @@ __global__ void __launch_bounds__(HH_WARPS * 32) k_hull_hull(NPArgs a, int max_p
         const b3gHull hA = a.hulls[a.cols[BA.collidableIdx].shapeIndex];
         const b3gHull hB = a.hulls[a.cols[BB.collidableIdx].shapeIndex];
         const v3 posA = f4v3(BA.pos), posB = f4v3(BB.pos);
-        const m33 RA = qmat(f4q(BA.quat)), RB = qmat(f4q(BB.quat));
+        const quat qA = f4q(BA.quat), qB = f4q(BB.quat);
+        const m33 RA = qmat(qA), RB = qmat(qB);
         const v3 c0 = mmul(RA, f4v3(hA.localCenter)) + posA;
         const v3 c1 = mmul(RB, f4v3(hB.localCenter)) + posB;
         const v3 deltaC2 = c0 - c1;
@@ -463,10 +465,10 @@ __global__ void __launch_bounds__(HH_WARPS * 32) k_hull_hull(NPArgs a, int max_p
         const b3gFloat4* vB = &a.verts[hB.vertexOffset];
         for (int k = lane; k < naxes; k += 32) {
             v3 axis;
-            if (!sat_axis(k, hA, hB, a.faces, a.edges, RA, RB, deltaC2, axis)) continue;
+            if (!sat_axis(k, hA, hB, a.faces, a.edges, qA, qB, deltaC2, axis)) continue;
             float min0, max0, min1, max1;
-            project(vA, hA.numVertices, posA, RA, axis, min0, max0);
-            project(vB, hB.numVertices, posB, RB, axis, min1, max1);
+            project(vA, hA.numVertices, posA, qA, axis, min0, max0);
+            project(vB, hB.numVertices, posB, qB, axis, min1, max1);
             if (max0 < min1 || max1 < min0) {
                 separated = true;
                 continue;
@@ -482,20 +484,24 @@ __global__ void __launch_bounds__(HH_WARPS * 32) k_hull_hull(NPArgs a, int max_p
         best = warp_argmin(best);
         if (best.idx == 0x7fffffff) continue;  // no usable axis (degenerate)
         v3 sep;
-        sat_axis(best.idx, hA, hB, a.faces, a.edges, RA, RB, deltaC2, sep);
+        sat_axis(best.idx, hA, hB, a.faces, a.edges, qA, qB, deltaC2, sep);
         if (dot3(-deltaC2, sep) > 0.0f) sep = -sep;
 
+        // b3ClipHullHullSingle clips with the orientation round-tripped through a b3Transform
+        // (setRotation then getRotation, b3ContactConvexConvexSAT.h:315-330)
+        const quat cA = quat_from_mat(RA), cB = quat_from_mat(RB);
+        const m33 CA = qmat(cA), CB = qmat(cB);
         // incident face of B: max dot(world normal, sep), first max wins
         AxisBest fb{-FLT_MAX, 0x7fffffff};
         for (int f = lane; f < hB.numFaces; f += 32) {
-            float d = dot3(mmul(RB, ld3(&a.faces[hB.faceOffset + f].plane)), sep);
+            float d = dot3(qrotq(cB, ld3(&a.faces[hB.faceOffset + f].plane)), sep);
             if (d > fb.d || (d == fb.d && f < fb.idx)) { fb.d = d; fb.idx = f; }
         }
         fb = warp_argmax(fb);
         // reference face of A: min dot(world normal, sep), first min wins
         AxisBest fa{FLT_MAX, 0x7fffffff};
         for (int f = lane; f < hA.numFaces; f += 32) {
-            float d = dot3(mmul(RA, ld3(&a.faces[hA.faceOffset + f].plane)), sep);
+            float d = dot3(qrotq(cA, ld3(&a.faces[hA.faceOffset + f].plane)), sep);
             if (d < fa.d || (d == fa.d && f < fa.idx)) { fa.d = d; fa.idx = f; }
         }
         fa = warp_argmin(fa);
@@ -507,19 +513,19 @@ __global__ void __launch_bounds__(HH_WARPS * 32) k_hull_hull(NPArgs a, int max_p
             const b3gFace polyB = a.faces[hB.faceOffset + fb.idx];
             int nin = 0;
             for (int e = 0; e < polyB.numIndices && e < CLIP_CAP; e++) {
-                v3 w = mmul(RB, ld3(&vB[a.indices[polyB.indexOffset + e]])) + posB;
+                v3 w = mmul(CB, ld3(&vB[a.indices[polyB.indexOffset + e]])) + posB;
                 pin[nin++] = make_float4(w.x, w.y, w.z, 0.f);
             }
             const b3gFace polyA = a.faces[hA.faceOffset + fa.idx];
             const v3 planeNormalA = mk3(polyA.plane.x, polyA.plane.y, polyA.plane.z);
-            const v3 worldPlaneAnormal1 = mmul(RA, planeNormalA);
+            const v3 worldPlaneAnormal1 = qrotq(cA, planeNormalA);
             const int nva = polyA.numIndices;
             for (int e0 = 0; e0 < nva; e0++) {
                 v3 va = ld3(&vA[a.indices[polyA.indexOffset + e0]]);
                 v3 vb = ld3(&vA[a.indices[polyA.indexOffset + ((e0 + 1) % nva)]]);
-                v3 worldEdge0 = mmul(RA, va - vb);
+                v3 worldEdge0 = qrotq(cA, va - vb);
                 v3 planeNormalWS1 = -cross3(worldEdge0, worldPlaneAnormal1);
-                v3 worldA1 = mmul(RA, va) + posA;
+                v3 worldA1 = mmul(CA, va) + posA;
                 float planeEqWS1 = -dot3(worldA1, planeNormalWS1);
                 int nout = clip_face(pin, nin, planeNormalWS1, planeEqWS1, pout, a.status);
                 float4* tmp = pout; pout = pin; pin = tmp;

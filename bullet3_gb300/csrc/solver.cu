@@ -556,7 +556,8 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     int launches = 0;
     long long ll = 0;
     const int grid = d.num_sms * 4;
-    const int iters = cfg.solver_iterations > 0 ? cfg.solver_iterations : 1;
+    int iters = cfg.solver_iterations > 0 ? cfg.solver_iterations : 1;
+    if (iters > 4096) iters = 4096;  // residual_acc holds 2 doubles per iteration for 4096 iterations
     int* d_nc = &d.counters->num_contacts;
     int* d_n2 = &d.counters->pad[1];
     // per-step resets
@@ -603,7 +604,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     a.bar.gen = d.barrier + 1;
     a.bar.abort_flag = d.barrier + 2;
     a.bar.status = &d.counters->status;
-    a.spin_limit = B3G_BARRIER_SPIN_LIMIT;
+    a.spin_limit = cfg.barrier_spin_limit > 0 ? (unsigned)cfg.barrier_spin_limit : B3G_BARRIER_SPIN_LIMIT;
 
     if (cfg.solver_mode == B3G_SOLVER_JACOBI) {
         const uint32_t sentinel = (1u << d.body_bits) - 1u;
@@ -631,10 +632,12 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     attr[0].val.cooperative = 1;
     lc.attrs = attr;
     lc.numAttrs = 1;
+    cudaError_t e;
     if (cfg.solver_mode == B3G_SOLVER_JACOBI)
-        cudaLaunchKernelEx(&lc, k_solve_jacobi, a);
+        e = cudaLaunchKernelEx(&lc, k_solve_jacobi, a);
     else
-        cudaLaunchKernelEx(&lc, k_solve_pgs, a);
+        e = cudaLaunchKernelEx(&lc, k_solve_pgs, a);
+    if (e != cudaSuccess && d.launch_error == cudaSuccess) d.launch_error = e;
     launches++;
     return launches + (int)ll;
 }

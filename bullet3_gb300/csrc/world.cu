@@ -79,6 +79,7 @@ struct b3gWorld {
     long long launches = 0;
     long long graph_kernels = 0;
     b3gStepStats last_stats{};
+    cudaEvent_t user_events[16] = {};
 };
 
 static void free_device(b3gWorld* w) {
@@ -168,6 +169,8 @@ extern "C" b3gStatus b3g_destroy(b3g_handle h) {
     free_device(h);
     if (h->events.created)
         for (auto& e : h->events.ev) cudaEventDestroy(e);
+    for (auto& e : h->user_events)
+        if (e) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return B3G_OK;
@@ -421,7 +424,9 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     d.body_bits = bits_for(N + 1);
     if (2 * d.body_bits > 64) return fail(B3G_ERR_CAPACITY, "too many bodies");
     d.max_pairs = h->cfg.max_pairs > 0 ? h->cfg.max_pairs : std::max(1024, 12 * N);
-    d.max_contacts = h->cfg.max_contacts > 0 ? std::min(h->cfg.max_contacts, d.max_pairs) : d.max_pairs;
+    // at most one manifold per pair: contact storage is sized with the pair capacity so that no
+    // manifold index can exceed it
+    d.max_contacts = d.max_pairs;
     d.prim.sort_blocks = sms * 4;
     d.prim.scan_blocks = sms * 2;
 
@@ -520,6 +525,15 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
         if (!(h)->uploaded) return fail(B3G_ERR_NOT_UPLOADED, "call b3g_write_all_to_gpu first"); \
     } while (0)
 
+static b3gStatus check_launch(b3gWorld* h) {
+    cudaError_t e = h->d.launch_error;
+    h->d.launch_error = cudaSuccess;
+    cudaError_t e2 = cudaGetLastError();
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return fail(B3G_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+    return B3G_OK;
+}
+
 static void record(b3gWorld* h, int k) {
     if (h->profiling) cudaEventRecord(h->events.ev[k], h->stream);
 }
@@ -551,7 +565,7 @@ extern "C" b3gStatus b3g_step(b3g_handle h, float dt) {
     CUDA_TRY(cudaSetDevice(h->device));
     if (h->profiling || !h->cfg.use_cuda_graph) {
         enqueue_step(h, dt, h->profiling);
-        CUDA_TRY(cudaGetLastError());
+        TRY(check_launch(h));
         return B3G_OK;
     }
     if (!h->graph_exec || h->graph_dt != dt || h->graph_mode != h->cfg.solver_mode ||
@@ -565,6 +579,13 @@ extern "C" b3gStatus b3g_step(b3g_handle h, float dt) {
         CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
         enqueue_step(h, dt, false);
         CUDA_TRY(cudaStreamEndCapture(h->stream, &g));
+        {
+            b3gStatus st = check_launch(h);
+            if (st != B3G_OK) {
+                cudaGraphDestroy(g);
+                return st;
+            }
+        }
         CUDA_TRY(cudaGraphInstantiate(&h->graph_exec, g, 0));
         cudaGraphDestroy(g);
         h->graph_dt = dt;
@@ -582,31 +603,31 @@ extern "C" b3gStatus b3g_step(b3g_handle h, float dt) {
 extern "C" b3gStatus b3g_setup_aabbs(b3g_handle h) {
     REQUIRE_UPLOADED(h);
     h->launches += launch_aabbs(h->d, h->stream);
-    CUDA_TRY(cudaGetLastError());
+    TRY(check_launch(h));
     return B3G_OK;
 }
 extern "C" b3gStatus b3g_calculate_overlapping_pairs(b3g_handle h) {
     REQUIRE_UPLOADED(h);
     h->launches += launch_pairs(h->d, h->stream);
-    CUDA_TRY(cudaGetLastError());
+    TRY(check_launch(h));
     return B3G_OK;
 }
 extern "C" b3gStatus b3g_compute_contacts(b3g_handle h) {
     REQUIRE_UPLOADED(h);
     h->launches += launch_contacts(h->d, h->cfg.contact_friction, h->stream);
-    CUDA_TRY(cudaGetLastError());
+    TRY(check_launch(h));
     return B3G_OK;
 }
 extern "C" b3gStatus b3g_solve_contacts(b3g_handle h, float dt) {
     REQUIRE_UPLOADED(h);
     h->launches += launch_solver(h->d, h->cfg, dt, h->stream);
-    CUDA_TRY(cudaGetLastError());
+    TRY(check_launch(h));
     return B3G_OK;
 }
 extern "C" b3gStatus b3g_integrate(b3g_handle h, float dt) {
     REQUIRE_UPLOADED(h);
     h->launches += launch_integrate(h->d, h->cfg, dt, h->stream);
-    CUDA_TRY(cudaGetLastError());
+    TRY(check_launch(h));
     return B3G_OK;
 }
 extern "C" b3gStatus b3g_synchronize(b3g_handle h) {
@@ -772,7 +793,7 @@ extern "C" b3gStatus b3g_write_contacts(b3g_handle h, const void* host, int n) {
     k_expand_contacts<<<h->d.num_sms * 2, 256, 0, h->stream>>>(h->d.contacts_compact, n, h->d.contact_slots,
                                                               h->d.manifold_pair, h->d.contact_flag, h->d.counters);
     h->launches++;
-    CUDA_TRY(cudaGetLastError());
+    TRY(check_launch(h));
     return B3G_OK;
 }
 
@@ -881,6 +902,23 @@ extern "C" b3gStatus b3g_get_stage_times(b3g_handle h, float* ms7) {
 extern "C" b3gStatus b3g_get_launch_count(b3g_handle h, long long* n) {
     if (!h || !n) return fail(B3G_ERR_INVALID_ARG, "null argument");
     *n = h->launches;
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_record_event(b3g_handle h, int slot) {
+    REQUIRE_UPLOADED(h);
+    if (slot < 0 || slot >= 16) return fail(B3G_ERR_INVALID_ARG, "event slot out of range");
+    if (!h->user_events[slot]) CUDA_TRY(cudaEventCreate(&h->user_events[slot]));
+    CUDA_TRY(cudaEventRecord(h->user_events[slot], h->stream));
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_event_elapsed(b3g_handle h, int a, int b, float* ms) {
+    REQUIRE_UPLOADED(h);
+    if (!ms || a < 0 || a >= 16 || b < 0 || b >= 16 || !h->user_events[a] || !h->user_events[b])
+        return fail(B3G_ERR_INVALID_ARG, "event slots not recorded");
+    CUDA_TRY(cudaEventSynchronize(h->user_events[b]));
+    CUDA_TRY(cudaEventElapsedTime(ms, h->user_events[a], h->user_events[b]));
     return B3G_OK;
 }
 

@@ -96,6 +96,7 @@ struct DeviceState {
     int* d_num_dynamic = nullptr;          // device copy of num_dynamic (sort length)
     int* d_num_bodies = nullptr;           // device copy of num_bodies
     PrimConfig prim;
+    cudaError_t launch_error = cudaSuccess;  // first failed launch not reported through cudaGetLastError
 };
 
 #define B3G_MAX_COLORS 256

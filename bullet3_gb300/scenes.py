@@ -75,6 +75,27 @@ def box_pile(nx=10, ny=10, nz=10, spacing=1.1, base_y=0.6, jitter=0.01, half=0.5
     return sc
 
 
+def box_stack(nx=64, ny=64, nz=64, spacing=1.1, jitter=0.05, half=0.5, mass=1.0, seed=0, overlap=0.005) -> Scene:
+    """Settled form of the box_pile lattice: every lattice column rests on the plane as a stack
+    (each box `overlap` into the one below), lattice x/z positions with the same jitter."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sc = Scene(name=f"box_stack_{nx}x{ny}x{nz}")
+    sc.shapes.append({"type": "plane", "normal": (0.0, 1.0, 0.0), "constant": 0.0})
+    sc.shapes.append({"type": "hull", "verts": box_vertices(half, half, half)})
+    ii, jj, kk = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    p = np.stack([ii.ravel() * spacing, half - overlap + jj.ravel() * (2 * half - overlap), kk.ravel() * spacing], 1)
+    p = p - np.array([(nx - 1) * spacing * 0.5, 0.0, (nz - 1) * spacing * 0.5])
+    j = rng.uniform(-jitter, jitter, p.shape)
+    j[:, 1] = 0.0
+    p = p + j
+    n = len(p)
+    sc.body_shape = np.array([0] + [1] * n, np.int32)
+    sc.mass = np.array([0.0] + [mass] * n, np.float32)
+    sc.pos = np.vstack([np.zeros((1, 3)), p]).astype(np.float32)
+    sc.orn = np.tile(np.array([0, 0, 0, 1], np.float32), (n + 1, 1))
+    return sc
+
+
 def mixed_scene(n=131072, extent=64.0, seed=0, velocity_sigma=1.0, plane=False, cell_factor=2.0) -> Scene:
     rng = np.random.Generator(np.random.PCG64(seed))
     sc = Scene(name=f"mixed_{n}")

@@ -69,7 +69,8 @@ typedef struct b3gConfig {
     int update_world_inertia;  /* 0 = reference behaviour (world inverse inertia frozen at registration) */
     int use_cuda_graph;        /* capture the whole step as one CUDA graph */
     int warm_start;            /* 0 = cold start (reference); 1 = learned warm start if a model is loaded */
-    int reserved[8];
+    int barrier_spin_limit;    /* polls before a grid barrier gives up (0 = default, about a second) */
+    int reserved[7];
 } b3gConfig;
 
 /* Per-step counters, copied once per step from the device. */
@@ -189,6 +190,10 @@ b3gStatus b3g_set_profiling(b3g_handle h, int on);
 b3gStatus b3g_get_stage_times(b3g_handle h, float* ms7);
 /* Number of kernels this library launched since creation (counted on the host at launch). */
 b3gStatus b3g_get_launch_count(b3g_handle h, long long* n);
+/* Records timing event `slot` (0..15) on the world's stream; b3g_event_elapsed returns the
+ * milliseconds between two recorded slots (synchronising on the later one). */
+b3gStatus b3g_record_event(b3g_handle h, int slot);
+b3gStatus b3g_event_elapsed(b3g_handle h, int slot_start, int slot_end, float* ms);
 
 /* ------------------------------------------------------------------ convex hull (host only, no GPU) */
 /* b3ConvexUtility::initializePolyhedralFeatures (Bullet3Collision/NarrowPhaseCollision/b3ConvexUtility.cpp:26-246)

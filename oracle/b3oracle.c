@@ -45,7 +45,8 @@ static inline v3 scl(v3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
 static inline v3 lscl(float s, v3 a) { return mk(s * a.x, s * a.y, s * a.z); }
 static inline float dot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 static inline v3 cross(v3 a, v3 b) { return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
-static inline v3 nrm(v3 a) { float l = sqrtf(dot(a, a)); return mk(a.x / l, a.y / l, a.z / l); }
+/* b3Vector3::normalized / normalize: scale by the reciprocal length (Bullet3Common/b3Vector3.h:260-300) */
+static inline v3 nrm(v3 a) { float inv = 1.0f / sqrtf(dot(a, a)); return mk(a.x * inv, a.y * inv, a.z * inv); }
 
 static inline m3 qmat(qt q) {
     float d = q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w;
@@ -77,6 +78,68 @@ static inline qt qmul(qt a, qt b) {
     r.z = a.w * b.z + a.z * b.w + a.x * b.y - a.y * b.x;
     r.w = a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z;
     return r;
+}
+
+/* b3Quaternion * b3Vector3, scalar branch (Bullet3Common/b3Quaternion.h:651-729) */
+static inline qt qmulv(qt q, v3 w) {
+    qt r;
+    r.x = q.w * w.x + q.y * w.z - q.z * w.y;
+    r.y = q.w * w.y + q.z * w.x - q.x * w.z;
+    r.z = q.w * w.z + q.x * w.y - q.y * w.x;
+    r.w = -q.x * w.x - q.y * w.y - q.z * w.z;
+    return r;
+}
+static inline qt qconj(qt q) { qt r = {-q.x, -q.y, -q.z, q.w}; return r; }
+/* b3QuatRotate (b3Quaternion.h:868-879): (q * v) * q^-1 */
+static inline v3 qrotq(qt q, v3 v) { qt t = qmul(qmulv(q, v), qconj(q)); return mk(t.x, t.y, t.z); }
+/* b3Matrix3x3::getRotation, scalar branch (Bullet3Common/b3Matrix3x3.h:457-491) */
+static qt quat_from_mat(const m3* m) {
+    float e[3][3] = {{m->r0.x, m->r0.y, m->r0.z}, {m->r1.x, m->r1.y, m->r1.z}, {m->r2.x, m->r2.y, m->r2.z}};
+    float t[4], trace = e[0][0] + e[1][1] + e[2][2];
+    qt q;
+    if (trace > 0.0f) {
+        float s = sqrtf(trace + 1.0f);
+        t[3] = s * 0.5f;
+        s = 0.5f / s;
+        t[0] = (e[2][1] - e[1][2]) * s;
+        t[1] = (e[0][2] - e[2][0]) * s;
+        t[2] = (e[1][0] - e[0][1]) * s;
+    } else {
+        int i = e[0][0] < e[1][1] ? (e[1][1] < e[2][2] ? 2 : 1) : (e[0][0] < e[2][2] ? 2 : 0);
+        int j = (i + 1) % 3, k = (i + 2) % 3;
+        float s = sqrtf(e[i][i] - e[j][j] - e[k][k] + 1.0f);
+        t[i] = s * 0.5f;
+        s = 0.5f / s;
+        t[3] = (e[k][j] - e[j][k]) * s;
+        t[j] = (e[j][i] + e[i][j]) * s;
+        t[k] = (e[k][i] + e[i][k]) * s;
+    }
+    q.x = t[0]; q.y = t[1]; q.z = t[2]; q.w = t[3];
+    return q;
+}
+static inline m3 mtrans(const m3* m) {
+    m3 r;
+    r.r0 = mk(m->r0.x, m->r1.x, m->r2.x);
+    r.r1 = mk(m->r0.y, m->r1.y, m->r2.y);
+    r.r2 = mk(m->r0.z, m->r1.z, m->r2.z);
+    return r;
+}
+/* m1 * m2 with element (i,j) = m2.tdot_j(m1[i]) (b3Matrix3x3.h:1190-1272) */
+static inline v3 mrow_times(v3 a, const m3* m2) {
+    return mk(m2->r0.x * a.x + m2->r1.x * a.y + m2->r2.x * a.z, m2->r0.y * a.x + m2->r1.y * a.y + m2->r2.y * a.z,
+              m2->r0.z * a.x + m2->r1.z * a.y + m2->r2.z * a.z);
+}
+static inline m3 mmul33(const m3* m1, const m3* m2) {
+    m3 r;
+    r.r0 = mrow_times(m1->r0, m2);
+    r.r1 = mrow_times(m1->r1, m2);
+    r.r2 = mrow_times(m1->r2, m2);
+    return r;
+}
+/* b3Transform::inverse applied to p: basis^T p + basis^T (-origin) (b3Transform.h:182-186) */
+static inline v3 xform_inv(const m3* R, v3 origin, v3 p) {
+    m3 t = mtrans(R);
+    return add(mmul(&t, p), mmul(&t, neg(origin)));
 }
 
 /* ------------------------------------------------------------------ AABBs */
@@ -297,8 +360,11 @@ static int plane_hull(const obody* bodies, const oshapes* sh, int A, int B, ocon
     v3 planeNormal = mk(pe.x, pe.y, pe.z);
     float planeConstant = pe.w, maxDot = -1e30f;
     m3 RA = qmat(f4q(BA->quat)), RB = qmat(f4q(BB->quat));
-    v3 planeNormalWorld = mmul(&RA, planeNormal);
-    v3 planeNormalInConvex = mtmul(&RB, mmul(&RA, neg(planeNormal)));
+    v3 planeNormalWorld = qrotq(f4q(BA->quat), planeNormal);
+    /* planeInConvex = convexWorldTransform.inverse() * planeTransform (b3ConvexHullContact.cpp:1310-1318) */
+    m3 RBt = mtrans(&RB);
+    m3 PinC = mmul33(&RBt, &RA);
+    v3 planeNormalInConvex = mmul(&PinC, neg(planeNormal));
     p4 pts[64];
     int numPoints = 0, i, idx[4], nred;
     for (i = 0; i < hull->numVertices; i++) {
@@ -310,7 +376,7 @@ static int plane_hull(const obody* bodies, const oshapes* sh, int A, int B, ocon
         }
         if (numPoints < 64) {
             v3 vtxWorld = add(mmul(&RB, vtx), posB);
-            v3 vtxInPlane = mtmul(&RA, sub(vtxWorld, posA));
+            v3 vtxInPlane = xform_inv(&RA, posA, vtxWorld);
             float dist = dot(planeNormal, vtxInPlane) - planeConstant;
             if (dist < 0.f) {
                 pts[numPoints].x = vtxWorld.x; pts[numPoints].y = vtxWorld.y; pts[numPoints].z = vtxWorld.z;
@@ -392,7 +458,7 @@ static int sphere_hull(const obody* bodies, const oshapes* sh, int A, int B, oco
     float radius = sh->cols[BA->collidableIdx].radius, minDist = -1000000.f;
     v3 pos = f4v(BB->pos);
     m3 R = qmat(f4q(BB->quat));
-    v3 spherePos = mtmul(&R, sub(f4v(BA->pos), pos));
+    v3 spherePos = xform_inv(&R, pos, f4v(BA->pos));
     const ohull* hull = &sh->hulls[sh->cols[BB->collidableIdx].shapeIndex];
     v3 closest = mk(0, 0, 0), localHitNormal = mk(0, 0, 0);
     int bCollide = 1, f;
@@ -404,7 +470,7 @@ static int sphere_hull(const obody* bodies, const oshapes* sh, int A, int B, oco
         v3 pntReturn = sub(spherePos, lscl(dist, n));
         if (dist > radius) { bCollide = 0; break; }
         if (dist > 0.f) {
-            v3 out;
+            v3 out = mk(0.f, 0.f, 0.f);
             if (point_in_polygon(spherePos, face, base, sh->indices, &out)) {
                 if (dist > minDist) { minDist = dist; closest = pntReturn; localHitNormal = n; }
             } else {
@@ -415,7 +481,8 @@ static int sphere_hull(const obody* bodies, const oshapes* sh, int A, int B, oco
                     if (dist > minDist) {
                         minDist = dist;
                         closest = out;
-                        localHitNormal = mk(tmp.x / dist, tmp.y / dist, tmp.z / dist);
+                        float inv = 1.0f / dist; /* b3Vector3 operator/ scales by the reciprocal */
+                        localHitNormal = mk(tmp.x * inv, tmp.y * inv, tmp.z * inv);
                     }
                 } else { bCollide = 0; break; }
             }
@@ -455,8 +522,8 @@ static int sphere_sphere(const obody* bodies, const oshapes* sh, int A, int B, o
 }
 
 /* b3ProjectAxis (Bullet3Collision/NarrowPhaseCollision/shared/b3FindSeparatingAxis.h:4-33) */
-static void project(const of4* verts, int nv, v3 pos, const m3* R, v3 dir, float* mn, float* mx) {
-    v3 localDir = mtmul(R, dir);
+static void project(const of4* verts, int nv, v3 pos, qt orn, v3 dir, float* mn, float* mx) {
+    v3 localDir = qrotq(qconj(orn), dir);
     float offset = dot(pos, dir);
     int i;
     *mn = FLT_MAX;
@@ -472,11 +539,11 @@ static void project(const of4* verts, int nv, v3 pos, const m3* R, v3 dir, float
 }
 
 /* b3TestSepAxis (b3FindSeparatingAxis.h:35-53) */
-static int test_sep_axis(const ohull* hA, const ohull* hB, v3 posA, const m3* RA, v3 posB, const m3* RB, v3 axis,
+static int test_sep_axis(const ohull* hA, const ohull* hB, v3 posA, qt qA, v3 posB, qt qB, v3 axis,
                          const of4* verts, float* depth) {
     float min0, max0, min1, max1, d0, d1;
-    project(&verts[hA->vertexOffset], hA->numVertices, posA, RA, axis, &min0, &max0);
-    project(&verts[hB->vertexOffset], hB->numVertices, posB, RB, axis, &min1, &max1);
+    project(&verts[hA->vertexOffset], hA->numVertices, posA, qA, axis, &min0, &max0);
+    project(&verts[hB->vertexOffset], hB->numVertices, posB, qB, axis, &min1, &max1);
     if (max0 < min1 || max1 < min0) return 0;
     d0 = max0 - min1;
     d1 = max1 - min0;
@@ -484,36 +551,38 @@ static int test_sep_axis(const ohull* hA, const ohull* hB, v3 posA, const m3* RA
     return 1;
 }
 
-/* b3FindSeparatingAxis (b3FindSeparatingAxis.h:55-195): face normals of A, of B, exact edge-edge */
-static int find_separating_axis(const ohull* hA, const ohull* hB, v3 posA, const m3* RA, v3 posB, const m3* RB,
+/* b3FindSeparatingAxis (b3FindSeparatingAxis.h:55-195): face normals of A, of B, exact edge-edge;
+ * rotations by b3QuatRotate, centres by b3TransformPoint (matrix form) */
+static int find_separating_axis(const ohull* hA, const ohull* hB, v3 posA, qt qA, v3 posB, qt qB,
                                 const oshapes* sh, v3* sep) {
-    v3 c0 = add(mmul(RA, f4v(hA->localCenter)), posA);
-    v3 c1 = add(mmul(RB, f4v(hB->localCenter)), posB);
+    m3 RA = qmat(qA), RB = qmat(qB);
+    v3 c0 = add(mmul(&RA, f4v(hA->localCenter)), posA);
+    v3 c1 = add(mmul(&RB, f4v(hB->localCenter)), posB);
     v3 deltaC2 = sub(c0, c1);
     float dmin = FLT_MAX, d;
     int i, e0, e1;
     for (i = 0; i < hA->numFaces; i++) {
-        v3 n = mmul(RA, f4v(sh->faces[hA->faceOffset + i].plane));
+        v3 n = qrotq(qA, f4v(sh->faces[hA->faceOffset + i].plane));
         if (dot(deltaC2, n) < 0.f) n = neg(n);
-        if (!test_sep_axis(hA, hB, posA, RA, posB, RB, n, sh->verts, &d)) return 0;
+        if (!test_sep_axis(hA, hB, posA, qA, posB, qB, n, sh->verts, &d)) return 0;
         if (d < dmin) { dmin = d; *sep = n; }
     }
     for (i = 0; i < hB->numFaces; i++) {
-        v3 n = mmul(RB, f4v(sh->faces[hB->faceOffset + i].plane));
+        v3 n = qrotq(qB, f4v(sh->faces[hB->faceOffset + i].plane));
         if (dot(deltaC2, n) < 0.f) n = neg(n);
-        if (!test_sep_axis(hA, hB, posA, RA, posB, RB, n, sh->verts, &d)) return 0;
+        if (!test_sep_axis(hA, hB, posA, qA, posB, qB, n, sh->verts, &d)) return 0;
         if (d < dmin) { dmin = d; *sep = n; }
     }
     for (e0 = 0; e0 < hA->numUniqueEdges; e0++) {
-        v3 w0 = mmul(RA, f4v(sh->edges[hA->uniqueEdgesOffset + e0]));
+        v3 w0 = qrotq(qA, f4v(sh->edges[hA->uniqueEdgesOffset + e0]));
         for (e1 = 0; e1 < hB->numUniqueEdges; e1++) {
-            v3 w1 = mmul(RB, f4v(sh->edges[hB->uniqueEdgesOffset + e1]));
+            v3 w1 = qrotq(qB, f4v(sh->edges[hB->uniqueEdgesOffset + e1]));
             v3 cr = cross(w0, w1);
             /* b3IsAlmostZero compares against the double constant 1e-6 */
             if ((double)fabsf(cr.x) > 1e-6 || (double)fabsf(cr.y) > 1e-6 || (double)fabsf(cr.z) > 1e-6) {
                 cr = nrm(cr);
                 if (dot(deltaC2, cr) < 0.f) cr = neg(cr);
-                if (!test_sep_axis(hA, hB, posA, RA, posB, RB, cr, sh->verts, &d)) return 0;
+                if (!test_sep_axis(hA, hB, posA, qA, posB, qB, cr, sh->verts, &d)) return 0;
                 if (d < dmin) { dmin = d; *sep = cr; }
             }
         }
@@ -567,7 +636,8 @@ static int hull_hull(const obody* bodies, const oshapes* sh, int A, int B, ocont
     const ohull* hA = &sh->hulls[sh->cols[BA->collidableIdx].shapeIndex];
     const ohull* hB = &sh->hulls[sh->cols[BB->collidableIdx].shapeIndex];
     v3 posA = f4v(BA->pos), posB = f4v(BB->pos), sep, planeNormalA, worldPlaneAnormal1;
-    m3 RA = qmat(f4q(BA->quat)), RB = qmat(f4q(BB->quat));
+    qt qA = f4q(BA->quat), qB = f4q(BB->quat), cA, cB;
+    m3 RA = qmat(qA), RB = qmat(qB), CA, CB;
     p4 buf0[CLIP_CAP], buf1[CLIP_CAP];
     p4 *pin = buf0, *pout = buf1;
     int fb = -1, fa = -1, f, nin = 0, e, e0, nva, ncont = 0, i;
@@ -575,32 +645,38 @@ static int hull_hull(const obody* bodies, const oshapes* sh, int A, int B, ocont
     const of4* vA = &sh->verts[hA->vertexOffset];
     const of4* vB = &sh->verts[hB->vertexOffset];
     const oface *polyA, *polyB;
-    if (!find_separating_axis(hA, hB, posA, &RA, posB, &RB, sh, &sep)) return 0;
+    if (!find_separating_axis(hA, hB, posA, qA, posB, qB, sh, &sep)) return 0;
+    /* b3ClipHullHullSingle clips with the orientation round-tripped through a b3Transform
+     * (setRotation then getRotation, b3ContactConvexConvexSAT.h:315-330) */
+    cA = quat_from_mat(&RA);
+    cB = quat_from_mat(&RB);
+    CA = qmat(cA);
+    CB = qmat(cB);
     for (f = 0; f < hB->numFaces; f++) {
-        float d = dot(mmul(&RB, f4v(sh->faces[hB->faceOffset + f].plane)), sep);
+        float d = dot(qrotq(cB, f4v(sh->faces[hB->faceOffset + f].plane)), sep);
         if (d > dmax) { dmax = d; fb = f; }
     }
     for (f = 0; f < hA->numFaces; f++) {
-        float d = dot(mmul(&RA, f4v(sh->faces[hA->faceOffset + f].plane)), sep);
+        float d = dot(qrotq(cA, f4v(sh->faces[hA->faceOffset + f].plane)), sep);
         if (d < dmn) { dmn = d; fa = f; }
     }
     if (fb < 0 || fa < 0) return 0;
     polyB = &sh->faces[hB->faceOffset + fb];
     for (e = 0; e < polyB->numIndices && e < CLIP_CAP; e++) {
-        v3 w = add(mmul(&RB, f4v(vB[sh->indices[polyB->indexOffset + e]])), posB);
+        v3 w = add(mmul(&CB, f4v(vB[sh->indices[polyB->indexOffset + e]])), posB);
         pin[nin].x = w.x; pin[nin].y = w.y; pin[nin].z = w.z; pin[nin].w = 0.f;
         nin++;
     }
     polyA = &sh->faces[hA->faceOffset + fa];
     planeNormalA = mk(polyA->plane.x, polyA->plane.y, polyA->plane.z);
-    worldPlaneAnormal1 = mmul(&RA, planeNormalA);
+    worldPlaneAnormal1 = qrotq(cA, planeNormalA);
     nva = polyA->numIndices;
     for (e0 = 0; e0 < nva; e0++) {
         v3 va = f4v(vA[sh->indices[polyA->indexOffset + e0]]);
         v3 vb = f4v(vA[sh->indices[polyA->indexOffset + ((e0 + 1) % nva)]]);
-        v3 worldEdge0 = mmul(&RA, sub(va, vb));
+        v3 worldEdge0 = qrotq(cA, sub(va, vb));
         v3 planeNormalWS1 = neg(cross(worldEdge0, worldPlaneAnormal1));
-        v3 worldA1 = add(mmul(&RA, va), posA);
+        v3 worldA1 = add(mmul(&CA, va), posA);
         float planeEqWS1 = -dot(worldA1, planeNormalWS1);
         int nout = clip_face(pin, nin, planeNormalWS1, planeEqWS1, pout);
         p4* tmp = pout; pout = pin; pin = tmp;

@@ -158,6 +158,7 @@ int ref_contacts(const b3RigidBodyData* bodies, int nbodies, const b3Collidable*
             if (nc > 0 && n < cap) out[n++] = tmp[0];
         } else {
             b3Contact4 c4;
+            memset(&c4, 0, sizeof(c4));
             int nc = 0;
             if (ta == SHAPE_PLANE && tb == SHAPE_CONVEX_HULL)
                 computeContactPlaneConvex(p, a, b, ca, cb, bodies, cols, hulls, verts, indices, faces, &c4, nc, 1);

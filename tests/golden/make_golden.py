@@ -1,0 +1,253 @@
+"""Generates the golden vectors in tests/golden/ from the REFERENCE's own CPU code.
+
+Needs oracle/_ref/libb3ref.so, which oracle/build_ref.sh compiles in place from the reference
+sources (only possible where those sources exist).  The committed .npz files are what the
+test-suite uses everywhere else.
+
+Fixtures:
+  hulls.npz       box + Gaussian point sets -> b3ConvexUtility hull tables
+  pile.npz        4x4x4 interpenetrating unit boxes on a plane (reference hull tables):
+                  b3TransformAabb2 AABBs, dynamic-BVH pairs (tight-test filtered), contacts
+                  (b3ContactConvexConvexSAT / computeContactPlaneConvex), b3PgsJacobiSolver PGS and
+                  Jacobi velocities, integrateSingleTransform poses
+  mixed.npz       boxes, Gaussian hulls and spheres overlapping on a plane: same stages; the
+                  reference has no CPU code for sphere-sphere and plane-sphere, so those pairs carry
+                  no reference manifold
+  trajectory.npz  3x3x3 pile, 30 composed reference steps with the Jacobi solver (poses per step)
+  kat_aabb.npz    the touching-AABB known answer of test/b3DynamicBvhBroadphase/main.cpp:40-69
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+from oracle import oracle as O  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def box_vertices(h):
+    s = np.array([[x, y, z] for x in (-1, 1) for y in (-1, 1) for z in (-1, 1)], np.float32)
+    return s * np.asarray(h, np.float32)
+
+
+class TableBuilder:
+    """Shape tables in the device layout, built from REFERENCE hull tables."""
+
+    def __init__(self):
+        self.cols, self.laabbs, self.hulls, self.faces = [], [], [], []
+        self.indices, self.verts, self.edges = [], [], []
+
+    def plane(self, n, c):
+        f = np.zeros(1, O.FACE)[0]
+        f["plane"] = [n[0], n[1], n[2], c]
+        self.faces.append(f)
+        col = np.zeros(1, O.COLLIDABLE)[0]
+        col["radius"], col["shapeType"], col["shapeIndex"] = c, 4, len(self.faces) - 1
+        a = np.zeros(1, O.AABB)[0]
+        a["min"], a["max"] = -1e30, 1e30
+        self.cols.append(col)
+        self.laabbs.append(a)
+        return len(self.cols) - 1
+
+    def sphere(self, r):
+        col = np.zeros(1, O.COLLIDABLE)[0]
+        col["radius"], col["shapeType"], col["shapeIndex"] = r, 7, 0
+        a = np.zeros(1, O.AABB)[0]
+        a["min"], a["max"] = -r, r
+        self.cols.append(col)
+        self.laabbs.append(a)
+        return len(self.cols) - 1
+
+    def hull(self, points):
+        v, pl, fc, ix, e = O.ref_hull(points)
+        h = np.zeros(1, O.HULL)[0]
+        c = np.zeros(3, np.float32)
+        for p in v:  # vertex mean, float32, as b3GpuNarrowPhase::registerConvexHullShape
+            c = (c + p).astype(np.float32)
+        c = (c * np.float32(1.0 / np.float32(len(v)))).astype(np.float32)
+        h["localCenter"][:3] = c
+        h["uniqueEdgesOffset"], h["numUniqueEdges"] = len(self.edges), len(e)
+        for x in e:
+            self.edges.append([x[0], x[1], x[2], 0.0])
+        h["faceOffset"], h["numFaces"] = len(self.faces), len(fc)
+        off = 0
+        for k in range(len(fc)):
+            f = np.zeros(1, O.FACE)[0]
+            f["plane"] = pl[k]
+            f["indexOffset"], f["numIndices"] = len(self.indices), fc[k]
+            self.indices.extend(ix[off:off + fc[k]].tolist())
+            off += fc[k]
+            self.faces.append(f)
+        h["vertexOffset"], h["numVertices"] = len(self.verts), len(v)
+        for p in v:
+            self.verts.append([p[0], p[1], p[2], 0.0])
+        self.hulls.append(h)
+        col = np.zeros(1, O.COLLIDABLE)[0]
+        col["shapeType"], col["shapeIndex"] = 3, len(self.hulls) - 1
+        a = np.zeros(1, O.AABB)[0]
+        a["min"], a["max"] = v.min(0), v.max(0)
+        self.cols.append(col)
+        self.laabbs.append(a)
+        return len(self.cols) - 1
+
+    def shapes(self) -> O.Shapes:
+        def arr(x, dt):
+            return np.array(x, dt) if len(x) else np.zeros(1, dt)
+        return O.Shapes(arr(self.cols, O.COLLIDABLE), arr(self.laabbs, O.AABB), arr(self.hulls, O.HULL),
+                        arr(self.faces, O.FACE), np.array(self.indices or [0], np.int32),
+                        np.array(self.verts or [[0, 0, 0, 0]], np.float32),
+                        np.array(self.edges or [[0, 0, 0, 0]], np.float32))
+
+
+def quat_mat(q):
+    x, y, z, w = [np.float32(t) for t in q]
+    d = x * x + y * y + z * z + w * w
+    s = np.float32(2.0) / d
+    xs, ys, zs = x * s, y * s, z * s
+    wx, wy, wz = w * xs, w * ys, w * zs
+    xx, xy, xz = x * xs, x * ys, x * zs
+    yy, yz, zz = y * ys, y * zs, z * zs
+    one = np.float32(1.0)
+    return np.array([[one - (yy + zz), xy - wz, xz + wy], [xy + wz, one - (xx + zz), yz - wx],
+                     [xz - wy, yz + wx, one - (xx + yy)]], np.float32)
+
+
+def make_bodies(shapes: O.Shapes, body_shape, mass, pos, orn):
+    """registerPhysicsInstance + registerRigidBody: AABB with margin 0.01, AABB-box inertia with
+    the full extent used as half extent, world inverse inertia R diag(1/I) R^T."""
+    n = len(mass)
+    b = np.zeros(n, O.BODY)
+    I = np.zeros(n, O.INERTIA)
+    for i in range(n):
+        b[i]["pos"][:3] = pos[i]
+        b[i]["quat"] = orn[i]
+        b[i]["collidableIdx"] = body_shape[i]
+        b[i]["invMass"] = np.float32(1.0) / np.float32(mass[i]) if mass[i] else 0.0
+        b[i]["friction"] = 1.0
+        if mass[i]:
+            la = shapes.local_aabbs[body_shape[i]]
+            R = quat_mat(orn[i])
+            he = (np.float32(0.5) * (la["max"] - la["min"]) + np.float32(0.01)).astype(np.float32)
+            ext = np.abs(R) @ he
+            full = (2 * ext).astype(np.float32)
+            lx, ly, lz = [np.float32(2) * f for f in full]
+            m12 = np.float32(mass[i]) / np.float32(12.0)
+            li = np.array([m12 * (ly * ly + lz * lz), m12 * (lx * lx + lz * lz), m12 * (lx * lx + ly * ly)], np.float32)
+            inv = (np.float32(1) / li).astype(np.float32)
+            I[i]["initInvInertia"][0, 0], I[i]["initInvInertia"][1, 1], I[i]["initInvInertia"][2, 2] = inv
+            W = (R * inv[None, :]) @ R.T
+            I[i]["invInertiaWorld"][:, :3] = W
+    return b, I
+
+
+def stage_fixture(name, tb: TableBuilder, body_shape, mass, pos, orn, linvel=None, angvel=None):
+    shapes = tb.shapes()
+    bodies, inertias = make_bodies(shapes, body_shape, mass, pos, orn)
+    if linvel is not None:
+        bodies["linVel"][:, :3] = linvel
+    if angvel is not None:
+        bodies["angVel"][:, :3] = angvel
+    aabbs = O.ref_aabbs(bodies, shapes)
+    pairs = O.ref_pairs_dbvt(aabbs)
+    contacts, pidx = O.ref_contacts(bodies, shapes, pairs)
+    out = dict(bodies=bodies, inertias=inertias, aabbs=aabbs, pairs=pairs, contacts=contacts, contact_pair=pidx)
+    for it in (1, 10):
+        out[f"pgs_bodies_{it}"] = O.ref_solve(bodies, inertias, contacts, use_pgs=True, iterations=it)
+        out[f"jacobi_bodies_{it}"] = O.ref_solve(bodies, inertias, contacts, use_pgs=False, iterations=it)
+    out["integrated"] = O.ref_integrate(out["jacobi_bodies_10"])
+    for k in ("collidables", "local_aabbs", "hulls", "faces", "indices", "verts", "edges"):
+        out["shape_" + k] = getattr(shapes, k)
+    np.savez_compressed(OUT / f"{name}.npz", **out)
+    print(name, len(bodies), "bodies", len(pairs), "pairs", len(contacts), "manifolds")
+
+
+def main():
+    if O.load_reference() is None:
+        raise SystemExit("oracle/_ref/libb3ref.so is missing: run oracle/build_ref.sh first")
+    rng = np.random.Generator(np.random.PCG64(2024))
+    # hulls
+    inputs = [box_vertices([0.5, 0.5, 0.5])] + [box_vertices(rng.uniform(0.2, 0.6, 3)) for _ in range(5)]
+    inputs += [(rng.standard_normal((int(rng.integers(12, 33)), 3)) * 0.4).astype(np.float32) for _ in range(24)]
+    hd = {}
+    for i, p in enumerate(inputs):
+        v, pl, fc, ix, e = O.ref_hull(p)
+        hd[f"in_{i}"], hd[f"v_{i}"], hd[f"p_{i}"], hd[f"fc_{i}"], hd[f"ix_{i}"], hd[f"e_{i}"] = p, v, pl, fc, ix, e
+    hd["count"] = np.array(len(inputs))
+    np.savez_compressed(OUT / "hulls.npz", **hd)
+
+    # pile: interpenetrating boxes on a plane
+    tb = TableBuilder()
+    plane = tb.plane((0.0, 1.0, 0.0), 0.0)
+    box = tb.hull(box_vertices([0.5, 0.5, 0.5]))
+    g = np.stack(np.meshgrid(np.arange(4), np.arange(4), np.arange(4), indexing="ij"), -1).reshape(-1, 3)
+    pos = (g * np.array([1.0, 0.98, 1.0]) + [-1.5, 0.47, -1.5] + rng.uniform(-0.02, 0.02, g.shape)).astype(np.float32)
+    ang = rng.uniform(-0.03, 0.03, (len(g), 3))
+    orn = np.concatenate([np.sin(ang / 2) * [1, 1, 1], np.ones((len(g), 1))], 1)
+    orn = (orn / np.linalg.norm(orn, axis=1, keepdims=True)).astype(np.float32)
+    body_shape = [plane] + [box] * len(g)
+    mass = [0.0] + [1.0] * len(g)
+    pos = np.vstack([np.zeros((1, 3), np.float32), pos])
+    orn = np.vstack([np.array([[0, 0, 0, 1]], np.float32), orn])
+    lin = np.vstack([np.zeros((1, 3)), rng.normal(0, 0.3, (len(g), 3))]).astype(np.float32)
+    stage_fixture("pile", tb, body_shape, mass, pos, orn, linvel=lin)
+
+    # mixed shapes
+    tb = TableBuilder()
+    plane = tb.plane((0.0, 1.0, 0.0), 0.0)
+    n = 300
+    body_shape, mass = [plane], [0.0]
+    for i in range(n):
+        k = i % 4
+        if k in (0, 1):
+            body_shape.append(tb.hull(box_vertices(rng.uniform(0.2, 0.6, 3))))
+        elif k == 2:
+            body_shape.append(tb.sphere(float(rng.uniform(0.2, 0.5))))
+        else:
+            body_shape.append(tb.hull((rng.standard_normal((int(rng.integers(12, 33)), 3)) * 0.4).astype(np.float32)))
+        mass.append(1.0)
+    pos = np.vstack([np.zeros((1, 3)), rng.uniform([-3, 0.1, -3], [3, 4, 3], (n, 3))]).astype(np.float32)
+    q = rng.standard_normal((n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    orn = np.vstack([np.array([[0, 0, 0, 1]]), q]).astype(np.float32)
+    lin = np.vstack([np.zeros((1, 3)), rng.normal(0, 1.0, (n, 3))]).astype(np.float32)
+    stage_fixture("mixed", tb, body_shape, mass, pos, orn, linvel=lin)
+
+    # trajectory: composed reference step (AABB, dbvt pairs, contacts, Jacobi solve, integrate)
+    tb = TableBuilder()
+    plane = tb.plane((0.0, 1.0, 0.0), 0.0)
+    box = tb.hull(box_vertices([0.5, 0.5, 0.5]))
+    g = np.stack(np.meshgrid(np.arange(3), np.arange(3), np.arange(3), indexing="ij"), -1).reshape(-1, 3)
+    p = (g * 1.1 + [-1.1, 0.6, -1.1] + rng.uniform(-0.01, 0.01, g.shape)).astype(np.float32)
+    shapes = tb.shapes()
+    bodies, inertias = make_bodies(shapes, [plane] + [box] * len(g), [0.0] + [1.0] * len(g),
+                                   np.vstack([np.zeros((1, 3)), p]).astype(np.float32),
+                                   np.tile(np.array([0, 0, 0, 1], np.float32), (len(g) + 1, 1)))
+    traj = [bodies.copy()]
+    for step in range(30):
+        aabbs = O.ref_aabbs(bodies, shapes)
+        pairs = O.ref_pairs_dbvt(aabbs)
+        contacts, _ = O.ref_contacts(bodies, shapes, pairs)
+        bodies = O.ref_solve(bodies, inertias, contacts, use_pgs=False, iterations=10)
+        bodies = O.ref_integrate(bodies)
+        traj.append(bodies.copy())
+    out = dict(traj=np.stack(traj), inertias=inertias)
+    for k in ("collidables", "local_aabbs", "hulls", "faces", "indices", "verts", "edges"):
+        out["shape_" + k] = getattr(shapes, k)
+    np.savez_compressed(OUT / "trajectory.npz", **out)
+    print("trajectory", len(traj) - 1, "steps")
+
+    # touching AABBs [0,1]^3 and [1,2]^3 give exactly one pair (inclusive overlap)
+    a = np.zeros(2, O.AABB)
+    a[0]["min"], a[0]["max"], a[0]["minw"], a[0]["maxw"] = 0, 1, 0, 1
+    a[1]["min"], a[1]["max"], a[1]["minw"], a[1]["maxw"] = 1, 2, 1, 1
+    np.savez_compressed(OUT / "kat_aabb.npz", aabbs=a, pairs=O.ref_pairs_dbvt(a))
+    print("kat pairs", O.ref_pairs_dbvt(a).tolist())
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,114 @@
+"""CPU-only checks of the boundary: the library loads without a GPU, exports every entry point
+include/b3g_capi.h declares, and the host-side registry (shapes, bodies, hull builder, error
+codes) behaves like the reference's registration API."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, load_golden
+from bullet3_gb300 import capi, scenes
+from bullet3_gb300.pipeline import b3Config, b3GpuNarrowPhase, b3GpuRigidBodyPipeline
+
+
+def test_library_exports_every_declared_symbol():
+    lib = capi.load()
+    decl = set()
+    for hdr in Path(ROOT, "include").glob("*.h"):
+        decl |= set(re.findall(r"\b(b3g_[a-z0-9_]+)\s*\(", hdr.read_text()))
+    assert decl, "no declarations found"
+    missing = [s for s in sorted(decl) if not hasattr(lib, s)]
+    assert not missing, missing
+    assert set(capi.EXPORTS) <= decl
+
+
+def test_layouts_match_reference_sizes():
+    sizes = {capi.BODY: 80, capi.INERTIA: 96, capi.COLLIDABLE: 16, capi.HULL: 96, capi.FACE: 32, capi.AABB: 32,
+             capi.CONTACT: 112}
+    for dt, n in sizes.items():
+        assert dt.itemsize == n
+
+
+def test_registration_errors_match_reference_conventions():
+    np_ = b3GpuNarrowPhase(b3Config(m_maxConvexShapes=2, m_maxConvexBodies=2))
+    pl = b3GpuRigidBodyPipeline(np_)
+    s = np_.registerSphereShape(0.5)
+    assert s == 0
+    assert np_.registerPlaneShape((0, 1, 0), 0.0) == 1
+    assert np_.registerSphereShape(0.2) == -1  # capacity: -1 + b3Error (allocateCollidable)
+    assert pl.registerPhysicsInstance(1.0, (0, 0, 0), (0, 0, 0, 1), 7) == -1  # invalid collidable index
+    assert pl.registerPhysicsInstance(1.0, (0, 0, 0), (0, 0, 0, 1), s) == 0
+    assert pl.registerPhysicsInstance(0.0, (0, 0, 0), (0, 0, 0, 1), 1) == 1
+    assert pl.registerPhysicsInstance(1.0, (0, 0, 0), (0, 0, 0, 1), s) == -1  # body capacity
+    assert np_.registerCompoundShape([]) == -1 and np_.registerConcaveMesh(None, None, None) == -1
+    with pytest.raises(capi.B3GError):
+        capi.call("b3g_step", C.c_void_p(None), C.c_float(1 / 60))
+    with pytest.raises(capi.B3GError) as e:
+        capi.call("b3g_step", np_.world.handle, C.c_float(1 / 60))
+    assert e.value.status == 5  # not uploaded
+    assert np_.registerConvexHullShape(np.zeros((3, 3), np.float32)) == -1  # degenerate hull
+
+
+def test_registered_body_matches_reference_registration():
+    # registerPhysicsInstance: margin-0.01 AABB, AABB-box inertia using the full extent as the
+    # "half extent" (b3GpuNarrowPhase.cpp:876-901), friction 1, restitution 0
+    np_ = b3GpuNarrowPhase(b3Config())
+    pl = b3GpuRigidBodyPipeline(np_)
+    box = np_.registerConvexHullShape(scenes.box_vertices(0.5, 0.5, 0.5))
+    pl.registerPhysicsInstance(2.0, (1, 2, 3), (0, 0, 0, 1), box)
+    t = scenes.registered_tables(np_)
+    b, I = t["bodies"][0], t["inertias"][0]
+    assert b["invMass"] == np.float32(0.5) and b["friction"] == 1.0 and b["restitution"] == 0.0
+    l = 2 * (1.0 + 0.02)
+    expect = 1.0 / ((2.0 / 12.0) * (l * l + l * l))
+    np.testing.assert_allclose(np.diag(I["initInvInertia"][:, :3]), [expect] * 3, rtol=1e-6)
+    np.testing.assert_allclose(I["invInertiaWorld"][:, :3], np.diag([expect] * 3), rtol=1e-6, atol=1e-9)
+
+
+def _match_hull(mine, ref):
+    va, pa, fca, ia, ea = mine[:5]
+    vb, pb, fcb, ib, eb = ref
+    assert len(va) == len(vb)
+    d = np.abs(va[:, None, :] - vb[None, :, :]).max(-1)
+    m = d.argmin(1)
+    assert d[np.arange(len(va)), m].max() <= 1e-6 and len(set(m.tolist())) == len(va)
+    return m
+
+
+def test_hull_builder_against_reference_hulls():
+    """Same quantised vertices as b3ConvexHullComputer (bit-exact up to 1e-6), same face partition
+    and planes for unwelded faces; welded near-coplanar faces may take the other triangle's plane
+    (the reference picks by its internal face order), bounded by the 0.999 weld threshold."""
+    g = load_golden("hulls")
+    exact_faces = tight_planes = all_planes = 0
+    n = int(g["count"])
+    for i in range(n):
+        mine = capi.hull_compute(g[f"in_{i}"])
+        ref = (g[f"v_{i}"], g[f"p_{i}"], g[f"fc_{i}"], g[f"ix_{i}"], g[f"e_{i}"])
+        m = _match_hull(mine, ref)
+        off = 0
+        fa = []
+        for k, c in enumerate(mine[2]):
+            fa.append(frozenset(m[j] for j in mine[3][off:off + c]))
+            off += c
+        off = 0
+        fb = []
+        for c in ref[2]:
+            fb.append(frozenset(ref[3][off:off + c].tolist()))
+            off += c
+        if set(fa) == set(fb):
+            exact_faces += 1
+            for k, f in enumerate(fa):
+                j = fb.index(f)
+                dev = np.abs(mine[1][k] - ref[1][j]).max()
+                assert dev <= 0.05  # a welded face's normal is within the 0.999 weld cone
+                tight_planes += dev <= 1e-5
+                all_planes += 1
+    assert exact_faces >= n - 2
+    assert tight_planes >= 0.9 * all_planes
+    # boxes: identical topology, 6 quads, 3 unique edges
+    for i in range(6):
+        mine = capi.hull_compute(g[f"in_{i}"])
+        assert len(mine[2]) == 6 and (mine[2] == 4).all() and len(mine[4]) == 3

@@ -1,0 +1,188 @@
+"""GPU parity through the C ABI, stage by stage, against the reference's golden vectors and the
+CPU oracle on the same inputs.
+
+Bars (stated per test): pair sets bit-exact; manifolds bit-exact on their valid points (the kernels
+follow the reference's operation order and are compiled without FMA contraction); Jacobi
+velocities bit-exact; PGS velocities bit-exact against the oracle solving the same manifolds in the
+GPU's colour order, and batches legal; integrated poses within 1e-6 relative (sinf/cosf).
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from gpu_helpers import load, pairs_xy, run_stages, scene_from_golden, valid_points_equal
+from bullet3_gb300 import capi, scenes
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _write_golden_state(np_, d):
+    b = np_.readbackAllBodiesToCpu()
+    assert len(b) == len(d["bodies"])
+    b["linVel"], b["angVel"] = d["bodies"]["linVel"], d["bodies"]["angVel"]
+    np_.writeBodiesToGpu(b)
+    return b
+
+
+@pytest.mark.parametrize("name", ["pile", "mixed"])
+def test_golden_stages_match_reference(name):
+    d = load_golden(name)
+    np_, bp, pl, shapes = load(scene_from_golden(d))
+    b = _write_golden_state(np_, d)
+    run_stages(np_, bp, pl, solve=False)
+    # AABBs: bit-exact with the reference's b3TransformAabb2
+    ga = bp.getAllAabbsCPU()
+    assert np.array_equal(ga.view(np.uint8), d["aabbs"].view(np.uint8))
+    # pairs: bit-exact with the reference's filtered dynamic-BVH pair set
+    assert np.array_equal(pairs_xy(bp.getOverlappingPairsCPU()), d["pairs"])
+    # manifolds: bit-exact with the reference's CPU contact code where it has some
+    gc = np_.getContactsCPU()
+    oc, pr = O.contacts(b, shapes, bp.getOverlappingPairsCPU())
+    assert valid_points_equal(gc, oc)
+    has = np.where(pr["z"] >= 0)[0]
+    keep = [i for i, p in enumerate(has) if p in set(d["contact_pair"].tolist())]
+    assert valid_points_equal(gc[keep], d["contacts"])
+
+
+@pytest.mark.parametrize("name", ["pile", "mixed"])
+@pytest.mark.parametrize("iters", [1, 10])
+def test_golden_jacobi_bitexact(name, iters):
+    d = load_golden(name)
+    np_, bp, pl, shapes = load(scene_from_golden(d), solver_mode=capi.SOLVER_JACOBI, solver_iterations=iters)
+    b = _write_golden_state(np_, d)
+    I = np_.readInertiasToCpu()
+    run_stages(np_, bp, pl)
+    oc, _ = O.contacts(b, shapes, bp.getOverlappingPairsCPU())
+    ob, oimp, it, res = O.solve(b, I, oc, mode=1, iterations=iters)
+    gb = np_.readbackAllBodiesToCpu()
+    assert np.array_equal(gb["linVel"], ob["linVel"]) and np.array_equal(gb["angVel"], ob["angVel"])
+    gimp = pl.readImpulses()
+    assert np.array_equal(gimp, oimp)
+
+
+@pytest.mark.parametrize("name", ["pile", "mixed"])
+def test_golden_pgs_colour_order_bitexact(name):
+    d = load_golden(name)
+    np_, bp, pl, shapes = load(scene_from_golden(d), solver_mode=capi.SOLVER_PGS, solver_iterations=10)
+    b = _write_golden_state(np_, d)
+    I = np_.readInertiasToCpu()
+    run_stages(np_, bp, pl)
+    gc = np_.getContactsCPU()
+    col = pl.readBatches()
+    assert (col >= 0).all()
+    # batch legality (integer, exact): no dynamic body twice in a colour
+    assert O.check_batches(gc, col, b) == 0
+    order = np.lexsort((np.arange(len(col)), col)).astype(np.int32)
+    ob, _ = O.solve_ordered(b, I, gc, order, iterations=10)
+    gb = np_.readbackAllBodiesToCpu()
+    assert np.array_equal(gb["linVel"], ob["linVel"]) and np.array_equal(gb["angVel"], ob["angVel"])
+    st = pl.stats()
+    assert st.num_colors == col.max() + 1 and st.status == 0
+
+
+def test_integrate_matches_oracle():
+    d = load_golden("pile")
+    np_, bp, pl, shapes = load(scene_from_golden(d))
+    b = _write_golden_state(np_, d)
+    pl.integrate(1 / 60)
+    pl.synchronize()
+    gb = np_.readbackAllBodiesToCpu()
+    ob = O.integrate(b)
+    np.testing.assert_allclose(gb["pos"], ob["pos"], rtol=1e-6, atol=1e-7)
+    np.testing.assert_allclose(gb["quat"], ob["quat"], rtol=1e-6, atol=1e-7)
+    assert np.array_equal(gb["linVel"], ob["linVel"])
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_mixed_scene_stages_bitexact(seed):
+    # the C1 shape mix (boxes, Gaussian hulls, spheres, random orientations, N(0,1) velocities), 4k bodies
+    sc = scenes.mixed_scene(4096, extent=24.0, seed=seed, plane=True)
+    np_, bp, pl, shapes = load(sc, m_maxBroadphasePairs=400000, solver_mode=capi.SOLVER_JACOBI)
+    b = np_.readbackAllBodiesToCpu()
+    I = np_.readInertiasToCpu()
+    run_stages(np_, bp, pl)
+    ga = bp.getAllAabbsCPU()
+    assert np.array_equal(ga.view(np.uint8), O.aabbs(b, shapes).view(np.uint8))
+    gp = bp.getOverlappingPairsCPU()
+    op = O.pairs_grid(ga, sc.cell)
+    assert np.array_equal(pairs_xy(gp), pairs_xy(op))
+    assert np.array_equal(pairs_xy(op), pairs_xy(O.pairs_bruteforce(ga)))
+    gc = np_.getContactsCPU()
+    oc, _ = O.contacts(b, shapes, op)
+    assert valid_points_equal(gc, oc)
+    ob, _, _, _ = O.solve(b, I, oc, mode=1, iterations=10)
+    gb = np_.readbackAllBodiesToCpu()
+    assert np.array_equal(gb["linVel"], ob["linVel"]) and np.array_equal(gb["angVel"], ob["angVel"])
+    assert pl.status() == 0
+
+
+def test_box_pile_trajectory_jacobi():
+    # 1,000-box lattice on a plane, 120 steps: every stage bit-exact per step (from the GPU's own
+    # state), and after 120 graph-captured steps the poses stay within 1e-3 of an oracle trajectory
+    sc = scenes.box_pile(10, 10, 10, seed=0)
+    np_, bp, pl, shapes = load(sc, solver_mode=capi.SOLVER_JACOBI, solver_iterations=10)
+    I = np_.readInertiasToCpu()
+    dt = 1 / 60
+    ob = np_.readbackAllBodiesToCpu()
+    for step in range(120):
+        gb = np_.readbackAllBodiesToCpu()
+        run_stages(np_, bp, pl, dt)
+        op = O.pairs_bruteforce(O.aabbs(gb, shapes))
+        assert np.array_equal(pairs_xy(bp.getOverlappingPairsCPU()), pairs_xy(op)), step
+        oc, _ = O.contacts(gb, shapes, op)
+        assert valid_points_equal(np_.getContactsCPU(), oc), step
+        sb, _, _, _ = O.solve(gb, I, oc, mode=1, iterations=10)
+        after = np_.readbackAllBodiesToCpu()
+        assert np.array_equal(after["linVel"], sb["linVel"]), step
+        pl.integrate(dt)
+        ob, _, _, _ = O.step(ob, I, shapes, dt=dt, mode=1, iterations=10, use_grid=False)
+    pl.synchronize()
+    gb = np_.readbackAllBodiesToCpu()
+    assert np.abs(gb["pos"] - ob["pos"]).max() < 1e-3
+    assert gb["pos"][1:, 1].min() > 0.4  # resting on the plane, no tunnelling
+
+
+def test_pgs_residual_and_penetration_bounds():
+    # order-sensitive PGS: colour-order GPU solve vs the reference's sequential order on the same
+    # manifolds -- same contact residual class and penetration bounds
+    sc = scenes.box_stack(8, 16, 8, seed=1)
+    np_, bp, pl, shapes = load(sc, solver_mode=capi.SOLVER_PGS, solver_iterations=10)
+    I = np_.readInertiasToCpu()
+    dt = 1 / 60
+    for _ in range(30):
+        pl.stepSimulation(dt)
+    pl.synchronize()
+    b = np_.readbackAllBodiesToCpu()
+    run_stages(np_, bp, pl, dt)
+    gc = np_.getContactsCPU()
+    gpu_res = pl.stats().residual
+    _, _, _, seq_res = O.solve(b, I, gc, mode=0, iterations=10)
+    assert gpu_res < max(2.0 * seq_res, 0.05)
+    depth = gc["worldPosB"][..., 3][np.arange(4)[None, :] < gc["normal"][:, 3:4].astype(int)]
+    assert depth.min() > -0.05  # penetration bound for a resting stack
+    assert pl.status() == 0
+
+
+def test_determinism():
+    out = []
+    for _ in range(2):
+        sc = scenes.mixed_scene(2048, extent=16.0, seed=5, plane=True)
+        np_, bp, pl, shapes = load(sc, m_maxBroadphasePairs=300000)
+        for _ in range(10):
+            pl.stepSimulation(1 / 60)
+        pl.synchronize()
+        out.append(np_.readbackAllBodiesToCpu())
+    assert np.array_equal(out[0].view(np.uint8), out[1].view(np.uint8))
+
+
+def test_graph_step_equals_staged_step():
+    res = []
+    for graph in (True, False):
+        sc = scenes.box_pile(6, 6, 6, seed=3)
+        np_, bp, pl, shapes = load(sc, use_cuda_graph=graph)
+        for _ in range(40):
+            pl.stepSimulation(1 / 60)
+        pl.synchronize()
+        res.append(np_.readbackAllBodiesToCpu())
+    assert np.array_equal(res[0].view(np.uint8), res[1].view(np.uint8))

@@ -1,0 +1,107 @@
+"""The CPU oracle against golden vectors produced by the reference's own CPU code.
+
+Pins oracle/b3oracle.c (the checker every GPU parity test uses) to the reference:
+b3TransformAabb2, the dynamic-BVH pair set filtered by the tight test, b3ContactConvexConvexSAT,
+computeContactPlaneConvex, computeContactSphereConvex, b3PgsJacobiSolver (PGS and Jacobi) and
+integrateSingleTransform, plus a 30-step composed trajectory.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, shapes_from
+from oracle import oracle as O
+
+
+def _pairs_xy(p):
+    return np.stack([p["x"], p["y"]], 1)
+
+
+@pytest.mark.parametrize("name", ["pile", "mixed"])
+def test_aabbs_bitexact(name):
+    d = load_golden(name)
+    sh = shapes_from(d)
+    a = O.aabbs(d["bodies"], sh)
+    assert np.array_equal(a.view(np.uint8), d["aabbs"].view(np.uint8))
+
+
+@pytest.mark.parametrize("name", ["pile", "mixed"])
+def test_pairs_bitexact(name):
+    d = load_golden(name)
+    bf = O.pairs_bruteforce(d["aabbs"])
+    assert np.array_equal(_pairs_xy(bf), d["pairs"])
+    cell = float(np.max(d["aabbs"]["max"][d["aabbs"]["maxw"] == 1] - d["aabbs"]["min"][d["aabbs"]["maxw"] == 1]))
+    gr = O.pairs_grid(d["aabbs"], cell)
+    assert np.array_equal(_pairs_xy(gr), d["pairs"])
+
+
+def test_touching_aabbs_known_answer():
+    # test/b3DynamicBvhBroadphase/main.cpp:40-69: [0,1]^3 and [1,2]^3 touch -> exactly one pair
+    d = load_golden("kat_aabb")
+    assert d["pairs"].tolist() == [[0, 1]]
+    assert _pairs_xy(O.pairs_bruteforce(d["aabbs"])).tolist() == [[0, 1]]
+    assert _pairs_xy(O.pairs_grid(d["aabbs"], 1.0)).tolist() == [[0, 1]]
+
+
+@pytest.mark.parametrize("name", ["pile", "mixed"])
+def test_contacts_match_reference(name):
+    d = load_golden(name)
+    sh = shapes_from(d)
+    pairs = np.zeros(len(d["pairs"]), O.PAIR)
+    pairs["x"], pairs["y"] = d["pairs"][:, 0], d["pairs"][:, 1]
+    c, pr = O.contacts(d["bodies"], sh, pairs)
+    has = np.where(pr["z"] >= 0)[0]
+    # the reference has no CPU sphere-sphere / plane-sphere code: compare the other pairs
+    types = sh.collidables["shapeType"][d["bodies"]["collidableIdx"]]
+    ta, tb = types[d["pairs"][:, 0]], types[d["pairs"][:, 1]]
+    covered = ~(((ta == 7) & (tb == 7)) | ((ta == 4) & (tb == 7)) | ((ta == 7) & (tb == 4)))
+    mine = [i for i, p in enumerate(has) if covered[p]]
+    assert np.array_equal(has[mine], d["contact_pair"])
+    ref = d["contacts"]
+    got = c[mine]
+    assert len(got) == len(ref) > 0
+    np.testing.assert_array_equal(got["normal"][:, 3], ref["normal"][:, 3])  # point counts
+    npts = ref["normal"][:, 3].astype(int)
+    valid = np.arange(4)[None, :] < npts[:, None]
+    # stated tolerance: 1e-5 relative on points, depths and normals
+    np.testing.assert_allclose(got["worldPosB"][valid], ref["worldPosB"][valid], rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(got["normal"], ref["normal"], rtol=1e-5, atol=1e-6)
+    assert np.array_equal(got["bodyA"], ref["bodyA"]) and np.array_equal(got["bodyB"], ref["bodyB"])
+    assert np.array_equal(got["frictionCmp"], ref["frictionCmp"])
+    # on this machine the restatement reproduces the reference bit-for-bit
+    assert np.array_equal(got["worldPosB"][valid], ref["worldPosB"][valid])
+    assert np.array_equal(got["normal"], ref["normal"])
+
+
+@pytest.mark.parametrize("name", ["pile", "mixed"])
+@pytest.mark.parametrize("mode,key", [(0, "pgs"), (1, "jacobi")])
+@pytest.mark.parametrize("iters", [1, 10])
+def test_solver_matches_reference(name, mode, key, iters):
+    d = load_golden(name)
+    b, imp, it, res = O.solve(d["bodies"], d["inertias"], d["contacts"], mode=mode, iterations=iters)
+    ref = d[f"{key}_bodies_{iters}"]
+    np.testing.assert_allclose(b["linVel"], ref["linVel"], rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(b["angVel"], ref["angVel"], rtol=1e-5, atol=1e-6)
+    assert it == iters
+
+
+@pytest.mark.parametrize("name", ["pile", "mixed"])
+def test_integrate_matches_reference(name):
+    d = load_golden(name)
+    b = O.integrate(d["jacobi_bodies_10"])
+    ref = d["integrated"]
+    np.testing.assert_allclose(b["pos"], ref["pos"], rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(b["quat"], ref["quat"], rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(b["linVel"], ref["linVel"], rtol=1e-6, atol=1e-6)
+
+
+def test_composed_trajectory_matches_reference():
+    d = load_golden("trajectory")
+    sh = shapes_from(d)
+    traj = d["traj"]
+    b = traj[0].copy()
+    worst = 0.0
+    for s in range(1, len(traj)):
+        b, nc, npairs, npts = O.step(b, d["inertias"], sh, mode=1, iterations=10, use_grid=False)
+        worst = max(worst, float(np.abs(b["pos"] - traj[s]["pos"]).max()))
+    # stated tolerance for poses after 30 steps: 1e-4 absolute (transcendentals in the integrator)
+    assert worst < 1e-4, worst
