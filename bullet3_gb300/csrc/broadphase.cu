@@ -208,6 +208,7 @@ __global__ void __launch_bounds__(BP_THREADS) k_unpack_pairs(const uint64_t* __r
                                                              const int* __restrict__ d_np, int body_bits,
                                                              const b3gBody* __restrict__ bodies,
                                                              const b3gCollidable* __restrict__ cols,
+                                                             const int* __restrict__ col_small,
                                                              b3gPair* __restrict__ pairs, int* __restrict__ flags,
                                                              int* __restrict__ type_lists, int max_pairs,
                                                              int* __restrict__ type_count) {
@@ -226,9 +227,11 @@ __global__ void __launch_bounds__(BP_THREADS) k_unpack_pairs(const uint64_t* __r
             pr.x = a; pr.y = b; pr.z = -1; pr.w = -1;
             pairs[p] = pr;
             flags[p] = 0;
-            int ta = cols[bodies[a].collidableIdx].shapeType;
-            int tb = cols[bodies[b].collidableIdx].shapeType;
+            int ca = bodies[a].collidableIdx, cb = bodies[b].collidableIdx;
+            int ta = cols[ca].shapeType;
+            int tb = cols[cb].shapeType;
             t = pair_type(ta, tb);
+            if (t == PT_HULL_HULL && col_small[ca] && col_small[cb]) t = PT_HULL_HULL_SMALL;
         }
         unsigned peers = __match_any_sync(0xffffffffu, t);
         int leader = __ffs(peers) - 1;
@@ -275,7 +278,7 @@ int launch_pairs(DeviceState& d, cudaStream_t s) {
                             d.sort_scratch, s, &ll);
     // 5. unpack + classify
     k_unpack_pairs<<<d.num_sms * 4, BP_THREADS, 0, s>>>(d.pair_keys[w2], d_np, d.body_bits, d.bodies, d.collidables,
-                                                        d.pairs, d.contact_flag, d.type_lists, d.max_pairs,
+                                                        d.col_small, d.pairs, d.contact_flag, d.type_lists, d.max_pairs,
                                                         d.counters->type_count);
     launches++;
     return launches + (int)ll;

@@ -555,6 +555,138 @@ __global__ void __launch_bounds__(HH_WARPS * 32) k_hull_hull(NPArgs a, int max_p
     }
 }
 
+// ------------------------------------------------------------------ hull vs hull, one thread per pair
+// For small hulls (every face <= SMALL_FACE_VERTS vertices): the sequential form of the same
+// SAT -- axes in reference order, return at the first separating axis (b3FindSeparatingAxis
+// returns false there) -- then the same clip and reduction.  Bit-identical to the warp path.
+static constexpr int SMALL_CLIP = 2 * B3G_SMALL_FACE_VERTS;
+
+__global__ void __launch_bounds__(NP_THREADS) k_hull_hull_small(NPArgs a, int max_pairs) {
+    const int n = a.type_count[PT_HULL_HULL_SMALL];
+    const int* list = a.type_list + (size_t)PT_HULL_HULL_SMALL * max_pairs;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int p = list[t];
+        const b3gPair pr = a.pairs[p];
+        const int iA = pr.x, iB = pr.y;
+        const b3gBody& BA = a.bodies[iA];
+        const b3gBody& BB = a.bodies[iB];
+        const b3gHull hA = a.hulls[a.cols[BA.collidableIdx].shapeIndex];
+        const b3gHull hB = a.hulls[a.cols[BB.collidableIdx].shapeIndex];
+        const v3 posA = f4v3(BA.pos), posB = f4v3(BB.pos);
+        const quat qA = f4q(BA.quat), qB = f4q(BB.quat);
+        const m33 RA = qmat(qA), RB = qmat(qB);
+        const v3 deltaC2 = (mmul(RA, f4v3(hA.localCenter)) + posA) - (mmul(RB, f4v3(hB.localCenter)) + posB);
+        const b3gFloat4* vA = &a.verts[hA.vertexOffset];
+        const b3gFloat4* vB = &a.verts[hB.vertexOffset];
+        const int naxes = hA.numFaces + hB.numFaces + hA.numUniqueEdges * hB.numUniqueEdges;
+        float dmin = FLT_MAX;
+        v3 sep = mk3(0.f, 0.f, 0.f);
+        bool separated = false;
+        for (int k = 0; k < naxes; k++) {
+            v3 axis;
+            if (!sat_axis(k, hA, hB, a.faces, a.edges, qA, qB, deltaC2, axis)) continue;
+            float min0, max0, min1, max1;
+            project(vA, hA.numVertices, posA, qA, axis, min0, max0);
+            project(vB, hB.numVertices, posB, qB, axis, min1, max1);
+            if (max0 < min1 || max1 < min0) {
+                separated = true;
+                break;
+            }
+            float d0 = max0 - min1, d1 = max1 - min0;
+            float depth = d0 < d1 ? d0 : d1;
+            if (depth < dmin) {
+                dmin = depth;
+                sep = axis;
+            }
+        }
+        if (separated || dmin == FLT_MAX) continue;
+        if (dot3(-deltaC2, sep) > 0.0f) sep = -sep;
+        const quat cA = quat_from_mat(RA), cB = quat_from_mat(RB);
+        const m33 CA = qmat(cA), CB = qmat(cB);
+        int fbi = -1, fai = -1;
+        float dmax = -FLT_MAX, dmn = FLT_MAX;
+        for (int f = 0; f < hB.numFaces; f++) {
+            float d = dot3(qrotq(cB, ld3(&a.faces[hB.faceOffset + f].plane)), sep);
+            if (d > dmax) { dmax = d; fbi = f; }
+        }
+        for (int f = 0; f < hA.numFaces; f++) {
+            float d = dot3(qrotq(cA, ld3(&a.faces[hA.faceOffset + f].plane)), sep);
+            if (d < dmn) { dmn = d; fai = f; }
+        }
+        if (fbi < 0 || fai < 0) continue;
+        float4 buf0[SMALL_CLIP], buf1[SMALL_CLIP];
+        float4* pin = buf0;
+        float4* pout = buf1;
+        const b3gFace polyB = a.faces[hB.faceOffset + fbi];
+        int nin = 0;
+        for (int e = 0; e < polyB.numIndices && e < SMALL_CLIP; e++) {
+            v3 w = mmul(CB, ld3(&vB[a.indices[polyB.indexOffset + e]])) + posB;
+            pin[nin++] = make_float4(w.x, w.y, w.z, 0.f);
+        }
+        const b3gFace polyA = a.faces[hA.faceOffset + fai];
+        const v3 worldPlaneAnormal1 = qrotq(cA, mk3(polyA.plane.x, polyA.plane.y, polyA.plane.z));
+        const int nva = polyA.numIndices;
+        for (int e0 = 0; e0 < nva; e0++) {
+            v3 va = ld3(&vA[a.indices[polyA.indexOffset + e0]]);
+            v3 vb = ld3(&vA[a.indices[polyA.indexOffset + ((e0 + 1) % nva)]]);
+            v3 worldEdge0 = qrotq(cA, va - vb);
+            v3 planeNormalWS1 = -cross3(worldEdge0, worldPlaneAnormal1);
+            v3 worldA1 = mmul(CA, va) + posA;
+            float planeEqWS1 = -dot3(worldA1, planeNormalWS1);
+            // a convex polygon clipped by one plane gains at most one vertex: nin + 1 <= SMALL_CLIP
+            int nout = 0;
+            if (nin >= 2) {
+                float4 first = pin[nin - 1];
+                float ds = dot3(planeNormalWS1, mk3(first.x, first.y, first.z)) + planeEqWS1;
+                for (int ve = 0; ve < nin; ve++) {
+                    float4 end = pin[ve];
+                    float de = dot3(planeNormalWS1, mk3(end.x, end.y, end.z)) + planeEqWS1;
+                    if (ds < 0.f) {
+                        if (de < 0.f) {
+                            if (nout < SMALL_CLIP) pout[nout++] = end;
+                        } else {
+                            float tt = ds * 1.f / (ds - de);
+                            if (nout < SMALL_CLIP)
+                                pout[nout++] = make_float4(first.x + (end.x - first.x) * tt,
+                                                           first.y + (end.y - first.y) * tt,
+                                                           first.z + (end.z - first.z) * tt, 0.f);
+                        }
+                    } else if (de < 0.f) {
+                        float tt = ds * 1.f / (ds - de);
+                        if (nout < SMALL_CLIP)
+                            pout[nout++] = make_float4(first.x + (end.x - first.x) * tt,
+                                                       first.y + (end.y - first.y) * tt,
+                                                       first.z + (end.z - first.z) * tt, 0.f);
+                        if (nout < SMALL_CLIP) pout[nout++] = end;
+                    }
+                    first = end;
+                    ds = de;
+                }
+            }
+            float4* tmp = pout; pout = pin; pin = tmp;
+            nin = nout;
+        }
+        const float planeEqWS = polyA.plane.w - dot3(worldPlaneAnormal1, posA);
+        int ncont = 0;
+        for (int i = 0; i < nin; i++) {
+            float depth = dot3(worldPlaneAnormal1, mk3(pin[i].x, pin[i].y, pin[i].z)) + planeEqWS;
+            if (depth <= -1.0f) depth = -1.0f;
+            if (depth <= 0.0f) pout[ncont++] = make_float4(pin[i].x, pin[i].y, pin[i].z, depth);
+        }
+        if (ncont > 0) {
+            int idx[4];
+            int np = reduce_contacts(pout, ncont, sep, idx);
+            b3gContact4& c = a.slots[p];
+            write_header(c, a, iA, iB, sep, np);
+            for (int q = 0; q < np; q++) {
+                float4 v = pout[idx[q]];
+                c.worldPosB[q] = b3gFloat4{v.x, v.y, v.z, v.w};
+            }
+            a.flags[p] = 1;
+        }
+    }
+}
+
 // manifold list in pair order + pair.z = manifold index + point count
 __global__ void k_manifold_list(const int* __restrict__ flags, const int* __restrict__ cidx,
                                 const int* __restrict__ d_np, const b3gContact4* __restrict__ slots,
@@ -609,7 +741,9 @@ unsigned short friction_to_cmp(float f) {
 int launch_contacts(DeviceState& d, float friction, cudaStream_t s) {
     NPArgs a = make_args(d, friction_to_cmp(friction));
     int grid = d.num_sms * 4;
-    for (int t = PT_PLANE_HULL; t < PT_COUNT; t++) k_primitive_pairs<<<grid, NP_THREADS, 0, s>>>(a, t, d.max_pairs);
+    for (int t = PT_PLANE_HULL; t <= PT_PLANE_SPHERE; t++)
+        k_primitive_pairs<<<grid, NP_THREADS, 0, s>>>(a, t, d.max_pairs);
+    k_hull_hull_small<<<d.num_sms * 8, NP_THREADS, 0, s>>>(a, d.max_pairs);
     k_hull_hull<<<d.num_sms * 16, HH_WARPS * 32, 0, s>>>(a, d.max_pairs);
     long long ll = 0;
     int* d_np = &d.counters->pad[0];
@@ -617,7 +751,7 @@ int launch_contacts(DeviceState& d, float friction, cudaStream_t s) {
                        &ll);
     k_manifold_list<<<grid, NP_THREADS, 0, s>>>(d.contact_flag, d.contact_index, d_np, d.contact_slots, d.pairs,
                                                 d.manifold_pair, &d.counters->num_points);
-    return 4 + 1 + 1 + (int)ll;
+    return 4 + 2 + 1 + (int)ll;
 }
 
 int launch_compact_contacts(DeviceState& d, cudaStream_t s) {

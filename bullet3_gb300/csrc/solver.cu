@@ -11,16 +11,18 @@
 //   averageVelocities                :1552-1587
 //   solveGroupCacheFriendlyFinish    :1589-1691 (PGS: v += dv; Jacobi: v += (S/count) once per split copy)
 //
-// GB300 design: rows are built one thread per manifold; the iterations run in ONE
-// cooperative persistent kernel with a bounded grid barrier:
-//   PGS    : parallel greedy colouring of manifolds (per round, a manifold takes the colour when it
-//            holds the highest hashed priority on both of its dynamic bodies -- exact per-body claims,
-//            no aliasing), counting sort by colour, then per iteration: contact rows colour by colour,
-//            friction rows colour by colour, one barrier per colour.
+// GB300 design: compact per-point records are built one thread per manifold; the iterations run
+// in ONE cooperative persistent kernel with a bounded grid barrier.  A manifold's whole working
+// set (normal, up to 4 points, both inverse inertias, both body deltas) is loaded up front so the
+// per-manifold latency is one memory round trip, not one per row.
+//   PGS    : Jones-Plassmann greedy colouring of manifolds (a manifold holding the highest hashed
+//            priority on both of its dynamic bodies takes the smallest colour free on both, exact
+//            per-body 64-bit masks), counting sort by colour, then per iteration: contact rows colour
+//            by colour, friction rows colour by colour, one grid barrier per colour.
 //   Jacobi : per iteration: contact rows of every manifold on its own split copies, a per-body
 //            ordered reduction (same summation order as the reference's solver-body pool), friction
-//            rows, reduction.  Split copies live in a per-manifold array, per-body lists come from a
-//            stable radix sort, so the arithmetic matches the sequential reference order.
+//            rows, reduction.  Per-body lists come from a stable radix sort, so the arithmetic
+//            matches the sequential reference order bit for bit.
 #include <cfloat>
 
 #include "common.cuh"
@@ -37,7 +39,7 @@ struct SolverArgs {
     const b3gContact4* slots;
     const int* manifold_pair;
     const int* d_nc;          // number of manifolds
-    SolverRow* rows;          // 12 per manifold
+    SolverPoints sp;
     int4* hdr;                // bodyA, bodyB, active point mask, num points
     float2* inv_mass;         // invMass A, B
     float4* dv;               // per body: [2b] lin, [2b+1] ang (PGS, and Jacobi averaged delta)
@@ -52,6 +54,7 @@ struct SolverArgs {
     int* color_fill;          // B3G_MAX_COLORS + 1
     int* remaining;           // per round
     unsigned long long* claim;
+    unsigned long long* mask;  // per body: colours already taken by its manifolds
     b3gBody* bodies_out;      // velocities written at finish
     DevCounters* counters;
     double* residual_acc;     // 2 per iteration
@@ -104,7 +107,7 @@ __global__ void k_count_manifolds(const b3gContact4* __restrict__ slots, const i
     }
 }
 
-// Row setup: setupContactConstraint + convertContact friction rows.
+// Row setup: setupContactConstraint + convertContact friction rows, stored as compact records.
 __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
     const int nc = *a.d_nc;
     const bool pgs = a.mode == B3G_SOLVER_PGS;
@@ -119,7 +122,6 @@ __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
         int mask = 0;
         a.color[m] = -1;
         a.inv_mass[m] = make_float2(imA, imB);
-        SolverRow* R = a.rows + (size_t)m * 12;
         if (imA == 0.f && imB == 0.f) np = 0;  // static-static: no rows (b3PgsJacobiSolver.cpp:864-866)
         const b3gMat3 IA = a.inertias[iA].invInertiaWorld;
         const b3gMat3 IB = a.inertias[iB].invInertiaWorld;
@@ -131,18 +133,20 @@ __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
             if (imA != 0.f) countA = (float)a.body_count[iA];
             if (imB != 0.f) countB = (float)a.body_count[iB];
         }
+        const float fric = (float)c.frictionCmp / (float)0xffff;
         // getContactPoint: normalised normal
-        v3 n0 = mk3(c.worldNormalOnB.x, c.worldNormalOnB.y, c.worldNormalOnB.z);
-        v3 n = normalize3(n0);
+        v3 n = normalize3(mk3(c.worldNormalOnB.x, c.worldNormalOnB.y, c.worldNormalOnB.z));
+        a.sp.nf[m] = f4(n, fric);
         for (int j = 0; j < np; j++) {
             const float dist = c.worldPosB[j].w;
             if (!(dist <= a.threshold)) continue;
             mask |= 1 << j;
+            const size_t s = (size_t)m * 4 + j;
             const v3 pos2 = mk3(c.worldPosB[j].x, c.worldPosB[j].y, c.worldPosB[j].z);
             const v3 pos1 = pos2 + n * dist;
             const v3 rel1 = pos1 - posA;
             const v3 rel2 = pos2 - posB;
-            // contact row
+            // contact row (setupContactConstraint)
             {
                 v3 torqueAxis0 = cross3(rel1, n);
                 v3 angCompA = imul(IA, torqueAxis0);
@@ -164,15 +168,10 @@ __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
                 else
                     positionalError = -penetration * a.erp / a.dt;
                 float rhs = positionalError * scaled + velocityError * scaled;
-                SolverRow r;
-                r.normal_jac = f4(n, jac);
-                r.r1xn_rhs = f4(r1xn, rhs);
-                r.r2xn_imp = f4(r2xn, 0.f);
-                r.angA_fric = f4(angCompA, (float)c.frictionCmp / (float)0xffff);
-                r.angB_pad = f4(angCompB, 0.f);
-                R[j] = r;
+                a.sp.rel1[s] = f4(rel1, jac);
+                a.sp.rel2[s] = f4(rel2, rhs);
             }
-            // friction rows
+            // friction rows (convertContact: dir2 row first, then dir1)
             {
                 v3 vel1 = linA + cross3(angA, rel1);
                 v3 vel2 = linB + cross3(angB, rel2);
@@ -190,8 +189,8 @@ __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
                 } else {
                     plane_space(n, dir1, dir2);
                 }
-                const float fric = (float)c.frictionCmp / (float)0xffff;
                 v3 dirs[2] = {dir2, dir1};
+                float jacs[2], rhss[2];
                 for (int k = 0; k < 2; k++) {
                     v3 d = dirs[k];
                     v3 r1xn = cross3(rel1, d);
@@ -206,31 +205,27 @@ __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
                     float v2 = -dot3(d, linB) + dot3(r2xn, angB);
                     float rv = v1 + v2;
                     float velocityError = 0.0f - rv;
-                    SolverRow r;
-                    r.normal_jac = f4(d, jac);
-                    r.r1xn_rhs = f4(r1xn, velocityError * scaled);
-                    r.r2xn_imp = f4(r2xn, 0.f);
-                    r.angA_fric = f4(angCompA, fric);
-                    r.angB_pad = f4(angCompB, 0.f);
-                    R[4 + 2 * j + k] = r;
+                    jacs[k] = jac;
+                    rhss[k] = velocityError * scaled;
                 }
+                a.sp.dir2[s] = f4(dir2, jacs[0]);
+                a.sp.dir1[s] = f4(dir1, jacs[1]);
+                a.sp.rhsf[s] = make_float2(rhss[0], rhss[1]);
+                a.sp.imp[s] = make_float4(0.f, 0.f, 0.f, 0.f);
             }
         }
         a.hdr[m] = make_int4(iA, iB, mask, np);
     }
 }
 
-// One row against two body deltas; returns the impulse change.
+// One row (resolveSingleConstraintRowLowerLimit / Generic): returns the new applied impulse.
 template <bool FRICTION>
-__device__ __forceinline__ void solve_row(SolverRow& r, float lower, float upper, v3& dlA, v3& daA, v3& dlB, v3& daB,
-                                          float imA, float imB, float& delta_out) {
-    v3 n = xyz(r.normal_jac);
-    float jac = r.normal_jac.w;
-    float rhs = r.r1xn_rhs.w;
-    float applied = r.r2xn_imp.w;
+__device__ __forceinline__ float solve_row(v3 d, float jac, float rhs, float applied, v3 r1xn, v3 r2xn, v3 angA,
+                                           v3 angB, float lower, float upper, v3& dlA, v3& daA, v3& dlB, v3& daB,
+                                           float imA, float imB) {
     float deltaImpulse = rhs - applied * 0.0f;
-    float dv1 = dot3(n, dlA) + dot3(xyz(r.r1xn_rhs), daA);
-    float dv2 = -dot3(n, dlB) + dot3(xyz(r.r2xn_imp), daB);
+    float dv1 = dot3(d, dlA) + dot3(r1xn, daA);
+    float dv2 = -dot3(d, dlB) + dot3(r2xn, daB);
     deltaImpulse -= dv1 * jac;
     deltaImpulse -= dv2 * jac;
     float sum = applied + deltaImpulse;
@@ -243,49 +238,103 @@ __device__ __forceinline__ void solve_row(SolverRow& r, float lower, float upper
     } else {
         applied = sum;
     }
-    r.r2xn_imp.w = applied;
-    dlA = dlA + (n * imA) * deltaImpulse;
-    daA = daA + xyz(r.angA_fric) * deltaImpulse;
-    dlB = dlB + ((-n) * imB) * deltaImpulse;
-    daB = daB + xyz(r.angB_pad) * deltaImpulse;
-    delta_out = deltaImpulse;
+    dlA = dlA + (d * imA) * deltaImpulse;
+    daA = daA + angA * deltaImpulse;
+    dlB = dlB + ((-d) * imB) * deltaImpulse;
+    daB = daB + angB * deltaImpulse;
+    return applied;
 }
 
-// Solve the contact rows (pass 0) or friction rows (pass 1) of manifold m on the given deltas.
-__device__ __forceinline__ void solve_manifold(const SolverArgs& a, int m, int pass, v3& dlA, v3& daA, v3& dlB,
-                                               v3& daB, float imA, float imB, int mask, float& res_d, float& res_l) {
-    SolverRow* R = a.rows + (size_t)m * 12;
+__device__ __forceinline__ b3gMat3 ld_mat(const b3gMat3* p) {
+    b3gMat3 r;
+    const float4* q = reinterpret_cast<const float4*>(p);
+    float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+    r.row[0] = b3gFloat4{a.x, a.y, a.z, a.w};
+    r.row[1] = b3gFloat4{b.x, b.y, b.z, b.w};
+    r.row[2] = b3gFloat4{c.x, c.y, c.z, c.w};
+    return r;
+}
+
+// Contact rows (pass 0) or friction rows (pass 1) of manifold m against the given body deltas.
+__device__ __forceinline__ void solve_manifold(const SolverArgs& a, int m, int pass, const int4& h, float imA,
+                                               float imB, v3& dlA, v3& daA, v3& dlB, v3& daB, float& res_d,
+                                               float& res_l) {
+    const int mask = h.z;
+    const size_t base = (size_t)m * 4;
+    const float4 nf = __ldg(&a.sp.nf[m]);
+    const v3 n = xyz(nf);
+    const b3gMat3 IA = ld_mat(&a.inertias[h.x].invInertiaWorld);
+    const b3gMat3 IB = ld_mat(&a.inertias[h.y].invInertiaWorld);
+    float4 r1[4], r2[4], im[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        if (mask & (1 << j)) {
+            r1[j] = __ldg(&a.sp.rel1[base + j]);
+            r2[j] = __ldg(&a.sp.rel2[base + j]);
+            im[j] = __ldcg(&a.sp.imp[base + j]);
+        }
+    }
     if (pass == 0) {
+#pragma unroll
         for (int j = 0; j < 4; j++) {
             if (!(mask & (1 << j))) continue;
-            SolverRow r = R[j];
-            float old = r.r2xn_imp.w, d;
-            solve_row<false>(r, 0.f, LARGE_UPPER, dlA, daA, dlB, daB, imA, imB, d);
-            R[j].r2xn_imp.w = r.r2xn_imp.w;
-            float nd = r.r2xn_imp.w - old;
+            const v3 rel1 = xyz(r1[j]), rel2 = xyz(r2[j]);
+            v3 r1xn = cross3(rel1, n);
+            v3 ta1 = cross3(rel2, n);
+            v3 r2xn = -ta1;
+            v3 angA = imul(IA, r1xn);
+            v3 angB = imul(IB, -ta1);
+            float old = im[j].x;
+            float nw = solve_row<false>(n, r1[j].w, r2[j].w, old, r1xn, r2xn, angA, angB, 0.f, LARGE_UPPER, dlA, daA,
+                                        dlB, daB, imA, imB);
+            __stcg(&a.sp.imp[base + j].x, nw);
+            float nd = nw - old;
             res_d += nd * nd;
-            res_l += r.r2xn_imp.w * r.r2xn_imp.w;
+            res_l += nw * nw;
         }
     } else {
+        const float fr = nf.w;
+        float4 d2[4], d1[4];
+        float2 rf[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (mask & (1 << j)) {
+                d2[j] = __ldg(&a.sp.dir2[base + j]);
+                d1[j] = __ldg(&a.sp.dir1[base + j]);
+                rf[j] = __ldg(&a.sp.rhsf[base + j]);
+            }
+        }
+#pragma unroll
         for (int j = 0; j < 4; j++) {
             if (!(mask & (1 << j))) continue;
-            float totalImpulse = R[j].r2xn_imp.w;
-            for (int k = 0; k < 2; k++) {
-                SolverRow& rr = R[4 + 2 * j + k];
-                if (totalImpulse > 0.f) {
-                    SolverRow r = rr;
-                    float fr = r.angA_fric.w;
-                    float lower = -(fr * totalImpulse);
-                    float upper = fr * totalImpulse;
-                    float old = r.r2xn_imp.w, d;
-                    solve_row<true>(r, lower, upper, dlA, daA, dlB, daB, imA, imB, d);
-                    rr.r2xn_imp.w = r.r2xn_imp.w;
-                    float nd = r.r2xn_imp.w - old;
+            const float total = im[j].x;
+            const v3 rel1 = xyz(r1[j]), rel2 = xyz(r2[j]);
+            float f2 = im[j].y, f1 = im[j].z;
+            if (total > 0.f) {
+                const float lower = -(fr * total), upper = fr * total;
+                {
+                    v3 d = xyz(d2[j]);
+                    v3 r1xn = cross3(rel1, d);
+                    v3 r2xn = cross3(rel2, -d);
+                    float nw = solve_row<true>(d, d2[j].w, rf[j].x, f2, r1xn, r2xn, imul(IA, r1xn), imul(IB, r2xn),
+                                               lower, upper, dlA, daA, dlB, daB, imA, imB);
+                    float nd = nw - f2;
                     res_d += nd * nd;
+                    f2 = nw;
                 }
-                float l = rr.r2xn_imp.w;
-                res_l += l * l;
+                {
+                    v3 d = xyz(d1[j]);
+                    v3 r1xn = cross3(rel1, d);
+                    v3 r2xn = cross3(rel2, -d);
+                    float nw = solve_row<true>(d, d1[j].w, rf[j].y, f1, r1xn, r2xn, imul(IA, r1xn), imul(IB, r2xn),
+                                               lower, upper, dlA, daA, dlB, daB, imA, imB);
+                    float nd = nw - f1;
+                    res_d += nd * nd;
+                    f1 = nw;
+                }
+                __stcg(&a.sp.imp[base + j], make_float4(total, f2, f1, 0.f));
             }
+            res_l += f2 * f2 + f1 * f1;
         }
     }
 }
@@ -322,14 +371,42 @@ __device__ __forceinline__ unsigned int hash32(unsigned int x) {
     return x;
 }
 
+__device__ __forceinline__ void load_dv(const SolverArgs& a, int b, v3& l, v3& w) {
+    l = xyz(__ldcg(&a.dv[2 * b]));
+    w = xyz(__ldcg(&a.dv[2 * b + 1]));
+}
+__device__ __forceinline__ void store_dv(const SolverArgs& a, int b, v3 l, v3 w) {
+    __stcg(&a.dv[2 * b], f4(l, 0.f));
+    __stcg(&a.dv[2 * b + 1], f4(w, 0.f));
+}
+
+// residual bookkeeping shared by both kernels; returns true when the tolerance stops the solve
+__device__ __forceinline__ bool end_iteration(const SolverArgs& a, int it, float res_d, float res_l, bool& ok) {
+    block_accumulate(a.residual_acc + 2 * it, res_d, res_l);
+    if (!grid_barrier(a.bar, gridDim.x, a.spin_limit)) {
+        ok = false;
+        return true;
+    }
+    double dd = *((volatile double*)&a.residual_acc[2 * it]);
+    double ll = *((volatile double*)&a.residual_acc[2 * it + 1]);
+    double r = sqrt(dd) / fmax(sqrt(ll), 1e-12);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.counters->residual = (float)r;
+        a.counters->iterations = it + 1;
+    }
+    return a.residual_tol > 0.f && r <= (double)a.residual_tol;
+}
+
 // ------------------------------------------------------------------ persistent PGS kernel
 __global__ void __launch_bounds__(SV_THREADS) k_solve_pgs(SolverArgs a) {
     const int nc = *a.d_nc;
     const unsigned nb = gridDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int stride = gridDim.x * blockDim.x;
-    // ---- colouring
-    int ncolors = 0;
+    // ---- colouring: Jones-Plassmann greedy.  Per round a manifold that holds the highest hashed
+    // priority on both of its dynamic bodies takes the smallest colour used by neither body (exact
+    // per-body 64-bit masks, no aliasing); statics never conflict.
+    int rounds = 0;
     for (int r = 0; r < B3G_MAX_COLORS; r++) {
         const unsigned long long rk = (unsigned long long)r << 56;
         for (int m = tid; m < nc; m += stride) {
@@ -347,11 +424,21 @@ __global__ void __launch_bounds__(SV_THREADS) k_solve_pgs(SolverArgs a) {
             int4 h = a.hdr[m];
             float2 im = a.inv_mass[m];
             unsigned long long key = rk | ((unsigned long long)(hash32((unsigned)m) & 0xFFFFFFu) << 32) | (unsigned)m;
-            bool okA = im.x == 0.f || a.claim[h.x] == key;
-            bool okB = im.y == 0.f || a.claim[h.y] == key;
+            bool okA = im.x == 0.f || __ldcg(&a.claim[h.x]) == key;
+            bool okB = im.y == 0.f || __ldcg(&a.claim[h.y]) == key;
             if (okA && okB) {
-                a.color[m] = r;
-                atomicAdd(&a.color_fill[r], 1);
+                unsigned long long used = 0ull;
+                if (im.x != 0.f) used |= __ldcg(&a.mask[h.x]);
+                if (im.y != 0.f) used |= __ldcg(&a.mask[h.y]);
+                int c = __ffsll((long long)~used) - 1;
+                if (c >= 0 && c < 64) {
+                    a.color[m] = c;
+                    atomicAdd(&a.color_fill[c], 1);
+                    if (im.x != 0.f) atomicOr(&a.mask[h.x], 1ull << c);
+                    if (im.y != 0.f) atomicOr(&a.mask[h.y], 1ull << c);
+                } else {
+                    left++;
+                }
             } else {
                 left++;
             }
@@ -359,10 +446,14 @@ __global__ void __launch_bounds__(SV_THREADS) k_solve_pgs(SolverArgs a) {
         for (int o = 16; o; o >>= 1) left += __shfl_xor_sync(0xffffffffu, left, o);
         if ((threadIdx.x & 31) == 0 && left) atomicAdd(&a.remaining[r], left);
         if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
-        ncolors = r + 1;
+        rounds = r + 1;
         if (*((volatile int*)&a.remaining[r]) == 0) break;
     }
-    const bool overflow = *((volatile int*)&a.remaining[ncolors - 1 < 0 ? 0 : ncolors - 1]) != 0 && nc > 0;
+    int ncolors = 0;
+    for (int c = 0; c < 64; c++)
+        if (*((volatile int*)&a.color_fill[c]) > 0) ncolors = c + 1;
+    if (ncolors == 0) ncolors = 1;
+    const bool overflow = rounds > 0 && *((volatile int*)&a.remaining[rounds - 1]) != 0 && nc > 0;
     // ---- counting sort by colour (order inside a colour is irrelevant: its manifolds are independent)
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         int s = 0;
@@ -382,65 +473,53 @@ __global__ void __launch_bounds__(SV_THREADS) k_solve_pgs(SolverArgs a) {
     }
     if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
     // ---- iterations
-    int it = 0;
-    for (; it < a.iterations; it++) {
+    bool ok = true;
+    for (int it = 0; it < a.iterations; it++) {
         float res_d = 0.f, res_l = 0.f;
         for (int pass = 0; pass < 2; pass++) {
             for (int c = 0; c < ncolors; c++) {
-                const int lo = a.color_offsets[c], hi = a.color_offsets[c + 1];
+                const int lo = __ldcg(&a.color_offsets[c]), hi = __ldcg(&a.color_offsets[c + 1]);
                 for (int k = lo + tid; k < hi; k += stride) {
-                    const int m = a.color_order[k];
+                    const int m = __ldcg(&a.color_order[k]);
                     const int4 h = a.hdr[m];
                     if (!h.z) continue;
                     const float2 im = a.inv_mass[m];
-                    v3 dlA = xyz(a.dv[2 * h.x]), daA = xyz(a.dv[2 * h.x + 1]);
-                    v3 dlB = xyz(a.dv[2 * h.y]), daB = xyz(a.dv[2 * h.y + 1]);
-                    solve_manifold(a, m, pass, dlA, daA, dlB, daB, im.x, im.y, h.z, res_d, res_l);
-                    if (im.x != 0.f) {
-                        a.dv[2 * h.x] = f4(dlA, 0.f);
-                        a.dv[2 * h.x + 1] = f4(daA, 0.f);
-                    }
-                    if (im.y != 0.f) {
-                        a.dv[2 * h.y] = f4(dlB, 0.f);
-                        a.dv[2 * h.y + 1] = f4(daB, 0.f);
-                    }
+                    v3 dlA, daA, dlB, daB;
+                    load_dv(a, h.x, dlA, daA);
+                    load_dv(a, h.y, dlB, daB);
+                    solve_manifold(a, m, pass, h, im.x, im.y, dlA, daA, dlB, daB, res_d, res_l);
+                    if (im.x != 0.f) store_dv(a, h.x, dlA, daA);
+                    if (im.y != 0.f) store_dv(a, h.y, dlB, daB);
                 }
                 if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
             }
             // colour-overflow leftovers: one thread, in manifold order (always correct, slow)
-            if (overflow && tid == 0) {
-                for (int m = 0; m < nc; m++) {
-                    if (a.color[m] >= 0) continue;
-                    const int4 h = a.hdr[m];
-                    if (!h.z) continue;
-                    const float2 im = a.inv_mass[m];
-                    v3 dlA = xyz(a.dv[2 * h.x]), daA = xyz(a.dv[2 * h.x + 1]);
-                    v3 dlB = xyz(a.dv[2 * h.y]), daB = xyz(a.dv[2 * h.y + 1]);
-                    solve_manifold(a, m, pass, dlA, daA, dlB, daB, im.x, im.y, h.z, res_d, res_l);
-                    if (im.x != 0.f) { a.dv[2 * h.x] = f4(dlA, 0.f); a.dv[2 * h.x + 1] = f4(daA, 0.f); }
-                    if (im.y != 0.f) { a.dv[2 * h.y] = f4(dlB, 0.f); a.dv[2 * h.y + 1] = f4(daB, 0.f); }
+            if (overflow) {
+                if (tid == 0) {
+                    for (int m = 0; m < nc; m++) {
+                        if (a.color[m] >= 0) continue;
+                        const int4 h = a.hdr[m];
+                        if (!h.z) continue;
+                        const float2 im = a.inv_mass[m];
+                        v3 dlA, daA, dlB, daB;
+                        load_dv(a, h.x, dlA, daA);
+                        load_dv(a, h.y, dlB, daB);
+                        solve_manifold(a, m, pass, h, im.x, im.y, dlA, daA, dlB, daB, res_d, res_l);
+                        if (im.x != 0.f) store_dv(a, h.x, dlA, daA);
+                        if (im.y != 0.f) store_dv(a, h.y, dlB, daB);
+                    }
                 }
+                if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
             }
-            if (overflow && !grid_barrier(a.bar, nb, a.spin_limit)) return;
         }
-        block_accumulate(a.residual_acc + 2 * it, res_d, res_l);
-        if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
-        double dd = *((volatile double*)&a.residual_acc[2 * it]);
-        double ll = *((volatile double*)&a.residual_acc[2 * it + 1]);
-        double r = sqrt(dd) / fmax(sqrt(ll), 1e-12);
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            a.counters->residual = (float)r;
-            a.counters->iterations = it + 1;
-        }
-        if (a.residual_tol > 0.f && r <= (double)a.residual_tol) {
-            it++;
-            break;
-        }
+        if (end_iteration(a, it, res_d, res_l, ok)) break;
     }
+    if (!ok) return;
     // ---- finish: v += dv for dynamic bodies
     for (int b = tid; b < a.num_bodies; b += stride) {
         if (a.bodies[b].invMass == 0.f) continue;
-        v3 dl = xyz(a.dv[2 * b]), da = xyz(a.dv[2 * b + 1]);
+        v3 dl, da;
+        load_dv(a, b, dl, da);
         b3gBody& B = a.bodies_out[b];
         B.linVel.x = B.linVel.x + dl.x;
         B.linVel.y = B.linVel.y + dl.y;
@@ -461,14 +540,13 @@ __device__ __forceinline__ void jacobi_average(const SolverArgs& a, int tid, int
         for (int k = 0; k < cnt; k++) {
             uint32_t e = a.list[off + k];
             uint32_t m = e >> 1, side = e & 1u;
-            sl = sl + xyz(a.split[4 * m + 2 * side]);
-            sa = sa + xyz(a.split[4 * m + 2 * side + 1]);
+            sl = sl + xyz(__ldcg(&a.split[4 * m + 2 * side]));
+            sa = sa + xyz(__ldcg(&a.split[4 * m + 2 * side + 1]));
         }
         float factor = 1.f / (float)cnt;
         a.dv_sum[2 * b] = f4(sl, 0.f);
         a.dv_sum[2 * b + 1] = f4(sa, 0.f);
-        a.dv[2 * b] = f4(sl * factor, 0.f);
-        a.dv[2 * b + 1] = f4(sa * factor, 0.f);
+        store_dv(a, b, sl * factor, sa * factor);
     }
 }
 
@@ -478,40 +556,29 @@ __global__ void __launch_bounds__(SV_THREADS) k_solve_jacobi(SolverArgs a) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int stride = gridDim.x * blockDim.x;
     if (blockIdx.x == 0 && threadIdx.x == 0) a.counters->num_colors = 0;
-    int it = 0;
-    for (; it < a.iterations; it++) {
+    bool ok = true;
+    for (int it = 0; it < a.iterations; it++) {
         float res_d = 0.f, res_l = 0.f;
         for (int pass = 0; pass < 2; pass++) {
             for (int m = tid; m < nc; m += stride) {
                 const int4 h = a.hdr[m];
                 const float2 im = a.inv_mass[m];
                 v3 dlA = mk3(0, 0, 0), daA = mk3(0, 0, 0), dlB = mk3(0, 0, 0), daB = mk3(0, 0, 0);
-                if (im.x != 0.f) { dlA = xyz(a.dv[2 * h.x]); daA = xyz(a.dv[2 * h.x + 1]); }
-                if (im.y != 0.f) { dlB = xyz(a.dv[2 * h.y]); daB = xyz(a.dv[2 * h.y + 1]); }
-                if (h.z) solve_manifold(a, m, pass, dlA, daA, dlB, daB, im.x, im.y, h.z, res_d, res_l);
-                a.split[4 * m + 0] = f4(dlA, 0.f);
-                a.split[4 * m + 1] = f4(daA, 0.f);
-                a.split[4 * m + 2] = f4(dlB, 0.f);
-                a.split[4 * m + 3] = f4(daB, 0.f);
+                if (im.x != 0.f) load_dv(a, h.x, dlA, daA);
+                if (im.y != 0.f) load_dv(a, h.y, dlB, daB);
+                if (h.z) solve_manifold(a, m, pass, h, im.x, im.y, dlA, daA, dlB, daB, res_d, res_l);
+                __stcg(&a.split[4 * m + 0], f4(dlA, 0.f));
+                __stcg(&a.split[4 * m + 1], f4(daA, 0.f));
+                __stcg(&a.split[4 * m + 2], f4(dlB, 0.f));
+                __stcg(&a.split[4 * m + 3], f4(daB, 0.f));
             }
             if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
             jacobi_average(a, tid, stride);
             if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
         }
-        block_accumulate(a.residual_acc + 2 * it, res_d, res_l);
-        if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
-        double dd = *((volatile double*)&a.residual_acc[2 * it]);
-        double ll = *((volatile double*)&a.residual_acc[2 * it + 1]);
-        double r = sqrt(dd) / fmax(sqrt(ll), 1e-12);
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            a.counters->residual = (float)r;
-            a.counters->iterations = it + 1;
-        }
-        if (a.residual_tol > 0.f && r <= (double)a.residual_tol) {
-            it++;
-            break;
-        }
+        if (end_iteration(a, it, res_d, res_l, ok)) break;
     }
+    if (!ok) return;
     // finish: body velocity += (S * 1/count), applied once per split copy
     for (int b = tid; b < a.num_bodies; b += stride) {
         const int cnt = a.body_count[b];
@@ -544,12 +611,13 @@ __global__ void k_reset_solver(int* color_fill, int* remaining, unsigned int* ba
     }
 }
 
-static int solver_grid(DeviceState& d, const void* fn) {
+static int solver_grid(DeviceState& d, const void* fn, int blocks_per_sm) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, SV_THREADS, 0);
     if (per_sm < 1) per_sm = 1;
-    if (per_sm > 4) per_sm = 4;
-    return per_sm * d.num_sms;
+    int want = blocks_per_sm > 0 ? blocks_per_sm : 2;
+    if (want > per_sm) want = per_sm;  // cooperative launch: every block must be co-resident
+    return want * d.num_sms;
 }
 
 int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s) {
@@ -562,7 +630,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     int* d_n2 = &d.counters->pad[1];
     // per-step resets
     cudaMemsetAsync(d.dv, 0, sizeof(float4) * 2 * (size_t)d.num_bodies, s);
-    cudaMemsetAsync(d.color_claim, 0, sizeof(unsigned long long) * (size_t)d.num_bodies, s);
+    cudaMemsetAsync(d.color_claim, 0, sizeof(unsigned long long) * 2 * (size_t)d.num_bodies, s);
     cudaMemsetAsync(d.body_manifold_count, 0, sizeof(int) * (size_t)d.num_bodies, s);
     int* color_fill = d.color_offsets + (B3G_MAX_COLORS + 2);
     int* remaining = color_fill + (B3G_MAX_COLORS + 1);
@@ -575,7 +643,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     a.slots = d.contact_slots;
     a.manifold_pair = d.manifold_pair;
     a.d_nc = d_nc;
-    a.rows = d.rows;
+    a.sp = d.sp;
     a.hdr = d.manifold_hdr;
     a.inv_mass = d.manifold_inv_mass;
     a.dv = d.dv;
@@ -590,6 +658,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     a.color_fill = color_fill;
     a.remaining = remaining;
     a.claim = d.color_claim;
+    a.mask = d.color_claim + d.num_bodies;
     a.bodies_out = d.bodies;
     a.counters = d.counters;
     a.residual_acc = d.residual_acc;
@@ -621,8 +690,9 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     k_setup_rows<<<grid, SV_THREADS, 0, s>>>(a);
     launches++;
 
-    const void* fn = cfg.solver_mode == B3G_SOLVER_JACOBI ? (const void*)k_solve_jacobi : (const void*)k_solve_pgs;
-    int sgrid = solver_grid(d, fn);
+    const bool jac = cfg.solver_mode == B3G_SOLVER_JACOBI;
+    const void* fn = jac ? (const void*)k_solve_jacobi : (const void*)k_solve_pgs;
+    int sgrid = solver_grid(d, fn, cfg.reserved[0]);
     cudaLaunchConfig_t lc = {};
     lc.gridDim = dim3(sgrid);
     lc.blockDim = dim3(SV_THREADS);
@@ -632,11 +702,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     attr[0].val.cooperative = 1;
     lc.attrs = attr;
     lc.numAttrs = 1;
-    cudaError_t e;
-    if (cfg.solver_mode == B3G_SOLVER_JACOBI)
-        e = cudaLaunchKernelEx(&lc, k_solve_jacobi, a);
-    else
-        e = cudaLaunchKernelEx(&lc, k_solve_pgs, a);
+    cudaError_t e = jac ? cudaLaunchKernelEx(&lc, k_solve_jacobi, a) : cudaLaunchKernelEx(&lc, k_solve_pgs, a);
     if (e != cudaSuccess && d.launch_error == cudaSuccess) d.launch_error = e;
     launches++;
     return launches + (int)ll;

@@ -423,7 +423,7 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     d.grid_bits = bits_for(d.grid_dim);
     d.body_bits = bits_for(N + 1);
     if (2 * d.body_bits > 64) return fail(B3G_ERR_CAPACITY, "too many bodies");
-    d.max_pairs = h->cfg.max_pairs > 0 ? h->cfg.max_pairs : std::max(1024, 12 * N);
+    d.max_pairs = h->cfg.max_pairs > 0 ? h->cfg.max_pairs : std::max(4096, 24 * N);
     // at most one manifold per pair: contact storage is sized with the pair capacity so that no
     // manifold index can exceed it
     d.max_contacts = d.max_pairs;
@@ -443,6 +443,7 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     TRY(dalloc(h, &d.vertices, nvx));
     TRY(dalloc(h, &d.edges, ne));
     TRY(dalloc(h, &d.dyn_slot, N));
+    TRY(dalloc(h, &d.col_small, d.num_collidables));
     TRY(dalloc(h, &d.large_list, std::max(1, d.num_large)));
     TRY(dalloc(h, &d.aabbs, N));
     for (int k = 0; k < 2; k++) {
@@ -461,11 +462,17 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     TRY(dalloc(h, &d.contact_index, d.max_pairs));
     TRY(dalloc(h, &d.manifold_pair, d.max_pairs));
     TRY(dalloc(h, &d.contacts_compact, d.max_contacts));
-    TRY(dalloc(h, &d.rows, (size_t)12 * d.max_contacts));
+    TRY(dalloc(h, &d.sp.nf, d.max_contacts));
+    TRY(dalloc(h, &d.sp.rel1, 4 * (size_t)d.max_contacts));
+    TRY(dalloc(h, &d.sp.rel2, 4 * (size_t)d.max_contacts));
+    TRY(dalloc(h, &d.sp.dir2, 4 * (size_t)d.max_contacts));
+    TRY(dalloc(h, &d.sp.dir1, 4 * (size_t)d.max_contacts));
+    TRY(dalloc(h, &d.sp.rhsf, 4 * (size_t)d.max_contacts));
+    TRY(dalloc(h, &d.sp.imp, 4 * (size_t)d.max_contacts));
     TRY(dalloc(h, &d.manifold_color, d.max_contacts));
     TRY(dalloc(h, &d.color_order, d.max_contacts));
     TRY(dalloc(h, &d.color_offsets, 3 * (B3G_MAX_COLORS + 2)));
-    TRY(dalloc(h, &d.color_claim, N));
+    TRY(dalloc(h, &d.color_claim, 2 * (size_t)N));  // claims, then colour masks
     TRY(dalloc(h, &d.dv, 2 * (size_t)N));
     TRY(dalloc(h, &d.dv_sum, 2 * (size_t)N));
     TRY(dalloc(h, &d.manifold_hdr, d.max_contacts));
@@ -505,6 +512,18 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     if (!h->edges.empty())
         CUDA_TRY(cudaMemcpyAsync(d.edges, h->edges.data(), sizeof(b3gFloat4) * h->edges.size(), cudaMemcpyHostToDevice, s));
     CUDA_TRY(cudaMemcpyAsync(d.dyn_slot, dyn_slot.data(), sizeof(int) * N, cudaMemcpyHostToDevice, s));
+    std::vector<int> col_small(d.num_collidables, 0);
+    for (int c = 0; c < d.num_collidables; c++) {
+        const b3gCollidable& col = h->collidables[c];
+        if (col.shapeType != B3G_SHAPE_CONVEX_HULL) continue;
+        const b3gHull& hull = h->hulls[col.shapeIndex];
+        int small = 1;
+        for (int f = 0; f < hull.numFaces; f++)
+            if (h->faces[hull.faceOffset + f].numIndices > B3G_SMALL_FACE_VERTS) small = 0;
+        col_small[c] = small;
+    }
+    CUDA_TRY(cudaMemcpyAsync(d.col_small, col_small.data(), sizeof(int) * d.num_collidables, cudaMemcpyHostToDevice,
+                             s));
     if (!large.empty())
         CUDA_TRY(cudaMemcpyAsync(d.large_list, large.data(), sizeof(int) * large.size(), cudaMemcpyHostToDevice, s));
     int sizes[4] = {nd, N, 0, 0};
@@ -808,12 +827,13 @@ extern "C" b3gStatus b3g_read_batches(b3g_handle h, int* host, int capacity, int
     return B3G_OK;
 }
 
-__global__ void k_gather_impulses(const SolverRow* __restrict__ rows, int n, float* __restrict__ out) {
+__global__ void k_gather_impulses(const float4* __restrict__ imp, int n, float* __restrict__ out) {
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
         for (int j = 0; j < 4; j++) {
-            out[(size_t)m * 12 + 3 * j + 0] = rows[(size_t)m * 12 + j].r2xn_imp.w;
-            out[(size_t)m * 12 + 3 * j + 1] = rows[(size_t)m * 12 + 4 + 2 * j + 1].r2xn_imp.w;  // lateral dir 1
-            out[(size_t)m * 12 + 3 * j + 2] = rows[(size_t)m * 12 + 4 + 2 * j + 0].r2xn_imp.w;  // lateral dir 2
+            float4 v = imp[(size_t)m * 4 + j];
+            out[(size_t)m * 12 + 3 * j + 0] = v.x;  // normal
+            out[(size_t)m * 12 + 3 * j + 1] = v.z;  // lateral dir 1
+            out[(size_t)m * 12 + 3 * j + 2] = v.y;  // lateral dir 2
         }
     }
 }
@@ -828,7 +848,7 @@ extern "C" b3gStatus b3g_read_impulses(b3g_handle h, float* host, int capacity, 
     if (host && n > 0) {
         float* tmp = nullptr;
         CUDA_TRY(cudaMalloc(&tmp, sizeof(float) * 12 * (size_t)n));
-        k_gather_impulses<<<h->d.num_sms * 2, 256, 0, h->stream>>>(h->d.rows, n, tmp);
+        k_gather_impulses<<<h->d.num_sms * 2, 256, 0, h->stream>>>(h->d.sp.imp, n, tmp);
         b3gStatus st = copy_out(h, host, tmp, sizeof(float) * 12 * (size_t)n);
         cudaFree(tmp);
         return st;

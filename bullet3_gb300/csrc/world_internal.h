@@ -11,8 +11,11 @@
 
 namespace b3g {
 
+// hull-hull pairs whose faces all have at most this many vertices take the thread-per-pair path
+#define B3G_SMALL_FACE_VERTS 8
+
 enum PairType { PT_HULL_HULL = 0, PT_PLANE_HULL = 1, PT_SPHERE_HULL = 2, PT_SPHERE_SPHERE = 3, PT_PLANE_SPHERE = 4,
-                PT_COUNT = 5 };
+                PT_HULL_HULL_SMALL = 5, PT_COUNT = 6 };
 
 // Per-step device counters (one 256-byte block, copied to the host once per step).
 struct DevCounters {
@@ -24,17 +27,21 @@ struct DevCounters {
     float residual;
     unsigned int status;
     int type_count[PT_COUNT];
-    int pad[64 - 12];
+    int pad[64 - 7 - PT_COUNT];
 };
 
-// Solver row: b3SolverConstraint reduced to what a contact/friction row uses
-// (Bullet3Dynamics/ConstraintSolver/b3SolverConstraint.h).
-struct SolverRow {
-    float4 normal_jac;   // contact normal (or friction direction) xyz, w = jacDiagABInv
-    float4 r1xn_rhs;     // relpos1CrossNormal xyz, w = rhs
-    float4 r2xn_imp;     // relpos2CrossNormal xyz, w = applied impulse
-    float4 angA_fric;    // angularComponentA xyz, w = friction coefficient
-    float4 angB_pad;     // angularComponentB xyz, w = 0
+// Compact solver records.  A b3SolverConstraint row (Bullet3Dynamics/ConstraintSolver/
+// b3SolverConstraint.h) is rebuilt on the fly from these: relpos x axis and the inverse-inertia
+// products are recomputed with the same operations the setup used, so the iterations see the
+// same values as precomputed rows while reading 88 B per contact point instead of 240 B.
+struct SolverPoints {
+    float4* nf = nullptr;    // [m]      contact normal xyz, w = friction coefficient
+    float4* rel1 = nullptr;  // [4m+j]   rel_pos1 xyz, w = jacDiagABInv of the contact row
+    float4* rel2 = nullptr;  // [4m+j]   rel_pos2 xyz, w = rhs of the contact row
+    float4* dir2 = nullptr;  // [4m+j]   second friction direction xyz, w = its jacDiagABInv
+    float4* dir1 = nullptr;  // [4m+j]   first friction direction xyz, w = its jacDiagABInv
+    float2* rhsf = nullptr;  // [4m+j]   rhs of the dir2 row, rhs of the dir1 row
+    float4* imp = nullptr;   // [4m+j]   applied impulses: contact, dir2, dir1, (unused)
 };
 
 struct DeviceState {
@@ -53,6 +60,7 @@ struct DeviceState {
     b3gFloat4* vertices = nullptr;
     b3gFloat4* edges = nullptr;
     int* dyn_slot = nullptr;      // body -> dynamic slot or -1
+    int* col_small = nullptr;     // per collidable: 1 = hull whose faces all have <= B3G_SMALL_FACE_VERTS vertices
     int* large_list = nullptr;    // static bodies (large proxies)
     // broadphase
     b3gAabb* aabbs = nullptr;
@@ -72,7 +80,7 @@ struct DeviceState {
     int* manifold_pair = nullptr;          // manifold -> pair index
     b3gContact4* contacts_compact = nullptr;  // filled on demand for the drop-in getter
     // solver
-    SolverRow* rows = nullptr;             // 12 rows per manifold: 4 contact, 8 friction
+    SolverPoints sp;                       // compact contact-point records
     int* manifold_color = nullptr;
     int* color_order = nullptr;            // manifolds sorted by colour
     int* color_offsets = nullptr;          // B3G_MAX_COLORS + 1

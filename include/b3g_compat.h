@@ -1,0 +1,203 @@
+/*
+ * b3g_compat.h -- header-only C++ drop-in for the reference's GPU rigid-body API, implemented on
+ * the C ABI of libb3gpu.so (include/b3g_capi.h).
+ *
+ * Class names, method names, argument meaning and error behaviour follow
+ *   b3GpuNarrowPhase         src/Bullet3OpenCL/RigidBody/b3GpuNarrowPhase.h:9-99
+ *   b3GpuBroadphaseInterface src/Bullet3OpenCL/BroadphaseCollision/b3GpuBroadphaseInterface.h:12-40
+ *   b3GpuGridBroadphase      src/Bullet3OpenCL/BroadphaseCollision/b3GpuGridBroadphase.h
+ *   b3GpuRigidBodyPipeline   src/Bullet3OpenCL/RigidBody/b3GpuRigidBodyPipeline.h:25-67
+ *   b3Config                 src/Bullet3OpenCL/RigidBody/b3Config.h:4-37
+ * The OpenCL handles of the reference constructors (cl_context, cl_device_id, cl_command_queue)
+ * become a CUDA device ordinal; cl_mem results become device pointers (void*).  Indices the
+ * reference reports as -1 + b3Error are reported the same way (message on stderr); CUDA failures
+ * are reported through b3g_last_error().  Like the reference, the pipeline does not own the
+ * narrowphase or broadphase objects.
+ */
+#ifndef B3G_COMPAT_H
+#define B3G_COMPAT_H
+
+#include <cstdio>
+#include <vector>
+
+#include "b3g_capi.h"
+
+namespace b3g_compat {
+
+inline void b3Error(const char* what) { std::fprintf(stderr, "b3Error: %s: %s\n", what, b3g_last_error()); }
+
+struct b3Config {
+    int m_maxConvexBodies = 128 * 1024;
+    int m_maxConvexShapes = 8 * 1024;
+    int m_maxBroadphasePairs = 0;
+    int m_maxContactCapacity = 0;
+    b3gConfig toC() const {
+        b3gConfig c;
+        b3g_config_default(&c);
+        c.max_bodies = m_maxConvexBodies;
+        c.max_shapes = m_maxConvexShapes;
+        c.max_pairs = m_maxBroadphasePairs;
+        c.max_contacts = m_maxContactCapacity;
+        return c;
+    }
+};
+
+class b3GpuNarrowPhase {
+public:
+    b3GpuNarrowPhase(int cudaDevice, const b3Config& config) : m_config(config) {
+        b3gConfig c = config.toC();
+        if (b3g_create(&c, cudaDevice, &m_world) != B3G_OK) {
+            b3Error("b3GpuNarrowPhase");
+            m_world = nullptr;
+        }
+    }
+    virtual ~b3GpuNarrowPhase() {
+        if (m_world) b3g_destroy(m_world);
+    }
+    int registerSphereShape(float radius) { return reg(b3g_register_sphere(m_world, radius, &m_out), "registerSphereShape"); }
+    int registerPlaneShape(const float planeNormal[3], float planeConstant) {
+        return reg(b3g_register_plane(m_world, planeNormal, planeConstant, &m_out), "registerPlaneShape");
+    }
+    int registerConvexHullShape(const float* vertices, int strideInBytes, int numVertices, const float* scaling) {
+        return reg(b3g_register_hull(m_world, vertices, strideInBytes, numVertices, scaling, &m_out),
+                   "registerConvexHullShape");
+    }
+    int registerCompoundShape(void*) {
+        std::fprintf(stderr, "b3Error: registerCompoundShape: compound shapes are not supported\n");
+        return -1;
+    }
+    int registerConcaveMesh(void*, void*, const float*) {
+        std::fprintf(stderr, "b3Error: registerConcaveMesh: concave meshes are not supported\n");
+        return -1;
+    }
+    void writeAllBodiesToGpu() {
+        if (b3g_write_all_to_gpu(m_world) != B3G_OK) b3Error("writeAllBodiesToGpu");
+    }
+    int getNumRigidBodies() const {
+        int n = 0;
+        b3g_get_num_bodies(m_world, &n);
+        return n;
+    }
+    void readbackAllBodiesToCpu(std::vector<b3gBody>& out) {
+        out.resize(getNumRigidBodies());
+        if (b3g_read_bodies(m_world, out.data(), (int)out.size()) != B3G_OK) b3Error("readbackAllBodiesToCpu");
+    }
+    void computeContacts() {
+        if (b3g_compute_contacts(m_world) != B3G_OK) b3Error("computeContacts");
+    }
+    void* getBodiesGpu() {
+        void* p = nullptr;
+        b3g_get_body_buffer(m_world, &p);
+        return p;
+    }
+    void* getBodyInertiasGpu() {
+        void* p = nullptr;
+        b3g_get_inertia_buffer(m_world, &p);
+        return p;
+    }
+    void* getContactsGpu() {
+        void* p = nullptr;
+        int n = 0;
+        b3g_get_contact_buffer(m_world, &p, &n);
+        return p;
+    }
+    int getNumContactsGpu() {
+        void* p = nullptr;
+        int n = 0;
+        b3g_get_contact_buffer(m_world, &p, &n);
+        return n;
+    }
+    b3g_handle world() const { return m_world; }
+
+private:
+    int reg(b3gStatus st, const char* what) {
+        if (st == B3G_OK) return m_out;
+        b3Error(what);
+        return -1;
+    }
+    b3Config m_config;
+    b3g_handle m_world = nullptr;
+    int m_out = -1;
+};
+
+class b3GpuBroadphaseInterface {
+public:
+    virtual ~b3GpuBroadphaseInterface() {}
+    virtual void calculateOverlappingPairs(int maxPairs) = 0;
+    virtual int getNumOverlap() = 0;
+    virtual void* getOverlappingPairBuffer() = 0;
+    virtual void* getAabbBufferWS() = 0;
+};
+
+class b3GpuGridBroadphase : public b3GpuBroadphaseInterface {
+public:
+    explicit b3GpuGridBroadphase(b3GpuNarrowPhase* np = nullptr) : m_np(np) {}
+    void attach(b3GpuNarrowPhase* np) { m_np = np; }
+    void calculateOverlappingPairs(int) override {
+        if (b3g_calculate_overlapping_pairs(m_np->world()) != B3G_OK) b3Error("calculateOverlappingPairs");
+    }
+    int getNumOverlap() override {
+        void* p = nullptr;
+        int n = 0;
+        b3g_get_pair_buffer(m_np->world(), &p, &n);
+        return n;
+    }
+    void* getOverlappingPairBuffer() override {
+        void* p = nullptr;
+        int n = 0;
+        b3g_get_pair_buffer(m_np->world(), &p, &n);
+        return p;
+    }
+    void* getAabbBufferWS() override {
+        void* p = nullptr;
+        b3g_get_aabb_buffer(m_np->world(), &p);
+        return p;
+    }
+
+private:
+    b3GpuNarrowPhase* m_np;
+};
+
+class b3GpuRigidBodyPipeline {
+public:
+    b3GpuRigidBodyPipeline(b3GpuNarrowPhase* narrowphase, b3GpuGridBroadphase* broadphase, void* /*dbvt*/,
+                           const b3Config& config)
+        : m_np(narrowphase), m_bp(broadphase), m_config(config) {
+        if (m_bp) m_bp->attach(narrowphase);
+    }
+    int registerPhysicsInstance(float mass, const float* position, const float* orientation, int collidableIndex,
+                                int userData, bool /*writeInstanceToGpu*/) {
+        int out = -1;
+        if (b3g_register_body(m_np->world(), mass, position, orientation, collidableIndex, userData, &out) != B3G_OK) {
+            b3Error("registerPhysicsInstance");
+            return -1;
+        }
+        return out;
+    }
+    void writeAllInstancesToGpu() { m_np->writeAllBodiesToGpu(); }
+    void setGravity(const float* grav) { b3g_set_gravity(m_np->world(), grav); }
+    void stepSimulation(float deltaTime) {
+        if (b3g_step(m_np->world(), deltaTime) != B3G_OK) b3Error("stepSimulation");
+    }
+    void setupGpuAabbsFull() { b3g_setup_aabbs(m_np->world()); }
+    void integrate(float timeStep) { b3g_integrate(m_np->world(), timeStep); }
+    int getNumBodies() const { return m_np->getNumRigidBodies(); }
+    void* getBodyBuffer() { return m_np->getBodiesGpu(); }
+    int createPoint2PointConstraint(int, int, const float*, const float*, float) {
+        std::fprintf(stderr, "b3Error: createPoint2PointConstraint: joints are not supported\n");
+        return -1;
+    }
+    int createFixedConstraint(int, int, const float*, const float*, const float*, const float*, float) {
+        std::fprintf(stderr, "b3Error: createFixedConstraint: joints are not supported\n");
+        return -1;
+    }
+
+private:
+    b3GpuNarrowPhase* m_np;
+    b3GpuGridBroadphase* m_bp;
+    b3Config m_config;
+};
+
+}  // namespace b3g_compat
+
+#endif
