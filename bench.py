@@ -217,6 +217,7 @@ def gpu_arm(args):
     clocks = ClockSampler(local)
     dist_barrier(dist)
     pl.synchronize()
+    pl.status(clear=True)  # the device status word accumulates over the timed steps
     clocks.start()
     l0 = pl.launchCount()
     capi.call("b3g_record_event", h, C.c_int(0))
@@ -232,8 +233,7 @@ def gpu_arm(args):
     t_rank = ms.value / 1000.0
     t_max = dist_max(dist, t_rank)
     value = world * N * args.steps / t_max
-    st = pl.stats()
-    status = st.status
+    status = pl.status()
 
     # ---- per-stage times (profiled steps after the timed region, events around each stage)
     pl.setProfiling(True)

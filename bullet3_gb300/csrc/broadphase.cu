@@ -14,6 +14,8 @@
 // the pair kernel works in sorted (spatially coherent) order, buffers pairs per thread and
 // reserves output with one warp-aggregated atomic; pairs are then radix-sorted on a packed
 // (a, b) key so the pair list is canonical and deterministic (a < b, ascending).
+#include <cstddef>
+
 #include "common.cuh"
 #include "world_internal.h"
 
@@ -263,7 +265,10 @@ int launch_pairs(DeviceState& d, cudaStream_t s) {
     k_cell_start<<<grid, BP_THREADS, 0, s>>>(keys, d.num_dynamic, d.cell_start);
     launches++;
     // 3. pairs
-    cudaMemsetAsync(d.counters, 0, sizeof(DevCounters), s);
+    // per-step counters restart at zero; the status word accumulates until the host clears it
+    cudaMemsetAsync(d.counters, 0, offsetof(DevCounters, status), s);
+    cudaMemsetAsync(reinterpret_cast<char*>(d.counters) + offsetof(DevCounters, status) + sizeof(unsigned int), 0,
+                    sizeof(DevCounters) - offsetof(DevCounters, status) - sizeof(unsigned int), s);
     k_find_pairs<<<d.num_sms * 8, BP_THREADS, 0, s>>>(d.aabbs, keys, vals, d.cell_start, d.num_dynamic, d.large_list,
                                                       d.num_large, d.inv_cell, d.grid_bits, d.body_bits,
                                                       d.pair_keys[0], &d.counters->num_pairs, d.max_pairs,

@@ -51,7 +51,8 @@ struct SolverArgs {
     int* color;               // per manifold
     int* color_order;
     int* color_offsets;       // B3G_MAX_COLORS + 2
-    int* color_fill;          // B3G_MAX_COLORS + 1
+    int* color_fill;          // B3G_MAX_COLORS + 1: manifolds per colour
+    int* color_cursor;        // B3G_MAX_COLORS + 1: scatter cursors for the counting sort
     int* remaining;           // per round
     unsigned long long* claim;
     unsigned long long* mask;  // per body: colours already taken by its manifolds
@@ -454,13 +455,14 @@ __global__ void __launch_bounds__(SV_THREADS) k_solve_pgs(SolverArgs a) {
         if (*((volatile int*)&a.color_fill[c]) > 0) ncolors = c + 1;
     if (ncolors == 0) ncolors = 1;
     const bool overflow = rounds > 0 && *((volatile int*)&a.remaining[rounds - 1]) != 0 && nc > 0;
-    // ---- counting sort by colour (order inside a colour is irrelevant: its manifolds are independent)
+    // ---- counting sort by colour (order inside a colour is irrelevant: its manifolds are independent).
+    // color_fill stays read-only from here on (every block derived ncolors from it above); the
+    // scatter uses its own cursors, zeroed before the kernel started.
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         int s = 0;
         for (int c = 0; c < ncolors; c++) {
             a.color_offsets[c] = s;
             s += a.color_fill[c];
-            a.color_fill[c] = 0;
         }
         a.color_offsets[ncolors] = s;
         a.counters->num_colors = ncolors;
@@ -469,7 +471,7 @@ __global__ void __launch_bounds__(SV_THREADS) k_solve_pgs(SolverArgs a) {
     if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
     for (int m = tid; m < nc; m += stride) {
         int c = a.color[m];
-        if (c >= 0) a.color_order[a.color_offsets[c] + atomicAdd(&a.color_fill[c], 1)] = m;
+        if (c >= 0) a.color_order[__ldcg(&a.color_offsets[c]) + atomicAdd(&a.color_cursor[c], 1)] = m;
     }
     if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
     // ---- iterations
@@ -596,11 +598,12 @@ __global__ void __launch_bounds__(SV_THREADS) k_solve_jacobi(SolverArgs a) {
     }
 }
 
-__global__ void k_reset_solver(int* color_fill, int* remaining, unsigned int* barrier, double* residual_acc,
-                               int nres, DevCounters* counters) {
+__global__ void k_reset_solver(int* color_fill, int* remaining, int* color_cursor, unsigned int* barrier,
+                               double* residual_acc, int nres, DevCounters* counters) {
     for (int i = threadIdx.x; i < B3G_MAX_COLORS + 1; i += blockDim.x) {
         color_fill[i] = 0;
         remaining[i] = 0;
+        color_cursor[i] = 0;
     }
     for (int i = threadIdx.x; i < nres; i += blockDim.x) residual_acc[i] = 0.0;
     if (threadIdx.x < 4) barrier[threadIdx.x] = 0;
@@ -634,7 +637,9 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     cudaMemsetAsync(d.body_manifold_count, 0, sizeof(int) * (size_t)d.num_bodies, s);
     int* color_fill = d.color_offsets + (B3G_MAX_COLORS + 2);
     int* remaining = color_fill + (B3G_MAX_COLORS + 1);
-    k_reset_solver<<<1, 256, 0, s>>>(color_fill, remaining, d.barrier, d.residual_acc, 2 * iters, d.counters);
+    int* color_cursor = remaining + (B3G_MAX_COLORS + 1);
+    k_reset_solver<<<1, 256, 0, s>>>(color_fill, remaining, color_cursor, d.barrier, d.residual_acc, 2 * iters,
+                                     d.counters);
     launches++;
 
     SolverArgs a;
@@ -656,6 +661,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     a.color_order = d.color_order;
     a.color_offsets = d.color_offsets;
     a.color_fill = color_fill;
+    a.color_cursor = color_cursor;
     a.remaining = remaining;
     a.claim = d.color_claim;
     a.mask = d.color_claim + d.num_bodies;

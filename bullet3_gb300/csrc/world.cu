@@ -471,7 +471,7 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     TRY(dalloc(h, &d.sp.imp, 4 * (size_t)d.max_contacts));
     TRY(dalloc(h, &d.manifold_color, d.max_contacts));
     TRY(dalloc(h, &d.color_order, d.max_contacts));
-    TRY(dalloc(h, &d.color_offsets, 3 * (B3G_MAX_COLORS + 2)));
+    TRY(dalloc(h, &d.color_offsets, 4 * (B3G_MAX_COLORS + 2)));  // offsets, fill, remaining, cursors
     TRY(dalloc(h, &d.color_claim, 2 * (size_t)N));  // claims, then colour masks
     TRY(dalloc(h, &d.dv, 2 * (size_t)N));
     TRY(dalloc(h, &d.dv_sum, 2 * (size_t)N));
