@@ -19,8 +19,11 @@ namespace b3g {
 static constexpr int RS_THREADS = 256;
 static constexpr int RS_WARPS = RS_THREADS / 32;
 static constexpr int RADIX = 256;
+static_assert(RS_THREADS == RADIX, "rs_scatter scans one digit total per thread");
 
-size_t radix_scratch_bytes(const PrimConfig& pc) { return (size_t)RADIX * pc.sort_blocks * sizeof(int) + 256; }
+size_t radix_scratch_bytes(const PrimConfig& pc) {
+    return (size_t)RADIX * pc.sort_blocks * sizeof(int) + RADIX * sizeof(int) + 256;
+}
 size_t scan_scratch_bytes(const PrimConfig& pc) { return (size_t)(2 * pc.scan_blocks + 2) * sizeof(int) + 256; }
 
 template <typename K>
@@ -80,11 +83,47 @@ __global__ void __launch_bounds__(1024) scan_small(int* __restrict__ a, int len,
     if (total && threadIdx.x == T - 1) *total = sums[T - 1];
 }
 
+// One block per digit: exclusive scan of that digit's per-block counts (in place) and the
+// digit total.  Replaces a one-block scan of the whole digit-major table.
+__global__ void __launch_bounds__(RS_THREADS) rs_digit_scan(int* __restrict__ hist, int G,
+                                                            int* __restrict__ digit_total) {
+    __shared__ int wsum[RS_WARPS];
+    __shared__ int carry;
+    const int d = blockIdx.x;
+    int* row = hist + (size_t)d * G;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < G; base += RS_THREADS) {
+        int i = base + threadIdx.x;
+        int v = i < G ? row[i] : 0;
+        int x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        int wpre = 0, tot = 0;
+        for (int w = 0; w < RS_WARPS; w++) {
+            int c = wsum[w];
+            if (w < warp) wpre += c;
+            tot += c;
+        }
+        if (i < G) row[i] = carry + wpre + x - v;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) digit_total[d] = carry;
+}
+
 template <typename K, bool HAS_VALS>
 __global__ void __launch_bounds__(RS_THREADS) rs_scatter(const K* __restrict__ keys_in, K* __restrict__ keys_out,
                                                          const uint32_t* __restrict__ vals_in,
                                                          uint32_t* __restrict__ vals_out, const int* __restrict__ d_n,
-                                                         int shift, unsigned mask, const int* __restrict__ hist) {
+                                                         int shift, unsigned mask, const int* __restrict__ hist,
+                                                         const int* __restrict__ digit_total) {
     __shared__ int warp_cnt[RS_WARPS][RADIX];
     __shared__ int running[RADIX];
     __shared__ int round_total[RADIX];
@@ -93,7 +132,21 @@ __global__ void __launch_bounds__(RS_THREADS) rs_scatter(const K* __restrict__ k
     int lo, hi;
     chunk_range(n, G, blockIdx.x, lo, hi);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int d = threadIdx.x; d < RADIX; d += RS_THREADS) running[d] = hist[d * G + blockIdx.x];
+    // digit bases: exclusive scan of the 256 digit totals (RS_THREADS == RADIX: one digit per thread)
+    {
+        int v = digit_total[threadIdx.x];
+        int x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) round_total[warp] = x;
+        __syncthreads();
+        int wpre = 0;
+        for (int w = 0; w < warp; w++) wpre += round_total[w];
+        running[threadIdx.x] = wpre + x - v + hist[threadIdx.x * G + blockIdx.x];
+        __syncthreads();
+    }
     const unsigned lanemask_lt = (1u << lane) - 1u;
     for (int base = lo; base < hi; base += RS_THREADS) {
         for (int i = threadIdx.x; i < RS_WARPS * RADIX; i += RS_THREADS) (&warp_cnt[0][0])[i] = 0;
@@ -132,6 +185,7 @@ static int radix_sort_impl(const PrimConfig& pc, K* keys, K* keys_alt, uint32_t*
                            const int* d_n, int bits, void* scratch, cudaStream_t s, long long* launches) {
     int* hist = reinterpret_cast<int*>(scratch);
     const int G = pc.sort_blocks;
+    int* digit_total = hist + (size_t)RADIX * G;
     K* kin = keys;
     K* kout = keys_alt;
     uint32_t* vin = vals;
@@ -141,11 +195,12 @@ static int radix_sort_impl(const PrimConfig& pc, K* keys, K* keys_alt, uint32_t*
         int nb = bits - shift < 8 ? bits - shift : 8;
         unsigned mask = (1u << nb) - 1u;
         rs_histogram<K><<<G, RS_THREADS, 0, s>>>(kin, d_n, shift, mask, hist);
-        scan_small<<<1, 1024, 0, s>>>(hist, RADIX * G, nullptr);
+        rs_digit_scan<<<RADIX, RS_THREADS, 0, s>>>(hist, G, digit_total);
         if (vals)
-            rs_scatter<K, true><<<G, RS_THREADS, 0, s>>>(kin, kout, vin, vout, d_n, shift, mask, hist);
+            rs_scatter<K, true><<<G, RS_THREADS, 0, s>>>(kin, kout, vin, vout, d_n, shift, mask, hist, digit_total);
         else
-            rs_scatter<K, false><<<G, RS_THREADS, 0, s>>>(kin, kout, nullptr, nullptr, d_n, shift, mask, hist);
+            rs_scatter<K, false><<<G, RS_THREADS, 0, s>>>(kin, kout, nullptr, nullptr, d_n, shift, mask, hist,
+                                                          digit_total);
         if (launches) *launches += 3;
         K* tk = kin; kin = kout; kout = tk;
         uint32_t* tv = vin; vin = vout; vout = tv;
