@@ -30,7 +30,8 @@
 
 namespace b3g {
 
-static constexpr int SV_THREADS = 256;
+static constexpr int SV_THREADS = 256;   // setup kernels
+static constexpr int PK_THREADS = 512;   // persistent solver kernels: one block per SM, 16 warps
 static constexpr float LARGE_UPPER = 1e10f;
 
 struct SolverArgs {
@@ -40,8 +41,11 @@ struct SolverArgs {
     const int* manifold_pair;
     const int* d_nc;          // number of manifolds
     SolverPoints sp;
+    SolverPoints sp_ord;      // PGS: the same records in colour order
     int4* hdr;                // bodyA, bodyB, active point mask, num points
     float2* inv_mass;         // invMass A, B
+    int4* hdr_ord;            // PGS: colour-ordered copies
+    float2* inv_mass_ord;
     float4* dv;               // per body: [2b] lin, [2b+1] ang (PGS, and Jacobi averaged delta)
     float4* dv_sum;           // Jacobi: per body sum of split deltas from the last averaging
     float4* split;            // Jacobi: per manifold 4 float4: A lin, A ang, B lin, B ang
@@ -256,13 +260,15 @@ __device__ __forceinline__ b3gMat3 ld_mat(const b3gMat3* p) {
     return r;
 }
 
-// Contact rows (pass 0) or friction rows (pass 1) of manifold m against the given body deltas.
-__device__ __forceinline__ void solve_manifold(const SolverArgs& a, int m, int pass, const int4& h, float imA,
-                                               float imB, v3& dlA, v3& daA, v3& dlB, v3& daB, float& res_d,
-                                               float& res_l) {
+// Contact rows (pass 0) or friction rows (pass 1) of record m of `sp` against the given body
+// deltas.  Records may have been written earlier in the same kernel (colour-ordered copy), so
+// they are read through L2 (ld.cg), never through the non-coherent read-only path.
+__device__ __forceinline__ void solve_manifold(const SolverArgs& a, const SolverPoints& sp, int m, int pass,
+                                               const int4& h, float imA, float imB, v3& dlA, v3& daA, v3& dlB,
+                                               v3& daB, float& res_d, float& res_l) {
     const int mask = h.z;
     const size_t base = (size_t)m * 4;
-    const float4 nf = __ldg(&a.sp.nf[m]);
+    const float4 nf = __ldcg(&sp.nf[m]);
     const v3 n = xyz(nf);
     const b3gMat3 IA = ld_mat(&a.inertias[h.x].invInertiaWorld);
     const b3gMat3 IB = ld_mat(&a.inertias[h.y].invInertiaWorld);
@@ -270,9 +276,9 @@ __device__ __forceinline__ void solve_manifold(const SolverArgs& a, int m, int p
 #pragma unroll
     for (int j = 0; j < 4; j++) {
         if (mask & (1 << j)) {
-            r1[j] = __ldg(&a.sp.rel1[base + j]);
-            r2[j] = __ldg(&a.sp.rel2[base + j]);
-            im[j] = __ldcg(&a.sp.imp[base + j]);
+            r1[j] = __ldcg(&sp.rel1[base + j]);
+            r2[j] = __ldcg(&sp.rel2[base + j]);
+            im[j] = __ldcg(&sp.imp[base + j]);
         }
     }
     if (pass == 0) {
@@ -288,7 +294,7 @@ __device__ __forceinline__ void solve_manifold(const SolverArgs& a, int m, int p
             float old = im[j].x;
             float nw = solve_row<false>(n, r1[j].w, r2[j].w, old, r1xn, r2xn, angA, angB, 0.f, LARGE_UPPER, dlA, daA,
                                         dlB, daB, imA, imB);
-            __stcg(&a.sp.imp[base + j].x, nw);
+            __stcg(&sp.imp[base + j].x, nw);
             float nd = nw - old;
             res_d += nd * nd;
             res_l += nw * nw;
@@ -300,9 +306,9 @@ __device__ __forceinline__ void solve_manifold(const SolverArgs& a, int m, int p
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             if (mask & (1 << j)) {
-                d2[j] = __ldg(&a.sp.dir2[base + j]);
-                d1[j] = __ldg(&a.sp.dir1[base + j]);
-                rf[j] = __ldg(&a.sp.rhsf[base + j]);
+                d2[j] = __ldcg(&sp.dir2[base + j]);
+                d1[j] = __ldcg(&sp.dir1[base + j]);
+                rf[j] = __ldcg(&sp.rhsf[base + j]);
             }
         }
 #pragma unroll
@@ -333,7 +339,7 @@ __device__ __forceinline__ void solve_manifold(const SolverArgs& a, int m, int p
                     res_d += nd * nd;
                     f1 = nw;
                 }
-                __stcg(&a.sp.imp[base + j], make_float4(total, f2, f1, 0.f));
+                __stcg(&sp.imp[base + j], make_float4(total, f2, f1, 0.f));
             }
             res_l += f2 * f2 + f1 * f1;
         }
@@ -341,7 +347,7 @@ __device__ __forceinline__ void solve_manifold(const SolverArgs& a, int m, int p
 }
 
 __device__ __forceinline__ void block_accumulate(double* dst, float x, float y) {
-    __shared__ float sx[SV_THREADS / 32], sy[SV_THREADS / 32];
+    __shared__ float sx[PK_THREADS / 32], sy[PK_THREADS / 32];
     for (int o = 16; o; o >>= 1) {
         x += __shfl_xor_sync(0xffffffffu, x, o);
         y += __shfl_xor_sync(0xffffffffu, y, o);
@@ -353,7 +359,7 @@ __device__ __forceinline__ void block_accumulate(double* dst, float x, float y) 
     __syncthreads();
     if (threadIdx.x == 0) {
         float tx = 0, ty = 0;
-        for (int w = 0; w < SV_THREADS / 32; w++) {
+        for (int w = 0; w < (int)(blockDim.x / 32); w++) {
             tx += sx[w];
             ty += sy[w];
         }
@@ -399,7 +405,7 @@ __device__ __forceinline__ bool end_iteration(const SolverArgs& a, int it, float
 }
 
 // ------------------------------------------------------------------ persistent PGS kernel
-__global__ void __launch_bounds__(SV_THREADS) k_solve_pgs(SolverArgs a) {
+__global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
     const int nc = *a.d_nc;
     const unsigned nb = gridDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -474,6 +480,27 @@ __global__ void __launch_bounds__(SV_THREADS) k_solve_pgs(SolverArgs a) {
         if (c >= 0) a.color_order[__ldcg(&a.color_offsets[c]) + atomicAdd(&a.color_cursor[c], 1)] = m;
     }
     if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
+    // ---- colour-ordered copy of the records: a colour's manifolds become one contiguous range,
+    // so every phase below reads coalesced records without the order -> header indirection
+    const int ncol = __ldcg(&a.color_offsets[ncolors]);
+    for (int k = tid; k < ncol; k += stride) {
+        const int m = __ldcg(&a.color_order[k]);
+        const int4 h = a.hdr[m];
+        a.hdr_ord[k] = h;
+        a.inv_mass_ord[k] = a.inv_mass[m];
+        a.sp_ord.nf[k] = __ldcg(&a.sp.nf[m]);
+        for (int j = 0; j < 4; j++) {
+            if (!(h.z & (1 << j))) continue;
+            const size_t s = (size_t)m * 4 + j, t = (size_t)k * 4 + j;
+            a.sp_ord.rel1[t] = __ldcg(&a.sp.rel1[s]);
+            a.sp_ord.rel2[t] = __ldcg(&a.sp.rel2[s]);
+            a.sp_ord.dir2[t] = __ldcg(&a.sp.dir2[s]);
+            a.sp_ord.dir1[t] = __ldcg(&a.sp.dir1[s]);
+            a.sp_ord.rhsf[t] = __ldcg(&a.sp.rhsf[s]);
+            a.sp_ord.imp[t] = __ldcg(&a.sp.imp[s]);
+        }
+    }
+    if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
     // ---- iterations
     bool ok = true;
     for (int it = 0; it < a.iterations; it++) {
@@ -482,14 +509,13 @@ __global__ void __launch_bounds__(SV_THREADS) k_solve_pgs(SolverArgs a) {
             for (int c = 0; c < ncolors; c++) {
                 const int lo = __ldcg(&a.color_offsets[c]), hi = __ldcg(&a.color_offsets[c + 1]);
                 for (int k = lo + tid; k < hi; k += stride) {
-                    const int m = __ldcg(&a.color_order[k]);
-                    const int4 h = a.hdr[m];
+                    const int4 h = __ldcg(&a.hdr_ord[k]);
                     if (!h.z) continue;
-                    const float2 im = a.inv_mass[m];
+                    const float2 im = __ldcg(&a.inv_mass_ord[k]);
                     v3 dlA, daA, dlB, daB;
                     load_dv(a, h.x, dlA, daA);
                     load_dv(a, h.y, dlB, daB);
-                    solve_manifold(a, m, pass, h, im.x, im.y, dlA, daA, dlB, daB, res_d, res_l);
+                    solve_manifold(a, a.sp_ord, k, pass, h, im.x, im.y, dlA, daA, dlB, daB, res_d, res_l);
                     if (im.x != 0.f) store_dv(a, h.x, dlA, daA);
                     if (im.y != 0.f) store_dv(a, h.y, dlB, daB);
                 }
@@ -506,7 +532,7 @@ __global__ void __launch_bounds__(SV_THREADS) k_solve_pgs(SolverArgs a) {
                         v3 dlA, daA, dlB, daB;
                         load_dv(a, h.x, dlA, daA);
                         load_dv(a, h.y, dlB, daB);
-                        solve_manifold(a, m, pass, h, im.x, im.y, dlA, daA, dlB, daB, res_d, res_l);
+                        solve_manifold(a, a.sp, m, pass, h, im.x, im.y, dlA, daA, dlB, daB, res_d, res_l);
                         if (im.x != 0.f) store_dv(a, h.x, dlA, daA);
                         if (im.y != 0.f) store_dv(a, h.y, dlB, daB);
                     }
@@ -517,6 +543,13 @@ __global__ void __launch_bounds__(SV_THREADS) k_solve_pgs(SolverArgs a) {
         if (end_iteration(a, it, res_d, res_l, ok)) break;
     }
     if (!ok) return;
+    // ---- applied impulses back to manifold order (read by b3g_read_impulses)
+    for (int k = tid; k < ncol; k += stride) {
+        const int m = __ldcg(&a.color_order[k]);
+        const int4 h = __ldcg(&a.hdr_ord[k]);
+        for (int j = 0; j < 4; j++)
+            if (h.z & (1 << j)) a.sp.imp[(size_t)m * 4 + j] = __ldcg(&a.sp_ord.imp[(size_t)k * 4 + j]);
+    }
     // ---- finish: v += dv for dynamic bodies
     for (int b = tid; b < a.num_bodies; b += stride) {
         if (a.bodies[b].invMass == 0.f) continue;
@@ -552,7 +585,7 @@ __device__ __forceinline__ void jacobi_average(const SolverArgs& a, int tid, int
     }
 }
 
-__global__ void __launch_bounds__(SV_THREADS) k_solve_jacobi(SolverArgs a) {
+__global__ void __launch_bounds__(PK_THREADS, 1) k_solve_jacobi(SolverArgs a) {
     const int nc = *a.d_nc;
     const unsigned nb = gridDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -568,7 +601,7 @@ __global__ void __launch_bounds__(SV_THREADS) k_solve_jacobi(SolverArgs a) {
                 v3 dlA = mk3(0, 0, 0), daA = mk3(0, 0, 0), dlB = mk3(0, 0, 0), daB = mk3(0, 0, 0);
                 if (im.x != 0.f) load_dv(a, h.x, dlA, daA);
                 if (im.y != 0.f) load_dv(a, h.y, dlB, daB);
-                if (h.z) solve_manifold(a, m, pass, h, im.x, im.y, dlA, daA, dlB, daB, res_d, res_l);
+                if (h.z) solve_manifold(a, a.sp, m, pass, h, im.x, im.y, dlA, daA, dlB, daB, res_d, res_l);
                 __stcg(&a.split[4 * m + 0], f4(dlA, 0.f));
                 __stcg(&a.split[4 * m + 1], f4(daA, 0.f));
                 __stcg(&a.split[4 * m + 2], f4(dlB, 0.f));
@@ -616,7 +649,7 @@ __global__ void k_reset_solver(int* color_fill, int* remaining, int* color_curso
 
 static int solver_grid(DeviceState& d, const void* fn, int blocks_per_sm) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, SV_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, PK_THREADS, 0);
     if (per_sm < 1) per_sm = 1;
     int want = blocks_per_sm > 0 ? blocks_per_sm : 2;
     if (want > per_sm) want = per_sm;  // cooperative launch: every block must be co-resident
@@ -649,8 +682,11 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     a.manifold_pair = d.manifold_pair;
     a.d_nc = d_nc;
     a.sp = d.sp;
+    a.sp_ord = d.sp_ord;
     a.hdr = d.manifold_hdr;
     a.inv_mass = d.manifold_inv_mass;
+    a.hdr_ord = d.manifold_hdr_ord;
+    a.inv_mass_ord = d.manifold_inv_mass_ord;
     a.dv = d.dv;
     a.dv_sum = d.dv_sum;
     a.split = d.split_dv;
@@ -701,7 +737,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     int sgrid = solver_grid(d, fn, cfg.reserved[0]);
     cudaLaunchConfig_t lc = {};
     lc.gridDim = dim3(sgrid);
-    lc.blockDim = dim3(SV_THREADS);
+    lc.blockDim = dim3(PK_THREADS);
     lc.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;

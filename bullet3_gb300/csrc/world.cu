@@ -469,6 +469,15 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     TRY(dalloc(h, &d.sp.dir1, 4 * (size_t)d.max_contacts));
     TRY(dalloc(h, &d.sp.rhsf, 4 * (size_t)d.max_contacts));
     TRY(dalloc(h, &d.sp.imp, 4 * (size_t)d.max_contacts));
+    TRY(dalloc(h, &d.sp_ord.nf, d.max_contacts));
+    TRY(dalloc(h, &d.sp_ord.rel1, 4 * (size_t)d.max_contacts));
+    TRY(dalloc(h, &d.sp_ord.rel2, 4 * (size_t)d.max_contacts));
+    TRY(dalloc(h, &d.sp_ord.dir2, 4 * (size_t)d.max_contacts));
+    TRY(dalloc(h, &d.sp_ord.dir1, 4 * (size_t)d.max_contacts));
+    TRY(dalloc(h, &d.sp_ord.rhsf, 4 * (size_t)d.max_contacts));
+    TRY(dalloc(h, &d.sp_ord.imp, 4 * (size_t)d.max_contacts));
+    TRY(dalloc(h, &d.manifold_hdr_ord, d.max_contacts));
+    TRY(dalloc(h, &d.manifold_inv_mass_ord, d.max_contacts));
     TRY(dalloc(h, &d.manifold_color, d.max_contacts));
     TRY(dalloc(h, &d.color_order, d.max_contacts));
     TRY(dalloc(h, &d.color_offsets, 4 * (B3G_MAX_COLORS + 2)));  // offsets, fill, remaining, cursors

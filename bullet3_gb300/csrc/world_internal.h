@@ -81,6 +81,9 @@ struct DeviceState {
     b3gContact4* contacts_compact = nullptr;  // filled on demand for the drop-in getter
     // solver
     SolverPoints sp;                       // compact contact-point records
+    SolverPoints sp_ord;                   // PGS: the same records in colour order
+    int4* manifold_hdr_ord = nullptr;
+    float2* manifold_inv_mass_ord = nullptr;
     int* manifold_color = nullptr;
     int* color_order = nullptr;            // manifolds sorted by colour
     int* color_offsets = nullptr;          // B3G_MAX_COLORS + 1
