@@ -30,6 +30,7 @@ for _dt, _sz in ((BODY, 80), (INERTIA, 96), (COLLIDABLE, 16), (HULL, 96), (FACE,
 
 SHAPE_CONVEX_HULL, SHAPE_PLANE, SHAPE_SPHERE = 3, 4, 7
 SOLVER_PGS, SOLVER_JACOBI = 0, 1
+PGS_PARTITIONS_AUTO, PGS_PARTITIONS_GLOBAL_DELTAS, PGS_PARTITIONS_NONE = 0, 1, 2
 
 FLAG_PAIR_OVERFLOW = 0x1
 FLAG_CONTACT_OVERFLOW = 0x2
@@ -49,7 +50,7 @@ class b3gConfig(C.Structure):
                 ("solver_iterations", C.c_int), ("erp", C.c_float), ("contact_threshold", C.c_float),
                 ("contact_friction", C.c_float), ("residual_tol", C.c_float), ("update_world_inertia", C.c_int),
                 ("use_cuda_graph", C.c_int), ("warm_start", C.c_int), ("barrier_spin_limit", C.c_int),
-                ("reserved", C.c_int * 7)]
+                ("solver_blocks_per_sm", C.c_int), ("pgs_partitions", C.c_int), ("reserved", C.c_int * 5)]
 
 
 class b3gStepStats(C.Structure):
@@ -75,7 +76,7 @@ EXPORTS = [
     "b3g_synchronize", "b3g_get_stats", "b3g_status", "b3g_get_num_bodies", "b3g_get_body_buffer",
     "b3g_get_inertia_buffer", "b3g_get_aabb_buffer", "b3g_get_pair_buffer", "b3g_get_contact_buffer",
     "b3g_get_stream", "b3g_read_bodies", "b3g_write_bodies", "b3g_read_inertias", "b3g_read_aabbs",
-    "b3g_write_aabbs", "b3g_read_pairs", "b3g_read_contacts", "b3g_write_contacts", "b3g_read_batches",
+    "b3g_write_aabbs", "b3g_read_pairs", "b3g_read_contacts", "b3g_write_contacts", "b3g_read_batches", "b3g_read_solve_order",
     "b3g_read_impulses", "b3g_get_num_collidables", "b3g_read_registered_bodies", "b3g_read_shape_tables",
     "b3g_set_profiling",
     "b3g_get_stage_times", "b3g_get_launch_count", "b3g_record_event", "b3g_event_elapsed", "b3g_hull_compute",

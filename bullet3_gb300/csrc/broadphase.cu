@@ -260,6 +260,7 @@ int launch_pairs(DeviceState& d, cudaStream_t s) {
                                d.d_num_dynamic, 3 * d.grid_bits, d.sort_scratch, s, &ll);
     uint32_t* keys = d.cell_keys[which];
     uint32_t* vals = d.cell_vals[which];
+    d.cell_sorted_bodies = vals;  // dynamic bodies in cell order: the solver partitions this list
     int grid = d.num_sms * 4;
     // 2. run starts
     k_cell_start<<<grid, BP_THREADS, 0, s>>>(keys, d.num_dynamic, d.cell_start);

@@ -15,10 +15,12 @@
 // in ONE cooperative persistent kernel with a bounded grid barrier.  A manifold's whole working
 // set (normal, up to 4 points, both inverse inertias, both body deltas) is loaded up front so the
 // per-manifold latency is one memory round trip, not one per row.
-//   PGS    : Jones-Plassmann greedy colouring of manifolds (a manifold holding the highest hashed
-//            priority on both of its dynamic bodies takes the smallest colour free on both, exact
-//            per-body 64-bit masks), counting sort by colour, then per iteration: contact rows colour
-//            by colour, friction rows colour by colour, one grid barrier per colour.
+//   PGS    : dynamic bodies are split into one contiguous range of the broadphase's cell order per
+//            block.  Manifolds inside one range are solved by that block alone (shared-memory body
+//            deltas, __syncthreads between colours); the rest run grid-wide with one grid barrier
+//            per colour.  Both sets are Jones-Plassmann greedy coloured (a manifold holding the
+//            highest hashed priority on both of its dynamic bodies takes the smallest colour free
+//            on both, exact per-body 64-bit masks) and counting-sorted by (owner, colour).
 //   Jacobi : per iteration: contact rows of every manifold on its own split copies, a per-body
 //            ordered reduction (same summation order as the reference's solver-body pool), friction
 //            rows, reduction.  Per-body lists come from a stable radix sort, so the arithmetic
@@ -58,8 +60,18 @@ struct SolverArgs {
     int* color_fill;          // B3G_MAX_COLORS + 1: manifolds per colour
     int* color_cursor;        // B3G_MAX_COLORS + 1: scatter cursors for the counting sort
     int* remaining;           // per round
+    const uint32_t* sorted_bodies;  // PGS: dynamic bodies in broadphase cell order (block partitions)
+    int* body_slot;           // PGS: body -> position in sorted_bodies
+    int* manifold_group;      // PGS: processing group of each manifold
+    int* group_counts;        // PGS: 3 segments of group_seg ints: counts, offsets, cursors
+    int group_seg;
+    int num_dynamic;          // length of sorted_bodies (0: every manifold is cross-partition)
+    int chunk;                // dynamic bodies per block partition
+    int use_smem;             // block-local body deltas in shared memory
     unsigned long long* claim;
     unsigned long long* mask;  // per body: colours already taken by its manifolds
+    unsigned long long* claim_x;  // PGS: the same two arrays for the cross-partition colouring
+    unsigned long long* mask_x;
     b3gBody* bodies_out;      // velocities written at finish
     DevCounters* counters;
     double* residual_acc;     // 2 per iteration
@@ -262,20 +274,22 @@ __device__ __forceinline__ b3gMat3 ld_mat(const b3gMat3* p) {
 
 // Contact rows (pass 0) or friction rows (pass 1) of record m of `sp` against the given body
 // deltas.  Records may have been written earlier in the same kernel (colour-ordered copy), so
-// they are read through L2 (ld.cg), never through the non-coherent read-only path.
+// they are read through L2 (ld.cg), never through the non-coherent read-only path.  With
+// LOAD_ALL every point slot is loaded whatever the active mask (slots are always allocated; the
+// inactive ones are never used), so the loads do not wait for the manifold header.
+template <bool LOAD_ALL = false>
 __device__ __forceinline__ void solve_manifold(const SolverArgs& a, const SolverPoints& sp, int m, int pass,
-                                               const int4& h, float imA, float imB, v3& dlA, v3& daA, v3& dlB,
-                                               v3& daB, float& res_d, float& res_l) {
+                                               const int4& h, float imA, float imB, const b3gMat3& IA,
+                                               const b3gMat3& IB, v3& dlA, v3& daA, v3& dlB, v3& daB, float& res_d,
+                                               float& res_l) {
     const int mask = h.z;
     const size_t base = (size_t)m * 4;
     const float4 nf = __ldcg(&sp.nf[m]);
     const v3 n = xyz(nf);
-    const b3gMat3 IA = ld_mat(&a.inertias[h.x].invInertiaWorld);
-    const b3gMat3 IB = ld_mat(&a.inertias[h.y].invInertiaWorld);
     float4 r1[4], r2[4], im[4];
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-        if (mask & (1 << j)) {
+        if (LOAD_ALL || (mask & (1 << j))) {
             r1[j] = __ldcg(&sp.rel1[base + j]);
             r2[j] = __ldcg(&sp.rel2[base + j]);
             im[j] = __ldcg(&sp.imp[base + j]);
@@ -305,7 +319,7 @@ __device__ __forceinline__ void solve_manifold(const SolverArgs& a, const Solver
         float2 rf[4];
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            if (mask & (1 << j)) {
+            if (LOAD_ALL || (mask & (1 << j))) {
                 d2[j] = __ldcg(&sp.dir2[base + j]);
                 d1[j] = __ldcg(&sp.dir1[base + j]);
                 rf[j] = __ldcg(&sp.rhsf[base + j]);
@@ -404,45 +418,151 @@ __device__ __forceinline__ bool end_iteration(const SolverArgs& a, int it, float
     return a.residual_tol > 0.f && r <= (double)a.residual_tol;
 }
 
+// Block-wide exclusive scan of n ints (one block): out[i] = sum(in[0..i)), returns the total.
+__device__ int block_exclusive_scan(const int* in, int* out, int n) {
+    __shared__ int s_part[PK_THREADS];
+    const int T = blockDim.x;
+    const int per = (n + T - 1) / T;
+    const int lo = threadIdx.x * per, hi = min(lo + per, n);
+    int s = 0;
+    for (int i = lo; i < hi; i++) s += __ldcg(&in[i]);
+    s_part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < T; off <<= 1) {
+        int v = threadIdx.x >= off ? s_part[threadIdx.x - off] : 0;
+        __syncthreads();
+        s_part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    int run = threadIdx.x ? s_part[threadIdx.x - 1] : 0;
+    for (int i = lo; i < hi; i++) {
+        int v = __ldcg(&in[i]);
+        out[i] = run;
+        run += v;
+    }
+    int total = s_part[T - 1];
+    __syncthreads();
+    return total;
+}
+
+// Body deltas of the partitioned PGS: bodies owned by this block live in shared memory during
+// the block-local phase (6 floats each), everything else in global memory.
+__device__ __forceinline__ void load_dv_local(const SolverArgs& a, const float* s_dv, int body, int local, v3& l,
+                                              v3& w) {
+    if (local >= 0) {
+        const float* p = s_dv + 6 * local;
+        l = mk3(p[0], p[1], p[2]);
+        w = mk3(p[3], p[4], p[5]);
+    } else {
+        load_dv(a, body, l, w);
+    }
+}
+__device__ __forceinline__ void store_dv_local(const SolverArgs& a, float* s_dv, int body, int local, v3 l, v3 w) {
+    if (local >= 0) {
+        float* p = s_dv + 6 * local;
+        p[0] = l.x; p[1] = l.y; p[2] = l.z;
+        p[3] = w.x; p[4] = w.y; p[5] = w.z;
+    } else {
+        store_dv(a, body, l, w);
+    }
+}
+// World inverse inertia of an owned body from shared memory (9 floats, staged once per solve),
+// of any other body from global memory.
+__device__ __forceinline__ b3gMat3 load_inertia_local(const SolverArgs& a, const float* s_inv, int body, int local) {
+    if (local >= 0) {
+        const float* p = s_inv + 9 * local;
+        b3gMat3 r;
+        r.row[0] = b3gFloat4{p[0], p[1], p[2], 0.f};
+        r.row[1] = b3gFloat4{p[3], p[4], p[5], 0.f};
+        r.row[2] = b3gFloat4{p[6], p[7], p[8], 0.f};
+        return r;
+    }
+    return ld_mat(&a.inertias[body].invInertiaWorld);
+}
+
+// Partition owning a dynamic body: its cell-order position / chunk, or -2 when the body is not in
+// the cell-sorted list (inverse mass changed after upload, or no broadphase ran this step).
+__device__ __forceinline__ int owner_of(const SolverArgs& a, int body) {
+    const int p = __ldcg(&a.body_slot[body]);
+    if (p < 0 || p >= a.num_dynamic || (int)a.sorted_bodies[p] != body) return -2;
+    return p / a.chunk;
+}
+
 // ------------------------------------------------------------------ persistent PGS kernel
+// Processing order of one PGS pass (a valid Gauss-Seidel order: every group holds manifolds
+// that share no dynamic body, and groups run in key order):
+//   1. block-local groups: block g owns the dynamic bodies at positions [g*chunk, (g+1)*chunk) of
+//      the broadphase's cell-sorted body list; a manifold whose dynamic bodies are all owned by g
+//      (statics belong to nobody) is solved by block g, colour by colour, with __syncthreads
+//      between colours and the owned body deltas in shared memory.  Different blocks touch
+//      disjoint bodies, so running them concurrently equals running them in block order;
+//   2. one grid barrier, then the cross-partition manifolds, coloured on their own, colour by
+//      colour with a grid barrier per colour.
+// Group key = owner * NC + colour (block-local) or nblocks * NC + colour (cross), NC = number of
+// block-local colours; the solve order (b3g_read_solve_order) is the manifolds sorted by key.
 __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
+    extern __shared__ float s_dv[];
     const int nc = *a.d_nc;
     const unsigned nb = gridDim.x;
+    const int G = gridDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int stride = gridDim.x * blockDim.x;
-    // ---- colouring: Jones-Plassmann greedy.  Per round a manifold that holds the highest hashed
-    // priority on both of its dynamic bodies takes the smallest colour used by neither body (exact
-    // per-body 64-bit masks, no aliasing); statics never conflict.
+    const int nd = a.num_dynamic;
+    const int chunk = a.chunk;
+    // slot map: position of every dynamic body in cell order (read after the first barrier below)
+    for (int p = tid; p < nd; p += stride) a.body_slot[a.sorted_bodies[p]] = p;
+    // ---- partition owner of every manifold: a block index when all of its dynamic bodies belong
+    // to that block's partition, -1 (cross-partition) otherwise
+    if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
+    for (int m = tid; m < nc; m += stride) {
+        const int4 h = a.hdr[m];
+        const float2 im = a.inv_mass[m];
+        const int oA = im.x != 0.f ? owner_of(a, h.x) : -1;
+        const int oB = im.y != 0.f ? owner_of(a, h.y) : -1;
+        // -2 (a dynamic body outside the partitioned list) and differing owners go cross-partition
+        int owner = -1;
+        if (oA != -2 && oB != -2) owner = (oA >= 0 && oB >= 0) ? (oA == oB ? oA : -1) : (oA >= 0 ? oA : oB);
+        a.manifold_group[m] = owner;
+    }
+    // ---- colouring: Jones-Plassmann greedy, block-local and cross-partition manifolds coloured
+    // independently (they never run in the same phase).  Per round a manifold that holds the
+    // highest hashed priority on both of its dynamic bodies takes the smallest colour used by
+    // neither body (exact per-body 64-bit masks, no aliasing); statics never conflict.  The
+    // manifold_group reads below are the thread's own writes from the loop above (same m mapping).
     int rounds = 0;
     for (int r = 0; r < B3G_MAX_COLORS; r++) {
         const unsigned long long rk = (unsigned long long)r << 56;
         for (int m = tid; m < nc; m += stride) {
             if (a.color[m] >= 0) continue;
-            int4 h = a.hdr[m];
-            float2 im = a.inv_mass[m];
+            const int4 h = a.hdr[m];
+            const float2 im = a.inv_mass[m];
+            unsigned long long* claim = a.manifold_group[m] < 0 ? a.claim_x : a.claim;
             unsigned long long key = rk | ((unsigned long long)(hash32((unsigned)m) & 0xFFFFFFu) << 32) | (unsigned)m;
-            if (im.x != 0.f) atomicMax(&a.claim[h.x], key);
-            if (im.y != 0.f) atomicMax(&a.claim[h.y], key);
+            if (im.x != 0.f) atomicMax(&claim[h.x], key);
+            if (im.y != 0.f) atomicMax(&claim[h.y], key);
         }
         if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
         int left = 0;
         for (int m = tid; m < nc; m += stride) {
             if (a.color[m] >= 0) continue;
-            int4 h = a.hdr[m];
-            float2 im = a.inv_mass[m];
+            const int4 h = a.hdr[m];
+            const float2 im = a.inv_mass[m];
+            const bool cross = a.manifold_group[m] < 0;
+            unsigned long long* claim = cross ? a.claim_x : a.claim;
+            unsigned long long* mask = cross ? a.mask_x : a.mask;
             unsigned long long key = rk | ((unsigned long long)(hash32((unsigned)m) & 0xFFFFFFu) << 32) | (unsigned)m;
-            bool okA = im.x == 0.f || __ldcg(&a.claim[h.x]) == key;
-            bool okB = im.y == 0.f || __ldcg(&a.claim[h.y]) == key;
+            bool okA = im.x == 0.f || __ldcg(&claim[h.x]) == key;
+            bool okB = im.y == 0.f || __ldcg(&claim[h.y]) == key;
             if (okA && okB) {
                 unsigned long long used = 0ull;
-                if (im.x != 0.f) used |= __ldcg(&a.mask[h.x]);
-                if (im.y != 0.f) used |= __ldcg(&a.mask[h.y]);
+                if (im.x != 0.f) used |= __ldcg(&mask[h.x]);
+                if (im.y != 0.f) used |= __ldcg(&mask[h.y]);
                 int c = __ffsll((long long)~used) - 1;
                 if (c >= 0 && c < 64) {
                     a.color[m] = c;
-                    atomicAdd(&a.color_fill[c], 1);
-                    if (im.x != 0.f) atomicOr(&a.mask[h.x], 1ull << c);
-                    if (im.y != 0.f) atomicOr(&a.mask[h.y], 1ull << c);
+                    atomicAdd(&a.color_fill[c + (cross ? 64 : 0)], 1);
+                    if (im.x != 0.f) atomicOr(&mask[h.x], 1ull << c);
+                    if (im.y != 0.f) atomicOr(&mask[h.y], 1ull << c);
                 } else {
                     left++;
                 }
@@ -456,38 +576,69 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
         rounds = r + 1;
         if (*((volatile int*)&a.remaining[r]) == 0) break;
     }
-    int ncolors = 0;
-    for (int c = 0; c < 64; c++)
-        if (*((volatile int*)&a.color_fill[c]) > 0) ncolors = c + 1;
-    if (ncolors == 0) ncolors = 1;
+    int ncl = 0, ncx = 0;
+    for (int c = 0; c < 64; c++) {
+        if (*((volatile int*)&a.color_fill[c]) > 0) ncl = c + 1;
+        if (*((volatile int*)&a.color_fill[c + 64]) > 0) ncx = c + 1;
+    }
     const bool overflow = rounds > 0 && *((volatile int*)&a.remaining[rounds - 1]) != 0 && nc > 0;
-    // ---- counting sort by colour (order inside a colour is irrelevant: its manifolds are independent).
-    // color_fill stays read-only from here on (every block derived ncolors from it above); the
-    // scatter uses its own cursors, zeroed before the kernel started.
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        int s = 0;
-        for (int c = 0; c < ncolors; c++) {
-            a.color_offsets[c] = s;
-            s += a.color_fill[c];
+    const int NC = ncl > 0 ? ncl : 1;  // key stride of the block-local groups
+    const int ngroups = G * NC + ncx;
+    int* gcount = a.group_counts;
+    int* goff = gcount + a.group_seg;
+    int* gcur = goff + a.group_seg;
+    // ---- processing group of every manifold: owner * NC + colour (block-local) or
+    // G * NC + colour (cross-partition).  Reported colours: block-local c, cross ncl + c, so the
+    // batches stay legal as one colouring.
+    for (int m = tid; m < nc; m += stride) {
+        const int c = a.color[m];
+        if (c < 0) {
+            a.manifold_group[m] = -1;
+            continue;
         }
-        a.color_offsets[ncolors] = s;
-        a.counters->num_colors = ncolors;
-        if (overflow) atomicOr(&a.counters->status, B3G_FLAG_BATCH_OVERFLOW);
+        const int owner = a.manifold_group[m];
+        const int key = owner >= 0 ? owner * NC + c : G * NC + c;
+        if (owner < 0) a.color[m] = ncl + c;
+        a.manifold_group[m] = key;
+        atomicAdd(&gcount[key], 1);
+    }
+    if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
+    if (blockIdx.x == 0) {
+        int total = block_exclusive_scan(gcount, goff, ngroups);
+        if (threadIdx.x == 0) {
+            goff[ngroups] = total;
+            a.counters->num_colors = ncl + ncx;
+            if (overflow) atomicOr(&a.counters->status, B3G_FLAG_BATCH_OVERFLOW);
+        }
     }
     if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
     for (int m = tid; m < nc; m += stride) {
-        int c = a.color[m];
-        if (c >= 0) a.color_order[__ldcg(&a.color_offsets[c]) + atomicAdd(&a.color_cursor[c], 1)] = m;
+        const int key = a.manifold_group[m];
+        if (key >= 0) a.color_order[__ldcg(&goff[key]) + atomicAdd(&gcur[key], 1)] = m;
+    }
+    const int ncol = __ldcg(&goff[ngroups]);  // coloured manifolds; the rest are overflow leftovers
+    if (overflow && tid == 0) {
+        int k = ncol;
+        for (int m = 0; m < nc; m++)
+            if (a.color[m] < 0) a.color_order[k++] = m;
     }
     if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
-    // ---- colour-ordered copy of the records: a colour's manifolds become one contiguous range,
-    // so every phase below reads coalesced records without the order -> header indirection
-    const int ncol = __ldcg(&a.color_offsets[ncolors]);
-    for (int k = tid; k < ncol; k += stride) {
+    // ---- group-ordered copy of the records (coalesced phases, no order -> header indirection);
+    // block-local manifolds carry their bodies' shared-memory slots in hdr.w (0xffff = not owned)
+    const int nlocal = __ldcg(&goff[G * NC]);
+    for (int k = tid; k < nc; k += stride) {
         const int m = __ldcg(&a.color_order[k]);
-        const int4 h = a.hdr[m];
-        a.hdr_ord[k] = h;
-        a.inv_mass_ord[k] = a.inv_mass[m];
+        int4 h = a.hdr[m];
+        const float2 im = a.inv_mass[m];
+        int w = 0xffffffff;
+        if (k < nlocal) {
+            const int owner = __ldcg(&a.manifold_group[m]) / NC;
+            const int la = im.x != 0.f ? __ldcg(&a.body_slot[h.x]) - owner * chunk : 0xffff;
+            const int lb = im.y != 0.f ? __ldcg(&a.body_slot[h.y]) - owner * chunk : 0xffff;
+            w = (int)(((unsigned)la & 0xffffu) | (((unsigned)lb & 0xffffu) << 16));
+        }
+        a.hdr_ord[k] = make_int4(h.x, h.y, h.z, w);
+        a.inv_mass_ord[k] = im;
         a.sp_ord.nf[k] = __ldcg(&a.sp.nf[m]);
         for (int j = 0; j < 4; j++) {
             if (!(h.z & (1 << j))) continue;
@@ -501,40 +652,86 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
         }
     }
     if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
-    // ---- iterations
+    // ---- iterations.  Segments of one pass: the NC block-local colours (__syncthreads between
+    // them), then the ncx cross-partition colours and the colour-overflow leftovers (grid barrier
+    // after each).  One solve call site keeps the register budget of the kernel low.
+    const int myLo = blockIdx.x * chunk;
+    const int myN = max(0, min(chunk, nd - myLo));
+    const int nseg = NC + ncx + (overflow ? 1 : 0);
+    float* s_inv = s_dv + 6 * chunk;  // owned bodies' world inverse inertia (fixed during the solve)
+    if (a.use_smem) {
+        for (int l = threadIdx.x; l < myN; l += blockDim.x) {
+            const b3gMat3 I = ld_mat(&a.inertias[a.sorted_bodies[myLo + l]].invInertiaWorld);
+            float* p = s_inv + 9 * l;
+            p[0] = I.row[0].x; p[1] = I.row[0].y; p[2] = I.row[0].z;
+            p[3] = I.row[1].x; p[4] = I.row[1].y; p[5] = I.row[1].z;
+            p[6] = I.row[2].x; p[7] = I.row[2].y; p[8] = I.row[2].z;
+        }
+    }
     bool ok = true;
     for (int it = 0; it < a.iterations; it++) {
         float res_d = 0.f, res_l = 0.f;
         for (int pass = 0; pass < 2; pass++) {
-            for (int c = 0; c < ncolors; c++) {
-                const int lo = __ldcg(&a.color_offsets[c]), hi = __ldcg(&a.color_offsets[c + 1]);
-                for (int k = lo + tid; k < hi; k += stride) {
-                    const int4 h = __ldcg(&a.hdr_ord[k]);
-                    if (!h.z) continue;
-                    const float2 im = __ldcg(&a.inv_mass_ord[k]);
-                    v3 dlA, daA, dlB, daB;
-                    load_dv(a, h.x, dlA, daA);
-                    load_dv(a, h.y, dlB, daB);
-                    solve_manifold(a, a.sp_ord, k, pass, h, im.x, im.y, dlA, daA, dlB, daB, res_d, res_l);
-                    if (im.x != 0.f) store_dv(a, h.x, dlA, daA);
-                    if (im.y != 0.f) store_dv(a, h.y, dlB, daB);
+            if (a.use_smem) {
+                for (int l = threadIdx.x; l < myN; l += blockDim.x) {
+                    v3 dl, dw;
+                    load_dv(a, (int)a.sorted_bodies[myLo + l], dl, dw);
+                    float* p = s_dv + 6 * l;
+                    p[0] = dl.x; p[1] = dl.y; p[2] = dl.z;
+                    p[3] = dw.x; p[4] = dw.y; p[5] = dw.z;
                 }
-                if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
+                __syncthreads();
             }
-            // colour-overflow leftovers: one thread, in manifold order (always correct, slow)
-            if (overflow) {
-                if (tid == 0) {
-                    for (int m = 0; m < nc; m++) {
-                        if (a.color[m] >= 0) continue;
-                        const int4 h = a.hdr[m];
-                        if (!h.z) continue;
-                        const float2 im = a.inv_mass[m];
-                        v3 dlA, daA, dlB, daB;
-                        load_dv(a, h.x, dlA, daA);
-                        load_dv(a, h.y, dlB, daB);
-                        solve_manifold(a, a.sp, m, pass, h, im.x, im.y, dlA, daA, dlB, daB, res_d, res_l);
-                        if (im.x != 0.f) store_dv(a, h.x, dlA, daA);
-                        if (im.y != 0.f) store_dv(a, h.y, dlB, daB);
+            for (int sg = 0; sg < nseg; sg++) {
+                const bool local = sg < NC;
+                int first, hi, step;
+                if (local) {
+                    const int key = blockIdx.x * NC + sg;
+                    first = __ldcg(&goff[key]) + threadIdx.x;
+                    hi = __ldcg(&goff[key + 1]);
+                    step = blockDim.x;
+                } else if (sg < NC + ncx) {
+                    const int key = G * NC + sg - NC;
+                    const int lo = __ldcg(&goff[key]);
+                    hi = __ldcg(&goff[key + 1]);
+                    if (lo == hi) continue;  // uniform across blocks: goff is read-only here
+                    first = lo + tid;
+                    step = stride;
+                } else {  // leftovers: one thread, in manifold order (always correct, slow)
+                    first = ncol;
+                    hi = tid == 0 ? nc : ncol;
+                    step = 1;
+                }
+                const bool smem_here = local && a.use_smem;
+                for (int k = first; k < hi; k += step) {
+                    // no early exit for manifolds without active points: their deltas are read and
+                    // written back unchanged, and the record loads need not wait for the header
+                    const int4 h = __ldcg(&a.hdr_ord[k]);
+                    const float2 im = __ldcg(&a.inv_mass_ord[k]);
+                    int la = -1, lb = -1;
+                    if (smem_here) {
+                        la = (h.w & 0xffff) == 0xffff ? -1 : (h.w & 0xffff);
+                        lb = ((unsigned)h.w >> 16) == 0xffffu ? -1 : (int)((unsigned)h.w >> 16);
+                    }
+                    v3 dlA = mk3(0, 0, 0), daA = mk3(0, 0, 0), dlB = mk3(0, 0, 0), daB = mk3(0, 0, 0);
+                    if (im.x != 0.f) load_dv_local(a, s_dv, h.x, la, dlA, daA);
+                    if (im.y != 0.f) load_dv_local(a, s_dv, h.y, lb, dlB, daB);
+                    const b3gMat3 IA = load_inertia_local(a, s_inv, h.x, la);
+                    const b3gMat3 IB = load_inertia_local(a, s_inv, h.y, lb);
+                    solve_manifold<true>(a, a.sp_ord, k, pass, h, im.x, im.y, IA, IB, dlA, daA, dlB, daB, res_d,
+                                         res_l);
+                    if (im.x != 0.f) store_dv_local(a, s_dv, h.x, la, dlA, daA);
+                    if (im.y != 0.f) store_dv_local(a, s_dv, h.y, lb, dlB, daB);
+                }
+                if (local) {
+                    __syncthreads();
+                    if (sg < NC - 1) continue;
+                    if (a.use_smem) {
+                        for (int l = threadIdx.x; l < myN; l += blockDim.x) {
+                            const float* p = s_dv + 6 * l;
+                            store_dv(a, (int)a.sorted_bodies[myLo + l], mk3(p[0], p[1], p[2]),
+                                     mk3(p[3], p[4], p[5]));
+                        }
                     }
                 }
                 if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
@@ -544,7 +741,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
     }
     if (!ok) return;
     // ---- applied impulses back to manifold order (read by b3g_read_impulses)
-    for (int k = tid; k < ncol; k += stride) {
+    for (int k = tid; k < nc; k += stride) {
         const int m = __ldcg(&a.color_order[k]);
         const int4 h = __ldcg(&a.hdr_ord[k]);
         for (int j = 0; j < 4; j++)
@@ -601,7 +798,11 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_jacobi(SolverArgs a) {
                 v3 dlA = mk3(0, 0, 0), daA = mk3(0, 0, 0), dlB = mk3(0, 0, 0), daB = mk3(0, 0, 0);
                 if (im.x != 0.f) load_dv(a, h.x, dlA, daA);
                 if (im.y != 0.f) load_dv(a, h.y, dlB, daB);
-                if (h.z) solve_manifold(a, a.sp, m, pass, h, im.x, im.y, dlA, daA, dlB, daB, res_d, res_l);
+                if (h.z) {
+                    const b3gMat3 IA = ld_mat(&a.inertias[h.x].invInertiaWorld);
+                    const b3gMat3 IB = ld_mat(&a.inertias[h.y].invInertiaWorld);
+                    solve_manifold(a, a.sp, m, pass, h, im.x, im.y, IA, IB, dlA, daA, dlB, daB, res_d, res_l);
+                }
                 __stcg(&a.split[4 * m + 0], f4(dlA, 0.f));
                 __stcg(&a.split[4 * m + 1], f4(daA, 0.f));
                 __stcg(&a.split[4 * m + 2], f4(dlB, 0.f));
@@ -647,13 +848,18 @@ __global__ void k_reset_solver(int* color_fill, int* remaining, int* color_curso
     }
 }
 
-static int solver_grid(DeviceState& d, const void* fn, int blocks_per_sm) {
+static int solver_grid(DeviceState& d, const void* fn, int blocks_per_sm, size_t smem) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, PK_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, PK_THREADS, smem);
     if (per_sm < 1) per_sm = 1;
     int want = blocks_per_sm > 0 ? blocks_per_sm : 2;
     if (want > per_sm) want = per_sm;  // cooperative launch: every block must be co-resident
+    if (want > B3G_PGS_MAX_BLOCKS_PER_SM) want = B3G_PGS_MAX_BLOCKS_PER_SM;
     return want * d.num_sms;
+}
+
+cudaError_t solver_prepare() {
+    return cudaFuncSetAttribute(k_solve_pgs, cudaFuncAttributeMaxDynamicSharedMemorySize, B3G_PGS_MAX_SMEM);
 }
 
 int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s) {
@@ -666,7 +872,8 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     int* d_n2 = &d.counters->pad[1];
     // per-step resets
     cudaMemsetAsync(d.dv, 0, sizeof(float4) * 2 * (size_t)d.num_bodies, s);
-    cudaMemsetAsync(d.color_claim, 0, sizeof(unsigned long long) * 2 * (size_t)d.num_bodies, s);
+    const bool jac = cfg.solver_mode == B3G_SOLVER_JACOBI;
+    cudaMemsetAsync(d.color_claim, 0, sizeof(unsigned long long) * (jac ? 2 : 4) * (size_t)d.num_bodies, s);
     cudaMemsetAsync(d.body_manifold_count, 0, sizeof(int) * (size_t)d.num_bodies, s);
     int* color_fill = d.color_offsets + (B3G_MAX_COLORS + 2);
     int* remaining = color_fill + (B3G_MAX_COLORS + 1);
@@ -699,8 +906,18 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     a.color_fill = color_fill;
     a.color_cursor = color_cursor;
     a.remaining = remaining;
+    a.sorted_bodies = nullptr;
+    a.body_slot = d.body_slot;
+    a.manifold_group = d.manifold_group;
+    a.group_counts = d.group_counts;
+    a.group_seg = 0;
+    a.num_dynamic = 0;
+    a.chunk = 1;
+    a.use_smem = 0;
     a.claim = d.color_claim;
     a.mask = d.color_claim + d.num_bodies;
+    a.claim_x = d.color_claim + 2 * (size_t)d.num_bodies;
+    a.mask_x = d.color_claim + 3 * (size_t)d.num_bodies;
     a.bodies_out = d.bodies;
     a.counters = d.counters;
     a.residual_acc = d.residual_acc;
@@ -732,12 +949,35 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     k_setup_rows<<<grid, SV_THREADS, 0, s>>>(a);
     launches++;
 
-    const bool jac = cfg.solver_mode == B3G_SOLVER_JACOBI;
-    const void* fn = jac ? (const void*)k_solve_jacobi : (const void*)k_solve_pgs;
-    int sgrid = solver_grid(d, fn, cfg.reserved[0]);
+    // PGS partitions: a contiguous range of the cell-ordered dynamic bodies per block, the range's
+    // body deltas and world inverse inertias in shared memory when they fit (60 B per body)
+    size_t smem = 0;
+    int sgrid = 0;
+    const int bps = cfg.solver_blocks_per_sm;
+    if (jac) {
+        sgrid = solver_grid(d, (const void*)k_solve_jacobi, bps, 0);
+    } else {
+        const bool parts = cfg.pgs_partitions != B3G_PGS_PARTITIONS_NONE;
+        const int nd = parts && d.cell_sorted_bodies ? d.num_dynamic : 0;
+        sgrid = solver_grid(d, (const void*)k_solve_pgs, bps, 0);
+        const int chunk = nd > 0 ? (nd + sgrid - 1) / sgrid : 1;
+        smem = (size_t)chunk * 15 * sizeof(float);
+        if (nd == 0 || cfg.pgs_partitions != B3G_PGS_PARTITIONS_AUTO || chunk >= 0xffff ||
+            smem > (size_t)B3G_PGS_MAX_SMEM)
+            smem = 0;
+        // keep the grid co-resident: drop the shared-memory ranges if they would cost occupancy
+        if (smem > 0 && solver_grid(d, (const void*)k_solve_pgs, bps, smem) != sgrid) smem = 0;
+        a.sorted_bodies = d.cell_sorted_bodies;
+        a.num_dynamic = nd;
+        a.chunk = chunk;
+        a.use_smem = smem > 0 ? 1 : 0;
+        a.group_seg = sgrid * 64 + 64 + 2;
+        cudaMemsetAsync(d.group_counts, 0, sizeof(int) * 3 * (size_t)a.group_seg, s);
+    }
     cudaLaunchConfig_t lc = {};
     lc.gridDim = dim3(sgrid);
     lc.blockDim = dim3(PK_THREADS);
+    lc.dynamicSmemBytes = smem;
     lc.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;

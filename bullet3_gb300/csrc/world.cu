@@ -155,6 +155,14 @@ extern "C" b3gStatus b3g_create(const b3gConfig* cfg, int cuda_device, b3g_handl
         delete w;
         return fail(B3G_ERR_INVALID_ARG, "grid_dim must be <= 1024 (hash fits in 30 bits)");
     }
+    if (w->cfg.pgs_partitions < B3G_PGS_PARTITIONS_AUTO || w->cfg.pgs_partitions > B3G_PGS_PARTITIONS_NONE) {
+        delete w;
+        return fail(B3G_ERR_INVALID_ARG, "pgs_partitions must be one of B3G_PGS_PARTITIONS_*");
+    }
+    if (w->cfg.solver_blocks_per_sm < 0) {
+        delete w;
+        return fail(B3G_ERR_INVALID_ARG, "solver_blocks_per_sm must be >= 0");
+    }
     w->device = cuda_device;
     *out = w;
     return B3G_OK;
@@ -477,11 +485,15 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     TRY(dalloc(h, &d.sp_ord.rhsf, 4 * (size_t)d.max_contacts));
     TRY(dalloc(h, &d.sp_ord.imp, 4 * (size_t)d.max_contacts));
     TRY(dalloc(h, &d.manifold_hdr_ord, d.max_contacts));
+    TRY(dalloc(h, &d.body_slot, N));
+    TRY(dalloc(h, &d.manifold_group, d.max_contacts));
+    TRY(dalloc(h, &d.group_counts, 3 * ((size_t)sms * B3G_PGS_MAX_BLOCKS_PER_SM * 64 + 64 + 2)));
     TRY(dalloc(h, &d.manifold_inv_mass_ord, d.max_contacts));
     TRY(dalloc(h, &d.manifold_color, d.max_contacts));
     TRY(dalloc(h, &d.color_order, d.max_contacts));
     TRY(dalloc(h, &d.color_offsets, 4 * (B3G_MAX_COLORS + 2)));  // offsets, fill, remaining, cursors
-    TRY(dalloc(h, &d.color_claim, 2 * (size_t)N));  // claims, then colour masks
+    TRY(dalloc(h, &d.color_claim, 4 * (size_t)N));  // claims, colour masks; again for cross-partition
+    CUDA_TRY(solver_prepare());
     TRY(dalloc(h, &d.dv, 2 * (size_t)N));
     TRY(dalloc(h, &d.dv_sum, 2 * (size_t)N));
     TRY(dalloc(h, &d.manifold_hdr, d.max_contacts));
@@ -834,6 +846,22 @@ extern "C" b3gStatus b3g_read_batches(b3g_handle h, int* host, int capacity, int
     if (host && capacity > 0)
         TRY(copy_out(h, host, h->d.manifold_color, sizeof(int) * std::min(c.num_contacts, capacity)));
     return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_read_solve_order(b3g_handle h, int* host, int capacity, int* num) {
+    REQUIRE_UPLOADED(h);
+    if (!num) return fail(B3G_ERR_INVALID_ARG, "null count");
+    DevCounters c;
+    TRY(read_counters(h, c));
+    *num = c.num_contacts;
+    if (!host || capacity <= 0 || c.num_contacts == 0) return B3G_OK;
+    const int n = std::min(c.num_contacts, capacity);
+    if (h->cfg.solver_mode != B3G_SOLVER_PGS) {  // Jacobi: order-independent, manifold order
+        for (int m = 0; m < n; m++) host[m] = m;
+        return B3G_OK;
+    }
+    // the PGS kernel's processing order: groups by key, then the colour-overflow leftovers
+    return copy_out(h, host, h->d.color_order, sizeof(int) * n);
 }
 
 __global__ void k_gather_impulses(const float4* __restrict__ imp, int n, float* __restrict__ out) {

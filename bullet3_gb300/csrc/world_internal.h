@@ -84,6 +84,10 @@ struct DeviceState {
     SolverPoints sp_ord;                   // PGS: the same records in colour order
     int4* manifold_hdr_ord = nullptr;
     float2* manifold_inv_mass_ord = nullptr;
+    const uint32_t* cell_sorted_bodies = nullptr;  // set by the broadphase: dynamic bodies in cell order
+    int* body_slot = nullptr;              // body -> position in cell order (PGS partitions)
+    int* manifold_group = nullptr;         // PGS processing group of each manifold
+    int* group_counts = nullptr;           // 3 x (num_sms * B3G_PGS_MAX_BLOCKS_PER_SM * 64 + 64 + 2)
     int* manifold_color = nullptr;
     int* color_order = nullptr;            // manifolds sorted by colour
     int* color_offsets = nullptr;          // B3G_MAX_COLORS + 1
@@ -111,6 +115,10 @@ struct DeviceState {
 };
 
 #define B3G_MAX_COLORS 256
+// PGS partitioned solver: at most this many persistent blocks per SM (sizes group_counts), and
+// this much dynamic shared memory per block for the block-local body deltas
+#define B3G_PGS_MAX_BLOCKS_PER_SM 4
+#define B3G_PGS_MAX_SMEM (160 * 1024)
 
 // stage launchers (each returns the number of kernels it launched)
 int launch_aabbs(DeviceState& d, cudaStream_t s);
@@ -118,6 +126,7 @@ int launch_pairs(DeviceState& d, cudaStream_t s);
 int launch_contacts(DeviceState& d, float friction, cudaStream_t s);
 int launch_compact_contacts(DeviceState& d, cudaStream_t s);
 int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s);
+cudaError_t solver_prepare();  // kernel attributes, once per device before the first solve
 int launch_integrate(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s);
 
 }  // namespace b3g

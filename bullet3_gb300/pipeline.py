@@ -43,6 +43,8 @@ class b3Config:
         self.contact_friction = 0.7
         self.update_world_inertia = False
         self.gravity = (0.0, -9.8, 0.0)
+        self.solver_blocks_per_sm = 0
+        self.pgs_partitions = capi.PGS_PARTITIONS_AUTO
         for k, v in kw.items():
             if not hasattr(self, k):
                 raise AttributeError(k)
@@ -55,7 +57,9 @@ class b3Config:
                                    solver_mode=self.solver_mode, solver_iterations=self.solver_iterations,
                                    residual_tol=self.residual_tol, use_cuda_graph=int(self.use_cuda_graph),
                                    contact_friction=self.contact_friction,
-                                   update_world_inertia=int(self.update_world_inertia), gravity=self.gravity)
+                                   update_world_inertia=int(self.update_world_inertia), gravity=self.gravity,
+                                   solver_blocks_per_sm=self.solver_blocks_per_sm,
+                                   pgs_partitions=self.pgs_partitions)
 
 
 class _World:
@@ -376,6 +380,15 @@ class b3GpuRigidBodyPipeline:
         out = np.zeros(n.value, np.int32)
         if n.value:
             call("b3g_read_batches", self._h, iptr(out), C.c_int(n.value), C.byref(n))
+        return out
+
+    def readSolveOrder(self) -> np.ndarray:
+        """Manifold order whose sequential PGS sweep reproduces the GPU's last solve bit for bit."""
+        n = C.c_int()
+        call("b3g_read_solve_order", self._h, None, C.c_int(0), C.byref(n))
+        out = np.zeros(n.value, np.int32)
+        if n.value:
+            call("b3g_read_solve_order", self._h, iptr(out), C.c_int(n.value), C.byref(n))
         return out
 
     def readImpulses(self) -> np.ndarray:

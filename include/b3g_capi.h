@@ -46,7 +46,15 @@ typedef enum b3gStatus {
 #define B3G_FLAG_CLIP_OVERFLOW     0x20u
 
 #define B3G_SOLVER_PGS 0      /* b3PgsJacobiSolver(true)  -- graph-coloured Gauss-Seidel on the GPU */
-#define B3G_SOLVER_JACOBI 1   /* b3PgsJacobiSolver(false) -- mass-splitting Jacobi */
+#define B3G_SOLVER_JACOBI 1
+
+/* PGS work split.  AUTO: each block owns a contiguous range of the dynamic bodies in broadphase
+ * cell order and solves the manifolds inside its range alone, body deltas staged in shared memory;
+ * GLOBAL_DELTAS: the same ranges with the deltas left in global memory; NONE: every manifold is
+ * solved grid-wide, one grid barrier per colour.  All three are legal Gauss-Seidel orders. */
+#define B3G_PGS_PARTITIONS_AUTO 0
+#define B3G_PGS_PARTITIONS_GLOBAL_DELTAS 1
+#define B3G_PGS_PARTITIONS_NONE 2   /* b3PgsJacobiSolver(false) -- mass-splitting Jacobi */
 
 /* One configuration struct replaces b3Config (b3Config.h:4-37) plus the constants the
  * reference hard-codes (dt 1/60 b3GpuPgsContactSolver.cpp:672, damping 0.99
@@ -70,7 +78,9 @@ typedef struct b3gConfig {
     int use_cuda_graph;        /* capture the whole step as one CUDA graph */
     int warm_start;            /* 0 = cold start (reference); 1 = learned warm start if a model is loaded */
     int barrier_spin_limit;    /* polls before a grid barrier gives up (0 = default, about a second) */
-    int reserved[7];
+    int solver_blocks_per_sm;  /* persistent solver blocks per SM (0 = default; clamped to co-residency) */
+    int pgs_partitions;        /* B3G_PGS_PARTITIONS_*: how the PGS solver splits work across blocks */
+    int reserved[5];
 } b3gConfig;
 
 /* Per-step counters, copied once per step from the device. */
@@ -170,6 +180,11 @@ b3gStatus b3g_read_contacts(b3g_handle h, void* host_contacts, int capacity, int
 b3gStatus b3g_write_contacts(b3g_handle h, const void* host_contacts, int num_contacts);
 /* Reads the colour (batch) of every manifold after the solver stage (PGS). */
 b3gStatus b3g_read_batches(b3g_handle h, int* host_batch, int capacity, int* num);
+/* Reads the PGS solve order of the last solver stage: manifold indices in an order whose
+ * sequential Gauss-Seidel sweep gives the GPU's results bit for bit (manifolds the GPU solves
+ * concurrently share no dynamic body).  Colour-overflow leftovers come last, in manifold order.
+ * No counterpart in the reference (its order is the manifold order). */
+b3gStatus b3g_read_solve_order(b3g_handle h, int* host_order, int capacity, int* num);
 /* Reads per-point solver impulses (normal, lateral1, lateral2) after the solve: 3 floats per
  * point, 4 point slots per manifold. */
 b3gStatus b3g_read_impulses(b3g_handle h, float* host, int capacity_manifolds, int* num);

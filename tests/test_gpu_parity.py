@@ -73,7 +73,10 @@ def test_golden_pgs_colour_order_bitexact(name):
     assert (col >= 0).all()
     # batch legality (integer, exact): no dynamic body twice in a colour
     assert O.check_batches(gc, col, b) == 0
-    order = np.lexsort((np.arange(len(col)), col)).astype(np.int32)
+    # the GPU's processing order (block partitions, then cross-partition colours) is a permutation
+    # whose sequential Gauss-Seidel sweep the oracle reproduces bit for bit
+    order = pl.readSolveOrder()
+    assert np.array_equal(np.sort(order), np.arange(len(col)))
     ob, _ = O.solve_ordered(b, I, gc, order, iterations=10)
     gb = np_.readbackAllBodiesToCpu()
     assert np.array_equal(gb["linVel"], ob["linVel"]) and np.array_equal(gb["angVel"], ob["angVel"])
@@ -195,3 +198,33 @@ def test_graph_step_equals_staged_step():
         pl.synchronize()
         res.append(np_.readbackAllBodiesToCpu())
     assert np.array_equal(res[0].view(np.uint8), res[1].view(np.uint8))
+
+
+@pytest.mark.parametrize("parts", [capi.PGS_PARTITIONS_AUTO, capi.PGS_PARTITIONS_GLOBAL_DELTAS,
+                                   capi.PGS_PARTITIONS_NONE])
+@pytest.mark.parametrize("scene", ["stack", "mixed"])
+def test_pgs_partitioned_solve_bitexact(parts, scene):
+    # every PGS work split (block-owned body ranges with shared- or global-memory deltas, or
+    # grid-wide colours only) is a legal Gauss-Seidel order: the oracle sweeping the GPU's
+    # reported order over the GPU's own manifolds reproduces the velocities bit for bit
+    if scene == "stack":
+        sc = scenes.box_stack(16, 16, 16, seed=2)
+        np_, bp, pl, shapes = load(sc, solver_mode=capi.SOLVER_PGS, solver_iterations=10, pgs_partitions=parts)
+    else:
+        sc = scenes.mixed_scene(4096, extent=20.0, seed=3, plane=True)
+        np_, bp, pl, shapes = load(sc, m_maxBroadphasePairs=400000, solver_mode=capi.SOLVER_PGS,
+                                   solver_iterations=10, pgs_partitions=parts)
+    b = np_.readbackAllBodiesToCpu()
+    I = np_.readInertiasToCpu()
+    run_stages(np_, bp, pl)
+    gc = np_.getContactsCPU()
+    assert len(gc) > 1000
+    col = pl.readBatches()
+    assert (col >= 0).all() and O.check_batches(gc, col, b) == 0
+    order = pl.readSolveOrder()
+    assert np.array_equal(np.sort(order), np.arange(len(gc)))
+    ob, _ = O.solve_ordered(b, I, gc, order, iterations=10)
+    gb = np_.readbackAllBodiesToCpu()
+    assert np.array_equal(gb["linVel"], ob["linVel"]) and np.array_equal(gb["angVel"], ob["angVel"])
+    st = pl.stats()
+    assert st.status == 0 and st.num_colors == col.max() + 1
