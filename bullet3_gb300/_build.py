@@ -20,7 +20,8 @@ LIB = PKG / "libb3gpu.so"
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_LIB = ORACLE_DIR / "liboracle.so"
 
-CU_SOURCES = ["primitives.cu", "broadphase.cu", "narrowphase.cu", "solver.cu", "integrate.cu", "world.cu"]
+CU_SOURCES = ["primitives.cu", "broadphase.cu", "narrowphase.cu", "solver.cu", "integrate.cu", "world.cu",
+              "noalloc.cu"]
 CPP_SOURCES = ["hull.cpp"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 

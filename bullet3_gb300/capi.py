@@ -80,7 +80,7 @@ EXPORTS = [
     "b3g_read_impulses", "b3g_get_num_collidables", "b3g_read_registered_bodies", "b3g_read_shape_tables",
     "b3g_set_profiling",
     "b3g_get_stage_times", "b3g_get_launch_count", "b3g_record_event", "b3g_event_elapsed", "b3g_hull_compute",
-]
+    "b3g_grid_pairs_noalloc"]
 
 
 def lib_path() -> Path:

@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1001,5 +1002,63 @@ extern "C" b3gStatus b3g_hull_compute(const float* verts, int stride_bytes, int 
     if (indices_out) std::memcpy(indices_out, t.indices.data(), sizeof(int) * ni);
     if (edges_out && ne) std::memcpy(edges_out, t.edges.data(), sizeof(float) * 3 * ne);
     if (center_out) std::memcpy(center_out, t.center, sizeof(float) * 3);
+    return B3G_OK;
+}
+
+// ------------------------------------------------------------------ allocation-free broadphase
+// Per device: the static scratch array's address and the SM count, looked up on the first call
+// with that device current.
+namespace {
+constexpr int NA_MAX_DEVICES = 64;
+std::mutex g_na_mutex;
+void* g_na_scratch[NA_MAX_DEVICES] = {};
+int g_na_sms[NA_MAX_DEVICES] = {};
+}  // namespace
+
+extern "C" b3gStatus b3g_grid_pairs_noalloc(const void* d_aabbs, int n, float cell_size, int grid_dim, void* d_pairs,
+                                            int max_pairs, int* d_num_pairs, void* cuda_stream) {
+    if (n < 0 || n > B3G_NOALLOC_MAX_AABBS)
+        return fail(B3G_ERR_CAPACITY, "n = %d outside 0..%d (B3G_NOALLOC_MAX_AABBS)", n, B3G_NOALLOC_MAX_AABBS);
+    if (max_pairs < 1 || max_pairs > B3G_NOALLOC_MAX_PAIRS)
+        return fail(B3G_ERR_CAPACITY, "max_pairs = %d outside 1..%d (B3G_NOALLOC_MAX_PAIRS)", max_pairs,
+                    B3G_NOALLOC_MAX_PAIRS);
+    if (grid_dim < 4 || grid_dim > B3G_NOALLOC_MAX_GRID_DIM || (grid_dim & (grid_dim - 1)))
+        return fail(B3G_ERR_CAPACITY, "grid_dim = %d: needs a power of two in 4..%d (B3G_NOALLOC_MAX_GRID_DIM)",
+                    grid_dim, B3G_NOALLOC_MAX_GRID_DIM);
+    if (!(cell_size > 0.f) || !std::isfinite(cell_size))
+        return fail(B3G_ERR_INVALID_ARG, "cell_size must be positive and finite");
+    if ((n > 0 && !d_aabbs) || !d_pairs || !d_num_pairs) return fail(B3G_ERR_INVALID_ARG, "null device buffer");
+    if (reinterpret_cast<uintptr_t>(d_aabbs) % 16 != 0)
+        return fail(B3G_ERR_INVALID_ARG, "d_aabbs must be 16-byte aligned");
+    int dev = -1;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= NA_MAX_DEVICES) return fail(B3G_ERR_UNSUPPORTED, "device index %d not supported", dev);
+    void* scratch = nullptr;
+    int sms = 0;
+    {
+        std::lock_guard<std::mutex> lock(g_na_mutex);
+        if (!g_na_scratch[dev]) {  // first call on this device: one-time lookups
+            int s = 0;
+            CUDA_TRY(cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev));
+            if (s < 1 || s * 4 > B3G_NOALLOC_MAX_SORT_BLOCKS)
+                return fail(B3G_ERR_UNSUPPORTED, "%d SMs: the static sort scratch covers at most %d", s,
+                            B3G_NOALLOC_MAX_SORT_BLOCKS / 4);
+            void* p = nullptr;
+            CUDA_TRY(noalloc_scratch_address(&p));
+            if (!p) return fail(B3G_ERR_CUDA, "cudaGetSymbolAddress returned a null scratch address");
+            g_na_sms[dev] = s;
+            g_na_scratch[dev] = p;
+        }
+        scratch = g_na_scratch[dev];
+        sms = g_na_sms[dev];
+    }
+    int bits = 1;
+    while ((1 << bits) < grid_dim) bits++;
+    int body_bits = 1;
+    while ((1 << body_bits) < n + 1) body_bits++;
+    launch_grid_pairs_noalloc(scratch, sms, static_cast<const b3gAabb*>(d_aabbs), n, 1.f / cell_size, bits,
+                              body_bits, static_cast<b3gPair*>(d_pairs), max_pairs, d_num_pairs,
+                              static_cast<cudaStream_t>(cuda_stream));
+    CUDA_TRY(cudaPeekAtLastError());
     return B3G_OK;
 }

@@ -127,6 +127,14 @@ int launch_contacts(DeviceState& d, float friction, cudaStream_t s);
 int launch_compact_contacts(DeviceState& d, cudaStream_t s);
 int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s);
 cudaError_t solver_prepare();  // kernel attributes, once per device before the first solve
+
+// allocation-free grid broadphase (noalloc.cu): the radix sorts run with sms * 4 blocks, so the
+// static scratch covers devices with up to B3G_NOALLOC_MAX_SORT_BLOCKS / 4 SMs
+#define B3G_NOALLOC_MAX_SORT_BLOCKS 1024
+size_t noalloc_scratch_bytes();
+cudaError_t noalloc_scratch_address(void** out);
+int launch_grid_pairs_noalloc(void* scratch, int num_sms, const b3gAabb* aabbs, int n, float inv_cell, int bits,
+                              int body_bits, b3gPair* pairs, int max_pairs, int* num_out, cudaStream_t s);
 int launch_integrate(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s);
 
 }  // namespace b3g

@@ -220,6 +220,35 @@ b3gStatus b3g_hull_compute(const float* verts, int stride_bytes, int num_verts, 
                            float* verts_out, float* planes_out, int* face_counts_out, int* indices_out,
                            float* edges_out, float* center_out, int* counts6);
 
+/* ---- allocation-free grid broadphase (no counterpart in the reference) -------------------------
+ * The uniform-grid pair search of b3g_calculate_overlapping_pairs, run on the current CUDA device
+ * over caller-owned device buffers, with all scratch in one fixed, statically sized device array
+ * (about 7.4 MB) instead of memory from cudaMalloc.  For callers that must not allocate: code
+ * running inside a frame or real-time loop with a fixed memory budget, or a host that owns every
+ * device allocation itself.
+ *   d_aabbs      n world AABBs (b3gAabb, 32 B each, 16-byte aligned device memory); only the
+ *                min/max xyz are read.  Every AABB is a small proxy: no static-body list.
+ *   n            0 .. B3G_NOALLOC_MAX_AABBS
+ *   cell_size    > 0 and >= the largest AABB extent on any axis (the 27-cell search is then exact)
+ *   grid_dim     power of two, 4 .. B3G_NOALLOC_MAX_GRID_DIM cells per axis (coordinates wrap)
+ *   d_pairs      max_pairs b3gPair slots (device): (a, b, -1, -1), a < b, sorted by (a, b)
+ *   max_pairs    1 .. B3G_NOALLOC_MAX_PAIRS
+ *   d_num_pairs  one device int: the number of overlapping pairs found; when it exceeds
+ *                max_pairs, max_pairs of them (an unspecified subset) are written, sorted
+ *   cuda_stream  cudaStream_t the work is enqueued on (0 = legacy default stream); the call
+ *                returns without waiting for it.
+ * Larger sizes are rejected with B3G_ERR_CAPACITY before anything is enqueued.  The first call
+ * on a device looks up the scratch array's address (cudaGetSymbolAddress) and the SM count: make
+ * it before any stream capture.  No scratch content has to start at zero: each call resets the
+ * counters it uses in its first kernel and validates the never-cleared cell table on use.  All
+ * calls on one device share the one scratch array, so calls whose work overlaps in time (two
+ * streams, or two host threads) race: serialise them on one stream or with events. */
+#define B3G_NOALLOC_MAX_AABBS 65536
+#define B3G_NOALLOC_MAX_PAIRS 262144
+#define B3G_NOALLOC_MAX_GRID_DIM 64
+b3gStatus b3g_grid_pairs_noalloc(const void* d_aabbs, int n, float cell_size, int grid_dim, void* d_pairs,
+                                 int max_pairs, int* d_num_pairs, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
