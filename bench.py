@@ -33,6 +33,14 @@ WORKLOAD = ("box pile 64x64x64 = 262,144 unit boxes resting in 64x64 columns on 
             "(settled form of the spacing-1.1 jitter-0.05 lattice, seed 0), PGS 10 iterations, dt 1/60")
 
 
+def solver_mode_code(args):
+    """Oracle solver mode: 0 PGS (contact rows then friction rows), 1 Jacobi, 2 PGS with rows
+    interleaved per contact point (B3_SOLVER_INTERLEAVE_CONTACT_AND_FRICTION_CONSTRAINTS)."""
+    if args.solver != "pgs":
+        return 1
+    return 2 if args.row_order == "interleaved" else 0
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -44,6 +52,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--solver", choices=["pgs", "jacobi"], default="pgs")
     p.add_argument("--iterations", type=int, default=10)
+    p.add_argument("--row-order", choices=["interleaved", "separate"], default="interleaved",
+                   help="PGS row order: per contact point (reference B3_SOLVER_INTERLEAVE_CONTACT_AND_FRICTION_"
+                        "CONSTRAINTS mode) or all contact rows then all friction rows (reference default)")
     return p.parse_args()
 
 
@@ -171,7 +182,7 @@ def reference_arm(args):
     if rank != 0:
         return 0
     scene = make_scene(args.nx)
-    mode = 0 if args.solver == "pgs" else 1
+    mode = solver_mode_code(args)
     # warm-up steps are run (untimed) from the same initial state; each timed step is one full
     # composed CPU step of the whole 262,144-body scene
     cpu_run(scene, args.warmup, args.iterations, mode) if args.warmup else None
@@ -180,7 +191,8 @@ def reference_arm(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * secs / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "bodies": n, "solver": args.solver, "iterations": args.iterations},
+            "config": {"workload": WORKLOAD, "bodies": n, "solver": args.solver, "iterations": args.iterations,
+                       "row_order": args.row_order},
             "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": threads, "kind": "port",
                              "sample": f"{args.steps} composed CPU steps of the full {n}-body scene"},
             "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -205,7 +217,8 @@ def gpu_arm(args):
     capi.load()
     scene = make_scene(args.nx)
     mode = capi.SOLVER_PGS if args.solver == "pgs" else capi.SOLVER_JACOBI
-    cfg = b3Config(solver_mode=mode, solver_iterations=args.iterations, use_cuda_graph=True)
+    cfg = b3Config(solver_mode=mode, solver_iterations=args.iterations, use_cuda_graph=True,
+                   pgs_interleave=args.solver == "pgs" and args.row_order == "interleaved")
     np_, bp, pl = scenes.load_scene(scene, cfg, device=local)
     h = np_.world.handle
     N = scene.num_bodies
@@ -293,7 +306,7 @@ def gpu_arm(args):
     # ---- CPU baseline: the oracle's composed step on the same scene, bounded sample
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        secs, threads, n = cpu_run(scene, args.cpu_steps, args.iterations, 0 if args.solver == "pgs" else 1)
+        secs, threads, n = cpu_run(scene, args.cpu_steps, args.iterations, solver_mode_code(args))
         cpu = {"value": n * args.cpu_steps / secs, "unit": "body-steps/s", "cores": threads, "kind": "port",
                "sample": f"{args.cpu_steps} composed CPU oracle steps of the same {n}-body scene from its initial state"}
 
@@ -302,6 +315,7 @@ def gpu_arm(args):
                 "warmup": max(3, args.warmup), "ms_per_step": 1000 * t_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": WORKLOAD, "bodies": N, "solver": args.solver, "iterations": args.iterations,
+                           "row_order": args.row_order,
                            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                            "l2": "inputs larger than L2 (constraint rows and pair buffers exceed 129 MB)",
                            "pairs": P_, "manifolds": C_, "contact_points": st.num_points, "colors": st.num_colors},

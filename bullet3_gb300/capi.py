@@ -30,7 +30,8 @@ for _dt, _sz in ((BODY, 80), (INERTIA, 96), (COLLIDABLE, 16), (HULL, 96), (FACE,
 
 SHAPE_CONVEX_HULL, SHAPE_PLANE, SHAPE_SPHERE = 3, 4, 7
 SOLVER_PGS, SOLVER_JACOBI = 0, 1
-PGS_PARTITIONS_AUTO, PGS_PARTITIONS_GLOBAL_DELTAS, PGS_PARTITIONS_NONE = 0, 1, 2
+PGS_PARTITIONS_AUTO, PGS_PARTITIONS_GLOBAL_DELTAS, PGS_PARTITIONS_NONE, PGS_PARTITIONS_SHARED = 0, 1, 2, 3
+PGS_PARTITIONS_STREAMED = 4
 
 FLAG_PAIR_OVERFLOW = 0x1
 FLAG_CONTACT_OVERFLOW = 0x2
@@ -50,7 +51,8 @@ class b3gConfig(C.Structure):
                 ("solver_iterations", C.c_int), ("erp", C.c_float), ("contact_threshold", C.c_float),
                 ("contact_friction", C.c_float), ("residual_tol", C.c_float), ("update_world_inertia", C.c_int),
                 ("use_cuda_graph", C.c_int), ("warm_start", C.c_int), ("barrier_spin_limit", C.c_int),
-                ("solver_blocks_per_sm", C.c_int), ("pgs_partitions", C.c_int), ("reserved", C.c_int * 5)]
+                ("solver_blocks_per_sm", C.c_int), ("pgs_partitions", C.c_int), ("pgs_interleave", C.c_int),
+                ("reserved", C.c_int * 4)]
 
 
 class b3gStepStats(C.Structure):

@@ -158,8 +158,8 @@ B3G_DEV float4 ldg4(const b3gFloat4* p) { return __ldg(reinterpret_cast<const fl
 // and the barrier returns false in every block (they all poll the abort flag), so a
 // kernel can unwind and the host sees B3G_FLAG_BARRIER_TIMEOUT instead of a hang.
 struct GridBarrier {
-    unsigned int* count;      // arrivals in the current generation
-    unsigned int* gen;        // generation counter
+    unsigned int* count;      // arrivals since the launch started (reset to 0 before each launch)
+    unsigned int* gen;        // unused (kept for layout)
     unsigned int* abort_flag; // non-zero once any block gave up
     unsigned int* status;     // device status word
 };
@@ -168,35 +168,51 @@ struct GridBarrier {
 #define B3G_BARRIER_SPIN_LIMIT (1u << 22)
 #endif
 
+B3G_DEV unsigned int ld_acquire_gpu(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+B3G_DEV void red_release_add_gpu(unsigned int* p, unsigned int v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Barriers this block has passed in the current launch (thread 0's count; the kernel zeroes it
+// with grid_barrier_begin before its first barrier).
+B3G_DEV unsigned int& grid_barrier_epoch() {
+    __shared__ unsigned int s_epoch;
+    return s_epoch;
+}
+B3G_DEV void grid_barrier_begin() {
+    if (threadIdx.x == 0) grid_barrier_epoch() = 0;
+}
+
+// Grid-wide barrier of a cooperative launch: one arrival counter that only grows during the
+// launch (zeroed before the launch); the n-th barrier completes when it reaches n * nblocks.
+// Arrival is a fire-and-forget release add, waiting is acquire loads of the counter.  A wait
+// gives up after spin_limit polls (or when another block gave up): it raises the abort flag and
+// the timeout status bit and returns false, and every later barrier of the launch returns false.
 B3G_DEV bool grid_barrier(const GridBarrier& b, unsigned int nblocks, unsigned int spin_limit) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        volatile unsigned int* vgen = b.gen;
-        volatile unsigned int* vabort = b.abort_flag;
-        unsigned int g = *vgen;
-        __threadfence();
-        unsigned int arrived = atomicAdd(b.count, 1u);
-        if (arrived == nblocks - 1) {
-            atomicExch(b.count, 0u);
-            __threadfence();
-            atomicAdd(b.gen, 1u);
-        } else {
-            unsigned int spins = 0;
-            while (*vgen == g) {
-                if (*vabort) { ok = 0; break; }
-                if (++spins >= spin_limit) {
-                    atomicExch(b.abort_flag, 1u);
-                    atomicOr(b.status, B3G_FLAG_BARRIER_TIMEOUT);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
+        const unsigned int target = (++grid_barrier_epoch()) * nblocks;
+        red_release_add_gpu(b.count, 1u);
+        unsigned int spins = 0;
+        while (ld_acquire_gpu(b.count) < target) {
+            if (*(volatile unsigned int*)b.abort_flag) { ok = 0; break; }
+            if (++spins >= spin_limit) {
+                atomicExch(b.abort_flag, 1u);
+                atomicOr(b.status, B3G_FLAG_BARRIER_TIMEOUT);
+                ok = 0;
+                break;
             }
+            if (spins > 64) __nanosleep(32);
         }
-        __threadfence();
-        if (*vabort) ok = 0;
+        // (a block that reaches the target without waiting needs no abort check: every block
+        // arrived, so none gave up before this barrier; a later barrier sees any later abort)
         s_ok = ok;
     }
     __syncthreads();

@@ -47,7 +47,7 @@ struct SolverArgs {
     int4* hdr;                // bodyA, bodyB, active point mask, num points
     float2* inv_mass;         // invMass A, B
     int4* hdr_ord;            // PGS: colour-ordered copies
-    float2* inv_mass_ord;
+    float4* inv_mass_ord;     // (invMass A, invMass B, 0, 0): 16 B so tiles copy in bulk
     float4* dv;               // per body: [2b] lin, [2b+1] ang (PGS, and Jacobi averaged delta)
     float4* dv_sum;           // Jacobi: per body sum of split deltas from the last averaging
     float4* split;            // Jacobi: per manifold 4 float4: A lin, A ang, B lin, B ang
@@ -68,6 +68,8 @@ struct SolverArgs {
     int num_dynamic;          // length of sorted_bodies (0: every manifold is cross-partition)
     int chunk;                // dynamic bodies per block partition
     int use_smem;             // block-local body deltas in shared memory
+    int tile_R;               // > 0: block-local records streamed through shared memory, R per tile
+    int interleave;           // PGS: each point's friction rows right after its contact row
     unsigned long long* claim;
     unsigned long long* mask;  // per body: colours already taken by its manifolds
     unsigned long long* claim_x;  // PGS: the same two arrays for the cross-partition colouring
@@ -272,27 +274,72 @@ __device__ __forceinline__ b3gMat3 ld_mat(const b3gMat3* p) {
     return r;
 }
 
+// ---- bulk asynchronous copies (TMA, untiled) into shared memory, completed on an mbarrier
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// global -> shared, `bytes` a multiple of 16, both addresses 16-byte aligned
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait for the phase with the given parity; false after `limit` polls
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, unsigned limit) {
+    for (unsigned i = 0; i < limit; i++) {
+        if (mbar_test(bar, parity)) return true;
+        __nanosleep(20);
+    }
+    return false;
+}
+// generic-proxy accesses before async-proxy (bulk copy) accesses of the same memory
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// Record loads: from shared memory (a streamed tile) or through L2 (ld.cg) -- records may have
+// been written earlier in the same kernel, so never through the non-coherent read-only path.
+template <bool SMEM, typename T>
+__device__ __forceinline__ T ldrec(const T* p) {
+    if constexpr (SMEM)
+        return *p;
+    else
+        return __ldcg(p);
+}
+
 // Contact rows (pass 0) or friction rows (pass 1) of record m of `sp` against the given body
-// deltas.  Records may have been written earlier in the same kernel (colour-ordered copy), so
-// they are read through L2 (ld.cg), never through the non-coherent read-only path.  With
-// LOAD_ALL every point slot is loaded whatever the active mask (slots are always allocated; the
-// inactive ones are never used), so the loads do not wait for the manifold header.
-template <bool LOAD_ALL = false>
-__device__ __forceinline__ void solve_manifold(const SolverArgs& a, const SolverPoints& sp, int m, int pass,
+// deltas; the updated applied impulses go to imp_out[0..3] (global memory).  With LOAD_ALL every
+// point slot is loaded whatever the active mask (slots are always allocated; the inactive ones are
+// never used), so the loads do not wait for the manifold header.
+template <bool LOAD_ALL, bool SMEM>
+__device__ __forceinline__ void solve_manifold(const SolverPoints& sp, int m, float4* imp_out, int pass,
                                                const int4& h, float imA, float imB, const b3gMat3& IA,
                                                const b3gMat3& IB, v3& dlA, v3& daA, v3& dlB, v3& daB, float& res_d,
                                                float& res_l) {
     const int mask = h.z;
     const size_t base = (size_t)m * 4;
-    const float4 nf = __ldcg(&sp.nf[m]);
+    const float4 nf = ldrec<SMEM>(&sp.nf[m]);
     const v3 n = xyz(nf);
     float4 r1[4], r2[4], im[4];
 #pragma unroll
     for (int j = 0; j < 4; j++) {
         if (LOAD_ALL || (mask & (1 << j))) {
-            r1[j] = __ldcg(&sp.rel1[base + j]);
-            r2[j] = __ldcg(&sp.rel2[base + j]);
-            im[j] = __ldcg(&sp.imp[base + j]);
+            r1[j] = ldrec<SMEM>(&sp.rel1[base + j]);
+            r2[j] = ldrec<SMEM>(&sp.rel2[base + j]);
+            im[j] = ldrec<SMEM>(&sp.imp[base + j]);
         }
     }
     if (pass == 0) {
@@ -308,7 +355,7 @@ __device__ __forceinline__ void solve_manifold(const SolverArgs& a, const Solver
             float old = im[j].x;
             float nw = solve_row<false>(n, r1[j].w, r2[j].w, old, r1xn, r2xn, angA, angB, 0.f, LARGE_UPPER, dlA, daA,
                                         dlB, daB, imA, imB);
-            __stcg(&sp.imp[base + j].x, nw);
+            __stcg(&imp_out[j].x, nw);
             float nd = nw - old;
             res_d += nd * nd;
             res_l += nw * nw;
@@ -320,17 +367,33 @@ __device__ __forceinline__ void solve_manifold(const SolverArgs& a, const Solver
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             if (LOAD_ALL || (mask & (1 << j))) {
-                d2[j] = __ldcg(&sp.dir2[base + j]);
-                d1[j] = __ldcg(&sp.dir1[base + j]);
-                rf[j] = __ldcg(&sp.rhsf[base + j]);
+                d2[j] = ldrec<SMEM>(&sp.dir2[base + j]);
+                d1[j] = ldrec<SMEM>(&sp.dir1[base + j]);
+                rf[j] = ldrec<SMEM>(&sp.rhsf[base + j]);
             }
         }
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             if (!(mask & (1 << j))) continue;
-            const float total = im[j].x;
+            float total = im[j].x;
             const v3 rel1 = xyz(r1[j]), rel2 = xyz(r2[j]);
             float f2 = im[j].y, f1 = im[j].z;
+            if (pass == 2) {
+                // interleaved (B3_SOLVER_INTERLEAVE_CONTACT_AND_FRICTION_CONSTRAINTS,
+                // b3PgsJacobiSolver.cpp:1334-1377): this point's contact row first, its friction
+                // rows bounded by the new impulse
+                v3 r1xn = cross3(rel1, n);
+                v3 ta1 = cross3(rel2, n);
+                v3 r2xn = -ta1;
+                v3 angA = imul(IA, r1xn);
+                v3 angB = imul(IB, -ta1);
+                const float old = total;
+                total = solve_row<false>(n, r1[j].w, r2[j].w, old, r1xn, r2xn, angA, angB, 0.f, LARGE_UPPER, dlA,
+                                         daA, dlB, daB, imA, imB);
+                const float nd = total - old;
+                res_d += nd * nd;
+                res_l += total * total;
+            }
             if (total > 0.f) {
                 const float lower = -(fr * total), upper = fr * total;
                 {
@@ -353,7 +416,9 @@ __device__ __forceinline__ void solve_manifold(const SolverArgs& a, const Solver
                     res_d += nd * nd;
                     f1 = nw;
                 }
-                __stcg(&sp.imp[base + j], make_float4(total, f2, f1, 0.f));
+                __stcg(&imp_out[j], make_float4(total, f2, f1, 0.f));
+            } else if (pass == 2) {
+                __stcg(&imp_out[j].x, total);
             }
             res_l += f2 * f2 + f1 * f1;
         }
@@ -480,6 +545,61 @@ __device__ __forceinline__ b3gMat3 load_inertia_local(const SolverArgs& a, const
     return ld_mat(&a.inertias[body].invInertiaWorld);
 }
 
+// ---- streamed tiles: one tile = up to R consecutive block-local manifolds of one colour, copied
+// into a shared-memory buffer laid out as [hdr R][inv mass R][nf R][rel1 4R][rel2 4R][imp 4R]
+// [dir2 4R][dir1 4R][rhsf 4R] (16-byte elements except rhsf's 8, so every piece is a 16-byte
+// multiple at a 16-byte aligned offset); the contact pass copies only the first six pieces.
+__device__ __forceinline__ unsigned tile_bytes(int cnt, int pass) { return (unsigned)cnt * (pass ? 400u : 240u); }
+
+__device__ __forceinline__ void issue_tile(const SolverArgs& a, char* buf, int R, unsigned long long* bar, int k0,
+                                           int cnt, int pass) {
+    const unsigned c = (unsigned)cnt;
+    mbar_expect_tx(bar, tile_bytes(cnt, pass));
+    bulk_g2s(buf, a.hdr_ord + k0, 16u * c, bar);
+    bulk_g2s(buf + 16 * R, a.inv_mass_ord + k0, 16u * c, bar);
+    bulk_g2s(buf + 32 * R, a.sp_ord.nf + k0, 16u * c, bar);
+    bulk_g2s(buf + 48 * R, a.sp_ord.rel1 + 4 * (size_t)k0, 64u * c, bar);
+    bulk_g2s(buf + 112 * R, a.sp_ord.rel2 + 4 * (size_t)k0, 64u * c, bar);
+    bulk_g2s(buf + 176 * R, a.sp_ord.imp + 4 * (size_t)k0, 64u * c, bar);
+    if (pass) {
+        bulk_g2s(buf + 240 * R, a.sp_ord.dir2 + 4 * (size_t)k0, 64u * c, bar);
+        bulk_g2s(buf + 304 * R, a.sp_ord.dir1 + 4 * (size_t)k0, 64u * c, bar);
+        bulk_g2s(buf + 368 * R, a.sp_ord.rhsf + 4 * (size_t)k0, 32u * c, bar);
+    }
+}
+
+__device__ __forceinline__ void bulk_prefetch_l2(const void* p, unsigned bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+// L2 prefetch of the ordered records [k0, k0 + cnt) one pass reads (no-op for cnt <= 0)
+__device__ __forceinline__ void prefetch_records_l2(const SolverArgs& a, int k0, int cnt, int pass) {
+    if (cnt <= 0) return;
+    const unsigned c = (unsigned)cnt;
+    bulk_prefetch_l2(a.hdr_ord + k0, 16u * c);
+    bulk_prefetch_l2(a.inv_mass_ord + k0, 16u * c);
+    bulk_prefetch_l2(a.sp_ord.nf + k0, 16u * c);
+    bulk_prefetch_l2(a.sp_ord.rel1 + 4 * (size_t)k0, 64u * c);
+    bulk_prefetch_l2(a.sp_ord.rel2 + 4 * (size_t)k0, 64u * c);
+    bulk_prefetch_l2(a.sp_ord.imp + 4 * (size_t)k0, 64u * c);
+    if (pass) {
+        bulk_prefetch_l2(a.sp_ord.dir2 + 4 * (size_t)k0, 64u * c);
+        bulk_prefetch_l2(a.sp_ord.dir1 + 4 * (size_t)k0, 64u * c);
+        bulk_prefetch_l2(a.sp_ord.rhsf + 4 * (size_t)k0, 32u * c);
+    }
+}
+
+__device__ __forceinline__ SolverPoints tile_view(char* buf, int R) {
+    SolverPoints v;
+    v.nf = reinterpret_cast<float4*>(buf + 32 * R);
+    v.rel1 = reinterpret_cast<float4*>(buf + 48 * R);
+    v.rel2 = reinterpret_cast<float4*>(buf + 112 * R);
+    v.imp = reinterpret_cast<float4*>(buf + 176 * R);
+    v.dir2 = reinterpret_cast<float4*>(buf + 240 * R);
+    v.dir1 = reinterpret_cast<float4*>(buf + 304 * R);
+    v.rhsf = reinterpret_cast<float2*>(buf + 368 * R);
+    return v;
+}
+
 // Partition owning a dynamic body: its cell-order position / chunk, or -2 when the body is not in
 // the cell-sorted list (inverse mass changed after upload, or no broadphase ran this step).
 __device__ __forceinline__ int owner_of(const SolverArgs& a, int body) {
@@ -501,7 +621,8 @@ __device__ __forceinline__ int owner_of(const SolverArgs& a, int body) {
 // Group key = owner * NC + colour (block-local) or nblocks * NC + colour (cross), NC = number of
 // block-local colours; the solve order (b3g_read_solve_order) is the manifolds sorted by key.
 __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
-    extern __shared__ float s_dv[];
+    extern __shared__ __align__(128) float s_dv[];
+    grid_barrier_begin();
     const int nc = *a.d_nc;
     const unsigned nb = gridDim.x;
     const int G = gridDim.x;
@@ -576,10 +697,16 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
         rounds = r + 1;
         if (*((volatile int*)&a.remaining[r]) == 0) break;
     }
+    // highest used colour of each colouring: one L2 read per lane, then a warp vote
     int ncl = 0, ncx = 0;
-    for (int c = 0; c < 64; c++) {
-        if (*((volatile int*)&a.color_fill[c]) > 0) ncl = c + 1;
-        if (*((volatile int*)&a.color_fill[c + 64]) > 0) ncx = c + 1;
+    {
+        const int lane = threadIdx.x & 31;
+        const unsigned l0 = __ballot_sync(0xffffffffu, __ldcg(&a.color_fill[lane]) > 0);
+        const unsigned l1 = __ballot_sync(0xffffffffu, __ldcg(&a.color_fill[lane + 32]) > 0);
+        const unsigned x0 = __ballot_sync(0xffffffffu, __ldcg(&a.color_fill[lane + 64]) > 0);
+        const unsigned x1 = __ballot_sync(0xffffffffu, __ldcg(&a.color_fill[lane + 96]) > 0);
+        ncl = l1 ? 64 - __clz(l1) : (l0 ? 32 - __clz(l0) : 0);
+        ncx = x1 ? 64 - __clz(x1) : (x0 ? 32 - __clz(x0) : 0);
     }
     const bool overflow = rounds > 0 && *((volatile int*)&a.remaining[rounds - 1]) != 0 && nc > 0;
     const int NC = ncl > 0 ? ncl : 1;  // key stride of the block-local groups
@@ -638,7 +765,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
             w = (int)(((unsigned)la & 0xffffu) | (((unsigned)lb & 0xffffu) << 16));
         }
         a.hdr_ord[k] = make_int4(h.x, h.y, h.z, w);
-        a.inv_mass_ord[k] = im;
+        a.inv_mass_ord[k] = make_float4(im.x, im.y, 0.f, 0.f);
         a.sp_ord.nf[k] = __ldcg(&a.sp.nf[m]);
         for (int j = 0; j < 4; j++) {
             if (!(h.z & (1 << j))) continue;
@@ -651,6 +778,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
             a.sp_ord.imp[t] = __ldcg(&a.sp.imp[s]);
         }
     }
+    if (a.tile_R > 0) fence_proxy_async();  // the ordered records are read by bulk copies below
     if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
     // ---- iterations.  Segments of one pass: the NC block-local colours (__syncthreads between
     // them), then the ncx cross-partition colours and the colour-overflow leftovers (grid barrier
@@ -659,6 +787,46 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
     const int myN = max(0, min(chunk, nd - myLo));
     const int nseg = NC + ncx + (overflow ? 1 : 0);
     float* s_inv = s_dv + 6 * chunk;  // owned bodies' world inverse inertia (fixed during the solve)
+    // streamed tiles: two buffers after the owned-body arrays, then two mbarriers and the tile list
+    const int R = a.tile_R;
+    char* tbuf = reinterpret_cast<char*>(s_dv) + ((60 * (size_t)chunk + 15) & ~(size_t)15);
+    unsigned long long* tbar = reinterpret_cast<unsigned long long*>(tbuf + 2 * (size_t)R * B3G_PGS_TILE_BYTES);
+    int2* tiles = reinterpret_cast<int2*>(tbar + 2);
+    __shared__ int s_ntiles;
+    unsigned tpar0 = 0, tpar1 = 0;  // phase parity of each buffer's mbarrier
+    if (R > 0) {
+        if (threadIdx.x == 0) {
+            int nt = 0;
+            for (int c = 0; c < NC && nt >= 0; c++) {
+                const int lo = __ldcg(&goff[blockIdx.x * NC + c]), hi = __ldcg(&goff[blockIdx.x * NC + c + 1]);
+                for (int k0 = lo; k0 < hi; k0 += R) {
+                    if (nt == B3G_PGS_MAX_TILES) {  // too many tiles: this block reads records directly
+                        nt = -1;
+                        break;
+                    }
+                    tiles[nt++] = make_int2(k0, min(R, hi - k0));
+                }
+            }
+            s_ntiles = nt;
+            mbar_init(&tbar[0], 1);
+            mbar_init(&tbar[1], 1);
+            fence_mbar_init();
+        }
+        __syncthreads();
+    }
+    const int ntiles = R > 0 ? s_ntiles : -1;
+    // [lo, hi) of every segment, read once: block-local colours, cross colours, leftovers
+    __shared__ int2 s_seg[2 * 64 + 2];
+    for (int sg = threadIdx.x; sg < nseg; sg += blockDim.x) {
+        int lo = ncol, hi = nc;
+        if (sg < NC + ncx) {
+            const int key = sg < NC ? blockIdx.x * NC + sg : G * NC + sg - NC;
+            lo = __ldcg(&goff[key]);
+            hi = __ldcg(&goff[key + 1]);
+        }
+        s_seg[sg] = make_int2(lo, hi);
+    }
+    __syncthreads();
     if (a.use_smem) {
         for (int l = threadIdx.x; l < myN; l += blockDim.x) {
             const b3gMat3 I = ld_mat(&a.inertias[a.sorted_bodies[myLo + l]].invInertiaWorld);
@@ -669,9 +837,12 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
         }
     }
     bool ok = true;
+    // passes of one iteration: contact rows then friction rows, or one interleaved pass (2)
+    const int npasses = a.interleave ? 1 : 2;
     for (int it = 0; it < a.iterations; it++) {
         float res_d = 0.f, res_l = 0.f;
-        for (int pass = 0; pass < 2; pass++) {
+        for (int ps = 0; ps < npasses; ps++) {
+            const int pass = a.interleave ? 2 : ps;
             if (a.use_smem) {
                 for (int l = threadIdx.x; l < myN; l += blockDim.x) {
                     v3 dl, dw;
@@ -682,20 +853,83 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
                 }
                 __syncthreads();
             }
+            // block-local phase, streamed: tile t+1 is copied while tile t is solved
+            if (ntiles > 0) {
+                if (threadIdx.x == 0) {
+                    fence_proxy_async();
+                    issue_tile(a, tbuf, R, &tbar[0], tiles[0].x, tiles[0].y, pass);
+                }
+                for (int t = 0; t < ntiles; t++) {
+                    const int b = t & 1;
+                    char* buf = tbuf + (size_t)b * R * B3G_PGS_TILE_BYTES;
+                    if (threadIdx.x == 0 && t + 1 < ntiles) {
+                        fence_proxy_async();
+                        issue_tile(a, tbuf + (size_t)(b ^ 1) * R * B3G_PGS_TILE_BYTES, R, &tbar[b ^ 1],
+                                   tiles[t + 1].x, tiles[t + 1].y, pass);
+                    }
+                    const bool got = mbar_wait(&tbar[b], b ? tpar1 : tpar0, a.spin_limit);
+                    if (b)
+                        tpar1 ^= 1u;
+                    else
+                        tpar0 ^= 1u;
+                    if (__syncthreads_or(!got)) {
+                        // a copy never completed: raise the abort, drain what is still in flight
+                        if (threadIdx.x == 0) {
+                            atomicExch(a.bar.abort_flag, 1u);
+                            atomicOr(a.bar.status, B3G_FLAG_BARRIER_TIMEOUT);
+                            if (!got) mbar_wait(&tbar[b], b ? tpar1 ^ 1u : tpar0 ^ 1u, a.spin_limit);
+                            if (t + 1 < ntiles) mbar_wait(&tbar[b ^ 1], b ? tpar0 : tpar1, a.spin_limit);
+                        }
+                        __syncthreads();
+                        return;
+                    }
+                    const int2 tl = tiles[t];
+                    const SolverPoints tv = tile_view(buf, R);
+                    for (int i = threadIdx.x; i < tl.y; i += blockDim.x) {
+                        const int4 h = reinterpret_cast<const int4*>(buf)[i];
+                        const float4 im = reinterpret_cast<const float4*>(buf + 16 * R)[i];
+                        const int la = (h.w & 0xffff) == 0xffff ? -1 : (h.w & 0xffff);
+                        const int lb = ((unsigned)h.w >> 16) == 0xffffu ? -1 : (int)((unsigned)h.w >> 16);
+                        v3 dlA = mk3(0, 0, 0), daA = mk3(0, 0, 0), dlB = mk3(0, 0, 0), daB = mk3(0, 0, 0);
+                        if (im.x != 0.f) load_dv_local(a, s_dv, h.x, la, dlA, daA);
+                        if (im.y != 0.f) load_dv_local(a, s_dv, h.y, lb, dlB, daB);
+                        const b3gMat3 IA = load_inertia_local(a, s_inv, h.x, la);
+                        const b3gMat3 IB = load_inertia_local(a, s_inv, h.y, lb);
+                        solve_manifold<true, true>(tv, i, a.sp_ord.imp + 4 * (size_t)(tl.x + i), pass, h, im.x, im.y,
+                                                   IA, IB, dlA, daA, dlB, daB, res_d, res_l);
+                        if (im.x != 0.f) store_dv_local(a, s_dv, h.x, la, dlA, daA);
+                        if (im.y != 0.f) store_dv_local(a, s_dv, h.y, lb, dlB, daB);
+                    }
+                    __syncthreads();
+                }
+            }
             for (int sg = 0; sg < nseg; sg++) {
                 const bool local = sg < NC;
+                const int2 seg = s_seg[sg];
+                // warm L2 with this block's records of the next segment while this one runs
+                if (threadIdx.x == 0) {
+                    int ns = sg + 1, npass = pass;
+                    if (ns == nseg) {
+                        ns = 0;
+                        if (!a.interleave) npass ^= 1;
+                    }
+                    if (ns < NC) {
+                        if (ntiles < 0) prefetch_records_l2(a, s_seg[ns].x, s_seg[ns].y - s_seg[ns].x, npass);
+                    } else if (ns < NC + ncx) {
+                        const int k0 = s_seg[ns].x + blockIdx.x * blockDim.x;
+                        prefetch_records_l2(a, k0, min((int)blockDim.x, s_seg[ns].y - k0), npass);
+                    }
+                }
                 int first, hi, step;
                 if (local) {
-                    const int key = blockIdx.x * NC + sg;
-                    first = __ldcg(&goff[key]) + threadIdx.x;
-                    hi = __ldcg(&goff[key + 1]);
+                    first = seg.x + threadIdx.x;
+                    hi = seg.y;
                     step = blockDim.x;
+                    if (ntiles >= 0) first = hi;  // already solved by the streamed tiles
                 } else if (sg < NC + ncx) {
-                    const int key = G * NC + sg - NC;
-                    const int lo = __ldcg(&goff[key]);
-                    hi = __ldcg(&goff[key + 1]);
-                    if (lo == hi) continue;  // uniform across blocks: goff is read-only here
-                    first = lo + tid;
+                    if (seg.x == seg.y) continue;  // uniform across blocks
+                    first = seg.x + tid;
+                    hi = seg.y;
                     step = stride;
                 } else {  // leftovers: one thread, in manifold order (always correct, slow)
                     first = ncol;
@@ -707,7 +941,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
                     // no early exit for manifolds without active points: their deltas are read and
                     // written back unchanged, and the record loads need not wait for the header
                     const int4 h = __ldcg(&a.hdr_ord[k]);
-                    const float2 im = __ldcg(&a.inv_mass_ord[k]);
+                    const float4 im = __ldcg(&a.inv_mass_ord[k]);
                     int la = -1, lb = -1;
                     if (smem_here) {
                         la = (h.w & 0xffff) == 0xffff ? -1 : (h.w & 0xffff);
@@ -718,8 +952,8 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
                     if (im.y != 0.f) load_dv_local(a, s_dv, h.y, lb, dlB, daB);
                     const b3gMat3 IA = load_inertia_local(a, s_inv, h.x, la);
                     const b3gMat3 IB = load_inertia_local(a, s_inv, h.y, lb);
-                    solve_manifold<true>(a, a.sp_ord, k, pass, h, im.x, im.y, IA, IB, dlA, daA, dlB, daB, res_d,
-                                         res_l);
+                    solve_manifold<true, false>(a.sp_ord, k, a.sp_ord.imp + 4 * (size_t)k, pass, h, im.x, im.y, IA,
+                                                IB, dlA, daA, dlB, daB, res_d, res_l);
                     if (im.x != 0.f) store_dv_local(a, s_dv, h.x, la, dlA, daA);
                     if (im.y != 0.f) store_dv_local(a, s_dv, h.y, lb, dlB, daB);
                 }
@@ -734,6 +968,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
                         }
                     }
                 }
+                if (R > 0) fence_proxy_async();  // impulses written above are read by later bulk copies
                 if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
             }
         }
@@ -783,6 +1018,7 @@ __device__ __forceinline__ void jacobi_average(const SolverArgs& a, int tid, int
 }
 
 __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_jacobi(SolverArgs a) {
+    grid_barrier_begin();
     const int nc = *a.d_nc;
     const unsigned nb = gridDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -801,7 +1037,8 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_jacobi(SolverArgs a) {
                 if (h.z) {
                     const b3gMat3 IA = ld_mat(&a.inertias[h.x].invInertiaWorld);
                     const b3gMat3 IB = ld_mat(&a.inertias[h.y].invInertiaWorld);
-                    solve_manifold(a, a.sp, m, pass, h, im.x, im.y, IA, IB, dlA, daA, dlB, daB, res_d, res_l);
+                    solve_manifold<false, false>(a.sp, m, a.sp.imp + (size_t)m * 4, pass, h, im.x, im.y, IA, IB, dlA,
+                                                 daA, dlB, daB, res_d, res_l);
                 }
                 __stcg(&a.split[4 * m + 0], f4(dlA, 0.f));
                 __stcg(&a.split[4 * m + 1], f4(daA, 0.f));
@@ -914,6 +1151,8 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     a.num_dynamic = 0;
     a.chunk = 1;
     a.use_smem = 0;
+    a.tile_R = 0;
+    a.interleave = cfg.pgs_interleave ? 1 : 0;
     a.claim = d.color_claim;
     a.mask = d.color_claim + d.num_bodies;
     a.claim_x = d.color_claim + 2 * (size_t)d.num_bodies;
@@ -957,20 +1196,39 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     if (jac) {
         sgrid = solver_grid(d, (const void*)k_solve_jacobi, bps, 0);
     } else {
-        const bool parts = cfg.pgs_partitions != B3G_PGS_PARTITIONS_NONE;
+        // AUTO: the split measured fastest on GB300 for 256k-box piles -- block partitions with
+        // shared-memory deltas for interleaved rows, grid-wide colours otherwise
+        const int mode = cfg.pgs_partitions != B3G_PGS_PARTITIONS_AUTO ? cfg.pgs_partitions
+                         : cfg.pgs_interleave                          ? B3G_PGS_PARTITIONS_SHARED
+                                                                       : B3G_PGS_PARTITIONS_NONE;
+        const bool parts = mode != B3G_PGS_PARTITIONS_NONE;
         const int nd = parts && d.cell_sorted_bodies ? d.num_dynamic : 0;
         sgrid = solver_grid(d, (const void*)k_solve_pgs, bps, 0);
         const int chunk = nd > 0 ? (nd + sgrid - 1) / sgrid : 1;
-        smem = (size_t)chunk * 15 * sizeof(float);
-        if (nd == 0 || cfg.pgs_partitions != B3G_PGS_PARTITIONS_AUTO || chunk >= 0xffff ||
-            smem > (size_t)B3G_PGS_MAX_SMEM)
+        const size_t owned = ((size_t)chunk * 15 * sizeof(float) + 15) & ~(size_t)15;
+        const bool shared_mode = mode == B3G_PGS_PARTITIONS_SHARED || mode == B3G_PGS_PARTITIONS_STREAMED;
+        smem = owned;
+        if (nd == 0 || !shared_mode || chunk >= 0xffff || smem > (size_t)B3G_PGS_MAX_SMEM) smem = 0;
+        // streamed tiles: two buffers of R manifolds in what shared memory is left
+        int R = 0;
+        const size_t tile_extra = 16 + 8 * (size_t)B3G_PGS_MAX_TILES;  // mbarriers, tile list
+        if (smem > 0 && mode == B3G_PGS_PARTITIONS_STREAMED && owned + tile_extra < (size_t)B3G_PGS_MAX_SMEM) {
+            size_t r = ((size_t)B3G_PGS_MAX_SMEM - owned - tile_extra) / (2 * (size_t)B3G_PGS_TILE_BYTES);
+            if (r > (size_t)PK_THREADS) r = PK_THREADS;
+            R = (int)(r & ~(size_t)31);
+            if (R < 32) R = 0;
+        }
+        if (R > 0) smem = owned + 2 * (size_t)R * B3G_PGS_TILE_BYTES + tile_extra;
+        // keep the grid co-resident: drop the shared-memory use if it would cost occupancy
+        if (smem > 0 && solver_grid(d, (const void*)k_solve_pgs, bps, smem) != sgrid) {
             smem = 0;
-        // keep the grid co-resident: drop the shared-memory ranges if they would cost occupancy
-        if (smem > 0 && solver_grid(d, (const void*)k_solve_pgs, bps, smem) != sgrid) smem = 0;
+            R = 0;
+        }
         a.sorted_bodies = d.cell_sorted_bodies;
         a.num_dynamic = nd;
         a.chunk = chunk;
         a.use_smem = smem > 0 ? 1 : 0;
+        a.tile_R = R;
         a.group_seg = sgrid * 64 + 64 + 2;
         cudaMemsetAsync(d.group_counts, 0, sizeof(int) * 3 * (size_t)a.group_seg, s);
     }

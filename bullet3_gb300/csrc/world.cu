@@ -156,9 +156,13 @@ extern "C" b3gStatus b3g_create(const b3gConfig* cfg, int cuda_device, b3g_handl
         delete w;
         return fail(B3G_ERR_INVALID_ARG, "grid_dim must be <= 1024 (hash fits in 30 bits)");
     }
-    if (w->cfg.pgs_partitions < B3G_PGS_PARTITIONS_AUTO || w->cfg.pgs_partitions > B3G_PGS_PARTITIONS_NONE) {
+    if (w->cfg.pgs_partitions < B3G_PGS_PARTITIONS_AUTO || w->cfg.pgs_partitions > B3G_PGS_PARTITIONS_STREAMED) {
         delete w;
         return fail(B3G_ERR_INVALID_ARG, "pgs_partitions must be one of B3G_PGS_PARTITIONS_*");
+    }
+    if (w->cfg.pgs_interleave != 0 && w->cfg.pgs_interleave != 1) {
+        delete w;
+        return fail(B3G_ERR_INVALID_ARG, "pgs_interleave must be 0 or 1");
     }
     if (w->cfg.solver_blocks_per_sm < 0) {
         delete w;

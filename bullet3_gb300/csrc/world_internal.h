@@ -83,7 +83,7 @@ struct DeviceState {
     SolverPoints sp;                       // compact contact-point records
     SolverPoints sp_ord;                   // PGS: the same records in colour order
     int4* manifold_hdr_ord = nullptr;
-    float2* manifold_inv_mass_ord = nullptr;
+    float4* manifold_inv_mass_ord = nullptr;  // (invMass A, invMass B, 0, 0)
     const uint32_t* cell_sorted_bodies = nullptr;  // set by the broadphase: dynamic bodies in cell order
     int* body_slot = nullptr;              // body -> position in cell order (PGS partitions)
     int* manifold_group = nullptr;         // PGS processing group of each manifold
@@ -116,9 +116,13 @@ struct DeviceState {
 
 #define B3G_MAX_COLORS 256
 // PGS partitioned solver: at most this many persistent blocks per SM (sizes group_counts), and
-// this much dynamic shared memory per block for the block-local body deltas
+// this much dynamic shared memory per block (owned body deltas and inertias, streamed tiles)
 #define B3G_PGS_MAX_BLOCKS_PER_SM 4
-#define B3G_PGS_MAX_SMEM (160 * 1024)
+#define B3G_PGS_MAX_SMEM (220 * 1024)
+// streamed PGS tiles: bytes per manifold of one tile buffer (header, inverse masses, normal,
+// 4 points x (rel1, rel2, imp, dir2, dir1, rhsf)), and the per-block tile list capacity
+#define B3G_PGS_TILE_BYTES 400
+#define B3G_PGS_MAX_TILES 512
 
 // stage launchers (each returns the number of kernels it launched)
 int launch_aabbs(DeviceState& d, cudaStream_t s);

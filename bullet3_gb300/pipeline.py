@@ -45,6 +45,7 @@ class b3Config:
         self.gravity = (0.0, -9.8, 0.0)
         self.solver_blocks_per_sm = 0
         self.pgs_partitions = capi.PGS_PARTITIONS_AUTO
+        self.pgs_interleave = False
         for k, v in kw.items():
             if not hasattr(self, k):
                 raise AttributeError(k)
@@ -59,7 +60,8 @@ class b3Config:
                                    contact_friction=self.contact_friction,
                                    update_world_inertia=int(self.update_world_inertia), gravity=self.gravity,
                                    solver_blocks_per_sm=self.solver_blocks_per_sm,
-                                   pgs_partitions=self.pgs_partitions)
+                                   pgs_partitions=self.pgs_partitions,
+                                   pgs_interleave=int(self.pgs_interleave))
 
 
 class _World:

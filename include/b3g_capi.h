@@ -46,15 +46,20 @@ typedef enum b3gStatus {
 #define B3G_FLAG_CLIP_OVERFLOW     0x20u
 
 #define B3G_SOLVER_PGS 0      /* b3PgsJacobiSolver(true)  -- graph-coloured Gauss-Seidel on the GPU */
-#define B3G_SOLVER_JACOBI 1
+#define B3G_SOLVER_JACOBI 1   /* b3PgsJacobiSolver(false) -- mass-splitting Jacobi */
 
-/* PGS work split.  AUTO: each block owns a contiguous range of the dynamic bodies in broadphase
- * cell order and solves the manifolds inside its range alone, body deltas staged in shared memory;
- * GLOBAL_DELTAS: the same ranges with the deltas left in global memory; NONE: every manifold is
- * solved grid-wide, one grid barrier per colour.  All three are legal Gauss-Seidel orders. */
+/* PGS work split.  NONE: every manifold is solved grid-wide, one grid barrier per colour.
+ * SHARED: each block owns a contiguous range of the dynamic bodies in broadphase cell order and
+ * solves the manifolds inside its range alone, the range's body deltas and inverse inertias staged
+ * in shared memory (the rest run grid-wide); STREAMED: the same with the block's manifold records
+ * streamed through shared memory in bulk-copied tiles; GLOBAL_DELTAS: the same ranges with the
+ * deltas left in global memory.  AUTO picks the fastest measured on GB300 for piles of 256k boxes:
+ * SHARED with interleaved rows (pgs_interleave), NONE otherwise.  All are legal Gauss-Seidel orders. */
 #define B3G_PGS_PARTITIONS_AUTO 0
 #define B3G_PGS_PARTITIONS_GLOBAL_DELTAS 1
-#define B3G_PGS_PARTITIONS_NONE 2   /* b3PgsJacobiSolver(false) -- mass-splitting Jacobi */
+#define B3G_PGS_PARTITIONS_NONE 2
+#define B3G_PGS_PARTITIONS_SHARED 3
+#define B3G_PGS_PARTITIONS_STREAMED 4
 
 /* One configuration struct replaces b3Config (b3Config.h:4-37) plus the constants the
  * reference hard-codes (dt 1/60 b3GpuPgsContactSolver.cpp:672, damping 0.99
@@ -80,7 +85,11 @@ typedef struct b3gConfig {
     int barrier_spin_limit;    /* polls before a grid barrier gives up (0 = default, about a second) */
     int solver_blocks_per_sm;  /* persistent solver blocks per SM (0 = default; clamped to co-residency) */
     int pgs_partitions;        /* B3G_PGS_PARTITIONS_*: how the PGS solver splits work across blocks */
-    int reserved[5];
+    int pgs_interleave;        /* 1: PGS rows in the order of B3_SOLVER_INTERLEAVE_CONTACT_AND_FRICTION_CONSTRAINTS
+                                  (per point: contact row, then its two friction rows), one pass per iteration;
+                                  0: all contact rows, then all friction rows (the reference default).
+                                  PGS only; the Jacobi solver ignores it */
+    int reserved[4];
 } b3gConfig;
 
 /* Per-step counters, copied once per step from the device. */

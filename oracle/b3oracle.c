@@ -883,8 +883,31 @@ static float solve_row(orow* r, float lower, float upper, int friction, v3* dlA,
     return applied - old;
 }
 
+/* pass 0: contact rows, 1: friction rows, 2: interleaved (per point: its contact row, then its
+ * two friction rows bounded by that row's new impulse), the B3_SOLVER_INTERLEAVE_CONTACT_AND_
+ * FRICTION_CONSTRAINTS branch of solveSingleIteration (b3PgsJacobiSolver.cpp:1334-1377). */
 static void solve_manifold(omanifold* M, int pass, v3* dlA, v3* daA, v3* dlB, v3* daB, double* rd, double* rl) {
     int j, k;
+    if (pass == 2) {
+        for (j = 0; j < 4; j++) {
+            float d, total;
+            if (!(M->mask & (1 << j))) continue;
+            d = solve_row(&M->rows[j], 0.f, 1e10f, 0, dlA, daA, dlB, daB, M->imA, M->imB);
+            *rd += (double)d * d;
+            *rl += (double)M->rows[j].applied * M->rows[j].applied;
+            total = M->rows[j].applied;
+            for (k = 0; k < 2; k++) {
+                orow* r = &M->rows[4 + 2 * j + k];
+                if (total > 0.f) {
+                    float fr = r->fric;
+                    float dd = solve_row(r, -(fr * total), fr * total, 1, dlA, daA, dlB, daB, M->imA, M->imB);
+                    *rd += (double)dd * dd;
+                }
+                *rl += (double)r->applied * r->applied;
+            }
+        }
+        return;
+    }
     if (pass == 0) {
         for (j = 0; j < 4; j++) {
             float d;
@@ -923,8 +946,8 @@ static void gather_impulses(const omanifold* Ms, int nc, float* out) {
 }
 
 static int solve_pgs_impl(obody* bodies, const oinertia* inertias, int nbodies, const ocontact* contacts, int nc,
-                          const int* order, int iterations, float dt, float erp, float threshold, float tol,
-                          float* impulses_out, float* residual_out) {
+                          const int* order, int interleave, int iterations, float dt, float erp, float threshold,
+                          float tol, float* impulses_out, float* residual_out) {
     omanifold* Ms = (omanifold*)malloc(sizeof(omanifold) * (size_t)(nc > 0 ? nc : 1));
     v3* dl = (v3*)calloc((size_t)(nbodies > 0 ? nbodies : 1), sizeof(v3));
     v3* da = (v3*)calloc((size_t)(nbodies > 0 ? nbodies : 1), sizeof(v3));
@@ -933,12 +956,12 @@ static int solve_pgs_impl(obody* bodies, const oinertia* inertias, int nbodies, 
     for (m = 0; m < nc; m++) setup_manifold(bodies, inertias, &contacts[m], NULL, 1, dt, erp, threshold, &Ms[m]);
     for (it = 0; it < iterations; it++) {
         double rd = 0.0, rl = 0.0;
-        for (pass = 0; pass < 2; pass++)
+        for (pass = 0; pass < (interleave ? 1 : 2); pass++)
             for (k = 0; k < nc; k++) {
                 omanifold* M = &Ms[order ? order[k] : k];
                 v3 dlA = dl[M->A], daA = da[M->A], dlB = dl[M->B], daB = da[M->B];
                 if (!M->mask) continue;
-                solve_manifold(M, pass, &dlA, &daA, &dlB, &daB, &rd, &rl);
+                solve_manifold(M, interleave ? 2 : pass, &dlA, &daA, &dlB, &daB, &rd, &rl);
                 if (M->imA != 0.f) { dl[M->A] = dlA; da[M->A] = daA; }
                 if (M->imB != 0.f) { dl[M->B] = dlB; da[M->B] = daB; }
             }
@@ -1040,15 +1063,15 @@ int oracle_solve(obody* bodies, const oinertia* inertias, int nbodies, const oco
     if (mode == 1)
         return solve_jacobi_impl(bodies, inertias, nbodies, contacts, ncontacts, iterations, dt, erp, threshold,
                                  residual_tol, impulses_out, residual_out);
-    return solve_pgs_impl(bodies, inertias, nbodies, contacts, ncontacts, NULL, iterations, dt, erp, threshold,
-                          residual_tol, impulses_out, residual_out);
+    return solve_pgs_impl(bodies, inertias, nbodies, contacts, ncontacts, NULL, mode == 2, iterations, dt, erp,
+                          threshold, residual_tol, impulses_out, residual_out);
 }
 
 int oracle_solve_ordered(obody* bodies, const oinertia* inertias, int nbodies, const ocontact* contacts,
-                         int ncontacts, const int* order, int iterations, float dt, float erp, float threshold,
-                         float* impulses_out) {
-    return solve_pgs_impl(bodies, inertias, nbodies, contacts, ncontacts, order, iterations, dt, erp, threshold, 0.f,
-                          impulses_out, NULL);
+                         int ncontacts, const int* order, int interleave, int iterations, float dt, float erp,
+                         float threshold, float* impulses_out) {
+    return solve_pgs_impl(bodies, inertias, nbodies, contacts, ncontacts, order, interleave, iterations, dt, erp,
+                          threshold, 0.f, impulses_out, NULL);
 }
 
 /* ------------------------------------------------------------------ integrate */

@@ -75,16 +75,18 @@ int oracle_contacts(const obody* bodies, const oshapes* sh, opair* pairs, int np
 
 /* b3PgsJacobiSolver::solveGroup (Bullet3Dynamics/ConstraintSolver/b3PgsJacobiSolver.cpp:170)
  * with USE_2_FRICTION_DIRECTIONS, no warm start, no split impulse, erp, contact threshold.
- * mode 0 = PGS (usePgs=true, sequential row order), 1 = Jacobi (mass splitting).
+ * mode 0 = PGS (usePgs=true, sequential row order), 1 = Jacobi (mass splitting), 2 = PGS with
+ * B3_SOLVER_INTERLEAVE_CONTACT_AND_FRICTION_CONSTRAINTS (per point: contact row, then its friction rows).
  * impulses_out (optional): 12 floats per manifold: per point (normal, lateral1, lateral2).
  * Returns the number of iterations run. residual_out (optional): last relative residual. */
 int oracle_solve(obody* bodies, const oinertia* inertias, int nbodies, const ocontact* contacts, int ncontacts,
                  int mode, int iterations, float dt, float erp, float threshold, float residual_tol,
                  float* impulses_out, float* residual_out);
-/* Solve in a given manifold order (PGS only): order[k] = manifold index solved k-th. */
+/* Solve in a given manifold order (PGS only): order[k] = manifold index solved k-th; interleave as
+ * mode 2 of oracle_solve. */
 int oracle_solve_ordered(obody* bodies, const oinertia* inertias, int nbodies, const ocontact* contacts,
-                         int ncontacts, const int* order, int iterations, float dt, float erp, float threshold,
-                         float* impulses_out);
+                         int ncontacts, const int* order, int interleave, int iterations, float dt, float erp,
+                         float threshold, float* impulses_out);
 
 /* integrateSingleTransform (Bullet3Dynamics/shared/b3IntegrateTransforms.h:5-55) for every body */
 void oracle_integrate(obody* bodies, int n, float dt, float damping, const float gravity[3]);

@@ -154,15 +154,16 @@ def solve(bodies, inertias, contacts_, mode=0, iterations=10, dt=1 / 60, erp=0.2
     return b, imp[:len(c)], it, res.value
 
 
-def solve_ordered(bodies, inertias, contacts_, order, iterations=10, dt=1 / 60, erp=0.2, threshold=0.02):
+def solve_ordered(bodies, inertias, contacts_, order, iterations=10, dt=1 / 60, erp=0.2, threshold=0.02,
+                  interleave=False):
     b = np.array(bodies, BODY, copy=True)
     I = np.ascontiguousarray(inertias, INERTIA)
     c = np.ascontiguousarray(contacts_, CONTACT)
     o = np.ascontiguousarray(order, np.int32)
     imp = np.zeros((max(1, len(c)), 12), np.float32)
     load_oracle().oracle_solve_ordered(_p(b), _p(I), C.c_int(len(b)), _p(c), C.c_int(len(c)), _p(o),
-                                       C.c_int(iterations), C.c_float(dt), C.c_float(erp), C.c_float(threshold),
-                                       _p(imp))
+                                       C.c_int(1 if interleave else 0), C.c_int(iterations), C.c_float(dt),
+                                       C.c_float(erp), C.c_float(threshold), _p(imp))
     return b, imp[:len(c)]
 
 

@@ -177,6 +177,7 @@ int ref_contacts(const b3RigidBodyData* bodies, int nbodies, const b3Collidable*
 
 // b3PgsJacobiSolver(usePgs).solveGroup with 2 friction directions, no warm start (avoids the
 // dangling m_originalContactPoint write, b3PgsJacobiSolver.cpp:868,1595-1613), no split impulse.
+// use_pgs: 0 Jacobi, 1 PGS, 2 PGS with B3_SOLVER_INTERLEAVE_CONTACT_AND_FRICTION_CONSTRAINTS.
 void ref_solve(b3RigidBodyData* bodies, b3InertiaData* inertias, int nbodies, const b3Contact4Data* contacts, int nc,
                int use_pgs, int iterations, float dt) {
     b3AlignedObjectArray<b3Contact4> C;
@@ -185,6 +186,7 @@ void ref_solve(b3RigidBodyData* bodies, b3InertiaData* inertias, int nbodies, co
     b3PgsJacobiSolver solver(use_pgs != 0);
     b3ContactSolverInfo info;
     info.m_solverMode = B3_SOLVER_USE_2_FRICTION_DIRECTIONS | B3_SOLVER_SIMD;
+    if (use_pgs == 2) info.m_solverMode |= B3_SOLVER_INTERLEAVE_CONTACT_AND_FRICTION_CONSTRAINTS;
     info.m_splitImpulse = false;
     info.m_numIterations = iterations;
     info.m_timeStep = dt;

@@ -159,6 +159,8 @@ def stage_fixture(name, tb: TableBuilder, body_shape, mass, pos, orn, linvel=Non
     for it in (1, 10):
         out[f"pgs_bodies_{it}"] = O.ref_solve(bodies, inertias, contacts, use_pgs=True, iterations=it)
         out[f"jacobi_bodies_{it}"] = O.ref_solve(bodies, inertias, contacts, use_pgs=False, iterations=it)
+        # PGS with B3_SOLVER_INTERLEAVE_CONTACT_AND_FRICTION_CONSTRAINTS
+        out[f"pgsi_bodies_{it}"] = O.ref_solve(bodies, inertias, contacts, use_pgs=2, iterations=it)
     out["integrated"] = O.ref_integrate(out["jacobi_bodies_10"])
     for k in ("collidables", "local_aabbs", "hulls", "faces", "indices", "verts", "edges"):
         out["shape_" + k] = getattr(shapes, k)

@@ -53,12 +53,14 @@ def test_registration_errors_match_reference_conventions():
 
 def test_config_validation():
     h = C.c_void_p()
-    for bad in (dict(pgs_partitions=3), dict(pgs_partitions=-1), dict(solver_blocks_per_sm=-2), dict(grid_dim=100)):
+    for bad in (dict(pgs_partitions=5), dict(pgs_partitions=-1), dict(solver_blocks_per_sm=-2), dict(grid_dim=100),
+                dict(pgs_interleave=2)):
         cfg = capi.default_config(**bad)
         with pytest.raises(capi.B3GError) as e:
             capi.call("b3g_create", C.byref(cfg), C.c_int(0), C.byref(h))
         assert e.value.status == 1  # invalid argument
-    for ok in (capi.PGS_PARTITIONS_AUTO, capi.PGS_PARTITIONS_GLOBAL_DELTAS, capi.PGS_PARTITIONS_NONE):
+    for ok in (capi.PGS_PARTITIONS_AUTO, capi.PGS_PARTITIONS_GLOBAL_DELTAS, capi.PGS_PARTITIONS_NONE,
+               capi.PGS_PARTITIONS_SHARED, capi.PGS_PARTITIONS_STREAMED):
         cfg = capi.default_config(pgs_partitions=ok, solver_blocks_per_sm=1)
         capi.call("b3g_create", C.byref(cfg), C.c_int(0), C.byref(h))
         capi.call("b3g_destroy", h)

@@ -62,9 +62,11 @@ def test_golden_jacobi_bitexact(name, iters):
 
 
 @pytest.mark.parametrize("name", ["pile", "mixed"])
-def test_golden_pgs_colour_order_bitexact(name):
+@pytest.mark.parametrize("interleave", [False, True])
+def test_golden_pgs_colour_order_bitexact(name, interleave):
     d = load_golden(name)
-    np_, bp, pl, shapes = load(scene_from_golden(d), solver_mode=capi.SOLVER_PGS, solver_iterations=10)
+    np_, bp, pl, shapes = load(scene_from_golden(d), solver_mode=capi.SOLVER_PGS, solver_iterations=10,
+                               pgs_interleave=interleave)
     b = _write_golden_state(np_, d)
     I = np_.readInertiasToCpu()
     run_stages(np_, bp, pl)
@@ -77,7 +79,7 @@ def test_golden_pgs_colour_order_bitexact(name):
     # whose sequential Gauss-Seidel sweep the oracle reproduces bit for bit
     order = pl.readSolveOrder()
     assert np.array_equal(np.sort(order), np.arange(len(col)))
-    ob, _ = O.solve_ordered(b, I, gc, order, iterations=10)
+    ob, _ = O.solve_ordered(b, I, gc, order, iterations=10, interleave=interleave)
     gb = np_.readbackAllBodiesToCpu()
     assert np.array_equal(gb["linVel"], ob["linVel"]) and np.array_equal(gb["angVel"], ob["angVel"])
     st = pl.stats()
@@ -146,17 +148,19 @@ def test_box_pile_trajectory_jacobi():
     assert gb["pos"][1:, 1].min() > 0.4  # resting on the plane, no tunnelling
 
 
-def test_pgs_residual_and_penetration_bounds():
-    # order-sensitive PGS: colour-order GPU solve vs the reference's sequential order on the same
-    # manifolds -- same contact residual class and penetration bounds
+@pytest.mark.parametrize("interleave", [False, True])
+def test_pgs_residual_and_penetration_bounds(interleave):
+    # order-sensitive PGS: colour-order GPU solve vs the reference's sequential order (same row
+    # interleaving mode) on the same manifolds -- same contact residual class and penetration bounds
     sc = scenes.box_stack(8, 16, 8, seed=1)
-    np_, bp, pl, shapes = load(sc, solver_mode=capi.SOLVER_PGS, solver_iterations=10)
+    np_, bp, pl, shapes = load(sc, solver_mode=capi.SOLVER_PGS, solver_iterations=10, pgs_interleave=interleave)
     I = np_.readInertiasToCpu()
     dt = 1 / 60
+    mode = 2 if interleave else 0
     ob = np_.readbackAllBodiesToCpu()
     for _ in range(30):
         pl.stepSimulation(dt)
-        ob, _, _, _ = O.step(ob, I, shapes, dt=dt, mode=0, iterations=10, use_grid=False)
+        ob, _, _, _ = O.step(ob, I, shapes, dt=dt, mode=mode, iterations=10, use_grid=False)
     pl.synchronize()
     b = np_.readbackAllBodiesToCpu()
 
@@ -171,7 +175,7 @@ def test_pgs_residual_and_penetration_bounds():
     run_stages(np_, bp, pl, dt)
     gc = np_.getContactsCPU()
     gpu_res = pl.stats().residual
-    _, _, _, seq_res = O.solve(b, I, gc, mode=0, iterations=10)
+    _, _, _, seq_res = O.solve(b, I, gc, mode=mode, iterations=10)
     assert gpu_res < max(2.0 * seq_res, 0.05)
     assert pl.status() == 0
 
@@ -200,20 +204,23 @@ def test_graph_step_equals_staged_step():
     assert np.array_equal(res[0].view(np.uint8), res[1].view(np.uint8))
 
 
-@pytest.mark.parametrize("parts", [capi.PGS_PARTITIONS_AUTO, capi.PGS_PARTITIONS_GLOBAL_DELTAS,
+@pytest.mark.parametrize("parts", [capi.PGS_PARTITIONS_AUTO, capi.PGS_PARTITIONS_SHARED,
+                                   capi.PGS_PARTITIONS_STREAMED, capi.PGS_PARTITIONS_GLOBAL_DELTAS,
                                    capi.PGS_PARTITIONS_NONE])
 @pytest.mark.parametrize("scene", ["stack", "mixed"])
-def test_pgs_partitioned_solve_bitexact(parts, scene):
+@pytest.mark.parametrize("interleave", [False, True])
+def test_pgs_partitioned_solve_bitexact(parts, scene, interleave):
     # every PGS work split (block-owned body ranges with shared- or global-memory deltas, or
     # grid-wide colours only) is a legal Gauss-Seidel order: the oracle sweeping the GPU's
     # reported order over the GPU's own manifolds reproduces the velocities bit for bit
     if scene == "stack":
         sc = scenes.box_stack(16, 16, 16, seed=2)
-        np_, bp, pl, shapes = load(sc, solver_mode=capi.SOLVER_PGS, solver_iterations=10, pgs_partitions=parts)
+        np_, bp, pl, shapes = load(sc, solver_mode=capi.SOLVER_PGS, solver_iterations=10, pgs_partitions=parts,
+                                   pgs_interleave=interleave)
     else:
         sc = scenes.mixed_scene(4096, extent=20.0, seed=3, plane=True)
         np_, bp, pl, shapes = load(sc, m_maxBroadphasePairs=400000, solver_mode=capi.SOLVER_PGS,
-                                   solver_iterations=10, pgs_partitions=parts)
+                                   solver_iterations=10, pgs_partitions=parts, pgs_interleave=interleave)
     b = np_.readbackAllBodiesToCpu()
     I = np_.readInertiasToCpu()
     run_stages(np_, bp, pl)
@@ -223,7 +230,7 @@ def test_pgs_partitioned_solve_bitexact(parts, scene):
     assert (col >= 0).all() and O.check_batches(gc, col, b) == 0
     order = pl.readSolveOrder()
     assert np.array_equal(np.sort(order), np.arange(len(gc)))
-    ob, _ = O.solve_ordered(b, I, gc, order, iterations=10)
+    ob, _ = O.solve_ordered(b, I, gc, order, iterations=10, interleave=interleave)
     gb = np_.readbackAllBodiesToCpu()
     assert np.array_equal(gb["linVel"], ob["linVel"]) and np.array_equal(gb["angVel"], ob["angVel"])
     st = pl.stats()

@@ -73,7 +73,7 @@ def test_contacts_match_reference(name):
 
 
 @pytest.mark.parametrize("name", ["pile", "mixed"])
-@pytest.mark.parametrize("mode,key", [(0, "pgs"), (1, "jacobi")])
+@pytest.mark.parametrize("mode,key", [(0, "pgs"), (1, "jacobi"), (2, "pgsi")])
 @pytest.mark.parametrize("iters", [1, 10])
 def test_solver_matches_reference(name, mode, key, iters):
     d = load_golden(name)
