@@ -82,7 +82,9 @@ EXPORTS = [
     "b3g_read_impulses", "b3g_get_num_collidables", "b3g_read_registered_bodies", "b3g_read_shape_tables",
     "b3g_set_profiling",
     "b3g_get_stage_times", "b3g_get_launch_count", "b3g_record_event", "b3g_event_elapsed", "b3g_hull_compute",
-    "b3g_grid_pairs_noalloc"]
+    "b3g_grid_pairs_noalloc", "b3g_mlp_create", "b3g_mlp_destroy", "b3g_mlp_set_params", "b3g_mlp_get_params",
+    "b3g_mlp_set_normalization", "b3g_mlp_get_normalization", "b3g_mlp_predict", "b3g_mlp_set_training_data",
+    "b3g_mlp_train", "b3g_mlp_gradients"]
 
 
 def lib_path() -> Path:

@@ -1,0 +1,249 @@
+// Warm-start MLP (12 -> 128 -> 128 -> 128 -> 3, GELU) on the 5th-generation tensor cores.
+//
+// Every product of the forward and backward pass is one call of k_gemm: D[128 x N] tiles are
+// accumulated in tensor memory (TMEM) by tcgen05.mma (BF16 operands from shared memory, FP32
+// accumulation), then read back with tcgen05.ld by the four warps of the CTA (warp w owns TMEM
+// lanes 32w..32w+31, i.e. rows 32w..32w+31 of the tile) and finished by a fused epilogue: bias +
+// GELU (forward), bias only (output layer), upstream gradient x GELU'(pre-activation) with bias
+// gradient (backward), or split-K accumulation into FP32 weight gradients.
+//
+// Operand layout: both operands K-major (row r of A and row n of B hold their K elements
+// contiguously in global memory).  A K-chunk of 64 is copied into shared memory in the
+// canonical no-swizzle core-matrix layout: core matrix = 8 rows x 16 bytes; element (r, k) of a
+// chunk lives at (r % 8) * 16 + (k % 8) * 2 + (k / 8) * 128 + (r / 8) * 1024 bytes, so the
+// leading-dimension byte offset (next core matrix along K) is 128 and the stride-dimension byte
+// offset (next 8-row group) is 1024.  One MMA consumes K = 16 (two core matrices along K).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "b3g_capi.h"
+#include "mlp.h"
+
+namespace b3g {
+namespace mlp {
+
+static constexpr int GT = 128;         // threads per GEMM CTA (4 warps = 128 TMEM lanes)
+static constexpr int KC = 64;          // K elements per shared-memory chunk
+static constexpr int SBO = 1024;       // bytes between 8-row groups in a chunk (KC / 8 * 128)
+static constexpr int LBO = 128;        // bytes between core matrices along K
+static constexpr unsigned WAIT_LIMIT = 1u << 22;
+
+// ---------------------------------------------------------------------------- PTX wrappers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFFu);              // start address
+    d |= (uint64_t)((LBO >> 4) & 0x3FFFu) << 16;         // leading-dimension byte offset (along K)
+    d |= (uint64_t)((SBO >> 4) & 0x3FFFu) << 32;         // stride-dimension byte offset (8-row groups)
+    d |= (uint64_t)1 << 46;                              // descriptor version for tcgen05
+    // base offset 0, absolute LBO mode 0, layout type 0 = no swizzle
+    return d;
+}
+
+// kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major, M = 128, N = n
+__host__ __device__ constexpr uint32_t instr_desc(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(unsigned long long* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+    for (unsigned i = 0; i < WAIT_LIMIT; i++) {
+        if (mbar_test(bar, parity)) return true;
+        __nanosleep(20);
+    }
+    return false;
+}
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 16 consecutive FP32 columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// ---------------------------------------------------------------------------- activation
+// GELU(x) = x * Phi(x) (exact, erf form) and its derivative Phi(x) + x * phi(x)
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+    const float cdf = 0.5f * (1.f + erff(x * 0.70710678118654752f));
+    const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
+    return cdf + x * pdf;
+}
+
+// ---------------------------------------------------------------------------- the GEMM
+// Copies rows [r0, r0 + nrows_tile) x K [k0, k0 + kc) of a K-major bf16 matrix into the chunk
+// layout; rows >= rows_valid and K >= kend are zero.
+__device__ __forceinline__ void load_chunk(char* dst, const __nv_bfloat16* src, int ld, int r0, int nrows_tile,
+                                           int rows_valid, int k0, int kend) {
+    const int pieces = nrows_tile * (KC / 8);
+    for (int p = threadIdx.x; p < pieces; p += blockDim.x) {
+        const int r = p / (KC / 8), kq = p % (KC / 8);
+        const int row = r0 + r, k = k0 + kq * 8;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (row < rows_valid && k < kend) v = *reinterpret_cast<const uint4*>(src + (size_t)row * ld + k);
+        *reinterpret_cast<uint4*>(dst + (r & 7) * 16 + kq * LBO + (r >> 3) * SBO) = v;
+    }
+}
+
+__global__ void __launch_bounds__(GT) k_gemm(GemmArgs g) {
+    extern __shared__ __align__(1024) char smem[];
+    char* sA = smem;                       // 128 x KC bf16 = 16 KB
+    char* sB = smem + 128 * KC * 2;        // N x KC bf16
+    __shared__ unsigned long long bar;
+    __shared__ uint32_t tslot;
+    bool failed = false;  // block-uniform: set from a __syncthreads_or
+    const int N = g.N;
+    const uint32_t ncols = N <= 32 ? 32u : (N <= 64 ? 64u : (N <= 128 ? 128u : 256u));
+    const int rows = g.d_rows ? min(*g.d_rows, g.rows_cap) : g.rows;
+    const int m_tiles = (rows + 127) / 128;
+    const int units = m_tiles * g.k_split;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    if (threadIdx.x < 32) tmem_alloc(&tslot, ncols);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tslot;
+    const uint32_t idesc = instr_desc(N);
+    unsigned phase = 0;
+    const int ksteps_total = (g.K + 15) / 16;
+    const int kchunks_total = (g.K + KC - 1) / KC;
+    const int chunks_per_part = (kchunks_total + g.k_split - 1) / g.k_split;
+    for (int u = blockIdx.x; u < units && !failed; u += gridDim.x) {
+        const int mt = u % m_tiles, part = u / m_tiles;
+        const int r0 = mt * 128;
+        const int c_beg = part * chunks_per_part, c_end = min(kchunks_total, c_beg + chunks_per_part);
+        if (c_beg >= c_end) continue;
+        for (int c = c_beg; c < c_end; c++) {
+            const int k0 = c * KC;
+            load_chunk(sA, g.A, g.lda, r0, 128, rows, k0, g.K);
+            load_chunk(sB, g.B, g.ldb, 0, N, N, k0, g.K);
+            fence_async_smem();
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+            if (threadIdx.x == 0) {
+                const int steps = min(KC / 16, ksteps_total - k0 / 16);
+                for (int s = 0; s < steps; s++) {
+                    const uint64_t ad = smem_desc(smem_u32(sA) + s * 2 * LBO);
+                    const uint64_t bd = smem_desc(smem_u32(sB) + s * 2 * LBO);
+                    mma_bf16(tmem, ad, bd, idesc, (c > c_beg || s > 0) ? 1u : 0u);
+                }
+                mma_commit(&bar);
+            }
+            // the chunk buffers are rewritten next round: wait until the MMAs have read them
+            const bool ok = mbar_wait(&bar, phase);
+            phase ^= 1u;
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                if (threadIdx.x == 0) {
+                    if (g.status) atomicOr(g.status, B3G_FLAG_MLP_TIMEOUT);
+                    mbar_wait(&bar, phase ^ 1u);  // drain: one more bounded wait for the MMAs in flight
+                }
+                break;
+            }
+            tc_fence_after();
+        }
+        if (failed) break;
+        // ---- epilogue: thread t owns row r0 + t of the tile
+        const int r = r0 + threadIdx.x;
+        const uint32_t trow = tmem + ((uint32_t)(threadIdx.x & ~31) << 16);
+        for (int n0 = 0; n0 < N; n0 += 16) {
+            float v[16];
+            tmem_ld16(trow + n0, v);
+            if (r >= rows) continue;
+#pragma unroll
+            for (int i = 0; i < 16; i++) {
+                const int n = n0 + i;
+                float x = v[i];
+                switch (g.epi) {
+                    case EPI_BIAS_F32:
+                        g.out_f32[(size_t)r * g.ld_out + n] = x + g.bias[n];
+                        break;
+                    case EPI_BIAS_GELU: {
+                        const float pre = x + g.bias[n];
+                        if (g.pre_out) g.pre_out[(size_t)r * g.ld_out + n] = pre;
+                        const __nv_bfloat16 h = __float2bfloat16_rn(gelu(pre));
+                        g.out_row[(size_t)r * g.ld_row + n] = h;
+                        if (g.out_col) g.out_col[(size_t)n * g.ld_col + r] = h;
+                        break;
+                    }
+                    case EPI_DGELU: {
+                        const float d = x * gelu_grad(g.pre_in[(size_t)r * g.ld_out + n]);
+                        const __nv_bfloat16 hb = __float2bfloat16_rn(d);
+                        if (g.out_row) g.out_row[(size_t)r * g.ld_row + n] = hb;
+                        if (g.out_col) g.out_col[(size_t)n * g.ld_col + r] = hb;
+                        // bias gradient: sum of the rounded values, as the next layer consumes them
+                        if (g.atomic_out) atomicAdd(&g.atomic_out[n], __bfloat162float(hb));
+                        break;
+                    }
+                    case EPI_ATOMIC:
+                        atomicAdd(&g.atomic_out[(size_t)r * g.ld_out + n], x);
+                        break;
+                }
+            }
+        }
+        tc_fence_before();
+        __syncthreads();  // TMEM reads done before the next tile's MMAs overwrite it
+        tc_fence_after();
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x < 32) tmem_dealloc(tmem, ncols);
+}
+
+size_t gemm_smem_bytes(int N) { return (size_t)128 * KC * 2 + (size_t)N * KC * 2; }
+
+cudaError_t gemm_prepare() {
+    return cudaFuncSetAttribute(k_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem_bytes(256));
+}
+
+void launch_gemm(const GemmArgs& g, int grid, cudaStream_t s) {
+    k_gemm<<<grid, GT, gemm_smem_bytes(g.N), s>>>(g);
+}
+
+}  // namespace mlp
+}  // namespace b3g

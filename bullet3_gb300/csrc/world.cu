@@ -37,6 +37,11 @@ static b3gStatus fail(b3gStatus st, const char* fmt, ...) {
     return st;
 }
 
+b3gStatus b3g::report_error(b3gStatus st, const char* msg) {
+    g_last_error = msg ? msg : "";
+    return st;
+}
+
 #define CUDA_TRY(expr)                                                                              \
     do {                                                                                            \
         cudaError_t _e = (expr);                                                                    \

@@ -132,6 +132,9 @@ int launch_compact_contacts(DeviceState& d, cudaStream_t s);
 int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s);
 cudaError_t solver_prepare();  // kernel attributes, once per device before the first solve
 
+// sets the message b3g_last_error returns (this thread) and passes the status through
+b3gStatus report_error(b3gStatus st, const char* msg);
+
 // allocation-free grid broadphase (noalloc.cu): the radix sorts run with sms * 4 blocks, so the
 // static scratch covers devices with up to B3G_NOALLOC_MAX_SORT_BLOCKS / 4 SMs
 #define B3G_NOALLOC_MAX_SORT_BLOCKS 1024

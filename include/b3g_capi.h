@@ -44,6 +44,8 @@ typedef enum b3gStatus {
 #define B3G_FLAG_BARRIER_TIMEOUT   0x8u
 #define B3G_FLAG_NAN               0x10u
 #define B3G_FLAG_CLIP_OVERFLOW     0x20u
+#define B3G_FLAG_MLP_TIMEOUT       0x40u  /* a tensor-core wait of the warm-start network gave up */
+#define B3G_FLAG_WARM_DISCARDED    0x80u  /* a warm start was worse than a cold start and was dropped */
 
 #define B3G_SOLVER_PGS 0      /* b3PgsJacobiSolver(true)  -- graph-coloured Gauss-Seidel on the GPU */
 #define B3G_SOLVER_JACOBI 1   /* b3PgsJacobiSolver(false) -- mass-splitting Jacobi */
@@ -228,6 +230,38 @@ b3gStatus b3g_event_elapsed(b3g_handle h, int slot_start, int slot_end, float* m
 b3gStatus b3g_hull_compute(const float* verts, int stride_bytes, int num_verts, const float scaling[3],
                            float* verts_out, float* planes_out, int* face_counts_out, int* indices_out,
                            float* edges_out, float* center_out, int* counts6);
+
+/* ---- learned warm start (no counterpart in the reference) --------------------------------------
+ * A 12 -> 128 -> 128 -> 128 -> 3 GELU network predicting, per contact point, the converged
+ * impulses of its contact row and its two friction rows (second direction first) from 12 local
+ * features: relative velocity of A w.r.t. B at the point (3), normal (3), separation (1),
+ * inverse masses of A and B (2), points in the manifold (1), |tangential relative velocity| (1),
+ * dt * (gravity . normal) (1).  BF16 tensor-core forward and backward passes with FP32
+ * accumulation, Adam on FP32 master weights, all on the GPU.
+ * Parameter layout (B3G_MLP_PARAMS floats): W1[12][128] b1[128] W2[128][128] b2[128] W3[128][128]
+ * b3[128] W4[128][3] b4[3], W[in][out] row-major.  Normalisation (B3G_MLP_NORM floats): feature
+ * mean[12], feature 1/std[12], target mean[3], target 1/std[3]; the network works in normalised
+ * units and predictions are returned in impulse units.  Errors: b3g_last_error. */
+#define B3G_MLP_PARAMS 35075
+#define B3G_MLP_NORM 30
+typedef struct b3gMlpImpl* b3g_mlp;
+b3gStatus b3g_mlp_create(int cuda_device, unsigned long long seed, b3g_mlp* out);
+b3gStatus b3g_mlp_destroy(b3g_mlp m);
+b3gStatus b3g_mlp_set_params(b3g_mlp m, const float* params, int n);
+b3gStatus b3g_mlp_get_params(b3g_mlp m, float* params, int n);
+b3gStatus b3g_mlp_set_normalization(b3g_mlp m, const float* norm, int n);
+b3gStatus b3g_mlp_get_normalization(b3g_mlp m, float* norm, int n);
+/* n rows of 12 features (host) -> n rows of 3 predicted impulses (host) */
+b3gStatus b3g_mlp_predict(b3g_mlp m, const float* features, int n, float* impulses);
+/* uploads a training set (n x 12 features, n x 3 target impulses, host) */
+b3gStatus b3g_mlp_set_training_data(b3g_mlp m, const float* features, const float* targets, int n);
+/* `steps` Adam steps on consecutive batches of the training set starting at batch `first_batch`
+ * (wrapping); mean_loss = mean over the steps of the batch mean-squared error (normalised units) */
+b3gStatus b3g_mlp_train(b3g_mlp m, int steps, int batch, float lr, int first_batch, double* mean_loss);
+/* gradients of the mean-squared error of one batch w.r.t. every parameter (B3G_MLP_PARAMS floats,
+ * public layout), without an update: the gradient check of the backward kernels */
+b3gStatus b3g_mlp_gradients(b3g_mlp m, const float* features, const float* targets, int n, float* grads,
+                            double* loss);
 
 /* ---- allocation-free grid broadphase (no counterpart in the reference) -------------------------
  * The uniform-grid pair search of b3g_calculate_overlapping_pairs, run on the current CUDA device
