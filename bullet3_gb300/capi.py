@@ -39,6 +39,8 @@ FLAG_BATCH_OVERFLOW = 0x4
 FLAG_BARRIER_TIMEOUT = 0x8
 FLAG_NAN = 0x10
 FLAG_CLIP_OVERFLOW = 0x20
+FLAG_MLP_TIMEOUT = 0x40
+FLAG_WARM_DISCARDED = 0x80
 
 STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "INVALID_INDEX", 3: "CAPACITY", 4: "CUDA", 5: "NOT_UPLOADED",
                 6: "UNSUPPORTED", 7: "BARRIER_TIMEOUT", 8: "DEGENERATE"}
@@ -52,7 +54,7 @@ class b3gConfig(C.Structure):
                 ("contact_friction", C.c_float), ("residual_tol", C.c_float), ("update_world_inertia", C.c_int),
                 ("use_cuda_graph", C.c_int), ("warm_start", C.c_int), ("barrier_spin_limit", C.c_int),
                 ("solver_blocks_per_sm", C.c_int), ("pgs_partitions", C.c_int), ("pgs_interleave", C.c_int),
-                ("reserved", C.c_int * 4)]
+                ("warm_start_max_points", C.c_int), ("reserved", C.c_int * 3)]
 
 
 class b3gStepStats(C.Structure):
@@ -84,7 +86,8 @@ EXPORTS = [
     "b3g_get_stage_times", "b3g_get_launch_count", "b3g_record_event", "b3g_event_elapsed", "b3g_hull_compute",
     "b3g_grid_pairs_noalloc", "b3g_mlp_create", "b3g_mlp_destroy", "b3g_mlp_set_params", "b3g_mlp_get_params",
     "b3g_mlp_set_normalization", "b3g_mlp_get_normalization", "b3g_mlp_predict", "b3g_mlp_set_training_data",
-    "b3g_mlp_train", "b3g_mlp_gradients"]
+    "b3g_mlp_train", "b3g_mlp_gradients", "b3g_set_warm_start_model", "b3g_read_warm_samples",
+    "b3g_read_warm_start"]
 
 
 def lib_path() -> Path:

@@ -28,6 +28,7 @@
 #include <cfloat>
 
 #include "common.cuh"
+#include "warmstart.h"
 #include "world_internal.h"
 
 namespace b3g {
@@ -70,6 +71,11 @@ struct SolverArgs {
     int use_smem;             // block-local body deltas in shared memory
     int tile_R;               // > 0: block-local records streamed through shared memory, R per tile
     int interleave;           // PGS: each point's friction rows right after its contact row
+    float* ws_features;       // learned warm start: 12 features per point slot 4m+j (nullptr: none)
+    int ws_rows_cap;          // point slots that get features
+    int* ws_rows;             // device: min(4 * manifolds, ws_rows_cap)
+    float gx, gy, gz;         // gravity (the dt * (g . n) feature)
+    int warm;                 // PGS: the records' initial impulses are a warm start (apply, then iterate)
     unsigned long long* claim;
     unsigned long long* mask;  // per body: colours already taken by its manifolds
     unsigned long long* claim_x;  // PGS: the same two arrays for the cross-partition colouring
@@ -130,6 +136,7 @@ __global__ void k_count_manifolds(const b3gContact4* __restrict__ slots, const i
 __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
     const int nc = *a.d_nc;
     const bool pgs = a.mode == B3G_SOLVER_PGS;
+    if (a.ws_rows && blockIdx.x == 0 && threadIdx.x == 0) *a.ws_rows = min(4 * nc, a.ws_rows_cap);
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nc; m += gridDim.x * blockDim.x) {
         const b3gContact4 c = a.slots[a.manifold_pair[m]];
         const int iA = abs(c.bodyA), iB = abs(c.bodyB);
@@ -231,6 +238,17 @@ __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
                 a.sp.dir1[s] = f4(dir1, jacs[1]);
                 a.sp.rhsf[s] = make_float2(rhss[0], rhss[1]);
                 a.sp.imp[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (a.ws_features && s < (size_t)a.ws_rows_cap) {
+                    // warm-start features of this point (the network's input layout)
+                    float* f = a.ws_features + s * 12;
+                    f[0] = vel.x; f[1] = vel.y; f[2] = vel.z;
+                    f[3] = n.x; f[4] = n.y; f[5] = n.z;
+                    f[6] = dist;
+                    f[7] = imA; f[8] = imB;
+                    f[9] = (float)np;
+                    f[10] = sqrtf(lat);
+                    f[11] = a.dt * (a.gx * n.x + a.gy * n.y + a.gz * n.z);
+                }
             }
         }
         a.hdr[m] = make_int4(iA, iB, mask, np);
@@ -372,6 +390,41 @@ __device__ __forceinline__ void solve_manifold(const SolverPoints& sp, int m, fl
                 rf[j] = ldrec<SMEM>(&sp.rhsf[base + j]);
             }
         }
+        if (pass == 3) {
+            // warm start: the initial impulses (contact, dir2, dir1) applied to the body deltas
+            // as internalApplyImpulse does under B3_SOLVER_USE_WARMSTARTING
+            // (b3PgsJacobiSolver.cpp:745-752, 815-843); same vectors as the rows' own updates
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                if (!(mask & (1 << j))) continue;
+                const v3 rel1 = xyz(r1[j]), rel2 = xyz(r2[j]);
+                {
+                    const float w = im[j].x;
+                    v3 r1xn = cross3(rel1, n);
+                    v3 ta1 = cross3(rel2, n);
+                    v3 angA = imul(IA, r1xn);
+                    v3 angB = imul(IB, -ta1);
+                    dlA = dlA + (n * imA) * w;
+                    daA = daA + angA * w;
+                    dlB = dlB + ((-n) * imB) * w;
+                    daB = daB + angB * w;
+                }
+#pragma unroll
+                for (int k = 0; k < 2; k++) {
+                    const v3 d = xyz(k == 0 ? d2[j] : d1[j]);
+                    const float w = k == 0 ? im[j].y : im[j].z;
+                    v3 r1xn = cross3(rel1, d);
+                    v3 r2xn = cross3(rel2, -d);
+                    v3 angA = imul(IA, r1xn);
+                    v3 angB = imul(IB, r2xn);
+                    dlA = dlA + (d * imA) * w;
+                    daA = daA + angA * w;
+                    dlB = dlB + ((-d) * imB) * w;
+                    daB = daB + angB * w;
+                }
+            }
+            return;
+        }
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             if (!(mask & (1 << j))) continue;
@@ -466,8 +519,10 @@ __device__ __forceinline__ void store_dv(const SolverArgs& a, int b, v3 l, v3 w)
     __stcg(&a.dv[2 * b + 1], f4(w, 0.f));
 }
 
-// residual bookkeeping shared by both kernels; returns true when the tolerance stops the solve
-__device__ __forceinline__ bool end_iteration(const SolverArgs& a, int it, float res_d, float res_l, bool& ok) {
+// residual bookkeeping shared by both kernels; returns true when the tolerance stops the solve.
+// `it` indexes the residual slots and counts the sweeps run so far (it + 1 after this one).
+__device__ __forceinline__ bool end_iteration(const SolverArgs& a, int it, float res_d, float res_l, bool& ok,
+                                              double* r_out = nullptr) {
     block_accumulate(a.residual_acc + 2 * it, res_d, res_l);
     if (!grid_barrier(a.bar, gridDim.x, a.spin_limit)) {
         ok = false;
@@ -476,6 +531,7 @@ __device__ __forceinline__ bool end_iteration(const SolverArgs& a, int it, float
     double dd = *((volatile double*)&a.residual_acc[2 * it]);
     double ll = *((volatile double*)&a.residual_acc[2 * it + 1]);
     double r = sqrt(dd) / fmax(sqrt(ll), 1e-12);
+    if (r_out) *r_out = r;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.counters->residual = (float)r;
         a.counters->iterations = it + 1;
@@ -837,12 +893,16 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
         }
     }
     bool ok = true;
-    // passes of one iteration: contact rows then friction rows, or one interleaved pass (2)
+    // passes of one iteration: contact rows then friction rows, or one interleaved pass (2);
+    // a warm start adds one application pass (3) before the first iteration
     const int npasses = a.interleave ? 1 : 2;
-    for (int it = 0; it < a.iterations; it++) {
+    bool warm_live = a.warm != 0;
+    int extra = 0;  // 1 after a dropped warm start: its sweep still counts
+    for (int it = a.warm ? -1 : 0; it < a.iterations; it++) {
         float res_d = 0.f, res_l = 0.f;
-        for (int ps = 0; ps < npasses; ps++) {
-            const int pass = a.interleave ? 2 : ps;
+        const bool warm_pass = it < 0;
+        for (int ps = 0; ps < (warm_pass ? 1 : npasses); ps++) {
+            const int pass = warm_pass ? 3 : (a.interleave ? 2 : ps);
             if (a.use_smem) {
                 for (int l = threadIdx.x; l < myN; l += blockDim.x) {
                     v3 dl, dw;
@@ -972,7 +1032,24 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
                 if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
             }
         }
-        if (end_iteration(a, it, res_d, res_l, ok)) break;
+        if (warm_pass) continue;  // the application pass has no residual
+        double r = 0.0;
+        if (end_iteration(a, it + extra, res_d, res_l, ok, &r)) break;
+        if (it == 0 && warm_live) {
+            warm_live = false;
+            // a cold first sweep has residual exactly 1: a warm start that does worse is dropped
+            // and the solve restarts cold with the full iteration budget (every block sees the same r)
+            if (r > 1.0) {
+                for (int i = tid; i < 2 * a.num_bodies; i += stride) __stcg(&a.dv[i], make_float4(0.f, 0.f, 0.f, 0.f));
+                for (int k = tid; k < nc; k += stride)
+                    for (int j = 0; j < 4; j++) __stcg(&a.sp_ord.imp[(size_t)k * 4 + j], make_float4(0.f, 0.f, 0.f, 0.f));
+                if (tid == 0) atomicOr(&a.counters->status, B3G_FLAG_WARM_DISCARDED);
+                extra = 1;
+                it = -1;
+                if (R > 0) fence_proxy_async();
+                if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
+            }
+        }
     }
     if (!ok) return;
     // ---- applied impulses back to manifold order (read by b3g_read_impulses)
@@ -1069,6 +1146,35 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_jacobi(SolverArgs a) {
     }
 }
 
+// Network predictions (normalised units, 16 per slot) -> initial impulses of the point records:
+// contact impulse >= 0, friction impulses inside the friction cone of that impulse, non-finite
+// values dropped (cold).  Slots beyond the feature capacity start cold.
+__global__ void k_warm_fill(const float* __restrict__ pred, const float* __restrict__ tnorm, const int* __restrict__ d_nc,
+                            int rows_cap, const int4* __restrict__ hdr, SolverPoints sp, float4* __restrict__ init) {
+    const int nc = *d_nc;
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nc; m += gridDim.x * blockDim.x) {
+        const int mask = hdr[m].z;
+        const float fr = sp.nf[m].w;
+        for (int j = 0; j < 4; j++) {
+            const size_t s = (size_t)m * 4 + j;
+            float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+            if ((mask & (1 << j)) && s < (size_t)rows_cap) {
+                const float* y = pred + s * 16;
+                float lam = y[0] / tnorm[3] + tnorm[0];
+                float f2 = y[1] / tnorm[4] + tnorm[1];
+                float f1 = y[2] / tnorm[5] + tnorm[2];
+                if (!(lam > 0.f) || !isfinite(lam)) lam = 0.f;
+                const float lim = fr * lam;
+                f2 = isfinite(f2) ? fminf(fmaxf(f2, -lim), lim) : 0.f;
+                f1 = isfinite(f1) ? fminf(fmaxf(f1, -lim), lim) : 0.f;
+                w = make_float4(lam, f2, f1, 0.f);
+                sp.imp[s] = w;
+            }
+            if (init && s < (size_t)rows_cap) init[s] = w;
+        }
+    }
+}
+
 __global__ void k_reset_solver(int* color_fill, int* remaining, int* color_cursor, unsigned int* barrier,
                                double* residual_acc, int nres, DevCounters* counters) {
     for (int i = threadIdx.x; i < B3G_MAX_COLORS + 1; i += blockDim.x) {
@@ -1104,7 +1210,8 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     long long ll = 0;
     const int grid = d.num_sms * 4;
     int iters = cfg.solver_iterations > 0 ? cfg.solver_iterations : 1;
-    if (iters > 4096) iters = 4096;  // residual_acc holds 2 doubles per iteration for 4096 iterations
+    // residual_acc holds 2 doubles per sweep for 4096 sweeps: a dropped warm start adds one sweep
+    if (iters > 4095) iters = 4095;
     int* d_nc = &d.counters->num_contacts;
     int* d_n2 = &d.counters->pad[1];
     // per-step resets
@@ -1115,7 +1222,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     int* color_fill = d.color_offsets + (B3G_MAX_COLORS + 2);
     int* remaining = color_fill + (B3G_MAX_COLORS + 1);
     int* color_cursor = remaining + (B3G_MAX_COLORS + 1);
-    k_reset_solver<<<1, 256, 0, s>>>(color_fill, remaining, color_cursor, d.barrier, d.residual_acc, 2 * iters,
+    k_reset_solver<<<1, 256, 0, s>>>(color_fill, remaining, color_cursor, d.barrier, d.residual_acc, 2 * (iters + 1),
                                      d.counters);
     launches++;
 
@@ -1153,6 +1260,13 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     a.use_smem = 0;
     a.tile_R = 0;
     a.interleave = cfg.pgs_interleave ? 1 : 0;
+    a.ws_features = cfg.warm_start != 0 ? d.ws_features : nullptr;
+    a.ws_rows_cap = d.ws_rows_cap;
+    a.ws_rows = a.ws_features ? d.ws_rows : nullptr;
+    a.gx = cfg.gravity[0];
+    a.gy = cfg.gravity[1];
+    a.gz = cfg.gravity[2];
+    a.warm = (cfg.warm_start == 1 && d.ws_model && a.ws_features && cfg.solver_mode == B3G_SOLVER_PGS) ? 1 : 0;
     a.claim = d.color_claim;
     a.mask = d.color_claim + d.num_bodies;
     a.claim_x = d.color_claim + 2 * (size_t)d.num_bodies;
@@ -1187,6 +1301,14 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     }
     k_setup_rows<<<grid, SV_THREADS, 0, s>>>(a);
     launches++;
+    if (a.warm) {
+        // learned warm start: the network's predictions become the records' initial impulses
+        launches += mlp::forward_device(*d.ws_model, d.ws_features, 12, d.ws_rows, d.ws_rows_cap, s);
+        k_warm_fill<<<grid, SV_THREADS, 0, s>>>(mlp::last_predictions(*d.ws_model),
+                                                mlp::target_norm(*d.ws_model), d_nc, d.ws_rows_cap, d.manifold_hdr,
+                                                d.sp, d.ws_init);
+        launches++;
+    }
 
     // PGS partitions: a contiguous range of the cell-ordered dynamic bodies per block, the range's
     // body deltas and world inverse inertias in shared memory when they fit (60 B per body)

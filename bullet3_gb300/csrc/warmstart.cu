@@ -165,7 +165,8 @@ static cudaError_t dalloc(Model& m, T** p, size_t count) {
 static cudaError_t alloc_acts(Model& m, Acts& a, int cap, bool training) {
     a.cap = cap;
     WS_CUDA(dalloc(m, &a.x_row, (size_t)cap * FI));
-    for (int l = 0; l < 3; l++) WS_CUDA(dalloc(m, &a.h_row[l], (size_t)cap * H));
+    // inference ping-pongs two activation buffers; training keeps all three for the backward pass
+    for (int l = 0; l < (training ? 3 : 2); l++) WS_CUDA(dalloc(m, &a.h_row[l], (size_t)cap * H));
     WS_CUDA(dalloc(m, &a.y, (size_t)cap * FO));
     if (!training) return cudaSuccess;
     WS_CUDA(dalloc(m, &a.x_col, (size_t)cap * FI));
@@ -190,9 +191,10 @@ static int run_forward(Model& m, Acts& a, const int* d_rows, int rows, int rows_
     const int grid = gemm_grid(m, rows_cap);
     const __nv_bfloat16* wt[3] = {m.wt1, m.wt2, m.wt3};
     const size_t boff[3] = {OFF_B1, OFF_B2, OFF_B3};
+    auto hbuf = [&](int l) { return a.h_row[training ? l : (l & 1)]; };
     for (int l = 0; l < 3; l++) {
         GemmArgs g;
-        g.A = l == 0 ? a.x_row : a.h_row[l - 1];
+        g.A = l == 0 ? a.x_row : hbuf(l - 1);
         g.lda = l == 0 ? FI : H;
         g.B = wt[l];
         g.ldb = l == 0 ? FI : H;
@@ -205,7 +207,7 @@ static int run_forward(Model& m, Acts& a, const int* d_rows, int rows, int rows_
         g.bias = m.params + boff[l];
         g.pre_out = training ? a.pre[l] : nullptr;
         g.ld_out = H;
-        g.out_row = a.h_row[l];
+        g.out_row = hbuf(l);
         g.ld_row = H;
         g.out_col = training ? a.h_col[l] : nullptr;
         g.ld_col = a.cap;
@@ -213,7 +215,7 @@ static int run_forward(Model& m, Acts& a, const int* d_rows, int rows, int rows_
         launch_gemm(g, grid, s);
     }
     GemmArgs g;
-    g.A = a.h_row[2];
+    g.A = hbuf(2);
     g.lda = H;
     g.B = m.wt4;
     g.ldb = H;
@@ -314,6 +316,8 @@ int forward_device(Model& m, const float* x, int ld_x, const int* d_rows, int ro
 }
 
 const float* last_predictions(const Model& m) { return m.infer.y; }
+
+const float* target_norm(const Model& m) { return m.norm + 2 * WS_FEATURES; }
 
 }  // namespace mlp
 }  // namespace b3g

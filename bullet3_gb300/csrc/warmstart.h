@@ -54,14 +54,20 @@ struct Model {
 };
 
 // Forward pass over rows of 12 float features (row stride ld_x floats), the row count read on
-// the device (*d_rows, clamped to rows_cap); writes out[r][0..2] = predictions in target units
-// (row stride ld_y).  Buffers for rows_cap rows must exist (ensure_infer).
+// the device (*d_rows, clamped to rows_cap); the predictions, in normalised units, are left in
+// last_predictions().  Buffers for rows_cap rows must exist (ensure_infer).  Returns launches.
 cudaError_t ensure_infer(Model& m, int rows_cap);
 int forward_device(Model& m, const float* x, int ld_x, const int* d_rows, int rows_cap, cudaStream_t s);
 // the device predictions of the last forward_device: [rows][WS_OUT_PAD] normalised units
 const float* last_predictions(const Model& m);
+// device target normalisation: mean[3], 1/std[3]
+const float* target_norm(const Model& m);
 
 }  // namespace mlp
 }  // namespace b3g
+
+#include "b3g_capi.h"
+// the model behind a C handle (nullptr for nullptr)
+b3g::mlp::Model* b3g_mlp_model(b3g_mlp m);
 
 #endif

@@ -21,6 +21,7 @@
 #include "b3g_capi.h"
 #include "common.cuh"
 #include "hull.h"
+#include "warmstart.h"
 #include "world_internal.h"
 
 using namespace b3g;
@@ -86,6 +87,7 @@ struct b3gWorld {
     long long graph_kernels = 0;
     b3gStepStats last_stats{};
     cudaEvent_t user_events[16] = {};
+    b3g_mlp ws_mlp = nullptr;  // attached warm-start network (not owned)
 };
 
 static void free_device(b3gWorld* w) {
@@ -164,6 +166,10 @@ extern "C" b3gStatus b3g_create(const b3gConfig* cfg, int cuda_device, b3g_handl
     if (w->cfg.pgs_partitions < B3G_PGS_PARTITIONS_AUTO || w->cfg.pgs_partitions > B3G_PGS_PARTITIONS_STREAMED) {
         delete w;
         return fail(B3G_ERR_INVALID_ARG, "pgs_partitions must be one of B3G_PGS_PARTITIONS_*");
+    }
+    if (w->cfg.warm_start < 0 || w->cfg.warm_start > 2 || w->cfg.warm_start_max_points < 0) {
+        delete w;
+        return fail(B3G_ERR_INVALID_ARG, "warm_start must be 0, 1 or 2 and warm_start_max_points >= 0");
     }
     if (w->cfg.pgs_interleave != 0 && w->cfg.pgs_interleave != 1) {
         delete w;
@@ -504,6 +510,21 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     TRY(dalloc(h, &d.color_offsets, 4 * (B3G_MAX_COLORS + 2)));  // offsets, fill, remaining, cursors
     TRY(dalloc(h, &d.color_claim, 4 * (size_t)N));  // claims, colour masks; again for cross-partition
     CUDA_TRY(solver_prepare());
+    if (h->cfg.warm_start != 0) {
+        // warm-start features (and predictions) for the first `cap` point slots
+        long long cap = h->cfg.warm_start_max_points > 0 ? h->cfg.warm_start_max_points
+                                                         : std::max(8192LL, 8LL * (long long)N);
+        cap = std::min(cap, 4LL * (long long)d.max_contacts);
+        d.ws_rows_cap = (int)cap;
+        TRY(dalloc(h, &d.ws_features, (size_t)cap * 12));
+        TRY(dalloc(h, &d.ws_rows, 1));
+        TRY(dalloc(h, &d.ws_init, (size_t)cap));
+        if (h->ws_mlp) {
+            d.ws_model = b3g_mlp_model(h->ws_mlp);
+            CUDA_TRY(mlp::ensure_infer(*d.ws_model, d.ws_rows_cap));
+            CUDA_TRY(cudaSetDevice(h->device));
+        }
+    }
     TRY(dalloc(h, &d.dv, 2 * (size_t)N));
     TRY(dalloc(h, &d.dv_sum, 2 * (size_t)N));
     TRY(dalloc(h, &d.manifold_hdr, d.max_contacts));
@@ -1069,5 +1090,78 @@ extern "C" b3gStatus b3g_grid_pairs_noalloc(const void* d_aabbs, int n, float ce
                               body_bits, static_cast<b3gPair*>(d_pairs), max_pairs, d_num_pairs,
                               static_cast<cudaStream_t>(cuda_stream));
     CUDA_TRY(cudaPeekAtLastError());
+    return B3G_OK;
+}
+
+// ------------------------------------------------------------------ learned warm start
+extern "C" b3gStatus b3g_set_warm_start_model(b3g_handle h, b3g_mlp m) {
+    if (!h) return fail(B3G_ERR_INVALID_ARG, "null handle");
+    mlp::Model* model = b3g_mlp_model(m);
+    if (model && model->device != h->device) return fail(B3G_ERR_INVALID_ARG, "network and world on different devices");
+    h->ws_mlp = m;
+    if (h->uploaded) {
+        CUDA_TRY(cudaSetDevice(h->device));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+        h->d.ws_model = h->d.ws_features ? model : nullptr;
+        if (h->d.ws_model) CUDA_TRY(mlp::ensure_infer(*h->d.ws_model, h->d.ws_rows_cap));
+        CUDA_TRY(cudaSetDevice(h->device));
+        if (h->graph_exec) {  // the captured step has (or lacks) the network's launches
+            cudaGraphExecDestroy(h->graph_exec);
+            h->graph_exec = nullptr;
+        }
+    }
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_read_warm_samples(b3g_handle h, float* features, float* targets, int capacity, int* num) {
+    REQUIRE_UPLOADED(h);
+    if (!num) return fail(B3G_ERR_INVALID_ARG, "null count");
+    if (!h->d.ws_features) return fail(B3G_ERR_INVALID_ARG, "warm_start is 0: no features are recorded");
+    DevCounters c;
+    TRY(read_counters(h, c));
+    const int nc = c.num_contacts;
+    const int slots = std::min(4 * nc, h->d.ws_rows_cap);
+    std::vector<float> f((size_t)slots * 12);
+    std::vector<float4> imp(slots);
+    std::vector<int4> hdr(nc);
+    if (slots > 0) {
+        TRY(copy_out(h, f.data(), h->d.ws_features, sizeof(float) * f.size()));
+        TRY(copy_out(h, imp.data(), h->d.sp.imp, sizeof(float4) * imp.size()));
+        TRY(copy_out(h, hdr.data(), h->d.manifold_hdr, sizeof(int4) * hdr.size()));
+    }
+    int n = 0;
+    for (int s = 0; s < slots; s++) {
+        if (!((hdr[s / 4].z >> (s % 4)) & 1)) continue;
+        if (n < capacity && features && targets) {
+            std::memcpy(features + (size_t)n * 12, f.data() + (size_t)s * 12, sizeof(float) * 12);
+            targets[(size_t)n * 3 + 0] = imp[s].x;
+            targets[(size_t)n * 3 + 1] = imp[s].y;
+            targets[(size_t)n * 3 + 2] = imp[s].z;
+        }
+        n++;
+    }
+    *num = n;
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_read_warm_start(b3g_handle h, float* host, int capacity, int* num) {
+    REQUIRE_UPLOADED(h);
+    if (!num) return fail(B3G_ERR_INVALID_ARG, "null count");
+    DevCounters c;
+    TRY(read_counters(h, c));
+    *num = c.num_contacts;
+    if (!host || capacity <= 0) return B3G_OK;
+    const int nm = std::min(c.num_contacts, capacity);
+    std::memset(host, 0, sizeof(float) * 12 * (size_t)nm);
+    if (!h->d.ws_init) return B3G_OK;
+    const int slots = std::min(4 * nm, h->d.ws_rows_cap);
+    std::vector<float4> w(slots);
+    if (slots > 0) TRY(copy_out(h, w.data(), h->d.ws_init, sizeof(float4) * w.size()));
+    for (int s = 0; s < slots; s++) {
+        float* o = host + (size_t)(s / 4) * 12 + 3 * (s % 4);
+        o[0] = w[s].x;  // contact
+        o[1] = w[s].z;  // lateral 1 = first friction direction
+        o[2] = w[s].y;  // lateral 2 = second friction direction
+    }
     return B3G_OK;
 }

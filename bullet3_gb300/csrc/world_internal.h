@@ -11,6 +11,10 @@
 
 namespace b3g {
 
+namespace mlp {
+struct Model;
+}
+
 // hull-hull pairs whose faces all have at most this many vertices take the thread-per-pair path
 #define B3G_SMALL_FACE_VERTS 8
 
@@ -103,6 +107,12 @@ struct DeviceState {
     uint32_t* jac_vals[2] = {nullptr, nullptr};
     float4* split_dv = nullptr;            // Jacobi: 2 sides * 2 float4 per manifold
     double* residual_acc = nullptr;        // per iteration: sum d^2, sum l^2
+    // learned warm start
+    mlp::Model* ws_model = nullptr;        // attached network (not owned)
+    float* ws_features = nullptr;          // 12 features per point slot 4m+j
+    int ws_rows_cap = 0;                   // point slots with features
+    int* ws_rows = nullptr;                // device: slots of the current step
+    float4* ws_init = nullptr;             // initial impulses of the last solve (per slot)
     // control
     DevCounters* counters = nullptr;
     unsigned int* barrier = nullptr;       // count, gen, abort

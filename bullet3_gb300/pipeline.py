@@ -46,6 +46,8 @@ class b3Config:
         self.solver_blocks_per_sm = 0
         self.pgs_partitions = capi.PGS_PARTITIONS_AUTO
         self.pgs_interleave = False
+        self.warm_start = 0
+        self.warm_start_max_points = 0
         for k, v in kw.items():
             if not hasattr(self, k):
                 raise AttributeError(k)
@@ -61,7 +63,8 @@ class b3Config:
                                    update_world_inertia=int(self.update_world_inertia), gravity=self.gravity,
                                    solver_blocks_per_sm=self.solver_blocks_per_sm,
                                    pgs_partitions=self.pgs_partitions,
-                                   pgs_interleave=int(self.pgs_interleave))
+                                   pgs_interleave=int(self.pgs_interleave), warm_start=int(self.warm_start),
+                                   warm_start_max_points=int(self.warm_start_max_points))
 
 
 class _World:
@@ -391,6 +394,30 @@ class b3GpuRigidBodyPipeline:
         out = np.zeros(n.value, np.int32)
         if n.value:
             call("b3g_read_solve_order", self._h, iptr(out), C.c_int(n.value), C.byref(n))
+        return out
+
+    def setWarmStartModel(self, model):
+        """Attach a bullet3_gb300.warmstart.WarmStartMLP (None detaches); used when warm_start=1."""
+        self._warm_model = model  # keep it alive while attached
+        call("b3g_set_warm_start_model", self._h, model.handle if model is not None else None)
+
+    def readWarmSamples(self):
+        """(features n x 12, converged impulses n x 3) of the last solve's active contact points."""
+        n = C.c_int()
+        call("b3g_read_warm_samples", self._h, None, None, C.c_int(0), C.byref(n))
+        f = np.zeros((n.value, 12), np.float32)
+        t = np.zeros((n.value, 3), np.float32)
+        if n.value:
+            call("b3g_read_warm_samples", self._h, fptr(f), fptr(t), C.c_int(n.value), C.byref(n))
+        return f, t
+
+    def readWarmStart(self) -> np.ndarray:
+        """Initial impulses of the last solve, 12 per manifold in the readImpulses layout."""
+        n = C.c_int()
+        call("b3g_read_warm_start", self._h, None, C.c_int(0), C.byref(n))
+        out = np.zeros((n.value, 12), np.float32)
+        if n.value:
+            call("b3g_read_warm_start", self._h, fptr(out), C.c_int(n.value), C.byref(n))
         return out
 
     def readImpulses(self) -> np.ndarray:

@@ -83,7 +83,9 @@ typedef struct b3gConfig {
     float residual_tol;        /* >0: stop PGS/Jacobi when the impulse residual drops below it */
     int update_world_inertia;  /* 0 = reference behaviour (world inverse inertia frozen at registration) */
     int use_cuda_graph;        /* capture the whole step as one CUDA graph */
-    int warm_start;            /* 0 = cold start (reference); 1 = learned warm start if a model is loaded */
+    int warm_start;            /* 0 = cold start (reference); 1 = learned warm start from the network attached with
+                                  b3g_set_warm_start_model (PGS; cold while none is attached); 2 = cold start that
+                                  records the network's features for training (b3g_read_warm_samples) */
     int barrier_spin_limit;    /* polls before a grid barrier gives up (0 = default, about a second) */
     int solver_blocks_per_sm;  /* persistent solver blocks per SM (0 = default; clamped to co-residency) */
     int pgs_partitions;        /* B3G_PGS_PARTITIONS_*: how the PGS solver splits work across blocks */
@@ -91,7 +93,9 @@ typedef struct b3gConfig {
                                   (per point: contact row, then its two friction rows), one pass per iteration;
                                   0: all contact rows, then all friction rows (the reference default).
                                   PGS only; the Jacobi solver ignores it */
-    int reserved[4];
+    int warm_start_max_points; /* point slots (4 per manifold, in manifold order) that get features and
+                                  predictions when warm_start != 0; 0 = 8 x bodies (at least 8192) */
+    int reserved[3];
 } b3gConfig;
 
 /* Per-step counters, copied once per step from the device. */
@@ -262,6 +266,19 @@ b3gStatus b3g_mlp_train(b3g_mlp m, int steps, int batch, float lr, int first_bat
  * public layout), without an update: the gradient check of the backward kernels */
 b3gStatus b3g_mlp_gradients(b3g_mlp m, const float* features, const float* targets, int n, float* grads,
                             double* loss);
+
+/* Attaches a warm-start network to a world (same device; not owned; NULL detaches).  With
+ * warm_start = 1 every PGS solve predicts the initial impulses of its contact points, applies
+ * them before the first sweep and iterates as usual; a prediction whose first-sweep residual is
+ * above a cold start's (1) is dropped and the solve restarts cold (B3G_FLAG_WARM_DISCARDED). */
+b3gStatus b3g_set_warm_start_model(b3g_handle h, b3g_mlp m);
+/* Training samples of the last solve (warm_start != 0): for every active contact point with
+ * features, its 12 features and its 3 converged impulses (contact, second friction direction,
+ * first friction direction).  *num = samples available; at most `capacity` are written. */
+b3gStatus b3g_read_warm_samples(b3g_handle h, float* features, float* targets, int capacity, int* num);
+/* The initial impulses of the last solve, 12 floats per manifold in the b3g_read_impulses layout
+ * (per point: normal, lateral 1, lateral 2); zero for a cold start. */
+b3gStatus b3g_read_warm_start(b3g_handle h, float* host, int capacity_manifolds, int* num);
 
 /* ---- allocation-free grid broadphase (no counterpart in the reference) -------------------------
  * The uniform-grid pair search of b3g_calculate_overlapping_pairs, run on the current CUDA device

@@ -934,6 +934,36 @@ static void solve_manifold(omanifold* M, int pass, v3* dlA, v3* daA, v3* dlB, v3
     }
 }
 
+/* a row's impulse delta applied to the body deltas, as solve_row applies it */
+static void apply_row_impulse(const orow* r, float delta, v3* dlA, v3* daA, v3* dlB, v3* daB, float imA, float imB) {
+    *dlA = add(*dlA, scl(scl(r->n, imA), delta));
+    *daA = add(*daA, scl(r->angA, delta));
+    *dlB = add(*dlB, scl(scl(neg(r->n), imB), delta));
+    *daB = add(*daB, scl(r->angB, delta));
+}
+
+/* Warm start: each active point's initial impulses (w: normal, first lateral = dir1, second
+ * lateral = dir2, the layout of impulses_out) become the rows' applied impulses and are applied
+ * to the body deltas, contact row first, then the dir2 row, then the dir1 row -- the
+ * internalApplyImpulse calls of setupContactConstraint / setupFrictionConstraint under
+ * B3_SOLVER_USE_WARMSTARTING (b3PgsJacobiSolver.cpp:745-752, 815-843). */
+static void warm_manifold(omanifold* M, const float* w, v3* dlA, v3* daA, v3* dlB, v3* daB) {
+    int j;
+    for (j = 0; j < 4; j++) {
+        orow* c;
+        if (!(M->mask & (1 << j))) continue;
+        c = &M->rows[j];
+        c->applied = w[3 * j + 0];
+        apply_row_impulse(c, c->applied, dlA, daA, dlB, daB, M->imA, M->imB);
+        c = &M->rows[4 + 2 * j + 0];
+        c->applied = w[3 * j + 2];
+        apply_row_impulse(c, c->applied, dlA, daA, dlB, daB, M->imA, M->imB);
+        c = &M->rows[4 + 2 * j + 1];
+        c->applied = w[3 * j + 1];
+        apply_row_impulse(c, c->applied, dlA, daA, dlB, daB, M->imA, M->imB);
+    }
+}
+
 static void gather_impulses(const omanifold* Ms, int nc, float* out) {
     int m, j;
     if (!out) return;
@@ -946,14 +976,25 @@ static void gather_impulses(const omanifold* Ms, int nc, float* out) {
 }
 
 static int solve_pgs_impl(obody* bodies, const oinertia* inertias, int nbodies, const ocontact* contacts, int nc,
-                          const int* order, int interleave, int iterations, float dt, float erp, float threshold,
-                          float tol, float* impulses_out, float* residual_out) {
+                          const int* order, int interleave, const float* warm, int iterations, float dt, float erp,
+                          float threshold, float tol, float* impulses_out, float* residual_out, int* discarded) {
     omanifold* Ms = (omanifold*)malloc(sizeof(omanifold) * (size_t)(nc > 0 ? nc : 1));
     v3* dl = (v3*)calloc((size_t)(nbodies > 0 ? nbodies : 1), sizeof(v3));
     v3* da = (v3*)calloc((size_t)(nbodies > 0 ? nbodies : 1), sizeof(v3));
-    int m, it, pass, k, b, done = 0;
+    int m, it, pass, k, b, done = 0, extra = 0, warm_live = warm != NULL;
     double r = 0.0;
     for (m = 0; m < nc; m++) setup_manifold(bodies, inertias, &contacts[m], NULL, 1, dt, erp, threshold, &Ms[m]);
+    if (discarded) *discarded = 0;
+    if (warm)
+        for (k = 0; k < nc; k++) {
+            const int mm = order ? order[k] : k;
+            omanifold* M = &Ms[mm];
+            v3 dlA = dl[M->A], daA = da[M->A], dlB = dl[M->B], daB = da[M->B];
+            if (!M->mask) continue;
+            warm_manifold(M, warm + (size_t)mm * 12, &dlA, &daA, &dlB, &daB);
+            if (M->imA != 0.f) { dl[M->A] = dlA; da[M->A] = daA; }
+            if (M->imB != 0.f) { dl[M->B] = dlB; da[M->B] = daB; }
+        }
     for (it = 0; it < iterations; it++) {
         double rd = 0.0, rl = 0.0;
         for (pass = 0; pass < (interleave ? 1 : 2); pass++)
@@ -967,8 +1008,22 @@ static int solve_pgs_impl(obody* bodies, const oinertia* inertias, int nbodies, 
             }
         done = it + 1;
         r = sqrt(rd) / fmax(sqrt(rl), 1e-12);
+        /* a warm start whose first sweep moved the impulses more than a cold start does (a cold
+         * first sweep has residual exactly 1) is dropped: restart cold with the full budget */
+        if (it == 0 && warm_live && r > 1.0) {
+            int j;
+            warm_live = 0;
+            extra = 1;
+            if (discarded) *discarded = 1;
+            for (b = 0; b < nbodies; b++) { dl[b] = mk(0, 0, 0); da[b] = mk(0, 0, 0); }
+            for (m = 0; m < nc; m++)
+                for (j = 0; j < 12; j++) Ms[m].rows[j].applied = 0.f;
+            it = -1;
+            continue;
+        }
         if (tol > 0.f && r <= (double)tol) break;
     }
+    done += extra;
     /* solveGroupCacheFriendlyFinish, PGS branch: v += dv */
     for (b = 0; b < nbodies; b++) {
         if (bodies[b].invMass == 0.f) continue;
@@ -1063,15 +1118,23 @@ int oracle_solve(obody* bodies, const oinertia* inertias, int nbodies, const oco
     if (mode == 1)
         return solve_jacobi_impl(bodies, inertias, nbodies, contacts, ncontacts, iterations, dt, erp, threshold,
                                  residual_tol, impulses_out, residual_out);
-    return solve_pgs_impl(bodies, inertias, nbodies, contacts, ncontacts, NULL, mode == 2, iterations, dt, erp,
-                          threshold, residual_tol, impulses_out, residual_out);
+    return solve_pgs_impl(bodies, inertias, nbodies, contacts, ncontacts, NULL, mode == 2, NULL, iterations, dt, erp,
+                          threshold, residual_tol, impulses_out, residual_out, NULL);
 }
 
 int oracle_solve_ordered(obody* bodies, const oinertia* inertias, int nbodies, const ocontact* contacts,
                          int ncontacts, const int* order, int interleave, int iterations, float dt, float erp,
                          float threshold, float* impulses_out) {
-    return solve_pgs_impl(bodies, inertias, nbodies, contacts, ncontacts, order, interleave, iterations, dt, erp,
-                          threshold, 0.f, impulses_out, NULL);
+    return solve_pgs_impl(bodies, inertias, nbodies, contacts, ncontacts, order, interleave, NULL, iterations, dt, erp,
+                          threshold, 0.f, impulses_out, NULL, NULL);
+}
+
+int oracle_solve_ordered_ex(obody* bodies, const oinertia* inertias, int nbodies, const ocontact* contacts,
+                            int ncontacts, const int* order, int interleave, const float* warm, int iterations,
+                            float dt, float erp, float threshold, float residual_tol, float* impulses_out,
+                            float* residual_out, int* discarded_out) {
+    return solve_pgs_impl(bodies, inertias, nbodies, contacts, ncontacts, order, interleave, warm, iterations, dt, erp,
+                          threshold, residual_tol, impulses_out, residual_out, discarded_out);
 }
 
 /* ------------------------------------------------------------------ integrate */

@@ -88,6 +88,16 @@ int oracle_solve_ordered(obody* bodies, const oinertia* inertias, int nbodies, c
                          int ncontacts, const int* order, int interleave, int iterations, float dt, float erp,
                          float threshold, float* impulses_out);
 
+/* oracle_solve_ordered with a warm start (warm: 12 floats per manifold, per point normal,
+ * first lateral (dir1), second lateral (dir2) -- the layout of impulses_out; NULL = cold), a
+ * residual tolerance (0 = run all iterations) and the warm-start fallback: a warm start whose
+ * first-sweep residual exceeds 1 (a cold start's) is dropped and the solve restarts cold
+ * (*discarded_out = 1; the dropped sweep counts in the returned iteration count). */
+int oracle_solve_ordered_ex(obody* bodies, const oinertia* inertias, int nbodies, const ocontact* contacts,
+                            int ncontacts, const int* order, int interleave, const float* warm, int iterations,
+                            float dt, float erp, float threshold, float residual_tol, float* impulses_out,
+                            float* residual_out, int* discarded_out);
+
 /* integrateSingleTransform (Bullet3Dynamics/shared/b3IntegrateTransforms.h:5-55) for every body */
 void oracle_integrate(obody* bodies, int n, float dt, float damping, const float gravity[3]);
 

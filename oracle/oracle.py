@@ -167,6 +167,27 @@ def solve_ordered(bodies, inertias, contacts_, order, iterations=10, dt=1 / 60, 
     return b, imp[:len(c)]
 
 
+def solve_ordered_ex(bodies, inertias, contacts_, order, warm=None, iterations=10, residual_tol=0.0, dt=1 / 60,
+                     erp=0.2, threshold=0.02, interleave=False):
+    """PGS in a given manifold order with an optional warm start (12 floats per manifold, the
+    layout of the impulses) and residual tolerance.  Returns (bodies, impulses, iterations run,
+    final residual, warm start discarded)."""
+    b = np.array(bodies, BODY, copy=True)
+    I = np.ascontiguousarray(inertias, INERTIA)
+    c = np.ascontiguousarray(contacts_, CONTACT)
+    o = np.ascontiguousarray(order, np.int32)
+    imp = np.zeros((max(1, len(c)), 12), np.float32)
+    w = None if warm is None else np.ascontiguousarray(warm, np.float32).reshape(-1, 12)
+    res = C.c_float(0)
+    disc = C.c_int(0)
+    it = load_oracle().oracle_solve_ordered_ex(_p(b), _p(I), C.c_int(len(b)), _p(c), C.c_int(len(c)), _p(o),
+                                               C.c_int(1 if interleave else 0), _p(w) if w is not None else None,
+                                               C.c_int(iterations), C.c_float(dt), C.c_float(erp),
+                                               C.c_float(threshold), C.c_float(residual_tol), _p(imp), C.byref(res),
+                                               C.byref(disc))
+    return b, imp[:len(c)], it, res.value, bool(disc.value)
+
+
 def integrate(bodies, dt=1 / 60, damping=0.99, gravity=(0.0, -9.8, 0.0)):
     b = np.array(bodies, BODY, copy=True)
     g = (C.c_float * 3)(*gravity)

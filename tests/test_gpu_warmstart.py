@@ -1,0 +1,131 @@
+"""The learned warm start inside the step: features, the network's predictions as initial
+impulses, their application before the first sweep and the cold-start fallback.
+
+Bars: features within 1e-5 relative of a float32 restatement from the same state; warm-started
+PGS velocities bit-exact against the oracle sweeping the GPU's order from the same initial
+impulses; a warm start worse than a cold start is dropped and the result equals the cold solve
+bit for bit, with the dropped sweep counted.
+"""
+import numpy as np
+import pytest
+
+from gpu_helpers import load, run_stages
+from bullet3_gb300 import capi, scenes
+from oracle import mlp_oracle as MO
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _network(bias_out=(0.0, 0.0, 0.0), seed=4, scale=1.0):
+    from bullet3_gb300.warmstart import WarmStartMLP
+    m = WarmStartMLP(seed=seed)
+    p = MO.init_params(seed) * scale
+    p[-3:] = bias_out
+    m.params = p
+    n = MO.identity_norm()
+    n[24:27] = (0.5, 0.0, 0.0)  # target mean: a positive contact impulse
+    n[27:30] = (2.0, 10.0, 10.0)
+    m.normalization = n
+    return m
+
+
+def _features_cpu(b, c, dt=1 / 60, g=(0.0, -9.8, 0.0), threshold=0.02):
+    f32 = np.float32
+    rows = []
+    for m in range(len(c)):
+        A, B = abs(int(c["bodyA"][m])), abs(int(c["bodyB"][m]))
+        imA, imB = b["invMass"][A], b["invMass"][B]
+        npts = min(int(c["normal"][m, 3]), 4)
+        if imA == 0 and imB == 0:
+            continue
+        n = c["normal"][m, :3].astype(f32)
+        n = n * f32(f32(1.0) / np.sqrt(f32(n @ n)))
+        for j in range(npts):
+            dist = c["worldPosB"][m, j, 3]
+            if not dist <= threshold:
+                continue
+            p2 = c["worldPosB"][m, j, :3]
+            p1 = p2 + n * dist
+            r1 = p1 - b["pos"][A, :3]
+            r2 = p2 - b["pos"][B, :3]
+            v1 = b["linVel"][A, :3] + np.cross(b["angVel"][A, :3], r1)
+            v2 = b["linVel"][B, :3] + np.cross(b["angVel"][B, :3], r2)
+            v = (v1 - v2).astype(f32)
+            vt = v - n * f32(n @ v)
+            rows.append(np.concatenate([v, n, [dist, imA, imB, npts, np.sqrt(vt @ vt), dt * (np.dot(g, n))]]))
+    return np.array(rows, np.float32)
+
+
+def test_features_match_restatement():
+    sc = scenes.mixed_scene(2048, extent=14.0, seed=8, plane=True)
+    np_, bp, pl, shapes = load(sc, m_maxBroadphasePairs=300000, warm_start=2)
+    b = np_.readbackAllBodiesToCpu()
+    run_stages(np_, bp, pl)
+    f, t = pl.readWarmSamples()
+    ref = _features_cpu(b, np_.getContactsCPU())
+    assert len(f) == len(ref) > 1000
+    np.testing.assert_allclose(f, ref, rtol=1e-5, atol=2e-6)
+    # targets are the converged impulses of the same points
+    imp = pl.readImpulses()
+    assert np.isfinite(t).all() and (t[:, 0] >= 0).all()
+    assert np.isclose(t[:, 0].sum(), imp[:, 0::3].sum(), rtol=1e-5)
+
+
+@pytest.mark.parametrize("interleave", [False, True])
+@pytest.mark.parametrize("parts", [capi.PGS_PARTITIONS_AUTO, capi.PGS_PARTITIONS_STREAMED])
+def test_warm_started_solve_bitexact(interleave, parts):
+    sc = scenes.box_stack(12, 10, 12, seed=6)
+    np_, bp, pl, shapes = load(sc, solver_mode=capi.SOLVER_PGS, solver_iterations=10, warm_start=1,
+                               pgs_interleave=interleave, pgs_partitions=parts)
+    net = _network()
+    pl.setWarmStartModel(net)
+    b = np_.readbackAllBodiesToCpu()
+    I = np_.readInertiasToCpu()
+    run_stages(np_, bp, pl)
+    gc = np_.getContactsCPU()
+    warm = pl.readWarmStart()
+    assert (warm[:, 0::3] > 0).any()  # the network produced non-trivial initial impulses
+    order = pl.readSolveOrder()
+    ob, oimp, it, res, disc = O.solve_ordered_ex(b, I, gc, order, warm=warm, iterations=10, interleave=interleave)
+    gb = np_.readbackAllBodiesToCpu()
+    st = pl.stats()
+    assert bool(st.status & capi.FLAG_WARM_DISCARDED) == disc
+    assert np.array_equal(gb["linVel"], ob["linVel"]) and np.array_equal(gb["angVel"], ob["angVel"])
+    assert np.array_equal(pl.readImpulses(), oimp)
+    assert st.iterations == it
+
+
+def test_bad_warm_start_is_dropped():
+    # one layer of boxes on the plane: absurd initial contact impulses launch every box, so the
+    # first sweep clamps them back to ~0 (residual >> 1).  (In tall stacks a uniform impulse
+    # cancels between neighbours and would not be detected as worse -- nor is it.)
+    sc = scenes.box_stack(4, 1, 4, seed=2)
+    outs = []
+    for warm in (0, 1):
+        np_, bp, pl, shapes = load(sc, solver_mode=capi.SOLVER_PGS, solver_iterations=10, warm_start=warm,
+                                   pgs_interleave=True)
+        if warm:
+            pl.setWarmStartModel(_network(bias_out=(50.0, 0.0, 0.0)))  # absurd impulses
+        run_stages(np_, bp, pl)
+        st = pl.stats()
+        outs.append((np_.readbackAllBodiesToCpu(), st))
+    (cold, st0), (warmb, st1) = outs
+    assert st1.status & capi.FLAG_WARM_DISCARDED and not st0.status & capi.FLAG_WARM_DISCARDED
+    assert st1.iterations == st0.iterations + 1
+    assert np.array_equal(cold["linVel"], warmb["linVel"]) and np.array_equal(cold["angVel"], warmb["angVel"])
+
+
+def test_graph_step_with_network():
+    # the network's launches are part of the captured step; graph and staged steps agree
+    res = []
+    for graph in (True, False):
+        sc = scenes.box_pile(5, 5, 5, seed=3)
+        np_, bp, pl, shapes = load(sc, use_cuda_graph=graph, warm_start=1, pgs_interleave=True)
+        pl.setWarmStartModel(_network())
+        for _ in range(30):
+            pl.stepSimulation(1 / 60)
+        pl.synchronize()
+        res.append(np_.readbackAllBodiesToCpu())
+        assert pl.status() & ~capi.FLAG_WARM_DISCARDED == 0
+    assert np.array_equal(res[0].view(np.uint8), res[1].view(np.uint8))
