@@ -32,6 +32,7 @@ SHAPE_CONVEX_HULL, SHAPE_PLANE, SHAPE_SPHERE = 3, 4, 7
 SOLVER_PGS, SOLVER_JACOBI = 0, 1
 PGS_PARTITIONS_AUTO, PGS_PARTITIONS_GLOBAL_DELTAS, PGS_PARTITIONS_NONE, PGS_PARTITIONS_SHARED = 0, 1, 2, 3
 PGS_PARTITIONS_STREAMED = 4
+WARM_COLD, WARM_LEARNED, WARM_RECORD, WARM_PERSISTENT, WARM_PERSISTENT_LEARNED = 0, 1, 2, 3, 4
 
 FLAG_PAIR_OVERFLOW = 0x1
 FLAG_CONTACT_OVERFLOW = 0x2

@@ -1146,31 +1146,117 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_jacobi(SolverArgs a) {
     }
 }
 
-// Network predictions (normalised units, 16 per slot) -> initial impulses of the point records:
-// contact impulse >= 0, friction impulses inside the friction cone of that impulse, non-finite
-// values dropped (cold).  Slots beyond the feature capacity start cold.
-__global__ void k_warm_fill(const float* __restrict__ pred, const float* __restrict__ tnorm, const int* __restrict__ d_nc,
-                            int rows_cap, const int4* __restrict__ hdr, SolverPoints sp, float4* __restrict__ init) {
-    const int nc = *d_nc;
-    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nc; m += gridDim.x * blockDim.x) {
-        const int mask = hdr[m].z;
-        const float fr = sp.nf[m].w;
+// Initial impulses of the point records.  A point persists when the previous solve had a
+// manifold for the same body pair (binary search of the ascending pair keys) with an active point
+// on body B within 0.05 of it; it then starts from that point's converged impulses (persist).
+// Other points start from the network's prediction (pred, normalised units, 16 per slot: contact
+// impulse >= 0, friction impulses inside that impulse's friction cone, non-finite values cold)
+// or cold.  With write_imp 0 only the persistence flags are recorded.  Slots beyond rows_cap
+// start cold.
+struct WarmFill {
+    const float* pred;            // nullptr: no network
+    const float* tnorm;           // target mean[3], 1/std[3]
+    const int* d_nc;
+    int rows_cap;
+    const int4* hdr;
+    SolverPoints sp;
+    const b3gContact4* slots;
+    const int* manifold_pair;
+    int body_bits;
+    const unsigned long long* prev_keys;
+    const float4* prev_pts;
+    const float4* prev_imp;
+    const int* prev_n;
+    int persist;                  // take persisting points' previous impulses
+    int predict_all;              // network also for persisting points
+    int write_imp;
+    float4* init;
+    unsigned char* is_new;
+};
+
+__device__ __forceinline__ unsigned long long pair_key(int a, int b, int bits) {
+    const unsigned lo = (unsigned)min(a, b), hi = (unsigned)max(a, b);
+    return ((unsigned long long)lo << bits) | hi;
+}
+
+__global__ void k_warm_fill(WarmFill w) {
+    const int nc = *w.d_nc;
+    const int pn = *w.prev_n;
+    const int mmax = min(nc, w.rows_cap / 4);
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < mmax; m += gridDim.x * blockDim.x) {
+        const int4 h = w.hdr[m];
+        const int mask = h.z;
+        const float fr = w.sp.nf[m].w;
+        // previous manifold of the same body pair
+        const unsigned long long key = pair_key(h.x, h.y, w.body_bits);
+        int lo = 0, hi = pn;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (w.prev_keys[mid] < key)
+                lo = mid + 1;
+            else
+                hi = mid;
+        }
+        const int q = (lo < pn && w.prev_keys[lo] == key) ? lo : -1;
+        const b3gContact4& c = w.slots[w.manifold_pair[m]];
         for (int j = 0; j < 4; j++) {
             const size_t s = (size_t)m * 4 + j;
-            float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
-            if ((mask & (1 << j)) && s < (size_t)rows_cap) {
-                const float* y = pred + s * 16;
-                float lam = y[0] / tnorm[3] + tnorm[0];
-                float f2 = y[1] / tnorm[4] + tnorm[1];
-                float f1 = y[2] / tnorm[5] + tnorm[2];
-                if (!(lam > 0.f) || !isfinite(lam)) lam = 0.f;
-                const float lim = fr * lam;
-                f2 = isfinite(f2) ? fminf(fmaxf(f2, -lim), lim) : 0.f;
-                f1 = isfinite(f1) ? fminf(fmaxf(f1, -lim), lim) : 0.f;
-                w = make_float4(lam, f2, f1, 0.f);
-                sp.imp[s] = w;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            bool matched = false;
+            if (mask & (1 << j)) {
+                if (q >= 0) {
+                    float best = 0.05f * 0.05f;
+                    int bj = -1;
+                    for (int k = 0; k < 4; k++) {
+                        const float4 p = w.prev_pts[(size_t)q * 4 + k];
+                        if (p.w == 0.f) continue;
+                        const float dx = p.x - c.worldPosB[j].x, dy = p.y - c.worldPosB[j].y, dz = p.z - c.worldPosB[j].z;
+                        const float d2 = dx * dx + dy * dy + dz * dz;
+                        if (d2 < best) {
+                            best = d2;
+                            bj = k;
+                        }
+                    }
+                    if (bj >= 0) {
+                        matched = true;
+                        if (w.persist) v = w.prev_imp[(size_t)q * 4 + bj];
+                    }
+                }
+                if (w.pred && (!matched || w.predict_all || !w.persist)) {
+                    const float* y = w.pred + s * 16;
+                    float lam = y[0] / w.tnorm[3] + w.tnorm[0];
+                    float f2 = y[1] / w.tnorm[4] + w.tnorm[1];
+                    float f1 = y[2] / w.tnorm[5] + w.tnorm[2];
+                    if (!(lam > 0.f) || !isfinite(lam)) lam = 0.f;
+                    const float lim = fr * lam;
+                    f2 = isfinite(f2) ? fminf(fmaxf(f2, -lim), lim) : 0.f;
+                    f1 = isfinite(f1) ? fminf(fmaxf(f1, -lim), lim) : 0.f;
+                    v = make_float4(lam, f2, f1, 0.f);
+                }
+                if (w.write_imp) w.sp.imp[s] = v;
             }
-            if (init && s < (size_t)rows_cap) init[s] = w;
+            if (w.init) w.init[s] = w.write_imp ? v : make_float4(0.f, 0.f, 0.f, 0.f);
+            if (w.is_new) w.is_new[s] = matched ? 0 : 1;
+        }
+    }
+}
+
+// The solved manifolds (first rows_cap / 4) for the next step's persistence lookup.
+__global__ void k_warm_store(const int* __restrict__ d_nc, int rows_cap, const int4* __restrict__ hdr,
+                             const b3gContact4* __restrict__ slots, const int* __restrict__ manifold_pair,
+                             const float4* __restrict__ imp, int body_bits, unsigned long long* __restrict__ keys,
+                             float4* __restrict__ pts, float4* __restrict__ pimp, int* __restrict__ prev_n) {
+    const int n = min(*d_nc, rows_cap / 4);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *prev_n = n;
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
+        const int4 h = hdr[m];
+        keys[m] = pair_key(h.x, h.y, body_bits);
+        const b3gContact4& c = slots[manifold_pair[m]];
+        for (int j = 0; j < 4; j++) {
+            const size_t s = (size_t)m * 4 + j;
+            const bool on = (h.z >> j) & 1;
+            pts[s] = make_float4(c.worldPosB[j].x, c.worldPosB[j].y, c.worldPosB[j].z, on ? 1.f : 0.f);
+            pimp[s] = on ? imp[s] : make_float4(0.f, 0.f, 0.f, 0.f);
         }
     }
 }
@@ -1266,7 +1352,10 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     a.gx = cfg.gravity[0];
     a.gy = cfg.gravity[1];
     a.gz = cfg.gravity[2];
-    a.warm = (cfg.warm_start == 1 && d.ws_model && a.ws_features && cfg.solver_mode == B3G_SOLVER_PGS) ? 1 : 0;
+    const int wm = cfg.warm_start;
+    const bool ws_learned = (wm == B3G_WARM_LEARNED || wm == B3G_WARM_PERSISTENT_LEARNED) && d.ws_model && a.ws_features;
+    const bool ws_persist = wm == B3G_WARM_PERSISTENT || wm == B3G_WARM_PERSISTENT_LEARNED;
+    a.warm = (cfg.solver_mode == B3G_SOLVER_PGS && (ws_learned || ws_persist)) ? 1 : 0;
     a.claim = d.color_claim;
     a.mask = d.color_claim + d.num_bodies;
     a.claim_x = d.color_claim + 2 * (size_t)d.num_bodies;
@@ -1301,12 +1390,33 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     }
     k_setup_rows<<<grid, SV_THREADS, 0, s>>>(a);
     launches++;
-    if (a.warm) {
-        // learned warm start: the network's predictions become the records' initial impulses
-        launches += mlp::forward_device(*d.ws_model, d.ws_features, 12, d.ws_rows, d.ws_rows_cap, s);
-        k_warm_fill<<<grid, SV_THREADS, 0, s>>>(mlp::last_predictions(*d.ws_model),
-                                                mlp::target_norm(*d.ws_model), d_nc, d.ws_rows_cap, d.manifold_hdr,
-                                                d.sp, d.ws_init);
+    if (wm != B3G_WARM_COLD && d.ws_init) {
+        // initial impulses: persisting points from the previous solve, the others from the network
+        WarmFill w;
+        w.pred = nullptr;
+        w.tnorm = nullptr;
+        if (ws_learned && a.warm) {
+            launches += mlp::forward_device(*d.ws_model, d.ws_features, 12, d.ws_rows, d.ws_rows_cap, s);
+            w.pred = mlp::last_predictions(*d.ws_model);
+            w.tnorm = mlp::target_norm(*d.ws_model);
+        }
+        w.d_nc = d_nc;
+        w.rows_cap = d.ws_rows_cap;
+        w.hdr = d.manifold_hdr;
+        w.sp = d.sp;
+        w.slots = d.contact_slots;
+        w.manifold_pair = d.manifold_pair;
+        w.body_bits = d.body_bits;
+        w.prev_keys = d.prev_keys;
+        w.prev_pts = d.prev_pts;
+        w.prev_imp = d.prev_imp;
+        w.prev_n = d.prev_n;
+        w.persist = ws_persist ? 1 : 0;
+        w.predict_all = wm == B3G_WARM_LEARNED ? 1 : 0;
+        w.write_imp = a.warm;
+        w.init = d.ws_init;
+        w.is_new = d.ws_new;
+        k_warm_fill<<<grid, SV_THREADS, 0, s>>>(w);
         launches++;
     }
 
@@ -1367,6 +1477,12 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     cudaError_t e = jac ? cudaLaunchKernelEx(&lc, k_solve_jacobi, a) : cudaLaunchKernelEx(&lc, k_solve_pgs, a);
     if (e != cudaSuccess && d.launch_error == cudaSuccess) d.launch_error = e;
     launches++;
+    if (wm != B3G_WARM_COLD && d.prev_keys) {  // this solve's impulses for the next step's persisting points
+        k_warm_store<<<grid, SV_THREADS, 0, s>>>(d_nc, d.ws_rows_cap, d.manifold_hdr, d.contact_slots, d.manifold_pair,
+                                                 d.sp.imp, d.body_bits, d.prev_keys, d.prev_pts, d.prev_imp,
+                                                 d.prev_n);
+        launches++;
+    }
     return launches + (int)ll;
 }
 

@@ -167,9 +167,10 @@ extern "C" b3gStatus b3g_create(const b3gConfig* cfg, int cuda_device, b3g_handl
         delete w;
         return fail(B3G_ERR_INVALID_ARG, "pgs_partitions must be one of B3G_PGS_PARTITIONS_*");
     }
-    if (w->cfg.warm_start < 0 || w->cfg.warm_start > 2 || w->cfg.warm_start_max_points < 0) {
+    if (w->cfg.warm_start < B3G_WARM_COLD || w->cfg.warm_start > B3G_WARM_PERSISTENT_LEARNED ||
+        w->cfg.warm_start_max_points < 0) {
         delete w;
-        return fail(B3G_ERR_INVALID_ARG, "warm_start must be 0, 1 or 2 and warm_start_max_points >= 0");
+        return fail(B3G_ERR_INVALID_ARG, "warm_start must be one of B3G_WARM_* and warm_start_max_points >= 0");
     }
     if (w->cfg.pgs_interleave != 0 && w->cfg.pgs_interleave != 1) {
         delete w;
@@ -515,10 +516,19 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
         long long cap = h->cfg.warm_start_max_points > 0 ? h->cfg.warm_start_max_points
                                                          : std::max(8192LL, 8LL * (long long)N);
         cap = std::min(cap, 4LL * (long long)d.max_contacts);
+        cap = cap / 4 * 4;
         d.ws_rows_cap = (int)cap;
-        TRY(dalloc(h, &d.ws_features, (size_t)cap * 12));
+        const int wm = h->cfg.warm_start;
+        if (wm == B3G_WARM_LEARNED || wm == B3G_WARM_RECORD || wm == B3G_WARM_PERSISTENT_LEARNED)
+            TRY(dalloc(h, &d.ws_features, (size_t)cap * 12));
         TRY(dalloc(h, &d.ws_rows, 1));
         TRY(dalloc(h, &d.ws_init, (size_t)cap));
+        TRY(dalloc(h, &d.ws_new, (size_t)cap));
+        TRY(dalloc(h, &d.prev_keys, (size_t)cap / 4));
+        TRY(dalloc(h, &d.prev_pts, (size_t)cap));
+        TRY(dalloc(h, &d.prev_imp, (size_t)cap));
+        TRY(dalloc(h, &d.prev_n, 1));
+        CUDA_TRY(cudaMemsetAsync(d.prev_n, 0, sizeof(int), h->stream));
         if (h->ws_mlp) {
             d.ws_model = b3g_mlp_model(h->ws_mlp);
             CUDA_TRY(mlp::ensure_infer(*d.ws_model, d.ws_rows_cap));
@@ -1113,10 +1123,11 @@ extern "C" b3gStatus b3g_set_warm_start_model(b3g_handle h, b3g_mlp m) {
     return B3G_OK;
 }
 
-extern "C" b3gStatus b3g_read_warm_samples(b3g_handle h, float* features, float* targets, int capacity, int* num) {
+extern "C" b3gStatus b3g_read_warm_samples(b3g_handle h, float* features, float* targets, int* is_new, int capacity,
+                                           int* num) {
     REQUIRE_UPLOADED(h);
     if (!num) return fail(B3G_ERR_INVALID_ARG, "null count");
-    if (!h->d.ws_features) return fail(B3G_ERR_INVALID_ARG, "warm_start is 0: no features are recorded");
+    if (!h->d.ws_features) return fail(B3G_ERR_INVALID_ARG, "warm_start records no features (LEARNED, RECORD or PERSISTENT_LEARNED do)");
     DevCounters c;
     TRY(read_counters(h, c));
     const int nc = c.num_contacts;
@@ -1124,10 +1135,12 @@ extern "C" b3gStatus b3g_read_warm_samples(b3g_handle h, float* features, float*
     std::vector<float> f((size_t)slots * 12);
     std::vector<float4> imp(slots);
     std::vector<int4> hdr(nc);
+    std::vector<unsigned char> fresh(slots);
     if (slots > 0) {
         TRY(copy_out(h, f.data(), h->d.ws_features, sizeof(float) * f.size()));
         TRY(copy_out(h, imp.data(), h->d.sp.imp, sizeof(float4) * imp.size()));
         TRY(copy_out(h, hdr.data(), h->d.manifold_hdr, sizeof(int4) * hdr.size()));
+        TRY(copy_out(h, fresh.data(), h->d.ws_new, fresh.size()));
     }
     int n = 0;
     for (int s = 0; s < slots; s++) {
@@ -1137,6 +1150,7 @@ extern "C" b3gStatus b3g_read_warm_samples(b3g_handle h, float* features, float*
             targets[(size_t)n * 3 + 0] = imp[s].x;
             targets[(size_t)n * 3 + 1] = imp[s].y;
             targets[(size_t)n * 3 + 2] = imp[s].z;
+            if (is_new) is_new[n] = fresh[s];
         }
         n++;
     }

@@ -113,6 +113,12 @@ struct DeviceState {
     int ws_rows_cap = 0;                   // point slots with features
     int* ws_rows = nullptr;                // device: slots of the current step
     float4* ws_init = nullptr;             // initial impulses of the last solve (per slot)
+    unsigned char* ws_new = nullptr;       // per slot: 1 = no persisting predecessor
+    // the previous solve's manifolds (first ws_rows_cap / 4), for persisting contact points
+    unsigned long long* prev_keys = nullptr;  // body-pair key (min << body_bits | max), ascending
+    float4* prev_pts = nullptr;            // per slot: point on B (world), w = 1 if active
+    float4* prev_imp = nullptr;            // per slot: converged impulses (contact, dir2, dir1)
+    int* prev_n = nullptr;                 // device: manifolds stored
     // control
     DevCounters* counters = nullptr;
     unsigned int* barrier = nullptr;       // count, gen, abort

@@ -401,15 +401,16 @@ class b3GpuRigidBodyPipeline:
         self._warm_model = model  # keep it alive while attached
         call("b3g_set_warm_start_model", self._h, model.handle if model is not None else None)
 
-    def readWarmSamples(self):
-        """(features n x 12, converged impulses n x 3) of the last solve's active contact points."""
+    def readWarmSamples(self, with_new: bool = False):
+        """(features n x 12, converged impulses n x 3[, is_new n]) of the last solve's active points."""
         n = C.c_int()
-        call("b3g_read_warm_samples", self._h, None, None, C.c_int(0), C.byref(n))
+        call("b3g_read_warm_samples", self._h, None, None, None, C.c_int(0), C.byref(n))
         f = np.zeros((n.value, 12), np.float32)
         t = np.zeros((n.value, 3), np.float32)
+        new = np.zeros(n.value, np.int32)
         if n.value:
-            call("b3g_read_warm_samples", self._h, fptr(f), fptr(t), C.c_int(n.value), C.byref(n))
-        return f, t
+            call("b3g_read_warm_samples", self._h, fptr(f), fptr(t), iptr(new), C.c_int(n.value), C.byref(n))
+        return (f, t, new.astype(bool)) if with_new else (f, t)
 
     def readWarmStart(self) -> np.ndarray:
         """Initial impulses of the last solve, 12 per manifold in the readImpulses layout."""

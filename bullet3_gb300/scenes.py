@@ -48,6 +48,48 @@ def random_quaternions(rng, n) -> np.ndarray:
     return q.astype(np.float32)
 
 
+def batched_piles(n_scenes=4096, seed=0, min_bodies=8, max_bodies=256, spacing=1.1, base_y=0.6, jitter=0.01,
+                  half=0.5, sphere_fraction=0.5, pitch=None) -> Scene:
+    """Many independent piles on the plane y = 0, laid out on a square grid of scene cells far
+    enough apart that no two piles interact.  Body counts floor(exp(U(ln 8, ln 257))) clipped to
+    [8, 256] (mean ~72); each pile is a jittered lattice (spacing 1.1, base 0.6, jitter 0.01, zero
+    velocity, mass 1) of unit boxes and spheres of radius 0.5.  Returns the scene with
+    `scene_of` (per body: pile index, -1 for the plane) and `scene_offsets` (first body per pile)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    counts = np.clip(np.floor(np.exp(rng.uniform(np.log(min_bodies), np.log(max_bodies + 1), n_scenes))),
+                     min_bodies, max_bodies).astype(int)
+    side = int(np.ceil(np.sqrt(n_scenes)))
+    foot = int(np.ceil(np.sqrt(max_bodies / 4.0)))  # lattice columns per side at 4 layers
+    pitch = pitch if pitch else foot * spacing + 4.0
+    sc = Scene(name=f"batched_piles_{n_scenes}")
+    sc.shapes.append({"type": "plane", "normal": (0.0, 1.0, 0.0), "constant": 0.0})
+    sc.shapes.append({"type": "hull", "verts": box_vertices(half, half, half)})
+    sc.shapes.append({"type": "sphere", "radius": half})
+    shapes, pos, scene_of, offsets = [0], [np.zeros(3)], [-1], []
+    for s, n in enumerate(counts):
+        cx, cz = (s % side) * pitch, (s // side) * pitch
+        cols = max(1, int(np.ceil(np.sqrt(n / 4.0))))
+        layers = int(np.ceil(n / (cols * cols)))
+        ii, kk, jj = np.meshgrid(np.arange(cols), np.arange(cols), np.arange(layers), indexing="ij")
+        lat = np.stack([ii.ravel(), jj.ravel(), kk.ravel()], 1)
+        lat = lat[np.lexsort((lat[:, 2], lat[:, 0], lat[:, 1]))][:n]  # bottom layers first
+        p = np.stack([cx + (lat[:, 0] - (cols - 1) * 0.5) * spacing, base_y + lat[:, 1] * spacing,
+                      cz + (lat[:, 2] - (cols - 1) * 0.5) * spacing], 1)
+        p = p + rng.uniform(-jitter, jitter, p.shape)
+        kind = np.where(rng.uniform(size=n) < sphere_fraction, 2, 1)
+        offsets.append(len(shapes))
+        shapes.extend(kind.tolist())
+        pos.extend(list(p))
+        scene_of.extend([s] * n)
+    sc.body_shape = np.array(shapes, np.int32)
+    sc.mass = np.array([0.0] + [1.0] * (len(shapes) - 1), np.float32)
+    sc.pos = np.array(pos, np.float32)
+    sc.orn = np.tile(np.array([0, 0, 0, 1], np.float32), (len(shapes), 1))
+    sc.scene_of = np.array(scene_of, np.int32)
+    sc.scene_offsets = np.array(offsets, np.int32)
+    return sc
+
+
 def box_pile(nx=10, ny=10, nz=10, spacing=1.1, base_y=0.6, jitter=0.01, half=0.5, mass=1.0, seed=0,
              plane=True) -> Scene:
     rng = np.random.Generator(np.random.PCG64(seed))

@@ -63,6 +63,22 @@ typedef enum b3gStatus {
 #define B3G_PGS_PARTITIONS_SHARED 3
 #define B3G_PGS_PARTITIONS_STREAMED 4
 
+/* Warm start of the PGS solve (b3gConfig.warm_start).  A contact point "persists" when the
+ * previous step had a manifold for the same body pair with a point within 0.05 of it (points on
+ * body B, world space); persisting points then start from that point's converged impulses, as
+ * B3_SOLVER_USE_WARMSTARTING does with cached contact points.  LEARNED predicts the initial
+ * impulses of every point with the network attached by b3g_set_warm_start_model;
+ * PERSISTENT_LEARNED predicts only the new points.  RECORD starts cold and records the
+ * network's features and the points' persistence for training (b3g_read_warm_samples).
+ * Whatever the source, a warm start whose first sweep has a residual above a cold start's (1) is
+ * dropped and the solve restarts cold (B3G_FLAG_WARM_DISCARDED).  Without a network attached,
+ * LEARNED is cold and PERSISTENT_LEARNED is PERSISTENT. */
+#define B3G_WARM_COLD 0
+#define B3G_WARM_LEARNED 1
+#define B3G_WARM_RECORD 2
+#define B3G_WARM_PERSISTENT 3
+#define B3G_WARM_PERSISTENT_LEARNED 4
+
 /* One configuration struct replaces b3Config (b3Config.h:4-37) plus the constants the
  * reference hard-codes (dt 1/60 b3GpuPgsContactSolver.cpp:672, damping 0.99
  * b3GpuRigidBodyPipeline.cpp:468, gravity :92, friction 0.7 b3ConvexHullContact.cpp:1384). */
@@ -83,9 +99,7 @@ typedef struct b3gConfig {
     float residual_tol;        /* >0: stop PGS/Jacobi when the impulse residual drops below it */
     int update_world_inertia;  /* 0 = reference behaviour (world inverse inertia frozen at registration) */
     int use_cuda_graph;        /* capture the whole step as one CUDA graph */
-    int warm_start;            /* 0 = cold start (reference); 1 = learned warm start from the network attached with
-                                  b3g_set_warm_start_model (PGS; cold while none is attached); 2 = cold start that
-                                  records the network's features for training (b3g_read_warm_samples) */
+    int warm_start;            /* B3G_WARM_*: initial impulses of the PGS solve (0 = cold, the reference) */
     int barrier_spin_limit;    /* polls before a grid barrier gives up (0 = default, about a second) */
     int solver_blocks_per_sm;  /* persistent solver blocks per SM (0 = default; clamped to co-residency) */
     int pgs_partitions;        /* B3G_PGS_PARTITIONS_*: how the PGS solver splits work across blocks */
@@ -267,15 +281,15 @@ b3gStatus b3g_mlp_train(b3g_mlp m, int steps, int batch, float lr, int first_bat
 b3gStatus b3g_mlp_gradients(b3g_mlp m, const float* features, const float* targets, int n, float* grads,
                             double* loss);
 
-/* Attaches a warm-start network to a world (same device; not owned; NULL detaches).  With
- * warm_start = 1 every PGS solve predicts the initial impulses of its contact points, applies
- * them before the first sweep and iterates as usual; a prediction whose first-sweep residual is
- * above a cold start's (1) is dropped and the solve restarts cold (B3G_FLAG_WARM_DISCARDED). */
+/* Attaches a warm-start network to a world (same device; not owned; NULL detaches), used by
+ * B3G_WARM_LEARNED and B3G_WARM_PERSISTENT_LEARNED. */
 b3gStatus b3g_set_warm_start_model(b3g_handle h, b3g_mlp m);
-/* Training samples of the last solve (warm_start != 0): for every active contact point with
- * features, its 12 features and its 3 converged impulses (contact, second friction direction,
- * first friction direction).  *num = samples available; at most `capacity` are written. */
-b3gStatus b3g_read_warm_samples(b3g_handle h, float* features, float* targets, int capacity, int* num);
+/* Training samples of the last solve (warm_start LEARNED, RECORD or PERSISTENT_LEARNED): for every
+ * active contact point with features, its 12 features, its 3 converged impulses (contact, second
+ * friction direction, first friction direction) and (is_new, optional) whether it had no
+ * persisting predecessor.  *num = samples available; at most `capacity` are written. */
+b3gStatus b3g_read_warm_samples(b3g_handle h, float* features, float* targets, int* is_new, int capacity,
+                                int* num);
 /* The initial impulses of the last solve, 12 floats per manifold in the b3g_read_impulses layout
  * (per point: normal, lateral 1, lateral 2); zero for a cold start. */
 b3gStatus b3g_read_warm_start(b3g_handle h, float* host, int capacity_manifolds, int* num);

@@ -129,3 +129,52 @@ def test_graph_step_with_network():
         res.append(np_.readbackAllBodiesToCpu())
         assert pl.status() & ~capi.FLAG_WARM_DISCARDED == 0
     assert np.array_equal(res[0].view(np.uint8), res[1].view(np.uint8))
+
+
+def test_persistent_contacts_start_from_previous_impulses():
+    # a settled stack: after one cold step nearly every point persists; its initial impulses are
+    # the previous solve's converged impulses and the solve reaches the tolerance in fewer sweeps
+    sc = scenes.box_stack(6, 3, 6, seed=1)
+    np_, bp, pl, shapes = load(sc, solver_mode=capi.SOLVER_PGS, solver_iterations=1000, residual_tol=1e-4,
+                               warm_start=capi.WARM_PERSISTENT_LEARNED, pgs_interleave=True)
+    pl.stepSimulation(1 / 60)  # one full step (cold: nothing to persist from)
+    pl.synchronize()
+    it_cold = pl.stats().iterations
+    imp1 = pl.readImpulses()
+    _, _, new0 = pl.readWarmSamples(with_new=True)
+    assert new0.all()
+    b = np_.readbackAllBodiesToCpu()
+    I = np_.readInertiasToCpu()
+    run_stages(np_, bp, pl)  # the next step's stages from the integrated state
+    _, _, new1 = pl.readWarmSamples(with_new=True)
+    assert new1.mean() < 0.05
+    warm = pl.readWarmStart()
+    gc = np_.getContactsCPU()
+    assert len(warm) == len(imp1)
+    # persisting points of an unchanged manifold list carry the previous impulses
+    same = np.isclose(warm, imp1, rtol=0, atol=0).mean()
+    assert same > 0.9
+    st = pl.stats()
+    assert st.iterations < it_cold
+    # and the warm-started solve is the oracle's, bit for bit, over the same number of sweeps (the
+    # stopping test compares a float32-accumulated residual with the tolerance, so the sweep count
+    # is taken from the GPU)
+    order = pl.readSolveOrder()
+    ob, _, it, res, disc = O.solve_ordered_ex(b, I, gc, order, warm=warm, iterations=st.iterations,
+                                              interleave=True)
+    gb = np_.readbackAllBodiesToCpu()
+    assert np.array_equal(gb["linVel"], ob["linVel"]) and np.array_equal(gb["angVel"], ob["angVel"])
+    assert it == st.iterations and not disc and res <= 1.5e-4
+
+
+def test_trained_network_cuts_sweeps_on_held_out_piles():
+    # the committed network (trained on the GPU by bullet3_gb300.learned from the plain solver's
+    # converged impulses) against the cold start on piles it never saw, every solve run to 1e-4:
+    # fewer sweeps on average, no step falls back
+    from bullet3_gb300 import learned
+    from bullet3_gb300.warmstart import DEFAULT_WEIGHTS
+    r = learned.evaluate(DEFAULT_WEIGHTS, kind="piles", size=128, steps=60, first=20, cap=1000, seed=7,
+                         modes=("cold", "learned"))
+    assert r["cold"]["converged"] == 1.0 and r["learned"]["converged"] == 1.0
+    assert r["learned"]["dropped_steps"] == 0
+    assert r["learned"]["iterations"] < 0.97 * r["cold"]["iterations"], r
