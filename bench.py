@@ -6,7 +6,14 @@ resting on a static plane -- the settled form of the 64^3 lattice pile (x/z spac
 jitter +-0.05, seed 0) -- PGS solver, 10 iterations, dt 1/60, gravity -9.8.  One step =
 stepSimulation: AABBs, grid broadphase, narrowphase, colouring, PGS solve, integration.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload pile|batched]
+
+The line also carries `to_residual` (rank 0, one GPU, pile workload): the falling 64^3 lattice
+(spacing 1.1, jitter 0.05) stepped from rest with every PGS solve run to a 1e-4 contact residual,
+once per warm-start mode (plain = cold start, learned, persistent, persistent + learned), with
+the mean sweeps, solve ms and step ms per step of each.  --workload batched times 4,096
+independent scenes (counts log-uniform in [8, 256]) stepped together through per-scene offset
+tables instead of the pile.
 
 --impl reference times the reference's CPU algorithm for the same step (the composed CPU step:
 b3TransformAabb2, exact pair set, b3ContactConvexConvexSAT / computeContactPlaneConvex,
@@ -31,6 +38,12 @@ sys.path.insert(0, str(ROOT))
 METRIC = "body-steps/s at 256k bodies"
 WORKLOAD = ("box pile 64x64x64 = 262,144 unit boxes resting in 64x64 columns on a static plane "
             "(settled form of the spacing-1.1 jitter-0.05 lattice, seed 0), PGS 10 iterations, dt 1/60")
+WORKLOAD_BATCHED = ("{n} independent scenes (body counts log-uniform in [8, 256], seed 0; {bodies} bodies), each a "
+                    "jittered box/sphere pile (spacing 1.1, base 0.6, jitter 0.01) on its own plane, all at the "
+                    "origin, stepped together through per-scene offset tables, PGS 10 iterations, dt 1/60")
+RESIDUAL_WORKLOAD = ("box pile lattice 64x64x64 = 262,144 unit boxes (spacing 1.1, jitter 0.05, seed 0) falling onto "
+                     "a static plane from rest, steps 0..{last}, every PGS solve run to a {tol:g} contact residual "
+                     "(at most {cap} sweeps)")
 
 
 def solver_mode_code(args):
@@ -44,7 +57,7 @@ def solver_mode_code(args):
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=30)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--nx", type=int, default=64)
@@ -55,6 +68,13 @@ def parse():
     p.add_argument("--row-order", choices=["interleaved", "separate"], default="interleaved",
                    help="PGS row order: per contact point (reference B3_SOLVER_INTERLEAVE_CONTACT_AND_FRICTION_"
                         "CONSTRAINTS mode) or all contact rows then all friction rows (reference default)")
+    p.add_argument("--workload", choices=["pile", "batched"], default="pile",
+                   help="pile: the 262,144-box pile; batched: independent scenes stepped together")
+    p.add_argument("--scenes", type=int, default=4096, help="number of scenes of the batched workload")
+    p.add_argument("--residual-steps", type=int, default=60,
+                   help="steps of the falling 64^3 lattice solved to the residual, per warm-start mode (0 = skip)")
+    p.add_argument("--residual-cap", type=int, default=4000)
+    p.add_argument("--residual-tol", type=float, default=1e-4)
     return p.parse_args()
 
 
@@ -154,9 +174,17 @@ def solver_traffic():
     return None
 
 
-def make_scene(nx):
+def make_scene(args):
     from bullet3_gb300 import scenes
-    return scenes.box_stack(nx, 64, nx, seed=0)
+    if args.workload == "batched":
+        return scenes.batched_piles(args.scenes, seed=0, separate=True)
+    return scenes.box_stack(args.nx, 64, args.nx, seed=0)
+
+
+def workload_name(args, scene):
+    if args.workload == "batched":
+        return WORKLOAD_BATCHED.format(n=args.scenes, bodies=scene.num_bodies)
+    return WORKLOAD
 
 
 # ------------------------------------------------------------------------------ CPU arm
@@ -169,8 +197,28 @@ def cpu_run(scene, steps, iterations, mode):
     t = scenes.registered_tables(np_)
     shapes = O.Shapes.from_tables(t)
     threads = O.max_threads()
-    O.set_threads(threads)
     b, I = t["bodies"], t["inertias"]
+    first = getattr(scene, "scene_first", None)
+    if first is not None:
+        # independent scenes: the reference steps one pipeline per scene; the scenes are spread over
+        # the host threads, each stepped by the single-threaded oracle
+        from concurrent.futures import ThreadPoolExecutor
+        O.set_threads(1)
+        n = len(b)
+        ranges = [(int(a), int(first[k + 1]) if k + 1 < len(first) else n) for k, a in enumerate(first)]
+        parts = [(b[a:e].copy(), I[a:e].copy()) for a, e in ranges]
+
+        def one(k):
+            bb, II = parts[k]
+            for _ in range(steps):
+                bb, _, _, _ = O.step(bb, II, shapes, mode=mode, iterations=iterations, cell=1.7320508, use_grid=True)
+            return k
+
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(threads) as ex:
+            list(ex.map(one, range(len(parts))))
+        return time.perf_counter() - t0, threads, scene.num_bodies
+    O.set_threads(threads)
     t0 = time.perf_counter()
     for _ in range(steps):
         b, nc, npairs, npts = O.step(b, I, shapes, mode=mode, iterations=iterations, cell=1.7320508, use_grid=True)
@@ -181,7 +229,7 @@ def reference_arm(args):
     rank, world, local = dist_info()
     if rank != 0:
         return 0
-    scene = make_scene(args.nx)
+    scene = make_scene(args)
     mode = solver_mode_code(args)
     # warm-up steps are run (untimed) from the same initial state; each timed step is one full
     # composed CPU step of the whole 262,144-body scene
@@ -191,13 +239,66 @@ def reference_arm(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * secs / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "bodies": n, "solver": args.solver, "iterations": args.iterations,
-                       "row_order": args.row_order},
+            "config": {"workload": workload_name(args, scene), "bodies": n, "solver": args.solver,
+                       "iterations": args.iterations, "row_order": args.row_order},
             "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": threads, "kind": "port",
                              "sample": f"{args.steps} composed CPU steps of the full {n}-body scene"},
             "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+# ------------------------------------------------------------------------------ learned vs plain
+def to_residual(args, device):
+    """Sweeps and solve time per step when every solve runs to the residual target, per warm-start
+    mode, on the falling 64^3 lattice: plain (cold start, the reference's solver), learned (the
+    network predicts every point), persistent (points matched to the previous step's manifolds
+    start from their converged impulses) and persistent + learned (the network predicts the new
+    points).  Each mode steps the same initial state; a warm start whose first sweep is worse than
+    a cold start is dropped and counted in `fallback_steps`."""
+    import numpy as np
+
+    from bullet3_gb300 import capi, scenes
+    from bullet3_gb300.pipeline import b3Config
+    from bullet3_gb300.warmstart import DEFAULT_WEIGHTS, WarmStartMLP
+    net = WarmStartMLP.load(DEFAULT_WEIGHTS)
+    sc = scenes.box_pile(args.nx, 64, args.nx, jitter=0.05, seed=0)
+    modes = {"plain": capi.WARM_COLD, "learned": capi.WARM_LEARNED, "persistent": capi.WARM_PERSISTENT,
+             "persistent_learned": capi.WARM_PERSISTENT_LEARNED}
+    out = {}
+    for name, code in modes.items():
+        cfg = b3Config(solver_mode=capi.SOLVER_PGS, solver_iterations=args.residual_cap,
+                       residual_tol=args.residual_tol, pgs_interleave=True, warm_start=code, use_cuda_graph=True)
+        np_, bp, pl = scenes.load_scene(sc, cfg, device=device)
+        if code in (capi.WARM_LEARNED, capi.WARM_PERSISTENT_LEARNED):
+            pl.setWarmStartModel(net)
+        pl.setProfiling(True)
+        sweeps, solve_ms, step_ms, dropped, capped = [], [], [], 0, 0
+        for _ in range(args.residual_steps):
+            pl.stepSimulation(1.0 / 60.0)
+            pl.synchronize()
+            st = pl.stats()
+            t = pl.stageTimes()
+            sweeps.append(st.iterations)
+            solve_ms.append(float(t[4]))
+            step_ms.append(float(np.sum(t)))
+            dropped += bool(st.status & capi.FLAG_WARM_DISCARDED)
+            capped += st.iterations >= args.residual_cap
+            pl.status(clear=True)
+        pl.setProfiling(False)
+        out[name] = {"sweeps_per_step": float(np.mean(sweeps)), "solve_ms_per_step": float(np.mean(solve_ms)),
+                     "step_ms": float(np.mean(step_ms)), "steps_at_cap": int(capped), "fallback_steps": int(dropped),
+                     "manifolds_last_step": int(st.num_contacts)}
+        del np_, bp, pl
+    base = out["plain"]
+    for name in ("learned", "persistent", "persistent_learned"):
+        out[name]["sweeps_vs_plain"] = out[name]["sweeps_per_step"] / max(base["sweeps_per_step"], 1e-9)
+        out[name]["solve_ms_vs_plain"] = out[name]["solve_ms_per_step"] / max(base["solve_ms_per_step"], 1e-9)
+    return {"workload": RESIDUAL_WORKLOAD.format(last=args.residual_steps - 1, tol=args.residual_tol,
+                                                 cap=args.residual_cap),
+            "tol": args.residual_tol, "cap": args.residual_cap, "steps": args.residual_steps,
+            "residual": "||lambda_k - lambda_k-1||_2 / ||lambda_k||_2 over all contact and friction rows, per sweep",
+            "modes": out}
 
 
 # ------------------------------------------------------------------------------ GPU arm
@@ -215,7 +316,7 @@ def gpu_arm(args):
     from bullet3_gb300 import capi, scenes
     from bullet3_gb300.pipeline import b3Config
     capi.load()
-    scene = make_scene(args.nx)
+    scene = make_scene(args)
     mode = capi.SOLVER_PGS if args.solver == "pgs" else capi.SOLVER_JACOBI
     cfg = b3Config(solver_mode=mode, solver_iterations=args.iterations, use_cuda_graph=True,
                    pgs_interleave=args.solver == "pgs" and args.row_order == "interleaved")
@@ -226,12 +327,23 @@ def gpu_arm(args):
     for _ in range(max(3, args.warmup)):
         pl.stepSimulation(dt)
     pl.synchronize()
+    # the state after the warm-up steps is the timed workload (the e2e leg starts from it too)
+    state0 = np_.readbackAllBodiesToCpu()
     # ---- timed region: device events on the library's stream
     clocks = ClockSampler(local)
+    clocks.start()
+    # keep the GPU stepping while the clock sampler starts (its samples then cover load only),
+    # then put the warm-up state back
+    t_roll = time.perf_counter()
+    while time.perf_counter() - t_roll < 1.0:
+        for _ in range(10):
+            pl.stepSimulation(dt)
+        pl.synchronize()
+    np_.writeBodiesToGpu(state0)
+    pl.synchronize()
     dist_barrier(dist)
     pl.synchronize()
     pl.status(clear=True)  # the device status word accumulates over the timed steps
-    clocks.start()
     l0 = pl.launchCount()
     capi.call("b3g_record_event", h, C.c_int(0))
     for _ in range(args.steps):
@@ -288,7 +400,7 @@ def gpu_arm(args):
         pin_out = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
         host_in = pin_in.numpy().view(capi.BODY)
         host_out = pin_out.numpy().view(capi.BODY)
-        capi.call("b3g_read_bodies", h, capi.ptr(host_in), C.c_int(N))
+        host_in[:] = state0
         pl.synchronize()
         dist_barrier(dist)
         t0 = time.perf_counter()
@@ -307,20 +419,28 @@ def gpu_arm(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         secs, threads, n = cpu_run(scene, args.cpu_steps, args.iterations, solver_mode_code(args))
+        what = (f"every one of the {args.scenes} scenes" if args.workload == "batched" else "the same scene")
         cpu = {"value": n * args.cpu_steps / secs, "unit": "body-steps/s", "cores": threads, "kind": "port",
-               "sample": f"{args.cpu_steps} composed CPU oracle steps of the same {n}-body scene from its initial state"}
+               "sample": f"{args.cpu_steps} composed CPU oracle steps of {what} ({n} bodies) from its initial state"}
+
+    # ---- learned vs plain: sweeps and ms per step to the residual target (rank 0, one GPU)
+    residual = None
+    if rank == 0 and world == 1 and args.workload == "pile" and args.residual_steps > 0:
+        del np_, bp, pl
+        residual = to_residual(args, local)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world, "steps": args.steps,
                 "warmup": max(3, args.warmup), "ms_per_step": 1000 * t_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": WORKLOAD, "bodies": N, "solver": args.solver, "iterations": args.iterations,
+                "config": {"workload": workload_name(args, scene), "bodies": N, "solver": args.solver,
+                           "iterations": args.iterations,
                            "row_order": args.row_order,
                            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                            "l2": "inputs larger than L2 (constraint rows and pair buffers exceed 129 MB)",
                            "pairs": P_, "manifolds": C_, "contact_points": st.num_points, "colors": st.num_colors},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-                "clocks": clk, "stages": stages, "device_status": int(status)}
+                "clocks": clk, "stages": stages, "device_status": int(status), "to_residual": residual}
         print(json.dumps(line), flush=True)
     dist_barrier(dist)
     return 0

@@ -48,7 +48,7 @@ def _run(cmd):
 
 
 def build_library(force: bool = False, verbose: bool = False) -> Path:
-    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "b3g_capi.h"]
+    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h"))
     sources = [CSRC / s for s in CU_SOURCES + CPP_SOURCES]
     if not force and not _newer(LIB, sources + headers):
         return LIB

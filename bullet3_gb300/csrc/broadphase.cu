@@ -48,10 +48,28 @@ __device__ __forceinline__ uint32_t cell_hash(int x, int y, int z, int bits, int
     return ((uint32_t)(z & mask) << (2 * bits)) | ((uint32_t)(y & mask) << bits) | (uint32_t)(x & mask);
 }
 
+// Per-scene shift of the integer cell coordinates (batched independent scenes).  A constant shift
+// keeps a scene's neighbour cells neighbours after the wrap of cell_hash, so the 27-cell search
+// stays complete within the scene, while different scenes that occupy the same region of space
+// land in different cells of the hashed grid.  Cross-scene entries that still share a cell are
+// rejected by the scene test of the pair kernel.
+struct CellShift {
+    int x, y, z;
+};
+__device__ __forceinline__ CellShift scene_shift(int scene, int bits) {
+    uint32_t r = (uint32_t)scene * 0x9E3779B1u;
+    r ^= r >> 15;
+    r *= 0x85EBCA77u;
+    r ^= r >> 13;
+    const int mask = (1 << bits) - 1;
+    return CellShift{(int)(r & mask), (int)((r >> bits) & mask), (int)((r >> (2 * bits)) & mask)};
+}
+
 __global__ void __launch_bounds__(BP_THREADS) k_aabb_hash(const b3gBody* __restrict__ bodies,
                                                           const b3gCollidable* __restrict__ cols,
                                                           const b3gAabb* __restrict__ local_aabbs,
-                                                          const int* __restrict__ dyn_slot, int n,
+                                                          const int* __restrict__ dyn_slot,
+                                                          const int* __restrict__ body_scene, int n,
                                                           b3gAabb* __restrict__ aabbs, uint32_t* __restrict__ keys,
                                                           uint32_t* __restrict__ vals, float inv_cell, int bits) {
     const int mask = (1 << bits) - 1;
@@ -73,6 +91,10 @@ __global__ void __launch_bounds__(BP_THREADS) k_aabb_hash(const b3gBody* __restr
             float cx = (mn.x + mx.x) * 0.5f, cy = (mn.y + mx.y) * 0.5f, cz = (mn.z + mx.z) * 0.5f;
             int gx = cell_coord(cx, inv_cell, mask), gy = cell_coord(cy, inv_cell, mask),
                 gz = cell_coord(cz, inv_cell, mask);
+            if (body_scene) {
+                CellShift sh = scene_shift(body_scene[i], bits);
+                gx += sh.x; gy += sh.y; gz += sh.z;
+            }
             keys[slot] = cell_hash(gx, gy, gz, bits, mask);
             vals[slot] = (uint32_t)i;
         }
@@ -115,14 +137,17 @@ struct PairEmitter {
     }
 };
 
-__global__ void __launch_bounds__(BP_THREADS) k_find_pairs(const b3gAabb* __restrict__ aabbs,
-                                                           const uint32_t* __restrict__ keys,
-                                                           const uint32_t* __restrict__ vals,
-                                                           const uint32_t* __restrict__ cell_start, int n_dyn,
-                                                           const int* __restrict__ large_list, int n_large,
-                                                           float inv_cell, int bits, int body_bits,
-                                                           uint64_t* __restrict__ out, int* __restrict__ counter,
-                                                           int cap, unsigned int* __restrict__ status) {
+// SCENES: bodies carry a scene index (b3g_set_scene_offsets); cells are shifted per scene, pairs
+// need equal scenes and each body tests only its own scene's range of the large list.
+template <bool SCENES>
+__device__ __forceinline__ void find_pairs_body(const b3gAabb* __restrict__ aabbs, const uint32_t* __restrict__ keys,
+                                                const uint32_t* __restrict__ vals,
+                                                const uint32_t* __restrict__ cell_start, int n_dyn,
+                                                const int* __restrict__ large_list, int n_large,
+                                                const int* __restrict__ body_scene,
+                                                const int* __restrict__ large_off, float inv_cell, int bits,
+                                                int body_bits, uint64_t* __restrict__ out, int* __restrict__ counter,
+                                                int cap, unsigned int* __restrict__ status) {
     const int mask = (1 << bits) - 1;
     const int lane = threadIdx.x & 31;
     const float4* A = reinterpret_cast<const float4*>(aabbs);
@@ -140,6 +165,14 @@ __global__ void __launch_bounds__(BP_THREADS) k_find_pairs(const b3gAabb* __rest
             float4 amin = __ldg(&A[2 * i]), amax = __ldg(&A[2 * i + 1]);
             float cx = (amin.x + amax.x) * 0.5f, cy = (amin.y + amax.y) * 0.5f, cz = (amin.z + amax.z) * 0.5f;
             int gx = (int)floorf(cx * inv_cell), gy = (int)floorf(cy * inv_cell), gz = (int)floorf(cz * inv_cell);
+            int si = 0, l0 = 0, l1 = n_large;
+            if (SCENES) {
+                si = __ldg(&body_scene[i]);
+                CellShift sh = scene_shift(si, bits);
+                gx += sh.x; gy += sh.y; gz += sh.z;
+                l0 = __ldg(&large_off[si]);
+                l1 = __ldg(&large_off[si + 1]);
+            }
             for (int dz = -1; dz <= 1; dz++)
                 for (int dy = -1; dy <= 1; dy++)
                     for (int dx = -1; dx <= 1; dx++) {
@@ -152,12 +185,13 @@ __global__ void __launch_bounds__(BP_THREADS) k_find_pairs(const b3gAabb* __rest
                             if (__ldg(&keys[q]) != h) break;
                             uint32_t j = __ldg(&vals[q]);
                             if (j <= i) continue;
+                            if (SCENES && __ldg(&body_scene[j]) != si) continue;
                             float4 bmin = __ldg(&A[2 * j]), bmax = __ldg(&A[2 * j + 1]);
                             if (overlap(amin, amax, bmin, bmax))
                                 em.push(((uint64_t)i << body_bits) | j, out, counter, cap, status);
                         }
                     }
-            for (int l = 0; l < n_large; l++) {
+            for (int l = l0; l < l1; l++) {
                 uint32_t j = (uint32_t)__ldg(&large_list[l]);
                 float4 bmin = __ldg(&A[2 * j]), bmax = __ldg(&A[2 * j + 1]);
                 if (overlap(amin, amax, bmin, bmax)) {
@@ -185,6 +219,27 @@ __global__ void __launch_bounds__(BP_THREADS) k_find_pairs(const b3gAabb* __rest
         else
             atomicOr(status, B3G_FLAG_PAIR_OVERFLOW);
     }
+}
+
+__global__ void __launch_bounds__(BP_THREADS) k_find_pairs(const b3gAabb* __restrict__ aabbs,
+                                                           const uint32_t* __restrict__ keys,
+                                                           const uint32_t* __restrict__ vals,
+                                                           const uint32_t* __restrict__ cell_start, int n_dyn,
+                                                           const int* __restrict__ large_list, int n_large,
+                                                           float inv_cell, int bits, int body_bits,
+                                                           uint64_t* __restrict__ out, int* __restrict__ counter,
+                                                           int cap, unsigned int* __restrict__ status) {
+    find_pairs_body<false>(aabbs, keys, vals, cell_start, n_dyn, large_list, n_large, nullptr, nullptr, inv_cell, bits,
+                           body_bits, out, counter, cap, status);
+}
+
+__global__ void __launch_bounds__(BP_THREADS) k_find_pairs_scenes(
+    const b3gAabb* __restrict__ aabbs, const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
+    const uint32_t* __restrict__ cell_start, int n_dyn, const int* __restrict__ large_list, int n_large,
+    const int* __restrict__ body_scene, const int* __restrict__ large_off, float inv_cell, int bits, int body_bits,
+    uint64_t* __restrict__ out, int* __restrict__ counter, int cap, unsigned int* __restrict__ status) {
+    find_pairs_body<true>(aabbs, keys, vals, cell_start, n_dyn, large_list, n_large, body_scene, large_off, inv_cell,
+                          bits, body_bits, out, counter, cap, status);
 }
 
 __global__ void k_clamp_count(int* counter, int cap, int* clamped) {
@@ -247,7 +302,8 @@ __global__ void __launch_bounds__(BP_THREADS) k_unpack_pairs(const uint64_t* __r
 
 int launch_aabbs(DeviceState& d, cudaStream_t s) {
     int grid = d.num_sms * 4;
-    k_aabb_hash<<<grid, BP_THREADS, 0, s>>>(d.bodies, d.collidables, d.local_aabbs, d.dyn_slot, d.num_bodies, d.aabbs,
+    k_aabb_hash<<<grid, BP_THREADS, 0, s>>>(d.bodies, d.collidables, d.local_aabbs, d.dyn_slot,
+                                            d.num_scenes > 1 ? d.body_scene : nullptr, d.num_bodies, d.aabbs,
                                             d.cell_keys[0], d.cell_vals[0], d.inv_cell, d.grid_bits);
     return 1;
 }
@@ -270,10 +326,16 @@ int launch_pairs(DeviceState& d, cudaStream_t s) {
     cudaMemsetAsync(d.counters, 0, offsetof(DevCounters, status), s);
     cudaMemsetAsync(reinterpret_cast<char*>(d.counters) + offsetof(DevCounters, status) + sizeof(unsigned int), 0,
                     sizeof(DevCounters) - offsetof(DevCounters, status) - sizeof(unsigned int), s);
-    k_find_pairs<<<d.num_sms * 8, BP_THREADS, 0, s>>>(d.aabbs, keys, vals, d.cell_start, d.num_dynamic, d.large_list,
-                                                      d.num_large, d.inv_cell, d.grid_bits, d.body_bits,
-                                                      d.pair_keys[0], &d.counters->num_pairs, d.max_pairs,
-                                                      &d.counters->status);
+    if (d.num_scenes > 1)
+        k_find_pairs_scenes<<<d.num_sms * 8, BP_THREADS, 0, s>>>(
+            d.aabbs, keys, vals, d.cell_start, d.num_dynamic, d.large_list, d.num_large, d.body_scene, d.large_off,
+            d.inv_cell, d.grid_bits, d.body_bits, d.pair_keys[0], &d.counters->num_pairs, d.max_pairs,
+            &d.counters->status);
+    else
+        k_find_pairs<<<d.num_sms * 8, BP_THREADS, 0, s>>>(d.aabbs, keys, vals, d.cell_start, d.num_dynamic,
+                                                          d.large_list, d.num_large, d.inv_cell, d.grid_bits,
+                                                          d.body_bits, d.pair_keys[0], &d.counters->num_pairs,
+                                                          d.max_pairs, &d.counters->status);
     launches++;
     // clamp the count to capacity for the consumers (the raw count stays in num_pairs)
     int* d_np = &d.counters->pad[0];

@@ -71,6 +71,7 @@ struct b3gWorld {
     std::vector<b3gBody> bodies;
     std::vector<b3gInertia> inertias;
     std::vector<int> user_index;
+    std::vector<int> scene_first;  // first body of each independent scene (empty: one scene)
     bool uploaded = false;
     DeviceState d;
     std::vector<void*> allocations;
@@ -380,6 +381,24 @@ extern "C" b3gStatus b3g_register_body(b3g_handle h, float mass, const float pos
     return B3G_OK;
 }
 
+// ---------------------------------------------------------------------------------- batched scenes
+extern "C" b3gStatus b3g_set_scene_offsets(b3g_handle h, const int* first_body, int num_scenes) {
+    if (!h) return fail(B3G_ERR_INVALID_ARG, "null handle");
+    if (h->uploaded) return fail(B3G_ERR_INVALID_ARG, "set scene offsets before b3g_write_all_to_gpu");
+    if (num_scenes <= 1) {
+        h->scene_first.clear();
+        return B3G_OK;
+    }
+    if (!first_body) return fail(B3G_ERR_INVALID_ARG, "null scene offset table");
+    if (num_scenes > B3G_MAX_SCENES) return fail(B3G_ERR_CAPACITY, "%d scenes > %d", num_scenes, B3G_MAX_SCENES);
+    if (first_body[0] != 0) return fail(B3G_ERR_INVALID_ARG, "the first scene must start at body 0");
+    for (int s = 1; s < num_scenes; s++)
+        if (first_body[s] < first_body[s - 1])
+            return fail(B3G_ERR_INVALID_ARG, "scene offsets must be non-decreasing (scene %d)", s);
+    h->scene_first.assign(first_body, first_body + num_scenes);
+    return B3G_OK;
+}
+
 extern "C" b3gStatus b3g_set_gravity(b3g_handle h, const float g[3]) {
     if (!h || !g) return fail(B3G_ERR_INVALID_ARG, "null argument");
     h->cfg.gravity[0] = g[0];
@@ -439,6 +458,23 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     }
     d.num_dynamic = nd;
     d.num_large = (int)large.size();
+    // independent scenes: per-body scene index and, per scene, its range of the large list (bodies
+    // are registered scene by scene, so the large list is already grouped by scene)
+    std::vector<int> body_scene, large_off;
+    d.num_scenes = 1;
+    if (!h->scene_first.empty()) {
+        const int S = (int)h->scene_first.size();
+        if (h->scene_first.back() > N) return fail(B3G_ERR_INVALID_ARG, "scene offsets beyond the registered bodies");
+        d.num_scenes = S;
+        body_scene.assign(N, 0);
+        for (int sc = 0; sc < S; sc++) {
+            int e = sc + 1 < S ? h->scene_first[sc + 1] : N;
+            for (int i = h->scene_first[sc]; i < e; i++) body_scene[i] = sc;
+        }
+        large_off.assign(S + 1, 0);
+        for (int i : large) large_off[body_scene[i] + 1]++;
+        for (int sc = 0; sc < S; sc++) large_off[sc + 1] += large_off[sc];
+    }
     float cell = h->cfg.grid_cell_size > 0.f ? h->cfg.grid_cell_size : max_extent;
     // exactness of the 27-cell search needs cell >= every dynamic AABB extent
     if (cell < max_extent) cell = max_extent;
@@ -470,6 +506,10 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     TRY(dalloc(h, &d.dyn_slot, N));
     TRY(dalloc(h, &d.col_small, d.num_collidables));
     TRY(dalloc(h, &d.large_list, std::max(1, d.num_large)));
+    if (d.num_scenes > 1) {
+        TRY(dalloc(h, &d.body_scene, N));
+        TRY(dalloc(h, &d.large_off, d.num_scenes + 1));
+    }
     TRY(dalloc(h, &d.aabbs, N));
     for (int k = 0; k < 2; k++) {
         TRY(dalloc(h, &d.cell_keys[k], std::max(1, nd)));
@@ -588,6 +628,11 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
                              s));
     if (!large.empty())
         CUDA_TRY(cudaMemcpyAsync(d.large_list, large.data(), sizeof(int) * large.size(), cudaMemcpyHostToDevice, s));
+    if (d.num_scenes > 1) {
+        CUDA_TRY(cudaMemcpyAsync(d.body_scene, body_scene.data(), sizeof(int) * N, cudaMemcpyHostToDevice, s));
+        CUDA_TRY(cudaMemcpyAsync(d.large_off, large_off.data(), sizeof(int) * (d.num_scenes + 1),
+                                 cudaMemcpyHostToDevice, s));
+    }
     int sizes[4] = {nd, N, 0, 0};
     CUDA_TRY(cudaMemcpyAsync(d.d_num_dynamic, sizes, sizeof(sizes), cudaMemcpyHostToDevice, s));
     // an all-ones cell table is never a valid run start (validated against sorted keys)

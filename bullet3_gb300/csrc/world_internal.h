@@ -65,7 +65,11 @@ struct DeviceState {
     b3gFloat4* edges = nullptr;
     int* dyn_slot = nullptr;      // body -> dynamic slot or -1
     int* col_small = nullptr;     // per collidable: 1 = hull whose faces all have <= B3G_SMALL_FACE_VERTS vertices
-    int* large_list = nullptr;    // static bodies (large proxies)
+    int* large_list = nullptr;    // static bodies (large proxies), grouped by scene
+    // independent scenes (b3g_set_scene_offsets); nullptr / 1 when the world is one scene
+    int num_scenes = 1;
+    int* body_scene = nullptr;    // per body: its scene
+    int* large_off = nullptr;     // per scene: first entry in large_list (num_scenes + 1)
     // broadphase
     b3gAabb* aabbs = nullptr;
     uint32_t* cell_keys[2] = {nullptr, nullptr};

@@ -338,6 +338,13 @@ class b3GpuRigidBodyPipeline:
                 self.m_narrowphase.m_static0Index = 0
         return idx
 
+    def setSceneOffsets(self, firstBody):
+        """Independent scenes stepped together (no reference counterpart: the reference runs one
+        pipeline per scene).  Scene s owns bodies [firstBody[s], firstBody[s+1]), its static bodies
+        included; no pair is formed across scenes.  Call before writeAllInstancesToGpu."""
+        off = np.ascontiguousarray(np.asarray(firstBody, np.int32))
+        call("b3g_set_scene_offsets", self._h, iptr(off) if len(off) else None, C.c_int(len(off)))
+
     def writeAllInstancesToGpu(self):
         self.m_narrowphase.writeAllBodiesToGpu()
 

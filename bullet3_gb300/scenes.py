@@ -49,25 +49,35 @@ def random_quaternions(rng, n) -> np.ndarray:
 
 
 def batched_piles(n_scenes=4096, seed=0, min_bodies=8, max_bodies=256, spacing=1.1, base_y=0.6, jitter=0.01,
-                  half=0.5, sphere_fraction=0.5, pitch=None) -> Scene:
-    """Many independent piles on the plane y = 0, laid out on a square grid of scene cells far
-    enough apart that no two piles interact.  Body counts floor(exp(U(ln 8, ln 257))) clipped to
-    [8, 256] (mean ~72); each pile is a jittered lattice (spacing 1.1, base 0.6, jitter 0.01, zero
-    velocity, mass 1) of unit boxes and spheres of radius 0.5.  Returns the scene with
-    `scene_of` (per body: pile index, -1 for the plane) and `scene_offsets` (first body per pile)."""
+                  half=0.5, sphere_fraction=0.5, pitch=None, separate=False) -> Scene:
+    """Many independent piles.  Body counts floor(exp(U(ln 8, ln 257))) clipped to [8, 256] (mean
+    ~72); each pile is a jittered lattice (spacing 1.1, base 0.6, jitter 0.01, zero velocity, mass 1)
+    of unit boxes and spheres of radius 0.5.
+
+    separate=False: one shared plane y = 0, piles laid out on a square grid of scene cells far
+    enough apart that no two interact; `scene_of` (per body: pile index, -1 for the plane) and
+    `scene_offsets` (first body per pile).
+    separate=True: independent scenes all at the origin, each with its own plane as its first
+    body; `scene_first` (first body of each scene) is the offset table for setSceneOffsets and
+    `scene_of` gives every body's scene."""
     rng = np.random.Generator(np.random.PCG64(seed))
     counts = np.clip(np.floor(np.exp(rng.uniform(np.log(min_bodies), np.log(max_bodies + 1), n_scenes))),
                      min_bodies, max_bodies).astype(int)
     side = int(np.ceil(np.sqrt(n_scenes)))
     foot = int(np.ceil(np.sqrt(max_bodies / 4.0)))  # lattice columns per side at 4 layers
     pitch = pitch if pitch else foot * spacing + 4.0
-    sc = Scene(name=f"batched_piles_{n_scenes}")
+    sc = Scene(name=f"batched_{'scenes' if separate else 'piles'}_{n_scenes}")
     sc.shapes.append({"type": "plane", "normal": (0.0, 1.0, 0.0), "constant": 0.0})
     sc.shapes.append({"type": "hull", "verts": box_vertices(half, half, half)})
     sc.shapes.append({"type": "sphere", "radius": half})
-    shapes, pos, scene_of, offsets = [0], [np.zeros(3)], [-1], []
+    shapes, pos, scene_of, offsets, first = ([], [], [], [], []) if separate else ([0], [np.zeros(3)], [-1], [], [])
     for s, n in enumerate(counts):
-        cx, cz = (s % side) * pitch, (s // side) * pitch
+        cx, cz = (0.0, 0.0) if separate else ((s % side) * pitch, (s // side) * pitch)
+        if separate:
+            first.append(len(shapes))
+            shapes.append(0)
+            pos.append(np.zeros(3))
+            scene_of.append(s)
         cols = max(1, int(np.ceil(np.sqrt(n / 4.0))))
         layers = int(np.ceil(n / (cols * cols)))
         ii, kk, jj = np.meshgrid(np.arange(cols), np.arange(cols), np.arange(layers), indexing="ij")
@@ -82,12 +92,26 @@ def batched_piles(n_scenes=4096, seed=0, min_bodies=8, max_bodies=256, spacing=1
         pos.extend(list(p))
         scene_of.extend([s] * n)
     sc.body_shape = np.array(shapes, np.int32)
-    sc.mass = np.array([0.0] + [1.0] * (len(shapes) - 1), np.float32)
+    sc.mass = np.where(sc.body_shape == 0, 0.0, 1.0).astype(np.float32)
     sc.pos = np.array(pos, np.float32)
     sc.orn = np.tile(np.array([0, 0, 0, 1], np.float32), (len(shapes), 1))
     sc.scene_of = np.array(scene_of, np.int32)
     sc.scene_offsets = np.array(offsets, np.int32)
+    if separate:
+        sc.scene_first = np.array(first, np.int32)
     return sc
+
+
+def scene_part(sc: Scene, s: int) -> Scene:
+    """Scene `s` of a separate-scenes batch as a world of its own (same shapes, bodies in order)."""
+    first = sc.scene_first
+    a = int(first[s])
+    b = int(first[s + 1]) if s + 1 < len(first) else sc.num_bodies
+    out = Scene(shapes=sc.shapes, body_shape=sc.body_shape[a:b].copy(), mass=sc.mass[a:b].copy(),
+                pos=sc.pos[a:b].copy(), orn=sc.orn[a:b].copy(), cell=sc.cell, name=f"{sc.name}[{s}]")
+    if sc.linvel is not None:
+        out.linvel = sc.linvel[a:b].copy()
+    return out
 
 
 def box_pile(nx=10, ny=10, nz=10, spacing=1.1, base_y=0.6, jitter=0.01, half=0.5, mass=1.0, seed=0,
@@ -212,6 +236,8 @@ def load_scene(scene: Scene, config=None, device: int = 0, upload: bool = True):
         b = pl.registerPhysicsInstance(float(scene.mass[i]), scene.pos[i], scene.orn[i], col[scene.body_shape[i]], i)
         if b < 0:
             raise RuntimeError("body registration failed")
+    if getattr(scene, "scene_first", None) is not None:
+        pl.setSceneOffsets(scene.scene_first)
     if upload:
         pl.writeAllInstancesToGpu()
         if scene.linvel is not None or scene.angvel is not None:

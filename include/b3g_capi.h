@@ -170,6 +170,19 @@ b3gStatus b3g_set_gravity(b3g_handle h, const float g[3]);
 /* Changes the solver mode / iteration count / residual target between steps. */
 b3gStatus b3g_set_solver(b3g_handle h, int mode, int iterations, float residual_tol);
 
+/* Batched independent scenes.  The reference steps one world per pipeline; a batch of N scenes
+ * there is N pipelines stepped one after another (b3GpuRigidBodyPipeline::stepSimulation,
+ * b3GpuRigidBodyPipeline.cpp:221-463, once per scene).  Here one world holds every scene and one
+ * step advances them all: scene s owns the bodies [first_body[s], first_body[s+1]) (the last scene
+ * runs to the last registered body), including its own static bodies (planes), and no pair is
+ * formed across scenes, even where scenes occupy the same region of space.  Each scene's cells are
+ * shifted by a per-scene offset in the hashed grid, so overlapping scenes do not crowd the same
+ * cells; each body tests only its own scene's static bodies.  Call between registration and
+ * b3g_write_all_to_gpu; num_scenes <= 1 restores the single-scene world.  Offsets must start at 0
+ * and be non-decreasing (empty scenes are allowed). */
+#define B3G_MAX_SCENES (1 << 20)
+b3gStatus b3g_set_scene_offsets(b3g_handle h, const int* first_body, int num_scenes);
+
 /* ------------------------------------------------------------------ the step */
 /* b3GpuRigidBodyPipeline::stepSimulation (b3GpuRigidBodyPipeline.cpp:221-463): AABBs, pairs,
  * contacts, batching, solve, integrate -- enqueued on the world's stream (one CUDA graph

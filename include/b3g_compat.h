@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "b3g_capi.h"
+#include "b3g_types.h"
 
 namespace b3g_compat {
 
@@ -175,6 +176,15 @@ public:
         return out;
     }
     void writeAllInstancesToGpu() { m_np->writeAllBodiesToGpu(); }
+    /* independent scenes stepped together (no reference counterpart: the reference runs one
+       pipeline per scene); call before writeAllInstancesToGpu */
+    bool setSceneOffsets(const int* firstBody, int numScenes) {
+        if (b3g_set_scene_offsets(m_np->world(), firstBody, numScenes) != B3G_OK) {
+            b3Error("setSceneOffsets");
+            return false;
+        }
+        return true;
+    }
     void setGravity(const float* grav) { b3g_set_gravity(m_np->world(), grav); }
     void stepSimulation(float deltaTime) {
         if (b3g_step(m_np->world(), deltaTime) != B3G_OK) b3Error("stepSimulation");

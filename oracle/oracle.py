@@ -123,6 +123,26 @@ def pairs_bruteforce(aabbs_, cap=None):
     return out[:min(n, cap)].copy()
 
 
+def pairs_scenes(aabbs_, scene_first):
+    """Pair set of independent scenes: the reference runs one broadphase per scene (one
+    b3GpuGridBroadphase per b3GpuRigidBodyPipeline, b3GpuGridBroadphase.cpp:117-259, whose exact
+    set is calculateOverlappingPairsHost :260-294); here each scene's bodies are paired by the brute
+    force test on their own and the indices shifted back by the scene's first body, concatenated
+    in (a, b) order."""
+    n = len(aabbs_)
+    first = [int(x) for x in scene_first]
+    out = []
+    for s, a in enumerate(first):
+        b = first[s + 1] if s + 1 < len(first) else n
+        if b - a < 2:
+            continue
+        p = pairs_bruteforce(aabbs_[a:b])
+        p["x"] += a
+        p["y"] += a
+        out.append(p)
+    return np.concatenate(out) if out else np.zeros(0, PAIR)
+
+
 def pairs_grid(aabbs_, cell, cap=None):
     a = np.ascontiguousarray(aabbs_, AABB)
     cap = cap or max(1024, 64 * len(a))

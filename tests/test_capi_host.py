@@ -127,3 +127,40 @@ def test_hull_builder_against_reference_hulls():
     for i in range(6):
         mine = capi.hull_compute(g[f"in_{i}"])
         assert len(mine[2]) == 6 and (mine[2] == 4).all() and len(mine[4]) == 3
+
+
+def test_scene_offsets_validation():
+    np_ = b3GpuNarrowPhase(b3Config())
+    pl = b3GpuRigidBodyPipeline(np_)
+    plane = np_.registerPlaneShape((0, 1, 0), 0.0)
+    box = np_.registerConvexHullShape(scenes.box_vertices(0.5, 0.5, 0.5))
+    for k in range(6):
+        pl.registerPhysicsInstance(0.0 if k % 3 == 0 else 1.0, (0, 1 + k, 0), (0, 0, 0, 1), plane if k % 3 == 0 else box)
+    for bad in ([1, 3], [0, 4, 2]):  # must start at body 0 and never decrease
+        with pytest.raises(capi.B3GError) as e:
+            pl.setSceneOffsets(bad)
+        assert e.value.status == 1
+    pl.setSceneOffsets([0, 3, 3])  # an empty scene is allowed
+    pl.setSceneOffsets([0, 3])
+    pl.setSceneOffsets([])  # back to one scene
+
+
+def test_cpp_dropin_header_compiles(tmp_path):
+    # the C++ classes of include/b3g_compat.h compile on their own against the public headers
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    src = tmp_path / "use.cpp"
+    src.write_text('#include "b3g_compat.h"\n'
+                   "using namespace b3g_compat;\n"
+                   "int main() {\n"
+                   "  b3Config c; b3GpuNarrowPhase np(0, c); b3GpuGridBroadphase bp;\n"
+                   "  b3GpuRigidBodyPipeline rbp(&np, &bp, nullptr, c);\n"
+                   "  int first[2] = {0, 1}; rbp.setSceneOffsets(first, 2);\n"
+                   "  rbp.stepSimulation(1.f / 60.f); return rbp.getNumBodies();\n"
+                   "}\n")
+    r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-Wall", "-I", str(Path(ROOT, "include")), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
