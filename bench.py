@@ -75,6 +75,7 @@ def parse():
                    help="steps of the falling 64^3 lattice solved to the residual, per warm-start mode (0 = skip)")
     p.add_argument("--residual-cap", type=int, default=4000)
     p.add_argument("--residual-tol", type=float, default=1e-4)
+    p.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     return p.parse_args()
 
 
@@ -327,6 +328,8 @@ def gpu_arm(args):
     for _ in range(max(3, args.warmup)):
         pl.stepSimulation(dt)
     pl.synchronize()
+    # launch shapes chosen by the autotuner on this state (it leaves the state unchanged)
+    tuning = pl.autotune(dt, repeats=3) if not args.no_autotune else None
     # the state after the warm-up steps is the timed workload (the e2e leg starts from it too)
     state0 = np_.readbackAllBodiesToCpu()
     # ---- timed region: device events on the library's stream
@@ -438,7 +441,8 @@ def gpu_arm(args):
                            "row_order": args.row_order,
                            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                            "l2": "inputs larger than L2 (constraint rows and pair buffers exceed 129 MB)",
-                           "pairs": P_, "manifolds": C_, "contact_points": st.num_points, "colors": st.num_colors},
+                           "pairs": P_, "manifolds": C_, "contact_points": st.num_points, "colors": st.num_colors,
+                           "tuning": tuning},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
                 "clocks": clk, "stages": stages, "device_status": int(status), "to_residual": residual}
         print(json.dumps(line), flush=True)

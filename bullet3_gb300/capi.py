@@ -55,7 +55,13 @@ class b3gConfig(C.Structure):
                 ("contact_friction", C.c_float), ("residual_tol", C.c_float), ("update_world_inertia", C.c_int),
                 ("use_cuda_graph", C.c_int), ("warm_start", C.c_int), ("barrier_spin_limit", C.c_int),
                 ("solver_blocks_per_sm", C.c_int), ("pgs_partitions", C.c_int), ("pgs_interleave", C.c_int),
-                ("warm_start_max_points", C.c_int), ("reserved", C.c_int * 3)]
+                ("warm_start_max_points", C.c_int), ("autotune", C.c_int), ("reserved", C.c_int * 2)]
+
+
+class b3gTuning(C.Structure):
+    _fields_ = [("pgs_partitions", C.c_int), ("pairs_blocks_per_sm", C.c_int), ("narrow_blocks_per_sm", C.c_int),
+                ("sort_blocks_per_sm", C.c_int), ("pairs_ms", C.c_float), ("contacts_ms", C.c_float),
+                ("solve_ms", C.c_float), ("candidates_timed", C.c_int)]
 
 
 class b3gStepStats(C.Structure):
@@ -76,7 +82,7 @@ _LIB = None
 EXPORTS = [
     "b3g_config_default", "b3g_create", "b3g_destroy", "b3g_last_error", "b3g_version", "b3g_register_sphere",
     "b3g_register_plane", "b3g_register_hull", "b3g_register_hull_tables", "b3g_register_body",
-    "b3g_write_all_to_gpu", "b3g_set_gravity", "b3g_set_solver", "b3g_set_scene_offsets", "b3g_step", "b3g_setup_aabbs",
+    "b3g_write_all_to_gpu", "b3g_set_gravity", "b3g_set_solver", "b3g_set_scene_offsets", "b3g_autotune", "b3g_get_tuning", "b3g_step", "b3g_setup_aabbs",
     "b3g_calculate_overlapping_pairs", "b3g_compute_contacts", "b3g_solve_contacts", "b3g_integrate",
     "b3g_synchronize", "b3g_get_stats", "b3g_status", "b3g_get_num_bodies", "b3g_get_body_buffer",
     "b3g_get_inertia_buffer", "b3g_get_aabb_buffer", "b3g_get_pair_buffer", "b3g_get_contact_buffer",

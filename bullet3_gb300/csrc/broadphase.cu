@@ -312,6 +312,7 @@ int launch_pairs(DeviceState& d, cudaStream_t s) {
     int launches = 0;
     long long ll = 0;
     // 1. sort (cell hash, body) -- keys written by launch_aabbs
+    d.prim.sort_blocks = d.num_sms * d.tune.sort_blocks_per_sm;
     int which = radix_sort_u32(d.prim, d.cell_keys[0], d.cell_keys[1], d.cell_vals[0], d.cell_vals[1],
                                d.d_num_dynamic, 3 * d.grid_bits, d.sort_scratch, s, &ll);
     uint32_t* keys = d.cell_keys[which];
@@ -326,13 +327,14 @@ int launch_pairs(DeviceState& d, cudaStream_t s) {
     cudaMemsetAsync(d.counters, 0, offsetof(DevCounters, status), s);
     cudaMemsetAsync(reinterpret_cast<char*>(d.counters) + offsetof(DevCounters, status) + sizeof(unsigned int), 0,
                     sizeof(DevCounters) - offsetof(DevCounters, status) - sizeof(unsigned int), s);
+    const int pgrid = d.num_sms * d.tune.pairs_blocks_per_sm;
     if (d.num_scenes > 1)
-        k_find_pairs_scenes<<<d.num_sms * 8, BP_THREADS, 0, s>>>(
+        k_find_pairs_scenes<<<pgrid, BP_THREADS, 0, s>>>(
             d.aabbs, keys, vals, d.cell_start, d.num_dynamic, d.large_list, d.num_large, d.body_scene, d.large_off,
             d.inv_cell, d.grid_bits, d.body_bits, d.pair_keys[0], &d.counters->num_pairs, d.max_pairs,
             &d.counters->status);
     else
-        k_find_pairs<<<d.num_sms * 8, BP_THREADS, 0, s>>>(d.aabbs, keys, vals, d.cell_start, d.num_dynamic,
+        k_find_pairs<<<pgrid, BP_THREADS, 0, s>>>(d.aabbs, keys, vals, d.cell_start, d.num_dynamic,
                                                           d.large_list, d.num_large, d.inv_cell, d.grid_bits,
                                                           d.body_bits, d.pair_keys[0], &d.counters->num_pairs,
                                                           d.max_pairs, &d.counters->status);

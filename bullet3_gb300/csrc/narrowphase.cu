@@ -743,7 +743,7 @@ int launch_contacts(DeviceState& d, float friction, cudaStream_t s) {
     int grid = d.num_sms * 4;
     for (int t = PT_PLANE_HULL; t <= PT_PLANE_SPHERE; t++)
         k_primitive_pairs<<<grid, NP_THREADS, 0, s>>>(a, t, d.max_pairs);
-    k_hull_hull_small<<<d.num_sms * 8, NP_THREADS, 0, s>>>(a, d.max_pairs);
+    k_hull_hull_small<<<d.num_sms * d.tune.narrow_blocks_per_sm, NP_THREADS, 0, s>>>(a, d.max_pairs);
     k_hull_hull<<<d.num_sms * 16, HH_WARPS * 32, 0, s>>>(a, d.max_pairs);
     long long ll = 0;
     int* d_np = &d.counters->pad[0];

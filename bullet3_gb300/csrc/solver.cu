@@ -501,6 +501,24 @@ __device__ __forceinline__ void block_accumulate(double* dst, float x, float y) 
     __syncthreads();
 }
 
+// Warp-aggregated counters: lanes with the same key (key < 0: none) add their number with one
+// atomic.  All 32 lanes must call.
+__device__ __forceinline__ void warp_count(int* counts, int key) {
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    if (key >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&counts[key], __popc(peers));
+}
+// Warp-aggregated reservation: returns this lane's slot in the run reserved for its key.  All 32
+// lanes must call.  Within a key, slots follow lane order.
+__device__ __forceinline__ int warp_reserve(int* cursors, int key) {
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (key >= 0 && lane == leader) base = atomicAdd(&cursors[key], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + __popc(peers & ((1u << lane) - 1u));
+}
+
 __device__ __forceinline__ unsigned int hash32(unsigned int x) {
     x ^= x >> 16;
     x *= 0x7feb352dU;
@@ -720,8 +738,14 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
         }
         if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
         int left = 0;
-        for (int m = tid; m < nc; m += stride) {
-            if (a.color[m] >= 0) continue;
+        // every lane runs the same trip count so the per-colour counts aggregate across the warp
+        for (int m0 = tid - (threadIdx.x & 31); m0 < nc; m0 += stride) {
+            const int m = m0 + (threadIdx.x & 31);
+            int fill_key = -1;
+            if (m >= nc || a.color[m] >= 0) {
+                warp_count(a.color_fill, fill_key);
+                continue;
+            }
             const int4 h = a.hdr[m];
             const float2 im = a.inv_mass[m];
             const bool cross = a.manifold_group[m] < 0;
@@ -737,7 +761,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
                 int c = __ffsll((long long)~used) - 1;
                 if (c >= 0 && c < 64) {
                     a.color[m] = c;
-                    atomicAdd(&a.color_fill[c + (cross ? 64 : 0)], 1);
+                    fill_key = c + (cross ? 64 : 0);
                     if (im.x != 0.f) atomicOr(&mask[h.x], 1ull << c);
                     if (im.y != 0.f) atomicOr(&mask[h.y], 1ull << c);
                 } else {
@@ -746,6 +770,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
             } else {
                 left++;
             }
+            warp_count(a.color_fill, fill_key);
         }
         for (int o = 16; o; o >>= 1) left += __shfl_xor_sync(0xffffffffu, left, o);
         if ((threadIdx.x & 31) == 0 && left) atomicAdd(&a.remaining[r], left);
@@ -773,17 +798,19 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
     // ---- processing group of every manifold: owner * NC + colour (block-local) or
     // G * NC + colour (cross-partition).  Reported colours: block-local c, cross ncl + c, so the
     // batches stay legal as one colouring.
-    for (int m = tid; m < nc; m += stride) {
-        const int c = a.color[m];
-        if (c < 0) {
-            a.manifold_group[m] = -1;
-            continue;
+    for (int m0 = tid - (threadIdx.x & 31); m0 < nc; m0 += stride) {
+        const int m = m0 + (threadIdx.x & 31);
+        int key = -1;
+        if (m < nc) {
+            const int c = a.color[m];
+            if (c >= 0) {
+                const int owner = a.manifold_group[m];
+                key = owner >= 0 ? owner * NC + c : G * NC + c;
+                if (owner < 0) a.color[m] = ncl + c;
+            }
+            a.manifold_group[m] = key;
         }
-        const int owner = a.manifold_group[m];
-        const int key = owner >= 0 ? owner * NC + c : G * NC + c;
-        if (owner < 0) a.color[m] = ncl + c;
-        a.manifold_group[m] = key;
-        atomicAdd(&gcount[key], 1);
+        warp_count(gcount, key);
     }
     if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
     if (blockIdx.x == 0) {
@@ -795,9 +822,11 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
         }
     }
     if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
-    for (int m = tid; m < nc; m += stride) {
-        const int key = a.manifold_group[m];
-        if (key >= 0) a.color_order[__ldcg(&goff[key]) + atomicAdd(&gcur[key], 1)] = m;
+    for (int m0 = tid - (threadIdx.x & 31); m0 < nc; m0 += stride) {
+        const int m = m0 + (threadIdx.x & 31);
+        const int key = m < nc ? a.manifold_group[m] : -1;
+        const int pos = warp_reserve(gcur, key);
+        if (key >= 0) a.color_order[__ldcg(&goff[key]) + pos] = m;
     }
     const int ncol = __ldcg(&goff[ngroups]);  // coloured manifolds; the rest are overflow leftovers
     if (overflow && tid == 0) {
@@ -808,10 +837,44 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
     if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
     // ---- group-ordered copy of the records (coalesced phases, no order -> header indirection);
     // block-local manifolds carry their bodies' shared-memory slots in hdr.w (0xffff = not owned)
+    // One thread per point slot: the four slots of a record are read and written as one
+    // contiguous 64-byte run per array (slots of inactive points are copied too; never used).
+    // Four slots per thread are in flight at once (all loads issued before the stores).
     const int nlocal = __ldcg(&goff[G * NC]);
+    for (int t0 = tid; t0 < 4 * nc; t0 += 4 * stride) {
+        float4 r1[4], r2[4], d2[4], d1[4], im[4];
+        float2 rf[4];
+        size_t dst[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int t = t0 + u * stride;
+            dst[u] = ~(size_t)0;
+            if (t >= 4 * nc) continue;
+            const int k = t >> 2, j = t & 3;
+            const size_t s = (size_t)__ldcg(&a.color_order[k]) * 4 + j;
+            dst[u] = (size_t)k * 4 + j;
+            r1[u] = __ldcg(&a.sp.rel1[s]);
+            r2[u] = __ldcg(&a.sp.rel2[s]);
+            d2[u] = __ldcg(&a.sp.dir2[s]);
+            d1[u] = __ldcg(&a.sp.dir1[s]);
+            rf[u] = __ldcg(&a.sp.rhsf[s]);
+            im[u] = __ldcg(&a.sp.imp[s]);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            if (dst[u] == ~(size_t)0) continue;
+            const size_t d = dst[u];
+            a.sp_ord.rel1[d] = r1[u];
+            a.sp_ord.rel2[d] = r2[u];
+            a.sp_ord.dir2[d] = d2[u];
+            a.sp_ord.dir1[d] = d1[u];
+            a.sp_ord.rhsf[d] = rf[u];
+            a.sp_ord.imp[d] = im[u];
+        }
+    }
     for (int k = tid; k < nc; k += stride) {
         const int m = __ldcg(&a.color_order[k]);
-        int4 h = a.hdr[m];
+        const int4 h = a.hdr[m];
         const float2 im = a.inv_mass[m];
         int w = 0xffffffff;
         if (k < nlocal) {
@@ -823,16 +886,6 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
         a.hdr_ord[k] = make_int4(h.x, h.y, h.z, w);
         a.inv_mass_ord[k] = make_float4(im.x, im.y, 0.f, 0.f);
         a.sp_ord.nf[k] = __ldcg(&a.sp.nf[m]);
-        for (int j = 0; j < 4; j++) {
-            if (!(h.z & (1 << j))) continue;
-            const size_t s = (size_t)m * 4 + j, t = (size_t)k * 4 + j;
-            a.sp_ord.rel1[t] = __ldcg(&a.sp.rel1[s]);
-            a.sp_ord.rel2[t] = __ldcg(&a.sp.rel2[s]);
-            a.sp_ord.dir2[t] = __ldcg(&a.sp.dir2[s]);
-            a.sp_ord.dir1[t] = __ldcg(&a.sp.dir1[s]);
-            a.sp_ord.rhsf[t] = __ldcg(&a.sp.rhsf[s]);
-            a.sp_ord.imp[t] = __ldcg(&a.sp.imp[s]);
-        }
     }
     if (a.tile_R > 0) fence_proxy_async();  // the ordered records are read by bulk copies below
     if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
@@ -1428,10 +1481,10 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     if (jac) {
         sgrid = solver_grid(d, (const void*)k_solve_jacobi, bps, 0);
     } else {
-        // AUTO: the split measured fastest on GB300 for 256k-box piles -- block partitions with
-        // shared-memory deltas for interleaved rows, grid-wide colours otherwise
+        // AUTO: the autotuner's choice (b3g_autotune), else the split measured fastest on GB300 for
+        // 256k-box piles -- grid-wide colours
         const int mode = cfg.pgs_partitions != B3G_PGS_PARTITIONS_AUTO ? cfg.pgs_partitions
-                         : cfg.pgs_interleave                          ? B3G_PGS_PARTITIONS_SHARED
+                         : d.tune.pgs_partitions > 0                   ? d.tune.pgs_partitions
                                                                        : B3G_PGS_PARTITIONS_NONE;
         const bool parts = mode != B3G_PGS_PARTITIONS_NONE;
         const int nd = parts && d.cell_sorted_bodies ? d.num_dynamic : 0;

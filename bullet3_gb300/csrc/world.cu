@@ -89,6 +89,8 @@ struct b3gWorld {
     b3gStepStats last_stats{};
     cudaEvent_t user_events[16] = {};
     b3g_mlp ws_mlp = nullptr;  // attached warm-start network (not owned)
+    bool tuned = false;        // b3g_autotune ran on the current upload
+    b3gTuning tuning{};        // its last result
 };
 
 static void free_device(b3gWorld* w) {
@@ -431,6 +433,8 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     if (!h->stream) CUDA_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     cudaStreamSynchronize(h->stream);
     free_device(h);
+    h->tuned = false;
+    h->tuning = b3gTuning{};
     DeviceState& d = h->d;
     const int N = (int)h->bodies.size();
     if (N < 1) return fail(B3G_ERR_INVALID_ARG, "no bodies registered");
@@ -488,7 +492,7 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     // at most one manifold per pair: contact storage is sized with the pair capacity so that no
     // manifold index can exceed it
     d.max_contacts = d.max_pairs;
-    d.prim.sort_blocks = sms * 4;
+    d.prim.sort_blocks = sms * d.tune.sort_blocks_per_sm;
     d.prim.scan_blocks = sms * 2;
 
     const size_t nh = std::max<size_t>(1, h->hulls.size()), nf = std::max<size_t>(1, h->faces.size()),
@@ -587,7 +591,9 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     TRY(dalloc(h, &d.barrier, 64));
     {
         unsigned char* p = nullptr;
-        TRY(dalloc(h, &p, radix_scratch_bytes(d.prim)));
+        PrimConfig widest = d.prim;  // the autotuner may raise the sort's block count up to this
+        widest.sort_blocks = sms * B3G_MAX_SORT_BLOCKS_PER_SM;
+        TRY(dalloc(h, &p, radix_scratch_bytes(widest)));
         d.sort_scratch = p;
         TRY(dalloc(h, &p, scan_scratch_bytes(d.prim)));
         d.scan_scratch = p;
@@ -689,6 +695,7 @@ extern "C" b3gStatus b3g_step(b3g_handle h, float dt) {
     REQUIRE_UPLOADED(h);
     if (!(dt > 0.f)) return fail(B3G_ERR_INVALID_ARG, "dt must be positive");
     CUDA_TRY(cudaSetDevice(h->device));
+    if (h->cfg.autotune && !h->tuned) TRY(b3g_autotune(h, dt, 3, nullptr));
     if (h->profiling || !h->cfg.use_cuda_graph) {
         enqueue_step(h, dt, h->profiling);
         TRY(check_launch(h));
@@ -723,6 +730,157 @@ extern "C" b3gStatus b3g_step(b3g_handle h, float dt) {
     }
     CUDA_TRY(cudaGraphLaunch(h->graph_exec, h->stream));
     h->launches += h->graph_kernels;
+    return B3G_OK;
+}
+
+// ---------------------------------------------------------------------------------- autotuner
+// Times candidate launch shapes on the world's current state and keeps the fastest of each.
+// Every candidate sees the same input: the bodies are saved first and put back before each timed
+// run (and at the end), so tuning leaves the simulation state as it found it.
+namespace {
+
+struct TuneRun {
+    float ms[4];  // aabbs, pairs, contacts, solve
+};
+
+b3gStatus tune_time(b3gWorld* h, float dt, int repeats, const b3gBody* saved, bool solve, TuneRun& out) {
+    DeviceState& d = h->d;
+    cudaStream_t s = h->stream;
+    cudaEvent_t ev[5];
+    for (int k = 0; k < 5; k++) CUDA_TRY(cudaEventCreate(&ev[k]));
+    std::vector<float> t[4];
+    for (int r = 0; r < repeats + 1; r++) {  // the first run warms caches and is not kept
+        CUDA_TRY(cudaMemcpyAsync(d.bodies, saved, sizeof(b3gBody) * d.num_bodies, cudaMemcpyDeviceToDevice, s));
+        cudaEventRecord(ev[0], s);
+        launch_aabbs(d, s);
+        cudaEventRecord(ev[1], s);
+        launch_pairs(d, s);
+        cudaEventRecord(ev[2], s);
+        launch_contacts(d, h->cfg.contact_friction, s);
+        cudaEventRecord(ev[3], s);
+        if (solve) launch_solver(d, h->cfg, dt, s);
+        cudaEventRecord(ev[4], s);
+        CUDA_TRY(cudaStreamSynchronize(s));
+        TRY(check_launch(h));
+        if (r == 0) continue;
+        for (int k = 0; k < 4; k++) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+            t[k].push_back(ms);
+        }
+    }
+    for (int k = 0; k < 5; k++) cudaEventDestroy(ev[k]);
+    for (int k = 0; k < 4; k++) {  // median
+        std::sort(t[k].begin(), t[k].end());
+        out.ms[k] = t[k][t[k].size() / 2];
+    }
+    return B3G_OK;
+}
+
+}  // namespace
+
+extern "C" b3gStatus b3g_autotune(b3g_handle h, float dt, int repeats, b3gTuning* out) {
+    REQUIRE_UPLOADED(h);
+    if (!(dt > 0.f)) return fail(B3G_ERR_INVALID_ARG, "dt must be positive");
+    if (repeats < 1 || repeats > 100) return fail(B3G_ERR_INVALID_ARG, "repeats must be in [1, 100]");
+    CUDA_TRY(cudaSetDevice(h->device));
+    DeviceState& d = h->d;
+    cudaStream_t s = h->stream;
+    b3gBody* saved = nullptr;
+    CUDA_TRY(cudaMalloc(&saved, sizeof(b3gBody) * d.num_bodies));
+    b3gStatus st = B3G_OK;
+    b3gTuning res{};
+    int timed = 0;
+    do {
+        if (cudaMemcpyAsync(saved, d.bodies, sizeof(b3gBody) * d.num_bodies, cudaMemcpyDeviceToDevice, s) !=
+            cudaSuccess) {
+            st = fail(B3G_ERR_CUDA, "autotune: saving the bodies failed");
+            break;
+        }
+        TuneRun run;
+        // radix sort blocks, then the pair kernel's grid: both time the pair stage
+        static const int sort_c[] = {2, 4, 8};
+        float best = 1e30f;
+        int best_v = d.tune.sort_blocks_per_sm;
+        for (int v : sort_c) {
+            d.tune.sort_blocks_per_sm = v;
+            if ((st = tune_time(h, dt, repeats, saved, false, run)) != B3G_OK) break;
+            timed++;
+            if (run.ms[1] < best) { best = run.ms[1]; best_v = v; }
+        }
+        if (st != B3G_OK) break;
+        d.tune.sort_blocks_per_sm = best_v;
+        static const int grid_c[] = {2, 4, 8, 16};
+        best = 1e30f;
+        best_v = d.tune.pairs_blocks_per_sm;
+        for (int v : grid_c) {
+            d.tune.pairs_blocks_per_sm = v;
+            if ((st = tune_time(h, dt, repeats, saved, false, run)) != B3G_OK) break;
+            timed++;
+            if (run.ms[1] < best) { best = run.ms[1]; best_v = v; }
+        }
+        if (st != B3G_OK) break;
+        d.tune.pairs_blocks_per_sm = best_v;
+        res.pairs_ms = best;
+        // the thread-per-pair narrowphase kernel's grid: times the contact stage
+        best = 1e30f;
+        best_v = d.tune.narrow_blocks_per_sm;
+        for (int v : grid_c) {
+            d.tune.narrow_blocks_per_sm = v;
+            if ((st = tune_time(h, dt, repeats, saved, false, run)) != B3G_OK) break;
+            timed++;
+            if (run.ms[2] < best) { best = run.ms[2]; best_v = v; }
+        }
+        if (st != B3G_OK) break;
+        d.tune.narrow_blocks_per_sm = best_v;
+        res.contacts_ms = best;
+        // the PGS solver's work split (only when the configuration leaves it to AUTO)
+        if (h->cfg.solver_mode == B3G_SOLVER_PGS && h->cfg.pgs_partitions == B3G_PGS_PARTITIONS_AUTO) {
+            static const int split_c[] = {B3G_PGS_PARTITIONS_NONE, B3G_PGS_PARTITIONS_SHARED,
+                                          B3G_PGS_PARTITIONS_GLOBAL_DELTAS, B3G_PGS_PARTITIONS_STREAMED};
+            best = 1e30f;
+            best_v = B3G_PGS_PARTITIONS_NONE;
+            for (int v : split_c) {
+                d.tune.pgs_partitions = v;
+                if ((st = tune_time(h, dt, repeats, saved, true, run)) != B3G_OK) break;
+                timed++;
+                if (run.ms[3] < best) { best = run.ms[3]; best_v = v; }
+            }
+            if (st != B3G_OK) break;
+            d.tune.pgs_partitions = best_v;
+        } else {
+            if ((st = tune_time(h, dt, repeats, saved, true, run)) != B3G_OK) break;
+            timed++;
+            best = run.ms[3];
+        }
+        res.solve_ms = best;
+    } while (false);
+    // the state is put back whatever happened
+    cudaMemcpyAsync(d.bodies, saved, sizeof(b3gBody) * d.num_bodies, cudaMemcpyDeviceToDevice, s);
+    cudaStreamSynchronize(s);
+    cudaFree(saved);
+    h->graph_dt = -1.f;  // the captured step used the old launch shapes
+    h->tuned = true;
+    if (st != B3G_OK) return st;
+    res.pgs_partitions = d.tune.pgs_partitions;
+    res.pairs_blocks_per_sm = d.tune.pairs_blocks_per_sm;
+    res.narrow_blocks_per_sm = d.tune.narrow_blocks_per_sm;
+    res.sort_blocks_per_sm = d.tune.sort_blocks_per_sm;
+    res.candidates_timed = timed;
+    h->tuning = res;
+    if (out) *out = res;
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_get_tuning(b3g_handle h, b3gTuning* out) {
+    REQUIRE_UPLOADED(h);
+    if (!out) return fail(B3G_ERR_INVALID_ARG, "null output");
+    b3gTuning t = h->tuning;
+    t.pgs_partitions = h->d.tune.pgs_partitions;
+    t.pairs_blocks_per_sm = h->d.tune.pairs_blocks_per_sm;
+    t.narrow_blocks_per_sm = h->d.tune.narrow_blocks_per_sm;
+    t.sort_blocks_per_sm = h->d.tune.sort_blocks_per_sm;
+    *out = t;
     return B3G_OK;
 }
 

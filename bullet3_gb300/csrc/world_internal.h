@@ -48,7 +48,17 @@ struct SolverPoints {
     float4* imp = nullptr;   // [4m+j]   applied impulses: contact, dir2, dir1, (unused)
 };
 
+// Launch shapes chosen by the autotuner (b3g_autotune); the defaults are the untuned shapes.
+struct LaunchTuning {
+    int pgs_partitions = -1;        // B3G_PGS_PARTITIONS_* used when the config says AUTO (-1: rule)
+    int pairs_blocks_per_sm = 8;    // k_find_pairs grid = SMs x this (bodies per thread)
+    int narrow_blocks_per_sm = 8;   // k_hull_hull_small grid = SMs x this (pairs per thread)
+    int sort_blocks_per_sm = 4;     // radix sort: blocks (one contiguous chunk each) = SMs x this
+};
+static constexpr int B3G_MAX_SORT_BLOCKS_PER_SM = 8;
+
 struct DeviceState {
+    LaunchTuning tune;
     // sizes fixed at upload
     int num_bodies = 0, num_dynamic = 0, num_large = 0, num_collidables = 0;
     int max_pairs = 0, max_contacts = 0;

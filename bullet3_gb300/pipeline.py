@@ -48,6 +48,7 @@ class b3Config:
         self.pgs_interleave = False
         self.warm_start = 0
         self.warm_start_max_points = 0
+        self.autotune = False
         for k, v in kw.items():
             if not hasattr(self, k):
                 raise AttributeError(k)
@@ -64,7 +65,8 @@ class b3Config:
                                    solver_blocks_per_sm=self.solver_blocks_per_sm,
                                    pgs_partitions=self.pgs_partitions,
                                    pgs_interleave=int(self.pgs_interleave), warm_start=int(self.warm_start),
-                                   warm_start_max_points=int(self.warm_start_max_points))
+                                   warm_start_max_points=int(self.warm_start_max_points),
+                                   autotune=int(self.autotune))
 
 
 class _World:
@@ -337,6 +339,18 @@ class b3GpuRigidBodyPipeline:
             if self.m_narrowphase.m_static0Index < 0 and idx == 0:
                 self.m_narrowphase.m_static0Index = 0
         return idx
+
+    def autotune(self, deltaTime: float = 1.0 / 60.0, repeats: int = 3) -> dict:
+        """Times candidate launch shapes on the current state and keeps the fastest (b3g_autotune;
+        no reference counterpart).  The simulation state is left unchanged."""
+        t = capi.b3gTuning()
+        call("b3g_autotune", self._h, C.c_float(deltaTime), C.c_int(repeats), C.byref(t))
+        return {f: getattr(t, f) for f, _ in capi.b3gTuning._fields_}
+
+    def tuning(self) -> dict:
+        t = capi.b3gTuning()
+        call("b3g_get_tuning", self._h, C.byref(t))
+        return {f: getattr(t, f) for f, _ in capi.b3gTuning._fields_}
 
     def setSceneOffsets(self, firstBody):
         """Independent scenes stepped together (no reference counterpart: the reference runs one

@@ -55,8 +55,9 @@ typedef enum b3gStatus {
  * solves the manifolds inside its range alone, the range's body deltas and inverse inertias staged
  * in shared memory (the rest run grid-wide); STREAMED: the same with the block's manifold records
  * streamed through shared memory in bulk-copied tiles; GLOBAL_DELTAS: the same ranges with the
- * deltas left in global memory.  AUTO picks the fastest measured on GB300 for piles of 256k boxes:
- * SHARED with interleaved rows (pgs_interleave), NONE otherwise.  All are legal Gauss-Seidel orders. */
+ * deltas left in global memory.  AUTO uses the split b3g_autotune measured fastest on the world's
+ * own state when it has run, else NONE (the fastest measured on GB300 for piles of 256k boxes).
+ * All are legal Gauss-Seidel orders. */
 #define B3G_PGS_PARTITIONS_AUTO 0
 #define B3G_PGS_PARTITIONS_GLOBAL_DELTAS 1
 #define B3G_PGS_PARTITIONS_NONE 2
@@ -109,7 +110,8 @@ typedef struct b3gConfig {
                                   PGS only; the Jacobi solver ignores it */
     int warm_start_max_points; /* point slots (4 per manifold, in manifold order) that get features and
                                   predictions when warm_start != 0; 0 = 8 x bodies (at least 8192) */
-    int reserved[3];
+    int autotune;              /* 1: the first b3g_step after an upload runs b3g_autotune (3 repeats) */
+    int reserved[2];
 } b3gConfig;
 
 /* Per-step counters, copied once per step from the device. */
@@ -182,6 +184,28 @@ b3gStatus b3g_set_solver(b3g_handle h, int mode, int iterations, float residual_
  * and be non-decreasing (empty scenes are allowed). */
 #define B3G_MAX_SCENES (1 << 20)
 b3gStatus b3g_set_scene_offsets(b3g_handle h, const int* first_body, int num_scenes);
+
+/* Autotuner (no reference counterpart: the reference's OpenCL kernels use fixed work-group
+ * sizes).  Times candidate launch shapes on the world's current state and keeps the fastest of
+ * each: the radix sort's block count and the pair kernel's grid (pair stage), the thread-per-pair
+ * narrowphase kernel's grid (contact stage) and, for PGS with pgs_partitions = AUTO, the solver's
+ * work split (NONE / SHARED / GLOBAL_DELTAS / STREAMED; solve stage).  Each candidate runs the
+ * stages `repeats` + 1 times from the same saved body state (the first run is not kept; the
+ * median is); the bodies are put back afterwards, so the simulation state is unchanged.  Launch
+ * shapes never change results except the PGS split, whose orders are all legal Gauss-Seidel
+ * orders.  Allocates and frees one body-sized scratch buffer; synchronises the stream. */
+typedef struct b3gTuning {
+    int pgs_partitions;        /* chosen B3G_PGS_PARTITIONS_* (-1: not tuned, the AUTO rule applies) */
+    int pairs_blocks_per_sm;   /* pair kernel blocks per SM (256 threads each) */
+    int narrow_blocks_per_sm;  /* thread-per-pair narrowphase blocks per SM */
+    int sort_blocks_per_sm;    /* radix sort blocks per SM */
+    float pairs_ms;            /* median stage times with the chosen shapes */
+    float contacts_ms;
+    float solve_ms;
+    int candidates_timed;
+} b3gTuning;
+b3gStatus b3g_autotune(b3g_handle h, float dt, int repeats, b3gTuning* out);
+b3gStatus b3g_get_tuning(b3g_handle h, b3gTuning* out);
 
 /* ------------------------------------------------------------------ the step */
 /* b3GpuRigidBodyPipeline::stepSimulation (b3GpuRigidBodyPipeline.cpp:221-463): AABBs, pairs,

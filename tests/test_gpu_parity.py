@@ -235,3 +235,23 @@ def test_pgs_partitioned_solve_bitexact(parts, scene, interleave):
     assert np.array_equal(gb["linVel"], ob["linVel"]) and np.array_equal(gb["angVel"], ob["angVel"])
     st = pl.stats()
     assert st.status == 0 and st.num_colors == col.max() + 1
+
+
+def test_collision_at_scale_pair_sets_every_step():
+    # the collision-at-scale shapes at full size: 131,072 bodies in a 64^3 box (boxes, spheres,
+    # Gaussian hulls, random orientations, N(0,1) velocities), grid cell 2x the largest AABB
+    # extent, PGS 10 iterations; the pair set of every step is checked bit for bit against the
+    # oracle's grid pair search over the same AABBs, and the AABBs against the oracle's from the
+    # step's input bodies
+    sc = scenes.mixed_scene(131072, extent=64.0, seed=0)
+    np_, bp, pl, shapes = load(sc, solver_mode=capi.SOLVER_PGS, solver_iterations=10, use_cuda_graph=True)
+    for step in range(4):
+        b = np_.readbackAllBodiesToCpu()
+        pl.stepSimulation(1 / 60)
+        pl.synchronize()
+        ga = bp.getAllAabbsCPU()
+        assert np.array_equal(ga.view(np.uint8), O.aabbs(b, shapes).view(np.uint8)), step
+        gp = pairs_xy(bp.getOverlappingPairsCPU())
+        assert len(gp) > 100000
+        assert np.array_equal(gp, pairs_xy(O.pairs_grid(ga, sc.cell))), step
+    assert pl.status() == 0
