@@ -694,6 +694,9 @@ __device__ __forceinline__ int owner_of(const SolverArgs& a, int body) {
 //      colour with a grid barrier per colour.
 // Group key = owner * NC + colour (block-local) or nblocks * NC + colour (cross), NC = number of
 // block-local colours; the solve order (b3g_read_solve_order) is the manifolds sorted by key.
+// PARTS: block partitions (SHARED / STREAMED / GLOBAL_DELTAS splits); without it every manifold is
+// solved grid-wide and the shared-memory and tile paths are compiled out.
+template <bool PARTS>
 __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
     extern __shared__ __align__(128) float s_dv[];
     grid_barrier_begin();
@@ -887,7 +890,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
         a.inv_mass_ord[k] = make_float4(im.x, im.y, 0.f, 0.f);
         a.sp_ord.nf[k] = __ldcg(&a.sp.nf[m]);
     }
-    if (a.tile_R > 0) fence_proxy_async();  // the ordered records are read by bulk copies below
+    if (PARTS && a.tile_R > 0) fence_proxy_async();  // the ordered records are read by bulk copies below
     if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
     // ---- iterations.  Segments of one pass: the NC block-local colours (__syncthreads between
     // them), then the ncx cross-partition colours and the colour-overflow leftovers (grid barrier
@@ -897,7 +900,8 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
     const int nseg = NC + ncx + (overflow ? 1 : 0);
     float* s_inv = s_dv + 6 * chunk;  // owned bodies' world inverse inertia (fixed during the solve)
     // streamed tiles: two buffers after the owned-body arrays, then two mbarriers and the tile list
-    const int R = a.tile_R;
+    const int R = PARTS ? a.tile_R : 0;
+    const bool use_smem = PARTS && a.use_smem;
     char* tbuf = reinterpret_cast<char*>(s_dv) + ((60 * (size_t)chunk + 15) & ~(size_t)15);
     unsigned long long* tbar = reinterpret_cast<unsigned long long*>(tbuf + 2 * (size_t)R * B3G_PGS_TILE_BYTES);
     int2* tiles = reinterpret_cast<int2*>(tbar + 2);
@@ -936,7 +940,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
         s_seg[sg] = make_int2(lo, hi);
     }
     __syncthreads();
-    if (a.use_smem) {
+    if (use_smem) {
         for (int l = threadIdx.x; l < myN; l += blockDim.x) {
             const b3gMat3 I = ld_mat(&a.inertias[a.sorted_bodies[myLo + l]].invInertiaWorld);
             float* p = s_inv + 9 * l;
@@ -956,7 +960,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
         const bool warm_pass = it < 0;
         for (int ps = 0; ps < (warm_pass ? 1 : npasses); ps++) {
             const int pass = warm_pass ? 3 : (a.interleave ? 2 : ps);
-            if (a.use_smem) {
+            if (use_smem) {
                 for (int l = threadIdx.x; l < myN; l += blockDim.x) {
                     v3 dl, dw;
                     load_dv(a, (int)a.sorted_bodies[myLo + l], dl, dw);
@@ -1049,7 +1053,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
                     hi = tid == 0 ? nc : ncol;
                     step = 1;
                 }
-                const bool smem_here = local && a.use_smem;
+                const bool smem_here = local && use_smem;
                 for (int k = first; k < hi; k += step) {
                     // no early exit for manifolds without active points: their deltas are read and
                     // written back unchanged, and the record loads need not wait for the header
@@ -1073,7 +1077,10 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
                 if (local) {
                     __syncthreads();
                     if (sg < NC - 1) continue;
-                    if (a.use_smem) {
+                    // without partitions the local phase is empty in every block: the barrier
+                    // after the previous segment already orders the phases around it
+                    if (!PARTS || nd == 0) continue;
+                    if (use_smem) {
                         for (int l = threadIdx.x; l < myN; l += blockDim.x) {
                             const float* p = s_dv + 6 * l;
                             store_dv(a, (int)a.sorted_bodies[myLo + l], mk3(p[0], p[1], p[2]),
@@ -1086,6 +1093,12 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
             }
         }
         if (warm_pass) continue;  // the application pass has no residual
+        // the residual is read (one more grid barrier) only where it decides something: a
+        // tolerance, the warm-start check after the first sweep, and the last sweep's statistics
+        if (!(a.residual_tol > 0.f || (it == 0 && warm_live) || it == a.iterations - 1)) {
+            block_accumulate(a.residual_acc + 2 * (it + extra), res_d, res_l);
+            continue;
+        }
         double r = 0.0;
         if (end_iteration(a, it + extra, res_d, res_l, ok, &r)) break;
         if (it == 0 && warm_live) {
@@ -1341,7 +1354,10 @@ static int solver_grid(DeviceState& d, const void* fn, int blocks_per_sm, size_t
 }
 
 cudaError_t solver_prepare() {
-    return cudaFuncSetAttribute(k_solve_pgs, cudaFuncAttributeMaxDynamicSharedMemorySize, B3G_PGS_MAX_SMEM);
+    cudaError_t e = cudaFuncSetAttribute(k_solve_pgs<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         B3G_PGS_MAX_SMEM);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_solve_pgs<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, B3G_PGS_MAX_SMEM);
 }
 
 int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s) {
@@ -1488,7 +1504,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
                                                                        : B3G_PGS_PARTITIONS_NONE;
         const bool parts = mode != B3G_PGS_PARTITIONS_NONE;
         const int nd = parts && d.cell_sorted_bodies ? d.num_dynamic : 0;
-        sgrid = solver_grid(d, (const void*)k_solve_pgs, bps, 0);
+        sgrid = solver_grid(d, (const void*)k_solve_pgs<true>, bps, 0);
         const int chunk = nd > 0 ? (nd + sgrid - 1) / sgrid : 1;
         const size_t owned = ((size_t)chunk * 15 * sizeof(float) + 15) & ~(size_t)15;
         const bool shared_mode = mode == B3G_PGS_PARTITIONS_SHARED || mode == B3G_PGS_PARTITIONS_STREAMED;
@@ -1505,7 +1521,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
         }
         if (R > 0) smem = owned + 2 * (size_t)R * B3G_PGS_TILE_BYTES + tile_extra;
         // keep the grid co-resident: drop the shared-memory use if it would cost occupancy
-        if (smem > 0 && solver_grid(d, (const void*)k_solve_pgs, bps, smem) != sgrid) {
+        if (smem > 0 && solver_grid(d, (const void*)k_solve_pgs<true>, bps, smem) != sgrid) {
             smem = 0;
             R = 0;
         }
@@ -1527,7 +1543,9 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     attr[0].val.cooperative = 1;
     lc.attrs = attr;
     lc.numAttrs = 1;
-    cudaError_t e = jac ? cudaLaunchKernelEx(&lc, k_solve_jacobi, a) : cudaLaunchKernelEx(&lc, k_solve_pgs, a);
+    cudaError_t e = jac                 ? cudaLaunchKernelEx(&lc, k_solve_jacobi, a)
+                    : a.num_dynamic > 0 ? cudaLaunchKernelEx(&lc, k_solve_pgs<true>, a)
+                                        : cudaLaunchKernelEx(&lc, k_solve_pgs<false>, a);
     if (e != cudaSuccess && d.launch_error == cudaSuccess) d.launch_error = e;
     launches++;
     if (wm != B3G_WARM_COLD && d.prev_keys) {  // this solve's impulses for the next step's persisting points
