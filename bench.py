@@ -389,7 +389,8 @@ def gpu_arm(args):
     roofline = {"bound": "hbm", "kernel": "solve stage (k_setup_rows + k_solve_pgs persistent kernel)",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_kind": peak_kind, "algorithmic_bytes": solve_bytes,
-                "traffic": traffic.get("bytes_per_step_scaled") if traffic else None}
+                "traffic": (traffic["bytes_per_manifold"] * C_ if traffic and "bytes_per_manifold" in traffic
+                            else None)}
     stages = {k: {"ms": float(v), "algorithmic_GBps": stage_bytes[k] / (v / 1000.0) / 1e9 if v > 0 else None,
                   "frac_of_hbm": (stage_bytes[k] / (v / 1000.0) / 1e9 / peak) if v > 0 else None}
               for k, v in stage_ms.items()}

@@ -1,0 +1,71 @@
+"""Step a synthetic workload for a fixed number of steps and print one line of statistics.
+
+Meant for running the pipeline under an external profiler (ncu) or by hand: nothing but the
+scene upload, the warm-up steps and the measured steps touch the GPU.
+
+    python -m bullet3_gb300.stepper [--workload pile|lattice|batched|mixed] [--steps K] [--warmup W]
+                                    [--solver pgs|jacobi] [--iterations I] [--autotune]
+
+  pile     262,144 unit boxes resting in 64x64 columns on a plane (the settled 64^3 lattice)
+  lattice  the 64^3 lattice (spacing 1.1, jitter 0.05) falling onto the plane from rest
+  batched  4,096 independent box/sphere piles, each on its own plane, through per-scene offsets
+  mixed    131,072 boxes, spheres and Gaussian hulls in a 64^3 box, random orientations, N(0,1) velocities
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+from . import capi, scenes
+from .pipeline import b3Config
+
+
+def make(workload: str, n: int = 64):
+    if workload == "pile":
+        return scenes.box_stack(n, 64, n, seed=0)
+    if workload == "lattice":
+        return scenes.box_pile(n, 64, n, jitter=0.05, seed=0)
+    if workload == "batched":
+        return scenes.batched_piles(4096, seed=0, separate=True)
+    if workload == "mixed":
+        return scenes.mixed_scene(131072, extent=64.0, seed=0)
+    raise ValueError(workload)
+
+
+def main(argv=None):
+    p = argparse.ArgumentParser()
+    p.add_argument("--workload", choices=["pile", "lattice", "batched", "mixed"], default="pile")
+    p.add_argument("--nx", type=int, default=64)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--solver", choices=["pgs", "jacobi"], default="pgs")
+    p.add_argument("--iterations", type=int, default=10)
+    p.add_argument("--autotune", action="store_true")
+    p.add_argument("--no-graph", action="store_true")
+    a = p.parse_args(argv)
+    sc = make(a.workload, a.nx)
+    cfg = b3Config(solver_mode=capi.SOLVER_PGS if a.solver == "pgs" else capi.SOLVER_JACOBI,
+                   solver_iterations=a.iterations, pgs_interleave=a.solver == "pgs",
+                   use_cuda_graph=not a.no_graph)
+    np_, bp, pl = scenes.load_scene(sc, cfg)
+    dt = 1.0 / 60.0
+    for _ in range(a.warmup):
+        pl.stepSimulation(dt)
+    pl.synchronize()
+    tuning = pl.autotune(dt) if a.autotune else None
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        pl.stepSimulation(dt)
+    pl.synchronize()
+    secs = time.perf_counter() - t0
+    st = pl.stats()
+    print(json.dumps({"workload": a.workload, "bodies": sc.num_bodies, "steps": a.steps,
+                      "host_ms_per_step": 1000 * secs / max(a.steps, 1), "pairs": st.num_pairs,
+                      "manifolds": st.num_contacts, "points": st.num_points, "colors": st.num_colors,
+                      "status": int(pl.status()), "tuning": tuning}))
+    return 0 if pl.status() == 0 else 1
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
