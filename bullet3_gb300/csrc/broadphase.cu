@@ -137,6 +137,101 @@ struct PairEmitter {
     }
 };
 
+// 1-axis sweep and prune over the finite static proxies: per scene, the proxies sorted by their
+// AABB min along one axis, and the largest AABB extent along it (rounded up).  A proxy L can
+// overlap a body B only if L.min lies in [B.min - extent, B.max] on that axis, so each body scans
+// that window (two binary searches) instead of the whole list.
+struct SapView {
+    const int* sorted;   // body indices, per scene sorted by AABB min along `axis`
+    const float* mins;   // those mins
+    const int* off;      // per scene: first entry (num_scenes + 1)
+    const float* ext;    // per scene: largest extent along the axis (+inf: unsorted, scan all)
+    int axis;
+    int n;               // 0: no finite static proxies
+};
+
+__device__ __forceinline__ float axis_of(const float4& v, int axis) { return axis == 0 ? v.x : (axis == 1 ? v.y : v.z); }
+
+// One block per scene: bitonic sort of the scene's finite static proxies (<= B3G_SAP_MAX_PER_SCENE)
+// by AABB min along the axis, in shared memory; larger scenes are copied unsorted with extent +inf.
+__global__ void __launch_bounds__(512) k_sap_sort(const b3gAabb* __restrict__ aabbs, const int* __restrict__ list,
+                                                  const int* __restrict__ off, int axis, int* __restrict__ sorted,
+                                                  float* __restrict__ mins, float* __restrict__ ext) {
+    __shared__ float s_key[B3G_SAP_MAX_PER_SCENE];
+    __shared__ int s_idx[B3G_SAP_MAX_PER_SCENE];
+    __shared__ float s_ext[512 / 32];
+    const int sc = blockIdx.x;
+    const int lo = off[sc], n = off[sc + 1] - lo;
+    if (n <= 0) return;
+    const float4* A = reinterpret_cast<const float4*>(aabbs);
+    float e = 0.f;
+    if (n > B3G_SAP_MAX_PER_SCENE) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int b = list[lo + i];
+            sorted[lo + i] = b;
+            mins[lo + i] = axis_of(A[2 * b], axis);
+        }
+        if (threadIdx.x == 0) ext[sc] = __int_as_float(0x7f800000);
+        return;
+    }
+    int P = 2;
+    while (P < n) P <<= 1;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        if (i < n) {
+            const int b = list[lo + i];
+            const float mn = axis_of(A[2 * b], axis), mx = axis_of(A[2 * b + 1], axis);
+            s_key[i] = mn;
+            s_idx[i] = b;
+            e = fmaxf(e, __fsub_ru(mx, mn));
+        } else {
+            s_key[i] = __int_as_float(0x7f800000);
+            s_idx[i] = -1;
+        }
+    }
+    for (int o = 16; o; o >>= 1) e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, o));
+    if ((threadIdx.x & 31) == 0) s_ext[threadIdx.x >> 5] = e;
+    __syncthreads();
+    for (int k = 2; k <= P; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < P; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l <= i) continue;
+                const bool up = (i & k) == 0;
+                const float a = s_key[i], b = s_key[l];
+                if ((a > b) == up) {
+                    s_key[i] = b;
+                    s_key[l] = a;
+                    const int t = s_idx[i];
+                    s_idx[i] = s_idx[l];
+                    s_idx[l] = t;
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        sorted[lo + i] = s_idx[i];
+        mins[lo + i] = s_key[i];
+    }
+    if (threadIdx.x == 0) {
+        float m = 0.f;
+        for (int w = 0; w < (int)(blockDim.x / 32); w++) m = fmaxf(m, s_ext[w]);
+        ext[sc] = m;
+    }
+}
+
+// first index in [lo, hi) with v[index] >= x (lower) or > x (upper)
+__device__ __forceinline__ int bound_search(const float* v, int lo, int hi, float x, bool upper) {
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const float y = __ldg(&v[mid]);
+        if (upper ? (y <= x) : (y < x))
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
 // SCENES: bodies carry a scene index (b3g_set_scene_offsets); cells are shifted per scene, pairs
 // need equal scenes and each body tests only its own scene's range of the large list.
 template <bool SCENES>
@@ -145,9 +240,9 @@ __device__ __forceinline__ void find_pairs_body(const b3gAabb* __restrict__ aabb
                                                 const uint32_t* __restrict__ cell_start, int n_dyn,
                                                 const int* __restrict__ large_list, int n_large,
                                                 const int* __restrict__ body_scene,
-                                                const int* __restrict__ large_off, float inv_cell, int bits,
-                                                int body_bits, uint64_t* __restrict__ out, int* __restrict__ counter,
-                                                int cap, unsigned int* __restrict__ status) {
+                                                const int* __restrict__ large_off, const SapView sap, float inv_cell,
+                                                int bits, int body_bits, uint64_t* __restrict__ out,
+                                                int* __restrict__ counter, int cap, unsigned int* __restrict__ status) {
     const int mask = (1 << bits) - 1;
     const int lane = threadIdx.x & 31;
     const float4* A = reinterpret_cast<const float4*>(aabbs);
@@ -199,6 +294,24 @@ __device__ __forceinline__ void find_pairs_body(const b3gAabb* __restrict__ aabb
                     em.push(((uint64_t)a << body_bits) | b, out, counter, cap, status);
                 }
             }
+            if (sap.n > 0) {
+                int q0 = __ldg(&sap.off[si]), q1 = __ldg(&sap.off[si + 1]);
+                const float e = __ldg(&sap.ext[si]);
+                if (q0 < q1 && e <= 3.4e38f) {
+                    // window of mins in [min - extent, max]; the lower end rounded down so that no
+                    // proxy reaching this body is left out
+                    q0 = bound_search(sap.mins, q0, q1, __fsub_rd(axis_of(amin, sap.axis), e), false);
+                    q1 = bound_search(sap.mins, q0, q1, axis_of(amax, sap.axis), true);
+                }
+                for (int q = q0; q < q1; q++) {
+                    uint32_t j = (uint32_t)__ldg(&sap.sorted[q]);
+                    float4 bmin = __ldg(&A[2 * j]), bmax = __ldg(&A[2 * j + 1]);
+                    if (overlap(amin, amax, bmin, bmax)) {
+                        uint32_t a = i < j ? i : j, b = i < j ? j : i;
+                        em.push(((uint64_t)a << body_bits) | b, out, counter, cap, status);
+                    }
+                }
+            }
         }
     }
     // warp-aggregated reservation of the remaining buffered pairs
@@ -229,17 +342,20 @@ __global__ void __launch_bounds__(BP_THREADS) k_find_pairs(const b3gAabb* __rest
                                                            float inv_cell, int bits, int body_bits,
                                                            uint64_t* __restrict__ out, int* __restrict__ counter,
                                                            int cap, unsigned int* __restrict__ status) {
-    find_pairs_body<false>(aabbs, keys, vals, cell_start, n_dyn, large_list, n_large, nullptr, nullptr, inv_cell, bits,
-                           body_bits, out, counter, cap, status);
+    find_pairs_body<false>(aabbs, keys, vals, cell_start, n_dyn, large_list, n_large, nullptr, nullptr,
+                           SapView{nullptr, nullptr, nullptr, nullptr, 0, 0}, inv_cell, bits, body_bits, out, counter,
+                           cap, status);
 }
 
-__global__ void __launch_bounds__(BP_THREADS) k_find_pairs_scenes(
+// the world's pair kernel: large (unbounded) list, sweep and prune over finite statics, scenes
+template <bool SCENES>
+__global__ void __launch_bounds__(BP_THREADS) k_find_pairs_world(
     const b3gAabb* __restrict__ aabbs, const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
     const uint32_t* __restrict__ cell_start, int n_dyn, const int* __restrict__ large_list, int n_large,
-    const int* __restrict__ body_scene, const int* __restrict__ large_off, float inv_cell, int bits, int body_bits,
-    uint64_t* __restrict__ out, int* __restrict__ counter, int cap, unsigned int* __restrict__ status) {
-    find_pairs_body<true>(aabbs, keys, vals, cell_start, n_dyn, large_list, n_large, body_scene, large_off, inv_cell,
-                          bits, body_bits, out, counter, cap, status);
+    const int* __restrict__ body_scene, const int* __restrict__ large_off, const SapView sap, float inv_cell, int bits,
+    int body_bits, uint64_t* __restrict__ out, int* __restrict__ counter, int cap, unsigned int* __restrict__ status) {
+    find_pairs_body<SCENES>(aabbs, keys, vals, cell_start, n_dyn, large_list, n_large, body_scene, large_off, sap,
+                            inv_cell, bits, body_bits, out, counter, cap, status);
 }
 
 __global__ void k_clamp_count(int* counter, int cap, int* clamped) {
@@ -328,16 +444,22 @@ int launch_pairs(DeviceState& d, cudaStream_t s) {
     cudaMemsetAsync(reinterpret_cast<char*>(d.counters) + offsetof(DevCounters, status) + sizeof(unsigned int), 0,
                     sizeof(DevCounters) - offsetof(DevCounters, status) - sizeof(unsigned int), s);
     const int pgrid = d.num_sms * d.tune.pairs_blocks_per_sm;
+    const SapView sap{d.sap_sorted, d.sap_min, d.sap_off, d.sap_ext, d.sap_axis, d.num_sap};
+    if (d.num_sap > 0) {
+        k_sap_sort<<<d.num_scenes, 512, 0, s>>>(d.aabbs, d.sap_list, d.sap_off, d.sap_axis, d.sap_sorted, d.sap_min,
+                                                d.sap_ext);
+        launches++;
+    }
     if (d.num_scenes > 1)
-        k_find_pairs_scenes<<<pgrid, BP_THREADS, 0, s>>>(
+        k_find_pairs_world<true><<<pgrid, BP_THREADS, 0, s>>>(
             d.aabbs, keys, vals, d.cell_start, d.num_dynamic, d.large_list, d.num_large, d.body_scene, d.large_off,
-            d.inv_cell, d.grid_bits, d.body_bits, d.pair_keys[0], &d.counters->num_pairs, d.max_pairs,
+            sap, d.inv_cell, d.grid_bits, d.body_bits, d.pair_keys[0], &d.counters->num_pairs, d.max_pairs,
             &d.counters->status);
     else
-        k_find_pairs<<<pgrid, BP_THREADS, 0, s>>>(d.aabbs, keys, vals, d.cell_start, d.num_dynamic,
-                                                          d.large_list, d.num_large, d.inv_cell, d.grid_bits,
-                                                          d.body_bits, d.pair_keys[0], &d.counters->num_pairs,
-                                                          d.max_pairs, &d.counters->status);
+        k_find_pairs_world<false><<<pgrid, BP_THREADS, 0, s>>>(
+            d.aabbs, keys, vals, d.cell_start, d.num_dynamic, d.large_list, d.num_large, nullptr, nullptr, sap,
+            d.inv_cell, d.grid_bits, d.body_bits, d.pair_keys[0], &d.counters->num_pairs, d.max_pairs,
+            &d.counters->status);
     launches++;
     // clamp the count to capacity for the consumers (the raw count stays in num_pairs)
     int* d_np = &d.counters->pad[0];

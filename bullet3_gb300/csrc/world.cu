@@ -444,7 +444,9 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     d.num_bodies = N;
     d.num_collidables = (int)h->collidables.size();
     // dynamic (small) and static (large) proxies, as registerPhysicsInstance does (:650-657)
-    std::vector<int> dyn_slot(N, -1), large;
+    // static bodies: unbounded AABBs (planes) are tested by every body of their scene; finite
+    // ones go through the 1-axis sweep and prune
+    std::vector<int> dyn_slot(N, -1), large, sap;
     int nd = 0;
     float max_extent = 0.f;
     for (int i = 0; i < N; i++) {
@@ -457,11 +459,32 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
             float e = 2.f * std::sqrt(hx * hx + hy * hy + hz * hz);
             max_extent = std::max(max_extent, e);
         } else {
-            large.push_back(i);
+            const b3gAabb& la = h->local_aabbs[h->bodies[i].collidableIdx];
+            bool finite = true;
+            for (int k = 0; k < 3; k++)
+                if (!(std::fabs(la.minv[k]) < 1e10f && std::fabs(la.maxv[k]) < 1e10f)) finite = false;
+            (finite ? sap : large).push_back(i);
         }
     }
     d.num_dynamic = nd;
     d.num_large = (int)large.size();
+    d.num_sap = (int)sap.size();
+    {
+        // sweep axis: largest spread of the finite static bodies' positions
+        double m[3] = {0, 0, 0}, q[3] = {0, 0, 0};
+        for (int i : sap)
+            for (int k = 0; k < 3; k++) {
+                const double x = (&h->bodies[i].pos.x)[k];
+                m[k] += x;
+                q[k] += x * x;
+            }
+        d.sap_axis = 0;
+        double best = -1.0;
+        for (int k = 0; k < 3 && !sap.empty(); k++) {
+            const double var = q[k] / sap.size() - (m[k] / sap.size()) * (m[k] / sap.size());
+            if (var > best) { best = var; d.sap_axis = k; }
+        }
+    }
     // independent scenes: per-body scene index and, per scene, its range of the large list (bodies
     // are registered scene by scene, so the large list is already grouped by scene)
     std::vector<int> body_scene, large_off;
@@ -479,6 +502,9 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
         for (int i : large) large_off[body_scene[i] + 1]++;
         for (int sc = 0; sc < S; sc++) large_off[sc + 1] += large_off[sc];
     }
+    std::vector<int> sap_off(d.num_scenes + 1, 0);
+    for (int i : sap) sap_off[(d.num_scenes > 1 ? body_scene[i] : 0) + 1]++;
+    for (int sc = 0; sc < d.num_scenes; sc++) sap_off[sc + 1] += sap_off[sc];
     float cell = h->cfg.grid_cell_size > 0.f ? h->cfg.grid_cell_size : max_extent;
     // exactness of the 27-cell search needs cell >= every dynamic AABB extent
     if (cell < max_extent) cell = max_extent;
@@ -510,6 +536,11 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     TRY(dalloc(h, &d.dyn_slot, N));
     TRY(dalloc(h, &d.col_small, d.num_collidables));
     TRY(dalloc(h, &d.large_list, std::max(1, d.num_large)));
+    TRY(dalloc(h, &d.sap_list, std::max(1, d.num_sap)));
+    TRY(dalloc(h, &d.sap_sorted, std::max(1, d.num_sap)));
+    TRY(dalloc(h, &d.sap_min, std::max(1, d.num_sap)));
+    TRY(dalloc(h, &d.sap_off, d.num_scenes + 1));
+    TRY(dalloc(h, &d.sap_ext, d.num_scenes));
     if (d.num_scenes > 1) {
         TRY(dalloc(h, &d.body_scene, N));
         TRY(dalloc(h, &d.large_off, d.num_scenes + 1));
@@ -634,6 +665,9 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
                              s));
     if (!large.empty())
         CUDA_TRY(cudaMemcpyAsync(d.large_list, large.data(), sizeof(int) * large.size(), cudaMemcpyHostToDevice, s));
+    if (!sap.empty())
+        CUDA_TRY(cudaMemcpyAsync(d.sap_list, sap.data(), sizeof(int) * sap.size(), cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(d.sap_off, sap_off.data(), sizeof(int) * sap_off.size(), cudaMemcpyHostToDevice, s));
     if (d.num_scenes > 1) {
         CUDA_TRY(cudaMemcpyAsync(d.body_scene, body_scene.data(), sizeof(int) * N, cudaMemcpyHostToDevice, s));
         CUDA_TRY(cudaMemcpyAsync(d.large_off, large_off.data(), sizeof(int) * (d.num_scenes + 1),
@@ -938,7 +972,7 @@ extern "C" b3gStatus b3g_get_stats(b3g_handle h, b3gStepStats* out) {
     out->iterations = c.iterations;
     out->residual = c.residual;
     out->status = c.status;
-    out->num_large = h->d.num_large;
+    out->num_large = h->d.num_large + h->d.num_sap;
     return B3G_OK;
 }
 

@@ -56,6 +56,8 @@ struct LaunchTuning {
     int sort_blocks_per_sm = 4;     // radix sort: blocks (one contiguous chunk each) = SMs x this
 };
 static constexpr int B3G_MAX_SORT_BLOCKS_PER_SM = 8;
+// finite static proxies sorted per scene in shared memory; a scene with more is scanned whole
+static constexpr int B3G_SAP_MAX_PER_SCENE = 4096;
 
 struct DeviceState {
     LaunchTuning tune;
@@ -80,6 +82,14 @@ struct DeviceState {
     int num_scenes = 1;
     int* body_scene = nullptr;    // per body: its scene
     int* large_off = nullptr;     // per scene: first entry in large_list (num_scenes + 1)
+    // static bodies with finite AABBs: 1-axis sweep and prune instead of the brute-force list
+    int num_sap = 0;
+    int sap_axis = 0;             // axis of the sweep (largest spread of the proxies' centres)
+    int* sap_list = nullptr;      // finite static bodies, grouped by scene
+    int* sap_off = nullptr;       // per scene: first entry in sap_list (num_scenes + 1)
+    int* sap_sorted = nullptr;    // per scene: the same bodies sorted by AABB min along the axis
+    float* sap_min = nullptr;     // their AABB mins along the axis (sorted)
+    float* sap_ext = nullptr;     // per scene: largest AABB extent along the axis (rounded up; inf: unsorted)
     // broadphase
     b3gAabb* aabbs = nullptr;
     uint32_t* cell_keys[2] = {nullptr, nullptr};

@@ -204,6 +204,55 @@ def mixed_scene(n=131072, extent=64.0, seed=0, velocity_sigma=1.0, plane=False, 
     return sc
 
 
+def static_field(n_static=2000, n_dynamic=6000, extent=100.0, seed=0, plane=True, scenes=1) -> Scene:
+    """Large finite static bodies with small dynamic ones among them: static boxes with half
+    extents U[0.5, 6] (mass 0, random rotation about y) spread over an extent x extent area at
+    heights U[0, 4], and dynamic boxes (half extents U[0.2, 0.5]) and spheres (r U[0.2, 0.5]) at
+    heights U[0, 8] with N(0, 1) velocities, over a plane y = 0.  With scenes > 1 the bodies are
+    split into that many independent scenes (each with its own plane), all in the same region;
+    `scene_first` is the offset table."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sc = Scene(name=f"static_field_{n_static}_{n_dynamic}")
+    sc.shapes.append({"type": "plane", "normal": (0.0, 1.0, 0.0), "constant": 0.0})
+    shapes, masses, pos, orn, vel, first = [], [], [], [], [], []
+    per_s, per_d = n_static // scenes, n_dynamic // scenes
+    for k in range(scenes):
+        first.append(len(shapes))
+        if plane:
+            shapes.append(0)
+            masses.append(0.0)
+            pos.append(np.zeros(3))
+            orn.append(np.array([0, 0, 0, 1.0]))
+            vel.append(np.zeros(3))
+        for _ in range(per_s):
+            h = rng.uniform(0.5, 6.0, 3)
+            sc.shapes.append({"type": "hull", "verts": box_vertices(*h)})
+            shapes.append(len(sc.shapes) - 1)
+            masses.append(0.0)
+            pos.append(np.array([rng.uniform(0, extent), rng.uniform(0, 4), rng.uniform(0, extent)]))
+            a = rng.uniform(0, np.pi)
+            orn.append(np.array([0.0, np.sin(a / 2), 0.0, np.cos(a / 2)]))
+            vel.append(np.zeros(3))
+        for _ in range(per_d):
+            if rng.uniform() < 0.5:
+                sc.shapes.append({"type": "hull", "verts": box_vertices(*rng.uniform(0.2, 0.5, 3))})
+            else:
+                sc.shapes.append({"type": "sphere", "radius": float(rng.uniform(0.2, 0.5))})
+            shapes.append(len(sc.shapes) - 1)
+            masses.append(1.0)
+            pos.append(np.array([rng.uniform(0, extent), rng.uniform(0, 8), rng.uniform(0, extent)]))
+            orn.append(random_quaternions(rng, 1)[0])
+            vel.append(rng.standard_normal(3))
+    sc.body_shape = np.array(shapes, np.int32)
+    sc.mass = np.array(masses, np.float32)
+    sc.pos = np.array(pos, np.float32)
+    sc.orn = np.array(orn, np.float32)
+    sc.linvel = np.array(vel, np.float32)
+    if scenes > 1:
+        sc.scene_first = np.array(first, np.int32)
+    return sc
+
+
 def load_scene(scene: Scene, config=None, device: int = 0, upload: bool = True):
     """Register a Scene through the reference-style API; returns (narrowphase, broadphase, pipeline)."""
     from .pipeline import b3Config, b3GpuGridBroadphase, b3GpuNarrowPhase, b3GpuRigidBodyPipeline
