@@ -6,12 +6,12 @@ resting on a static plane -- the settled form of the 64^3 lattice pile (x/z spac
 jitter +-0.05, seed 0) -- PGS solver, 10 iterations, dt 1/60, gravity -9.8.  One step =
 stepSimulation: AABBs, grid broadphase, narrowphase, colouring, PGS solve, integration.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload pile|batched]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload pile|batched|stress]
 
-The line also carries `to_residual` (rank 0, one GPU, pile workload): the falling 64^3 lattice
-(spacing 1.1, jitter 0.05) stepped from rest with every PGS solve run to a 1e-4 contact residual,
-once per warm-start mode (plain = cold start, learned, persistent, persistent + learned), with
-the mean sweeps, solve ms and step ms per step of each.  --workload batched times 4,096
+The line also carries `to_residual` (rank 0, one GPU, pile workload): every PGS solve run to a
+1e-4 contact residual, once per warm-start mode (plain = cold start, learned, persistent,
+persistent + learned), with the mean sweeps, solve ms and step ms per step of each, on two
+workloads: the falling 64^3 lattice (spacing 1.1, jitter 0.05) and 512 held-out batched piles.  --workload batched times 4,096
 independent scenes (counts log-uniform in [8, 256]) stepped together through per-scene offset
 tables instead of the pile.
 
@@ -41,6 +41,13 @@ WORKLOAD = ("box pile 64x64x64 = 262,144 unit boxes resting in 64x64 columns on 
 WORKLOAD_BATCHED = ("{n} independent scenes (body counts log-uniform in [8, 256], seed 0; {bodies} bodies), each a "
                     "jittered box/sphere pile (spacing 1.1, base 0.6, jitter 0.01) on its own plane, all at the "
                     "origin, stepped together through per-scene offset tables, PGS 10 iterations, dt 1/60")
+WORKLOAD_STRESS = ("{bodies} bodies: 1,048,576 mixed convex bodies (50% boxes, 25% spheres, 25% Gaussian hulls, "
+                   "random orientations, zero velocity) poured from heights U[0, 512] into a 128x64x128 container of "
+                   "5 static planes; PGS to a 1e-4 residual with a 16-sweep cap, persistent + learned warm start with "
+                   "the cold fallback, graph-captured step; timed steps {first}..{last} of the 600-step pour")
+PILES_WORKLOAD = ("512 batched box/sphere piles (counts log-uniform in [8, 256], {bodies} bodies, seed 1007, not a "
+                  "training seed) falling onto a shared plane, steps 20..79, every PGS solve run to a {tol:g} contact "
+                  "residual (at most {cap} sweeps)")
 RESIDUAL_WORKLOAD = ("box pile lattice 64x64x64 = 262,144 unit boxes (spacing 1.1, jitter 0.05, seed 0) falling onto "
                      "a static plane from rest, steps 0..{last}, every PGS solve run to a {tol:g} contact residual "
                      "(at most {cap} sweeps)")
@@ -57,7 +64,7 @@ def solver_mode_code(args):
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=30)
+    p.add_argument("--steps", type=int, default=None, help="timed steps (default 30; stress: 597)")
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--nx", type=int, default=64)
@@ -68,15 +75,25 @@ def parse():
     p.add_argument("--row-order", choices=["interleaved", "separate"], default="interleaved",
                    help="PGS row order: per contact point (reference B3_SOLVER_INTERLEAVE_CONTACT_AND_FRICTION_"
                         "CONSTRAINTS mode) or all contact rows then all friction rows (reference default)")
-    p.add_argument("--workload", choices=["pile", "batched"], default="pile",
-                   help="pile: the 262,144-box pile; batched: independent scenes stepped together")
+    p.add_argument("--workload", choices=["pile", "batched", "stress"], default="pile",
+                   help="pile: the 262,144-box pile; batched: independent scenes stepped together; stress: "
+                        "1,048,576 mixed bodies poured into a 5-plane container")
+    p.add_argument("--settle", type=int, default=None,
+                   help="untimed steps before the warm-up (default: 120 for batched, so the piles have landed; 0 otherwise)")
     p.add_argument("--scenes", type=int, default=4096, help="number of scenes of the batched workload")
     p.add_argument("--residual-steps", type=int, default=60,
                    help="steps of the falling 64^3 lattice solved to the residual, per warm-start mode (0 = skip)")
     p.add_argument("--residual-cap", type=int, default=4000)
     p.add_argument("--residual-tol", type=float, default=1e-4)
     p.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
-    return p.parse_args()
+    a = p.parse_args()
+    if a.steps is None:
+        a.steps = 597 if a.workload == "stress" else 30
+    if a.settle is None:
+        a.settle = 120 if a.workload == "batched" else 0
+    if a.workload == "stress":
+        a.iterations = 16
+    return a
 
 
 def dist_info():
@@ -179,12 +196,16 @@ def make_scene(args):
     from bullet3_gb300 import scenes
     if args.workload == "batched":
         return scenes.batched_piles(args.scenes, seed=0, separate=True)
+    if args.workload == "stress":
+        return scenes.stress_container(1048576, seed=0)
     return scenes.box_stack(args.nx, 64, args.nx, seed=0)
 
 
 def workload_name(args, scene):
     if args.workload == "batched":
-        return WORKLOAD_BATCHED.format(n=args.scenes, bodies=scene.num_bodies)
+        return WORKLOAD_BATCHED.format(n=args.scenes, bodies=scene.num_bodies) + f", steps {args.settle + args.warmup}.."
+    if args.workload == "stress":
+        return WORKLOAD_STRESS.format(bodies=scene.num_bodies, first=args.warmup, last=args.warmup + args.steps - 1)
     return WORKLOAD
 
 
@@ -234,36 +255,31 @@ def reference_arm(args):
     mode = solver_mode_code(args)
     # warm-up steps are run (untimed) from the same initial state; each timed step is one full
     # composed CPU step of the whole 262,144-body scene
+    # (the million-body pour is sampled: at most 3 timed CPU steps, as its CPU baseline is)
+    steps = args.steps if args.workload != "stress" else min(args.steps, 3)
     cpu_run(scene, args.warmup, args.iterations, mode) if args.warmup else None
-    secs, threads, n = cpu_run(scene, args.steps, args.iterations, mode)
-    value = n * args.steps / secs
+    secs, threads, n = cpu_run(scene, steps, args.iterations, mode)
+    value = n * steps / secs
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * secs / args.steps,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": 1000 * secs / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": workload_name(args, scene), "bodies": n, "solver": args.solver,
                        "iterations": args.iterations, "row_order": args.row_order},
             "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} composed CPU steps of the full {n}-body scene"},
+                             "sample": f"{steps} composed CPU steps of the full {n}-body scene"},
             "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
 # ------------------------------------------------------------------------------ learned vs plain
-def to_residual(args, device):
-    """Sweeps and solve time per step when every solve runs to the residual target, per warm-start
-    mode, on the falling 64^3 lattice: plain (cold start, the reference's solver), learned (the
-    network predicts every point), persistent (points matched to the previous step's manifolds
-    start from their converged impulses) and persistent + learned (the network predicts the new
-    points).  Each mode steps the same initial state; a warm start whose first sweep is worse than
-    a cold start is dropped and counted in `fallback_steps`."""
+def _residual_modes(sc, args, device, net, steps, first):
+    """Mean sweeps / solve ms / step ms per step over steps [first, steps) for each warm-start mode,
+    every mode stepped from the same initial state."""
     import numpy as np
 
     from bullet3_gb300 import capi, scenes
     from bullet3_gb300.pipeline import b3Config
-    from bullet3_gb300.warmstart import DEFAULT_WEIGHTS, WarmStartMLP
-    net = WarmStartMLP.load(DEFAULT_WEIGHTS)
-    sc = scenes.box_pile(args.nx, 64, args.nx, jitter=0.05, seed=0)
     modes = {"plain": capi.WARM_COLD, "learned": capi.WARM_LEARNED, "persistent": capi.WARM_PERSISTENT,
              "persistent_learned": capi.WARM_PERSISTENT_LEARNED}
     out = {}
@@ -275,16 +291,17 @@ def to_residual(args, device):
             pl.setWarmStartModel(net)
         pl.setProfiling(True)
         sweeps, solve_ms, step_ms, dropped, capped = [], [], [], 0, 0
-        for _ in range(args.residual_steps):
+        for step in range(steps):
             pl.stepSimulation(1.0 / 60.0)
             pl.synchronize()
             st = pl.stats()
             t = pl.stageTimes()
-            sweeps.append(st.iterations)
-            solve_ms.append(float(t[4]))
-            step_ms.append(float(np.sum(t)))
-            dropped += bool(st.status & capi.FLAG_WARM_DISCARDED)
-            capped += st.iterations >= args.residual_cap
+            if step >= first:
+                sweeps.append(st.iterations)
+                solve_ms.append(float(t[4]))
+                step_ms.append(float(np.sum(t)))
+                dropped += bool(st.status & capi.FLAG_WARM_DISCARDED)
+                capped += st.iterations >= args.residual_cap
             pl.status(clear=True)
         pl.setProfiling(False)
         out[name] = {"sweeps_per_step": float(np.mean(sweeps)), "solve_ms_per_step": float(np.mean(solve_ms)),
@@ -295,11 +312,30 @@ def to_residual(args, device):
     for name in ("learned", "persistent", "persistent_learned"):
         out[name]["sweeps_vs_plain"] = out[name]["sweeps_per_step"] / max(base["sweeps_per_step"], 1e-9)
         out[name]["solve_ms_vs_plain"] = out[name]["solve_ms_per_step"] / max(base["solve_ms_per_step"], 1e-9)
-    return {"workload": RESIDUAL_WORKLOAD.format(last=args.residual_steps - 1, tol=args.residual_tol,
-                                                 cap=args.residual_cap),
-            "tol": args.residual_tol, "cap": args.residual_cap, "steps": args.residual_steps,
+    return out
+
+
+def to_residual(args, device):
+    """Sweeps and solve time per step when every solve runs to the residual target, per warm-start
+    mode: plain (cold start, the reference's solver), learned (the network predicts every point),
+    persistent (points matched to the previous step's manifolds start from their converged
+    impulses) and persistent + learned (the network predicts the new points).  Two workloads: the
+    falling 64^3 lattice, and held-out batched piles like the ones the network was trained on
+    (seeds it never saw).  A warm start whose first sweep is worse than a cold start is dropped and
+    counted in `fallback_steps`."""
+    from bullet3_gb300 import scenes
+    from bullet3_gb300.warmstart import DEFAULT_WEIGHTS, WarmStartMLP
+    net = WarmStartMLP.load(DEFAULT_WEIGHTS)
+    lattice = scenes.box_pile(args.nx, 64, args.nx, jitter=0.05, seed=0)
+    piles = scenes.batched_piles(512, seed=1007)
+    return {"tol": args.residual_tol, "cap": args.residual_cap,
             "residual": "||lambda_k - lambda_k-1||_2 / ||lambda_k||_2 over all contact and friction rows, per sweep",
-            "modes": out}
+            "lattice": {"workload": RESIDUAL_WORKLOAD.format(last=args.residual_steps - 1, tol=args.residual_tol,
+                                                             cap=args.residual_cap),
+                        "modes": _residual_modes(lattice, args, device, net, args.residual_steps, 0)},
+            "held_out_piles": {"workload": PILES_WORKLOAD.format(bodies=piles.num_bodies, tol=args.residual_tol,
+                                                                 cap=args.residual_cap),
+                               "modes": _residual_modes(piles, args, device, net, 80, 20)}}
 
 
 # ------------------------------------------------------------------------------ GPU arm
@@ -321,10 +357,20 @@ def gpu_arm(args):
     mode = capi.SOLVER_PGS if args.solver == "pgs" else capi.SOLVER_JACOBI
     cfg = b3Config(solver_mode=mode, solver_iterations=args.iterations, use_cuda_graph=True,
                    pgs_interleave=args.solver == "pgs" and args.row_order == "interleaved")
+    stress = args.workload == "stress"
+    if stress:
+        cfg.residual_tol = 1e-4
+        cfg.warm_start = capi.WARM_PERSISTENT_LEARNED
     np_, bp, pl = scenes.load_scene(scene, cfg, device=local)
+    if stress:
+        from bullet3_gb300.warmstart import DEFAULT_WEIGHTS, WarmStartMLP
+        net = WarmStartMLP.load(DEFAULT_WEIGHTS, device=local)
+        pl.setWarmStartModel(net)
     h = np_.world.handle
     N = scene.num_bodies
     dt = 1.0 / 60.0
+    for _ in range(args.settle):
+        pl.stepSimulation(dt)
     for _ in range(max(3, args.warmup)):
         pl.stepSimulation(dt)
     pl.synchronize()
@@ -337,8 +383,9 @@ def gpu_arm(args):
     clocks.start()
     # keep the GPU stepping while the clock sampler starts (its samples then cover load only),
     # then put the warm-up state back
+    # (the pour is timed as one long run from its warm-up state: no pre-roll there)
     t_roll = time.perf_counter()
-    while time.perf_counter() - t_roll < 1.0:
+    while not stress and time.perf_counter() - t_roll < 1.0:
         for _ in range(10):
             pl.stepSimulation(dt)
         pl.synchronize()

@@ -404,7 +404,13 @@ __global__ void __launch_bounds__(BP_THREADS) k_unpack_pairs(const uint64_t* __r
             int ta = cols[ca].shapeType;
             int tb = cols[cb].shapeType;
             t = pair_type(ta, tb);
-            if (t == PT_HULL_HULL && col_small[ca] && col_small[cb]) t = PT_HULL_HULL_SMALL;
+            if (t == PT_HULL_HULL) {
+                const int sa = col_small[ca], sb = col_small[cb];
+                if (sa && sb) {
+                    const int axes = ((sa >> 1) & 0x7fff) + ((sb >> 1) & 0x7fff) + (sa >> 16) * (sb >> 16);
+                    if (axes <= B3G_SMALL_PAIR_AXES) t = PT_HULL_HULL_SMALL;
+                }
+            }
         }
         unsigned peers = __match_any_sync(0xffffffffu, t);
         int leader = __ffs(peers) - 1;

@@ -463,22 +463,27 @@ __global__ void __launch_bounds__(HH_WARPS * 32) k_hull_hull(NPArgs a, int max_p
         bool separated = false;
         const b3gFloat4* vA = &a.verts[hA.vertexOffset];
         const b3gFloat4* vB = &a.verts[hB.vertexOffset];
-        for (int k = lane; k < naxes; k += 32) {
+        // 32 axes per round; a separating axis found by any lane ends the test (the pair has no
+        // contact whichever axis separates it, so the reference's early return gives the same result)
+        for (int k0 = 0; k0 < naxes; k0 += 32) {
+            const int k = k0 + lane;
             v3 axis;
-            if (!sat_axis(k, hA, hB, a.faces, a.edges, qA, qB, deltaC2, axis)) continue;
-            float min0, max0, min1, max1;
-            project(vA, hA.numVertices, posA, qA, axis, min0, max0);
-            project(vB, hB.numVertices, posB, qB, axis, min1, max1);
-            if (max0 < min1 || max1 < min0) {
-                separated = true;
-                continue;
+            if (k < naxes && sat_axis(k, hA, hB, a.faces, a.edges, qA, qB, deltaC2, axis)) {
+                float min0, max0, min1, max1;
+                project(vA, hA.numVertices, posA, qA, axis, min0, max0);
+                project(vB, hB.numVertices, posB, qB, axis, min1, max1);
+                if (max0 < min1 || max1 < min0) {
+                    separated = true;
+                } else {
+                    float d0 = max0 - min1, d1 = max1 - min0;
+                    float depth = d0 < d1 ? d0 : d1;
+                    if (depth < best.d || (depth == best.d && k < best.idx)) {
+                        best.d = depth;
+                        best.idx = k;
+                    }
+                }
             }
-            float d0 = max0 - min1, d1 = max1 - min0;
-            float depth = d0 < d1 ? d0 : d1;
-            if (depth < best.d || (depth == best.d && k < best.idx)) {
-                best.d = depth;
-                best.idx = k;
-            }
+            if (__any_sync(0xffffffffu, separated)) break;
         }
         if (__any_sync(0xffffffffu, separated)) continue;
         best = warp_argmin(best);

@@ -7,6 +7,7 @@
 // The step enqueues every stage on one stream with no host synchronisation; device-side
 // counts drive all kernels (fixed launch shapes), so the whole step can be captured once
 // as a CUDA graph and replayed.
+#include <cuda_profiler_api.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -659,7 +660,9 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
         int small = 1;
         for (int f = 0; f < hull.numFaces; f++)
             if (h->faces[hull.faceOffset + f].numIndices > B3G_SMALL_FACE_VERTS) small = 0;
-        col_small[c] = small;
+        // small-faced hulls carry their SAT axis counts (faces, unique edges) for the per-pair choice
+        col_small[c] = small ? (1 | (std::min(hull.numFaces, 0x7fff) << 1) | (std::min(hull.numUniqueEdges, 0x7fff) << 16))
+                             : 0;
     }
     CUDA_TRY(cudaMemcpyAsync(d.col_small, col_small.data(), sizeof(int) * d.num_collidables, cudaMemcpyHostToDevice,
                              s));
@@ -903,6 +906,11 @@ extern "C" b3gStatus b3g_autotune(b3g_handle h, float dt, int repeats, b3gTuning
     res.candidates_timed = timed;
     h->tuning = res;
     if (out) *out = res;
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_profiler_range(int on) {
+    CUDA_TRY(on ? cudaProfilerStart() : cudaProfilerStop());
     return B3G_OK;
 }
 

@@ -17,6 +17,9 @@ struct Model;
 
 // hull-hull pairs whose faces all have at most this many vertices take the thread-per-pair path
 #define B3G_SMALL_FACE_VERTS 8
+// ... and whose pair has at most this many SAT axes (faces of both + edge pairs); pairs with more
+// take the warp-per-pair path, whose lanes split the axes
+#define B3G_SMALL_PAIR_AXES 64
 
 enum PairType { PT_HULL_HULL = 0, PT_PLANE_HULL = 1, PT_SPHERE_HULL = 2, PT_SPHERE_SPHERE = 3, PT_PLANE_SPHERE = 4,
                 PT_HULL_HULL_SMALL = 5, PT_COUNT = 6 };
@@ -76,7 +79,8 @@ struct DeviceState {
     b3gFloat4* vertices = nullptr;
     b3gFloat4* edges = nullptr;
     int* dyn_slot = nullptr;      // body -> dynamic slot or -1
-    int* col_small = nullptr;     // per collidable: 1 = hull whose faces all have <= B3G_SMALL_FACE_VERTS vertices
+    int* col_small = nullptr;     // per collidable: 0, or for a hull whose faces all have <= B3G_SMALL_FACE_VERTS
+                                  // vertices: 1 | faces << 1 | unique edges << 16
     int* large_list = nullptr;    // static bodies (large proxies), grouped by scene
     // independent scenes (b3g_set_scene_offsets); nullptr / 1 when the world is one scene
     int num_scenes = 1;

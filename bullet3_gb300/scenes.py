@@ -31,6 +31,7 @@ class Scene:
     angvel: np.ndarray = None
     cell: float = 0.0                                 # grid cell size (0 = automatic)
     name: str = ""
+    pairs_per_body: int = 0                           # pair capacity hint (0 = the library default)
 
     @property
     def num_bodies(self) -> int:
@@ -253,6 +254,46 @@ def static_field(n_static=2000, n_dynamic=6000, extent=100.0, seed=0, plane=True
     return sc
 
 
+def stress_container(n=1048576, width=128.0, depth=128.0, height=512.0, seed=0, cell_factor=2.0) -> Scene:
+    """The collision-at-scale shape mix poured into a static container: 50% boxes (half extents
+    U[0.2, 0.6]), 25% spheres (r U[0.2, 0.5]), 25% hulls of 12-32 N(0, 0.4^2) points, uniform random
+    orientations, zero velocity, x in U[1, width-1], z in U[1, depth-1], y in U[0, height]; the
+    container is five static planes (floor y = 0 and the walls x = 0, x = width, z = 0, z = depth,
+    normals pointing inwards).  Grid cell = cell_factor x the largest AABB extent."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sc = Scene(name=f"stress_{n}")
+    walls = [((0.0, 1.0, 0.0), 0.0), ((1.0, 0.0, 0.0), 0.0), ((-1.0, 0.0, 0.0), -width), ((0.0, 0.0, 1.0), 0.0),
+             ((0.0, 0.0, -1.0), -depth)]
+    for nrm, c in walls:  # plane n . p = c
+        sc.shapes.append({"type": "plane", "normal": nrm, "constant": c})
+    kinds = rng.permutation(np.repeat([0, 1, 2], [n // 2, n // 4, n - n // 2 - n // 4]))
+    shapes = list(range(len(walls)))
+    max_ext = 0.0
+    for k in kinds:
+        if k == 0:
+            h = rng.uniform(0.2, 0.6, 3).astype(np.float32)
+            sc.shapes.append({"type": "hull", "verts": box_vertices(*h)})
+            max_ext = max(max_ext, 2 * float(h.max()))
+        elif k == 1:
+            r = float(rng.uniform(0.2, 0.5))
+            sc.shapes.append({"type": "sphere", "radius": r})
+            max_ext = max(max_ext, 2 * r)
+        else:
+            pts = (rng.standard_normal((int(rng.integers(12, 33)), 3)) * 0.4).astype(np.float32)
+            sc.shapes.append({"type": "hull", "verts": pts})
+            max_ext = max(max_ext, float((pts.max(0) - pts.min(0)).max()))
+        shapes.append(len(sc.shapes) - 1)
+    pos = np.stack([rng.uniform(1.0, width - 1.0, n), rng.uniform(0.0, height, n), rng.uniform(1.0, depth - 1.0, n)], 1)
+    nw = len(walls)
+    sc.body_shape = np.array(shapes, np.int32)
+    sc.mass = np.concatenate([np.zeros(nw), np.ones(n)]).astype(np.float32)
+    sc.pos = np.vstack([np.zeros((nw, 3)), pos]).astype(np.float32)
+    sc.orn = np.vstack([np.tile([0, 0, 0, 1.0], (nw, 1)), random_quaternions(rng, n)]).astype(np.float32)
+    sc.cell = cell_factor * max_ext
+    sc.pairs_per_body = 48  # the settled pour reaches ~24 overlapping AABBs per body
+    return sc
+
+
 def load_scene(scene: Scene, config=None, device: int = 0, upload: bool = True):
     """Register a Scene through the reference-style API; returns (narrowphase, broadphase, pipeline)."""
     from .pipeline import b3Config, b3GpuGridBroadphase, b3GpuNarrowPhase, b3GpuRigidBodyPipeline
@@ -262,6 +303,8 @@ def load_scene(scene: Scene, config=None, device: int = 0, upload: bool = True):
     config.m_maxConvexShapes = max(config.m_maxConvexShapes, len(scene.shapes))
     if scene.cell and not config.grid_cell_size:
         config.grid_cell_size = scene.cell
+    if scene.pairs_per_body and not config.m_maxBroadphasePairs:
+        config.m_maxBroadphasePairs = scene.pairs_per_body * scene.num_bodies
     np_ = b3GpuNarrowPhase(config, device)
     bp = b3GpuGridBroadphase()
     pl = b3GpuRigidBodyPipeline(np_, bp, None, config)

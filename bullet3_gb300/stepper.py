@@ -3,13 +3,18 @@
 Meant for running the pipeline under an external profiler (ncu) or by hand: nothing but the
 scene upload, the warm-up steps and the measured steps touch the GPU.
 
-    python -m bullet3_gb300.stepper [--workload pile|lattice|batched|mixed] [--steps K] [--warmup W]
-                                    [--solver pgs|jacobi] [--iterations I] [--autotune]
+    python -m bullet3_gb300.stepper [--workload pile|lattice|batched|mixed|stress] [--settle S] [--steps K]
+                                    [--warmup W] [--solver pgs|jacobi] [--iterations I] [--autotune]
+                                    [--profile-range]
+
+--profile-range brackets the K measured steps with b3g_profiler_range, for a profiler started
+with profiling off (ncu --profile-from-start off); --settle steps first, untimed.
 
   pile     262,144 unit boxes resting in 64x64 columns on a plane (the settled 64^3 lattice)
   lattice  the 64^3 lattice (spacing 1.1, jitter 0.05) falling onto the plane from rest
   batched  4,096 independent box/sphere piles, each on its own plane, through per-scene offsets
   mixed    131,072 boxes, spheres and Gaussian hulls in a 64^3 box, random orientations, N(0,1) velocities
+  stress   1,048,576 bodies of the same mix poured into a 5-plane container from heights U[0, 512]
 """
 from __future__ import annotations
 
@@ -30,12 +35,16 @@ def make(workload: str, n: int = 64):
         return scenes.batched_piles(4096, seed=0, separate=True)
     if workload == "mixed":
         return scenes.mixed_scene(131072, extent=64.0, seed=0)
+    if workload == "stress":
+        return scenes.stress_container(1048576, seed=0)
     raise ValueError(workload)
 
 
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("--workload", choices=["pile", "lattice", "batched", "mixed"], default="pile")
+    p.add_argument("--workload", choices=["pile", "lattice", "batched", "mixed", "stress"], default="pile")
+    p.add_argument("--settle", type=int, default=0)
+    p.add_argument("--profile-range", action="store_true")
     p.add_argument("--nx", type=int, default=64)
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
@@ -50,15 +59,21 @@ def main(argv=None):
                    use_cuda_graph=not a.no_graph)
     np_, bp, pl = scenes.load_scene(sc, cfg)
     dt = 1.0 / 60.0
+    for _ in range(a.settle):
+        pl.stepSimulation(dt)
     for _ in range(a.warmup):
         pl.stepSimulation(dt)
     pl.synchronize()
     tuning = pl.autotune(dt) if a.autotune else None
+    if a.profile_range:
+        capi.call("b3g_profiler_range", capi.C.c_int(1))
     t0 = time.perf_counter()
     for _ in range(a.steps):
         pl.stepSimulation(dt)
     pl.synchronize()
     secs = time.perf_counter() - t0
+    if a.profile_range:
+        capi.call("b3g_profiler_range", capi.C.c_int(0))
     st = pl.stats()
     print(json.dumps({"workload": a.workload, "bodies": sc.num_bodies, "steps": a.steps,
                       "host_ms_per_step": 1000 * secs / max(a.steps, 1), "pairs": st.num_pairs,

@@ -206,6 +206,9 @@ typedef struct b3gTuning {
 } b3gTuning;
 b3gStatus b3g_autotune(b3g_handle h, float dt, int repeats, b3gTuning* out);
 b3gStatus b3g_get_tuning(b3g_handle h, b3gTuning* out);
+/* Marks the start (on = 1) and end (0) of the region an external profiler started with profiling
+ * off should capture (cudaProfilerStart / cudaProfilerStop; no reference counterpart). */
+b3gStatus b3g_profiler_range(int on);
 
 /* ------------------------------------------------------------------ the step */
 /* b3GpuRigidBodyPipeline::stepSimulation (b3GpuRigidBodyPipeline.cpp:221-463): AABBs, pairs,
