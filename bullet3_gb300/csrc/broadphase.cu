@@ -232,6 +232,41 @@ __device__ __forceinline__ int bound_search(const float* v, int lo, int hi, floa
     return lo;
 }
 
+// Pairs of dynamic body i with the static proxies of its scene: the unbounded ones [l0, l1) of
+// large_list brute force, the finite ones through the sweep-and-prune window.
+__device__ __forceinline__ void static_pairs(const float4* __restrict__ A, uint32_t i, const float4& amin,
+                                             const float4& amax, const int* __restrict__ large_list, int l0, int l1,
+                                             const SapView& sap, int si, int body_bits, PairEmitter& em,
+                                             uint64_t* __restrict__ out, int* __restrict__ counter, int cap,
+                                             unsigned int* __restrict__ status) {
+    for (int l = l0; l < l1; l++) {
+        uint32_t j = (uint32_t)__ldg(&large_list[l]);
+        float4 bmin = __ldg(&A[2 * j]), bmax = __ldg(&A[2 * j + 1]);
+        if (overlap(amin, amax, bmin, bmax)) {
+            uint32_t a = i < j ? i : j, b = i < j ? j : i;
+            em.push(((uint64_t)a << body_bits) | b, out, counter, cap, status);
+        }
+    }
+    if (sap.n > 0) {
+        int q0 = __ldg(&sap.off[si]), q1 = __ldg(&sap.off[si + 1]);
+        const float e = __ldg(&sap.ext[si]);
+        if (q0 < q1 && e <= 3.4e38f) {
+            // window of mins in [min - extent, max]; the lower end rounded down so that no
+            // proxy reaching this body is left out
+            q0 = bound_search(sap.mins, q0, q1, __fsub_rd(axis_of(amin, sap.axis), e), false);
+            q1 = bound_search(sap.mins, q0, q1, axis_of(amax, sap.axis), true);
+        }
+        for (int q = q0; q < q1; q++) {
+            uint32_t j = (uint32_t)__ldg(&sap.sorted[q]);
+            float4 bmin = __ldg(&A[2 * j]), bmax = __ldg(&A[2 * j + 1]);
+            if (overlap(amin, amax, bmin, bmax)) {
+                uint32_t a = i < j ? i : j, b = i < j ? j : i;
+                em.push(((uint64_t)a << body_bits) | b, out, counter, cap, status);
+            }
+        }
+    }
+}
+
 // SCENES: bodies carry a scene index (b3g_set_scene_offsets); cells are shifted per scene, pairs
 // need equal scenes and each body tests only its own scene's range of the large list.
 template <bool SCENES>
@@ -286,32 +321,7 @@ __device__ __forceinline__ void find_pairs_body(const b3gAabb* __restrict__ aabb
                                 em.push(((uint64_t)i << body_bits) | j, out, counter, cap, status);
                         }
                     }
-            for (int l = l0; l < l1; l++) {
-                uint32_t j = (uint32_t)__ldg(&large_list[l]);
-                float4 bmin = __ldg(&A[2 * j]), bmax = __ldg(&A[2 * j + 1]);
-                if (overlap(amin, amax, bmin, bmax)) {
-                    uint32_t a = i < j ? i : j, b = i < j ? j : i;
-                    em.push(((uint64_t)a << body_bits) | b, out, counter, cap, status);
-                }
-            }
-            if (sap.n > 0) {
-                int q0 = __ldg(&sap.off[si]), q1 = __ldg(&sap.off[si + 1]);
-                const float e = __ldg(&sap.ext[si]);
-                if (q0 < q1 && e <= 3.4e38f) {
-                    // window of mins in [min - extent, max]; the lower end rounded down so that no
-                    // proxy reaching this body is left out
-                    q0 = bound_search(sap.mins, q0, q1, __fsub_rd(axis_of(amin, sap.axis), e), false);
-                    q1 = bound_search(sap.mins, q0, q1, axis_of(amax, sap.axis), true);
-                }
-                for (int q = q0; q < q1; q++) {
-                    uint32_t j = (uint32_t)__ldg(&sap.sorted[q]);
-                    float4 bmin = __ldg(&A[2 * j]), bmax = __ldg(&A[2 * j + 1]);
-                    if (overlap(amin, amax, bmin, bmax)) {
-                        uint32_t a = i < j ? i : j, b = i < j ? j : i;
-                        em.push(((uint64_t)a << body_bits) | b, out, counter, cap, status);
-                    }
-                }
-            }
+            static_pairs(A, i, amin, amax, large_list, l0, l1, sap, si, body_bits, em, out, counter, cap, status);
         }
     }
     // warp-aggregated reservation of the remaining buffered pairs
@@ -347,14 +357,159 @@ __global__ void __launch_bounds__(BP_THREADS) k_find_pairs(const b3gAabb* __rest
                            cap, status);
 }
 
+// Warp-cooperative form of the same search.  A warp takes 32 consecutive dynamic bodies in cell
+// order, which mostly share a cell and so the same 27 neighbour cells.  For each neighbour offset
+// the lanes are grouped by target cell; the warp streams each distinct cell's members through
+// shared memory 32 at a time (coalesced float4 AABB loads, once per group instead of once per
+// lane), and every lane of the group tests its own body against the staged members.  The pair
+// set is the thread-per-body one: same candidates, same inclusive test, j > i.
+static constexpr int BP_WARPS = BP_THREADS / 32;
+static constexpr int BP_COOP_MAX_CELLS = 2;  // distinct own cells in a warp for the cooperative scan
+
+template <bool SCENES>
+__device__ __forceinline__ void find_pairs_warp(const b3gAabb* __restrict__ aabbs, const uint32_t* __restrict__ keys,
+                                                const uint32_t* __restrict__ vals,
+                                                const uint32_t* __restrict__ cell_start, int n_dyn,
+                                                const int* __restrict__ large_list, int n_large,
+                                                const int* __restrict__ body_scene,
+                                                const int* __restrict__ large_off, const SapView sap, float inv_cell,
+                                                int bits, int body_bits, uint64_t* __restrict__ out,
+                                                int* __restrict__ counter, int cap, unsigned int* __restrict__ status) {
+    __shared__ float4 s_min[BP_WARPS][32], s_max[BP_WARPS][32];
+    __shared__ uint32_t s_j[BP_WARPS][32];
+    __shared__ int s_sc[BP_WARPS][32];
+    const int mask = (1 << bits) - 1;
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const float4* A = reinterpret_cast<const float4*>(aabbs);
+    const int nwarps = gridDim.x * BP_WARPS;
+    PairEmitter em;
+    em.cnt = 0;
+    for (int base = (blockIdx.x * BP_WARPS + w) * 32; base < n_dyn; base += nwarps * 32) {
+        const int p = base + lane;
+        const bool live = p < n_dyn;
+        uint32_t i = 0;
+        float4 amin = make_float4(0, 0, 0, 0), amax = amin;
+        int gx = 0, gy = 0, gz = 0, si = 0, l0 = 0, l1 = n_large;
+        if (live) {
+            i = vals[p];
+            amin = __ldg(&A[2 * i]);
+            amax = __ldg(&A[2 * i + 1]);
+            const float cx = (amin.x + amax.x) * 0.5f, cy = (amin.y + amax.y) * 0.5f, cz = (amin.z + amax.z) * 0.5f;
+            gx = (int)floorf(cx * inv_cell);
+            gy = (int)floorf(cy * inv_cell);
+            gz = (int)floorf(cz * inv_cell);
+            if (SCENES) {
+                si = __ldg(&body_scene[i]);
+                CellShift sh = scene_shift(si, bits);
+                gx += sh.x; gy += sh.y; gz += sh.z;
+                l0 = __ldg(&large_off[si]);
+                l1 = __ldg(&large_off[si + 1]);
+            }
+        }
+        // cooperative streaming pays off where the warp's bodies crowd into few cells; a warp
+        // spread over many sparse cells scans per lane instead (same candidates either way)
+        const uint32_t h_own = live ? cell_hash(gx, gy, gz, bits, mask) : 0xffffffffu;
+        const unsigned own_peers = __match_any_sync(0xffffffffu, h_own);
+        const int distinct = __popc(__ballot_sync(0xffffffffu, live && lane == __ffs(own_peers) - 1));
+        if (distinct > BP_COOP_MAX_CELLS) {
+            if (live)
+                for (int dz = -1; dz <= 1; dz++)
+                    for (int dy = -1; dy <= 1; dy++)
+                        for (int dx = -1; dx <= 1; dx++) {
+                            const uint32_t hh = cell_hash(gx + dx, gy + dy, gz + dz, bits, mask);
+                            const uint32_t s0 = __ldg(&cell_start[hh]);
+                            if (s0 >= (uint32_t)n_dyn) continue;
+                            if (__ldg(&keys[s0]) != hh) continue;
+                            if (s0 > 0 && __ldg(&keys[s0 - 1]) == hh) continue;
+                            for (uint32_t q = s0; q < (uint32_t)n_dyn; q++) {
+                                if (__ldg(&keys[q]) != hh) break;
+                                const uint32_t j = __ldg(&vals[q]);
+                                if (j <= i) continue;
+                                if (SCENES && __ldg(&body_scene[j]) != si) continue;
+                                if (overlap(amin, amax, __ldg(&A[2 * j]), __ldg(&A[2 * j + 1])))
+                                    em.push(((uint64_t)i << body_bits) | j, out, counter, cap, status);
+                            }
+                        }
+        } else
+        for (int off = 0; off < 27; off++) {
+            const int dx = off % 3 - 1, dy = (off / 3) % 3 - 1, dz = off / 9 - 1;
+            // this lane's target cell and its run start (validated against the sorted keys)
+            uint32_t h = 0xffffffffu, st = 0;
+            if (live) {
+                const uint32_t hh = cell_hash(gx + dx, gy + dy, gz + dz, bits, mask);
+                const uint32_t s0 = __ldg(&cell_start[hh]);
+                if (s0 < (uint32_t)n_dyn && __ldg(&keys[s0]) == hh && !(s0 > 0 && __ldg(&keys[s0 - 1]) == hh)) {
+                    h = hh;
+                    st = s0;
+                }
+            }
+            unsigned pending = __ballot_sync(0xffffffffu, h != 0xffffffffu);
+            while (pending) {
+                const int leader = __ffs(pending) - 1;
+                const uint32_t H = __shfl_sync(0xffffffffu, h, leader);
+                const uint32_t S = __shfl_sync(0xffffffffu, st, leader);
+                const bool mine = h == H;
+                pending &= ~__ballot_sync(0xffffffffu, mine);
+                // stream the cell's members through shared memory, 32 at a time
+                for (uint32_t q0 = S;; q0 += 32) {
+                    const uint32_t q = q0 + lane;
+                    const bool in = q < (uint32_t)n_dyn && __ldg(&keys[q]) == H;
+                    const unsigned inmask = __ballot_sync(0xffffffffu, in);
+                    // members are contiguous from S: the run ends at the first lane outside it
+                    const int cnt = __ffs(~inmask) ? __ffs(~inmask) - 1 : 32;
+                    if (lane < cnt) {
+                        const uint32_t j = __ldg(&vals[q]);
+                        s_j[w][lane] = j;
+                        s_min[w][lane] = __ldg(&A[2 * j]);
+                        s_max[w][lane] = __ldg(&A[2 * j + 1]);
+                        if (SCENES) s_sc[w][lane] = __ldg(&body_scene[j]);
+                    }
+                    __syncwarp();
+                    if (mine) {
+                        for (int c = 0; c < cnt; c++) {
+                            const uint32_t j = s_j[w][c];
+                            if (j <= i) continue;
+                            if (SCENES && s_sc[w][c] != si) continue;
+                            if (overlap(amin, amax, s_min[w][c], s_max[w][c]))
+                                em.push(((uint64_t)i << body_bits) | j, out, counter, cap, status);
+                        }
+                    }
+                    __syncwarp();
+                    if (cnt < 32) break;
+                }
+            }
+        }
+        if (live) static_pairs(A, i, amin, amax, large_list, l0, l1, sap, si, body_bits, em, out, counter, cap, status);
+    }
+    // warp-aggregated reservation of the remaining buffered pairs
+    int c = em.cnt;
+    int incl = c;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    int total = __shfl_sync(0xffffffffu, incl, 31);
+    int wbase = 0;
+    if (lane == 31 && total > 0) wbase = atomicAdd(counter, total);
+    wbase = __shfl_sync(0xffffffffu, wbase, 31);
+    int my = wbase + incl - c;
+    for (int k = 0; k < c; k++) {
+        if (my + k < cap)
+            out[my + k] = em.buf[k];
+        else
+            atomicOr(status, B3G_FLAG_PAIR_OVERFLOW);
+    }
+}
+
 // the world's pair kernel: large (unbounded) list, sweep and prune over finite statics, scenes
 template <bool SCENES>
-__global__ void __launch_bounds__(BP_THREADS) k_find_pairs_world(
+__global__ void __launch_bounds__(BP_THREADS, 8) k_find_pairs_world(
     const b3gAabb* __restrict__ aabbs, const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
     const uint32_t* __restrict__ cell_start, int n_dyn, const int* __restrict__ large_list, int n_large,
     const int* __restrict__ body_scene, const int* __restrict__ large_off, const SapView sap, float inv_cell, int bits,
     int body_bits, uint64_t* __restrict__ out, int* __restrict__ counter, int cap, unsigned int* __restrict__ status) {
-    find_pairs_body<SCENES>(aabbs, keys, vals, cell_start, n_dyn, large_list, n_large, body_scene, large_off, sap,
+    find_pairs_warp<SCENES>(aabbs, keys, vals, cell_start, n_dyn, large_list, n_large, body_scene, large_off, sap,
                             inv_cell, bits, body_bits, out, counter, cap, status);
 }
 
