@@ -192,10 +192,17 @@ def solver_traffic():
     return None
 
 
-def make_scene(args):
+def scene_seed(args, rank: int) -> int:
+    """Seed of a rank's scene set: under torchrun the batched workload gives every rank its own
+    scenes (seed = rank: independent scenes, no exchange between ranks, per-GPU work fixed); the
+    single-scene workloads run the same scene on every rank (replicas)."""
+    return rank if args.workload == "batched" else 0
+
+
+def make_scene(args, rank: int = 0):
     from bullet3_gb300 import scenes
     if args.workload == "batched":
-        return scenes.batched_piles(args.scenes, seed=0, separate=True)
+        return scenes.batched_piles(args.scenes, seed=scene_seed(args, rank), separate=True)
     if args.workload == "stress":
         return scenes.stress_container(1048576, seed=0)
     return scenes.box_stack(args.nx, 64, args.nx, seed=0)
@@ -353,7 +360,7 @@ def gpu_arm(args):
     from bullet3_gb300 import capi, scenes
     from bullet3_gb300.pipeline import b3Config
     capi.load()
-    scene = make_scene(args)
+    scene = make_scene(args, rank)
     mode = capi.SOLVER_PGS if args.solver == "pgs" else capi.SOLVER_JACOBI
     cfg = b3Config(solver_mode=mode, solver_iterations=args.iterations, use_cuda_graph=True,
                    pgs_interleave=args.solver == "pgs" and args.row_order == "interleaved")
@@ -487,7 +494,9 @@ def gpu_arm(args):
                 "config": {"workload": workload_name(args, scene), "bodies": N, "solver": args.solver,
                            "iterations": args.iterations,
                            "row_order": args.row_order,
-                           "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                           "parallelism": (f"{world} ranks, own scene set each (seed = rank)"
+                                           if world > 1 and args.workload == "batched"
+                                           else f"replicas x{world}" if world > 1 else "single GPU"),
                            "l2": "inputs larger than L2 (constraint rows and pair buffers exceed 129 MB)",
                            "pairs": P_, "manifolds": C_, "contact_points": st.num_points, "colors": st.num_colors,
                            "tuning": tuning},
