@@ -49,6 +49,7 @@ struct SolverArgs {
     float2* inv_mass;         // invMass A, B
     int4* hdr_ord;            // PGS: colour-ordered copies
     float4* inv_mass_ord;     // (invMass A, invMass B, 0, 0): 16 B so tiles copy in bulk
+    float4* inertia_ord;      // PGS: per ordered manifold both bodies' inverse world inertia rows (6 float4)
     float4* dv;               // per body: [2b] lin, [2b+1] ang (PGS, and Jacobi averaged delta)
     float4* dv_sum;           // Jacobi: per body sum of split deltas from the last averaging
     float4* split;            // Jacobi: per manifold 4 float4: A lin, A ang, B lin, B ang
@@ -607,6 +608,16 @@ __device__ __forceinline__ void store_dv_local(const SolverArgs& a, float* s_dv,
 }
 // World inverse inertia of an owned body from shared memory (9 floats, staged once per solve),
 // of any other body from global memory.
+// rows written earlier in the same launch: read through L2, never the non-coherent path
+__device__ __forceinline__ b3gMat3 ld_mat_cg(const float4* q) {
+    b3gMat3 r;
+    const float4 x = __ldcg(q), y = __ldcg(q + 1), z = __ldcg(q + 2);
+    r.row[0] = b3gFloat4{x.x, x.y, x.z, x.w};
+    r.row[1] = b3gFloat4{y.x, y.y, y.z, y.w};
+    r.row[2] = b3gFloat4{z.x, z.y, z.z, z.w};
+    return r;
+}
+
 __device__ __forceinline__ b3gMat3 load_inertia_local(const SolverArgs& a, const float* s_inv, int body, int local) {
     if (local >= 0) {
         const float* p = s_inv + 9 * local;
@@ -652,6 +663,7 @@ __device__ __forceinline__ void prefetch_records_l2(const SolverArgs& a, int k0,
     bulk_prefetch_l2(a.hdr_ord + k0, 16u * c);
     bulk_prefetch_l2(a.inv_mass_ord + k0, 16u * c);
     bulk_prefetch_l2(a.sp_ord.nf + k0, 16u * c);
+    bulk_prefetch_l2(a.inertia_ord + 6 * (size_t)k0, 96u * c);
     bulk_prefetch_l2(a.sp_ord.rel1 + 4 * (size_t)k0, 64u * c);
     bulk_prefetch_l2(a.sp_ord.rel2 + 4 * (size_t)k0, 64u * c);
     bulk_prefetch_l2(a.sp_ord.imp + 4 * (size_t)k0, 64u * c);
@@ -889,6 +901,15 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
         a.hdr_ord[k] = make_int4(h.x, h.y, h.z, w);
         a.inv_mass_ord[k] = make_float4(im.x, im.y, 0.f, 0.f);
         a.sp_ord.nf[k] = __ldcg(&a.sp.nf[m]);
+        // both bodies' inverse inertias next to the record: the solve reads them by position
+        // instead of gathering them through the header's body indices
+        {
+            const float4* IA = reinterpret_cast<const float4*>(&a.inertias[h.x].invInertiaWorld);
+            const float4* IB = reinterpret_cast<const float4*>(&a.inertias[h.y].invInertiaWorld);
+            float4* o = a.inertia_ord + 6 * (size_t)k;
+            o[0] = __ldg(IA); o[1] = __ldg(IA + 1); o[2] = __ldg(IA + 2);
+            o[3] = __ldg(IB); o[4] = __ldg(IB + 1); o[5] = __ldg(IB + 2);
+        }
     }
     if (PARTS && a.tile_R > 0) fence_proxy_async();  // the ordered records are read by bulk copies below
     if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
@@ -1067,8 +1088,10 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_solve_pgs(SolverArgs a) {
                     v3 dlA = mk3(0, 0, 0), daA = mk3(0, 0, 0), dlB = mk3(0, 0, 0), daB = mk3(0, 0, 0);
                     if (im.x != 0.f) load_dv_local(a, s_dv, h.x, la, dlA, daA);
                     if (im.y != 0.f) load_dv_local(a, s_dv, h.y, lb, dlB, daB);
-                    const b3gMat3 IA = load_inertia_local(a, s_inv, h.x, la);
-                    const b3gMat3 IB = load_inertia_local(a, s_inv, h.y, lb);
+                    const b3gMat3 IA = la >= 0 ? load_inertia_local(a, s_inv, h.x, la)
+                                               : ld_mat_cg(a.inertia_ord + 6 * (size_t)k);
+                    const b3gMat3 IB = lb >= 0 ? load_inertia_local(a, s_inv, h.y, lb)
+                                               : ld_mat_cg(a.inertia_ord + 6 * (size_t)k + 3);
                     solve_manifold<true, false>(a.sp_ord, k, a.sp_ord.imp + 4 * (size_t)k, pass, h, im.x, im.y, IA,
                                                 IB, dlA, daA, dlB, daB, res_d, res_l);
                     if (im.x != 0.f) store_dv_local(a, s_dv, h.x, la, dlA, daA);
@@ -1393,6 +1416,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     a.inv_mass = d.manifold_inv_mass;
     a.hdr_ord = d.manifold_hdr_ord;
     a.inv_mass_ord = d.manifold_inv_mass_ord;
+    a.inertia_ord = d.inertia_ord;
     a.dv = d.dv;
     a.dv_sum = d.dv_sum;
     a.split = d.split_dv;

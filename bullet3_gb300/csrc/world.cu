@@ -582,6 +582,7 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     TRY(dalloc(h, &d.manifold_group, d.max_contacts));
     TRY(dalloc(h, &d.group_counts, 3 * ((size_t)sms * B3G_PGS_MAX_BLOCKS_PER_SM * 64 + 64 + 2)));
     TRY(dalloc(h, &d.manifold_inv_mass_ord, d.max_contacts));
+    TRY(dalloc(h, &d.inertia_ord, 6 * (size_t)d.max_contacts));
     TRY(dalloc(h, &d.manifold_color, d.max_contacts));
     TRY(dalloc(h, &d.color_order, d.max_contacts));
     TRY(dalloc(h, &d.color_offsets, 4 * (B3G_MAX_COLORS + 2)));  // offsets, fill, remaining, cursors

@@ -116,6 +116,7 @@ struct DeviceState {
     SolverPoints sp_ord;                   // PGS: the same records in colour order
     int4* manifold_hdr_ord = nullptr;
     float4* manifold_inv_mass_ord = nullptr;  // (invMass A, invMass B, 0, 0)
+    float4* inertia_ord = nullptr;         // PGS: per ordered manifold, A's then B's inverse world inertia rows (6)
     const uint32_t* cell_sorted_bodies = nullptr;  // set by the broadphase: dynamic bodies in cell order
     int* body_slot = nullptr;              // body -> position in cell order (PGS partitions)
     int* manifold_group = nullptr;         // PGS processing group of each manifold
