@@ -1,0 +1,86 @@
+"""The C++ drop-in: a program written against the reference's class names (include/b3g_compat.h)
+is compiled with g++, linked against libb3gpu.so, and steps a box pile on the GPU through the C
+ABI.  Bar: it builds, runs without a b3Error, the boxes come to rest on the plane, and the
+broadphase/narrowphase getters report the pairs and contacts of the settled pile."""
+import shutil
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from conftest import ROOT
+
+pytestmark = pytest.mark.gpu
+
+PROGRAM = r'''
+#include <cmath>
+#include <cstdio>
+#include <vector>
+#include "b3g_compat.h"
+using namespace b3g_compat;
+
+int main() {
+    b3Config config;
+    config.m_maxConvexBodies = 1000;
+    b3GpuNarrowPhase* np = new b3GpuNarrowPhase(0, config);        // was (ctx, device, queue, config)
+    b3GpuGridBroadphase* bp = new b3GpuGridBroadphase();
+    b3GpuRigidBodyPipeline* rbp = new b3GpuRigidBodyPipeline(np, bp, nullptr, config);
+    float box[8 * 3];
+    for (int i = 0; i < 8; i++) {
+        box[3 * i + 0] = (i & 4) ? 0.5f : -0.5f;
+        box[3 * i + 1] = (i & 2) ? 0.5f : -0.5f;
+        box[3 * i + 2] = (i & 1) ? 0.5f : -0.5f;
+    }
+    const float scaling[3] = {1, 1, 1}, up[3] = {0, 1, 0}, orn[4] = {0, 0, 0, 1};
+    const int boxShape = np->registerConvexHullShape(box, 3 * sizeof(float), 8, scaling);
+    const int ground = np->registerPlaneShape(up, 0.f);
+    if (boxShape < 0 || ground < 0) return 2;
+    const float origin[3] = {0, 0, 0};
+    rbp->registerPhysicsInstance(0.f, origin, orn, ground, 0, false);
+    for (int x = 0; x < 4; x++)
+        for (int y = 0; y < 4; y++)
+            for (int z = 0; z < 4; z++) {
+                const float pos[3] = {1.1f * x, 0.6f + 1.1f * y, 1.1f * z};
+                if (rbp->registerPhysicsInstance(1.f, pos, orn, boxShape, 1, false) < 0) return 3;
+            }
+    rbp->writeAllInstancesToGpu();
+    for (int frame = 0; frame < 150; frame++) rbp->stepSimulation(1.f / 60.f);
+    std::vector<b3gBody> bodies;
+    np->readbackAllBodiesToCpu(bodies);
+    float ymin = 1e30f, vmax = 0.f;
+    for (size_t i = 1; i < bodies.size(); i++) {
+        ymin = std::fmin(ymin, bodies[i].pos.y);
+        vmax = std::fmax(vmax, std::fabs(bodies[i].linVel.y));
+    }
+    // the drop-in stage calls on the settled state: 16 columns of 4 boxes -> 16 plane + 48 box-box manifolds
+    rbp->setupGpuAabbsFull();
+    bp->calculateOverlappingPairs(0);
+    np->computeContacts();
+    const int pairs = bp->getNumOverlap(), contacts = np->getNumContactsGpu();
+    std::printf("bodies %d ymin %.4f vmax %.4f pairs %d contacts %d\n", rbp->getNumBodies(), ymin, vmax, pairs,
+                contacts);
+    const bool ok = rbp->getNumBodies() == 65 && ymin > 0.4f && vmax < 0.5f && pairs >= 64 && contacts == 64 &&
+                    np->getBodiesGpu() != nullptr && bp->getOverlappingPairBuffer() != nullptr;
+    delete rbp;
+    delete bp;
+    delete np;
+    return ok ? 0 : 1;
+}
+'''
+
+
+def test_cpp_program_steps_a_pile_through_the_dropin(tmp_path):
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    lib_dir = Path(ROOT, "bullet3_gb300")
+    src = tmp_path / "dropin.cpp"
+    exe = tmp_path / "dropin"
+    src.write_text(PROGRAM)
+    r = subprocess.run([gxx, "-std=c++17", "-O1", "-I", str(Path(ROOT, "include")), str(src), "-o", str(exe),
+                        "-L", str(lib_dir), "-lb3gpu", f"-Wl,-rpath,{lib_dir}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "b3Error" not in r.stderr, r.stderr
+    assert r.stdout.startswith("bodies 65"), r.stdout

@@ -74,3 +74,20 @@ def test_scene_pgs_contacts_stay_within_scenes():
     dyn = bodies["invMass"] > 0
     # every pile has landed on its own plane and rests there (boxes and spheres of half size 0.5)
     assert bodies["pos"][dyn, 1].min() > 0.4
+
+
+def test_empty_scenes_in_the_offset_table():
+    # empty scenes (repeated offsets, at the start, middle and end) change nothing
+    sc = scenes.batched_piles(8, seed=21, separate=True)
+    runs = []
+    for first in (sc.scene_first, np.array([0, 0] + sc.scene_first[1:4].tolist() + [sc.scene_first[4]] * 3
+                                           + sc.scene_first[5:].tolist() + [sc.num_bodies], np.int32)):
+        sc.scene_first = first
+        np_, bp, pl, _ = load(sc, solver_mode=capi.SOLVER_JACOBI, solver_iterations=10, use_cuda_graph=True)
+        for _ in range(20):
+            pl.stepSimulation(1 / 60)
+        pl.synchronize()
+        assert pl.status() == 0
+        runs.append((pairs_xy(bp.getOverlappingPairsCPU()), np_.readbackAllBodiesToCpu()))
+    assert np.array_equal(runs[0][0], runs[1][0])
+    assert np.array_equal(runs[0][1].view(np.uint8), runs[1][1].view(np.uint8))
