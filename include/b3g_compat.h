@@ -26,6 +26,7 @@
 namespace b3g_compat {
 
 inline void b3Error(const char* what) { std::fprintf(stderr, "b3Error: %s: %s\n", what, b3g_last_error()); }
+inline void b3Warning(const char* what) { std::fprintf(stderr, "b3Warning: %s\n", what); }
 
 struct b3Config {
     int m_maxConvexBodies = 128 * 1024;
@@ -71,8 +72,80 @@ public:
         std::fprintf(stderr, "b3Error: registerConcaveMesh: concave meshes are not supported\n");
         return -1;
     }
+    /* b3GpuNarrowPhase::registerRigidBody (b3GpuNarrowPhase.cpp:816-908).  The AABB arguments are
+       recomputed from the shape (the reference stores them for the proxy it creates). */
+    int registerRigidBody(int collidableIndex, float mass, const float* position, const float* orientation,
+                          const float* /*aabbMin*/, const float* /*aabbMax*/, bool /*writeToGpu*/) {
+        return registerBody(mass, position, orientation, collidableIndex, -1);
+    }
+    int registerBody(float mass, const float* position, const float* orientation, int collidableIndex, int user) {
+        int out = -1;
+        if (b3g_register_body(m_world, mass, position, orientation, collidableIndex, user, &out) != B3G_OK) {
+            b3Error("registerRigidBody");
+            return -1;
+        }
+        if (mass == 0.f && m_static0 < 0) m_static0 = out;  // first static body (m_static0Index)
+        return out;
+    }
+    /* The first call uploads every registry (b3g_write_all_to_gpu); later calls write the host
+       copy of the bodies (after setObjectTransformCpu / setObjectVelocityCpu), as the reference's
+       writeAllBodiesToGpu copies m_bodyBufferCPU (b3GpuNarrowPhase.cpp:915-944). */
     void writeAllBodiesToGpu() {
-        if (b3g_write_all_to_gpu(m_world) != B3G_OK) b3Error("writeAllBodiesToGpu");
+        if (!m_uploaded) {
+            if (b3g_write_all_to_gpu(m_world) != B3G_OK) {
+                b3Error("writeAllBodiesToGpu");
+                return;
+            }
+            m_uploaded = true;
+            return;
+        }
+        if (!m_bodiesCPU.empty() &&
+            b3g_write_bodies(m_world, m_bodiesCPU.data(), (int)m_bodiesCPU.size()) != B3G_OK)
+            b3Error("writeAllBodiesToGpu");
+    }
+    void readbackAllBodiesToCpu() { readbackAllBodiesToCpu(m_bodiesCPU); }
+    /* host copy of a body's pose (b3GpuNarrowPhase::getObjectTransformFromCpu): valid after
+       readbackAllBodiesToCpu() */
+    bool getObjectTransformFromCpu(float* position, float* orientation, int bodyIndex) const {
+        if (bodyIndex < 0 || bodyIndex >= (int)m_bodiesCPU.size()) {
+            b3Warning("getObjectTransformFromCpu out of range.");
+            return false;
+        }
+        const b3gBody& b = m_bodiesCPU[bodyIndex];
+        position[0] = b.pos.x; position[1] = b.pos.y; position[2] = b.pos.z;
+        orientation[0] = b.quat.x; orientation[1] = b.quat.y; orientation[2] = b.quat.z; orientation[3] = b.quat.w;
+        return true;
+    }
+    void setObjectTransformCpu(const float* position, const float* orientation, int bodyIndex) {
+        if (bodyIndex < 0 || bodyIndex >= (int)m_bodiesCPU.size()) {
+            b3Warning("setObjectTransformCpu out of range.");  // b3GpuNarrowPhase.cpp:979
+            return;
+        }
+        b3gBody& b = m_bodiesCPU[bodyIndex];
+        b.pos.x = position[0]; b.pos.y = position[1]; b.pos.z = position[2];
+        b.quat.x = orientation[0]; b.quat.y = orientation[1]; b.quat.z = orientation[2]; b.quat.w = orientation[3];
+    }
+    void setObjectVelocityCpu(const float* linVel, const float* angVel, int bodyIndex) {
+        if (bodyIndex < 0 || bodyIndex >= (int)m_bodiesCPU.size()) {
+            b3Warning("setObjectVelocityCpu out of range.");  // b3GpuNarrowPhase.cpp:991
+            return;
+        }
+        b3gBody& b = m_bodiesCPU[bodyIndex];
+        b.linVel.x = linVel[0]; b.linVel.y = linVel[1]; b.linVel.z = linVel[2];
+        b.angVel.x = angVel[0]; b.angVel.y = angVel[1]; b.angVel.z = angVel[2];
+    }
+    int getNumBodiesGpu() const { return getNumRigidBodies(); }
+    int getNumCollidablesGpu() const {
+        int n = 0;
+        b3g_get_num_collidables(m_world, &n);
+        return n;
+    }
+    int getStatic0Index() const { return m_static0; }
+    void getContactsCPU(std::vector<b3gContact4>& out) {
+        int n = getNumContactsGpu();
+        out.resize(n);
+        if (n > 0 && b3g_read_contacts(m_world, out.data(), n, &n) != B3G_OK) b3Error("getContactsCPU");
+        out.resize(n);
     }
     int getNumRigidBodies() const {
         int n = 0;
@@ -85,6 +158,11 @@ public:
     }
     void computeContacts() {
         if (b3g_compute_contacts(m_world) != B3G_OK) b3Error("computeContacts");
+    }
+    /* computeContacts(pairs, numPairs, aabbs, numObjects) (b3GpuNarrowPhase.h:53): the world's own
+       pair and AABB buffers are the ones the broadphase filled */
+    void computeContacts(void* /*pairs*/, int /*numPairs*/, void* /*aabbsWorldSpace*/, int /*numObjects*/) {
+        computeContacts();
     }
     void* getBodiesGpu() {
         void* p = nullptr;
@@ -119,10 +197,16 @@ private:
     b3Config m_config;
     b3g_handle m_world = nullptr;
     int m_out = -1;
+    int m_static0 = -1;
+    bool m_uploaded = false;
+    std::vector<b3gBody> m_bodiesCPU;
 };
 
 class b3GpuBroadphaseInterface {
 public:
+    /* b3GpuBroadphaseInterface::CreateFunc (b3GpuBroadphaseInterface.h:14): the OpenCL handles
+       become a CUDA device ordinal */
+    typedef b3GpuBroadphaseInterface*(CreateFunc)(int cudaDevice);
     virtual ~b3GpuBroadphaseInterface() {}
     virtual void calculateOverlappingPairs(int maxPairs) = 0;
     virtual int getNumOverlap() = 0;
@@ -133,10 +217,32 @@ public:
 class b3GpuGridBroadphase : public b3GpuBroadphaseInterface {
 public:
     explicit b3GpuGridBroadphase(b3GpuNarrowPhase* np = nullptr) : m_np(np) {}
+    static b3GpuBroadphaseInterface* CreateFunc(int /*cudaDevice*/) { return new b3GpuGridBroadphase(); }
     void attach(b3GpuNarrowPhase* np) { m_np = np; }
+    /* Proxies: registerPhysicsInstance / registerRigidBody create them (dynamic bodies small,
+       static bodies large), as the reference pipeline does (b3GpuRigidBodyPipeline.cpp:650-657) */
+    void createProxy(const float*, const float*, int, int, int) {}
+    void createLargeProxy(const float*, const float*, int, int, int) {}
     void calculateOverlappingPairs(int) override {
         if (b3g_calculate_overlapping_pairs(m_np->world()) != B3G_OK) b3Error("calculateOverlappingPairs");
     }
+    /* calculateOverlappingPairsHost (b3GpuGridBroadphase.cpp:260-294) computes the exact pair set;
+       the device search gives the same set */
+    void calculateOverlappingPairsHost(int maxPairs) { calculateOverlappingPairs(maxPairs); }
+    /* host copies of the world AABBs (getAllAabbsCPU) and their upload (writeAabbsToGpu) */
+    std::vector<b3gAabb>& getAllAabbsCPU() {
+        m_aabbsCPU.resize(m_np->getNumRigidBodies());
+        if (!m_aabbsCPU.empty() && b3g_read_aabbs(m_np->world(), m_aabbsCPU.data(), (int)m_aabbsCPU.size()) != B3G_OK)
+            b3Error("getAllAabbsCPU");
+        return m_aabbsCPU;
+    }
+    void writeAabbsToGpu() {
+        if (!m_aabbsCPU.empty() &&
+            b3g_write_aabbs(m_np->world(), m_aabbsCPU.data(), (int)m_aabbsCPU.size()) != B3G_OK)
+            b3Error("writeAabbsToGpu");
+    }
+    void* getAllAabbsGPU() { return getAabbBufferWS(); }
+    void* getOverlappingPairsGPU() { return getOverlappingPairBuffer(); }
     int getNumOverlap() override {
         void* p = nullptr;
         int n = 0;
@@ -157,6 +263,15 @@ public:
 
 private:
     b3GpuNarrowPhase* m_np;
+    std::vector<b3gAabb> m_aabbsCPU;
+};
+
+/* b3GpuSapBroadphase (b3GpuSapBroadphase.cpp): the same exact pair set; here the grid search
+   with the 1-axis sweep and prune for large static proxies serves both names. */
+class b3GpuSapBroadphase : public b3GpuGridBroadphase {
+public:
+    explicit b3GpuSapBroadphase(b3GpuNarrowPhase* np = nullptr) : b3GpuGridBroadphase(np) {}
+    static b3GpuBroadphaseInterface* CreateFunc(int /*cudaDevice*/) { return new b3GpuSapBroadphase(); }
 };
 
 class b3GpuRigidBodyPipeline {
@@ -168,12 +283,7 @@ public:
     }
     int registerPhysicsInstance(float mass, const float* position, const float* orientation, int collidableIndex,
                                 int userData, bool /*writeInstanceToGpu*/) {
-        int out = -1;
-        if (b3g_register_body(m_np->world(), mass, position, orientation, collidableIndex, userData, &out) != B3G_OK) {
-            b3Error("registerPhysicsInstance");
-            return -1;
-        }
-        return out;
+        return m_np->registerBody(mass, position, orientation, collidableIndex, userData);
     }
     void writeAllInstancesToGpu() { m_np->writeAllBodiesToGpu(); }
     /* independent scenes stepped together (no reference counterpart: the reference runs one
@@ -193,6 +303,14 @@ public:
     void integrate(float timeStep) { b3g_integrate(m_np->world(), timeStep); }
     int getNumBodies() const { return m_np->getNumRigidBodies(); }
     void* getBodyBuffer() { return m_np->getBodiesGpu(); }
+    void reset() { b3Error("reset: re-create the pipeline (registries are fixed once uploaded)"); }
+    /* joints and ray casts are outside this GPU step: the reference API exists and reports failure */
+    void copyConstraintsToHost() {}
+    void removeConstraintByUid(int) { std::fprintf(stderr, "b3Error: removeConstraintByUid: joints are not supported\n"); }
+    template <class Rays, class Hits>
+    void castRays(const Rays&, Hits&) {
+        std::fprintf(stderr, "b3Error: castRays: ray casting is not part of this GPU step; no hits reported\n");
+    }
     int createPoint2PointConstraint(int, int, const float*, const float*, float) {
         std::fprintf(stderr, "b3Error: createPoint2PointConstraint: joints are not supported\n");
         return -1;

@@ -159,6 +159,9 @@ def test_cpp_dropin_header_compiles(tmp_path):
                    "  b3Config c; b3GpuNarrowPhase np(0, c); b3GpuGridBroadphase bp;\n"
                    "  b3GpuRigidBodyPipeline rbp(&np, &bp, nullptr, c);\n"
                    "  int first[2] = {0, 1}; rbp.setSceneOffsets(first, 2);\n"
+                   "  b3GpuBroadphaseInterface::CreateFunc* f = b3GpuSapBroadphase::CreateFunc; delete f(0);\n"
+                   "  float p[3], q[4]; np.getObjectTransformFromCpu(p, q, 0); np.setObjectTransformCpu(p, q, 0);\n"
+                   "  bp.calculateOverlappingPairsHost(0); bp.getAllAabbsCPU(); rbp.copyConstraintsToHost();\n"
                    "  rbp.stepSimulation(1.f / 60.f); return rbp.getNumBodies();\n"
                    "}\n")
     r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-Wall", "-I", str(Path(ROOT, "include")), str(src)],

@@ -59,8 +59,27 @@ int main() {
     const int pairs = bp->getNumOverlap(), contacts = np->getNumContactsGpu();
     std::printf("bodies %d ymin %.4f vmax %.4f pairs %d contacts %d\n", rbp->getNumBodies(), ymin, vmax, pairs,
                 contacts);
-    const bool ok = rbp->getNumBodies() == 65 && ymin > 0.4f && vmax < 0.5f && pairs >= 64 && contacts == 64 &&
-                    np->getBodiesGpu() != nullptr && bp->getOverlappingPairBuffer() != nullptr;
+    bool ok = rbp->getNumBodies() == 65 && ymin > 0.4f && vmax < 0.5f && pairs >= 64 && contacts == 64 &&
+              np->getBodiesGpu() != nullptr && bp->getOverlappingPairBuffer() != nullptr;
+    // host copies: read the pose of the top box of one column (body 13), kick it upwards, write, step
+    ok = ok && np->getStatic0Index() == 0 && (int)bp->getAllAabbsCPU().size() == 65;
+    bp->calculateOverlappingPairsHost(0);
+    ok = ok && bp->getNumOverlap() == pairs;
+    np->readbackAllBodiesToCpu();
+    float p0[3], q0[4];
+    ok = ok && np->getObjectTransformFromCpu(p0, q0, 13);
+    const float up5[3] = {0.f, 5.f, 0.f}, zero[3] = {0.f, 0.f, 0.f};
+    np->setObjectVelocityCpu(up5, zero, 13);
+    np->writeAllBodiesToGpu();
+    rbp->stepSimulation(1.f / 60.f);
+    np->readbackAllBodiesToCpu();
+    float p1[3], q1[4];
+    ok = ok && np->getObjectTransformFromCpu(p1, q1, 13) && p1[1] > p0[1] + 0.05f;
+    b3GpuBroadphaseInterface::CreateFunc* create = b3GpuSapBroadphase::CreateFunc;
+    b3GpuBroadphaseInterface* other = create(0);
+    ok = ok && other != nullptr;
+    delete other;
+    std::printf("kicked box %.4f -> %.4f\n", p0[1], p1[1]);
     delete rbp;
     delete bp;
     delete np;
