@@ -94,7 +94,8 @@ EXPORTS = [
     "b3g_grid_pairs_noalloc", "b3g_mlp_create", "b3g_mlp_destroy", "b3g_mlp_set_params", "b3g_mlp_get_params",
     "b3g_mlp_set_normalization", "b3g_mlp_get_normalization", "b3g_mlp_predict", "b3g_mlp_set_training_data",
     "b3g_mlp_train", "b3g_mlp_gradients", "b3g_set_warm_start_model", "b3g_read_warm_samples",
-    "b3g_read_warm_start"]
+    "b3g_read_warm_start", "b3g_radix_sort32", "b3g_radix_sort32_keys", "b3g_prefix_scan32", "b3g_bound_search",
+    "b3g_fill32"]
 
 
 def lib_path() -> Path:

@@ -210,6 +210,30 @@ b3gStatus b3g_get_tuning(b3g_handle h, b3gTuning* out);
  * off should capture (cudaProfilerStart / cudaProfilerStop; no reference counterpart). */
 b3gStatus b3g_profiler_range(int on);
 
+/* ------------------------------------------------------------------ parallel primitives */
+/* The reference's ParallelPrimitives classes (src/Bullet3OpenCL/ParallelPrimitives/), on caller
+ * device buffers.  Each call allocates its own scratch, runs on the device's default stream and
+ * synchronises before returning. */
+/* b3RadixSort32CL::execute(keyValuesInOut, sortBits) (b3RadixSort32CL.cpp:174): stable LSD sort of
+ * n (key, value) pairs of uint32 (b3SortData), in place, by key bits [0, sort_bits) exactly (the
+ * reference rounds sort_bits up to its pass width; the two agree for multiples of 8). */
+b3gStatus b3g_radix_sort32(int cuda_device, void* d_key_values, int n, int sort_bits);
+/* b3RadixSort32CL::execute(keysInOut, sortBits): the same for keys alone. */
+b3gStatus b3g_radix_sort32_keys(int cuda_device, void* d_keys, int n, int sort_bits);
+/* b3PrefixScanCL::execute(src, dst, n, &sum): EXCLUSIVE scan of n uint32 (src may equal dst);
+ * *host_sum = the total. */
+b3gStatus b3g_prefix_scan32(int cuda_device, const void* d_src, void* d_dst, int n, unsigned int* host_sum);
+/* b3BoundSearchCL::execute(src, nSrc, dst, nDst, option) (b3BoundSearchCL.cpp:69): src is n
+ * (key, value) int pairs sorted by key; for every key k in [0, n_dst) present in src, LOWER writes
+ * dst[k] = its first index, UPPER one past its last; buckets without elements are left as they
+ * are; COUNT writes upper - lower for every bucket (0 where absent). */
+#define B3G_BOUND_LOWER 0
+#define B3G_BOUND_UPPER 1
+#define B3G_BOUND_COUNT 2
+b3gStatus b3g_bound_search(int cuda_device, const void* d_sorted_pairs, int n, void* d_dst, int n_dst, int option);
+/* b3FillCL::execute(src, value, n, offset): d_dst[offset + i] = value for i in [0, n). */
+b3gStatus b3g_fill32(int cuda_device, void* d_dst, int value, int n, int offset);
+
 /* ------------------------------------------------------------------ the step */
 /* b3GpuRigidBodyPipeline::stepSimulation (b3GpuRigidBodyPipeline.cpp:221-463): AABBs, pairs,
  * contacts, batching, solve, integrate -- enqueued on the world's stream (one CUDA graph
