@@ -33,6 +33,7 @@ struct NPArgs {
     const b3gBody* bodies;
     const b3gCollidable* cols;
     const b3gHull* hulls;
+    const uint32_t* face_dup;  // per hull: faces whose SAT axis repeats an earlier face's
     const b3gFace* faces;
     const int* indices;
     const b3gFloat4* verts;
@@ -378,6 +379,15 @@ __device__ __forceinline__ void project(const b3gFloat4* verts, int nv, v3 pos, 
     mx = mx + offset;
 }
 
+// Face axes k that repeat an earlier face axis of the same hull (exactly opposite normals): the
+// same axis after the sign flip and the same overlap, so they can never be the first minimum and
+// never separate where the earlier one did not.
+__device__ __forceinline__ bool dup_face_axis(int k, int nfA, uint32_t dupA, uint32_t dupB) {
+    if (k < nfA) return k < 32 && ((dupA >> k) & 1u);
+    const int f = k - nfA;
+    return f < 32 && ((dupB >> f) & 1u);
+}
+
 // Axis k of the SAT sequence: faces of A, faces of B, then edges (e0 of A major, e1 of B minor).
 // Returns false when the edge cross product is almost zero (axis skipped).
 __device__ __forceinline__ bool sat_axis(int k, const b3gHull& hA, const b3gHull& hB, const b3gFace* faces,
@@ -459,6 +469,9 @@ __global__ void __launch_bounds__(HH_WARPS * 32) k_hull_hull(NPArgs a, int max_p
         const v3 c1 = mmul(RB, f4v3(hB.localCenter)) + posB;
         const v3 deltaC2 = c0 - c1;
         const int naxes = hA.numFaces + hB.numFaces + hA.numUniqueEdges * hB.numUniqueEdges;
+        const int nfaces = hA.numFaces + hB.numFaces;
+        const uint32_t dupA = __ldg(&a.face_dup[a.cols[BA.collidableIdx].shapeIndex]);
+        const uint32_t dupB = __ldg(&a.face_dup[a.cols[BB.collidableIdx].shapeIndex]);
         AxisBest best{FLT_MAX, 0x7fffffff};
         bool separated = false;
         const b3gFloat4* vA = &a.verts[hA.vertexOffset];
@@ -468,7 +481,8 @@ __global__ void __launch_bounds__(HH_WARPS * 32) k_hull_hull(NPArgs a, int max_p
         for (int k0 = 0; k0 < naxes; k0 += 32) {
             const int k = k0 + lane;
             v3 axis;
-            if (k < naxes && sat_axis(k, hA, hB, a.faces, a.edges, qA, qB, deltaC2, axis)) {
+            if (k < naxes && !(k < nfaces && dup_face_axis(k, hA.numFaces, dupA, dupB)) &&
+                sat_axis(k, hA, hB, a.faces, a.edges, qA, qB, deltaC2, axis)) {
                 float min0, max0, min1, max1;
                 project(vA, hA.numVertices, posA, qA, axis, min0, max0);
                 project(vB, hB.numVertices, posB, qB, axis, min1, max1);
@@ -584,11 +598,15 @@ __global__ void __launch_bounds__(NP_THREADS) k_hull_hull_small(NPArgs a, int ma
         const b3gFloat4* vA = &a.verts[hA.vertexOffset];
         const b3gFloat4* vB = &a.verts[hB.vertexOffset];
         const int naxes = hA.numFaces + hB.numFaces + hA.numUniqueEdges * hB.numUniqueEdges;
+        const int nfaces = hA.numFaces + hB.numFaces;
+        const uint32_t dupA = __ldg(&a.face_dup[a.cols[BA.collidableIdx].shapeIndex]);
+        const uint32_t dupB = __ldg(&a.face_dup[a.cols[BB.collidableIdx].shapeIndex]);
         float dmin = FLT_MAX;
         v3 sep = mk3(0.f, 0.f, 0.f);
         bool separated = false;
         for (int k = 0; k < naxes; k++) {
             v3 axis;
+            if (k < nfaces && dup_face_axis(k, hA.numFaces, dupA, dupB)) continue;
             if (!sat_axis(k, hA, hB, a.faces, a.edges, qA, qB, deltaC2, axis)) continue;
             float min0, max0, min1, max1;
             project(vA, hA.numVertices, posA, qA, axis, min0, max0);
@@ -723,6 +741,7 @@ static NPArgs make_args(DeviceState& d, unsigned short friction_cmp) {
     a.bodies = d.bodies;
     a.cols = d.collidables;
     a.hulls = d.hulls;
+    a.face_dup = d.hull_face_dup;
     a.faces = d.faces;
     a.indices = d.indices;
     a.verts = d.vertices;

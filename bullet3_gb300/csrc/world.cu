@@ -536,6 +536,7 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     TRY(dalloc(h, &d.edges, ne));
     TRY(dalloc(h, &d.dyn_slot, N));
     TRY(dalloc(h, &d.col_small, d.num_collidables));
+    TRY(dalloc(h, &d.hull_face_dup, nh));
     TRY(dalloc(h, &d.large_list, std::max(1, d.num_large)));
     TRY(dalloc(h, &d.sap_list, std::max(1, d.num_sap)));
     TRY(dalloc(h, &d.sap_sorted, std::max(1, d.num_sap)));
@@ -653,6 +654,30 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     if (!h->edges.empty())
         CUDA_TRY(cudaMemcpyAsync(d.edges, h->edges.data(), sizeof(b3gFloat4) * h->edges.size(), cudaMemcpyHostToDevice, s));
     CUDA_TRY(cudaMemcpyAsync(d.dyn_slot, dyn_slot.data(), sizeof(int) * N, cudaMemcpyHostToDevice, s));
+    {
+        // faces whose normal is the exact negation of an earlier face's (a box's opposite faces):
+        // rotated and sign-flipped towards the other body they give the earlier face's SAT axis
+        // and the same overlap, which never wins (the first minimum is kept), so the SAT skips them
+        std::vector<uint32_t> dup(nh, 0u);
+        for (size_t k = 0; k < h->hulls.size(); k++) {
+            const b3gHull& hull = h->hulls[k];
+            const int nf = std::min(hull.numFaces, 32);
+            for (int f = 1; f < nf; f++) {
+                const b3gFloat4& pf = h->faces[hull.faceOffset + f].plane;
+                for (int g = 0; g < f; g++) {
+                    const b3gFloat4& pg = h->faces[hull.faceOffset + g].plane;
+                    // equal as numbers (the sign of a zero component only changes the sign of zeros in
+                    // the rotated axis and its projections, never a comparison)
+                    if (-pg.x == pf.x && -pg.y == pf.y && -pg.z == pf.z) {
+                        dup[k] |= 1u << f;
+                        break;
+                    }
+                }
+            }
+        }
+        CUDA_TRY(cudaMemcpyAsync(d.hull_face_dup, dup.data(), sizeof(uint32_t) * nh, cudaMemcpyHostToDevice, s));
+        CUDA_TRY(cudaStreamSynchronize(s));  // `dup` is a local: finish the copy before it goes
+    }
     std::vector<int> col_small(d.num_collidables, 0);
     for (int c = 0; c < d.num_collidables; c++) {
         const b3gCollidable& col = h->collidables[c];

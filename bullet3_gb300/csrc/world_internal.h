@@ -79,6 +79,8 @@ struct DeviceState {
     b3gFloat4* vertices = nullptr;
     b3gFloat4* edges = nullptr;
     int* dyn_slot = nullptr;      // body -> dynamic slot or -1
+    uint32_t* hull_face_dup = nullptr;  // per hull: bit f set when face f's normal is exactly the negation of
+                                        // an earlier face's (f < 32): its SAT axis repeats that face's
     int* col_small = nullptr;     // per collidable: 0, or for a hull whose faces all have <= B3G_SMALL_FACE_VERTS
                                   // vertices: 1 | faces << 1 | unique edges << 16
     int* large_list = nullptr;    // static bodies (large proxies), grouped by scene
