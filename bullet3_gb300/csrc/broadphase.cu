@@ -14,6 +14,7 @@
 // the pair kernel works in sorted (spatially coherent) order, buffers pairs per thread and
 // reserves output with one warp-aggregated atomic; pairs are then radix-sorted on a packed
 // (a, b) key so the pair list is canonical and deterministic (a < b, ascending).
+#include <algorithm>
 #include <cstddef>
 
 #include "common.cuh"
@@ -578,7 +579,8 @@ __global__ void __launch_bounds__(BP_THREADS) k_unpack_pairs(const uint64_t* __r
 }
 
 int launch_aabbs(DeviceState& d, cudaStream_t s) {
-    int grid = d.num_sms * 4;
+    // one body per thread in a single wave (latency-bound: body -> collidable -> local AABB chain)
+    const int grid = std::max(1, std::min((d.num_bodies + BP_THREADS - 1) / BP_THREADS, d.num_sms * 32));
     k_aabb_hash<<<grid, BP_THREADS, 0, s>>>(d.bodies, d.collidables, d.local_aabbs, d.dyn_slot,
                                             d.num_scenes > 1 ? d.body_scene : nullptr, d.num_bodies, d.aabbs,
                                             d.cell_keys[0], d.cell_vals[0], d.inv_cell, d.grid_bits);

@@ -6,6 +6,8 @@
 // normalisation, then x += v*dt, then v += g*dt; bodies with invMass 0 are skipped.
 // Optional (off by default, as in the reference which freezes it at registration,
 // b3GpuNarrowPhase.cpp:899-901): refresh the world inverse inertia R diag(I0^-1) R^T.
+#include <algorithm>
+
 #include "common.cuh"
 #include "world_internal.h"
 
@@ -67,7 +69,9 @@ __global__ void __launch_bounds__(256) k_integrate(b3gBody* __restrict__ bodies,
 }
 
 int launch_integrate(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s) {
-    k_integrate<<<d.num_sms * 4, 256, 0, s>>>(d.bodies, d.inertias, d.num_bodies, dt, cfg.angular_damping,
+    // one body per thread in a single wave (the kernel is latency-bound: a dependent chain per body)
+    const int grid = std::max(1, std::min((d.num_bodies + 255) / 256, d.num_sms * 32));
+    k_integrate<<<grid, 256, 0, s>>>(d.bodies, d.inertias, d.num_bodies, dt, cfg.angular_damping,
                                               cfg.gravity[0], cfg.gravity[1], cfg.gravity[2], cfg.update_world_inertia,
                                               &d.counters->status);
     return 1;

@@ -309,11 +309,19 @@ __device__ void sphere_sphere(const NPArgs& a, int pairIdx, int bodyA, int bodyB
 
 __device__ __forceinline__ int shape_type(const NPArgs& a, int body) { return a.cols[a.bodies[body].collidableIdx].shapeType; }
 
-__global__ void __launch_bounds__(NP_THREADS) k_primitive_pairs(NPArgs a, int type, int max_pairs) {
-    const int n = a.type_count[type];
-    const int* list = a.type_list + (size_t)type * max_pairs;
+// All four primitive pair types (plane-hull, sphere-hull, sphere-sphere, plane-sphere) in one
+// launch: work item t walks the concatenation of the four type lists.
+__global__ void __launch_bounds__(NP_THREADS) k_primitive_pairs(NPArgs a, int max_pairs) {
+    const int c1 = a.type_count[PT_PLANE_HULL], c2 = a.type_count[PT_SPHERE_HULL],
+              c3 = a.type_count[PT_SPHERE_SPHERE], c4 = a.type_count[PT_PLANE_SPHERE];
+    const int n = c1 + c2 + c3 + c4;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        int p = list[t];
+        int type, k;
+        if (t < c1) { type = PT_PLANE_HULL; k = t; }
+        else if (t < c1 + c2) { type = PT_SPHERE_HULL; k = t - c1; }
+        else if (t < c1 + c2 + c3) { type = PT_SPHERE_SPHERE; k = t - c1 - c2; }
+        else { type = PT_PLANE_SPHERE; k = t - c1 - c2 - c3; }
+        int p = a.type_list[(size_t)type * max_pairs + k];
         b3gPair pr = a.pairs[p];
         int A = pr.x, B = pr.y;
         int ta = shape_type(a, A);
@@ -765,8 +773,7 @@ unsigned short friction_to_cmp(float f) {
 int launch_contacts(DeviceState& d, float friction, cudaStream_t s) {
     NPArgs a = make_args(d, friction_to_cmp(friction));
     int grid = d.num_sms * 4;
-    for (int t = PT_PLANE_HULL; t <= PT_PLANE_SPHERE; t++)
-        k_primitive_pairs<<<grid, NP_THREADS, 0, s>>>(a, t, d.max_pairs);
+    k_primitive_pairs<<<grid, NP_THREADS, 0, s>>>(a, d.max_pairs);
     k_hull_hull_small<<<d.num_sms * d.tune.narrow_blocks_per_sm, NP_THREADS, 0, s>>>(a, d.max_pairs);
     k_hull_hull<<<d.num_sms * 16, HH_WARPS * 32, 0, s>>>(a, d.max_pairs);
     long long ll = 0;
@@ -775,7 +782,7 @@ int launch_contacts(DeviceState& d, float friction, cudaStream_t s) {
                        &ll);
     k_manifold_list<<<grid, NP_THREADS, 0, s>>>(d.contact_flag, d.contact_index, d_np, d.contact_slots, d.pairs,
                                                 d.manifold_pair, &d.counters->num_points);
-    return 4 + 2 + 1 + (int)ll;
+    return 1 + 2 + 1 + (int)ll;
 }
 
 int launch_compact_contacts(DeviceState& d, cudaStream_t s) {
