@@ -108,3 +108,20 @@ def test_sphere_sphere_and_plane_sphere_contacts():
     assert len(gc) == len(oc) >= 2
     np.testing.assert_array_equal(gc["normal"], oc["normal"])
     np.testing.assert_array_equal(gc["worldPosB"][:, 0], oc["worldPosB"][:, 0])
+
+
+def test_free_fall_without_contacts():
+    # bodies far apart and no plane: no pairs, no manifolds, an empty solve; the step is pure
+    # integration, bit-identical to the oracle's integrateSingleTransform over the same state
+    sc = scenes.box_pile(3, 3, 3, spacing=4.0, plane=False, seed=5)
+    np_, bp, pl, shapes = load(sc, solver_mode=capi.SOLVER_PGS, use_cuda_graph=True)
+    for _ in range(3):
+        b = np_.readbackAllBodiesToCpu()
+        pl.stepSimulation(1 / 60)
+        pl.synchronize()
+        st = pl.stats()
+        assert st.num_pairs == 0 and st.num_contacts == 0 and pl.status() == 0
+        ob = O.integrate(b)
+        gb = np_.readbackAllBodiesToCpu()
+        np.testing.assert_allclose(gb["pos"], ob["pos"], rtol=0, atol=0)
+        np.testing.assert_allclose(gb["linVel"], ob["linVel"], rtol=0, atol=0)
