@@ -24,8 +24,11 @@ CONTACT = np.dtype([("worldPosB", "<f4", (4, 4)), ("normal", "<f4", 4), ("restit
                     ("frictionCmp", "<u2"), ("batchIdx", "<i4"), ("bodyA", "<i4"), ("bodyB", "<i4"),
                     ("childA", "<i4"), ("childB", "<i4"), ("unused", "<i4", 2)])
 PAIR = np.dtype([("x", "<i4"), ("y", "<i4"), ("z", "<i4"), ("w", "<i4")])
+RAY = np.dtype([("from", "<f4", 4), ("to", "<f4", 4)])
+RAYHIT = np.dtype([("hitFraction", "<f4"), ("hitBody", "<i4"), ("hitResult1", "<i4"), ("hitResult2", "<i4"),
+                   ("hitPoint", "<f4", 4), ("hitNormal", "<f4", 4)])
 for _dt, _sz in ((BODY, 80), (INERTIA, 96), (COLLIDABLE, 16), (HULL, 96), (FACE, 32), (AABB, 32), (CONTACT, 112),
-                 (PAIR, 16)):
+                 (PAIR, 16), (RAY, 32), (RAYHIT, 48)):
     assert _dt.itemsize == _sz, (_dt, _sz)
 
 SHAPE_CONVEX_HULL, SHAPE_PLANE, SHAPE_SPHERE = 3, 4, 7
@@ -82,7 +85,7 @@ _LIB = None
 EXPORTS = [
     "b3g_config_default", "b3g_create", "b3g_destroy", "b3g_last_error", "b3g_version", "b3g_register_sphere",
     "b3g_register_plane", "b3g_register_hull", "b3g_register_hull_tables", "b3g_register_body",
-    "b3g_write_all_to_gpu", "b3g_set_gravity", "b3g_set_solver", "b3g_set_scene_offsets", "b3g_autotune", "b3g_get_tuning", "b3g_profiler_range", "b3g_step", "b3g_setup_aabbs",
+    "b3g_write_all_to_gpu", "b3g_set_gravity", "b3g_set_solver", "b3g_set_scene_offsets", "b3g_autotune", "b3g_get_tuning", "b3g_profiler_range", "b3g_cast_rays", "b3g_step", "b3g_setup_aabbs",
     "b3g_calculate_overlapping_pairs", "b3g_compute_contacts", "b3g_solve_contacts", "b3g_integrate",
     "b3g_synchronize", "b3g_get_stats", "b3g_status", "b3g_get_num_bodies", "b3g_get_body_buffer",
     "b3g_get_inertia_buffer", "b3g_get_aabb_buffer", "b3g_get_pair_buffer", "b3g_get_contact_buffer",

@@ -45,27 +45,6 @@ __device__ __forceinline__ int cell_coord(float c, float inv_cell, int mask) {
     return ((int)floorf(c * inv_cell)) & mask;
 }
 
-__device__ __forceinline__ uint32_t cell_hash(int x, int y, int z, int bits, int mask) {
-    return ((uint32_t)(z & mask) << (2 * bits)) | ((uint32_t)(y & mask) << bits) | (uint32_t)(x & mask);
-}
-
-// Per-scene shift of the integer cell coordinates (batched independent scenes).  A constant shift
-// keeps a scene's neighbour cells neighbours after the wrap of cell_hash, so the 27-cell search
-// stays complete within the scene, while different scenes that occupy the same region of space
-// land in different cells of the hashed grid.  Cross-scene entries that still share a cell are
-// rejected by the scene test of the pair kernel.
-struct CellShift {
-    int x, y, z;
-};
-__device__ __forceinline__ CellShift scene_shift(int scene, int bits) {
-    uint32_t r = (uint32_t)scene * 0x9E3779B1u;
-    r ^= r >> 15;
-    r *= 0x85EBCA77u;
-    r ^= r >> 13;
-    const int mask = (1 << bits) - 1;
-    return CellShift{(int)(r & mask), (int)((r >> bits) & mask), (int)((r >> (2 * bits)) & mask)};
-}
-
 __global__ void __launch_bounds__(BP_THREADS) k_aabb_hash(const b3gBody* __restrict__ bodies,
                                                           const b3gCollidable* __restrict__ cols,
                                                           const b3gAabb* __restrict__ local_aabbs,
@@ -587,20 +566,25 @@ int launch_aabbs(DeviceState& d, cudaStream_t s) {
     return 1;
 }
 
-int launch_pairs(DeviceState& d, cudaStream_t s) {
-    int launches = 0;
+// The grid of the current AABBs: (cell hash, body) sorted, run starts in the dense table.
+int launch_cells(DeviceState& d, cudaStream_t s) {
     long long ll = 0;
-    // 1. sort (cell hash, body) -- keys written by launch_aabbs
     d.prim.sort_blocks = d.num_sms * d.tune.sort_blocks_per_sm;
     int which = radix_sort_u32(d.prim, d.cell_keys[0], d.cell_keys[1], d.cell_vals[0], d.cell_vals[1],
                                d.d_num_dynamic, 3 * d.grid_bits, d.sort_scratch, s, &ll);
-    uint32_t* keys = d.cell_keys[which];
-    uint32_t* vals = d.cell_vals[which];
-    d.cell_sorted_bodies = vals;  // dynamic bodies in cell order: the solver partitions this list
-    int grid = d.num_sms * 4;
-    // 2. run starts
-    k_cell_start<<<grid, BP_THREADS, 0, s>>>(keys, d.num_dynamic, d.cell_start);
-    launches++;
+    d.cell_sorted_keys = d.cell_keys[which];
+    d.cell_sorted_bodies = d.cell_vals[which];  // dynamic bodies in cell order: the solver partitions this list
+    k_cell_start<<<d.num_sms * 4, BP_THREADS, 0, s>>>(d.cell_sorted_keys, d.num_dynamic, d.cell_start);
+    return 1 + (int)ll;
+}
+
+int launch_pairs(DeviceState& d, cudaStream_t s) {
+    int launches = 0;
+    long long ll = 0;
+    // 1-2. sort (cell hash, body) -- keys written by launch_aabbs -- and run starts
+    launches += launch_cells(d, s);
+    uint32_t* keys = const_cast<uint32_t*>(d.cell_sorted_keys);
+    uint32_t* vals = const_cast<uint32_t*>(d.cell_sorted_bodies);
     // 3. pairs
     // per-step counters restart at zero; the status word accumulates until the host clears it
     cudaMemsetAsync(d.counters, 0, offsetof(DevCounters, status), s);

@@ -149,6 +149,28 @@ B3G_HD v3 imul(const b3gMat3& m, v3 v) {
               m.row[2].x * v.x + m.row[2].y * v.y + m.row[2].z * v.z};
 }
 
+// ---- uniform grid hashing (broadphase and ray casts)
+B3G_DEV uint32_t cell_hash(int x, int y, int z, int bits, int mask) {
+    return ((uint32_t)(z & mask) << (2 * bits)) | ((uint32_t)(y & mask) << bits) | (uint32_t)(x & mask);
+}
+
+// Per-scene shift of the integer cell coordinates (batched independent scenes).  A constant shift
+// keeps a scene's neighbour cells neighbours after the wrap of cell_hash, so the 27-cell search
+// stays complete within the scene, while different scenes that occupy the same region of space
+// land in different cells of the hashed grid.  Cross-scene entries that still share a cell are
+// rejected by the scene test of the pair kernel.
+struct CellShift {
+    int x, y, z;
+};
+B3G_DEV CellShift scene_shift(int scene, int bits) {
+    uint32_t r = (uint32_t)scene * 0x9E3779B1u;
+    r ^= r >> 15;
+    r *= 0x85EBCA77u;
+    r ^= r >> 13;
+    const int mask = (1 << bits) - 1;
+    return CellShift{(int)(r & mask), (int)((r >> bits) & mask), (int)((r >> (2 * bits)) & mask)};
+}
+
 B3G_DEV float4 ldg4(const b3gFloat4* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
 
 // ----------------------------------------------------------------------------------------

@@ -935,6 +935,31 @@ extern "C" b3gStatus b3g_autotune(b3g_handle h, float dt, int repeats, b3gTuning
     return B3G_OK;
 }
 
+// ---------------------------------------------------------------------------------- ray casts
+extern "C" b3gStatus b3g_cast_rays(b3g_handle h, const void* host_rays, void* host_hits, int n) {
+    REQUIRE_UPLOADED(h);
+    if (n < 0 || (n > 0 && (!host_rays || !host_hits))) return fail(B3G_ERR_INVALID_ARG, "invalid ray arguments");
+    CUDA_TRY(cudaSetDevice(h->device));
+    DeviceState& d = h->d;
+    if (n > d.ray_cap) {
+        const int cap = std::max(n, 2 * d.ray_cap);
+        TRY(dalloc(h, &d.ray_buf, 2 * (size_t)cap));
+        TRY(dalloc(h, &d.hit_buf, (size_t)cap));
+        d.ray_cap = cap;
+    }
+    cudaStream_t s = h->stream;
+    if (n > 0) {
+        CUDA_TRY(cudaMemcpyAsync(d.ray_buf, host_rays, sizeof(b3gRayInfo) * (size_t)n, cudaMemcpyHostToDevice, s));
+        CUDA_TRY(cudaMemcpyAsync(d.hit_buf, host_hits, sizeof(b3gRayHit) * (size_t)n, cudaMemcpyHostToDevice, s));
+    }
+    h->launches += launch_cast_rays(d, d.ray_buf, d.hit_buf, n, s);
+    TRY(check_launch(h));
+    if (n > 0)
+        CUDA_TRY(cudaMemcpyAsync(host_hits, d.hit_buf, sizeof(b3gRayHit) * (size_t)n, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    return B3G_OK;
+}
+
 extern "C" b3gStatus b3g_profiler_range(int on) {
     CUDA_TRY(on ? cudaProfilerStart() : cudaProfilerStop());
     return B3G_OK;

@@ -64,6 +64,9 @@ static constexpr int B3G_SAP_MAX_PER_SCENE = 4096;
 
 struct DeviceState {
     LaunchTuning tune;
+    float4* ray_buf = nullptr;    // b3g_cast_rays: rays (2 float4 each) and hits, grown on demand
+    b3gRayHit* hit_buf = nullptr;
+    int ray_cap = 0;
     // sizes fixed at upload
     int num_bodies = 0, num_dynamic = 0, num_large = 0, num_collidables = 0;
     int max_pairs = 0, max_contacts = 0;
@@ -120,6 +123,7 @@ struct DeviceState {
     float4* manifold_inv_mass_ord = nullptr;  // (invMass A, invMass B, 0, 0)
     float4* inertia_ord = nullptr;         // PGS: per ordered manifold, A's then B's inverse world inertia rows (6)
     const uint32_t* cell_sorted_bodies = nullptr;  // set by the broadphase: dynamic bodies in cell order
+    const uint32_t* cell_sorted_keys = nullptr;    // ... and their cell hashes
     int* body_slot = nullptr;              // body -> position in cell order (PGS partitions)
     int* manifold_group = nullptr;         // PGS processing group of each manifold
     int* group_counts = nullptr;           // 3 x (num_sms * B3G_PGS_MAX_BLOCKS_PER_SM * 64 + 64 + 2)
@@ -174,6 +178,8 @@ struct DeviceState {
 // stage launchers (each returns the number of kernels it launched)
 int launch_aabbs(DeviceState& d, cudaStream_t s);
 int launch_pairs(DeviceState& d, cudaStream_t s);
+int launch_cells(DeviceState& d, cudaStream_t s);
+int launch_cast_rays(DeviceState& d, const float4* rays, b3gRayHit* hits, int n, cudaStream_t s);
 int launch_contacts(DeviceState& d, float friction, cudaStream_t s);
 int launch_compact_contacts(DeviceState& d, cudaStream_t s);
 int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s);

@@ -475,6 +475,22 @@ class b3GpuRigidBodyPipeline:
     def removeConstraintByUid(self, uid: int):
         b3Error("removeConstraintByUid: joints are not supported by this GPU step")
 
-    def castRays(self, rays):
-        b3Error("castRays: ray casting is not part of this GPU step; no hits reported")
-        return [None] * len(rays)
+    def castRays(self, rays, hitResults=None) -> np.ndarray:
+        """b3GpuRigidBodyPipeline::castRays: rays as a capi.RAY array (from, to; from[3] = scene in a
+        world of several scenes) or a sequence of (from, to) points; hitResults (capi.RAYHIT, optional)
+        carries each ray's body to ignore in hitResult2.  Returns the hits: hitFraction 1 = no hit."""
+        if not isinstance(rays, np.ndarray) or rays.dtype != capi.RAY:
+            r = np.zeros(len(rays), capi.RAY)
+            for i, (f, t) in enumerate(rays):
+                r["from"][i, :3] = f[:3]
+                r["to"][i, :3] = t[:3]
+            rays = r
+        rays = np.ascontiguousarray(rays, capi.RAY)
+        if hitResults is None:
+            hits = np.zeros(len(rays), capi.RAYHIT)
+            hits["hitBody"] = -1
+            hits["hitResult2"] = -1
+        else:
+            hits = np.array(hitResults, capi.RAYHIT, copy=True)
+        call("b3g_cast_rays", self._h, ptr(rays), ptr(hits), C.c_int(len(rays)))
+        return hits

@@ -210,6 +210,18 @@ b3gStatus b3g_get_tuning(b3g_handle h, b3gTuning* out);
  * off should capture (cudaProfilerStart / cudaProfilerStop; no reference counterpart). */
 b3gStatus b3g_profiler_range(int on);
 
+/* ------------------------------------------------------------------ ray casts */
+/* b3GpuRigidBodyPipeline::castRays (b3GpuRigidBodyPipeline.cpp) -> b3GpuRaycast::castRays
+ * (Bullet3OpenCL/Raycast/b3GpuRaycast.cpp:248-373): n rays (b3gRayInfo == b3RayInfo) from host
+ * memory against the bodies' current poses; hits (b3gRayHit == b3RayHit) in/out: on input
+ * hitResult2 names a body the ray ignores (-1: none); on output hitFraction is 1 when nothing is
+ * hit, else the closest hit's fraction along from->to, hitBody, hitPoint and the normalised
+ * hitNormal (a hull's face normal in the body's own frame, as the reference's kernel returns it;
+ * a sphere's from its centre).  Hulls and spheres are hit, planes are not (as in the reference);
+ * equal fractions go to the lower body index.  In a world of several scenes a ray sees only the
+ * scene (int)from.w.  Rebuilds the broadphase grid from the current poses; synchronises. */
+b3gStatus b3g_cast_rays(b3g_handle h, const void* host_rays, void* host_hits, int n);
+
 /* ------------------------------------------------------------------ parallel primitives */
 /* The reference's ParallelPrimitives classes (src/Bullet3OpenCL/ParallelPrimitives/), on caller
  * device buffers.  Each call allocates its own scratch, runs on the device's default stream and

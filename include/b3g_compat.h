@@ -307,9 +307,17 @@ public:
     /* joints and ray casts are outside this GPU step: the reference API exists and reports failure */
     void copyConstraintsToHost() {}
     void removeConstraintByUid(int) { std::fprintf(stderr, "b3Error: removeConstraintByUid: joints are not supported\n"); }
+    /* castRays(rays, hitResults) (b3GpuRigidBodyPipeline.h:63): arrays of b3RayInfo / b3RayHit (or
+       b3gRayInfo / b3gRayHit, the same layouts) of equal size; hitResults[i].m_hitResult2 names a
+       body the ray ignores */
     template <class Rays, class Hits>
-    void castRays(const Rays&, Hits&) {
-        std::fprintf(stderr, "b3Error: castRays: ray casting is not part of this GPU step; no hits reported\n");
+    void castRays(const Rays& rays, Hits& hitResults) {
+        const int n = (int)rays.size();
+        if ((int)hitResults.size() != n) {
+            b3Warning("castRays: hitResults must have one entry per ray");
+            return;
+        }
+        if (n > 0 && b3g_cast_rays(m_np->world(), &rays[0], &hitResults[0], n) != B3G_OK) b3Error("castRays");
     }
     int createPoint2PointConstraint(int, int, const float*, const float*, float) {
         std::fprintf(stderr, "b3Error: createPoint2PointConstraint: joints are not supported\n");

@@ -12,6 +12,8 @@
  *   b3gAabb        == b3Aabb / b3SapAabb   (Bullet3Collision/BroadPhaseCollision/shared/b3Aabb.h:10)            32 B
  *   b3gContact4    == b3Contact4Data       (.../shared/b3Contact4Data.h:8)                                     112 B
  *   b3gPair        == b3Int4 overlapping pair (x=bodyA, y=bodyB, z=contact index or -1, w=-1)                  16 B
+ *   b3gRayInfo     == b3RayInfo            (Bullet3Collision/NarrowPhaseCollision/b3RaycastInfo.h:7)          32 B
+ *   b3gRayHit      == b3RayHit             (same file :14)                                                    48 B
  * Shape type codes follow b3ShapeTypes (b3Collidable.h:8).
  */
 #ifndef B3G_TYPES_H
@@ -96,6 +98,20 @@ typedef struct b3gContact4 {
 } b3gContact4;
 
 typedef struct b3gPair { int x, y, z, w; } b3gPair;
+
+typedef struct b3gRayInfo {
+    b3gFloat4 from;  /* w: the ray's scene in a world of several scenes (b3g_set_scene_offsets) */
+    b3gFloat4 to;
+} b3gRayInfo;
+
+typedef struct b3gRayHit {
+    float hitFraction;  /* 1 when nothing is hit */
+    int hitBody;
+    int hitResult1;
+    int hitResult2;     /* input: a body the ray ignores (-1: none) */
+    b3gFloat4 hitPoint;
+    b3gFloat4 hitNormal;
+} b3gRayHit;
 
 #ifdef __cplusplus
 }

@@ -1226,3 +1226,120 @@ int oracle_step(obody* bodies, const oinertia* inertias, int n, const oshapes* s
     free(contacts);
     return nc;
 }
+
+/* ------------------------------------------------------------------ ray casts */
+/* qtMul / qtRotate of rayCastKernels.cl:101-131: ans = cross(a, b) + (a.w b + b.w a),
+ * ans.w = a.w b.w - dot3(a, b) */
+static inline qt cl_qmul(qt a, qt b) {
+    qt r;
+    r.x = (a.y * b.z - a.z * b.y) + (a.w * b.x + b.w * a.x);
+    r.y = (a.z * b.x - a.x * b.z) + (a.w * b.y + b.w * a.y);
+    r.z = (a.x * b.y - a.y * b.x) + (a.w * b.z + b.w * a.z);
+    r.w = a.w * b.w - (a.x * b.x + a.y * b.y + a.z * b.z);
+    return r;
+}
+static inline v3 cl_qrot(qt q, v3 v) {
+    qt vq = {v.x, v.y, v.z, 0.0f};
+    qt inv = {-q.x, -q.y, -q.z, q.w};
+    qt t = cl_qmul(cl_qmul(q, vq), inv);
+    return mk(t.x, t.y, t.z);
+}
+
+/* rayConvex (rayCastKernels.cl:157-217) with hitFraction in/out */
+static int ray_convex(v3 from, v3 to, const oface* faces, int nf, float* hitFraction, v3* hitNormal) {
+    float exitFraction = *hitFraction, enterFraction = -0.3f;
+    v3 cur = mk(0.0f, 0.0f, 0.0f);
+    int result = 1, i;
+    for (i = 0; i < nf && result; i++) {
+        const oface* f = &faces[i];
+        v3 n = mk(f->plane.x, f->plane.y, f->plane.z);
+        float fromd = dot(from, n) + f->plane.w;
+        float tod = dot(to, n) + f->plane.w;
+        if (fromd < 0.0f) {
+            if (tod >= 0.0f) {
+                float fraction = fromd / (fromd - tod);
+                if (exitFraction > fraction) exitFraction = fraction;
+            }
+        } else {
+            if (tod < 0.0f) {
+                float fraction = fromd / (fromd - tod);
+                if (enterFraction <= fraction) {
+                    enterFraction = fraction;
+                    cur = n;
+                }
+            } else {
+                result = 0;
+            }
+        }
+        if (exitFraction <= enterFraction) result = 0;
+    }
+    if (enterFraction < 0.0f) result = 0;
+    if (result) {
+        *hitFraction = enterFraction;
+        *hitNormal = cur;
+    }
+    return result;
+}
+
+/* sphere_intersect (rayCastKernels.cl:224-248) */
+static int ray_sphere(v3 c, float radius, v3 from, v3 to, float* hitFraction) {
+    v3 rs = sub(from, c), d = sub(to, from);
+    float A = dot(d, d), B = dot(rs, d), C = dot(rs, rs) - radius * radius;
+    float D = B * B - A * C;
+    if (D > 0.0f) {
+        float t = (-B - sqrtf(D)) / A;
+        if (t >= 0.0f && t < *hitFraction) {
+            *hitFraction = t;
+            return 1;
+        }
+    }
+    return 0;
+}
+
+/* setInterpolate3 (rayCastKernels.cl:250-258) */
+static inline v3 ray_lerp(v3 a, v3 b, float t) {
+    float s = 1.0f - t;
+    return mk(s * a.x + t * b.x, s * a.y + t * b.y, s * a.z + t * b.z);
+}
+
+void oracle_cast_rays(const obody* bodies, int nbodies, const oshapes* sh, const oray* rays, oray_hit* hits,
+                      int nrays, const int* body_scene) {
+    int r;
+#pragma omp parallel for num_threads(g_threads) schedule(dynamic, 64)
+    for (r = 0; r < nrays; r++) {
+        v3 from = f4v(rays[r].from), to = f4v(rays[r].to), hp = mk(0, 0, 0), hn = mk(0, 0, 0);
+        float hf = 1.0f;
+        int hb = -1, b;
+        const int scene = body_scene ? (int)rays[r].from.w : 0;
+        hits[r].hitFraction = 1.0f;
+        for (b = 0; b < nbodies; b++) {
+            const obody* B = &bodies[b];
+            const ocollidable* c = &sh->cols[B->collidableIdx];
+            if (hits[r].hitResult2 == b) continue;
+            if (body_scene && body_scene[b] != scene) continue;
+            if (c->shapeType == 3) {
+                qt inv = {-B->quat.x, -B->quat.y, -B->quat.z, B->quat.w};
+                v3 invPos = cl_qrot(inv, neg(f4v(B->pos)));
+                v3 lf = add(cl_qrot(inv, from), invPos), lt = add(cl_qrot(inv, to), invPos);
+                const ohull* hull = &sh->hulls[c->shapeIndex];
+                if (hull->numFaces && ray_convex(lf, lt, &sh->faces[hull->faceOffset], hull->numFaces, &hf, &hn)) {
+                    hb = b;
+                    hp = ray_lerp(from, to, hf);
+                }
+            } else if (c->shapeType == 7) {
+                if (ray_sphere(f4v(B->pos), c->radius, from, to, &hf)) {
+                    hb = b;
+                    hp = ray_lerp(from, to, hf);
+                    hn = sub(hp, f4v(B->pos));
+                }
+            }
+        }
+        if (hb >= 0) {
+            v3 n = nrm(hn);
+            hits[r].hitFraction = hf;
+            hits[r].hitBody = hb;
+            hits[r].hitPoint.x = hp.x; hits[r].hitPoint.y = hp.y; hits[r].hitPoint.z = hp.z; hits[r].hitPoint.w = 0.0f;
+            hits[r].hitNormal.x = n.x; hits[r].hitNormal.y = n.y; hits[r].hitNormal.z = n.z; hits[r].hitNormal.w = 0.0f;
+        }
+    }
+}

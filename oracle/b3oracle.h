@@ -114,6 +114,19 @@ typedef struct {
 int oracle_step(obody* bodies, const oinertia* inertias, int n, const oshapes* sh, const ostep_params* p,
                 int* npairs_out, int* npoints_out);
 
+/* Ray casts (b3GpuRaycast::castRays, Bullet3OpenCL/Raycast/b3GpuRaycast.cpp:248-373, whose per-ray
+ * work is rayCastPairsKernel / rayCastKernel, kernels/rayCastKernels.cl:261-439): for every ray,
+ * the bodies in index order; hulls by rayConvex (:157-217) in the body's frame (qtRotate
+ * quaternion form), spheres by sphere_intersect (:224-248); planes and other shapes are skipped;
+ * a body equal to the hit's m_hitResult2 on input is skipped.  Output per ray: hitFraction 1 when
+ * nothing is hit, else the closest fraction, hit body, interpolated point and normalised normal
+ * (a hull's face normal in the body's frame, as the kernel returns it).  With body_scene, ray r
+ * only sees the bodies of scene (int)from.w. */
+typedef struct { of4 from, to; } oray;
+typedef struct { float hitFraction; int hitBody, hitResult1, hitResult2; of4 hitPoint, hitNormal; } oray_hit;
+void oracle_cast_rays(const obody* bodies, int nbodies, const oshapes* sh, const oray* rays, oray_hit* hits,
+                      int nrays, const int* body_scene);
+
 #ifdef __cplusplus
 }
 #endif

@@ -215,6 +215,26 @@ def integrate(bodies, dt=1 / 60, damping=0.99, gravity=(0.0, -9.8, 0.0)):
     return b
 
 
+RAY = np.dtype([("from", "<f4", 4), ("to", "<f4", 4)])
+RAYHIT = np.dtype([("hitFraction", "<f4"), ("hitBody", "<i4"), ("hitResult1", "<i4"), ("hitResult2", "<i4"),
+                   ("hitPoint", "<f4", 4), ("hitNormal", "<f4", 4)])
+
+
+def cast_rays(bodies, shapes: Shapes, rays, hits=None, body_scene=None):
+    """Ray casts as the reference's ray kernels compute them (see oracle_cast_rays)."""
+    b = np.ascontiguousarray(bodies, BODY)
+    r = np.ascontiguousarray(rays, RAY)
+    h = np.zeros(len(r), RAYHIT) if hits is None else np.array(hits, RAYHIT, copy=True)
+    if hits is None:
+        h["hitResult2"] = -1
+        h["hitBody"] = -1
+    sc = shapes.c()
+    bs = None if body_scene is None else np.ascontiguousarray(body_scene, np.int32)
+    load_oracle().oracle_cast_rays(_p(b), C.c_int(len(b)), C.byref(sc), _p(r), _p(h), C.c_int(len(r)),
+                                   _p(bs) if bs is not None else None)
+    return h
+
+
 def check_batches(contacts_, colors, bodies) -> int:
     c = np.ascontiguousarray(contacts_, CONTACT)
     col = np.ascontiguousarray(colors, np.int32)

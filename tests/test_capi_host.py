@@ -26,7 +26,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_layouts_match_reference_sizes():
     sizes = {capi.BODY: 80, capi.INERTIA: 96, capi.COLLIDABLE: 16, capi.HULL: 96, capi.FACE: 32, capi.AABB: 32,
-             capi.CONTACT: 112}
+             capi.CONTACT: 112, capi.RAY: 32, capi.RAYHIT: 48}
     for dt, n in sizes.items():
         assert dt.itemsize == n
 
@@ -162,6 +162,7 @@ def test_cpp_dropin_header_compiles(tmp_path):
                    "  b3GpuBroadphaseInterface::CreateFunc* f = b3GpuSapBroadphase::CreateFunc; delete f(0);\n"
                    "  float p[3], q[4]; np.getObjectTransformFromCpu(p, q, 0); np.setObjectTransformCpu(p, q, 0);\n"
                    "  bp.calculateOverlappingPairsHost(0); bp.getAllAabbsCPU(); rbp.copyConstraintsToHost();\n"
+                   "  std::vector<b3gRayInfo> rays(2); std::vector<b3gRayHit> hits(2); rbp.castRays(rays, hits);\n"
                    "  rbp.stepSimulation(1.f / 60.f); return rbp.getNumBodies();\n"
                    "}\n")
     r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-Wall", "-I", str(Path(ROOT, "include")), str(src)],

@@ -75,6 +75,14 @@ int main() {
     np->readbackAllBodiesToCpu();
     float p1[3], q1[4];
     ok = ok && np->getObjectTransformFromCpu(p1, q1, 13) && p1[1] > p0[1] + 0.05f;
+    // a ray straight down onto column (0, 0) hits its top box, the one just kicked
+    std::vector<b3gRayInfo> rays(1);
+    std::vector<b3gRayHit> hits(1);
+    rays[0].from = b3gFloat4{0.f, 20.f, 0.f, 0.f};
+    rays[0].to = b3gFloat4{0.f, -1.f, 0.f, 0.f};
+    hits[0].hitResult2 = -1;
+    rbp->castRays(rays, hits);
+    ok = ok && hits[0].hitFraction < 1.f && hits[0].hitBody == 13;
     b3GpuBroadphaseInterface::CreateFunc* create = b3GpuSapBroadphase::CreateFunc;
     b3GpuBroadphaseInterface* other = create(0);
     ok = ok && other != nullptr;
