@@ -21,7 +21,7 @@ ORACLE_DIR = ROOT / "oracle"
 ORACLE_LIB = ORACLE_DIR / "liboracle.so"
 
 CU_SOURCES = ["primitives.cu", "broadphase.cu", "narrowphase.cu", "solver.cu", "integrate.cu", "world.cu",
-              "noalloc.cu", "mlp.cu", "warmstart.cu", "primitives_capi.cu", "raycast.cu"]
+              "noalloc.cu", "mlp.cu", "warmstart.cu", "primitives_capi.cu", "raycast.cu", "joints.cu"]
 CPP_SOURCES = ["hull.cpp"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 

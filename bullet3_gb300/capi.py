@@ -27,12 +27,17 @@ PAIR = np.dtype([("x", "<i4"), ("y", "<i4"), ("z", "<i4"), ("w", "<i4")])
 RAY = np.dtype([("from", "<f4", 4), ("to", "<f4", 4)])
 RAYHIT = np.dtype([("hitFraction", "<f4"), ("hitBody", "<i4"), ("hitResult1", "<i4"), ("hitResult2", "<i4"),
                    ("hitPoint", "<f4", 4), ("hitNormal", "<f4", 4)])
+JOINT = np.dtype([("type", "<i4"), ("rbA", "<i4"), ("rbB", "<i4"), ("breakingImpulseThreshold", "<f4"),
+                  ("pivotInA", "<f4", 4), ("pivotInB", "<f4", 4), ("relTargetAB", "<f4", 4), ("flags", "<i4"),
+                  ("uid", "<i4"), ("pad", "<i4", 2)])
 for _dt, _sz in ((BODY, 80), (INERTIA, 96), (COLLIDABLE, 16), (HULL, 96), (FACE, 32), (AABB, 32), (CONTACT, 112),
-                 (PAIR, 16), (RAY, 32), (RAYHIT, 48)):
+                 (PAIR, 16), (RAY, 32), (RAYHIT, 48), (JOINT, 80)):
     assert _dt.itemsize == _sz, (_dt, _sz)
 
 SHAPE_CONVEX_HULL, SHAPE_PLANE, SHAPE_SPHERE = 3, 4, 7
 SOLVER_PGS, SOLVER_JACOBI = 0, 1
+JOINT_POINT2POINT, JOINT_FIXED = 3, 4
+CONSTRAINT_FLAG_ENABLED = 1
 PGS_PARTITIONS_AUTO, PGS_PARTITIONS_GLOBAL_DELTAS, PGS_PARTITIONS_NONE, PGS_PARTITIONS_SHARED = 0, 1, 2, 3
 PGS_PARTITIONS_STREAMED = 4
 WARM_COLD, WARM_LEARNED, WARM_RECORD, WARM_PERSISTENT, WARM_PERSISTENT_LEARNED = 0, 1, 2, 3, 4
@@ -85,7 +90,9 @@ _LIB = None
 EXPORTS = [
     "b3g_config_default", "b3g_create", "b3g_destroy", "b3g_last_error", "b3g_version", "b3g_register_sphere",
     "b3g_register_plane", "b3g_register_hull", "b3g_register_hull_tables", "b3g_register_body",
-    "b3g_write_all_to_gpu", "b3g_set_gravity", "b3g_set_solver", "b3g_set_scene_offsets", "b3g_autotune", "b3g_get_tuning", "b3g_profiler_range", "b3g_cast_rays", "b3g_step", "b3g_setup_aabbs",
+    "b3g_write_all_to_gpu", "b3g_set_gravity", "b3g_set_solver", "b3g_set_scene_offsets", "b3g_autotune", "b3g_get_tuning", "b3g_profiler_range", "b3g_cast_rays", "b3g_create_point2point_constraint", "b3g_create_fixed_constraint",
+    "b3g_remove_constraint", "b3g_get_num_constraints", "b3g_read_constraints", "b3g_read_joint_order",
+    "b3g_solve_joints", "b3g_step", "b3g_setup_aabbs",
     "b3g_calculate_overlapping_pairs", "b3g_compute_contacts", "b3g_solve_contacts", "b3g_integrate",
     "b3g_synchronize", "b3g_get_stats", "b3g_status", "b3g_get_num_bodies", "b3g_get_body_buffer",
     "b3g_get_inertia_buffer", "b3g_get_aabb_buffer", "b3g_get_pair_buffer", "b3g_get_contact_buffer",

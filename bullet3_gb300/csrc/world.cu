@@ -92,7 +92,25 @@ struct b3gWorld {
     b3g_mlp ws_mlp = nullptr;  // attached warm-start network (not owned)
     bool tuned = false;        // b3g_autotune ran on the current upload
     b3gTuning tuning{};        // its last result
+    // joints: the host registry; the device copy matches it (but for the enabled flags, which
+    // the device's break check clears) while joints_dirty is false
+    std::vector<b3gJoint> joints;
+    int next_joint_uid = 0;
+    bool joints_dirty = false;
+    std::vector<int> joint_order, joint_batch_off;
 };
+
+static b3gStatus sync_joint_flags(b3gWorld* h);
+
+static void free_joint_buffers(b3g::DeviceState& d) {
+    cudaFree(d.joints);
+    cudaFree(d.joint_rows);
+    cudaFree(d.joint_order);
+    cudaFree(d.joint_batch_off);
+    cudaFree(d.joint_uniq);
+    cudaFree(d.joint_mass);
+    cudaFree(d.joint_dv);
+}
 
 static void free_device(b3gWorld* w) {
     if (w->graph_exec) {
@@ -101,6 +119,7 @@ static void free_device(b3gWorld* w) {
     }
     for (void* p : w->allocations) cudaFree(p);
     w->allocations.clear();
+    free_joint_buffers(w->d);
     w->d = DeviceState();
     w->uploaded = false;
 }
@@ -433,7 +452,9 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     CUDA_TRY(cudaSetDevice(h->device));
     if (!h->stream) CUDA_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     cudaStreamSynchronize(h->stream);
+    if (sync_joint_flags(h) != B3G_OK) return B3G_ERR_CUDA;
     free_device(h);
+    h->joints_dirty = true;  // a new upload: batch and upload the joints again at the next solve
     h->tuned = false;
     h->tuning = b3gTuning{};
     DeviceState& d = h->d;
@@ -733,6 +754,238 @@ static void record(b3gWorld* h, int k) {
     if (h->profiling) cudaEventRecord(h->events.ev[k], h->stream);
 }
 
+// ---------------------------------------------------------------------------------- joints
+// b3GpuRigidBodyPipeline::createPoint2PointConstraint / createFixedConstraint /
+// removeConstraintByUid (b3GpuRigidBodyPipeline.cpp:159-219) keep a host list of
+// b3GpuGenericConstraint and clear the joint solver's batches; the batches are rebuilt before the
+// next solve.  Same here: every change marks the registry dirty, and the next step (or
+// b3g_solve_joints) batches and uploads it.
+
+// Copies the device's enabled flags (cleared by the break check) into the host registry; valid
+// while the device copy matches the registry.
+static b3gStatus sync_joint_flags(b3gWorld* h) {
+    DeviceState& d = h->d;
+    if (h->joints_dirty || !h->uploaded || d.num_joints <= 0 || !d.joints) return B3G_OK;
+    std::vector<b3gJoint> dev((size_t)d.num_joints);
+    CUDA_TRY(cudaMemcpyAsync(dev.data(), d.joints, sizeof(b3gJoint) * dev.size(), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    for (size_t i = 0; i < dev.size() && i < h->joints.size(); ++i) h->joints[i].flags = dev[i].flags;
+    return B3G_OK;
+}
+
+// sortConstraintByBatch3 (b3GpuPgsConstraintSolver.cpp:781-907) as the joint solver calls it
+// (simdWidth = numConstraints + 1, staticIdx = -1, b3GpuPgsConstraintSolver.cpp:193,641-644): a
+// body is "static" when its signed index is negative (inverse mass zero, index > 0; body 0 keeps
+// index 0 and so counts as dynamic).  Each pass over the joints not yet batched takes, in list
+// order, every joint whose non-static bodies no earlier joint of the pass took, and moves it to
+// the front by swapping it with the first unbatched entry.
+static void batch_joints(const std::vector<int>& sa, const std::vector<int>& sb, int num_bodies,
+                         std::vector<int>& order, std::vector<int>& offsets) {
+    const int n = (int)sa.size();
+    std::vector<int> A(sa), B(sb);
+    order.resize((size_t)n);
+    for (int i = 0; i < n; ++i) order[(size_t)i] = i;
+    offsets.assign(1, 0);
+    std::vector<uint32_t> used((size_t)num_bodies / 32 + 1, 0u);
+    std::vector<int> touched;
+    int done = 0;
+    while (done < n) {
+        for (int b : touched) used[(size_t)b / 32] = 0;
+        touched.clear();
+        int count = 0;
+        for (int i = done; i < n; ++i) {
+            const int as = A[(size_t)i], bs = B[(size_t)i];
+            const int a = as < 0 ? -as : as, b = bs < 0 ? -bs : bs;
+            const bool a_static = as < 0, b_static = bs < 0;
+            bool a_busy = false, b_busy = false;
+            if (!a_static) a_busy = (used[(size_t)a / 32] >> (a & 31)) & 1u;
+            if (!a_busy && !b_static) b_busy = (used[(size_t)b / 32] >> (b & 31)) & 1u;
+            if (a_busy || b_busy) continue;
+            if (!a_static) {
+                used[(size_t)a / 32] |= 1u << (a & 31);
+                touched.push_back(a);
+            }
+            if (!b_static) {
+                used[(size_t)b / 32] |= 1u << (b & 31);
+                touched.push_back(b);
+            }
+            if (i != done) {
+                std::swap(A[(size_t)i], A[(size_t)done]);
+                std::swap(B[(size_t)i], B[(size_t)done]);
+                std::swap(order[(size_t)i], order[(size_t)done]);
+            }
+            ++done;
+            ++count;
+        }
+        offsets.push_back(offsets.back() + count);
+    }
+}
+
+template <typename T>
+static b3gStatus joint_alloc(T** p, size_t count) {
+    cudaFree(*p);
+    *p = nullptr;
+    CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(p), (count ? count : 1) * sizeof(T)));
+    return B3G_OK;
+}
+
+// Batches and uploads a changed registry; the captured step graph is dropped when the joint
+// stage's shape changed.
+static b3gStatus prepare_joints(b3gWorld* h) {
+    if (!h->joints_dirty) return B3G_OK;
+    DeviceState& d = h->d;
+    cudaStream_t s = h->stream;
+    const int n = (int)h->joints.size();
+    if (h->graph_exec) {
+        cudaGraphExecDestroy(h->graph_exec);
+        h->graph_exec = nullptr;
+    }
+    d.num_joints = 0;
+    d.num_joint_batches = 0;
+    d.num_joint_uniq = 0;
+    d.max_joint_batch = 0;
+    h->joint_order.clear();
+    h->joint_batch_off.assign(1, 0);
+    if (n == 0) {
+        h->joints_dirty = false;
+        return B3G_OK;
+    }
+    if (n > d.joint_cap) {
+        const int cap = std::max(n, std::max(64, 2 * d.joint_cap));
+        TRY(joint_alloc(&d.joints, (size_t)cap));
+        TRY(joint_alloc(&d.joint_rows, 6 * (size_t)cap));
+        TRY(joint_alloc(&d.joint_order, (size_t)cap));
+        TRY(joint_alloc(&d.joint_batch_off, (size_t)cap + 1));
+        TRY(joint_alloc(&d.joint_uniq, 2 * (size_t)cap));
+        TRY(joint_alloc(&d.joint_mass, (size_t)cap));
+        d.joint_cap = cap;
+    }
+    if (d.joint_dv_bodies != d.num_bodies) {
+        TRY(joint_alloc(&d.joint_dv, 2 * (size_t)d.num_bodies));
+        CUDA_TRY(cudaMemsetAsync(d.joint_dv, 0, 2 * sizeof(float4) * (size_t)d.num_bodies, s));
+        d.joint_dv_bodies = d.num_bodies;
+    }
+    CUDA_TRY(cudaMemcpyAsync(d.joints, h->joints.data(), sizeof(b3gJoint) * (size_t)n, cudaMemcpyHostToDevice, s));
+    // signed body indices from the bodies' current inverse masses (initBatchConstraintsKernel,
+    // jointSolver.cl:400-419)
+    launch_joint_masses(d, n, d.joint_mass, s);
+    std::vector<float2> mass((size_t)n);
+    CUDA_TRY(cudaMemcpyAsync(mass.data(), d.joint_mass, sizeof(float2) * (size_t)n, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    std::vector<int> sa((size_t)n), sb((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        const b3gJoint& c = h->joints[(size_t)i];
+        sa[(size_t)i] = mass[(size_t)i].x != 0.f ? c.rbA : -c.rbA;
+        sb[(size_t)i] = mass[(size_t)i].y != 0.f ? c.rbB : -c.rbB;
+    }
+    batch_joints(sa, sb, d.num_bodies, h->joint_order, h->joint_batch_off);
+    std::vector<int> uniq;
+    uniq.reserve(2 * (size_t)n);
+    for (const b3gJoint& c : h->joints) {
+        uniq.push_back(c.rbA);
+        uniq.push_back(c.rbB);
+    }
+    std::sort(uniq.begin(), uniq.end());
+    uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+    int widest = 0;
+    for (size_t b = 0; b + 1 < h->joint_batch_off.size(); ++b)
+        widest = std::max(widest, h->joint_batch_off[b + 1] - h->joint_batch_off[b]);
+    CUDA_TRY(cudaMemcpyAsync(d.joint_order, h->joint_order.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(d.joint_batch_off, h->joint_batch_off.data(), sizeof(int) * h->joint_batch_off.size(),
+                             cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(d.joint_uniq, uniq.data(), sizeof(int) * uniq.size(), cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors above are locals
+    d.num_joints = n;
+    d.num_joint_batches = (int)h->joint_batch_off.size() - 1;
+    d.num_joint_uniq = (int)uniq.size();
+    d.max_joint_batch = widest;
+    h->joints_dirty = false;
+    return B3G_OK;
+}
+
+static b3gStatus add_joint(b3gWorld* h, int type, int body_a, int body_b, const float* pa, const float* pb,
+                           const float* rel, float threshold, int* out_uid) {
+    if (!h || !pa || !pb) return fail(B3G_ERR_INVALID_ARG, "null argument");
+    const int nb = (int)h->bodies.size();
+    if (body_a < 0 || body_a >= nb || body_b < 0 || body_b >= nb)
+        return fail(B3G_ERR_INVALID_INDEX, "joint body index out of range (%d, %d of %d bodies)", body_a, body_b, nb);
+    if (body_a == body_b) return fail(B3G_ERR_INVALID_ARG, "a joint needs two different bodies");
+    TRY(sync_joint_flags(h));
+    b3gJoint c;
+    std::memset(&c, 0, sizeof(c));
+    c.type = type;
+    c.rbA = body_a;
+    c.rbB = body_b;
+    c.breakingImpulseThreshold = threshold;
+    c.pivotInA = b3gFloat4{pa[0], pa[1], pa[2], 0.f};
+    c.pivotInB = b3gFloat4{pb[0], pb[1], pb[2], 0.f};
+    if (rel) c.relTargetAB = b3gFloat4{rel[0], rel[1], rel[2], rel[3]};
+    c.flags = 1;
+    c.uid = h->next_joint_uid++;
+    h->joints.push_back(c);
+    h->joints_dirty = true;
+    if (out_uid) *out_uid = c.uid;
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_create_point2point_constraint(b3g_handle h, int body_a, int body_b, const float pivot_in_a[3],
+                                                       const float pivot_in_b[3], float breaking_threshold,
+                                                       int* out_uid) {
+    return add_joint(h, B3G_JOINT_POINT2POINT, body_a, body_b, pivot_in_a, pivot_in_b, nullptr, breaking_threshold,
+                     out_uid);
+}
+
+extern "C" b3gStatus b3g_create_fixed_constraint(b3g_handle h, int body_a, int body_b, const float pivot_in_a[3],
+                                                 const float pivot_in_b[3], const float rel_target_ab[4],
+                                                 float breaking_threshold, int* out_uid) {
+    if (!rel_target_ab) return fail(B3G_ERR_INVALID_ARG, "null relative target");
+    return add_joint(h, B3G_JOINT_FIXED, body_a, body_b, pivot_in_a, pivot_in_b, rel_target_ab, breaking_threshold,
+                     out_uid);
+}
+
+extern "C" b3gStatus b3g_remove_constraint(b3g_handle h, int uid) {
+    if (!h) return fail(B3G_ERR_INVALID_ARG, "null handle");
+    TRY(sync_joint_flags(h));
+    for (size_t i = 0; i < h->joints.size(); ++i) {
+        if (h->joints[i].uid == uid) {  // swap with the last and pop, as the reference does
+            std::swap(h->joints[i], h->joints.back());
+            h->joints.pop_back();
+            h->joints_dirty = true;
+            return B3G_OK;
+        }
+    }
+    return fail(B3G_ERR_INVALID_INDEX, "no joint with uid %d", uid);
+}
+
+extern "C" b3gStatus b3g_get_num_constraints(b3g_handle h, int* n) {
+    if (!h || !n) return fail(B3G_ERR_INVALID_ARG, "null argument");
+    *n = (int)h->joints.size();
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_read_constraints(b3g_handle h, void* host_joints, int capacity, int* n) {
+    if (!h || (!host_joints && capacity > 0)) return fail(B3G_ERR_INVALID_ARG, "null argument");
+    if (h->uploaded) CUDA_TRY(cudaSetDevice(h->device));
+    TRY(sync_joint_flags(h));
+    const int m = std::min(capacity, (int)h->joints.size());
+    if (m > 0) std::memcpy(host_joints, h->joints.data(), sizeof(b3gJoint) * (size_t)m);
+    if (n) *n = (int)h->joints.size();
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_read_joint_order(b3g_handle h, int* order, int capacity, int* batch_offsets,
+                                          int offsets_capacity, int* num_batches) {
+    if (!h) return fail(B3G_ERR_INVALID_ARG, "null handle");
+    if (h->joints_dirty) return fail(B3G_ERR_INVALID_ARG, "joints changed since the last joint solve");
+    const int n = (int)h->joint_order.size(), nb = (int)h->joint_batch_off.size();
+    if ((order && capacity < n) || (batch_offsets && offsets_capacity < nb))
+        return fail(B3G_ERR_CAPACITY, "need %d order and %d offset entries", n, nb);
+    if (order && n) std::memcpy(order, h->joint_order.data(), sizeof(int) * (size_t)n);
+    if (batch_offsets && nb) std::memcpy(batch_offsets, h->joint_batch_off.data(), sizeof(int) * (size_t)nb);
+    if (num_batches) *num_batches = nb > 0 ? nb - 1 : 0;
+    return B3G_OK;
+}
+
 static void enqueue_step(b3gWorld* h, float dt, bool with_events) {
     cudaStream_t s = h->stream;
     DeviceState& d = h->d;
@@ -744,7 +997,8 @@ static void enqueue_step(b3gWorld* h, float dt, bool with_events) {
     if (with_events) record(h, 2);
     n += launch_contacts(d, h->cfg.contact_friction, s);
     if (with_events) record(h, 3);
-    // batching is fused into the solver kernel; stage 3->4 is empty
+    // stage 3->4: the joints (contact batching is fused into the solver kernel)
+    n += launch_joints(d, h->cfg, s);
     if (with_events) record(h, 4);
     n += launch_solver(d, h->cfg, dt, s);
     if (with_events) record(h, 5);
@@ -758,6 +1012,7 @@ extern "C" b3gStatus b3g_step(b3g_handle h, float dt) {
     REQUIRE_UPLOADED(h);
     if (!(dt > 0.f)) return fail(B3G_ERR_INVALID_ARG, "dt must be positive");
     CUDA_TRY(cudaSetDevice(h->device));
+    TRY(prepare_joints(h));
     if (h->cfg.autotune && !h->tuned) TRY(b3g_autotune(h, dt, 3, nullptr));
     if (h->profiling || !h->cfg.use_cuda_graph) {
         enqueue_step(h, dt, h->profiling);
@@ -992,6 +1247,13 @@ extern "C" b3gStatus b3g_calculate_overlapping_pairs(b3g_handle h) {
 extern "C" b3gStatus b3g_compute_contacts(b3g_handle h) {
     REQUIRE_UPLOADED(h);
     h->launches += launch_contacts(h->d, h->cfg.contact_friction, h->stream);
+    TRY(check_launch(h));
+    return B3G_OK;
+}
+extern "C" b3gStatus b3g_solve_joints(b3g_handle h) {
+    REQUIRE_UPLOADED(h);
+    TRY(prepare_joints(h));
+    h->launches += launch_joints(h->d, h->cfg, h->stream);
     TRY(check_launch(h));
     return B3G_OK;
 }

@@ -51,6 +51,15 @@ struct SolverPoints {
     float4* imp = nullptr;   // [4m+j]   applied impulses: contact, dir2, dir1, (unused)
 };
 
+// One joint row (b3SolverConstraint's fields a joint row uses, jointSolver.cl:129-160), 80 B.
+struct JointRow {
+    float4 n_rhs;     // J1 linear axis (contact normal) xyz, w = rhs
+    float4 r1_jinv;   // J1 angular axis xyz, w = jacDiagABInv
+    float4 r2_lo;     // J2 angular axis xyz, w = lower limit
+    float4 angA_hi;   // angular component A xyz, w = upper limit
+    float4 angB_imp;  // angular component B xyz, w = applied impulse
+};
+
 // Launch shapes chosen by the autotuner (b3g_autotune); the defaults are the untuned shapes.
 struct LaunchTuning {
     int pgs_partitions = -1;        // B3G_PGS_PARTITIONS_* used when the config says AUTO (-1: rule)
@@ -67,6 +76,17 @@ struct DeviceState {
     float4* ray_buf = nullptr;    // b3g_cast_rays: rays (2 float4 each) and hits, grown on demand
     b3gRayHit* hit_buf = nullptr;
     int ray_cap = 0;
+    // joints (own allocations, grown on demand; the host registry is authoritative except for
+    // the enabled flags, which the device's break check clears)
+    b3gJoint* joints = nullptr;
+    JointRow* joint_rows = nullptr;  // 6 per joint
+    int* joint_order = nullptr;      // joint indices batch by batch
+    int* joint_batch_off = nullptr;  // num_joint_batches + 1
+    int* joint_uniq = nullptr;       // the bodies joints name, once each
+    float2* joint_mass = nullptr;    // batching scratch: both bodies' inverse masses per joint
+    float4* joint_dv = nullptr;      // 2 per body
+    int joint_cap = 0, joint_dv_bodies = 0;
+    int num_joints = 0, num_joint_batches = 0, num_joint_uniq = 0, max_joint_batch = 0;
     // sizes fixed at upload
     int num_bodies = 0, num_dynamic = 0, num_large = 0, num_collidables = 0;
     int max_pairs = 0, max_contacts = 0;
@@ -180,6 +200,8 @@ int launch_aabbs(DeviceState& d, cudaStream_t s);
 int launch_pairs(DeviceState& d, cudaStream_t s);
 int launch_cells(DeviceState& d, cudaStream_t s);
 int launch_cast_rays(DeviceState& d, const float4* rays, b3gRayHit* hits, int n, cudaStream_t s);
+long long launch_joints(DeviceState& d, const b3gConfig& cfg, cudaStream_t s);
+long long launch_joint_masses(const DeviceState& d, int n, float2* out, cudaStream_t s);
 int launch_contacts(DeviceState& d, float friction, cudaStream_t s);
 int launch_compact_contacts(DeviceState& d, cudaStream_t s);
 int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s);

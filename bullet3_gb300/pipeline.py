@@ -362,6 +362,59 @@ class b3GpuRigidBodyPipeline:
     def writeAllInstancesToGpu(self):
         self.m_narrowphase.writeAllBodiesToGpu()
 
+    # joints (b3GpuRigidBodyPipeline.cpp:159-219); solved every step right before the contacts
+    def createPoint2PointConstraint(self, bodyA: int, bodyB: int, pivotInA, pivotInB,
+                                    breakingThreshold: float) -> int:
+        """Ball joint: pivotInA (in A's frame) and pivotInB (in B's frame) are held together.  Returns
+        the joint's uid.  Breaks for good once a row's impulse reaches breakingThreshold."""
+        uid = C.c_int()
+        pa = (C.c_float * 3)(*[float(x) for x in pivotInA[:3]])
+        pb = (C.c_float * 3)(*[float(x) for x in pivotInB[:3]])
+        call("b3g_create_point2point_constraint", self._h, C.c_int(bodyA), C.c_int(bodyB), pa, pb,
+             C.c_float(breakingThreshold), C.byref(uid))
+        return uid.value
+
+    def createFixedConstraint(self, bodyA: int, bodyB: int, pivotInA, pivotInB, relTargetAB,
+                              breakingThreshold: float) -> int:
+        """Point to point plus the relative orientation ornA * ornB^-1 held at relTargetAB (x, y, z, w)."""
+        uid = C.c_int()
+        pa = (C.c_float * 3)(*[float(x) for x in pivotInA[:3]])
+        pb = (C.c_float * 3)(*[float(x) for x in pivotInB[:3]])
+        rel = (C.c_float * 4)(*[float(x) for x in relTargetAB[:4]])
+        call("b3g_create_fixed_constraint", self._h, C.c_int(bodyA), C.c_int(bodyB), pa, pb, rel,
+             C.c_float(breakingThreshold), C.byref(uid))
+        return uid.value
+
+    def removeConstraintByUid(self, uid: int):
+        call("b3g_remove_constraint", self._h, C.c_int(uid))
+
+    def getNumConstraints(self) -> int:
+        n = C.c_int()
+        call("b3g_get_num_constraints", self._h, C.byref(n))
+        return n.value
+
+    def copyConstraintsToHost(self) -> np.ndarray:
+        """The joints (b3GpuGenericConstraint layout) with the enabled flags as the device left them."""
+        n = self.getNumConstraints()
+        out = np.zeros(n, capi.JOINT)
+        if n:
+            got = C.c_int()
+            call("b3g_read_constraints", self._h, C.c_void_p(out.ctypes.data), C.c_int(n), C.byref(got))
+        return out
+
+    def readJointOrder(self):
+        """(joint indices batch by batch, batch offsets) of the last joint solve."""
+        n = self.getNumConstraints()
+        order = np.zeros(max(1, n), np.int32)
+        off = np.zeros(n + 2, np.int32)
+        nb = C.c_int()
+        call("b3g_read_joint_order", self._h, iptr(order), C.c_int(n), iptr(off), C.c_int(n + 2), C.byref(nb))
+        return order[:n], off[:nb.value + 1]
+
+    def solveJoints(self):
+        """The joint stage alone (b3GpuPgsConstraintSolver::solveJoints)."""
+        call("b3g_solve_joints", self._h)
+
     def setGravity(self, grav):
         g = (C.c_float * 3)(*[float(x) for x in grav[:3]])
         call("b3g_set_gravity", self._h, g)
@@ -462,18 +515,6 @@ class b3GpuRigidBodyPipeline:
         n = C.c_longlong()
         call("b3g_get_launch_count", self._h, C.byref(n))
         return n.value
-
-    # joints are outside this GPU step: the reference API exists, the call reports -1
-    def createPoint2PointConstraint(self, *a, **k) -> int:
-        b3Error("createPoint2PointConstraint: joints are not supported by this GPU step")
-        return -1
-
-    def createFixedConstraint(self, *a, **k) -> int:
-        b3Error("createFixedConstraint: joints are not supported by this GPU step")
-        return -1
-
-    def removeConstraintByUid(self, uid: int):
-        b3Error("removeConstraintByUid: joints are not supported by this GPU step")
 
     def castRays(self, rays, hitResults=None) -> np.ndarray:
         """b3GpuRigidBodyPipeline::castRays: rays as a capi.RAY array (from, to; from[3] = scene in a

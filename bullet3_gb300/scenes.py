@@ -32,6 +32,7 @@ class Scene:
     cell: float = 0.0                                 # grid cell size (0 = automatic)
     name: str = ""
     pairs_per_body: int = 0                           # pair capacity hint (0 = the library default)
+    joints: list = field(default_factory=list)        # dicts: type p2p/fixed, a, b, pivot_a, pivot_b, rel, threshold
 
     @property
     def num_bodies(self) -> int:
@@ -294,6 +295,123 @@ def stress_container(n=1048576, width=128.0, depth=128.0, height=512.0, seed=0, 
     return sc
 
 
+def hanging_chains(n_chains=8, links=12, spacing=1.0, radius=0.2, seed=0, fixed_every=0, threshold=1e30,
+                   anchor_index=0, ground=False, swing=1.0, random_orn=True) -> Scene:
+    """Chains of spheres hanging from one static anchor box, neighbours joined by ball joints at
+    the midpoint (every fixed_every-th joint a fixed joint holding the initial relative
+    orientation).  The anchor is body `anchor_index` (0 or the last body).  Links start with
+    random horizontal velocities of about `swing` m/s; chains are 3 apart, links do not touch.
+    random_orn=False starts every link unrotated (the fixed joints' target is then the identity,
+    the case the reference's fixed-joint rows are built for: they drive wA - wB, the rate of the
+    orientation error only while ornA ornB^-1 is near the identity)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    top = links * spacing + 2.0
+    nb = n_chains * links + 1 + (1 if ground else 0)
+    sc = Scene(name=f"chains{n_chains}x{links}")
+    sc.shapes = [{"type": "hull", "verts": box_vertices(1.5 * n_chains + 1.0, 0.1, 1.0)},
+                 {"type": "sphere", "radius": radius}]
+    if ground:
+        sc.shapes.append({"type": "plane", "normal": (0.0, 1.0, 0.0), "constant": 0.0})
+    shape = np.ones(nb, np.int32)
+    mass = np.ones(nb, np.float32)
+    pos = np.zeros((nb, 3), np.float32)
+    orn = np.tile(np.array([0, 0, 0, 1], np.float32), (nb, 1))
+    anchor = 0 if anchor_index == 0 else nb - 1 - (1 if ground else 0)
+    dyn = [i for i in range(nb - (1 if ground else 0)) if i != anchor]
+    shape[anchor], mass[anchor] = 0, 0.0
+    pos[anchor] = (0.0, top, 0.0)
+    if ground:
+        shape[nb - 1], mass[nb - 1] = 2, 0.0
+    if random_orn:
+        orn[dyn] = random_quaternions(rng, len(dyn))
+    lin = np.zeros((nb, 3), np.float32)
+    k = 0
+    for c in range(n_chains):
+        x = 3.0 * (c - (n_chains - 1) / 2)
+        prev = None
+        for l in range(links):
+            i = dyn[k]
+            k += 1
+            pos[i] = (x, top - (l + 1) * spacing, 0.0)
+            lin[i] = (rng.uniform(-swing, swing), 0.0, rng.uniform(-swing, swing))
+            jt = "fixed" if fixed_every and (l % fixed_every == fixed_every - 1) else "p2p"
+            if prev is None:
+                a, pa = anchor, (x, -0.5 * spacing, 0.0)
+            else:
+                a, pa = prev, None
+            j = {"type": jt, "a": a, "b": i, "threshold": threshold}
+            # pivots in each body's own frame: the midpoint between the two centres
+            mid = pos[i] + np.array([0.0, 0.5 * spacing, 0.0], np.float32)
+            j["pivot_a"] = _to_local(mid - pos[a], orn[a])
+            j["pivot_b"] = _to_local(mid - pos[i], orn[i])
+            j["rel"] = _qmul(orn[a], _qconj(orn[i]))
+            sc.joints.append(j)
+            prev = i
+    sc.body_shape, sc.mass, sc.pos, sc.orn, sc.linvel = shape, mass, pos, orn, lin
+    return sc
+
+
+def welded_pairs(n_pairs=64, seed=0, twist=0.3, threshold=1e30) -> Scene:
+    """Pairs of boxes far apart from each other, each pair joined by a fixed joint whose target
+    relative orientation is the initial one turned by up to `twist` radians, with random spins."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sc = Scene(name=f"welded{n_pairs}")
+    sc.shapes = [{"type": "hull", "verts": box_vertices(0.4, 0.3, 0.2)}]
+    nb = 2 * n_pairs
+    pos = np.zeros((nb, 3), np.float32)
+    g = int(np.ceil(np.sqrt(n_pairs)))
+    orn = random_quaternions(rng, nb)
+    for p in range(n_pairs):
+        base = np.array([4.0 * (p % g), 10.0, 4.0 * (p // g)], np.float32)
+        pos[2 * p] = base
+        pos[2 * p + 1] = base + np.array([1.2, 0.0, 0.0], np.float32)
+        axis = rng.standard_normal(3)
+        axis /= np.linalg.norm(axis)
+        ang = rng.uniform(-twist, twist)
+        dq = np.array([*(np.sin(ang / 2) * axis), np.cos(ang / 2)], np.float32)
+        mid = pos[2 * p] + np.array([0.6, 0.0, 0.0], np.float32)
+        sc.joints.append({"type": "fixed", "a": 2 * p, "b": 2 * p + 1, "threshold": threshold,
+                          "pivot_a": _to_local(mid - pos[2 * p], orn[2 * p]),
+                          "pivot_b": _to_local(mid - pos[2 * p + 1], orn[2 * p + 1]),
+                          "rel": _qmul(dq, _qmul(orn[2 * p], _qconj(orn[2 * p + 1])))})
+    sc.body_shape = np.zeros(nb, np.int32)
+    sc.mass = rng.uniform(0.5, 2.0, nb).astype(np.float32)
+    sc.pos, sc.orn = pos, orn
+    sc.linvel = rng.standard_normal((nb, 3)).astype(np.float32)
+    sc.angvel = (2.0 * rng.standard_normal((nb, 3))).astype(np.float32)
+    return sc
+
+
+def _qconj(q):
+    return np.array([-q[0], -q[1], -q[2], q[3]], np.float32)
+
+
+def _qmul(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    v = np.cross(a[:3], b[:3]) + a[3] * b[:3] + b[3] * a[:3]
+    return np.array([*v, a[3] * b[3] - np.dot(a[:3], b[:3])], np.float32)
+
+
+def _to_local(v, q):
+    """v (world) in the frame of orientation q: q^-1 v q."""
+    r = _qmul(_qmul(_qconj(q), [*v, 0.0]), q)
+    return r[:3].astype(np.float32)
+
+
+def add_joints(pipeline, joints) -> list:
+    """Registers joint dicts (as Scene.joints holds them) on a pipeline; returns their uids."""
+    uids = []
+    for j in joints:
+        if j["type"] == "fixed":
+            uids.append(pipeline.createFixedConstraint(j["a"], j["b"], j["pivot_a"], j["pivot_b"], j["rel"],
+                                                       j["threshold"]))
+        else:
+            uids.append(pipeline.createPoint2PointConstraint(j["a"], j["b"], j["pivot_a"], j["pivot_b"],
+                                                             j["threshold"]))
+    return uids
+
+
 def load_scene(scene: Scene, config=None, device: int = 0, upload: bool = True):
     """Register a Scene through the reference-style API; returns (narrowphase, broadphase, pipeline)."""
     from .pipeline import b3Config, b3GpuGridBroadphase, b3GpuNarrowPhase, b3GpuRigidBodyPipeline
@@ -330,6 +448,8 @@ def load_scene(scene: Scene, config=None, device: int = 0, upload: bool = True):
             raise RuntimeError("body registration failed")
     if getattr(scene, "scene_first", None) is not None:
         pl.setSceneOffsets(scene.scene_first)
+    if scene.joints:
+        add_joints(pl, scene.joints)
     if upload:
         pl.writeAllInstancesToGpu()
         if scene.linvel is not None or scene.angvel is not None:

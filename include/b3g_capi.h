@@ -32,7 +32,7 @@ typedef enum b3gStatus {
     B3G_ERR_CAPACITY = 3,         /* a b3Config capacity was exceeded (b3GpuNarrowPhase.cpp:821-825) */
     B3G_ERR_CUDA = 4,             /* a CUDA runtime call failed; see b3g_last_error() */
     B3G_ERR_NOT_UPLOADED = 5,     /* step/stage called before b3g_write_all_to_gpu */
-    B3G_ERR_UNSUPPORTED = 6,      /* compound / concave shapes, joints */
+    B3G_ERR_UNSUPPORTED = 6,      /* compound / concave shapes */
     B3G_ERR_BARRIER_TIMEOUT = 7,  /* a persistent kernel's bounded grid barrier gave up */
     B3G_ERR_DEGENERATE = 8        /* convex hull input is degenerate (fewer than 4 affinely independent points) */
 } b3gStatus;
@@ -210,6 +210,29 @@ b3gStatus b3g_get_tuning(b3g_handle h, b3gTuning* out);
  * off should capture (cudaProfilerStart / cudaProfilerStop; no reference counterpart). */
 b3gStatus b3g_profiler_range(int on);
 
+/* ------------------------------------------------------------------ joints */
+/* b3GpuRigidBodyPipeline::createPoint2PointConstraint / createFixedConstraint / removeConstraintByUid
+ * (b3GpuRigidBodyPipeline.cpp:159-219).  Joints are solved every step right before the contacts,
+ * as b3GpuPgsConstraintSolver::solveJoints does (b3GpuPgsConstraintSolver.cpp:927-944: PGS, 4
+ * iterations, dt 1/60, erp 0.2, damping 1, batches from a greedy colouring of the joints): rows
+ * from getInfo2Point2Point / getInfo2FixedOrientation (kernels/jointSolver.cl:488-630), a joint
+ * whose row impulse reaches its breaking threshold is disabled for good.  Joints may be created
+ * and removed before or after the upload; *out_uid is the joint's id. */
+#define B3G_JOINT_POINT2POINT 3
+#define B3G_JOINT_FIXED 4
+b3gStatus b3g_create_point2point_constraint(b3g_handle h, int body_a, int body_b, const float pivot_in_a[3],
+                                            const float pivot_in_b[3], float breaking_threshold, int* out_uid);
+b3gStatus b3g_create_fixed_constraint(b3g_handle h, int body_a, int body_b, const float pivot_in_a[3],
+                                      const float pivot_in_b[3], const float rel_target_ab[4],
+                                      float breaking_threshold, int* out_uid);
+b3gStatus b3g_remove_constraint(b3g_handle h, int uid);
+b3gStatus b3g_get_num_constraints(b3g_handle h, int* n);
+/* the joints (b3gJoint == b3GpuGenericConstraint, flags as the device last left them) and the
+ * order the solver sweeps them in: joint indices batch by batch, batch_offsets[num_batches + 1] */
+b3gStatus b3g_read_constraints(b3g_handle h, void* host_joints, int capacity, int* n);
+b3gStatus b3g_read_joint_order(b3g_handle h, int* order, int capacity, int* batch_offsets, int offsets_capacity,
+                               int* num_batches);
+
 /* ------------------------------------------------------------------ ray casts */
 /* b3GpuRigidBodyPipeline::castRays (b3GpuRigidBodyPipeline.cpp) -> b3GpuRaycast::castRays
  * (Bullet3OpenCL/Raycast/b3GpuRaycast.cpp:248-373): n rays (b3gRayInfo == b3RayInfo) from host
@@ -255,6 +278,7 @@ b3gStatus b3g_step(b3g_handle h, float dt);
 b3gStatus b3g_setup_aabbs(b3g_handle h);                     /* setupGpuAabbsFull :500-575 */
 b3gStatus b3g_calculate_overlapping_pairs(b3g_handle h);     /* b3GpuGridBroadphase::calculateOverlappingPairs :117-259 */
 b3gStatus b3g_compute_contacts(b3g_handle h);                /* b3GpuNarrowPhase::computeContacts :751-809 */
+b3gStatus b3g_solve_joints(b3g_handle h);                    /* b3GpuPgsConstraintSolver::solveJoints :927-944 */
 b3gStatus b3g_solve_contacts(b3g_handle h, float dt);        /* b3GpuPgsContactSolver::solveContacts :568-1103 */
 b3gStatus b3g_integrate(b3g_handle h, float dt);             /* b3GpuRigidBodyPipeline::integrate :465-498 */
 /* Waits for the world's stream. */
@@ -305,8 +329,9 @@ b3gStatus b3g_read_shape_tables(b3g_handle h, void* collidables, void* hulls, vo
 /* ------------------------------------------------------------------ stage profiling */
 /* Records CUDA events around each stage on the world's stream when on=1. */
 b3gStatus b3g_set_profiling(b3g_handle h, int on);
-/* Milliseconds per stage of the last profiled step: aabb, pairs, contacts, batching,
- * setup, solve, integrate (7 floats). */
+/* Milliseconds per stage of the last profiled step: aabb, pairs, contacts, joints (the
+ * reference's batching slot: contact batching is fused into the solve), setup, solve,
+ * integrate (7 floats). */
 b3gStatus b3g_get_stage_times(b3g_handle h, float* ms7);
 /* Number of kernels this library launched since creation (counted on the host at launch). */
 b3gStatus b3g_get_launch_count(b3g_handle h, long long* n);

@@ -304,9 +304,40 @@ public:
     int getNumBodies() const { return m_np->getNumRigidBodies(); }
     void* getBodyBuffer() { return m_np->getBodiesGpu(); }
     void reset() { b3Error("reset: re-create the pipeline (registries are fixed once uploaded)"); }
-    /* joints and ray casts are outside this GPU step: the reference API exists and reports failure */
-    void copyConstraintsToHost() {}
-    void removeConstraintByUid(int) { std::fprintf(stderr, "b3Error: removeConstraintByUid: joints are not supported\n"); }
+    /* joints (b3GpuRigidBodyPipeline.h:52-58): solved every step right before the contacts.  The
+       host copy (b3gJoint == b3GpuGenericConstraint) carries the enabled flags as the device's break
+       check left them after copyConstraintsToHost(). */
+    void copyConstraintsToHost() {
+        int n = 0;
+        b3g_get_num_constraints(m_np->world(), &n);
+        m_constraints.resize((size_t)n);
+        if (n > 0 && b3g_read_constraints(m_np->world(), m_constraints.data(), n, &n) != B3G_OK)
+            b3Error("copyConstraintsToHost");
+    }
+    const std::vector<b3gJoint>& getConstraintsCPU() const { return m_constraints; }
+    void removeConstraintByUid(int uid) {
+        if (b3g_remove_constraint(m_np->world(), uid) != B3G_OK) b3Error("removeConstraintByUid");
+    }
+    int createPoint2PointConstraint(int bodyA, int bodyB, const float* pivotInA, const float* pivotInB,
+                                    float breakingThreshold) {
+        int uid = -1;
+        if (b3g_create_point2point_constraint(m_np->world(), bodyA, bodyB, pivotInA, pivotInB, breakingThreshold,
+                                              &uid) != B3G_OK) {
+            b3Error("createPoint2PointConstraint");
+            return -1;
+        }
+        return uid;
+    }
+    int createFixedConstraint(int bodyA, int bodyB, const float* pivotInA, const float* pivotInB,
+                              const float* relTargetAB, float breakingThreshold) {
+        int uid = -1;
+        if (b3g_create_fixed_constraint(m_np->world(), bodyA, bodyB, pivotInA, pivotInB, relTargetAB,
+                                        breakingThreshold, &uid) != B3G_OK) {
+            b3Error("createFixedConstraint");
+            return -1;
+        }
+        return uid;
+    }
     /* castRays(rays, hitResults) (b3GpuRigidBodyPipeline.h:63): arrays of b3RayInfo / b3RayHit (or
        b3gRayInfo / b3gRayHit, the same layouts) of equal size; hitResults[i].m_hitResult2 names a
        body the ray ignores */
@@ -319,19 +350,12 @@ public:
         }
         if (n > 0 && b3g_cast_rays(m_np->world(), &rays[0], &hitResults[0], n) != B3G_OK) b3Error("castRays");
     }
-    int createPoint2PointConstraint(int, int, const float*, const float*, float) {
-        std::fprintf(stderr, "b3Error: createPoint2PointConstraint: joints are not supported\n");
-        return -1;
-    }
-    int createFixedConstraint(int, int, const float*, const float*, const float*, const float*, float) {
-        std::fprintf(stderr, "b3Error: createFixedConstraint: joints are not supported\n");
-        return -1;
-    }
 
 private:
     b3GpuNarrowPhase* m_np;
     b3GpuGridBroadphase* m_bp;
     b3Config m_config;
+    std::vector<b3gJoint> m_constraints;
 };
 
 }  // namespace b3g_compat

@@ -14,6 +14,7 @@
  *   b3gPair        == b3Int4 overlapping pair (x=bodyA, y=bodyB, z=contact index or -1, w=-1)                  16 B
  *   b3gRayInfo     == b3RayInfo            (Bullet3Collision/NarrowPhaseCollision/b3RaycastInfo.h:7)          32 B
  *   b3gRayHit      == b3RayHit             (same file :14)                                                    48 B
+ *   b3gJoint       == b3GpuGenericConstraint (Bullet3OpenCL/RigidBody/b3GpuGenericConstraint.h:77)            80 B
  * Shape type codes follow b3ShapeTypes (b3Collidable.h:8).
  */
 #ifndef B3G_TYPES_H
@@ -98,6 +99,18 @@ typedef struct b3gContact4 {
 } b3gContact4;
 
 typedef struct b3gPair { int x, y, z, w; } b3gPair;
+
+typedef struct b3gJoint {
+    int type;            /* 3 point to point, 4 fixed (b3GpuGenericConstraintType) */
+    int rbA, rbB;
+    float breakingImpulseThreshold;
+    b3gFloat4 pivotInA;
+    b3gFloat4 pivotInB;
+    b3gFloat4 relTargetAB;  /* fixed: target relative orientation (quaternion x, y, z, w) */
+    int flags;           /* 1 = enabled; 0 once broken */
+    int uid;
+    int padding[2];
+} b3gJoint;
 
 typedef struct b3gRayInfo {
     b3gFloat4 from;  /* w: the ray's scene in a world of several scenes (b3g_set_scene_offsets) */

@@ -1343,3 +1343,219 @@ void oracle_cast_rays(const obody* bodies, int nbodies, const oshapes* sh, const
         }
     }
 }
+
+/* ------------------------------------------------------------------ joints */
+/* The joint kernels' quaternion product is the ray kernels' (cl_qmul / cl_qrot above:
+ * jointSolver.cl:222-262 has the same qtMul / qtRotate). */
+
+/* acos for getAngle (jointSolver.cl:557-572): asin(z) = sum (2n)!/(4^n n!^2 (2n+1)) z^(2n+1),
+ * 12 terms in Horner form, with acos(x) = 2 asin(sqrt((1-x)/2)) for x > 1/2,
+ * pi - 2 asin(sqrt((1+x)/2)) for x < -1/2, pi/2 - asin(x) between. */
+static const float j_asin[11] = {0.166666672f,   0.075000003f,   0.0446428582f,  0.030381944f,
+                                 0.0223721582f,  0.0173527636f,  0.0139648439f,  0.0115518011f,
+                                 0.00976160914f, 0.00839033537f, 0.007312526f};
+static float j_asin_series(float z) {
+    float t = z * z, p = j_asin[10];
+    int i;
+    for (i = 9; i >= 0; --i) p = j_asin[i] + t * p;
+    return z + (z * t) * p;
+}
+float oracle_joint_acos(float x) {
+    if (x > 0.5f) return 2.0f * j_asin_series(sqrtf((1.0f - x) * 0.5f));
+    if (x < -0.5f) return 3.14159274f - 2.0f * j_asin_series(sqrtf((1.0f + x) * 0.5f));
+    return 1.57079637f - j_asin_series(x);
+}
+
+int oracle_joint_batches(const ojoint* joints, int n, const obody* bodies, int nbodies, int* order, int* batch_off) {
+    int *A = (int*)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1)), *B = (int*)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    unsigned* used = (unsigned*)calloc((size_t)nbodies / 32 + 1, sizeof(unsigned));
+    int i, valid = 0, nb = 0;
+    for (i = 0; i < n; i++) {
+        A[i] = bodies[joints[i].rbA].invMass != 0.f ? joints[i].rbA : -joints[i].rbA;
+        B[i] = bodies[joints[i].rbB].invMass != 0.f ? joints[i].rbB : -joints[i].rbB;
+        order[i] = i;
+    }
+    batch_off[0] = 0;
+    while (valid < n) {
+        int count = 0;
+        memset(used, 0, sizeof(unsigned) * ((size_t)nbodies / 32 + 1));
+        for (i = valid; i < n; i++) {
+            int as = A[i], bs = B[i], a = abs(as), b = abs(bs);
+            int a_static = as < 0 || as == -1, b_static = bs < 0 || bs == -1; /* staticIdx = -1 */
+            int a_busy = 0, b_busy = 0;
+            if (!a_static) a_busy = (used[a / 32] >> (a & 31)) & 1u;
+            if (!a_busy && !b_static) b_busy = (used[b / 32] >> (b & 31)) & 1u;
+            if (a_busy || b_busy) continue;
+            if (!a_static) used[a / 32] |= 1u << (a & 31);
+            if (!b_static) used[b / 32] |= 1u << (b & 31);
+            if (i != valid) {
+                int t;
+                t = A[i]; A[i] = A[valid]; A[valid] = t;
+                t = B[i]; B[i] = B[valid]; B[valid] = t;
+                t = order[i]; order[i] = order[valid]; order[valid] = t;
+            }
+            valid++;
+            count++;
+        }
+        batch_off[nb + 1] = batch_off[nb] + count;
+        nb++;
+    }
+    free(A);
+    free(B);
+    free(used);
+    return nb;
+}
+
+typedef struct {
+    v3 n, r1, r2, angA, angB;
+    float rhs, jinv, lo, hi, applied;
+} ojrow;
+
+static inline v3 j_mtmul1(const omat3* m, v3 b) {
+    return mk(dot(f4v(m->row[0]), b), dot(f4v(m->row[1]), b), dot(f4v(m->row[2]), b));
+}
+static inline v3 j_mtmul3(v3 a, const omat3* m) {
+    return mk(dot(a, mk(m->row[0].x, m->row[1].x, m->row[2].x)), dot(a, mk(m->row[0].y, m->row[1].y, m->row[2].y)),
+              dot(a, mk(m->row[0].z, m->row[1].z, m->row[2].z)));
+}
+
+/* calculateDiffAxisAngleQuaternion with nearest / getAngle / b3Acos (jointSolver.cl:543-590) */
+static void j_diff_axis_angle(qt orn0, qt orn1a, v3* axis, float* angle) {
+    qt d = {orn0.x - orn1a.x, orn0.y - orn1a.y, orn0.z - orn1a.z, orn0.w - orn1a.w};
+    qt s = {orn0.x + orn1a.x, orn0.y + orn1a.y, orn0.z + orn1a.z, orn0.w + orn1a.w};
+    float dd = d.x * d.x + d.y * d.y + d.z * d.z + d.w * d.w, ss = s.x * s.x + s.y * s.y + s.z * s.z + s.w * s.w;
+    qt orn1 = orn1a, dorn;
+    float w, len;
+    if (!(dd < ss)) { orn1.x = -orn1a.x; orn1.y = -orn1a.y; orn1.z = -orn1a.z; orn1.w = -orn1a.w; }
+    dorn = cl_qmul(orn1, qconj(orn0));
+    w = dorn.w;
+    if (w >= 1.f) w = 1.f;
+    if (w < -1.f) w = -1.f;
+    *angle = 2.f * oracle_joint_acos(w);
+    *axis = mk(dorn.x, dorn.y, dorn.z);
+    len = dot(*axis, *axis);
+    if (len < FLT_EPSILON * FLT_EPSILON) {
+        *axis = mk(1.f, 0.f, 0.f);
+    } else {
+        float r = sqrtf(len);
+        *axis = mk(axis->x / r, axis->y / r, axis->z / r);
+    }
+}
+
+static int j_rows(int type) { return type == 4 ? 6 : type == 3 ? 3 : 0; }
+
+/* getInfo2Kernel (jointSolver.cl:651-870) for one joint: getInfo2Point2Point (:488-541),
+ * getInfo2FixedOrientation (:592-628), then the finalize loop */
+static void j_setup(const obody* bodies, const oinertia* inertias, const ojoint* c, ojrow* rows) {
+    const float dt = 1.f / 60.f, erp = 0.2f, damping = 1.f, k = (1.f / dt) * erp;
+    const obody *bA = &bodies[c->rbA], *bB = &bodies[c->rbB];
+    int nr = j_rows(c->type), j;
+    qt qA = f4q(bA->quat), qB = f4q(bB->quat);
+    v3 a1 = cl_qrot(qA, f4v(c->pivotInA)), a2 = cl_qrot(qB, f4v(c->pivotInB)), m1 = neg(a1);
+    v3 vA = f4v(bA->linVel), wA = f4v(bA->angVel), vB = f4v(bB->linVel), wB = f4v(bB->angVel);
+    const omat3 *IA = &inertias[c->rbA].invInertiaWorld, *IB = &inertias[c->rbB].invInertiaWorld;
+    rows[0].n = mk(1.f, 0.f, 0.f);
+    rows[1].n = mk(0.f, 1.f, 0.f);
+    rows[2].n = mk(0.f, 0.f, 1.f);
+    rows[0].r1 = mk(0.f, -m1.z, m1.y);
+    rows[1].r1 = mk(m1.z, 0.f, -m1.x);
+    rows[2].r1 = mk(-m1.y, m1.x, 0.f);
+    rows[0].r2 = mk(0.f, -a2.z, a2.y);
+    rows[1].r2 = mk(a2.z, 0.f, -a2.x);
+    rows[2].r2 = mk(-a2.y, a2.x, 0.f);
+    rows[0].rhs = k * (((a2.x + bB->pos.x) - a1.x) - bA->pos.x);
+    rows[1].rhs = k * (((a2.y + bB->pos.y) - a1.y) - bA->pos.y);
+    rows[2].rhs = k * (((a2.z + bB->pos.z) - a1.z) - bA->pos.z);
+    if (nr == 6) {
+        v3 axis;
+        float angle, na;
+        for (j = 0; j < 3; j++) {
+            rows[3 + j].n = mk(0.f, 0.f, 0.f);
+            rows[3 + j].r1 = mk(j == 0 ? 1.f : 0.f, j == 1 ? 1.f : 0.f, j == 2 ? 1.f : 0.f);
+            rows[3 + j].r2 = mk(j == 0 ? -1.f : 0.f, j == 1 ? -1.f : 0.f, j == 2 ? -1.f : 0.f);
+        }
+        j_diff_axis_angle(f4q(c->relTargetAB), cl_qmul(qA, qconj(qB)), &axis, &angle);
+        na = -angle;
+        rows[3].rhs = k * (axis.x * na);
+        rows[4].rhs = k * (axis.y * na);
+        rows[5].rhs = k * (axis.z * na);
+    }
+    for (j = 0; j < nr; j++) {
+        ojrow* r = &rows[j];
+        float sum, vel1, vel2, rel;
+        r->lo = -1e30f;
+        r->hi = 1e30f;
+        if (r->hi >= c->breakingImpulseThreshold) r->hi = c->breakingImpulseThreshold;
+        if (r->lo <= -c->breakingImpulseThreshold) r->lo = -c->breakingImpulseThreshold;
+        r->angA = j_mtmul1(IA, r->r1);
+        r->angB = j_mtmul1(IB, r->r2);
+        sum = dot(scl(r->n, bA->invMass), r->n);
+        sum += dot(j_mtmul3(r->r1, IA), r->r1);
+        sum += dot(scl(r->n, bB->invMass), r->n);
+        sum += dot(j_mtmul3(r->r2, IB), r->r2);
+        r->jinv = fabsf(sum) > FLT_EPSILON ? 1.f / sum : 0.f;
+        vel1 = dot(r->n, vA) + dot(r->r1, wA);
+        vel2 = -dot(r->n, vB) + dot(r->r2, wB);
+        rel = vel1 + vel2;
+        r->rhs = r->rhs * r->jinv + (0.f - rel * damping) * r->jinv;
+        r->applied = 0.f;
+    }
+}
+
+/* resolveSingleConstraintRowGeneric (jointSolver.cl:273-301) */
+static void j_resolve(ojrow* r, float imA, float imB, v3* dlA, v3* daA, v3* dlB, v3* daB) {
+    const float cfm = 0.f;
+    float delta = r->rhs - r->applied * cfm, d1, d2, sum;
+    d1 = dot(r->n, *dlA) + dot(r->r1, *daA);
+    d2 = -dot(r->n, *dlB) + dot(r->r2, *daB);
+    delta -= d1 * r->jinv;
+    delta -= d2 * r->jinv;
+    sum = r->applied + delta;
+    if (sum < r->lo) {
+        delta = r->lo - r->applied;
+        r->applied = r->lo;
+    } else if (sum > r->hi) {
+        delta = r->hi - r->applied;
+        r->applied = r->hi;
+    } else {
+        r->applied = sum;
+    }
+    *dlA = add(*dlA, scl(scl(r->n, imA), delta));
+    *daA = add(*daA, scl(r->angA, delta));
+    *dlB = add(*dlB, scl(scl(neg(r->n), imB), delta));
+    *daB = add(*daB, scl(r->angB, delta));
+}
+
+void oracle_solve_joints(obody* bodies, const oinertia* inertias, int nbodies, ojoint* joints, int n,
+                         const int* order, const int* batch_off, int nbatches) {
+    ojrow* rows = (ojrow*)calloc((size_t)(n > 0 ? n : 1) * 6, sizeof(ojrow));
+    v3* dl = (v3*)calloc((size_t)nbodies, sizeof(v3));
+    v3* da = (v3*)calloc((size_t)nbodies, sizeof(v3));
+    int i, j, it, b, k;
+    for (i = 0; i < n; i++) j_setup(bodies, inertias, &joints[i], rows + 6 * (size_t)i);
+    for (it = 0; it < 4; it++)
+        for (b = 0; b < nbatches; b++)
+            for (k = batch_off[b]; k < batch_off[b + 1]; k++) {
+                const ojoint* c = &joints[order[k]];
+                ojrow* r = rows + 6 * (size_t)order[k];
+                if (!(c->flags & 1)) continue;
+                for (j = 0; j < j_rows(c->type); j++)
+                    j_resolve(&r[j], bodies[c->rbA].invMass, bodies[c->rbB].invMass, &dl[c->rbA], &da[c->rbA],
+                              &dl[c->rbB], &da[c->rbB]);
+            }
+    for (i = 0; i < n; i++)
+        for (j = 0; j < j_rows(joints[i].type); j++)
+            if (fabsf(rows[6 * (size_t)i + j].applied) >= joints[i].breakingImpulseThreshold) joints[i].flags = 0;
+    for (i = 0; i < nbodies; i++) {
+        if (bodies[i].invMass == 0.f) continue;
+        bodies[i].linVel.x += dl[i].x;
+        bodies[i].linVel.y += dl[i].y;
+        bodies[i].linVel.z += dl[i].z;
+        bodies[i].angVel.x += da[i].x;
+        bodies[i].angVel.y += da[i].y;
+        bodies[i].angVel.z += da[i].z;
+    }
+    free(rows);
+    free(dl);
+    free(da);
+}

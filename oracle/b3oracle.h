@@ -127,6 +127,28 @@ typedef struct { float hitFraction; int hitBody, hitResult1, hitResult2; of4 hit
 void oracle_cast_rays(const obody* bodies, int nbodies, const oshapes* sh, const oray* rays, oray_hit* hits,
                       int nrays, const int* body_scene);
 
+/* Joints (b3GpuGenericConstraint, Bullet3OpenCL/RigidBody/b3GpuGenericConstraint.h:77-93):
+ * type 3 point to point, 4 fixed; flags bit 0 = enabled. */
+typedef struct {
+    int type, rbA, rbB;
+    float breakingImpulseThreshold;
+    of4 pivotInA, pivotInB, relTargetAB;
+    int flags, uid, pad[2];
+} ojoint;
+/* The joint solver's batching (initBatchConstraintsKernel, kernels/jointSolver.cl:400-419, then
+ * b3GpuPgsConstraintSolver::sortConstraintByBatch3, b3GpuPgsConstraintSolver.cpp:781-907, with
+ * simdWidth = n + 1 and staticIdx = -1).  Writes the joint indices batch by batch into order[n]
+ * and the batch offsets into batch_off[nbatches + 1]; returns nbatches. */
+int oracle_joint_batches(const ojoint* joints, int n, const obody* bodies, int nbodies, int* order, int* batch_off);
+/* b3GpuPgsConstraintSolver::solveJoints (b3GpuPgsConstraintSolver.cpp:927-944): rows of every
+ * joint (getInfo2Kernel, jointSolver.cl:651-870), 4 PGS iterations over the batches in order
+ * (solveJointConstraintRows, :303-329), the break check (:352-371) and the velocity write-back
+ * (:631-648).  Updates the bodies' velocities and the joints' flags in place. */
+void oracle_solve_joints(obody* bodies, const oinertia* inertias, int nbodies, ojoint* joints, int n,
+                         const int* order, const int* batch_off, int nbatches);
+/* The acos the joint rows use (asin Maclaurin series with half-angle reduction). */
+float oracle_joint_acos(float x);
+
 #ifdef __cplusplus
 }
 #endif

@@ -215,6 +215,42 @@ def integrate(bodies, dt=1 / 60, damping=0.99, gravity=(0.0, -9.8, 0.0)):
     return b
 
 
+JOINT = np.dtype([("type", "<i4"), ("rbA", "<i4"), ("rbB", "<i4"), ("breakingImpulseThreshold", "<f4"),
+                  ("pivotInA", "<f4", 4), ("pivotInB", "<f4", 4), ("relTargetAB", "<f4", 4), ("flags", "<i4"),
+                  ("uid", "<i4"), ("pad", "<i4", 2)])
+
+
+def joint_batches(joints, bodies):
+    """The joint solver's greedy batching: (order, batch offsets)."""
+    j = np.ascontiguousarray(joints, JOINT)
+    b = np.ascontiguousarray(bodies, BODY)
+    order = np.zeros(max(1, len(j)), np.int32)
+    off = np.zeros(len(j) + 2, np.int32)
+    nb = load_oracle().oracle_joint_batches(_p(j), C.c_int(len(j)), _p(b), C.c_int(len(b)), _p(order), _p(off))
+    return order[:len(j)], off[:nb + 1]
+
+
+def solve_joints(bodies, inertias, joints, order=None, batch_off=None):
+    """One joint stage: returns (new bodies, new joints).  Batches from joint_batches unless given."""
+    b = np.array(bodies, BODY, copy=True)
+    I = np.ascontiguousarray(inertias, INERTIA)
+    j = np.array(joints, JOINT, copy=True)
+    if order is None:
+        order, batch_off = joint_batches(j, b)
+    o = np.ascontiguousarray(order, np.int32)
+    off = np.ascontiguousarray(batch_off, np.int32)
+    load_oracle().oracle_solve_joints(_p(b), _p(I), C.c_int(len(b)), _p(j), C.c_int(len(j)), _p(o), _p(off),
+                                      C.c_int(len(off) - 1))
+    return b, j
+
+
+def joint_acos(x):
+    f = load_oracle().oracle_joint_acos
+    f.restype = C.c_float
+    f.argtypes = [C.c_float]
+    return np.array([f(float(v)) for v in np.asarray(x, np.float32).ravel()], np.float32)
+
+
 RAY = np.dtype([("from", "<f4", 4), ("to", "<f4", 4)])
 RAYHIT = np.dtype([("hitFraction", "<f4"), ("hitBody", "<i4"), ("hitResult1", "<i4"), ("hitResult2", "<i4"),
                    ("hitPoint", "<f4", 4), ("hitNormal", "<f4", 4)])

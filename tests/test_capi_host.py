@@ -26,7 +26,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_layouts_match_reference_sizes():
     sizes = {capi.BODY: 80, capi.INERTIA: 96, capi.COLLIDABLE: 16, capi.HULL: 96, capi.FACE: 32, capi.AABB: 32,
-             capi.CONTACT: 112, capi.RAY: 32, capi.RAYHIT: 48}
+             capi.CONTACT: 112, capi.RAY: 32, capi.RAYHIT: 48, capi.JOINT: 80}
     for dt, n in sizes.items():
         assert dt.itemsize == n
 
@@ -163,6 +163,10 @@ def test_cpp_dropin_header_compiles(tmp_path):
                    "  float p[3], q[4]; np.getObjectTransformFromCpu(p, q, 0); np.setObjectTransformCpu(p, q, 0);\n"
                    "  bp.calculateOverlappingPairsHost(0); bp.getAllAabbsCPU(); rbp.copyConstraintsToHost();\n"
                    "  std::vector<b3gRayInfo> rays(2); std::vector<b3gRayHit> hits(2); rbp.castRays(rays, hits);\n"
+                   "  float pa[3] = {0, 0, 0}, rel[4] = {0, 0, 0, 1};\n"
+                   "  int u = rbp.createPoint2PointConstraint(0, 1, pa, pa, 1e30f);\n"
+                   "  u += rbp.createFixedConstraint(0, 1, pa, pa, rel, 1e30f); rbp.removeConstraintByUid(u);\n"
+                   "  u += (int)rbp.getConstraintsCPU().size();\n"
                    "  rbp.stepSimulation(1.f / 60.f); return rbp.getNumBodies();\n"
                    "}\n")
     r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-Wall", "-I", str(Path(ROOT, "include")), str(src)],
