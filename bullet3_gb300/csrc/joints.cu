@@ -139,65 +139,61 @@ __device__ void joint_setup(const JArgs& a, int i) {
     a.dv[2 * B + 1] = z4;
     const b3gBody bA = a.bodies[A], bB = a.bodies[B];
     const float k = (1.f / a.dt) * a.erp;
-    v3j n[6], r1[6], r2[6];
-    float rhs[6];
-    // getInfo2Point2Point: J1 linear = identity rows, J1 angular = skew(-a1), J2 angular = skew(a2)
+    // getInfo2Point2Point: J1 linear = identity rows, J1 angular = skew(-a1), J2 angular = skew(a2),
+    // rhs k (a2 + posB - a1 - posA); getInfo2FixedOrientation: J1 angular = identity rows, J2
+    // angular = -identity rows, rhs k axis (-angle).  Each row is rebuilt inside the finalize loop.
     const float4 qA = q4(bA.quat), qB = q4(bB.quat);
     const v3j a1 = jq_rot(qA, q4(c.pivotInA)), a2 = jq_rot(qB, q4(c.pivotInB));
     const v3j m1 = mkj(-a1.x, -a1.y, -a1.z);
-    n[0] = mkj(1.f, 0.f, 0.f);
-    n[1] = mkj(0.f, 1.f, 0.f);
-    n[2] = mkj(0.f, 0.f, 1.f);
-    r1[0] = mkj(0.f, -m1.z, m1.y);
-    r1[1] = mkj(m1.z, 0.f, -m1.x);
-    r1[2] = mkj(-m1.y, m1.x, 0.f);
-    r2[0] = mkj(0.f, -a2.z, a2.y);
-    r2[1] = mkj(a2.z, 0.f, -a2.x);
-    r2[2] = mkj(-a2.y, a2.x, 0.f);
-    rhs[0] = k * (((a2.x + bB.pos.x) - a1.x) - bA.pos.x);
-    rhs[1] = k * (((a2.y + bB.pos.y) - a1.y) - bA.pos.y);
-    rhs[2] = k * (((a2.z + bB.pos.z) - a1.z) - bA.pos.z);
+    const v3j err = mkj(((a2.x + bB.pos.x) - a1.x) - bA.pos.x, ((a2.y + bB.pos.y) - a1.y) - bA.pos.y,
+                        ((a2.z + bB.pos.z) - a1.z) - bA.pos.z);
+    v3j ang = mkj(0.f, 0.f, 0.f);
     if (nr == 6) {
-        // getInfo2FixedOrientation: J1 angular = identity rows, J2 angular = -identity rows
-        n[3] = n[4] = n[5] = mkj(0.f, 0.f, 0.f);
-        r1[3] = mkj(1.f, 0.f, 0.f);
-        r1[4] = mkj(0.f, 1.f, 0.f);
-        r1[5] = mkj(0.f, 0.f, 1.f);
-        r2[3] = mkj(-1.f, 0.f, 0.f);
-        r2[4] = mkj(0.f, -1.f, 0.f);
-        r2[5] = mkj(0.f, 0.f, -1.f);
         v3j axis;
         float angle;
         diff_axis_angle(q4(c.relTargetAB), jq_mul(qA, jq_inv(qB)), axis, angle);
         const float na = -angle;
-        rhs[3] = k * (axis.x * na);
-        rhs[4] = k * (axis.y * na);
-        rhs[5] = k * (axis.z * na);
+        ang = mkj(axis.x * na, axis.y * na, axis.z * na);
     }
     const b3gMat3 IA = a.inertias[A].invInertiaWorld, IB = a.inertias[B].invInertiaWorld;
     const v3j vA = xyz(bA.linVel), wA = xyz(bA.angVel), vB = xyz(bB.linVel), wB = xyz(bB.angVel);
     JointRow* out = a.rows + 6 * (size_t)i;
+#pragma unroll 1
     for (int j = 0; j < nr; ++j) {
+        v3j n, r1, r2;
+        float rhs;
+        const int e = j < 3 ? j : j - 3;
+        if (j < 3) {
+            n = mkj(e == 0 ? 1.f : 0.f, e == 1 ? 1.f : 0.f, e == 2 ? 1.f : 0.f);
+            r1 = e == 0 ? mkj(0.f, -m1.z, m1.y) : e == 1 ? mkj(m1.z, 0.f, -m1.x) : mkj(-m1.y, m1.x, 0.f);
+            r2 = e == 0 ? mkj(0.f, -a2.z, a2.y) : e == 1 ? mkj(a2.z, 0.f, -a2.x) : mkj(-a2.y, a2.x, 0.f);
+            rhs = k * (e == 0 ? err.x : e == 1 ? err.y : err.z);
+        } else {
+            n = mkj(0.f, 0.f, 0.f);
+            r1 = mkj(e == 0 ? 1.f : 0.f, e == 1 ? 1.f : 0.f, e == 2 ? 1.f : 0.f);
+            r2 = mkj(e == 0 ? -1.f : 0.f, e == 1 ? -1.f : 0.f, e == 2 ? -1.f : 0.f);
+            rhs = k * (e == 0 ? ang.x : e == 1 ? ang.y : ang.z);
+        }
         float lo = -JT_INFINITY, hi = JT_INFINITY;
         if (hi >= c.breakingImpulseThreshold) hi = c.breakingImpulseThreshold;
         if (lo <= -c.breakingImpulseThreshold) lo = -c.breakingImpulseThreshold;
-        const v3j angA = mt_mul1(IA, r1[j]), angB = mt_mul1(IB, r2[j]);
-        const v3j lA = mkj(n[j].x * bA.invMass, n[j].y * bA.invMass, n[j].z * bA.invMass);
-        const v3j lB = mkj(n[j].x * bB.invMass, n[j].y * bB.invMass, n[j].z * bB.invMass);
-        float sum = dotj(lA, n[j]);
-        sum += dotj(mt_mul3(r1[j], IA), r1[j]);
-        sum += dotj(lB, n[j]);
-        sum += dotj(mt_mul3(r2[j], IB), r2[j]);
+        const v3j angA = mt_mul1(IA, r1), angB = mt_mul1(IB, r2);
+        const v3j lA = mkj(n.x * bA.invMass, n.y * bA.invMass, n.z * bA.invMass);
+        const v3j lB = mkj(n.x * bB.invMass, n.y * bB.invMass, n.z * bB.invMass);
+        float sum = dotj(lA, n);
+        sum += dotj(mt_mul3(r1, IA), r1);
+        sum += dotj(lB, n);
+        sum += dotj(mt_mul3(r2, IB), r2);
         const float jinv = fabsf(sum) > FLT_EPSILON ? 1.f / sum : 0.f;
-        const float vel1 = dotj(n[j], vA) + dotj(r1[j], wA);
-        const float vel2 = -dotj(n[j], vB) + dotj(r2[j], wB);
+        const float vel1 = dotj(n, vA) + dotj(r1, wA);
+        const float vel2 = -dotj(n, vB) + dotj(r2, wB);
         const float rel = vel1 + vel2;
-        const float pen = rhs[j] * jinv;
+        const float pen = rhs * jinv;
         const float vimp = (0.f - rel * a.damping) * jinv;
         JointRow r;
-        r.n_rhs = make_float4(n[j].x, n[j].y, n[j].z, pen + vimp);
-        r.r1_jinv = make_float4(r1[j].x, r1[j].y, r1[j].z, jinv);
-        r.r2_lo = make_float4(r2[j].x, r2[j].y, r2[j].z, lo);
+        r.n_rhs = make_float4(n.x, n.y, n.z, pen + vimp);
+        r.r1_jinv = make_float4(r1.x, r1.y, r1.z, jinv);
+        r.r2_lo = make_float4(r2.x, r2.y, r2.z, lo);
         r.angA_hi = make_float4(angA.x, angA.y, angA.z, hi);
         r.angB_imp = make_float4(angB.x, angB.y, angB.z, 0.f);
         out[j] = r;
@@ -343,10 +339,18 @@ long long launch_joints(DeviceState& d, const b3gConfig& cfg, cudaStream_t s) {
     a.bar.abort_flag = d.barrier + 10;
     a.bar.status = &d.counters->status;
     a.spin_limit = cfg.barrier_spin_limit > 0 ? (unsigned)cfg.barrier_spin_limit : B3G_BARRIER_SPIN_LIMIT;
-    // one block while the widest batch fits it; else a co-resident grid (one block per SM at most)
+    // one block while the widest batch fits it; else a co-resident grid of up to two blocks per SM
+    // (262,144 joints in 2 batches: 0.35 ms at one block per SM, 0.27 ms at two, 0.33 ms at three,
+    // where the extra arrivals at each grid barrier cost more than the extra warps hide)
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_joints, JT_THREADS, 0) != cudaSuccess || per_sm < 1)
+            per_sm = 1;
+        if (per_sm > 2) per_sm = 2;
+    }
     int grid = (d.max_joint_batch + JT_THREADS - 1) / JT_THREADS;
     if (grid < 1) grid = 1;
-    if (grid > d.num_sms) grid = d.num_sms;
+    if (grid > d.num_sms * per_sm) grid = d.num_sms * per_sm;
     long long n = 0;
     if (grid > 1) {
         cudaMemsetAsync(d.barrier + 8, 0, 3 * sizeof(unsigned int), s);

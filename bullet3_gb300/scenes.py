@@ -296,11 +296,12 @@ def stress_container(n=1048576, width=128.0, depth=128.0, height=512.0, seed=0, 
 
 
 def hanging_chains(n_chains=8, links=12, spacing=1.0, radius=0.2, seed=0, fixed_every=0, threshold=1e30,
-                   anchor_index=0, ground=False, swing=1.0, random_orn=True) -> Scene:
+                   anchor_index=0, ground=False, swing=1.0, random_orn=True, per_row=0) -> Scene:
     """Chains of spheres hanging from one static anchor box, neighbours joined by ball joints at
     the midpoint (every fixed_every-th joint a fixed joint holding the initial relative
     orientation).  The anchor is body `anchor_index` (0 or the last body).  Links start with
-    random horizontal velocities of about `swing` m/s; chains are 3 apart, links do not touch.
+    random horizontal velocities of about `swing` m/s; chains are 3 apart (in a row along x, or
+    in rows of `per_row` chains along z), links do not touch.
     random_orn=False starts every link unrotated (the fixed joints' target is then the identity,
     the case the reference's fixed-joint rows are built for: they drive wA - wB, the rate of the
     orientation error only while ornA ornB^-1 is near the identity)."""
@@ -308,7 +309,9 @@ def hanging_chains(n_chains=8, links=12, spacing=1.0, radius=0.2, seed=0, fixed_
     top = links * spacing + 2.0
     nb = n_chains * links + 1 + (1 if ground else 0)
     sc = Scene(name=f"chains{n_chains}x{links}")
-    sc.shapes = [{"type": "hull", "verts": box_vertices(1.5 * n_chains + 1.0, 0.1, 1.0)},
+    per_row = per_row if per_row > 0 else n_chains
+    n_rows = (n_chains + per_row - 1) // per_row
+    sc.shapes = [{"type": "hull", "verts": box_vertices(1.5 * per_row + 1.0, 0.1, 1.5 * n_rows)},
                  {"type": "sphere", "radius": radius}]
     if ground:
         sc.shapes.append({"type": "plane", "normal": (0.0, 1.0, 0.0), "constant": 0.0})
@@ -325,28 +328,26 @@ def hanging_chains(n_chains=8, links=12, spacing=1.0, radius=0.2, seed=0, fixed_
     if random_orn:
         orn[dyn] = random_quaternions(rng, len(dyn))
     lin = np.zeros((nb, 3), np.float32)
-    k = 0
-    for c in range(n_chains):
-        x = 3.0 * (c - (n_chains - 1) / 2)
-        prev = None
-        for l in range(links):
-            i = dyn[k]
-            k += 1
-            pos[i] = (x, top - (l + 1) * spacing, 0.0)
-            lin[i] = (rng.uniform(-swing, swing), 0.0, rng.uniform(-swing, swing))
-            jt = "fixed" if fixed_every and (l % fixed_every == fixed_every - 1) else "p2p"
-            if prev is None:
-                a, pa = anchor, (x, -0.5 * spacing, 0.0)
-            else:
-                a, pa = prev, None
-            j = {"type": jt, "a": a, "b": i, "threshold": threshold}
-            # pivots in each body's own frame: the midpoint between the two centres
-            mid = pos[i] + np.array([0.0, 0.5 * spacing, 0.0], np.float32)
-            j["pivot_a"] = _to_local(mid - pos[a], orn[a])
-            j["pivot_b"] = _to_local(mid - pos[i], orn[i])
-            j["rel"] = _qmul(orn[a], _qconj(orn[i]))
-            sc.joints.append(j)
-            prev = i
+    dyn = np.asarray(dyn, np.int64)
+    c = np.repeat(np.arange(n_chains), links)
+    l = np.tile(np.arange(links), n_chains)
+    pos[dyn, 0] = 3.0 * (c % per_row - (per_row - 1) / 2)
+    pos[dyn, 1] = top - (l + 1) * spacing
+    pos[dyn, 2] = 3.0 * (c // per_row - (n_rows - 1) / 2)
+    u = rng.uniform(-swing, swing, (len(dyn), 2))
+    lin[dyn, 0] = u[:, 0]
+    lin[dyn, 2] = u[:, 1]
+    # joint k joins link k to the link above it (the anchor for a chain's first link); pivots in
+    # each body's own frame at the midpoint between the two centres
+    a = np.where(l == 0, anchor, np.roll(dyn, 1))
+    b = dyn
+    mid = pos[b] + np.array([0.0, 0.5 * spacing, 0.0], np.float32)
+    pa = _to_local_n(mid - pos[a], orn[a])
+    pb = _to_local_n(mid - pos[b], orn[b])
+    rel = _qmul_n(orn[a], _qconj_n(orn[b]))
+    fixed = (l % fixed_every == fixed_every - 1) if fixed_every else np.zeros(len(dyn), bool)
+    sc.joints = [{"type": "fixed" if fixed[k] else "p2p", "a": int(a[k]), "b": int(b[k]), "threshold": threshold,
+                  "pivot_a": pa[k], "pivot_b": pb[k], "rel": rel[k]} for k in range(len(dyn))]
     sc.body_shape, sc.mass, sc.pos, sc.orn, sc.linvel = shape, mass, pos, orn, lin
     return sc
 
@@ -380,6 +381,25 @@ def welded_pairs(n_pairs=64, seed=0, twist=0.3, threshold=1e30) -> Scene:
     sc.linvel = rng.standard_normal((nb, 3)).astype(np.float32)
     sc.angvel = (2.0 * rng.standard_normal((nb, 3))).astype(np.float32)
     return sc
+
+
+def _qconj_n(q):
+    q = np.asarray(q, np.float64)
+    return np.concatenate([-q[:, :3], q[:, 3:4]], 1)
+
+
+def _qmul_n(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    v = np.cross(a[:, :3], b[:, :3]) + a[:, 3:4] * b[:, :3] + b[:, 3:4] * a[:, :3]
+    w = a[:, 3] * b[:, 3] - np.einsum("ij,ij->i", a[:, :3], b[:, :3])
+    return np.concatenate([v, w[:, None]], 1).astype(np.float32)
+
+
+def _to_local_n(v, q):
+    """Rows of v (world) in the frames of the rows of q: q^-1 v q."""
+    v4 = np.concatenate([np.asarray(v, np.float64), np.zeros((len(v), 1))], 1)
+    return _qmul_n(_qmul_n(_qconj_n(q), v4), q)[:, :3].astype(np.float32)
 
 
 def _qconj(q):

@@ -15,6 +15,8 @@ with profiling off (ncu --profile-from-start off); --settle steps first, untimed
   batched  4,096 independent box/sphere piles, each on its own plane, through per-scene offsets
   mixed    131,072 boxes, spheres and Gaussian hulls in a 64^3 box, random orientations, N(0,1) velocities
   stress   1,048,576 bodies of the same mix poured into a 5-plane container from heights U[0, 512]
+  chains   8,192 chains of 32 spheres (262,144 bodies and ball joints, every 8th joint fixed)
+           hanging from one static box in a 3 m grid, swinging
 """
 from __future__ import annotations
 
@@ -37,12 +39,16 @@ def make(workload: str, n: int = 64):
         return scenes.mixed_scene(131072, extent=64.0, seed=0)
     if workload == "stress":
         return scenes.stress_container(1048576, seed=0)
+    if workload == "chains":
+        return scenes.hanging_chains(8192, 32, seed=0, fixed_every=8, anchor_index=-1, random_orn=False,
+                                     per_row=91)
     raise ValueError(workload)
 
 
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("--workload", choices=["pile", "lattice", "batched", "mixed", "stress"], default="pile")
+    p.add_argument("--workload", choices=["pile", "lattice", "batched", "mixed", "stress", "chains"],
+                   default="pile")
     p.add_argument("--settle", type=int, default=0)
     p.add_argument("--profile-range", action="store_true")
     p.add_argument("--nx", type=int, default=64)
@@ -52,6 +58,8 @@ def main(argv=None):
     p.add_argument("--iterations", type=int, default=10)
     p.add_argument("--autotune", action="store_true")
     p.add_argument("--no-graph", action="store_true")
+    p.add_argument("--stage-times", action="store_true",
+                   help="also run the measured steps once more with per-stage events and print their means")
     a = p.parse_args(argv)
     sc = make(a.workload, a.nx)
     cfg = b3Config(solver_mode=capi.SOLVER_PGS if a.solver == "pgs" else capi.SOLVER_JACOBI,
@@ -74,8 +82,21 @@ def main(argv=None):
     secs = time.perf_counter() - t0
     if a.profile_range:
         capi.call("b3g_profiler_range", capi.C.c_int(0))
+    stage_ms = None
+    if a.stage_times:
+        import numpy as np
+        pl.setProfiling(True)
+        acc = np.zeros(7)
+        for _ in range(a.steps):
+            pl.stepSimulation(dt)
+            pl.synchronize()
+            acc += pl.stageTimes()
+        pl.setProfiling(False)
+        names = ["aabbs", "pairs", "contacts", "joints", "setup", "solve", "integrate"]
+        stage_ms = {k: round(float(v) / max(a.steps, 1), 4) for k, v in zip(names, acc)}
     st = pl.stats()
     print(json.dumps({"workload": a.workload, "bodies": sc.num_bodies, "steps": a.steps,
+                      "joints": pl.getNumConstraints(), "stage_ms": stage_ms,
                       "host_ms_per_step": 1000 * secs / max(a.steps, 1), "pairs": st.num_pairs,
                       "manifolds": st.num_contacts, "points": st.num_points, "colors": st.num_colors,
                       "status": int(pl.status()), "tuning": tuning}))
