@@ -1,7 +1,8 @@
 """The C++ drop-in: a program written against the reference's class names (include/b3g_compat.h)
 is compiled with g++, linked against libb3gpu.so, and steps a box pile on the GPU through the C
-ABI.  Bar: it builds, runs without a b3Error, the boxes come to rest on the plane, and the
-broadphase/narrowphase getters report the pairs and contacts of the settled pile."""
+ABI.  Bar: it builds, runs without a b3Error, the boxes come to rest on the plane, the
+broadphase/narrowphase getters report the pairs and contacts of the settled pile, a ray hits the
+top box, and a ball joint lifts and holds a box until it is removed."""
 import shutil
 import subprocess
 from pathlib import Path
@@ -83,6 +84,24 @@ int main() {
     hits[0].hitResult2 = -1;
     rbp->castRays(rays, hits);
     ok = ok && hits[0].hitFraction < 1.f && hits[0].hitBody == 13;
+    // a ball joint from the static plane (body 0) at (0, 10, 0) to the centre of box 13 lifts it
+    // there and holds it; removing the joint lets it fall
+    const float pivotA[3] = {0.f, 10.f, 0.f}, pivotB[3] = {0.f, 0.f, 0.f};
+    const int uid = rbp->createPoint2PointConstraint(0, 13, pivotA, pivotB, 1e30f);
+    for (int frame = 0; frame < 120; frame++) rbp->stepSimulation(1.f / 60.f);
+    rbp->copyConstraintsToHost();
+    np->readbackAllBodiesToCpu();
+    float p2[3], q2[4];
+    ok = ok && uid >= 0 && np->getObjectTransformFromCpu(p2, q2, 13);
+    const float hang = std::sqrt(p2[0] * p2[0] + (p2[1] - 10.f) * (p2[1] - 10.f) + p2[2] * p2[2]);
+    ok = ok && hang < 0.1f && rbp->getConstraintsCPU().size() == 1 && rbp->getConstraintsCPU()[0].flags == 1;
+    rbp->removeConstraintByUid(uid);
+    for (int frame = 0; frame < 20; frame++) rbp->stepSimulation(1.f / 60.f);
+    np->readbackAllBodiesToCpu();
+    float p3[3], q3[4];
+    ok = ok && np->getObjectTransformFromCpu(p3, q3, 13) && p3[1] < p2[1] - 0.5f;
+    std::printf("joint holds box at %.4f %.4f %.4f (off %.4f); released -> y %.4f\n", p2[0], p2[1], p2[2], hang,
+                p3[1]);
     b3GpuBroadphaseInterface::CreateFunc* create = b3GpuSapBroadphase::CreateFunc;
     b3GpuBroadphaseInterface* other = create(0);
     ok = ok && other != nullptr;
