@@ -37,6 +37,7 @@ for _dt, _sz in ((BODY, 80), (INERTIA, 96), (COLLIDABLE, 16), (HULL, 96), (FACE,
 SHAPE_CONVEX_HULL, SHAPE_PLANE, SHAPE_SPHERE = 3, 4, 7
 SOLVER_PGS, SOLVER_JACOBI = 0, 1
 JOINT_POINT2POINT, JOINT_FIXED = 3, 4
+BROADPHASE_GRID, BROADPHASE_LBVH = 0, 1
 CONSTRAINT_FLAG_ENABLED = 1
 PGS_PARTITIONS_AUTO, PGS_PARTITIONS_GLOBAL_DELTAS, PGS_PARTITIONS_NONE, PGS_PARTITIONS_SHARED = 0, 1, 2, 3
 PGS_PARTITIONS_STREAMED = 4
@@ -63,7 +64,8 @@ class b3gConfig(C.Structure):
                 ("contact_friction", C.c_float), ("residual_tol", C.c_float), ("update_world_inertia", C.c_int),
                 ("use_cuda_graph", C.c_int), ("warm_start", C.c_int), ("barrier_spin_limit", C.c_int),
                 ("solver_blocks_per_sm", C.c_int), ("pgs_partitions", C.c_int), ("pgs_interleave", C.c_int),
-                ("warm_start_max_points", C.c_int), ("autotune", C.c_int), ("reserved", C.c_int * 2)]
+                ("warm_start_max_points", C.c_int), ("autotune", C.c_int), ("broadphase", C.c_int),
+                ("reserved", C.c_int * 1)]
 
 
 class b3gTuning(C.Structure):
@@ -90,7 +92,7 @@ _LIB = None
 EXPORTS = [
     "b3g_config_default", "b3g_create", "b3g_destroy", "b3g_last_error", "b3g_version", "b3g_register_sphere",
     "b3g_register_plane", "b3g_register_hull", "b3g_register_hull_tables", "b3g_register_body",
-    "b3g_write_all_to_gpu", "b3g_set_gravity", "b3g_set_solver", "b3g_set_scene_offsets", "b3g_autotune", "b3g_get_tuning", "b3g_profiler_range", "b3g_cast_rays", "b3g_create_point2point_constraint", "b3g_create_fixed_constraint",
+    "b3g_write_all_to_gpu", "b3g_set_gravity", "b3g_set_solver", "b3g_set_scene_offsets", "b3g_set_broadphase", "b3g_autotune", "b3g_get_tuning", "b3g_profiler_range", "b3g_cast_rays", "b3g_create_point2point_constraint", "b3g_create_fixed_constraint",
     "b3g_remove_constraint", "b3g_get_num_constraints", "b3g_read_constraints", "b3g_read_joint_order",
     "b3g_solve_joints", "b3g_step", "b3g_setup_aabbs",
     "b3g_calculate_overlapping_pairs", "b3g_compute_contacts", "b3g_solve_contacts", "b3g_integrate",

@@ -493,6 +493,264 @@ __global__ void __launch_bounds__(BP_THREADS, 8) k_find_pairs_world(
                             inv_cell, bits, body_bits, out, counter, cap, status);
 }
 
+// ---------------------------------------------------------------------------------------- LBVH
+// The alternative broadphase for the dynamic bodies, after b3GpuParallelLinearBvhBroadphase
+// (b3GpuParallelLinearBvh.cpp:108-359, kernels/parallelLinearBvh.cl): the bounds of all AABB
+// centres, a 30-bit Morton code per centre in that box (10 bits per axis,
+// assignMortonCodesAndAabbIndicies :116-165), a sort, a binary radix tree over the sorted codes
+// (Karras 2012, as constructBinaryRadixTree builds it), node AABBs bottom up, then one traversal
+// per leaf that only visits leaves after it in sorted order, so every pair is found once
+// (plbvhCalculateOverlappingPairs :176-300).  Here the scene index sits above the Morton code, so
+// each scene is a contiguous run of leaves and a traversal never leaves its scene's run; the
+// refit is one bottom-up pass with an arrival counter per node instead of one launch per tree
+// level; the pairs go through the same canonical (lower, higher) key list as the grid's.
+
+// float -> unsigned with the same order (so atomicMin/atomicMax order floats)
+__device__ __forceinline__ unsigned int ord_enc(float f) {
+    const unsigned int u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord_dec(unsigned int e) {
+    return __uint_as_float((e & 0x80000000u) ? (e & 0x7fffffffu) : ~e);
+}
+
+// bounds[0..2] = encoded min of the centres, bounds[3..5] = ~encoded max (both start all ones)
+__global__ void __launch_bounds__(BP_THREADS) k_lbvh_bounds(const b3gAabb* __restrict__ aabbs,
+                                                            const uint32_t* __restrict__ dyn, int n,
+                                                            unsigned int* __restrict__ bounds) {
+    const float4* A = reinterpret_cast<const float4*>(aabbs);
+    float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const uint32_t i = __ldg(&dyn[p]);
+        const float4 a = __ldg(&A[2 * i]), b = __ldg(&A[2 * i + 1]);
+        const float c[3] = {(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f};
+        for (int k = 0; k < 3; k++) {
+            mn[k] = fminf(mn[k], c[k]);
+            mx[k] = fmaxf(mx[k], c[k]);
+        }
+    }
+    for (int k = 0; k < 3; k++)
+        for (int o = 16; o; o >>= 1) {
+            mn[k] = fminf(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+            mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+        }
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 3; k++) {
+            atomicMin(&bounds[k], ord_enc(mn[k]));
+            atomicMin(&bounds[3 + k], ~ord_enc(mx[k]));
+        }
+}
+
+// 10 bits -> every third bit of 30
+__device__ __forceinline__ uint32_t spread3(uint32_t x) {
+    x = (x | (x << 16)) & 0x030000FFu;
+    x = (x | (x << 8)) & 0x0300F00Fu;
+    x = (x | (x << 4)) & 0x030C30C3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+__global__ void __launch_bounds__(BP_THREADS) k_lbvh_keys(const b3gAabb* __restrict__ aabbs,
+                                                          const uint32_t* __restrict__ dyn, int n,
+                                                          const unsigned int* __restrict__ bounds,
+                                                          const int* __restrict__ body_scene,
+                                                          uint64_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    const float4* A = reinterpret_cast<const float4*>(aabbs);
+    float lo[3], scale[3];
+    for (int k = 0; k < 3; k++) {
+        lo[k] = ord_dec(bounds[k]);
+        const float ext = ord_dec(~bounds[3 + k]) - lo[k];
+        scale[k] = ext > 0.f ? 1024.f / ext : 0.f;
+    }
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const uint32_t i = __ldg(&dyn[p]);
+        const float4 a = __ldg(&A[2 * i]), b = __ldg(&A[2 * i + 1]);
+        const float c[3] = {(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f};
+        uint32_t q[3];
+        for (int k = 0; k < 3; k++) q[k] = (uint32_t)fminf(fmaxf((c[k] - lo[k]) * scale[k], 0.f), 1023.f);
+        const uint32_t morton = (spread3(q[0]) << 2) | (spread3(q[1]) << 1) | spread3(q[2]);
+        const uint64_t sc = body_scene ? (uint64_t)__ldg(&body_scene[i]) : 0ull;
+        keys[p] = (sc << 30) | morton;
+        vals[p] = i;
+    }
+}
+
+// length of the common prefix of sorted keys i and j (-1 outside [0, n)); equal keys are told
+// apart by their indices
+__device__ __forceinline__ int lbvh_delta(const uint64_t* __restrict__ k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    const uint64_t a = __ldg(&k[i]), b = __ldg(&k[j]);
+    if (a == b) return 64 + __clz((unsigned int)(i ^ j));
+    return __clzll((long long)(a ^ b));
+}
+
+// The tree's depth is at most the key bits plus the index bits that break ties between equal keys.
+static constexpr int LBVH_MAX_DEPTH = 64 + 32;
+
+// internal node i of the binary radix tree over n sorted keys: its leaf range, split and
+// children (leaf l stored as ~l); node 0 is the root
+__global__ void __launch_bounds__(BP_THREADS) k_lbvh_build(const uint64_t* __restrict__ keys, int n,
+                                                           int2* __restrict__ child, int2* __restrict__ range,
+                                                           int* __restrict__ parent, int* __restrict__ flag) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n - 1; i += gridDim.x * blockDim.x) {
+        const int d = lbvh_delta(keys, n, i, i + 1) - lbvh_delta(keys, n, i, i - 1) >= 0 ? 1 : -1;
+        const int dmin = lbvh_delta(keys, n, i, i - d);
+        int lmax = 2;
+        while (lbvh_delta(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+        int l = 0;
+        for (int t = lmax >> 1; t >= 1; t >>= 1)
+            if (lbvh_delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+        const int j = i + l * d;
+        const int dnode = lbvh_delta(keys, n, i, j);
+        int s = 0, t = l;
+        do {
+            t = (t + 1) >> 1;
+            if (lbvh_delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
+        } while (t > 1);
+        const int gamma = i + s * d + (d < 0 ? -1 : 0);
+        const int lo = i < j ? i : j, hi = i < j ? j : i;
+        const int left = lo == gamma ? ~gamma : gamma;
+        const int right = hi == gamma + 1 ? ~(gamma + 1) : gamma + 1;
+        child[i] = make_int2(left, right);
+        range[i] = make_int2(lo, hi);
+        parent[left < 0 ? ~left : n + left] = i;
+        parent[right < 0 ? ~right : n + right] = i;
+        flag[i] = 0;
+        if (i == 0) parent[n] = -1;
+    }
+}
+
+// node AABBs bottom up: every leaf walks towards the root; the first child to arrive at a node
+// stops there, the second (which sees both children finished) merges them and goes on
+__global__ void __launch_bounds__(BP_THREADS) k_lbvh_refit(const b3gAabb* __restrict__ aabbs,
+                                                           const uint32_t* __restrict__ vals, int n,
+                                                           const int2* __restrict__ child,
+                                                           const int* __restrict__ parent, int* __restrict__ flag,
+                                                           float4* __restrict__ box, unsigned int* __restrict__ status) {
+    const float4* A = reinterpret_cast<const float4*>(aabbs);
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        int node = parent[p];
+        for (int level = 0; node >= 0; ++level) {
+            if (level > LBVH_MAX_DEPTH) {  // deeper than any radix tree over these keys: report, stop
+                atomicOr(status, B3G_FLAG_PAIR_OVERFLOW);
+                break;
+            }
+            __threadfence();
+            if (atomicAdd(&flag[node], 1) == 0) break;
+            const int2 c = child[node];
+            float4 mn[2], mx[2];
+            const int cc[2] = {c.x, c.y};
+            for (int k = 0; k < 2; k++) {
+                if (cc[k] < 0) {
+                    const uint32_t b = __ldg(&vals[~cc[k]]);
+                    mn[k] = __ldg(&A[2 * b]);
+                    mx[k] = __ldg(&A[2 * b + 1]);
+                } else {
+                    mn[k] = __ldcg(&box[2 * cc[k]]);
+                    mx[k] = __ldcg(&box[2 * cc[k] + 1]);
+                }
+            }
+            __stcg(&box[2 * node], make_float4(fminf(mn[0].x, mn[1].x), fminf(mn[0].y, mn[1].y),
+                                               fminf(mn[0].z, mn[1].z), 0.f));
+            __stcg(&box[2 * node + 1], make_float4(fmaxf(mx[0].x, mx[1].x), fmaxf(mx[0].y, mx[1].y),
+                                                   fmaxf(mx[0].z, mx[1].z), 0.f));
+            node = parent[n + node];
+        }
+    }
+}
+
+// Depth-first stack of a traversal: one pending sibling per level at most.
+static constexpr int LBVH_STACK = LBVH_MAX_DEPTH + 2;
+
+// One sorted leaf q per thread: the leaves after q in its scene's run whose AABBs overlap its
+// body's, then the static proxies (same path as the grid's pair kernel).
+template <bool SCENES>
+__global__ void __launch_bounds__(BP_THREADS) k_lbvh_pairs(
+    const b3gAabb* __restrict__ aabbs, const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals, int n,
+    const int2* __restrict__ child, const int2* __restrict__ range, const float4* __restrict__ box,
+    const int* __restrict__ large_list, int n_large, const int* __restrict__ body_scene,
+    const int* __restrict__ large_off, const SapView sap, int body_bits, uint64_t* __restrict__ out,
+    int* __restrict__ counter, int cap, unsigned int* __restrict__ status) {
+    const float4* A = reinterpret_cast<const float4*>(aabbs);
+    const int lane = threadIdx.x & 31;
+    const int stride = gridDim.x * blockDim.x;
+    const int start = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iters = (n + stride - 1) / stride;  // equal for every lane: the final flush is convergent
+    PairEmitter em;
+    em.cnt = 0;
+    int stack[LBVH_STACK];
+    for (int it = 0; it < iters; it++) {
+        const int q = start + it * stride;
+        if (q >= n) continue;
+        const uint32_t i = __ldg(&vals[q]);
+        const float4 amin = __ldg(&A[2 * i]), amax = __ldg(&A[2 * i + 1]);
+        int si = 0, l0 = 0, l1 = n_large, s_hi = n;
+        if (SCENES) {
+            si = __ldg(&body_scene[i]);
+            l0 = __ldg(&large_off[si]);
+            l1 = __ldg(&large_off[si + 1]);
+            // end of the scene's run: the first sorted key of a later scene
+            const uint64_t lim = (uint64_t)(si + 1) << 30;
+            int lo = q + 1, hi = n;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (__ldg(&keys[mid]) < lim)
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            s_hi = lo;
+        }
+        if (n > 1 && q + 1 < s_hi) {
+            int sp = 0;
+            stack[sp++] = 0;
+            while (sp > 0) {
+                const int node = stack[--sp];
+                if (node < 0) {
+                    const int l = ~node;
+                    if (l <= q || l >= s_hi) continue;
+                    const uint32_t j = __ldg(&vals[l]);
+                    const float4 bmin = __ldg(&A[2 * j]), bmax = __ldg(&A[2 * j + 1]);
+                    if (overlap(amin, amax, bmin, bmax)) {
+                        const uint32_t a = i < j ? i : j, b = i < j ? j : i;
+                        em.push(((uint64_t)a << body_bits) | b, out, counter, cap, status);
+                    }
+                    continue;
+                }
+                const int2 r = __ldg(&range[node]);
+                if (r.y <= q || r.x >= s_hi) continue;
+                if (!overlap(amin, amax, __ldg(&box[2 * node]), __ldg(&box[2 * node + 1]))) continue;
+                const int2 c = __ldg(&child[node]);
+                if (sp + 2 > LBVH_STACK) {  // cannot happen (see LBVH_STACK); reported, never silent
+                    atomicOr(status, B3G_FLAG_PAIR_OVERFLOW);
+                    continue;
+                }
+                stack[sp++] = c.y;
+                stack[sp++] = c.x;
+            }
+        }
+        static_pairs(A, i, amin, amax, large_list, l0, l1, sap, si, body_bits, em, out, counter, cap, status);
+    }
+    // warp-aggregated reservation of the remaining buffered pairs
+    const int c = em.cnt;
+    int incl = c;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int wbase = 0;
+    if (lane == 31 && total > 0) wbase = atomicAdd(counter, total);
+    wbase = __shfl_sync(0xffffffffu, wbase, 31);
+    const int my = wbase + incl - c;
+    for (int k = 0; k < c; k++) {
+        if (my + k < cap)
+            out[my + k] = em.buf[k];
+        else
+            atomicOr(status, B3G_FLAG_PAIR_OVERFLOW);
+    }
+}
+
 __global__ void k_clamp_count(int* counter, int cap, int* clamped) {
     int n = *counter;
     *clamped = n < cap ? n : cap;
@@ -578,11 +836,46 @@ int launch_cells(DeviceState& d, cudaStream_t s) {
     return 1 + (int)ll;
 }
 
+// The LBVH of the current AABBs: centre bounds, keys, sort, tree, node AABBs.  The dynamic bodies
+// in (scene, Morton) order also serve the solver's partitions, as the cell order does for the grid.
+static int launch_lbvh(DeviceState& d, cudaStream_t s) {
+    const int n = d.num_dynamic;
+    if (n == 0) return 0;
+    long long ll = 0;
+    const int grid = std::max(1, std::min((n + BP_THREADS - 1) / BP_THREADS, d.num_sms * 8));
+    cudaMemsetAsync(d.lbvh_bounds, 0xff, 6 * sizeof(unsigned int), s);
+    // the dynamic bodies, in slot order, are the values launch_aabbs wrote next to the cell keys
+    k_lbvh_bounds<<<grid, BP_THREADS, 0, s>>>(d.aabbs, d.cell_vals[0], n, d.lbvh_bounds);
+    k_lbvh_keys<<<grid, BP_THREADS, 0, s>>>(d.aabbs, d.cell_vals[0], n, d.lbvh_bounds,
+                                            d.num_scenes > 1 ? d.body_scene : nullptr, d.lbvh_keys[0],
+                                            d.lbvh_vals[0]);
+    d.prim.sort_blocks = d.num_sms * d.tune.sort_blocks_per_sm;
+    const int w = radix_sort_u64(d.prim, d.lbvh_keys[0], d.lbvh_keys[1], d.lbvh_vals[0], d.lbvh_vals[1],
+                                 d.d_num_dynamic, 30 + d.scene_bits, d.sort_scratch, s, &ll);
+    d.lbvh_sorted_keys = d.lbvh_keys[w];
+    d.lbvh_sorted_vals = d.lbvh_vals[w];
+    d.cell_sorted_bodies = d.lbvh_sorted_vals;
+    d.cell_sorted_keys = nullptr;
+    int launches = 3 + (int)ll;
+    if (n > 1) {
+        k_lbvh_build<<<grid, BP_THREADS, 0, s>>>(d.lbvh_sorted_keys, n, d.lbvh_child, d.lbvh_range, d.lbvh_parent,
+                                                 d.lbvh_flag);
+        k_lbvh_refit<<<grid, BP_THREADS, 0, s>>>(d.aabbs, d.lbvh_sorted_vals, n, d.lbvh_child, d.lbvh_parent,
+                                                 d.lbvh_flag, d.lbvh_box, &d.counters->status);
+        launches += 2;
+    }
+    return launches;
+}
+
 int launch_pairs(DeviceState& d, cudaStream_t s) {
     int launches = 0;
     long long ll = 0;
-    // 1-2. sort (cell hash, body) -- keys written by launch_aabbs -- and run starts
-    launches += launch_cells(d, s);
+    const bool lbvh = d.broadphase == B3G_BROADPHASE_LBVH && d.lbvh_cap > 0;
+    // 1-2. sort (cell hash, body) -- keys written by launch_aabbs -- and run starts; or the LBVH
+    if (lbvh)
+        launches += launch_lbvh(d, s);
+    else
+        launches += launch_cells(d, s);
     uint32_t* keys = const_cast<uint32_t*>(d.cell_sorted_keys);
     uint32_t* vals = const_cast<uint32_t*>(d.cell_sorted_bodies);
     // 3. pairs
@@ -597,7 +890,17 @@ int launch_pairs(DeviceState& d, cudaStream_t s) {
                                                 d.sap_ext);
         launches++;
     }
-    if (d.num_scenes > 1)
+    if (lbvh && d.num_scenes > 1)
+        k_lbvh_pairs<true><<<pgrid, BP_THREADS, 0, s>>>(
+            d.aabbs, d.lbvh_sorted_keys, d.lbvh_sorted_vals, d.num_dynamic, d.lbvh_child, d.lbvh_range, d.lbvh_box,
+            d.large_list, d.num_large, d.body_scene, d.large_off, sap, d.body_bits, d.pair_keys[0],
+            &d.counters->num_pairs, d.max_pairs, &d.counters->status);
+    else if (lbvh)
+        k_lbvh_pairs<false><<<pgrid, BP_THREADS, 0, s>>>(
+            d.aabbs, d.lbvh_sorted_keys, d.lbvh_sorted_vals, d.num_dynamic, d.lbvh_child, d.lbvh_range, d.lbvh_box,
+            d.large_list, d.num_large, nullptr, nullptr, sap, d.body_bits, d.pair_keys[0], &d.counters->num_pairs,
+            d.max_pairs, &d.counters->status);
+    else if (d.num_scenes > 1)
         k_find_pairs_world<true><<<pgrid, BP_THREADS, 0, s>>>(
             d.aabbs, keys, vals, d.cell_start, d.num_dynamic, d.large_list, d.num_large, d.body_scene, d.large_off,
             sap, d.inv_cell, d.grid_bits, d.body_bits, d.pair_keys[0], &d.counters->num_pairs, d.max_pairs,

@@ -102,6 +102,40 @@ struct b3gWorld {
 
 static b3gStatus sync_joint_flags(b3gWorld* h);
 
+static void free_lbvh_buffers(b3g::DeviceState& d) {
+    for (auto* p : d.lbvh_keys) cudaFree(p);
+    for (auto* p : d.lbvh_vals) cudaFree(p);
+    cudaFree(d.lbvh_child);
+    cudaFree(d.lbvh_range);
+    cudaFree(d.lbvh_parent);
+    cudaFree(d.lbvh_box);
+    cudaFree(d.lbvh_flag);
+    cudaFree(d.lbvh_bounds);
+}
+
+// LBVH buffers for the world's dynamic bodies (84 B per body), allocated on first use
+static b3gStatus alloc_lbvh(b3g::DeviceState& d) {
+    const int n = std::max(2, d.num_dynamic);
+    if (d.lbvh_cap >= n) return B3G_OK;
+    free_lbvh_buffers(d);
+    d.lbvh_keys[0] = d.lbvh_keys[1] = nullptr;
+    d.lbvh_vals[0] = d.lbvh_vals[1] = nullptr;
+    d.lbvh_cap = 0;
+    const size_t m = (size_t)n;
+    CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&d.lbvh_keys[0]), m * sizeof(uint64_t)));
+    CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&d.lbvh_keys[1]), m * sizeof(uint64_t)));
+    CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&d.lbvh_vals[0]), m * sizeof(uint32_t)));
+    CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&d.lbvh_vals[1]), m * sizeof(uint32_t)));
+    CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&d.lbvh_child), m * sizeof(int2)));
+    CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&d.lbvh_range), m * sizeof(int2)));
+    CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&d.lbvh_parent), 2 * m * sizeof(int)));
+    CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&d.lbvh_box), 2 * m * sizeof(float4)));
+    CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&d.lbvh_flag), m * sizeof(int)));
+    CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&d.lbvh_bounds), 8 * sizeof(unsigned int)));
+    d.lbvh_cap = n;
+    return B3G_OK;
+}
+
 static void free_joint_buffers(b3g::DeviceState& d) {
     cudaFree(d.joints);
     cudaFree(d.joint_rows);
@@ -120,6 +154,7 @@ static void free_device(b3gWorld* w) {
     for (void* p : w->allocations) cudaFree(p);
     w->allocations.clear();
     free_joint_buffers(w->d);
+    free_lbvh_buffers(w->d);
     w->d = DeviceState();
     w->uploaded = false;
 }
@@ -202,6 +237,10 @@ extern "C" b3gStatus b3g_create(const b3gConfig* cfg, int cuda_device, b3g_handl
     if (w->cfg.solver_blocks_per_sm < 0) {
         delete w;
         return fail(B3G_ERR_INVALID_ARG, "solver_blocks_per_sm must be >= 0");
+    }
+    if (w->cfg.broadphase != B3G_BROADPHASE_GRID && w->cfg.broadphase != B3G_BROADPHASE_LBVH) {
+        delete w;
+        return fail(B3G_ERR_INVALID_ARG, "broadphase must be B3G_BROADPHASE_GRID or B3G_BROADPHASE_LBVH");
     }
     w->device = cuda_device;
     *out = w;
@@ -730,7 +769,27 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     CUDA_TRY(cudaMemsetAsync(d.counters, 0, sizeof(DevCounters), s));
     CUDA_TRY(cudaMemsetAsync(d.barrier, 0, 64 * sizeof(unsigned int), s));
     CUDA_TRY(cudaStreamSynchronize(s));
+    d.scene_bits = d.num_scenes > 1 ? bits_for(d.num_scenes) : 0;
+    d.broadphase = h->cfg.broadphase;
+    if (d.broadphase == B3G_BROADPHASE_LBVH) TRY(alloc_lbvh(d));
     h->uploaded = true;
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_set_broadphase(b3g_handle h, int mode) {
+    if (!h) return fail(B3G_ERR_INVALID_ARG, "null handle");
+    if (mode != B3G_BROADPHASE_GRID && mode != B3G_BROADPHASE_LBVH)
+        return fail(B3G_ERR_INVALID_ARG, "unknown broadphase %d", mode);
+    h->cfg.broadphase = mode;
+    if (!h->uploaded) return B3G_OK;
+    CUDA_TRY(cudaSetDevice(h->device));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    if (mode == B3G_BROADPHASE_LBVH) TRY(alloc_lbvh(h->d));
+    h->d.broadphase = mode;
+    if (h->graph_exec) {  // the captured step has the other broadphase's launches
+        cudaGraphExecDestroy(h->graph_exec);
+        h->graph_exec = nullptr;
+    }
     return B3G_OK;
 }
 

@@ -76,6 +76,21 @@ struct DeviceState {
     float4* ray_buf = nullptr;    // b3g_cast_rays: rays (2 float4 each) and hits, grown on demand
     b3gRayHit* hit_buf = nullptr;
     int ray_cap = 0;
+    // LBVH broadphase (b3gConfig.broadphase = B3G_BROADPHASE_LBVH; own allocations): the dynamic
+    // bodies sorted by (scene, Morton code of the AABB centre), a binary radix tree over them
+    int broadphase = 0;
+    int scene_bits = 0;                    // bits of the scene index above the 30 Morton bits
+    uint64_t* lbvh_keys[2] = {nullptr, nullptr};
+    uint32_t* lbvh_vals[2] = {nullptr, nullptr};
+    const uint64_t* lbvh_sorted_keys = nullptr;
+    const uint32_t* lbvh_sorted_vals = nullptr;
+    int2* lbvh_child = nullptr;            // internal node -> children (leaf l stored as ~l)
+    int2* lbvh_range = nullptr;            // internal node -> first and last leaf below it
+    int* lbvh_parent = nullptr;            // parents of the leaves [0, n), of the internal nodes [n, 2n)
+    float4* lbvh_box = nullptr;            // internal node -> AABB min, max
+    int* lbvh_flag = nullptr;              // bottom-up refit: children finished per internal node
+    unsigned int* lbvh_bounds = nullptr;   // centre bounds, order-preserving encodings: min xyz, ~max xyz
+    int lbvh_cap = 0;
     // joints (own allocations, grown on demand; the host registry is authoritative except for
     // the enabled flags, which the device's break check clears)
     b3gJoint* joints = nullptr;

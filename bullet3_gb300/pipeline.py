@@ -49,6 +49,7 @@ class b3Config:
         self.warm_start = 0
         self.warm_start_max_points = 0
         self.autotune = False
+        self.broadphase = capi.BROADPHASE_GRID
         for k, v in kw.items():
             if not hasattr(self, k):
                 raise AttributeError(k)
@@ -66,7 +67,7 @@ class b3Config:
                                    pgs_partitions=self.pgs_partitions,
                                    pgs_interleave=int(self.pgs_interleave), warm_start=int(self.warm_start),
                                    warm_start_max_points=int(self.warm_start_max_points),
-                                   autotune=int(self.autotune))
+                                   autotune=int(self.autotune), broadphase=int(self.broadphase))
 
 
 class _World:
@@ -305,6 +306,16 @@ class b3GpuGridBroadphase(b3GpuBroadphaseInterface):
         call("b3g_write_aabbs", self._h, ptr(a), C.c_int(len(a)))
 
 
+class b3GpuParallelLinearBvhBroadphase(b3GpuGridBroadphase):
+    """Linear-BVH broadphase (b3GpuParallelLinearBvhBroadphase.cpp): Morton-ordered binary radix
+    tree over the dynamic bodies, complete for any AABB sizes; the same canonical pair list as the
+    grid.  Attaching it to a pipeline switches the world's pair search to the LBVH."""
+
+    def _attach(self, narrowphase: b3GpuNarrowPhase):
+        self._np = narrowphase
+        call("b3g_set_broadphase", self._h, C.c_int(capi.BROADPHASE_LBVH))
+
+
 class b3GpuRigidBodyPipeline:
     """b3GpuRigidBodyPipeline: registration and the per-frame step."""
 
@@ -351,6 +362,10 @@ class b3GpuRigidBodyPipeline:
         t = capi.b3gTuning()
         call("b3g_get_tuning", self._h, C.byref(t))
         return {f: getattr(t, f) for f, _ in capi.b3gTuning._fields_}
+
+    def setBroadphase(self, mode: int):
+        """capi.BROADPHASE_GRID or capi.BROADPHASE_LBVH for the pair search (b3g_set_broadphase)."""
+        call("b3g_set_broadphase", self._h, C.c_int(mode))
 
     def setSceneOffsets(self, firstBody):
         """Independent scenes stepped together (no reference counterpart: the reference runs one

@@ -3,9 +3,9 @@
 Meant for running the pipeline under an external profiler (ncu) or by hand: nothing but the
 scene upload, the warm-up steps and the measured steps touch the GPU.
 
-    python -m bullet3_gb300.stepper [--workload pile|lattice|batched|mixed|stress] [--settle S] [--steps K]
-                                    [--warmup W] [--solver pgs|jacobi] [--iterations I] [--autotune]
-                                    [--profile-range]
+    python -m bullet3_gb300.stepper [--workload pile|lattice|batched|mixed|stress|chains] [--settle S]
+                                    [--steps K] [--warmup W] [--solver pgs|jacobi] [--iterations I]
+                                    [--autotune] [--broadphase grid|lbvh] [--stage-times] [--profile-range]
 
 --profile-range brackets the K measured steps with b3g_profiler_range, for a profiler started
 with profiling off (ncu --profile-from-start off); --settle steps first, untimed.
@@ -58,13 +58,15 @@ def main(argv=None):
     p.add_argument("--iterations", type=int, default=10)
     p.add_argument("--autotune", action="store_true")
     p.add_argument("--no-graph", action="store_true")
+    p.add_argument("--broadphase", choices=["grid", "lbvh"], default="grid")
     p.add_argument("--stage-times", action="store_true",
                    help="also run the measured steps once more with per-stage events and print their means")
     a = p.parse_args(argv)
     sc = make(a.workload, a.nx)
     cfg = b3Config(solver_mode=capi.SOLVER_PGS if a.solver == "pgs" else capi.SOLVER_JACOBI,
                    solver_iterations=a.iterations, pgs_interleave=a.solver == "pgs",
-                   use_cuda_graph=not a.no_graph)
+                   use_cuda_graph=not a.no_graph,
+                   broadphase=capi.BROADPHASE_LBVH if a.broadphase == "lbvh" else capi.BROADPHASE_GRID)
     np_, bp, pl = scenes.load_scene(sc, cfg)
     dt = 1.0 / 60.0
     for _ in range(a.settle):
@@ -92,10 +94,10 @@ def main(argv=None):
             pl.synchronize()
             acc += pl.stageTimes()
         pl.setProfiling(False)
-        names = ["aabbs", "pairs", "contacts", "joints", "setup", "solve", "integrate"]
-        stage_ms = {k: round(float(v) / max(a.steps, 1), 4) for k, v in zip(names, acc)}
+        names = ["aabbs", "pairs", "contacts", "joints", "solver", None, "integrate"]
+        stage_ms = {k: round(float(v) / max(a.steps, 1), 4) for k, v in zip(names, acc) if k}
     st = pl.stats()
-    print(json.dumps({"workload": a.workload, "bodies": sc.num_bodies, "steps": a.steps,
+    print(json.dumps({"workload": a.workload, "broadphase": a.broadphase, "bodies": sc.num_bodies, "steps": a.steps,
                       "joints": pl.getNumConstraints(), "stage_ms": stage_ms,
                       "host_ms_per_step": 1000 * secs / max(a.steps, 1), "pairs": st.num_pairs,
                       "manifolds": st.num_contacts, "points": st.num_points, "colors": st.num_colors,

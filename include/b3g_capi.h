@@ -111,7 +111,8 @@ typedef struct b3gConfig {
     int warm_start_max_points; /* point slots (4 per manifold, in manifold order) that get features and
                                   predictions when warm_start != 0; 0 = 8 x bodies (at least 8192) */
     int autotune;              /* 1: the first b3g_step after an upload runs b3g_autotune (3 repeats) */
-    int reserved[2];
+    int broadphase;            /* B3G_BROADPHASE_GRID (0) or B3G_BROADPHASE_LBVH (1), see b3g_set_broadphase */
+    int reserved[1];
 } b3gConfig;
 
 /* Per-step counters, copied once per step from the device. */
@@ -184,6 +185,17 @@ b3gStatus b3g_set_solver(b3g_handle h, int mode, int iterations, float residual_
  * and be non-decreasing (empty scenes are allowed). */
 #define B3G_MAX_SCENES (1 << 20)
 b3gStatus b3g_set_scene_offsets(b3g_handle h, const int* first_body, int num_scenes);
+
+/* Broadphase algorithm for the dynamic bodies (b3GpuBroadphaseInterface implementations,
+ * Bullet3OpenCL/BroadphaseCollision/).  GRID: the uniform hashed grid of b3GpuGridBroadphase
+ * (complete while every dynamic AABB fits one grid cell).  LBVH: the linear BVH of
+ * b3GpuParallelLinearBvhBroadphase (b3GpuParallelLinearBvh.cpp:108-359): Morton codes of the AABB
+ * centres, a binary radix tree, one traversal per body; complete for any AABB sizes.  Both emit the
+ * same canonical pair list (static bodies go through the same sweep and prune / unbounded list
+ * either way).  Valid before or after the upload; takes effect at the next pair search. */
+#define B3G_BROADPHASE_GRID 0
+#define B3G_BROADPHASE_LBVH 1
+b3gStatus b3g_set_broadphase(b3g_handle h, int mode);
 
 /* Autotuner (no reference counterpart: the reference's OpenCL kernels use fixed work-group
  * sizes).  Times candidate launch shapes on the world's current state and keeps the fastest of
@@ -329,9 +341,9 @@ b3gStatus b3g_read_shape_tables(b3g_handle h, void* collidables, void* hulls, vo
 /* ------------------------------------------------------------------ stage profiling */
 /* Records CUDA events around each stage on the world's stream when on=1. */
 b3gStatus b3g_set_profiling(b3g_handle h, int on);
-/* Milliseconds per stage of the last profiled step: aabb, pairs, contacts, joints (the
- * reference's batching slot: contact batching is fused into the solve), setup, solve,
- * integrate (7 floats). */
+/* Milliseconds per stage of the last profiled step (7 floats): aabb, pairs, contacts, joints
+ * (the reference's batching slot: contact batching is fused into the solver), the contact solver
+ * (row setup, colouring and sweeps), 0 (the solver is one stage), integrate. */
 b3gStatus b3g_get_stage_times(b3g_handle h, float* ms7);
 /* Number of kernels this library launched since creation (counted on the host at launch). */
 b3gStatus b3g_get_launch_count(b3g_handle h, long long* n);

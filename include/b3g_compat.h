@@ -218,7 +218,7 @@ class b3GpuGridBroadphase : public b3GpuBroadphaseInterface {
 public:
     explicit b3GpuGridBroadphase(b3GpuNarrowPhase* np = nullptr) : m_np(np) {}
     static b3GpuBroadphaseInterface* CreateFunc(int /*cudaDevice*/) { return new b3GpuGridBroadphase(); }
-    void attach(b3GpuNarrowPhase* np) { m_np = np; }
+    virtual void attach(b3GpuNarrowPhase* np) { m_np = np; }
     /* Proxies: registerPhysicsInstance / registerRigidBody create them (dynamic bodies small,
        static bodies large), as the reference pipeline does (b3GpuRigidBodyPipeline.cpp:650-657) */
     void createProxy(const float*, const float*, int, int, int) {}
@@ -272,6 +272,21 @@ class b3GpuSapBroadphase : public b3GpuGridBroadphase {
 public:
     explicit b3GpuSapBroadphase(b3GpuNarrowPhase* np = nullptr) : b3GpuGridBroadphase(np) {}
     static b3GpuBroadphaseInterface* CreateFunc(int /*cudaDevice*/) { return new b3GpuSapBroadphase(); }
+};
+
+/* b3GpuParallelLinearBvhBroadphase (Bullet3OpenCL/BroadphaseCollision/b3GpuParallelLinearBvhBroadphase.h):
+   the linear-BVH pair search, complete for any AABB sizes; same pair list as the grid.  Attaching it
+   to a pipeline switches the world's pair search to it. */
+class b3GpuParallelLinearBvhBroadphase : public b3GpuGridBroadphase {
+public:
+    explicit b3GpuParallelLinearBvhBroadphase(b3GpuNarrowPhase* np = nullptr) : b3GpuGridBroadphase(np) {
+        if (np) attach(np);
+    }
+    static b3GpuBroadphaseInterface* CreateFunc(int /*cudaDevice*/) { return new b3GpuParallelLinearBvhBroadphase(); }
+    void attach(b3GpuNarrowPhase* np) override {
+        b3GpuGridBroadphase::attach(np);
+        if (np && b3g_set_broadphase(np->world(), B3G_BROADPHASE_LBVH) != B3G_OK) b3Error("b3GpuParallelLinearBvhBroadphase");
+    }
 };
 
 class b3GpuRigidBodyPipeline {

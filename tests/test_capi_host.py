@@ -54,7 +54,7 @@ def test_registration_errors_match_reference_conventions():
 def test_config_validation():
     h = C.c_void_p()
     for bad in (dict(pgs_partitions=5), dict(pgs_partitions=-1), dict(solver_blocks_per_sm=-2), dict(grid_dim=100),
-                dict(pgs_interleave=2)):
+                dict(pgs_interleave=2), dict(broadphase=2)):
         cfg = capi.default_config(**bad)
         with pytest.raises(capi.B3GError) as e:
             capi.call("b3g_create", C.byref(cfg), C.c_int(0), C.byref(h))
@@ -160,6 +160,8 @@ def test_cpp_dropin_header_compiles(tmp_path):
                    "  b3GpuRigidBodyPipeline rbp(&np, &bp, nullptr, c);\n"
                    "  int first[2] = {0, 1}; rbp.setSceneOffsets(first, 2);\n"
                    "  b3GpuBroadphaseInterface::CreateFunc* f = b3GpuSapBroadphase::CreateFunc; delete f(0);\n"
+                   "  f = b3GpuParallelLinearBvhBroadphase::CreateFunc; delete f(0);\n"
+                   "  b3GpuParallelLinearBvhBroadphase lbvh(&np);\n"
                    "  float p[3], q[4]; np.getObjectTransformFromCpu(p, q, 0); np.setObjectTransformCpu(p, q, 0);\n"
                    "  bp.calculateOverlappingPairsHost(0); bp.getAllAabbsCPU(); rbp.copyConstraintsToHost();\n"
                    "  std::vector<b3gRayInfo> rays(2); std::vector<b3gRayHit> hits(2); rbp.castRays(rays, hits);\n"
