@@ -362,8 +362,10 @@ def gpu_arm(args):
     capi.load()
     scene = make_scene(args, rank)
     mode = capi.SOLVER_PGS if args.solver == "pgs" else capi.SOLVER_JACOBI
+    # broadphase AUTO: the autotuner (below) times the grid and the LBVH and keeps the faster
     cfg = b3Config(solver_mode=mode, solver_iterations=args.iterations, use_cuda_graph=True,
-                   pgs_interleave=args.solver == "pgs" and args.row_order == "interleaved")
+                   pgs_interleave=args.solver == "pgs" and args.row_order == "interleaved",
+                   broadphase=capi.BROADPHASE_AUTO)
     stress = args.workload == "stress"
     if stress:
         cfg.residual_tol = 1e-4

@@ -37,7 +37,7 @@ for _dt, _sz in ((BODY, 80), (INERTIA, 96), (COLLIDABLE, 16), (HULL, 96), (FACE,
 SHAPE_CONVEX_HULL, SHAPE_PLANE, SHAPE_SPHERE = 3, 4, 7
 SOLVER_PGS, SOLVER_JACOBI = 0, 1
 JOINT_POINT2POINT, JOINT_FIXED = 3, 4
-BROADPHASE_GRID, BROADPHASE_LBVH = 0, 1
+BROADPHASE_GRID, BROADPHASE_LBVH, BROADPHASE_AUTO = 0, 1, 2
 CONSTRAINT_FLAG_ENABLED = 1
 PGS_PARTITIONS_AUTO, PGS_PARTITIONS_GLOBAL_DELTAS, PGS_PARTITIONS_NONE, PGS_PARTITIONS_SHARED = 0, 1, 2, 3
 PGS_PARTITIONS_STREAMED = 4
@@ -71,7 +71,7 @@ class b3gConfig(C.Structure):
 class b3gTuning(C.Structure):
     _fields_ = [("pgs_partitions", C.c_int), ("pairs_blocks_per_sm", C.c_int), ("narrow_blocks_per_sm", C.c_int),
                 ("sort_blocks_per_sm", C.c_int), ("pairs_ms", C.c_float), ("contacts_ms", C.c_float),
-                ("solve_ms", C.c_float), ("candidates_timed", C.c_int)]
+                ("solve_ms", C.c_float), ("candidates_timed", C.c_int), ("broadphase", C.c_int)]
 
 
 class b3gStepStats(C.Structure):

@@ -238,9 +238,9 @@ extern "C" b3gStatus b3g_create(const b3gConfig* cfg, int cuda_device, b3g_handl
         delete w;
         return fail(B3G_ERR_INVALID_ARG, "solver_blocks_per_sm must be >= 0");
     }
-    if (w->cfg.broadphase != B3G_BROADPHASE_GRID && w->cfg.broadphase != B3G_BROADPHASE_LBVH) {
+    if (w->cfg.broadphase < B3G_BROADPHASE_GRID || w->cfg.broadphase > B3G_BROADPHASE_AUTO) {
         delete w;
-        return fail(B3G_ERR_INVALID_ARG, "broadphase must be B3G_BROADPHASE_GRID or B3G_BROADPHASE_LBVH");
+        return fail(B3G_ERR_INVALID_ARG, "broadphase must be B3G_BROADPHASE_GRID, _LBVH or _AUTO");
     }
     w->device = cuda_device;
     *out = w;
@@ -770,7 +770,7 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     CUDA_TRY(cudaMemsetAsync(d.barrier, 0, 64 * sizeof(unsigned int), s));
     CUDA_TRY(cudaStreamSynchronize(s));
     d.scene_bits = d.num_scenes > 1 ? bits_for(d.num_scenes) : 0;
-    d.broadphase = h->cfg.broadphase;
+    d.broadphase = h->cfg.broadphase == B3G_BROADPHASE_LBVH ? B3G_BROADPHASE_LBVH : B3G_BROADPHASE_GRID;
     if (d.broadphase == B3G_BROADPHASE_LBVH) TRY(alloc_lbvh(d));
     h->uploaded = true;
     return B3G_OK;
@@ -778,14 +778,16 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
 
 extern "C" b3gStatus b3g_set_broadphase(b3g_handle h, int mode) {
     if (!h) return fail(B3G_ERR_INVALID_ARG, "null handle");
-    if (mode != B3G_BROADPHASE_GRID && mode != B3G_BROADPHASE_LBVH)
+    if (mode < B3G_BROADPHASE_GRID || mode > B3G_BROADPHASE_AUTO)
         return fail(B3G_ERR_INVALID_ARG, "unknown broadphase %d", mode);
     h->cfg.broadphase = mode;
     if (!h->uploaded) return B3G_OK;
     CUDA_TRY(cudaSetDevice(h->device));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     if (mode == B3G_BROADPHASE_LBVH) TRY(alloc_lbvh(h->d));
-    h->d.broadphase = mode;
+    // AUTO: the grid until the autotuner (at its next run) picks
+    h->d.broadphase = mode == B3G_BROADPHASE_LBVH ? B3G_BROADPHASE_LBVH : B3G_BROADPHASE_GRID;
+    if (mode == B3G_BROADPHASE_AUTO) h->tuned = false;
     if (h->graph_exec) {  // the captured step has the other broadphase's launches
         cudaGraphExecDestroy(h->graph_exec);
         h->graph_exec = nullptr;
@@ -1199,6 +1201,28 @@ extern "C" b3gStatus b3g_autotune(b3g_handle h, float dt, int repeats, b3gTuning
         if (st != B3G_OK) break;
         d.tune.pairs_blocks_per_sm = best_v;
         res.pairs_ms = best;
+        // broadphase AUTO: the LBVH's pair stage over the same grid sizes; the faster search stays
+        if (h->cfg.broadphase == B3G_BROADPHASE_AUTO && d.num_dynamic > 1) {
+            if ((st = alloc_lbvh(d)) != B3G_OK) break;
+            const int grid_best = best_v;
+            float lbest = 1e30f;
+            int lbest_v = grid_best;
+            d.broadphase = B3G_BROADPHASE_LBVH;
+            for (int v : grid_c) {
+                d.tune.pairs_blocks_per_sm = v;
+                if ((st = tune_time(h, dt, repeats, saved, false, run)) != B3G_OK) break;
+                timed++;
+                if (run.ms[1] < lbest) { lbest = run.ms[1]; lbest_v = v; }
+            }
+            if (st != B3G_OK) break;
+            if (lbest < best) {
+                d.tune.pairs_blocks_per_sm = lbest_v;
+                res.pairs_ms = lbest;
+            } else {
+                d.broadphase = B3G_BROADPHASE_GRID;
+                d.tune.pairs_blocks_per_sm = grid_best;
+            }
+        }
         // the thread-per-pair narrowphase kernel's grid: times the contact stage
         best = 1e30f;
         best_v = d.tune.narrow_blocks_per_sm;
@@ -1244,6 +1268,7 @@ extern "C" b3gStatus b3g_autotune(b3g_handle h, float dt, int repeats, b3gTuning
     res.narrow_blocks_per_sm = d.tune.narrow_blocks_per_sm;
     res.sort_blocks_per_sm = d.tune.sort_blocks_per_sm;
     res.candidates_timed = timed;
+    res.broadphase = d.broadphase;
     h->tuning = res;
     if (out) *out = res;
     return B3G_OK;

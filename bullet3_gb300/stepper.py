@@ -58,7 +58,7 @@ def main(argv=None):
     p.add_argument("--iterations", type=int, default=10)
     p.add_argument("--autotune", action="store_true")
     p.add_argument("--no-graph", action="store_true")
-    p.add_argument("--broadphase", choices=["grid", "lbvh"], default="grid")
+    p.add_argument("--broadphase", choices=["grid", "lbvh", "auto"], default="grid")
     p.add_argument("--stage-times", action="store_true",
                    help="also run the measured steps once more with per-stage events and print their means")
     a = p.parse_args(argv)
@@ -66,7 +66,8 @@ def main(argv=None):
     cfg = b3Config(solver_mode=capi.SOLVER_PGS if a.solver == "pgs" else capi.SOLVER_JACOBI,
                    solver_iterations=a.iterations, pgs_interleave=a.solver == "pgs",
                    use_cuda_graph=not a.no_graph,
-                   broadphase=capi.BROADPHASE_LBVH if a.broadphase == "lbvh" else capi.BROADPHASE_GRID)
+                   broadphase={"grid": capi.BROADPHASE_GRID, "lbvh": capi.BROADPHASE_LBVH,
+                               "auto": capi.BROADPHASE_AUTO}[a.broadphase])
     np_, bp, pl = scenes.load_scene(sc, cfg)
     dt = 1.0 / 60.0
     for _ in range(a.settle):

@@ -111,7 +111,7 @@ typedef struct b3gConfig {
     int warm_start_max_points; /* point slots (4 per manifold, in manifold order) that get features and
                                   predictions when warm_start != 0; 0 = 8 x bodies (at least 8192) */
     int autotune;              /* 1: the first b3g_step after an upload runs b3g_autotune (3 repeats) */
-    int broadphase;            /* B3G_BROADPHASE_GRID (0) or B3G_BROADPHASE_LBVH (1), see b3g_set_broadphase */
+    int broadphase;            /* B3G_BROADPHASE_GRID (0), _LBVH (1) or _AUTO (2), see b3g_set_broadphase */
     int reserved[1];
 } b3gConfig;
 
@@ -195,6 +195,7 @@ b3gStatus b3g_set_scene_offsets(b3g_handle h, const int* first_body, int num_sce
  * either way).  Valid before or after the upload; takes effect at the next pair search. */
 #define B3G_BROADPHASE_GRID 0
 #define B3G_BROADPHASE_LBVH 1
+#define B3G_BROADPHASE_AUTO 2 /* the grid until b3g_autotune times both and keeps the faster */
 b3gStatus b3g_set_broadphase(b3g_handle h, int mode);
 
 /* Autotuner (no reference counterpart: the reference's OpenCL kernels use fixed work-group
@@ -215,6 +216,7 @@ typedef struct b3gTuning {
     float contacts_ms;
     float solve_ms;
     int candidates_timed;
+    int broadphase;            /* the pair search in use: B3G_BROADPHASE_GRID or _LBVH (AUTO: the faster) */
 } b3gTuning;
 b3gStatus b3g_autotune(b3g_handle h, float dt, int repeats, b3gTuning* out);
 b3gStatus b3g_get_tuning(b3g_handle h, b3gTuning* out);

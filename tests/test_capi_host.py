@@ -54,7 +54,7 @@ def test_registration_errors_match_reference_conventions():
 def test_config_validation():
     h = C.c_void_p()
     for bad in (dict(pgs_partitions=5), dict(pgs_partitions=-1), dict(solver_blocks_per_sm=-2), dict(grid_dim=100),
-                dict(pgs_interleave=2), dict(broadphase=2)):
+                dict(pgs_interleave=2), dict(broadphase=3)):
         cfg = capi.default_config(**bad)
         with pytest.raises(capi.B3GError) as e:
             capi.call("b3g_create", C.byref(cfg), C.c_int(0), C.byref(h))

@@ -101,3 +101,17 @@ def test_broadphase_class_switches_the_world():
     run_stages(np_, bp, pl)
     got = pairs_xy(bp.getOverlappingPairsCPU())
     assert np.array_equal(got, pairs_xy(O.pairs_bruteforce(bp.getAllAabbsCPU())))
+
+
+def test_autotune_picks_a_broadphase_and_keeps_the_pairs():
+    sc = scenes.mixed_scene(16384, extent=36.0, seed=11, plane=True)
+    np_, bp, pl, shapes = load(sc, m_maxBroadphasePairs=1000000, broadphase=capi.BROADPHASE_AUTO)
+    grid, _ = _pairs(np_, bp, pl, capi.BROADPHASE_AUTO)  # AUTO before tuning: the grid
+    pl.setBroadphase(capi.BROADPHASE_AUTO)
+    t = pl.autotune(1 / 60, repeats=2)
+    assert t["broadphase"] in (capi.BROADPHASE_GRID, capi.BROADPHASE_LBVH)
+    pl.setupGpuAabbsFull()
+    bp.calculateOverlappingPairs()
+    pl.synchronize()
+    assert np.array_equal(pairs_xy(bp.getOverlappingPairsCPU()), grid)
+    assert pl.status() == 0
