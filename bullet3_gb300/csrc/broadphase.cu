@@ -534,11 +534,21 @@ __global__ void __launch_bounds__(BP_THREADS) k_lbvh_bounds(const b3gAabb* __res
             mn[k] = fminf(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
             mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
         }
+    // then across the block's warps, so that each block adds 6 atomics on the 6 shared words
+    __shared__ float s_b[6][BP_THREADS / 32];
+    const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0)
         for (int k = 0; k < 3; k++) {
-            atomicMin(&bounds[k], ord_enc(mn[k]));
-            atomicMin(&bounds[3 + k], ~ord_enc(mx[k]));
+            s_b[k][w] = mn[k];
+            s_b[3 + k][w] = mx[k];
         }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int k = threadIdx.x;
+        float v = s_b[k][0];
+        for (int j = 1; j < BP_THREADS / 32; j++) v = k < 3 ? fminf(v, s_b[k][j]) : fmaxf(v, s_b[k][j]);
+        atomicMin(&bounds[k], k < 3 ? ord_enc(v) : ~ord_enc(v));
+    }
 }
 
 // 10 bits -> every third bit of 30
