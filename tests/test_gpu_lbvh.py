@@ -115,3 +115,15 @@ def test_autotune_picks_a_broadphase_and_keeps_the_pairs():
     pl.synchronize()
     assert np.array_equal(pairs_xy(bp.getOverlappingPairsCPU()), grid)
     assert pl.status() == 0
+
+
+def test_lbvh_equals_grid_at_scale_every_step():
+    # the 131,072-body collision-at-scale mix: pair lists identical at every step while it moves
+    sc = scenes.mixed_scene(131072, extent=64.0, seed=0)
+    np_, bp, pl, shapes = load(sc, use_cuda_graph=False)
+    for step in range(4):
+        grid, _ = _pairs(np_, bp, pl, capi.BROADPHASE_GRID)
+        lbvh, _ = _pairs(np_, bp, pl, capi.BROADPHASE_LBVH)
+        assert len(grid) > 100000 and np.array_equal(lbvh, grid), step
+        pl.stepSimulation(1 / 60)
+    assert pl.status() == 0
