@@ -34,7 +34,9 @@ struct JArgs {
     b3gBody* bodies;
     const b3gInertia* inertias;
     b3gJoint* joints;
+    JointHdr* hdr;       // 1 per joint
     JointRow* rows;      // 6 per joint
+    float* imp;          // 6 per joint: applied impulses
     float4* dv;          // 2 per body: delta linear, delta angular velocity
     const int* order;    // joint indices, batch by batch
     const int* batch_off;
@@ -125,6 +127,23 @@ __device__ __forceinline__ int joint_rows(int type) {
     return type == B3G_JOINT_FIXED ? 6 : type == B3G_JOINT_POINT2POINT ? 3 : 0;
 }
 
+// Axes of row j: linear Jacobian n, angular Jacobians r1 (body A) and r2 (body B).  Rows 0-2 of
+// getInfo2Point2Point: n = unit axis, r1 = skew row of -a1, r2 = skew row of a2; rows 3-5 of
+// getInfo2FixedOrientation: n = 0, r1 = unit axis, r2 = -unit axis (jointSolver.cl:479-486,
+// 488-541, 592-628).  Setup and sweeps both rebuild the rows through this function.
+__device__ __forceinline__ void row_axes(int j, v3j m1, v3j a2, v3j& n, v3j& r1, v3j& r2) {
+    const int e = j < 3 ? j : j - 3;
+    if (j < 3) {
+        n = mkj(e == 0 ? 1.f : 0.f, e == 1 ? 1.f : 0.f, e == 2 ? 1.f : 0.f);
+        r1 = e == 0 ? mkj(0.f, -m1.z, m1.y) : e == 1 ? mkj(m1.z, 0.f, -m1.x) : mkj(-m1.y, m1.x, 0.f);
+        r2 = e == 0 ? mkj(0.f, -a2.z, a2.y) : e == 1 ? mkj(a2.z, 0.f, -a2.x) : mkj(-a2.y, a2.x, 0.f);
+    } else {
+        n = mkj(0.f, 0.f, 0.f);
+        r1 = mkj(e == 0 ? 1.f : 0.f, e == 1 ? 1.f : 0.f, e == 2 ? 1.f : 0.f);
+        r2 = mkj(e == 0 ? -1.f : 0.f, e == 1 ? -1.f : 0.f, e == 2 ? -1.f : 0.f);
+    }
+}
+
 // getInfo2Kernel for joint i: rows, then the finalize loop (limits, angular components,
 // jacDiagABInv, rhs from the positional error and the bodies' current velocities)
 __device__ void joint_setup(const JArgs& a, int i) {
@@ -158,25 +177,18 @@ __device__ void joint_setup(const JArgs& a, int i) {
     const b3gMat3 IA = a.inertias[A].invInertiaWorld, IB = a.inertias[B].invInertiaWorld;
     const v3j vA = xyz(bA.linVel), wA = xyz(bA.angVel), vB = xyz(bB.linVel), wB = xyz(bB.angVel);
     JointRow* out = a.rows + 6 * (size_t)i;
+    float* imp = a.imp + 6 * (size_t)i;
+    // every row's limits: +-infinity clamped to the breaking threshold
+    float lo = -JT_INFINITY, hi = JT_INFINITY;
+    if (hi >= c.breakingImpulseThreshold) hi = c.breakingImpulseThreshold;
+    if (lo <= -c.breakingImpulseThreshold) lo = -c.breakingImpulseThreshold;
 #pragma unroll 1
     for (int j = 0; j < nr; ++j) {
         v3j n, r1, r2;
-        float rhs;
+        row_axes(j, m1, a2, n, r1, r2);
         const int e = j < 3 ? j : j - 3;
-        if (j < 3) {
-            n = mkj(e == 0 ? 1.f : 0.f, e == 1 ? 1.f : 0.f, e == 2 ? 1.f : 0.f);
-            r1 = e == 0 ? mkj(0.f, -m1.z, m1.y) : e == 1 ? mkj(m1.z, 0.f, -m1.x) : mkj(-m1.y, m1.x, 0.f);
-            r2 = e == 0 ? mkj(0.f, -a2.z, a2.y) : e == 1 ? mkj(a2.z, 0.f, -a2.x) : mkj(-a2.y, a2.x, 0.f);
-            rhs = k * (e == 0 ? err.x : e == 1 ? err.y : err.z);
-        } else {
-            n = mkj(0.f, 0.f, 0.f);
-            r1 = mkj(e == 0 ? 1.f : 0.f, e == 1 ? 1.f : 0.f, e == 2 ? 1.f : 0.f);
-            r2 = mkj(e == 0 ? -1.f : 0.f, e == 1 ? -1.f : 0.f, e == 2 ? -1.f : 0.f);
-            rhs = k * (e == 0 ? ang.x : e == 1 ? ang.y : ang.z);
-        }
-        float lo = -JT_INFINITY, hi = JT_INFINITY;
-        if (hi >= c.breakingImpulseThreshold) hi = c.breakingImpulseThreshold;
-        if (lo <= -c.breakingImpulseThreshold) lo = -c.breakingImpulseThreshold;
+        const float rhs = j < 3 ? k * (e == 0 ? err.x : e == 1 ? err.y : err.z)
+                                : k * (e == 0 ? ang.x : e == 1 ? ang.y : ang.z);
         const v3j angA = mt_mul1(IA, r1), angB = mt_mul1(IB, r2);
         const v3j lA = mkj(n.x * bA.invMass, n.y * bA.invMass, n.z * bA.invMass);
         const v3j lB = mkj(n.x * bB.invMass, n.y * bB.invMass, n.z * bB.invMass);
@@ -191,59 +203,71 @@ __device__ void joint_setup(const JArgs& a, int i) {
         const float pen = rhs * jinv;
         const float vimp = (0.f - rel * a.damping) * jinv;
         JointRow r;
-        r.n_rhs = make_float4(n.x, n.y, n.z, pen + vimp);
-        r.r1_jinv = make_float4(r1.x, r1.y, r1.z, jinv);
-        r.r2_lo = make_float4(r2.x, r2.y, r2.z, lo);
-        r.angA_hi = make_float4(angA.x, angA.y, angA.z, hi);
-        r.angB_imp = make_float4(angB.x, angB.y, angB.z, 0.f);
+        r.angA_rhs = make_float4(angA.x, angA.y, angA.z, pen + vimp);
+        r.angB_jinv = make_float4(angB.x, angB.y, angB.z, jinv);
         out[j] = r;
+        imp[j] = 0.f;
     }
+    JointHdr h;
+    h.m1_lo = make_float4(m1.x, m1.y, m1.z, lo);
+    h.a2_hi = make_float4(a2.x, a2.y, a2.z, hi);
+    h.A = A;
+    h.B = B;
+    h.active_rows = (c.flags & 1) ? nr : 0;  // the flags change only in the break check, after the sweeps
+    h.imA = bA.invMass;
+    h.imB = bB.invMass;
+    h.pad[0] = h.pad[1] = h.pad[2] = 0;
+    a.hdr[i] = h;
 }
 
 // resolveSingleConstraintRowGeneric over a joint's rows (jointSolver.cl:273-301); the deltas stay in
 // registers across the rows.  A static body's deltas stay exactly zero (its inverse mass and world
 // inverse inertia are zero), so they are not stored: joints of one batch may share a static body.
 __device__ void joint_solve(const JArgs& a, int ci) {
-    const b3gJoint& c = a.joints[ci];
-    if (!(c.flags & 1)) return;
-    const int nr = joint_rows(c.type);
-    const int A = c.rbA, B = c.rbB;
-    const float imA = a.bodies[A].invMass, imB = a.bodies[B].invMass;
+    const JointHdr h = a.hdr[ci];
+    const int nr = h.active_rows;
+    if (nr == 0) return;
+    const int A = h.A, B = h.B;
+    const float imA = h.imA, imB = h.imB;
+    const v3j m1 = xyz(h.m1_lo), a2 = xyz(h.a2_hi);
+    const float lo = h.m1_lo.w, hi = h.a2_hi.w;
     float4 dlA = a.dv[2 * A], daA = a.dv[2 * A + 1], dlB = a.dv[2 * B], daB = a.dv[2 * B + 1];
-    JointRow* rows = a.rows + 6 * (size_t)ci;
+    const JointRow* rows = a.rows + 6 * (size_t)ci;
+    float* imp = a.imp + 6 * (size_t)ci;
     for (int j = 0; j < nr; ++j) {
-        JointRow r = rows[j];
-        const v3j n = xyz(r.n_rhs), r1 = xyz(r.r1_jinv), r2 = xyz(r.r2_lo);
-        const float applied = r.angB_imp.w, jinv = r.r1_jinv.w;
-        float delta = r.n_rhs.w - applied * a.cfm;
+        v3j n, r1, r2;
+        row_axes(j, m1, a2, n, r1, r2);
+        const JointRow r = rows[j];
+        const float applied = imp[j], jinv = r.angB_jinv.w;
+        float delta = r.angA_rhs.w - applied * a.cfm;
         const float d1 = dotj(n, xyz(dlA)) + dotj(r1, xyz(daA));
         const float d2 = -dotj(n, xyz(dlB)) + dotj(r2, xyz(daB));
         delta -= d1 * jinv;
         delta -= d2 * jinv;
         const float sum = applied + delta;
         float now;
-        if (sum < r.r2_lo.w) {
-            delta = r.r2_lo.w - applied;
-            now = r.r2_lo.w;
-        } else if (sum > r.angA_hi.w) {
-            delta = r.angA_hi.w - applied;
-            now = r.angA_hi.w;
+        if (sum < lo) {
+            delta = lo - applied;
+            now = lo;
+        } else if (sum > hi) {
+            delta = hi - applied;
+            now = hi;
         } else {
             now = sum;
         }
-        rows[j].angB_imp.w = now;
+        imp[j] = now;
         dlA.x += (n.x * imA) * delta;
         dlA.y += (n.y * imA) * delta;
         dlA.z += (n.z * imA) * delta;
-        daA.x += r.angA_hi.x * delta;
-        daA.y += r.angA_hi.y * delta;
-        daA.z += r.angA_hi.z * delta;
+        daA.x += r.angA_rhs.x * delta;
+        daA.y += r.angA_rhs.y * delta;
+        daA.z += r.angA_rhs.z * delta;
         dlB.x += (-n.x * imB) * delta;
         dlB.y += (-n.y * imB) * delta;
         dlB.z += (-n.z * imB) * delta;
-        daB.x += r.angB_imp.x * delta;
-        daB.y += r.angB_imp.y * delta;
-        daB.z += r.angB_imp.z * delta;
+        daB.x += r.angB_jinv.x * delta;
+        daB.y += r.angB_jinv.y * delta;
+        daB.z += r.angB_jinv.z * delta;
     }
     if (imA != 0.f) {
         a.dv[2 * A] = dlA;
@@ -281,7 +305,7 @@ __global__ void __launch_bounds__(JT_THREADS) k_joints(JArgs a) {
         const int nr = joint_rows(a.joints[i].type);
         const float thr = a.joints[i].breakingImpulseThreshold;
         for (int j = 0; j < nr; ++j)
-            if (fabsf(a.rows[6 * (size_t)i + j].angB_imp.w) >= thr) a.joints[i].flags = 0;
+            if (fabsf(a.imp[6 * (size_t)i + j]) >= thr) a.joints[i].flags = 0;
     }
     // writeBackVelocitiesKernel for the bodies the joints name (the others' deltas are zero)
     for (int u = tid; u < a.num_uniq; u += nth) {
@@ -319,7 +343,9 @@ long long launch_joints(DeviceState& d, const b3gConfig& cfg, cudaStream_t s) {
     a.bodies = d.bodies;
     a.inertias = d.inertias;
     a.joints = d.joints;
+    a.hdr = d.joint_hdr;
     a.rows = d.joint_rows;
+    a.imp = d.joint_imp;
     a.dv = d.joint_dv;
     a.order = d.joint_order;
     a.batch_off = d.joint_batch_off;

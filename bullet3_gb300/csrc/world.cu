@@ -138,7 +138,9 @@ static b3gStatus alloc_lbvh(b3g::DeviceState& d) {
 
 static void free_joint_buffers(b3g::DeviceState& d) {
     cudaFree(d.joints);
+    cudaFree(d.joint_hdr);
     cudaFree(d.joint_rows);
+    cudaFree(d.joint_imp);
     cudaFree(d.joint_order);
     cudaFree(d.joint_batch_off);
     cudaFree(d.joint_uniq);
@@ -914,7 +916,9 @@ static b3gStatus prepare_joints(b3gWorld* h) {
     if (n > d.joint_cap) {
         const int cap = std::max(n, std::max(64, 2 * d.joint_cap));
         TRY(joint_alloc(&d.joints, (size_t)cap));
+        TRY(joint_alloc(&d.joint_hdr, (size_t)cap));
         TRY(joint_alloc(&d.joint_rows, 6 * (size_t)cap));
+        TRY(joint_alloc(&d.joint_imp, 6 * (size_t)cap));
         TRY(joint_alloc(&d.joint_order, (size_t)cap));
         TRY(joint_alloc(&d.joint_batch_off, (size_t)cap + 1));
         TRY(joint_alloc(&d.joint_uniq, 2 * (size_t)cap));

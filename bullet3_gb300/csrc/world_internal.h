@@ -51,13 +51,21 @@ struct SolverPoints {
     float4* imp = nullptr;   // [4m+j]   applied impulses: contact, dir2, dir1, (unused)
 };
 
-// One joint row (b3SolverConstraint's fields a joint row uses, jointSolver.cl:129-160), 80 B.
-struct JointRow {
-    float4 n_rhs;     // J1 linear axis (contact normal) xyz, w = rhs
-    float4 r1_jinv;   // J1 angular axis xyz, w = jacDiagABInv
-    float4 r2_lo;     // J2 angular axis xyz, w = lower limit
-    float4 angA_hi;   // angular component A xyz, w = upper limit
-    float4 angB_imp;  // angular component B xyz, w = applied impulse
+// Joint solver records.  A row of b3SolverConstraint (jointSolver.cl:129-160) is rebuilt from
+// them with the same values: a ball joint's rows have the unit axes as linear Jacobian and the
+// skew rows of -a1 and a2 (the rotated pivots) as angular Jacobians; a fixed joint's angular rows
+// have +-unit axes.  So the joint keeps -a1 and a2 once and a row keeps only what differs.
+struct JointHdr {      // 64 B per joint
+    float4 m1_lo;      // -a1 xyz, w = lower limit of every row
+    float4 a2_hi;      // a2 xyz, w = upper limit
+    int A, B;          // bodies
+    int active_rows;   // rows to sweep: 3 / 6, 0 when the joint is disabled
+    float imA, imB;    // inverse masses at setup
+    int pad[3];
+};
+struct JointRow {      // 32 B per row (+ 4 B applied impulse in its own array)
+    float4 angA_rhs;   // angular component A xyz, w = rhs
+    float4 angB_jinv;  // angular component B xyz, w = jacDiagABInv
 };
 
 // Launch shapes chosen by the autotuner (b3g_autotune); the defaults are the untuned shapes.
@@ -94,7 +102,9 @@ struct DeviceState {
     // joints (own allocations, grown on demand; the host registry is authoritative except for
     // the enabled flags, which the device's break check clears)
     b3gJoint* joints = nullptr;
+    JointHdr* joint_hdr = nullptr;   // 1 per joint
     JointRow* joint_rows = nullptr;  // 6 per joint
+    float* joint_imp = nullptr;      // 6 per joint: applied impulses
     int* joint_order = nullptr;      // joint indices batch by batch
     int* joint_batch_off = nullptr;  // num_joint_batches + 1
     int* joint_uniq = nullptr;       // the bodies joints name, once each
