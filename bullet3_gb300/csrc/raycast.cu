@@ -26,6 +26,8 @@ namespace b3g {
 struct RayArgs {
     const float4* rays;     // 2 per ray: from, to
     b3gRayHit* hits;
+    const uint32_t* order;  // rays in Morton order of their origin cell (thread i casts ray order[i])
+    const b3gAabb* aabbs;   // world AABBs of the current poses
     int n;
     const b3gBody* bodies;
     const b3gCollidable* cols;
@@ -116,6 +118,34 @@ struct RayBest {
     v3 normal;  // hull: face normal (body frame); sphere: from the centre to the hit point
 };
 
+// Conservative rejection: does the segment, up to the best fraction so far, come within a margin
+// of the body's world AABB?  The body lies inside that AABB, so a body rejected here cannot be
+// hit at a fraction <= best; the margin (1e-3 + 1e-4 x the coordinate's magnitude) is far above
+// the rounding of the exact tests, so no hit is lost and the results do not change.
+__device__ __forceinline__ bool ray_near_aabb(const RayArgs& a, int j, v3 from, v3 to, float tmax) {
+    const float4 mn = __ldg(reinterpret_cast<const float4*>(a.aabbs) + 2 * j);
+    const float4 mx = __ldg(reinterpret_cast<const float4*>(a.aabbs) + 2 * j + 1);
+    const float f[3] = {from.x, from.y, from.z}, d[3] = {to.x - from.x, to.y - from.y, to.z - from.z};
+    const float lo[3] = {mn.x, mn.y, mn.z}, hi[3] = {mx.x, mx.y, mx.z};
+    float t0 = 0.f, t1 = tmax;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float m = 1e-3f + 1e-4f * fmaxf(fabsf(lo[k]), fabsf(hi[k]));
+        const float l = lo[k] - m, h = hi[k] + m;
+        if (fabsf(d[k]) < 1e-20f) {
+            if (f[k] < l || f[k] > h) return false;
+            continue;
+        }
+        const float inv = 1.f / d[k];
+        float ta = (l - f[k]) * inv, tb = (h - f[k]) * inv;
+        if (ta > tb) { const float t = ta; ta = tb; tb = t; }
+        t0 = fmaxf(t0, ta - 1e-4f);
+        t1 = fminf(t1, tb + 1e-4f);
+        if (t0 > t1) return false;
+    }
+    return true;
+}
+
 __device__ __forceinline__ void ray_test(const RayArgs& a, int j, v3 from, v3 to, int ignore, RayBest& best) {
     if (j == ignore) return;
     const b3gBody& B = a.bodies[j];
@@ -148,7 +178,8 @@ __device__ __forceinline__ void ray_test(const RayArgs& a, int j, v3 from, v3 to
 
 __global__ void __launch_bounds__(128) k_cast_rays(RayArgs a) {
     const int mask = (1 << a.bits) - 1;
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < a.n; r += gridDim.x * blockDim.x) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+        const int r = (int)a.order[i];
         const float4 f4 = a.rays[2 * r], t4 = a.rays[2 * r + 1];
         const v3 from = mk3(f4.x, f4.y, f4.z), to = mk3(t4.x, t4.y, t4.z);
         const int ignore = a.hits[r].hitResult2;
@@ -189,18 +220,31 @@ __global__ void __launch_bounds__(128) k_cast_rays(RayArgs a) {
                 }
             }
             const int max_cells = (int)(fabs(d[0]) + fabs(d[1]) + fabs(d[2])) + 4;
+            // the bodies whose centre cell lies within one cell of a visited cell: the whole 3x3x3
+            // neighbourhood of the first cell, then per step only the 3x3 slab that enters it (the
+            // union is the same set, each cell scanned once; the best hit is the minimum of
+            // (fraction, body index), so the order of the tests does not matter)
+            int entered = -1;  // axis of the last step (-1: the first cell)
+            const int step0 = step[0], step1 = step[1], step2 = step[2];
             for (int visit = 0; visit < max_cells; visit++) {
-                for (int nz = -1; nz <= 1; nz++)
-                    for (int ny = -1; ny <= 1; ny++)
-                        for (int nx = -1; nx <= 1; nx++) {
-                            const uint32_t h =
-                                cell_hash(c[0] + nx + sh.x, c[1] + ny + sh.y, c[2] + nz + sh.z, a.bits, mask);
+                const int ulo = entered < 0 ? -1 : 0, uhi = entered < 0 ? 1 : 0;
+                for (int u = ulo; u <= uhi; u++)
+                    for (int v = -1; v <= 1; v++)
+                        for (int w = -1; w <= 1; w++) {
+                            // offsets from the cell: the full cube, or the entered slab (fixed one
+                            // step ahead along the stepped axis, the other two axes spanning -1..1)
+                            const int ox = entered == 0 ? step0 : w;
+                            const int oy = entered == 1 ? step1 : (entered == 0 ? w : v);
+                            const int oz = entered == 2 ? step2 : (entered < 0 ? u : v);
+                            const uint32_t h = cell_hash(c[0] + ox + sh.x, c[1] + oy + sh.y, c[2] + oz + sh.z,
+                                                         a.bits, mask);
                             const uint32_t s0 = __ldg(&a.cell_start[h]);
                             if (s0 >= (uint32_t)a.n_dyn || __ldg(&a.keys[s0]) != h) continue;
                             if (s0 > 0 && __ldg(&a.keys[s0 - 1]) == h) continue;
                             for (uint32_t q = s0; q < (uint32_t)a.n_dyn && __ldg(&a.keys[q]) == h; q++) {
                                 const int j = (int)__ldg(&a.vals[q]);
                                 if (a.body_scene && __ldg(&a.body_scene[j]) != scene) continue;
+                                if (!ray_near_aabb(a, j, from, to, best.t)) continue;
                                 ray_test(a, j, from, to, ignore, best);
                             }
                         }
@@ -210,6 +254,7 @@ __global__ void __launch_bounds__(128) k_cast_rays(RayArgs a) {
                 if (tn > 1.0 || tn > (double)best.t) break;
                 c[k] += step[k];
                 tmax[k] += tdelta[k];
+                entered = k;
             }
         }
         b3gRayHit& out = a.hits[r];
@@ -226,13 +271,44 @@ __global__ void __launch_bounds__(128) k_cast_rays(RayArgs a) {
     }
 }
 
+// Morton code of the grid cell of each ray's origin (10 bits per axis), for the ray order
+__device__ __forceinline__ uint32_t ray_spread3(uint32_t x) {
+    x = (x | (x << 16)) & 0x030000FFu;
+    x = (x | (x << 8)) & 0x0300F00Fu;
+    x = (x | (x << 4)) & 0x030C30C3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+__global__ void k_ray_keys(const float4* __restrict__ rays, int n, float inv_cell, uint32_t* __restrict__ keys,
+                           uint32_t* __restrict__ vals) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const float4 f = rays[2 * r];
+        const uint32_t cx = (uint32_t)(int)floorf(f.x * inv_cell) & 1023u;
+        const uint32_t cy = (uint32_t)(int)floorf(f.y * inv_cell) & 1023u;
+        const uint32_t cz = (uint32_t)(int)floorf(f.z * inv_cell) & 1023u;
+        keys[r] = (ray_spread3(cx) << 2) | (ray_spread3(cy) << 1) | ray_spread3(cz);
+        vals[r] = (uint32_t)r;
+    }
+}
+
 int launch_cast_rays(DeviceState& d, const float4* rays, b3gRayHit* hits, int n, cudaStream_t s) {
     int launches = launch_aabbs(d, s);  // the grid of the current poses
     launches += launch_cells(d, s);
     if (n <= 0) return launches;
+    // neighbouring rays in neighbouring lanes: they walk the same cells and test the same bodies
+    const int kgrid = std::max(1, std::min((n + 255) / 256, d.num_sms * 8));
+    uint32_t* rk = d.ray_order;
+    k_ray_keys<<<kgrid, 256, 0, s>>>(rays, n, d.inv_cell, rk, rk + 2 * (size_t)d.ray_cap);
+    long long ll = 0;
+    d.prim.sort_blocks = d.num_sms * d.tune.sort_blocks_per_sm;
+    const int w = radix_sort_u32(d.prim, rk, rk + d.ray_cap, rk + 2 * (size_t)d.ray_cap, rk + 3 * (size_t)d.ray_cap,
+                                 d.ray_n, 30, d.sort_scratch, s, &ll);
+    launches += 1 + (int)ll;
     RayArgs a;
     a.rays = rays;
     a.hits = hits;
+    a.order = rk + (w ? 3 : 2) * (size_t)d.ray_cap;
+    a.aabbs = d.aabbs;
     a.n = n;
     a.bodies = d.bodies;
     a.cols = d.collidables;

@@ -1288,6 +1288,8 @@ extern "C" b3gStatus b3g_cast_rays(b3g_handle h, const void* host_rays, void* ho
         const int cap = std::max(n, 2 * d.ray_cap);
         TRY(dalloc(h, &d.ray_buf, 2 * (size_t)cap));
         TRY(dalloc(h, &d.hit_buf, (size_t)cap));
+        TRY(dalloc(h, &d.ray_order, 4 * (size_t)cap));
+        if (!d.ray_n) TRY(dalloc(h, &d.ray_n, 1));
         d.ray_cap = cap;
     }
     cudaStream_t s = h->stream;
@@ -1295,6 +1297,8 @@ extern "C" b3gStatus b3g_cast_rays(b3g_handle h, const void* host_rays, void* ho
         CUDA_TRY(cudaMemcpyAsync(d.ray_buf, host_rays, sizeof(b3gRayInfo) * (size_t)n, cudaMemcpyHostToDevice, s));
         CUDA_TRY(cudaMemcpyAsync(d.hit_buf, host_hits, sizeof(b3gRayHit) * (size_t)n, cudaMemcpyHostToDevice, s));
     }
+    const int count = n;  // the sort length; the stream is synchronised before this function returns
+    if (n > 0) CUDA_TRY(cudaMemcpyAsync(d.ray_n, &count, sizeof(int), cudaMemcpyHostToDevice, s));
     h->launches += launch_cast_rays(d, d.ray_buf, d.hit_buf, n, s);
     TRY(check_launch(h));
     if (n > 0)

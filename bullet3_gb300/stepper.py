@@ -59,6 +59,8 @@ def main(argv=None):
     p.add_argument("--autotune", action="store_true")
     p.add_argument("--no-graph", action="store_true")
     p.add_argument("--broadphase", choices=["grid", "lbvh", "auto"], default="grid")
+    p.add_argument("--rays", type=int, default=0,
+                   help="after the steps, time castRays of this many random downward rays over the bodies")
     p.add_argument("--stage-times", action="store_true",
                    help="also run the measured steps once more with per-stage events and print their means")
     a = p.parse_args(argv)
@@ -97,8 +99,34 @@ def main(argv=None):
         pl.setProfiling(False)
         names = ["aabbs", "pairs", "contacts", "joints", "solver", None, "integrate"]
         stage_ms = {k: round(float(v) / max(a.steps, 1), 4) for k, v in zip(names, acc) if k}
+    rays_out = None
+    if a.rays > 0:
+        import numpy as np
+        b = np_.readbackAllBodiesToCpu()
+        dyn = b[b["invMass"] != 0]["pos"][:, :3]
+        lo, hi = dyn.min(0), dyn.max(0)
+        rng = np.random.Generator(np.random.PCG64(0))
+        rays = np.zeros(a.rays, capi.RAY)
+        xz = rng.uniform(lo[[0, 2]], hi[[0, 2]], (a.rays, 2)).astype(np.float32)
+        rays["from"][:, 0], rays["from"][:, 2], rays["from"][:, 1] = xz[:, 0], xz[:, 1], hi[1] + 5.0
+        rays["to"][:, 0], rays["to"][:, 2], rays["to"][:, 1] = xz[:, 0], xz[:, 1], lo[1] - 1.0
+        h = np_.world.handle
+        for _ in range(3):
+            hits = pl.castRays(rays)
+        reps = 5
+        t0 = time.perf_counter()
+        capi.call("b3g_record_event", h, capi.C.c_int(0))
+        for _ in range(reps):
+            hits = pl.castRays(rays)
+        capi.call("b3g_record_event", h, capi.C.c_int(1))
+        wall = (time.perf_counter() - t0) / reps
+        ms = capi.C.c_float()
+        capi.call("b3g_event_elapsed", h, capi.C.c_int(0), capi.C.c_int(1), capi.C.byref(ms))
+        rays_out = {"rays": a.rays, "hit_fraction": float((hits["hitFraction"] < 1.0).mean()),
+                    "device_ms_per_cast": ms.value / reps, "host_ms_per_cast": 1000 * wall,
+                    "rays_per_s": a.rays / wall}
     st = pl.stats()
-    print(json.dumps({"workload": a.workload, "broadphase": a.broadphase, "bodies": sc.num_bodies, "steps": a.steps,
+    print(json.dumps({"workload": a.workload, "broadphase": a.broadphase, "rays": rays_out, "bodies": sc.num_bodies, "steps": a.steps,
                       "joints": pl.getNumConstraints(), "stage_ms": stage_ms,
                       "host_ms_per_step": 1000 * secs / max(a.steps, 1), "pairs": st.num_pairs,
                       "manifolds": st.num_contacts, "points": st.num_points, "colors": st.num_colors,

@@ -157,3 +157,18 @@ def test_trajectory_matches_oracle_and_chains_hold():
     assert err.max() < 0.15, err.max()
     # the chains swung and still hang below the anchor
     assert (gb["pos"][sc.mass > 0, 1] < b["pos"][0, 1]).all()
+
+
+def test_edge_joints_static_pair_and_zero_threshold():
+    # a joint between two static bodies (rows with no mass: jacDiagABInv 0, inert) and a joint whose
+    # breaking threshold is 0 (|impulse| >= 0 holds at once: it breaks in its first stage)
+    sc = scenes.hanging_chains(2, 3, seed=9, ground=True)
+    np_, bp, pl, shapes = load(sc)
+    anchor, ground = 0, sc.num_bodies - 1
+    u_static = pl.createPoint2PointConstraint(anchor, ground, (0, 0, 0), (0, 5, 0), 1e30)
+    u_zero = pl.createFixedConstraint(1, 4, (0, 0, 0), (0, 0, 0), (0, 0, 0, 1), 0.0)
+    gj = _run_stages(np_, pl, 3)
+    flags = dict(zip(gj["uid"], gj["flags"]))
+    assert flags[u_zero] == 0 and flags[u_static] == 1
+    b = np_.readbackAllBodiesToCpu()
+    assert np.array_equal(b["linVel"][[anchor, ground]], np.zeros((2, 4), np.float32))
