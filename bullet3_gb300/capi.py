@@ -92,7 +92,7 @@ _LIB = None
 EXPORTS = [
     "b3g_config_default", "b3g_create", "b3g_destroy", "b3g_last_error", "b3g_version", "b3g_register_sphere",
     "b3g_register_plane", "b3g_register_hull", "b3g_register_hull_tables", "b3g_register_body",
-    "b3g_write_all_to_gpu", "b3g_set_gravity", "b3g_set_solver", "b3g_set_scene_offsets", "b3g_set_broadphase", "b3g_autotune", "b3g_get_tuning", "b3g_profiler_range", "b3g_cast_rays", "b3g_create_point2point_constraint", "b3g_create_fixed_constraint",
+    "b3g_write_all_to_gpu", "b3g_set_gravity", "b3g_set_solver", "b3g_set_scene_offsets", "b3g_set_broadphase", "b3g_autotune", "b3g_get_tuning", "b3g_profiler_range", "b3g_cast_rays", "b3g_cast_rays_device", "b3g_create_point2point_constraint", "b3g_create_fixed_constraint",
     "b3g_remove_constraint", "b3g_get_num_constraints", "b3g_read_constraints", "b3g_read_joint_order",
     "b3g_solve_joints", "b3g_step", "b3g_setup_aabbs",
     "b3g_calculate_overlapping_pairs", "b3g_compute_contacts", "b3g_solve_contacts", "b3g_integrate",

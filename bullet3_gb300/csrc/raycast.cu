@@ -271,6 +271,9 @@ __global__ void __launch_bounds__(128) k_cast_rays(RayArgs a) {
     }
 }
 
+__global__ void k_set_int(int* p, int v) { *p = v; }
+void launch_set_int(int* p, int v, cudaStream_t s) { k_set_int<<<1, 1, 0, s>>>(p, v); }
+
 // Morton code of the grid cell of each ray's origin (10 bits per axis), for the ray order
 __device__ __forceinline__ uint32_t ray_spread3(uint32_t x) {
     x = (x | (x << 16)) & 0x030000FFu;

@@ -1279,19 +1279,42 @@ extern "C" b3gStatus b3g_autotune(b3g_handle h, float dt, int repeats, b3gTuning
 }
 
 // ---------------------------------------------------------------------------------- ray casts
+static b3gStatus ray_buffers(b3gWorld* h, int n) {
+    DeviceState& d = h->d;
+    if (n <= d.ray_cap) return B3G_OK;
+    const int cap = std::max(n, 2 * d.ray_cap);
+    TRY(dalloc(h, &d.ray_buf, 2 * (size_t)cap));
+    TRY(dalloc(h, &d.hit_buf, (size_t)cap));
+    TRY(dalloc(h, &d.ray_order, 4 * (size_t)cap));
+    if (!d.ray_n) TRY(dalloc(h, &d.ray_n, 1));
+    d.ray_cap = cap;
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_cast_rays_device(b3g_handle h, const void* device_rays, void* device_hits, int n) {
+    REQUIRE_UPLOADED(h);
+    if (n < 0 || (n > 0 && (!device_rays || !device_hits))) return fail(B3G_ERR_INVALID_ARG, "invalid ray arguments");
+    if ((reinterpret_cast<uintptr_t>(device_rays) | reinterpret_cast<uintptr_t>(device_hits)) & 15u)
+        return fail(B3G_ERR_INVALID_ARG, "ray and hit buffers must be 16-byte aligned");
+    CUDA_TRY(cudaSetDevice(h->device));
+    TRY(ray_buffers(h, n));
+    DeviceState& d = h->d;
+    if (n > 0) {
+        // the sort length, written by a kernel so that the call stays asynchronous
+        b3g::launch_set_int(d.ray_n, n, h->stream);
+    }
+    h->launches += launch_cast_rays(d, reinterpret_cast<const float4*>(device_rays),
+                                    reinterpret_cast<b3gRayHit*>(device_hits), n, h->stream) + (n > 0 ? 1 : 0);
+    TRY(check_launch(h));
+    return B3G_OK;
+}
+
 extern "C" b3gStatus b3g_cast_rays(b3g_handle h, const void* host_rays, void* host_hits, int n) {
     REQUIRE_UPLOADED(h);
     if (n < 0 || (n > 0 && (!host_rays || !host_hits))) return fail(B3G_ERR_INVALID_ARG, "invalid ray arguments");
     CUDA_TRY(cudaSetDevice(h->device));
     DeviceState& d = h->d;
-    if (n > d.ray_cap) {
-        const int cap = std::max(n, 2 * d.ray_cap);
-        TRY(dalloc(h, &d.ray_buf, 2 * (size_t)cap));
-        TRY(dalloc(h, &d.hit_buf, (size_t)cap));
-        TRY(dalloc(h, &d.ray_order, 4 * (size_t)cap));
-        if (!d.ray_n) TRY(dalloc(h, &d.ray_n, 1));
-        d.ray_cap = cap;
-    }
+    TRY(ray_buffers(h, n));
     cudaStream_t s = h->stream;
     if (n > 0) {
         CUDA_TRY(cudaMemcpyAsync(d.ray_buf, host_rays, sizeof(b3gRayInfo) * (size_t)n, cudaMemcpyHostToDevice, s));

@@ -227,6 +227,7 @@ int launch_aabbs(DeviceState& d, cudaStream_t s);
 int launch_pairs(DeviceState& d, cudaStream_t s);
 int launch_cells(DeviceState& d, cudaStream_t s);
 int launch_cast_rays(DeviceState& d, const float4* rays, b3gRayHit* hits, int n, cudaStream_t s);
+void launch_set_int(int* p, int v, cudaStream_t s);
 long long launch_joints(DeviceState& d, const b3gConfig& cfg, cudaStream_t s);
 long long launch_joint_masses(const DeviceState& d, int n, float2* out, cudaStream_t s);
 int launch_contacts(DeviceState& d, float friction, cudaStream_t s);

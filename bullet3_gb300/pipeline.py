@@ -531,6 +531,11 @@ class b3GpuRigidBodyPipeline:
         call("b3g_get_launch_count", self._h, C.byref(n))
         return n.value
 
+    def castRaysDevice(self, deviceRays: int, deviceHits: int, numRays: int):
+        """castRays on device buffers (b3g_cast_rays_device): capi.RAY and capi.RAYHIT arrays already
+        on the world's device, given by address; enqueued, not synchronised."""
+        call("b3g_cast_rays_device", self._h, C.c_void_p(deviceRays), C.c_void_p(deviceHits), C.c_int(numRays))
+
     def castRays(self, rays, hitResults=None) -> np.ndarray:
         """b3GpuRigidBodyPipeline::castRays: rays as a capi.RAY array (from, to; from[3] = scene in a
         world of several scenes) or a sequence of (from, to) points; hitResults (capi.RAYHIT, optional)

@@ -258,6 +258,10 @@ b3gStatus b3g_read_joint_order(b3g_handle h, int* order, int capacity, int* batc
  * equal fractions go to the lower body index.  In a world of several scenes a ray sees only the
  * scene (int)from.w.  Rebuilds the broadphase grid from the current poses; synchronises. */
 b3gStatus b3g_cast_rays(b3g_handle h, const void* host_rays, void* host_hits, int n);
+/* The same cast on device buffers (b3gRayInfo / b3gRayHit arrays already on the world's device;
+ * the work b3GpuRaycast::castRays does after its uploads, b3GpuRaycast.cpp:282-366): enqueued on
+ * the world's stream, returns without synchronising. */
+b3gStatus b3g_cast_rays_device(b3g_handle h, const void* device_rays, void* device_hits, int n);
 
 /* ------------------------------------------------------------------ parallel primitives */
 /* The reference's ParallelPrimitives classes (src/Bullet3OpenCL/ParallelPrimitives/), on caller

@@ -95,3 +95,23 @@ def test_rays_see_only_their_scene():
     g, hit = _compare(pl, np_, shapes, rays, body_scene=sc.scene_of)
     assert (sc.scene_of[g["hitBody"][hit]] == rays["from"][hit, 3].astype(int)).all()
     assert hit.mean() > 0.1  # small piles cover part of the ray footprint
+
+
+def test_device_buffers_give_the_host_call_hits():
+    torch = pytest.importorskip("torch")
+    sc = scenes.box_stack(12, 6, 12, seed=5)
+    np_, bp, pl, shapes = load(sc)
+    rng = np.random.Generator(np.random.PCG64(9))
+    rays = np.concatenate([_rays(rng, 3000, (-7, 0, -7), (7, 6, 7), down=True),
+                           _rays(rng, 3000, (-7, 0, -7), (7, 6, 7))])
+    host = pl.castRays(rays)
+    d_rays = torch.from_numpy(rays.view(np.uint8)).cuda()
+    h0 = np.zeros(len(rays), capi.RAYHIT)
+    h0["hitBody"] = -1
+    h0["hitResult2"] = -1
+    d_hits = torch.from_numpy(h0.view(np.uint8)).cuda()
+    torch.cuda.synchronize()
+    pl.castRaysDevice(d_rays.data_ptr(), d_hits.data_ptr(), len(rays))
+    pl.synchronize()
+    dev = d_hits.cpu().numpy().view(capi.RAYHIT)
+    assert np.array_equal(dev.view(np.uint8), host.view(np.uint8))
