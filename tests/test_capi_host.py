@@ -174,3 +174,16 @@ def test_cpp_dropin_header_compiles(tmp_path):
     r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-Wall", "-I", str(Path(ROOT, "include")), str(src)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_broadphase_switch_validation_before_upload():
+    np_ = b3GpuNarrowPhase(b3Config())
+    pl = b3GpuRigidBodyPipeline(np_)
+    for mode in (capi.BROADPHASE_GRID, capi.BROADPHASE_LBVH, capi.BROADPHASE_AUTO):
+        pl.setBroadphase(mode)  # before the upload: recorded in the config, no device work
+    for bad in (-1, 3):
+        with pytest.raises(capi.B3GError) as e:
+            pl.setBroadphase(bad)
+        assert e.value.status == 1
+    with pytest.raises(capi.B3GError):
+        capi.call("b3g_cast_rays_device", np_.world.handle, C.c_void_p(None), C.c_void_p(None), C.c_int(4))
