@@ -127,3 +127,19 @@ def test_lbvh_equals_grid_at_scale_every_step():
         assert len(grid) > 100000 and np.array_equal(lbvh, grid), step
         pl.stepSimulation(1 / 60)
     assert pl.status() == 0
+
+
+def test_million_body_pour_grid_and_lbvh_agree():
+    # the 1,048,576-body pour (five static planes, mixed shapes, heights U[0, 512]): after 240 steps
+    # of the pour the two pair searches, built independently, give the same pair list on 3 steps
+    sc = scenes.stress_container(1048576, seed=0)
+    np_, bp, pl, shapes = load(sc, use_cuda_graph=True)
+    for _ in range(240):
+        pl.stepSimulation(1 / 60)
+    for step in range(3):
+        grid, _ = _pairs(np_, bp, pl, capi.BROADPHASE_GRID)
+        lbvh, _ = _pairs(np_, bp, pl, capi.BROADPHASE_LBVH)
+        assert len(grid) > 100000 and np.array_equal(lbvh, grid), step
+        pl.setBroadphase(capi.BROADPHASE_GRID)
+        pl.stepSimulation(1 / 60)
+    assert pl.status() == 0
