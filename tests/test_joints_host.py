@@ -95,3 +95,59 @@ def test_oracle_batches_are_legal_and_greedy():
     j2["rbB"] = [x["b"] for x in sc2.joints]
     _, off2 = O.joint_batches(j2, b2)
     assert len(off2) - 1 == 2  # a chain is 2-colourable
+
+
+def _two_bodies(inv_mass_b, vel_b, pos_b=(0.0, 0.0, 0.0)):
+    b = np.zeros(2, O.BODY)
+    b["quat"][:, 3] = 1.0
+    b["pos"][1, :3] = pos_b
+    b["invMass"] = [0.0, inv_mass_b]
+    b["linVel"][1, :3] = vel_b
+    I = np.zeros(2, O.INERTIA)
+    for r in range(3):
+        I["invInertiaWorld"][1, r, r] = inv_mass_b  # a unit-inertia-like body
+    return b, I
+
+
+def _joint(kind, threshold=1e30, pivot_a=(0, 0, 0), pivot_b=(0, 0, 0)):
+    j = np.zeros(1, O.JOINT)
+    j["type"] = kind
+    j["rbA"], j["rbB"] = 0, 1
+    j["pivotInA"][0, :3] = pivot_a
+    j["pivotInB"][0, :3] = pivot_b
+    j["relTargetAB"][0] = (0, 0, 0, 1)
+    j["breakingImpulseThreshold"] = threshold
+    j["flags"] = 1
+    return j
+
+
+@pytest.mark.parametrize("inv_mass", [1.0, 0.5, 0.25])
+@pytest.mark.parametrize("kind", [capi.JOINT_POINT2POINT, capi.JOINT_FIXED])
+def test_oracle_joint_cancels_the_velocity_of_a_hanging_body(inv_mass, kind):
+    # pivots coincide at the body's centre: no positional error, so the stage drives the velocity
+    # along every row to zero (power-of-two masses keep every product exact)
+    b, I = _two_bodies(inv_mass, (0.0, -9.8 / 60, 0.0))
+    nb, nj = O.solve_joints(b, I, _joint(kind))
+    assert np.array_equal(nb["linVel"][1, :3], np.zeros(3, np.float32))
+    assert np.array_equal(nb["linVel"][0], b["linVel"][0])  # the static anchor is untouched
+    assert nj["flags"][0] == 1
+
+
+def test_oracle_joint_breaks_above_its_threshold():
+    # the impulse that stops the body is m |v| = 0.163 > 0.1: the joint breaks in its first stage,
+    # and a disabled joint is not solved any more
+    b, I = _two_bodies(1.0, (0.0, -9.8 / 60, 0.0))
+    nb, nj = O.solve_joints(b, I, _joint(capi.JOINT_POINT2POINT, threshold=0.1))
+    assert nj["flags"][0] == 0
+    # its rows were clamped at the threshold: the velocity change is exactly the threshold impulse
+    assert np.isclose(nb["linVel"][1, 1] - b["linVel"][1, 1], 0.1, rtol=1e-6)
+    nb2, nj2 = O.solve_joints(nb, I, nj)
+    assert np.array_equal(nb2["linVel"], nb["linVel"]) and nj2["flags"][0] == 0
+
+
+def test_oracle_joint_pulls_a_displaced_pivot_back():
+    # body B's pivot sits 0.1 below the anchor's: the rows ask for a velocity of erp/dt x error
+    b, I = _two_bodies(1.0, (0.0, 0.0, 0.0), pos_b=(0.0, -0.1, 0.0))
+    nb, _ = O.solve_joints(b, I, _joint(capi.JOINT_POINT2POINT))
+    assert np.isclose(nb["linVel"][1, 1], 0.2 * 60 * 0.1, rtol=1e-5)
+    assert np.allclose(nb["linVel"][1, [0, 2]], 0.0)
