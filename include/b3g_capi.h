@@ -242,7 +242,9 @@ b3gStatus b3g_create_fixed_constraint(b3g_handle h, int body_a, int body_b, cons
 b3gStatus b3g_remove_constraint(b3g_handle h, int uid);
 b3gStatus b3g_get_num_constraints(b3g_handle h, int* n);
 /* the joints (b3gJoint == b3GpuGenericConstraint, flags as the device last left them) and the
- * order the solver sweeps them in: joint indices batch by batch, batch_offsets[num_batches + 1] */
+ * order the solver sweeps them in: joint indices batch by batch, batch_offsets[num_batches + 1]
+ * (the order of the last joint solve: B3G_ERR_INVALID_ARG while a change to the joint list has
+ * not been solved yet; order or batch_offsets may be NULL to query sizes) */
 b3gStatus b3g_read_constraints(b3g_handle h, void* host_joints, int capacity, int* n);
 b3gStatus b3g_read_joint_order(b3g_handle h, int* order, int capacity, int* batch_offsets, int offsets_capacity,
                                int* num_batches);
