@@ -182,11 +182,13 @@ def measured_peaks():
 
 
 def solver_traffic():
+    """DRAM bytes per manifold of the solve stage's kernels from a committed ncu capture (ncu cannot
+    run inside this measurement): the file names the command, workload and launch shapes of the
+    capture, which the roofline object repeats beside the scaled figure."""
     p = ROOT / "profiles" / "solver_traffic.json"
     if p.exists():
         try:
-            d = json.loads(p.read_text())
-            return d
+            return json.loads(p.read_text())
         except Exception:
             return None
     return None
@@ -217,13 +219,33 @@ def workload_name(args, scene):
 
 
 # ------------------------------------------------------------------------------ CPU arm
-def cpu_run(scene, steps, iterations, mode):
-    """Times `steps` composed oracle steps on the scene; returns (seconds, threads, bodies)."""
-    from bullet3_gb300 import scenes
-    from bullet3_gb300.pipeline import b3Config
+CPU_KIND = ("the oracle's composed step (the reference CPU algorithms, pinned bit for bit to the compiled "
+            "reference; exact pair set from a uniform-grid search, which is the set the reference's dynamic-BVH "
+            "broadphase gives after its tight AABB test) with OpenMP over bodies and pairs, {threads} threads; "
+            "the PGS sweep is sequential, as in the reference; the reference's own CPU pipeline is single-threaded")
+
+
+def bench_config(args, scene, world: int = 1) -> dict:
+    """The configuration both arms report (identical keys and values for the same workload)."""
+    return {"workload": workload_name(args, scene), "bodies": int(scene.num_bodies), "solver": args.solver,
+            "iterations": args.iterations, "row_order": args.row_order,
+            "parallelism": (f"{world} ranks, own scene set each (seed = rank)"
+                            if world > 1 and args.workload == "batched"
+                            else f"replicas x{world}" if world > 1 else "single GPU"),
+            "l2": "inputs larger than L2 (constraint rows and pair buffers exceed 129 MB)"}
+
+
+def cpu_tables(scene):
+    """The scene's shape, body and inertia tables, registered by the oracle's restatement of the
+    reference's registration (oracle/b3hull.c): the CPU legs load nothing of the product."""
     from oracle import oracle as O
-    np_, bp, pl = scenes.load_scene(scene, b3Config(), upload=False)
-    t = scenes.registered_tables(np_)
+    return O.register_scene(scene)
+
+
+def cpu_run(scene, tables, steps, iterations, mode):
+    """Times `steps` composed oracle steps on the scene; returns (seconds, threads, bodies)."""
+    from oracle import oracle as O
+    t = tables
     shapes = O.Shapes.from_tables(t)
     threads = O.max_threads()
     b, I = t["bodies"], t["inertias"]
@@ -260,20 +282,21 @@ def reference_arm(args):
         return 0
     scene = make_scene(args)
     mode = solver_mode_code(args)
+    tables = cpu_tables(scene)
     # warm-up steps are run (untimed) from the same initial state; each timed step is one full
     # composed CPU step of the whole 262,144-body scene
     # (the million-body pour is sampled: at most 3 timed CPU steps, as its CPU baseline is)
     steps = args.steps if args.workload != "stress" else min(args.steps, 3)
-    cpu_run(scene, args.warmup, args.iterations, mode) if args.warmup else None
-    secs, threads, n = cpu_run(scene, steps, args.iterations, mode)
+    cpu_run(scene, tables, args.warmup, args.iterations, mode) if args.warmup else None
+    secs, threads, n = cpu_run(scene, tables, steps, args.iterations, mode)
     value = n * steps / secs
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": args.gpus,
             "steps": steps, "warmup": args.warmup, "ms_per_step": 1000 * secs / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": workload_name(args, scene), "bodies": n, "solver": args.solver,
-                       "iterations": args.iterations, "row_order": args.row_order},
+            "config": bench_config(args, scene, world),
             "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": threads, "kind": "port",
-                             "sample": f"{steps} composed CPU steps of the full {n}-body scene"},
+                             "sample": f"{steps} composed CPU steps of the full {n}-body scene: "
+                                       + CPU_KIND.format(threads=threads)},
             "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -446,7 +469,12 @@ def gpu_arm(args):
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_kind": peak_kind, "algorithmic_bytes": solve_bytes,
                 "traffic": (traffic["bytes_per_manifold"] * C_ if traffic and "bytes_per_manifold" in traffic
-                            else None)}
+                            else None),
+                "traffic_source": ((f"not measured in this run: ncu dram__bytes_read.sum + dram__bytes_write.sum of "
+                                    f"{', '.join(traffic.get('kernels', []))} per manifold from profiles/"
+                                    f"solver_traffic.json ({traffic.get('workload', '')}; "
+                                    f"{traffic.get('launch', 'launch shapes as captured')}), times this run's "
+                                    f"{C_} manifolds") if traffic else None)}
     stages = {k: {"ms": float(v), "algorithmic_GBps": stage_bytes[k] / (v / 1000.0) / 1e9 if v > 0 else None,
                   "frac_of_hbm": (stage_bytes[k] / (v / 1000.0) / 1e9 / peak) if v > 0 else None}
               for k, v in stage_ms.items()}
@@ -478,10 +506,11 @@ def gpu_arm(args):
     # ---- CPU baseline: the oracle's composed step on the same scene, bounded sample
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        secs, threads, n = cpu_run(scene, args.cpu_steps, args.iterations, solver_mode_code(args))
+        secs, threads, n = cpu_run(scene, cpu_tables(scene), args.cpu_steps, args.iterations, solver_mode_code(args))
         what = (f"every one of the {args.scenes} scenes" if args.workload == "batched" else "the same scene")
         cpu = {"value": n * args.cpu_steps / secs, "unit": "body-steps/s", "cores": threads, "kind": "port",
-               "sample": f"{args.cpu_steps} composed CPU oracle steps of {what} ({n} bodies) from its initial state"}
+               "sample": f"{args.cpu_steps} composed CPU steps of {what} ({n} bodies) from its initial state: "
+                         + CPU_KIND.format(threads=threads)}
 
     # ---- learned vs plain: sweeps and ms per step to the residual target (rank 0, one GPU)
     residual = None
@@ -493,15 +522,9 @@ def gpu_arm(args):
         line = {"metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world, "steps": args.steps,
                 "warmup": max(3, args.warmup), "ms_per_step": 1000 * t_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": workload_name(args, scene), "bodies": N, "solver": args.solver,
-                           "iterations": args.iterations,
-                           "row_order": args.row_order,
-                           "parallelism": (f"{world} ranks, own scene set each (seed = rank)"
-                                           if world > 1 and args.workload == "batched"
-                                           else f"replicas x{world}" if world > 1 else "single GPU"),
-                           "l2": "inputs larger than L2 (constraint rows and pair buffers exceed 129 MB)",
-                           "pairs": P_, "manifolds": C_, "contact_points": st.num_points, "colors": st.num_colors,
-                           "tuning": tuning},
+                "config": bench_config(args, scene, world),
+                "workload_stats": {"pairs": P_, "manifolds": C_, "contact_points": st.num_points,
+                                   "colors": st.num_colors, "tuning": tuning},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
                 "clocks": clk, "stages": stages, "device_status": int(status), "to_residual": residual}
         print(json.dumps(line), flush=True)

@@ -1,4 +1,4 @@
-"""In-tree build of the CUDA library (libb3gpu.so) and of the CPU oracle (oracle/liboracle.so).
+"""In-tree build of the CUDA library (libb3gpu.so).
 
 The CUDA translation units are compiled for sm_103a only, in parallel, with --fmad=false so the
 physics kernels follow the same IEEE operation sequence as the oracle.  Rebuilds only when a
@@ -17,8 +17,6 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libb3gpu.so"
-ORACLE_DIR = ROOT / "oracle"
-ORACLE_LIB = ORACLE_DIR / "liboracle.so"
 
 CU_SOURCES = ["primitives.cu", "broadphase.cu", "narrowphase.cu", "solver.cu", "integrate.cu", "world.cu",
               "noalloc.cu", "mlp.cu", "warmstart.cu", "primitives_capi.cu", "raycast.cu", "joints.cu"]
@@ -79,33 +77,5 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
     return LIB
 
 
-def build_oracle(force: bool = False) -> Path:
-    src = ORACLE_DIR / "b3oracle.c"
-    hdr = ORACLE_DIR / "b3oracle.h"
-    if not force and not _newer(ORACLE_LIB, [src, hdr]):
-        return ORACLE_LIB
-    tmp = ORACLE_LIB.with_suffix(".so.tmp")
-    base = ["gcc", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-shared", "-o", str(tmp), str(src), "-lm"]
-    try:
-        _run(base[:1] + ["-fopenmp"] + base[1:])
-    except RuntimeError:
-        _run(base)
-    os.replace(tmp, ORACLE_LIB)
-    return ORACLE_LIB
-
-
-def build_reference(ref_root: str = "/root/reference") -> Path | None:
-    """oracle/_ref/libb3ref.so from the reference sources, when they are present on this machine."""
-    if not Path(ref_root, "src", "Bullet3Common").is_dir():
-        return None
-    out = ORACLE_DIR / "_ref" / "libb3ref.so"
-    if out.exists() and out.stat().st_mtime > (ORACLE_DIR / "ref_shim.cpp").stat().st_mtime:
-        return out
-    _run(["bash", str(ORACLE_DIR / "build_ref.sh"), ref_root])
-    return out
-
-
 if __name__ == "__main__":
     print(build_library(verbose=True))
-    print(build_oracle())
-    print(build_reference())

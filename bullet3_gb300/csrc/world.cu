@@ -1279,15 +1279,37 @@ extern "C" b3gStatus b3g_autotune(b3g_handle h, float dt, int repeats, b3gTuning
 }
 
 // ---------------------------------------------------------------------------------- ray casts
-static b3gStatus ray_buffers(b3gWorld* h, int n) {
+// Frees a buffer that dalloc made, after the stream has drained (work in flight may still read it).
+template <typename T>
+static void dfree(b3gWorld* w, T** p) {
+    if (!*p) return;
+    cudaStreamSynchronize(w->stream);
+    auto it = std::find(w->allocations.begin(), w->allocations.end(), static_cast<void*>(*p));
+    if (it != w->allocations.end()) {
+        cudaFree(*p);
+        w->allocations.erase(it);
+    }
+    *p = nullptr;
+}
+
+// Ray-cast scratch: the sort keys for every call; device copies of the rays and hits only for
+// calls with host buffers (b3g_cast_rays).  Growth frees the smaller buffers.
+static b3gStatus ray_buffers(b3gWorld* h, int n, bool host_copies) {
     DeviceState& d = h->d;
-    if (n <= d.ray_cap) return B3G_OK;
-    const int cap = std::max(n, 2 * d.ray_cap);
-    TRY(dalloc(h, &d.ray_buf, 2 * (size_t)cap));
-    TRY(dalloc(h, &d.hit_buf, (size_t)cap));
-    TRY(dalloc(h, &d.ray_order, 4 * (size_t)cap));
+    if (n > d.ray_cap) {
+        const int cap = std::max(n, 2 * d.ray_cap);
+        dfree(h, &d.ray_order);
+        TRY(dalloc(h, &d.ray_order, 4 * (size_t)cap));
+        d.ray_cap = cap;
+    }
+    if (host_copies && d.ray_host_cap < n) {
+        dfree(h, &d.ray_buf);
+        dfree(h, &d.hit_buf);
+        TRY(dalloc(h, &d.ray_buf, 2 * (size_t)d.ray_cap));
+        TRY(dalloc(h, &d.hit_buf, (size_t)d.ray_cap));
+        d.ray_host_cap = d.ray_cap;
+    }
     if (!d.ray_n) TRY(dalloc(h, &d.ray_n, 1));
-    d.ray_cap = cap;
     return B3G_OK;
 }
 
@@ -1297,7 +1319,7 @@ extern "C" b3gStatus b3g_cast_rays_device(b3g_handle h, const void* device_rays,
     if ((reinterpret_cast<uintptr_t>(device_rays) | reinterpret_cast<uintptr_t>(device_hits)) & 15u)
         return fail(B3G_ERR_INVALID_ARG, "ray and hit buffers must be 16-byte aligned");
     CUDA_TRY(cudaSetDevice(h->device));
-    TRY(ray_buffers(h, n));
+    TRY(ray_buffers(h, n, false));
     DeviceState& d = h->d;
     if (n > 0) {
         // the sort length, written by a kernel so that the call stays asynchronous
@@ -1314,7 +1336,7 @@ extern "C" b3gStatus b3g_cast_rays(b3g_handle h, const void* host_rays, void* ho
     if (n < 0 || (n > 0 && (!host_rays || !host_hits))) return fail(B3G_ERR_INVALID_ARG, "invalid ray arguments");
     CUDA_TRY(cudaSetDevice(h->device));
     DeviceState& d = h->d;
-    TRY(ray_buffers(h, n));
+    TRY(ray_buffers(h, n, true));
     cudaStream_t s = h->stream;
     if (n > 0) {
         CUDA_TRY(cudaMemcpyAsync(d.ray_buf, host_rays, sizeof(b3gRayInfo) * (size_t)n, cudaMemcpyHostToDevice, s));

@@ -83,7 +83,8 @@ struct DeviceState {
     LaunchTuning tune;
     float4* ray_buf = nullptr;    // b3g_cast_rays: rays (2 float4 each) and hits, grown on demand
     b3gRayHit* hit_buf = nullptr;
-    int ray_cap = 0;
+    int ray_cap = 0;              // capacity of ray_order (rays per call)
+    int ray_host_cap = 0;         // capacity of ray_buf / hit_buf (host-buffer calls only)
     uint32_t* ray_order = nullptr;  // 4 * ray_cap: Morton keys and ray indices, ping-pong for the sort
     int* ray_n = nullptr;           // device copy of the ray count (sort length)
     // LBVH broadphase (b3gConfig.broadphase = B3G_BROADPHASE_LBVH; own allocations): the dynamic

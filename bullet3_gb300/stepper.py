@@ -8,7 +8,7 @@ scene upload, the warm-up steps and the measured steps touch the GPU.
                                     [--autotune] [--broadphase grid|lbvh] [--stage-times] [--profile-range]
 
 --profile-range brackets the K measured steps with b3g_profiler_range, for a profiler started
-with profiling off (ncu --profile-from-start off); --settle steps first, untimed.
+with profiling off (ncu --profile-from-start off --clock-control none); --settle steps first, untimed.
 
   pile     262,144 unit boxes resting in 64x64 columns on a plane (the settled 64^3 lattice)
   lattice  the 64^3 lattice (spacing 1.1, jitter 0.05) falling onto the plane from rest

@@ -434,7 +434,9 @@ b3gStatus b3g_read_warm_start(b3g_handle h, float* host, int capacity_manifolds,
  *                returns without waiting for it.
  * Larger sizes are rejected with B3G_ERR_CAPACITY before anything is enqueued.  The first call
  * on a device looks up the scratch array's address (cudaGetSymbolAddress) and the SM count: make
- * it before any stream capture.  No scratch content has to start at zero: each call resets the
+ * it before any stream capture.  Both are cached per device index for the life of the process; a
+ * cudaDeviceReset (or any other teardown of the device's primary context) leaves the cached
+ * address stale, so do not call this entry point on a device after resetting it.  No scratch content has to start at zero: each call resets the
  * counters it uses in its first kernel and validates the never-cleared cell table on use.  All
  * calls on one device share the one scratch array, so calls whose work overlaps in time (two
  * streams, or two host threads) race: serialise them on one stream or with events. */

@@ -149,6 +149,18 @@ void oracle_solve_joints(obody* bodies, const oinertia* inertias, int nbodies, o
 /* The acos the joint rows use (asin Maclaurin series with half-angle reduction). */
 float oracle_joint_acos(float x);
 
+/* Shape and body registration (oracle/b3hull.c).  oracle_hull: the hull tables
+ * registerConvexHullShape builds from a point cloud (b3ConvexHullComputer + b3ConvexUtility +
+ * vertex-mean local centre): vertices xyz, face planes xyzw, face index counts and indices, unique
+ * edge directions xyz.  counts4 in: capacities (vertices, faces, indices, edges); out: sizes.
+ * Returns 0, 1 when a buffer is too small, -1 on allocation failure. */
+int oracle_hull(const float* xyz, int n, float* verts_out, float* planes_out, int* face_counts_out,
+                int* indices_out, float* edges_out, float* center_out, int* counts4);
+/* registerPhysicsInstance + registerRigidBody: the body record (b3RigidBodyData, 20 floats) and
+ * the inertia record (b3InertiaData, 24 floats) for a body of the given shape's local AABB. */
+int oracle_register_body(float mass, const float pos[3], const float orn[4], int collidable, const float local_min[3],
+                         const float local_max[3], float* body_out, float* inertia_out);
+
 #ifdef __cplusplus
 }
 #endif

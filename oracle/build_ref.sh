@@ -3,12 +3,16 @@
 # is copied into this repository), plus oracle/ref_shim.cpp.  Test infrastructure only: the
 # library generates the golden vectors under tests/golden/ and pins the plain-C oracle.
 #
-# Usage: oracle/build_ref.sh [reference_root]   (default: /root/reference)
+# Usage: oracle/build_ref.sh <reference_root>   (or set B3G_REFERENCE_ROOT)
 # Needs only g++; does not run the reference's own build system.  The OpenCL host files are
 # compiled with -DB3_USE_CLEW against the vendored clew loader; no OpenCL runtime is needed
 # because only the CPU entry points are called.
 set -euo pipefail
-REF=${1:-/root/reference}
+REF=${1:-${B3G_REFERENCE_ROOT:-}}
+if [ -z "$REF" ]; then
+  echo "usage: $0 <reference_root> (or set B3G_REFERENCE_ROOT)" >&2
+  exit 2
+fi
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 SRC="$REF/src"

@@ -50,10 +50,8 @@ def load_oracle():
     if _ORACLE is None:
         p = HERE / "liboracle.so"
         if not p.exists():
-            import sys
-            sys.path.insert(0, str(HERE.parent))
-            from bullet3_gb300 import _build
-            _build.build_oracle()
+            from oracle import build as _b
+            _b.build_oracle()
         _ORACLE = C.CDLL(str(p))
         _ORACLE.oracle_solve.restype = C.c_int
     return _ORACLE
@@ -360,3 +358,146 @@ def ref_integrate(bodies, dt=1 / 60, damping=0.99, gravity=(0.0, -9.8, 0.0)):
     g = (C.c_float * 3)(*gravity)
     lib.ref_integrate(_p(b), C.c_int(len(b)), C.c_float(dt), C.c_float(damping), g)
     return b
+
+
+def ref_register_body(mass, pos, orn, collidable, local_min, local_max):
+    """The reference's body and inertia records for one registerPhysicsInstance call."""
+    lib = load_reference()
+    b = np.zeros(1, BODY)
+    inr = np.zeros(1, INERTIA)
+    p = np.ascontiguousarray(pos, np.float32)[:3]
+    q = np.ascontiguousarray(orn, np.float32)[:4]
+    lo = np.ascontiguousarray(local_min, np.float32)[:3]
+    hi = np.ascontiguousarray(local_max, np.float32)[:3]
+    lib.ref_register_body(C.c_float(mass), _p(p), _p(q), C.c_int(collidable), _p(lo), _p(hi), _p(b), _p(inr))
+    return b[0], inr[0]
+
+
+# ------------------------------------------------------------------ registration (oracle/b3hull.c)
+def hull(points, scaling=(1.0, 1.0, 1.0)):
+    """Hull tables of registerConvexHullShape: (vertices (n,3), planes (f,4), face_counts (f,),
+    indices, unique edges (e,3), local centre (3,))."""
+    lib = load_oracle()
+    pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    # registerConvexHullShape scales every input vertex first (b3GpuNarrowPhase.cpp:302-307)
+    pts = (pts * np.asarray(scaling, np.float32)).astype(np.float32)
+    cap = max(64, 8 * len(pts))
+    v = np.zeros((cap, 3), np.float32)
+    pl = np.zeros((cap, 4), np.float32)
+    fc = np.zeros(cap, np.int32)
+    ix = np.zeros(8 * cap, np.int32)
+    e = np.zeros((cap, 3), np.float32)
+    c = np.zeros(3, np.float32)
+    counts = np.array([cap, cap, 8 * cap, cap], np.int32)
+    r = lib.oracle_hull(_p(pts), C.c_int(len(pts)), _p(v), _p(pl), _p(fc), _p(ix), _p(e), _p(c), _p(counts))
+    if r != 0:
+        raise RuntimeError(f"oracle_hull failed ({r})")
+    nv, nf, ni, ne = (int(x) for x in counts)
+    return v[:nv].copy(), pl[:nf].copy(), fc[:nf].copy(), ix[:ni].copy(), e[:ne].copy(), c
+
+
+class Registry:
+    """Shape and body tables in the device layout, registered the way b3GpuNarrowPhase and
+    b3GpuRigidBodyPipeline register them (hull tables from oracle_hull, bodies and inertias from
+    oracle_register_body).  Used by the CPU legs to build their scene without the product."""
+
+    def __init__(self):
+        self.cols, self.laabbs, self.hull_recs, self.faces = [], [], [], []
+        self.indices, self.verts, self.edges = [], [], []
+        self.bodies, self.inertias = [], []
+
+    def plane(self, normal, constant):
+        f = np.zeros(1, FACE)[0]
+        f["plane"] = [normal[0], normal[1], normal[2], constant]
+        self.faces.append(f)
+        col = np.zeros(1, COLLIDABLE)[0]
+        col["radius"], col["shapeType"], col["shapeIndex"] = constant, 4, len(self.faces) - 1
+        a = np.zeros(1, AABB)[0]
+        a["min"], a["max"] = -1e30, 1e30
+        self.cols.append(col)
+        self.laabbs.append(a)
+        return len(self.cols) - 1
+
+    def sphere(self, radius):
+        col = np.zeros(1, COLLIDABLE)[0]
+        col["radius"], col["shapeType"], col["shapeIndex"] = radius, 7, 0
+        a = np.zeros(1, AABB)[0]
+        a["min"], a["max"] = -np.float32(radius), np.float32(radius)
+        self.cols.append(col)
+        self.laabbs.append(a)
+        return len(self.cols) - 1
+
+    def convex_hull(self, points, scaling=(1.0, 1.0, 1.0)):
+        v, pl, fc, ix, e, c = hull(points, scaling)
+        h = np.zeros(1, HULL)[0]
+        h["localCenter"][:3] = c
+        h["uniqueEdgesOffset"], h["numUniqueEdges"] = len(self.edges), len(e)
+        self.edges.extend(np.concatenate([e, np.zeros((len(e), 1), np.float32)], 1))
+        h["faceOffset"], h["numFaces"] = len(self.faces), len(fc)
+        off = 0
+        for k in range(len(fc)):
+            f = np.zeros(1, FACE)[0]
+            f["plane"] = pl[k]
+            f["indexOffset"], f["numIndices"] = len(self.indices), fc[k]
+            self.indices.extend(ix[off:off + fc[k]].tolist())
+            off += fc[k]
+            self.faces.append(f)
+        h["vertexOffset"], h["numVertices"] = len(self.verts), len(v)
+        self.verts.extend(np.concatenate([v, np.zeros((len(v), 1), np.float32)], 1))
+        self.hull_recs.append(h)
+        col = np.zeros(1, COLLIDABLE)[0]
+        col["shapeType"], col["shapeIndex"] = 3, len(self.hull_recs) - 1
+        a = np.zeros(1, AABB)[0]
+        a["min"], a["max"] = v.min(0), v.max(0)  # b3Vector3::setMin / setMax over the hull vertices
+        self.cols.append(col)
+        self.laabbs.append(a)
+        return len(self.cols) - 1
+
+    def body(self, mass, pos, orn, collidable):
+        lib = load_oracle()
+        b = np.zeros(1, BODY)
+        inr = np.zeros(1, INERTIA)
+        la = self.laabbs[collidable]
+        lo = np.ascontiguousarray(la["min"], np.float32)
+        hi = np.ascontiguousarray(la["max"], np.float32)
+        p = np.ascontiguousarray(pos, np.float32)[:3]
+        q = np.ascontiguousarray(orn, np.float32)[:4]
+        lib.oracle_register_body(C.c_float(mass), _p(p), _p(q), C.c_int(collidable), _p(lo), _p(hi), _p(b), _p(inr))
+        self.bodies.append(b[0])
+        self.inertias.append(inr[0])
+        return len(self.bodies) - 1
+
+    def tables(self) -> dict:
+        def arr(x, dt):
+            return np.array(x, dt) if len(x) else np.zeros(1, dt)
+        return {"collidables": arr(self.cols, COLLIDABLE), "local_aabbs": arr(self.laabbs, AABB),
+                "hulls": arr(self.hull_recs, HULL), "faces": arr(self.faces, FACE),
+                "indices": np.array(self.indices or [0], np.int32),
+                "verts": np.array(self.verts, np.float32).reshape(-1, 4) if self.verts else np.zeros((1, 4), np.float32),
+                "edges": np.array(self.edges, np.float32).reshape(-1, 4) if self.edges else np.zeros((1, 4), np.float32),
+                "bodies": np.array(self.bodies, BODY), "inertias": np.array(self.inertias, INERTIA)}
+
+
+def register_scene(scene) -> dict:
+    """Tables of a synthetic scene (shapes: dicts of type hull / sphere / plane; per body its shape,
+    mass, position, orientation and optional velocities), registered in scene order.  Same
+    dictionary keys as the product's registered tables."""
+    reg = Registry()
+    col = []
+    for s in scene.shapes:
+        if s["type"] == "hull":
+            col.append(reg.convex_hull(s["verts"]))
+        elif s["type"] == "sphere":
+            col.append(reg.sphere(s["radius"]))
+        elif s["type"] == "plane":
+            col.append(reg.plane(s["normal"], s["constant"]))
+        else:
+            raise ValueError(s["type"])
+    for i in range(len(scene.mass)):
+        reg.body(float(scene.mass[i]), scene.pos[i], scene.orn[i], col[scene.body_shape[i]])
+    t = reg.tables()
+    if getattr(scene, "linvel", None) is not None:
+        t["bodies"]["linVel"][:, :3] = scene.linvel
+    if getattr(scene, "angvel", None) is not None:
+        t["bodies"]["angVel"][:, :3] = scene.angvel
+    return t

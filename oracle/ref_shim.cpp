@@ -11,6 +11,7 @@
 //   computeContactPlaneConvex / SphereConvex        Bullet3OpenCL/NarrowphaseCollision/b3ConvexHullContact.cpp:1272, :2323
 //   b3PgsJacobiSolver::solveGroup                   Bullet3Dynamics/ConstraintSolver/b3PgsJacobiSolver.cpp:170
 //   integrateSingleTransform                        Bullet3Dynamics/shared/b3IntegrateTransforms.h:5
+//   registerPhysicsInstance / registerRigidBody     Bullet3OpenCL/RigidBody/b3GpuRigidBodyPipeline.cpp:603, b3GpuNarrowPhase.cpp:816
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -20,6 +21,7 @@
 #include "Bullet3Common/b3Quaternion.h"
 #include "Bullet3Common/b3Matrix3x3.h"
 #include "Bullet3Common/b3Transform.h"
+#include "Bullet3Geometry/b3AabbUtil.h"
 #include "Bullet3Common/shared/b3Int4.h"
 #include "Bullet3Collision/BroadPhaseCollision/shared/b3Aabb.h"
 #include "Bullet3Collision/BroadPhaseCollision/b3DynamicBvhBroadphase.h"
@@ -196,6 +198,56 @@ void ref_solve(b3RigidBodyData* bodies, b3InertiaData* inertias, int nbodies, co
 void ref_integrate(b3RigidBodyData* bodies, int n, float dt, float damping, const float* g) {
     b3Float4 grav = b3MakeFloat4(g[0], g[1], g[2], 0.f);
     for (int i = 0; i < n; i++) integrateSingleTransform(bodies, i, dt, damping, grav);
+}
+
+// registerPhysicsInstance (b3GpuRigidBodyPipeline.cpp:603-625: the world AABB through the
+// reference's own b3TransformAabb with margin 0.01) followed by the record-filling lines of
+// b3GpuNarrowPhase::registerRigidBody (b3GpuNarrowPhase.cpp:830-901), in the reference's types:
+// b3RigidBodyData and b3InertiaData of one body.  (registerRigidBody itself needs an OpenCL
+// context; its arithmetic is these lines.)
+void ref_register_body(float mass, const float* position, const float* orientation, int collidableIndex,
+                       const float* localMin, const float* localMax, b3RigidBodyData* body, b3InertiaData* inertia) {
+    b3Vector3 localAabbMin = b3MakeVector3(localMin[0], localMin[1], localMin[2]);
+    b3Vector3 localAabbMax = b3MakeVector3(localMax[0], localMax[1], localMax[2]);
+    b3Vector3 aabbMin, aabbMax;
+    b3Scalar margin = 0.01f;
+    b3Transform t;
+    t.setIdentity();
+    t.setOrigin(b3MakeVector3(position[0], position[1], position[2]));
+    t.setRotation(b3Quaternion(orientation[0], orientation[1], orientation[2], orientation[3]));
+    b3TransformAabb(localAabbMin, localAabbMax, margin, t, aabbMin, aabbMax);
+
+    memset(body, 0, sizeof(*body));
+    body->m_frictionCoeff = 1.f;
+    body->m_restituitionCoeff = 0.f;
+    body->m_angVel = b3MakeVector3(0, 0, 0);
+    body->m_linVel = b3MakeVector3(0, 0, 0);
+    body->m_pos = b3MakeVector3(position[0], position[1], position[2]);
+    body->m_quat.setValue(orientation[0], orientation[1], orientation[2], orientation[3]);
+    body->m_collidableIdx = collidableIndex;
+    body->m_invMass = mass ? 1.f / mass : 0.f;
+    memset(inertia, 0, sizeof(*inertia));
+    if (mass == 0.f) {
+        inertia->m_initInvInertia.setValue(0, 0, 0, 0, 0, 0, 0, 0, 0);
+        inertia->m_invInertiaWorld.setValue(0, 0, 0, 0, 0, 0, 0, 0, 0);
+    } else {
+        b3Vector3 halfExtents = (aabbMax - aabbMin);
+        b3Vector3 localInertia;
+        float lx = 2.f * halfExtents[0];
+        float ly = 2.f * halfExtents[1];
+        float lz = 2.f * halfExtents[2];
+        localInertia.setValue((mass / 12.0f) * (ly * ly + lz * lz), (mass / 12.0f) * (lx * lx + lz * lz),
+                              (mass / 12.0f) * (lx * lx + ly * ly));
+        b3Vector3 invLocalInertia;
+        invLocalInertia[0] = 1.f / localInertia[0];
+        invLocalInertia[1] = 1.f / localInertia[1];
+        invLocalInertia[2] = 1.f / localInertia[2];
+        invLocalInertia[3] = 0.f;
+        inertia->m_initInvInertia.setValue(invLocalInertia[0], 0, 0, 0, invLocalInertia[1], 0, 0, 0,
+                                           invLocalInertia[2]);
+        b3Matrix3x3 m(body->m_quat);
+        inertia->m_invInertiaWorld = m.scaled(invLocalInertia) * m.transpose();
+    }
 }
 
 int ref_sizeof(int which) {

@@ -19,8 +19,9 @@ def pytest_configure(config):
 def _built():
     """Compile the CUDA library (sm_103a, cross-compiles without a GPU) and the CPU oracle once."""
     from bullet3_gb300 import _build
+    from oracle import build as oracle_build
     _build.build_library()
-    _build.build_oracle()
+    oracle_build.build_oracle()
     yield
 
 

@@ -15,6 +15,12 @@ Fixtures:
                   no reference manifold
   trajectory.npz  3x3x3 pile, 30 composed reference steps with the Jacobi solver (poses per step)
   kat_aabb.npz    the touching-AABB known answer of test/b3DynamicBvhBroadphase/main.cpp:40-69
+  registration.npz  registerConvexHullShape tables of 140 point clouds (Gaussian clouds of the
+                  collision-at-scale mix, boxes, rotated boxes, cylinders, lattice points, sphere
+                  clouds, clouds with repeated points) and registerPhysicsInstance body / inertia
+                  records of 400 bodies (the reference's b3TransformAabb and b3Matrix3x3)
+
+  python tests/golden/make_golden.py [registration]   (no argument: every fixture)
 """
 from __future__ import annotations
 
@@ -251,5 +257,64 @@ def main():
     print("kat pairs", O.ref_pairs_dbvt(a).tolist())
 
 
+def registration_fixture():
+    """registration.npz: hull tables and body records from the reference's registration code."""
+    rng = np.random.Generator(np.random.PCG64(77))
+
+    def rot(q):
+        x, y, z, w = q
+        return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                         [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                         [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+
+    clouds = []
+    for _ in range(50):
+        clouds.append((rng.standard_normal((int(rng.integers(12, 33)), 3)) * 0.4).astype(np.float32))
+    for _ in range(20):
+        clouds.append(box_vertices(rng.uniform(0.2, 0.6, 3)))
+    for _ in range(20):
+        q = rng.standard_normal(4)
+        clouds.append((box_vertices(rng.uniform(0.2, 0.6, 3)) @ rot(q / np.linalg.norm(q)).T).astype(np.float32))
+    for _ in range(15):
+        k = int(rng.integers(6, 24))
+        a = np.linspace(0, 2 * np.pi, k, endpoint=False)
+        ring = np.stack([np.cos(a), np.zeros(k), np.sin(a)], 1)
+        clouds.append((np.concatenate([ring + [0, -0.5, 0], ring + [0, 0.5, 0]]) * rng.uniform(0.2, 1.0)).astype(np.float32))
+    for _ in range(10):
+        g = np.stack(np.meshgrid(*[np.arange(int(rng.integers(2, 4)))] * 3, indexing="ij"), -1).reshape(-1, 3)
+        clouds.append((g * rng.uniform(0.1, 1.0)).astype(np.float32))
+    for _ in range(15):
+        p = rng.standard_normal((int(rng.integers(20, 120)), 3))
+        clouds.append((p / np.linalg.norm(p, axis=1, keepdims=True)).astype(np.float32))
+    for _ in range(10):
+        p = (rng.standard_normal((int(rng.integers(12, 33)), 3)) * 0.4).astype(np.float32)
+        clouds.append(np.concatenate([p, p[:int(rng.integers(1, 6))]]))
+    out = {"count": np.array(len(clouds))}
+    for i, p in enumerate(clouds):
+        v, pl, fc, ix, e = O.ref_hull(p)
+        out[f"in_{i}"], out[f"v_{i}"], out[f"p_{i}"], out[f"fc_{i}"], out[f"ix_{i}"], out[f"e_{i}"] = p, v, pl, fc, ix, e
+    n = 400
+    mass = np.where(rng.uniform(size=n) < 0.1, 0.0, rng.uniform(0.1, 5.0, n)).astype(np.float32)
+    pos = rng.uniform(-100, 100, (n, 3)).astype(np.float32)
+    q = rng.standard_normal((n, 4))
+    q = (q / np.linalg.norm(q, axis=1, keepdims=True)).astype(np.float32)
+    lo = -rng.uniform(0.1, 1.0, (n, 3)).astype(np.float32)
+    hi = rng.uniform(0.1, 1.0, (n, 3)).astype(np.float32)
+    bodies = np.zeros(n, O.BODY)
+    inertias = np.zeros(n, O.INERTIA)
+    for i in range(n):
+        bodies[i], inertias[i] = O.ref_register_body(float(mass[i]), pos[i], q[i], 3, lo[i], hi[i])
+    out.update(body_mass=mass, body_pos=pos, body_orn=q, body_local_min=lo, body_local_max=hi, bodies=bodies,
+               inertias=inertias)
+    np.savez_compressed(OUT / "registration.npz", **out)
+    print("registration", len(clouds), "hulls", n, "bodies")
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "registration":
+        if O.load_reference() is None:
+            raise SystemExit("oracle/_ref/libb3ref.so is missing: run oracle/build_ref.sh first")
+        registration_fixture()
+    else:
+        main()
+        registration_fixture()

@@ -82,51 +82,47 @@ def test_registered_body_matches_reference_registration():
     np.testing.assert_allclose(I["invInertiaWorld"][:, :3], np.diag([expect] * 3), rtol=1e-6, atol=1e-9)
 
 
-def _match_hull(mine, ref):
-    va, pa, fca, ia, ea = mine[:5]
-    vb, pb, fcb, ib, eb = ref
-    assert len(va) == len(vb)
-    d = np.abs(va[:, None, :] - vb[None, :, :]).max(-1)
-    m = d.argmin(1)
-    assert d[np.arange(len(va)), m].max() <= 1e-6 and len(set(m.tolist())) == len(va)
-    return m
-
-
-def test_hull_builder_against_reference_hulls():
-    """Same quantised vertices as b3ConvexHullComputer (bit-exact up to 1e-6), same face partition
-    and planes for unwelded faces; welded near-coplanar faces may take the other triangle's plane
-    (the reference picks by its internal face order), bounded by the 0.999 weld threshold."""
+def test_hull_builder_bitexact_against_reference():
+    """registerConvexHullShape's tables from the product's hull builder equal the reference's bit
+    for bit (same vertex order, faces in the same order with the same planes and start vertices,
+    same unique edges) on 170 point clouds: Gaussian clouds, boxes, rotated boxes, cylinders,
+    lattice points, sphere clouds and clouds with repeated points."""
+    n = 0
+    for name in ("hulls", "registration"):
+        g = load_golden(name)
+        for i in range(int(g["count"])):
+            mine = capi.hull_compute(g[f"in_{i}"])
+            ref = (g[f"v_{i}"], g[f"p_{i}"], g[f"fc_{i}"], g[f"ix_{i}"], g[f"e_{i}"])
+            for a, b in zip(mine[:5], ref):
+                assert a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8)), (name, i)
+            n += 1
+    assert n == 170
+    # boxes: 6 quads, 3 unique edges
     g = load_golden("hulls")
-    exact_faces = tight_planes = all_planes = 0
-    n = int(g["count"])
-    for i in range(n):
-        mine = capi.hull_compute(g[f"in_{i}"])
-        ref = (g[f"v_{i}"], g[f"p_{i}"], g[f"fc_{i}"], g[f"ix_{i}"], g[f"e_{i}"])
-        m = _match_hull(mine, ref)
-        off = 0
-        fa = []
-        for k, c in enumerate(mine[2]):
-            fa.append(frozenset(m[j] for j in mine[3][off:off + c]))
-            off += c
-        off = 0
-        fb = []
-        for c in ref[2]:
-            fb.append(frozenset(ref[3][off:off + c].tolist()))
-            off += c
-        if set(fa) == set(fb):
-            exact_faces += 1
-            for k, f in enumerate(fa):
-                j = fb.index(f)
-                dev = np.abs(mine[1][k] - ref[1][j]).max()
-                assert dev <= 0.05  # a welded face's normal is within the 0.999 weld cone
-                tight_planes += dev <= 1e-5
-                all_planes += 1
-    assert exact_faces >= n - 2
-    assert tight_planes >= 0.9 * all_planes
-    # boxes: identical topology, 6 quads, 3 unique edges
     for i in range(6):
         mine = capi.hull_compute(g[f"in_{i}"])
         assert len(mine[2]) == 6 and (mine[2] == 4).all() and len(mine[4]) == 3
+
+
+def test_body_registration_bitexact_against_reference():
+    """registerPhysicsInstance through the C ABI writes the reference's body and inertia records bit
+    for bit (margin-0.01 world AABB, full-extent AABB-box inertia, frozen world inverse inertia)."""
+    g = load_golden("registration")
+    n = len(g["bodies"])
+    np_ = b3GpuNarrowPhase(b3Config(m_maxConvexBodies=n, m_maxConvexShapes=n))
+    pl = b3GpuRigidBodyPipeline(np_)
+    for i in range(n):
+        lo, hi = g["body_local_min"][i], g["body_local_max"][i]
+        corners = np.array([[x, y, z] for x in (lo[0], hi[0]) for y in (lo[1], hi[1]) for z in (lo[2], hi[2])],
+                           np.float32)
+        # a hull registered from its tables: its local AABB is exactly [lo, hi]
+        col = np_.registerConvexHullShapeTables(corners, np.array([[0, 1, 0, 0]], np.float32), [3], [0, 1, 2],
+                                                np.zeros((0, 3), np.float32))
+        assert pl.registerPhysicsInstance(float(g["body_mass"][i]), g["body_pos"][i], g["body_orn"][i], col, i) == i
+    t = scenes.registered_tables(np_)
+    t["bodies"]["collidableIdx"] = 3
+    assert t["bodies"].tobytes() == g["bodies"].tobytes()
+    assert t["inertias"].tobytes() == g["inertias"].tobytes()
 
 
 def test_scene_offsets_validation():

@@ -3,7 +3,9 @@
 Pins oracle/b3oracle.c (the checker every GPU parity test uses) to the reference:
 b3TransformAabb2, the dynamic-BVH pair set filtered by the tight test, b3ContactConvexConvexSAT,
 computeContactPlaneConvex, computeContactSphereConvex, b3PgsJacobiSolver (PGS and Jacobi) and
-integrateSingleTransform, plus a 30-step composed trajectory.
+integrateSingleTransform, plus a 30-step composed trajectory; and the registration path
+(b3ConvexHullComputer + b3ConvexUtility hull tables, registerPhysicsInstance body and inertia
+records) that the CPU legs use to build their scenes.
 """
 import numpy as np
 import pytest
@@ -105,3 +107,39 @@ def test_composed_trajectory_matches_reference():
         worst = max(worst, float(np.abs(b["pos"] - traj[s]["pos"]).max()))
     # stated tolerance for poses after 30 steps: 1e-4 absolute (transcendentals in the integrator)
     assert worst < 1e-4, worst
+
+
+def _hull_fixtures():
+    for name in ("hulls", "registration"):
+        g = load_golden(name)
+        for i in range(int(g["count"])):
+            yield g[f"in_{i}"], (g[f"v_{i}"], g[f"p_{i}"], g[f"fc_{i}"], g[f"ix_{i}"], g[f"e_{i}"])
+
+
+def test_hull_tables_bitexact():
+    """Vertices, face planes, face polygons (same faces, same order, same start vertex) and unique
+    edges of 170 point clouds equal the reference's bit for bit, welded faces included."""
+    n = 0
+    for pts, ref in _hull_fixtures():
+        mine = O.hull(pts)
+        for a, b in zip(mine[:5], ref):
+            assert a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8))
+        c = np.zeros(3, np.float32)
+        for p in ref[0]:
+            c = (c + p).astype(np.float32)
+        assert np.array_equal(mine[5], (c * np.float32(1.0 / np.float32(len(ref[0])))).astype(np.float32))
+        n += 1
+    assert n == 170
+
+
+def test_body_registration_bitexact():
+    g = load_golden("registration")
+    reg = O.Registry()
+    for i in range(len(g["bodies"])):
+        reg.laabbs.append(np.zeros(1, O.AABB)[0])
+        reg.laabbs[-1]["min"], reg.laabbs[-1]["max"] = g["body_local_min"][i], g["body_local_max"][i]
+        reg.body(float(g["body_mass"][i]), g["body_pos"][i], g["body_orn"][i], len(reg.laabbs) - 1)
+    t = reg.tables()
+    t["bodies"]["collidableIdx"] = 3  # the fixture registers every body with collidable 3
+    assert t["bodies"].tobytes() == g["bodies"].tobytes()
+    assert t["inertias"].tobytes() == g["inertias"].tobytes()

@@ -66,7 +66,7 @@ def test_noalloc_pairs_match_allocating_entry_on_two_calls():
             pl.stepSimulation(1 / 60)
         pl.synchronize()
     assert not np.array_equal(seen[0], seen[1])
-    # overflow: the raw count is reported, the first max_pairs pairs of the sorted order written
+    # overflow: the raw count is reported; max_pairs of the pairs (an unspecified subset) are written, sorted
     pl.setupGpuAabbsFull()
     bp.calculateOverlappingPairs()
     pl.synchronize()
