@@ -65,7 +65,7 @@ class b3gConfig(C.Structure):
                 ("use_cuda_graph", C.c_int), ("warm_start", C.c_int), ("barrier_spin_limit", C.c_int),
                 ("solver_blocks_per_sm", C.c_int), ("pgs_partitions", C.c_int), ("pgs_interleave", C.c_int),
                 ("warm_start_max_points", C.c_int), ("autotune", C.c_int), ("broadphase", C.c_int),
-                ("reserved", C.c_int * 1)]
+                ("pgs_tail_manifolds", C.c_int)]
 
 
 class b3gTuning(C.Structure):
@@ -107,7 +107,8 @@ EXPORTS = [
     "b3g_mlp_set_normalization", "b3g_mlp_get_normalization", "b3g_mlp_predict", "b3g_mlp_set_training_data",
     "b3g_mlp_train", "b3g_mlp_gradients", "b3g_set_warm_start_model", "b3g_read_warm_samples",
     "b3g_read_warm_start", "b3g_radix_sort32", "b3g_radix_sort32_keys", "b3g_prefix_scan32", "b3g_bound_search",
-    "b3g_fill32"]
+    "b3g_fill32", "b3g_reset", "b3g_compute_contacts_for_pairs", "b3g_buffer_alloc", "b3g_buffer_free",
+    "b3g_buffer_copy"]
 
 
 def lib_path() -> Path:

@@ -936,4 +936,45 @@ int launch_pairs(DeviceState& d, cudaStream_t s) {
     return launches + (int)ll;
 }
 
+// Caller-supplied pairs (computeContacts(pairs, ...)): packed (min, max) keys of the valid ones;
+// an invalid pair becomes the all-ones key, which the sort moves behind the valid ones, and leaves
+// the count.
+__global__ void k_user_pair_keys(const b3gPair* __restrict__ pairs, int n, int num_bodies, int body_bits,
+                                 uint64_t* __restrict__ keys, int* __restrict__ count, int cap,
+                                 unsigned int* __restrict__ status) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n && i < cap; i += gridDim.x * blockDim.x) {
+        const b3gPair p = pairs[i];
+        const int a = min(p.x, p.y), b = max(p.x, p.y);
+        if (a < 0 || b >= num_bodies || a == b) {
+            keys[i] = ~0ull;
+            atomicSub(count, 1);
+            atomicOr(status, B3G_FLAG_PAIR_OVERFLOW);
+            continue;
+        }
+        keys[i] = ((uint64_t)a << body_bits) | (uint64_t)b;
+    }
+    if (n > cap && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(status, B3G_FLAG_PAIR_OVERFLOW);
+}
+
+int launch_pairs_external(DeviceState& d, const b3gPair* pairs, int n, cudaStream_t s) {
+    long long ll = 0;
+    cudaMemsetAsync(d.counters, 0, offsetof(DevCounters, status), s);
+    cudaMemsetAsync(reinterpret_cast<char*>(d.counters) + offsetof(DevCounters, status) + sizeof(unsigned int), 0,
+                    sizeof(DevCounters) - offsetof(DevCounters, status) - sizeof(unsigned int), s);
+    int* d_np = &d.counters->pad[0];       // valid pairs (the consumers' count)
+    int* d_written = &d.counters->pad[2];  // keys written: the sort covers the invalid ones too
+    const int m = std::min(n, d.max_pairs);
+    launch_set_int(d_np, m, s);
+    launch_set_int(d_written, m, s);
+    k_user_pair_keys<<<d.num_sms * 4, BP_THREADS, 0, s>>>(pairs, n, d.num_bodies, d.body_bits, d.pair_keys[0], d_np,
+                                                          d.max_pairs, &d.counters->status);
+    const int w = radix_sort_u64(d.prim, d.pair_keys[0], d.pair_keys[1], nullptr, nullptr, d_written,
+                                 2 * d.body_bits, d.sort_scratch, s, &ll);
+    k_clamp_count<<<1, 1, 0, s>>>(d_np, d.max_pairs, &d.counters->num_pairs);
+    k_unpack_pairs<<<d.num_sms * 4, BP_THREADS, 0, s>>>(d.pair_keys[w], d_np, d.body_bits, d.bodies, d.collidables,
+                                                        d.col_small, d.pairs, d.contact_flag, d.type_lists,
+                                                        d.max_pairs, d.counters->type_count);
+    return 6 + (int)ll;
+}
+
 }  // namespace b3g

@@ -93,6 +93,16 @@ struct SolverArgs {
     float threshold;
     GridBarrier bar;
     unsigned int spin_limit;
+    // PGS in colour order from the setup on (k_manifold_prep / k_colour / k_pgs_sweeps)
+    int* pos_of;                  // manifold -> position in colour order (nullptr: the in-kernel path)
+    unsigned long long* prev_key; // last solve's manifold keys (ascending) and colours
+    int* prev_color;
+    int* d_prev_n;
+    int* d_new;                   // manifolds without a carried colour
+    int* color_goff;              // colour offsets of the ordered records: [c] start, [65] total
+    int body_bits;
+    int tail_max;                 // trailing colours of at most this many manifolds run in one block
+    GridBarrier bar2;             // barrier of k_colour (separate counters from the sweeps')
 };
 
 // b3PlaneSpace1 (Bullet3Common/b3Vector3.h:1184-1212)
@@ -111,6 +121,7 @@ __device__ __forceinline__ void plane_space(v3 n, v3& p, v3& q) {
 }
 
 __device__ __forceinline__ float4 f4(v3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
+__device__ __forceinline__ float4 f4v(b3gFloat4 r) { return make_float4(r.x, r.y, r.z, r.w); }
 __device__ __forceinline__ v3 xyz(float4 a) { return mk3(a.x, a.y, a.z); }
 
 // Jacobi split counts: number of manifolds touching each dynamic body.
@@ -138,6 +149,8 @@ __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
     const int nc = *a.d_nc;
     const bool pgs = a.mode == B3G_SOLVER_PGS;
     if (a.ws_rows && blockIdx.x == 0 && threadIdx.x == 0) *a.ws_rows = min(4 * nc, a.ws_rows_cap);
+    const bool ordered = a.pos_of != nullptr;  // records straight into colour order
+    SolverPoints& out = ordered ? a.sp_ord : a.sp;
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nc; m += gridDim.x * blockDim.x) {
         const b3gContact4 c = a.slots[a.manifold_pair[m]];
         const int iA = abs(c.bodyA), iB = abs(c.bodyB);
@@ -147,8 +160,11 @@ __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
         int np = (int)c.worldNormalOnB.w;
         if (np > 4) np = 4;
         int mask = 0;
-        a.color[m] = -1;
-        a.inv_mass[m] = make_float2(imA, imB);
+        const int k = ordered ? __ldcg(&a.pos_of[m]) : m;  // record slot
+        if (!ordered) {
+            a.color[m] = -1;
+            a.inv_mass[m] = make_float2(imA, imB);
+        }
         if (imA == 0.f && imB == 0.f) np = 0;  // static-static: no rows (b3PgsJacobiSolver.cpp:864-866)
         const b3gMat3 IA = a.inertias[iA].invInertiaWorld;
         const b3gMat3 IB = a.inertias[iB].invInertiaWorld;
@@ -163,12 +179,20 @@ __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
         const float fric = (float)c.frictionCmp / (float)0xffff;
         // getContactPoint: normalised normal
         v3 n = normalize3(mk3(c.worldNormalOnB.x, c.worldNormalOnB.y, c.worldNormalOnB.z));
-        a.sp.nf[m] = f4(n, fric);
+        out.nf[k] = f4(n, fric);
+        if (ordered) {
+            // both inverse inertias next to the record, so that the sweeps read them by position
+            float4* o = a.inertia_ord + 6 * (size_t)k;
+            o[0] = f4v(IA.row[0]); o[1] = f4v(IA.row[1]); o[2] = f4v(IA.row[2]);
+            o[3] = f4v(IB.row[0]); o[4] = f4v(IB.row[1]); o[5] = f4v(IB.row[2]);
+            a.inv_mass_ord[k] = make_float4(imA, imB, 0.f, 0.f);
+        }
         for (int j = 0; j < np; j++) {
             const float dist = c.worldPosB[j].w;
             if (!(dist <= a.threshold)) continue;
             mask |= 1 << j;
-            const size_t s = (size_t)m * 4 + j;
+            const size_t s = (size_t)k * 4 + j;     // record slot of the point
+            const size_t sf = (size_t)m * 4 + j;    // feature slot (manifold order)
             const v3 pos2 = mk3(c.worldPosB[j].x, c.worldPosB[j].y, c.worldPosB[j].z);
             const v3 pos1 = pos2 + n * dist;
             const v3 rel1 = pos1 - posA;
@@ -195,8 +219,8 @@ __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
                 else
                     positionalError = -penetration * a.erp / a.dt;
                 float rhs = positionalError * scaled + velocityError * scaled;
-                a.sp.rel1[s] = f4(rel1, jac);
-                a.sp.rel2[s] = f4(rel2, rhs);
+                out.rel1[s] = f4(rel1, jac);
+                out.rel2[s] = f4(rel2, rhs);
             }
             // friction rows (convertContact: dir2 row first, then dir1)
             {
@@ -235,13 +259,13 @@ __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
                     jacs[k] = jac;
                     rhss[k] = velocityError * scaled;
                 }
-                a.sp.dir2[s] = f4(dir2, jacs[0]);
-                a.sp.dir1[s] = f4(dir1, jacs[1]);
-                a.sp.rhsf[s] = make_float2(rhss[0], rhss[1]);
-                a.sp.imp[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (a.ws_features && s < (size_t)a.ws_rows_cap) {
+                out.dir2[s] = f4(dir2, jacs[0]);
+                out.dir1[s] = f4(dir1, jacs[1]);
+                out.rhsf[s] = make_float2(rhss[0], rhss[1]);
+                out.imp[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (a.ws_features && sf < (size_t)a.ws_rows_cap) {
                     // warm-start features of this point (the network's input layout)
-                    float* f = a.ws_features + s * 12;
+                    float* f = a.ws_features + sf * 12;
                     f[0] = vel.x; f[1] = vel.y; f[2] = vel.z;
                     f[3] = n.x; f[4] = n.y; f[5] = n.z;
                     f[6] = dist;
@@ -252,7 +276,10 @@ __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
                 }
             }
         }
-        a.hdr[m] = make_int4(iA, iB, mask, np);
+        if (ordered)
+            a.hdr_ord[k] = make_int4(iA, iB, mask, -1);
+        else
+            a.hdr[m] = make_int4(iA, iB, mask, np);
     }
 }
 
@@ -1261,6 +1288,8 @@ struct WarmFill {
     int write_imp;
     float4* init;
     unsigned char* is_new;
+    const int* pos_of;            // non-null: initial impulses go to the colour-ordered records
+    float4* imp_ord;
 };
 
 __device__ __forceinline__ unsigned long long pair_key(int a, int b, int bits) {
@@ -1275,7 +1304,8 @@ __global__ void k_warm_fill(WarmFill w) {
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < mmax; m += gridDim.x * blockDim.x) {
         const int4 h = w.hdr[m];
         const int mask = h.z;
-        const float fr = w.sp.nf[m].w;
+        float4* imp_out = w.pos_of ? w.imp_ord + 4 * (size_t)__ldcg(&w.pos_of[m]) : w.sp.imp + 4 * (size_t)m;
+        const float fr = (float)w.slots[w.manifold_pair[m]].frictionCmp / (float)0xffff;
         // previous manifold of the same body pair
         const unsigned long long key = pair_key(h.x, h.y, w.body_bits);
         int lo = 0, hi = pn;
@@ -1322,7 +1352,7 @@ __global__ void k_warm_fill(WarmFill w) {
                     f1 = isfinite(f1) ? fminf(fmaxf(f1, -lim), lim) : 0.f;
                     v = make_float4(lam, f2, f1, 0.f);
                 }
-                if (w.write_imp) w.sp.imp[s] = v;
+                if (w.write_imp) imp_out[j] = v;
             }
             if (w.init) w.init[s] = w.write_imp ? v : make_float4(0.f, 0.f, 0.f, 0.f);
             if (w.is_new) w.is_new[s] = matched ? 0 : 1;
@@ -1350,6 +1380,314 @@ __global__ void k_warm_store(const int* __restrict__ d_nc, int rows_cap, const i
     }
 }
 
+// ------------------------------------------------------------------ PGS in colour order from the setup on
+// The grid-wide PGS path (no block partitions) colours the manifolds BEFORE the row setup, so the
+// setup writes every record at its position in colour order and the sweeps read them in order:
+//   k_manifold_prep   per manifold: header, inverse masses, and the colour the same body pair had
+//                     in the last solve (manifolds follow the sorted pair list, so the last
+//                     solve's keys are sorted too: a binary search, tried at the same index first)
+//   k_colour          carried colours claim their bits in the per-body colour masks (a clash,
+//                     possible only when a body's inverse mass changed, drops the later one);
+//                     Jones-Plassmann rounds colour the rest against those masks; counting sort by
+//                     colour gives every manifold its record position
+//   k_setup_rows      records straight into colour order (and the warm start's impulses)
+//   k_pgs_sweeps      the iterations; colours up to the first of a run of small trailing colours
+//                     are grid-wide phases with a grid barrier each, the trailing small colours
+//                     run in one block with __syncthreads between them and one grid barrier after
+//                     the run; then impulses back to manifold order, v += dv, and this solve's keys
+//                     and colours for the next one
+// Any legal colouring gives a legal Gauss-Seidel order (the solve order stays readable through
+// b3g_read_solve_order); colours carried over keep the persisting contacts' batches stable from
+// step to step, and a scene whose contact set does not change is coloured once.
+__global__ void __launch_bounds__(SV_THREADS) k_manifold_prep(SolverArgs a) {
+    const int nc = *a.d_nc;
+    const int pn = *a.d_prev_n;
+    int fresh = 0;
+    for (int m0 = blockIdx.x * blockDim.x; m0 < nc; m0 += gridDim.x * blockDim.x) {
+        const int m = m0 + (int)threadIdx.x;
+        int col = -1;
+        if (m < nc) {
+            const b3gContact4& c = a.slots[a.manifold_pair[m]];
+            const int iA = abs(c.bodyA), iB = abs(c.bodyB);
+            const float imA = a.bodies[iA].invMass, imB = a.bodies[iB].invMass;
+            int np = (int)c.worldNormalOnB.w;
+            if (np > 4) np = 4;
+            if (imA == 0.f && imB == 0.f) np = 0;
+            int mask = 0;
+            for (int j = 0; j < np; j++)
+                if (c.worldPosB[j].w <= a.threshold) mask |= 1 << j;
+            a.hdr[m] = make_int4(iA, iB, mask, np);
+            a.inv_mass[m] = make_float2(imA, imB);
+            if (pn > 0) {
+                const unsigned long long key = pair_key(iA, iB, a.body_bits);
+                int q = min(m, pn - 1);
+                if (__ldcg(&a.prev_key[q]) != key) {
+                    int lo = 0, hi = pn;
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1;
+                        if (__ldcg(&a.prev_key[mid]) < key)
+                            lo = mid + 1;
+                        else
+                            hi = mid;
+                    }
+                    q = (lo < pn && __ldcg(&a.prev_key[lo]) == key) ? lo : -1;
+                }
+                if (q >= 0) {
+                    col = __ldcg(&a.prev_color[q]);
+                    if (col >= 64) col = -1;
+                }
+            }
+            a.color[m] = col;
+            fresh += col < 0;
+        }
+    }
+    for (int o = 16; o; o >>= 1) fresh += __shfl_xor_sync(0xffffffffu, fresh, o);
+    if ((threadIdx.x & 31) == 0 && fresh) atomicAdd(a.d_new, fresh);
+}
+
+// Cooperative: carried colours, Jones-Plassmann for the rest, record positions.  Colour 64 holds
+// the manifolds that found no colour below 64 (solved one after another by one thread).
+__global__ void __launch_bounds__(PK_THREADS, 1) k_colour(SolverArgs a) {
+    grid_barrier_begin();
+    const int nc = *a.d_nc;
+    const unsigned nb = gridDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int stride = gridDim.x * blockDim.x;
+    // carried colours claim their mask bits; a clash on a body drops the manifold to recolouring
+    int dropped = 0;
+    if (*((volatile int*)a.d_new) < nc) {
+        for (int m = tid; m < nc; m += stride) {
+            const int c = a.color[m];
+            if (c < 0) continue;
+            const int4 h = a.hdr[m];
+            const float2 im = a.inv_mass[m];
+            const unsigned long long bit = 1ull << c;
+            bool clash = false;
+            if (im.x != 0.f) clash |= (atomicOr(&a.mask[h.x], bit) & bit) != 0ull;
+            if (im.y != 0.f) clash |= (atomicOr(&a.mask[h.y], bit) & bit) != 0ull;
+            if (clash) {
+                a.color[m] = -1;
+                dropped++;
+            }
+        }
+    }
+    for (int o = 16; o; o >>= 1) dropped += __shfl_xor_sync(0xffffffffu, dropped, o);
+    if ((threadIdx.x & 31) == 0 && dropped) atomicAdd(a.d_new, dropped);
+    if (!grid_barrier(a.bar2, nb, a.spin_limit)) return;
+    // Jones-Plassmann rounds over the uncoloured manifolds (the highest hashed priority on both of
+    // its dynamic bodies takes the smallest colour free on both); statics never conflict
+    bool overflow = false;
+    if (*((volatile int*)a.d_new) > 0) {
+        for (int r = 0; r < B3G_MAX_COLORS; r++) {
+            const unsigned long long rk = (unsigned long long)r << 56;
+            for (int m = tid; m < nc; m += stride) {
+                if (a.color[m] >= 0) continue;
+                const int4 h = a.hdr[m];
+                const float2 im = a.inv_mass[m];
+                const unsigned long long key =
+                    rk | ((unsigned long long)(hash32((unsigned)m) & 0xFFFFFFu) << 32) | (unsigned)m;
+                if (im.x != 0.f) atomicMax(&a.claim[h.x], key);
+                if (im.y != 0.f) atomicMax(&a.claim[h.y], key);
+            }
+            if (!grid_barrier(a.bar2, nb, a.spin_limit)) return;
+            int left = 0;
+            for (int m = tid; m < nc; m += stride) {
+                if (a.color[m] >= 0) continue;
+                const int4 h = a.hdr[m];
+                const float2 im = a.inv_mass[m];
+                const unsigned long long key =
+                    rk | ((unsigned long long)(hash32((unsigned)m) & 0xFFFFFFu) << 32) | (unsigned)m;
+                const bool okA = im.x == 0.f || __ldcg(&a.claim[h.x]) == key;
+                const bool okB = im.y == 0.f || __ldcg(&a.claim[h.y]) == key;
+                if (okA && okB) {
+                    unsigned long long used = 0ull;
+                    if (im.x != 0.f) used |= __ldcg(&a.mask[h.x]);
+                    if (im.y != 0.f) used |= __ldcg(&a.mask[h.y]);
+                    const int c = __ffsll((long long)~used) - 1;
+                    if (c >= 0 && c < 64) {
+                        a.color[m] = c;
+                        if (im.x != 0.f) atomicOr(&a.mask[h.x], 1ull << c);
+                        if (im.y != 0.f) atomicOr(&a.mask[h.y], 1ull << c);
+                    } else {
+                        left++;
+                    }
+                } else {
+                    left++;
+                }
+            }
+            for (int o = 16; o; o >>= 1) left += __shfl_xor_sync(0xffffffffu, left, o);
+            if ((threadIdx.x & 31) == 0 && left) atomicAdd(&a.remaining[r], left);
+            if (!grid_barrier(a.bar2, nb, a.spin_limit)) return;
+            if (*((volatile int*)&a.remaining[r]) == 0) break;
+            overflow = r == B3G_MAX_COLORS - 1;
+        }
+    }
+    // counting sort by colour (64: the manifolds left without one)
+    for (int m0 = tid - (threadIdx.x & 31); m0 < nc; m0 += stride) {
+        const int m = m0 + (threadIdx.x & 31);
+        int key = -1;
+        if (m < nc) {
+            const int c = a.color[m];
+            key = c >= 0 ? c : 64;
+        }
+        warp_count(a.color_fill, key);
+    }
+    if (!grid_barrier(a.bar2, nb, a.spin_limit)) return;
+    if (blockIdx.x == 0) {
+        const int total = block_exclusive_scan(a.color_fill, a.color_goff, 65);
+        if (threadIdx.x == 0) {
+            a.color_goff[65] = total;
+            int ncl = 0;
+            for (int c = 0; c < 64; c++)
+                if (__ldcg(&a.color_fill[c]) > 0) ncl = c + 1;
+            a.counters->num_colors = ncl;
+            if (overflow || __ldcg(&a.color_fill[64]) > 0) atomicOr(&a.counters->status, B3G_FLAG_BATCH_OVERFLOW);
+        }
+    }
+    if (!grid_barrier(a.bar2, nb, a.spin_limit)) return;
+    for (int m0 = tid - (threadIdx.x & 31); m0 < nc; m0 += stride) {
+        const int m = m0 + (threadIdx.x & 31);
+        int key = -1;
+        if (m < nc) {
+            const int c = a.color[m];
+            key = c >= 0 ? c : 64;
+        }
+        const int pos = warp_reserve(a.color_cursor, key);
+        if (key >= 0) {
+            const int k = __ldcg(&a.color_goff[key]) + pos;
+            a.color_order[k] = m;
+            a.pos_of[m] = k;
+        }
+    }
+}
+
+// One record of the ordered sweeps: the manifold at position k against the global body deltas.
+__device__ __forceinline__ void sweep_record(const SolverArgs& a, int k, int pass, float& res_d, float& res_l) {
+    const int4 h = __ldcg(&a.hdr_ord[k]);
+    const float4 im = __ldcg(&a.inv_mass_ord[k]);
+    v3 dlA = mk3(0, 0, 0), daA = mk3(0, 0, 0), dlB = mk3(0, 0, 0), daB = mk3(0, 0, 0);
+    if (im.x != 0.f) load_dv(a, h.x, dlA, daA);
+    if (im.y != 0.f) load_dv(a, h.y, dlB, daB);
+    const b3gMat3 IA = ld_mat_cg(a.inertia_ord + 6 * (size_t)k);
+    const b3gMat3 IB = ld_mat_cg(a.inertia_ord + 6 * (size_t)k + 3);
+    solve_manifold<true, false>(a.sp_ord, k, a.sp_ord.imp + 4 * (size_t)k, pass, h, im.x, im.y, IA, IB, dlA, daA,
+                                dlB, daB, res_d, res_l);
+    if (im.x != 0.f) store_dv(a, h.x, dlA, daA);
+    if (im.y != 0.f) store_dv(a, h.y, dlB, daB);
+}
+
+__global__ void __launch_bounds__(PK_THREADS, 1) k_pgs_sweeps(SolverArgs a) {
+    grid_barrier_begin();
+    const int nc = *a.d_nc;
+    const unsigned nb = gridDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int stride = gridDim.x * blockDim.x;
+    // colour ranges, read once; the trailing run of colours with at most tail_max manifolds each
+    // (and the uncoloured remainder) is solved by block 0 alone
+    __shared__ int s_off[66];
+    for (int i = threadIdx.x; i < 66; i += blockDim.x) s_off[i] = __ldcg(&a.color_goff[i]);
+    __syncthreads();
+    int ncol = 0;
+    for (int c = 0; c < 64; c++)
+        if (s_off[c + 1] > s_off[c]) ncol = c + 1;
+    int tail = ncol;
+    while (tail > 0 && s_off[tail] - s_off[tail - 1] <= a.tail_max) tail--;
+    const bool leftovers = s_off[65] > s_off[64];
+    // phases per pass: the grid-wide colours, and when there is a tail, its colours plus one
+    // phase for the remainder (which ends with the grid barrier)
+    const int nphase = (tail < ncol || leftovers) ? ncol + 1 : tail;
+    bool ok = true;
+    const int npasses = a.interleave ? 1 : 2;
+    bool warm_live = a.warm != 0;
+    int extra = 0;  // 1 after a dropped warm start: its sweep still counts
+    for (int it = a.warm ? -1 : 0; it < a.iterations; it++) {
+        float res_d = 0.f, res_l = 0.f;
+        const bool warm_pass = it < 0;
+        for (int ps = 0; ps < (warm_pass ? 1 : npasses); ps++) {
+            const int pass = warm_pass ? 3 : (a.interleave ? 2 : ps);
+            // phases of one pass: grid-wide colours [0, tail), then (block 0 only) the trailing
+            // colours [tail, ncol) and the uncoloured remainder; one solve call site keeps the
+            // register budget of the kernel low
+            for (int ph = 0; ph < nphase; ph++) {
+                int first, hi, step;
+                if (ph < tail) {
+                    first = s_off[ph];
+                    hi = s_off[ph + 1];
+                    if (first == hi) continue;  // uniform across blocks
+                    // warm L2 with this block's share of the next grid-wide colour
+                    if (threadIdx.x == 0 && ph + 1 < tail) {
+                        const int k0 = s_off[ph + 1] + blockIdx.x * blockDim.x;
+                        prefetch_records_l2(a, k0, min((int)blockDim.x, s_off[ph + 2] - k0), pass);
+                    }
+                    first += tid;
+                    step = stride;
+                } else if (ph < ncol) {
+                    if (blockIdx.x != 0) continue;
+                    first = s_off[ph] + (int)threadIdx.x;
+                    hi = s_off[ph + 1];
+                    step = blockDim.x;
+                } else {  // uncoloured remainder: in order, one thread
+                    first = s_off[64];
+                    hi = blockIdx.x == 0 && threadIdx.x == 0 ? s_off[65] : first;
+                    step = 1;
+                }
+                for (int k = first; k < hi; k += step) sweep_record(a, k, pass, res_d, res_l);
+                if (ph < tail || ph == ncol) {
+                    if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
+                } else {
+                    __syncthreads();  // block 0 between trailing colours
+                }
+            }
+        }
+        if (warm_pass) continue;  // the application pass has no residual
+        if (!(a.residual_tol > 0.f || (it == 0 && warm_live) || it == a.iterations - 1)) {
+            block_accumulate(a.residual_acc + 2 * (it + extra), res_d, res_l);
+            continue;
+        }
+        double r = 0.0;
+        if (end_iteration(a, it + extra, res_d, res_l, ok, &r)) break;
+        if (it == 0 && warm_live) {
+            warm_live = false;
+            // a cold first sweep has residual exactly 1: a warm start that does worse is dropped
+            // and the solve restarts cold with the full iteration budget (every block sees the same r)
+            if (r > 1.0) {
+                for (int i = tid; i < 2 * a.num_bodies; i += stride) __stcg(&a.dv[i], make_float4(0.f, 0.f, 0.f, 0.f));
+                for (int k = tid; k < nc; k += stride)
+                    for (int j = 0; j < 4; j++) __stcg(&a.sp_ord.imp[(size_t)k * 4 + j], make_float4(0.f, 0.f, 0.f, 0.f));
+                if (tid == 0) atomicOr(&a.counters->status, B3G_FLAG_WARM_DISCARDED);
+                extra = 1;
+                it = -1;
+                if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
+            }
+        }
+    }
+    if (!ok) return;
+    // applied impulses back to manifold order (b3g_read_impulses, the warm-start store), and this
+    // solve's manifold keys and colours for the next solve
+    for (int k = tid; k < nc; k += stride) {
+        const int m = __ldcg(&a.color_order[k]);
+        const int4 h = __ldcg(&a.hdr_ord[k]);
+        for (int j = 0; j < 4; j++)
+            if (h.z & (1 << j)) a.sp.imp[(size_t)m * 4 + j] = __ldcg(&a.sp_ord.imp[(size_t)k * 4 + j]);
+        a.prev_key[m] = pair_key(h.x, h.y, a.body_bits);
+        a.prev_color[m] = a.color[m];
+    }
+    if (tid == 0) *a.d_prev_n = nc;
+    // finish: v += dv for dynamic bodies
+    for (int b = tid; b < a.num_bodies; b += stride) {
+        if (a.bodies[b].invMass == 0.f) continue;
+        v3 dl, da;
+        load_dv(a, b, dl, da);
+        b3gBody& B = a.bodies_out[b];
+        B.linVel.x = B.linVel.x + dl.x;
+        B.linVel.y = B.linVel.y + dl.y;
+        B.linVel.z = B.linVel.z + dl.z;
+        B.angVel.x = B.angVel.x + da.x;
+        B.angVel.y = B.angVel.y + da.y;
+        B.angVel.z = B.angVel.z + da.z;
+    }
+}
+
 __global__ void k_reset_solver(int* color_fill, int* remaining, int* color_cursor, unsigned int* barrier,
                                double* residual_acc, int nres, DevCounters* counters) {
     for (int i = threadIdx.x; i < B3G_MAX_COLORS + 1; i += blockDim.x) {
@@ -1358,11 +1696,15 @@ __global__ void k_reset_solver(int* color_fill, int* remaining, int* color_curso
         color_cursor[i] = 0;
     }
     for (int i = threadIdx.x; i < nres; i += blockDim.x) residual_acc[i] = 0.0;
-    if (threadIdx.x < 4) barrier[threadIdx.x] = 0;
+    if (threadIdx.x < 4) {
+        barrier[threadIdx.x] = 0;       // the sweeps' grid barrier
+        barrier[16 + threadIdx.x] = 0;  // k_colour's
+    }
     if (threadIdx.x == 0) {
         counters->iterations = 0;
         counters->residual = 0.f;
         counters->num_colors = 0;
+        counters->new_manifolds = 0;
     }
 }
 
@@ -1468,6 +1810,45 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     a.bar.abort_flag = d.barrier + 2;
     a.bar.status = &d.counters->status;
     a.spin_limit = cfg.barrier_spin_limit > 0 ? (unsigned)cfg.barrier_spin_limit : B3G_BARRIER_SPIN_LIMIT;
+    a.pos_of = nullptr;
+    a.prev_key = d.prev_mkey;
+    a.prev_color = d.prev_mcolor;
+    a.d_prev_n = d.prev_mn;
+    a.d_new = &d.counters->new_manifolds;
+    a.color_goff = d.color_offsets;
+    a.body_bits = d.body_bits;
+    a.tail_max = cfg.pgs_tail_manifolds > 0 ? cfg.pgs_tail_manifolds : 1024;
+    a.bar2.count = d.barrier + 16;
+    a.bar2.gen = d.barrier + 17;
+    a.bar2.abort_flag = d.barrier + 18;
+    a.bar2.status = &d.counters->status;
+    // PGS work split: the autotuner's choice (b3g_autotune) when the config says AUTO, else the
+    // split measured fastest on GB300 for 256k-box piles -- grid-wide colours, coloured before
+    // the row setup (records written in colour order)
+    const int pgs_mode = cfg.pgs_partitions != B3G_PGS_PARTITIONS_AUTO ? cfg.pgs_partitions
+                         : d.tune.pgs_partitions > 0                   ? d.tune.pgs_partitions
+                                                                       : B3G_PGS_PARTITIONS_NONE;
+    const bool ordered = cfg.solver_mode == B3G_SOLVER_PGS && pgs_mode == B3G_PGS_PARTITIONS_NONE;
+    const int cgrid = ordered ? solver_grid(d, (const void*)k_pgs_sweeps, cfg.solver_blocks_per_sm, 0) : 0;
+    if (ordered) {
+        a.pos_of = d.manifold_pos;
+        a.color_fill = color_fill;
+        a.color_cursor = color_cursor;
+        k_manifold_prep<<<grid, SV_THREADS, 0, s>>>(a);
+        launches++;
+        cudaLaunchConfig_t lc = {};
+        lc.gridDim = dim3(cgrid);
+        lc.blockDim = dim3(PK_THREADS);
+        lc.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        lc.attrs = attr;
+        lc.numAttrs = 1;
+        cudaError_t e = cudaLaunchKernelEx(&lc, k_colour, a);
+        if (e != cudaSuccess && d.launch_error == cudaSuccess) d.launch_error = e;
+        launches++;
+    }
 
     if (cfg.solver_mode == B3G_SOLVER_JACOBI) {
         const uint32_t sentinel = (1u << d.body_bits) - 1u;
@@ -1509,6 +1890,8 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
         w.write_imp = a.warm;
         w.init = d.ws_init;
         w.is_new = d.ws_new;
+        w.pos_of = a.pos_of;
+        w.imp_ord = d.sp_ord.imp;
         k_warm_fill<<<grid, SV_THREADS, 0, s>>>(w);
         launches++;
     }
@@ -1520,12 +1903,10 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     const int bps = cfg.solver_blocks_per_sm;
     if (jac) {
         sgrid = solver_grid(d, (const void*)k_solve_jacobi, bps, 0);
+    } else if (ordered) {
+        sgrid = cgrid;
     } else {
-        // AUTO: the autotuner's choice (b3g_autotune), else the split measured fastest on GB300 for
-        // 256k-box piles -- grid-wide colours
-        const int mode = cfg.pgs_partitions != B3G_PGS_PARTITIONS_AUTO ? cfg.pgs_partitions
-                         : d.tune.pgs_partitions > 0                   ? d.tune.pgs_partitions
-                                                                       : B3G_PGS_PARTITIONS_NONE;
+        const int mode = pgs_mode;
         const bool parts = mode != B3G_PGS_PARTITIONS_NONE;
         const int nd = parts && d.cell_sorted_bodies ? d.num_dynamic : 0;
         sgrid = solver_grid(d, (const void*)k_solve_pgs<true>, bps, 0);
@@ -1568,6 +1949,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     lc.attrs = attr;
     lc.numAttrs = 1;
     cudaError_t e = jac                 ? cudaLaunchKernelEx(&lc, k_solve_jacobi, a)
+                    : ordered           ? cudaLaunchKernelEx(&lc, k_pgs_sweeps, a)
                     : a.num_dynamic > 0 ? cudaLaunchKernelEx(&lc, k_solve_pgs<true>, a)
                                         : cudaLaunchKernelEx(&lc, k_solve_pgs<false>, a);
     if (e != cudaSuccess && d.launch_error == cudaSuccess) d.launch_error = e;

@@ -76,17 +76,20 @@ struct b3gWorld {
     bool uploaded = false;
     DeviceState d;
     std::vector<void*> allocations;
-    // graph
-    cudaGraphExec_t graph_exec = nullptr;
-    float graph_dt = -1.f;
-    int graph_mode = -1, graph_iters = -1;
-    float graph_tol = -1.f;
+    // captured steps: [0] the plain step, [1] the same step with an event-record node between
+    // stages (profiling), each rebuilt when the step's parameters change
+    struct StepGraph {
+        cudaGraphExec_t exec = nullptr;
+        float dt = -1.f;
+        int mode = -1, iters = -1;
+        float tol = -1.f;
+        long long kernels = 0;
+    } graphs[2];
     // profiling
     bool profiling = false;
     StageEvents events;
     float stage_ms[7] = {0, 0, 0, 0, 0, 0, 0};
     long long launches = 0;
-    long long graph_kernels = 0;
     b3gStepStats last_stats{};
     cudaEvent_t user_events[16] = {};
     b3g_mlp ws_mlp = nullptr;  // attached warm-start network (not owned)
@@ -148,11 +151,16 @@ static void free_joint_buffers(b3g::DeviceState& d) {
     cudaFree(d.joint_dv);
 }
 
-static void free_device(b3gWorld* w) {
-    if (w->graph_exec) {
-        cudaGraphExecDestroy(w->graph_exec);
-        w->graph_exec = nullptr;
+// Drops the captured step graphs (the next step captures again).
+static void drop_graphs(b3gWorld* w) {
+    for (auto& g : w->graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = b3gWorld::StepGraph();
     }
+}
+
+static void free_device(b3gWorld* w) {
+    drop_graphs(w);
     for (void* p : w->allocations) cudaFree(p);
     w->allocations.clear();
     free_joint_buffers(w->d);
@@ -246,6 +254,40 @@ extern "C" b3gStatus b3g_create(const b3gConfig* cfg, int cuda_device, b3g_handl
     }
     w->device = cuda_device;
     *out = w;
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_reset(b3g_handle h, int what) {
+    if (!h) return fail(B3G_ERR_INVALID_ARG, "null handle");
+    if (what & ~(B3G_RESET_SHAPES_AND_BODIES | B3G_RESET_CONSTRAINTS)) return fail(B3G_ERR_INVALID_ARG, "unknown reset flags");
+    if (h->uploaded) {
+        CUDA_TRY(cudaSetDevice(h->device));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+    }
+    if (what & B3G_RESET_CONSTRAINTS) {
+        h->joints.clear();
+        h->joint_order.clear();
+        h->joint_batch_off.clear();
+        h->joints_dirty = true;
+    }
+    if (what & B3G_RESET_SHAPES_AND_BODIES) {
+        free_device(h);  // the next upload allocates afresh
+        h->collidables.clear();
+        h->local_aabbs.clear();
+        h->hulls.clear();
+        h->faces.clear();
+        h->indices.clear();
+        h->vertices.clear();
+        h->edges.clear();
+        h->bodies.clear();
+        h->inertias.clear();
+        h->user_index.clear();
+        h->scene_first.clear();
+        h->tuned = false;
+        h->tuning = b3gTuning{};
+        h->last_stats = b3gStepStats{};
+        h->joints_dirty = true;
+    }
     return B3G_OK;
 }
 
@@ -467,7 +509,7 @@ extern "C" b3gStatus b3g_set_gravity(b3g_handle h, const float g[3]) {
     h->cfg.gravity[0] = g[0];
     h->cfg.gravity[1] = g[1];
     h->cfg.gravity[2] = g[2];
-    h->graph_dt = -1.f;  // force re-capture
+    drop_graphs(h);  // force re-capture
     return B3G_OK;
 }
 
@@ -648,6 +690,11 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     TRY(dalloc(h, &d.inertia_ord, 6 * (size_t)d.max_contacts));
     TRY(dalloc(h, &d.manifold_color, d.max_contacts));
     TRY(dalloc(h, &d.color_order, d.max_contacts));
+    TRY(dalloc(h, &d.manifold_pos, d.max_contacts));
+    TRY(dalloc(h, &d.prev_mkey, d.max_contacts));
+    TRY(dalloc(h, &d.prev_mcolor, d.max_contacts));
+    TRY(dalloc(h, &d.prev_mn, 1));
+    CUDA_TRY(cudaMemsetAsync(d.prev_mn, 0, sizeof(int), h->stream));
     TRY(dalloc(h, &d.color_offsets, 4 * (B3G_MAX_COLORS + 2)));  // offsets, fill, remaining, cursors
     TRY(dalloc(h, &d.color_claim, 4 * (size_t)N));  // claims, colour masks; again for cross-partition
     CUDA_TRY(solver_prepare());
@@ -790,10 +837,7 @@ extern "C" b3gStatus b3g_set_broadphase(b3g_handle h, int mode) {
     // AUTO: the grid until the autotuner (at its next run) picks
     h->d.broadphase = mode == B3G_BROADPHASE_LBVH ? B3G_BROADPHASE_LBVH : B3G_BROADPHASE_GRID;
     if (mode == B3G_BROADPHASE_AUTO) h->tuned = false;
-    if (h->graph_exec) {  // the captured step has the other broadphase's launches
-        cudaGraphExecDestroy(h->graph_exec);
-        h->graph_exec = nullptr;
-    }
+    drop_graphs(h);  // the captured step has the other broadphase's launches
     return B3G_OK;
 }
 
@@ -813,8 +857,17 @@ static b3gStatus check_launch(b3gWorld* h) {
     return B3G_OK;
 }
 
+// Stage boundary k of a profiled step: an event record on the stream, or, while the step is being
+// captured, an event-record node of the graph (so a replay of the profiled graph times the stages
+// of the captured step itself).
 static void record(b3gWorld* h, int k) {
-    if (h->profiling) cudaEventRecord(h->events.ev[k], h->stream);
+    if (!h->profiling) return;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(h->stream, &cs);
+    if (cs == cudaStreamCaptureStatusActive)
+        cudaEventRecordWithFlags(h->events.ev[k], h->stream, cudaEventRecordExternal);
+    else
+        cudaEventRecord(h->events.ev[k], h->stream);
 }
 
 // ---------------------------------------------------------------------------------- joints
@@ -899,10 +952,7 @@ static b3gStatus prepare_joints(b3gWorld* h) {
     DeviceState& d = h->d;
     cudaStream_t s = h->stream;
     const int n = (int)h->joints.size();
-    if (h->graph_exec) {
-        cudaGraphExecDestroy(h->graph_exec);
-        h->graph_exec = nullptr;
-    }
+    drop_graphs(h);
     d.num_joints = 0;
     d.num_joint_batches = 0;
     d.num_joint_uniq = 0;
@@ -1079,40 +1129,41 @@ extern "C" b3gStatus b3g_step(b3g_handle h, float dt) {
     CUDA_TRY(cudaSetDevice(h->device));
     TRY(prepare_joints(h));
     if (h->cfg.autotune && !h->tuned) TRY(b3g_autotune(h, dt, 3, nullptr));
-    if (h->profiling || !h->cfg.use_cuda_graph) {
+    if (!h->cfg.use_cuda_graph) {
         enqueue_step(h, dt, h->profiling);
         TRY(check_launch(h));
         return B3G_OK;
     }
-    if (!h->graph_exec || h->graph_dt != dt || h->graph_mode != h->cfg.solver_mode ||
-        h->graph_iters != h->cfg.solver_iterations || h->graph_tol != h->cfg.residual_tol) {
-        if (h->graph_exec) {
-            cudaGraphExecDestroy(h->graph_exec);
-            h->graph_exec = nullptr;
+    b3gWorld::StepGraph& g = h->graphs[h->profiling ? 1 : 0];
+    if (!g.exec || g.dt != dt || g.mode != h->cfg.solver_mode || g.iters != h->cfg.solver_iterations ||
+        g.tol != h->cfg.residual_tol) {
+        if (g.exec) {
+            cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
         }
-        cudaGraph_t g;
+        cudaGraph_t graph;
         long long before = h->launches;
         CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-        enqueue_step(h, dt, false);
-        CUDA_TRY(cudaStreamEndCapture(h->stream, &g));
+        enqueue_step(h, dt, h->profiling);
+        CUDA_TRY(cudaStreamEndCapture(h->stream, &graph));
         {
             b3gStatus st = check_launch(h);
             if (st != B3G_OK) {
-                cudaGraphDestroy(g);
+                cudaGraphDestroy(graph);
                 return st;
             }
         }
-        CUDA_TRY(cudaGraphInstantiate(&h->graph_exec, g, 0));
-        cudaGraphDestroy(g);
-        h->graph_dt = dt;
-        h->graph_mode = h->cfg.solver_mode;
-        h->graph_iters = h->cfg.solver_iterations;
-        h->graph_tol = h->cfg.residual_tol;
-        h->graph_kernels = h->launches - before;
+        CUDA_TRY(cudaGraphInstantiate(&g.exec, graph, 0));
+        cudaGraphDestroy(graph);
+        g.dt = dt;
+        g.mode = h->cfg.solver_mode;
+        g.iters = h->cfg.solver_iterations;
+        g.tol = h->cfg.residual_tol;
+        g.kernels = h->launches - before;
         h->launches = before;
     }
-    CUDA_TRY(cudaGraphLaunch(h->graph_exec, h->stream));
-    h->launches += h->graph_kernels;
+    CUDA_TRY(cudaGraphLaunch(g.exec, h->stream));
+    h->launches += g.kernels;
     return B3G_OK;
 }
 
@@ -1264,7 +1315,7 @@ extern "C" b3gStatus b3g_autotune(b3g_handle h, float dt, int repeats, b3gTuning
     cudaMemcpyAsync(d.bodies, saved, sizeof(b3gBody) * d.num_bodies, cudaMemcpyDeviceToDevice, s);
     cudaStreamSynchronize(s);
     cudaFree(saved);
-    h->graph_dt = -1.f;  // the captured step used the old launch shapes
+    drop_graphs(h);  // the captured step used the old launch shapes
     h->tuned = true;
     if (st != B3G_OK) return st;
     res.pgs_partitions = d.tune.pgs_partitions;
@@ -1387,6 +1438,17 @@ extern "C" b3gStatus b3g_compute_contacts(b3g_handle h) {
     TRY(check_launch(h));
     return B3G_OK;
 }
+extern "C" b3gStatus b3g_compute_contacts_for_pairs(b3g_handle h, const void* d_pairs, int n) {
+    REQUIRE_UPLOADED(h);
+    if (n < 0 || (n > 0 && !d_pairs)) return fail(B3G_ERR_INVALID_ARG, "invalid pair buffer");
+    if (reinterpret_cast<uintptr_t>(d_pairs) & 15u) return fail(B3G_ERR_INVALID_ARG, "pairs must be 16-byte aligned");
+    CUDA_TRY(cudaSetDevice(h->device));
+    h->launches += launch_pairs_external(h->d, static_cast<const b3gPair*>(d_pairs), n, h->stream);
+    h->launches += launch_contacts(h->d, h->cfg.contact_friction, h->stream);
+    TRY(check_launch(h));
+    return B3G_OK;
+}
+
 extern "C" b3gStatus b3g_solve_joints(b3g_handle h) {
     REQUIRE_UPLOADED(h);
     TRY(prepare_joints(h));
@@ -1740,6 +1802,36 @@ extern "C" b3gStatus b3g_hull_compute(const float* verts, int stride_bytes, int 
     return B3G_OK;
 }
 
+// ---------------------------------------------------------------------------------- device buffers
+extern "C" b3gStatus b3g_buffer_alloc(int cuda_device, size_t bytes, void** out) {
+    if (!out) return fail(B3G_ERR_INVALID_ARG, "null output");
+    *out = nullptr;
+    CUDA_TRY(cudaSetDevice(cuda_device));
+    if (bytes == 0) return B3G_OK;
+    CUDA_TRY(cudaMalloc(out, bytes));
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_buffer_free(int cuda_device, void* p) {
+    if (!p) return B3G_OK;
+    CUDA_TRY(cudaSetDevice(cuda_device));
+    CUDA_TRY(cudaFree(p));
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_buffer_copy(int cuda_device, void* dst, const void* src, size_t bytes, int kind) {
+    if (bytes == 0) return B3G_OK;
+    if (!dst || !src) return fail(B3G_ERR_INVALID_ARG, "null buffer");
+    const cudaMemcpyKind k = kind == B3G_COPY_H2D   ? cudaMemcpyHostToDevice
+                             : kind == B3G_COPY_D2H ? cudaMemcpyDeviceToHost
+                             : kind == B3G_COPY_D2D ? cudaMemcpyDeviceToDevice
+                                                    : cudaMemcpyDefault;
+    if (k == cudaMemcpyDefault) return fail(B3G_ERR_INVALID_ARG, "unknown copy kind %d", kind);
+    CUDA_TRY(cudaSetDevice(cuda_device));
+    CUDA_TRY(cudaMemcpy(dst, src, bytes, k));
+    return B3G_OK;
+}
+
 // ------------------------------------------------------------------ allocation-free broadphase
 // Per device: the static scratch array's address and the SM count, looked up on the first call
 // with that device current.
@@ -1810,10 +1902,7 @@ extern "C" b3gStatus b3g_set_warm_start_model(b3g_handle h, b3g_mlp m) {
         h->d.ws_model = h->d.ws_features ? model : nullptr;
         if (h->d.ws_model) CUDA_TRY(mlp::ensure_infer(*h->d.ws_model, h->d.ws_rows_cap));
         CUDA_TRY(cudaSetDevice(h->device));
-        if (h->graph_exec) {  // the captured step has (or lacks) the network's launches
-            cudaGraphExecDestroy(h->graph_exec);
-            h->graph_exec = nullptr;
-        }
+        drop_graphs(h);  // the captured step has (or lacks) the network's launches
     }
     return B3G_OK;
 }

@@ -34,7 +34,8 @@ struct DevCounters {
     float residual;
     unsigned int status;
     int type_count[PT_COUNT];
-    int pad[64 - 7 - PT_COUNT];
+    int new_manifolds;    // PGS: manifolds without a colour carried over from the last solve
+    int pad[64 - 8 - PT_COUNT];
 };
 
 // Compact solver records.  A b3SolverConstraint row (Bullet3Dynamics/ConstraintSolver/
@@ -177,6 +178,10 @@ struct DeviceState {
     int* group_counts = nullptr;           // 3 x (num_sms * B3G_PGS_MAX_BLOCKS_PER_SM * 64 + 64 + 2)
     int* manifold_color = nullptr;
     int* color_order = nullptr;            // manifolds sorted by colour
+    int* manifold_pos = nullptr;           // PGS: position of each manifold in colour order
+    unsigned long long* prev_mkey = nullptr;  // PGS: last solve's manifold body-pair keys (ascending)
+    int* prev_mcolor = nullptr;            // PGS: ... and their colours
+    int* prev_mn = nullptr;                // PGS: ... and their number
     int* color_offsets = nullptr;          // B3G_MAX_COLORS + 1
     unsigned long long* color_claim = nullptr;  // per body
     float4* dv = nullptr;                  // per body: lin xyz | ang xyz (2 float4)
@@ -234,6 +239,7 @@ long long launch_joint_masses(const DeviceState& d, int n, float2* out, cudaStre
 int launch_contacts(DeviceState& d, float friction, cudaStream_t s);
 int launch_compact_contacts(DeviceState& d, cudaStream_t s);
 int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s);
+int launch_pairs_external(DeviceState& d, const b3gPair* pairs, int n, cudaStream_t s);
 cudaError_t solver_prepare();  // kernel attributes, once per device before the first solve
 
 // sets the message b3g_last_error returns (this thread) and passes the status through

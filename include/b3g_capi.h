@@ -112,7 +112,9 @@ typedef struct b3gConfig {
                                   predictions when warm_start != 0; 0 = 8 x bodies (at least 8192) */
     int autotune;              /* 1: the first b3g_step after an upload runs b3g_autotune (3 repeats) */
     int broadphase;            /* B3G_BROADPHASE_GRID (0), _LBVH (1) or _AUTO (2), see b3g_set_broadphase */
-    int reserved[1];
+    int pgs_tail_manifolds;    /* PGS with grid-wide colours: the trailing colours of at most this many
+                                  manifolds each are solved by one block, one grid barrier for all of
+                                  them (0 = 1024; 1 effectively turns it off) */
 } b3gConfig;
 
 /* Per-step counters, copied once per step from the device. */
@@ -135,6 +137,14 @@ b3gStatus b3g_config_default(b3gConfig* cfg);
  * Host registries only; no device memory is touched until b3g_write_all_to_gpu. */
 b3gStatus b3g_create(const b3gConfig* cfg, int cuda_device, b3g_handle* out);
 b3gStatus b3g_destroy(b3g_handle h);
+/* b3GpuNarrowPhase::reset (b3GpuNarrowPhase.cpp:946-962) with what = B3G_RESET_SHAPES_AND_BODIES:
+ * every shape and body is dropped (and the device state freed; the next b3g_write_all_to_gpu
+ * uploads afresh); b3GpuRigidBodyPipeline::reset (b3GpuRigidBodyPipeline.cpp:141-147) with
+ * B3G_RESET_CONSTRAINTS: every joint is dropped.  Flags may be combined; the configuration,
+ * device, stream and attached network stay. */
+#define B3G_RESET_SHAPES_AND_BODIES 1
+#define B3G_RESET_CONSTRAINTS 2
+b3gStatus b3g_reset(b3g_handle h, int what);
 /* Text of the last error on this thread. */
 const char* b3g_last_error(void);
 /* Library version string. */
@@ -298,6 +308,12 @@ b3gStatus b3g_step(b3g_handle h, float dt);
 b3gStatus b3g_setup_aabbs(b3g_handle h);                     /* setupGpuAabbsFull :500-575 */
 b3gStatus b3g_calculate_overlapping_pairs(b3g_handle h);     /* b3GpuGridBroadphase::calculateOverlappingPairs :117-259 */
 b3gStatus b3g_compute_contacts(b3g_handle h);                /* b3GpuNarrowPhase::computeContacts :751-809 */
+/* b3GpuNarrowPhase::computeContacts(pairs, numPairs, aabbs, numObjects) (b3GpuNarrowPhase.cpp:751)
+ * on the caller's pairs: d_pairs holds n b3gPair (b3Int4: x, y = body indices) in device memory on
+ * the world's device.  The pairs replace the world's pair list (kept in the canonical (min, max)
+ * order, so the manifolds come out in that order); pairs naming a body outside [0, bodies) or a
+ * body twice are dropped and flag B3G_FLAG_PAIR_OVERFLOW.  Asynchronous on the world's stream. */
+b3gStatus b3g_compute_contacts_for_pairs(b3g_handle h, const void* d_pairs, int n);
 b3gStatus b3g_solve_joints(b3g_handle h);                    /* b3GpuPgsConstraintSolver::solveJoints :927-944 */
 b3gStatus b3g_solve_contacts(b3g_handle h, float dt);        /* b3GpuPgsContactSolver::solveContacts :568-1103 */
 b3gStatus b3g_integrate(b3g_handle h, float dt);             /* b3GpuRigidBodyPipeline::integrate :465-498 */
@@ -414,6 +430,18 @@ b3gStatus b3g_read_warm_samples(b3g_handle h, float* features, float* targets, i
 /* The initial impulses of the last solve, 12 floats per manifold in the b3g_read_impulses layout
  * (per point: normal, lateral 1, lateral 2); zero for a cold start. */
 b3gStatus b3g_read_warm_start(b3g_handle h, float* host, int capacity_manifolds, int* num);
+
+/* ---- device buffers of the C++ layer's b3OpenCLArray ----------------------------------------------
+ * The reference's b3OpenCLArray (Bullet3OpenCL/ParallelPrimitives/b3OpenCLArray.h:39-300) wraps
+ * clCreateBuffer / clEnqueueWriteBuffer / clEnqueueReadBuffer / clEnqueueCopyBuffer; these three
+ * calls are what its CUDA look-alike in include/b3g_compat.h uses, so that header needs no CUDA
+ * headers.  Copies are synchronous; kind: B3G_COPY_H2D, B3G_COPY_D2H or B3G_COPY_D2D. */
+#define B3G_COPY_H2D 0
+#define B3G_COPY_D2H 1
+#define B3G_COPY_D2D 2
+b3gStatus b3g_buffer_alloc(int cuda_device, size_t bytes, void** out);
+b3gStatus b3g_buffer_free(int cuda_device, void* p);
+b3gStatus b3g_buffer_copy(int cuda_device, void* dst, const void* src, size_t bytes, int kind);
 
 /* ---- allocation-free grid broadphase (no counterpart in the reference) -------------------------
  * The uniform-grid pair search of b3g_calculate_overlapping_pairs, run on the current CUDA device

@@ -360,6 +360,38 @@ def ref_integrate(bodies, dt=1 / 60, damping=0.99, gravity=(0.0, -9.8, 0.0)):
     return b
 
 
+def ref_cast_rays(bodies, shapes: Shapes, rays, hits=None):
+    """The reference's b3GpuRaycast::castRaysHost on the given bodies and shape tables."""
+    lib = load_reference()
+    b = np.ascontiguousarray(bodies, BODY)
+    r = np.ascontiguousarray(rays, RAY)
+    h = np.zeros(len(r), RAYHIT) if hits is None else np.array(hits, RAYHIT, copy=True)
+    if hits is None:
+        h["hitFraction"] = 1.0
+        h["hitBody"] = -1
+        h["hitResult2"] = -1
+    lib.ref_cast_rays(_p(r), C.c_int(len(r)), _p(h), _p(b), C.c_int(len(b)), _p(shapes.collidables),
+                      C.c_int(len(shapes.collidables)), _p(shapes.hulls), C.c_int(len(shapes.hulls)),
+                      _p(shapes.faces), C.c_int(len(shapes.faces)))
+    return h
+
+
+def ref_solve_joints(bodies, inertias, joints, iterations=4, dt=1 / 60):
+    """The reference's CPU joint path: b3Point2PointConstraint / b3FixedConstraint rows solved by
+    b3PgsJacobiSolver (PGS, joints only), one solveGroup call; returns the bodies."""
+    lib = load_reference()
+    b = np.array(bodies, BODY, copy=True)
+    I = np.ascontiguousarray(inertias, INERTIA)
+    j = np.ascontiguousarray(joints, JOINT)
+    t = np.ascontiguousarray(j["type"], np.int32)
+    ab = np.ascontiguousarray(np.stack([j["rbA"], j["rbB"]], 1), np.int32)
+    prm = np.ascontiguousarray(np.concatenate([j["pivotInA"][:, :3], j["pivotInB"][:, :3], j["relTargetAB"]], 1),
+                               np.float32)
+    lib.ref_solve_joints(_p(b), _p(I), C.c_int(len(b)), _p(t), _p(ab), _p(prm), C.c_int(len(t)),
+                         C.c_int(iterations), C.c_float(dt))
+    return b
+
+
 def ref_register_body(mass, pos, orn, collidable, local_min, local_max):
     """The reference's body and inertia records for one registerPhysicsInstance call."""
     lib = load_reference()

@@ -12,6 +12,9 @@
 //   b3PgsJacobiSolver::solveGroup                   Bullet3Dynamics/ConstraintSolver/b3PgsJacobiSolver.cpp:170
 //   integrateSingleTransform                        Bullet3Dynamics/shared/b3IntegrateTransforms.h:5
 //   registerPhysicsInstance / registerRigidBody     Bullet3OpenCL/RigidBody/b3GpuRigidBodyPipeline.cpp:603, b3GpuNarrowPhase.cpp:816
+//   b3GpuRaycast::castRaysHost                      Bullet3OpenCL/Raycast/b3GpuRaycast.cpp:175-247
+//   b3Point2PointConstraint / b3FixedConstraint     Bullet3Dynamics/ConstraintSolver/b3Point2PointConstraint.cpp, b3FixedConstraint.cpp
+//     through b3PgsJacobiSolver::solveGroup         (joints only, no contacts)
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -33,7 +36,11 @@
 #include "Bullet3Collision/NarrowPhaseCollision/shared/b3ContactConvexConvexSAT.h"
 #include "Bullet3Dynamics/ConstraintSolver/b3PgsJacobiSolver.h"
 #include "Bullet3Dynamics/ConstraintSolver/b3ContactSolverInfo.h"
+#include "Bullet3Dynamics/ConstraintSolver/b3Point2PointConstraint.h"
+#include "Bullet3Dynamics/ConstraintSolver/b3FixedConstraint.h"
 #include "Bullet3Dynamics/shared/b3IntegrateTransforms.h"
+#include "Bullet3OpenCL/Raycast/b3GpuRaycast.h"
+#include "Bullet3OpenCL/RigidBody/b3GpuNarrowPhaseInternalData.h"
 
 void computeContactPlaneConvex(int pairIndex, int bodyIndexA, int bodyIndexB, int collidableIndexA,
                                int collidableIndexB, const b3RigidBodyData* rigidBodies,
@@ -248,6 +255,62 @@ void ref_register_body(float mass, const float* position, const float* orientati
         b3Matrix3x3 m(body->m_quat);
         inertia->m_invInertiaWorld = m.scaled(invLocalInertia) * m.transpose();
     }
+}
+
+// b3GpuRaycast::castRaysHost (b3GpuRaycast.cpp:175-247), the reference's CPU twin of its ray
+// kernels: every body in index order, spheres by sphere_intersect, hulls by rayConvex in the
+// body's frame.  It reads no member of the b3GpuRaycast object (whose constructor compiles
+// OpenCL programs), so it is called on uninitialised storage of the class; of the narrowphase
+// data it reads the hull records and faces only.  hits: in/out (hitFraction is the bound).
+void ref_cast_rays(const b3RayInfo* rays, int nrays, b3RayHit* hits, const b3RigidBodyData* bodies, int nbodies,
+                   const b3Collidable* cols, int ncols, const b3ConvexPolyhedronData* hulls, int nhulls,
+                   const b3GpuFace* faces, int nfaces) {
+    b3AlignedObjectArray<b3RayInfo> r;
+    b3AlignedObjectArray<b3RayHit> h;
+    for (int i = 0; i < nrays; i++) {
+        r.push_back(rays[i]);
+        h.push_back(hits[i]);
+    }
+    b3GpuNarrowPhaseInternalData* npd = new b3GpuNarrowPhaseInternalData();
+    for (int i = 0; i < nhulls; i++) npd->m_convexPolyhedra.push_back(hulls[i]);
+    for (int i = 0; i < nfaces; i++) npd->m_convexFaces.push_back(faces[i]);
+    alignas(16) static unsigned char storage[sizeof(b3GpuRaycast)];
+    reinterpret_cast<b3GpuRaycast*>(storage)->castRaysHost(r, h, nbodies, bodies, ncols, cols, npd);
+    for (int i = 0; i < nrays; i++) hits[i] = h[i];
+    delete npd;
+}
+
+// Joints through the reference's CPU constraint classes and b3PgsJacobiSolver (PGS, no
+// contacts): type 3 = b3Point2PointConstraint(a, b, pivotInA, pivotInB), type 4 =
+// b3FixedConstraint(a, b, frameInA = (identity, pivotInA), frameInB = (inverse(relTargetAB),
+// pivotInB)) so that its m_relTargetAB equals the given one.  spec per joint: type, a, b, then
+// pivotInA xyz, pivotInB xyz, relTargetAB xyzw (10 floats after the 3 ints, as floats).
+void ref_solve_joints(b3RigidBodyData* bodies, b3InertiaData* inertias, int nbodies, const int* types, const int* ab,
+                      const float* params, int njoints, int iterations, float dt) {
+    b3AlignedObjectArray<b3TypedConstraint*> cons;
+    for (int j = 0; j < njoints; j++) {
+        const float* p = params + 10 * j;
+        b3Vector3 pa = b3MakeVector3(p[0], p[1], p[2]), pb = b3MakeVector3(p[3], p[4], p[5]);
+        if (types[j] == 3) {
+            cons.push_back(new b3Point2PointConstraint(ab[2 * j], ab[2 * j + 1], pa, pb));
+        } else {
+            b3Transform fa, fb;
+            fa.setIdentity();
+            fa.setOrigin(pa);
+            fb.setIdentity();
+            fb.setOrigin(pb);
+            fb.setRotation(b3Quaternion(p[6], p[7], p[8], p[9]).inverse());
+            cons.push_back(new b3FixedConstraint(ab[2 * j], ab[2 * j + 1], fa, fb));
+        }
+    }
+    b3PgsJacobiSolver solver(true);
+    b3ContactSolverInfo info;
+    info.m_solverMode = B3_SOLVER_USE_2_FRICTION_DIRECTIONS | B3_SOLVER_SIMD;
+    info.m_splitImpulse = false;
+    info.m_numIterations = iterations;
+    info.m_timeStep = dt;
+    solver.solveGroup(bodies, inertias, nbodies, 0, 0, njoints ? &cons[0] : 0, njoints, info);
+    for (int j = 0; j < cons.size(); j++) delete cons[j];
 }
 
 int ref_sizeof(int which) {

@@ -20,7 +20,15 @@ Fixtures:
                   clouds, clouds with repeated points) and registerPhysicsInstance body / inertia
                   records of 400 bodies (the reference's b3TransformAabb and b3Matrix3x3)
 
-  python tests/golden/make_golden.py [registration]   (no argument: every fixture)
+  rays.npz        b3GpuRaycast::castRaysHost hits of 3,000 rays over a plane and 240 rotated boxes and
+                  Gaussian hulls (no spheres: the host twin's sphere case falls through into its
+                  hull case, b3GpuRaycast.cpp:196-207, which the ray kernels do not do)
+
+  joints.npz      120 independent joints (ball and fixed, one or both bodies dynamic, random pivots,
+                  poses and velocities), each solved alone by the reference's b3PgsJacobiSolver over
+                  b3Point2PointConstraint / b3FixedConstraint rows (4 iterations, dt 1/60)
+
+  python tests/golden/make_golden.py [registration|rays|joints]   (no argument: every fixture)
 """
 from __future__ import annotations
 
@@ -310,11 +318,104 @@ def registration_fixture():
     print("registration", len(clouds), "hulls", n, "bodies")
 
 
+def rays_fixture():
+    """rays.npz: the reference's host ray cast over rotated boxes and Gaussian hulls on a plane."""
+    rng = np.random.Generator(np.random.PCG64(91))
+    tb = TableBuilder()
+    plane = tb.plane((0.0, 1.0, 0.0), 0.0)
+    body_shape, mass = [plane], [0.0]
+    n = 240
+    for i in range(n):
+        if i % 3 == 2:
+            body_shape.append(tb.hull((rng.standard_normal((int(rng.integers(12, 33)), 3)) * 0.4).astype(np.float32)))
+        else:
+            body_shape.append(tb.hull(box_vertices(rng.uniform(0.2, 0.8, 3))))
+        mass.append(1.0)
+    pos = np.vstack([np.zeros((1, 3)), rng.uniform([-10, 0.5, -10], [10, 6, 10], (n, 3))]).astype(np.float32)
+    q = rng.standard_normal((n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    orn = np.vstack([np.array([[0, 0, 0, 1]]), q]).astype(np.float32)
+    shapes = tb.shapes()
+    bodies, inertias = make_bodies(shapes, body_shape, mass, pos, orn)
+    nr = 3000
+    rays = np.zeros(nr, O.RAY)
+    f = rng.uniform([-11, 0, -11], [11, 7, 11], (nr, 3)).astype(np.float32)
+    t = f.copy()
+    down = np.arange(nr) < nr // 2
+    f[down, 1] = 12.0
+    t[down, 1] = -1.0
+    d = rng.standard_normal(((~down).sum(), 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    t[~down] = (f[~down] + d * rng.uniform(2.0, 25.0, ((~down).sum(), 1))).astype(np.float32)
+    rays["from"][:, :3] = f
+    rays["to"][:, :3] = t
+    hits = O.ref_cast_rays(bodies, shapes, rays)
+    out = dict(bodies=bodies, rays=rays, hits=hits)
+    for k in ("collidables", "local_aabbs", "hulls", "faces", "indices", "verts", "edges"):
+        out["shape_" + k] = getattr(shapes, k)
+    np.savez_compressed(OUT / "rays.npz", **out)
+    print("rays", nr, "rays", int((hits["hitBody"] >= 0).sum()), "hits")
+
+
+def joints_fixture():
+    """joints.npz: single joints solved by the reference's CPU constraint classes."""
+    rng = np.random.Generator(np.random.PCG64(123))
+
+    def quat(scale=None):
+        if scale is None:
+            x = rng.standard_normal(4)
+            return (x / np.linalg.norm(x)).astype(np.float32)
+        a = rng.uniform(-scale, scale, 3)
+        t = np.linalg.norm(a)
+        return np.concatenate([np.sin(t / 2) * a / t, [np.cos(t / 2)]]).astype(np.float32)
+
+    reg = O.Registry()
+    box = reg.convex_hull(box_vertices([0.5, 0.4, 0.3]))
+    n = 120
+    joints = np.zeros(n, O.JOINT)
+    for k in range(n):
+        static_a = k % 4 == 0
+        reg.body(0.0 if static_a else float(rng.uniform(0.5, 3.0)), rng.uniform(-1, 1, 3), quat(), box)
+        reg.body(float(rng.uniform(0.5, 3.0)), rng.uniform(-1, 1, 3), quat(), box)
+        j = joints[k]
+        j["type"] = 3 if k % 2 == 0 else 4
+        j["rbA"], j["rbB"] = 2 * k, 2 * k + 1
+        j["breakingImpulseThreshold"] = 1e30
+        j["flags"] = 1
+        j["uid"] = k
+        j["pivotInA"][:3] = rng.uniform(-0.6, 0.6, 3)
+        j["pivotInB"][:3] = rng.uniform(-0.6, 0.6, 3)
+        j["relTargetAB"] = [0, 0, 0, 1] if k % 6 != 3 else quat(0.3)
+    t = reg.tables()
+    bodies, inertias = t["bodies"], t["inertias"]
+    dyn = bodies["invMass"] != 0
+    bodies["linVel"][:, :3] = rng.standard_normal((len(bodies), 3)) * dyn[:, None]
+    bodies["angVel"][:, :3] = rng.standard_normal((len(bodies), 3)) * dyn[:, None]
+    out = bodies.copy()
+    for k in range(n):  # each joint alone: its two bodies and nothing else
+        sub = bodies[2 * k:2 * k + 2].copy()
+        jj = joints[k:k + 1].copy()
+        jj["rbA"], jj["rbB"] = 0, 1
+        out[2 * k:2 * k + 2] = O.ref_solve_joints(sub, inertias[2 * k:2 * k + 2], jj)
+    shapes = t
+    res = dict(bodies=bodies, inertias=inertias, joints=joints, solved=out)
+    for k in ("collidables", "local_aabbs", "hulls", "faces", "indices", "verts", "edges"):
+        res["shape_" + k] = shapes[k]
+    np.savez_compressed(OUT / "joints.npz", **res)
+    print("joints", n)
+
+
 if __name__ == "__main__":
+    if O.load_reference() is None:
+        raise SystemExit("oracle/_ref/libb3ref.so is missing: run oracle/build_ref.sh first")
     if len(sys.argv) > 1 and sys.argv[1] == "registration":
-        if O.load_reference() is None:
-            raise SystemExit("oracle/_ref/libb3ref.so is missing: run oracle/build_ref.sh first")
         registration_fixture()
+    elif len(sys.argv) > 1 and sys.argv[1] == "rays":
+        rays_fixture()
+    elif len(sys.argv) > 1 and sys.argv[1] == "joints":
+        joints_fixture()
     else:
         main()
         registration_fixture()
+        rays_fixture()
+        joints_fixture()

@@ -172,3 +172,24 @@ def test_edge_joints_static_pair_and_zero_threshold():
     assert flags[u_zero] == 0 and flags[u_static] == 1
     b = np_.readbackAllBodiesToCpu()
     assert np.array_equal(b["linVel"][[anchor, ground]], np.zeros((2, 4), np.float32))
+
+
+def test_joint_stage_matches_reference_constraint_classes():
+    # 120 independent joints (ball and fixed; static or dynamic first body) against the reference's
+    # own b3Point2PointConstraint / b3FixedConstraint rows solved by b3PgsJacobiSolver, each joint
+    # alone (golden vectors); and bit for bit against the oracle
+    from conftest import load_golden
+    from gpu_helpers import scene_from_golden
+    from test_oracle_golden import _joints_close
+    g = load_golden("joints")
+    np_, bp, pl, shapes = load(scene_from_golden(g))
+    np_.writeBodiesToGpu(g["bodies"])
+    for j in g["joints"]:
+        if j["type"] == capi.JOINT_POINT2POINT:
+            pl.createPoint2PointConstraint(int(j["rbA"]), int(j["rbB"]), j["pivotInA"], j["pivotInB"], 1e30)
+        else:
+            pl.createFixedConstraint(int(j["rbA"]), int(j["rbB"]), j["pivotInA"], j["pivotInB"], j["relTargetAB"],
+                                     1e30)
+    gj = _stage_step(np_, pl)
+    _joints_close(np_.readbackAllBodiesToCpu(), g["solved"])
+    assert (gj["flags"] == 1).all()

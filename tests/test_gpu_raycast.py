@@ -115,3 +115,22 @@ def test_device_buffers_give_the_host_call_hits():
     pl.synchronize()
     dev = d_hits.cpu().numpy().view(capi.RAYHIT)
     assert np.array_equal(dev.view(np.uint8), host.view(np.uint8))
+
+
+def test_rays_match_reference_host_twin():
+    # the golden hits of the reference's own b3GpuRaycast::castRaysHost (rotated boxes and Gaussian
+    # hulls on a plane, reference hull tables): same hit bodies and faces, fractions within the
+    # tolerance the host twin's matrix transform allows; and bit for bit the oracle's
+    from conftest import load_golden, shapes_from
+    from gpu_helpers import scene_from_golden
+    from test_oracle_golden import _ray_close
+    g = load_golden("rays")
+    sc = scene_from_golden(g)
+    np_, bp, pl, shapes = load(sc)
+    b = np_.readbackAllBodiesToCpu()
+    assert np.array_equal(b["pos"], g["bodies"]["pos"]) and np.array_equal(b["quat"], g["bodies"]["quat"])
+    hits = pl.castRays(g["rays"])
+    hit = _ray_close(hits, g["hits"], g["rays"])
+    assert hit.sum() > 1000
+    o = O.cast_rays(b, shapes_from(g), g["rays"])
+    assert np.array_equal(hits["hitFraction"], o["hitFraction"]) and np.array_equal(hits["hitBody"], o["hitBody"])

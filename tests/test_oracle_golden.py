@@ -143,3 +143,40 @@ def test_body_registration_bitexact():
     t["bodies"]["collidableIdx"] = 3  # the fixture registers every body with collidable 3
     assert t["bodies"].tobytes() == g["bodies"].tobytes()
     assert t["inertias"].tobytes() == g["inertias"].tobytes()
+
+
+def _ray_close(mine, ref, rays):
+    """Hits of the ray kernels against the reference's host twin b3GpuRaycast::castRaysHost: the
+    same rays hit the same bodies (the same faces: equal normals within 1 ulp); the twin moves each
+    ray into the body's frame with b3Transform::inverse, the kernels with quaternion rotations, so
+    fractions agree within 4e-6 and hit points within 4e-6 of the ray length."""
+    hit = ref["hitBody"] >= 0
+    assert np.array_equal(mine["hitBody"], ref["hitBody"])
+    assert np.abs(mine["hitFraction"][hit] - ref["hitFraction"][hit]).max() <= 4e-6
+    assert np.abs(mine["hitNormal"][hit] - ref["hitNormal"][hit]).max() <= 2.5e-7
+    length = np.linalg.norm(rays["to"][:, :3] - rays["from"][:, :3], axis=1)[hit]
+    assert (np.abs(mine["hitPoint"][hit, :3] - ref["hitPoint"][hit, :3]).max(1) <= 4e-6 * length + 1e-6).all()
+    return hit
+
+
+def test_rays_match_reference_host_twin():
+    g = load_golden("rays")
+    o = O.cast_rays(g["bodies"], shapes_from(g), g["rays"])
+    hit = _ray_close(o, g["hits"], g["rays"])
+    assert hit.sum() > 1000
+
+
+def _joints_close(mine, ref):
+    """One joint stage against the reference's CPU constraint classes solved by b3PgsJacobiSolver:
+    the velocities agree within 1e-5 of max(|v|, 1) (the CPU rows round a few operations
+    differently from the joint kernels the oracle and the GPU follow; measured 3.1e-6)."""
+    for f in ("linVel", "angVel"):
+        d = np.abs(mine[f][:, :3] - ref[f][:, :3])
+        assert (d <= 1e-5 * np.maximum(np.abs(ref[f][:, :3]), 1.0)).all(), (f, d.max())
+
+
+def test_joints_match_reference_constraint_classes():
+    g = load_golden("joints")
+    ob, oj = O.solve_joints(g["bodies"], g["inertias"], g["joints"])
+    _joints_close(ob, g["solved"])
+    assert (oj["flags"] == 1).all()
