@@ -47,14 +47,27 @@ def build_oracle(force: bool = False) -> Path:
 
 
 def build_reference(ref_root: str | None) -> Path | None:
-    """oracle/_ref/libb3ref.so from the reference sources under ref_root (None or absent: skipped)."""
+    """oracle/_ref/libb3ref.so from the reference sources under ref_root (None or absent: skipped),
+    and oracle/_ref/source_root naming that root."""
     if not ref_root or not Path(ref_root, "src", "Bullet3Common").is_dir():
         return None
     out = HERE / "_ref" / "libb3ref.so"
+    out.parent.mkdir(exist_ok=True)
+    # where the reference's sources were found (tests that read them look here)
+    (HERE / "_ref" / "source_root").write_text(str(Path(ref_root).resolve()))
     if out.exists() and out.stat().st_mtime > (HERE / "ref_shim.cpp").stat().st_mtime:
         return out
     _run(["bash", str(HERE / "build_ref.sh"), ref_root])
     return out
+
+
+def reference_root() -> Path | None:
+    """The reference source root the last build_reference used, when it is still present."""
+    p = HERE / "_ref" / "source_root"
+    if not p.exists():
+        return None
+    root = Path(p.read_text().strip())
+    return root if (root / "src" / "Bullet3Common").is_dir() else None
 
 
 if __name__ == "__main__":

@@ -142,7 +142,8 @@ def test_scene_offsets_validation():
 
 
 def test_cpp_dropin_header_compiles(tmp_path):
-    # the C++ classes of include/b3g_compat.h compile on their own against the public headers
+    # the C++ classes of include/b3g_compat.h compile on their own against the public headers, with
+    # the reference's constructor and method signatures
     import shutil
     import subprocess
     gxx = shutil.which("g++")
@@ -150,26 +151,162 @@ def test_cpp_dropin_header_compiles(tmp_path):
         pytest.skip("g++ not available")
     src = tmp_path / "use.cpp"
     src.write_text('#include "b3g_compat.h"\n'
-                   "using namespace b3g_compat;\n"
                    "int main() {\n"
-                   "  b3Config c; b3GpuNarrowPhase np(0, c); b3GpuGridBroadphase bp;\n"
-                   "  b3GpuRigidBodyPipeline rbp(&np, &bp, nullptr, c);\n"
+                   "  cl_context ctx = b3gCreateContext(0); cl_device_id dev = b3gGetDevice(ctx);\n"
+                   "  cl_command_queue q = b3gCreateCommandQueue(ctx, dev);\n"
+                   "  b3Config c; b3GpuNarrowPhase np(ctx, dev, q, c); b3GpuGridBroadphase bp(ctx, dev, q);\n"
+                   "  b3DynamicBvhBroadphase dbvt(c.m_maxConvexBodies);\n"
+                   "  b3GpuRigidBodyPipeline rbp(ctx, dev, q, &np, &bp, &dbvt, c);\n"
                    "  int first[2] = {0, 1}; rbp.setSceneOffsets(first, 2);\n"
-                   "  b3GpuBroadphaseInterface::CreateFunc* f = b3GpuSapBroadphase::CreateFunc; delete f(0);\n"
-                   "  f = b3GpuParallelLinearBvhBroadphase::CreateFunc; delete f(0);\n"
-                   "  b3GpuParallelLinearBvhBroadphase lbvh(&np);\n"
-                   "  float p[3], q[4]; np.getObjectTransformFromCpu(p, q, 0); np.setObjectTransformCpu(p, q, 0);\n"
+                   "  b3GpuBroadphaseInterface::CreateFunc* f = b3GpuSapBroadphase::CreateFuncBarrier; delete f(ctx, dev, q);\n"
+                   "  f = b3GpuParallelLinearBvhBroadphase::CreateFunc; delete f(ctx, dev, q);\n"
+                   "  f = b3GpuGridBroadphase::CreateFunc; delete f(ctx, dev, q);\n"
+                   "  b3GpuParallelLinearBvhBroadphase lbvh(ctx, dev, q);\n"
+                   "  float p[3], o[4]; np.getObjectTransformFromCpu(p, o, 0); np.setObjectTransformCpu(p, o, 0);\n"
+                   "  np.registerPlaneShape(b3MakeVector3(0, 1, 0), 0.f);\n"
+                   "  b3ConvexUtility u; b3AlignedObjectArray<b3Vector3> v; v.push_back(b3MakeVector3(0, 0, 0));\n"
+                   "  u.initializePolyhedralFeatures(&v[0], v.size()); np.registerConvexHullShape(&u);\n"
+                   "  rbp.registerConvexPolyhedron(&u);\n"
                    "  bp.calculateOverlappingPairsHost(0); bp.getAllAabbsCPU(); rbp.copyConstraintsToHost();\n"
-                   "  std::vector<b3gRayInfo> rays(2); std::vector<b3gRayHit> hits(2); rbp.castRays(rays, hits);\n"
+                   "  b3OpenCLArray<b3Int4>& pairs = bp.getOverlappingPairsGPU();\n"
+                   "  np.computeContacts(pairs.getBufferCL(), (int)pairs.size(), bp.getAabbBufferWS(), 0);\n"
+                   "  b3AlignedObjectArray<b3RayInfo> rays; b3AlignedObjectArray<b3RayHit> hits; rbp.castRays(rays, hits);\n"
                    "  float pa[3] = {0, 0, 0}, rel[4] = {0, 0, 0, 1};\n"
-                   "  int u = rbp.createPoint2PointConstraint(0, 1, pa, pa, 1e30f);\n"
-                   "  u += rbp.createFixedConstraint(0, 1, pa, pa, rel, 1e30f); rbp.removeConstraintByUid(u);\n"
-                   "  u += (int)rbp.getConstraintsCPU().size();\n"
-                   "  rbp.stepSimulation(1.f / 60.f); return rbp.getNumBodies();\n"
+                   "  int id = rbp.createPoint2PointConstraint(0, 1, pa, pa, 1e30f);\n"
+                   "  id += rbp.createFixedConstraint(0, 1, pa, pa, rel, 1e30f); rbp.removeConstraintByUid(id);\n"
+                   "  rbp.reset(); np.reset(); const b3Contact4* cc = np.getContactsCPU(); (void)cc;\n"
+                   "  b3Quaternion orn(0, 0, 0, 1); rbp.registerPhysicsInstance(1.f, b3MakeVector3(0, 1, 0), orn, 0, 0, false);\n"
+                   "  rbp.stepSimulation(1.f / 60.f); b3gRelease(q); b3gRelease(dev); b3gRelease(ctx);\n"
+                   "  return rbp.getNumBodies();\n"
                    "}\n")
     r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-Wall", "-I", str(Path(ROOT, "include")), str(src)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+# The physics parts of the reference's own GPU rigid-body demos, read from the reference's sources
+# when they are on this machine (they are not part of this repository): the pipeline construction
+# of GpuRigidBodyDemo::initPhysics, the scene setup of GpuConvexScene::createDynamicsObjects2 and
+# the step of GpuRigidBodyDemo::stepSimulation.
+DEMO_SNIPPETS = [
+    ("examples/OpenCL/rigidbody/GpuRigidBodyDemo.cpp", "m_data->m_config.m_maxConvexBodies = b3Max(",
+     "bp->writeAabbsToGpu();"),
+    ("examples/OpenCL/rigidbody/GpuConvexScene.cpp",
+     "int shapeId = m_guiHelper->getRenderInterface()->registerShape(&vertices[0], numVertices, indices, "
+     "numIndices, B3_GL_TRIANGLES, textureIndex);", "return index;"),
+    ("examples/OpenCL/rigidbody/GpuRigidBodyDemo.cpp", "m_data->m_rigidBodyPipeline->stepSimulation(1. / 60.f);",
+     "m_data->m_rigidBodyPipeline->stepSimulation(1. / 60.f);"),
+]
+
+DEMO_HARNESS = r"""
+#include <cstdio>
+#include "b3g_compat.h"
+// stand-ins for the demo framework's renderer, its state and its globals
+#define B3_GL_TRIANGLES 1
+#define b3Assert(x) ((void)0)
+struct RenderInterface {
+    int registerShape(const float*, int, const int*, int, int, int) { return 0; }
+    int registerGraphicsInstance(int, const float*, const float*, const float*, const float*) { return 0; }
+};
+struct GuiHelper {
+    RenderInterface r;
+    RenderInterface* getRenderInterface() { return &r; }
+};
+struct ClData {
+    cl_context m_clContext;
+    cl_device_id m_clDevice;
+    cl_command_queue m_clQueue;
+};
+struct DemoData {
+    b3Config m_config;
+    b3GpuNarrowPhase* m_np = nullptr;
+    b3GpuBroadphaseInterface* m_bp = nullptr;
+    b3DynamicBvhBroadphase* m_broadphaseDbvt = nullptr;
+    b3GpuRigidBodyPipeline* m_rigidBodyPipeline = nullptr;
+};
+static bool gUseInstancedCollisionShapes = true;
+static bool useUniformGrid = true;
+static int gGpuArraySizeX = 4, gGpuArraySizeY = 4, gGpuArraySizeZ = 4;
+static b3Vector4 colors[4] = {b3MakeVector4(1, 0, 0, 1), b3MakeVector4(0, 1, 0, 1), b3MakeVector4(0, 0, 1, 1),
+                              b3MakeVector4(0, 1, 1, 1)};
+struct Demo {
+    GuiHelper guiHelper;
+    GuiHelper* m_guiHelper = &guiHelper;
+    ClData clData;
+    ClData* m_clData = &clData;
+    DemoData data;
+    DemoData* m_data = &data;
+    void setupScene() {}
+    void initPhysics() {
+@@INIT@@
+    }
+    int createDynamicsObjects2(const float* vertices, int numVertices, const int* indices, int numIndices,
+                               int strideInBytes, int textureIndex) {
+@@SCENE@@
+    }
+    void stepSimulation() {
+@@STEP@@
+    }
+};
+int main(int argc, char**) {
+    Demo d;
+    d.clData.m_clContext = b3gCreateContext(0);
+    d.clData.m_clDevice = b3gGetDevice(d.clData.m_clContext);
+    d.clData.m_clQueue = b3gCreateCommandQueue(d.clData.m_clContext, d.clData.m_clDevice);
+    const float cube[8 * 9] = {
+        -1, -1, -1, 1, 0, 0, 0, 0, 0,  1, -1, -1, 1, 0, 0, 0, 0, 0,  -1, 1, -1, 1, 0, 0, 0, 0, 0,
+        1, 1, -1, 1, 0, 0, 0, 0, 0,    -1, -1, 1, 1, 0, 0, 0, 0, 0,  1, -1, 1, 1, 0, 0, 0, 0, 0,
+        -1, 1, 1, 1, 0, 0, 0, 0, 0,    1, 1, 1, 1, 0, 0, 0, 0, 0};
+    const int idx[3] = {0, 1, 2};
+    if (argc > 1) {  // with a GPU: construct, set up, upload and step
+        d.initPhysics();
+        int n = d.createDynamicsObjects2(cube, 8, idx, 3, 9 * sizeof(float), 0);
+        d.m_data->m_rigidBodyPipeline->writeAllInstancesToGpu();
+        for (int i = 0; i < 10; i++) d.stepSimulation();
+        std::printf("bodies %d\n", n);
+    }
+    return 0;
+}
+"""
+
+
+def _demo_source():
+    from oracle import build as oracle_build
+    root = oracle_build.reference_root()
+    if root is None:
+        return None
+    parts = []
+    for rel, first, last in DEMO_SNIPPETS:
+        lines = Path(root, rel).read_text().splitlines()
+        i = next(k for k, l in enumerate(lines) if first in l)
+        j = next(k for k in range(i, len(lines)) if last in lines[k])
+        parts.append("\n".join(lines[i:j + 1]))
+    return (DEMO_HARNESS.replace("@@INIT@@", parts[0]).replace("@@SCENE@@", parts[1])
+            .replace("@@STEP@@", parts[2]))
+
+
+def test_reference_demo_physics_code_builds_against_the_dropin(tmp_path):
+    """The reference demos' own pipeline construction, scene setup (hull registration through
+    b3ConvexUtility, registerPhysicsInstance with b3Vector3 / b3Quaternion) and step compile and
+    link, unmodified, against include/b3g_compat.h and libb3gpu.so; only the renderer and the
+    OpenCL context creation are stand-ins.  Skipped where the reference's sources are absent."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    src = _demo_source()
+    if src is None:
+        pytest.skip("the reference's sources are not on this machine")
+    f = tmp_path / "demo.cpp"
+    f.write_text(src)
+    lib_dir = Path(ROOT, "bullet3_gb300")
+    exe = tmp_path / "demo"
+    r = subprocess.run([gxx, "-std=c++17", "-O1", "-I", str(Path(ROOT, "include")), str(f), "-o", str(exe),
+                        "-L", str(lib_dir), "-lb3gpu", f"-Wl,-rpath,{lib_dir}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
 
 
 def test_broadphase_switch_validation_before_upload():
