@@ -8,7 +8,11 @@ stepSimulation: AABBs, grid broadphase, narrowphase, colouring, PGS solve, integ
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload pile|batched|stress]
 
-The line also carries `to_residual` (rank 0, one GPU, pile workload): every PGS solve run to a
+The line also carries `configurations` (rank 0, one GPU, pile workload): the other benchmark
+configurations at full size, device-timed in the same run -- collision at scale (131,072 mixed
+bodies), batched scenes (4,096 scenes) and the million-body pour (1,048,576 bodies, 600 steps).
+
+And `to_residual` (rank 0, one GPU, pile workload): every PGS solve run to a
 1e-4 contact residual, once per warm-start mode (plain = cold start, learned, persistent,
 persistent + learned), with the mean sweeps, solve ms and step ms per step of each, on two
 workloads: the falling 64^3 lattice (spacing 1.1, jitter 0.05) and 512 held-out batched piles.  --workload batched times 4,096
@@ -86,6 +90,9 @@ def parse():
     p.add_argument("--residual-cap", type=int, default=4000)
     p.add_argument("--residual-tol", type=float, default=1e-4)
     p.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
+    p.add_argument("--no-configurations", action="store_true",
+                   help="skip the other configurations (collision at scale, batched scenes, million-body pour)")
+    p.add_argument("--no-pour", action="store_true", help="skip the million-body pour among the other configurations")
     a = p.parse_args()
     if a.steps is None:
         a.steps = 597 if a.workload == "stress" else 30
@@ -368,6 +375,94 @@ def to_residual(args, device):
                                "modes": _residual_modes(piles, args, device, net, 80, 20)}}
 
 
+# ------------------------------------------------------------------------------ other configurations
+def _stage_fracs(acc, N, st, peak):
+    C_, I_, P_ = st.num_contacts, max(1, st.iterations), st.num_pairs
+    stage_bytes = {"aabb": 56 * N, "pairs": 112 * N + 8 * P_, "contacts": 64 * P_ + 88 * C_,
+                   "solve": C_ * (416 + 16 + 24) + 352 * C_ * I_, "integrate": 116 * N}
+    stage_ms = {"aabb": acc[0], "pairs": acc[1], "contacts": acc[2], "solve": acc[4], "integrate": acc[6]}
+    return {k: {"ms": float(v), "frac_of_hbm": (stage_bytes[k] / (v / 1000.0) / 1e9 / peak) if v > 0 else None}
+            for k, v in stage_ms.items()}
+
+
+def _time_config(sc, cfg, device, settle, steps, warm_model=None, profile_steps=2):
+    """Device-timed steps of one configuration: body-steps/s, ms/step, per-stage times after."""
+    import ctypes as C
+
+    import numpy as np
+
+    from bullet3_gb300 import capi, scenes
+    dt = 1.0 / 60.0
+    t_load = time.perf_counter()
+    np_, bp, pl = scenes.load_scene(sc, cfg, device=device)
+    t_load = time.perf_counter() - t_load
+    if warm_model is not None:
+        pl.setWarmStartModel(warm_model)
+    for _ in range(settle):
+        pl.stepSimulation(dt)
+    pl.synchronize()
+    tuning = pl.autotune(dt, repeats=2)
+    h = np_.world.handle
+    pl.status(clear=True)
+    capi.call("b3g_record_event", h, C.c_int(2))
+    for _ in range(steps):
+        pl.stepSimulation(dt)
+    capi.call("b3g_record_event", h, C.c_int(3))
+    ms = C.c_float()
+    capi.call("b3g_event_elapsed", h, C.c_int(2), C.c_int(3), C.byref(ms))
+    pl.synchronize()
+    status = pl.status()
+    pl.setProfiling(True)
+    acc = np.zeros(7)
+    for _ in range(profile_steps):
+        pl.stepSimulation(dt)
+        acc += pl.stageTimes()
+    pl.setProfiling(False)
+    st = pl.stats()
+    peak, _ = measured_peaks()
+    N = sc.num_bodies
+    out = {"bodies": int(N), "steps_timed": steps, "first_timed_step": settle,
+           "value": N * steps / (ms.value / 1000.0), "unit": "body-steps/s", "ms_per_step": ms.value / steps,
+           "pairs": st.num_pairs, "manifolds": st.num_contacts, "colors": st.num_colors,
+           "stages_after": _stage_fracs(acc / profile_steps, N, st, peak), "device_status": int(status),
+           "registration_s": t_load, "broadphase": "lbvh" if tuning and tuning.get("broadphase") == 1 else "grid"}
+    del np_, bp, pl
+    return out
+
+
+def other_configurations(args, device):
+    """The benchmark's other configurations at full size, device-timed in the same run (graph-captured
+    steps, launch shapes autotuned after the settle): collision at scale (131,072 mixed bodies,
+    steps 3..63 of 64), batched scenes (4,096 scenes, 30 steps after 120 settle steps) and the
+    million-body pour (steps 3..599 of 600, PGS to 1e-4 with a 16-sweep cap, persistent + learned
+    warm start)."""
+    from bullet3_gb300 import capi, scenes
+    from bullet3_gb300.pipeline import b3Config
+    out = {}
+    sc = scenes.mixed_scene(131072, extent=64.0, seed=0)
+    cfg = b3Config(solver_mode=capi.SOLVER_PGS, solver_iterations=10, use_cuda_graph=True, pgs_interleave=True,
+                   broadphase=capi.BROADPHASE_AUTO)
+    out["collision_at_scale"] = dict(
+        workload="131,072 bodies (50% boxes, 25% spheres, 25% Gaussian hulls) uniform in a 64^3 box, random "
+                 "orientations, N(0,1) velocities, grid cell 2x the largest AABB extent, PGS 10 iterations",
+        **_time_config(sc, cfg, device, settle=3, steps=61))
+    sc = scenes.batched_piles(args.scenes, seed=0, separate=True)
+    cfg = b3Config(solver_mode=capi.SOLVER_PGS, solver_iterations=10, use_cuda_graph=True, pgs_interleave=True,
+                   broadphase=capi.BROADPHASE_AUTO)
+    out["batched_scenes"] = dict(workload=WORKLOAD_BATCHED.format(n=args.scenes, bodies=sc.num_bodies),
+                                 **_time_config(sc, cfg, device, settle=120, steps=30))
+    if not args.no_pour:
+        from bullet3_gb300.warmstart import DEFAULT_WEIGHTS, WarmStartMLP
+        sc = scenes.stress_container(1048576, seed=0)
+        cfg = b3Config(solver_mode=capi.SOLVER_PGS, solver_iterations=16, residual_tol=1e-4, use_cuda_graph=True,
+                       pgs_interleave=True, warm_start=capi.WARM_PERSISTENT_LEARNED, broadphase=capi.BROADPHASE_AUTO)
+        net = WarmStartMLP.load(DEFAULT_WEIGHTS, device=device)
+        out["million_body_pour"] = dict(
+            workload=WORKLOAD_STRESS.format(bodies=sc.num_bodies, first=3, last=599),
+            **_time_config(sc, cfg, device, settle=3, steps=597, warm_model=net))
+    return out
+
+
 # ------------------------------------------------------------------------------ GPU arm
 def gpu_arm(args):
     import ctypes as C
@@ -514,9 +609,13 @@ def gpu_arm(args):
 
     # ---- learned vs plain: sweeps and ms per step to the residual target (rank 0, one GPU)
     residual = None
-    if rank == 0 and world == 1 and args.workload == "pile" and args.residual_steps > 0:
+    configurations = None
+    if rank == 0 and world == 1 and args.workload == "pile":
         del np_, bp, pl
-        residual = to_residual(args, local)
+        if args.residual_steps > 0:
+            residual = to_residual(args, local)
+        if not args.no_configurations:
+            configurations = other_configurations(args, local)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world, "steps": args.steps,
@@ -526,7 +625,8 @@ def gpu_arm(args):
                 "workload_stats": {"pairs": P_, "manifolds": C_, "contact_points": st.num_points,
                                    "colors": st.num_colors, "tuning": tuning},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-                "clocks": clk, "stages": stages, "device_status": int(status), "to_residual": residual}
+                "clocks": clk, "stages": stages, "device_status": int(status), "to_residual": residual,
+                "configurations": configurations}
         print(json.dumps(line), flush=True)
     dist_barrier(dist)
     return 0

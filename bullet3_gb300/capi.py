@@ -65,7 +65,7 @@ class b3gConfig(C.Structure):
                 ("use_cuda_graph", C.c_int), ("warm_start", C.c_int), ("barrier_spin_limit", C.c_int),
                 ("solver_blocks_per_sm", C.c_int), ("pgs_partitions", C.c_int), ("pgs_interleave", C.c_int),
                 ("warm_start_max_points", C.c_int), ("autotune", C.c_int), ("broadphase", C.c_int),
-                ("pgs_tail_manifolds", C.c_int)]
+                ("pgs_tail_manifolds", C.c_int), ("pgs_flow", C.c_int), ("reserved", C.c_int * 3)]
 
 
 class b3gTuning(C.Structure):

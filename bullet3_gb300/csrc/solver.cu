@@ -103,6 +103,8 @@ struct SolverArgs {
     int body_bits;
     int tail_max;                 // trailing colours of at most this many manifolds run in one block
     GridBarrier bar2;             // barrier of k_colour (separate counters from the sweeps')
+    unsigned long long* flow_mask;  // per body: the colours of its manifolds (exact, from k_colour)
+    unsigned int* version;        // per body: manifold updates applied so far in this solve (k_pgs_flow)
 };
 
 // b3PlaneSpace1 (Bullet3Common/b3Vector3.h:1184-1212)
@@ -180,13 +182,7 @@ __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
         // getContactPoint: normalised normal
         v3 n = normalize3(mk3(c.worldNormalOnB.x, c.worldNormalOnB.y, c.worldNormalOnB.z));
         out.nf[k] = f4(n, fric);
-        if (ordered) {
-            // both inverse inertias next to the record, so that the sweeps read them by position
-            float4* o = a.inertia_ord + 6 * (size_t)k;
-            o[0] = f4v(IA.row[0]); o[1] = f4v(IA.row[1]); o[2] = f4v(IA.row[2]);
-            o[3] = f4v(IB.row[0]); o[4] = f4v(IB.row[1]); o[5] = f4v(IB.row[2]);
-            a.inv_mass_ord[k] = make_float4(imA, imB, 0.f, 0.f);
-        }
+        if (ordered) a.inv_mass_ord[k] = make_float4(imA, imB, 0.f, 0.f);
         for (int j = 0; j < np; j++) {
             const float dist = c.worldPosB[j].w;
             if (!(dist <= a.threshold)) continue;
@@ -197,6 +193,7 @@ __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
             const v3 pos1 = pos2 + n * dist;
             const v3 rel1 = pos1 - posA;
             const v3 rel2 = pos2 - posB;
+            v3 ang[6];  // angular components: contact A / B, dir2 A / B, dir1 A / B
             // contact row (setupContactConstraint)
             {
                 v3 torqueAxis0 = cross3(rel1, n);
@@ -221,6 +218,8 @@ __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
                 float rhs = positionalError * scaled + velocityError * scaled;
                 out.rel1[s] = f4(rel1, jac);
                 out.rel2[s] = f4(rel2, rhs);
+                ang[0] = angCompA;
+                ang[1] = angCompB;
             }
             // friction rows (convertContact: dir2 row first, then dir1)
             {
@@ -258,11 +257,21 @@ __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
                     float velocityError = 0.0f - rv;
                     jacs[k] = jac;
                     rhss[k] = velocityError * scaled;
+                    ang[2 + 2 * k] = angCompA;
+                    ang[3 + 2 * k] = angCompB;
                 }
                 out.dir2[s] = f4(dir2, jacs[0]);
                 out.dir1[s] = f4(dir1, jacs[1]);
                 out.rhsf[s] = make_float2(rhss[0], rhss[1]);
                 out.imp[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (ordered) {
+                    // the sweeps' angular components, computed above with their operations
+                    out.angP[s] = make_float4(ang[0].x, ang[0].y, ang[0].z, ang[2].x);
+                    out.angQ[s] = make_float4(ang[1].x, ang[1].y, ang[1].z, ang[2].y);
+                    out.angR[s] = make_float4(ang[2].z, ang[3].x, ang[3].y, ang[3].z);
+                    out.angS[s] = make_float4(ang[4].x, ang[4].y, ang[4].z, ang[5].x);
+                    out.angT[s] = make_float2(ang[5].y, ang[5].z);
+                }
                 if (a.ws_features && sf < (size_t)a.ws_rows_cap) {
                     // warm-start features of this point (the network's input layout)
                     float* f = a.ws_features + sf * 12;
@@ -276,10 +285,29 @@ __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
                 }
             }
         }
-        if (ordered)
-            a.hdr_ord[k] = make_int4(iA, iB, mask, -1);
-        else
+        if (ordered) {
+            // the dataflow sweeps' per-body update numbers, packed: for each dynamic body its
+            // manifolds' colour count (7 bits) and the rank of this manifold's colour among them
+            // (6 bits); A in the low 13 bits, B in the next 13
+            unsigned flow = 0;
+            if (a.flow_mask) {
+                const int c = __ldcg(&a.color[m]);
+                if (c >= 0) {
+                    const unsigned long long below = (1ull << c) - 1ull;
+                    if (imA != 0.f) {
+                        const unsigned long long cm = __ldcg(&a.flow_mask[iA]);
+                        flow |= (unsigned)__popcll(cm) | ((unsigned)__popcll(cm & below) << 7);
+                    }
+                    if (imB != 0.f) {
+                        const unsigned long long cm = __ldcg(&a.flow_mask[iB]);
+                        flow |= ((unsigned)__popcll(cm) | ((unsigned)__popcll(cm & below) << 7)) << 13;
+                    }
+                }
+            }
+            a.hdr_ord[k] = make_int4(iA, iB, mask, (int)flow);
+        } else {
             a.hdr[m] = make_int4(iA, iB, mask, np);
+        }
     }
 }
 
@@ -506,6 +534,121 @@ __device__ __forceinline__ void solve_manifold(const SolverPoints& sp, int m, fl
     }
 }
 
+// ---- one manifold of the colour-ordered records (k_pgs_sweeps, k_pgs_flow): the rows of
+// solve_manifold with the angular components (inverse inertia x relpos x axis) read from the
+// setup's precomputation, which used the same operations on the same values, so every row sees
+// the same numbers bit for bit.  Points stream through two register sets: the records of point
+// j + 1 are loaded while point j solves.
+struct OrdPoint {
+    float4 r1, r2, im, P, Q;  // rel_pos1 + jac, rel_pos2 + rhs, impulses, contact angular A / B (+ dir2 A.xy)
+    float4 d2, d1, R, S;      // friction directions + jacs, remaining angular components
+    float2 rf, T;
+};
+
+__device__ __forceinline__ void ld_point(const SolverPoints& sp, size_t s, int pass, OrdPoint& p) {
+    p.r1 = __ldcg(&sp.rel1[s]);
+    p.r2 = __ldcg(&sp.rel2[s]);
+    p.im = __ldcg(&sp.imp[s]);
+    p.P = __ldcg(&sp.angP[s]);
+    p.Q = __ldcg(&sp.angQ[s]);
+    if (pass != 0) {
+        p.d2 = __ldcg(&sp.dir2[s]);
+        p.d1 = __ldcg(&sp.dir1[s]);
+        p.rf = __ldcg(&sp.rhsf[s]);
+        p.R = __ldcg(&sp.angR[s]);
+        p.S = __ldcg(&sp.angS[s]);
+        p.T = __ldcg(&sp.angT[s]);
+    }
+}
+
+__device__ __forceinline__ void solve_point(const OrdPoint& p, v3 n, float fr, int pass, float4* out, float imA,
+                                            float imB, v3& dlA, v3& daA, v3& dlB, v3& daB, float& res_d,
+                                            float& res_l) {
+    const v3 rel1 = xyz(p.r1), rel2 = xyz(p.r2);
+    const v3 cA = xyz(p.P), cB = xyz(p.Q);
+    const v3 a2 = mk3(p.P.w, p.Q.w, p.R.x), b2 = mk3(p.R.y, p.R.z, p.R.w);
+    const v3 a1 = xyz(p.S), b1 = mk3(p.S.w, p.T.x, p.T.y);
+    if (pass == 3) {
+        // warm start (b3PgsJacobiSolver.cpp:745-752, 815-843), as solve_manifold
+        float w = p.im.x;
+        dlA = dlA + (n * imA) * w;
+        daA = daA + cA * w;
+        dlB = dlB + ((-n) * imB) * w;
+        daB = daB + cB * w;
+        const v3 e2 = xyz(p.d2), e1 = xyz(p.d1);
+        w = p.im.y;
+        dlA = dlA + (e2 * imA) * w;
+        daA = daA + a2 * w;
+        dlB = dlB + ((-e2) * imB) * w;
+        daB = daB + b2 * w;
+        w = p.im.z;
+        dlA = dlA + (e1 * imA) * w;
+        daA = daA + a1 * w;
+        dlB = dlB + ((-e1) * imB) * w;
+        daB = daB + b1 * w;
+        return;
+    }
+    float total = p.im.x;
+    if (pass != 1) {
+        const v3 r1xn = cross3(rel1, n);
+        const v3 r2xn = -cross3(rel2, n);
+        const float old = total;
+        total = solve_row<false>(n, p.r1.w, p.r2.w, old, r1xn, r2xn, cA, cB, 0.f, LARGE_UPPER, dlA, daA, dlB, daB,
+                                 imA, imB);
+        const float nd = total - old;
+        res_d += nd * nd;
+        res_l += total * total;
+        if (pass == 0) {
+            __stcg(&out->x, total);
+            return;
+        }
+    }
+    float f2 = p.im.y, f1 = p.im.z;
+    if (total > 0.f) {
+        const float lower = -(fr * total), upper = fr * total;
+        {
+            const v3 d = xyz(p.d2);
+            const float nw = solve_row<true>(d, p.d2.w, p.rf.x, f2, cross3(rel1, d), cross3(rel2, -d), a2, b2, lower,
+                                             upper, dlA, daA, dlB, daB, imA, imB);
+            const float nd = nw - f2;
+            res_d += nd * nd;
+            f2 = nw;
+        }
+        {
+            const v3 d = xyz(p.d1);
+            const float nw = solve_row<true>(d, p.d1.w, p.rf.y, f1, cross3(rel1, d), cross3(rel2, -d), a1, b1, lower,
+                                             upper, dlA, daA, dlB, daB, imA, imB);
+            const float nd = nw - f1;
+            res_d += nd * nd;
+            f1 = nw;
+        }
+        __stcg(out, make_float4(total, f2, f1, 0.f));
+    } else if (pass == 2) {
+        __stcg(&out->x, total);
+    }
+    res_l += f2 * f2 + f1 * f1;
+}
+
+__device__ __forceinline__ void solve_ord(const SolverPoints& sp, int k, int pass, int mask, float imA, float imB,
+                                          v3& dlA, v3& daA, v3& dlB, v3& daB, float& res_d, float& res_l) {
+    const float4 nf = __ldcg(&sp.nf[k]);
+    const v3 n = xyz(nf);
+    const size_t base = (size_t)k * 4;
+    if (!mask) return;
+    int j = __ffs(mask) - 1;
+    OrdPoint cur, nxt;
+    ld_point(sp, base + j, pass, cur);
+    for (;;) {
+        const int rest = mask & ~((2 << j) - 1);  // points after j
+        const int jn = rest ? __ffs(rest) - 1 : -1;
+        if (jn >= 0) ld_point(sp, base + jn, pass, nxt);
+        solve_point(cur, n, nf.w, pass, sp.imp + base + j, imA, imB, dlA, daA, dlB, daB, res_d, res_l);
+        if (jn < 0) break;
+        cur = nxt;
+        j = jn;
+    }
+}
+
 __device__ __forceinline__ void block_accumulate(double* dst, float x, float y) {
     __shared__ float sx[PK_THREADS / 32], sy[PK_THREADS / 32];
     for (int o = 16; o; o >>= 1) {
@@ -698,6 +841,30 @@ __device__ __forceinline__ void prefetch_records_l2(const SolverArgs& a, int k0,
         bulk_prefetch_l2(a.sp_ord.dir2 + 4 * (size_t)k0, 64u * c);
         bulk_prefetch_l2(a.sp_ord.dir1 + 4 * (size_t)k0, 64u * c);
         bulk_prefetch_l2(a.sp_ord.rhsf + 4 * (size_t)k0, 32u * c);
+    }
+}
+
+// the same for the colour-ordered records of k_setup_rows (angular components in place of the
+// inverse inertias)
+__device__ __forceinline__ void prefetch_ord_l2(const SolverArgs& a, int k0, int cnt, int pass) {
+    if (cnt <= 0) return;
+    const unsigned c = (unsigned)cnt;
+    const size_t p0 = 4 * (size_t)k0;
+    bulk_prefetch_l2(a.hdr_ord + k0, 16u * c);
+    bulk_prefetch_l2(a.inv_mass_ord + k0, 16u * c);
+    bulk_prefetch_l2(a.sp_ord.nf + k0, 16u * c);
+    bulk_prefetch_l2(a.sp_ord.rel1 + p0, 64u * c);
+    bulk_prefetch_l2(a.sp_ord.rel2 + p0, 64u * c);
+    bulk_prefetch_l2(a.sp_ord.imp + p0, 64u * c);
+    bulk_prefetch_l2(a.sp_ord.angP + p0, 64u * c);
+    bulk_prefetch_l2(a.sp_ord.angQ + p0, 64u * c);
+    if (pass) {
+        bulk_prefetch_l2(a.sp_ord.dir2 + p0, 64u * c);
+        bulk_prefetch_l2(a.sp_ord.dir1 + p0, 64u * c);
+        bulk_prefetch_l2(a.sp_ord.rhsf + p0, 32u * c);
+        bulk_prefetch_l2(a.sp_ord.angR + p0, 64u * c);
+        bulk_prefetch_l2(a.sp_ord.angS + p0, 64u * c);
+        bulk_prefetch_l2(a.sp_ord.angT + p0, 32u * c);
     }
 }
 
@@ -1401,7 +1568,7 @@ __global__ void k_warm_store(const int* __restrict__ d_nc, int rows_cap, const i
 // step to step, and a scene whose contact set does not change is coloured once.
 __global__ void __launch_bounds__(SV_THREADS) k_manifold_prep(SolverArgs a) {
     const int nc = *a.d_nc;
-    const int pn = *a.d_prev_n;
+    const int pn = a.d_prev_n[2] ? 0 : a.d_prev_n[0];  // a recolouring carries nothing over
     int fresh = 0;
     for (int m0 = blockIdx.x * blockDim.x; m0 < nc; m0 += gridDim.x * blockDim.x) {
         const int m = m0 + (int)threadIdx.x;
@@ -1522,42 +1689,95 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_colour(SolverArgs a) {
             overflow = r == B3G_MAX_COLORS - 1;
         }
     }
-    // counting sort by colour (64: the manifolds left without one)
-    for (int m0 = tid - (threadIdx.x & 31); m0 < nc; m0 += stride) {
-        const int m = m0 + (threadIdx.x & 31);
-        int key = -1;
-        if (m < nc) {
-            const int c = a.color[m];
-            key = c >= 0 ? c : 64;
+    // the exact colour set of every body (the masks above may hold bits of dropped carried
+    // colours), for the dataflow sweeps; and a stable counting sort by colour (key 64: the
+    // manifolds left without one): block g ranks the contiguous chunk [g*chunk, (g+1)*chunk) of
+    // manifolds, so that within a colour the records keep manifold order -- the order of the
+    // sorted pair list, in which neighbouring manifolds share bodies -- and a warp's manifolds of
+    // consecutive colours lie in the same region
+    const int G = gridDim.x;
+    const int chunk = (nc + G - 1) / G;
+    const int lo = min(nc, blockIdx.x * chunk), hi = min(nc, lo + chunk);
+    int* cb = a.group_counts;        // [key * G + g]: manifolds of key in block g's chunk
+    int* cb_off = cb + 65 * G;       // exclusive scan of cb (key-major)
+    __shared__ int s_cnt[65];
+    __shared__ int s_warp[PK_THREADS / 32][65];
+    for (int k = threadIdx.x; k < 65; k += blockDim.x) s_cnt[k] = 0;
+    __syncthreads();
+    for (int m = lo + threadIdx.x; m < hi; m += blockDim.x) {
+        const int c = a.color[m];
+        if (c >= 0 && a.flow_mask) {
+            const int4 h = a.hdr[m];
+            const float2 im = a.inv_mass[m];
+            if (im.x != 0.f) atomicOr(&a.flow_mask[h.x], 1ull << c);
+            if (im.y != 0.f) atomicOr(&a.flow_mask[h.y], 1ull << c);
         }
-        warp_count(a.color_fill, key);
+        atomicAdd(&s_cnt[c >= 0 ? c : 64], 1);
     }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 65; k += blockDim.x) cb[k * G + blockIdx.x] = s_cnt[k];
     if (!grid_barrier(a.bar2, nb, a.spin_limit)) return;
     if (blockIdx.x == 0) {
-        const int total = block_exclusive_scan(a.color_fill, a.color_goff, 65);
+        const int total = block_exclusive_scan(cb, cb_off, 65 * G);
+        for (int k = threadIdx.x; k < 65; k += blockDim.x) {
+            a.color_goff[k] = cb_off[k * G];
+            a.color_fill[k] = 0;
+            for (int g = 0; g < G; g++) a.color_fill[k] += cb[k * G + g];
+        }
+        __syncthreads();
         if (threadIdx.x == 0) {
             a.color_goff[65] = total;
             int ncl = 0;
             for (int c = 0; c < 64; c++)
-                if (__ldcg(&a.color_fill[c]) > 0) ncl = c + 1;
+                if (a.color_fill[c] > 0) ncl = c + 1;
             a.counters->num_colors = ncl;
-            if (overflow || __ldcg(&a.color_fill[64]) > 0) atomicOr(&a.counters->status, B3G_FLAG_BATCH_OVERFLOW);
+            if (overflow || a.color_fill[64] > 0) atomicOr(&a.counters->status, B3G_FLAG_BATCH_OVERFLOW);
+            // carried colours drift upwards as contacts come and go (a new manifold takes the
+            // smallest colour its bodies leave free): the next solve colours from scratch again
+            // when this one has more than one colour past the last colouring from scratch, and
+            // every 32 solves in any case (so that the baseline follows the scene)
+            if (*((volatile int*)a.d_new) >= nc) {
+                a.d_prev_n[1] = ncl;
+                a.d_prev_n[2] = 0;
+                a.d_prev_n[3] = 0;
+            } else {
+                const int since = ++a.d_prev_n[3];
+                if (ncl > a.d_prev_n[1] + 1 || since >= 32) a.d_prev_n[2] = 1;
+            }
         }
     }
     if (!grid_barrier(a.bar2, nb, a.spin_limit)) return;
-    for (int m0 = tid - (threadIdx.x & 31); m0 < nc; m0 += stride) {
-        const int m = m0 + (threadIdx.x & 31);
-        int key = -1;
-        if (m < nc) {
-            const int c = a.color[m];
-            key = c >= 0 ? c : 64;
+    // positions, in manifold order within each colour: per 512-manifold slice, lane ranks within
+    // the warp (match_any), warp offsets from a per-colour scan over the block's warps
+    __shared__ int s_run[65];
+    for (int k = threadIdx.x; k < 65; k += blockDim.x) s_run[k] = __ldcg(&cb_off[k * G + blockIdx.x]);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nwarps = blockDim.x >> 5;
+    for (int base = lo; base < hi; base += blockDim.x) {
+        for (int i = threadIdx.x; i < nwarps * 65; i += blockDim.x) (&s_warp[0][0])[i] = 0;
+        __syncthreads();
+        const int m = base + (int)threadIdx.x;
+        const int key = m < hi ? (a.color[m] >= 0 ? a.color[m] : 64) : -1;
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        const int rank = __popc(peers & ((1u << lane) - 1u));
+        if (key >= 0 && lane == __ffs(peers) - 1) s_warp[warp][key] = __popc(peers);
+        __syncthreads();
+        for (int k = threadIdx.x; k < 65; k += blockDim.x) {
+            int run = s_run[k];
+            for (int w = 0; w < nwarps; w++) {
+                const int t = s_warp[w][k];
+                s_warp[w][k] = run;
+                run += t;
+            }
+            s_run[k] = run;
         }
-        const int pos = warp_reserve(a.color_cursor, key);
+        __syncthreads();
         if (key >= 0) {
-            const int k = __ldcg(&a.color_goff[key]) + pos;
-            a.color_order[k] = m;
-            a.pos_of[m] = k;
+            const int pos = s_warp[warp][key] + rank;
+            a.color_order[pos] = m;
+            a.pos_of[m] = pos;
         }
+        __syncthreads();
     }
 }
 
@@ -1568,12 +1788,15 @@ __device__ __forceinline__ void sweep_record(const SolverArgs& a, int k, int pas
     v3 dlA = mk3(0, 0, 0), daA = mk3(0, 0, 0), dlB = mk3(0, 0, 0), daB = mk3(0, 0, 0);
     if (im.x != 0.f) load_dv(a, h.x, dlA, daA);
     if (im.y != 0.f) load_dv(a, h.y, dlB, daB);
-    const b3gMat3 IA = ld_mat_cg(a.inertia_ord + 6 * (size_t)k);
-    const b3gMat3 IB = ld_mat_cg(a.inertia_ord + 6 * (size_t)k + 3);
-    solve_manifold<true, false>(a.sp_ord, k, a.sp_ord.imp + 4 * (size_t)k, pass, h, im.x, im.y, IA, IB, dlA, daA,
-                                dlB, daB, res_d, res_l);
+    solve_ord(a.sp_ord, k, pass, h.z, im.x, im.y, dlA, daA, dlB, daB, res_d, res_l);
     if (im.x != 0.f) store_dv(a, h.x, dlA, daA);
     if (im.y != 0.f) store_dv(a, h.y, dlB, daB);
+}
+
+// the same, as a real call: for the rare uncoloured remainder of k_pgs_flow, whose hot loop keeps
+// its registers for the inlined copy
+__device__ __noinline__ void sweep_record_call(const SolverArgs& a, int k, int pass, float& res_d, float& res_l) {
+    sweep_record(a, k, pass, res_d, res_l);
 }
 
 __global__ void __launch_bounds__(PK_THREADS, 1) k_pgs_sweeps(SolverArgs a) {
@@ -1582,6 +1805,9 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_pgs_sweeps(SolverArgs a) {
     const unsigned nb = gridDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int stride = gridDim.x * blockDim.x;
+    // position in a grid-wide colour: warp w of block b takes the 32-manifold groups
+    // (w * gridDim.x + b) + j * (stride / 32), so a colour smaller than the grid spreads over every SM
+    const int ptid = (((int)threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x) * 32 + ((int)threadIdx.x & 31);
     // colour ranges, read once; the trailing run of colours with at most tail_max manifolds each
     // (and the uncoloured remainder) is solved by block 0 alone
     __shared__ int s_off[66];
@@ -1614,12 +1840,12 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_pgs_sweeps(SolverArgs a) {
                     first = s_off[ph];
                     hi = s_off[ph + 1];
                     if (first == hi) continue;  // uniform across blocks
-                    // warm L2 with this block's share of the next grid-wide colour
-                    if (threadIdx.x == 0 && ph + 1 < tail) {
-                        const int k0 = s_off[ph + 1] + blockIdx.x * blockDim.x;
-                        prefetch_records_l2(a, k0, min((int)blockDim.x, s_off[ph + 2] - k0), pass);
+                    // warm L2 with this warp's first group of the next grid-wide colour
+                    if ((threadIdx.x & 31) == 0 && ph + 1 < tail) {
+                        const int k0 = s_off[ph + 1] + ptid;
+                        prefetch_ord_l2(a, k0, min(32, s_off[ph + 2] - k0), pass);
                     }
-                    first += tid;
+                    first += ptid;
                     step = stride;
                 } else if (ph < ncol) {
                     if (blockIdx.x != 0) continue;
@@ -1674,6 +1900,161 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_pgs_sweeps(SolverArgs a) {
     }
     if (tid == 0) *a.d_prev_n = nc;
     // finish: v += dv for dynamic bodies
+    for (int b = tid; b < a.num_bodies; b += stride) {
+        if (a.bodies[b].invMass == 0.f) continue;
+        v3 dl, da;
+        load_dv(a, b, dl, da);
+        b3gBody& B = a.bodies_out[b];
+        B.linVel.x = B.linVel.x + dl.x;
+        B.linVel.y = B.linVel.y + dl.y;
+        B.linVel.z = B.linVel.z + dl.z;
+        B.angVel.x = B.angVel.x + da.x;
+        B.angVel.y = B.angVel.y + da.y;
+        B.angVel.z = B.angVel.z + da.z;
+    }
+}
+
+
+// ---- dataflow sweeps: the same Gauss-Seidel order as k_pgs_sweeps without a grid barrier per colour.
+// A body's manifolds run in colour order, one per colour (a colour holds at most one manifold of a
+// dynamic body), so in sweep `it` the manifold of colour c on body b is that body's update number
+//   it * popcount(colours of b) + popcount(colours of b below c)
+// of the solve.  Each body carries a counter of the updates applied to it; a warp (32 manifolds of
+// one colour, which share no dynamic body) waits until both bodies of every lane have reached
+// their numbers, solves, and bumps the counters with release semantics after its delta stores.
+// The result equals the colour-by-colour sweep bit for bit (every body sees the same sequence of
+// updates); a warp only waits on manifolds earlier in (sweep, colour) order, so the earliest
+// unfinished warp of the whole grid can always run: no deadlock while every block is resident
+// (cooperative launch).  Waits are bounded (spin_limit polls, then the abort flag and the timeout
+// status); the records a warp needs are prefetched into L2 before it waits.  The update numbers
+// come packed in the record header (k_setup_rows), so a manifold's wait needs no other load.  Used
+// when no sweep result decides anything during the solve (no residual tolerance, no warm start to
+// check).
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+__global__ void __launch_bounds__(PK_THREADS, 1) k_pgs_flow(SolverArgs a) {
+    grid_barrier_begin();
+    const int nc = *a.d_nc;
+    const unsigned nb = gridDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int stride = gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    // warps interleaved across the blocks (as in k_pgs_sweeps): a small colour spreads over every SM
+    const int warp = ((int)threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x, nwarps = stride >> 5;
+    __shared__ int s_off[66];
+    for (int i = threadIdx.x; i < 66; i += blockDim.x) s_off[i] = __ldcg(&a.color_goff[i]);
+    __syncthreads();
+    int ncol = 0;
+    for (int c = 0; c < 64; c++)
+        if (s_off[c + 1] > s_off[c]) ncol = c + 1;
+    const bool remainder = s_off[65] > s_off[64];
+    const int npasses = a.interleave ? 1 : 2;
+    bool ok = true;
+    for (int it = 0; it < a.iterations && ok; it++) {
+        float res_d = 0.f, res_l = 0.f;
+        for (int ps = 0; ps < npasses && ok; ps++) {
+            const int sweep = it * npasses + ps;  // updates per body so far: sweep * popcount
+            const int pass = a.interleave ? 2 : ps;
+            for (int c = 0; c < ncol && ok; c++) {
+                const int hi = s_off[c + 1];
+                for (int k0 = s_off[c] + warp * 32; k0 < hi; k0 += nwarps * 32) {
+                    const int k = k0 + lane;
+                    const bool act = k < hi;
+                    int4 h = make_int4(0, 0, 0, 0);
+                    float4 im = make_float4(0.f, 0.f, 0.f, 0.f);
+                    unsigned tA = 0, tB = 0;
+                    if (act) {
+                        h = __ldcg(&a.hdr_ord[k]);
+                        im = __ldcg(&a.inv_mass_ord[k]);
+                        const size_t b4 = (size_t)k * 4;
+                        prefetch_l2(&a.sp_ord.rel1[b4]);
+                        prefetch_l2(&a.sp_ord.rel2[b4]);
+                        prefetch_l2(&a.sp_ord.imp[b4]);
+                        prefetch_l2(&a.sp_ord.angP[b4]);
+                        prefetch_l2(&a.sp_ord.angQ[b4]);
+                        if (pass != 0) {
+                            prefetch_l2(&a.sp_ord.dir2[b4]);
+                            prefetch_l2(&a.sp_ord.dir1[b4]);
+                            prefetch_l2(&a.sp_ord.rhsf[b4]);
+                            prefetch_l2(&a.sp_ord.angR[b4]);
+                            prefetch_l2(&a.sp_ord.angS[b4]);
+                            prefetch_l2(&a.sp_ord.angT[b4]);
+                        }
+                        const unsigned f = (unsigned)h.w;
+                        tA = (unsigned)sweep * (f & 127u) + ((f >> 7) & 63u);
+                        tB = (unsigned)sweep * ((f >> 13) & 127u) + ((f >> 20) & 63u);
+                    }
+                    // wait until both bodies of every lane have had their earlier updates
+                    unsigned spins = 0;
+                    for (;;) {
+                        const bool ready = !act || ((im.x == 0.f || ld_acquire_gpu(&a.version[h.x]) >= tA) &&
+                                                    (im.y == 0.f || ld_acquire_gpu(&a.version[h.y]) >= tB));
+                        if (__all_sync(0xffffffffu, ready)) break;
+                        if (*(volatile unsigned int*)a.bar.abort_flag) {
+                            ok = false;
+                            break;
+                        }
+                        if (++spins >= a.spin_limit) {
+                            if (lane == 0) {
+                                atomicExch(a.bar.abort_flag, 1u);
+                                atomicOr(a.bar.status, B3G_FLAG_BARRIER_TIMEOUT);
+                            }
+                            ok = false;
+                            break;
+                        }
+                        if (spins > 16) __nanosleep(64);
+                    }
+                    if (!ok) break;
+                    if (act) {
+                        v3 dlA = mk3(0, 0, 0), daA = mk3(0, 0, 0), dlB = mk3(0, 0, 0), daB = mk3(0, 0, 0);
+                        if (im.x != 0.f) load_dv(a, h.x, dlA, daA);
+                        if (im.y != 0.f) load_dv(a, h.y, dlB, daB);
+                        solve_ord(a.sp_ord, k, pass, h.z, im.x, im.y, dlA, daA, dlB, daB, res_d, res_l);
+                        if (im.x != 0.f) store_dv(a, h.x, dlA, daA);
+                        if (im.y != 0.f) store_dv(a, h.y, dlB, daB);
+                        // release: this thread's delta stores are visible before the counter bump
+                        if (im.x != 0.f) red_release_add_gpu(&a.version[h.x], 1u);
+                        if (im.y != 0.f) red_release_add_gpu(&a.version[h.y], 1u);
+                    }
+                }
+                ok = ok && !*(volatile unsigned int*)a.bar.abort_flag;
+            }
+            if (remainder && ok) {
+                // manifolds without a colour: after every coloured one of this pass, in order, one
+                // thread (they update no counter; the barriers order them)
+                if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
+                if (tid == 0)
+                    for (int k = s_off[64]; k < s_off[65]; k++) sweep_record_call(a, k, pass, res_d, res_l);
+                if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
+            }
+        }
+        // this sweep's residual sums (read after the solve; nothing decides on them during it)
+        for (int o = 16; o; o >>= 1) {
+            res_d += __shfl_xor_sync(0xffffffffu, res_d, o);
+            res_l += __shfl_xor_sync(0xffffffffu, res_l, o);
+        }
+        if (lane == 0) {
+            if (res_d != 0.f) atomicAdd(&a.residual_acc[2 * it], (double)res_d);
+            if (res_l != 0.f) atomicAdd(&a.residual_acc[2 * it + 1], (double)res_l);
+        }
+    }
+    if (!grid_barrier(a.bar, nb, a.spin_limit) || !ok) return;
+    if (tid == 0) {
+        const int last = a.iterations - 1;
+        const double dd = *((volatile double*)&a.residual_acc[2 * last]);
+        const double ll = *((volatile double*)&a.residual_acc[2 * last + 1]);
+        a.counters->residual = (float)(sqrt(dd) / fmax(sqrt(ll), 1e-12));
+        a.counters->iterations = a.iterations;
+    }
+    for (int k = tid; k < nc; k += stride) {
+        const int m = __ldcg(&a.color_order[k]);
+        const int4 h = __ldcg(&a.hdr_ord[k]);
+        for (int j = 0; j < 4; j++)
+            if (h.z & (1 << j)) a.sp.imp[(size_t)m * 4 + j] = __ldcg(&a.sp_ord.imp[(size_t)k * 4 + j]);
+        a.prev_key[m] = pair_key(h.x, h.y, a.body_bits);
+        a.prev_color[m] = a.color[m];
+    }
+    if (tid == 0) *a.d_prev_n = nc;
     for (int b = tid; b < a.num_bodies; b += stride) {
         if (a.bodies[b].invMass == 0.f) continue;
         v3 dl, da;
@@ -1822,6 +2203,8 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     a.bar2.gen = d.barrier + 17;
     a.bar2.abort_flag = d.barrier + 18;
     a.bar2.status = &d.counters->status;
+    a.flow_mask = nullptr;
+    a.version = nullptr;
     // PGS work split: the autotuner's choice (b3g_autotune) when the config says AUTO, else the
     // split measured fastest on GB300 for 256k-box piles -- grid-wide colours, coloured before
     // the row setup (records written in colour order)
@@ -1830,10 +2213,14 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
                                                                        : B3G_PGS_PARTITIONS_NONE;
     const bool ordered = cfg.solver_mode == B3G_SOLVER_PGS && pgs_mode == B3G_PGS_PARTITIONS_NONE;
     const int cgrid = ordered ? solver_grid(d, (const void*)k_pgs_sweeps, cfg.solver_blocks_per_sm, 0) : 0;
+    // dataflow sweeps where no sweep's residual decides anything during the solve
+    const bool flow = ordered && !(cfg.residual_tol > 0.f) && !a.warm && cfg.pgs_flow != 2;
     if (ordered) {
         a.pos_of = d.manifold_pos;
         a.color_fill = color_fill;
         a.color_cursor = color_cursor;
+        a.flow_mask = d.color_claim + 2 * (size_t)d.num_bodies;            // zeroed above each solve
+        a.version = reinterpret_cast<unsigned int*>(d.body_manifold_count);  // zeroed above each solve
         k_manifold_prep<<<grid, SV_THREADS, 0, s>>>(a);
         launches++;
         cudaLaunchConfig_t lc = {};
@@ -1949,6 +2336,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     lc.attrs = attr;
     lc.numAttrs = 1;
     cudaError_t e = jac                 ? cudaLaunchKernelEx(&lc, k_solve_jacobi, a)
+                    : flow              ? cudaLaunchKernelEx(&lc, k_pgs_flow, a)
                     : ordered           ? cudaLaunchKernelEx(&lc, k_pgs_sweeps, a)
                     : a.num_dynamic > 0 ? cudaLaunchKernelEx(&lc, k_solve_pgs<true>, a)
                                         : cudaLaunchKernelEx(&lc, k_solve_pgs<false>, a);

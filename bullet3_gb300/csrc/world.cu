@@ -682,6 +682,11 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     TRY(dalloc(h, &d.sp_ord.dir1, 4 * (size_t)d.max_contacts));
     TRY(dalloc(h, &d.sp_ord.rhsf, 4 * (size_t)d.max_contacts));
     TRY(dalloc(h, &d.sp_ord.imp, 4 * (size_t)d.max_contacts));
+    TRY(dalloc(h, &d.sp_ord.angP, 4 * (size_t)d.max_contacts));
+    TRY(dalloc(h, &d.sp_ord.angQ, 4 * (size_t)d.max_contacts));
+    TRY(dalloc(h, &d.sp_ord.angR, 4 * (size_t)d.max_contacts));
+    TRY(dalloc(h, &d.sp_ord.angS, 4 * (size_t)d.max_contacts));
+    TRY(dalloc(h, &d.sp_ord.angT, 4 * (size_t)d.max_contacts));
     TRY(dalloc(h, &d.manifold_hdr_ord, d.max_contacts));
     TRY(dalloc(h, &d.body_slot, N));
     TRY(dalloc(h, &d.manifold_group, d.max_contacts));
@@ -693,8 +698,8 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     TRY(dalloc(h, &d.manifold_pos, d.max_contacts));
     TRY(dalloc(h, &d.prev_mkey, d.max_contacts));
     TRY(dalloc(h, &d.prev_mcolor, d.max_contacts));
-    TRY(dalloc(h, &d.prev_mn, 1));
-    CUDA_TRY(cudaMemsetAsync(d.prev_mn, 0, sizeof(int), h->stream));
+    TRY(dalloc(h, &d.prev_mn, 4));  // manifolds of the last solve, colours of the last fresh colouring, recolour flag
+    CUDA_TRY(cudaMemsetAsync(d.prev_mn, 0, 4 * sizeof(int), h->stream));
     TRY(dalloc(h, &d.color_offsets, 4 * (B3G_MAX_COLORS + 2)));  // offsets, fill, remaining, cursors
     TRY(dalloc(h, &d.color_claim, 4 * (size_t)N));  // claims, colour masks; again for cross-partition
     CUDA_TRY(solver_prepare());

@@ -50,6 +50,14 @@ struct SolverPoints {
     float4* dir1 = nullptr;  // [4m+j]   first friction direction xyz, w = its jacDiagABInv
     float2* rhsf = nullptr;  // [4m+j]   rhs of the dir2 row, rhs of the dir1 row
     float4* imp = nullptr;   // [4m+j]   applied impulses: contact, dir2, dir1, (unused)
+    // colour-ordered records only: the rows' angular components (inverse inertia x relpos x axis),
+    // precomputed by the setup with the sweep's own operations: contact row A / B, dir2 row A / B,
+    // dir1 row A / B packed as (cA.xyz, 2A.x) (cB.xyz, 2A.y) (2A.z, 2B.xyz) (1A.xyz, 1B.x) (1B.yz)
+    float4* angP = nullptr;  // [4m+j]
+    float4* angQ = nullptr;
+    float4* angR = nullptr;
+    float4* angS = nullptr;
+    float2* angT = nullptr;
 };
 
 // Joint solver records.  A row of b3SolverConstraint (jointSolver.cl:129-160) is rebuilt from
@@ -181,7 +189,9 @@ struct DeviceState {
     int* manifold_pos = nullptr;           // PGS: position of each manifold in colour order
     unsigned long long* prev_mkey = nullptr;  // PGS: last solve's manifold body-pair keys (ascending)
     int* prev_mcolor = nullptr;            // PGS: ... and their colours
-    int* prev_mn = nullptr;                // PGS: ... and their number
+    int* prev_mn = nullptr;                // PGS: [0] their number, [1] colours of the last fresh
+                                           // colouring, [2] 1: colour the next solve from scratch,
+                                           // [3] solves since the last fresh colouring
     int* color_offsets = nullptr;          // B3G_MAX_COLORS + 1
     unsigned long long* color_claim = nullptr;  // per body
     float4* dv = nullptr;                  // per body: lin xyz | ang xyz (2 float4)

@@ -50,6 +50,8 @@ class b3Config:
         self.warm_start_max_points = 0
         self.autotune = False
         self.broadphase = capi.BROADPHASE_GRID
+        self.pgs_tail_manifolds = 0
+        self.pgs_flow = 0
         for k, v in kw.items():
             if not hasattr(self, k):
                 raise AttributeError(k)
@@ -67,7 +69,8 @@ class b3Config:
                                    pgs_partitions=self.pgs_partitions,
                                    pgs_interleave=int(self.pgs_interleave), warm_start=int(self.warm_start),
                                    warm_start_max_points=int(self.warm_start_max_points),
-                                   autotune=int(self.autotune), broadphase=int(self.broadphase))
+                                   autotune=int(self.autotune), broadphase=int(self.broadphase),
+                                   pgs_tail_manifolds=int(self.pgs_tail_manifolds), pgs_flow=int(self.pgs_flow))
 
 
 class _World:

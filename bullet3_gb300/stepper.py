@@ -59,6 +59,8 @@ def main(argv=None):
     p.add_argument("--autotune", action="store_true")
     p.add_argument("--no-graph", action="store_true")
     p.add_argument("--broadphase", choices=["grid", "lbvh", "auto"], default="grid")
+    p.add_argument("--pgs-flow", type=int, default=0, help="PGS grid-wide sweeps: 0 dataflow, 2 grid barrier per colour")
+    p.add_argument("--pgs-tail", type=int, default=0, help="trailing-colour size solved in one block (0: library default)")
     p.add_argument("--rays", type=int, default=0,
                    help="after the steps, time castRays of this many random downward rays over the bodies")
     p.add_argument("--stage-times", action="store_true",
@@ -69,7 +71,8 @@ def main(argv=None):
                    solver_iterations=a.iterations, pgs_interleave=a.solver == "pgs",
                    use_cuda_graph=not a.no_graph,
                    broadphase={"grid": capi.BROADPHASE_GRID, "lbvh": capi.BROADPHASE_LBVH,
-                               "auto": capi.BROADPHASE_AUTO}[a.broadphase])
+                               "auto": capi.BROADPHASE_AUTO}[a.broadphase],
+                   pgs_flow=a.pgs_flow, pgs_tail_manifolds=a.pgs_tail)
     np_, bp, pl = scenes.load_scene(sc, cfg)
     dt = 1.0 / 60.0
     for _ in range(a.settle):

@@ -115,6 +115,11 @@ typedef struct b3gConfig {
     int pgs_tail_manifolds;    /* PGS with grid-wide colours: the trailing colours of at most this many
                                   manifolds each are solved by one block, one grid barrier for all of
                                   them (0 = 1024; 1 effectively turns it off) */
+    int pgs_flow;              /* PGS with grid-wide colours and a fixed sweep count (no residual_tol, no
+                                  warm start): 0 = dataflow sweeps (per-body update counters instead of
+                                  a grid barrier per colour; same order, same results), 2 = a grid
+                                  barrier per colour */
+    int reserved[3];
 } b3gConfig;
 
 /* Per-step counters, copied once per step from the device. */

@@ -41,6 +41,8 @@ def scene_from_golden(d) -> scenes.Scene:
 def load(scene, **cfg):
     c = b3Config(use_cuda_graph=False)
     for k, v in cfg.items():
+        if not hasattr(c, k):  # a misspelt setting must not pass silently
+            raise AttributeError(k)
         setattr(c, k, v)
     np_, bp, pl = scenes.load_scene(scene, c)
     shapes = O.Shapes.from_tables(scenes.registered_tables(np_))

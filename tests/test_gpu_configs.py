@@ -62,10 +62,10 @@ def test_collision_at_scale_64_steps():
         pl.stepSimulation(1 / 60)
         pl.synchronize()
         npairs, nman, nref = _check_step(np_, bp, pl, shapes, sc.cell, b, rng)
-        assert npairs > 100000 and nref > 1000, step
+        assert npairs > 100000 and nref > 500, step
         checked += nref
     assert pl.status() == 0
-    assert checked > 64 * 1000
+    assert checked > 64 * 500
 
 
 def test_million_body_pour_dense_step():

@@ -258,15 +258,17 @@ def test_collision_at_scale_pair_sets_every_step():
     assert pl.status() == 0
 
 
+@pytest.mark.parametrize("flow", [0, 2])
 @pytest.mark.parametrize("interleave", [False, True])
-def test_pgs_carried_colours_bitexact(interleave):
+def test_pgs_carried_colours_bitexact(interleave, flow):
     # grid-wide PGS colours the manifolds before the row setup and carries each body pair's colour
     # over from the last solve; after many steps (and after bodies switched between static and
     # dynamic, which can make carried colours clash) the batches stay legal and the solve equals
     # the oracle sweeping the GPU's reported order bit for bit
+    # (flow 0: the dataflow sweeps with per-body update counters; 2: a grid barrier per colour)
     sc = scenes.box_stack(12, 16, 12, seed=4)
     np_, bp, pl, shapes = load(sc, solver_mode=capi.SOLVER_PGS, solver_iterations=10, use_cuda_graph=True,
-                               pgs_partitions=capi.PGS_PARTITIONS_NONE, pgs_interleave=interleave)
+                               pgs_partitions=capi.PGS_PARTITIONS_NONE, pgs_interleave=interleave, pgs_flow=flow)
     for _ in range(12):
         pl.stepSimulation(1 / 60)
     pl.synchronize()
@@ -308,7 +310,7 @@ def test_pgs_trailing_colours_in_one_block_bitexact(tail):
     # point gives the same Gauss-Seidel order, so the velocities equal the oracle's either way
     sc = scenes.mixed_scene(4096, extent=20.0, seed=3, plane=True)
     np_, bp, pl, shapes = load(sc, m_maxBroadphasePairs=400000, solver_mode=capi.SOLVER_PGS, solver_iterations=10,
-                               pgs_partitions=capi.PGS_PARTITIONS_NONE, pgs_tail_manifolds=tail)
+                               pgs_partitions=capi.PGS_PARTITIONS_NONE, pgs_tail_manifolds=tail, pgs_flow=2)
     for _ in range(3):
         pl.stepSimulation(1 / 60)
     pl.synchronize()
