@@ -540,28 +540,31 @@ __device__ __forceinline__ void solve_manifold(const SolverPoints& sp, int m, fl
 // the same numbers bit for bit.  Points stream through two register sets: the records of point
 // j + 1 are loaded while point j solves.
 struct OrdPoint {
-    float4 r1, r2, im, P, Q;  // rel_pos1 + jac, rel_pos2 + rhs, impulses, contact angular A / B (+ dir2 A.xy)
+    float4 r1, r2, P, Q;      // rel_pos1 + jac, rel_pos2 + rhs, contact angular A / B (+ dir2 A.xy)
     float4 d2, d1, R, S;      // friction directions + jacs, remaining angular components
     float2 rf, T;
 };
 
+// The records are read-only while the sweeps run (k_setup_rows wrote them in an earlier launch),
+// so they go through the non-coherent path and hit the lines prefetch_manifold brought into L1;
+// the applied impulses, rewritten every sweep, are read from L2 (all points at once, beside the
+// body deltas, by solve_ord).
 __device__ __forceinline__ void ld_point(const SolverPoints& sp, size_t s, int pass, OrdPoint& p) {
-    p.r1 = __ldcg(&sp.rel1[s]);
-    p.r2 = __ldcg(&sp.rel2[s]);
-    p.im = __ldcg(&sp.imp[s]);
-    p.P = __ldcg(&sp.angP[s]);
-    p.Q = __ldcg(&sp.angQ[s]);
+    p.r1 = __ldg(&sp.rel1[s]);
+    p.r2 = __ldg(&sp.rel2[s]);
+    p.P = __ldg(&sp.angP[s]);
+    p.Q = __ldg(&sp.angQ[s]);
     if (pass != 0) {
-        p.d2 = __ldcg(&sp.dir2[s]);
-        p.d1 = __ldcg(&sp.dir1[s]);
-        p.rf = __ldcg(&sp.rhsf[s]);
-        p.R = __ldcg(&sp.angR[s]);
-        p.S = __ldcg(&sp.angS[s]);
-        p.T = __ldcg(&sp.angT[s]);
+        p.d2 = __ldg(&sp.dir2[s]);
+        p.d1 = __ldg(&sp.dir1[s]);
+        p.rf = __ldg(&sp.rhsf[s]);
+        p.R = __ldg(&sp.angR[s]);
+        p.S = __ldg(&sp.angS[s]);
+        p.T = __ldg(&sp.angT[s]);
     }
 }
 
-__device__ __forceinline__ void solve_point(const OrdPoint& p, v3 n, float fr, int pass, float4* out, float imA,
+__device__ __forceinline__ void solve_point(const OrdPoint& p, float4 im, v3 n, float fr, int pass, float4* out, float imA,
                                             float imB, v3& dlA, v3& daA, v3& dlB, v3& daB, float& res_d,
                                             float& res_l) {
     const v3 rel1 = xyz(p.r1), rel2 = xyz(p.r2);
@@ -570,25 +573,25 @@ __device__ __forceinline__ void solve_point(const OrdPoint& p, v3 n, float fr, i
     const v3 a1 = xyz(p.S), b1 = mk3(p.S.w, p.T.x, p.T.y);
     if (pass == 3) {
         // warm start (b3PgsJacobiSolver.cpp:745-752, 815-843), as solve_manifold
-        float w = p.im.x;
+        float w = im.x;
         dlA = dlA + (n * imA) * w;
         daA = daA + cA * w;
         dlB = dlB + ((-n) * imB) * w;
         daB = daB + cB * w;
         const v3 e2 = xyz(p.d2), e1 = xyz(p.d1);
-        w = p.im.y;
+        w = im.y;
         dlA = dlA + (e2 * imA) * w;
         daA = daA + a2 * w;
         dlB = dlB + ((-e2) * imB) * w;
         daB = daB + b2 * w;
-        w = p.im.z;
+        w = im.z;
         dlA = dlA + (e1 * imA) * w;
         daA = daA + a1 * w;
         dlB = dlB + ((-e1) * imB) * w;
         daB = daB + b1 * w;
         return;
     }
-    float total = p.im.x;
+    float total = im.x;
     if (pass != 1) {
         const v3 r1xn = cross3(rel1, n);
         const v3 r2xn = -cross3(rel2, n);
@@ -603,7 +606,7 @@ __device__ __forceinline__ void solve_point(const OrdPoint& p, v3 n, float fr, i
             return;
         }
     }
-    float f2 = p.im.y, f1 = p.im.z;
+    float f2 = im.y, f1 = im.z;
     if (total > 0.f) {
         const float lower = -(fr * total), upper = fr * total;
         {
@@ -631,23 +634,55 @@ __device__ __forceinline__ void solve_point(const OrdPoint& p, v3 n, float fr, i
 
 __device__ __forceinline__ void solve_ord(const SolverPoints& sp, int k, int pass, int mask, float imA, float imB,
                                           v3& dlA, v3& daA, v3& dlB, v3& daB, float& res_d, float& res_l) {
-    const float4 nf = __ldcg(&sp.nf[k]);
+    const float4 nf = __ldg(&sp.nf[k]);
     const v3 n = xyz(nf);
     const size_t base = (size_t)k * 4;
     if (!mask) return;
+    float4 im[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+        if (mask & (1 << q)) im[q] = __ldcg(&sp.imp[base + q]);
     int j = __ffs(mask) - 1;
     OrdPoint cur, nxt;
     ld_point(sp, base + j, pass, cur);
-    for (;;) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        if (q != j) continue;  // q walks the set points in order (unrolled: im[] stays in registers)
         const int rest = mask & ~((2 << j) - 1);  // points after j
         const int jn = rest ? __ffs(rest) - 1 : -1;
         if (jn >= 0) ld_point(sp, base + jn, pass, nxt);
-        solve_point(cur, n, nf.w, pass, sp.imp + base + j, imA, imB, dlA, daA, dlB, daB, res_d, res_l);
+        solve_point(cur, im[q], n, nf.w, pass, sp.imp + base + j, imA, imB, dlA, daA, dlB, daB, res_d, res_l);
         if (jn < 0) break;
         cur = nxt;
         j = jn;
     }
 }
+
+__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// One manifold's colour-ordered records on their way into this SM's L1 (issued before the wait
+// that precedes the manifold's solve, so that only the body deltas cost an L2 round trip after
+// it); its applied impulses into L2.  A manifold's 4 point slots of one array are 64 contiguous
+// bytes, one line.
+__device__ __forceinline__ void prefetch_manifold(const SolverArgs& a, int k) {
+    const size_t b4 = (size_t)k * 4;
+    prefetch_l1(&a.hdr_ord[k]);
+    prefetch_l1(&a.inv_mass_ord[k]);
+    prefetch_l1(&a.sp_ord.nf[k]);
+    prefetch_l1(&a.sp_ord.rel1[b4]);
+    prefetch_l1(&a.sp_ord.rel2[b4]);
+    prefetch_l1(&a.sp_ord.angP[b4]);
+    prefetch_l1(&a.sp_ord.angQ[b4]);
+    prefetch_l1(&a.sp_ord.dir2[b4]);
+    prefetch_l1(&a.sp_ord.dir1[b4]);
+    prefetch_l1(&a.sp_ord.rhsf[b4]);
+    prefetch_l1(&a.sp_ord.angR[b4]);
+    prefetch_l1(&a.sp_ord.angS[b4]);
+    prefetch_l1(&a.sp_ord.angT[b4]);
+    prefetch_l2(&a.sp_ord.imp[b4]);
+}
+
 
 __device__ __forceinline__ void block_accumulate(double* dst, float x, float y) {
     __shared__ float sx[PK_THREADS / 32], sy[PK_THREADS / 32];
@@ -841,30 +876,6 @@ __device__ __forceinline__ void prefetch_records_l2(const SolverArgs& a, int k0,
         bulk_prefetch_l2(a.sp_ord.dir2 + 4 * (size_t)k0, 64u * c);
         bulk_prefetch_l2(a.sp_ord.dir1 + 4 * (size_t)k0, 64u * c);
         bulk_prefetch_l2(a.sp_ord.rhsf + 4 * (size_t)k0, 32u * c);
-    }
-}
-
-// the same for the colour-ordered records of k_setup_rows (angular components in place of the
-// inverse inertias)
-__device__ __forceinline__ void prefetch_ord_l2(const SolverArgs& a, int k0, int cnt, int pass) {
-    if (cnt <= 0) return;
-    const unsigned c = (unsigned)cnt;
-    const size_t p0 = 4 * (size_t)k0;
-    bulk_prefetch_l2(a.hdr_ord + k0, 16u * c);
-    bulk_prefetch_l2(a.inv_mass_ord + k0, 16u * c);
-    bulk_prefetch_l2(a.sp_ord.nf + k0, 16u * c);
-    bulk_prefetch_l2(a.sp_ord.rel1 + p0, 64u * c);
-    bulk_prefetch_l2(a.sp_ord.rel2 + p0, 64u * c);
-    bulk_prefetch_l2(a.sp_ord.imp + p0, 64u * c);
-    bulk_prefetch_l2(a.sp_ord.angP + p0, 64u * c);
-    bulk_prefetch_l2(a.sp_ord.angQ + p0, 64u * c);
-    if (pass) {
-        bulk_prefetch_l2(a.sp_ord.dir2 + p0, 64u * c);
-        bulk_prefetch_l2(a.sp_ord.dir1 + p0, 64u * c);
-        bulk_prefetch_l2(a.sp_ord.rhsf + p0, 32u * c);
-        bulk_prefetch_l2(a.sp_ord.angR + p0, 64u * c);
-        bulk_prefetch_l2(a.sp_ord.angS + p0, 64u * c);
-        bulk_prefetch_l2(a.sp_ord.angT + p0, 32u * c);
     }
 }
 
@@ -1783,8 +1794,8 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_colour(SolverArgs a) {
 
 // One record of the ordered sweeps: the manifold at position k against the global body deltas.
 __device__ __forceinline__ void sweep_record(const SolverArgs& a, int k, int pass, float& res_d, float& res_l) {
-    const int4 h = __ldcg(&a.hdr_ord[k]);
-    const float4 im = __ldcg(&a.inv_mass_ord[k]);
+    const int4 h = __ldg(&a.hdr_ord[k]);
+    const float4 im = __ldg(&a.inv_mass_ord[k]);
     v3 dlA = mk3(0, 0, 0), daA = mk3(0, 0, 0), dlB = mk3(0, 0, 0), daB = mk3(0, 0, 0);
     if (im.x != 0.f) load_dv(a, h.x, dlA, daA);
     if (im.y != 0.f) load_dv(a, h.y, dlB, daB);
@@ -1822,6 +1833,23 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_pgs_sweeps(SolverArgs a) {
     // phases per pass: the grid-wide colours, and when there is a tail, its colours plus one
     // phase for the remainder (which ends with the grid barrier)
     const int nphase = (tail < ncol || leftovers) ? ncol + 1 : tail;
+    // this thread's first manifold of phase ph (-1: none); its records are prefetched into L1
+    // before the barrier that precedes the phase
+    auto first_item = [&](int ph) -> int {
+        if (ph < tail) {
+            const int k = s_off[ph] + ptid;
+            return k < s_off[ph + 1] ? k : -1;
+        }
+        if (ph < ncol && blockIdx.x == 0) {
+            const int k = s_off[ph] + (int)threadIdx.x;
+            return k < s_off[ph + 1] ? k : -1;
+        }
+        return -1;
+    };
+    {
+        const int k = first_item(0);
+        if (k >= 0) prefetch_manifold(a, k);
+    }
     bool ok = true;
     const int npasses = a.interleave ? 1 : 2;
     bool warm_live = a.warm != 0;
@@ -1840,11 +1868,6 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_pgs_sweeps(SolverArgs a) {
                     first = s_off[ph];
                     hi = s_off[ph + 1];
                     if (first == hi) continue;  // uniform across blocks
-                    // warm L2 with this warp's first group of the next grid-wide colour
-                    if ((threadIdx.x & 31) == 0 && ph + 1 < tail) {
-                        const int k0 = s_off[ph + 1] + ptid;
-                        prefetch_ord_l2(a, k0, min(32, s_off[ph + 2] - k0), pass);
-                    }
                     first += ptid;
                     step = stride;
                 } else if (ph < ncol) {
@@ -1857,7 +1880,14 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_pgs_sweeps(SolverArgs a) {
                     hi = blockIdx.x == 0 && threadIdx.x == 0 ? s_off[65] : first;
                     step = 1;
                 }
-                for (int k = first; k < hi; k += step) sweep_record(a, k, pass, res_d, res_l);
+                for (int k = first; k < hi; k += step) {
+                    if (k + step < hi) prefetch_manifold(a, k + step);
+                    sweep_record(a, k, pass, res_d, res_l);
+                }
+                {
+                    const int nk = first_item(ph + 1 < nphase ? ph + 1 : 0);
+                    if (nk >= 0) prefetch_manifold(a, nk);
+                }
                 if (ph < tail || ph == ncol) {
                     if (!grid_barrier(a.bar, nb, a.spin_limit)) return;
                 } else {
@@ -1930,7 +1960,6 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_pgs_sweeps(SolverArgs a) {
 // come packed in the record header (k_setup_rows), so a manifold's wait needs no other load.  Used
 // when no sweep result decides anything during the solve (no residual tolerance, no warm start to
 // check).
-__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
 __global__ void __launch_bounds__(PK_THREADS, 1) k_pgs_flow(SolverArgs a) {
     grid_barrier_begin();
@@ -1960,35 +1989,29 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_pgs_flow(SolverArgs a) {
                 for (int k0 = s_off[c] + warp * 32; k0 < hi; k0 += nwarps * 32) {
                     const int k = k0 + lane;
                     const bool act = k < hi;
-                    int4 h = make_int4(0, 0, 0, 0);
-                    float4 im = make_float4(0.f, 0.f, 0.f, 0.f);
+                    // the dynamic bodies to wait for (-1: none) and their update numbers; the
+                    // solve reloads the header from L1
+                    int wA = -1, wB = -1;
                     unsigned tA = 0, tB = 0;
                     if (act) {
-                        h = __ldcg(&a.hdr_ord[k]);
-                        im = __ldcg(&a.inv_mass_ord[k]);
-                        const size_t b4 = (size_t)k * 4;
-                        prefetch_l2(&a.sp_ord.rel1[b4]);
-                        prefetch_l2(&a.sp_ord.rel2[b4]);
-                        prefetch_l2(&a.sp_ord.imp[b4]);
-                        prefetch_l2(&a.sp_ord.angP[b4]);
-                        prefetch_l2(&a.sp_ord.angQ[b4]);
-                        if (pass != 0) {
-                            prefetch_l2(&a.sp_ord.dir2[b4]);
-                            prefetch_l2(&a.sp_ord.dir1[b4]);
-                            prefetch_l2(&a.sp_ord.rhsf[b4]);
-                            prefetch_l2(&a.sp_ord.angR[b4]);
-                            prefetch_l2(&a.sp_ord.angS[b4]);
-                            prefetch_l2(&a.sp_ord.angT[b4]);
-                        }
+                        prefetch_manifold(a, k);
+                        const int4 h = __ldg(&a.hdr_ord[k]);
+                        const float4 im = __ldg(&a.inv_mass_ord[k]);
                         const unsigned f = (unsigned)h.w;
-                        tA = (unsigned)sweep * (f & 127u) + ((f >> 7) & 63u);
-                        tB = (unsigned)sweep * ((f >> 13) & 127u) + ((f >> 20) & 63u);
+                        if (im.x != 0.f) {
+                            wA = h.x;
+                            tA = (unsigned)sweep * (f & 127u) + ((f >> 7) & 63u);
+                        }
+                        if (im.y != 0.f) {
+                            wB = h.y;
+                            tB = (unsigned)sweep * ((f >> 13) & 127u) + ((f >> 20) & 63u);
+                        }
                     }
                     // wait until both bodies of every lane have had their earlier updates
                     unsigned spins = 0;
                     for (;;) {
-                        const bool ready = !act || ((im.x == 0.f || ld_acquire_gpu(&a.version[h.x]) >= tA) &&
-                                                    (im.y == 0.f || ld_acquire_gpu(&a.version[h.y]) >= tB));
+                        const bool ready = (wA < 0 || ld_acquire_gpu(&a.version[wA]) >= tA) &&
+                                           (wB < 0 || ld_acquire_gpu(&a.version[wB]) >= tB);
                         if (__all_sync(0xffffffffu, ready)) break;
                         if (*(volatile unsigned int*)a.bar.abort_flag) {
                             ok = false;
@@ -2006,15 +2029,10 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_pgs_flow(SolverArgs a) {
                     }
                     if (!ok) break;
                     if (act) {
-                        v3 dlA = mk3(0, 0, 0), daA = mk3(0, 0, 0), dlB = mk3(0, 0, 0), daB = mk3(0, 0, 0);
-                        if (im.x != 0.f) load_dv(a, h.x, dlA, daA);
-                        if (im.y != 0.f) load_dv(a, h.y, dlB, daB);
-                        solve_ord(a.sp_ord, k, pass, h.z, im.x, im.y, dlA, daA, dlB, daB, res_d, res_l);
-                        if (im.x != 0.f) store_dv(a, h.x, dlA, daA);
-                        if (im.y != 0.f) store_dv(a, h.y, dlB, daB);
+                        sweep_record(a, k, pass, res_d, res_l);
                         // release: this thread's delta stores are visible before the counter bump
-                        if (im.x != 0.f) red_release_add_gpu(&a.version[h.x], 1u);
-                        if (im.y != 0.f) red_release_add_gpu(&a.version[h.y], 1u);
+                        if (wA >= 0) red_release_add_gpu(&a.version[wA], 1u);
+                        if (wB >= 0) red_release_add_gpu(&a.version[wB], 1u);
                     }
                 }
                 ok = ok && !*(volatile unsigned int*)a.bar.abort_flag;
@@ -2102,6 +2120,12 @@ static int solver_grid(DeviceState& d, const void* fn, int blocks_per_sm, size_t
 cudaError_t solver_prepare() {
     cudaError_t e = cudaFuncSetAttribute(k_solve_pgs<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          B3G_PGS_MAX_SMEM);
+    if (e != cudaSuccess) return e;
+    // the colour-ordered sweeps use < 1 KB of shared memory: the rest of the SM's 256 KB as L1
+    // for the prefetched records
+    e = cudaFuncSetAttribute(k_pgs_sweeps, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_pgs_flow, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(k_solve_pgs<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, B3G_PGS_MAX_SMEM);
 }
@@ -2198,7 +2222,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     a.d_new = &d.counters->new_manifolds;
     a.color_goff = d.color_offsets;
     a.body_bits = d.body_bits;
-    a.tail_max = cfg.pgs_tail_manifolds > 0 ? cfg.pgs_tail_manifolds : 1024;
+    a.tail_max = cfg.pgs_tail_manifolds > 0 ? cfg.pgs_tail_manifolds : 32;
     a.bar2.count = d.barrier + 16;
     a.bar2.gen = d.barrier + 17;
     a.bar2.abort_flag = d.barrier + 18;
@@ -2214,7 +2238,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     const bool ordered = cfg.solver_mode == B3G_SOLVER_PGS && pgs_mode == B3G_PGS_PARTITIONS_NONE;
     const int cgrid = ordered ? solver_grid(d, (const void*)k_pgs_sweeps, cfg.solver_blocks_per_sm, 0) : 0;
     // dataflow sweeps where no sweep's residual decides anything during the solve
-    const bool flow = ordered && !(cfg.residual_tol > 0.f) && !a.warm && cfg.pgs_flow != 2;
+    const bool flow = ordered && !(cfg.residual_tol > 0.f) && !a.warm && cfg.pgs_flow == 1;
     if (ordered) {
         a.pos_of = d.manifold_pos;
         a.color_fill = color_fill;

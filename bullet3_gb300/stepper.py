@@ -59,7 +59,7 @@ def main(argv=None):
     p.add_argument("--autotune", action="store_true")
     p.add_argument("--no-graph", action="store_true")
     p.add_argument("--broadphase", choices=["grid", "lbvh", "auto"], default="grid")
-    p.add_argument("--pgs-flow", type=int, default=0, help="PGS grid-wide sweeps: 0 dataflow, 2 grid barrier per colour")
+    p.add_argument("--pgs-flow", type=int, default=0, help="PGS grid-wide sweeps: 0 default (grid barrier per colour), 1 dataflow, 2 grid barrier")
     p.add_argument("--pgs-tail", type=int, default=0, help="trailing-colour size solved in one block (0: library default)")
     p.add_argument("--rays", type=int, default=0,
                    help="after the steps, time castRays of this many random downward rays over the bodies")

@@ -114,11 +114,14 @@ typedef struct b3gConfig {
     int broadphase;            /* B3G_BROADPHASE_GRID (0), _LBVH (1) or _AUTO (2), see b3g_set_broadphase */
     int pgs_tail_manifolds;    /* PGS with grid-wide colours: the trailing colours of at most this many
                                   manifolds each are solved by one block, one grid barrier for all of
-                                  them (0 = 1024; 1 effectively turns it off) */
+                                  them (0 = 32: a colour that fits one warp; measured on GB300, larger
+                                  tails serialise their colours on one SM and cost more than the
+                                  barriers they save; 1 effectively turns it off) */
     int pgs_flow;              /* PGS with grid-wide colours and a fixed sweep count (no residual_tol, no
-                                  warm start): 0 = dataflow sweeps (per-body update counters instead of
-                                  a grid barrier per colour; same order, same results), 2 = a grid
-                                  barrier per colour */
+                                  warm start): 1 = dataflow sweeps (per-body update counters instead of
+                                  a grid barrier per colour; same order, same results); 0 (default) and
+                                  2 = a grid barrier per colour, measured faster on GB300 from 16k to
+                                  300k manifolds */
     int reserved[3];
 } b3gConfig;
 

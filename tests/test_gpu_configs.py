@@ -24,8 +24,9 @@ pytestmark = pytest.mark.gpu
 
 
 def _pair_key(x, y):
-    lo, hi = np.minimum(x, y).astype(np.int64), np.maximum(x, y).astype(np.int64)
-    return lo << 32 | hi
+    # (a manifold stores a static body's index negated; pairs store it as is)
+    x, y = np.abs(x).astype(np.int64), np.abs(y).astype(np.int64)
+    return np.minimum(x, y) << 32 | np.maximum(x, y)
 
 
 def _check_step(np_, bp, pl, shapes, cell, b, rng, sample=20000):
@@ -75,7 +76,8 @@ def test_million_body_pour_dense_step():
     for _ in range(590):
         pl.stepSimulation(1 / 60)
     pl.synchronize()
-    assert pl.status() == 0
+    # (a persistent warm start that did worse than a cold start was dropped: informational)
+    assert pl.status() & ~capi.FLAG_WARM_DISCARDED == 0
     b = np_.readbackAllBodiesToCpu()
     pl.stepSimulation(1 / 60)
     pl.synchronize()
@@ -83,4 +85,4 @@ def test_million_body_pour_dense_step():
     npairs, nman, nref = _check_step(np_, bp, pl, shapes, sc.cell, b, rng)
     # the dense end of the pour: most bodies rest on others
     assert npairs > 2_000_000 and nman > 1_000_000 and nref > 5000
-    assert pl.status() == 0
+    assert pl.status() & ~capi.FLAG_WARM_DISCARDED == 0
