@@ -7,7 +7,7 @@
                        valid points against the oracle's contacts from the same input state
   million-body pour    1,048,576 bodies of the same mix poured into a 5-plane container: after 590
                        steps of the pour (the dense end), one step checked the same way (AABBs,
-                       pair set, 20,000 sampled pairs' manifolds)
+                       pair set, 60,000 sampled pairs' manifolds)
 
 The oracle's contacts follow the reference's b3ContactConvexConvexSAT / computeContactPlaneConvex
 / computeContactSphereConvex bit for bit (tests/test_oracle_golden.py); its pair set is the exact
@@ -82,7 +82,8 @@ def test_million_body_pour_dense_step():
     pl.stepSimulation(1 / 60)
     pl.synchronize()
     rng = np.random.Generator(np.random.PCG64(12))
-    npairs, nman, nref = _check_step(np_, bp, pl, shapes, sc.cell, b, rng)
+    # (one pair in eight has a manifold at the dense end: 60,000 sampled pairs give ~7,500)
+    npairs, nman, nref = _check_step(np_, bp, pl, shapes, sc.cell, b, rng, sample=60000)
     # the dense end of the pour: most bodies rest on others
     assert npairs > 2_000_000 and nman > 1_000_000 and nref > 5000
     assert pl.status() & ~capi.FLAG_WARM_DISCARDED == 0
