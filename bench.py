@@ -188,6 +188,16 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def solve_kernels(tuning) -> str:
+    """The solve stage's kernels for the PGS work split that ran (the autotuner's choice, else the
+    library's rule for AUTO: grid-wide colours)."""
+    split = (tuning or {}).get("pgs_partitions", -1)
+    if split in (-1, 0, 2):  # AUTO rule / B3G_PGS_PARTITIONS_NONE
+        return ("solve stage: k_manifold_prep + k_colour (colouring) + k_setup_rows (rows in colour order) "
+                "+ k_pgs_sweeps (persistent, a grid barrier per colour)")
+    return "solve stage: k_setup_rows + k_solve_pgs (persistent, block partitions)"
+
+
 def solver_traffic():
     """DRAM bytes per manifold of the solve stage's kernels from a committed ncu capture (ncu cannot
     run inside this measurement): the file names the command, workload and launch shapes of the
@@ -560,7 +570,7 @@ def gpu_arm(args):
     solve_s = stage_ms["solve"] / 1000.0
     achieved = solve_bytes / solve_s / 1e9 if solve_s > 0 else 0.0
     traffic = solver_traffic()
-    roofline = {"bound": "hbm", "kernel": "solve stage (k_setup_rows + k_solve_pgs persistent kernel)",
+    roofline = {"bound": "hbm", "kernel": solve_kernels(tuning),
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_kind": peak_kind, "algorithmic_bytes": solve_bytes,
                 "traffic": (traffic["bytes_per_manifold"] * C_ if traffic and "bytes_per_manifold" in traffic

@@ -147,167 +147,188 @@ __global__ void k_count_manifolds(const b3gContact4* __restrict__ slots, const i
 }
 
 // Row setup: setupContactConstraint + convertContact friction rows, stored as compact records.
+// One thread per contact point (the 4 point slots of a manifold are 4 consecutive lanes of a
+// warp): the point's contact row and two friction rows; lane 0 of the 4 writes the manifold's
+// header with the point mask (a ballot over the 4).
 __global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
     const int nc = *a.d_nc;
     const bool pgs = a.mode == B3G_SOLVER_PGS;
     if (a.ws_rows && blockIdx.x == 0 && threadIdx.x == 0) *a.ws_rows = min(4 * nc, a.ws_rows_cap);
     const bool ordered = a.pos_of != nullptr;  // records straight into colour order
     SolverPoints& out = ordered ? a.sp_ord : a.sp;
-    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nc; m += gridDim.x * blockDim.x) {
-        const b3gContact4 c = a.slots[a.manifold_pair[m]];
-        const int iA = abs(c.bodyA), iB = abs(c.bodyB);
-        const b3gBody& A = a.bodies[iA];
-        const b3gBody& B = a.bodies[iB];
-        const float imA = A.invMass, imB = B.invMass;
-        int np = (int)c.worldNormalOnB.w;
-        if (np > 4) np = 4;
-        int mask = 0;
-        const int k = ordered ? __ldcg(&a.pos_of[m]) : m;  // record slot
+    const int total = 4 * nc;
+    const int lane = threadIdx.x & 31;
+    // (warp-uniform loop: every lane reaches the ballot)
+    for (int base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
+        const int t = base + (int)threadIdx.x;
+        const int k = t >> 2, j = t & 3;  // record slot (ordered: record i holds manifold color_order[i])
+        bool active = false;
+        int m = 0, iA = 0, iB = 0, np = 0;
+        float imA = 0.f, imB = 0.f;
+        v3 n = mk3(0.f, 0.f, 0.f);
+        float fric = 0.f;
+        if (t < total) {
+            m = ordered ? __ldcg(&a.color_order[k]) : k;
+            const b3gContact4* cp = a.slots + a.manifold_pair[m];
+            const float4 nw = ldg4(&cp->worldNormalOnB);
+            const int4 ids = __ldg(reinterpret_cast<const int4*>(&cp->worldNormalOnB) + 1);  // cmp, batch, A, B
+            iA = abs(ids.z);
+            iB = abs(ids.w);
+            const float4* bA = reinterpret_cast<const float4*>(a.bodies + iA);
+            const float4* bB = reinterpret_cast<const float4*>(a.bodies + iB);
+            imA = __ldg(&bA[4]).y;
+            imB = __ldg(&bB[4]).y;
+            np = (int)nw.w;
+            if (np > 4) np = 4;
+            if (imA == 0.f && imB == 0.f) np = 0;  // static-static: no rows (b3PgsJacobiSolver.cpp:864-866)
+            fric = (float)((unsigned)ids.x >> 16) / (float)0xffff;
+            // getContactPoint: normalised normal
+            n = normalize3(mk3(nw.x, nw.y, nw.z));
+            const float4 wp = j < np ? ldg4(&cp->worldPosB[j]) : make_float4(0.f, 0.f, 0.f, 1e30f);
+            const float dist = wp.w;
+            active = j < np && dist <= a.threshold;
+            if (active) {
+                const size_t s = (size_t)k * 4 + j;     // record slot of the point
+                const size_t sf = (size_t)m * 4 + j;    // feature slot (manifold order)
+                const b3gMat3 IA = a.inertias[iA].invInertiaWorld;
+                const b3gMat3 IB = a.inertias[iB].invInertiaWorld;
+                const float4 pA = __ldg(&bA[0]), lA = __ldg(&bA[2]), wA = __ldg(&bA[3]);
+                const float4 pB = __ldg(&bB[0]), lB = __ldg(&bB[2]), wB = __ldg(&bB[3]);
+                const v3 posA = mk3(pA.x, pA.y, pA.z), posB = mk3(pB.x, pB.y, pB.z);
+                const v3 linA = mk3(lA.x, lA.y, lA.z), angA = mk3(wA.x, wA.y, wA.z);
+                const v3 linB = mk3(lB.x, lB.y, lB.z), angB = mk3(wB.x, wB.y, wB.z);
+                float countA = 1.f, countB = 1.f;
+                if (!pgs) {
+                    if (imA != 0.f) countA = (float)a.body_count[iA];
+                    if (imB != 0.f) countB = (float)a.body_count[iB];
+                }
+                const v3 pos2 = mk3(wp.x, wp.y, wp.z);
+                const v3 pos1 = pos2 + n * dist;
+                const v3 rel1 = pos1 - posA;
+                const v3 rel2 = pos2 - posB;
+                v3 ang[6];  // angular components: contact A / B, dir2 A / B, dir1 A / B
+                // contact row (setupContactConstraint)
+                {
+                    v3 torqueAxis0 = cross3(rel1, n);
+                    v3 angCompA = imul(IA, torqueAxis0);
+                    v3 torqueAxis1 = cross3(rel2, n);
+                    v3 angCompB = imul(IB, -torqueAxis1);
+                    float denom0 = imA + dot3(n, cross3(angCompA, rel1));
+                    float denom1 = imB + dot3(n, cross3(-angCompB, rel2));
+                    float jac = 1.0f / (denom0 + denom1);
+                    float scaled = pgs ? jac : 1.0f / (denom0 * countA + denom1 * countB);
+                    v3 r1xn = torqueAxis0, r2xn = -torqueAxis1;
+                    float penetration = dist + 0.0f;
+                    float vel1Dotn = dot3(n, linA) + dot3(r1xn, angA);
+                    float vel2Dotn = -dot3(n, linB) + dot3(r2xn, angB);
+                    float rel_vel = vel1Dotn + vel2Dotn;
+                    float positionalError = 0.f;
+                    float velocityError = 0.0f - rel_vel;
+                    if (penetration > 0.f)
+                        velocityError -= penetration / a.dt;
+                    else
+                        positionalError = -penetration * a.erp / a.dt;
+                    float rhs = positionalError * scaled + velocityError * scaled;
+                    out.rel1[s] = f4(rel1, jac);
+                    out.rel2[s] = f4(rel2, rhs);
+                    ang[0] = angCompA;
+                    ang[1] = angCompB;
+                }
+                // friction rows (convertContact: dir2 row first, then dir1)
+                {
+                    v3 vel1 = linA + cross3(angA, rel1);
+                    v3 vel2 = linB + cross3(angB, rel2);
+                    v3 vel = vel1 - vel2;
+                    float rel_vel = dot3(n, vel);
+                    v3 dir1 = vel - n * rel_vel;
+                    float lat = dot3(dir1, dir1);
+                    v3 dir2;
+                    if (lat > FLT_EPSILON) {
+                        float inv = 1.f / sqrtf(lat);
+                        dir1 = dir1 * inv;
+                        dir2 = cross3(dir1, n);
+                        float l2 = sqrtf(dot3(dir2, dir2));
+                        dir2 = dir2 * (1.f / l2);
+                    } else {
+                        plane_space(n, dir1, dir2);
+                    }
+                    v3 dirs[2] = {dir2, dir1};
+                    float jacs[2], rhss[2];
+                    for (int r = 0; r < 2; r++) {
+                        v3 d = dirs[r];
+                        v3 r1xn = cross3(rel1, d);
+                        v3 angCompA = imul(IA, r1xn);
+                        v3 r2xn = cross3(rel2, -d);
+                        v3 angCompB = imul(IB, r2xn);
+                        float denom0 = imA + dot3(d, cross3(angCompA, rel1));
+                        float denom1 = imB + dot3(d, cross3(-angCompB, rel2));
+                        float jac = 1.0f / (denom0 + denom1);
+                        float scaled = pgs ? jac : 1.0f / (denom0 * countA + denom1 * countB);
+                        float v1 = dot3(d, linA) + dot3(r1xn, angA);
+                        float v2 = -dot3(d, linB) + dot3(r2xn, angB);
+                        float rv = v1 + v2;
+                        float velocityError = 0.0f - rv;
+                        jacs[r] = jac;
+                        rhss[r] = velocityError * scaled;
+                        ang[2 + 2 * r] = angCompA;
+                        ang[3 + 2 * r] = angCompB;
+                    }
+                    out.dir2[s] = f4(dir2, jacs[0]);
+                    out.dir1[s] = f4(dir1, jacs[1]);
+                    out.rhsf[s] = make_float2(rhss[0], rhss[1]);
+                    out.imp[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (ordered) {
+                        // the sweeps' angular components, computed above with their operations
+                        out.angP[s] = make_float4(ang[0].x, ang[0].y, ang[0].z, ang[2].x);
+                        out.angQ[s] = make_float4(ang[1].x, ang[1].y, ang[1].z, ang[2].y);
+                        out.angR[s] = make_float4(ang[2].z, ang[3].x, ang[3].y, ang[3].z);
+                        out.angS[s] = make_float4(ang[4].x, ang[4].y, ang[4].z, ang[5].x);
+                        out.angT[s] = make_float2(ang[5].y, ang[5].z);
+                    }
+                    if (a.ws_features && sf < (size_t)a.ws_rows_cap) {
+                        // warm-start features of this point (the network's input layout)
+                        float* f = a.ws_features + sf * 12;
+                        f[0] = vel.x; f[1] = vel.y; f[2] = vel.z;
+                        f[3] = n.x; f[4] = n.y; f[5] = n.z;
+                        f[6] = dist;
+                        f[7] = imA; f[8] = imB;
+                        f[9] = (float)np;
+                        f[10] = sqrtf(lat);
+                        f[11] = a.dt * (a.gx * n.x + a.gy * n.y + a.gz * n.z);
+                    }
+                }
+            }
+        }
+        const int mask = (int)(__ballot_sync(0xffffffffu, active) >> (lane & 28)) & 15;
+        if (t >= total || j != 0) continue;
+        // the manifold: normal + friction, inverse masses, header
+        out.nf[k] = f4(n, fric);
         if (!ordered) {
             a.color[m] = -1;
             a.inv_mass[m] = make_float2(imA, imB);
-        }
-        if (imA == 0.f && imB == 0.f) np = 0;  // static-static: no rows (b3PgsJacobiSolver.cpp:864-866)
-        const b3gMat3 IA = a.inertias[iA].invInertiaWorld;
-        const b3gMat3 IB = a.inertias[iB].invInertiaWorld;
-        const v3 posA = f4v3(A.pos), posB = f4v3(B.pos);
-        const v3 linA = f4v3(A.linVel), angA = f4v3(A.angVel);
-        const v3 linB = f4v3(B.linVel), angB = f4v3(B.angVel);
-        float countA = 1.f, countB = 1.f;
-        if (!pgs) {
-            if (imA != 0.f) countA = (float)a.body_count[iA];
-            if (imB != 0.f) countB = (float)a.body_count[iB];
-        }
-        const float fric = (float)c.frictionCmp / (float)0xffff;
-        // getContactPoint: normalised normal
-        v3 n = normalize3(mk3(c.worldNormalOnB.x, c.worldNormalOnB.y, c.worldNormalOnB.z));
-        out.nf[k] = f4(n, fric);
-        if (ordered) a.inv_mass_ord[k] = make_float4(imA, imB, 0.f, 0.f);
-        for (int j = 0; j < np; j++) {
-            const float dist = c.worldPosB[j].w;
-            if (!(dist <= a.threshold)) continue;
-            mask |= 1 << j;
-            const size_t s = (size_t)k * 4 + j;     // record slot of the point
-            const size_t sf = (size_t)m * 4 + j;    // feature slot (manifold order)
-            const v3 pos2 = mk3(c.worldPosB[j].x, c.worldPosB[j].y, c.worldPosB[j].z);
-            const v3 pos1 = pos2 + n * dist;
-            const v3 rel1 = pos1 - posA;
-            const v3 rel2 = pos2 - posB;
-            v3 ang[6];  // angular components: contact A / B, dir2 A / B, dir1 A / B
-            // contact row (setupContactConstraint)
-            {
-                v3 torqueAxis0 = cross3(rel1, n);
-                v3 angCompA = imul(IA, torqueAxis0);
-                v3 torqueAxis1 = cross3(rel2, n);
-                v3 angCompB = imul(IB, -torqueAxis1);
-                float denom0 = imA + dot3(n, cross3(angCompA, rel1));
-                float denom1 = imB + dot3(n, cross3(-angCompB, rel2));
-                float jac = 1.0f / (denom0 + denom1);
-                float scaled = pgs ? jac : 1.0f / (denom0 * countA + denom1 * countB);
-                v3 r1xn = torqueAxis0, r2xn = -torqueAxis1;
-                float penetration = dist + 0.0f;
-                float vel1Dotn = dot3(n, linA) + dot3(r1xn, angA);
-                float vel2Dotn = -dot3(n, linB) + dot3(r2xn, angB);
-                float rel_vel = vel1Dotn + vel2Dotn;
-                float positionalError = 0.f;
-                float velocityError = 0.0f - rel_vel;
-                if (penetration > 0.f)
-                    velocityError -= penetration / a.dt;
-                else
-                    positionalError = -penetration * a.erp / a.dt;
-                float rhs = positionalError * scaled + velocityError * scaled;
-                out.rel1[s] = f4(rel1, jac);
-                out.rel2[s] = f4(rel2, rhs);
-                ang[0] = angCompA;
-                ang[1] = angCompB;
-            }
-            // friction rows (convertContact: dir2 row first, then dir1)
-            {
-                v3 vel1 = linA + cross3(angA, rel1);
-                v3 vel2 = linB + cross3(angB, rel2);
-                v3 vel = vel1 - vel2;
-                float rel_vel = dot3(n, vel);
-                v3 dir1 = vel - n * rel_vel;
-                float lat = dot3(dir1, dir1);
-                v3 dir2;
-                if (lat > FLT_EPSILON) {
-                    float inv = 1.f / sqrtf(lat);
-                    dir1 = dir1 * inv;
-                    dir2 = cross3(dir1, n);
-                    float l2 = sqrtf(dot3(dir2, dir2));
-                    dir2 = dir2 * (1.f / l2);
-                } else {
-                    plane_space(n, dir1, dir2);
-                }
-                v3 dirs[2] = {dir2, dir1};
-                float jacs[2], rhss[2];
-                for (int k = 0; k < 2; k++) {
-                    v3 d = dirs[k];
-                    v3 r1xn = cross3(rel1, d);
-                    v3 angCompA = imul(IA, r1xn);
-                    v3 r2xn = cross3(rel2, -d);
-                    v3 angCompB = imul(IB, r2xn);
-                    float denom0 = imA + dot3(d, cross3(angCompA, rel1));
-                    float denom1 = imB + dot3(d, cross3(-angCompB, rel2));
-                    float jac = 1.0f / (denom0 + denom1);
-                    float scaled = pgs ? jac : 1.0f / (denom0 * countA + denom1 * countB);
-                    float v1 = dot3(d, linA) + dot3(r1xn, angA);
-                    float v2 = -dot3(d, linB) + dot3(r2xn, angB);
-                    float rv = v1 + v2;
-                    float velocityError = 0.0f - rv;
-                    jacs[k] = jac;
-                    rhss[k] = velocityError * scaled;
-                    ang[2 + 2 * k] = angCompA;
-                    ang[3 + 2 * k] = angCompB;
-                }
-                out.dir2[s] = f4(dir2, jacs[0]);
-                out.dir1[s] = f4(dir1, jacs[1]);
-                out.rhsf[s] = make_float2(rhss[0], rhss[1]);
-                out.imp[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (ordered) {
-                    // the sweeps' angular components, computed above with their operations
-                    out.angP[s] = make_float4(ang[0].x, ang[0].y, ang[0].z, ang[2].x);
-                    out.angQ[s] = make_float4(ang[1].x, ang[1].y, ang[1].z, ang[2].y);
-                    out.angR[s] = make_float4(ang[2].z, ang[3].x, ang[3].y, ang[3].z);
-                    out.angS[s] = make_float4(ang[4].x, ang[4].y, ang[4].z, ang[5].x);
-                    out.angT[s] = make_float2(ang[5].y, ang[5].z);
-                }
-                if (a.ws_features && sf < (size_t)a.ws_rows_cap) {
-                    // warm-start features of this point (the network's input layout)
-                    float* f = a.ws_features + sf * 12;
-                    f[0] = vel.x; f[1] = vel.y; f[2] = vel.z;
-                    f[3] = n.x; f[4] = n.y; f[5] = n.z;
-                    f[6] = dist;
-                    f[7] = imA; f[8] = imB;
-                    f[9] = (float)np;
-                    f[10] = sqrtf(lat);
-                    f[11] = a.dt * (a.gx * n.x + a.gy * n.y + a.gz * n.z);
-                }
-            }
-        }
-        if (ordered) {
-            // the dataflow sweeps' per-body update numbers, packed: for each dynamic body its
-            // manifolds' colour count (7 bits) and the rank of this manifold's colour among them
-            // (6 bits); A in the low 13 bits, B in the next 13
-            unsigned flow = 0;
-            if (a.flow_mask) {
-                const int c = __ldcg(&a.color[m]);
-                if (c >= 0) {
-                    const unsigned long long below = (1ull << c) - 1ull;
-                    if (imA != 0.f) {
-                        const unsigned long long cm = __ldcg(&a.flow_mask[iA]);
-                        flow |= (unsigned)__popcll(cm) | ((unsigned)__popcll(cm & below) << 7);
-                    }
-                    if (imB != 0.f) {
-                        const unsigned long long cm = __ldcg(&a.flow_mask[iB]);
-                        flow |= ((unsigned)__popcll(cm) | ((unsigned)__popcll(cm & below) << 7)) << 13;
-                    }
-                }
-            }
-            a.hdr_ord[k] = make_int4(iA, iB, mask, (int)flow);
-        } else {
             a.hdr[m] = make_int4(iA, iB, mask, np);
+            continue;
         }
+        a.inv_mass_ord[k] = make_float4(imA, imB, 0.f, 0.f);
+        // the dataflow sweeps' per-body update numbers, packed: for each dynamic body its
+        // manifolds' colour count (7 bits) and the rank of this manifold's colour among them
+        // (6 bits); A in the low 13 bits, B in the next 13
+        unsigned flow = 0;
+        if (a.flow_mask) {
+            const int c = __ldcg(&a.color[m]);
+            if (c >= 0) {
+                const unsigned long long below = (1ull << c) - 1ull;
+                if (imA != 0.f) {
+                    const unsigned long long cm = __ldcg(&a.flow_mask[iA]);
+                    flow |= (unsigned)__popcll(cm) | ((unsigned)__popcll(cm & below) << 7);
+                }
+                if (imB != 0.f) {
+                    const unsigned long long cm = __ldcg(&a.flow_mask[iB]);
+                    flow |= ((unsigned)__popcll(cm) | ((unsigned)__popcll(cm & below) << 7)) << 13;
+                }
+            }
+        }
+        a.hdr_ord[k] = make_int4(iA, iB, mask, (int)flow);
     }
 }
 
@@ -1631,34 +1652,57 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_colour(SolverArgs a) {
     const unsigned nb = gridDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int stride = gridDim.x * blockDim.x;
-    // carried colours claim their mask bits; a clash on a body drops the manifold to recolouring
+    // carried colours claim their mask bits; a clash on a body drops the manifold to recolouring.
+    // The manifolds left without a colour (new ones, dropped ones) are listed (in pos_of, which the
+    // scatter below overwrites), so that the colouring rounds visit only them.
     int dropped = 0;
-    if (*((volatile int*)a.d_new) < nc) {
-        for (int m = tid; m < nc; m += stride) {
-            const int c = a.color[m];
-            if (c < 0) continue;
-            const int4 h = a.hdr[m];
-            const float2 im = a.inv_mass[m];
-            const unsigned long long bit = 1ull << c;
-            bool clash = false;
-            if (im.x != 0.f) clash |= (atomicOr(&a.mask[h.x], bit) & bit) != 0ull;
-            if (im.y != 0.f) clash |= (atomicOr(&a.mask[h.y], bit) & bit) != 0ull;
-            if (clash) {
-                a.color[m] = -1;
-                dropped++;
+    const bool carried = *((volatile int*)a.d_new) < nc;
+    int* list = a.pos_of;
+    unsigned int* list_n = a.bar2.count + 8;  // zeroed by k_reset_solver
+    if (carried) {
+        const int lane = threadIdx.x & 31;
+        for (int m0 = tid - lane; m0 < nc; m0 += stride) {  // warp-uniform: every lane reaches the ballot
+            const int m = m0 + lane;
+            bool unc = false;
+            if (m < nc) {
+                const int c = a.color[m];
+                if (c < 0) {
+                    unc = true;
+                } else {
+                    const int4 h = a.hdr[m];
+                    const float2 im = a.inv_mass[m];
+                    const unsigned long long bit = 1ull << c;
+                    bool clash = false;
+                    if (im.x != 0.f) clash |= (atomicOr(&a.mask[h.x], bit) & bit) != 0ull;
+                    if (im.y != 0.f) clash |= (atomicOr(&a.mask[h.y], bit) & bit) != 0ull;
+                    if (clash) {
+                        a.color[m] = -1;
+                        dropped++;
+                        unc = true;
+                    }
+                }
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, unc);
+            if (bal) {
+                int base = 0;
+                if (lane == 0) base = (int)atomicAdd(list_n, (unsigned)__popc(bal));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (unc) list[base + __popc(bal & ((1u << lane) - 1u))] = m;
             }
         }
     }
     for (int o = 16; o; o >>= 1) dropped += __shfl_xor_sync(0xffffffffu, dropped, o);
     if ((threadIdx.x & 31) == 0 && dropped) atomicAdd(a.d_new, dropped);
     if (!grid_barrier(a.bar2, nb, a.spin_limit)) return;
+    const int nlist = carried ? (int)*((volatile unsigned int*)list_n) : nc;
     // Jones-Plassmann rounds over the uncoloured manifolds (the highest hashed priority on both of
     // its dynamic bodies takes the smallest colour free on both); statics never conflict
     bool overflow = false;
     if (*((volatile int*)a.d_new) > 0) {
         for (int r = 0; r < B3G_MAX_COLORS; r++) {
             const unsigned long long rk = (unsigned long long)r << 56;
-            for (int m = tid; m < nc; m += stride) {
+            for (int idx = tid; idx < nlist; idx += stride) {
+                const int m = carried ? __ldcg(&list[idx]) : idx;
                 if (a.color[m] >= 0) continue;
                 const int4 h = a.hdr[m];
                 const float2 im = a.inv_mass[m];
@@ -1669,7 +1713,8 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_colour(SolverArgs a) {
             }
             if (!grid_barrier(a.bar2, nb, a.spin_limit)) return;
             int left = 0;
-            for (int m = tid; m < nc; m += stride) {
+            for (int idx = tid; idx < nlist; idx += stride) {
+                const int m = carried ? __ldcg(&list[idx]) : idx;
                 if (a.color[m] >= 0) continue;
                 const int4 h = a.hdr[m];
                 const float2 im = a.inv_mass[m];
@@ -2099,6 +2144,7 @@ __global__ void k_reset_solver(int* color_fill, int* remaining, int* color_curso
         barrier[threadIdx.x] = 0;       // the sweeps' grid barrier
         barrier[16 + threadIdx.x] = 0;  // k_colour's
     }
+    if (threadIdx.x == 0) barrier[24] = 0;  // k_colour's count of manifolds to colour
     if (threadIdx.x == 0) {
         counters->iterations = 0;
         counters->residual = 0.f;
@@ -2243,8 +2289,10 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
         a.pos_of = d.manifold_pos;
         a.color_fill = color_fill;
         a.color_cursor = color_cursor;
-        a.flow_mask = d.color_claim + 2 * (size_t)d.num_bodies;            // zeroed above each solve
-        a.version = reinterpret_cast<unsigned int*>(d.body_manifold_count);  // zeroed above each solve
+        if (flow) {  // the per-body colour sets and update counters of the dataflow sweeps
+            a.flow_mask = d.color_claim + 2 * (size_t)d.num_bodies;            // zeroed above each solve
+            a.version = reinterpret_cast<unsigned int*>(d.body_manifold_count);  // zeroed above each solve
+        }
         k_manifold_prep<<<grid, SV_THREADS, 0, s>>>(a);
         launches++;
         cudaLaunchConfig_t lc = {};
@@ -2273,7 +2321,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
         exclusive_scan_i32(d.prim, d.body_manifold_count, d.body_list_offsets, d.d_num_bodies, nullptr,
                            d.scan_scratch, s, &ll);
     }
-    k_setup_rows<<<grid, SV_THREADS, 0, s>>>(a);
+    k_setup_rows<<<grid * 4, SV_THREADS, 0, s>>>(a);  // a thread per contact point
     launches++;
     if (wm != B3G_WARM_COLD && d.ws_init) {
         // initial impulses: persisting points from the previous solve, the others from the network
