@@ -588,7 +588,7 @@ __global__ void __launch_bounds__(HH_WARPS * 32) k_hull_hull(NPArgs a, int max_p
 // returns false there) -- then the same clip and reduction.  Bit-identical to the warp path.
 static constexpr int SMALL_CLIP = 2 * B3G_SMALL_FACE_VERTS;
 
-__global__ void __launch_bounds__(NP_THREADS) k_hull_hull_small(NPArgs a, int max_pairs) {
+__global__ void __launch_bounds__(NP_THREADS, 3) k_hull_hull_small(NPArgs a, int max_pairs) {
     const int n = a.type_count[PT_HULL_HULL_SMALL];
     const int* list = a.type_list + (size_t)PT_HULL_HULL_SMALL * max_pairs;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {

@@ -150,7 +150,7 @@ __global__ void k_count_manifolds(const b3gContact4* __restrict__ slots, const i
 // One thread per contact point (the 4 point slots of a manifold are 4 consecutive lanes of a
 // warp): the point's contact row and two friction rows; lane 0 of the 4 writes the manifold's
 // header with the point mask (a ballot over the 4).
-__global__ void __launch_bounds__(SV_THREADS) k_setup_rows(SolverArgs a) {
+__global__ void __launch_bounds__(SV_THREADS, 3) k_setup_rows(SolverArgs a) {
     const int nc = *a.d_nc;
     const bool pgs = a.mode == B3G_SOLVER_PGS;
     if (a.ws_rows && blockIdx.x == 0 && threadIdx.x == 0) *a.ws_rows = min(4 * nc, a.ws_rows_cap);
@@ -1791,14 +1791,16 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_colour(SolverArgs a) {
             // carried colours drift upwards as contacts come and go (a new manifold takes the
             // smallest colour its bodies leave free): the next solve colours from scratch again
             // when this one has more than one colour past the last colouring from scratch, and
-            // every 32 solves in any case (so that the baseline follows the scene)
+            // every 8 solves in any case, so that the baseline follows the scene (a colouring
+            // from scratch costs about one colour's sweep time on a 262k-box pile; a drifted
+            // colouring costs one per extra colour and sweep)
             if (*((volatile int*)a.d_new) >= nc) {
                 a.d_prev_n[1] = ncl;
                 a.d_prev_n[2] = 0;
                 a.d_prev_n[3] = 0;
             } else {
                 const int since = ++a.d_prev_n[3];
-                if (ncl > a.d_prev_n[1] + 1 || since >= 32) a.d_prev_n[2] = 1;
+                if (ncl > a.d_prev_n[1] + 1 || since >= 8) a.d_prev_n[2] = 1;
             }
         }
     }

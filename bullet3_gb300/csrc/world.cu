@@ -1580,7 +1580,12 @@ extern "C" b3gStatus b3g_read_bodies(b3g_handle h, void* host, int n) {
 extern "C" b3gStatus b3g_write_bodies(b3g_handle h, const void* host, int n) {
     REQUIRE_UPLOADED(h);
     if (!host || n < 0 || n > h->d.num_bodies) return fail(B3G_ERR_INVALID_ARG, "bad body buffer");
-    return copy_in(h, h->d.bodies, host, sizeof(b3gBody) * n);
+    TRY(copy_in(h, h->d.bodies, host, sizeof(b3gBody) * n));
+    // a body state from the host may be anywhere: the next PGS solve colours from scratch rather
+    // than carrying the last solve's colours over
+    static const int recolour = 1;
+    CUDA_TRY(cudaMemcpyAsync(h->d.prev_mn + 2, &recolour, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    return B3G_OK;
 }
 extern "C" b3gStatus b3g_read_inertias(b3g_handle h, void* host, int n) {
     REQUIRE_UPLOADED(h);
