@@ -1646,6 +1646,56 @@ __global__ void __launch_bounds__(SV_THREADS) k_manifold_prep(SolverArgs a) {
 
 // Cooperative: carried colours, Jones-Plassmann for the rest, record positions.  Colour 64 holds
 // the manifolds that found no colour below 64 (solved one after another by one thread).
+// One Jones-Plassmann round over the uncoloured manifolds [first, nlist) step `step` of the list
+// (or the manifold indices themselves when !listed): claim -- each manifold's key (round, hashed
+// priority, index) into both dynamic bodies' claim words (atomic max); assign -- a manifold that
+// holds both claims takes the smallest colour free on both bodies.  Returns the manifolds left.
+constexpr int JP_LOCAL_MAX = 8192;
+__device__ __forceinline__ unsigned long long jp_key(int r, int m) {
+    return ((unsigned long long)r << 56) | ((unsigned long long)(hash32((unsigned)m) & 0xFFFFFFu) << 32) | (unsigned)m;
+}
+__device__ __forceinline__ void jp_claim(const SolverArgs& a, int r, const int* list, bool listed, int nlist,
+                                         int first, int step) {
+    for (int idx = first; idx < nlist; idx += step) {
+        const int m = listed ? __ldcg(&list[idx]) : idx;
+        if (a.color[m] >= 0) continue;
+        const int4 h = a.hdr[m];
+        const float2 im = a.inv_mass[m];
+        const unsigned long long key = jp_key(r, m);
+        if (im.x != 0.f) atomicMax(&a.claim[h.x], key);
+        if (im.y != 0.f) atomicMax(&a.claim[h.y], key);
+    }
+}
+__device__ __forceinline__ int jp_assign(const SolverArgs& a, int r, const int* list, bool listed, int nlist,
+                                         int first, int step) {
+    int left = 0;
+    for (int idx = first; idx < nlist; idx += step) {
+        const int m = listed ? __ldcg(&list[idx]) : idx;
+        if (a.color[m] >= 0) continue;
+        const int4 h = a.hdr[m];
+        const float2 im = a.inv_mass[m];
+        const unsigned long long key = jp_key(r, m);
+        const bool okA = im.x == 0.f || __ldcg(&a.claim[h.x]) == key;
+        const bool okB = im.y == 0.f || __ldcg(&a.claim[h.y]) == key;
+        if (okA && okB) {
+            unsigned long long used = 0ull;
+            if (im.x != 0.f) used |= __ldcg(&a.mask[h.x]);
+            if (im.y != 0.f) used |= __ldcg(&a.mask[h.y]);
+            const int c = __ffsll((long long)~used) - 1;
+            if (c >= 0 && c < 64) {
+                a.color[m] = c;
+                if (im.x != 0.f) atomicOr(&a.mask[h.x], 1ull << c);
+                if (im.y != 0.f) atomicOr(&a.mask[h.y], 1ull << c);
+            } else {
+                left++;
+            }
+        } else {
+            left++;
+        }
+    }
+    return left;
+}
+
 __global__ void __launch_bounds__(PK_THREADS, 1) k_colour(SolverArgs a) {
     grid_barrier_begin();
     const int nc = *a.d_nc;
@@ -1696,53 +1746,40 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_colour(SolverArgs a) {
     if (!grid_barrier(a.bar2, nb, a.spin_limit)) return;
     const int nlist = carried ? (int)*((volatile unsigned int*)list_n) : nc;
     // Jones-Plassmann rounds over the uncoloured manifolds (the highest hashed priority on both of
-    // its dynamic bodies takes the smallest colour free on both); statics never conflict
+    // its dynamic bodies takes the smallest colour free on both); statics never conflict.  A short
+    // list (new contacts between colourings from scratch) is coloured by block 0 alone, with
+    // __syncthreads between the halves of a round instead of grid barriers.
     bool overflow = false;
     if (*((volatile int*)a.d_new) > 0) {
-        for (int r = 0; r < B3G_MAX_COLORS; r++) {
-            const unsigned long long rk = (unsigned long long)r << 56;
-            for (int idx = tid; idx < nlist; idx += stride) {
-                const int m = carried ? __ldcg(&list[idx]) : idx;
-                if (a.color[m] >= 0) continue;
-                const int4 h = a.hdr[m];
-                const float2 im = a.inv_mass[m];
-                const unsigned long long key =
-                    rk | ((unsigned long long)(hash32((unsigned)m) & 0xFFFFFFu) << 32) | (unsigned)m;
-                if (im.x != 0.f) atomicMax(&a.claim[h.x], key);
-                if (im.y != 0.f) atomicMax(&a.claim[h.y], key);
-            }
-            if (!grid_barrier(a.bar2, nb, a.spin_limit)) return;
-            int left = 0;
-            for (int idx = tid; idx < nlist; idx += stride) {
-                const int m = carried ? __ldcg(&list[idx]) : idx;
-                if (a.color[m] >= 0) continue;
-                const int4 h = a.hdr[m];
-                const float2 im = a.inv_mass[m];
-                const unsigned long long key =
-                    rk | ((unsigned long long)(hash32((unsigned)m) & 0xFFFFFFu) << 32) | (unsigned)m;
-                const bool okA = im.x == 0.f || __ldcg(&a.claim[h.x]) == key;
-                const bool okB = im.y == 0.f || __ldcg(&a.claim[h.y]) == key;
-                if (okA && okB) {
-                    unsigned long long used = 0ull;
-                    if (im.x != 0.f) used |= __ldcg(&a.mask[h.x]);
-                    if (im.y != 0.f) used |= __ldcg(&a.mask[h.y]);
-                    const int c = __ffsll((long long)~used) - 1;
-                    if (c >= 0 && c < 64) {
-                        a.color[m] = c;
-                        if (im.x != 0.f) atomicOr(&a.mask[h.x], 1ull << c);
-                        if (im.y != 0.f) atomicOr(&a.mask[h.y], 1ull << c);
-                    } else {
-                        left++;
-                    }
-                } else {
-                    left++;
+        if (carried && nlist <= JP_LOCAL_MAX) {
+            if (blockIdx.x == 0) {
+                __shared__ int s_left;
+                for (int r = 0; r < B3G_MAX_COLORS; r++) {
+                    if (threadIdx.x == 0) s_left = 0;
+                    jp_claim(a, r, list, true, nlist, threadIdx.x, blockDim.x);
+                    __syncthreads();
+                    int left = jp_assign(a, r, list, true, nlist, threadIdx.x, blockDim.x);
+                    for (int o = 16; o; o >>= 1) left += __shfl_xor_sync(0xffffffffu, left, o);
+                    if ((threadIdx.x & 31) == 0 && left) atomicAdd(&s_left, left);
+                    __syncthreads();
+                    const int l = s_left;
+                    __syncthreads();
+                    if (l == 0) break;
+                    overflow = r == B3G_MAX_COLORS - 1;
                 }
             }
-            for (int o = 16; o; o >>= 1) left += __shfl_xor_sync(0xffffffffu, left, o);
-            if ((threadIdx.x & 31) == 0 && left) atomicAdd(&a.remaining[r], left);
             if (!grid_barrier(a.bar2, nb, a.spin_limit)) return;
-            if (*((volatile int*)&a.remaining[r]) == 0) break;
-            overflow = r == B3G_MAX_COLORS - 1;
+        } else {
+            for (int r = 0; r < B3G_MAX_COLORS; r++) {
+                jp_claim(a, r, list, carried, nlist, tid, stride);
+                if (!grid_barrier(a.bar2, nb, a.spin_limit)) return;
+                int left = jp_assign(a, r, list, carried, nlist, tid, stride);
+                for (int o = 16; o; o >>= 1) left += __shfl_xor_sync(0xffffffffu, left, o);
+                if ((threadIdx.x & 31) == 0 && left) atomicAdd(&a.remaining[r], left);
+                if (!grid_barrier(a.bar2, nb, a.spin_limit)) return;
+                if (*((volatile int*)&a.remaining[r]) == 0) break;
+                overflow = r == B3G_MAX_COLORS - 1;
+            }
         }
     }
     // the exact colour set of every body (the masks above may hold bits of dropped carried
@@ -1776,9 +1813,10 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_colour(SolverArgs a) {
     if (blockIdx.x == 0) {
         const int total = block_exclusive_scan(cb, cb_off, 65 * G);
         for (int k = threadIdx.x; k < 65; k += blockDim.x) {
-            a.color_goff[k] = cb_off[k * G];
-            a.color_fill[k] = 0;
-            for (int g = 0; g < G; g++) a.color_fill[k] += cb[k * G + g];
+            // (key-major scan: a key's count is the step to the next key's first offset)
+            const int o = __ldcg(&cb_off[k * G]);
+            a.color_goff[k] = o;
+            a.color_fill[k] = (k < 64 ? __ldcg(&cb_off[(k + 1) * G]) : total) - o;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
