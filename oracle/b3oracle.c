@@ -19,6 +19,7 @@
 #define SHAPE_CONVEX_HULL 3
 #define SHAPE_PLANE 4
 #define SHAPE_SPHERE 7
+#define SHAPE_COMPOUND_OF_CONVEX_HULLS 6
 
 static int g_threads = 1;
 int oracle_num_threads(void) {
@@ -737,6 +738,272 @@ int oracle_contacts(const obody* bodies, const oshapes* sh, opair* pairs, int np
     free(tmp);
     free(has);
     return n;
+}
+
+/* ------------------------------------------------------------------ compound shapes
+ * A compound (SHAPE_COMPOUND_OF_CONVEX_HULLS) lists child convex hulls with local poses.  Its
+ * pairs expand to child pairs in the order (pair, child of A, child of B) -- the set of
+ * findCompoundPairsKernel (b3ConvexHullContact.cpp:1419-1775): compound-compound child pairs whose
+ * world AABBs overlap (the reference walks quantized child BVHs, whose conservative boxes add only
+ * child pairs that cannot touch), compound-hull every child against the hull, plane-compound
+ * every child against the plane.  Each child pair yields at most one manifold. */
+
+/* child pose: newPos = b3QuatRotate(orn, childPos) + pos, newOrn = b3QuatMul(orn, childOrn)
+ * (processCompoundPairsKernel, b3ConvexHullContact.cpp:1813-1829) */
+static void child_pose(const obody* b, const ochild* ch, v3* pos, qt* orn) {
+    qt q = f4q(b->quat);
+    *pos = add(qrotq(q, f4v(ch->pos)), f4v(b->pos));
+    *orn = qmul(q, f4q(ch->orn));
+}
+
+static int is_compound(const oshapes* sh, const obody* b) {
+    return sh->cols[b->collidableIdx].shapeType == SHAPE_COMPOUND_OF_CONVEX_HULLS;
+}
+
+/* registerCompoundShape's local AABB (b3GpuNarrowPhase.cpp:391-431): the union (b3Vector3 setMin /
+ * setMax) of the children's local AABBs moved by b3TransformAabb with margin 0 into the compound's
+ * frame (the same arithmetic as b3TransformAabb2 of a quaternion pose) */
+void oracle_compound_local_aabb(const oaabb* child_local, const ochild* children, int n, oaabb* out) {
+    v3 mn = mk(1e30f, 1e30f, 1e30f), mx = mk(-1e30f, -1e30f, -1e30f);
+    int i;
+    for (i = 0; i < n; i++) {
+        v3 a, b;
+        transform_aabb(&child_local[i], f4v(children[i].pos), f4q(children[i].orn), 0.f, &a, &b);
+        if (a.x < mn.x) mn.x = a.x;
+        if (a.y < mn.y) mn.y = a.y;
+        if (a.z < mn.z) mn.z = a.z;
+        if (mx.x < b.x) mx.x = b.x;
+        if (mx.y < b.y) mx.y = b.y;
+        if (mx.z < b.z) mx.z = b.z;
+    }
+    out->minv[0] = mn.x; out->minv[1] = mn.y; out->minv[2] = mn.z; out->minw = 0;
+    out->maxv[0] = mx.x; out->maxv[1] = mx.y; out->maxv[2] = mx.z; out->maxw = 0;
+}
+
+int oracle_compound_pairs(const obody* bodies, const oshapes* sh, const opair* pairs, int npairs, opair* out,
+                          int cap) {
+    int p, n = 0;
+    for (p = 0; p < npairs; p++) {
+        const int A = pairs[p].x, B = pairs[p].y;
+        const ocollidable* cA = &sh->cols[bodies[A].collidableIdx];
+        const ocollidable* cB = &sh->cols[bodies[B].collidableIdx];
+        const int compA = cA->shapeType == SHAPE_COMPOUND_OF_CONVEX_HULLS;
+        const int compB = cB->shapeType == SHAPE_COMPOUND_OF_CONVEX_HULLS;
+        int a, b;
+        if (!compA && !compB) continue;
+        /* once the broadphase avoids static-static pairs this test goes (findCompoundPairsKernel :1446) */
+        if (bodies[A].invMass == 0.f && bodies[B].invMass == 0.f) continue;
+        if (compA && compB) {
+            for (a = 0; a < cA->numChildShapes; a++) {
+                const ochild* chA = &sh->children[cA->shapeIndex + a];
+                oaabb la = sh->local_aabbs[chA->shapeIndex], wa;
+                v3 pA, mnA, mxA;
+                qt qA;
+                child_pose(&bodies[A], chA, &pA, &qA);
+                transform_aabb(&la, pA, qA, 0.f, &mnA, &mxA);
+                wa.minv[0] = mnA.x; wa.minv[1] = mnA.y; wa.minv[2] = mnA.z;
+                wa.maxv[0] = mxA.x; wa.maxv[1] = mxA.y; wa.maxv[2] = mxA.z;
+                for (b = 0; b < cB->numChildShapes; b++) {
+                    const ochild* chB = &sh->children[cB->shapeIndex + b];
+                    oaabb lb = sh->local_aabbs[chB->shapeIndex], wb;
+                    v3 pB, mnB, mxB;
+                    qt qB;
+                    child_pose(&bodies[B], chB, &pB, &qB);
+                    transform_aabb(&lb, pB, qB, 0.f, &mnB, &mxB);
+                    wb.minv[0] = mnB.x; wb.minv[1] = mnB.y; wb.minv[2] = mnB.z;
+                    wb.maxv[0] = mxB.x; wb.maxv[1] = mxB.y; wb.maxv[2] = mxB.z;
+                    if (!overlap(&wa, &wb)) continue;
+                    if (n < cap) { out[n].x = A; out[n].y = B; out[n].z = cA->shapeIndex + a; out[n].w = cB->shapeIndex + b; }
+                    n++;
+                }
+            }
+        } else if (compA) {
+            for (a = 0; a < cA->numChildShapes; a++) {
+                if (n < cap) { out[n].x = A; out[n].y = B; out[n].z = cA->shapeIndex + a; out[n].w = -1; }
+                n++;
+            }
+        } else {
+            for (b = 0; b < cB->numChildShapes; b++) {
+                if (n < cap) { out[n].x = A; out[n].y = B; out[n].z = -1; out[n].w = cB->shapeIndex + b; }
+                n++;
+            }
+        }
+    }
+    return n;
+}
+
+/* findSeparatingAxisEdgeEdge (b3ConvexHullContact.cpp:702-785): every edge-edge axis projected
+ * (no early exit, the separation test is discarded), the smallest overlap kept in *sep / *dmin */
+static void edge_edge_axis(const ohull* hA, const ohull* hB, v3 posA, qt qA, v3 posB, qt qB, v3 deltaC2,
+                           const oshapes* sh, v3* sep, float* dmin) {
+    int e0, e1;
+    for (e0 = 0; e0 < hA->numUniqueEdges; e0++) {
+        v3 w0 = qrotq(qA, f4v(sh->edges[hA->uniqueEdgesOffset + e0]));
+        for (e1 = 0; e1 < hB->numUniqueEdges; e1++) {
+            v3 w1 = qrotq(qB, f4v(sh->edges[hB->uniqueEdgesOffset + e1]));
+            v3 cr = cross(w0, w1);
+            if ((double)fabsf(cr.x) > 1e-6 || (double)fabsf(cr.y) > 1e-6 || (double)fabsf(cr.z) > 1e-6) {
+                float min0, max0, min1, max1, d0, d1, dist;
+                cr = nrm(cr);
+                if (dot(deltaC2, cr) < 0.f) cr = neg(cr);
+                project(&sh->verts[hA->vertexOffset], hA->numVertices, posA, qA, cr, &min0, &max0);
+                project(&sh->verts[hB->vertexOffset], hB->numVertices, posB, qB, cr, &min1, &max1);
+                d0 = max0 - min1;
+                d1 = max1 - min0;
+                dist = d0 < d1 ? d0 : d1;
+                if (dist < *dmin) { *dmin = dist; *sep = cr; }
+            }
+        }
+    }
+    if (dot(neg(deltaC2), *sep) > 0.0f) *sep = neg(*sep);
+}
+
+/* clipHullAgainstHull -> clipFaceAgainstHull -> clipFace (b3ConvexHullContact.cpp:939-1044,
+ * :834-937, :787-832): incident face of B by max dot with the separating normal, reference face of
+ * A by min, points behind A's side planes, depth clamped at minDist and kept if <= maxDist (at most
+ * 64); rotations by b3QuatRotate of the poses themselves, points by b3Transform */
+static int clip_hull_against_hull(v3 sep, const ohull* hA, const ohull* hB, v3 posA, qt qA, v3 posB, qt qB,
+                                  float minDist, float maxDist, const oshapes* sh, p4* out) {
+    m3 RA = qmat(qA), RB = qmat(qB);
+    p4 buf0[CLIP_CAP], buf1[CLIP_CAP];
+    p4 *pin = buf0, *pout = buf1;
+    int fb = -1, fa = -1, f, nin = 0, e, e0, nva, n = 0, i;
+    float dmax = -FLT_MAX, dmn = FLT_MAX, planeEqWS;
+    v3 planeNormalWS;
+    const oface *polyA, *polyB;
+    for (f = 0; f < hB->numFaces; f++) {
+        float d = dot(qrotq(qB, f4v(sh->faces[hB->faceOffset + f].plane)), sep);
+        if (d > dmax) { dmax = d; fb = f; }
+    }
+    if (fb < 0) return 0;
+    polyB = &sh->faces[hB->faceOffset + fb];
+    for (e = 0; e < polyB->numIndices && e < CLIP_CAP; e++) {
+        v3 w = add(mmul(&RB, f4v(sh->verts[hB->vertexOffset + sh->indices[polyB->indexOffset + e]])), posB);
+        pin[nin].x = w.x; pin[nin].y = w.y; pin[nin].z = w.z; pin[nin].w = 0.f;
+        nin++;
+    }
+    for (f = 0; f < hA->numFaces; f++) {
+        float d = dot(qrotq(qA, f4v(sh->faces[hA->faceOffset + f].plane)), sep);
+        if (d < dmn) { dmn = d; fa = f; }
+    }
+    if (fa < 0) return 0;
+    polyA = &sh->faces[hA->faceOffset + fa];
+    nva = polyA->numIndices;
+    for (e0 = 0; e0 < nva; e0++) {
+        v3 a = f4v(sh->verts[hA->vertexOffset + sh->indices[polyA->indexOffset + e0]]);
+        v3 b = f4v(sh->verts[hA->vertexOffset + sh->indices[polyA->indexOffset + ((e0 + 1) % nva)]]);
+        v3 worldEdge0 = qrotq(qA, sub(a, b));
+        v3 worldPlaneAnormal1 = qrotq(qA, mk(polyA->plane.x, polyA->plane.y, polyA->plane.z));
+        v3 planeNormalWS1 = neg(cross(worldEdge0, worldPlaneAnormal1));
+        v3 worldA1 = add(mmul(&RA, a), posA);
+        float planeEqWS1 = -dot(worldA1, planeNormalWS1);
+        int nout = clip_face(pin, nin, planeNormalWS1, planeEqWS1, pout);
+        p4* tmp = pout; pout = pin; pin = tmp;
+        nin = nout;
+    }
+    planeNormalWS = qrotq(qA, mk(polyA->plane.x, polyA->plane.y, polyA->plane.z));
+    planeEqWS = polyA->plane.w - dot(planeNormalWS, posA);
+    for (i = 0; i < nin; i++) {
+        float depth = dot(planeNormalWS, mk(pin[i].x, pin[i].y, pin[i].z)) + planeEqWS;
+        if (depth <= minDist) depth = minDist;
+        if (n < CLIP_CAP && depth <= maxDist) {
+            out[n].x = pin[i].x; out[n].y = pin[i].y; out[n].z = pin[i].z; out[n].w = depth;
+            n++;
+        }
+    }
+    return n;
+}
+
+/* processCompoundPairsKernel + clipCompoundsHullHullKernel (b3ConvexHullContact.cpp:1777-2022)
+ * for one child pair of hulls: the separating axis of findSeparatingAxis(A, B), then of
+ * findSeparatingAxis(B, A) (which overwrites it), then the edge-edge pass from FLT_MAX; clipped
+ * with minDist -1e30, maxDist 0, reduced by extractManifoldSequentialGlobal against -sep */
+static int compound_hulls(const obody* bodies, const oshapes* sh, const opair* cp, int index, ocontact* c) {
+    const obody* BA = &bodies[cp->x];
+    const obody* BB = &bodies[cp->y];
+    v3 posA = f4v(BA->pos), posB = f4v(BB->pos), sep = mk(1.f, 0.f, 0.f), deltaC2;
+    qt qA = f4q(BA->quat), qB = f4q(BB->quat);
+    int colA = BA->collidableIdx, colB = BB->collidableIdx, np, idx[4], q;
+    const ohull *hA, *hB;
+    m3 RA, RB;
+    p4 pts[CLIP_CAP];
+    float dmin = FLT_MAX;
+    if (cp->z >= 0) { colA = sh->children[cp->z].shapeIndex; child_pose(BA, &sh->children[cp->z], &posA, &qA); }
+    if (cp->w >= 0) { colB = sh->children[cp->w].shapeIndex; child_pose(BB, &sh->children[cp->w], &posB, &qB); }
+    if (sh->cols[colA].shapeType != SHAPE_CONVEX_HULL || sh->cols[colB].shapeType != SHAPE_CONVEX_HULL) return 0;
+    hA = &sh->hulls[sh->cols[colA].shapeIndex];
+    hB = &sh->hulls[sh->cols[colB].shapeIndex];
+    RA = qmat(qA);
+    RB = qmat(qB);
+    deltaC2 = sub(add(mmul(&RA, f4v(hA->localCenter)), posA), add(mmul(&RB, f4v(hB->localCenter)), posB));
+    if (!find_separating_axis(hA, hB, posA, qA, posB, qB, sh, &sep)) return 0;
+    if (!find_separating_axis(hB, hA, posB, qB, posA, qA, sh, &sep)) return 0;
+    edge_edge_axis(hA, hB, posA, qA, posB, qB, deltaC2, sh, &sep, &dmin);
+    np = clip_hull_against_hull(sep, hA, hB, posA, qA, posB, qB, -1e30f, 0.0f, sh, pts);
+    if (np <= 0) return 0;
+    np = reduce_contacts(pts, np, neg(sep), idx);
+    write_header(c, bodies, cp->x, cp->y, sep, np, (unsigned short)(0.7f * 0xffff));
+    c->batchIdx = index;
+    c->childIndexA = cp->z;
+    c->childIndexB = cp->w;
+    for (q = 0; q < np; q++) {
+        p4 v = pts[idx[q]];
+        c->worldPosB[q].x = v.x; c->worldPosB[q].y = v.y; c->worldPosB[q].z = v.z; c->worldPosB[q].w = v.w;
+    }
+    return 1;
+}
+
+/* computeContactPlaneCompound (b3ConvexHullContact.cpp:2182-2321), one child: A = plane body, B =
+ * compound body, child = child shape index; the plane-hull contact with the child's pose */
+static int plane_child(const obody* bodies, const oshapes* sh, int A, int B, int child, int index, ocontact* c) {
+    obody body = bodies[B];
+    const ochild* ch = &sh->children[child];
+    v3 pos;
+    qt orn;
+    int r;
+    child_pose(&bodies[B], ch, &pos, &orn);
+    body.pos.x = pos.x; body.pos.y = pos.y; body.pos.z = pos.z;
+    body.quat.x = orn.x; body.quat.y = orn.y; body.quat.z = orn.z; body.quat.w = orn.w;
+    body.collidableIdx = ch->shapeIndex;
+    {
+        /* plane_hull reads both bodies from one array: a two-body view with the child in B's place */
+        obody two[2];
+        two[0] = bodies[A];
+        two[1] = body;
+        r = plane_hull(two, sh, 0, 1, c, (unsigned short)(0.7f * 0xffff));
+    }
+    if (r) {
+        c->bodyA = sgn_index(bodies, A);
+        c->bodyB = sgn_index(bodies, B);
+        c->batchIdx = index;
+        c->childIndexA = -1;
+        c->childIndexB = child;
+    }
+    return r;
+}
+
+int oracle_compound_contacts(const obody* bodies, const oshapes* sh, const opair* child_pairs, int n, ocontact* out,
+                             int* out_index, int cap) {
+    int i, m = 0;
+    for (i = 0; i < n; i++) {
+        const opair* cp = &child_pairs[i];
+        ocontact c;
+        int tA = cp->z >= 0 ? SHAPE_CONVEX_HULL : sh->cols[bodies[cp->x].collidableIdx].shapeType;
+        int tB = cp->w >= 0 ? SHAPE_CONVEX_HULL : sh->cols[bodies[cp->y].collidableIdx].shapeType;
+        int r = 0;
+        memset(&c, 0, sizeof(c));
+        if (tA == SHAPE_CONVEX_HULL && tB == SHAPE_CONVEX_HULL)
+            r = compound_hulls(bodies, sh, cp, i, &c);
+        else if (tA == SHAPE_PLANE && cp->w >= 0)
+            r = plane_child(bodies, sh, cp->x, cp->y, cp->w, i, &c);
+        else if (tB == SHAPE_PLANE && cp->z >= 0)
+            r = plane_child(bodies, sh, cp->y, cp->x, cp->z, i, &c);
+        if (r) {
+            if (m < cap) { out[m] = c; if (out_index) out_index[m] = i; }
+            m++;
+        }
+    }
+    return m;
 }
 
 /* ------------------------------------------------------------------ solver */

@@ -40,6 +40,9 @@ typedef struct {
     int batchIdx, bodyA, bodyB, childIndexA, childIndexB, unused1, unused2;
 } ocontact;
 typedef struct { int x, y, z, w; } opair;
+/* b3GpuChildShape (Bullet3Collision/NarrowPhaseCollision/shared/b3Collidable.h:41-62): child pose
+ * and its convex hull collidable */
+typedef struct { of4 pos, orn; int shapeIndex, numChildShapes, collidableShapeIndex, shapeType; } ochild;
 
 typedef struct {
     const ocollidable* cols;
@@ -50,6 +53,7 @@ typedef struct {
     const of4* verts;
     const of4* edges;
     int num_collidables;
+    const ochild* children; /* child shapes of the compounds (collidable.shapeIndex = first child) */
 } oshapes;
 
 /* 1 = OpenMP threads available in this build */
@@ -72,6 +76,19 @@ int oracle_pairs_grid(const oaabb* aabbs, int n, float cell, opair* out, int cap
  * writes pair.z = manifold index or -1.  See b3oracle.c for the per-shape reference functions. */
 int oracle_contacts(const obody* bodies, const oshapes* sh, opair* pairs, int npairs, ocontact* out, int cap,
                     unsigned short friction_cmp);
+
+/* Local AABB of a compound of n children (child_local[i] = the local AABB of child i's hull). */
+void oracle_compound_local_aabb(const oaabb* child_local, const ochild* children, int n, oaabb* out);
+/* Compound pairs: the child pairs (bodyA, bodyB, child shape of A or -1, child shape of B or -1) of
+ * every pair with a compound, in (pair, child of A, child of B) order; returns the count (only cap
+ * written). */
+int oracle_compound_pairs(const obody* bodies, const oshapes* sh, const opair* pairs, int npairs, opair* out,
+                          int cap);
+/* One manifold or none per child pair (hull children: processCompoundPairsKernel +
+ * clipCompoundsHullHullKernel; plane against a child: computeContactPlaneCompound), in child-pair
+ * order; out_index[m] = child pair index.  Returns the count. */
+int oracle_compound_contacts(const obody* bodies, const oshapes* sh, const opair* child_pairs, int n, ocontact* out,
+                             int* out_index, int cap);
 
 /* b3PgsJacobiSolver::solveGroup (Bullet3Dynamics/ConstraintSolver/b3PgsJacobiSolver.cpp:170)
  * with USE_2_FRICTION_DIRECTIONS, no warm start, no split impulse, erp, contact threshold.

@@ -24,11 +24,14 @@ CONTACT = np.dtype([("worldPosB", "<f4", (4, 4)), ("normal", "<f4", 4), ("restit
                     ("frictionCmp", "<u2"), ("batchIdx", "<i4"), ("bodyA", "<i4"), ("bodyB", "<i4"),
                     ("childA", "<i4"), ("childB", "<i4"), ("unused", "<i4", 2)])
 PAIR = np.dtype([("x", "<i4"), ("y", "<i4"), ("z", "<i4"), ("w", "<i4")])
+CHILD = np.dtype([("pos", "<f4", 4), ("orn", "<f4", 4), ("shapeIndex", "<i4"), ("numChildShapes", "<i4"),
+                  ("collidableShapeIndex", "<i4"), ("shapeType", "<i4")])
 
 
 class OShapes(C.Structure):
     _fields_ = [("cols", C.c_void_p), ("local_aabbs", C.c_void_p), ("hulls", C.c_void_p), ("faces", C.c_void_p),
-                ("indices", C.c_void_p), ("verts", C.c_void_p), ("edges", C.c_void_p), ("num_collidables", C.c_int)]
+                ("indices", C.c_void_p), ("verts", C.c_void_p), ("edges", C.c_void_p), ("num_collidables", C.c_int),
+                ("children", C.c_void_p)]
 
 
 class OStepParams(C.Structure):
@@ -71,7 +74,9 @@ def load_reference():
 class Shapes:
     """Shape tables as numpy arrays (same layout the GPU library uses)."""
 
-    def __init__(self, collidables, local_aabbs, hulls, faces, indices, verts, edges):
+    def __init__(self, collidables, local_aabbs, hulls, faces, indices, verts, edges, children=None):
+        self.children = np.ascontiguousarray(children if children is not None and len(children) else
+                                             np.zeros(1, CHILD), CHILD)
         self.collidables = np.ascontiguousarray(collidables, COLLIDABLE)
         self.local_aabbs = np.ascontiguousarray(local_aabbs, AABB)
         self.hulls = np.ascontiguousarray(hulls, HULL)
@@ -82,7 +87,8 @@ class Shapes:
 
     @classmethod
     def from_tables(cls, t: dict):
-        return cls(t["collidables"], t["local_aabbs"], t["hulls"], t["faces"], t["indices"], t["verts"], t["edges"])
+        return cls(t["collidables"], t["local_aabbs"], t["hulls"], t["faces"], t["indices"], t["verts"], t["edges"],
+                   t.get("children"))
 
     def c(self) -> OShapes:
         s = OShapes()
@@ -94,6 +100,7 @@ class Shapes:
         s.verts = self.verts.ctypes.data
         s.edges = self.edges.ctypes.data
         s.num_collidables = len(self.collidables)
+        s.children = self.children.ctypes.data
         return s
 
 
@@ -147,6 +154,31 @@ def pairs_grid(aabbs_, cell, cap=None):
     out = np.zeros(cap, PAIR)
     n = load_oracle().oracle_pairs_grid(_p(a), C.c_int(len(a)), C.c_float(cell), _p(out), C.c_int(cap))
     return out[:min(n, cap)].copy()
+
+
+def compound_pairs(bodies, shapes: Shapes, pairs):
+    """Child pairs (x, y, child of x or -1, child of y or -1) of the pairs with a compound, in
+    (pair, child of x, child of y) order."""
+    b = np.ascontiguousarray(bodies, BODY)
+    pr = np.ascontiguousarray(pairs, PAIR)
+    sc = shapes.c()
+    lib = load_oracle()
+    n = lib.oracle_compound_pairs(_p(b), C.byref(sc), _p(pr), C.c_int(len(pr)), None, C.c_int(0))
+    out = np.zeros(max(1, n), PAIR)
+    lib.oracle_compound_pairs(_p(b), C.byref(sc), _p(pr), C.c_int(len(pr)), _p(out), C.c_int(len(out)))
+    return out[:n].copy()
+
+
+def compound_contacts(bodies, shapes: Shapes, child_pairs):
+    """(manifolds, child-pair index of each) of the given child pairs."""
+    b = np.ascontiguousarray(bodies, BODY)
+    cp = np.ascontiguousarray(child_pairs, PAIR)
+    out = np.zeros(max(1, len(cp)), CONTACT)
+    idx = np.zeros(max(1, len(cp)), np.int32)
+    sc = shapes.c()
+    n = load_oracle().oracle_compound_contacts(_p(b), C.byref(sc), _p(cp), C.c_int(len(cp)), _p(out), _p(idx),
+                                               C.c_int(len(out)))
+    return out[:n].copy(), idx[:n].copy()
 
 
 def contacts(bodies, shapes: Shapes, pairs, friction_cmp=45874):
@@ -342,6 +374,34 @@ def ref_contacts(bodies, shapes: Shapes, pairs_xy):
     return out[:n].copy(), pidx[:n].copy()
 
 
+def ref_compound_hull_contacts(bodies, shapes: Shapes, child_pairs):
+    """The reference's processCompoundPairsKernel + clipCompoundsHullHullKernel host twins on the
+    given child pairs (both sides convex hulls): (manifolds, child-pair index of each)."""
+    lib = load_reference()
+    b = np.ascontiguousarray(bodies, BODY)
+    cp = np.ascontiguousarray(child_pairs, PAIR)
+    out = np.zeros(max(1, len(cp)), CONTACT)
+    idx = np.zeros(max(1, len(cp)), np.int32)
+    n = lib.ref_compound_hull_contacts(_p(b), _p(shapes.collidables), _p(shapes.hulls), _p(shapes.faces),
+                                       C.c_int(len(shapes.faces)), _p(shapes.indices), C.c_int(len(shapes.indices)),
+                                       _p(shapes.verts), C.c_int(len(shapes.verts)), _p(shapes.edges),
+                                       C.c_int(len(shapes.edges)), _p(shapes.children), _p(cp), C.c_int(len(cp)),
+                                       _p(out), _p(idx), C.c_int(len(out)))
+    return out[:n].copy(), idx[:n].copy()
+
+
+def ref_plane_compound_contacts(bodies, shapes: Shapes, plane_body, compound_body):
+    """The reference's computeContactPlaneCompound for one (plane, compound) body pair."""
+    lib = load_reference()
+    b = np.ascontiguousarray(bodies, BODY)
+    out = np.zeros(64, CONTACT)
+    n = lib.ref_plane_compound_contacts(_p(b), _p(shapes.collidables), _p(shapes.hulls), _p(shapes.faces),
+                                        _p(shapes.indices), _p(shapes.verts), _p(shapes.children),
+                                        C.c_int(int(plane_body)), C.c_int(int(compound_body)), _p(out),
+                                        C.c_int(len(out)))
+    return out[:n].copy()
+
+
 def ref_solve(bodies, inertias, contacts_, use_pgs=True, iterations=10, dt=1 / 60):
     lib = load_reference()
     b = np.array(bodies, BODY, copy=True)
@@ -437,6 +497,7 @@ class Registry:
         self.cols, self.laabbs, self.hull_recs, self.faces = [], [], [], []
         self.indices, self.verts, self.edges = [], [], []
         self.bodies, self.inertias = [], []
+        self.children = []
 
     def plane(self, normal, constant):
         f = np.zeros(1, FACE)[0]
@@ -485,6 +546,27 @@ class Registry:
         self.laabbs.append(a)
         return len(self.cols) - 1
 
+    def compound(self, children):
+        """registerCompoundShape (b3GpuNarrowPhase.cpp:370-433): children = [(hull collidable, pos,
+        orn), ...]; the compound's local AABB is the union of the children's, moved into its frame."""
+        recs = np.zeros(len(children), CHILD)
+        for i, (c, pos, orn) in enumerate(children):
+            if self.cols[c]["shapeType"] != 3:
+                raise ValueError("compound children must be convex hulls")
+            recs[i]["pos"][:3] = np.asarray(pos, np.float32)[:3]
+            recs[i]["orn"] = np.asarray(orn, np.float32)[:4]
+            recs[i]["shapeIndex"] = c
+            recs[i]["shapeType"] = 3
+        local = np.array([self.laabbs[int(c)] for c, _, _ in children], AABB)
+        out = np.zeros(1, AABB)
+        load_oracle().oracle_compound_local_aabb(_p(local), _p(recs), C.c_int(len(recs)), _p(out))
+        col = np.zeros(1, COLLIDABLE)[0]
+        col["shapeType"], col["shapeIndex"], col["numChildShapes"] = 6, len(self.children), len(recs)
+        self.children.extend(recs)
+        self.cols.append(col)
+        self.laabbs.append(out[0])
+        return len(self.cols) - 1
+
     def body(self, mass, pos, orn, collidable):
         lib = load_oracle()
         b = np.zeros(1, BODY)
@@ -507,7 +589,8 @@ class Registry:
                 "indices": np.array(self.indices or [0], np.int32),
                 "verts": np.array(self.verts, np.float32).reshape(-1, 4) if self.verts else np.zeros((1, 4), np.float32),
                 "edges": np.array(self.edges, np.float32).reshape(-1, 4) if self.edges else np.zeros((1, 4), np.float32),
-                "bodies": np.array(self.bodies, BODY), "inertias": np.array(self.inertias, INERTIA)}
+                "bodies": np.array(self.bodies, BODY), "inertias": np.array(self.inertias, INERTIA),
+                "children": arr(self.children, CHILD)}
 
 
 def register_scene(scene) -> dict:
@@ -523,6 +606,9 @@ def register_scene(scene) -> dict:
             col.append(reg.sphere(s["radius"]))
         elif s["type"] == "plane":
             col.append(reg.plane(s["normal"], s["constant"]))
+        elif s["type"] == "compound":
+            # children: (index of an earlier shape of the scene, position, orientation)
+            col.append(reg.compound([(col[i], p, q) for i, p, q in s["children"]]))
         else:
             raise ValueError(s["type"])
     for i in range(len(scene.mass)):

@@ -15,6 +15,8 @@
 //   b3GpuRaycast::castRaysHost                      Bullet3OpenCL/Raycast/b3GpuRaycast.cpp:175-247
 //   b3Point2PointConstraint / b3FixedConstraint     Bullet3Dynamics/ConstraintSolver/b3Point2PointConstraint.cpp, b3FixedConstraint.cpp
 //     through b3PgsJacobiSolver::solveGroup         (joints only, no contacts)
+//   processCompoundPairsKernel + clipCompoundsHullHullKernel, computeContactPlaneCompound
+//                                                   Bullet3OpenCL/NarrowphaseCollision/b3ConvexHullContact.cpp:1777-2022, :2182
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -53,7 +55,89 @@ void computeContactSphereConvex(int pairIndex, int bodyIndexA, int bodyIndexB, i
                                 const b3Vector3* convexVertices, const int* convexIndices, const b3GpuFace* faces,
                                 b3Contact4* globalContactsOut, int& nGlobalContactsOut, int maxContactCapacity);
 
+// host twins of the compound kernels (b3ConvexHullContact.cpp, external linkage there)
+void processCompoundPairsKernel(const b3Int4* gpuCompoundPairs, const b3RigidBodyData* rigidBodies,
+                                const b3Collidable* collidables, const b3ConvexPolyhedronData* convexShapes,
+                                const b3AlignedObjectArray<b3Vector3>& vertices,
+                                const b3AlignedObjectArray<b3Vector3>& uniqueEdges,
+                                const b3AlignedObjectArray<b3GpuFace>& faces, const b3AlignedObjectArray<int>& indices,
+                                b3Aabb* aabbs, const b3GpuChildShape* gpuChildShapes,
+                                b3AlignedObjectArray<b3Vector3>& gpuCompoundSepNormalsOut,
+                                b3AlignedObjectArray<int>& gpuHasCompoundSepNormalsOut, int numCompoundPairs, int i);
+void clipCompoundsHullHullKernel(const b3Int4* gpuCompoundPairs, const b3RigidBodyData* rigidBodies,
+                                 const b3Collidable* collidables, const b3ConvexPolyhedronData* convexShapes,
+                                 const b3AlignedObjectArray<b3Vector3>& vertices,
+                                 const b3AlignedObjectArray<b3Vector3>& uniqueEdges,
+                                 const b3AlignedObjectArray<b3GpuFace>& faces, const b3AlignedObjectArray<int>& indices,
+                                 const b3GpuChildShape* gpuChildShapes,
+                                 const b3AlignedObjectArray<b3Vector3>& gpuCompoundSepNormalsOut,
+                                 const b3AlignedObjectArray<int>& gpuHasCompoundSepNormalsOut,
+                                 b3Contact4Data* globalContactsOut, int* nGlobalContactsOut, int numCompoundPairs,
+                                 int maxContactCapacity, int i);
+void computeContactPlaneCompound(int pairIndex, int bodyIndexA, int bodyIndexB, int collidableIndexA,
+                                 int collidableIndexB, const b3RigidBodyData* rigidBodies,
+                                 const b3Collidable* collidables, const b3ConvexPolyhedronData* convexShapes,
+                                 const b3GpuChildShape* cpuChildShapes, const b3Vector3* convexVertices,
+                                 const int* convexIndices, const b3GpuFace* faces, b3Contact4* globalContactsOut,
+                                 int& nGlobalContactsOut, int maxContactCapacity);
+
 extern "C" {
+
+// The reference's compound kernels (host twins), one child pair at a time, on the given child pairs
+// (int4: bodyA, bodyB, child shape of A or -1, child shape of B or -1; both sides convex hulls):
+// processCompoundPairsKernel then clipCompoundsHullHullKernel.  Writes the manifolds in child-pair
+// order, out_index[m] = child pair index; returns the count.
+int ref_compound_hull_contacts(const b3RigidBodyData* bodies, const b3Collidable* cols,
+                               const b3ConvexPolyhedronData* hulls, const b3GpuFace* faces, int nfaces,
+                               const int* indices, int nindices, const b3Vector3* verts, int nverts,
+                               const b3Vector3* edges, int nedges, const b3GpuChildShape* children,
+                               const int* child_pairs, int n, b3Contact4Data* out, int* out_index, int cap) {
+    b3AlignedObjectArray<b3Vector3> V, E, sep;
+    b3AlignedObjectArray<b3GpuFace> F;
+    b3AlignedObjectArray<int> I, has;
+    V.resize(nverts);
+    for (int i = 0; i < nverts; i++) V[i] = verts[i];
+    E.resize(nedges > 0 ? nedges : 1);
+    for (int i = 0; i < nedges; i++) E[i] = edges[i];
+    F.resize(nfaces);
+    for (int i = 0; i < nfaces; i++) F[i] = faces[i];
+    I.resize(nindices);
+    for (int i = 0; i < nindices; i++) I[i] = indices[i];
+    sep.resize(n > 0 ? n : 1);
+    has.resize(n > 0 ? n : 1);
+    const b3Int4* cp = reinterpret_cast<const b3Int4*>(child_pairs);
+    int m = 0;
+    std::vector<b3Contact4Data> tmp(1);
+    for (int i = 0; i < n; i++) {
+        processCompoundPairsKernel(cp, bodies, cols, hulls, V, E, F, I, nullptr, children, sep, has, n, i);
+        if (!has[i]) continue;
+        int nc = 0;
+        memset(&tmp[0], 0, sizeof(b3Contact4Data));
+        clipCompoundsHullHullKernel(cp, bodies, cols, hulls, V, E, F, I, children, sep, has, &tmp[0], &nc, n, 64, i);
+        if (nc > 0 && m < cap) {
+            out[m] = tmp[0];
+            out_index[m] = i;
+            m++;
+        }
+    }
+    return m;
+}
+
+// computeContactPlaneCompound for one (plane body, compound body) pair: one manifold per child
+// that touches the plane, in child order.  Returns the count.
+int ref_plane_compound_contacts(const b3RigidBodyData* bodies, const b3Collidable* cols,
+                                const b3ConvexPolyhedronData* hulls, const b3GpuFace* faces, const int* indices,
+                                const b3Vector3* verts, const b3GpuChildShape* children, int plane_body,
+                                int compound_body, b3Contact4Data* out, int cap) {
+    std::vector<b3Contact4> tmp(cap > 0 ? cap : 1);
+    memset(tmp.data(), 0, sizeof(b3Contact4) * tmp.size());
+    int nc = 0;
+    computeContactPlaneCompound(0, plane_body, compound_body, bodies[plane_body].m_collidableIdx,
+                                bodies[compound_body].m_collidableIdx, bodies, cols, hulls, children, verts, indices,
+                                faces, tmp.data(), nc, cap);
+    for (int i = 0; i < nc && i < cap; i++) memcpy(&out[i], &tmp[i], sizeof(b3Contact4Data));
+    return nc;
+}
 
 // Hull tables from b3ConvexUtility (+ vertex-mean local centre as registerConvexHullShape sets it).
 // counts4 in: capacities (verts, faces, indices, edges); out: sizes.  Returns 0 on success.

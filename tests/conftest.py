@@ -41,4 +41,4 @@ def load_golden(name):
 def shapes_from(d):
     from oracle import oracle as O
     return O.Shapes(d["shape_collidables"], d["shape_local_aabbs"], d["shape_hulls"], d["shape_faces"],
-                    d["shape_indices"], d["shape_verts"], d["shape_edges"])
+                    d["shape_indices"], d["shape_verts"], d["shape_edges"], d.get("shape_children"))

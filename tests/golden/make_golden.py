@@ -28,7 +28,13 @@ Fixtures:
                   poses and velocities), each solved alone by the reference's b3PgsJacobiSolver over
                   b3Point2PointConstraint / b3FixedConstraint rows (4 iterations, dt 1/60)
 
-  python tests/golden/make_golden.py [registration|rays|joints]   (no argument: every fixture)
+  compound.npz    compounds of boxes and Gaussian hulls among boxes and hulls over a plane: the
+                  child pairs of every pair with a compound (the oracle's expansion), the manifolds
+                  of the reference's processCompoundPairsKernel + clipCompoundsHullHullKernel host
+                  twins for the hull child pairs, and computeContactPlaneCompound's for each
+                  (plane, compound) pair
+
+  python tests/golden/make_golden.py [registration|rays|joints|compound]   (no argument: every fixture)
 """
 from __future__ import annotations
 
@@ -405,6 +411,59 @@ def joints_fixture():
     print("joints", n)
 
 
+def compound_fixture():
+    """compound.npz: the reference's compound kernels on a dense mix of compounds, boxes and hulls."""
+    rng = np.random.Generator(np.random.PCG64(77))
+
+    def quat():
+        x = rng.standard_normal(4)
+        return (x / np.linalg.norm(x)).astype(np.float32)
+
+    reg = O.Registry()
+    plane = reg.plane((0.0, 1.0, 0.0), 0.0)
+    bx = reg.convex_hull(box_vertices([0.5, 0.25, 0.25]))
+    by = reg.convex_hull(box_vertices([0.25, 0.5, 0.25]))
+    gauss = reg.convex_hull((rng.standard_normal((20, 3)) * 0.3).astype(np.float32))
+    ell = reg.compound([(bx, (0.25, 0.0, 0.0), (0, 0, 0, 1)), (by, (0.0, 0.5, 0.0), (0, 0, 0, 1))])
+    dumb = reg.compound([(gauss, (-0.6, 0.0, 0.0), quat()), (bx, (0.0, 0.0, 0.0), (0, 0, 0, 1)),
+                         (gauss, (0.6, 0.0, 0.0), quat())])
+    cols = [ell, dumb, bx, gauss]
+    reg.body(0.0, (0, 0, 0), (0, 0, 0, 1), plane)
+    for i in range(300):
+        p = rng.uniform(-3, 3, 3)
+        p[1] = rng.uniform(0.0, 1.5)
+        reg.body(1.0, p, quat(), cols[i % 4])
+    t = reg.tables()
+    shapes = O.Shapes.from_tables(t)
+    bodies = t["bodies"]
+    pairs = O.pairs_bruteforce(O.aabbs(bodies, shapes))
+    cp = O.compound_pairs(bodies, shapes, pairs)
+
+    def side(body, child):
+        return 3 if child >= 0 else int(shapes.collidables[bodies[body]["collidableIdx"]]["shapeType"])
+    hh = np.array([side(p["x"], p["z"]) == 3 and side(p["y"], p["w"]) == 3 for p in cp])
+    sel = np.where(hh)[0]
+    ref, ridx = O.ref_compound_hull_contacts(bodies, shapes, cp[hh])
+    plane_pairs, plane_contacts, plane_owner = [], [], []
+    for p in pairs:
+        x, y = int(p["x"]), int(p["y"])
+        tx = int(shapes.collidables[bodies[x]["collidableIdx"]]["shapeType"])
+        ty = int(shapes.collidables[bodies[y]["collidableIdx"]]["shapeType"])
+        if tx == 4 and ty == 6:
+            c = O.ref_plane_compound_contacts(bodies, shapes, x, y)
+            plane_contacts.append(c)
+            plane_owner.extend([len(plane_pairs)] * len(c))
+            plane_pairs.append((x, y))
+    out = dict(bodies=bodies, pairs=pairs, child_pairs=cp, hull_contacts=ref, hull_child_index=sel[ridx],
+               plane_pairs=np.array(plane_pairs, np.int32).reshape(-1, 2),
+               plane_contacts=np.concatenate(plane_contacts) if plane_contacts else np.zeros(0, O.CONTACT),
+               plane_owner=np.array(plane_owner, np.int32))
+    for k in ("collidables", "local_aabbs", "hulls", "faces", "indices", "verts", "edges", "children"):
+        out["shape_" + k] = t[k]
+    np.savez_compressed(OUT / "compound.npz", **out)
+    print("compound", len(cp), "child pairs,", len(ref), "hull manifolds,", len(out["plane_contacts"]), "plane manifolds")
+
+
 if __name__ == "__main__":
     if O.load_reference() is None:
         raise SystemExit("oracle/_ref/libb3ref.so is missing: run oracle/build_ref.sh first")
@@ -414,8 +473,12 @@ if __name__ == "__main__":
         rays_fixture()
     elif len(sys.argv) > 1 and sys.argv[1] == "joints":
         joints_fixture()
+    elif len(sys.argv) > 1 and sys.argv[1] == "compound":
+        compound_fixture()
     else:
         main()
         registration_fixture()
         rays_fixture()
+        joints_fixture()
+        compound_fixture()
         joints_fixture()

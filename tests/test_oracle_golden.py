@@ -3,9 +3,10 @@
 Pins oracle/b3oracle.c (the checker every GPU parity test uses) to the reference:
 b3TransformAabb2, the dynamic-BVH pair set filtered by the tight test, b3ContactConvexConvexSAT,
 computeContactPlaneConvex, computeContactSphereConvex, b3PgsJacobiSolver (PGS and Jacobi) and
-integrateSingleTransform, plus a 30-step composed trajectory; and the registration path
+integrateSingleTransform, plus a 30-step composed trajectory; the registration path
 (b3ConvexHullComputer + b3ConvexUtility hull tables, registerPhysicsInstance body and inertia
-records) that the CPU legs use to build their scenes.
+records) that the CPU legs use to build their scenes; and the compound path
+(processCompoundPairsKernel + clipCompoundsHullHullKernel host twins, computeContactPlaneCompound).
 """
 import numpy as np
 import pytest
@@ -180,3 +181,49 @@ def test_joints_match_reference_constraint_classes():
     ob, oj = O.solve_joints(g["bodies"], g["inertias"], g["joints"])
     _joints_close(ob, g["solved"])
     assert (oj["flags"] == 1).all()
+
+
+def _manifold_equal(a, b):
+    n = int(b["normal"][3])
+    return (np.array_equal(a["normal"], b["normal"]) and np.array_equal(a["worldPosB"][:n], b["worldPosB"][:n])
+            and a["bodyA"] == b["bodyA"] and a["bodyB"] == b["bodyB"] and a["frictionCmp"] == b["frictionCmp"])
+
+
+def test_compound_contacts_match_reference_kernels():
+    # compound children against hulls and other compounds: the reference's own kernel host twins
+    # (processCompoundPairsKernel's three separating-axis passes, clipCompoundsHullHullKernel's clip
+    # and reduction) give these manifolds; the oracle reproduces them bit for bit, child indices too
+    d = load_golden("compound")
+    sh = shapes_from(d)
+    b = d["bodies"]
+    cp = O.compound_pairs(b, sh, d["pairs"])
+    assert np.array_equal(cp.view(np.int32), d["child_pairs"].view(np.int32))
+    mine, idx = O.compound_contacts(b, sh, cp)
+    by_child = {int(i): m for m, i in zip(mine, idx)}
+    ref = d["hull_contacts"]
+    assert len(ref) > 1000
+    for r, i in zip(ref, d["hull_child_index"]):
+        m = by_child[int(i)]
+        assert _manifold_equal(m, r) and m["childA"] == r["childA"] and m["childB"] == r["childB"], int(i)
+    # and no other hull child pair has one
+    def hull_side(body, child):
+        return child >= 0 or sh.collidables[b[body]["collidableIdx"]]["shapeType"] == 3
+    hull_mine = {int(i) for i in idx if hull_side(cp[i]["x"], cp[i]["z"]) and hull_side(cp[i]["y"], cp[i]["w"])}
+    assert hull_mine == set(int(i) for i in d["hull_child_index"])
+
+
+def test_plane_compound_contacts_match_reference():
+    # computeContactPlaneCompound: one manifold per child below the plane, in child order
+    d = load_golden("compound")
+    sh = shapes_from(d)
+    b = d["bodies"]
+    cp = O.compound_pairs(b, sh, d["pairs"])
+    mine, idx = O.compound_contacts(b, sh, cp)
+    ref, owner = d["plane_contacts"], d["plane_owner"]
+    assert len(ref) > 50
+    for k, (x, y) in enumerate(d["plane_pairs"]):
+        r = ref[owner == k]
+        m = [c for c, i in zip(mine, idx) if cp[i]["x"] == x and cp[i]["y"] == y]
+        assert len(m) == len(r)
+        for mc, rc in zip(m, r):
+            assert _manifold_equal(mc, rc)
