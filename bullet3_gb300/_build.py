@@ -52,7 +52,7 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
         return LIB
     BUILD.mkdir(exist_ok=True)
     nvcc = _nvcc()
-    common = ["-std=c++17", "-O3", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
+    common = ["-std=c++17", "-O3", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I" + str(ROOT / "include"), "-I" + str(CSRC)]
     jobs = []
     objs = []

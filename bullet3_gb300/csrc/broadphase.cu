@@ -24,22 +24,6 @@ namespace b3g {
 
 static constexpr int BP_THREADS = 256;
 
-__device__ __forceinline__ void transform_aabb(const b3gAabb& local, v3 pos, quat q, float margin, v3& mn, v3& mx) {
-    v3 lmin = mk3(local.minv[0], local.minv[1], local.minv[2]);
-    v3 lmax = mk3(local.maxv[0], local.maxv[1], local.maxv[2]);
-    v3 he = 0.5f * (lmax - lmin);
-    he = he + mk3(margin, margin, margin);
-    v3 lc = 0.5f * (lmax + lmin);
-    m33 m = qmat(q);
-    m33 a;
-    a.r0 = mk3(fabsf(m.r0.x), fabsf(m.r0.y), fabsf(m.r0.z));
-    a.r1 = mk3(fabsf(m.r1.x), fabsf(m.r1.y), fabsf(m.r1.z));
-    a.r2 = mk3(fabsf(m.r2.x), fabsf(m.r2.y), fabsf(m.r2.z));
-    v3 c = mmul(m, lc) + pos;
-    v3 e = mk3(dot3(he, a.r0), dot3(he, a.r1), dot3(he, a.r2));
-    mn = c - e;
-    mx = c + e;
-}
 
 __device__ __forceinline__ int cell_coord(float c, float inv_cell, int mask) {
     return ((int)floorf(c * inv_cell)) & mask;

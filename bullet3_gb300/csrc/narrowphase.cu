@@ -45,6 +45,9 @@ struct NPArgs {
     int* flags;
     unsigned int* status;
     unsigned short friction_cmp;
+    // compounds
+    const b3gChildShape* children;
+    const b3gAabb* local_aabbs;
 };
 
 __device__ __forceinline__ v3 ld3(const b3gFloat4* p) {
@@ -114,14 +117,14 @@ __device__ int reduce_contacts(const float4* p, int n, v3 nearNormal, int idx[4]
 }
 
 // ------------------------------------------------------------------ plane (A) vs hull (B)
-__device__ void plane_hull(const NPArgs& a, int pairIdx, int bodyA, int bodyB) {
+// computeContactPlaneConvex (b3ConvexHullContact.cpp:1272-1395) for a hull at pose (posB, ornB):
+// the points below the plane (reduced to 4), returns their count; nWorld = the plane's world normal
+__device__ int plane_hull_points(const NPArgs& a, int bodyA, const b3gHull& hull, v3 posB, quat ornB, float4* pts,
+                                 int idx[4], v3& nWorld) {
     const b3gBody& BA = a.bodies[bodyA];
-    const b3gBody& BB = a.bodies[bodyB];
     const b3gCollidable colA = a.cols[BA.collidableIdx];
-    const b3gCollidable colB = a.cols[BB.collidableIdx];
-    const b3gHull hull = a.hulls[colB.shapeIndex];
-    v3 posB = f4v3(BB.pos), posA = f4v3(BA.pos);
-    quat ornB = f4q(BB.quat), ornA = f4q(BA.quat);
+    v3 posA = f4v3(BA.pos);
+    quat ornA = f4q(BA.quat);
     float4 pe = ldf4(&a.faces[colA.shapeIndex].plane);
     v3 planeNormal = mk3(pe.x, pe.y, pe.z);
     float planeConstant = pe.w;
@@ -129,7 +132,6 @@ __device__ void plane_hull(const NPArgs& a, int pairIdx, int bodyA, int bodyB) {
     v3 planeNormalWorld = qrotq(ornA, planeNormal);
     // planeInConvex = inverse(convexWorld) * planeTransform: basis RB^T * RA (b3Transform order)
     v3 planeNormalInConvex = mmul(mmul33(mtrans(RB), RA), -planeNormal);
-    float4 pts[64];
     int numPoints = 0;
     float maxDot = -1e30f;
     for (int i = 0; i < hull.numVertices; i++) {
@@ -149,8 +151,17 @@ __device__ void plane_hull(const NPArgs& a, int pairIdx, int bodyA, int bodyB) {
             }
         }
     }
+    nWorld = planeNormalWorld;
+    return reduce_contacts(pts, numPoints, planeNormalInConvex, idx);
+}
+
+__device__ void plane_hull(const NPArgs& a, int pairIdx, int bodyA, int bodyB) {
+    const b3gBody& BB = a.bodies[bodyB];
+    const b3gHull hull = a.hulls[a.cols[BB.collidableIdx].shapeIndex];
+    float4 pts[64];
     int idx[4];
-    int nred = reduce_contacts(pts, numPoints, planeNormalInConvex, idx);
+    v3 planeNormalWorld;
+    const int nred = plane_hull_points(a, bodyA, hull, f4v3(BB.pos), f4q(BB.quat), pts, idx, planeNormalWorld);
     if (nred > 0) {
         b3gContact4& c = a.slots[pairIdx];
         write_header(c, a, bodyA, bodyB, -planeNormalWorld, nred);
@@ -720,16 +731,16 @@ __global__ void __launch_bounds__(NP_THREADS, 3) k_hull_hull_small(NPArgs a, int
 
 // manifold list in pair order + pair.z = manifold index + point count
 __global__ void k_manifold_list(const int* __restrict__ flags, const int* __restrict__ cidx,
-                                const int* __restrict__ d_np, const b3gContact4* __restrict__ slots,
-                                b3gPair* __restrict__ pairs, int* __restrict__ manifold_pair,
-                                int* __restrict__ num_points) {
-    const int np = *d_np;
+                                const int* __restrict__ d_nslots, const int* __restrict__ d_np,
+                                const b3gContact4* __restrict__ slots, b3gPair* __restrict__ pairs,
+                                int* __restrict__ manifold_pair, int* __restrict__ num_points) {
+    const int ns = *d_nslots, np = *d_np;  // slots: the pairs', then the compound child pairs'
     int local = 0;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < ns; p += gridDim.x * blockDim.x) {
         if (flags[p]) {
             int m = cidx[p];
             manifold_pair[m] = p;
-            pairs[p].z = m;
+            if (p < np) pairs[p].z = m;
             local += (int)slots[p].worldNormalOnB.w;
         }
     }
@@ -742,6 +753,303 @@ __global__ void k_compact_contacts(const int* __restrict__ d_nc, const int* __re
     const int nc = *d_nc;
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nc; m += gridDim.x * blockDim.x)
         out[m] = slots[manifold_pair[m]];
+}
+
+// ------------------------------------------------------------------ compound shapes
+// A pair with a compound (SHAPE_COMPOUND_OF_CONVEX_HULLS) expands into child pairs in (pair, child
+// of A, child of B) order -- the set of findCompoundPairsKernel (b3ConvexHullContact.cpp:1419-1775):
+// compound-compound the children whose world AABBs overlap (the reference walks quantized child
+// BVHs, whose conservative boxes add only child pairs that cannot touch), compound against another
+// shape every child.  Each child pair has its own manifold slot after the pair slots.
+
+// child pose: newPos = b3QuatRotate(orn, childPos) + pos, newOrn = b3QuatMul(orn, childOrn)
+// (processCompoundPairsKernel, b3ConvexHullContact.cpp:1813-1829)
+__device__ __forceinline__ void child_pose(const b3gBody& b, const b3gChildShape& ch, v3& pos, quat& orn) {
+    const quat q = f4q(b.quat);
+    pos = qrotq(q, f4v3(ch.childPosition)) + f4v3(b.pos);
+    orn = qmul(q, f4q(ch.childOrientation));
+}
+
+__device__ __forceinline__ bool aabb_overlap(v3 amn, v3 amx, v3 bmn, v3 bmx) {
+    return amn.x <= bmx.x && bmn.x <= amx.x && amn.y <= bmx.y && bmn.y <= amx.y && amn.z <= bmx.z && bmn.z <= amx.z;
+}
+
+// the child pairs of pair p: counted (out == nullptr), or written at out[0..cap)
+__device__ int compound_child_pairs(const NPArgs& a, int p, int4* out, int cap) {
+    const b3gPair pr = a.pairs[p];
+    const int A = pr.x, B = pr.y;
+    const b3gBody& BA = a.bodies[A];
+    const b3gBody& BB = a.bodies[B];
+    const b3gCollidable cA = a.cols[BA.collidableIdx], cB = a.cols[BB.collidableIdx];
+    const bool compA = cA.shapeType == B3G_SHAPE_COMPOUND, compB = cB.shapeType == B3G_SHAPE_COMPOUND;
+    if (!compA && !compB) return 0;
+    if (BA.invMass == 0.f && BB.invMass == 0.f) return 0;  // findCompoundPairsKernel :1446
+    int n = 0;
+    if (compA && compB) {
+        for (int i = 0; i < cA.numChildShapes; i++) {
+            const b3gChildShape chA = a.children[cA.shapeIndex + i];
+            v3 pA, mnA, mxA;
+            quat qA;
+            child_pose(BA, chA, pA, qA);
+            transform_aabb(a.local_aabbs[chA.shapeIndex], pA, qA, 0.f, mnA, mxA);
+            for (int k = 0; k < cB.numChildShapes; k++) {
+                const b3gChildShape chB = a.children[cB.shapeIndex + k];
+                v3 pB, mnB, mxB;
+                quat qB;
+                child_pose(BB, chB, pB, qB);
+                transform_aabb(a.local_aabbs[chB.shapeIndex], pB, qB, 0.f, mnB, mxB);
+                if (!aabb_overlap(mnA, mxA, mnB, mxB)) continue;
+                if (out && n < cap) out[n] = make_int4(A, B, cA.shapeIndex + i, cB.shapeIndex + k);
+                n++;
+            }
+        }
+    } else if (compA) {
+        for (int i = 0; i < cA.numChildShapes; i++) {
+            if (out && n < cap) out[n] = make_int4(A, B, cA.shapeIndex + i, -1);
+            n++;
+        }
+    } else {
+        for (int k = 0; k < cB.numChildShapes; k++) {
+            if (out && n < cap) out[n] = make_int4(A, B, -1, cB.shapeIndex + k);
+            n++;
+        }
+    }
+    return n;
+}
+
+__global__ void k_compound_count(NPArgs a, const int* __restrict__ d_np, int* __restrict__ counts) {
+    const int np = *d_np;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x)
+        counts[p] = compound_child_pairs(a, p, nullptr, 0);
+}
+
+// the child-pair count clamped to capacity (pad[4]) and the slot count (pairs + child pairs, pad[5])
+__global__ void k_compound_total(const int* __restrict__ d_np, int* __restrict__ d_total, int* __restrict__ d_slots,
+                                 int cap, unsigned int* __restrict__ status) {
+    const int total = *d_total;
+    const int J = total < cap ? total : cap;
+    if (total > cap) atomicOr(status, B3G_FLAG_CONTACT_OVERFLOW);
+    *d_total = J;
+    *d_slots = *d_np + J;
+}
+
+__global__ void k_compound_expand(NPArgs a, const int* __restrict__ d_np, const int* __restrict__ offsets,
+                                  int4* __restrict__ child_pairs, int cap) {
+    const int np = *d_np;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+        const int o = offsets[p];
+        if (o < cap) compound_child_pairs(a, p, child_pairs + o, cap - o);
+    }
+}
+
+// findSeparatingAxis (b3ConvexHullContact.cpp:562-700): face normals of A, of B, edge-edge axes,
+// returning at the first separating axis; sep = the smallest overlap's axis, pointing from B to A
+__device__ bool find_sep_full(const NPArgs& a, const b3gHull& hA, const b3gHull& hB, v3 posA, quat qA, v3 posB,
+                              quat qB, v3& sep) {
+    const v3 deltaC2 = (mmul(qmat(qA), f4v3(hA.localCenter)) + posA) - (mmul(qmat(qB), f4v3(hB.localCenter)) + posB);
+    const b3gFloat4* vA = &a.verts[hA.vertexOffset];
+    const b3gFloat4* vB = &a.verts[hB.vertexOffset];
+    float dmin = FLT_MAX;
+    for (int i = 0; i < hA.numFaces + hB.numFaces; i++) {
+        v3 n = i < hA.numFaces ? qrotq(qA, ld3(&a.faces[hA.faceOffset + i].plane))
+                               : qrotq(qB, ld3(&a.faces[hB.faceOffset + (i - hA.numFaces)].plane));
+        if (dot3(deltaC2, n) < 0.f) n = -n;
+        float min0, max0, min1, max1;
+        project(vA, hA.numVertices, posA, qA, n, min0, max0);
+        project(vB, hB.numVertices, posB, qB, n, min1, max1);
+        if (max0 < min1 || max1 < min0) return false;
+        const float d0 = max0 - min1, d1 = max1 - min0;
+        const float d = d0 < d1 ? d0 : d1;
+        if (d < dmin) { dmin = d; sep = n; }
+    }
+    for (int e0 = 0; e0 < hA.numUniqueEdges; e0++) {
+        const v3 w0 = qrotq(qA, ld3(&a.edges[hA.uniqueEdgesOffset + e0]));
+        for (int e1 = 0; e1 < hB.numUniqueEdges; e1++) {
+            const v3 w1 = qrotq(qB, ld3(&a.edges[hB.uniqueEdgesOffset + e1]));
+            v3 c = cross3(w0, w1);
+            if (!((double)fabsf(c.x) > 1e-6 || (double)fabsf(c.y) > 1e-6 || (double)fabsf(c.z) > 1e-6)) continue;
+            c = normalize3(c);
+            if (dot3(deltaC2, c) < 0.f) c = -c;
+            float min0, max0, min1, max1;
+            project(vA, hA.numVertices, posA, qA, c, min0, max0);
+            project(vB, hB.numVertices, posB, qB, c, min1, max1);
+            if (max0 < min1 || max1 < min0) return false;
+            const float d0 = max0 - min1, d1 = max1 - min0;
+            const float d = d0 < d1 ? d0 : d1;
+            if (d < dmin) { dmin = d; sep = c; }
+        }
+    }
+    if (dmin == FLT_MAX) return false;
+    if (dot3(-deltaC2, sep) > 0.0f) sep = -sep;
+    return true;
+}
+
+// findSeparatingAxisEdgeEdge (b3ConvexHullContact.cpp:702-785): every edge-edge axis projected, no
+// early exit (its separation test is discarded); the smallest overlap replaces sep
+__device__ void edge_edge_axis(const NPArgs& a, const b3gHull& hA, const b3gHull& hB, v3 posA, quat qA, v3 posB,
+                               quat qB, v3 deltaC2, v3& sep) {
+    const b3gFloat4* vA = &a.verts[hA.vertexOffset];
+    const b3gFloat4* vB = &a.verts[hB.vertexOffset];
+    float dmin = FLT_MAX;
+    for (int e0 = 0; e0 < hA.numUniqueEdges; e0++) {
+        const v3 w0 = qrotq(qA, ld3(&a.edges[hA.uniqueEdgesOffset + e0]));
+        for (int e1 = 0; e1 < hB.numUniqueEdges; e1++) {
+            const v3 w1 = qrotq(qB, ld3(&a.edges[hB.uniqueEdgesOffset + e1]));
+            v3 c = cross3(w0, w1);
+            if (!((double)fabsf(c.x) > 1e-6 || (double)fabsf(c.y) > 1e-6 || (double)fabsf(c.z) > 1e-6)) continue;
+            c = normalize3(c);
+            if (dot3(deltaC2, c) < 0.f) c = -c;
+            float min0, max0, min1, max1;
+            project(vA, hA.numVertices, posA, qA, c, min0, max0);
+            project(vB, hB.numVertices, posB, qB, c, min1, max1);
+            const float d0 = max0 - min1, d1 = max1 - min0;
+            const float dist = d0 < d1 ? d0 : d1;
+            if (dist < dmin) { dmin = dist; sep = c; }
+        }
+    }
+    if (dot3(-deltaC2, sep) > 0.0f) sep = -sep;
+}
+
+// clipHullAgainstHull -> clipFaceAgainstHull (b3ConvexHullContact.cpp:939-1044, :834-937): the
+// incident face of B (max dot), its vertices clipped by the side planes of A's reference face (min
+// dot), depth clamped at minDist and kept if <= maxDist; rotations by b3QuatRotate of the poses,
+// points by their matrices.  pin / pout: CLIP_CAP float4 each; returns the count of the points,
+// left in *result (one of the two buffers)
+__device__ int clip_hull_against_hull(const NPArgs& a, v3 sep, const b3gHull& hA, const b3gHull& hB, v3 posA,
+                                      quat qA, v3 posB, quat qB, float minDist, float maxDist, float4* pin,
+                                      float4* pout, float4** result) {
+    int fb = -1, fa = -1;
+    float dmax = -FLT_MAX, dmn = FLT_MAX;
+    for (int f = 0; f < hB.numFaces; f++) {
+        const float d = dot3(qrotq(qB, ld3(&a.faces[hB.faceOffset + f].plane)), sep);
+        if (d > dmax) { dmax = d; fb = f; }
+    }
+    if (fb < 0) return 0;
+    const m33 RA = qmat(qA), RB = qmat(qB);
+    const b3gFace polyB = a.faces[hB.faceOffset + fb];
+    int nin = 0;
+    for (int e = 0; e < polyB.numIndices && e < CLIP_CAP; e++) {
+        const v3 w = mmul(RB, ld3(&a.verts[hB.vertexOffset + a.indices[polyB.indexOffset + e]])) + posB;
+        pin[nin++] = make_float4(w.x, w.y, w.z, 0.f);
+    }
+    for (int f = 0; f < hA.numFaces; f++) {
+        const float d = dot3(qrotq(qA, ld3(&a.faces[hA.faceOffset + f].plane)), sep);
+        if (d < dmn) { dmn = d; fa = f; }
+    }
+    if (fa < 0) return 0;
+    const b3gFace polyA = a.faces[hA.faceOffset + fa];
+    const v3 planeNormalA = mk3(polyA.plane.x, polyA.plane.y, polyA.plane.z);
+    const int nva = polyA.numIndices;
+    for (int e0 = 0; e0 < nva; e0++) {
+        const v3 va = ld3(&a.verts[hA.vertexOffset + a.indices[polyA.indexOffset + e0]]);
+        const v3 vb = ld3(&a.verts[hA.vertexOffset + a.indices[polyA.indexOffset + ((e0 + 1) % nva)]]);
+        const v3 worldEdge0 = qrotq(qA, va - vb);
+        const v3 worldPlaneAnormal1 = qrotq(qA, planeNormalA);
+        const v3 planeNormalWS1 = -cross3(worldEdge0, worldPlaneAnormal1);
+        const v3 worldA1 = mmul(RA, va) + posA;
+        const float planeEqWS1 = -dot3(worldA1, planeNormalWS1);
+        const int nout = clip_face(pin, nin, planeNormalWS1, planeEqWS1, pout, a.status);
+        float4* t = pout;
+        pout = pin;
+        pin = t;
+        nin = nout;
+    }
+    const v3 planeNormalWS = qrotq(qA, planeNormalA);
+    const float planeEqWS = polyA.plane.w - dot3(planeNormalWS, posA);
+    int n = 0;
+    for (int i = 0; i < nin; i++) {
+        float depth = dot3(planeNormalWS, mk3(pin[i].x, pin[i].y, pin[i].z)) + planeEqWS;
+        if (depth <= minDist) depth = minDist;
+        if (n < CLIP_CAP && depth <= maxDist) pout[n++] = make_float4(pin[i].x, pin[i].y, pin[i].z, depth);
+    }
+    *result = pout;
+    return n;
+}
+
+// One child pair per thread (slot = pair count + child pair index): processCompoundPairsKernel +
+// clipCompoundsHullHullKernel (b3ConvexHullContact.cpp:1777-2022) for two hulls -- the axis of
+// findSeparatingAxis(A, B), then of findSeparatingAxis(B, A), then the edge-edge pass; clipped with
+// minDist -1e30 and maxDist 0, reduced against -sep, friction 0.7 -- or computeContactPlaneCompound
+// (:2182-2321) for a plane against a child.  Compound children against spheres give nothing.
+__global__ void __launch_bounds__(NP_THREADS, 2) k_compound_contacts(NPArgs a, const int* __restrict__ d_np,
+                                                                     const int* __restrict__ d_J,
+                                                                     const int4* __restrict__ child_pairs) {
+    const int P = *d_np, J = *d_J;
+    const unsigned short fr07 = (unsigned short)(0.7f * 0xffff);
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < J; j += gridDim.x * blockDim.x) {
+        const int slot = P + j;
+        a.flags[slot] = 0;
+        const int4 cp = child_pairs[j];
+        const b3gBody& BA = a.bodies[cp.x];
+        const b3gBody& BB = a.bodies[cp.y];
+        v3 posA = f4v3(BA.pos), posB = f4v3(BB.pos);
+        quat qA = f4q(BA.quat), qB = f4q(BB.quat);
+        int colA = BA.collidableIdx, colB = BB.collidableIdx;
+        if (cp.z >= 0) {
+            const b3gChildShape ch = a.children[cp.z];
+            colA = ch.shapeIndex;
+            child_pose(BA, ch, posA, qA);
+        }
+        if (cp.w >= 0) {
+            const b3gChildShape ch = a.children[cp.w];
+            colB = ch.shapeIndex;
+            child_pose(BB, ch, posB, qB);
+        }
+        const b3gCollidable cA = a.cols[colA], cB = a.cols[colB];
+        b3gContact4& c = a.slots[slot];
+        if (cA.shapeType == B3G_SHAPE_CONVEX_HULL && cB.shapeType == B3G_SHAPE_CONVEX_HULL) {
+            const b3gHull hA = a.hulls[cA.shapeIndex], hB = a.hulls[cB.shapeIndex];
+            const v3 deltaC2 =
+                (mmul(qmat(qA), f4v3(hA.localCenter)) + posA) - (mmul(qmat(qB), f4v3(hB.localCenter)) + posB);
+            v3 sep = mk3(1.f, 0.f, 0.f);
+            if (!find_sep_full(a, hA, hB, posA, qA, posB, qB, sep)) continue;
+            if (!find_sep_full(a, hB, hA, posB, qB, posA, qA, sep)) continue;
+            edge_edge_axis(a, hA, hB, posA, qA, posB, qB, deltaC2, sep);
+            float4 buf0[CLIP_CAP], buf1[CLIP_CAP];
+            float4* pts = buf0;
+            const int np = clip_hull_against_hull(a, sep, hA, hB, posA, qA, posB, qB, -1e30f, 0.0f, buf0, buf1, &pts);
+            if (np <= 0) continue;
+            int idx[4];
+            const int nred = reduce_contacts(pts, np, -sep, idx);
+            write_header(c, a, cp.x, cp.y, sep, nred);
+            c.frictionCmp = fr07;
+            c.batchIdx = j;
+            c.childIndexA = cp.z;
+            c.childIndexB = cp.w;
+            for (int i = 0; i < nred; i++) {
+                const float4 q = pts[idx[i]];
+                c.worldPosB[i] = b3gFloat4{q.x, q.y, q.z, q.w};
+            }
+            a.flags[slot] = 1;
+        } else {
+            // a plane against a child: the plane body first in the manifold, the child's hull at its pose
+            int plane = -1, comp = -1, child = -1;
+            v3 pos;
+            quat q;
+            if (cA.shapeType == B3G_SHAPE_PLANE && cB.shapeType == B3G_SHAPE_CONVEX_HULL && cp.w >= 0) {
+                plane = cp.x; comp = cp.y; child = cp.w; pos = posB; q = qB;
+            } else if (cB.shapeType == B3G_SHAPE_PLANE && cA.shapeType == B3G_SHAPE_CONVEX_HULL && cp.z >= 0) {
+                plane = cp.y; comp = cp.x; child = cp.z; pos = posA; q = qA;
+            }
+            if (plane < 0) continue;
+            float4 pts[64];
+            int idx[4];
+            v3 nWorld;
+            const int hull = a.cols[a.children[child].shapeIndex].shapeIndex;
+            const int nred = plane_hull_points(a, plane, a.hulls[hull], pos, q, pts, idx, nWorld);
+            if (nred > 0) {
+                write_header(c, a, plane, comp, -nWorld, nred);
+                c.frictionCmp = fr07;
+                c.batchIdx = j;
+                c.childIndexB = child;
+                for (int i = 0; i < nred; i++) {
+                    const float4 qq = pts[idx[i]];
+                    c.worldPosB[i] = b3gFloat4{qq.x, qq.y, qq.z, qq.w};
+                }
+                a.flags[slot] = 1;
+            }
+        }
+    }
 }
 
 static NPArgs make_args(DeviceState& d, unsigned short friction_cmp) {
@@ -761,6 +1069,8 @@ static NPArgs make_args(DeviceState& d, unsigned short friction_cmp) {
     a.flags = d.contact_flag;
     a.status = &d.counters->status;
     a.friction_cmp = friction_cmp;
+    a.children = d.children;
+    a.local_aabbs = d.local_aabbs;
     return a;
 }
 
@@ -778,11 +1088,25 @@ int launch_contacts(DeviceState& d, float friction, cudaStream_t s) {
     k_hull_hull<<<d.num_sms * 16, HH_WARPS * 32, 0, s>>>(a, d.max_pairs);
     long long ll = 0;
     int* d_np = &d.counters->pad[0];
-    exclusive_scan_i32(d.prim, d.contact_flag, d.contact_index, d_np, &d.counters->num_contacts, d.scan_scratch, s,
-                       &ll);
-    k_manifold_list<<<grid, NP_THREADS, 0, s>>>(d.contact_flag, d.contact_index, d_np, d.contact_slots, d.pairs,
-                                                d.manifold_pair, &d.counters->num_points);
-    return 1 + 2 + 1 + (int)ll;
+    int* d_slots = d_np;
+    int launches = 0;
+    if (d.num_children > 0) {
+        // compound pairs: child-pair counts, their scan (total in pad[4]), the clamped count and the
+        // slot count (pairs + child pairs, pad[5]), the child pairs, their manifolds
+        int* d_J = &d.counters->pad[4];
+        d_slots = &d.counters->pad[5];
+        k_compound_count<<<grid, NP_THREADS, 0, s>>>(a, d_np, d.child_count);
+        exclusive_scan_i32(d.prim, d.child_count, d.child_offset, d_np, d_J, d.scan_scratch, s, &ll);
+        k_compound_total<<<1, 1, 0, s>>>(d_np, d_J, d_slots, d.max_child_pairs, &d.counters->status);
+        k_compound_expand<<<grid, NP_THREADS, 0, s>>>(a, d_np, d.child_offset, d.child_pairs, d.max_child_pairs);
+        k_compound_contacts<<<grid, NP_THREADS, 0, s>>>(a, d_np, d_J, d.child_pairs);
+        launches += 4;
+    }
+    exclusive_scan_i32(d.prim, d.contact_flag, d.contact_index, d_slots, &d.counters->num_contacts, d.scan_scratch,
+                       s, &ll);
+    k_manifold_list<<<grid, NP_THREADS, 0, s>>>(d.contact_flag, d.contact_index, d_slots, d_np, d.contact_slots,
+                                                d.pairs, d.manifold_pair, &d.counters->num_points);
+    return 1 + 2 + 1 + launches + (int)ll;
 }
 
 int launch_compact_contacts(DeviceState& d, cudaStream_t s) {

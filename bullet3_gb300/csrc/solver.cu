@@ -42,6 +42,7 @@ struct SolverArgs {
     const b3gInertia* inertias;
     const b3gContact4* slots;
     const int* manifold_pair;
+    const int* d_npairs;      // slots below this hold pairs' manifolds, the rest compound child pairs'
     const int* d_nc;          // number of manifolds
     SolverPoints sp;
     SolverPoints sp_ord;      // PGS: the same records in colour order
@@ -1477,6 +1478,7 @@ struct WarmFill {
     SolverPoints sp;
     const b3gContact4* slots;
     const int* manifold_pair;
+    const int* d_npairs;
     int body_bits;
     const unsigned long long* prev_keys;
     const float4* prev_pts;
@@ -1490,6 +1492,12 @@ struct WarmFill {
     const int* pos_of;            // non-null: initial impulses go to the colour-ordered records
     float4* imp_ord;
 };
+
+// A compound child pair's manifold is never carried over (several share a body pair): its key
+// sorts after every pair's and matches nothing.
+__device__ __forceinline__ bool is_child_manifold(const int* manifold_pair, const int* d_npairs, int m) {
+    return __ldcg(&manifold_pair[m]) >= __ldcg(d_npairs);
+}
 
 __device__ __forceinline__ unsigned long long pair_key(int a, int b, int bits) {
     const unsigned lo = (unsigned)min(a, b), hi = (unsigned)max(a, b);
@@ -1515,7 +1523,7 @@ __global__ void k_warm_fill(WarmFill w) {
             else
                 hi = mid;
         }
-        const int q = (lo < pn && w.prev_keys[lo] == key) ? lo : -1;
+        const int q = (lo < pn && w.prev_keys[lo] == key && !is_child_manifold(w.manifold_pair, w.d_npairs, m)) ? lo : -1;
         const b3gContact4& c = w.slots[w.manifold_pair[m]];
         for (int j = 0; j < 4; j++) {
             const size_t s = (size_t)m * 4 + j;
@@ -1562,13 +1570,14 @@ __global__ void k_warm_fill(WarmFill w) {
 // The solved manifolds (first rows_cap / 4) for the next step's persistence lookup.
 __global__ void k_warm_store(const int* __restrict__ d_nc, int rows_cap, const int4* __restrict__ hdr,
                              const b3gContact4* __restrict__ slots, const int* __restrict__ manifold_pair,
-                             const float4* __restrict__ imp, int body_bits, unsigned long long* __restrict__ keys,
-                             float4* __restrict__ pts, float4* __restrict__ pimp, int* __restrict__ prev_n) {
+                             const int* __restrict__ d_npairs, const float4* __restrict__ imp, int body_bits,
+                             unsigned long long* __restrict__ keys, float4* __restrict__ pts,
+                             float4* __restrict__ pimp, int* __restrict__ prev_n) {
     const int n = min(*d_nc, rows_cap / 4);
     if (blockIdx.x == 0 && threadIdx.x == 0) *prev_n = n;
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
         const int4 h = hdr[m];
-        keys[m] = pair_key(h.x, h.y, body_bits);
+        keys[m] = is_child_manifold(manifold_pair, d_npairs, m) ? ~0ull : pair_key(h.x, h.y, body_bits);
         const b3gContact4& c = slots[manifold_pair[m]];
         for (int j = 0; j < 4; j++) {
             const size_t s = (size_t)m * 4 + j;
@@ -1617,7 +1626,7 @@ __global__ void __launch_bounds__(SV_THREADS) k_manifold_prep(SolverArgs a) {
                 if (c.worldPosB[j].w <= a.threshold) mask |= 1 << j;
             a.hdr[m] = make_int4(iA, iB, mask, np);
             a.inv_mass[m] = make_float2(imA, imB);
-            if (pn > 0) {
+            if (pn > 0 && a.manifold_pair[m] < *a.d_npairs) {
                 const unsigned long long key = pair_key(iA, iB, a.body_bits);
                 int q = min(m, pn - 1);
                 if (__ldcg(&a.prev_key[q]) != key) {
@@ -2010,7 +2019,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_pgs_sweeps(SolverArgs a) {
         const int4 h = __ldcg(&a.hdr_ord[k]);
         for (int j = 0; j < 4; j++)
             if (h.z & (1 << j)) a.sp.imp[(size_t)m * 4 + j] = __ldcg(&a.sp_ord.imp[(size_t)k * 4 + j]);
-        a.prev_key[m] = pair_key(h.x, h.y, a.body_bits);
+        a.prev_key[m] = is_child_manifold(a.manifold_pair, a.d_npairs, m) ? ~0ull : pair_key(h.x, h.y, a.body_bits);
         a.prev_color[m] = a.color[m];
     }
     if (tid == 0) *a.d_prev_n = nc;
@@ -2154,7 +2163,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) k_pgs_flow(SolverArgs a) {
         const int4 h = __ldcg(&a.hdr_ord[k]);
         for (int j = 0; j < 4; j++)
             if (h.z & (1 << j)) a.sp.imp[(size_t)m * 4 + j] = __ldcg(&a.sp_ord.imp[(size_t)k * 4 + j]);
-        a.prev_key[m] = pair_key(h.x, h.y, a.body_bits);
+        a.prev_key[m] = is_child_manifold(a.manifold_pair, a.d_npairs, m) ? ~0ull : pair_key(h.x, h.y, a.body_bits);
         a.prev_color[m] = a.color[m];
     }
     if (tid == 0) *a.d_prev_n = nc;
@@ -2242,6 +2251,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     a.inertias = d.inertias;
     a.slots = d.contact_slots;
     a.manifold_pair = d.manifold_pair;
+    a.d_npairs = &d.counters->pad[0];
     a.d_nc = d_nc;
     a.sp = d.sp;
     a.sp_ord = d.sp_ord;
@@ -2379,6 +2389,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
         w.sp = d.sp;
         w.slots = d.contact_slots;
         w.manifold_pair = d.manifold_pair;
+        w.d_npairs = &d.counters->pad[0];
         w.body_bits = d.body_bits;
         w.prev_keys = d.prev_keys;
         w.prev_pts = d.prev_pts;
@@ -2456,7 +2467,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
     launches++;
     if (wm != B3G_WARM_COLD && d.prev_keys) {  // this solve's impulses for the next step's persisting points
         k_warm_store<<<grid, SV_THREADS, 0, s>>>(d_nc, d.ws_rows_cap, d.manifold_hdr, d.contact_slots, d.manifold_pair,
-                                                 d.sp.imp, d.body_bits, d.prev_keys, d.prev_pts, d.prev_imp,
+                                                 &d.counters->pad[0], d.sp.imp, d.body_bits, d.prev_keys, d.prev_pts, d.prev_imp,
                                                  d.prev_n);
         launches++;
     }

@@ -69,6 +69,7 @@ struct b3gWorld {
     std::vector<int> indices;
     std::vector<b3gFloat4> vertices;
     std::vector<b3gFloat4> edges;
+    std::vector<b3gChildShape> children;  // the compounds' children (collidable.shapeIndex = first)
     std::vector<b3gBody> bodies;
     std::vector<b3gInertia> inertias;
     std::vector<int> user_index;
@@ -394,6 +395,52 @@ static b3gStatus add_hull(b3gWorld* w, const std::vector<float>& vxyz, const std
     return add_collidable(w, c, make_aabb(mn[0], mn[1], mn[2], mx[0], mx[1], mx[2]), out);
 }
 
+extern "C" b3gStatus b3g_register_compound(b3g_handle h, const b3gChildShape* children, int num_children,
+                                           int* out) {
+    if (!h || !out) return fail(B3G_ERR_INVALID_ARG, "null argument");
+    if (h->uploaded) return fail(B3G_ERR_INVALID_ARG, "register shapes before the upload");
+    // the collidable slot is taken first, as allocateCollidable runs first (b3GpuNarrowPhase.cpp:372-374)
+    if ((int)h->collidables.size() >= h->cfg.max_shapes)
+        return fail(B3G_ERR_CAPACITY, "allocateCollidable out-of-range %d", h->cfg.max_shapes);
+    if (!children || num_children < 1) return fail(B3G_ERR_INVALID_ARG, "a compound needs at least one child");
+    // the union of the children's local AABBs moved into the compound's frame (b3GpuNarrowPhase.cpp:391-431)
+    float mn[3] = {1e30f, 1e30f, 1e30f}, mx[3] = {-1e30f, -1e30f, -1e30f};
+    for (int i = 0; i < num_children; i++) {
+        const int c = children[i].shapeIndex;
+        if (c < 0 || c >= (int)h->collidables.size() || h->collidables[c].shapeType != B3G_SHAPE_CONVEX_HULL)
+            return fail(B3G_ERR_INVALID_INDEX, "compound child %d is not a convex hull collidable", i);
+        v3 a, b;
+        transform_aabb(h->local_aabbs[c], f4v3(children[i].childPosition), f4q(children[i].childOrientation), 0.f, a,
+                       b);
+        if (a.x < mn[0]) mn[0] = a.x;
+        if (a.y < mn[1]) mn[1] = a.y;
+        if (a.z < mn[2]) mn[2] = a.z;
+        if (mx[0] < b.x) mx[0] = b.x;
+        if (mx[1] < b.y) mx[1] = b.y;
+        if (mx[2] < b.z) mx[2] = b.z;
+    }
+    b3gCollidable col{num_children, 0.f, B3G_SHAPE_COMPOUND, (int)h->children.size()};
+    const b3gStatus st = add_collidable(h, col, make_aabb(mn[0], mn[1], mn[2], mx[0], mx[1], mx[2]), out);
+    if (st != B3G_OK) return st;
+    for (int i = 0; i < num_children; i++) {
+        b3gChildShape c = children[i];
+        c.childPosition.w = 0.f;
+        c.numChildShapes = 0;
+        c.collidableShapeIndex = 0;
+        c.shapeType = B3G_SHAPE_CONVEX_HULL;
+        h->children.push_back(c);
+    }
+    return B3G_OK;
+}
+
+extern "C" b3gStatus b3g_read_child_shapes(b3g_handle h, b3gChildShape* host, int capacity, int* num) {
+    if (!h || !num) return fail(B3G_ERR_INVALID_ARG, "null argument");
+    *num = (int)h->children.size();
+    if (host && capacity > 0)
+        std::copy(h->children.begin(), h->children.begin() + std::min(capacity, *num), host);
+    return B3G_OK;
+}
+
 extern "C" b3gStatus b3g_register_hull(b3g_handle h, const float* verts, int stride_bytes, int num_verts,
                                        const float scaling[3], int* out) {
     if (!h || !verts || !out) return fail(B3G_ERR_INVALID_ARG, "null argument");
@@ -620,9 +667,13 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     d.body_bits = bits_for(N + 1);
     if (2 * d.body_bits > 64) return fail(B3G_ERR_CAPACITY, "too many bodies");
     d.max_pairs = h->cfg.max_pairs > 0 ? h->cfg.max_pairs : std::max(4096, 24 * N);
-    // at most one manifold per pair: contact storage is sized with the pair capacity so that no
-    // manifold index can exceed it
-    d.max_contacts = d.max_pairs;
+    // at most one manifold per pair, and one per compound child pair: contact storage is sized with
+    // the pair capacity (plus the child pairs') so that no manifold index can exceed it
+    d.num_children = (int)h->children.size();
+    d.max_child_pairs = d.num_children > 0 ? (h->cfg.max_compound_child_pairs > 0 ? h->cfg.max_compound_child_pairs
+                                                                                  : d.max_pairs)
+                                           : 0;
+    d.max_contacts = d.max_pairs + d.max_child_pairs;
     d.prim.sort_blocks = sms * d.tune.sort_blocks_per_sm;
     d.prim.scan_blocks = sms * 2;
 
@@ -663,10 +714,16 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     TRY(dalloc(h, &d.cell_start, ncells));
     TRY(dalloc(h, &d.pairs, d.max_pairs));
     TRY(dalloc(h, &d.type_lists, (size_t)PT_COUNT * d.max_pairs));
-    TRY(dalloc(h, &d.contact_slots, d.max_pairs));
-    TRY(dalloc(h, &d.contact_flag, d.max_pairs));
-    TRY(dalloc(h, &d.contact_index, d.max_pairs));
-    TRY(dalloc(h, &d.manifold_pair, d.max_pairs));
+    TRY(dalloc(h, &d.contact_slots, d.max_contacts));
+    TRY(dalloc(h, &d.contact_flag, d.max_contacts));
+    TRY(dalloc(h, &d.contact_index, d.max_contacts));
+    TRY(dalloc(h, &d.manifold_pair, d.max_contacts));
+    if (d.num_children > 0) {
+        TRY(dalloc(h, &d.children, d.num_children));
+        TRY(dalloc(h, &d.child_count, d.max_pairs));
+        TRY(dalloc(h, &d.child_offset, d.max_pairs));
+        TRY(dalloc(h, &d.child_pairs, d.max_child_pairs));
+    }
     TRY(dalloc(h, &d.contacts_compact, d.max_contacts));
     TRY(dalloc(h, &d.sp.nf, d.max_contacts));
     TRY(dalloc(h, &d.sp.rel1, 4 * (size_t)d.max_contacts));
@@ -768,6 +825,9 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     if (!h->edges.empty())
         CUDA_TRY(cudaMemcpyAsync(d.edges, h->edges.data(), sizeof(b3gFloat4) * h->edges.size(), cudaMemcpyHostToDevice, s));
     CUDA_TRY(cudaMemcpyAsync(d.dyn_slot, dyn_slot.data(), sizeof(int) * N, cudaMemcpyHostToDevice, s));
+    if (d.num_children > 0)
+        CUDA_TRY(cudaMemcpyAsync(d.children, h->children.data(), sizeof(b3gChildShape) * h->children.size(),
+                                 cudaMemcpyHostToDevice, s));
     {
         // faces whose normal is the exact negation of an earlier face's (a box's opposite faces):
         // rotated and sign-flipped towards the other body they give the earlier face's SAT axis
@@ -1631,7 +1691,10 @@ __global__ void k_expand_contacts(const b3gContact4* __restrict__ in, int n, b3g
         manifold_pair[m] = m;
         flags[m] = 1;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) counters->num_contacts = n;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        counters->num_contacts = n;
+        counters->pad[0] = n;  // every written manifold counts as a pair's (none as a compound child pair's)
+    }
 }
 
 extern "C" b3gStatus b3g_write_contacts(b3g_handle h, const void* host, int n) {

@@ -168,10 +168,18 @@ struct DeviceState {
     b3gPair* pairs = nullptr;
     int* type_lists = nullptr;        // PT_COUNT * max_pairs
     // narrowphase
-    b3gContact4* contact_slots = nullptr;  // one per pair slot
-    int* contact_flag = nullptr;           // per pair: 1 if a manifold was produced
-    int* contact_index = nullptr;          // per pair: exclusive scan of contact_flag
-    int* manifold_pair = nullptr;          // manifold -> pair index
+    b3gContact4* contact_slots = nullptr;  // one per pair slot, then one per compound child pair
+    int* contact_flag = nullptr;           // per slot: 1 if a manifold was produced
+    int* contact_index = nullptr;          // per slot: exclusive scan of contact_flag
+    int* manifold_pair = nullptr;          // manifold -> slot index (< pair count: a pair)
+    // compounds (allocated when one is registered): child shapes, the per-pair child-pair counts
+    // and their scan, the child pairs (bodyA, bodyB, child of A or -1, child of B or -1)
+    b3gChildShape* children = nullptr;
+    int num_children = 0;
+    int max_child_pairs = 0;
+    int* child_count = nullptr;
+    int* child_offset = nullptr;
+    int4* child_pairs = nullptr;
     b3gContact4* contacts_compact = nullptr;  // filled on demand for the drop-in getter
     // solver
     SolverPoints sp;                       // compact contact-point records

@@ -34,6 +34,7 @@ class b3Config:
         self.m_maxConvexShapes = 8 * 1024
         self.m_maxBroadphasePairs = 0
         self.m_maxContactCapacity = 0
+        self.m_compoundPairCapacity = 0  # child pairs of compounds per step (0 = m_maxBroadphasePairs)
         self.grid_cell_size = 0.0
         self.grid_dim = 128
         self.solver_mode = capi.SOLVER_PGS
@@ -70,7 +71,8 @@ class b3Config:
                                    pgs_interleave=int(self.pgs_interleave), warm_start=int(self.warm_start),
                                    warm_start_max_points=int(self.warm_start_max_points),
                                    autotune=int(self.autotune), broadphase=int(self.broadphase),
-                                   pgs_tail_manifolds=int(self.pgs_tail_manifolds), pgs_flow=int(self.pgs_flow))
+                                   pgs_tail_manifolds=int(self.pgs_tail_manifolds), pgs_flow=int(self.pgs_flow),
+                                   max_compound_child_pairs=int(self.m_compoundPairCapacity))
 
 
 class _World:
@@ -143,8 +145,18 @@ class b3GpuNarrowPhase:
                          iptr(ix), fptr(e), C.c_int(len(e)))
 
     def registerCompoundShape(self, childShapes) -> int:
-        b3Error("registerCompoundShape: compound shapes are not supported by this GPU step")
-        return -1
+        """registerCompoundShape(b3AlignedObjectArray<b3GpuChildShape>*): childShapes is a
+        capi.CHILD array, or a list of (hull collidable, position, orientation)."""
+        if isinstance(childShapes, np.ndarray) and childShapes.dtype == capi.CHILD:
+            ch = np.ascontiguousarray(childShapes)
+        else:
+            ch = np.zeros(len(childShapes), capi.CHILD)
+            for i, (c, pos, orn) in enumerate(childShapes):
+                ch[i]["childPosition"][:3] = np.asarray(pos, np.float32)[:3]
+                ch[i]["childOrientation"] = np.asarray(orn, np.float32)[:4]
+                ch[i]["shapeIndex"] = int(c)
+                ch[i]["shapeType"] = 3
+        return self._reg("b3g_register_compound", capi.ptr(ch), C.c_int(len(ch)))
 
     def registerConcaveMesh(self, vertices, indices, scaling) -> int:
         b3Error("registerConcaveMesh: concave meshes are not supported by this GPU step")

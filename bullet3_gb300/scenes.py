@@ -8,6 +8,8 @@ configurations (numpy.random.Generator(PCG64(seed))).
                  extents U[0.2,0.6], 25% spheres r U[0.2,0.5], 25% hulls of 12-32 N(0, 0.4^2) points;
                  linear velocities N(0,1)
   batched_piles  many independent box/sphere piles, each on its own plane, body counts log-uniform
+  compound_scene compounds of convex hulls (an L of two boxes, a dumbbell of two hulls and a box)
+                 among boxes and hulls over a plane
 
 A Scene is plain numpy data; `load_scene` registers it through the reference-style API.
 """
@@ -203,6 +205,57 @@ def mixed_scene(n=131072, extent=64.0, seed=0, velocity_sigma=1.0, plane=False, 
     sc.orn = orn
     sc.linvel = vel
     sc.cell = cell_factor * max_ext
+    return sc
+
+
+def compound_scene(n=2048, extent=None, seed=0, plane=True, velocity_sigma=0.5, lattice=False) -> Scene:
+    """Compounds of convex hulls among single hulls: an L of two boxes (0.5 x 0.25 x 0.25 and
+    0.25 x 0.5 x 0.25 half extents), a dumbbell (two hulls of 20 N(0, 0.3^2) points at x = +-0.6
+    around a 0.5 x 0.25 x 0.25 box), that box and that hull alone, in turn, over a plane y = 0.
+    Uniform positions (x, z in [0, extent), y in [0, 1.5 + extent / 8)) with random orientations
+    and N(0, velocity_sigma^2) velocities, or with lattice=True a jittered lattice spaced by the
+    widest body's reach (random orientations, at rest, nothing overlapping) that settles into a
+    pile."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sc = Scene(name=f"compound_{n}")
+    if plane:
+        sc.shapes.append({"type": "plane", "normal": (0.0, 1.0, 0.0), "constant": 0.0})
+    base = len(sc.shapes)
+    gauss = (rng.standard_normal((20, 3)) * 0.3).astype(np.float32)
+    sc.shapes += [{"type": "hull", "verts": box_vertices(0.5, 0.25, 0.25)},
+                  {"type": "hull", "verts": box_vertices(0.25, 0.5, 0.25)},
+                  {"type": "hull", "verts": gauss}]
+    bx, by, gh = base, base + 1, base + 2
+    q0 = (0.0, 0.0, 0.0, 1.0)
+    sc.shapes.append({"type": "compound", "children": [(bx, (0.25, 0.0, 0.0), q0), (by, (0.0, 0.5, 0.0), q0)]})
+    qa, qb = random_quaternions(rng, 2)
+    sc.shapes.append({"type": "compound", "children": [(gh, (-0.6, 0.0, 0.0), tuple(qa)), (bx, (0.0, 0.0, 0.0), q0),
+                                                        (gh, (0.6, 0.0, 0.0), tuple(qb))]})
+    kinds = np.array([base + 3, base + 4, bx, gh], np.int32)[np.arange(n) % 4]
+    # the widest body: the dumbbell, its hulls' farthest points 0.6 off the centre
+    reach = 0.6 + float(np.linalg.norm(gauss, axis=1).max())
+    if lattice:
+        side = int(np.ceil(np.sqrt(n / 4)))
+        i = np.arange(n)
+        sp = 2.0 * reach + 0.1  # no two bodies and no body and the plane overlap at the start
+        pos = np.stack([(i % side) * sp, reach + 0.1 + (i // (side * side)) * sp, ((i // side) % side) * sp], 1)
+        pos = (pos + rng.uniform(-0.04, 0.04, (n, 3))).astype(np.float32)
+        vel = np.zeros((n, 3), np.float32)
+    else:
+        extent = extent if extent is not None else float(np.sqrt(n) * 0.6)
+        pos = np.stack([rng.uniform(0, extent, n), rng.uniform(0, 1.5 + extent / 8, n), rng.uniform(0, extent, n)],
+                       1).astype(np.float32)
+        vel = (rng.standard_normal((n, 3)) * velocity_sigma).astype(np.float32)
+    orn = random_quaternions(rng, n)
+    if plane:
+        kinds = np.concatenate([[0], kinds]).astype(np.int32)
+        pos = np.vstack([np.zeros((1, 3), np.float32), pos])
+        orn = np.vstack([np.array([[0, 0, 0, 1]], np.float32), orn])
+        vel = np.vstack([np.zeros((1, 3), np.float32), vel])
+    sc.body_shape = kinds
+    sc.mass = np.where(kinds == 0, 0.0, 1.0).astype(np.float32) if plane else np.ones(n, np.float32)
+    sc.pos, sc.orn, sc.linvel = pos, orn, vel
+    sc.cell = 2.0 * 2.0 * reach
     return sc
 
 
@@ -457,6 +510,9 @@ def load_scene(scene: Scene, config=None, device: int = 0, upload: bool = True):
         elif s["type"] == "hull_tables":
             c = np_.registerConvexHullShapeTables(s["verts"], s["planes"], s["face_counts"], s["indices"],
                                                   s["edges"])
+        elif s["type"] == "compound":
+            # children: (index of an earlier shape of the scene, position, orientation)
+            c = np_.registerCompoundShape([(col[i], p, q) for i, p, q in s["children"]])
         else:
             raise ValueError(s["type"])
         if c < 0:
@@ -502,6 +558,11 @@ def registered_tables(narrowphase):
     capi.call("b3g_read_shape_tables", h, capi.ptr(t["collidables"]), capi.ptr(t["hulls"]), capi.ptr(t["faces"]),
               capi.iptr(t["indices"]), capi.ptr(t["verts"]), capi.ptr(t["edges"]), capi.ptr(t["local_aabbs"]),
               capi.iptr(caps))
+    nch = C.c_int()
+    capi.call("b3g_read_child_shapes", h, None, C.c_int(0), C.byref(nch))
+    t["children"] = np.zeros(max(nch.value, 1), capi.CHILD)
+    if nch.value:
+        capi.call("b3g_read_child_shapes", h, capi.ptr(t["children"]), C.c_int(nch.value), C.byref(nch))
     nb = narrowphase.getNumRigidBodies()
     bodies = np.zeros(nb, capi.BODY)
     inertias = np.zeros(nb, capi.INERTIA)

@@ -122,7 +122,9 @@ typedef struct b3gConfig {
                                   a grid barrier per colour; same order, same results); 0 (default) and
                                   2 = a grid barrier per colour, measured faster on GB300 from 16k to
                                   300k manifolds */
-    int reserved[3];
+    int max_compound_child_pairs;  /* child pairs of the compound pairs per step (0 = max_pairs); only
+                                      allocated when a compound is registered */
+    int reserved[2];
 } b3gConfig;
 
 /* Per-step counters, copied once per step from the device. */
@@ -175,6 +177,19 @@ b3gStatus b3g_register_hull_tables(b3g_handle h, const float* verts_xyz, int num
                                    const float* face_planes, const int* face_index_counts, int num_faces,
                                    const int* face_indices, const float* unique_edges_xyz, int num_edges,
                                    int* out_collidable);
+/* b3GpuNarrowPhase::registerCompoundShape (b3GpuNarrowPhase.cpp:370-433): a compound of convex
+ * hulls (each child's shapeIndex an earlier hull collidable).  Its local AABB is the union of the
+ * children's, moved into the compound's frame (b3TransformAabb, margin 0).  A pair with a compound
+ * expands into child pairs (compound-compound: children whose world AABBs overlap; compound against
+ * a hull or a plane: every child), one manifold per child pair at most, as the reference's
+ * findCompoundPairsKernel / processCompoundPairsKernel / clipCompoundsHullHullKernel
+ * (b3ConvexHullContact.cpp:1419-2022) and computeContactPlaneCompound (:2182) compute them.  Compounds
+ * against spheres give no contacts. */
+struct b3gChildShape;
+b3gStatus b3g_register_compound(b3g_handle h, const struct b3gChildShape* children, int num_children,
+                                int* out_collidable);
+/* Host copy of the registered compound children (b3gChildShape, b3g_types.h; capacity 0: count only). */
+b3gStatus b3g_read_child_shapes(b3g_handle h, struct b3gChildShape* host_children, int capacity, int* num);
 
 /* ------------------------------------------------------------------ bodies (b3GpuRigidBodyPipeline) */
 /* b3GpuRigidBodyPipeline::registerPhysicsInstance (b3GpuRigidBodyPipeline.cpp:603-669) together with

@@ -199,6 +199,7 @@ inline b3gConfig b3gConfigFrom(const b3Config& c) {
     out.max_shapes = c.m_maxConvexShapes;
     out.max_pairs = c.m_maxBroadphasePairs;
     out.max_contacts = c.m_maxContactCapacity;
+    out.max_compound_child_pairs = c.m_compoundPairCapacity;
     return out;
 }
 
@@ -221,9 +222,16 @@ public:
         const float n[3] = {planeNormal.getX(), planeNormal.getY(), planeNormal.getZ()};
         return reg(b3g_register_plane(m_world, n, planeConstant, &m_out), "registerPlaneShape");
     }
-    int registerCompoundShape(b3AlignedObjectArray<b3GpuChildShape>* /*childShapes*/) {
-        std::fprintf(stderr, "b3Error: registerCompoundShape: compound shapes are not supported\n");
-        return -1;
+    /* registerCompoundShape (b3GpuNarrowPhase.cpp:370-433): children are convex hull collidables at
+       poses in the compound's frame; the compound's local AABB is the union of theirs */
+    int registerCompoundShape(b3AlignedObjectArray<b3GpuChildShape>* childShapes) {
+        if (!childShapes || childShapes->size() == 0) {
+            std::fprintf(stderr, "b3Error: registerCompoundShape: no child shapes\n");
+            return -1;
+        }
+        return reg(b3g_register_compound(m_world, reinterpret_cast<const b3gChildShape*>(&childShapes->at(0)),
+                                         childShapes->size(), &m_out),
+                   "registerCompoundShape");
     }
     int registerConcaveMesh(b3AlignedObjectArray<b3Vector3>* /*vertices*/, b3AlignedObjectArray<int>* /*indices*/,
                             const float* /*scaling*/) {

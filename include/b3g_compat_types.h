@@ -221,7 +221,26 @@ typedef b3gCollidable b3Collidable;
 typedef b3gContact4 b3Contact4;
 #endif
 
-struct b3GpuChildShape;  // compound children (registerCompoundShape is not supported)
+/* b3GpuChildShape (Bullet3Collision/NarrowPhaseCollision/shared/b3Collidable.h:41-58): a child of a
+ * compound, the layout of b3gChildShape (48 B) */
+struct alignas(16) b3GpuChildShape {
+    b3Vector3 m_childPosition;
+    b3Quaternion m_childOrientation;
+    union {
+        int m_shapeIndex;  // the child's collidable (a convex hull)
+        int m_capsuleAxis;
+    };
+    union {
+        float m_radius;
+        int m_numChildShapes;
+    };
+    union {
+        float m_height;
+        int m_collidableShapeIndex;
+    };
+    int m_shapeType;
+};
+static_assert(sizeof(b3GpuChildShape) == sizeof(b3gChildShape), "b3GpuChildShape layout");
 
 #ifndef B3_GEN_MINMAX_H
 #define B3_GEN_MINMAX_H

@@ -26,6 +26,7 @@ extern "C" {
 
 #define B3G_SHAPE_CONVEX_HULL 3
 #define B3G_SHAPE_PLANE 4
+#define B3G_SHAPE_COMPOUND 6   /* SHAPE_COMPOUND_OF_CONVEX_HULLS */
 #define B3G_SHAPE_SPHERE 7
 
 typedef struct b3gFloat4 { float x, y, z, w; } b3gFloat4;
@@ -97,6 +98,17 @@ typedef struct b3gContact4 {
     int unused1;
     int unused2;
 } b3gContact4;
+
+/* b3GpuChildShape (Bullet3Collision/NarrowPhaseCollision/shared/b3Collidable.h:41-62), 48 B: a
+ * compound's child, a convex hull collidable at a pose in the compound's frame */
+typedef struct b3gChildShape {
+    b3gFloat4 childPosition;
+    b3gFloat4 childOrientation;  /* x,y,z,w */
+    int shapeIndex;              /* the child's collidable (a convex hull) */
+    int numChildShapes;          /* unused for children */
+    int collidableShapeIndex;    /* unused for children */
+    int shapeType;               /* B3G_SHAPE_CONVEX_HULL */
+} b3gChildShape;
 
 typedef struct b3gPair { int x, y, z, w; } b3gPair;
 

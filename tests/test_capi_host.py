@@ -51,6 +51,24 @@ def test_registration_errors_match_reference_conventions():
     assert np_.registerConvexHullShape(np.zeros((3, 3), np.float32)) == -1  # degenerate hull
 
 
+def test_compound_registration_matches_the_oracle_registry():
+    # registerCompoundShape: the collidable (type 6, first child, child count), the children with
+    # their poses, and the local AABB as the union of the children's moved into the compound's frame
+    # (b3GpuNarrowPhase.cpp:370-433), bit-exact with the oracle's registry
+    from bullet3_gb300 import scenes
+    from oracle import oracle as O
+    sc = scenes.compound_scene(64, seed=5)
+    np_, bp, pl = scenes.load_scene(sc, b3Config(use_cuda_graph=False), upload=False)
+    t = scenes.registered_tables(np_)
+    ref = O.register_scene(sc)
+    for k in ("collidables", "local_aabbs", "children"):
+        assert np.array_equal(t[k].view(np.uint8), ref[k].view(np.uint8)), k
+    assert (t["collidables"]["shapeType"] == capi.SHAPE_COMPOUND).sum() == 2
+    # a child that is not a convex hull is refused (-1 + b3Error), the table left unchanged
+    assert np_.registerCompoundShape([(0, (0, 0, 0), (0, 0, 0, 1))]) == -1  # collidable 0 is the plane
+    assert np_.getNumCollidablesGpu() == len(t["collidables"])
+
+
 def test_config_validation():
     h = C.c_void_p()
     for bad in (dict(pgs_partitions=5), dict(pgs_partitions=-1), dict(solver_blocks_per_sm=-2), dict(grid_dim=100),
@@ -167,6 +185,10 @@ def test_cpp_dropin_header_compiles(tmp_path):
                    "  b3ConvexUtility u; b3AlignedObjectArray<b3Vector3> v; v.push_back(b3MakeVector3(0, 0, 0));\n"
                    "  u.initializePolyhedralFeatures(&v[0], v.size()); np.registerConvexHullShape(&u);\n"
                    "  rbp.registerConvexPolyhedron(&u);\n"
+                   "  b3AlignedObjectArray<b3GpuChildShape> kids; b3GpuChildShape ch;\n"
+                   "  ch.m_childPosition = b3MakeVector3(0.5f, 0, 0); ch.m_childOrientation = b3Quaternion(0, 0, 0, 1);\n"
+                   "  ch.m_shapeIndex = 1; ch.m_numChildShapes = 0; ch.m_collidableShapeIndex = 0; ch.m_shapeType = 3;\n"
+                   "  kids.push_back(ch); np.registerCompoundShape(&kids);\n"
                    "  bp.calculateOverlappingPairsHost(0); bp.getAllAabbsCPU(); rbp.copyConstraintsToHost();\n"
                    "  b3OpenCLArray<b3Int4>& pairs = bp.getOverlappingPairsGPU();\n"
                    "  np.computeContacts(pairs.getBufferCL(), (int)pairs.size(), bp.getAabbBufferWS(), 0);\n"
