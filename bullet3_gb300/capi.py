@@ -81,7 +81,7 @@ class b3gTuning(C.Structure):
 class b3gStepStats(C.Structure):
     _fields_ = [("num_pairs", C.c_int), ("num_contacts", C.c_int), ("num_points", C.c_int),
                 ("num_colors", C.c_int), ("iterations", C.c_int), ("residual", C.c_float),
-                ("status", C.c_uint), ("num_large", C.c_int)]
+                ("status", C.c_uint), ("num_large", C.c_int), ("num_child_pairs", C.c_int)]
 
 
 class B3GError(RuntimeError):

@@ -884,93 +884,9 @@ __device__ bool find_sep_full(const NPArgs& a, const b3gHull& hA, const b3gHull&
     return true;
 }
 
-// findSeparatingAxisEdgeEdge (b3ConvexHullContact.cpp:702-785): every edge-edge axis projected, no
-// early exit (its separation test is discarded); the smallest overlap replaces sep
-__device__ void edge_edge_axis(const NPArgs& a, const b3gHull& hA, const b3gHull& hB, v3 posA, quat qA, v3 posB,
-                               quat qB, v3 deltaC2, v3& sep) {
-    const b3gFloat4* vA = &a.verts[hA.vertexOffset];
-    const b3gFloat4* vB = &a.verts[hB.vertexOffset];
-    float dmin = FLT_MAX;
-    for (int e0 = 0; e0 < hA.numUniqueEdges; e0++) {
-        const v3 w0 = qrotq(qA, ld3(&a.edges[hA.uniqueEdgesOffset + e0]));
-        for (int e1 = 0; e1 < hB.numUniqueEdges; e1++) {
-            const v3 w1 = qrotq(qB, ld3(&a.edges[hB.uniqueEdgesOffset + e1]));
-            v3 c = cross3(w0, w1);
-            if (!((double)fabsf(c.x) > 1e-6 || (double)fabsf(c.y) > 1e-6 || (double)fabsf(c.z) > 1e-6)) continue;
-            c = normalize3(c);
-            if (dot3(deltaC2, c) < 0.f) c = -c;
-            float min0, max0, min1, max1;
-            project(vA, hA.numVertices, posA, qA, c, min0, max0);
-            project(vB, hB.numVertices, posB, qB, c, min1, max1);
-            const float d0 = max0 - min1, d1 = max1 - min0;
-            const float dist = d0 < d1 ? d0 : d1;
-            if (dist < dmin) { dmin = dist; sep = c; }
-        }
-    }
-    if (dot3(-deltaC2, sep) > 0.0f) sep = -sep;
-}
-
-// clipHullAgainstHull -> clipFaceAgainstHull (b3ConvexHullContact.cpp:939-1044, :834-937): the
-// incident face of B (max dot), its vertices clipped by the side planes of A's reference face (min
-// dot), depth clamped at minDist and kept if <= maxDist; rotations by b3QuatRotate of the poses,
-// points by their matrices.  pin / pout: CLIP_CAP float4 each; returns the count of the points,
-// left in *result (one of the two buffers)
-__device__ int clip_hull_against_hull(const NPArgs& a, v3 sep, const b3gHull& hA, const b3gHull& hB, v3 posA,
-                                      quat qA, v3 posB, quat qB, float minDist, float maxDist, float4* pin,
-                                      float4* pout, float4** result) {
-    int fb = -1, fa = -1;
-    float dmax = -FLT_MAX, dmn = FLT_MAX;
-    for (int f = 0; f < hB.numFaces; f++) {
-        const float d = dot3(qrotq(qB, ld3(&a.faces[hB.faceOffset + f].plane)), sep);
-        if (d > dmax) { dmax = d; fb = f; }
-    }
-    if (fb < 0) return 0;
-    const m33 RA = qmat(qA), RB = qmat(qB);
-    const b3gFace polyB = a.faces[hB.faceOffset + fb];
-    int nin = 0;
-    for (int e = 0; e < polyB.numIndices && e < CLIP_CAP; e++) {
-        const v3 w = mmul(RB, ld3(&a.verts[hB.vertexOffset + a.indices[polyB.indexOffset + e]])) + posB;
-        pin[nin++] = make_float4(w.x, w.y, w.z, 0.f);
-    }
-    for (int f = 0; f < hA.numFaces; f++) {
-        const float d = dot3(qrotq(qA, ld3(&a.faces[hA.faceOffset + f].plane)), sep);
-        if (d < dmn) { dmn = d; fa = f; }
-    }
-    if (fa < 0) return 0;
-    const b3gFace polyA = a.faces[hA.faceOffset + fa];
-    const v3 planeNormalA = mk3(polyA.plane.x, polyA.plane.y, polyA.plane.z);
-    const int nva = polyA.numIndices;
-    for (int e0 = 0; e0 < nva; e0++) {
-        const v3 va = ld3(&a.verts[hA.vertexOffset + a.indices[polyA.indexOffset + e0]]);
-        const v3 vb = ld3(&a.verts[hA.vertexOffset + a.indices[polyA.indexOffset + ((e0 + 1) % nva)]]);
-        const v3 worldEdge0 = qrotq(qA, va - vb);
-        const v3 worldPlaneAnormal1 = qrotq(qA, planeNormalA);
-        const v3 planeNormalWS1 = -cross3(worldEdge0, worldPlaneAnormal1);
-        const v3 worldA1 = mmul(RA, va) + posA;
-        const float planeEqWS1 = -dot3(worldA1, planeNormalWS1);
-        const int nout = clip_face(pin, nin, planeNormalWS1, planeEqWS1, pout, a.status);
-        float4* t = pout;
-        pout = pin;
-        pin = t;
-        nin = nout;
-    }
-    const v3 planeNormalWS = qrotq(qA, planeNormalA);
-    const float planeEqWS = polyA.plane.w - dot3(planeNormalWS, posA);
-    int n = 0;
-    for (int i = 0; i < nin; i++) {
-        float depth = dot3(planeNormalWS, mk3(pin[i].x, pin[i].y, pin[i].z)) + planeEqWS;
-        if (depth <= minDist) depth = minDist;
-        if (n < CLIP_CAP && depth <= maxDist) pout[n++] = make_float4(pin[i].x, pin[i].y, pin[i].z, depth);
-    }
-    *result = pout;
-    return n;
-}
-
-// One child pair per thread (slot = pair count + child pair index): processCompoundPairsKernel +
-// clipCompoundsHullHullKernel (b3ConvexHullContact.cpp:1777-2022) for two hulls -- the axis of
-// findSeparatingAxis(A, B), then of findSeparatingAxis(B, A), then the edge-edge pass; clipped with
-// minDist -1e30 and maxDist 0, reduced against -sep, friction 0.7 -- or computeContactPlaneCompound
-// (:2182-2321) for a plane against a child.  Compound children against spheres give nothing.
+// One child pair per thread (slot = pair count + child pair index): every slot's flag cleared, and
+// computeContactPlaneCompound (b3ConvexHullContact.cpp:2182-2321) for a plane against a child.
+// Two hulls are k_compound_hull_hull's; compound children against spheres give nothing.
 __global__ void __launch_bounds__(NP_THREADS, 2) k_compound_contacts(NPArgs a, const int* __restrict__ d_np,
                                                                      const int* __restrict__ d_J,
                                                                      const int4* __restrict__ child_pairs) {
@@ -997,31 +913,9 @@ __global__ void __launch_bounds__(NP_THREADS, 2) k_compound_contacts(NPArgs a, c
         }
         const b3gCollidable cA = a.cols[colA], cB = a.cols[colB];
         b3gContact4& c = a.slots[slot];
-        if (cA.shapeType == B3G_SHAPE_CONVEX_HULL && cB.shapeType == B3G_SHAPE_CONVEX_HULL) {
-            const b3gHull hA = a.hulls[cA.shapeIndex], hB = a.hulls[cB.shapeIndex];
-            const v3 deltaC2 =
-                (mmul(qmat(qA), f4v3(hA.localCenter)) + posA) - (mmul(qmat(qB), f4v3(hB.localCenter)) + posB);
-            v3 sep = mk3(1.f, 0.f, 0.f);
-            if (!find_sep_full(a, hA, hB, posA, qA, posB, qB, sep)) continue;
-            if (!find_sep_full(a, hB, hA, posB, qB, posA, qA, sep)) continue;
-            edge_edge_axis(a, hA, hB, posA, qA, posB, qB, deltaC2, sep);
-            float4 buf0[CLIP_CAP], buf1[CLIP_CAP];
-            float4* pts = buf0;
-            const int np = clip_hull_against_hull(a, sep, hA, hB, posA, qA, posB, qB, -1e30f, 0.0f, buf0, buf1, &pts);
-            if (np <= 0) continue;
-            int idx[4];
-            const int nred = reduce_contacts(pts, np, -sep, idx);
-            write_header(c, a, cp.x, cp.y, sep, nred);
-            c.frictionCmp = fr07;
-            c.batchIdx = j;
-            c.childIndexA = cp.z;
-            c.childIndexB = cp.w;
-            for (int i = 0; i < nred; i++) {
-                const float4 q = pts[idx[i]];
-                c.worldPosB[i] = b3gFloat4{q.x, q.y, q.z, q.w};
-            }
-            a.flags[slot] = 1;
-        } else {
+        // two hulls: k_compound_hull_hull, a warp per child pair
+        if (cA.shapeType == B3G_SHAPE_CONVEX_HULL && cB.shapeType == B3G_SHAPE_CONVEX_HULL) continue;
+        {
             // a plane against a child: the plane body first in the manifold, the child's hull at its pose
             int plane = -1, comp = -1, child = -1;
             v3 pos;
@@ -1049,6 +943,160 @@ __global__ void __launch_bounds__(NP_THREADS, 2) k_compound_contacts(NPArgs a, c
                 a.flags[slot] = 1;
             }
         }
+    }
+}
+
+// Two hulls of a child pair, one warp per child pair (slot = pair count + child pair index):
+// processCompoundPairsKernel + clipCompoundsHullHullKernel (b3ConvexHullContact.cpp:1777-2022).
+// The reference runs findSeparatingAxis(A, B), findSeparatingAxis(B, A) and
+// findSeparatingAxisEdgeEdge(A, B) in turn and keeps the axis the last one leaves.  The second
+// pass tests the first pass's axes, each exactly negated (negation is exact and x - y = -(y - x)),
+// with the same overlaps, so it separates exactly when the first does; the edge pass recomputes
+// the first pass's edge overlaps.  So one pass over the faces of A, the faces of B and the edge
+// axes decides the separation and keeps the first minimum of the edge axes, the contact normal;
+// only when no edge axis is usable (every cross product almost zero) does the second pass's face
+// minimum stand, computed then as the reference computes it.  Clipped at the child poses with
+// minDist -1e30 and maxDist 0, reduced against -sep, friction 0.7.
+static constexpr int CH_WARPS = 4;
+
+__global__ void __launch_bounds__(CH_WARPS * 32) k_compound_hull_hull(NPArgs a, const int* __restrict__ d_np,
+                                                                     const int* __restrict__ d_J,
+                                                                     const int4* __restrict__ child_pairs) {
+    __shared__ float4 s_poly[CH_WARPS][2][CLIP_CAP];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int P = *d_np, J = *d_J;
+    const unsigned short fr07 = (unsigned short)(0.7f * 0xffff);
+    for (int j = blockIdx.x * CH_WARPS + wib; j < J; j += gridDim.x * CH_WARPS) {
+        const int4 cp = child_pairs[j];
+        const b3gBody& BA = a.bodies[cp.x];
+        const b3gBody& BB = a.bodies[cp.y];
+        v3 posA = f4v3(BA.pos), posB = f4v3(BB.pos);
+        quat qA = f4q(BA.quat), qB = f4q(BB.quat);
+        int colA = BA.collidableIdx, colB = BB.collidableIdx;
+        if (cp.z >= 0) {
+            const b3gChildShape ch = a.children[cp.z];
+            colA = ch.shapeIndex;
+            child_pose(BA, ch, posA, qA);
+        }
+        if (cp.w >= 0) {
+            const b3gChildShape ch = a.children[cp.w];
+            colB = ch.shapeIndex;
+            child_pose(BB, ch, posB, qB);
+        }
+        const b3gCollidable cA = a.cols[colA], cB = a.cols[colB];
+        if (cA.shapeType != B3G_SHAPE_CONVEX_HULL || cB.shapeType != B3G_SHAPE_CONVEX_HULL) continue;
+        const b3gHull hA = a.hulls[cA.shapeIndex], hB = a.hulls[cB.shapeIndex];
+        const v3 deltaC2 =
+            (mmul(qmat(qA), f4v3(hA.localCenter)) + posA) - (mmul(qmat(qB), f4v3(hB.localCenter)) + posB);
+        const int nfaces = hA.numFaces + hB.numFaces;
+        const int naxes = nfaces + hA.numUniqueEdges * hB.numUniqueEdges;
+        const uint32_t dupA = __ldg(&a.face_dup[cA.shapeIndex]);
+        const uint32_t dupB = __ldg(&a.face_dup[cB.shapeIndex]);
+        const b3gFloat4* vA = &a.verts[hA.vertexOffset];
+        const b3gFloat4* vB = &a.verts[hB.vertexOffset];
+        AxisBest best{FLT_MAX, 0x7fffffff};  // edge axes only
+        bool separated = false;
+        for (int k0 = 0; k0 < naxes; k0 += 32) {
+            const int k = k0 + lane;
+            v3 axis;
+            if (k < naxes && !(k < nfaces && dup_face_axis(k, hA.numFaces, dupA, dupB)) &&
+                sat_axis(k, hA, hB, a.faces, a.edges, qA, qB, deltaC2, axis)) {
+                float min0, max0, min1, max1;
+                project(vA, hA.numVertices, posA, qA, axis, min0, max0);
+                project(vB, hB.numVertices, posB, qB, axis, min1, max1);
+                if (max0 < min1 || max1 < min0) {
+                    separated = true;
+                } else if (k >= nfaces) {
+                    const float d0 = max0 - min1, d1 = max1 - min0;
+                    const float dist = d0 < d1 ? d0 : d1;
+                    if (dist < best.d || (dist == best.d && k < best.idx)) {
+                        best.d = dist;
+                        best.idx = k;
+                    }
+                }
+            }
+            if (__any_sync(0xffffffffu, separated)) break;
+        }
+        if (__any_sync(0xffffffffu, separated)) continue;
+        best = warp_argmin(best);
+        v3 sep;
+        if (best.idx != 0x7fffffff) {
+            sat_axis(best.idx, hA, hB, a.faces, a.edges, qA, qB, deltaC2, sep);
+        } else if (!find_sep_full(a, hB, hA, posB, qB, posA, qA, sep)) {
+            continue;
+        }
+        if (dot3(-deltaC2, sep) > 0.0f) sep = -sep;  // findSeparatingAxisEdgeEdge's last step
+
+        // clipHullAgainstHull (b3ConvexHullContact.cpp:939-1044): incident face of B (first max of
+        // dot(world normal, sep)), reference face of A (first min)
+        AxisBest fb{-FLT_MAX, 0x7fffffff};
+        for (int f = lane; f < hB.numFaces; f += 32) {
+            const float d = dot3(qrotq(qB, ld3(&a.faces[hB.faceOffset + f].plane)), sep);
+            if (d > fb.d || (d == fb.d && fb.idx != 0x7fffffff && f < fb.idx)) { fb.d = d; fb.idx = f; }
+        }
+        fb = warp_argmax(fb);
+        AxisBest fa{FLT_MAX, 0x7fffffff};
+        for (int f = lane; f < hA.numFaces; f += 32) {
+            const float d = dot3(qrotq(qA, ld3(&a.faces[hA.faceOffset + f].plane)), sep);
+            if (d < fa.d || (d == fa.d && fa.idx != 0x7fffffff && f < fa.idx)) { fa.d = d; fa.idx = f; }
+        }
+        fa = warp_argmin(fa);
+        if (fb.idx == 0x7fffffff || fa.idx == 0x7fffffff) continue;
+
+        if (lane == 0) {
+            float4* pin = s_poly[wib][0];
+            float4* pout = s_poly[wib][1];
+            const m33 RA = qmat(qA), RB = qmat(qB);
+            const b3gFace polyB = a.faces[hB.faceOffset + fb.idx];
+            int nin = 0;
+            for (int e = 0; e < polyB.numIndices && e < CLIP_CAP; e++) {
+                const v3 w = mmul(RB, ld3(&vB[a.indices[polyB.indexOffset + e]])) + posB;
+                pin[nin++] = make_float4(w.x, w.y, w.z, 0.f);
+            }
+            const b3gFace polyA = a.faces[hA.faceOffset + fa.idx];
+            const v3 planeNormalA = mk3(polyA.plane.x, polyA.plane.y, polyA.plane.z);
+            const int nva = polyA.numIndices;
+            for (int e0 = 0; e0 < nva; e0++) {
+                const v3 va = ld3(&vA[a.indices[polyA.indexOffset + e0]]);
+                const v3 vb = ld3(&vA[a.indices[polyA.indexOffset + ((e0 + 1) % nva)]]);
+                const v3 worldEdge0 = qrotq(qA, va - vb);
+                const v3 worldPlaneAnormal1 = qrotq(qA, planeNormalA);
+                const v3 planeNormalWS1 = -cross3(worldEdge0, worldPlaneAnormal1);
+                const v3 worldA1 = mmul(RA, va) + posA;
+                const float planeEqWS1 = -dot3(worldA1, planeNormalWS1);
+                const int nout = clip_face(pin, nin, planeNormalWS1, planeEqWS1, pout, a.status);
+                float4* t = pout;
+                pout = pin;
+                pin = t;
+                nin = nout;
+            }
+            const v3 planeNormalWS = qrotq(qA, planeNormalA);
+            const float planeEqWS = polyA.plane.w - dot3(planeNormalWS, posA);
+            int np = 0;
+            for (int i = 0; i < nin; i++) {
+                float depth = dot3(planeNormalWS, mk3(pin[i].x, pin[i].y, pin[i].z)) + planeEqWS;
+                if (depth <= -1e30f) depth = -1e30f;
+                if (np < CLIP_CAP && depth <= 0.0f) pout[np++] = make_float4(pin[i].x, pin[i].y, pin[i].z, depth);
+            }
+            if (np > 0) {
+                int idx[4];
+                const int nred = reduce_contacts(pout, np, -sep, idx);
+                const int slot = P + j;
+                b3gContact4& c = a.slots[slot];
+                write_header(c, a, cp.x, cp.y, sep, nred);
+                c.frictionCmp = fr07;
+                c.batchIdx = j;
+                c.childIndexA = cp.z;
+                c.childIndexB = cp.w;
+                for (int i = 0; i < nred; i++) {
+                    const float4 q = pout[idx[i]];
+                    c.worldPosB[i] = b3gFloat4{q.x, q.y, q.z, q.w};
+                }
+                a.flags[slot] = 1;
+            }
+        }
+        __syncwarp();
     }
 }
 
@@ -1092,7 +1140,8 @@ int launch_contacts(DeviceState& d, float friction, cudaStream_t s) {
     int launches = 0;
     if (d.num_children > 0) {
         // compound pairs: child-pair counts, their scan (total in pad[4]), the clamped count and the
-        // slot count (pairs + child pairs, pad[5]), the child pairs, their manifolds
+        // slot count (pairs + child pairs, pad[5]), the child pairs, their manifolds (the flags
+        // cleared and plane-child pairs, then hull-hull child pairs a warp each)
         int* d_J = &d.counters->pad[4];
         d_slots = &d.counters->pad[5];
         k_compound_count<<<grid, NP_THREADS, 0, s>>>(a, d_np, d.child_count);
@@ -1100,7 +1149,8 @@ int launch_contacts(DeviceState& d, float friction, cudaStream_t s) {
         k_compound_total<<<1, 1, 0, s>>>(d_np, d_J, d_slots, d.max_child_pairs, &d.counters->status);
         k_compound_expand<<<grid, NP_THREADS, 0, s>>>(a, d_np, d.child_offset, d.child_pairs, d.max_child_pairs);
         k_compound_contacts<<<grid, NP_THREADS, 0, s>>>(a, d_np, d_J, d.child_pairs);
-        launches += 4;
+        k_compound_hull_hull<<<d.num_sms * 16, CH_WARPS * 32, 0, s>>>(a, d_np, d_J, d.child_pairs);
+        launches += 5;
     }
     exclusive_scan_i32(d.prim, d.contact_flag, d.contact_index, d_slots, &d.counters->num_contacts, d.scan_scratch,
                        s, &ll);

@@ -1558,6 +1558,7 @@ extern "C" b3gStatus b3g_get_stats(b3g_handle h, b3gStepStats* out) {
     out->residual = c.residual;
     out->status = c.status;
     out->num_large = h->d.num_large + h->d.num_sap;
+    out->num_child_pairs = h->d.num_children > 0 ? c.pad[4] : 0;
     return B3G_OK;
 }
 

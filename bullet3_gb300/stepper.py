@@ -3,7 +3,7 @@
 Meant for running the pipeline under an external profiler (ncu) or by hand: nothing but the
 scene upload, the warm-up steps and the measured steps touch the GPU.
 
-    python -m bullet3_gb300.stepper [--workload pile|lattice|batched|mixed|stress|chains] [--settle S]
+    python -m bullet3_gb300.stepper [--workload pile|lattice|batched|mixed|stress|chains|compound] [--settle S]
                                     [--steps K] [--warmup W] [--solver pgs|jacobi] [--iterations I]
                                     [--autotune] [--broadphase grid|lbvh] [--stage-times] [--profile-range]
 
@@ -17,6 +17,8 @@ with profiling off (ncu --profile-from-start off --clock-control none); --settle
   stress   1,048,576 bodies of the same mix poured into a 5-plane container from heights U[0, 512]
   chains   8,192 chains of 32 spheres (262,144 bodies and ball joints, every 8th joint fixed)
            hanging from one static box in a 3 m grid, swinging
+  compound 131,072 bodies (2,048 x nx) on a plane: compounds of convex hulls (an L of two boxes, a
+           dumbbell of two hulls and a box) among single boxes and hulls, dropped as a lattice from rest
 """
 from __future__ import annotations
 
@@ -42,12 +44,14 @@ def make(workload: str, n: int = 64):
     if workload == "chains":
         return scenes.hanging_chains(8192, 32, seed=0, fixed_every=8, anchor_index=-1, random_orn=False,
                                      per_row=91)
+    if workload == "compound":
+        return scenes.compound_scene(2048 * n, seed=0, lattice=True)
     raise ValueError(workload)
 
 
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("--workload", choices=["pile", "lattice", "batched", "mixed", "stress", "chains"],
+    p.add_argument("--workload", choices=["pile", "lattice", "batched", "mixed", "stress", "chains", "compound"],
                    default="pile")
     p.add_argument("--settle", type=int, default=0)
     p.add_argument("--profile-range", action="store_true")
@@ -150,6 +154,7 @@ def main(argv=None):
                       "joints": pl.getNumConstraints(), "stage_ms": stage_ms,
                       "host_ms_per_step": 1000 * secs / max(a.steps, 1), "pairs": st.num_pairs,
                       "manifolds": st.num_contacts, "points": st.num_points, "colors": st.num_colors,
+                      "child_pairs": st.num_child_pairs,
                       "status": int(pl.status()), "tuning": tuning}))
     return 0 if pl.status() == 0 else 1
 

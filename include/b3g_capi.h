@@ -137,6 +137,7 @@ typedef struct b3gStepStats {
     float residual;         /* last relative impulse residual (0 if not tracked) */
     unsigned int status;    /* B3G_FLAG_* bits */
     int num_large;          /* bodies handled by the large-AABB path */
+    int num_child_pairs;    /* compound child pairs of the last contact stage (after the capacity clamp) */
 } b3gStepStats;
 
 /* ------------------------------------------------------------------ lifetime */
