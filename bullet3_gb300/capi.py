@@ -27,6 +27,10 @@ PAIR = np.dtype([("x", "<i4"), ("y", "<i4"), ("z", "<i4"), ("w", "<i4")])
 # b3GpuChildShape: a compound's child (its convex hull collidable at a pose in the compound's frame)
 CHILD = np.dtype([("childPosition", "<f4", 4), ("childOrientation", "<f4", 4), ("shapeIndex", "<i4"),
                   ("numChildShapes", "<i4"), ("collidableShapeIndex", "<i4"), ("shapeType", "<i4")])
+# a concave mesh's quantized triangle BVH (b3gBvhInfo / b3gBvhNode)
+BVHINFO = np.dtype([("aabbMin", "<f4", 4), ("aabbMax", "<f4", 4), ("quantization", "<f4", 4), ("numNodes", "<i4"),
+                    ("nodeOffset", "<i4"), ("numTriangles", "<i4"), ("pad", "<i4")])
+BVHNODE = np.dtype([("qmin", "<u2", 3), ("qmax", "<u2", 3), ("escapeOrTriangle", "<i4")])
 RAY = np.dtype([("from", "<f4", 4), ("to", "<f4", 4)])
 RAYHIT = np.dtype([("hitFraction", "<f4"), ("hitBody", "<i4"), ("hitResult1", "<i4"), ("hitResult2", "<i4"),
                    ("hitPoint", "<f4", 4), ("hitNormal", "<f4", 4)])
@@ -34,10 +38,10 @@ JOINT = np.dtype([("type", "<i4"), ("rbA", "<i4"), ("rbB", "<i4"), ("breakingImp
                   ("pivotInA", "<f4", 4), ("pivotInB", "<f4", 4), ("relTargetAB", "<f4", 4), ("flags", "<i4"),
                   ("uid", "<i4"), ("pad", "<i4", 2)])
 for _dt, _sz in ((BODY, 80), (INERTIA, 96), (COLLIDABLE, 16), (HULL, 96), (FACE, 32), (AABB, 32), (CONTACT, 112),
-                 (PAIR, 16), (RAY, 32), (RAYHIT, 48), (JOINT, 80)):
+                 (PAIR, 16), (RAY, 32), (RAYHIT, 48), (JOINT, 80), (BVHINFO, 64), (BVHNODE, 16)):
     assert _dt.itemsize == _sz, (_dt, _sz)
 
-SHAPE_CONVEX_HULL, SHAPE_PLANE, SHAPE_COMPOUND, SHAPE_SPHERE = 3, 4, 6, 7
+SHAPE_CONVEX_HULL, SHAPE_PLANE, SHAPE_CONCAVE_TRIMESH, SHAPE_COMPOUND, SHAPE_SPHERE = 3, 4, 5, 6, 7
 SOLVER_PGS, SOLVER_JACOBI = 0, 1
 JOINT_POINT2POINT, JOINT_FIXED = 3, 4
 BROADPHASE_GRID, BROADPHASE_LBVH, BROADPHASE_AUTO = 0, 1, 2
@@ -69,7 +73,7 @@ class b3gConfig(C.Structure):
                 ("solver_blocks_per_sm", C.c_int), ("pgs_partitions", C.c_int), ("pgs_interleave", C.c_int),
                 ("warm_start_max_points", C.c_int), ("autotune", C.c_int), ("broadphase", C.c_int),
                 ("pgs_tail_manifolds", C.c_int), ("pgs_flow", C.c_int),
-                ("max_compound_child_pairs", C.c_int), ("reserved", C.c_int * 2)]
+                ("max_compound_child_pairs", C.c_int), ("max_concave_pairs", C.c_int), ("reserved", C.c_int * 1)]
 
 
 class b3gTuning(C.Structure):
@@ -81,7 +85,8 @@ class b3gTuning(C.Structure):
 class b3gStepStats(C.Structure):
     _fields_ = [("num_pairs", C.c_int), ("num_contacts", C.c_int), ("num_points", C.c_int),
                 ("num_colors", C.c_int), ("iterations", C.c_int), ("residual", C.c_float),
-                ("status", C.c_uint), ("num_large", C.c_int), ("num_child_pairs", C.c_int)]
+                ("status", C.c_uint), ("num_large", C.c_int), ("num_child_pairs", C.c_int),
+                ("num_concave_pairs", C.c_int)]
 
 
 class B3GError(RuntimeError):
@@ -104,7 +109,7 @@ EXPORTS = [
     "b3g_get_inertia_buffer", "b3g_get_aabb_buffer", "b3g_get_pair_buffer", "b3g_get_contact_buffer",
     "b3g_get_stream", "b3g_read_bodies", "b3g_write_bodies", "b3g_read_inertias", "b3g_read_aabbs",
     "b3g_write_aabbs", "b3g_read_pairs", "b3g_read_contacts", "b3g_write_contacts", "b3g_read_batches", "b3g_read_solve_order",
-    "b3g_register_compound", "b3g_read_child_shapes",
+    "b3g_register_compound", "b3g_read_child_shapes", "b3g_register_concave_mesh", "b3g_read_mesh_bvh",
     "b3g_read_impulses", "b3g_get_num_collidables", "b3g_read_registered_bodies", "b3g_read_shape_tables",
     "b3g_set_profiling",
     "b3g_get_stage_times", "b3g_get_launch_count", "b3g_record_event", "b3g_event_elapsed", "b3g_hull_compute",

@@ -48,6 +48,10 @@ struct NPArgs {
     // compounds
     const b3gChildShape* children;
     const b3gAabb* local_aabbs;
+    // concave meshes
+    const b3gAabb* aabbs;  // world AABBs by body
+    const b3gBvhInfo* bvh_infos;
+    const b3gBvhNode* bvh_nodes;
 };
 
 __device__ __forceinline__ v3 ld3(const b3gFloat4* p) {
@@ -823,14 +827,17 @@ __global__ void k_compound_count(NPArgs a, const int* __restrict__ d_np, int* __
         counts[p] = compound_child_pairs(a, p, nullptr, 0);
 }
 
-// the child-pair count clamped to capacity (pad[4]) and the slot count (pairs + child pairs, pad[5])
-__global__ void k_compound_total(const int* __restrict__ d_np, int* __restrict__ d_total, int* __restrict__ d_slots,
-                                 int cap, unsigned int* __restrict__ status) {
+// an expansion's total clamped to its capacity (the overflow flag beyond it)
+__global__ void k_clamp_total(int* __restrict__ d_total, int cap, unsigned int* __restrict__ status) {
     const int total = *d_total;
-    const int J = total < cap ? total : cap;
     if (total > cap) atomicOr(status, B3G_FLAG_CONTACT_OVERFLOW);
-    *d_total = J;
-    *d_slots = *d_np + J;
+    *d_total = total < cap ? total : cap;
+}
+
+// manifold slots: the pairs', the compound child pairs', the concave triangle-convex pairs'
+__global__ void k_slot_total(const int* __restrict__ d_np, const int* __restrict__ d_J, const int* __restrict__ d_K,
+                             int* __restrict__ d_slots) {
+    *d_slots = *d_np + (d_J ? *d_J : 0) + (d_K ? *d_K : 0);
 }
 
 __global__ void k_compound_expand(NPArgs a, const int* __restrict__ d_np, const int* __restrict__ offsets,
@@ -1100,6 +1107,353 @@ __global__ void __launch_bounds__(CH_WARPS * 32) k_compound_hull_hull(NPArgs a, 
     }
 }
 
+// ------------------------------------------------------------------ concave meshes
+// A pair whose first body is a concave mesh and whose second is a hull or a compound expands into
+// triangle-convex pairs (b3BvhTraversal, shared/b3BvhTraversal.h:11-111): the triangles whose
+// quantized leaf box overlaps the other body's world AABB quantized into the mesh's BVH bounds
+// (as the reference does, in the mesh's own frame: meshes stay at the identity pose), with every
+// child of a compound; in (pair, triangle, child) order, the BVH's depth-first order being the
+// triangle order.  Static-static pairs are skipped.
+
+// b3QuantizeWithClamp (shared/b3QuantizedBvhNodeData.h:42-60)
+__device__ __forceinline__ void quantize_clamp(unsigned short out[3], const float p[3], bool isMax,
+                                               const b3gBvhInfo& bi) {
+    const float mn[3] = {bi.aabbMin.x, bi.aabbMin.y, bi.aabbMin.z};
+    const float mx[3] = {bi.aabbMax.x, bi.aabbMax.y, bi.aabbMax.z};
+    const float q[3] = {bi.quantization.x, bi.quantization.y, bi.quantization.z};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        float c = p[k];
+        if (c < mn[k]) c = mn[k];
+        if (mx[k] < c) c = mx[k];
+        const float v = (c - mn[k]) * q[k];
+        out[k] = isMax ? (unsigned short)(((unsigned short)(v + 1.f)) | 1) : (unsigned short)(((unsigned short)v) & 0xfffe);
+    }
+}
+
+// the triangle-convex pairs of pair p: counted (out == nullptr), or written at out[0..cap)
+__device__ int concave_tri_pairs(const NPArgs& a, int p, int4* out, int cap) {
+    const b3gPair pr = a.pairs[p];
+    const int A = pr.x, B = pr.y;
+    const b3gBody& BA = a.bodies[A];
+    const b3gBody& BB = a.bodies[B];
+    if (BA.invMass == 0.f && BB.invMass == 0.f) return 0;
+    const b3gCollidable cA = a.cols[BA.collidableIdx];
+    if (cA.shapeType != B3G_SHAPE_CONCAVE_TRIMESH) return 0;
+    const b3gCollidable cB = a.cols[BB.collidableIdx];
+    // (spheres against meshes take the reference's findConcaveSphereContactsKernel: not built)
+    if (cB.shapeType != B3G_SHAPE_CONVEX_HULL && cB.shapeType != B3G_SHAPE_COMPOUND) return 0;
+    const bool comp = cB.shapeType == B3G_SHAPE_COMPOUND;
+    const int nch = comp ? cB.numChildShapes : 1;
+    const b3gBvhInfo bi = a.bvh_infos[cA.numChildShapes];
+    const b3gAabb box = a.aabbs[B];
+    unsigned short qmn[3], qmx[3];
+    quantize_clamp(qmn, box.minv, false, bi);
+    quantize_clamp(qmx, box.maxv, true, bi);
+    const int4* nodes = reinterpret_cast<const int4*>(a.bvh_nodes + bi.nodeOffset);
+    int n = 0, cur = 0;
+    while (cur < bi.numNodes) {
+        const int4 raw = __ldg(&nodes[cur]);
+        const unsigned short nmn0 = (unsigned short)(raw.x & 0xffff), nmn1 = (unsigned short)((unsigned)raw.x >> 16);
+        const unsigned short nmn2 = (unsigned short)(raw.y & 0xffff), nmx0 = (unsigned short)((unsigned)raw.y >> 16);
+        const unsigned short nmx1 = (unsigned short)(raw.z & 0xffff), nmx2 = (unsigned short)((unsigned)raw.z >> 16);
+        const int e = raw.w;
+        // b3TestQuantizedAabbAgainstQuantizedAabbSlow (shared/b3QuantizedBvhNodeData.h:62-85)
+        const bool ov = !(qmn[0] > nmx0 || qmx[0] < nmn0 || qmn[1] > nmx1 || qmx[1] < nmn1 || qmn[2] > nmx2 ||
+                          qmx[2] < nmn2);
+        const bool leaf = e >= 0;
+        if (ov && leaf) {
+            for (int c = 0; c < nch; c++) {
+                if (out && n < cap) out[n] = make_int4(A, B, e, comp ? cB.shapeIndex + c : 0);
+                n++;
+            }
+        }
+        cur += (ov || leaf) ? 1 : -e;
+    }
+    return n;
+}
+
+__global__ void k_concave_count(NPArgs a, const int* __restrict__ d_np, int* __restrict__ counts) {
+    const int np = *d_np;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x)
+        counts[p] = concave_tri_pairs(a, p, nullptr, 0);
+}
+
+__global__ void k_concave_expand(NPArgs a, const int* __restrict__ d_np, const int* __restrict__ offsets,
+                                 int4* __restrict__ tri_pairs, int cap) {
+    const int np = *d_np;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+        const int o = offsets[p];
+        if (o < cap) concave_tri_pairs(a, p, tri_pairs + o, cap - o);
+    }
+}
+
+// clipFaceGlobal (shared/b3ClipFaces.h:20-61): as clip_face, but a polygon of one vertex is
+// clipped too (the reference has no lower bound on the input)
+__device__ int clip_face_global(const float4* in, int nin, v3 n, float eq, float4* out, unsigned int* status) {
+    if (nin < 1) return 0;
+    int nout = 0;
+    float4 first = in[nin - 1];
+    float ds = dot3(n, mk3(first.x, first.y, first.z)) + eq;
+    for (int ve = 0; ve < nin; ve++) {
+        const float4 end = in[ve];
+        const float de = dot3(n, mk3(end.x, end.y, end.z)) + eq;
+        if (ds < 0.f) {
+            if (de < 0.f) {
+                if (nout < CLIP_CAP) out[nout++] = end; else atomicOr(status, B3G_FLAG_CLIP_OVERFLOW);
+            } else {
+                const float t = ds * 1.f / (ds - de);
+                const float4 l = make_float4(first.x + (end.x - first.x) * t, first.y + (end.y - first.y) * t,
+                                             first.z + (end.z - first.z) * t, 0.f);
+                if (nout < CLIP_CAP) out[nout++] = l; else atomicOr(status, B3G_FLAG_CLIP_OVERFLOW);
+            }
+        } else if (de < 0.f) {
+            const float t = ds * 1.f / (ds - de);
+            const float4 l = make_float4(first.x + (end.x - first.x) * t, first.y + (end.y - first.y) * t,
+                                         first.z + (end.z - first.z) * t, 0.f);
+            if (nout < CLIP_CAP) out[nout++] = l; else atomicOr(status, B3G_FLAG_CLIP_OVERFLOW);
+            if (nout < CLIP_CAP) out[nout++] = end; else atomicOr(status, B3G_FLAG_CLIP_OVERFLOW);
+        }
+        first = end;
+        ds = de;
+    }
+    return nout;
+}
+
+// A triangle as the reference's five-face prism (b3FindConcaveSeparatingAxisKernel,
+// shared/b3FindConcaveSatAxis.h:506-797): its 3 vertices; faces 0 front (the mesh face's plane), 1
+// back (negated), 2..4 the edge planes normalize(n x (v[prev] - v[i])); unique edges v1 - v0,
+// v2 - v1, v0 - v2; local centre (v0 + v1 + v2) / 3.
+struct TriPrism {
+    v3 v[3];
+    v3 n[5];
+    v3 e[3];
+    v3 center;
+};
+
+__device__ __forceinline__ void tri_prism(const NPArgs& a, const b3gHull& mesh, int t, TriPrism& P) {
+    const b3gFace face = a.faces[mesh.faceOffset + t];
+    v3 lc = mk3(0.f, 0.f, 0.f);
+    for (int i = 0; i < 3; i++) {
+        P.v[i] = ld3(&a.verts[mesh.vertexOffset + a.indices[face.indexOffset + i]]);
+        lc = lc + P.v[i];
+    }
+    const v3 normal = mk3(face.plane.x, face.plane.y, face.plane.z);
+    P.n[0] = normal;
+    P.n[1] = -normal;
+    int prev = 2;
+    for (int i = 0; i < 3; i++) {
+        P.n[2 + i] = normalize3(cross3(normal, P.v[prev] - P.v[i]));
+        prev = i;
+    }
+    P.e[0] = P.v[1] - P.v[0];
+    P.e[1] = P.v[2] - P.v[1];
+    P.e[2] = P.v[0] - P.v[2];
+    P.center = lc * (1.f / 3.f);
+}
+
+// b3Project over the prism's 3 vertices
+__device__ __forceinline__ void project_tri(const TriPrism& P, v3 pos, quat orn, v3 dir, float& mn, float& mx) {
+    const v3 localDir = qrotq(qconj(orn), dir);
+    const float offset = dot3(pos, dir);
+    mn = FLT_MAX;
+    mx = -FLT_MAX;
+    for (int i = 0; i < 3; i++) {
+        const float dp = dot3(P.v[i], localDir);
+        if (dp < mn) mn = dp;
+        if (dp > mx) mx = dp;
+    }
+    if (mn > mx) {
+        const float t = mn; mn = mx; mx = t;
+    }
+    mn = mn + offset;
+    mx = mx + offset;
+}
+
+// SAT axis k of a triangle-convex pair, in the reference's order: the prism's 5 faces, the hull's
+// faces, then the edge pairs (prism edge major); false when the edge cross product is almost zero
+__device__ __forceinline__ bool concave_axis(int k, const TriPrism& P, const b3gHull& hB, const NPArgs& a, quat qA,
+                                             quat qB, v3 D, v3& axis) {
+    if (k < 5) {
+        axis = qrotq(qA, P.n[k]);
+    } else if (k < 5 + hB.numFaces) {
+        axis = qrotq(qB, ld3(&a.faces[hB.faceOffset + (k - 5)].plane));
+    } else {
+        const int e = k - 5 - hB.numFaces;
+        const int e0 = e / hB.numUniqueEdges, e1 = e - e0 * hB.numUniqueEdges;
+        const v3 w0 = qrotq(qA, P.e[e0]);
+        const v3 w1 = qrotq(qB, ld3(&a.edges[hB.uniqueEdgesOffset + e1]));
+        const v3 c = cross3(w0, w1);
+        if (!((double)fabsf(c.x) > 1e-6 || (double)fabsf(c.y) > 1e-6 || (double)fabsf(c.z) > 1e-6)) return false;
+        axis = normalize3(c);
+    }
+    if (dot3(D, axis) < 0.f) axis = -axis;
+    return true;
+}
+
+// One warp per triangle-convex pair (slot = pairs + compound child pairs + its index):
+// b3FindConcaveSeparatingAxisKernel, then b3FindClippingFaces (shared/b3FindConcaveSatAxis.h:421-504),
+// clipFacesAndFindContactsKernel (shared/b3ClipFaces.h:67-177) and b3NewContactReductionKernel
+// (shared/b3NewContactReduction.h:88-177).  The reference's three passes (the prism's faces, the
+// hull's faces, the edge pairs) share one running minimum and orient every axis towards the
+// triangle, so the normal is the first minimum over the whole sequence; every pass returns at a
+// separating axis.  Clipped with minDist -1e30 and maxDist 0.02, reduced against -sep, friction
+// 0.7, no child indices (the reference stores -1 for both).
+static constexpr int CC_WARPS = 4;
+
+__global__ void __launch_bounds__(CC_WARPS * 32) k_concave_contacts(NPArgs a, const int* __restrict__ d_np,
+                                                                   const int* __restrict__ d_J,
+                                                                   const int* __restrict__ d_K,
+                                                                   const int4* __restrict__ tri_pairs) {
+    __shared__ float4 s_poly[CC_WARPS][2][CLIP_CAP];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int base = *d_np + (d_J ? *d_J : 0), K = *d_K;
+    const unsigned short fr07 = (unsigned short)(0.7f * 0xffff);
+    for (int k = blockIdx.x * CC_WARPS + wib; k < K; k += gridDim.x * CC_WARPS) {
+        const int slot = base + k;
+        if (lane == 0) a.flags[slot] = 0;
+        const int4 cp = tri_pairs[k];
+        const b3gBody& BA = a.bodies[cp.x];
+        const b3gBody& BB = a.bodies[cp.y];
+        const b3gHull mesh = a.hulls[a.cols[BA.collidableIdx].shapeIndex];
+        TriPrism P;
+        tri_prism(a, mesh, cp.z, P);
+        // the triangle's local AABB against the other body's world AABB
+        {
+            const b3gAabb box = a.aabbs[cp.y];
+            float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+            for (int i = 0; i < 3; i++) {
+                const float c[3] = {P.v[i].x, P.v[i].y, P.v[i].z};
+                for (int q = 0; q < 3; q++) {
+                    if (c[q] < lo[q]) lo[q] = c[q];
+                    if (hi[q] < c[q]) hi[q] = c[q];
+                }
+            }
+            bool ov = true;
+            for (int q = 0; q < 3; q++)
+                if (lo[q] > box.maxv[q] || hi[q] < box.minv[q]) ov = false;
+            if (!ov) continue;
+        }
+        const v3 posA = f4v3(BA.pos);
+        const quat qA = f4q(BA.quat);
+        v3 posB = f4v3(BB.pos);
+        quat qB = f4q(BB.quat);
+        // b3TransformPoint of the host code is b3Transform's (the quaternion's rotation matrix): for
+        // the child pose, the centres and the clipping faces' vertices
+        int colB = BB.collidableIdx;
+        if (a.cols[colB].shapeType == B3G_SHAPE_COMPOUND) {
+            const b3gChildShape ch = a.children[cp.w];
+            colB = ch.shapeIndex;
+            posB = mmul(qmat(qB), f4v3(ch.childPosition)) + posB;
+            qB = qmul(qB, f4q(ch.childOrientation));
+        }
+        const b3gHull hB = a.hulls[a.cols[colB].shapeIndex];
+        const m33 RA = qmat(qA), RB = qmat(qB);
+        const v3 c0 = mmul(RA, P.center) + posA;
+        const v3 c1 = mmul(RB, f4v3(hB.localCenter)) + posB;
+        const v3 D = c0 - c1;
+        const b3gFloat4* vB = &a.verts[hB.vertexOffset];
+        const int naxes = 5 + hB.numFaces + 3 * hB.numUniqueEdges;
+        AxisBest best{FLT_MAX, 0x7fffffff};
+        bool separated = false;
+        for (int k0 = 0; k0 < naxes; k0 += 32) {
+            const int ax = k0 + lane;
+            v3 axis;
+            if (ax < naxes && concave_axis(ax, P, hB, a, qA, qB, D, axis)) {
+                float min0, max0, min1, max1;
+                project_tri(P, posA, qA, axis, min0, max0);
+                project(vB, hB.numVertices, posB, qB, axis, min1, max1);
+                if (max0 < min1 || max1 < min0) {
+                    separated = true;
+                } else {
+                    const float d0 = max0 - min1, d1 = max1 - min0;
+                    const float d = d0 < d1 ? d0 : d1;
+                    if (d < best.d || (d == best.d && ax < best.idx)) {
+                        best.d = d;
+                        best.idx = ax;
+                    }
+                }
+            }
+            if (__any_sync(0xffffffffu, separated)) break;
+        }
+        if (__any_sync(0xffffffffu, separated)) continue;
+        best = warp_argmin(best);
+        if (best.idx == 0x7fffffff) continue;
+        v3 sep;
+        concave_axis(best.idx, P, hB, a, qA, qB, D, sep);
+
+        // b3FindClippingFaces: the hull's face most along sep (first max), the prism's face most
+        // against it (first min)
+        AxisBest fb{-FLT_MAX, 0x7fffffff};
+        for (int f = lane; f < hB.numFaces; f += 32) {
+            const float d = dot3(qrotq(qB, ld3(&a.faces[hB.faceOffset + f].plane)), sep);
+            if (d > fb.d || (d == fb.d && fb.idx != 0x7fffffff && f < fb.idx)) { fb.d = d; fb.idx = f; }
+        }
+        fb = warp_argmax(fb);
+        if (fb.idx == 0x7fffffff) continue;
+
+        if (lane == 0) {
+            int fa = -1;
+            float dmn = FLT_MAX;
+            v3 nA = mk3(0.f, 0.f, 0.f);
+            for (int f = 0; f < 5; f++) {
+                const v3 wn = qrotq(qA, P.n[f]);
+                const float d = dot3(wn, sep);
+                if (d < dmn) { dmn = d; fa = f; nA = wn; }
+            }
+            if (fa >= 0) {
+                // the prism face's vertices: front 0 1 2, back 2 1 0, edge plane 2 + i: i, prev(i)
+                int ia[3], na;
+                if (fa == 0) { ia[0] = 0; ia[1] = 1; ia[2] = 2; na = 3; }
+                else if (fa == 1) { ia[0] = 2; ia[1] = 1; ia[2] = 0; na = 3; }
+                else { const int i = fa - 2; ia[0] = i; ia[1] = i == 0 ? 2 : i - 1; na = 2; }
+                v3 wA[3];
+                for (int i = 0; i < na; i++) wA[i] = mmul(RA, P.v[ia[i]]) + posA;
+                float4* pin = s_poly[wib][0];
+                float4* pout = s_poly[wib][1];
+                const b3gFace polyB = a.faces[hB.faceOffset + fb.idx];
+                int nin = 0;
+                for (int e = 0; e < polyB.numIndices && e < CLIP_CAP; e++) {
+                    const v3 w = mmul(RB, ld3(&vB[a.indices[polyB.indexOffset + e]])) + posB;
+                    pin[nin++] = make_float4(w.x, w.y, w.z, 0.f);
+                }
+                for (int e0 = 0; e0 < na; e0++) {
+                    const v3 aw = wA[e0], bw = wA[(e0 + 1) % na];
+                    const v3 pn = -cross3(aw - bw, nA);
+                    const float eq = -dot3(aw, pn);
+                    const int nout = clip_face_global(pin, nin, pn, eq, pout, a.status);
+                    float4* t = pout;
+                    pout = pin;
+                    pin = t;
+                    nin = nout;
+                }
+                const float eqA = -dot3(nA, wA[0]);
+                int np = 0;
+                for (int i = 0; i < nin; i++) {
+                    float depth = dot3(nA, mk3(pin[i].x, pin[i].y, pin[i].z)) + eqA;
+                    if (depth <= -1e30f) depth = -1e30f;
+                    if (depth <= 0.02f) pout[np++] = make_float4(pin[i].x, pin[i].y, pin[i].z, depth);
+                }
+                if (np > 0) {
+                    int idx[4];
+                    const int nred = reduce_contacts(pout, np, -sep, idx);
+                    b3gContact4& c = a.slots[slot];
+                    write_header(c, a, cp.x, cp.y, sep, nred);
+                    c.frictionCmp = fr07;
+                    c.batchIdx = k;
+                    for (int i = 0; i < nred; i++) {
+                        const float4 q = pout[idx[i]];
+                        c.worldPosB[i] = b3gFloat4{q.x, q.y, q.z, q.w};
+                    }
+                    a.flags[slot] = 1;
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
 static NPArgs make_args(DeviceState& d, unsigned short friction_cmp) {
     NPArgs a;
     a.bodies = d.bodies;
@@ -1119,6 +1473,9 @@ static NPArgs make_args(DeviceState& d, unsigned short friction_cmp) {
     a.friction_cmp = friction_cmp;
     a.children = d.children;
     a.local_aabbs = d.local_aabbs;
+    a.aabbs = d.aabbs;
+    a.bvh_infos = d.bvh_infos;
+    a.bvh_nodes = d.bvh_nodes;
     return a;
 }
 
@@ -1138,19 +1495,36 @@ int launch_contacts(DeviceState& d, float friction, cudaStream_t s) {
     int* d_np = &d.counters->pad[0];
     int* d_slots = d_np;
     int launches = 0;
+    int* d_J = nullptr;
     if (d.num_children > 0) {
-        // compound pairs: child-pair counts, their scan (total in pad[4]), the clamped count and the
-        // slot count (pairs + child pairs, pad[5]), the child pairs, their manifolds (the flags
-        // cleared and plane-child pairs, then hull-hull child pairs a warp each)
-        int* d_J = &d.counters->pad[4];
-        d_slots = &d.counters->pad[5];
+        // compound pairs: child-pair counts, their scan (total in pad[4]) clamped to capacity, the
+        // child pairs, their manifolds (the flags cleared and plane-child pairs, then hull-hull
+        // child pairs a warp each)
+        d_J = &d.counters->pad[4];
         k_compound_count<<<grid, NP_THREADS, 0, s>>>(a, d_np, d.child_count);
         exclusive_scan_i32(d.prim, d.child_count, d.child_offset, d_np, d_J, d.scan_scratch, s, &ll);
-        k_compound_total<<<1, 1, 0, s>>>(d_np, d_J, d_slots, d.max_child_pairs, &d.counters->status);
+        k_clamp_total<<<1, 1, 0, s>>>(d_J, d.max_child_pairs, &d.counters->status);
         k_compound_expand<<<grid, NP_THREADS, 0, s>>>(a, d_np, d.child_offset, d.child_pairs, d.max_child_pairs);
         k_compound_contacts<<<grid, NP_THREADS, 0, s>>>(a, d_np, d_J, d.child_pairs);
         k_compound_hull_hull<<<d.num_sms * 16, CH_WARPS * 32, 0, s>>>(a, d_np, d_J, d.child_pairs);
         launches += 5;
+    }
+    int* d_K = nullptr;
+    if (d.num_meshes > 0) {
+        // concave-mesh pairs: triangle-convex pair counts, their scan (total in pad[6]) clamped to
+        // capacity, the triangle-convex pairs, their manifolds a warp each
+        d_K = &d.counters->pad[6];
+        k_concave_count<<<grid, NP_THREADS, 0, s>>>(a, d_np, d.concave_count);
+        exclusive_scan_i32(d.prim, d.concave_count, d.concave_offset, d_np, d_K, d.scan_scratch, s, &ll);
+        k_clamp_total<<<1, 1, 0, s>>>(d_K, d.max_concave_pairs, &d.counters->status);
+        k_concave_expand<<<grid, NP_THREADS, 0, s>>>(a, d_np, d.concave_offset, d.concave_pairs, d.max_concave_pairs);
+        k_concave_contacts<<<d.num_sms * 16, CC_WARPS * 32, 0, s>>>(a, d_np, d_J, d_K, d.concave_pairs);
+        launches += 4;
+    }
+    if (d_J || d_K) {
+        d_slots = &d.counters->pad[7];
+        k_slot_total<<<1, 1, 0, s>>>(d_np, d_J, d_K, d_slots);
+        launches++;
     }
     exclusive_scan_i32(d.prim, d.contact_flag, d.contact_index, d_slots, &d.counters->num_contacts, d.scan_scratch,
                        s, &ll);

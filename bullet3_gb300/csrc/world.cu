@@ -70,6 +70,8 @@ struct b3gWorld {
     std::vector<b3gFloat4> vertices;
     std::vector<b3gFloat4> edges;
     std::vector<b3gChildShape> children;  // the compounds' children (collidable.shapeIndex = first)
+    std::vector<b3gBvhInfo> bvh_infos;    // per concave mesh (collidable.numChildShapes = its index)
+    std::vector<b3gBvhNode> bvh_nodes;
     std::vector<b3gBody> bodies;
     std::vector<b3gInertia> inertias;
     std::vector<int> user_index;
@@ -280,6 +282,9 @@ extern "C" b3gStatus b3g_reset(b3g_handle h, int what) {
         h->indices.clear();
         h->vertices.clear();
         h->edges.clear();
+        h->children.clear();
+        h->bvh_infos.clear();
+        h->bvh_nodes.clear();
         h->bodies.clear();
         h->inertias.clear();
         h->user_index.clear();
@@ -438,6 +443,137 @@ extern "C" b3gStatus b3g_read_child_shapes(b3g_handle h, b3gChildShape* host, in
     *num = (int)h->children.size();
     if (host && capacity > 0)
         std::copy(h->children.begin(), h->children.begin() + std::min(capacity, *num), host);
+    return B3G_OK;
+}
+
+// b3QuantizedBvh::quantize (b3QuantizedBvh.h:314-341) with the bounds of a mesh's BVH: min corners
+// rounded down to even, max corners up to odd, so that dequantized boxes contain the originals
+static void mesh_quantize(unsigned short out[3], const float p[3], bool isMax, const b3gBvhInfo& bi) {
+    const float mn[3] = {bi.aabbMin.x, bi.aabbMin.y, bi.aabbMin.z};
+    const float q[3] = {bi.quantization.x, bi.quantization.y, bi.quantization.z};
+    for (int k = 0; k < 3; k++) {
+        const float v = (p[k] - mn[k]) * q[k];
+        out[k] = isMax ? (unsigned short)(((unsigned short)(v + 1.f)) | 1) : (unsigned short)(((unsigned short)v) & 0xfffe);
+    }
+}
+
+// The triangle BVH of a concave mesh, built over the triangles in index order (each internal node
+// halves its triangle range), so that a depth-first walk meets the overlapping triangles in index
+// order; nodes in depth-first order, an internal node's box the union of its children's quantized
+// boxes.  Returns the subtree's node count.
+static int build_mesh_bvh(std::vector<b3gBvhNode>& nodes, const std::vector<b3gBvhNode>& leaves, int lo, int hi) {
+    const size_t me = nodes.size();
+    if (hi - lo == 1) {
+        nodes.push_back(leaves[lo]);
+        return 1;
+    }
+    nodes.push_back(b3gBvhNode{});
+    const int mid = lo + (hi - lo) / 2;
+    const int nl = build_mesh_bvh(nodes, leaves, lo, mid);
+    const int nr = build_mesh_bvh(nodes, leaves, mid, hi);
+    const b3gBvhNode L = nodes[me + 1], R = nodes[me + 1 + nl];
+    b3gBvhNode& n = nodes[me];
+    for (int k = 0; k < 3; k++) {
+        n.quantizedAabbMin[k] = std::min(L.quantizedAabbMin[k], R.quantizedAabbMin[k]);
+        n.quantizedAabbMax[k] = std::max(L.quantizedAabbMax[k], R.quantizedAabbMax[k]);
+    }
+    n.escapeIndexOrTriangleIndex = -(1 + nl + nr);
+    return 1 + nl + nr;
+}
+
+extern "C" b3gStatus b3g_register_concave_mesh(b3g_handle h, const float* verts, int stride_bytes, int num_vertices,
+                                               const int* tri, int num_triangles, const float scaling[3], int* out) {
+    if (!h || !verts || !tri || !out) return fail(B3G_ERR_INVALID_ARG, "null argument");
+    if (h->uploaded) return fail(B3G_ERR_INVALID_ARG, "register shapes before the upload");
+    if ((int)h->collidables.size() >= h->cfg.max_shapes)
+        return fail(B3G_ERR_CAPACITY, "allocateCollidable out-of-range %d", h->cfg.max_shapes);
+    if (stride_bytes < 12) return fail(B3G_ERR_INVALID_ARG, "stride must be >= 12 bytes");
+    if (num_vertices < 3 || num_triangles < 1) return fail(B3G_ERR_INVALID_ARG, "a mesh needs a triangle");
+    for (int i = 0; i < 3 * num_triangles; i++)
+        if (tri[i] < 0 || tri[i] >= num_vertices)
+            return fail(B3G_ERR_INVALID_INDEX, "triangle index %d out of range", tri[i]);
+    const float sx = scaling ? scaling[0] : 1.f, sy = scaling ? scaling[1] : 1.f, sz = scaling ? scaling[2] : 1.f;
+    std::vector<v3> v(num_vertices);
+    for (int i = 0; i < num_vertices; i++) {
+        const float* p = reinterpret_cast<const float*>(reinterpret_cast<const char*>(verts) + (size_t)i * stride_bytes);
+        v[i] = mk3(p[0] * sx, p[1] * sy, p[2] * sz);
+    }
+    // the shape record: the triangles as faces, the scaled vertices (b3GpuNarrowPhase.cpp:615-667)
+    b3gHull hull{};
+    hull.uniqueEdgesOffset = (int)h->edges.size();
+    hull.faceOffset = (int)h->faces.size();
+    hull.numFaces = num_triangles;
+    for (int t = 0; t < num_triangles; t++) {
+        const v3 v0 = v[tri[3 * t]], v1 = v[tri[3 * t + 1]], v2 = v[tri[3 * t + 2]];
+        const v3 c = cross3(v1 - v0, v2 - v0);
+        const float inv = 1.f / sqrtf(dot3(c, c));
+        const v3 n = mk3(c.x * inv, c.y * inv, c.z * inv);
+        b3gFace f{};
+        f.plane = b3gFloat4{n.x, n.y, n.z, -dot3(n, v0)};
+        f.indexOffset = (int)h->indices.size();
+        f.numIndices = 3;
+        for (int k = 0; k < 3; k++) h->indices.push_back(tri[3 * t + k]);
+        h->faces.push_back(f);
+    }
+    hull.numVertices = num_vertices;
+    hull.vertexOffset = (int)h->vertices.size();
+    float mn[3] = {1e30f, 1e30f, 1e30f}, mx[3] = {-1e30f, -1e30f, -1e30f};
+    for (int i = 0; i < num_vertices; i++) {
+        h->vertices.push_back(b3gFloat4{v[i].x, v[i].y, v[i].z, 0.f});
+        const float p[3] = {v[i].x, v[i].y, v[i].z};
+        for (int k = 0; k < 3; k++) {
+            if (p[k] < mn[k]) mn[k] = p[k];
+            if (mx[k] < p[k]) mx[k] = p[k];
+        }
+    }
+    const int hullIndex = (int)h->hulls.size();
+    h->hulls.push_back(hull);
+    // the quantization (b3QuantizedBvh::setQuantizationValues, margin 1) and the leaves: each
+    // triangle's AABB widened to at least 0.002 per axis (b3OptimizedBvh::build's quantized leaf
+    // callback), from the scaled vertices
+    b3gBvhInfo bi{};
+    bi.aabbMin = b3gFloat4{mn[0] - 1.f, mn[1] - 1.f, mn[2] - 1.f, 0.f};
+    bi.aabbMax = b3gFloat4{mx[0] + 1.f, mx[1] + 1.f, mx[2] + 1.f, 0.f};
+    bi.quantization = b3gFloat4{65533.f / (bi.aabbMax.x - bi.aabbMin.x), 65533.f / (bi.aabbMax.y - bi.aabbMin.y),
+                                65533.f / (bi.aabbMax.z - bi.aabbMin.z), 0.f};
+    bi.nodeOffset = (int)h->bvh_nodes.size();
+    bi.numTriangles = num_triangles;
+    std::vector<b3gBvhNode> leaves(num_triangles);
+    for (int t = 0; t < num_triangles; t++) {
+        float lo[3] = {1e18f, 1e18f, 1e18f}, hi[3] = {-1e18f, -1e18f, -1e18f};
+        for (int k = 0; k < 3; k++) {
+            const v3 p = v[tri[3 * t + k]];
+            const float c[3] = {p.x, p.y, p.z};
+            for (int a = 0; a < 3; a++) {
+                if (c[a] < lo[a]) lo[a] = c[a];
+                if (hi[a] < c[a]) hi[a] = c[a];
+            }
+        }
+        for (int a = 0; a < 3; a++)
+            if (hi[a] - lo[a] < 0.002f) {
+                hi[a] = hi[a] + 0.001f;
+                lo[a] = lo[a] - 0.001f;
+            }
+        mesh_quantize(leaves[t].quantizedAabbMin, lo, false, bi);
+        mesh_quantize(leaves[t].quantizedAabbMax, hi, true, bi);
+        leaves[t].escapeIndexOrTriangleIndex = t;
+    }
+    bi.numNodes = build_mesh_bvh(h->bvh_nodes, leaves, 0, num_triangles);
+    const int bvhIndex = (int)h->bvh_infos.size();
+    h->bvh_infos.push_back(bi);
+    b3gCollidable col{bvhIndex, 0.f, B3G_SHAPE_CONCAVE_TRIMESH, hullIndex};
+    return add_collidable(h, col, make_aabb(mn[0], mn[1], mn[2], mx[0], mx[1], mx[2]), out);
+}
+
+extern "C" b3gStatus b3g_read_mesh_bvh(b3g_handle h, b3gBvhInfo* infos, int capacity_infos, b3gBvhNode* nodes,
+                                       int capacity_nodes, int* num_infos, int* num_nodes) {
+    if (!h || !num_infos || !num_nodes) return fail(B3G_ERR_INVALID_ARG, "null argument");
+    *num_infos = (int)h->bvh_infos.size();
+    *num_nodes = (int)h->bvh_nodes.size();
+    if (infos && capacity_infos > 0)
+        std::copy(h->bvh_infos.begin(), h->bvh_infos.begin() + std::min(capacity_infos, *num_infos), infos);
+    if (nodes && capacity_nodes > 0)
+        std::copy(h->bvh_nodes.begin(), h->bvh_nodes.begin() + std::min(capacity_nodes, *num_nodes), nodes);
     return B3G_OK;
 }
 
@@ -673,7 +809,10 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     d.max_child_pairs = d.num_children > 0 ? (h->cfg.max_compound_child_pairs > 0 ? h->cfg.max_compound_child_pairs
                                                                                   : d.max_pairs)
                                            : 0;
-    d.max_contacts = d.max_pairs + d.max_child_pairs;
+    d.num_meshes = (int)h->bvh_infos.size();
+    d.max_concave_pairs =
+        d.num_meshes > 0 ? (h->cfg.max_concave_pairs > 0 ? h->cfg.max_concave_pairs : d.max_pairs) : 0;
+    d.max_contacts = d.max_pairs + d.max_child_pairs + d.max_concave_pairs;
     d.prim.sort_blocks = sms * d.tune.sort_blocks_per_sm;
     d.prim.scan_blocks = sms * 2;
 
@@ -723,6 +862,13 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
         TRY(dalloc(h, &d.child_count, d.max_pairs));
         TRY(dalloc(h, &d.child_offset, d.max_pairs));
         TRY(dalloc(h, &d.child_pairs, d.max_child_pairs));
+    }
+    if (d.num_meshes > 0) {
+        TRY(dalloc(h, &d.bvh_infos, d.num_meshes));
+        TRY(dalloc(h, &d.bvh_nodes, h->bvh_nodes.size()));
+        TRY(dalloc(h, &d.concave_count, d.max_pairs));
+        TRY(dalloc(h, &d.concave_offset, d.max_pairs));
+        TRY(dalloc(h, &d.concave_pairs, d.max_concave_pairs));
     }
     TRY(dalloc(h, &d.contacts_compact, d.max_contacts));
     TRY(dalloc(h, &d.sp.nf, d.max_contacts));
@@ -828,6 +974,12 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
     if (d.num_children > 0)
         CUDA_TRY(cudaMemcpyAsync(d.children, h->children.data(), sizeof(b3gChildShape) * h->children.size(),
                                  cudaMemcpyHostToDevice, s));
+    if (d.num_meshes > 0) {
+        CUDA_TRY(cudaMemcpyAsync(d.bvh_infos, h->bvh_infos.data(), sizeof(b3gBvhInfo) * h->bvh_infos.size(),
+                                 cudaMemcpyHostToDevice, s));
+        CUDA_TRY(cudaMemcpyAsync(d.bvh_nodes, h->bvh_nodes.data(), sizeof(b3gBvhNode) * h->bvh_nodes.size(),
+                                 cudaMemcpyHostToDevice, s));
+    }
     {
         // faces whose normal is the exact negation of an earlier face's (a box's opposite faces):
         // rotated and sign-flipped towards the other body they give the earlier face's SAT axis
@@ -1559,6 +1711,7 @@ extern "C" b3gStatus b3g_get_stats(b3g_handle h, b3gStepStats* out) {
     out->status = c.status;
     out->num_large = h->d.num_large + h->d.num_sap;
     out->num_child_pairs = h->d.num_children > 0 ? c.pad[4] : 0;
+    out->num_concave_pairs = h->d.num_meshes > 0 ? c.pad[6] : 0;
     return B3G_OK;
 }
 

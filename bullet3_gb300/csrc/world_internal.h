@@ -168,7 +168,8 @@ struct DeviceState {
     b3gPair* pairs = nullptr;
     int* type_lists = nullptr;        // PT_COUNT * max_pairs
     // narrowphase
-    b3gContact4* contact_slots = nullptr;  // one per pair slot, then one per compound child pair
+    b3gContact4* contact_slots = nullptr;  // one per pair slot, then one per compound child pair, then
+                                           // one per concave triangle-convex pair
     int* contact_flag = nullptr;           // per slot: 1 if a manifold was produced
     int* contact_index = nullptr;          // per slot: exclusive scan of contact_flag
     int* manifold_pair = nullptr;          // manifold -> slot index (< pair count: a pair)
@@ -180,6 +181,16 @@ struct DeviceState {
     int* child_count = nullptr;
     int* child_offset = nullptr;
     int4* child_pairs = nullptr;
+    // concave meshes (allocated when one is registered): their BVHs, the per-pair triangle-convex
+    // pair counts and their scan, the triangle-convex pairs (mesh body, other body, triangle,
+    // child of the other body or 0)
+    b3gBvhInfo* bvh_infos = nullptr;
+    b3gBvhNode* bvh_nodes = nullptr;
+    int num_meshes = 0;
+    int max_concave_pairs = 0;
+    int* concave_count = nullptr;
+    int* concave_offset = nullptr;
+    int4* concave_pairs = nullptr;
     b3gContact4* contacts_compact = nullptr;  // filled on demand for the drop-in getter
     // solver
     SolverPoints sp;                       // compact contact-point records

@@ -35,6 +35,7 @@ class b3Config:
         self.m_maxBroadphasePairs = 0
         self.m_maxContactCapacity = 0
         self.m_compoundPairCapacity = 0  # child pairs of compounds per step (0 = m_maxBroadphasePairs)
+        self.m_maxTriConvexPairCapacity = 0  # triangle-convex pairs of meshes per step (0 = m_maxBroadphasePairs)
         self.grid_cell_size = 0.0
         self.grid_dim = 128
         self.solver_mode = capi.SOLVER_PGS
@@ -72,7 +73,8 @@ class b3Config:
                                    warm_start_max_points=int(self.warm_start_max_points),
                                    autotune=int(self.autotune), broadphase=int(self.broadphase),
                                    pgs_tail_manifolds=int(self.pgs_tail_manifolds), pgs_flow=int(self.pgs_flow),
-                                   max_compound_child_pairs=int(self.m_compoundPairCapacity))
+                                   max_compound_child_pairs=int(self.m_compoundPairCapacity),
+                                   max_concave_pairs=int(self.m_maxTriConvexPairCapacity))
 
 
 class _World:
@@ -158,9 +160,24 @@ class b3GpuNarrowPhase:
                 ch[i]["shapeType"] = 3
         return self._reg("b3g_register_compound", capi.ptr(ch), C.c_int(len(ch)))
 
-    def registerConcaveMesh(self, vertices, indices, scaling) -> int:
-        b3Error("registerConcaveMesh: concave meshes are not supported by this GPU step")
-        return -1
+    def registerConcaveMesh(self, vertices, indices, scaling=(1.0, 1.0, 1.0)) -> int:
+        """registerConcaveMesh(b3AlignedObjectArray<b3Vector3>*, b3AlignedObjectArray<int>*, const float*):
+        vertices (n, 3), indices (3 per triangle); -1 + b3Error on invalid input."""
+        if vertices is None or indices is None:
+            b3Error("registerConcaveMesh: no vertices or indices")
+            return -1
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+        ix = np.ascontiguousarray(indices, np.int32).reshape(-1)
+        if len(ix) % 3:
+            b3Error("registerConcaveMesh: the index count is not a multiple of 3")
+            return -1
+        sc = (C.c_float * 3)(*[float(x) for x in scaling])
+        st = capi.load().b3g_register_concave_mesh(self._w.handle, fptr(v), C.c_int(12), C.c_int(len(v)), iptr(ix),
+                                                   C.c_int(len(ix) // 3), sc, C.byref(out := C.c_int(-1)))
+        if st != 0:
+            b3Error(capi._LIB.b3g_last_error().decode())
+            return -1
+        return out.value
 
     # -- bodies -------------------------------------------------------------------------
     def getNumRigidBodies(self) -> int:

@@ -10,6 +10,7 @@ configurations (numpy.random.Generator(PCG64(seed))).
   batched_piles  many independent box/sphere piles, each on its own plane, body counts log-uniform
   compound_scene compounds of convex hulls (an L of two boxes, a dumbbell of two hulls and a box)
                  among boxes and hulls over a plane
+  terrain_scene  boxes, hulls and compounds on a static concave height-field mesh
 
 A Scene is plain numpy data; `load_scene` registers it through the reference-style API.
 """
@@ -256,6 +257,75 @@ def compound_scene(n=2048, extent=None, seed=0, plane=True, velocity_sigma=0.5, 
     sc.mass = np.where(kinds == 0, 0.0, 1.0).astype(np.float32) if plane else np.ones(n, np.float32)
     sc.pos, sc.orn, sc.linvel = pos, orn, vel
     sc.cell = 2.0 * 2.0 * reach
+    return sc
+
+
+def terrain_mesh(grid=64, cell=1.0, amplitude=1.5, seed=0):
+    """A height field as a triangle mesh: (grid + 1)^2 vertices (x, h, z), x and z multiples of cell,
+    h a sum of two sines plus N(0, 0.05^2); two triangles per quad, row by row, wound so that their
+    normals point up.  Returns (vertices (n, 3) float32, indices (3 t,) int32, height function)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    k = np.arange(grid + 1, dtype=np.float64) * cell
+    X, Z = np.meshgrid(k, k, indexing="xy")  # row j (z), column i (x)
+
+    def height(x, z):
+        return amplitude * (np.sin(x * 0.35) * np.cos(z * 0.27) + 0.5 * np.sin(0.6 * x + 0.4 * z))
+
+    H = height(X, Z) + rng.normal(0.0, 0.05, X.shape)
+    verts = np.stack([X, H, Z], -1).reshape(-1, 3).astype(np.float32)
+    idx = []
+    w = grid + 1
+    for j in range(grid):
+        for i in range(grid):
+            p00, p10, p01, p11 = j * w + i, j * w + i + 1, (j + 1) * w + i, (j + 1) * w + i + 1
+            idx += [p00, p01, p10, p10, p01, p11]
+    return verts, np.array(idx, np.int32), height
+
+
+def terrain_scene(n=2048, grid=64, cell=1.0, seed=0, drop=False, velocity_sigma=0.3) -> Scene:
+    """A static concave height-field mesh (terrain_mesh, body 0 at the identity pose) under boxes
+    (half extents 0.5 x 0.25 x 0.25), 20-point Gaussian hulls and compounds (an L of two boxes, a
+    dumbbell of two hulls around a box), in turn.  Either scattered just over the surface with
+    random orientations and N(0, velocity_sigma^2) velocities (heights from 0.2 below the surface to
+    0.6 above it, so that many touch it), or (drop=True) a lattice of them at rest, from 2 above
+    the highest point, that falls onto it."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sc = Scene(name=f"terrain_{n}")
+    verts, idx, height = terrain_mesh(grid, cell, seed=seed)
+    sc.shapes.append({"type": "mesh", "verts": verts, "indices": idx})
+    gauss = (rng.standard_normal((20, 3)) * 0.3).astype(np.float32)
+    sc.shapes += [{"type": "hull", "verts": box_vertices(0.5, 0.25, 0.25)},
+                  {"type": "hull", "verts": box_vertices(0.25, 0.5, 0.25)},
+                  {"type": "hull", "verts": gauss}]
+    q0 = (0.0, 0.0, 0.0, 1.0)
+    sc.shapes.append({"type": "compound", "children": [(1, (0.25, 0.0, 0.0), q0), (2, (0.0, 0.5, 0.0), q0)]})
+    qa, qb = random_quaternions(rng, 2)
+    sc.shapes.append({"type": "compound", "children": [(3, (-0.6, 0.0, 0.0), tuple(qa)), (1, (0.0, 0.0, 0.0), q0),
+                                                        (3, (0.6, 0.0, 0.0), tuple(qb))]})
+    kinds = np.array([1, 3, 4, 5], np.int32)[np.arange(n) % 4]
+    reach = 0.6 + float(np.linalg.norm(gauss, axis=1).max())
+    span = grid * cell
+    if drop:
+        sp = 2.0 * reach + 0.1  # nothing overlaps at the start
+        side = max(1, min(int(np.ceil(np.sqrt(n / 3))), int((span - 2 * reach) // sp) + 1))
+        i = np.arange(n)
+        top = float(verts[:, 1].max()) + reach + 2.0
+        pos = np.stack([reach + (i % side) * sp, top + (i // (side * side)) * (2.0 * reach + 0.1),
+                        reach + ((i // side) % side) * sp], 1)
+        pos = (pos + rng.uniform(-0.04, 0.04, (n, 3))).astype(np.float32)
+        vel = np.zeros((n, 3), np.float32)
+    else:
+        x = rng.uniform(reach, span - reach, n)
+        z = rng.uniform(reach, span - reach, n)
+        pos = np.stack([x, height(x, z) + rng.uniform(-0.2, 0.6, n), z], 1).astype(np.float32)
+        vel = (rng.standard_normal((n, 3)) * velocity_sigma).astype(np.float32)
+    orn = random_quaternions(rng, n)
+    sc.body_shape = np.concatenate([[0], kinds]).astype(np.int32)
+    sc.mass = np.concatenate([[0.0], np.ones(n)]).astype(np.float32)
+    sc.pos = np.vstack([np.zeros((1, 3), np.float32), pos])
+    sc.orn = np.vstack([np.array([[0, 0, 0, 1]], np.float32), orn])
+    sc.linvel = np.vstack([np.zeros((1, 3), np.float32), vel])
+    sc.cell = 4.0 * reach
     return sc
 
 
@@ -513,6 +583,8 @@ def load_scene(scene: Scene, config=None, device: int = 0, upload: bool = True):
         elif s["type"] == "compound":
             # children: (index of an earlier shape of the scene, position, orientation)
             c = np_.registerCompoundShape([(col[i], p, q) for i, p, q in s["children"]])
+        elif s["type"] == "mesh":
+            c = np_.registerConcaveMesh(s["verts"], s["indices"], s.get("scaling", (1.0, 1.0, 1.0)))
         else:
             raise ValueError(s["type"])
         if c < 0:

@@ -124,7 +124,10 @@ typedef struct b3gConfig {
                                   300k manifolds */
     int max_compound_child_pairs;  /* child pairs of the compound pairs per step (0 = max_pairs); only
                                       allocated when a compound is registered */
-    int reserved[2];
+    int max_concave_pairs;     /* triangle-convex pairs of the concave-mesh pairs per step
+                                  (m_maxTriConvexPairCapacity; 0 = max_pairs); only allocated when a
+                                  concave mesh is registered */
+    int reserved[1];
 } b3gConfig;
 
 /* Per-step counters, copied once per step from the device. */
@@ -138,6 +141,7 @@ typedef struct b3gStepStats {
     unsigned int status;    /* B3G_FLAG_* bits */
     int num_large;          /* bodies handled by the large-AABB path */
     int num_child_pairs;    /* compound child pairs of the last contact stage (after the capacity clamp) */
+    int num_concave_pairs;  /* triangle-convex pairs of the last contact stage (after the capacity clamp) */
 } b3gStepStats;
 
 /* ------------------------------------------------------------------ lifetime */
@@ -187,10 +191,28 @@ b3gStatus b3g_register_hull_tables(b3g_handle h, const float* verts_xyz, int num
  * (b3ConvexHullContact.cpp:1419-2022) and computeContactPlaneCompound (:2182) compute them.  Compounds
  * against spheres give no contacts. */
 struct b3gChildShape;
+struct b3gBvhInfo;
+struct b3gBvhNode;
 b3gStatus b3g_register_compound(b3g_handle h, const struct b3gChildShape* children, int num_children,
                                 int* out_collidable);
 /* Host copy of the registered compound children (b3gChildShape, b3g_types.h; capacity 0: count only). */
 b3gStatus b3g_read_child_shapes(b3g_handle h, struct b3gChildShape* host_children, int capacity, int* num);
+/* b3GpuNarrowPhase::registerConcaveMesh (b3GpuNarrowPhase.cpp:521-613) + registerConcaveMeshShape
+ * (:615-667): a static triangle mesh.  vertices: num_vertices points stride_bytes apart (>= 12),
+ * indices: 3 per triangle; scaling multiplies the vertices.  The collidable's shape record lists
+ * the triangles as faces (plane = normalised (v1 - v0) x (v2 - v0), w = -n.v0) and a quantized BVH
+ * over them (b3g_read_mesh_bvh).  A mesh collides with hulls and compounds (one manifold per
+ * touching triangle, or triangle and child, as b3BvhTraversal / b3FindConcaveSeparatingAxisKernel /
+ * clipFacesAndFindContactsKernel / b3NewContactReductionKernel compute them) when its body is the
+ * pair's first (lower index), as in the reference; not with spheres, planes or other meshes.  The
+ * reference traverses with the other body's world AABB in the mesh's own frame, so meshes are
+ * meant to stay at the identity pose.  -> -1 + b3Error in the Python / C++ layers on invalid input. */
+b3gStatus b3g_register_concave_mesh(b3g_handle h, const float* vertices, int stride_bytes, int num_vertices,
+                                    const int* indices, int num_triangles, const float scaling[3],
+                                    int* out_collidable);
+/* Host copy of the meshes' BVHs (b3gBvhInfo / b3gBvhNode, b3g_types.h; capacities 0: counts only). */
+b3gStatus b3g_read_mesh_bvh(b3g_handle h, struct b3gBvhInfo* infos, int capacity_infos, struct b3gBvhNode* nodes,
+                            int capacity_nodes, int* num_infos, int* num_nodes);
 
 /* ------------------------------------------------------------------ bodies (b3GpuRigidBodyPipeline) */
 /* b3GpuRigidBodyPipeline::registerPhysicsInstance (b3GpuRigidBodyPipeline.cpp:603-669) together with

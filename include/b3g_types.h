@@ -26,6 +26,7 @@ extern "C" {
 
 #define B3G_SHAPE_CONVEX_HULL 3
 #define B3G_SHAPE_PLANE 4
+#define B3G_SHAPE_CONCAVE_TRIMESH 5  /* SHAPE_CONCAVE_TRIMESH */
 #define B3G_SHAPE_COMPOUND 6   /* SHAPE_COMPOUND_OF_CONVEX_HULLS */
 #define B3G_SHAPE_SPHERE 7
 
@@ -111,6 +112,27 @@ typedef struct b3gChildShape {
 } b3gChildShape;
 
 typedef struct b3gPair { int x, y, z, w; } b3gPair;
+
+/* A concave mesh's triangle BVH (the quantized form of b3QuantizedBvh / b3BvhInfo,
+ * Bullet3OpenCL/NarrowphaseCollision/b3BvhInfo.h:6-15): the mesh's local AABB widened by 1 on every
+ * side, 65533 / its extent per axis, and the mesh's nodes (depth-first, nodeOffset..+numNodes). */
+typedef struct b3gBvhInfo {
+    b3gFloat4 aabbMin;
+    b3gFloat4 aabbMax;
+    b3gFloat4 quantization;
+    int numNodes;
+    int nodeOffset;
+    int numTriangles;
+    int pad;
+} b3gBvhInfo;
+
+/* b3QuantizedBvhNodeData (shared/b3QuantizedBvhNodeData.h:14-22), 16 B: quantized AABB; a leaf
+ * holds its triangle index (>= 0), an internal node minus the size of its subtree in nodes. */
+typedef struct b3gBvhNode {
+    unsigned short quantizedAabbMin[3];
+    unsigned short quantizedAabbMax[3];
+    int escapeIndexOrTriangleIndex;
+} b3gBvhNode;
 
 typedef struct b3gJoint {
     int type;            /* 3 point to point, 4 fixed (b3GpuGenericConstraintType) */

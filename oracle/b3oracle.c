@@ -1006,6 +1006,355 @@ int oracle_compound_contacts(const obody* bodies, const oshapes* sh, const opair
     return m;
 }
 
+/* ------------------------------------------------------------------ concave meshes
+ * A concave mesh (SHAPE_CONCAVE_TRIMESH) is a shape record whose faces are its triangles
+ * (registerConcaveMeshShape, b3GpuNarrowPhase.cpp:615-667) with a quantized triangle BVH over its
+ * local AABB widened by 1 (b3QuantizedBvh::setQuantizationValues, b3QuantizedBvh.cpp:79-88; its
+ * collidable's numChildShapes is the BVH index).  A pair whose first body is the mesh and whose
+ * second is a hull or a compound yields the triangles whose quantized leaf box overlaps the second
+ * body's quantized world AABB (b3BvhTraversal, shared/b3BvhTraversal.h:11-111) -- any BVH over
+ * those leaf boxes finds the same set -- with every child of a compound, in (pair, triangle,
+ * child) order.  Each triangle-convex pair yields at most one manifold
+ * (b3FindConcaveSeparatingAxisKernel, shared/b3FindConcaveSatAxis.h:506-797; b3FindClippingFaces
+ * :421-504; clipFacesAndFindContactsKernel, shared/b3ClipFaces.h:67-177;
+ * b3NewContactReductionKernel, shared/b3NewContactReduction.h:88-177).  The leaf boxes are taken
+ * from the scaled vertices (the reference builds them from the unscaled ones: the same for a
+ * scaling of 1). */
+#define SHAPE_CONCAVE_TRIMESH 5
+
+typedef struct { float mn[3], mx[3], q[3]; } obvhq;
+
+static void mesh_bvhq(const oaabb* local, obvhq* b) {
+    int k;
+    for (k = 0; k < 3; k++) {
+        b->mn[k] = local->minv[k] - 1.0f;
+        b->mx[k] = local->maxv[k] + 1.0f;
+        b->q[k] = 65533.0f / (b->mx[k] - b->mn[k]);
+    }
+}
+
+/* b3QuantizedBvh::quantize (clamp = 0) and b3QuantizeWithClamp (clamp = 1) */
+static void bvh_quantize(unsigned short out[3], const float p[3], int isMax, const obvhq* b, int clamp) {
+    int k;
+    for (k = 0; k < 3; k++) {
+        float c = p[k], v;
+        if (clamp) {
+            if (c < b->mn[k]) c = b->mn[k];
+            if (b->mx[k] < c) c = b->mx[k];
+        }
+        v = (c - b->mn[k]) * b->q[k];
+        out[k] = isMax ? (unsigned short)(((unsigned short)(v + 1.f)) | 1) : (unsigned short)(((unsigned short)v) & 0xfffe);
+    }
+}
+
+static const ohull* mesh_of(const oshapes* sh, const obody* b) { return &sh->hulls[sh->cols[b->collidableIdx].shapeIndex]; }
+
+static v3 mesh_vertex(const oshapes* sh, const ohull* mesh, int t, int k) {
+    const oface* f = &sh->faces[mesh->faceOffset + t];
+    return f4v(sh->verts[mesh->vertexOffset + sh->indices[f->indexOffset + k]]);
+}
+
+/* the quantized leaf box of triangle t: its AABB widened to at least 0.002 per axis
+ * (b3OptimizedBvh::build, QuantizedNodeTriangleCallback) */
+static void tri_leaf(const oshapes* sh, const ohull* mesh, int t, const obvhq* b, unsigned short qmn[3],
+                     unsigned short qmx[3]) {
+    float lo[3] = {1e18f, 1e18f, 1e18f}, hi[3] = {-1e18f, -1e18f, -1e18f};
+    int k, a;
+    for (k = 0; k < 3; k++) {
+        v3 p = mesh_vertex(sh, mesh, t, k);
+        float c[3];
+        c[0] = p.x; c[1] = p.y; c[2] = p.z;
+        for (a = 0; a < 3; a++) {
+            if (c[a] < lo[a]) lo[a] = c[a];
+            if (hi[a] < c[a]) hi[a] = c[a];
+        }
+    }
+    for (a = 0; a < 3; a++)
+        if (hi[a] - lo[a] < 0.002f) {
+            hi[a] = hi[a] + 0.001f;
+            lo[a] = lo[a] - 0.001f;
+        }
+    bvh_quantize(qmn, lo, 0, b, 0);
+    bvh_quantize(qmx, hi, 1, b, 0);
+}
+
+int oracle_concave_pairs(const obody* bodies, const oshapes* sh, const oaabb* aabbs, const opair* pairs, int npairs,
+                         opair* out, int cap) {
+    int p, n = 0;
+    for (p = 0; p < npairs; p++) {
+        int A = pairs[p].x, B = pairs[p].y, t, c, tB, nch;
+        const ocollidable *cA, *cB;
+        const ohull* mesh;
+        obvhq bq;
+        unsigned short qmn[3], qmx[3];
+        if (bodies[A].invMass == 0.f && bodies[B].invMass == 0.f) continue;
+        cA = &sh->cols[bodies[A].collidableIdx];
+        cB = &sh->cols[bodies[B].collidableIdx];
+        if (cA->shapeType != SHAPE_CONCAVE_TRIMESH) continue;
+        tB = cB->shapeType;
+        /* (spheres take the reference's findConcaveSphereContactsKernel, not restated here) */
+        if (tB != SHAPE_CONVEX_HULL && tB != SHAPE_COMPOUND_OF_CONVEX_HULLS) continue;
+        nch = tB == SHAPE_COMPOUND_OF_CONVEX_HULLS ? cB->numChildShapes : 1;
+        mesh = &sh->hulls[cA->shapeIndex];
+        mesh_bvhq(&sh->local_aabbs[bodies[A].collidableIdx], &bq);
+        bvh_quantize(qmn, aabbs[B].minv, 0, &bq, 1);
+        bvh_quantize(qmx, aabbs[B].maxv, 1, &bq, 1);
+        for (t = 0; t < mesh->numFaces; t++) {
+            unsigned short lmn[3], lmx[3];
+            tri_leaf(sh, mesh, t, &bq, lmn, lmx);
+            /* b3TestQuantizedAabbAgainstQuantizedAabbSlow */
+            if (qmn[0] > lmx[0] || qmx[0] < lmn[0] || qmn[1] > lmx[1] || qmx[1] < lmn[1] || qmn[2] > lmx[2] ||
+                qmx[2] < lmn[2])
+                continue;
+            for (c = 0; c < nch; c++) {
+                if (n < cap) {
+                    out[n].x = A;
+                    out[n].y = B;
+                    out[n].z = t;
+                    out[n].w = tB == SHAPE_COMPOUND_OF_CONVEX_HULLS ? cB->shapeIndex + c : 0;
+                }
+                n++;
+            }
+        }
+    }
+    return n;
+}
+
+/* clipFaceGlobal (shared/b3ClipFaces.h:20-61): no lower bound on the input polygon */
+static int clip_face_global(const p4* in, int nin, v3 n, float eq, p4* out) {
+    int nout = 0, ve;
+    p4 first;
+    float ds;
+    if (nin < 1) return 0;
+    first = in[nin - 1];
+    ds = dot(n, mk(first.x, first.y, first.z)) + eq;
+    for (ve = 0; ve < nin; ve++) {
+        p4 end = in[ve];
+        float de = dot(n, mk(end.x, end.y, end.z)) + eq;
+        if (ds < 0.f) {
+            if (de < 0.f) {
+                if (nout < CLIP_CAP) out[nout++] = end;
+            } else {
+                float t = ds * 1.f / (ds - de);
+                p4 l = {first.x + (end.x - first.x) * t, first.y + (end.y - first.y) * t,
+                        first.z + (end.z - first.z) * t, 0.f};
+                if (nout < CLIP_CAP) out[nout++] = l;
+            }
+        } else if (de < 0.f) {
+            float t = ds * 1.f / (ds - de);
+            p4 l = {first.x + (end.x - first.x) * t, first.y + (end.y - first.y) * t, first.z + (end.z - first.z) * t,
+                    0.f};
+            if (nout < CLIP_CAP) out[nout++] = l;
+            if (nout < CLIP_CAP) out[nout++] = end;
+        }
+        first = end;
+        ds = de;
+    }
+    return nout;
+}
+
+/* b3Project over the triangle's 3 local vertices */
+static void project_tri(const v3* tv, v3 pos, qt orn, v3 dir, float* mn, float* mx) {
+    v3 localDir = qrotq(qconj(orn), dir);
+    float offset = dot(pos, dir);
+    int i;
+    *mn = FLT_MAX;
+    *mx = -FLT_MAX;
+    for (i = 0; i < 3; i++) {
+        float dp = dot(tv[i], localDir);
+        if (dp < *mn) *mn = dp;
+        if (dp > *mx) *mx = dp;
+    }
+    if (*mn > *mx) { float t = *mn; *mn = *mx; *mx = t; }
+    *mn = *mn + offset;
+    *mx = *mx + offset;
+}
+
+/* one triangle-convex pair: the triangle as a five-face prism (front, back, three edge planes),
+ * the SAT over its faces, the hull's faces and the edge pairs with one running minimum, then the
+ * clipping faces, the clip (minDist -1e30, maxDist 0.02) and the reduction */
+static int concave_tri(const obody* bodies, const oshapes* sh, const oaabb* aabbs, const opair* cp, int index,
+                       ocontact* c) {
+    const obody* BA = &bodies[cp->x];
+    const obody* BB = &bodies[cp->y];
+    const ohull* mesh = mesh_of(sh, BA);
+    const oface* face = &sh->faces[mesh->faceOffset + cp->z];
+    v3 tv[3], fn[5], te[3], lc = mk(0.f, 0.f, 0.f), normal, posA, posB, c0, c1, D, sep = mk(1.f, 2.f, 3.f);
+    qt qA, qB;
+    float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f}, dmin = FLT_MAX, d, min0, max0, min1, max1;
+    int i, k, prev, colB = BB->collidableIdx, e0, e1, f, fb, fa, na, ia[3], nin, np, idx[4];
+    const ohull* hB;
+    v3 nA = mk(0.f, 0.f, 0.f), wA[3];
+    m3 RA, RB;
+    p4 buf0[CLIP_CAP], buf1[CLIP_CAP], *pin, *pout;
+    float dmax;
+    int tB = sh->cols[colB].shapeType;
+    if (tB != SHAPE_CONVEX_HULL && tB != SHAPE_COMPOUND_OF_CONVEX_HULLS) return 0;
+    for (i = 0; i < 3; i++) {
+        float q3[3];
+        tv[i] = mesh_vertex(sh, mesh, cp->z, i);
+        lc = add(lc, tv[i]);
+        q3[0] = tv[i].x; q3[1] = tv[i].y; q3[2] = tv[i].z;
+        for (k = 0; k < 3; k++) {
+            if (q3[k] < lo[k]) lo[k] = q3[k];
+            if (hi[k] < q3[k]) hi[k] = q3[k];
+        }
+    }
+    for (k = 0; k < 3; k++)
+        if (lo[k] > aabbs[cp->y].maxv[k] || hi[k] < aabbs[cp->y].minv[k]) return 0;
+    te[0] = sub(tv[1], tv[0]);
+    te[1] = sub(tv[2], tv[1]);
+    te[2] = sub(tv[0], tv[2]);
+    normal = f4v(face->plane);
+    fn[0] = normal;
+    fn[1] = neg(normal);
+    prev = 2;
+    for (i = 0; i < 3; i++) {
+        fn[2 + i] = nrm(cross(normal, sub(tv[prev], tv[i])));
+        prev = i;
+    }
+    lc = scl(lc, 1.f / 3.f);
+    posA = f4v(BA->pos);
+    qA = f4q(BA->quat);
+    posB = f4v(BB->pos);
+    qB = f4q(BB->quat);
+    /* b3TransformPoint of the host code is b3Transform's: the rotation matrix of the quaternion
+     * (b3Quat.h's C++ branch), for the child pose, the centres and the clipping faces' vertices */
+    if (tB == SHAPE_COMPOUND_OF_CONVEX_HULLS) {
+        const ochild* ch = &sh->children[cp->w];
+        m3 RB0 = qmat(qB);
+        colB = ch->shapeIndex;
+        posB = add(mmul(&RB0, f4v(ch->pos)), posB);
+        qB = qmul(qB, f4q(ch->orn));
+    }
+    hB = &sh->hulls[sh->cols[colB].shapeIndex];
+    RA = qmat(qA);
+    RB = qmat(qB);
+    c0 = add(mmul(&RA, lc), posA);
+    c1 = add(mmul(&RB, f4v(hB->localCenter)), posB);
+    D = sub(c0, c1);
+    /* the prism's faces */
+    for (f = 0; f < 5; f++) {
+        v3 n = qrotq(qA, fn[f]);
+        if (dot(D, n) < 0.f) n = neg(n);
+        project_tri(tv, posA, qA, n, &min0, &max0);
+        project(&sh->verts[hB->vertexOffset], hB->numVertices, posB, qB, n, &min1, &max1);
+        if (max0 < min1 || max1 < min0) return 0;
+        d = (max0 - min1) < (max1 - min0) ? (max0 - min1) : (max1 - min0);
+        if (d < dmin) { dmin = d; sep = n; }
+    }
+    if (dot(neg(D), sep) > 0.0f) sep = neg(sep);
+    /* the hull's faces (the hull projected first) */
+    for (f = 0; f < hB->numFaces; f++) {
+        v3 n = qrotq(qB, f4v(sh->faces[hB->faceOffset + f].plane));
+        if (dot(D, n) < 0.f) n = neg(n);
+        project(&sh->verts[hB->vertexOffset], hB->numVertices, posB, qB, n, &min0, &max0);
+        project_tri(tv, posA, qA, n, &min1, &max1);
+        if (max0 < min1 || max1 < min0) return 0;
+        d = (max0 - min1) < (max1 - min0) ? (max0 - min1) : (max1 - min0);
+        if (d < dmin) { dmin = d; sep = n; }
+    }
+    if (dot(neg(D), sep) > 0.0f) sep = neg(sep);
+    /* the edge pairs */
+    for (e0 = 0; e0 < 3; e0++) {
+        v3 w0 = qrotq(qA, te[e0]);
+        for (e1 = 0; e1 < hB->numUniqueEdges; e1++) {
+            v3 w1 = qrotq(qB, f4v(sh->edges[hB->uniqueEdgesOffset + e1]));
+            v3 cr = cross(w0, w1);
+            if ((double)fabsf(cr.x) > 1e-6 || (double)fabsf(cr.y) > 1e-6 || (double)fabsf(cr.z) > 1e-6) {
+                cr = nrm(cr);
+                if (dot(D, cr) < 0.f) cr = neg(cr);
+                project_tri(tv, posA, qA, cr, &min0, &max0);
+                project(&sh->verts[hB->vertexOffset], hB->numVertices, posB, qB, cr, &min1, &max1);
+                if (max0 < min1 || max1 < min0) return 0;
+                d = (max0 - min1) < (max1 - min0) ? (max0 - min1) : (max1 - min0);
+                if (d < dmin) { dmin = d; sep = cr; }
+            }
+        }
+    }
+    if (dot(neg(D), sep) > 0.0f) sep = neg(sep);
+    /* b3FindClippingFaces */
+    fb = -1;
+    dmax = -FLT_MAX;
+    for (f = 0; f < hB->numFaces; f++) {
+        float dd = dot(qrotq(qB, f4v(sh->faces[hB->faceOffset + f].plane)), sep);
+        if (dd > dmax) { dmax = dd; fb = f; }
+    }
+    if (fb < 0) return 0;
+    fa = -1;
+    {
+        float dmn = FLT_MAX;
+        for (f = 0; f < 5; f++) {
+            v3 wn = qrotq(qA, fn[f]);
+            float dd = dot(wn, sep);
+            if (dd < dmn) { dmn = dd; fa = f; nA = wn; }
+        }
+    }
+    if (fa < 0) return 0;
+    if (fa == 0) { ia[0] = 0; ia[1] = 1; ia[2] = 2; na = 3; }
+    else if (fa == 1) { ia[0] = 2; ia[1] = 1; ia[2] = 0; na = 3; }
+    else { i = fa - 2; ia[0] = i; ia[1] = i == 0 ? 2 : i - 1; na = 2; }
+    for (i = 0; i < na; i++) wA[i] = add(mmul(&RA, tv[ia[i]]), posA);
+    {
+        const oface* polyB = &sh->faces[hB->faceOffset + fb];
+        pin = buf0;
+        pout = buf1;
+        nin = 0;
+        for (i = 0; i < polyB->numIndices && i < CLIP_CAP; i++) {
+            v3 w = add(mmul(&RB, f4v(sh->verts[hB->vertexOffset + sh->indices[polyB->indexOffset + i]])), posB);
+            p4 q = {w.x, w.y, w.z, 0.f};
+            pin[nin++] = q;
+        }
+    }
+    /* clipFacesAndFindContactsKernel */
+    for (e0 = 0; e0 < na; e0++) {
+        v3 aw = wA[e0], bw = wA[(e0 + 1) % na];
+        v3 pn = neg(cross(sub(aw, bw), nA));
+        float eq = -dot(aw, pn);
+        int nout = clip_face_global(pin, nin, pn, eq, pout);
+        p4* t = pout;
+        pout = pin;
+        pin = t;
+        nin = nout;
+    }
+    {
+        float eqA = -dot(nA, wA[0]);
+        np = 0;
+        for (i = 0; i < nin; i++) {
+            float depth = dot(nA, mk(pin[i].x, pin[i].y, pin[i].z)) + eqA;
+            if (depth <= -1e30f) depth = -1e30f;
+            if (depth <= 0.02f) {
+                p4 q = {pin[i].x, pin[i].y, pin[i].z, depth};
+                pout[np++] = q;
+            }
+        }
+    }
+    if (np <= 0) return 0;
+    /* b3NewContactReductionKernel */
+    np = reduce_contacts(pout, np, neg(sep), idx);
+    write_header(c, bodies, cp->x, cp->y, sep, np, (unsigned short)(0.7f * 0xffff));
+    c->batchIdx = index;
+    for (k = 0; k < np; k++) {
+        p4 v = pout[idx[k]];
+        c->worldPosB[k].x = v.x; c->worldPosB[k].y = v.y; c->worldPosB[k].z = v.z; c->worldPosB[k].w = v.w;
+    }
+    return 1;
+}
+
+int oracle_concave_contacts(const obody* bodies, const oshapes* sh, const oaabb* aabbs, const opair* tri_pairs, int n,
+                            ocontact* out, int* out_index, int cap) {
+    int i, m = 0;
+    for (i = 0; i < n; i++) {
+        ocontact c;
+        memset(&c, 0, sizeof(c));
+        if (concave_tri(bodies, sh, aabbs, &tri_pairs[i], i, &c)) {
+            if (m < cap) { out[m] = c; if (out_index) out_index[m] = i; }
+            m++;
+        }
+    }
+    return m;
+}
+
 /* ------------------------------------------------------------------ solver */
 typedef struct {
     v3 n;

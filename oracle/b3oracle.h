@@ -90,6 +90,20 @@ int oracle_compound_pairs(const obody* bodies, const oshapes* sh, const opair* p
 int oracle_compound_contacts(const obody* bodies, const oshapes* sh, const opair* child_pairs, int n, ocontact* out,
                              int* out_index, int cap);
 
+/* Concave meshes (collidable shapeType 5: a shape record whose faces are the triangles, the
+ * collidable's numChildShapes = its BVH index).  Triangle-convex pairs (mesh body, other body,
+ * triangle, child shape of a compound or 0) of the pairs whose first body is a mesh and whose second
+ * a hull or a compound, in (pair, triangle, child) order: the triangles whose quantized leaf box
+ * overlaps the second body's quantized world AABB (b3BvhTraversal, shared/b3BvhTraversal.h:11-111).
+ * aabbs: the world AABBs by body.  Returns the count (only cap written). */
+int oracle_concave_pairs(const obody* bodies, const oshapes* sh, const oaabb* aabbs, const opair* pairs, int npairs,
+                         opair* out, int cap);
+/* One manifold or none per triangle-convex pair (b3FindConcaveSeparatingAxisKernel,
+ * b3FindClippingFaces, clipFacesAndFindContactsKernel, b3NewContactReductionKernel), in pair order;
+ * out_index[m] = the pair's index.  Returns the count. */
+int oracle_concave_contacts(const obody* bodies, const oshapes* sh, const oaabb* aabbs, const opair* tri_pairs, int n,
+                            ocontact* out, int* out_index, int cap);
+
 /* b3PgsJacobiSolver::solveGroup (Bullet3Dynamics/ConstraintSolver/b3PgsJacobiSolver.cpp:170)
  * with USE_2_FRICTION_DIRECTIONS, no warm start, no split impulse, erp, contact threshold.
  * mode 0 = PGS (usePgs=true, sequential row order), 1 = Jacobi (mass splitting), 2 = PGS with

@@ -181,6 +181,33 @@ def compound_contacts(bodies, shapes: Shapes, child_pairs):
     return out[:n].copy(), idx[:n].copy()
 
 
+def concave_pairs(bodies, shapes: Shapes, aabbs_, pairs):
+    """Triangle-convex pairs (mesh body, other body, triangle, child shape or 0) of the pairs whose
+    first body is a concave mesh, in (pair, triangle, child) order."""
+    b = np.ascontiguousarray(bodies, BODY)
+    a = np.ascontiguousarray(aabbs_, AABB)
+    pr = np.ascontiguousarray(pairs, PAIR)
+    sc = shapes.c()
+    lib = load_oracle()
+    n = lib.oracle_concave_pairs(_p(b), C.byref(sc), _p(a), _p(pr), C.c_int(len(pr)), None, C.c_int(0))
+    out = np.zeros(max(1, n), PAIR)
+    lib.oracle_concave_pairs(_p(b), C.byref(sc), _p(a), _p(pr), C.c_int(len(pr)), _p(out), C.c_int(len(out)))
+    return out[:n].copy()
+
+
+def concave_contacts(bodies, shapes: Shapes, aabbs_, tri_pairs):
+    """(manifolds, triangle-convex pair index of each) of the given triangle-convex pairs."""
+    b = np.ascontiguousarray(bodies, BODY)
+    a = np.ascontiguousarray(aabbs_, AABB)
+    tp = np.ascontiguousarray(tri_pairs, PAIR)
+    out = np.zeros(max(1, len(tp)), CONTACT)
+    idx = np.zeros(max(1, len(tp)), np.int32)
+    sc = shapes.c()
+    n = load_oracle().oracle_concave_contacts(_p(b), C.byref(sc), _p(a), _p(tp), C.c_int(len(tp)), _p(out), _p(idx),
+                                              C.c_int(len(out)))
+    return out[:n].copy(), idx[:n].copy()
+
+
 def contacts(bodies, shapes: Shapes, pairs, friction_cmp=45874):
     b = np.ascontiguousarray(bodies, BODY)
     pr = np.array(pairs, PAIR, copy=True)
@@ -402,6 +429,46 @@ def ref_plane_compound_contacts(bodies, shapes: Shapes, plane_body, compound_bod
     return out[:n].copy()
 
 
+def ref_concave_pairs(bodies, shapes: Shapes, aabbs_, pairs, mesh_verts, mesh_indices):
+    """The reference's registerConcaveMesh BVH (b3OptimizedBvh over the given unscaled mesh, with the
+    mesh collidable's local AABB) and b3BvhTraversal for every pair; the triangle-convex pairs in
+    the traversal's order."""
+    lib = load_reference()
+    b = np.ascontiguousarray(bodies, BODY)
+    a = np.ascontiguousarray(aabbs_, AABB)
+    pr = np.ascontiguousarray(pairs, PAIR)
+    v = np.ascontiguousarray(mesh_verts, np.float32).reshape(-1, 3)
+    ix = np.ascontiguousarray(mesh_indices, np.int32).reshape(-1)
+    mesh_col = [i for i, c in enumerate(shapes.collidables) if c["shapeType"] == 5]
+    if len(mesh_col) != 1:
+        raise ValueError("one concave mesh expected")
+    la = shapes.local_aabbs[mesh_col[0]]
+    mn = np.ascontiguousarray(la["min"], np.float32)
+    mx = np.ascontiguousarray(la["max"], np.float32)
+    cap = 64 * max(1, len(pr)) * 8
+    out = np.zeros(cap, PAIR)
+    n = lib.ref_concave_pairs(_p(v), C.c_int(len(v)), _p(ix), C.c_int(len(ix) // 3), _p(mn), _p(mx), _p(b),
+                              _p(shapes.collidables), _p(a), C.c_int(len(b)), _p(pr), C.c_int(len(pr)), _p(out),
+                              C.c_int(cap))
+    return out[:min(n, cap)].copy()
+
+
+def ref_concave_contacts(bodies, shapes: Shapes, aabbs_, tri_pairs):
+    """The reference's b3FindConcaveSeparatingAxisKernel, clipFacesAndFindContactsKernel and
+    b3NewContactReductionKernel (host twins) on the given triangle-convex pairs, in order:
+    (manifolds, pair index of each)."""
+    lib = load_reference()
+    b = np.ascontiguousarray(bodies, BODY)
+    a = np.ascontiguousarray(aabbs_, AABB)
+    tp = np.ascontiguousarray(tri_pairs, PAIR)
+    out = np.zeros(max(1, len(tp)), CONTACT)
+    idx = np.zeros(max(1, len(tp)), np.int32)
+    n = lib.ref_concave_contacts(_p(b), _p(shapes.collidables), _p(shapes.hulls), _p(shapes.faces),
+                                 _p(shapes.indices), _p(shapes.verts), _p(shapes.edges), _p(shapes.children), _p(a),
+                                 C.c_int(len(b)), _p(tp), C.c_int(len(tp)), _p(out), _p(idx), C.c_int(len(out)))
+    return out[:n].copy(), idx[:n].copy()
+
+
 def ref_solve(bodies, inertias, contacts_, use_pgs=True, iterations=10, dt=1 / 60):
     lib = load_reference()
     b = np.array(bodies, BODY, copy=True)
@@ -498,6 +565,42 @@ class Registry:
         self.indices, self.verts, self.edges = [], [], []
         self.bodies, self.inertias = [], []
         self.children = []
+        self.num_meshes = 0
+
+    def concave_mesh(self, vertices, indices, scaling=(1.0, 1.0, 1.0)):
+        """registerConcaveMesh + registerConcaveMeshShape (b3GpuNarrowPhase.cpp:521-667): the scaled
+        vertices, one face per triangle (plane = normalised (v1 - v0) x (v2 - v0), w = -n.v0, float32
+        throughout), the local AABB over the scaled vertices; the collidable's numChildShapes is the
+        mesh's BVH index."""
+        f32 = np.float32
+        v = (np.asarray(vertices, f32).reshape(-1, 3) * np.asarray(scaling, f32)).astype(f32)
+        tri = np.asarray(indices, np.int32).reshape(-1, 3)
+        h = np.zeros(1, HULL)[0]
+        h["uniqueEdgesOffset"], h["numUniqueEdges"] = len(self.edges), 0
+        h["faceOffset"], h["numFaces"] = len(self.faces), len(tri)
+        for t in tri:
+            a, b, c = v[t[0]], v[t[1]], v[t[2]]
+            e1, e2 = b - a, c - a
+            n = np.array([e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                          e1[0] * e2[1] - e1[1] * e2[0]], f32)
+            inv = f32(1.0) / np.sqrt(f32(n[0] * n[0] + n[1] * n[1]) + f32(n[2] * n[2]))
+            n = (n * inv).astype(f32)
+            f = np.zeros(1, FACE)[0]
+            f["plane"] = [n[0], n[1], n[2], -(f32(f32(n[0] * a[0] + n[1] * a[1]) + f32(n[2] * a[2])))]
+            f["indexOffset"], f["numIndices"] = len(self.indices), 3
+            self.indices.extend(int(x) for x in t)
+            self.faces.append(f)
+        h["vertexOffset"], h["numVertices"] = len(self.verts), len(v)
+        self.verts.extend(np.concatenate([v, np.zeros((len(v), 1), f32)], 1))
+        self.hull_recs.append(h)
+        col = np.zeros(1, COLLIDABLE)[0]
+        col["shapeType"], col["shapeIndex"], col["numChildShapes"] = 5, len(self.hull_recs) - 1, self.num_meshes
+        self.num_meshes += 1
+        a = np.zeros(1, AABB)[0]
+        a["min"], a["max"] = v.min(0), v.max(0)
+        self.cols.append(col)
+        self.laabbs.append(a)
+        return len(self.cols) - 1
 
     def plane(self, normal, constant):
         f = np.zeros(1, FACE)[0]
@@ -609,6 +712,8 @@ def register_scene(scene) -> dict:
         elif s["type"] == "compound":
             # children: (index of an earlier shape of the scene, position, orientation)
             col.append(reg.compound([(col[i], p, q) for i, p, q in s["children"]]))
+        elif s["type"] == "mesh":
+            col.append(reg.concave_mesh(s["verts"], s["indices"], s.get("scaling", (1.0, 1.0, 1.0))))
         else:
             raise ValueError(s["type"])
     for i in range(len(scene.mass)):

@@ -17,6 +17,9 @@
 //     through b3PgsJacobiSolver::solveGroup         (joints only, no contacts)
 //   processCompoundPairsKernel + clipCompoundsHullHullKernel, computeContactPlaneCompound
 //                                                   Bullet3OpenCL/NarrowphaseCollision/b3ConvexHullContact.cpp:1777-2022, :2182
+//   registerConcaveMesh's BVH (b3OptimizedBvh)      Bullet3OpenCL/RigidBody/b3GpuNarrowPhase.cpp:521-613
+//   b3BvhTraversal, b3FindConcaveSeparatingAxisKernel, clipFacesAndFindContactsKernel,
+//   b3NewContactReductionKernel                     Bullet3Collision/NarrowPhaseCollision/shared/ (host twins)
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -37,6 +40,9 @@
 #include "Bullet3Collision/NarrowPhaseCollision/shared/b3ConvexPolyhedronData.h"
 #include "Bullet3Collision/NarrowPhaseCollision/shared/b3ContactConvexConvexSAT.h"
 #include "Bullet3Dynamics/ConstraintSolver/b3PgsJacobiSolver.h"
+#include "Bullet3OpenCL/NarrowphaseCollision/b3BvhInfo.h"
+#include "Bullet3OpenCL/NarrowphaseCollision/b3OptimizedBvh.h"
+#include "Bullet3OpenCL/NarrowphaseCollision/b3TriangleIndexVertexArray.h"
 #include "Bullet3Dynamics/ConstraintSolver/b3ContactSolverInfo.h"
 #include "Bullet3Dynamics/ConstraintSolver/b3Point2PointConstraint.h"
 #include "Bullet3Dynamics/ConstraintSolver/b3FixedConstraint.h"
@@ -81,7 +87,113 @@ void computeContactPlaneCompound(int pairIndex, int bodyIndexA, int bodyIndexB, 
                                  const int* convexIndices, const b3GpuFace* faces, b3Contact4* globalContactsOut,
                                  int& nGlobalContactsOut, int maxContactCapacity);
 
+// host twins of the concave kernels (shared headers, compiled into b3ConvexHullContact.cpp)
+void b3BvhTraversal(const b3Int4* pairs, const b3RigidBodyData* rigidBodies, const b3Collidable* collidables,
+                    b3Aabb* aabbs, b3Int4* concavePairsOut, volatile int* numConcavePairsOut,
+                    const b3BvhSubtreeInfo* subtreeHeadersRoot, const b3QuantizedBvhNode* quantizedNodesRoot,
+                    const b3BvhInfo* bvhInfos, int numPairs, int maxNumConcavePairsCapacity, int id);
+void b3FindConcaveSeparatingAxisKernel(b3Int4* concavePairs, const b3RigidBodyData* rigidBodies,
+                                       const b3Collidable* collidables, const b3ConvexPolyhedronData* convexShapes,
+                                       const b3Vector3* vertices, const b3Vector3* uniqueEdges, const b3GpuFace* faces,
+                                       const int* indices, const b3GpuChildShape* gpuChildShapes, b3Aabb* aabbs,
+                                       b3Vector3* concaveSeparatingNormalsOut, b3Int4* clippingFacesOut,
+                                       b3Vector3* worldVertsA1Out, b3Vector3* worldNormalsA1Out,
+                                       b3Vector3* worldVertsB1Out, int* hasSeparatingNormals, int vertexFaceCapacity,
+                                       int numConcavePairs, int pairIdx);
+void clipFacesAndFindContactsKernel(const b3Vector3* separatingNormals, const int* hasSeparatingAxis,
+                                    b3Int4* clippingFacesOut, b3Vector3* worldVertsA1, b3Vector3* worldNormalsA1,
+                                    b3Vector3* worldVertsB1, b3Vector3* worldVertsB2, int vertexFaceCapacity,
+                                    int pairIndex);
+void b3NewContactReductionKernel(b3Int4* pairs, const b3RigidBodyData* rigidBodies,
+                                 const b3Vector3* separatingNormals, const int* hasSeparatingAxis,
+                                 b3Contact4Data* globalContactsOut, b3Int4* clippingFaces, b3Vector3* worldVertsB2,
+                                 volatile int* nGlobalContactsOut, int vertexFaceCapacity, int contactCapacity,
+                                 int numPairs, int pairIndex);
+
 extern "C" {
+
+// registerConcaveMesh's BVH for one mesh (b3GpuNarrowPhase.cpp:556-610: b3OptimizedBvh::build over
+// the unscaled vertices with quantized AABB compression and the mesh's local AABB), then
+// b3BvhTraversal for every pair.  The collidable of the mesh must carry BVH index 0.  Writes the
+// triangle-convex pairs (int4: bodyA, bodyB, triangle, child or 0) in the traversal's order;
+// returns their count (only cap written).
+int ref_concave_pairs(const float* mesh_verts, int nverts, const int* mesh_indices, int ntris, const float* aabb_min,
+                      const float* aabb_max, const b3RigidBodyData* bodies, const b3Collidable* cols,
+                      const b3Aabb* aabbs, int nbodies, const int* pairs, int npairs, int* out, int cap) {
+    b3AlignedObjectArray<b3Vector3> V;
+    V.resize(nverts);
+    for (int i = 0; i < nverts; i++) V[i] = b3MakeVector3(mesh_verts[3 * i], mesh_verts[3 * i + 1], mesh_verts[3 * i + 2]);
+    b3AlignedObjectArray<int> I;
+    I.resize(3 * ntris);
+    for (int i = 0; i < 3 * ntris; i++) I[i] = mesh_indices[i];
+    b3TriangleIndexVertexArray meshInterface;
+    b3IndexedMesh mesh;
+    mesh.m_numTriangles = ntris;
+    mesh.m_numVertices = nverts;
+    mesh.m_vertexBase = (const unsigned char*)&V.at(0).x;
+    mesh.m_vertexStride = sizeof(b3Vector3);
+    mesh.m_triangleIndexStride = 3 * sizeof(int);
+    mesh.m_triangleIndexBase = (const unsigned char*)&I.at(0);
+    meshInterface.addIndexedMesh(mesh);
+    b3OptimizedBvh bvh;
+    const b3Vector3 mn = b3MakeVector3(aabb_min[0], aabb_min[1], aabb_min[2]);
+    const b3Vector3 mx = b3MakeVector3(aabb_max[0], aabb_max[1], aabb_max[2]);
+    bvh.build(&meshInterface, true, mn, mx);
+    b3BvhInfo info;
+    info.m_aabbMin = bvh.m_bvhAabbMin;
+    info.m_aabbMax = bvh.m_bvhAabbMax;
+    info.m_quantization = bvh.m_bvhQuantization;
+    info.m_numNodes = bvh.getQuantizedNodeArray().size();
+    info.m_numSubTrees = bvh.getSubtreeInfoArray().size();
+    info.m_nodeOffset = 0;
+    info.m_subTreeOffset = 0;
+    std::vector<b3Aabb> A(aabbs, aabbs + nbodies);
+    std::vector<b3Int4> outv(cap > 0 ? cap : 1);
+    volatile int n = 0;
+    const b3Int4* P = reinterpret_cast<const b3Int4*>(pairs);
+    for (int i = 0; i < npairs; i++)
+        b3BvhTraversal(P, bodies, cols, A.data(), outv.data(), &n, &bvh.getSubtreeInfoArray()[0],
+                       &bvh.getQuantizedNodeArray()[0], &info, npairs, cap, i);
+    for (int i = 0; i < n && i < cap; i++) memcpy(&out[4 * i], &outv[i], sizeof(b3Int4));
+    return n;
+}
+
+// b3FindConcaveSeparatingAxisKernel, clipFacesAndFindContactsKernel and b3NewContactReductionKernel
+// for every triangle-convex pair in order (vertexFaceCapacity 64, as the pipeline allocates);
+// out_index[m] = the pair's index.  Returns the manifold count.
+int ref_concave_contacts(const b3RigidBodyData* bodies, const b3Collidable* cols, const b3ConvexPolyhedronData* hulls,
+                         const b3GpuFace* faces, const int* indices, const b3Vector3* verts, const b3Vector3* edges,
+                         const b3GpuChildShape* children, const b3Aabb* aabbs, int nbodies, const int* tri_pairs, int n,
+                         b3Contact4Data* out, int* out_index, int cap) {
+    const int capv = 64;
+    const int m = n > 0 ? n : 1;
+    std::vector<b3Int4> tp(m);
+    memcpy(tp.data(), tri_pairs, sizeof(b3Int4) * n);
+    std::vector<b3Aabb> A(aabbs, aabbs + nbodies);
+    std::vector<b3Vector3> sep(m), wA1((size_t)m * capv), nA1(m), wB1((size_t)m * capv), wB2((size_t)m * capv);
+    std::vector<b3Int4> clip(m);
+    std::vector<int> has(m, 0);
+    std::vector<b3Contact4Data> tmp(m);
+    memset(tmp.data(), 0, sizeof(b3Contact4Data) * m);
+    volatile int nc = 0;
+    int k = 0;
+    for (int i = 0; i < n; i++) {
+        b3FindConcaveSeparatingAxisKernel(tp.data(), bodies, cols, hulls, verts, edges, faces, indices, children,
+                                          A.data(), sep.data(), clip.data(), wA1.data(), nA1.data(), wB1.data(),
+                                          has.data(), capv, n, i);
+        clipFacesAndFindContactsKernel(sep.data(), has.data(), clip.data(), wA1.data(), nA1.data(), wB1.data(),
+                                       wB2.data(), capv, i);
+        const int before = nc;
+        b3NewContactReductionKernel(tp.data(), bodies, sep.data(), has.data(), tmp.data(), clip.data(), wB2.data(),
+                                    &nc, capv, m, n, i);
+        if (nc > before && k < cap) {
+            out[k] = tmp[before];
+            out_index[k] = i;
+            k++;
+        }
+    }
+    return k;
+}
 
 // The reference's compound kernels (host twins), one child pair at a time, on the given child pairs
 // (int4: bodyA, bodyB, child shape of A or -1, child shape of B or -1; both sides convex hulls):

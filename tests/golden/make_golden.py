@@ -464,6 +464,30 @@ def compound_fixture():
     print("compound", len(cp), "child pairs,", len(ref), "hull manifolds,", len(out["plane_contacts"]), "plane manifolds")
 
 
+def concave_fixture():
+    """concave.npz: the reference's concave-mesh path on a height-field mesh (scenes.terrain_mesh,
+    24 x 24 quads) under 300 boxes, Gaussian hulls and compounds touching it: the BVH of
+    registerConcaveMesh (b3OptimizedBvh) with b3BvhTraversal gives the triangle-convex pairs, the
+    host twins b3FindConcaveSeparatingAxisKernel / clipFacesAndFindContactsKernel /
+    b3NewContactReductionKernel give the manifolds."""
+    from bullet3_gb300 import scenes
+    sc = scenes.terrain_scene(300, grid=24, seed=21)
+    t = O.register_scene(sc)
+    shapes = O.Shapes.from_tables(t)
+    bodies = t["bodies"]
+    aabbs = O.aabbs(bodies, shapes)
+    pairs = O.pairs_bruteforce(aabbs)
+    rp = O.ref_concave_pairs(bodies, shapes, aabbs, pairs, sc.shapes[0]["verts"], sc.shapes[0]["indices"])
+    rp = rp[np.lexsort((rp["w"], rp["z"], rp["y"], rp["x"]))]
+    ref, ridx = O.ref_concave_contacts(bodies, shapes, aabbs, rp)
+    out = dict(bodies=bodies, pairs=pairs, aabbs=aabbs, tri_pairs=rp, contacts=ref, contact_pair=ridx,
+               mesh_verts=sc.shapes[0]["verts"], mesh_indices=sc.shapes[0]["indices"])
+    for k in ("collidables", "local_aabbs", "hulls", "faces", "indices", "verts", "edges", "children"):
+        out["shape_" + k] = t[k]
+    np.savez_compressed(OUT / "concave.npz", **out)
+    print("concave", len(rp), "triangle-convex pairs,", len(ref), "manifolds")
+
+
 if __name__ == "__main__":
     if O.load_reference() is None:
         raise SystemExit("oracle/_ref/libb3ref.so is missing: run oracle/build_ref.sh first")
@@ -475,10 +499,13 @@ if __name__ == "__main__":
         joints_fixture()
     elif len(sys.argv) > 1 and sys.argv[1] == "compound":
         compound_fixture()
+    elif len(sys.argv) > 1 and sys.argv[1] == "concave":
+        concave_fixture()
     else:
         main()
         registration_fixture()
         rays_fixture()
         joints_fixture()
         compound_fixture()
+        concave_fixture()
         joints_fixture()

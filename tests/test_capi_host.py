@@ -42,7 +42,7 @@ def test_registration_errors_match_reference_conventions():
     assert pl.registerPhysicsInstance(1.0, (0, 0, 0), (0, 0, 0, 1), s) == 0
     assert pl.registerPhysicsInstance(0.0, (0, 0, 0), (0, 0, 0, 1), 1) == 1
     assert pl.registerPhysicsInstance(1.0, (0, 0, 0), (0, 0, 0, 1), s) == -1  # body capacity
-    assert np_.registerCompoundShape([]) == -1 and np_.registerConcaveMesh(None, None, None) == -1
+    assert np_.registerCompoundShape([]) == -1 and np_.registerConcaveMesh(None, None) == -1
     with pytest.raises(capi.B3GError):
         capi.call("b3g_step", C.c_void_p(None), C.c_float(1 / 60))
     with pytest.raises(capi.B3GError) as e:
@@ -67,6 +67,75 @@ def test_compound_registration_matches_the_oracle_registry():
     # a child that is not a convex hull is refused (-1 + b3Error), the table left unchanged
     assert np_.registerCompoundShape([(0, (0, 0, 0), (0, 0, 0, 1))]) == -1  # collidable 0 is the plane
     assert np_.getNumCollidablesGpu() == len(t["collidables"])
+
+
+def test_concave_mesh_registration_and_bvh():
+    # registerConcaveMesh: the collidable (type 5, BVH index), one face per triangle with the
+    # reference's plane (normalised (v1 - v0) x (v2 - v0), w = -n.v0), the scaled vertices and the
+    # local AABB, bit-exact with the oracle's registry; the BVH holds every triangle once as a leaf,
+    # in index order depth first, inside the mesh's quantization bounds, and a walk of it finds the
+    # oracle's triangle-convex pairs (the reference's traversal on the same leaf boxes)
+    from bullet3_gb300 import scenes
+    from oracle import oracle as O
+    sc = scenes.terrain_scene(200, grid=16, seed=4)
+    np_, bp, pl = scenes.load_scene(sc, b3Config(use_cuda_graph=False), upload=False)
+    t = scenes.registered_tables(np_)
+    ref = O.register_scene(sc)
+    for k in ("collidables", "local_aabbs", "hulls", "faces", "indices", "verts"):
+        assert np.array_equal(t[k].view(np.uint8), ref[k].view(np.uint8)), k
+    ni, nn = C.c_int(), C.c_int()
+    capi.call("b3g_read_mesh_bvh", np_.world.handle, None, C.c_int(0), None, C.c_int(0), C.byref(ni), C.byref(nn))
+    infos = np.zeros(ni.value, capi.BVHINFO)
+    nodes = np.zeros(nn.value, capi.BVHNODE)
+    capi.call("b3g_read_mesh_bvh", np_.world.handle, capi.ptr(infos), C.c_int(ni.value), capi.ptr(nodes),
+              C.c_int(nn.value), C.byref(ni), C.byref(nn))
+    assert ni.value == 1 and infos[0]["numTriangles"] == 2 * 16 * 16 and infos[0]["numNodes"] == 2 * 512 - 1
+    la = t["local_aabbs"][0]
+    f32 = np.float32
+    assert np.array_equal(infos[0]["aabbMin"][:3], (la["min"] - f32(1)).astype(f32))
+    assert np.array_equal(infos[0]["quantization"][:3],
+                          (f32(65533) / (infos[0]["aabbMax"][:3] - infos[0]["aabbMin"][:3])).astype(f32))
+    leaves = nodes["escapeOrTriangle"][nodes["escapeOrTriangle"] >= 0]
+    assert np.array_equal(leaves, np.arange(512))
+
+    def walk(qmin, qmax):
+        out, cur = [], 0
+        while cur < len(nodes):
+            n = nodes[cur]
+            ov = not ((qmin > n["qmax"]).any() or (qmax < n["qmin"]).any())
+            e = int(n["escapeOrTriangle"])
+            if ov and e >= 0:
+                out.append(e)
+            cur += 1 if (ov or e >= 0) else -e
+        return out
+
+    b = ref["bodies"]
+    sh = O.Shapes.from_tables(ref)
+    aabbs = O.aabbs(b, sh)
+    pairs = O.pairs_bruteforce(aabbs)
+    want = O.concave_pairs(b, sh, aabbs, pairs)
+    info = infos[0]
+
+    def quant(p, is_max):
+        c = np.minimum(np.maximum(p.astype(f32), info["aabbMin"][:3]), info["aabbMax"][:3])
+        v = ((c - info["aabbMin"][:3]) * info["quantization"][:3]).astype(f32)
+        return ((v + f32(1)).astype(np.uint16) | 1) if is_max else (v.astype(np.uint16) & 0xfffe)
+
+    got = []
+    for p in pairs:
+        x, y = int(p["x"]), int(p["y"])
+        if x != 0 or b[y]["invMass"] == 0:
+            continue
+        col = t["collidables"][b[y]["collidableIdx"]]
+        nch = int(col["numChildShapes"]) if col["shapeType"] == capi.SHAPE_COMPOUND else 1
+        for tri in walk(quant(aabbs[y]["min"], False), quant(aabbs[y]["max"], True)):
+            for c in range(nch):
+                got.append((x, y, tri, int(col["shapeIndex"]) + c if col["shapeType"] == capi.SHAPE_COMPOUND else 0))
+    assert len(want) > 500
+    assert np.array_equal(np.array(got, np.int32).reshape(-1, 4), want.view(np.int32).reshape(-1, 4))
+    # invalid input: -1 + b3Error, as the reference's registration reports it
+    assert np_.registerConcaveMesh(np.zeros((3, 3), np.float32), [0, 1, 5]) == -1
+    assert np_.registerConcaveMesh(None, None) == -1
 
 
 def test_config_validation():

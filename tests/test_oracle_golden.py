@@ -227,3 +227,27 @@ def test_plane_compound_contacts_match_reference():
         assert len(m) == len(r)
         for mc, rc in zip(m, r):
             assert _manifold_equal(mc, rc)
+
+
+def test_concave_pairs_match_reference_traversal():
+    # registerConcaveMesh's BVH (b3OptimizedBvh with quantized AABBs) walked by the reference's
+    # b3BvhTraversal gives these triangle-convex pairs (sorted); the oracle's quantized leaf test
+    # over every triangle finds exactly the same set, in (pair, triangle, child) order
+    d = load_golden("concave")
+    sh = shapes_from(d)
+    cp = O.concave_pairs(d["bodies"], sh, d["aabbs"], d["pairs"])
+    assert len(cp) > 5000
+    assert np.array_equal(cp.view(np.int32), d["tri_pairs"].view(np.int32))
+
+
+def test_concave_contacts_match_reference_kernels():
+    # b3FindConcaveSeparatingAxisKernel, clipFacesAndFindContactsKernel and
+    # b3NewContactReductionKernel (the reference's host twins) give these manifolds, one per
+    # touching triangle (and child); the oracle's records equal them byte for byte
+    d = load_golden("concave")
+    sh = shapes_from(d)
+    mine, idx = O.concave_contacts(d["bodies"], sh, d["aabbs"], d["tri_pairs"])
+    assert len(mine) > 500
+    assert np.array_equal(idx, d["contact_pair"])
+    assert np.array_equal(mine.view(np.uint8), d["contacts"].view(np.uint8))
+    assert (mine["childA"] == -1).all() and (mine["childB"] == -1).all()
