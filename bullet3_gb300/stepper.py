@@ -3,7 +3,7 @@
 Meant for running the pipeline under an external profiler (ncu) or by hand: nothing but the
 scene upload, the warm-up steps and the measured steps touch the GPU.
 
-    python -m bullet3_gb300.stepper [--workload pile|lattice|batched|mixed|stress|chains|compound] [--settle S]
+    python -m bullet3_gb300.stepper [--workload pile|lattice|batched|mixed|stress|chains|compound|terrain] [--settle S]
                                     [--steps K] [--warmup W] [--solver pgs|jacobi] [--iterations I]
                                     [--autotune] [--broadphase grid|lbvh] [--stage-times] [--profile-range]
 
@@ -19,6 +19,8 @@ with profiling off (ncu --profile-from-start off --clock-control none); --settle
            hanging from one static box in a 3 m grid, swinging
   compound 131,072 bodies (2,048 x nx) on a plane: compounds of convex hulls (an L of two boxes, a
            dumbbell of two hulls and a box) among single boxes and hulls, dropped as a lattice from rest
+  terrain  32,768 bodies (512 x nx) of the same four kinds dropped as a lattice onto a static
+           256 x 256-quad height-field mesh (131,072 triangles)
 """
 from __future__ import annotations
 
@@ -46,12 +48,14 @@ def make(workload: str, n: int = 64):
                                      per_row=91)
     if workload == "compound":
         return scenes.compound_scene(2048 * n, seed=0, lattice=True)
+    if workload == "terrain":
+        return scenes.terrain_scene(512 * n, grid=256, seed=0, drop=True)
     raise ValueError(workload)
 
 
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("--workload", choices=["pile", "lattice", "batched", "mixed", "stress", "chains", "compound"],
+    p.add_argument("--workload", choices=["pile", "lattice", "batched", "mixed", "stress", "chains", "compound", "terrain"],
                    default="pile")
     p.add_argument("--settle", type=int, default=0)
     p.add_argument("--profile-range", action="store_true")
@@ -77,6 +81,8 @@ def main(argv=None):
                    broadphase={"grid": capi.BROADPHASE_GRID, "lbvh": capi.BROADPHASE_LBVH,
                                "auto": capi.BROADPHASE_AUTO}[a.broadphase],
                    pgs_flow=a.pgs_flow, pgs_tail_manifolds=a.pgs_tail)
+    if a.workload == "terrain":
+        cfg.m_maxTriConvexPairCapacity = 64 * sc.num_bodies  # about 30 triangle-convex pairs a body at rest
     np_, bp, pl = scenes.load_scene(sc, cfg)
     dt = 1.0 / 60.0
     for _ in range(a.settle):
@@ -154,7 +160,7 @@ def main(argv=None):
                       "joints": pl.getNumConstraints(), "stage_ms": stage_ms,
                       "host_ms_per_step": 1000 * secs / max(a.steps, 1), "pairs": st.num_pairs,
                       "manifolds": st.num_contacts, "points": st.num_points, "colors": st.num_colors,
-                      "child_pairs": st.num_child_pairs,
+                      "child_pairs": st.num_child_pairs, "concave_pairs": st.num_concave_pairs,
                       "status": int(pl.status()), "tuning": tuning}))
     return 0 if pl.status() == 0 else 1
 

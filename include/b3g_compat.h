@@ -200,6 +200,7 @@ inline b3gConfig b3gConfigFrom(const b3Config& c) {
     out.max_pairs = c.m_maxBroadphasePairs;
     out.max_contacts = c.m_maxContactCapacity;
     out.max_compound_child_pairs = c.m_compoundPairCapacity;
+    out.max_concave_pairs = c.m_maxTriConvexPairCapacity;
     return out;
 }
 
@@ -233,10 +234,18 @@ public:
                                          childShapes->size(), &m_out),
                    "registerCompoundShape");
     }
-    int registerConcaveMesh(b3AlignedObjectArray<b3Vector3>* /*vertices*/, b3AlignedObjectArray<int>* /*indices*/,
-                            const float* /*scaling*/) {
-        std::fprintf(stderr, "b3Error: registerConcaveMesh: concave meshes are not supported\n");
-        return -1;
+    /* registerConcaveMesh (b3GpuNarrowPhase.cpp:521-613): a static triangle mesh (3 indices per
+       triangle) with a quantized triangle BVH; meant to stay at the identity pose, as in the reference */
+    int registerConcaveMesh(b3AlignedObjectArray<b3Vector3>* vertices, b3AlignedObjectArray<int>* indices,
+                            const float* scaling) {
+        if (!vertices || !indices || vertices->size() == 0 || indices->size() < 3) {
+            std::fprintf(stderr, "b3Error: registerConcaveMesh: no vertices or triangles\n");
+            return -1;
+        }
+        const float one[3] = {1.f, 1.f, 1.f};
+        return reg(b3g_register_concave_mesh(m_world, vertices->at(0).m_floats, (int)sizeof(b3Vector3), vertices->size(),
+                                             &indices->at(0), indices->size() / 3, scaling ? scaling : one, &m_out),
+                   "registerConcaveMesh");
     }
     /* registerConvexHullShape(b3ConvexUtility*) (b3GpuNarrowPhase.cpp:322-368): the utility's tables
        as they are, with the vertex mean as local centre */

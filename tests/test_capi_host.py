@@ -258,6 +258,8 @@ def test_cpp_dropin_header_compiles(tmp_path):
                    "  ch.m_childPosition = b3MakeVector3(0.5f, 0, 0); ch.m_childOrientation = b3Quaternion(0, 0, 0, 1);\n"
                    "  ch.m_shapeIndex = 1; ch.m_numChildShapes = 0; ch.m_collidableShapeIndex = 0; ch.m_shapeType = 3;\n"
                    "  kids.push_back(ch); np.registerCompoundShape(&kids);\n"
+                   "  b3AlignedObjectArray<int> tri; tri.push_back(0); tri.push_back(0); tri.push_back(0);\n"
+                   "  float one[3] = {1.f, 1.f, 1.f}; np.registerConcaveMesh(&v, &tri, one);\n"
                    "  bp.calculateOverlappingPairsHost(0); bp.getAllAabbsCPU(); rbp.copyConstraintsToHost();\n"
                    "  b3OpenCLArray<b3Int4>& pairs = bp.getOverlappingPairsGPU();\n"
                    "  np.computeContacts(pairs.getBufferCL(), (int)pairs.size(), bp.getAabbBufferWS(), 0);\n"
