@@ -19,6 +19,7 @@
 
 #include "b3g_capi.h"
 #include "mlp.h"
+#include "warmstart.h"
 
 namespace b3g {
 namespace mlp {
@@ -237,8 +238,137 @@ __global__ void __launch_bounds__(GT) k_gemm(GemmArgs g) {
 
 size_t gemm_smem_bytes(int N) { return (size_t)128 * KC * 2 + (size_t)N * KC * 2; }
 
+// ---------------------------------------------------------------------------- fused inference
+// Shared memory (chunk layout of load_chunk, every chunk 1 KB aligned): W1 (128 x 16, one chunk),
+// W2 and W3 (128 x 128, two chunks each), W4 (16 x 128, two 16-row chunks), the tile's inputs
+// (128 x 16, one chunk) and its activations (128 x 128, two chunks), 132 KB.
+static constexpr int FIN = 16, FOUT = 16, HID = 128;
+static constexpr size_t CH128 = 128 * KC * 2;  // a 128-row chunk: 16 KB
+static constexpr size_t CH16 = 16 * KC * 2;    // a 16-row chunk: 2 KB
+static constexpr size_t S_W1 = 0, S_W2 = S_W1 + CH128, S_W3 = S_W2 + 2 * CH128, S_W4 = S_W3 + 2 * CH128;
+static constexpr size_t S_X = S_W4 + 2 * CH16, S_H = S_X + CH128, S_END = S_H + 2 * CH128;
+
+// thread t's row of 16 values (bf16) at columns n0..n0+15 of a 128-row, K-chunked operand
+__device__ __forceinline__ void put_row16(char* base, int r, int n0, const float* v) {
+    uint32_t w[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+        w[i] = *reinterpret_cast<const uint32_t*>(&h);
+    }
+    char* chunk = base + (size_t)(n0 / KC) * CH128;
+    const int k = n0 % KC;
+    char* row = chunk + (r & 7) * 16 + (r >> 3) * SBO;
+    *reinterpret_cast<uint4*>(row + (k / 8) * LBO) = make_uint4(w[0], w[1], w[2], w[3]);
+    *reinterpret_cast<uint4*>(row + (k / 8 + 1) * LBO) = make_uint4(w[4], w[5], w[6], w[7]);
+}
+
+__global__ void __launch_bounds__(GT, 1) k_mlp_infer(InferArgs a) {
+    extern __shared__ __align__(1024) char smem[];
+    __shared__ unsigned long long bar;
+    __shared__ uint32_t tslot;
+    const int rows = min(*a.d_rows, a.rows_cap);
+    const int m_tiles = (rows + 127) / 128;
+    if ((int)blockIdx.x >= m_tiles) return;  // block-uniform, before any barrier or TMEM use
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    if (threadIdx.x < 32) tmem_alloc(&tslot, HID);
+    load_chunk(smem + S_W1, a.wt1, FIN, 0, HID, HID, 0, FIN);
+    for (int c = 0; c < 2; c++) {
+        load_chunk(smem + S_W2 + c * CH128, a.wt2, HID, 0, HID, HID, c * KC, HID);
+        load_chunk(smem + S_W3 + c * CH128, a.wt3, HID, 0, HID, HID, c * KC, HID);
+        load_chunk(smem + S_W4 + c * CH16, a.wt4, HID, 0, FOUT, FOUT, c * KC, HID);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tslot;
+    const uint32_t trow = tmem + ((uint32_t)(threadIdx.x & ~31) << 16);
+    const int t = threadIdx.x;
+    unsigned phase = 0;
+    bool failed = false;
+    // one layer: `steps` MMAs of K = 16 over `chunks` K-chunks of A at sA and B at sB; returns false
+    // when the wait gave up (the status flag is set and the MMAs drained)
+    auto layer = [&](uint32_t sA, uint32_t sB, size_t b_chunk, int chunks, int steps, uint32_t idesc) -> bool {
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (t == 0) {
+            for (int c = 0; c < chunks; c++)
+                for (int s = 0; s < steps; s++) {
+                    const uint64_t ad = smem_desc(sA + (uint32_t)(c * CH128) + s * 2 * LBO);
+                    const uint64_t bd = smem_desc(sB + (uint32_t)(c * b_chunk) + s * 2 * LBO);
+                    mma_bf16(tmem, ad, bd, idesc, (c > 0 || s > 0) ? 1u : 0u);
+                }
+            mma_commit(&bar);
+        }
+        const bool ok = mbar_wait(&bar, phase);
+        phase ^= 1u;
+        if (__syncthreads_or(!ok)) {
+            if (t == 0) {
+                if (a.status) atomicOr(a.status, B3G_FLAG_MLP_TIMEOUT);
+                mbar_wait(&bar, phase ^ 1u);
+            }
+            return false;
+        }
+        tc_fence_after();
+        return true;
+    };
+    const uint32_t sX = smem_u32(smem + S_X), sH = smem_u32(smem + S_H);
+    for (int tile = blockIdx.x; tile < m_tiles && !failed; tile += gridDim.x) {
+        const int r = tile * 128 + t;
+        {
+            // the normalised features of row r (k_pack's arithmetic), zero past the rows
+            float v[16];
+#pragma unroll
+            for (int f = 0; f < 16; f++)
+                v[f] = (r < rows && f < WS_FEATURES) ? (a.x[(size_t)r * a.ld_x + f] - a.norm[f]) * a.norm[WS_FEATURES + f]
+                                                       : 0.f;
+            put_row16(smem + S_X, t, 0, v);
+        }
+        const float* bias[3] = {a.b1, a.b2, a.b3};
+        for (int l = 0; l < 3 && !failed; l++) {
+            const bool ok = l == 0 ? layer(sX, smem_u32(smem + S_W1), CH128, 1, 1, instr_desc(HID))
+                                   : layer(sH, smem_u32(smem + (l == 1 ? S_W2 : S_W3)), CH128, 2, KC / 16,
+                                           instr_desc(HID));
+            if (!ok) { failed = true; break; }
+            for (int n0 = 0; n0 < HID; n0 += 16) {
+                float v[16];
+                tmem_ld16(trow + n0, v);
+#pragma unroll
+                for (int i = 0; i < 16; i++) v[i] = gelu(v[i] + bias[l][n0 + i]);
+                put_row16(smem + S_H, t, n0, v);
+            }
+            tc_fence_before();  // TMEM reads done before the next layer's MMAs overwrite it
+        }
+        if (failed) break;
+        if (!layer(sH, smem_u32(smem + S_W4), CH16, 2, KC / 16, instr_desc(FOUT))) { failed = true; break; }
+        {
+            float v[16];
+            tmem_ld16(trow, v);
+            if (r < rows) {
+                float4* out = reinterpret_cast<float4*>(a.y + (size_t)r * FOUT);
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    out[q] = make_float4(v[4 * q] + a.b4[4 * q], v[4 * q + 1] + a.b4[4 * q + 1],
+                                         v[4 * q + 2] + a.b4[4 * q + 2], v[4 * q + 3] + a.b4[4 * q + 3]);
+            }
+        }
+        tc_fence_before();
+        __syncthreads();  // TMEM reads done before the next tile's MMAs
+        tc_fence_after();
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x < 32) tmem_dealloc(tmem, HID);
+}
+
+void launch_infer(const InferArgs& a, int grid, cudaStream_t s) { k_mlp_infer<<<grid, GT, S_END, s>>>(a); }
+
 cudaError_t gemm_prepare() {
-    return cudaFuncSetAttribute(k_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem_bytes(256));
+    cudaError_t e = cudaFuncSetAttribute(k_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem_bytes(256));
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S_END);
+    return e;
 }
 
 void launch_gemm(const GemmArgs& g, int grid, cudaStream_t s) {

@@ -46,8 +46,26 @@ struct GemmArgs {
 };
 
 size_t gemm_smem_bytes(int N);
-cudaError_t gemm_prepare();  // once per device: the dynamic shared-memory attribute
+cudaError_t gemm_prepare();  // once per device: the dynamic shared-memory attributes (GEMM and inference)
 void launch_gemm(const GemmArgs& g, int grid, cudaStream_t s);
+
+// The whole forward pass of the 16 (12 used) -> 128 -> 128 -> 128 -> 16 (3 used) network on one
+// SM per 128-row tile: the four weight matrices stay in shared memory, each layer's activations go
+// from TMEM through the epilogue back into shared memory as the next layer's A operand; only the
+// features are read and the FP32 outputs written.  The same MMA sequence, biases, GELU and bf16
+// roundings as the layer-by-layer GEMMs, so the same outputs.
+struct InferArgs {
+    const float* x = nullptr;  // features, WS_FEATURES used of ld_x per row
+    int ld_x = 0;
+    const int* d_rows = nullptr;  // rows on the device, clamped to rows_cap
+    int rows_cap = 0;
+    const float* norm = nullptr;  // feature mean[12], 1/std[12]
+    const __nv_bfloat16 *wt1 = nullptr, *wt2 = nullptr, *wt3 = nullptr, *wt4 = nullptr;  // [N][K] K-major
+    const float *b1 = nullptr, *b2 = nullptr, *b3 = nullptr, *b4 = nullptr;
+    float* y = nullptr;  // [rows][16]
+    unsigned int* status = nullptr;
+};
+void launch_infer(const InferArgs& a, int grid, cudaStream_t s);
 
 }  // namespace mlp
 }  // namespace b3g

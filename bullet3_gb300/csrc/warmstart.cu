@@ -311,8 +311,27 @@ cudaError_t ensure_infer(Model& m, int rows_cap) {
 }
 
 int forward_device(Model& m, const float* x, int ld_x, const int* d_rows, int rows_cap, cudaStream_t s) {
-    k_pack<<<m.num_sms * 2, 256, 0, s>>>(x, ld_x, d_rows, 0, rows_cap, m.norm, m.infer.x_row, nullptr, 0, 0);
-    return 1 + run_forward(m, m.infer, d_rows, 0, rows_cap, false, s);
+    // the fused on-chip forward pass (mlp.cu k_mlp_infer): the same outputs as packing the features
+    // and running the four layer GEMMs, with the activations kept in shared memory and TMEM
+    InferArgs a;
+    a.x = x;
+    a.ld_x = ld_x;
+    a.d_rows = d_rows;
+    a.rows_cap = rows_cap;
+    a.norm = m.norm;
+    a.wt1 = m.wt1;
+    a.wt2 = m.wt2;
+    a.wt3 = m.wt3;
+    a.wt4 = m.wt4;
+    a.b1 = m.params + OFF_B1;
+    a.b2 = m.params + OFF_B2;
+    a.b3 = m.params + OFF_B3;
+    a.b4 = m.params + OFF_B4;
+    a.y = m.infer.y;
+    a.status = m.status;
+    const int tiles = (rows_cap + 127) / 128;
+    launch_infer(a, tiles < m.num_sms ? (tiles > 0 ? tiles : 1) : m.num_sms, s);
+    return 1;
 }
 
 const float* last_predictions(const Model& m) { return m.infer.y; }
