@@ -33,11 +33,11 @@ static constexpr unsigned WAIT_LIMIT = 1u << 22;
 // ---------------------------------------------------------------------------- PTX wrappers
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t sbo = SBO) {
     uint64_t d = 0;
     d |= (uint64_t)((addr >> 4) & 0x3FFFu);              // start address
     d |= (uint64_t)((LBO >> 4) & 0x3FFFu) << 16;         // leading-dimension byte offset (along K)
-    d |= (uint64_t)((SBO >> 4) & 0x3FFFu) << 32;         // stride-dimension byte offset (8-row groups)
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;         // stride-dimension byte offset (8-row groups)
     d |= (uint64_t)1 << 46;                              // descriptor version for tcgen05
     // base offset 0, absolute LBO mode 0, layout type 0 = no swizzle
     return d;
@@ -195,6 +195,29 @@ __global__ void __launch_bounds__(GT) k_gemm(GemmArgs g) {
         for (int n0 = 0; n0 < N; n0 += 16) {
             float v[16];
             tmem_ld16(trow + n0, v);
+            if (g.epi == EPI_DGELU) {
+                // every lane takes part in the warp sums of the bias gradient (rows past the end
+                // add zero), so the rows are masked instead of skipped
+#pragma unroll
+                for (int i = 0; i < 16; i++) {
+                    const int n = n0 + i;
+                    float hv = 0.f;
+                    if (r < rows) {
+                        const float d = v[i] * gelu_grad(g.pre_in[(size_t)r * g.ld_out + n]);
+                        const __nv_bfloat16 hb = __float2bfloat16_rn(d);
+                        if (g.out_row) g.out_row[(size_t)r * g.ld_row + n] = hb;
+                        if (g.out_col) g.out_col[(size_t)n * g.ld_col + r] = hb;
+                        hv = __bfloat162float(hb);
+                    }
+                    // bias gradient: sum of the rounded values, as the next layer consumes them,
+                    // over the warp's 32 rows first, one atomic per warp
+                    if (g.atomic_out) {
+                        for (int o = 16; o; o >>= 1) hv += __shfl_xor_sync(0xffffffffu, hv, o);
+                        if ((threadIdx.x & 31) == 0) atomicAdd(&g.atomic_out[n], hv);
+                    }
+                }
+                continue;
+            }
             if (r >= rows) continue;
 #pragma unroll
             for (int i = 0; i < 16; i++) {
@@ -210,15 +233,6 @@ __global__ void __launch_bounds__(GT) k_gemm(GemmArgs g) {
                         const __nv_bfloat16 h = __float2bfloat16_rn(gelu(pre));
                         g.out_row[(size_t)r * g.ld_row + n] = h;
                         if (g.out_col) g.out_col[(size_t)n * g.ld_col + r] = h;
-                        break;
-                    }
-                    case EPI_DGELU: {
-                        const float d = x * gelu_grad(g.pre_in[(size_t)r * g.ld_out + n]);
-                        const __nv_bfloat16 hb = __float2bfloat16_rn(d);
-                        if (g.out_row) g.out_row[(size_t)r * g.ld_row + n] = hb;
-                        if (g.out_col) g.out_col[(size_t)n * g.ld_col + r] = hb;
-                        // bias gradient: sum of the rounded values, as the next layer consumes them
-                        if (g.atomic_out) atomicAdd(&g.atomic_out[n], __bfloat162float(hb));
                         break;
                     }
                     case EPI_ATOMIC:
@@ -239,31 +253,45 @@ __global__ void __launch_bounds__(GT) k_gemm(GemmArgs g) {
 size_t gemm_smem_bytes(int N) { return (size_t)128 * KC * 2 + (size_t)N * KC * 2; }
 
 // ---------------------------------------------------------------------------- fused inference
-// Shared memory (chunk layout of load_chunk, every chunk 1 KB aligned): W1 (128 x 16, one chunk),
-// W2 and W3 (128 x 128, two chunks each), W4 (16 x 128, two 16-row chunks), the tile's inputs
-// (128 x 16, one chunk) and its activations (128 x 128, two chunks), 132 KB.
-static constexpr int FIN = 16, FOUT = 16, HID = 128;
+// Shared memory, every block 1 KB aligned: W1 (128 x 16) and the tile's inputs (128 x 16) in a
+// 16-wide layout (core matrices of 8 rows x 8 K as in load_chunk, 256 bytes between 8-row groups),
+// W2 and W3 (128 x 128, two 64-K chunks each), W4 (16 x 128, two 16-row chunks) and the
+// activations (128 x 128, two chunks) in the chunk layout of load_chunk; 108 KB, so two CTAs share
+// an SM.  Eight warps: the TMEM lane quarter of warp w is w % 4 (rows 32 (w % 4) ..), warps 0-3 take
+// columns 0-63 of each hidden layer's epilogue and warps 4-7 columns 64-127.
+static constexpr int FIN = 16, FOUT = 16, HID = 128, IT = 256;
 static constexpr size_t CH128 = 128 * KC * 2;  // a 128-row chunk: 16 KB
 static constexpr size_t CH16 = 16 * KC * 2;    // a 16-row chunk: 2 KB
-static constexpr size_t S_W1 = 0, S_W2 = S_W1 + CH128, S_W3 = S_W2 + 2 * CH128, S_W4 = S_W3 + 2 * CH128;
-static constexpr size_t S_X = S_W4 + 2 * CH16, S_H = S_X + CH128, S_END = S_H + 2 * CH128;
+static constexpr uint32_t SBO16 = 256;         // 8-row group stride of the 16-wide layout
+static constexpr size_t N16 = 128 * FIN * 2;   // a 128 x 16 operand: 4 KB
+static constexpr size_t S_W1 = 0, S_X = S_W1 + N16, S_W2 = S_X + N16, S_W3 = S_W2 + 2 * CH128,
+                        S_W4 = S_W3 + 2 * CH128, S_H = S_W4 + 2 * CH16, S_END = S_H + 2 * CH128;
 
-// thread t's row of 16 values (bf16) at columns n0..n0+15 of a 128-row, K-chunked operand
-__device__ __forceinline__ void put_row16(char* base, int r, int n0, const float* v) {
+// 16 values (bf16) of row r at columns n0..n0+15 of a K-chunked 128-row operand (base: chunk 0)
+__device__ __forceinline__ void put_row16(char* base, int r, int n0, const float* v, uint32_t sbo, size_t chunk_bytes) {
     uint32_t w[8];
 #pragma unroll
     for (int i = 0; i < 8; i++) {
         const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
         w[i] = *reinterpret_cast<const uint32_t*>(&h);
     }
-    char* chunk = base + (size_t)(n0 / KC) * CH128;
+    char* chunk = base + (size_t)(n0 / KC) * chunk_bytes;
     const int k = n0 % KC;
-    char* row = chunk + (r & 7) * 16 + (r >> 3) * SBO;
+    char* row = chunk + (r & 7) * 16 + (r >> 3) * sbo;
     *reinterpret_cast<uint4*>(row + (k / 8) * LBO) = make_uint4(w[0], w[1], w[2], w[3]);
     *reinterpret_cast<uint4*>(row + (k / 8 + 1) * LBO) = make_uint4(w[4], w[5], w[6], w[7]);
 }
 
-__global__ void __launch_bounds__(GT, 1) k_mlp_infer(InferArgs a) {
+// the rows of a K-major bf16 matrix with 16 K elements into the 16-wide layout
+__device__ __forceinline__ void load16(char* dst, const __nv_bfloat16* src, int nrows) {
+    for (int p = threadIdx.x; p < nrows * 2; p += blockDim.x) {
+        const int r = p >> 1, kq = p & 1;
+        *reinterpret_cast<uint4*>(dst + (r & 7) * 16 + kq * LBO + (r >> 3) * SBO16) =
+            *reinterpret_cast<const uint4*>(src + (size_t)r * FIN + kq * 8);
+    }
+}
+
+__global__ void __launch_bounds__(IT, 2) k_mlp_infer(InferArgs a) {
     extern __shared__ __align__(1024) char smem[];
     __shared__ unsigned long long bar;
     __shared__ uint32_t tslot;
@@ -272,7 +300,7 @@ __global__ void __launch_bounds__(GT, 1) k_mlp_infer(InferArgs a) {
     if ((int)blockIdx.x >= m_tiles) return;  // block-uniform, before any barrier or TMEM use
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     if (threadIdx.x < 32) tmem_alloc(&tslot, HID);
-    load_chunk(smem + S_W1, a.wt1, FIN, 0, HID, HID, 0, FIN);
+    load16(smem + S_W1, a.wt1, HID);
     for (int c = 0; c < 2; c++) {
         load_chunk(smem + S_W2 + c * CH128, a.wt2, HID, 0, HID, HID, c * KC, HID);
         load_chunk(smem + S_W3 + c * CH128, a.wt3, HID, 0, HID, HID, c * KC, HID);
@@ -282,13 +310,16 @@ __global__ void __launch_bounds__(GT, 1) k_mlp_infer(InferArgs a) {
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tslot;
-    const uint32_t trow = tmem + ((uint32_t)(threadIdx.x & ~31) << 16);
     const int t = threadIdx.x;
+    const int lane_row = t & 127;        // this thread's row of the tile (its TMEM lane)
+    const int half = t >> 7;             // 0: columns 0-63, 1: columns 64-127
+    const uint32_t trow = tmem + ((uint32_t)(lane_row & ~31) << 16);
     unsigned phase = 0;
     bool failed = false;
-    // one layer: `steps` MMAs of K = 16 over `chunks` K-chunks of A at sA and B at sB; returns false
-    // when the wait gave up (the status flag is set and the MMAs drained)
-    auto layer = [&](uint32_t sA, uint32_t sB, size_t b_chunk, int chunks, int steps, uint32_t idesc) -> bool {
+    // one layer: MMAs of K = 16 over `chunks` K-chunks of A at sA and B at sB; false when the wait
+    // gave up (the status flag is set and the MMAs drained)
+    auto layer = [&](uint32_t sA, size_t a_chunk, uint32_t sB, size_t b_chunk, uint32_t sbo, int chunks, int steps,
+                     uint32_t idesc) -> bool {
         fence_async_smem();
         tc_fence_before();
         __syncthreads();
@@ -296,8 +327,8 @@ __global__ void __launch_bounds__(GT, 1) k_mlp_infer(InferArgs a) {
         if (t == 0) {
             for (int c = 0; c < chunks; c++)
                 for (int s = 0; s < steps; s++) {
-                    const uint64_t ad = smem_desc(sA + (uint32_t)(c * CH128) + s * 2 * LBO);
-                    const uint64_t bd = smem_desc(sB + (uint32_t)(c * b_chunk) + s * 2 * LBO);
+                    const uint64_t ad = smem_desc(sA + (uint32_t)(c * a_chunk) + s * 2 * LBO, sbo);
+                    const uint64_t bd = smem_desc(sB + (uint32_t)(c * b_chunk) + s * 2 * LBO, sbo);
                     mma_bf16(tmem, ad, bd, idesc, (c > 0 || s > 0) ? 1u : 0u);
                 }
             mma_commit(&bar);
@@ -315,35 +346,35 @@ __global__ void __launch_bounds__(GT, 1) k_mlp_infer(InferArgs a) {
         return true;
     };
     const uint32_t sX = smem_u32(smem + S_X), sH = smem_u32(smem + S_H);
+    const float* bias[3] = {a.b1, a.b2, a.b3};
     for (int tile = blockIdx.x; tile < m_tiles && !failed; tile += gridDim.x) {
-        const int r = tile * 128 + t;
-        {
+        const int r = tile * 128 + lane_row;
+        if (half == 0) {
             // the normalised features of row r (k_pack's arithmetic), zero past the rows
             float v[16];
 #pragma unroll
             for (int f = 0; f < 16; f++)
                 v[f] = (r < rows && f < WS_FEATURES) ? (a.x[(size_t)r * a.ld_x + f] - a.norm[f]) * a.norm[WS_FEATURES + f]
-                                                       : 0.f;
-            put_row16(smem + S_X, t, 0, v);
+                                                    : 0.f;
+            put_row16(smem + S_X, lane_row, 0, v, SBO16, N16);
         }
-        const float* bias[3] = {a.b1, a.b2, a.b3};
-        for (int l = 0; l < 3 && !failed; l++) {
-            const bool ok = l == 0 ? layer(sX, smem_u32(smem + S_W1), CH128, 1, 1, instr_desc(HID))
-                                   : layer(sH, smem_u32(smem + (l == 1 ? S_W2 : S_W3)), CH128, 2, KC / 16,
-                                           instr_desc(HID));
+        for (int l = 0; l < 3; l++) {
+            const bool ok = l == 0 ? layer(sX, N16, smem_u32(smem + S_W1), N16, SBO16, 1, 1, instr_desc(HID))
+                                   : layer(sH, CH128, smem_u32(smem + (l == 1 ? S_W2 : S_W3)), CH128, SBO, 2,
+                                           KC / 16, instr_desc(HID));
             if (!ok) { failed = true; break; }
-            for (int n0 = 0; n0 < HID; n0 += 16) {
+            for (int n0 = half * 64; n0 < half * 64 + 64; n0 += 16) {
                 float v[16];
                 tmem_ld16(trow + n0, v);
 #pragma unroll
                 for (int i = 0; i < 16; i++) v[i] = gelu(v[i] + bias[l][n0 + i]);
-                put_row16(smem + S_H, t, n0, v);
+                put_row16(smem + S_H, lane_row, n0, v, SBO, CH128);
             }
             tc_fence_before();  // TMEM reads done before the next layer's MMAs overwrite it
         }
         if (failed) break;
-        if (!layer(sH, smem_u32(smem + S_W4), CH16, 2, KC / 16, instr_desc(FOUT))) { failed = true; break; }
-        {
+        if (!layer(sH, CH128, smem_u32(smem + S_W4), CH16, SBO, 2, KC / 16, instr_desc(FOUT))) { failed = true; break; }
+        if (half == 0) {
             float v[16];
             tmem_ld16(trow, v);
             if (r < rows) {
@@ -363,7 +394,7 @@ __global__ void __launch_bounds__(GT, 1) k_mlp_infer(InferArgs a) {
     if (threadIdx.x < 32) tmem_dealloc(tmem, HID);
 }
 
-void launch_infer(const InferArgs& a, int grid, cudaStream_t s) { k_mlp_infer<<<grid, GT, S_END, s>>>(a); }
+void launch_infer(const InferArgs& a, int grid, cudaStream_t s) { k_mlp_infer<<<grid, IT, S_END, s>>>(a); }
 
 cudaError_t gemm_prepare() {
     cudaError_t e = cudaFuncSetAttribute(k_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem_bytes(256));

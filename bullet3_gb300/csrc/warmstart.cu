@@ -330,7 +330,7 @@ int forward_device(Model& m, const float* x, int ld_x, const int* d_rows, int ro
     a.y = m.infer.y;
     a.status = m.status;
     const int tiles = (rows_cap + 127) / 128;
-    launch_infer(a, tiles < m.num_sms ? (tiles > 0 ? tiles : 1) : m.num_sms, s);
+    launch_infer(a, tiles < 2 * m.num_sms ? (tiles > 0 ? tiles : 1) : 2 * m.num_sms, s);  // two CTAs an SM
     return 1;
 }
 

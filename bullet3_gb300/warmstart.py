@@ -100,3 +100,43 @@ class WarmStartMLP:
         m.params = d["params"]
         m.normalization = d["normalization"]
         return m
+
+
+def _time_kernels(argv=None) -> int:
+    """Times the network's device work on random features, for profiling runs:
+
+        python -m bullet3_gb300.warmstart [--rows N] [--batch B] [--train-steps S] [--repeat R]
+
+    `predict` over N rows (the fused forward kernel; the call also copies the features in and the
+    predictions out) and S training steps of batch B (forward and backward GEMMs, Adam); prints the
+    wall times per call."""
+    import argparse
+    import json
+    import time
+    p = argparse.ArgumentParser()
+    p.add_argument("--rows", type=int, default=1 << 20)
+    p.add_argument("--batch", type=int, default=65536)
+    p.add_argument("--train-steps", type=int, default=1)
+    p.add_argument("--repeat", type=int, default=3)
+    a = p.parse_args(argv)
+    rng = np.random.Generator(np.random.PCG64(0))
+    m = WarmStartMLP.load()
+    x = rng.standard_normal((a.rows, N_FEATURES)).astype(np.float32)
+    t = rng.standard_normal((a.rows, N_OUTPUTS)).astype(np.float32)
+    m.predict(x[:1024])
+    t0 = time.perf_counter()
+    for _ in range(a.repeat):
+        m.predict(x)
+    predict_s = (time.perf_counter() - t0) / a.repeat
+    m.set_training_data(x, t)
+    m.train(1, a.batch, 1e-4)
+    t0 = time.perf_counter()
+    loss = m.train(a.train_steps, a.batch, 1e-4)
+    train_s = (time.perf_counter() - t0) / max(a.train_steps, 1)
+    print(json.dumps({"rows": a.rows, "predict_ms": 1000 * predict_s, "batch": a.batch,
+                      "train_step_ms": 1000 * train_s, "loss": loss}))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(_time_kernels())
