@@ -170,11 +170,16 @@ def test_persistent_contacts_start_from_previous_impulses():
 def test_trained_network_cuts_sweeps_on_held_out_piles():
     # the committed network (trained on the GPU by bullet3_gb300.learned from the plain solver's
     # converged impulses) against the cold start on piles it never saw, every solve run to 1e-4:
-    # fewer sweeps on average, no step falls back
+    # alone it saves at least 15% of the sweeps (measured 28%); predicting the new points beside
+    # the persisting ones' carried impulses it reaches the target of at least 30% fewer sweeps than
+    # the cold start (measured 53%) and fewer than persistence alone (measured 6%); no step falls
+    # back to a cold start
     from bullet3_gb300 import learned
     from bullet3_gb300.warmstart import DEFAULT_WEIGHTS
-    r = learned.evaluate(DEFAULT_WEIGHTS, kind="piles", size=128, steps=60, first=20, cap=1000, seed=7,
-                         modes=("cold", "learned"))
-    assert r["cold"]["converged"] == 1.0 and r["learned"]["converged"] == 1.0
-    assert r["learned"]["dropped_steps"] == 0
-    assert r["learned"]["iterations"] < 0.97 * r["cold"]["iterations"], r
+    r = learned.evaluate(DEFAULT_WEIGHTS, kind="piles", size=128, steps=60, first=20, cap=1000, seed=7)
+    for mode in r.values():
+        assert mode["converged"] == 1.0 and mode["dropped_steps"] == 0, r
+    cold = r["cold"]["iterations"]
+    assert r["learned"]["iterations"] < 0.85 * cold, r
+    assert r["persistent_learned"]["iterations"] <= 0.70 * cold, r
+    assert r["persistent_learned"]["iterations"] < r["persistent"]["iterations"], r
