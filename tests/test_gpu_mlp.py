@@ -58,7 +58,10 @@ def test_forward_matches_oracle(n):
     y = m.predict(x)
     yo, _ = MO.forward(p, norm, x)
     scale = np.abs(yo).max() + 1e-6
-    assert np.abs(y - yo).max() <= 2e-2 * scale, (np.abs(y - yo).max(), scale)
+    # the oracle rounds the same values to BF16; only the FP32 accumulation order inside the tensor
+    # cores differs, which can move an activation's BF16 rounding by one unit (measured: at most
+    # 5.2e-4 of the output scale up to 4,099 rows, 1.2e-3 at 65,536)
+    assert np.abs(y - yo).max() <= 2e-3 * scale, (np.abs(y - yo).max(), scale)
 
 
 @pytest.mark.parametrize("n", [64, 777, 5000])
@@ -68,10 +71,11 @@ def test_gradients_match_oracle(n):
     t = rng.normal(0, 1, (n, 3)).astype(np.float32)
     g, loss = m.gradients(x, t)
     go, lo = MO.gradients(p, norm, x, t)
-    assert abs(loss - lo) <= 1e-3 * abs(lo)
+    # (measured: loss within 3.2e-6, every parameter block's gradient within 5.7e-5, relative)
+    assert abs(loss - lo) <= 2e-5 * abs(lo)
     for name, a, b in zip(NAMES, _split(g), _split(go)):
         err = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
-        assert err <= 3e-2, (name, err)
+        assert err <= 2e-4, (name, err)
     # parameters are untouched by a gradient evaluation
     assert np.array_equal(m.params, p)
 
