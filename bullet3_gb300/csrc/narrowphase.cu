@@ -1141,8 +1141,8 @@ __device__ int concave_tri_pairs(const NPArgs& a, int p, int4* out, int cap) {
     const b3gCollidable cA = a.cols[BA.collidableIdx];
     if (cA.shapeType != B3G_SHAPE_CONCAVE_TRIMESH) return 0;
     const b3gCollidable cB = a.cols[BB.collidableIdx];
-    // (spheres against meshes take the reference's findConcaveSphereContactsKernel: not built)
-    if (cB.shapeType != B3G_SHAPE_CONVEX_HULL && cB.shapeType != B3G_SHAPE_COMPOUND) return 0;
+    if (cB.shapeType != B3G_SHAPE_CONVEX_HULL && cB.shapeType != B3G_SHAPE_SPHERE && cB.shapeType != B3G_SHAPE_COMPOUND)
+        return 0;
     const bool comp = cB.shapeType == B3G_SHAPE_COMPOUND;
     const int nch = comp ? cB.numChildShapes : 1;
     const b3gBvhInfo bi = a.bvh_infos[cA.numChildShapes];
@@ -1291,6 +1291,80 @@ __device__ __forceinline__ bool concave_axis(int k, const TriPrism& P, const b3g
     return true;
 }
 
+// computeContactSphereTriangle (kernels/primitiveContacts.cl:1163-1302, run by
+// findConcaveSphereContactsKernel :1319-1370): the sphere centre in the mesh's frame; the
+// triangle's plane turned towards it; a contact on the face when the centre's projection is inside
+// the triangle (pointInTriangle), else the nearest point of an edge within the radius (the last such
+// edge, segmentSqrDistance); one point at most the radius deep, the sphere as body A, childIndexB
+// the triangle
+__device__ bool concave_sphere(const NPArgs& a, const b3gHull& mesh, int4 cp, int index, b3gContact4& c) {
+    const b3gBody& BM = a.bodies[cp.x];
+    const b3gBody& BS = a.bodies[cp.y];
+    const float radius = a.cols[BS.collidableIdx].radius;
+    const b3gFace face = a.faces[mesh.faceOffset + cp.z];
+    v3 tv[3];
+    for (int i = 0; i < 3; i++) tv[i] = ld3(&a.verts[mesh.vertexOffset + a.indices[face.indexOffset + i]]);
+    const v3 pos = f4v3(BM.pos);
+    const quat q = f4q(BM.quat), qi = qconj(q);
+    const v3 centre = qrotq(qi, f4v3(BS.pos)) + qrotq(qi, -pos);
+    v3 normal = normalize3(cross3(tv[1] - tv[0], tv[2] - tv[0]));
+    float dist = dot3(centre - tv[0], normal);
+    if (dist < 0.f) {
+        dist = dist * -1.f;
+        normal = normal * -1.f;
+    }
+    bool has = false;
+    v3 cpt = mk3(0.f, 0.f, 0.f);
+    if (dist < radius) {
+        const v3 e1 = tv[1] - tv[0], e2 = tv[2] - tv[1], e3 = tv[0] - tv[2];
+        const float r1 = dot3(cross3(e1, normal), centre - tv[0]);
+        const float r2 = dot3(cross3(e2, normal), centre - tv[1]);
+        const float r3 = dot3(cross3(e3, normal), centre - tv[2]);
+        if ((r1 > 0.f && r2 > 0.f && r3 > 0.f) || (r1 <= 0.f && r2 <= 0.f && r3 <= 0.f)) {
+            has = true;
+            cpt = centre - normal * dist;
+        } else {
+            const float rr = radius * radius;
+            for (int i = 0; i < 3; i++) {
+                const v3 from = tv[i], to = tv[(i + 1) % 3];
+                v3 diff = centre - from;
+                const v3 v = to - from;
+                float t = dot3(v, diff);
+                if (t > 0.f) {
+                    const float vv = dot3(v, v);
+                    if (t < vv) {
+                        t = t / vv;
+                        diff = diff - t * v;
+                    } else {
+                        t = 1.f;
+                        diff = diff - v;
+                    }
+                } else {
+                    t = 0.f;
+                }
+                if (dot3(diff, diff) < rr) {
+                    has = true;
+                    cpt = from + t * v;
+                }
+            }
+        }
+    }
+    if (!has) return false;
+    const v3 toc = centre - cpt;
+    const float md = sqrtf(dot3(toc, toc));
+    if (!(md > FLT_EPSILON)) return false;
+    const float depth = md - radius;
+    const v3 n1 = qrotq(q, -normalize3(toc));
+    const v3 pB = qrotq(q, cpt) + pos;
+    if (!(depth <= 0.f) || !(dot3(n1, n1) > FLT_EPSILON)) return false;
+    write_header(c, a, cp.y, cp.x, -n1, 1);
+    c.frictionCmp = (unsigned short)(0.7f * 0xffff);
+    c.batchIdx = index;
+    c.childIndexB = cp.z;
+    c.worldPosB[0] = b3gFloat4{pB.x, pB.y, pB.z, depth};
+    return true;
+}
+
 // One warp per triangle-convex pair (slot = pairs + compound child pairs + its index):
 // b3FindConcaveSeparatingAxisKernel, then b3FindClippingFaces (shared/b3FindConcaveSatAxis.h:421-504),
 // clipFacesAndFindContactsKernel (shared/b3ClipFaces.h:67-177) and b3NewContactReductionKernel
@@ -1317,6 +1391,10 @@ __global__ void __launch_bounds__(CC_WARPS * 32) k_concave_contacts(NPArgs a, co
         const b3gBody& BA = a.bodies[cp.x];
         const b3gBody& BB = a.bodies[cp.y];
         const b3gHull mesh = a.hulls[a.cols[BA.collidableIdx].shapeIndex];
+        if (a.cols[BB.collidableIdx].shapeType == B3G_SHAPE_SPHERE) {
+            if (lane == 0 && concave_sphere(a, mesh, cp, k, a.slots[slot])) a.flags[slot] = 1;
+            continue;
+        }
         TriPrism P;
         tri_prism(a, mesh, cp.z, P);
         // the triangle's local AABB against the other body's world AABB

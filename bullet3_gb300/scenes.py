@@ -282,10 +282,10 @@ def terrain_mesh(grid=64, cell=1.0, amplitude=1.5, seed=0):
     return verts, np.array(idx, np.int32), height
 
 
-def terrain_scene(n=2048, grid=64, cell=1.0, seed=0, drop=False, velocity_sigma=0.3) -> Scene:
+def terrain_scene(n=2048, grid=64, cell=1.0, seed=0, drop=False, velocity_sigma=0.3, spheres=True) -> Scene:
     """A static concave height-field mesh (terrain_mesh, body 0 at the identity pose) under boxes
-    (half extents 0.5 x 0.25 x 0.25), 20-point Gaussian hulls and compounds (an L of two boxes, a
-    dumbbell of two hulls around a box), in turn.  Either scattered just over the surface with
+    (half extents 0.5 x 0.25 x 0.25), 20-point Gaussian hulls, compounds (an L of two boxes, a
+    dumbbell of two hulls around a box) and, with spheres, spheres of radius 0.3, in turn.  Either scattered just over the surface with
     random orientations and N(0, velocity_sigma^2) velocities (heights from 0.2 below the surface to
     0.6 above it, so that many touch it), or (drop=True) a lattice of them at rest, from 2 above
     the highest point, that falls onto it."""
@@ -302,7 +302,11 @@ def terrain_scene(n=2048, grid=64, cell=1.0, seed=0, drop=False, velocity_sigma=
     qa, qb = random_quaternions(rng, 2)
     sc.shapes.append({"type": "compound", "children": [(3, (-0.6, 0.0, 0.0), tuple(qa)), (1, (0.0, 0.0, 0.0), q0),
                                                         (3, (0.6, 0.0, 0.0), tuple(qb))]})
-    kinds = np.array([1, 3, 4, 5], np.int32)[np.arange(n) % 4]
+    kinds = [1, 3, 4, 5]
+    if spheres:
+        sc.shapes.append({"type": "sphere", "radius": 0.3})
+        kinds.append(6)
+    kinds = np.array(kinds, np.int32)[np.arange(n) % len(kinds)]
     reach = 0.6 + float(np.linalg.norm(gauss, axis=1).max())
     span = grid * cell
     if drop:

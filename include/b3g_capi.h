@@ -203,8 +203,9 @@ b3gStatus b3g_read_child_shapes(b3g_handle h, struct b3gChildShape* host_childre
  * the triangles as faces (plane = normalised (v1 - v0) x (v2 - v0), w = -n.v0) and a quantized BVH
  * over them (b3g_read_mesh_bvh).  A mesh collides with hulls and compounds (one manifold per
  * touching triangle, or triangle and child, as b3BvhTraversal / b3FindConcaveSeparatingAxisKernel /
- * clipFacesAndFindContactsKernel / b3NewContactReductionKernel compute them) when its body is the
- * pair's first (lower index), as in the reference; not with spheres, planes or other meshes.  The
+ * clipFacesAndFindContactsKernel / b3NewContactReductionKernel compute them), and with spheres (one
+ * point per touching triangle, computeContactSphereTriangle) when its body is the pair's first
+ * (lower index), as in the reference; not with planes or other meshes.  The
  * reference traverses with the other body's world AABB in the mesh's own frame, so meshes are
  * meant to stay at the identity pose.  -> -1 + b3Error in the Python / C++ layers on invalid input. */
 b3gStatus b3g_register_concave_mesh(b3g_handle h, const float* vertices, int stride_bytes, int num_vertices,

@@ -1092,8 +1092,7 @@ int oracle_concave_pairs(const obody* bodies, const oshapes* sh, const oaabb* aa
         cB = &sh->cols[bodies[B].collidableIdx];
         if (cA->shapeType != SHAPE_CONCAVE_TRIMESH) continue;
         tB = cB->shapeType;
-        /* (spheres take the reference's findConcaveSphereContactsKernel, not restated here) */
-        if (tB != SHAPE_CONVEX_HULL && tB != SHAPE_COMPOUND_OF_CONVEX_HULLS) continue;
+        if (tB != SHAPE_CONVEX_HULL && tB != SHAPE_SPHERE && tB != SHAPE_COMPOUND_OF_CONVEX_HULLS) continue;
         nch = tB == SHAPE_COMPOUND_OF_CONVEX_HULLS ? cB->numChildShapes : 1;
         mesh = &sh->hulls[cA->shapeIndex];
         mesh_bvhq(&sh->local_aabbs[bodies[A].collidableIdx], &bq);
@@ -1168,6 +1167,92 @@ static void project_tri(const v3* tv, v3 pos, qt orn, v3 dir, float* mn, float* 
     if (*mn > *mx) { float t = *mn; *mn = *mx; *mx = t; }
     *mn = *mn + offset;
     *mx = *mx + offset;
+}
+
+/* computeContactSphereTriangle (kernels/primitiveContacts.cl:1163-1302, run by
+ * findConcaveSphereContactsKernel :1319-1370; GPU-only in the reference, so this restatement is
+ * not pinned to reference output): the sphere centre in the mesh's frame; the triangle's plane
+ * (normalised (v1 - v0) x (v2 - v0), turned towards the centre); a contact on the face when the
+ * centre's projection is inside the triangle (pointInTriangle :1100-1133), else the nearest point
+ * of an edge within the radius (segmentSqrDistance :1136-1160, the last such edge); normal from
+ * the contact point to the centre; one point, at most the radius deep.  The sphere is body A of
+ * the manifold, the mesh body B, childIndexB the triangle. */
+static int point_in_triangle(const v3* tv, v3 n, v3 p) {
+    v3 e1 = sub(tv[1], tv[0]), e2 = sub(tv[2], tv[1]), e3 = sub(tv[0], tv[2]);
+    float r1 = dot(cross(e1, n), sub(p, tv[0]));
+    float r2 = dot(cross(e2, n), sub(p, tv[1]));
+    float r3 = dot(cross(e3, n), sub(p, tv[2]));
+    if (r1 > 0.f && r2 > 0.f && r3 > 0.f) return 1;
+    if (r1 <= 0.f && r2 <= 0.f && r3 <= 0.f) return 1;
+    return 0;
+}
+
+static float segment_sqr_distance(v3 from, v3 to, v3 p, v3* nearest) {
+    v3 diff = sub(p, from), v = sub(to, from);
+    float t = dot(v, diff);
+    if (t > 0.f) {
+        float dotVV = dot(v, v);
+        if (t < dotVV) {
+            t = t / dotVV;
+            diff = sub(diff, lscl(t, v));
+        } else {
+            t = 1.f;
+            diff = sub(diff, v);
+        }
+    } else {
+        t = 0.f;
+    }
+    *nearest = add(from, lscl(t, v));
+    return dot(diff, diff);
+}
+
+static int concave_sphere(const obody* bodies, const oshapes* sh, const opair* cp, int index, ocontact* c) {
+    const obody* BM = &bodies[cp->x];
+    const obody* BS = &bodies[cp->y];
+    const ohull* mesh = mesh_of(sh, BM);
+    const float radius = sh->cols[BS->collidableIdx].radius;
+    v3 tv[3], pos = f4v(BM->pos), centre, normal, hit, cpt = mk(0.f, 0.f, 0.f);
+    qt q = f4q(BM->quat), qi = qconj(f4q(BM->quat));
+    float dist;
+    int i, has = 0;
+    for (i = 0; i < 3; i++) tv[i] = mesh_vertex(sh, mesh, cp->z, i);
+    centre = add(qrotq(qi, f4v(BS->pos)), qrotq(qi, neg(pos)));
+    normal = nrm(cross(sub(tv[1], tv[0]), sub(tv[2], tv[0])));
+    dist = dot(sub(centre, tv[0]), normal);
+    if (dist < 0.f) { dist = dist * -1.f; normal = scl(normal, -1.f); }
+    hit = normal;
+    if (dist < radius) {
+        if (point_in_triangle(tv, normal, centre)) {
+            has = 1;
+            cpt = sub(centre, scl(normal, dist));
+        } else {
+            float r2 = radius * radius;
+            for (i = 0; i < 3; i++) {
+                v3 nearest;
+                float d2 = segment_sqr_distance(tv[i], tv[(i + 1) % 3], centre, &nearest);
+                if (d2 < r2) { has = 1; cpt = nearest; }
+            }
+        }
+    }
+    if (has) {
+        v3 toc = sub(centre, cpt);
+        float md = sqrtf(dot(toc, toc));
+        if (md > FLT_EPSILON) {
+            v3 n1, pB;
+            float depth = md - radius;
+            hit = nrm(toc);
+            n1 = qrotq(q, neg(hit));
+            pB = add(qrotq(q, cpt), pos);
+            if (depth <= 0.f && dot(n1, n1) > FLT_EPSILON) {
+                write_header(c, bodies, cp->y, cp->x, neg(n1), 1, (unsigned short)(0.7f * 0xffff));
+                c->batchIdx = index;
+                c->childIndexB = cp->z;
+                c->worldPosB[0].x = pB.x; c->worldPosB[0].y = pB.y; c->worldPosB[0].z = pB.z; c->worldPosB[0].w = depth;
+                return 1;
+            }
+        }
+    }
+    return 0;
 }
 
 /* one triangle-convex pair: the triangle as a five-face prism (front, back, three edge planes),
@@ -1347,7 +1432,9 @@ int oracle_concave_contacts(const obody* bodies, const oshapes* sh, const oaabb*
     for (i = 0; i < n; i++) {
         ocontact c;
         memset(&c, 0, sizeof(c));
-        if (concave_tri(bodies, sh, aabbs, &tri_pairs[i], i, &c)) {
+        if (sh->cols[bodies[tri_pairs[i].y].collidableIdx].shapeType == SHAPE_SPHERE
+                ? concave_sphere(bodies, sh, &tri_pairs[i], i, &c)
+                : concave_tri(bodies, sh, aabbs, &tri_pairs[i], i, &c)) {
             if (m < cap) { out[m] = c; if (out_index) out_index[m] = i; }
             m++;
         }

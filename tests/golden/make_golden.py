@@ -471,7 +471,7 @@ def concave_fixture():
     host twins b3FindConcaveSeparatingAxisKernel / clipFacesAndFindContactsKernel /
     b3NewContactReductionKernel give the manifolds."""
     from bullet3_gb300 import scenes
-    sc = scenes.terrain_scene(300, grid=24, seed=21)
+    sc = scenes.terrain_scene(300, grid=24, seed=21, spheres=False)
     t = O.register_scene(sc)
     shapes = O.Shapes.from_tables(t)
     bodies = t["bodies"]
