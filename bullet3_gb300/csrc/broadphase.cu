@@ -376,11 +376,15 @@ __device__ __forceinline__ void find_pairs_warp(const b3gAabb* __restrict__ aabb
         const uint32_t h_own = live ? cell_hash(gx, gy, gz, bits, mask) : 0xffffffffu;
         const unsigned own_peers = __match_any_sync(0xffffffffu, h_own);
         const int distinct = __popc(__ballot_sync(0xffffffffu, live && lane == __ffs(own_peers) - 1));
+        // Half stencil: a body scans its own cell (partners of higher index) and the 13 neighbour
+        // cells after it in (z, y, x) order (every partner); two overlapping bodies' cells are
+        // neighbours (cell >= every extent), so exactly one of them scans the other's cell, and
+        // with at least 4 cells an axis no two of the 14 cells share a hash.  Keys are (lower,
+        // higher) whichever body found the pair.
         if (distinct > BP_COOP_MAX_CELLS) {
             if (live)
-                for (int dz = -1; dz <= 1; dz++)
-                    for (int dy = -1; dy <= 1; dy++)
-                        for (int dx = -1; dx <= 1; dx++) {
+                for (int off = 13; off < 27; off++) {
+                            const int dx = off % 3 - 1, dy = (off / 3) % 3 - 1, dz = off / 9 - 1;
                             const uint32_t hh = cell_hash(gx + dx, gy + dy, gz + dz, bits, mask);
                             const uint32_t s0 = __ldg(&cell_start[hh]);
                             if (s0 >= (uint32_t)n_dyn) continue;
@@ -389,14 +393,15 @@ __device__ __forceinline__ void find_pairs_warp(const b3gAabb* __restrict__ aabb
                             for (uint32_t q = s0; q < (uint32_t)n_dyn; q++) {
                                 if (__ldg(&keys[q]) != hh) break;
                                 const uint32_t j = __ldg(&vals[q]);
-                                if (j <= i) continue;
+                                if (off == 13 ? j <= i : j == i) continue;
                                 if (SCENES && __ldg(&body_scene[j]) != si) continue;
                                 if (overlap(amin, amax, __ldg(&A[2 * j]), __ldg(&A[2 * j + 1])))
-                                    em.push(((uint64_t)i << body_bits) | j, out, counter, cap, status);
+                                    em.push(i < j ? ((uint64_t)i << body_bits) | j : ((uint64_t)j << body_bits) | i, out,
+                                            counter, cap, status);
                             }
-                        }
+                }
         } else
-        for (int off = 0; off < 27; off++) {
+        for (int off = 13; off < 27; off++) {
             const int dx = off % 3 - 1, dy = (off / 3) % 3 - 1, dz = off / 9 - 1;
             // this lane's target cell and its run start (validated against the sorted keys)
             uint32_t h = 0xffffffffu, st = 0;
@@ -433,10 +438,11 @@ __device__ __forceinline__ void find_pairs_warp(const b3gAabb* __restrict__ aabb
                     if (mine) {
                         for (int c = 0; c < cnt; c++) {
                             const uint32_t j = s_j[w][c];
-                            if (j <= i) continue;
+                            if (off == 13 ? j <= i : j == i) continue;
                             if (SCENES && s_sc[w][c] != si) continue;
                             if (overlap(amin, amax, s_min[w][c], s_max[w][c]))
-                                em.push(((uint64_t)i << body_bits) | j, out, counter, cap, status);
+                                em.push(i < j ? ((uint64_t)i << body_bits) | j : ((uint64_t)j << body_bits) | i, out,
+                                        counter, cap, status);
                         }
                     }
                     __syncwarp();
