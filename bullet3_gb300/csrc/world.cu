@@ -820,7 +820,6 @@ extern "C" b3gStatus b3g_write_all_to_gpu(b3g_handle h) {
                  ni = std::max<size_t>(1, h->indices.size()), nvx = std::max<size_t>(1, h->vertices.size()),
                  ne = std::max<size_t>(1, h->edges.size());
     TRY(dalloc(h, &d.bodies, N));
-    TRY(dalloc(h, &d.body_stage, N));
     TRY(dalloc(h, &d.inertias, N));
     TRY(dalloc(h, &d.collidables, d.num_collidables));
     TRY(dalloc(h, &d.local_aabbs, d.num_collidables));
@@ -1792,29 +1791,14 @@ extern "C" b3gStatus b3g_read_bodies(b3g_handle h, void* host, int n) {
     if (!host || n < 0 || n > h->d.num_bodies) return fail(B3G_ERR_INVALID_ARG, "bad body buffer");
     return copy_out(h, host, h->d.bodies, sizeof(b3gBody) * n);
 }
-// The host's bodies replace the device's; a body that turns static or dynamic (its inverse mass
-// changes to or from 0) makes the next PGS solve colour from scratch: carried colours are legal
-// only while the same bodies are static (positions and velocities do not matter to them; contacts
-// that come or go are coloured as any new or dropped contact).
-__global__ void k_write_bodies(const b3gBody* __restrict__ in, b3gBody* __restrict__ bodies, int n,
-                               int* __restrict__ recolour) {
-    bool changed = false;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const b3gBody b = in[i];
-        changed |= (b.invMass == 0.f) != (bodies[i].invMass == 0.f);
-        bodies[i] = b;
-    }
-    if (__any_sync(0xffffffffu, changed) && (threadIdx.x & 31) == 0) *recolour = 1;
-}
-
 extern "C" b3gStatus b3g_write_bodies(b3g_handle h, const void* host, int n) {
     REQUIRE_UPLOADED(h);
     if (!host || n < 0 || n > h->d.num_bodies) return fail(B3G_ERR_INVALID_ARG, "bad body buffer");
-    if (n == 0) return B3G_OK;
-    TRY(copy_in(h, h->d.body_stage, host, sizeof(b3gBody) * n));
-    k_write_bodies<<<h->d.num_sms * 4, 256, 0, h->stream>>>(h->d.body_stage, h->d.bodies, n, h->d.prev_mn + 2);
-    h->launches++;
-    TRY(check_launch(h));
+    TRY(copy_in(h, h->d.bodies, host, sizeof(b3gBody) * n));
+    // a body state from the host may be anywhere: the next PGS solve colours from scratch rather
+    // than carrying the last solve's colours over
+    static const int recolour = 1;
+    CUDA_TRY(cudaMemcpyAsync(h->d.prev_mn + 2, &recolour, sizeof(int), cudaMemcpyHostToDevice, h->stream));
     return B3G_OK;
 }
 extern "C" b3gStatus b3g_read_inertias(b3g_handle h, void* host, int n) {

@@ -130,7 +130,6 @@ struct DeviceState {
     int num_sms = 0;
     // registries
     b3gBody* bodies = nullptr;
-    b3gBody* body_stage = nullptr;  // b3g_write_bodies: the host's bodies before they replace these
     b3gInertia* inertias = nullptr;
     b3gCollidable* collidables = nullptr;
     b3gAabb* local_aabbs = nullptr;

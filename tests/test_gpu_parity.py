@@ -262,8 +262,8 @@ def test_collision_at_scale_pair_sets_every_step():
 @pytest.mark.parametrize("interleave", [False, True])
 def test_pgs_carried_colours_bitexact(interleave, flow):
     # grid-wide PGS colours the manifolds before the row setup and carries each body pair's colour
-    # over from the last solve (from scratch again every 8 solves and after a host write that turns
-    # a body static or dynamic); after many steps, and after bodies switched between static and dynamic, the
+    # over from the last solve (from scratch again every 8 solves and after a host write of the
+    # bodies); after many steps, and after bodies switched between static and dynamic, the
     # batches stay legal and the solve equals the oracle sweeping the GPU's reported order bit for
     # bit
     # (flow 1: the dataflow sweeps with per-body update counters; 2: a grid barrier per colour)
