@@ -443,9 +443,9 @@ def _time_config(sc, cfg, device, settle, steps, warm_model=None, profile_steps=
 def other_configurations(args, device):
     """The benchmark's other configurations at full size, device-timed in the same run (graph-captured
     steps, launch shapes autotuned after the settle): collision at scale (131,072 mixed bodies,
-    steps 3..63 of 64), batched scenes (4,096 scenes, 30 steps after 120 settle steps) and the
-    million-body pour (steps 3..599 of 600, PGS to 1e-4 with a 16-sweep cap, persistent + learned
-    warm start)."""
+    steps 3..63 of 64), batched scenes (4,096 scenes, 30 steps after 120 settle steps), the 64^3
+    lattice while it falls and settles (steps 60..119, PGS 10 iterations) and the million-body pour
+    (steps 3..599 of 600, PGS to 1e-4 with a 16-sweep cap, persistent + learned warm start)."""
     from bullet3_gb300 import capi, scenes
     from bullet3_gb300.pipeline import b3Config
     out = {}
@@ -461,6 +461,17 @@ def other_configurations(args, device):
                    broadphase=capi.BROADPHASE_AUTO)
     out["batched_scenes"] = dict(workload=WORKLOAD_BATCHED.format(n=args.scenes, bodies=sc.num_bodies),
                                  **_time_config(sc, cfg, device, settle=120, steps=30))
+    # the pile while it falls and topples (the learned-warm-start configuration's lattice, at the
+    # headline's fixed 10 iterations): every box in contact with its neighbours, several manifolds
+    # a body, far more colours than the settled columns
+    sc = scenes.box_pile(args.nx, 64, args.nx, jitter=0.05, seed=0)
+    cfg = b3Config(solver_mode=capi.SOLVER_PGS, solver_iterations=10, use_cuda_graph=True, pgs_interleave=True,
+                   broadphase=capi.BROADPHASE_AUTO)
+    out["falling_lattice"] = dict(
+        workload=f"box pile lattice {args.nx}x64x{args.nx} = {sc.num_bodies - 1:,} unit boxes (spacing 1.1, jitter "
+                 "0.05, seed 0) falling onto a static plane from rest, PGS 10 iterations; timed steps 60..119, "
+                 "while the lattice lands and its columns settle",
+        **_time_config(sc, cfg, device, settle=60, steps=60))
     if not args.no_pour:
         from bullet3_gb300.warmstart import DEFAULT_WEIGHTS, WarmStartMLP
         sc = scenes.stress_container(1048576, seed=0)
