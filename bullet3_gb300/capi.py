@@ -73,7 +73,7 @@ class b3gConfig(C.Structure):
                 ("solver_blocks_per_sm", C.c_int), ("pgs_partitions", C.c_int), ("pgs_interleave", C.c_int),
                 ("warm_start_max_points", C.c_int), ("autotune", C.c_int), ("broadphase", C.c_int),
                 ("pgs_tail_manifolds", C.c_int), ("pgs_flow", C.c_int),
-                ("max_compound_child_pairs", C.c_int), ("max_concave_pairs", C.c_int), ("reserved", C.c_int * 1)]
+                ("max_compound_child_pairs", C.c_int), ("max_concave_pairs", C.c_int), ("warm_start_factor", C.c_float)]
 
 
 class b3gTuning(C.Structure):

@@ -1485,6 +1485,7 @@ struct WarmFill {
     const float4* prev_imp;
     const int* prev_n;
     int persist;                  // take persisting points' previous impulses
+    float factor;                 // ... scaled by this
     int predict_all;              // network also for persisting points
     int write_imp;
     float4* init;
@@ -1545,7 +1546,10 @@ __global__ void k_warm_fill(WarmFill w) {
                     }
                     if (bj >= 0) {
                         matched = true;
-                        if (w.persist) v = w.prev_imp[(size_t)q * 4 + bj];
+                        if (w.persist) {
+                            const float4 pv = w.prev_imp[(size_t)q * 4 + bj];
+                            v = w.factor == 1.f ? pv : make_float4(pv.x * w.factor, pv.y * w.factor, pv.z * w.factor, 0.f);
+                        }
                     }
                 }
                 if (w.pred && (!matched || w.predict_all || !w.persist)) {
@@ -2396,6 +2400,7 @@ int launch_solver(DeviceState& d, const b3gConfig& cfg, float dt, cudaStream_t s
         w.prev_imp = d.prev_imp;
         w.prev_n = d.prev_n;
         w.persist = ws_persist ? 1 : 0;
+        w.factor = cfg.warm_start_factor > 0.f ? cfg.warm_start_factor : 1.f;
         w.predict_all = wm == B3G_WARM_LEARNED ? 1 : 0;
         w.write_imp = a.warm;
         w.init = d.ws_init;

@@ -50,6 +50,7 @@ class b3Config:
         self.pgs_interleave = False
         self.warm_start = 0
         self.warm_start_max_points = 0
+        self.warm_start_factor = 0.0  # persisting impulses scaled by this (0 = 1; the reference uses 0.85)
         self.autotune = False
         self.broadphase = capi.BROADPHASE_GRID
         self.pgs_tail_manifolds = 0
@@ -71,6 +72,7 @@ class b3Config:
                                    pgs_partitions=self.pgs_partitions,
                                    pgs_interleave=int(self.pgs_interleave), warm_start=int(self.warm_start),
                                    warm_start_max_points=int(self.warm_start_max_points),
+                                   warm_start_factor=float(self.warm_start_factor),
                                    autotune=int(self.autotune), broadphase=int(self.broadphase),
                                    pgs_tail_manifolds=int(self.pgs_tail_manifolds), pgs_flow=int(self.pgs_flow),
                                    max_compound_child_pairs=int(self.m_compoundPairCapacity),

@@ -127,7 +127,9 @@ typedef struct b3gConfig {
     int max_concave_pairs;     /* triangle-convex pairs of the concave-mesh pairs per step
                                   (m_maxTriConvexPairCapacity; 0 = max_pairs); only allocated when a
                                   concave mesh is registered */
-    int reserved[1];
+    float warm_start_factor;   /* B3G_WARM_PERSISTENT*: the persisting points' carried impulses are
+                                  scaled by this (b3ContactSolverInfo::m_warmstartingFactor, 0.85 in
+                                  the reference's B3_SOLVER_USE_WARMSTARTING); 0 counts as 1 */
 } b3gConfig;
 
 /* Per-step counters, copied once per step from the device. */
